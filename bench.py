@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Benchmark of the FastS solve step on GB300.
+
+Workload (the configuration the headline metric is quoted on): laminar
+Taylor-Green vortex on a 256^3 periodic box, Re 1600, Mach 0.1, AUSM+(P) o3,
+implicit dual time stepping with 4 LU-SGS sub-iterations, FP64.  A "step" is
+one physical time step (all sub-iterations).  Synthetic data generated by
+fast_gb300.cases (the reference's benchmarks use no public dataset).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line.  `value` = Mcell-updates/s with the state resident in
+HBM, device-timed with CUDA events on the solver stream; `e2e` = the same
+metric through fasts._compute with host arrays (levels n, n-1 copied in, the
+new level copied out every step).  The state (>= 700 MB) is larger than L2,
+so no flush is needed between steps.  Multi-GPU: replicas (one independent
+case per GPU, weak scaling), value = all ranks' cell updates / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mcell-updates/s; time to 1e-10 residual drop, mixed vs FP64; adjoint/primal cost"
+UNIT = "Mcell-updates/s"
+# compulsory FP64 traffic per cell and launch group (8 B words, NEQ = 5):
+# residual (W^p, W^n, W^{n-1} in, drodm out) = 160 B; LU-SGS lower + upper
+# (drodm, W^p, coe in / increment, W^{p+1} out) = 320 B per sub-iteration.
+ALG_BYTES = {"residual": 160.0, "lu_sgs": 320.0}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=256)
+    p.add_argument("--ss", type=int, default=4)
+    p.add_argument("--cpu-n", type=int, default=96, help="CPU sample size (cells per side)")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+# ----------------------------------------------------------- distributed
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# ----------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi sampling during the timed region (every 200 ms)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU side
+def cpu_sample(n, ss, steps=1):
+    """The oracle (C restatement of the FastS kernels, OpenMP on every host
+    core, one LU-SGS block per thread as FastS does) on an n^3 sample of the
+    workload.  Returns (Mcell-updates/s, threads, seconds)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    from fast_gb300 import cases, fasts
+    threads = os.cpu_count() or 1
+    t = cases.taylor_green(n=n, ss_iteration=ss)
+    m = fasts.prepare(t)
+    c = oracle.Case(fasts.zone_data(t, m))
+    oracle.set_threads(threads)
+    oracle.load().or_set_lu_tiles(threads)
+    c.apply_bc(0)
+    c.apply_bc(1)
+    t0 = time.perf_counter()
+    for it in range(1, steps + 1):
+        c.compute(it, 1, ss + 1, 1, modulo_verif=200)
+    dt = time.perf_counter() - t0
+    oracle.load().or_set_lu_tiles(1)
+    return n ** 3 * steps / dt / 1e6, threads, dt
+
+
+def run_reference(args, d: Dist):
+    if d.rank != 0:
+        return
+    n = args.cpu_n
+    for _ in range(args.warmup):
+        cpu_sample(n, args.ss, 1)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        v, threads, dt = cpu_sample(n, args.ss, 1)
+        vals.append(v)
+        secs += dt
+    value = args.steps * n ** 3 / secs / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"taylor_green_{args.n}^3_ausmpred_o3_implicit_lusgs_ss{args.ss}",
+                   "sample": f"{n}^3 cells, 1 physical step ({args.ss} sub-iterations) per step",
+                   "parallelism": "host OpenMP"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"taylor_green {n}^3, {args.ss} LU-SGS sub-iterations, "
+                                   f"one LU block per thread"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- GPU side
+def run_ours(args, d: Dist):
+    import json as _json
+    from fast_gb300 import cases, fasts, fastc
+    from fast_gb300 import _native
+    dev = d.local
+    n, ss = args.n, args.ss
+    cells = n ** 3
+    peaks = {}
+    pf = ROOT / "MEASURED_PEAKS.json"
+    if pf.exists():
+        peaks = _json.loads(pf.read_text())
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    t = cases.taylor_green(n=n, ss_iteration=ss)
+    t, tc, metrics = fasts.warmup(t, None, device=dev, gpu_resident=True)
+    s = fasts.HOOK["solver"]
+    it = 1
+    for _ in range(args.warmup):
+        fasts._compute(t, metrics, it)
+        it += 1
+    s.synchronize()
+
+    # ---- device-resident timed region
+    clocks = Clocks(dev)
+    d.barrier()
+    s.synchronize()
+    l0 = s.launch_count()
+    clocks.start()
+    s.timer_start()
+    for _ in range(args.steps):
+        fasts._compute(t, metrics, it)
+        it += 1
+    ms = s.timer_stop()
+    clk = clocks.stop()
+    launches = s.launch_count() - l0
+    d.barrier()
+    ms_max = d.max(ms)
+    value = d.world * cells * args.steps / (ms_max * 1e-3) / 1e6
+
+    # ---- per-kernel groups (separate profiled step; not part of `value`)
+    s.set_option("profile", 1)
+    s.kernel_stats(reset=True)
+    fasts._compute(t, metrics, it)
+    it += 1
+    stats = s.kernel_stats(reset=True)
+    s.set_option("profile", 0)
+    groups = {"residual": ("face_flux", "assemble_bdf"), "lu_sgs": ("lu_sgs",)}
+    gt = {}
+    for g, names in groups.items():
+        cnt = max((stats.get(nm, (0, 0.0))[0] for nm in names), default=0)
+        tot = sum(stats.get(nm, (0, 0.0))[1] for nm in names)
+        if cnt:
+            gt[g] = (cnt, tot)
+    dom = max(gt, key=lambda g: gt[g][1])
+    cnt, tot = gt[dom]
+    avg_ms = tot / cnt
+    achieved = ALG_BYTES[dom] * cells / (avg_ms * 1e-3) / 1e9
+    fp64 = _native.fp64_peak_gflops(dev)
+    total_prof = sum(v[1] for v in stats.values())
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
+        "avg_launch_ms": avg_ms,
+        "fp64_fma_peak_gflops_measured": fp64,
+        "kernel_share": {k: round(v[1] / total_prof, 4) for k, v in stats.items()},
+    }
+
+    # ---- end to end through the public API with host arrays
+    e2e = None
+    if not args.no_e2e:
+        fasts._syncHost(t)
+        fasts.HOOK["gpu_resident"] = False
+        nd = (n + 4) ** 3
+        k2 = max(1, min(args.steps, 3))
+        fasts._compute(t, metrics, it)   # untimed first call (page-in)
+        it += 1
+        d.barrier()
+        t0 = time.perf_counter()
+        for _ in range(k2):
+            fasts._compute(t, metrics, it)
+            it += 1
+        s.synchronize()
+        el = d.max(time.perf_counter() - t0)
+        e2e = {"value": d.world * cells * k2 / el / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": 2 * 5 * nd * 8, "d2h_bytes_per_step": 5 * nd * 8,
+               "steps": k2, "timer": "host wall clock around fasts._compute"}
+
+    cpu = None
+    if d.rank == 0 and not args.no_cpu:
+        v, threads, sec = cpu_sample(args.cpu_n, ss, 1)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"taylor_green {args.cpu_n}^3, one physical step ({ss} LU-SGS "
+                         f"sub-iterations), {sec:.1f} s"}
+    d.barrier()
+    if d.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"taylor_green_{n}^3_ausmpred_o3_implicit_lusgs_ss{ss}",
+                       "cells": cells, "global_batch": d.world, "sub_iterations": ss,
+                       "parallelism": f"replicas x{d.world}",
+                       "l2": "state (>=700 MB) larger than L2; no flush"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": launches,
+            "kernel_ms_per_step": {k: v[1] for k, v in stats.items()},
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    d = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, d)
+        else:
+            run_ours(args, d)
+    finally:
+        d.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,150 @@
+"""Synthetic cases of the benchmark configurations (meshes, initial fields,
+boundary conditions), built directly as pyTrees.
+
+Cassiopee's Generator / Initiator / Connector are not available, so the mesh
+generators and initial conditions are written here from their published
+definitions:
+
+* isentropic vortex (Yee, Sandham & Djomehri, J. Comput. Phys. 150, 1999):
+  du = -beta/(2 pi) (y-yc) e^{(1-r^2)/2}, dv = beta/(2 pi) (x-xc) e^{(1-r^2)/2},
+  dT = -(gamma-1) beta^2 / (8 gamma pi^2) e^{1-r^2}, isentropic density,
+  lengths scaled by the core radius;
+* Taylor-Green vortex, with the density / pressure formula that
+  FastS/test/explicitLocalTgv_t1.py:86-90 uses.
+
+Zones carry two layers of ghost cells as after Internal.addGhostCells; BC
+PointRanges follow that convention (windows extended through the ghost
+layers), which FastC's getRange converts back to interior windows.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import fastc as FastC
+from . import pytree as I
+
+NG = 2
+
+
+def cart_zone(name, x0, h, n, ng=NG):
+    """Uniform cartesian zone of n = (ni, nj, nk) interior cells, origin x0
+    (first interior vertex), steps h, with ng ghost layers on every side."""
+    ni, nj, nk = n
+    nv = [ni + 1 + 2 * ng, nj + 1 + 2 * ng, nk + 1 + 2 * ng]
+    z = I.newZone(name, nv)
+    ii = np.arange(nv[0]) - ng
+    jj = np.arange(nv[1]) - ng
+    kk = np.arange(nv[2]) - ng
+    X, Y, Z = np.meshgrid(x0[0] + ii * h[0], x0[1] + jj * h[1], x0[2] + kk * h[2], indexing="ij")
+    gc = I.createChild(z, "GridCoordinates", "GridCoordinates_t")
+    for nm, arr in (("CoordinateX", X), ("CoordinateY", Y), ("CoordinateZ", Z)):
+        I.createChild(gc, nm, "DataArray_t")[1] = np.asfortranarray(arr)
+    I.createChild(z, "Rind", "Rind_t", np.array([ng] * 6, dtype=np.int64))
+    return z
+
+
+def cell_centers(z):
+    gc = I.getNodeFromName1(z, "GridCoordinates")
+    out = []
+    for nm in ("CoordinateX", "CoordinateY", "CoordinateZ"):
+        a = I.getNodeFromName1(gc, nm)[1]
+        c = 0.125 * (a[:-1, :-1, :-1] + a[1:, :-1, :-1] + a[:-1, 1:, :-1] + a[:-1, :-1, 1:] +
+                     a[1:, 1:, :-1] + a[1:, :-1, 1:] + a[:-1, 1:, 1:] + a[1:, 1:, 1:])
+        out.append(np.asfortranarray(c))
+    return out
+
+
+def add_bc(z, name, btype, face, ng=NG):
+    """Full-face BC on face 'imin'..'kmax' with a ghost-extended PointRange."""
+    nv = [int(z[1][0, 0]), int(z[1][1, 0]), int(z[1][2, 0])]
+    rg = np.array([[1, nv[0]], [1, nv[1]], [1, nv[2]]], dtype=np.int64)
+    d = "ijk".index(face[0])
+    rg[d, :] = 1 if face[1:] == "min" else nv[d]
+    zbc = I.getNodeFromName1(z, "ZoneBC") or I.createChild(z, "ZoneBC", "ZoneBC_t")
+    bc = I.createChild(zbc, name, "BC_t", btype)
+    I.createChild(bc, "PointRange", "IndexRange_t")[1] = np.asfortranarray(rg)
+    return bc
+
+
+def set_conservative(z, ro, u, v, w, p, gamma):
+    sol = I.createUniqueChild(z, I.__FlowSolutionCenters__, "FlowSolution_t")
+    roe = p / (gamma - 1.0) + 0.5 * ro * (u * u + v * v + w * w)
+    for nm, arr in (("Density", ro), ("MomentumX", ro * u), ("MomentumY", ro * v),
+                    ("MomentumZ", ro * w), ("EnergyStagnationDensity", roe)):
+        I.createUniqueChild(sol, nm, "DataArray_t")[1] = np.asfortranarray(arr)
+
+
+def _tree(zones, model, numb, numz, mach, reynolds, gamma=1.4, prandtl=0.72, sutherland=True):
+    t = I.newCGNSTree()
+    b = I.newCGNSBase("Base", 3, 3, t)
+    for z in zones:
+        b[2].append(z)
+    I.createChild(b, "FlowEquationSet", "FlowEquationSet_t")
+    I.createChild(I.getNodeFromName1(b, "FlowEquationSet"), "GoverningEquations",
+                  "GoverningEquations_t", model)
+    FastC.addReferenceState(t, mach=mach, reynolds=reynolds, gamma=gamma, prandtl=prandtl,
+                            sutherland=sutherland)
+    FastC._setNum2Base(t, numb)
+    FastC._setNum2Zones(t, numz)
+    return t
+
+
+def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0, gamma=1.4,
+                      numb=None, numz=None):
+    """Config: plain FP64, 128x128x4 periodic box [-box, box]^2, Euler vortex
+    (Mach 0.5, strength 5, core radius 1), Roe + minmod, explicit RK3."""
+    ni, nj, nk = n
+    h = (2 * box / ni, 2 * box / nj, 2 * box / ni)
+    z = cart_zone("vortex", (-box, -box, 0.0), h, n)
+    xc, yc, _ = cell_centers(z)
+    x = xc / radius
+    y = yc / radius
+    r2 = x * x + y * y
+    e = np.exp(0.5 * (1.0 - r2))
+    du = -beta / (2 * math.pi) * y * e
+    dv = beta / (2 * math.pi) * x * e
+    T = 1.0 - (gamma - 1.0) * beta ** 2 / (8.0 * gamma * math.pi ** 2) * e * e
+    ro = T ** (1.0 / (gamma - 1.0))
+    p = ro * T / gamma
+    set_conservative(z, ro, mach + du, dv, np.zeros_like(ro), p, gamma)
+    for f in ("imin", "imax", "jmin", "jmax", "kmin", "kmax"):
+        add_bc(z, "per_" + f, "BCautoperiod", f)
+    numb = numb or {"temporal_scheme": "explicit", "ss_iteration": 1, "modulo_verif": 1000000}
+    numz = numz or {"scheme": "roe_min", "slope": "minmod", "time_step": 0.01,
+                    "cache_blocking_I": 1000000, "cache_blocking_J": 1000000,
+                    "cache_blocking_K": 1000000}
+    return _tree([z], "Euler", numb, numz, mach, 0.0, gamma=gamma)
+
+
+def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_iteration=4,
+                 dt=None, scheme="ausmpred", slope="o3", numb=None, numz=None, name="tgv"):
+    """Config: laminar Taylor-Green vortex on the periodic box [0, 2 pi]^3,
+    Re = 1600, Mach 0.1, Pr 0.71, mu ~ sqrt(T) (FastS Sutherland form with
+    Cs = 0), AUSM+(P) o3, implicit LU-SGS dual time stepping."""
+    N = (n, n, n) if isinstance(n, int) else tuple(n)
+    L = 1.0
+    h = tuple(2 * math.pi * L / k for k in N)
+    z = cart_zone(name, (0.0, 0.0, 0.0), h, N)
+    xc, yc, zc = cell_centers(z)
+    U0 = mach
+    ro0, T0 = 1.0, 1.0
+    p0 = ro0 * T0 / gamma
+    u = U0 * np.sin(xc / L) * np.cos(yc / L) * np.cos(zc / L)
+    v = -U0 * np.cos(xc / L) * np.sin(yc / L) * np.cos(zc / L)
+    w = np.zeros_like(u)
+    p = p0 + ro0 * U0 ** 2 / 16.0 * (np.cos(2 * xc / L) + np.cos(2 * yc / L)) * (np.cos(2 * zc / L) + 2.0)
+    ro = p * gamma / T0   # T = T0 everywhere (R = 1/gamma)
+    set_conservative(z, ro, u, v, w, p, gamma)
+    for f in ("imin", "imax", "jmin", "jmax", "kmin", "kmax"):
+        add_bc(z, "per_" + f, "BCautoperiod", f)
+    if dt is None:
+        dt = 0.1 * h[0] / (U0 + 1.0) * 5.0   # acoustic CFL ~ 5 (implicit)
+    numb = numb or {"temporal_scheme": "implicit", "ss_iteration": ss_iteration,
+                    "modulo_verif": 1}
+    numz = numz or {"scheme": scheme, "slope": slope, "time_step": dt,
+                    "cache_blocking_I": 1000000, "cache_blocking_J": 1000000,
+                    "cache_blocking_K": 1000000}
+    return _tree([z], "NSLaminar", numb, numz, mach, reynolds, gamma=gamma, prandtl=prandtl,
+                 sutherland=False)

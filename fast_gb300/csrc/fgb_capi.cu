@@ -1,0 +1,757 @@
+// fgb_capi.cu -- C ABI and host-side orchestration of the solve step.
+//
+// The solver handle owns every device array of every zone.  fgb_compute is
+// the sub-step loop of FastS/FastS/Compute/computePT.cpp:534-680 with the
+// array choice of gsdr3.cpp:152-173, the verification flags of
+// FastC/FastC/Compute/souszones_list.cpp:31-97, the per-zone sub-step of
+// navier_stokes_struct.for / lhs.cpp and the ghost fill of
+// transfert_multiblock.cpp + bcs.cpp; every numerical step is a CUDA kernel
+// on the solver's stream (no host arithmetic on field data, no CPU fallback).
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "../../include/fast_gb300.h"
+#include "fgb_kernels.cuh"
+
+using namespace fgb;
+
+static thread_local std::string g_err;
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+#define CK(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(FGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+template <typename T>
+static cudaError_t dev_upload(T** d, const std::vector<T>& h) {
+  *d = nullptr;
+  if (h.empty()) return cudaSuccess;
+  cudaError_t e = cudaMalloc((void**)d, h.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+struct GatherList {
+  int32_t* dst = nullptr; int32_t* src = nullptr; int64_t n = 0; int op = 0;
+};
+struct ZoneData {
+  std::vector<int64_t> pi;
+  std::vector<double> pr;
+  Zone z{};
+  double* lvl[3] = {nullptr, nullptr, nullptr};  // n, n-1, n+1
+  double* scratch = nullptr;
+  double *drodm = nullptr, *coe = nullptr, *xmut = nullptr, *rdm = nullptr;
+  double *ti = nullptr, *tj = nullptr, *tk = nullptr, *vol = nullptr;
+  double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
+  int64_t n_rdm = 0, ijkv_lu[3] = {1, 1, 1};
+  std::vector<GatherList> bcs;
+  int32_t *co_dst = nullptr, *co_a = nullptr, *co_b = nullptr, *co_c = nullptr;
+  int64_t co_nedge = 0, co_n = 0;
+  double coesut = 0., cmus1 = 0.;
+};
+struct Transfer {
+  int dnr, rcv; int64_t n; int32_t* dnr_idx; int32_t* rcv_idx;
+};
+
+struct fgb_solver {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::vector<ZoneData> zones;
+  std::vector<Transfer> tr;
+  int first_it = 0;
+  int modulo_verif = 200;
+  int lu_precision = 64;
+  int nit_recorded = 0;
+  int64_t launches = 0;
+  // optional per-kernel timing with CUDA events on the solver stream
+  bool profile = false;
+  struct Ev { const char* name; cudaEvent_t a, b; };
+  std::vector<Ev> events;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+static cudaEvent_t ev_get(fgb_solver* s) {
+  if (!s->pool.empty()) { cudaEvent_t e = s->pool.back(); s->pool.pop_back(); return e; }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+// brackets a group of launches named `name` when profiling is on
+struct ProfScope {
+  fgb_solver* s; const char* name; cudaEvent_t a = nullptr;
+  ProfScope(fgb_solver* s_, const char* n) : s(s_), name(n) {
+    if (s->profile) { a = ev_get(s); cudaEventRecord(a, s->st); }
+  }
+  ~ProfScope() {
+    if (s->profile) {
+      cudaEvent_t b = ev_get(s);
+      cudaEventRecord(b, s->st);
+      s->events.push_back({name, a, b});
+    }
+  }
+};
+
+// ------------------------------------------------------------- helpers
+static int64_t idx(const std::vector<int64_t>& p, int64_t i, int64_t j, int64_t k) {
+  return (i + p[NIJK + 3] - 1) + (j + p[NIJK + 3] - 1) * p[NIJK] +
+         (k + p[NIJK + 4] - 1) * p[NIJK] * p[NIJK + 1];
+}
+
+// BC windows of FastC/FastC/BC/indice_cl_sdm.for with npass = 0 for a
+// single-tile zone: the ghost layers beyond the face, tangential range =
+// window intersected with the interior.
+static void bc_window(const std::vector<int64_t>& p, const int64_t* fen, int idir, int64_t* cl) {
+  int64_t ng = p[NIJK + 3], ngk = p[NIJK + 4];
+  int64_t sdm[6] = {1, p[IJKV], 1, p[IJKV + 1], 1, p[IJKV + 2]};
+  for (int d = 0; d < 3; d++) {
+    cl[2 * d] = std::max(fen[2 * d], sdm[2 * d]);
+    cl[2 * d + 1] = std::min(fen[2 * d + 1], sdm[2 * d + 1]);
+  }
+  if (idir == 1) { cl[1] = cl[0] - 1; cl[0] = cl[0] - ng; }
+  else if (idir == 2) { cl[1] = cl[0] + ng; cl[0] = cl[0] + 1; }
+  else if (idir == 3) { cl[3] = cl[2] - 1; cl[2] = cl[2] - ng; }
+  else if (idir == 4) { cl[3] = cl[2] + ng; cl[2] = cl[2] + 1; }
+  else if (idir == 5) { cl[5] = cl[4] - 1; cl[4] = cl[4] - ngk; }
+  else { cl[5] = cl[4] + ngk; cl[4] = cl[4] + 1; }
+}
+
+static int build_ghost_lists(ZoneData& Z) {
+  const std::vector<int64_t>& p = Z.pi;
+  int64_t pt_bcs = p[PT_BC];
+  if (pt_bcs > 0 && pt_bcs < (int64_t)p.size()) {
+    int64_t nb = p[pt_bcs];
+    for (int64_t n = 0; n < nb; n++) {
+      int64_t pt = p[pt_bcs + 1 + n];
+      int64_t type = p[pt + 0];
+      int idir = (int)p[pt + 1];
+      if (type != 11 && type != 0)
+        return fail(FGB_ERR_ARG, "boundary condition type " + std::to_string(type) +
+                                     " is not implemented on the GPU path");
+      int64_t cl[6];
+      bc_window(p, &p[pt + 2], idir, cl);
+      int d = (idir - 1) / 2;
+      bool low = (idir % 2) == 1;
+      int64_t nD = p[IJKV + d];
+      std::vector<int32_t> dst, src;
+      for (int64_t k = cl[4]; k <= cl[5]; k++)
+        for (int64_t j = cl[2]; j <= cl[3]; j++)
+          for (int64_t i = cl[0]; i <= cl[1]; i++) {
+            int64_t c[3] = {i, j, k}, s[3] = {i, j, k};
+            if (type == 11) s[d] = low ? c[d] + nD : c[d] - nD;
+            else s[d] = low ? cl[2 * d + 1] + 1 : cl[2 * d] - 1;
+            dst.push_back((int32_t)idx(p, i, j, k));
+            src.push_back((int32_t)idx(p, s[0], s[1], s[2]));
+          }
+      GatherList g;
+      g.n = (int64_t)dst.size();
+      g.op = type == 11 ? 0 : 1;
+      if (dev_upload(&g.dst, dst) != cudaSuccess || dev_upload(&g.src, src) != cudaSuccess)
+        return fail(FGB_ERR_CUDA, "cannot upload BC lists");
+      Z.bcs.push_back(g);
+    }
+  }
+  // correct_coins.for lists (edges first, then corners)
+  int64_t ng = p[NIJK + 3], ngk = p[NIJK + 4];
+  int64_t N[3] = {p[IJKV], p[IJKV + 1], p[IJKV + 2]};
+  std::vector<int32_t> dst, a, b, c;
+  auto add2 = [&](int64_t d_, int64_t a_, int64_t b_) {
+    dst.push_back((int32_t)d_); a.push_back((int32_t)a_); b.push_back((int32_t)b_); c.push_back(0);
+  };
+  for (int idir = 1; idir <= 2; idir++) {  // faces I: bands jmin/jmax, kmin/kmax
+    int64_t is = idir == 1 ? -1 : 1, i0 = idir == 1 ? 1 : N[0];
+    for (int side = 0; side < 2; side++) {
+      int64_t j0 = side == 0 ? 1 : N[1], js = side == 0 ? -1 : 1;
+      for (int64_t k = 1; k <= N[2]; k++)
+        for (int64_t j = 1; j <= ng; j++)
+          for (int64_t i = 1; i <= ng; i++) {
+            int64_t i1 = std::min(ng, i + 1), j1 = std::min(ng, j + 1);
+            add2(idx(p, i0 + i * is, j0 + js * j, k), idx(p, i0 + i1 * is, j0, k),
+                 idx(p, i0, j0 + js * j1, k));
+          }
+    }
+    for (int side = 0; side < 2; side++) {
+      int64_t k0 = side == 0 ? 1 : N[2], ks = side == 0 ? -1 : 1;
+      for (int64_t k = 1; k <= ngk; k++)
+        for (int64_t j = 1; j <= N[1]; j++)
+          for (int64_t i = 1; i <= ng; i++) {
+            int64_t k1 = std::min(ngk, k + 1), i1 = std::min(ng, i + 1);
+            add2(idx(p, i0 + i * is, j, k0 + ks * k), idx(p, i0, j, k0 + ks * k1),
+                 idx(p, i0 + i1 * is, j, k0));
+          }
+    }
+  }
+  for (int idir = 3; idir <= 4; idir++) {  // faces J: bands kmin/kmax
+    int64_t js = idir == 3 ? -1 : 1, j0 = idir == 3 ? 1 : N[1];
+    for (int side = 0; side < 2; side++) {
+      int64_t k0 = side == 0 ? 1 : N[2], ks = side == 0 ? -1 : 1;
+      for (int64_t k = 1; k <= ngk; k++)
+        for (int64_t j = 1; j <= ng; j++)
+          for (int64_t i = 1; i <= N[0]; i++) {
+            int64_t k1 = std::min(ngk, k + 1), j1 = std::min(ng, j + 1);
+            add2(idx(p, i, j0 + j * js, k0 + ks * k), idx(p, i, j0, k0 + ks * k1),
+                 idx(p, i, j0 + j1 * js, k0));
+          }
+    }
+  }
+  int64_t n_edge = (int64_t)dst.size();
+  for (int corner = 0; corner < 8; corner++) {
+    int hi_i = corner & 1, hi_j = (corner >> 1) & 1, hi_k = (corner >> 2) & 1;
+    int64_t i0 = hi_i ? N[0] : 1, j0 = hi_j ? N[1] : 1, k0 = hi_k ? N[2] : 1;
+    int64_t si = hi_i ? 1 : -1, sj = hi_j ? 1 : -1, sk = hi_k ? 1 : -1;
+    for (int64_t k = 1; k <= ngk; k++)
+      for (int64_t j = 1; j <= ng; j++)
+        for (int64_t i = 1; i <= ng; i++) {
+          int64_t i1 = std::min(ng, i + 1), j1 = std::min(ng, j + 1), k1 = std::min(ngk, k + 1);
+          dst.push_back((int32_t)idx(p, i0 + si * i, j0 + sj * j, k0 + sk * k));
+          a.push_back((int32_t)idx(p, i0, j0, k0 + sk * k1));
+          b.push_back((int32_t)idx(p, i0 + si * i1, j0, k0));
+          c.push_back((int32_t)idx(p, i0, j0 + sj * j1, k0));
+        }
+  }
+  Z.co_nedge = n_edge;
+  Z.co_n = (int64_t)dst.size();
+  if (dev_upload(&Z.co_dst, dst) != cudaSuccess || dev_upload(&Z.co_a, a) != cudaSuccess ||
+      dev_upload(&Z.co_b, b) != cudaSuccess || dev_upload(&Z.co_c, c) != cudaSuccess)
+    return fail(FGB_ERR_CUDA, "cannot upload corner lists");
+  return FGB_OK;
+}
+
+// constants of template_FluxAndBalance.for:108-156, invist.for:23-26,
+// evaluated once on the host (compiled without contraction)
+static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const double* tk,
+                      const double* vol) {
+  const std::vector<int64_t>& p = Z.pi;
+  const std::vector<double>& r = Z.pr;
+  Zone& z = Z.z;
+  z.ni = p[IJKV]; z.nj = p[IJKV + 1]; z.nk = p[IJKV + 2];
+  z.ng = p[NIJK + 3]; z.ngk = p[NIJK + 4];
+  z.nip = p[NIJK]; z.njp = p[NIJK + 1]; z.nkp = p[NIJK + 2];
+  z.nd = p[NDIMDX];
+  z.inc[0] = 1; z.inc[1] = z.nip; z.inc[2] = z.nip * z.njp;
+  z.minc[0] = p[NIJK_MTR]; z.minc[1] = p[NIJK_MTR + 1]; z.minc[2] = p[NIJK_MTR + 2];
+  z.mg = p[NIJK_MTR + 3]; z.mgk = p[NIJK_MTR + 4];
+  z.ndm = p[NDIMDX_MTR];
+  z.typ = (int)p[ITYPZONE]; z.iflow = (int)p[IFLOW]; z.kflu = (int)p[KFLUDOM];
+  z.slope = (int)p[SLOPE]; z.neq = (int)p[NEQ]; z.itypcp = (int)p[ITYPCP];
+  z.rk = (int)p[RK]; z.dtloc = (int)p[DTLOC];
+  z.gam = r[GAMMA];
+  z.cv = r[CVINF];
+  z.rgp = r[CVINF] * (z.gam - 1.);
+  z.gam1 = z.gam / (z.gam - 1.);
+  z.gam3 = z.gam1 / r[PRANDT] * z.rgp;
+  z.dtc = r[DTC];
+  z.psiroe = r[PSIROE];
+  z.wig_cte = r[WIG_AMP];
+  z.tmin_1 = 100. / r[TINF];
+  double uref = r[VINF], roref = r[ROINF];
+  z.c1 = 0.02 * uref;
+  z.c2 = 0.02 / (uref * roref);
+  z.c3 = -2.;
+  double c6 = 1. / 6.;
+  z.c4 = 5. * c6;
+  z.c5 = 2. * c6;
+  z.c6 = -1. * c6;
+  z.cvisq = 1. / 3;
+  z.tcx = ti[0]; z.tcy = tj[0]; z.tcz = tk[0];
+  z.si = std::fabs(z.tcx); z.sj = std::fabs(z.tcy); z.sk = std::fabs(z.tcz);
+  z.volinv = 0.5 / vol[0];
+  z.prandt = r[PRANDT]; z.xmul0 = r[XMUL0]; z.temp0 = r[TEMP0]; z.cs = r[CS];
+  Z.cmus1 = r[CS];
+  double temp01 = 1. / r[TEMP0];
+  Z.coesut = r[XMUL0] * (1. + Z.cmus1 * temp01) * std::sqrt(temp01);
+}
+
+// ------------------------------------------------------------- C ABI
+extern "C" {
+
+const char* fgb_last_error(void) { return g_err.c_str(); }
+
+int fgb_version(int* major, int* minor, int* sm) {
+  if (major) *major = 1;
+  if (minor) *minor = 0;
+  if (sm) *sm = 103;
+  return FGB_OK;
+}
+
+int fgb_create(int device, fgb_solver** out) {
+  if (!out) return fail(FGB_ERR_ARG, "null output pointer");
+  int n = 0;
+  CK(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(FGB_ERR_ARG, "no such CUDA device");
+  CK(cudaSetDevice(device));
+  fgb_solver* s = new fgb_solver();
+  s->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete s; return fail(FGB_ERR_CUDA, cudaGetErrorString(e)); }
+  *out = s;
+  return FGB_OK;
+}
+
+int fgb_destroy(fgb_solver* s) {
+  if (!s) return FGB_OK;
+  cudaSetDevice(s->device);
+  cudaStreamSynchronize(s->st);
+  for (ZoneData& Z : s->zones) {
+    for (int i = 0; i < 3; i++) cudaFree(Z.lvl[i]);
+    cudaFree(Z.scratch); cudaFree(Z.drodm); cudaFree(Z.coe); cudaFree(Z.xmut); cudaFree(Z.rdm);
+    cudaFree(Z.ti); cudaFree(Z.tj); cudaFree(Z.tk); cudaFree(Z.vol);
+    cudaFree(Z.Fi); cudaFree(Z.Fj); cudaFree(Z.Fk);
+    for (GatherList& g : Z.bcs) { cudaFree(g.dst); cudaFree(g.src); }
+    cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
+  }
+  for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
+  for (auto& e : s->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+  for (auto e : s->pool) cudaEventDestroy(e);
+  if (s->t0) cudaEventDestroy(s->t0);
+  if (s->t1) cudaEventDestroy(s->t1);
+  cudaStreamDestroy(s->st);
+  delete s;
+  return FGB_OK;
+}
+
+int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
+                 const double* param_real, int64_t n_real, const double* ti,
+                 const double* tj, const double* tk, const double* vol, int* zone_id) {
+  if (!s || !param_int || !param_real || !ti || !tj || !tk || !vol)
+    return fail(FGB_ERR_ARG, "null argument");
+  if (n_int < 137 || n_real < 73) return fail(FGB_ERR_ARG, "param_int/param_real too short");
+  CK(cudaSetDevice(s->device));
+  ZoneData Z;
+  Z.pi.assign(param_int, param_int + n_int);
+  Z.pr.assign(param_real, param_real + n_real);
+  const std::vector<int64_t>& p = Z.pi;
+  if (p[ITYPZONE] != Z3DCART && p[ITYPZONE] != Z3DFULL)
+    return fail(FGB_ERR_ARG, "zone type " + std::to_string(p[ITYPZONE]) + " not supported on the GPU path");
+  if (p[NEQ] != 5) return fail(FGB_ERR_ARG, "only 5-equation models are supported on the GPU path");
+  if (p[NIJK + 3] != 2 || p[NIJK + 4] != 2) return fail(FGB_ERR_ARG, "two ghost layers expected");
+  if (p[NDIMDX] != p[NIJK] * p[NIJK + 1] * p[NIJK + 2])
+    return fail(FGB_ERR_ARG, "NDIMDX inconsistent with NIJK (shiftvar must be 0)");
+  if (p[NDIMDX] >= (int64_t)INT32_MAX / 2) return fail(FGB_ERR_ARG, "zone too large");
+  if (p[ITYPCP] <= 1 && (p[NB_RELAX] > 1 || p[LU_MATCH] != 0))
+    return fail(FGB_ERR_ARG, "only nb_relax=1, lu_match=0 LU-SGS is supported");
+  if (p[ITYPCP] > 1 && p[RK] != 3) return fail(FGB_ERR_ARG, "explicit path needs rk=3");
+  if (p[EXPLOC] != 0 || p[DTLOC] != 0 || p[LALE] != 0)
+    return fail(FGB_ERR_ARG, "local time stepping and moving meshes are not supported");
+  int64_t nd = p[NDIMDX], neq = p[NEQ], ndm = p[NDIMDX_MTR];
+  int64_t nmtr_ij = p[ITYPZONE] == Z3DCART ? 1 : 3;
+  std::vector<double> hti(ti, ti + ndm * nmtr_ij), htj(tj, tj + ndm * nmtr_ij),
+      htk(tk, tk + ndm * nmtr_ij), hvol(vol, vol + ndm);
+  fill_zone(Z, ti, tj, tk, vol);
+  if (Z.z.iflow >= 2 && Z.z.typ != Z3DCART)
+    return fail(FGB_ERR_ARG, "viscous fluxes on curvilinear zones are not implemented on the GPU path");
+  size_t st_bytes = sizeof(double) * neq * nd;
+  for (int i = 0; i < 3; i++) {
+    CK(cudaMalloc(&Z.lvl[i], st_bytes));
+    CK(cudaMemset(Z.lvl[i], 0, st_bytes));
+  }
+  CK(cudaMalloc(&Z.scratch, st_bytes));
+  CK(cudaMalloc(&Z.drodm, st_bytes));
+  CK(cudaMemset(Z.drodm, 0, st_bytes));
+  CK(cudaMalloc(&Z.coe, sizeof(double) * 5 * nd));
+  CK(cudaMemset(Z.coe, 0, sizeof(double) * 5 * nd));
+  CK(cudaMalloc(&Z.xmut, sizeof(double) * nd));
+  CK(cudaMemset(Z.xmut, 0, sizeof(double) * nd));
+  CK(dev_upload(&Z.ti, hti)); CK(dev_upload(&Z.tj, htj));
+  CK(dev_upload(&Z.tk, htk)); CK(dev_upload(&Z.vol, hvol));
+  Z.z.ti = Z.ti; Z.z.tj = Z.tj; Z.z.tk = Z.tk; Z.z.vol = Z.vol;
+  int64_t ni = Z.z.ni, nj = Z.z.nj, nk = Z.z.nk;
+  CK(cudaMalloc(&Z.Fi, sizeof(double) * 5 * (ni + 1) * nj * nk));
+  CK(cudaMalloc(&Z.Fj, sizeof(double) * 5 * ni * (nj + 1) * nk));
+  CK(cudaMalloc(&Z.Fk, sizeof(double) * 5 * ni * nj * (nk + 1)));
+  for (int d = 0; d < 3; d++) {
+    int64_t q = p[IJKV + d] / p[SIZE_SSDOM + d];
+    Z.ijkv_lu[d] = q > 1 ? q : 1;
+  }
+  Z.n_rdm = p[NSSITER] * neq * 2 * Z.ijkv_lu[0] * Z.ijkv_lu[1] * Z.ijkv_lu[2];
+  CK(cudaMalloc(&Z.rdm, sizeof(double) * Z.n_rdm));
+  CK(cudaMemset(Z.rdm, 0, sizeof(double) * Z.n_rdm));
+  int rc = build_ghost_lists(Z);
+  if (rc != FGB_OK) return rc;
+  s->zones.push_back(Z);
+  if (zone_id) *zone_id = (int)s->zones.size() - 1;
+  return FGB_OK;
+}
+
+int fgb_add_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
+                     const int64_t* dnr_idx, const int64_t* rcv_idx) {
+  if (!s) return fail(FGB_ERR_ARG, "null solver");
+  if (dnr_zone < 0 || rcv_zone < 0 || dnr_zone >= (int)s->zones.size() ||
+      rcv_zone >= (int)s->zones.size())
+    return fail(FGB_ERR_ARG, "transfer zone out of range");
+  if (n < 0 || (n > 0 && (!dnr_idx || !rcv_idx))) return fail(FGB_ERR_ARG, "bad transfer list");
+  std::vector<int32_t> d(n), r(n);
+  int64_t ndd = s->zones[dnr_zone].z.nd, ndr = s->zones[rcv_zone].z.nd;
+  for (int64_t t = 0; t < n; t++) {
+    if (dnr_idx[t] < 0 || dnr_idx[t] >= ndd || rcv_idx[t] < 0 || rcv_idx[t] >= ndr)
+      return fail(FGB_ERR_ARG, "transfer index out of range");
+    d[t] = (int32_t)dnr_idx[t];
+    r[t] = (int32_t)rcv_idx[t];
+  }
+  CK(cudaSetDevice(s->device));
+  Transfer T{dnr_zone, rcv_zone, n, nullptr, nullptr};
+  CK(dev_upload(&T.dnr_idx, d));
+  CK(dev_upload(&T.rcv_idx, r));
+  s->tr.push_back(T);
+  return FGB_OK;
+}
+
+int fgb_set_option(fgb_solver* s, const char* key, double value) {
+  if (!s || !key) return fail(FGB_ERR_ARG, "null argument");
+  std::string k(key);
+  if (k == "lu_precision") {
+    if (value != 64. && value != 32.) return fail(FGB_ERR_ARG, "lu_precision must be 64 or 32");
+    s->lu_precision = (int)value;
+  } else if (k == "modulo_verif") {
+    if (value < 1) return fail(FGB_ERR_ARG, "modulo_verif must be >= 1");
+    s->modulo_verif = (int)value;
+  } else if (k == "first_it") {
+    s->first_it = value != 0.;
+  } else if (k == "profile") {
+    s->profile = value != 0.;
+  } else {
+    return fail(FGB_ERR_ARG, "unknown option " + k);
+  }
+  return FGB_OK;
+}
+
+int fgb_get_option(fgb_solver* s, const char* key, double* value) {
+  if (!s || !key || !value) return fail(FGB_ERR_ARG, "null argument");
+  std::string k(key);
+  if (k == "lu_precision") *value = s->lu_precision;
+  else if (k == "modulo_verif") *value = s->modulo_verif;
+  else if (k == "first_it") *value = s->first_it;
+  else if (k == "profile") *value = s->profile;
+  else return fail(FGB_ERR_ARG, "unknown option " + k);
+  return FGB_OK;
+}
+
+static int check_zone(fgb_solver* s, int zone) {
+  if (!s) return fail(FGB_ERR_ARG, "null solver");
+  if (zone < 0 || zone >= (int)s->zones.size()) return fail(FGB_ERR_ARG, "zone out of range");
+  return FGB_OK;
+}
+
+int fgb_upload_state(fgb_solver* s, int zone, int level, const double* host) {
+  int rc = check_zone(s, zone);
+  if (rc) return rc;
+  if (level < 0 || level > 2 || !host) return fail(FGB_ERR_ARG, "bad level or buffer");
+  ZoneData& Z = s->zones[zone];
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpyAsync(Z.lvl[level], host, sizeof(double) * Z.z.neq * Z.z.nd,
+                     cudaMemcpyHostToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return FGB_OK;
+}
+
+int fgb_download_state(fgb_solver* s, int zone, int level, double* host) {
+  int rc = check_zone(s, zone);
+  if (rc) return rc;
+  if (level < 0 || level > 2 || !host) return fail(FGB_ERR_ARG, "bad level or buffer");
+  ZoneData& Z = s->zones[zone];
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpyAsync(host, Z.lvl[level], sizeof(double) * Z.z.neq * Z.z.nd,
+                     cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return FGB_OK;
+}
+
+int fgb_download_work(fgb_solver* s, int zone, const char* which, double* host, int64_t n) {
+  int rc = check_zone(s, zone);
+  if (rc) return rc;
+  if (!which || !host) return fail(FGB_ERR_ARG, "null argument");
+  ZoneData& Z = s->zones[zone];
+  std::string w(which);
+  const double* src = nullptr;
+  int64_t need = 0;
+  if (w == "drodm") { src = Z.drodm; need = Z.z.neq * Z.z.nd; }
+  else if (w == "coe") { src = Z.coe; need = 5 * Z.z.nd; }
+  else if (w == "xmut") { src = Z.xmut; need = Z.z.nd; }
+  else if (w == "rdm") { src = Z.rdm; need = Z.n_rdm; }
+  else return fail(FGB_ERR_ARG, "unknown work array " + w);
+  if (n < need) return fail(FGB_ERR_ARG, "buffer too small for " + w);
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpyAsync(host, src, sizeof(double) * need, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return FGB_OK;
+}
+
+// ghost fill of one level of every zone: transfers, face BCs, edges/corners
+static int ghost_fill(fgb_solver* s, int level) {
+  for (Transfer& T : s->tr) {
+    ZoneData& D = s->zones[T.dnr];
+    ZoneData& R = s->zones[T.rcv];
+    CK(launch_gather(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, T.rcv_idx, T.dnr_idx, T.n,
+                     R.z.neq, 0, 1., s->st));
+    s->launches++;
+  }
+  for (ZoneData& Z : s->zones) {
+    for (GatherList& g : Z.bcs) {
+      CK(launch_gather(Z.lvl[level], Z.z.nd, Z.lvl[level], Z.z.nd, g.dst, g.src, g.n, Z.z.neq,
+                       g.op, 1., s->st));
+      s->launches++;
+    }
+    CK(launch_coins(Z.lvl[level], Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n,
+                    Z.z.neq, s->st));
+    s->launches++;
+  }
+  return FGB_OK;
+}
+
+int fgb_apply_bc(fgb_solver* s, int level) {
+  if (!s) return fail(FGB_ERR_ARG, "null solver");
+  if (level < 0 || level > 2) return fail(FGB_ERR_ARG, "bad level");
+  CK(cudaSetDevice(s->device));
+  return ghost_fill(s, level);
+}
+
+int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int layer_mode,
+                int nit_c) {
+  if (!s) return fail(FGB_ERR_ARG, "null solver");
+  if (s->zones.empty()) return fail(FGB_ERR_STATE, "no zone");
+  if (layer_mode != 1) return fail(FGB_ERR_ARG, "only layer_mode=1 (the C layer) is supported");
+  if (nstep_deb < 1 || nstep_fin < nstep_deb || nit_c < 1) return fail(FGB_ERR_ARG, "bad step range");
+  if (s->lu_precision != 64) return fail(FGB_ERR_ARG, "FP32 LU sweeps are not available");
+  CK(cudaSetDevice(s->device));
+  const std::vector<int64_t>& p0 = s->zones[0].pi;
+  const int64_t nssiter = p0[NSSITER];
+  const bool implicit = p0[ITYPCP] <= 1;
+  for (ZoneData& Z : s->zones)
+    if ((Z.pi[ITYPCP] <= 1) != implicit || Z.pi[NSSITER] != nssiter)
+      return fail(FGB_ERR_ARG, "all zones must share the temporal scheme");
+  const double cxsi1 = -0.6830127018922193, cxsi2 = -4. / 3.;
+  const double cg[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
+  for (int it = 0; it < nit_c; it++) {
+    int64_t nitrun_loc = (int64_t)nitrun * nit_c + it;
+    for (int nstep = nstep_deb; nstep <= nstep_fin; nstep++) {
+      int verif = 0, lexit_lu = 0;
+      if (nitrun_loc % s->modulo_verif == 0) {
+        verif = 1;
+        if (nstep == nssiter && implicit) lexit_lu = 1;
+      }
+      if (!verif && nstep == nssiter && p0[ITYPCP] == 1) continue;  // computePT.cpp:581
+      if (verif) s->nit_recorded = nstep;
+      for (ZoneData& Z : s->zones) {
+        Zone& z = Z.z;
+        double* ssiter;
+        double* out;
+        if (nstep == 1) { ssiter = Z.lvl[0]; out = Z.lvl[2]; }
+        else if (implicit) { ssiter = Z.lvl[2]; out = Z.lvl[2]; }
+        else if (nstep % 2 == 0) { ssiter = Z.lvl[2]; out = Z.lvl[0]; }
+        else { ssiter = Z.lvl[0]; out = Z.lvl[2]; }
+        if (nstep == 1) {  // navier_stokes_struct.for:226-296 (first sub-step only)
+          CoeArgs ca{};
+          ca.rop = ssiter; ca.xmut_in = Z.xmut; ca.xmut = Z.xmut; ca.coe = Z.coe;
+          int64_t g = implicit ? 2 : (z.iflow == 2 ? 1 : 0);
+          int64_t gk = implicit ? z.ngk : (z.iflow == 2 ? (z.ngk ? 1 : 0) : 0);
+          ca.lo[0] = 1 - g; ca.hi[0] = z.ni + g;
+          ca.lo[1] = 1 - g; ca.hi[1] = z.nj + g;
+          ca.lo[2] = 1 - gk; ca.hi[2] = z.nk + gk;
+          ca.do_invist = z.iflow == 2;
+          ca.do_lu = implicit;
+          ca.first_it = s->first_it;
+          ca.coesut = Z.coesut; ca.cmus1 = Z.cmus1;
+          {
+            ProfScope ps(s, "coefficients");
+            CK(launch_coefficients(z, ca, s->st));
+          }
+          s->launches++;
+        }
+        cudaError_t e;
+        {
+          ProfScope ps(s, "face_flux");
+          e = launch_faces(z, ssiter, Z.xmut, Z.Fi, Z.Fj, Z.Fk, s->st);
+        }
+        if (e == cudaErrorNotSupported)
+          return fail(FGB_ERR_ARG, "scheme/slope/zone combination not implemented on the GPU path");
+        CK(e);
+        s->launches += 3;
+        StageArgs sa{};
+        sa.Fi = Z.Fi; sa.Fj = Z.Fj; sa.Fk = Z.Fk; sa.drodm = Z.drodm; sa.coe = Z.coe;
+        sa.rop_in = ssiter; sa.rop_out = out; sa.rop_n = Z.lvl[0]; sa.rop_n1 = Z.lvl[1];
+        if (implicit) {
+          sa.zero_init = 1;
+          if (s->first_it == 0 || z.dtloc == 1) { sa.c1 = -1.; sa.c2 = 1.; sa.c3 = 0.; }
+          else { sa.c1 = -1.5; sa.c2 = 2.; sa.c3 = -0.5; }
+          sa.first_sub = nstep == 1;
+        } else {
+          sa.zero_init = nstep == 1;
+          sa.coefH = nstep == 2 ? cxsi1 : (nstep == 3 ? cxsi2 : 0.);
+          sa.coefW = cg[nstep <= 3 ? nstep : 0];
+        }
+        {
+          ProfScope ps(s, implicit ? "assemble_bdf" : "assemble_rk3");
+          CK(launch_assemble(z, sa, implicit, s->st));
+        }
+        s->launches++;
+        if (implicit) {
+          if (verif) {  // lhs.cpp residus_navier.h -> cprdu3s1
+            NormArgs na{};
+            na.drodm = Z.drodm; na.rdm = Z.rdm; na.nssiter = nssiter; na.it_bloc = nstep;
+            na.neq = z.neq;
+            for (int d = 0; d < 3; d++) { na.ijkv_lu[d] = Z.ijkv_lu[d]; na.size[d] = Z.pi[SIZE_SSDOM + d]; }
+            ProfScope ps(s, "block_norms");
+            CK(launch_norms(z, na, s->st));
+            s->launches++;
+          }
+          if (!lexit_lu) {  // lhs.cpp -> invlu (lower, upper + mjr_newton)
+            LuArgs la{};
+            bool inplace = ssiter == out;
+            la.rop_old = ssiter;
+            la.rop_new = inplace ? Z.scratch : out;
+            la.rop_knb = inplace ? Z.scratch : ssiter;
+            la.coe = Z.coe; la.din = Z.drodm; la.dout = Z.drodm;
+            {
+              ProfScope ps(s, "lu_sgs");
+              CK(launch_lusgs(z, la, s->st));
+            }
+            s->launches += 2 * (z.ni + z.nj + z.nk - 2);
+            if (inplace) std::swap(Z.lvl[2], Z.scratch);
+          }
+        }
+      }
+      int wl = (implicit || nstep % 2 == 1) ? 2 : 0;
+      int rc;
+      {
+        ProfScope ps(s, "ghost_fill");
+        rc = ghost_fill(s, wl);
+      }
+      if (rc) return rc;
+    }
+    s->first_it = 1;
+    for (ZoneData& Z : s->zones) {
+      double* save = Z.lvl[1];
+      Z.lvl[1] = Z.lvl[0];
+      Z.lvl[0] = Z.lvl[2];
+      Z.lvl[2] = save;
+    }
+  }
+  return FGB_OK;
+}
+
+int fgb_residuals(fgb_solver* s, int zone, double* out, int64_t n, int* nit_out) {
+  int rc = check_zone(s, zone);
+  if (rc) return rc;
+  ZoneData& Z = s->zones[zone];
+  int64_t nssiter = Z.pi[NSSITER], neq = Z.z.neq;
+  int nit = s->nit_recorded;
+  if (nit_out) *nit_out = nit;
+  if (!out || n < 2 * neq * nit) return fail(FGB_ERR_ARG, "output buffer too small");
+  std::vector<double> h(Z.n_rdm);
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpyAsync(h.data(), Z.rdm, sizeof(double) * Z.n_rdm, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  double xpt_1 = 1. / (double)(Z.z.ni * Z.z.nj * Z.z.nk);
+  for (int64_t ne = 0; ne < neq; ne++)
+    for (int i = 0; i < nit; i++) {
+      double rmax = 0., rmoy = 0.;
+      for (int64_t k = 0; k < Z.ijkv_lu[2]; k++)
+        for (int64_t j = 0; j < Z.ijkv_lu[1]; j++)
+          for (int64_t ii = 0; ii < Z.ijkv_lu[0]; ii++) {
+            int64_t no = ii + j * Z.ijkv_lu[0] + k * Z.ijkv_lu[0] * Z.ijkv_lu[1];
+            rmax = std::max(rmax, h[i + (ne + neq) * nssiter + no * neq * 2 * nssiter]);
+            rmoy = rmoy + h[i + ne * nssiter + no * neq * 2 * nssiter];
+          }
+      out[nit * ne + i] = std::sqrt(rmoy * xpt_1) / Z.pr[DTC];
+      out[nit * (ne + neq) + i] = rmax / Z.pr[DTC];
+    }
+  return FGB_OK;
+}
+
+int fgb_synchronize(fgb_solver* s) {
+  if (!s) return fail(FGB_ERR_ARG, "null solver");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->st));
+  return FGB_OK;
+}
+
+int fgb_kernel_stats(fgb_solver* s, int index, char* name, int name_len, int64_t* count,
+                     double* total_ms) {
+  if (!s || !name || name_len < 2 || !count || !total_ms) return fail(FGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->st));
+  std::vector<std::string> names;
+  for (auto& e : s->events)
+    if (std::find(names.begin(), names.end(), e.name) == names.end()) names.push_back(e.name);
+  if (index < 0) {  // reset
+    for (auto& e : s->events) { s->pool.push_back(e.a); s->pool.push_back(e.b); }
+    s->events.clear();
+    *count = (int64_t)names.size();
+    return FGB_OK;
+  }
+  if (index >= (int)names.size()) { *count = 0; *total_ms = 0.; name[0] = 0; return FGB_OK; }
+  int64_t c = 0;
+  double tot = 0.;
+  for (auto& e : s->events)
+    if (names[index] == e.name) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e.a, e.b));
+      tot += ms;
+      c++;
+    }
+  std::snprintf(name, (size_t)name_len, "%s", names[index].c_str());
+  *count = c;
+  *total_ms = tot;
+  return FGB_OK;
+}
+
+int fgb_stream_timer(fgb_solver* s, int op, double* ms) {
+  if (!s) return fail(FGB_ERR_ARG, "null solver");
+  CK(cudaSetDevice(s->device));
+  if (op == 0) {
+    if (!s->t0) CK(cudaEventCreate(&s->t0));
+    if (!s->t1) CK(cudaEventCreate(&s->t1));
+    CK(cudaEventRecord(s->t0, s->st));
+    return FGB_OK;
+  }
+  if (!s->t0 || !s->t1 || !ms) return fail(FGB_ERR_STATE, "timer not started");
+  CK(cudaEventRecord(s->t1, s->st));
+  CK(cudaEventSynchronize(s->t1));
+  float m = 0.f;
+  CK(cudaEventElapsedTime(&m, s->t0, s->t1));
+  *ms = m;
+  return FGB_OK;
+}
+
+int fgb_fp64_peak(int device, double* gflops) {
+  if (!gflops) return fail(FGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(device));
+  int nsm = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+  double* out = nullptr;
+  CK(cudaMalloc(&out, sizeof(double) * nsm * 8 * 256));
+  cudaStream_t st;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  const int iters = 4096;
+  CK(run_fp64_probe(nsm, 256, out, st));  // warm-up
+  CK(cudaEventRecord(a, st));
+  CK(run_fp64_probe(nsm, iters, out, st));
+  CK(cudaEventRecord(b, st));
+  CK(cudaEventSynchronize(b));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  double flops = 2.0 * 8.0 * iters * (double)nsm * 8 * 256;
+  *gflops = flops / (ms * 1e-3) / 1e9;
+  cudaEventDestroy(a); cudaEventDestroy(b); cudaStreamDestroy(st); cudaFree(out);
+  return FGB_OK;
+}
+
+int fgb_launch_count(fgb_solver* s, int64_t* count) {
+  if (!s || !count) return fail(FGB_ERR_ARG, "null argument");
+  *count = s->launches;
+  return FGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+// fgb_common.cuh -- zone descriptor, index maps and FP64 helpers shared by
+// the sm_103a kernels of the FastS solve step.
+//
+// Memory layout in HBM is FastS's own (FastS/FastS/formule_param.h):
+// structure-of-arrays, one contiguous block per variable,
+//   q[v*nd + l],  l = (i+ng-1) + (j+ng-1)*nip + (k+ngk-1)*nip*njp
+// with Fortran cell indices i in [1-ng, ni+ng] (ng = 2 ghost layers, ngk = 0
+// for a 2-d zone).  Keeping the reference layout makes every host<->device
+// copy a single memcpy of the pyTree's compacted time-level array.
+//
+// All FP64 kernels are compiled with --fmad=false and evaluate expressions in
+// the reference's left-to-right order, so their results are the reference
+// arithmetic bit for bit (checked against the CPU oracle in tests/).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fgb {
+
+// FastS param_int / param_real index map (FastS/FastS/param_solver.h)
+enum PI : int {
+  NIJK = 0, NIJK_MTR = 5, NIJK_XYZ = 10, IJKV = 20, MXSSDOM_LU = 24, ITYPZONE = 25,
+  IFLOW = 27, ILES = 28, ITYPCP = 29, SIZE_SSDOM = 30, KFLUDOM = 33, LALE = 34, NEQ = 36,
+  NEQ_IJ = 37, NEQ_K = 38, NEQ_COE = 39, NDIMDX = 41, NDIMDX_MTR = 43, DTLOC = 46,
+  RK = 52, LEVEL = 53, EXPLOC = 54, NSSITER = 58, SLOPE = 64, PT_BC = 70, NB_RELAX = 71,
+  LU_MATCH = 75
+};
+enum PR : int {
+  DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6, MINF = 7,
+  PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14, PSIROE = 34, WIG_AMP = 72
+};
+enum ZoneType : int { Z3DFULL = 0, Z3DHOMO = 1, Z3DCART = 2, Z2D = 3 };
+enum Scheme : int { AUSM = 1, SENSEUR = 2, ROE = 5 };
+enum Slope : int { O1 = 1, O3 = 2, MINMOD = 3 };
+
+// Everything a kernel needs about one zone; passed by value.
+struct Zone {
+  int64_t ni, nj, nk;        // interior cells (IJKV)
+  int64_t ng, ngk;           // ghost layers (i/j, k)
+  int64_t nip, njp, nkp;     // cells incl. ghosts (NIJK)
+  int64_t nd;                // NDIMDX
+  int64_t inc[3];            // cell strides i, j, k
+  int64_t minc[3];           // metric strides (NIJK_MTR)
+  int64_t mg, mgk;           // metric ghost offsets
+  int64_t ndm;               // NDIMDX_MTR
+  int typ, iflow, kflu, slope, neq, itypcp, rk, dtloc;
+  // constants of template_FluxAndBalance.for:108-156 and friends
+  double gam, rgp, gam1, gam3, cv, dtc, psiroe, wig_cte, tmin_1;
+  double c1, c2, c3, c4, c5, c6, cvisq;
+  double tcx, tcy, tcz, si, sj, sk, volinv;  // 3d cartesian metric
+  double prandt, xmul0, temp0, cs;
+  const double *ti, *tj, *tk, *vol;
+};
+
+__host__ __device__ inline int64_t inddm(const Zone& z, int64_t i, int64_t j, int64_t k) {
+  return (i + z.ng - 1) + (j + z.ng - 1) * z.nip + (k + z.ngk - 1) * z.nip * z.njp;
+}
+__host__ __device__ inline int64_t indmtr(const Zone& z, int64_t i, int64_t j, int64_t k) {
+  return (i + z.mg - 1) * z.minc[0] + (j + z.mg - 1) * z.minc[1] + (k + z.mgk - 1) * z.minc[2];
+}
+
+// Fortran intrinsics with the semantics the reference relies on
+__device__ __forceinline__ double fmaxF(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double fminF(double a, double b) { return a < b ? a : b; }
+__device__ __forceinline__ double fsignF(double a, double b) { return copysign(fabs(a), b); }
+
+// Device error word shared by all kernels of a solver (bounded waits set it).
+struct DevStatus { int code; int where; };
+
+}  // namespace fgb

@@ -1,0 +1,530 @@
+// fgb_flux.cu -- face-flux residual and fused stage updates (sm_103a).
+//
+// Replaces the per-tile loop nest of FastS/FastS/Compute/template_FluxAndBalance.for
+// (generated as ROE/*/fluroe_*.for and AUSM/*/fluausm_*.for) and the update
+// routines core3ark3.for / core3as2.for / init_rhs.for.
+//
+// GPU design.  On GB300 these FP64 kernels are bound by the FP64 pipe, not by
+// HBM, so each face flux is computed exactly once:
+//   * face_flux<D,...>: one thread per face of direction D writes the 5 flux
+//     components to a face array (SoA).  Threads run along i, so every stencil
+//     load is coalesced; reconstruction stencils are re-read through L1.
+//   * assemble<...>: one thread per interior cell adds its six face fluxes in
+//     the reference's accumulation order (+F_k lo, +F_j lo, +F_i lo, -F_i hi,
+//     -F_j hi, -F_k hi) and applies, in the same kernel, the RK3 low-storage
+//     stage update (explicit) or the BDF Newton residual (implicit).
+// The cartesian face kernels are specialised per direction at compile time:
+// products with the zero tangential metric components of a cartesian face are
+// not issued at all, which is exact (they are exact zeros in the general form).
+#include "fgb_kernels.cuh"
+
+namespace fgb {
+
+// ---------------------------------------------------------------- slopes
+// Slope/o1_slope_var.for, o3_slope_var.for, minmod_slope_var.for.
+// a = q(l-2*inc), b = q(l-inc), c = q(l), d = q(l+inc); qm = right state of
+// the face (cell l side), qp = left state.
+template <int SL>
+__device__ __forceinline__ void reconstruct(const Zone& z, double a, double b, double c, double d,
+                                            double roff, double& qm, double& qp) {
+  if (SL == O1) {
+    qm = c;
+    qp = b;
+  } else if (SL == O3) {
+    qm = z.c4 * c + z.c5 * b + z.c6 * d;
+    qp = z.c4 * b + z.c6 * a + z.c5 * c;
+  } else {  // minmod with the low-temperature cut-off roff
+    double delm = c - b, delp = d - c, delq = b - a;
+    double sm = fsignF(1., delm);
+    double slp = roff * (sm * fmaxF(0., fminF(fabs(delm), sm * delp)));
+    double sq = fsignF(1., delq);
+    double slq = roff * (sq * fmaxF(0., fminF(fabs(delq), sq * delm)));
+    qm = c - slp;
+    qp = b + slq;
+  }
+}
+
+// ------------------------------------------------------------- Roe (cart)
+// Roe average + Harten-fixed dissipation for a cartesian face of direction D
+// (Vit_ent/fludiffer_3dcart_{i,j,k}.for, etat_roe_GD.for).
+template <int D>
+__device__ __forceinline__ void roe_cart(const Zone& z, const double qm[5], const double qp[5],
+                                         double F[5]) {
+  const double tc = D == 0 ? z.tcx : (D == 1 ? z.tcy : z.tcz);
+  const double s = D == 0 ? z.si : (D == 1 ? z.sj : z.sk);
+  const double rgp = z.rgp, gam1 = z.gam1;
+  double r1 = qp[0];
+  double p1 = r1 * qp[4] * rgp;
+  double h1 = gam1 * qp[4] * rgp + .5 * (qp[1] * qp[1] + qp[2] * qp[2] + qp[3] * qp[3]);
+  double r2 = qm[0];
+  double p2 = r2 * qm[4] * rgp;
+  double h2 = gam1 * qm[4] * rgp + .5 * (qm[1] * qm[1] + qm[2] * qm[2] + qm[3] * qm[3]);
+  double s1 = sqrt(r1), s2 = sqrt(r2);
+  double r = s1 * s2;
+  double r_1 = 1. / (s1 + s2);
+  double vel[3], dvel[3];
+#pragma unroll
+  for (int m = 0; m < 3; m++) vel[m] = (s1 * qp[m + 1] + s2 * qm[m + 1]) * r_1;
+  double h = (s1 * h1 + s2 * h2) * r_1;
+  double q = .5 * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+  double c = sqrt((z.gam - 1.) * fabs(h - q));
+  double qn1 = qp[D + 1] * tc, qn2 = qm[D + 1] * tc;
+#pragma unroll
+  for (int m = 0; m < 3; m++) dvel[m] = (qm[m + 1] - qp[m + 1]) * s;
+  double dp = p2 - p1, dqn = qn2 - qn1;
+  double s_1 = 1. / fmaxF(s, 1.e-30);
+  double nn = tc * s_1;
+  double qn = vel[D] * nn;
+  double f1 = qn;
+  double f4 = z.psiroe * (fabs(f1) + c);
+  double f2 = .5 + fsignF(.5, fabs(f1) - f4);
+  double f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (r2 - r1 - dp / (c * c)) * s;
+  double fl[5];
+  fl[0] = f3 * (f1);
+#pragma unroll
+  for (int m = 0; m < 3; m++)
+    fl[m + 1] = (m == D) ? f3 * (f1 * vel[m] + r * (dvel[m] - nn * dqn))
+                         : f3 * (f1 * vel[m] + r * (dvel[m]));
+  fl[4] = f3 * (f1 * q + r * (vel[0] * dvel[0] + vel[1] * dvel[1] + vel[2] * dvel[2] - qn * dqn));
+  // lambda4 = qn + c
+  f1 = qn + c;
+  f2 = .5 + fsignF(.5, fabs(f1) - f4);
+  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (dp + r * c * dqn * s_1) / (2. * c * c) * s * f3;
+  fl[0] = fl[0] + f1;
+#pragma unroll
+  for (int m = 0; m < 3; m++) fl[m + 1] = fl[m + 1] + f1 * ((m == D) ? (vel[m] + nn * c) : vel[m]);
+  fl[4] = fl[4] + f1 * (h + qn * c);
+  // lambda5 = qn - c
+  f1 = qn - c;
+  f2 = .5 + fsignF(.5, fabs(f1) - f4);
+  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (dp - r * c * dqn * s_1) / (2. * c * c) * f3 * s;
+  fl[0] = fl[0] + f1;
+#pragma unroll
+  for (int m = 0; m < 3; m++) fl[m + 1] = fl[m + 1] + f1 * ((m == D) ? (vel[m] - nn * c) : vel[m]);
+  fl[4] = fl[4] + f1 * (h - qn * c);
+  double rou1 = r1 * qn1, rou2 = r2 * qn2, p1p2 = p1 + p2;
+  F[0] = (fl[0] + rou1 + rou2) * 0.5;
+#pragma unroll
+  for (int m = 0; m < 3; m++)
+    F[m + 1] = (m == D) ? (fl[m + 1] + rou1 * qp[m + 1] + rou2 * qm[m + 1] + tc * p1p2) * 0.5
+                        : (fl[m + 1] + rou1 * qp[m + 1] + rou2 * qm[m + 1]) * 0.5;
+  F[4] = (fl[4] + rou1 * h1 + rou2 * h2) * 0.5;
+}
+
+// ----------------------------------------------------------- Roe (general)
+// Vit_ent/fludiffer_3dfull_i.for with the face normal (tcx,tcy,tcz), |S| = s.
+__device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], const double qp[5],
+                                         double tcx, double tcy, double tcz, double s, double F[5]) {
+  const double rgp = z.rgp, gam1 = z.gam1;
+  double r1 = qp[0], p1 = r1 * qp[4] * rgp;
+  double h1 = gam1 * qp[4] * rgp + .5 * (qp[1] * qp[1] + qp[2] * qp[2] + qp[3] * qp[3]);
+  double r2 = qm[0], p2 = r2 * qm[4] * rgp;
+  double h2 = gam1 * qm[4] * rgp + .5 * (qm[1] * qm[1] + qm[2] * qm[2] + qm[3] * qm[3]);
+  double s1 = sqrt(r1), s2 = sqrt(r2);
+  double r = s1 * s2, r_1 = 1. / (s1 + s2);
+  double u = (s1 * qp[1] + s2 * qm[1]) * r_1;
+  double v = (s1 * qp[2] + s2 * qm[2]) * r_1;
+  double w = (s1 * qp[3] + s2 * qm[3]) * r_1;
+  double h = (s1 * h1 + s2 * h2) * r_1;
+  double q = .5 * (u * u + v * v + w * w);
+  double c = sqrt((z.gam - 1.) * fabs(h - q));
+  double qn1 = qp[1] * tcx + qp[2] * tcy + qp[3] * tcz;
+  double qn2 = qm[1] * tcx + qm[2] * tcy + qm[3] * tcz;
+  double du = (qm[1] - qp[1]) * s, dv = (qm[2] - qp[2]) * s, dw = (qm[3] - qp[3]) * s;
+  double dp = p2 - p1, dqn = qn2 - qn1;
+  double s_1 = 1.0 / fmaxF(s, 1.E-30);
+  double nx = tcx * s_1, ny = tcy * s_1, nz = tcz * s_1;
+  double qn = u * nx + v * ny + w * nz;
+  double f1 = qn;
+  double f4 = z.psiroe * (fabs(f1) + c);
+  double f2 = 0.5 + fsignF(0.5, fabs(f1) - f4);
+  double f3 = (f2 - 1.0) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (r2 - r1 - dp / (c * c)) * s;
+  double fl1 = f3 * (f1);
+  double fl2 = f3 * (f1 * u + r * (du - nx * dqn));
+  double fl3 = f3 * (f1 * v + r * (dv - ny * dqn));
+  double fl4 = f3 * (f1 * w + r * (dw - nz * dqn));
+  double fl5 = f3 * (f1 * q + r * (u * du + v * dv + w * dw - qn * dqn));
+  f1 = qn + c;
+  f2 = 0.5 + fsignF(0.5, fabs(f1) - f4);
+  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (dp + r * c * dqn * s_1) / (2. * c * c) * s * f3;
+  fl1 = fl1 + f1;
+  fl2 = fl2 + f1 * (u + nx * c);
+  fl3 = fl3 + f1 * (v + ny * c);
+  fl4 = fl4 + f1 * (w + nz * c);
+  fl5 = fl5 + f1 * (h + qn * c);
+  f1 = qn - c;
+  f2 = 0.5 + fsignF(0.5, fabs(f1) - f4);
+  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (dp - r * c * dqn * s_1) / (2. * c * c) * f3 * s;
+  fl1 = fl1 + f1;
+  fl2 = fl2 + f1 * (u - nx * c);
+  fl3 = fl3 + f1 * (v - ny * c);
+  fl4 = fl4 + f1 * (w - nz * c);
+  fl5 = fl5 + f1 * (h - qn * c);
+  double rou1 = r1 * qn1, rou2 = r2 * qn2, p1p2 = p1 + p2;
+  F[0] = (fl1 + rou1 + rou2) * 0.5;
+  F[1] = (fl2 + rou1 * qp[1] + rou2 * qm[1] + tcx * p1p2) * 0.5;
+  F[2] = (fl3 + rou1 * qp[2] + rou2 * qm[2] + tcy * p1p2) * 0.5;
+  F[3] = (fl4 + rou1 * qp[3] + rou2 * qm[3] + tcz * p1p2) * 0.5;
+  F[4] = (fl5 + rou1 * h1 + rou2 * h2) * 0.5;
+}
+
+// ------------------------------------------------------------- AUSM+(P)
+// AUSM/fluFaceEuler.for:36-57 + etat_GD.for + Vit_ent/fluvector_*.for.
+// NX = number of non-zero normal components the face can have (1: cartesian
+// face of direction D, 3: general).
+template <int D, bool CART>
+__device__ __forceinline__ void ausm_face(const Zone& z, const double qm[5], const double qp[5],
+                                          double tl, double tcx, double tcy, double tcz,
+                                          double s, double F[5]) {
+  const double rgp = z.rgp, gam1 = z.gam1;
+  double r1 = qp[0], rou1 = r1 * qp[1], rov1 = r1 * qp[2], row1 = r1 * qp[3];
+  double p1 = r1 * qp[4] * rgp;
+  double h1 = gam1 * p1 + .5 * (rou1 * qp[1] + rov1 * qp[2] + row1 * qp[3]);
+  double r2 = qm[0], rou2 = r2 * qm[1], rov2 = r2 * qm[2], row2 = r2 * qm[3];
+  double p2 = r2 * qm[4] * rgp;
+  double h2 = gam1 * p2 + .5 * (rou2 * qm[1] + rov2 * qm[2] + row2 * qm[3]);
+  double qn1, qn2;
+  if (CART) {
+    const double tc = D == 0 ? tcx : (D == 1 ? tcy : tcz);
+    qn1 = qp[D + 1] * tc;
+    qn2 = qm[D + 1] * tc;
+  } else {
+    qn1 = qp[1] * tcx + qp[2] * tcy + qp[3] * tcz;
+    qn2 = qm[1] * tcx + qm[2] * tcy + qm[3] * tcz;
+  }
+  double cc = rgp * z.gam * tl;  // c^2 from the temperature of cell l
+  double son = sqrt(qn1 * qn1 / cc);
+  double tam = z.c3 * son + s;
+  double tam1 = fmaxF(0., tam) * z.c2;
+  double u = 0.25 * (qn1 + qn2) - tam1 * (p2 - p1);
+  double tdu = fmaxF(fabs(u), z.c1 * s) * z.wig_cte;
+  double p1p2 = (p1 + p2) * 0.5;
+  F[0] = u * (r1 + r2) - tdu * (r2 - r1);
+  F[1] = u * (rou1 + rou2) - tdu * (rou2 - rou1);
+  F[2] = u * (rov1 + rov2) - tdu * (rov2 - rov1);
+  F[3] = u * (row1 + row2) - tdu * (row2 - row1);
+  F[4] = u * (h1 + h2) - tdu * (h2 - h1);
+  if (CART) {
+    const double tc = D == 0 ? tcx : (D == 1 ? tcy : tcz);
+    F[D + 1] = F[D + 1] + tc * p1p2;
+  } else {
+    F[1] = F[1] + tcx * p1p2;
+    F[2] = F[2] + tcy * p1p2;
+    F[3] = F[3] + tcz * p1p2;
+  }
+}
+
+// ------------------------------------------------------ viscous (cart)
+// fluvisq_3dcart_{i,j,k}.for + mut_interface.for.  Face D of cell l.
+template <int D>
+__device__ __forceinline__ void visc_cart(const Zone& z, const double* __restrict__ q,
+                                          const double* __restrict__ xmut, int64_t l, double F[5]) {
+  const int64_t nd = z.nd;
+  const double* U = q + nd;
+  const double* V = q + 2 * nd;
+  const double* W = q + 3 * nd;
+  const double* T = q + 4 * nd;
+  const int64_t ii = z.inc[0], ij = z.inc[1], ik = z.inc[2];
+  const double tcx = z.tcx, tcy = z.tcy, tcz = z.tcz, cvisq = z.cvisq;
+  // neighbours of the two cells (il = l - inc_D, ir = l) in the two
+  // transverse directions; a = first transverse, b = second transverse
+  const int64_t inD = D == 0 ? ii : (D == 1 ? ij : ik);
+  const int64_t il = l - inD, ir = l;
+  double fv, fv5;
+  if (D == 0) {
+    const double tix = tcx, tjy = .25 * tcy, tkz = .25 * tcz;
+    double f1 = U[il], f2 = U[ir], s = f1 + f2;
+    double f3 = s + U[l - ii - ij] + U[l - ij];
+    double f4 = s + U[l - ii + ij] + U[l + ij];
+    double f5 = s + U[l - ii - ik] + U[l - ik];
+    double f6 = s + U[l - ii + ik] + U[l + ik];
+    double gUx = (f2 - f1) * tix, gUy = (f4 - f3) * tjy, gUz = (f6 - f5) * tkz;
+    f1 = V[il]; f2 = V[ir]; s = f1 + f2;
+    f3 = s + V[l - ii - ij] + V[l - ij];
+    f4 = s + V[l - ii + ij] + V[l + ij];
+    double gVx = (f2 - f1) * tix, gVy = (f4 - f3) * tjy;
+    f1 = W[il]; f2 = W[ir]; s = f1 + f2;
+    f5 = s + W[l - ii - ik] + W[l - ik];
+    f6 = s + W[l - ii + ik] + W[l + ik];
+    double gWx = (f2 - f1) * tix, gWz = (f6 - f5) * tkz;
+    double gTx = (T[ir] - T[il]) * tix;
+    double div = (gUx + gVy + gWz) * cvisq;
+    double e1 = gUx - div, e2 = gUy + gVx, e3 = gUz + gWx;
+    double xmutvol = (xmut[ir] + xmut[il]) * z.volinv;
+    double xktvol = xmutvol * z.gam3;
+    fv = -(2. * e1 * tcx) * xmutvol;
+    fv5 = fv * (U[ir] + U[il]);
+    F[1] = F[1] + fv;
+    fv = -(e2 * tcx) * xmutvol;
+    fv5 = fv5 + fv * (V[ir] + V[il]);
+    F[2] = F[2] + fv;
+    fv = -(e3 * tcx) * xmutvol;
+    fv5 = fv5 + fv * (W[ir] + W[il]);
+    F[3] = F[3] + fv;
+    fv = fv5 * 0.5 - (gTx * tcx) * xktvol;
+    F[4] = F[4] + fv;
+  } else if (D == 1) {
+    const double tiy = tcy, tjz = .25 * tcz, tkx = .25 * tcx;
+    double f1 = U[il], f2 = U[ir], s = f1 + f2;
+    double f5 = s + U[l - ii - ij] + U[l - ii];
+    double f6 = s + U[l + ii - ij] + U[l + ii];
+    double gUx = (f6 - f5) * tkx, gUy = (f2 - f1) * tiy;
+    f1 = V[il]; f2 = V[ir]; s = f1 + f2;
+    double f3 = s + V[l - ij - ik] + V[l - ik];
+    double f4 = s + V[l - ij + ik] + V[l + ik];
+    f5 = s + V[l - ii - ij] + V[l - ii];
+    f6 = s + V[l + ii - ij] + V[l + ii];
+    double gVx = (f6 - f5) * tkx, gVy = (f2 - f1) * tiy, gVz = (f4 - f3) * tjz;
+    f1 = W[il]; f2 = W[ir]; s = f1 + f2;
+    f3 = s + W[l - ij - ik] + W[l - ik];
+    f4 = s + W[l - ij + ik] + W[l + ik];
+    double gWy = (f2 - f1) * tiy, gWz = (f4 - f3) * tjz;
+    double gTy = (T[ir] - T[il]) * tiy;
+    double div = (gUx + gVy + gWz) * cvisq;
+    double e2 = gUy + gVx, e4 = gVy - div, e5 = gVz + gWy;
+    double xmutvol = (xmut[ir] + xmut[il]) * z.volinv;
+    double xktvol = xmutvol * z.gam3;
+    fv = -(e2 * tcy) * xmutvol;
+    fv5 = fv * (U[ir] + U[il]);
+    F[1] = F[1] + fv;
+    fv = -(2. * e4 * tcy) * xmutvol;
+    fv5 = fv5 + fv * (V[ir] + V[il]);
+    F[2] = F[2] + fv;
+    fv = -(e5 * tcy) * xmutvol;
+    fv5 = fv5 + fv * (W[ir] + W[il]);
+    F[3] = F[3] + fv;
+    fv = fv5 * 0.5 - (gTy * tcy) * xktvol;
+    F[4] = F[4] + fv;
+  } else {
+    const double tiz = tcz, tky = 0.25 * tcy, tjx = 0.25 * tcx;
+    double f1 = U[il], f2 = U[ir], s = f1 + f2;
+    double f3 = s + U[l - ii - ik] + U[l - ii];
+    double f4 = s + U[l + ii - ik] + U[l + ii];
+    double gUx = (f4 - f3) * tjx, gUz = (f2 - f1) * tiz;
+    f1 = V[il]; f2 = V[ir]; s = f1 + f2;
+    double f5 = s + V[l - ij - ik] + V[l - ij];
+    double f6 = s + V[l + ij - ik] + V[l + ij];
+    double gVy = (f6 - f5) * tky, gVz = (f2 - f1) * tiz;
+    f1 = W[il]; f2 = W[ir]; s = f1 + f2;
+    f3 = s + W[l - ii - ik] + W[l - ii];
+    f4 = s + W[l + ii - ik] + W[l + ii];
+    f5 = s + W[l - ij - ik] + W[l - ij];
+    f6 = s + W[l + ij - ik] + W[l + ij];
+    double gWx = (f4 - f3) * tjx, gWy = (f6 - f5) * tky, gWz = (f2 - f1) * tiz;
+    double gTz = (T[ir] - T[il]) * tiz;
+    double div = (gUx + gVy + gWz) * cvisq;
+    double e3 = gUz + gWx, e5 = gVz + gWy, e6 = gWz - div;
+    double xmutvol = (xmut[ir] + xmut[il]) * z.volinv;
+    double xktvol = xmutvol * z.gam3;
+    fv = -e3 * tcz * xmutvol;
+    fv5 = fv * (U[ir] + U[il]);
+    F[1] = F[1] + fv;
+    fv = -e5 * tcz * xmutvol;
+    fv5 = fv5 + fv * (V[ir] + V[il]);
+    F[2] = F[2] + fv;
+    fv = -2. * e6 * tcz * xmutvol;
+    fv5 = fv5 + fv * (W[ir] + W[il]);
+    F[3] = F[3] + fv;
+    fv = fv5 * 0.5 - gTz * tcz * xktvol;
+    F[4] = F[4] + fv;
+  }
+}
+
+// ------------------------------------------------------------- face kernel
+// One thread per face of direction D; faces of direction D are indexed
+// f = ii + NI*(jj + NJ*kk) over the interior face box (NI = ni+1 for D=0 ...).
+template <int D, int TYP, int KF, int SL, bool VISC>
+__global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restrict__ q,
+                                                 const double* __restrict__ xmut,
+                                                 double* __restrict__ Fo) {
+  const int64_t NI = z.ni + (D == 0), NJ = z.nj + (D == 1), NK = z.nk + (D == 2);
+  const int64_t nf = NI * NJ * NK;
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int64_t ii = f % NI;
+  const int64_t r = f / NI;
+  const int64_t jj = r % NJ, kk = r / NJ;
+  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
+  const int64_t inc = z.inc[D];
+  const int64_t nd = z.nd;
+  double qm[5], qp[5];
+  double roff = 0.;
+  if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    const double* Q = q + v * nd;
+    double a = (SL == O1) ? 0. : Q[l - 2 * inc];
+    double b = Q[l - inc], c = Q[l];
+    double d = (SL == O1) ? 0. : Q[l + inc];
+    reconstruct<SL>(z, a, b, c, d, roff, qm[v], qp[v]);
+  }
+  double F[5];
+  if (TYP == Z3DCART) {
+    if (KF == ROE) roe_cart<D>(z, qm, qp, F);
+    else ausm_face<D, true>(z, qm, qp, q[l + 4 * nd], z.tcx, z.tcy, z.tcz,
+                            D == 0 ? z.si : (D == 1 ? z.sj : z.sk), F);
+    if (VISC) visc_cart<D>(z, q, xmut, l, F);
+  } else {
+    const int64_t lt = indmtr(z, ii + 1, jj + 1, kk + 1);
+    const double* t = D == 0 ? z.ti : (D == 1 ? z.tj : z.tk);
+    double tcx = t[lt], tcy = t[lt + z.ndm], tcz = t[lt + 2 * z.ndm];
+    double s = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
+    if (KF == ROE) roe_full(z, qm, qp, tcx, tcy, tcz, s, F);
+    else ausm_face<D, false>(z, qm, qp, q[l + 4 * nd], tcx, tcy, tcz, s, F);
+  }
+#pragma unroll
+  for (int v = 0; v < 5; v++) Fo[v * nf + f] = F[v];
+}
+
+// --------------------------------------------------------- assemble+update
+// cons energy of a primitive state (core3ark3.for:127-150 / core3as2.for)
+__device__ __forceinline__ double roe_of(double cv, double r, double u, double v, double w,
+                                         double t) {
+  return r * (cv * t + 0.5 * (u * u + v * v + w * w));
+}
+
+template <bool IMPL>
+__global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
+  const int64_t n = z.ni * z.nj * z.nk;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int64_t ii = t % z.ni;
+  const int64_t r = t / z.ni;
+  const int64_t jj = r % z.nj, kk = r / z.nj;
+  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
+  const int64_t nd = z.nd;
+  const int64_t nfi = (z.ni + 1) * z.nj * z.nk, nfj = z.ni * (z.nj + 1) * z.nk,
+                nfk = z.ni * z.nj * (z.nk + 1);
+  const int64_t ai = ii + (z.ni + 1) * (jj + z.nj * kk);
+  const int64_t aj = ii + z.ni * (jj + (z.nj + 1) * kk);
+  const int64_t ak = ii + z.ni * (jj + z.nj * kk);
+  double x[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    double s = a.zero_init ? 0. : a.drodm[l + v * nd] * a.coefH;
+    s = s + a.Fk[v * nfk + ak];
+    s = s + a.Fj[v * nfj + aj];
+    s = s + a.Fi[v * nfi + ai];
+    s = s - a.Fi[v * nfi + ai + 1];
+    s = s - a.Fj[v * nfj + aj + z.ni];
+    s = s - a.Fk[v * nfk + ak + z.ni * z.nj];
+    x[v] = s;
+  }
+  const double cv = z.cv;
+  if (!IMPL) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) a.drodm[l + v * nd] = x[v];
+    // core3ark3.for:99-125
+    const double* R = a.rop_in;
+    double r_1 = a.coefW * a.coe[l];
+    double tab1 = x[0] * r_1, tab2 = x[1] * r_1, tab3 = x[2] * r_1, tab4 = x[3] * r_1,
+           tab5 = x[4] * r_1;
+    double ro = R[l], u = R[l + nd], v = R[l + 2 * nd], w = R[l + 3 * nd], tt = R[l + 4 * nd];
+    double n1 = ro + tab1;
+    double rr = 1. / n1;
+    double n2 = (ro * u + tab2) * rr;
+    double n3 = (ro * v + tab3) * rr;
+    double n4 = (ro * w + tab4) * rr;
+    double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v + w * w));
+    double cvinv = 1. / cv, cvinv2 = 0.5 * cvinv;
+    double n5 = (roe_old + tab5) * rr * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
+    double* O = a.rop_out;
+    O[l] = n1; O[l + nd] = n2; O[l + 2 * nd] = n3; O[l + 3 * nd] = n4; O[l + 4 * nd] = n5;
+  } else {
+    // core3as2.for:233-330 (5 equations, 3d)
+    const double* P = a.rop_in;   // W^p (rop_ssiter)
+    const double* N = a.rop_n;    // W^n
+    const double* M = a.rop_n1;   // W^{n-1}
+    const double cf = a.coe[l];
+    double pr_ = P[l], pu = P[l + nd], pv = P[l + 2 * nd], pw = P[l + 3 * nd], pt = P[l + 4 * nd];
+    double mr = M[l], mu = M[l + nd], mv = M[l + 2 * nd], mw = M[l + 3 * nd], mt = M[l + 4 * nd];
+    double y[5];
+    if (a.first_sub) {
+      double c4 = a.c1 + a.c2;
+      y[0] = cf * x[0] + c4 * pr_ + a.c3 * mr;
+      y[1] = cf * x[1] + c4 * pu * pr_ + a.c3 * mu * mr;
+      y[2] = cf * x[2] + c4 * pv * pr_ + a.c3 * mv * mr;
+      y[3] = cf * x[3] + c4 * pw * pr_ + a.c3 * mw * mr;
+      double roe = roe_of(cv, pr_, pu, pv, pw, pt);
+      double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
+      y[4] = cf * x[4] + c4 * roe + a.c3 * roe1;
+    } else {
+      double nr = N[l], nu = N[l + nd], nv = N[l + 2 * nd], nw = N[l + 3 * nd], nt = N[l + 4 * nd];
+      y[0] = cf * x[0] + a.c1 * pr_ + a.c2 * nr + a.c3 * mr;
+      y[1] = cf * x[1] + a.c1 * pu * pr_ + a.c2 * nu * nr + a.c3 * mu * mr;
+      y[2] = cf * x[2] + a.c1 * pv * pr_ + a.c2 * nv * nr + a.c3 * mv * mr;
+      y[3] = cf * x[3] + a.c1 * pw * pr_ + a.c2 * nw * nr + a.c3 * mw * mr;
+      double roe = roe_of(cv, pr_, pu, pv, pw, pt);
+      double roen = roe_of(cv, nr, nu, nv, nw, nt);
+      double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
+      y[4] = cf * x[4] + a.c1 * roe + a.c2 * roen + a.c3 * roe1;
+    }
+#pragma unroll
+    for (int v = 0; v < 5; v++) a.drodm[l + v * nd] = y[v];
+  }
+}
+
+// ------------------------------------------------------------ host glue
+#define FGB_CHECK_LAUNCH() \
+  do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) return e_; } while (0)
+
+template <int TYP, int KF, int SL, bool VISC>
+static cudaError_t launch_faces_t(const Zone& z, const double* q, const double* xmut, double* Fi,
+                                  double* Fj, double* Fk, cudaStream_t st) {
+  const int B = 128;
+  int64_t nfi = (z.ni + 1) * z.nj * z.nk, nfj = z.ni * (z.nj + 1) * z.nk,
+          nfk = z.ni * z.nj * (z.nk + 1);
+  face_flux<0, TYP, KF, SL, VISC><<<(unsigned)((nfi + B - 1) / B), B, 0, st>>>(z, q, xmut, Fi);
+  FGB_CHECK_LAUNCH();
+  face_flux<1, TYP, KF, SL, VISC><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, xmut, Fj);
+  FGB_CHECK_LAUNCH();
+  face_flux<2, TYP, KF, SL, VISC><<<(unsigned)((nfk + B - 1) / B), B, 0, st>>>(z, q, xmut, Fk);
+  FGB_CHECK_LAUNCH();
+  return cudaSuccess;
+}
+
+// Dispatch over the (zone type, scheme, slope, viscous) combinations that the
+// reference generates for 3d zones.  Returns cudaErrorNotSupported for the
+// others (host code reports it as an argument error, never falls back).
+cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
+                         double* Fj, double* Fk, cudaStream_t st) {
+  const bool visc = z.iflow >= 2;
+  if (z.typ == Z3DCART) {
+    if (z.kflu == ROE) {
+      if (z.slope == O1) return visc ? launch_faces_t<Z3DCART, ROE, O1, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                     : launch_faces_t<Z3DCART, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O3) return visc ? launch_faces_t<Z3DCART, ROE, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                     : launch_faces_t<Z3DCART, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == MINMOD) return visc ? launch_faces_t<Z3DCART, ROE, MINMOD, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                         : launch_faces_t<Z3DCART, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
+    } else if (z.kflu == AUSM && z.slope == O3) {
+      return visc ? launch_faces_t<Z3DCART, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DCART, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+    }
+  } else if (z.typ == Z3DFULL && !visc) {
+    if (z.kflu == ROE) {
+      if (z.slope == O1) return launch_faces_t<Z3DFULL, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O3) return launch_faces_t<Z3DFULL, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == MINMOD) return launch_faces_t<Z3DFULL, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
+    } else if (z.kflu == AUSM && z.slope == O3) {
+      return launch_faces_t<Z3DFULL, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+    }
+  }
+  return cudaErrorNotSupported;
+}
+
+cudaError_t launch_assemble(const Zone& z, const StageArgs& a, bool implicit, cudaStream_t st) {
+  const int B = 256;
+  int64_t n = z.ni * z.nj * z.nk;
+  if (implicit) assemble<true><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a);
+  else assemble<false><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a);
+  return cudaGetLastError();
+}
+
+}  // namespace fgb

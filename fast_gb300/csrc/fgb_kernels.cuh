@@ -1,0 +1,64 @@
+// fgb_kernels.cuh -- launch interfaces of the solve-step kernels, shared by
+// the kernel translation units and the host orchestration (fgb_capi.cu).
+#pragma once
+#include "fgb_common.cuh"
+
+namespace fgb {
+
+// fgb_flux.cu: face fluxes + fused init_rhs / RK3 stage / BDF residual
+struct StageArgs {
+  const double* Fi; const double* Fj; const double* Fk;
+  double* drodm;
+  const double* coe;
+  // explicit: rop_out = RK stage of rop_in; implicit: BDF residual from
+  // rop_in (W^p), rop_n (W^n), rop_n1 (W^{n-1})
+  const double* rop_in; double* rop_out;
+  const double* rop_n; const double* rop_n1;
+  double coefH; int zero_init;       // init_rhs.for
+  double coefW;                      // core3ark3.for
+  double c1, c2, c3; int first_sub;  // core3as2.for
+};
+cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
+                         double* Fj, double* Fk, cudaStream_t st);
+cudaError_t launch_assemble(const Zone& z, const StageArgs& a, bool implicit, cudaStream_t st);
+
+// fgb_lu.cu: coefficients and LU-SGS
+struct CoeArgs {
+  const double* rop; const double* xmut_in; double* xmut; double* coe;
+  int64_t lo[3], hi[3];      // Fortran index range (may include ghosts)
+  int do_invist, do_lu, first_it;
+  double coesut, cmus1;      // invist.for constants
+};
+struct LuArgs {
+  const double* rop_old;  // W^p for the B matrices and the Newton update
+  const double* rop_knb;  // state read for the k+1 neighbour in the upper sweep
+  double* rop_new;        // W^{p+1}
+  const double* coe;
+  const double* din;      // Newton residual (lower sweep input)
+  double* dout;           // increment, in place over din is allowed
+  int64_t s;              // hyperplane index (i-1)+(j-1)+(k-1)
+  int64_t jlo, klo, nbj, nbk;  // (j,k) box holding the hyperplane
+};
+cudaError_t launch_coefficients(const Zone& z, const CoeArgs& a, cudaStream_t st);
+cudaError_t launch_lusgs(const Zone& z, LuArgs a, cudaStream_t st);
+
+// fgb_ghost.cu: ghost fill and residual norms
+struct NormArgs {
+  const double* drodm;
+  double* rdm;
+  int64_t ijkv_lu[3];   // number of LU blocks per direction
+  int64_t size[3];      // SIZE_SSDOM
+  int64_t nssiter;
+  int it_bloc;          // 1-based sub-iteration slot
+  int neq;
+};
+cudaError_t launch_gather(double* dst, int64_t nd_dst, const double* src, int64_t nd_src,
+                          const int32_t* d_idx, const int32_t* s_idx, int64_t n, int neq,
+                          int op, double c, cudaStream_t st);
+cudaError_t launch_coins(double* q, int64_t nd, const int32_t* dst, const int32_t* a,
+                         const int32_t* b, const int32_t* c, int64_t n_edge, int64_t n, int neq,
+                         cudaStream_t st);
+cudaError_t launch_norms(const Zone& z, const NormArgs& a, cudaStream_t st);
+cudaError_t run_fp64_probe(int nsm, int iters, double* out, cudaStream_t st);
+
+}  // namespace fgb

@@ -1,0 +1,311 @@
+"""FastS Python API of the solve step, on the GB300 library.
+
+Same entry points, arguments and tree conventions as FastS/FastS/PyTree.py:
+``warmup`` (:341), ``_compute`` (:42), ``display_temporal_criteria`` (:2039),
+``_createConvergenceHistory`` (:2152), ``_extractConvergenceHistory``
+(:2245) and ``allocate_metric`` (the ``fasts.allocate_metric`` C call).
+The work dictionary is the module global ``HOOK`` (FastC.HOOK in the
+reference); it owns the GPU solver handle.  Every numerical operation runs in
+libfastgb300.so on the GPU; this module only moves the tree's compacted
+time-level arrays to and from the device.
+"""
+from __future__ import annotations
+
+import math
+import sys
+
+import numpy as np
+
+from . import fastc as FastC
+from . import pytree as I
+from ._native import Solver
+
+HOOK: dict | None = None
+FIRST_IT = 0
+
+
+# --------------------------------------------------------------- metric
+def _coords(z):
+    gc = I.getNodeFromName1(z, "GridCoordinates")
+    return [I.getNodeFromName1(gc, n)[1] for n in ("CoordinateX", "CoordinateY", "CoordinateZ")]
+
+
+def allocate_metric(z, nssiter, verbose=0):
+    """fasts.allocate_metric (FastS/FastS/Metric/allocate_metric.cpp:40-200):
+    zone sizes into Parameter_int, zone type (FastC nature_geom_dom.for), and
+    the metric list [ti|tj|tk|vol, ti0, vent, ti_df, rdm, ind_dm, it_lu, degen]
+    (METRIC_* slots of FastS/FastS/param_solver.h)."""
+    o = I.getNodeFromName1(z, ".Solver#ownData")
+    pi = I.getNodeFromName1(o, "Parameter_int")[1]
+    dims = I.getZoneDim(z)
+    ni, nj, nk = dims[1], dims[2], dims[3]
+    ific = 2
+    pi[FastC.NIJK_XYZ:FastC.NIJK_XYZ + 5] = [ni, nj, nk, ific, 0 if nk == 2 else ific]
+    pi[FastC.NIJK:FastC.NIJK + 5] = [ni - 1, nj - 1, nk - 1, ific, 0 if nk == 2 else ific]
+    pi[FastC.IJKV:FastC.IJKV + 3] = [pi[0] - 2 * pi[3], pi[1] - 2 * pi[3], pi[2] - 2 * pi[4]]
+    pi[FastC.NDIMDX] = pi[0] * pi[1] * pi[2]
+    pi[FastC.NDIMDX_XYZ] = ni * nj * nk
+    x, y, z_ = _coords(z)
+    typ = _zone_type(x, y, z_, nk)
+    pi[FastC.ITYPZONE] = typ
+    if typ == 2:
+        pi[FastC.NIJK_MTR:FastC.NIJK_MTR + 5] = 0
+        pi[FastC.NDIMDX_MTR] = 1
+        pi[FastC.NEQ_IJ] = 1
+        pi[FastC.NEQ_K] = 1
+    else:
+        raise NotImplementedError("curvilinear metrics are computed by fast_gb300.metric")
+    itypcp = pi[FastC.ITYPCP]
+    pi[FastC.NEQ] = 6 if pi[FastC.IFLOW] == 3 else 5
+    pi[FastC.NEQ_COE] = (6 if pi[FastC.IFLOW] == 3 else 5) if itypcp <= 1 else 1
+    pi[FastC.ITYPVENT] = 2
+    pi[FastC.NEQ_VENT] = 3
+    pi[FastC.NDIMDX_VENT] = 1
+    # 3d cartesian metric: face areas and cell volume of a uniform box
+    dx = float(x[ific + 1, ific, ific] - x[ific, ific, ific])
+    dy = float(y[ific, ific + 1, ific] - y[ific, ific, ific])
+    dz = float(z_[ific, ific, ific + 1] - z_[ific, ific, ific])
+    mtr = np.array([dy * dz, dx * dz, dx * dy, dx * dy * dz], dtype=np.float64)
+    ijkv_lu = [max(1, int(pi[FastC.IJKV + d]) // int(pi[FastC.SIZE_SSDOM + d])) for d in range(3)]
+    rdm = np.zeros(int(nssiter) * int(pi[FastC.NEQ]) * 2 * ijkv_lu[0] * ijkv_lu[1] * ijkv_lu[2])
+    return [mtr, None, None, None, rdm, None, None, None]
+
+
+def _zone_type(x, y, z, nk, tol=2.0e-8):
+    """FastC/FastC/Metric/nature_geom_dom.for: 3 = 2d (nk = 2 vertices),
+    2 = 3d cartesian with constant steps, 0 = general."""
+    if nk == 2:
+        return 3
+    dx = np.diff(x, axis=0)
+    dy = np.diff(y, axis=1)
+    dz = np.diff(z, axis=2)
+    cart = (np.ptp(np.diff(x, axis=1)) < tol and np.ptp(np.diff(x, axis=2)) < tol and
+            np.ptp(np.diff(y, axis=0)) < tol and np.ptp(np.diff(y, axis=2)) < tol and
+            np.ptp(np.diff(z, axis=0)) < tol and np.ptp(np.diff(z, axis=1)) < tol)
+    cte = np.ptp(dx) < tol and np.ptp(dy) < tol and np.ptp(dz) < tol
+    return 2 if (cart and cte) else 0
+
+
+def metric_arrays(pi, mtr):
+    """Split the metric list slot into (ti, tj, tk, vol) views."""
+    ndm = int(pi[FastC.NDIMDX_MTR])
+    nij, nk_ = int(pi[FastC.NEQ_IJ]), int(pi[FastC.NEQ_K])
+    ti = mtr[:ndm * nij]
+    tj = mtr[ndm * nij:2 * ndm * nij]
+    tk = mtr[2 * ndm * nij:2 * ndm * nij + ndm * nk_]
+    vol = mtr[2 * ndm * nij + ndm * nk_:2 * ndm * nij + ndm * nk_ + ndm]
+    return ti, tj, tk, vol
+
+
+# --------------------------------------------------------------- warmup
+def prepare(t):
+    """Host part of warmup (no GPU): numerics packing, metric, BC block,
+    primitive variables.  Returns the metric list of every zone."""
+    zones = I.getZones(t)
+    FastC._buildOwnData(t)
+    dtloc = I.getNodeFromName1(I.getNodeFromName1(t, ".Solver#ownData"), ".Solver#dtloc")[1]
+    nssiter = int(dtloc[0])
+    metrics = [allocate_metric(z, nssiter) for z in zones]
+    FastC._BCcompact(t)
+    FastC.createPrimVars(t)
+    return metrics
+
+
+def zone_data(t, metrics):
+    """Per zone: param_int, param_real, metric views and the three compacted
+    time levels (flat float64 views into the tree)."""
+    out = []
+    for z, m in zip(I.getZones(t), metrics):
+        o = I.getNodeFromName1(z, ".Solver#ownData")
+        pi = I.getNodeFromName1(o, "Parameter_int")[1]
+        pr = I.getNodeFromName1(o, "Parameter_real")[1]
+        ti, tj, tk, vol = metric_arrays(pi, m[0])
+        out.append(dict(pi=pi, pr=pr, ti=ti, tj=tj, tk=tk, vol=vol,
+                        ro=FastC.compactArray(z, "").reshape(-1),
+                        ro_m1=FastC.compactArray(z, "_M1").reshape(-1),
+                        ro_p1=FastC.compactArray(z, "_P1").reshape(-1)))
+    return out
+
+
+def warmup(t, tc=None, graph=None, infos_ale=None, Adjoint=False, tmy=None, list_graph=None,
+           Padding=None, verbose=0, device=0, gpu_resident=False):
+    """FastS/FastS/PyTree.py:341: numerics, metric, primitive variables,
+    ghost cells; creates the GPU solver in HOOK.  ``tc`` may hold 1-to-1
+    interfaces as produced by fast_gb300.cases (list of dicts with keys
+    dnr, rcv, dnr_idx, rcv_idx); Cassiopee's connectivity trees are not
+    supported.  With ``gpu_resident`` the state stays on the GPU between
+    ``_compute`` calls and the tree is refreshed by ``_syncHost``."""
+    global HOOK, FIRST_IT
+    metrics = prepare(t)
+    zones = I.getZones(t)
+    dtloc = I.getNodeFromName1(I.getNodeFromName1(t, ".Solver#ownData"), ".Solver#dtloc")[1]
+    nssiter = int(dtloc[0])
+    solver = Solver(device)
+    for zd in zone_data(t, metrics):
+        solver.add_zone(zd["pi"], zd["pr"], zd["ti"], zd["tj"], zd["tk"], zd["vol"])
+    for tr in (tc or []):
+        solver.add_transfer(tr["dnr"], tr["rcv"], tr["dnr_idx"], tr["rcv_idx"])
+    solver.set_option("modulo_verif", int(dtloc[1]))
+    FIRST_IT = 0
+    solver.set_option("first_it", FIRST_IT)
+    HOOK = {"solver": solver, "nssiter": nssiter, "FIRST_IT": FIRST_IT,
+            "gpu_resident": bool(gpu_resident), "zones": zones, "device_valid": False}
+    _upload(t)
+    for lvl in (0, 1):
+        solver.apply_bc(lvl)
+    _download(t)
+    return t, tc, metrics
+
+
+def _upload(t):
+    s = HOOK["solver"]
+    for n, z in enumerate(I.getZones(t)):
+        for lvl, suf in enumerate(("", "_M1", "_P1")):
+            s.upload(n, lvl, FastC.compactArray(z, suf).reshape(-1))
+    HOOK["device_valid"] = True
+
+
+def _download(t):
+    s = HOOK["solver"]
+    for n, z in enumerate(I.getZones(t)):
+        for lvl, suf in enumerate(("", "_M1", "_P1")):
+            s.download(n, lvl, FastC.compactArray(z, suf).reshape(-1))
+
+
+def _itypcp(z):
+    o = I.getNodeFromName1(z, ".Solver#ownData")
+    return int(I.getNodeFromName1(o, "Parameter_int")[1][FastC.ITYPCP])
+
+
+def _syncHost(t):
+    """Copy the GPU state of every time level back into the tree."""
+    _download(t)
+
+
+def _compute(t, metrics, nitrun, tc=None, graph=None, tc2=None, graph2=None, layer="c",
+             NIT=1, ucData=None, vtune=None):
+    """FastS/FastS/PyTree.py:42 (layer 'c'): NIT physical steps of all the
+    sub-steps through fasts._computePT -> fgb_compute, then the time-level
+    rotation (done on the device; the tree arrays receive the new levels)."""
+    global FIRST_IT
+    if HOOK is None:
+        raise RuntimeError("warmup must be called before _compute")
+    if layer != "c":
+        raise NotImplementedError("only layer='c' is implemented")
+    s = HOOK["solver"]
+    zones = I.getZones(t)
+    if not HOOK["gpu_resident"]:
+        # inputs of the step: levels n and n-1 as the tree holds them
+        for n, z in enumerate(zones):
+            s.upload(n, 0, FastC.compactArray(z, "").reshape(-1))
+            s.upload(n, 1, FastC.compactArray(z, "_M1").reshape(-1))
+    s.set_option("first_it", HOOK["FIRST_IT"])
+    s.compute(nitrun, 1, HOOK["nssiter"], 1, NIT)
+    if not HOOK["gpu_resident"]:
+        # the device rotated its levels after every physical step; the tree
+        # does the same by swapping arrays (FastC.switchPointers__), so only
+        # the new level n is copied back (into the array that becomes n)
+        # (an explicit RK3 step overwrites level n with its second stage,
+        # which then becomes n-1, so that level is copied back too)
+        rot = NIT % 3
+        explicit = HOOK["nssiter"] <= 3 and _itypcp(zones[0]) == 2
+        for n, z in enumerate(zones):
+            for _ in range(rot):
+                FastC.switchPointers__([z])
+            s.download(n, 0, FastC.compactArray(z, "").reshape(-1))
+            if rot != 1 or explicit:
+                s.download(n, 1, FastC.compactArray(z, "_M1").reshape(-1))
+            if rot != 1:
+                s.download(n, 2, FastC.compactArray(z, "_P1").reshape(-1))
+    HOOK["FIRST_IT"] = 1
+    FIRST_IT = 1
+    return None
+
+
+# ----------------------------------------------------- convergence data
+def display_temporal_criteria(t, metrics, nitrun, format=None, gmres=None, verbose="firstlast",
+                              stopAtNan=True):
+    """FastS/FastS/PyTree.py:2039 -> fasts.display_ss_iteration: Newton
+    residual norms per zone (L2 = sqrt(sum/ncell)/dt, Loo = max/dt), printed
+    (format None/'double'), or stored in ZoneConvergenceHistory ('store')."""
+    s = HOOK["solver"]
+    s.synchronize()
+    zones = I.getZones(t)
+    resL2, resLoo = 0.0, -1.0e15
+    for n, z in enumerate(zones):
+        res = s.residuals(n)
+        if res.shape[1] == 0:
+            continue
+        neq = res.shape[0] // 2
+        L2, Loo = res[:neq], res[neq:]
+        resL2 += float(L2.sum())
+        resLoo = max(resLoo, float(Loo.max()))
+        cut = 1.0e-30
+        cvg = np.concatenate([np.log10(np.maximum(L2[:, 0], cut)),
+                              np.log10(np.maximum(Loo[:, 0], cut)),
+                              np.log10(np.maximum(L2[:, -1], cut)) - np.log10(np.maximum(L2[:, 0], cut)),
+                              np.log10(np.maximum(Loo[:, -1], cut)) - np.log10(np.maximum(Loo[:, 0], cut))])
+        if format == "store":
+            _store_history(z, nitrun, neq, cvg)
+        elif format is None or format == "double":
+            if verbose != "none":
+                for it in range(L2.shape[1]):
+                    if verbose == "firstlast" and it not in (0, L2.shape[1] - 1):
+                        continue
+                    print("%s it=%d ss=%d L2 %s Loo %s" % (
+                        z[0], nitrun, it + 1,
+                        " ".join("%7.3f" % math.log10(max(v, 1e-30)) for v in L2[:, it]),
+                        " ".join("%7.3f" % math.log10(max(v, 1e-30)) for v in Loo[:, it])))
+    if stopAtNan and not (np.isfinite(resL2) and np.isfinite(resLoo)):
+        print("Nan in the residual: stop.")
+        sys.exit(1)
+    return {"L2": resL2, "Loo": resLoo}
+
+
+def _createConvergenceHistory(t, nrecs):
+    """FastS/FastS/PyTree.py:2152: ZoneConvergenceHistory of nrecs records."""
+    for z in I.getZones(t):
+        pi = I.getNodeFromName1(I.getNodeFromName1(z, ".Solver#ownData"), "Parameter_int")[1]
+        neq = int(pi[FastC.NEQ])
+        ch = I.createUniqueChild(z, "ZoneConvergenceHistory", "ConvergenceHistory_t", 0)
+        I.createUniqueChild(ch, "IterationNumber", "DataArray_t")[1] = np.zeros(nrecs, np.int64)
+        for name in ("RSD_L2", "RSD_oo", "RSD_L2_diff", "RSD_oo_diff"):
+            I.createUniqueChild(ch, name, "DataArray_t")[1] = np.zeros(nrecs * neq)
+
+
+def _store_history(z, nitrun, neq, cvg):
+    """conv2pytree.for:56-66 (lft >= 0 branch)."""
+    ch = I.getNodeFromName1(z, "ZoneConvergenceHistory")
+    if ch is None:
+        return
+    last = int(I.getValue(ch))
+    it = I.getNodeFromName1(ch, "IterationNumber")[1]
+    if last >= it.size:
+        return
+    it[last] = nitrun
+    for k, name in enumerate(("RSD_L2", "RSD_oo", "RSD_L2_diff", "RSD_oo_diff")):
+        I.getNodeFromName1(ch, name)[1][last * neq:(last + 1) * neq] = cvg[k * neq:(k + 1) * neq]
+    ch[1] = np.array([last + 1], dtype=np.int64)
+
+
+def _extractConvergenceHistory(t, fileout):
+    """FastS/FastS/PyTree.py:2245: write the stored records as residuals.dat
+    (conv2pytree.for text layout: It, L2 per equation, Loo per equation)."""
+    names5 = ["Ro", "RoU", "RoV", "RoW", "RoE", "Nut"]
+    with open(fileout, "w") as f:
+        for nd, z in enumerate(I.getZones(t)):
+            ch = I.getNodeFromName1(z, "ZoneConvergenceHistory")
+            if ch is None:
+                continue
+            last = int(I.getValue(ch))
+            it = I.getNodeFromName1(ch, "IterationNumber")[1]
+            l2 = I.getNodeFromName1(ch, "RSD_L2")[1]
+            oo = I.getNodeFromName1(ch, "RSD_oo")[1]
+            neq = l2.size // max(it.size, 1)
+            if nd == 0:
+                f.write("VARIABLES=\"It\" " + " ".join('"%s_L2"' % n for n in names5[:neq]) + " " +
+                        " ".join('"%s_oo"' % n for n in names5[:neq]) + "\n")
+            f.write('ZONE T="%s"\n' % z[0])
+            for r in range(last):
+                vals = [l2[r * neq + j] for j in range(neq)] + [oo[r * neq + j] for j in range(neq)]
+                f.write("%7d " % it[r] + " ".join("%15.8E" % v for v in vals) + "\n")

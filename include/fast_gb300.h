@@ -1,0 +1,133 @@
+/*
+ * fast_gb300.h -- C ABI of the GB300 implementation of the FastS structured
+ * solve step.  Plain pointers and sizes only; every call returns an int
+ * status (FGB_OK = 0) and never exits the process; fgb_last_error() gives the
+ * message of the last failure on the calling thread.
+ *
+ * The reference crosses the Python/C boundary in the CPython module `fasts`
+ * (FastS/FastS/fastS.cpp:25-67).  Each entry point below names the reference
+ * interface it replaces.  Arrays keep the reference layout
+ * (FastS/FastS/formule_param.h): structure-of-arrays q[v*NDIMDX + l] with
+ * ghost cells, param_int / param_real with the FastS index map
+ * (FastS/FastS/param_solver.h).  Host buffers are only read or written during
+ * the call; device state lives in the solver handle.
+ */
+#ifndef FAST_GB300_H
+#define FAST_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  FGB_OK = 0,
+  FGB_ERR_ARG = 1,      /* invalid argument / unsupported numerics         */
+  FGB_ERR_CUDA = 2,     /* CUDA runtime error (message has the CUDA text)  */
+  FGB_ERR_DEVICE = 3,   /* a kernel reported an error through its status   */
+  FGB_ERR_STATE = 4     /* call out of sequence (e.g. compute before data) */
+};
+
+typedef struct fgb_solver fgb_solver;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* fgb_last_error(void);
+
+/* Library version and the compute capability it was built for. */
+int fgb_version(int* major, int* minor, int* sm);
+
+/* Create / destroy a solver on CUDA device `device` (one stream per solver).
+ * Replaces the work dictionary built by FastC.createWorkArrays__
+ * (FastC/FastC/PyTree.py:2064) and the device side of FastS.PyTree.warmup
+ * (FastS/FastS/PyTree.py:341). */
+int fgb_create(int device, fgb_solver** out);
+int fgb_destroy(fgb_solver* s);
+
+/* Add one structured zone.  param_int / param_real: the zone's
+ * .Solver#ownData/Parameter_int|real (FastC/FastC/PyTree.py:1817-2030, with
+ * the BC block appended by _BCcompact, FastC/FastC/PyTree.py:2788).
+ * ti, tj, tk, vol: the metric of fasts.allocate_metric
+ * (FastS/FastS/Metric/allocate_metric.cpp, list slot METRIC_TI).
+ * The returned zone id is the zone's position in the solver (0, 1, ...). */
+int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
+                 const double* param_real, int64_t n_real,
+                 const double* ti, const double* tj, const double* tk,
+                 const double* vol, int* zone_id);
+
+/* Add a 1-to-1 interface (interpolation type 0 of
+ * FastC/FastC/Com/setInterpTransfersFast.cpp:852-883): for t < n, receiver
+ * cell rcv_idx[t] of zone rcv_zone takes the value of donor cell dnr_idx[t]
+ * of zone dnr_zone (0-based cell indices into the zone arrays). */
+int fgb_add_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
+                     const int64_t* dnr_idx, const int64_t* rcv_idx);
+
+/* Solver options.  "lu_precision": 64 (default) or 32 -- FP32 LU-SGS sweeps
+ * inside the FP64 defect-correction loop; "modulo_verif": residual check
+ * period (FastC numerics key modulo_verif, default 200); "first_it": the
+ * HOOK["FIRST_IT"] flag (0 = BDF1 step); "profile": 1 to time every kernel
+ * group with CUDA events (see fgb_kernel_stats). */
+int fgb_set_option(fgb_solver* s, const char* key, double value);
+int fgb_get_option(fgb_solver* s, const char* key, double* value);
+
+/* Host <-> device copies of one time level of one zone (NEQ*NDIMDX doubles).
+ * level 0 = n (FlowSolution#Centers "Density"... compacted), 1 = n-1
+ * ("..._M1"), 2 = n+1 ("..._P1").  These are the arrays the reference's
+ * _computePT reads in place through K_PYTREE::getValueAF
+ * (FastS/FastS/Compute/computePT.cpp:140-260). */
+int fgb_upload_state(fgb_solver* s, int zone, int level, const double* host);
+int fgb_download_state(fgb_solver* s, int zone, int level, double* host);
+
+/* Work arrays for inspection: which = "drodm" (NEQ*NDIMDX), "coe"
+ * (NEQ_COE*NDIMDX), "xmut" (NDIMDX), "rdm" (nssiter*NEQ*2*n_lu_blocks). */
+int fgb_download_work(fgb_solver* s, int zone, const char* which, double* host,
+                      int64_t n);
+
+/* One call of the solve step: replaces fasts._computePT(zones, metrics,
+ * nitrun, nstep_deb, nstep_fin, layer_mode, nit_c, hook)
+ * (FastS/FastS/Compute/computePT.cpp:44-721): nit_c physical steps of
+ * sub-steps nstep_deb..nstep_fin, each followed by the time-level rotation
+ * M1 <- N <- P1.  layer_mode must be 1 (the "c" layer).  Asynchronous on the
+ * solver stream; errors of the kernels are reported by fgb_synchronize. */
+int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin,
+                int layer_mode, int nit_c);
+
+/* Ghost-cell fill of one time level of every zone: replaces
+ * fasts._applyBC(zones, metrics, hook, nstep, var) (FastS/FastS/BC/applyBC.cpp)
+ * together with the 1-to-1 transfers of FastS.PyTree._fillGhostcells
+ * (FastS/FastS/PyTree.py:1162). */
+int fgb_apply_bc(fgb_solver* s, int level);
+
+/* Newton residual history of the last verified step, reduced over LU blocks
+ * as in fasts.display_ss_iteration (FastS/FastS/DISPLAY/
+ * display_ss_iteration.cpp:112-145): out[ne*nit + it] = L2,
+ * out[(neq+ne)*nit + it] = Loo for it < nit (nit = number of sub-iterations
+ * recorded); returns nit through *nit_out. */
+int fgb_residuals(fgb_solver* s, int zone, double* out, int64_t n, int* nit_out);
+
+/* Wait for the solver stream and report any kernel error. */
+int fgb_synchronize(fgb_solver* s);
+
+/* Per-kernel timing (option "profile" = 1): CUDA events recorded on the
+ * solver stream around each kernel group.  index >= 0: name, number of
+ * timed groups and total milliseconds of group `index` (count = 0 past the
+ * last group); index < 0: clear the records, *count = number of groups. */
+int fgb_kernel_stats(fgb_solver* s, int index, char* name, int name_len, int64_t* count,
+                     double* total_ms);
+
+/* Kernel launches issued by the solver since creation (for launch counts). */
+int fgb_launch_count(fgb_solver* s, int64_t* count);
+
+/* Device time of a region of the solver stream: op = 0 records the start
+ * event, op = 1 records the stop event, waits for it and returns the elapsed
+ * milliseconds in *ms.  (Measurement support; no reference counterpart.) */
+int fgb_stream_timer(fgb_solver* s, int op, double* ms);
+
+/* Measured FP64 FMA throughput of device `device` in GFLOP/s (2 flops per
+ * FMA): the compute roof of the FP64 kernels.  (Measurement support; no
+ * reference counterpart.) */
+int fgb_fp64_peak(int device, double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1321 @@
+/*
+ * fast_oracle.c -- CPU oracle (FP64 restatement) of the FastS solve step.
+ *
+ * TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py as the checker.  The product path never loads
+ * or calls it.  Parity status: unpinned by reference data (the reference ships
+ * no golden vectors and cannot be compiled here); see fast_oracle.h.
+ *
+ * Every routine restates the FastS Fortran routine cited in its comment
+ * (paths relative to the Fast/ project directory).  Compiled with
+ * -ffp-contract=off so that every multiply and add rounds separately, and
+ * written with the reference's left-to-right evaluation order, so that the
+ * result is the reference's arithmetic with one thread and one cache block
+ * per zone (cache_blocking_I/J/K >= zone size).  With FastS's default cache
+ * blocking the only difference is the order of the last two face-flux
+ * summands of cells on a cache-block boundary (one rounding of drodm).
+ */
+#include "fast_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---- FastS/FastS/param_solver.h index map (the subset used here) ---- */
+enum { NIJK = 0, NIJK_MTR = 5, IJKV = 20, ITYPZONE = 25, IFLOW = 27, ILES = 28,
+       ITYPCP = 29, SIZE_SSDOM = 30, KFLUDOM = 33, LALE = 34, NEQ = 36,
+       NEQ_IJ = 37, NEQ_K = 38, NEQ_COE = 39, NDIMDX = 41, NDIMDX_MTR = 43,
+       DTLOC = 46, RK = 52, LEVEL = 53, EXPLOC = 54, NSSITER = 58, SLOPE = 64,
+       PT_BC = 70, NB_RELAX = 71, LU_MATCH = 75 };
+enum { DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6,
+       PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14,
+       PSIROE = 34, WIG_AMP = 72 };
+enum { BC_TYPE = 0, BC_IDIR = 1, BC_FEN = 2 };
+
+#define OMAX(a, b) ((a) > (b) ? (a) : (b))
+#define OMIN(a, b) ((a) < (b) ? (a) : (b))
+/* Fortran SIGN(a,b): |a| with the sign of b */
+static inline double fsign(double a, double b) { return copysign(fabs(a), b); }
+
+static int g_threads = 1;
+static int g_lu_tiles = 1;
+void or_set_threads(int n) { g_threads = n > 0 ? n : 1; }
+/* LU-SGS tiles (FastS with OMP_NUM_THREADS = n: one LU block per thread,
+ * block-Jacobi between them, lhs.cpp ipt_shift_lu).  1 = one tile per zone. */
+void or_set_lu_tiles(int n) { g_lu_tiles = n > 0 ? n : 1; }
+int or_version(void) { return 3; }
+
+/* formule_param.h: inddm (returned 0-based) */
+static inline int64_t inddm(const int64_t* p, int64_t i, int64_t j, int64_t k) {
+  return (i + p[NIJK + 3] - 1) + (j + p[NIJK + 3] - 1) * p[NIJK] +
+         (k + p[NIJK + 4] - 1) * p[NIJK] * p[NIJK + 1];
+}
+/* formule_mtr_param.h: indmtr (returned 0-based) */
+static inline int64_t indmtr(const int64_t* p, int64_t i, int64_t j, int64_t k) {
+  return (i + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR] + (j + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR + 1] +
+         (k + p[NIJK_MTR + 4] - 1) * p[NIJK_MTR + 2];
+}
+
+/* ======================================================================
+ * invist -- FastS/FastS/Compute/invist.for:28-36 (Sutherland law)
+ * ====================================================================== */
+void or_invist(const int64_t* pi, const double* pr, const int64_t* ind,
+               const double* rop, double* xmut) {
+  double cmus1 = pr[CS];
+  double temp01 = 1. / pr[TEMP0];
+  double coesut = pr[XMUL0] * (1. + cmus1 * temp01) * sqrt(temp01);
+  int64_t v5 = 4 * pi[NDIMDX];
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        double t1 = rop[l + v5];
+        xmut[l] = coesut * sqrt(t1) * t1 / (t1 + cmus1);
+      }
+}
+
+/* ======================================================================
+ * tstb3_global -- FastS/FastS/Compute/tstb3_global.for:43-66 (coe1 = dt/vol)
+ * ====================================================================== */
+void or_tstb3_global(const int64_t* pi, const double* pr, const int64_t* ind,
+                     double* coe, const double* vol) {
+  double volinv = pr[DTC] / vol[0];
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        if (pi[ITYPZONE] != 2) coe[l] = pr[DTC] / vol[indmtr(pi, i, j, k)];
+        else coe[l] = volinv;
+      }
+}
+
+/* ======================================================================
+ * tstb3c -- FastS/FastS/Compute/tstb3c.for:121-171 (3d general),
+ *           :300-345 (3d cartesian), :346-390 (2d): spectral radii coe2..4
+ *           and the scalar LU diagonal coe5.
+ * ====================================================================== */
+void or_tstb3c(const int64_t* pi, const double* pr, int first_it, const int64_t* ind,
+               const double* rop, double* coe, const double* xmut,
+               const double* ti, const double* tj, const double* tk, const double* vol) {
+  if (pi[ITYPCP] > 1) return;
+  const int64_t nd = pi[NDIMDX], ndm = pi[NDIMDX_MTR];
+  const double cut0x = 1e-20;
+  double gamma = pr[GAMMA];
+  double rgp = pr[CVINF] * (gamma - 1.);
+  double prandt = pr[PRANDT];
+  double xid = 1.5;
+  if (first_it == 0) xid = 1.;
+  double gam1 = gamma / prandt;
+  if (pi[IFLOW] == 1) gam1 = 0.;
+  double gam2 = gamma * rgp;
+  const double *r_ = rop, *u_ = rop + nd, *v_ = rop + 2 * nd, *w_ = rop + 3 * nd, *t_ = rop + 4 * nd;
+  double *c1 = coe, *c2 = coe + nd, *c3 = coe + 2 * nd, *c4 = coe + 3 * nd, *c5 = coe + 4 * nd;
+  int typ = (int)pi[ITYPZONE];
+
+  if (typ == 2) {
+    double tcxi = ti[0], tcyj = tj[0], tczk = tk[0];
+    double tc2i = sqrt(tcxi * tcxi), tc2j = sqrt(tcyj * tcyj), tc2k = sqrt(tczk * tczk);
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t k = ind[4]; k <= ind[5]; k++)
+      for (int64_t j = ind[2]; j <= ind[3]; j++)
+        for (int64_t i = ind[0]; i <= ind[1]; i++) {
+          int64_t l = inddm(pi, i, j, k);
+          double r = r_[l];
+          double detj = OMAX(vol[0], cut0x);
+          double u = u_[l], v = v_[l], w = w_[l];
+          double c = sqrt(gam2 * t_[l]);
+          double vmu = gam1 * xmut[l];
+          double volu = detj * r;
+          double xmvis = vmu / volu;
+          double qni = tcxi * u, cni = c * tc2i, vmi = fabs(qni) + cni;
+          c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+          double qnj = tcyj * v, cnj = c * tc2j, vmj = fabs(qnj) + cnj;
+          c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+          double qnk = tczk * w, cnk = c * tc2k, vmk = fabs(qnk) + cnk;
+          c4[l] = vmk * 2. + xmvis * tc2k * tc2k * 4.;
+          c5[l] = xid + c1[l] * (c2[l] + c3[l] + c4[l]) * 0.5;
+        }
+    return;
+  }
+  const int64_t mi = pi[NIJK_MTR], mj = pi[NIJK_MTR + 1], mk = pi[NIJK_MTR + 2];
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        int64_t lt = indmtr(pi, i, j, k);
+        int64_t li = lt + mi, lj = lt + mj, lk = lt + mk;
+        double r = r_[l];
+        double detj = OMAX(vol[lt], cut0x);
+        double u = u_[l], v = v_[l];
+        double c = sqrt(gam2 * t_[l]);
+        double vmu = gam1 * xmut[l], volu = detj * r, xmvis = vmu / volu;
+        if (typ == 0) {
+          double w = w_[l];
+          const double *tix = ti, *tiy = ti + ndm, *tiz = ti + 2 * ndm;
+          const double *tjx = tj, *tjy = tj + ndm, *tjz = tj + 2 * ndm;
+          const double *tkx = tk, *tky = tk + ndm, *tkz = tk + 2 * ndm;
+          double tcxi = .5 * (tix[lt] + tix[li]);
+          double tcyi = .5 * (tiy[lt] + tiy[li]);
+          double tczi = .5 * (tiz[lt] + tiz[li]);
+          double tc2i = .5 * (sqrt(tix[lt] * tix[lt] + tiy[lt] * tiy[lt] + tiz[lt] * tiz[lt]) +
+                              sqrt(tix[li] * tix[li] + tiy[li] * tiy[li] + tiz[li] * tiz[li]));
+          double qni = tcxi * u + tcyi * v + tczi * w;
+          double vmi = fabs(qni) + c * tc2i;
+          c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+          double tcxj = .5 * (tjx[lt] + tjx[lj]);
+          double tcyj = .5 * (tjy[lt] + tjy[lj]);
+          double tczj = .5 * (tjz[lt] + tjz[lj]);
+          double tc2j = .5 * (sqrt(tjx[lt] * tjx[lt] + tjy[lt] * tjy[lt] + tjz[lt] * tjz[lt]) +
+                              sqrt(tjx[lj] * tjx[lj] + tjy[lj] * tjy[lj] + tjz[lj] * tjz[lj]));
+          double qnj = tcxj * u + tcyj * v + tczj * w;
+          double vmj = fabs(qnj) + c * tc2j;
+          c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+          double tcxk = .5 * (tkx[lt] + tkx[lk]);
+          double tcyk = .5 * (tky[lt] + tky[lk]);
+          double tczk = .5 * (tkz[lt] + tkz[lk]);
+          double tc2k = .5 * (sqrt(tkx[lt] * tkx[lt] + tky[lt] * tky[lt] + tkz[lt] * tkz[lt]) +
+                              sqrt(tkx[lk] * tkx[lk] + tky[lk] * tky[lk] + tkz[lk] * tkz[lk]));
+          double qnk = tcxk * u + tcyk * v + tczk * w;
+          double vmk = fabs(qnk) + c * tc2k;
+          c4[l] = vmk * 2. + xmvis * tc2k * tc2k * 4.;
+          c5[l] = xid + c1[l] * (c2[l] + c3[l] + c4[l]) * 0.5;
+        } else { /* 2d */
+          const double *tix = ti, *tiy = ti + ndm;
+          const double *tjx = tj, *tjy = tj + ndm;
+          double tcxi = .5 * (tix[lt] + tix[li]);
+          double tcyi = .5 * (tiy[lt] + tiy[li]);
+          double tc2i = .5 * (sqrt(tix[lt] * tix[lt] + tiy[lt] * tiy[lt]) +
+                              sqrt(tix[li] * tix[li] + tiy[li] * tiy[li]));
+          double qni = tcxi * u + tcyi * v;
+          double vmi = fabs(qni) + c * tc2i;
+          c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+          double tcxj = .5 * (tjx[lt] + tjx[lj]);
+          double tcyj = .5 * (tjy[lt] + tjy[lj]);
+          double tc2j = .5 * (sqrt(tjx[lt] * tjx[lt] + tjy[lt] * tjy[lt]) +
+                              sqrt(tjx[lj] * tjx[lj] + tjy[lj] * tjy[lj]));
+          double qnj = tcxj * u + tcyj * v;
+          double vmj = fabs(qnj) + c * tc2j;
+          c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+          c5[l] = xid + c1[l] * (c2[l] + c3[l]) * 0.5;
+        }
+      }
+}
+
+/* ======================================================================
+ * init_rhs -- FastS/FastS/Compute/init_rhs.for:49-129 (RK low-storage A)
+ * ====================================================================== */
+void or_init_rhs(const int64_t* pi, int nitcfg, const int64_t* ind, double* drodm) {
+  const double cxsi1 = -0.6830127018922193, cxsi2 = -4. / 3.;
+  int64_t b = pi[RK], nd = pi[NDIMDX], neq = pi[NEQ];
+  double coefH = 0.;
+  if (b == 3) {
+    if (nitcfg == 2) coefH = cxsi1;
+    else if (nitcfg == 3) coefH = cxsi2;
+    else if (nitcfg == 1) coefH = 0.;
+  } else if (b == 2) {
+    if (nitcfg == 2) coefH = -1.;
+    else if (nitcfg == 1) coefH = 0.;
+  }
+  int zero = (pi[ITYPCP] <= 1 || nitcfg == 1);
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        for (int64_t ne = 0; ne < neq; ne++) {
+          if (zero) drodm[l + ne * nd] = 0.;
+          else drodm[l + ne * nd] = drodm[l + ne * nd] * coefH;
+        }
+      }
+}
+
+/* ======================================================================
+ * Face fluxes -- FastS/FastS/Compute/template_FluxAndBalance.for:192-271
+ * (generated per scheme under ROE/, AUSM/): face "dir" of cell l is the
+ * face between l-inc and l; assemble_drodm_plus_vec1.for adds it to l and
+ * subtracts it from l-inc.
+ * ====================================================================== */
+typedef struct {
+  const int64_t* pi; const double* pr;
+  const double *rop, *xmut, *ti, *tj, *tk, *vol;
+  int64_t inc[3], nd, ndm, inc_mtr[3];
+  int typ, iflow, kflu, slope;
+  double gam, rgp, gam1, gam3, c1, c2, c3, c4, c5, c6, cvisq, psiroe, wig_cte, tmin_1;
+  double tcx, tcy, tcz, si, sj, sk, volinv; /* 3d cartesian constants */
+} fctx;
+
+static void fctx_init(fctx* c, const int64_t* pi, const double* pr, const double* rop,
+                      const double* xmut, const double* ti, const double* tj,
+                      const double* tk, const double* vol) {
+  c->pi = pi; c->pr = pr; c->rop = rop; c->xmut = xmut; c->ti = ti; c->tj = tj; c->tk = tk; c->vol = vol;
+  c->inc[0] = 1; c->inc[1] = pi[NIJK]; c->inc[2] = pi[NIJK] * pi[NIJK + 1];
+  c->inc_mtr[0] = pi[NIJK_MTR]; c->inc_mtr[1] = pi[NIJK_MTR + 1]; c->inc_mtr[2] = pi[NIJK_MTR + 2];
+  c->nd = pi[NDIMDX]; c->ndm = pi[NDIMDX_MTR];
+  c->typ = (int)pi[ITYPZONE]; c->iflow = (int)pi[IFLOW]; c->kflu = (int)pi[KFLUDOM];
+  c->slope = (int)pi[SLOPE];
+  /* template_FluxAndBalance.for:108-156 */
+  c->tcx = ti[0]; c->tcy = tj[0]; c->tcz = tk[0];
+  c->si = fabs(c->tcx); c->sj = fabs(c->tcy); c->sk = fabs(c->tcz);
+  c->volinv = 0.5 / vol[0];
+  c->gam = pr[GAMMA];
+  c->rgp = pr[CVINF] * (c->gam - 1.);
+  c->gam1 = c->gam / (c->gam - 1.);
+  c->gam3 = c->gam1 / pr[PRANDT] * c->rgp;
+  c->psiroe = pr[PSIROE];
+  c->wig_cte = pr[WIG_AMP];
+  c->tmin_1 = 100. / pr[TINF];
+  double uref = pr[VINF], roref = pr[ROINF];
+  c->c1 = 0.02 * uref;
+  c->c2 = 0.02 / (uref * roref);
+  c->c3 = -2.;
+  double c6 = 1. / 6.;
+  c->c4 = 5. * c6;
+  c->c5 = 2. * c6;
+  c->c6 = -1. * c6;
+  c->cvisq = 1. / 3;
+}
+
+/* Slope/minmod_slope_var.for:1-17 limiter */
+static inline double avmin(double c, double r) {
+  return fsign(1., c) * OMAX(0., OMIN(fabs(c), fsign(1., c) * r));
+}
+
+/* Slope/{o1,o3,minmod}_slope_var.for: qm = right state, qp = left state */
+static void slopes(const fctx* c, int64_t l, int64_t inc, double qm[5], double qp[5]) {
+  const double* rop = c->rop;
+  int64_t nd = c->nd, nm = l - inc, nm2 = l - 2 * inc, np = l + inc;
+  for (int v = 0; v < 5; v++) {
+    if (c->typ == 3 && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
+    int64_t vs = v * nd;
+    if (c->slope == 1) {
+      qm[v] = rop[l + vs];
+      qp[v] = rop[nm + vs];
+    } else if (c->slope == 2) {
+      qm[v] = c->c4 * rop[l + vs] + c->c5 * rop[nm + vs] + c->c6 * rop[np + vs];
+      qp[v] = c->c4 * rop[nm + vs] + c->c6 * rop[nm2 + vs] + c->c5 * rop[l + vs];
+    } else { /* minmod */
+      double roff = .5 * OMAX(0., OMIN(rop[l + 4 * nd] * c->tmin_1 - .5, 1.));
+      double delm = rop[l + vs] - rop[nm + vs];
+      double delp = rop[np + vs] - rop[l + vs];
+      double delq = rop[nm + vs] - rop[nm2 + vs];
+      double slp = roff * avmin(delm, delp);
+      double slq = roff * avmin(delq, delm);
+      qm[v] = rop[l + vs] - slp;
+      qp[v] = rop[nm + vs] + slq;
+    }
+  }
+}
+
+/* face normal for direction d at metric index lt (Normale/normale_*.for) */
+static void face_normal(const fctx* c, int d, int64_t lt, double* tcx, double* tcy,
+                        double* tcz, double* s) {
+  if (c->typ == 2) {
+    *tcx = c->tcx; *tcy = c->tcy; *tcz = c->tcz;
+    *s = d == 0 ? c->si : (d == 1 ? c->sj : c->sk);
+    return;
+  }
+  const double* t = d == 0 ? c->ti : (d == 1 ? c->tj : c->tk);
+  *tcx = t[lt];
+  *tcy = t[lt + c->ndm];
+  if (c->typ == 3) { *tcz = 0.; *s = sqrt(*tcx * *tcx + *tcy * *tcy); return; }
+  *tcz = t[lt + 2 * c->ndm];
+  *s = sqrt(*tcx * *tcx + *tcy * *tcy + *tcz * *tcz);
+}
+
+
+/* Roe flux with Harten entropy fix -- etat_roe_GD.for:1-20,
+ * Vit_ent/qn_3dfull_*.for, Vit_ent/fludiffer_3dfull_i.for:1-61.
+ * The general (3d full) form is used for every zone type: for a cartesian
+ * face the normal has exact zeros in its two tangential components
+ * (tcx,0,0), so every extra product is an exact zero and the result is the
+ * cartesian files' (Vit_ent/fludiffer_3dcart_*.for) bit for bit, up to the
+ * sign of zero results. */
+static void roe_face(const fctx* c, const double qm[5], const double qp[5],
+                     double tcx, double tcy, double tcz, double s, double flu[5]) {
+  double gam = c->gam, rgp = c->rgp, gam1 = c->gam1, psiroe = c->psiroe;
+  double qp1 = qp[0], qp2 = qp[1], qp3 = qp[2], qp4 = qp[3], qp5 = qp[4];
+  double qm1 = qm[0], qm2 = qm[1], qm3 = qm[2], qm4 = qm[3], qm5 = qm[4];
+  double r1 = qp1;
+  double p1 = r1 * qp5 * rgp;
+  double h1 = gam1 * qp5 * rgp + .5 * (qp2 * qp2 + qp3 * qp3 + qp4 * qp4);
+  double r2 = qm1;
+  double p2 = r2 * qm5 * rgp;
+  double h2 = gam1 * qm5 * rgp + .5 * (qm2 * qm2 + qm3 * qm3 + qm4 * qm4);
+  qp1 = sqrt(r1);
+  qm1 = sqrt(r2);
+  double r = qp1 * qm1;
+  double r_1 = 1. / (qp1 + qm1);
+  double u = (qp1 * qp2 + qm1 * qm2) * r_1;
+  double v = (qp1 * qp3 + qm1 * qm3) * r_1;
+  double w = (qp1 * qp4 + qm1 * qm4) * r_1;
+  double h = (qp1 * h1 + qm1 * h2) * r_1;
+  double q = .5 * (u * u + v * v + w * w);
+  double cc = sqrt((gam - 1.) * fabs(h - q));
+  double qn1 = qp2 * tcx + qp3 * tcy + qp4 * tcz;
+  double qn2 = qm2 * tcx + qm3 * tcy + qm4 * tcz;
+  double du = (qm2 - qp2) * s, dv = (qm3 - qp3) * s, dw = (qm4 - qp4) * s;
+  double dp = p2 - p1;
+  double dqn = qn2 - qn1;
+  double s_1 = 1.0 / OMAX(s, 1.E-30);
+  double nx = tcx * s_1, ny = tcy * s_1, nz = tcz * s_1;
+  double qn = u * nx + v * ny + w * nz;
+  double f1 = qn;
+  double f4 = psiroe * (fabs(f1) + cc);
+  double f2 = 0.5 + fsign(0.5, fabs(f1) - f4);
+  double f3 = (f2 - 1.0) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (r2 - r1 - dp / (cc * cc)) * s;
+  double flu1 = f3 * (f1);
+  double flu2 = f3 * (f1 * u + r * (du - nx * dqn));
+  double flu3 = f3 * (f1 * v + r * (dv - ny * dqn));
+  double flu4 = f3 * (f1 * w + r * (dw - nz * dqn));
+  double flu5 = f3 * (f1 * q + r * (u * du + v * dv + w * dw - qn * dqn));
+  f1 = qn + cc;
+  f2 = 0.5 + fsign(0.5, fabs(f1) - f4);
+  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (dp + r * cc * dqn * s_1) / (2. * cc * cc) * s * f3;
+  flu1 = flu1 + f1;
+  flu2 = flu2 + f1 * (u + nx * cc);
+  flu3 = flu3 + f1 * (v + ny * cc);
+  flu4 = flu4 + f1 * (w + nz * cc);
+  flu5 = flu5 + f1 * (h + qn * cc);
+  f1 = qn - cc;
+  f2 = 0.5 + fsign(0.5, fabs(f1) - f4);
+  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  f1 = (dp - r * cc * dqn * s_1) / (2. * cc * cc) * f3 * s;
+  flu1 = flu1 + f1;
+  flu2 = flu2 + f1 * (u - nx * cc);
+  flu3 = flu3 + f1 * (v - ny * cc);
+  flu4 = flu4 + f1 * (w - nz * cc);
+  flu5 = flu5 + f1 * (h - qn * cc);
+  double rou1 = r1 * qn1, rou2 = r2 * qn2, p1p2 = p1 + p2;
+  flu[0] = (flu1 + rou1 + rou2) * 0.5;
+  flu[1] = (flu2 + rou1 * qp2 + rou2 * qm2 + tcx * p1p2) * 0.5;
+  flu[2] = (flu3 + rou1 * qp3 + rou2 * qm3 + tcy * p1p2) * 0.5;
+  flu[3] = (flu4 + rou1 * qp4 + rou2 * qm4 + tcz * p1p2) * 0.5;
+  flu[4] = (flu5 + rou1 * h1 + rou2 * h2) * 0.5;
+}
+
+/* AUSM+(P) -- etat_GD.for:1-15, AUSM/fluFaceEuler.for:36-57,
+ * Vit_ent/fluvector_3dfull_i.for:1-5.  Same general-form remark as Roe.
+ * tl = temperature of cell l (the right cell), used for the sound speed. */
+static void ausm_face(const fctx* c, const double qm[5], const double qp[5], double tl,
+                      double tcx, double tcy, double tcz, double s, double flu[5]) {
+  double rgp = c->rgp, gam1 = c->gam1;
+  double r1 = qp[0], rou1 = r1 * qp[1], rov1 = r1 * qp[2], row1 = r1 * qp[3];
+  double p1 = r1 * qp[4] * rgp;
+  double h1 = gam1 * p1 + .5 * (rou1 * qp[1] + rov1 * qp[2] + row1 * qp[3]);
+  double r2 = qm[0], rou2 = r2 * qm[1], rov2 = r2 * qm[2], row2 = r2 * qm[3];
+  double p2 = r2 * qm[4] * rgp;
+  double h2 = gam1 * p2 + .5 * (rou2 * qm[1] + rov2 * qm[2] + row2 * qm[3]);
+  double qn1 = qp[1] * tcx + qp[2] * tcy + qp[3] * tcz;
+  double qn2 = qm[1] * tcx + qm[2] * tcy + qm[3] * tcz;
+  double cc = rgp * c->gam * tl;
+  double son = sqrt(qn1 * qn1 / cc);
+  double tam = c->c3 * son + s;
+  double tam1 = OMAX(0., tam) * c->c2;
+  double u = 0.25 * (qn1 + qn2) - tam1 * (p2 - p1);
+  double tdu = OMAX(fabs(u), c->c1 * s) * c->wig_cte;
+  double p1p2 = (p1 + p2) * 0.5;
+  flu[0] = u * (r1 + r2) - tdu * (r2 - r1);
+  flu[1] = u * (rou1 + rou2) - tdu * (rou2 - rou1) + tcx * p1p2;
+  flu[2] = u * (rov1 + rov2) - tdu * (rov2 - rov1) + tcy * p1p2;
+  flu[3] = u * (row1 + row2) - tdu * (row2 - row1) + tcz * p1p2;
+  flu[4] = u * (h1 + h2) - tdu * (h2 - h1);
+}
+
+/* Viscous face flux on a 3d cartesian zone: fluvisq_3dcart_{i,j,k}.for and
+ * mut_interface.for (xmutvol = (mu_r + mu_l) * 0.5/vol, xktvol = xmutvol*gam3). */
+static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
+  const double* rop = c->rop;
+  int64_t nd = c->nd, inci = c->inc[0], incj = c->inc[1], inck = c->inc[2];
+  int64_t v2 = nd, v3 = 2 * nd, v4 = 3 * nd, v5 = 4 * nd;
+  double tcx = c->tcx, tcy = c->tcy, tcz = c->tcz, cvisq = c->cvisq;
+  double f1, f2, f3, f4, f5, f6, fv, fv5, div;
+  int64_t il, ir = l;
+  if (d == 0) {
+    il = l - inci;
+    int64_t l220 = l - inci - incj, l020 = l - incj, l210 = l - inci + incj, l010 = l + incj;
+    int64_t l202 = l - inci - inck, l002 = l - inck, l201 = l - inci + inck, l001 = l + inck;
+    double tix = tcx, tjy = .25 * tcy, tkz = .25 * tcz;
+    f1 = rop[il + v2]; f2 = rop[ir + v2]; fv = f1 + f2;
+    f3 = fv + rop[l220 + v2] + rop[l020 + v2];
+    f4 = fv + rop[l210 + v2] + rop[l010 + v2];
+    f5 = fv + rop[l202 + v2] + rop[l002 + v2];
+    f6 = fv + rop[l201 + v2] + rop[l001 + v2];
+    double gradU_nx = (f2 - f1) * tix, gradU_ny = (f4 - f3) * tjy, gradU_nz = (f6 - f5) * tkz;
+    f1 = rop[il + v3]; f2 = rop[ir + v3]; fv = f1 + f2;
+    f3 = fv + rop[l220 + v3] + rop[l020 + v3];
+    f4 = fv + rop[l210 + v3] + rop[l010 + v3];
+    double gradV_nx = (f2 - f1) * tix, gradV_ny = (f4 - f3) * tjy;
+    f1 = rop[il + v4]; f2 = rop[ir + v4]; fv = f1 + f2;
+    f5 = fv + rop[l202 + v4] + rop[l002 + v4];
+    f6 = fv + rop[l201 + v4] + rop[l001 + v4];
+    double gradW_nx = (f2 - f1) * tix, gradW_nz = (f6 - f5) * tkz;
+    f1 = rop[il + v5]; f2 = rop[ir + v5];
+    double gradT_nx = (f2 - f1) * tix;
+    div = (gradU_nx + gradV_ny + gradW_nz) * cvisq;
+    f1 = gradU_nx - div;
+    f2 = gradU_ny + gradV_nx;
+    f3 = gradU_nz + gradW_nx;
+    double xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
+    double xktvol = xmutvol * c->gam3;
+    fv = -(2. * f1 * tcx) * xmutvol;
+    fv5 = fv * (rop[ir + v2] + rop[il + v2]);
+    flu[1] = flu[1] + fv;
+    fv = -(f2 * tcx) * xmutvol;
+    fv5 = fv5 + fv * (rop[ir + v3] + rop[il + v3]);
+    flu[2] = flu[2] + fv;
+    fv = -(f3 * tcx) * xmutvol;
+    fv5 = fv5 + fv * (rop[ir + v4] + rop[il + v4]);
+    flu[3] = flu[3] + fv;
+    fv = fv5 * 0.5 - (gradT_nx * tcx) * xktvol;
+    flu[4] = flu[4] + fv;
+  } else if (d == 1) {
+    il = l - incj;
+    int64_t l022 = l - incj - inck, l002 = l - inck, l021 = l - incj + inck, l001 = l + inck;
+    int64_t l220 = l - inci - incj, l200 = l - inci, l120 = l + inci - incj, l100 = l + inci;
+    double tiy = tcy, tjz = .25 * tcz, tkx = .25 * tcx;
+    f1 = rop[il + v2]; f2 = rop[ir + v2]; fv = f1 + f2;
+    f5 = fv + rop[l220 + v2] + rop[l200 + v2];
+    f6 = fv + rop[l120 + v2] + rop[l100 + v2];
+    double gradU_nx = (f6 - f5) * tkx, gradU_ny = (f2 - f1) * tiy;
+    f1 = rop[il + v3]; f2 = rop[ir + v3]; fv = f1 + f2;
+    f3 = fv + rop[l022 + v3] + rop[l002 + v3];
+    f4 = fv + rop[l021 + v3] + rop[l001 + v3];
+    f5 = fv + rop[l220 + v3] + rop[l200 + v3];
+    f6 = fv + rop[l120 + v3] + rop[l100 + v3];
+    double gradV_nx = (f6 - f5) * tkx, gradV_ny = (f2 - f1) * tiy, gradV_nz = (f4 - f3) * tjz;
+    f1 = rop[il + v4]; f2 = rop[ir + v4]; fv = f1 + f2;
+    f3 = fv + rop[l022 + v4] + rop[l002 + v4];
+    f4 = fv + rop[l021 + v4] + rop[l001 + v4];
+    double gradW_ny = (f2 - f1) * tiy, gradW_nz = (f4 - f3) * tjz;
+    f1 = rop[il + v5]; f2 = rop[ir + v5];
+    double gradT_ny = (f2 - f1) * tiy;
+    div = (gradU_nx + gradV_ny + gradW_nz) * cvisq;
+    f2 = gradU_ny + gradV_nx;
+    f4 = gradV_ny - div;
+    f5 = gradV_nz + gradW_ny;
+    double xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
+    double xktvol = xmutvol * c->gam3;
+    fv = -(f2 * tcy) * xmutvol;
+    fv5 = fv * (rop[ir + v2] + rop[il + v2]);
+    flu[1] = flu[1] + fv;
+    fv = -(2. * f4 * tcy) * xmutvol;
+    fv5 = fv5 + fv * (rop[ir + v3] + rop[il + v3]);
+    flu[2] = flu[2] + fv;
+    fv = -(f5 * tcy) * xmutvol;
+    fv5 = fv5 + fv * (rop[ir + v4] + rop[il + v4]);
+    flu[3] = flu[3] + fv;
+    fv = fv5 * 0.5 - (gradT_ny * tcy) * xktvol;
+    flu[4] = flu[4] + fv;
+  } else {
+    il = l - inck;
+    int64_t l200 = l - inci, l202 = l - inci - inck, l102 = l + inci - inck, l100 = l + inci;
+    int64_t l022 = l - incj - inck, l020 = l - incj, l012 = l + incj - inck, l010 = l + incj;
+    double tiz = tcz, tky = 0.25 * tcy, tjx = 0.25 * tcx;
+    f1 = rop[il + v2]; f2 = rop[ir + v2]; fv = f1 + f2;
+    f3 = fv + rop[l202 + v2] + rop[l200 + v2];
+    f4 = fv + rop[l102 + v2] + rop[l100 + v2];
+    double gradU_nx = (f4 - f3) * tjx, gradU_nz = (f2 - f1) * tiz;
+    f1 = rop[il + v3]; f2 = rop[ir + v3]; fv = f1 + f2;
+    f5 = fv + rop[l022 + v3] + rop[l020 + v3];
+    f6 = fv + rop[l012 + v3] + rop[l010 + v3];
+    double gradV_ny = (f6 - f5) * tky, gradV_nz = (f2 - f1) * tiz;
+    f1 = rop[il + v4]; f2 = rop[l + v4]; fv = f1 + f2;
+    f3 = fv + rop[l202 + v4] + rop[l200 + v4];
+    f4 = fv + rop[l102 + v4] + rop[l100 + v4];
+    f5 = fv + rop[l022 + v4] + rop[l020 + v4];
+    f6 = fv + rop[l012 + v4] + rop[l010 + v4];
+    double gradW_nx = (f4 - f3) * tjx, gradW_ny = (f6 - f5) * tky, gradW_nz = (f2 - f1) * tiz;
+    f1 = rop[il + v5]; f2 = rop[ir + v5];
+    double gradT_nz = (f2 - f1) * tiz;
+    div = (gradU_nx + gradV_ny + gradW_nz) * cvisq;
+    f3 = gradU_nz + gradW_nx;
+    f5 = gradV_nz + gradW_ny;
+    f6 = gradW_nz - div;
+    double xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
+    double xktvol = xmutvol * c->gam3;
+    fv = -f3 * tcz * xmutvol;
+    fv5 = fv * (rop[ir + v2] + rop[il + v2]);
+    flu[1] = flu[1] + fv;
+    fv = -f5 * tcz * xmutvol;
+    fv5 = fv5 + fv * (rop[ir + v3] + rop[il + v3]);
+    flu[2] = flu[2] + fv;
+    fv = -2. * f6 * tcz * xmutvol;
+    fv5 = fv5 + fv * (rop[ir + v4] + rop[il + v4]);
+    flu[3] = flu[3] + fv;
+    fv = fv5 * 0.5 - gradT_nz * tcz * xktvol;
+    flu[4] = flu[4] + fv;
+  }
+}
+
+/* One face flux (convective + viscous) of direction d at cell (i,j,k). */
+static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, double flu[5]) {
+  int64_t l = inddm(c->pi, i, j, k);
+  int64_t lt = indmtr(c->pi, i, j, k);
+  double qm[5], qp[5], tcx, tcy, tcz, s;
+  slopes(c, l, c->inc[d], qm, qp);
+  if (c->typ == 2) {
+    tcx = d == 0 ? c->tcx : 0.; tcy = d == 1 ? c->tcy : 0.; tcz = d == 2 ? c->tcz : 0.;
+    s = d == 0 ? c->si : (d == 1 ? c->sj : c->sk);
+  } else {
+    face_normal(c, d, lt, &tcx, &tcy, &tcz, &s);
+  }
+  if (c->kflu == 5) roe_face(c, qm, qp, tcx, tcy, tcz, s, flu);
+  else ausm_face(c, qm, qp, c->rop[l + 4 * c->nd], tcx, tcy, tcz, s, flu);
+  if (c->iflow >= 2) visc_cart(c, d, l, flu);
+}
+
+/* Flux balance of template_FluxAndBalance.for:192-271 for one zone: every
+ * face flux is computed once; each interior cell then receives, in the
+ * order the reference's k/j/i loop nest produces, drodm + F_k(lo) + F_j(lo)
+ * + F_i(lo) - F_i(hi) - F_j(hi) - F_k(hi). */
+void or_flux(const int64_t* pi, const double* pr, const int64_t* ind,
+             const double* rop, double* drodm, const double* xmut,
+             const double* ti, const double* tj, const double* tk, const double* vol) {
+  fctx c;
+  fctx_init(&c, pi, pr, rop, xmut, ti, tj, tk, vol);
+  int64_t ni = ind[1] - ind[0] + 1, nj = ind[3] - ind[2] + 1, nk = ind[5] - ind[4] + 1;
+  int two_d = (c.typ == 3);
+  int64_t fi = (ni + 1) * nj * nk, fj = ni * (nj + 1) * nk, fk = ni * nj * (nk + 1);
+  double* Fi = (double*)malloc(sizeof(double) * 5 * fi);
+  double* Fj = (double*)malloc(sizeof(double) * 5 * fj);
+  double* Fk = two_d ? NULL : (double*)malloc(sizeof(double) * 5 * fk);
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t kk = 0; kk < nk + 1; kk++) {
+    double flu[5];
+    int64_t k = ind[4] + kk;
+    for (int64_t jj = 0; jj < nj + 1; jj++)
+      for (int64_t ii = 0; ii < ni + 1; ii++) {
+        int64_t i = ind[0] + ii, j = ind[2] + jj;
+        if (kk < nk && jj < nj) {
+          face_flux(&c, 0, i, j, k, flu);
+          for (int v = 0; v < 5; v++) Fi[v * fi + ii + (ni + 1) * (jj + nj * kk)] = flu[v];
+        }
+        if (kk < nk && ii < ni) {
+          face_flux(&c, 1, i, j, k, flu);
+          for (int v = 0; v < 5; v++) Fj[v * fj + ii + ni * (jj + (nj + 1) * kk)] = flu[v];
+        }
+        if (!two_d && jj < nj && ii < ni) {
+          face_flux(&c, 2, i, j, k, flu);
+          for (int v = 0; v < 5; v++) Fk[v * fk + ii + ni * (jj + nj * kk)] = flu[v];
+        }
+      }
+  }
+  int64_t nd = pi[NDIMDX];
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t kk = 0; kk < nk; kk++)
+    for (int64_t jj = 0; jj < nj; jj++)
+      for (int64_t ii = 0; ii < ni; ii++) {
+        int64_t l = inddm(pi, ind[0] + ii, ind[2] + jj, ind[4] + kk);
+        int64_t ai = ii + (ni + 1) * (jj + nj * kk);
+        int64_t aj = ii + ni * (jj + (nj + 1) * kk);
+        int64_t ak = ii + ni * (jj + nj * kk);
+        for (int v = 0; v < 5; v++) {
+          double x = drodm[l + v * nd];
+          if (!two_d) x = x + Fk[v * fk + ak];
+          x = x + Fj[v * fj + aj];
+          x = x + Fi[v * fi + ai];
+          x = x - Fi[v * fi + ai + 1];
+          x = x - Fj[v * fj + aj + ni];
+          if (!two_d) x = x - Fk[v * fk + ak + ni * nj];
+          drodm[l + v * nd] = x;
+        }
+      }
+  free(Fi); free(Fj); free(Fk);
+}
+
+/* ======================================================================
+ * core3ark3 -- FastS/FastS/Compute/core3ark3.for:6-150 (RK3 low storage,
+ * B = 0.5, 0.9106836025229591, 0.3660254037844387; prim <-> cons update)
+ * ====================================================================== */
+void or_core3ark3(const int64_t* pi, const double* pr, int nitcfg, const int64_t* ind,
+                  double* rop_1, const double* rop, const double* drodm, const double* coe) {
+  const double cgamma1 = 0.5, cgamma2 = 0.9106836025229591, cgamma3 = 0.3660254037844387;
+  int64_t nd = pi[NDIMDX];
+  double cv = pr[CVINF], cvinv = 1. / cv, cvinv2 = 0.5 * cvinv;
+  int64_t b = pi[RK];
+  double coefW = 0.;
+  if (b == 1) { if (nitcfg == 1) coefW = 1.; }
+  else if (b == 2) { if (nitcfg == 1) coefW = 1.; else if (nitcfg == 2) coefW = 0.5; }
+  else if (b == 3) {
+    if (nitcfg == 1) coefW = cgamma1;
+    else if (nitcfg == 2) coefW = cgamma2;
+    else if (nitcfg == 3) coefW = cgamma3;
+  }
+  int two_d = pi[ITYPZONE] == 3;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        double r_1 = coefW * coe[l];
+        double tab1 = drodm[l] * r_1, tab2 = drodm[l + nd] * r_1, tab3 = drodm[l + 2 * nd] * r_1;
+        double tab4 = drodm[l + 3 * nd] * r_1, tab5 = drodm[l + 4 * nd] * r_1;
+        double ro_old = rop[l], u_old = rop[l + nd], v_old = rop[l + 2 * nd];
+        double w_old = rop[l + 3 * nd], t_old = rop[l + 4 * nd];
+        rop_1[l] = rop[l] + tab1;
+        r_1 = 1. / rop_1[l];
+        rop_1[l + nd] = (ro_old * u_old + tab2) * r_1;
+        rop_1[l + 2 * nd] = (ro_old * v_old + tab3) * r_1;
+        if (!two_d) {
+          rop_1[l + 3 * nd] = (ro_old * w_old + tab4) * r_1;
+          double roe_old = ro_old * (cv * t_old + 0.5 * (u_old * u_old + v_old * v_old + w_old * w_old));
+          rop_1[l + 4 * nd] = (roe_old + tab5) * r_1 * cvinv -
+              cvinv2 * (rop_1[l + nd] * rop_1[l + nd] + rop_1[l + 2 * nd] * rop_1[l + 2 * nd] +
+                        rop_1[l + 3 * nd] * rop_1[l + 3 * nd]);
+        } else {
+          rop_1[l + 3 * nd] = 0.;
+          double roe_old = ro_old * (cv * t_old + 0.5 * (u_old * u_old + v_old * v_old));
+          rop_1[l + 4 * nd] = (roe_old + tab5) * r_1 * cvinv -
+              cvinv2 * (rop_1[l + nd] * rop_1[l + nd] + rop_1[l + 2 * nd] * rop_1[l + 2 * nd]);
+        }
+      }
+}
+
+/* ======================================================================
+ * core3as2 -- FastS/FastS/Compute/core3as2.for:233-374 (5 eq.): dual time
+ * Newton residual; BDF1 on the first physical step, BDF2 after.
+ * ====================================================================== */
+void or_core3as2(const int64_t* pi, const double* pr, int nitcfg, int first_it,
+                 const int64_t* ind, const double* rop, const double* rop_n,
+                 const double* rop_n1, double* drodm, const double* coe) {
+  int64_t nd = pi[NDIMDX];
+  double cv = pr[CVINF];
+  double c1, c2, c3;
+  if (first_it == 0 || pi[DTLOC] == 1) { c1 = -1.; c2 = 1.; c3 = 0.; }
+  else { c1 = -1.5; c2 = 2.; c3 = -0.5; }
+  int two_d = pi[ITYPZONE] == 3;
+  double c4 = c1 + c2;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        const double *a = rop, *b = rop_n, *m = rop_n1;
+        double cf = coe[l];
+        if (nitcfg == 1) {
+          drodm[l] = cf * drodm[l] + c4 * a[l] + c3 * m[l];
+          for (int v = 1; v <= 3; v++) {
+            if (two_d && v == 3) continue;
+            int64_t o = v * nd;
+            drodm[l + o] = cf * drodm[l + o] + c4 * a[l + o] * a[l] + c3 * m[l + o] * m[l];
+          }
+          double roe, roe_n1;
+          if (!two_d) {
+            roe = a[l] * (cv * a[l + 4 * nd] + 0.5 * (a[l + nd] * a[l + nd] + a[l + 2 * nd] * a[l + 2 * nd] + a[l + 3 * nd] * a[l + 3 * nd]));
+            roe_n1 = m[l] * (cv * m[l + 4 * nd] + 0.5 * (m[l + nd] * m[l + nd] + m[l + 2 * nd] * m[l + 2 * nd] + m[l + 3 * nd] * m[l + 3 * nd]));
+          } else {
+            roe = a[l] * (cv * a[l + 4 * nd] + 0.5 * (a[l + nd] * a[l + nd] + a[l + 2 * nd] * a[l + 2 * nd]));
+            roe_n1 = m[l] * (cv * m[l + 4 * nd] + 0.5 * (m[l + nd] * m[l + nd] + m[l + 2 * nd] * m[l + 2 * nd]));
+          }
+          drodm[l + 4 * nd] = cf * drodm[l + 4 * nd] + c4 * roe + c3 * roe_n1;
+        } else {
+          drodm[l] = cf * drodm[l] + c1 * a[l] + c2 * b[l] + c3 * m[l];
+          for (int v = 1; v <= 3; v++) {
+            if (two_d && v == 3) continue;
+            int64_t o = v * nd;
+            drodm[l + o] = cf * drodm[l + o] + c1 * a[l + o] * a[l] + c2 * b[l + o] * b[l] + c3 * m[l + o] * m[l];
+          }
+          double roe, roe_n, roe_n1;
+          if (!two_d) {
+            roe = a[l] * (cv * a[l + 4 * nd] + 0.5 * (a[l + nd] * a[l + nd] + a[l + 2 * nd] * a[l + 2 * nd] + a[l + 3 * nd] * a[l + 3 * nd]));
+            roe_n = b[l] * (cv * b[l + 4 * nd] + 0.5 * (b[l + nd] * b[l + nd] + b[l + 2 * nd] * b[l + 2 * nd] + b[l + 3 * nd] * b[l + 3 * nd]));
+            roe_n1 = m[l] * (cv * m[l + 4 * nd] + 0.5 * (m[l + nd] * m[l + nd] + m[l + 2 * nd] * m[l + 2 * nd] + m[l + 3 * nd] * m[l + 3 * nd]));
+          } else {
+            roe = a[l] * (cv * a[l + 4 * nd] + 0.5 * (a[l + nd] * a[l + nd] + a[l + 2 * nd] * a[l + 2 * nd]));
+            roe_n = b[l] * (cv * b[l + 4 * nd] + 0.5 * (b[l + nd] * b[l + nd] + b[l + 2 * nd] * b[l + 2 * nd]));
+            roe_n1 = m[l] * (cv * m[l + 4 * nd] + 0.5 * (m[l + nd] * m[l + nd] + m[l + 2 * nd] * m[l + 2 * nd]));
+          }
+          drodm[l + 4 * nd] = cf * drodm[l + 4 * nd] + c1 * roe + c2 * roe_n + c3 * roe_n1;
+        }
+      }
+}
+
+/* ======================================================================
+ * LU-SGS -- FastS/FastS/Compute/LU/invlu_l.for (lower), invlu_u.for
+ * (upper + mjr_newton.for), neighbour terms lu_{i,j,k}_{3dcart,3dfull,2d}.for.
+ * ====================================================================== */
+typedef struct {
+  const int64_t* pi; const double *rop, *coe, *ti, *tj, *tk;
+  int64_t nd, ndm, inc[3], inc_mtr[3];
+  int typ;
+  double gam1, gamm1, cp, gam2;
+} luctx;
+
+/* b = B(W_nb) . out_nb for direction d, neighbour l1 (= l - inc for the
+ * lower sweep, l + inc for the upper).  signe = +-0.5.  For the 3d full /
+ * 2d zones the normal is the mean of the neighbour's two faces in d. */
+static void lu_nb(const luctx* c, int d, int64_t l1, int64_t ltnb1, int64_t ltnb2,
+                  double signe, const double* out, double b[5]) {
+  int64_t nd = c->nd;
+  double tcx = 0., tcy = 0., tcz = 0.;
+  if (c->typ == 2) {
+    if (d == 0) tcx = c->ti[0]; else if (d == 1) tcy = c->tj[0]; else tcz = c->tk[0];
+  } else {
+    const double* t = d == 0 ? c->ti : (d == 1 ? c->tj : c->tk);
+    tcx = 0.5 * (t[ltnb2] + t[ltnb1]);
+    tcy = 0.5 * (t[ltnb2 + c->ndm] + t[ltnb1 + c->ndm]);
+    if (c->typ == 0) tcz = 0.5 * (t[ltnb2 + 2 * c->ndm] + t[ltnb1 + 2 * c->ndm]);
+  }
+  double u = c->rop[l1 + nd], v = c->rop[l1 + 2 * nd], w = c->rop[l1 + 3 * nd], t = c->rop[l1 + 4 * nd];
+  double gam1 = c->gam1, gamm1 = c->gamm1, gam2 = c->gam2;
+  double o1 = out[l1], o2 = out[l1 + nd], o3 = out[l1 + 2 * nd], o4 = out[l1 + 3 * nd], o5 = out[l1 + 4 * nd];
+  double cs = c->coe[l1 + (d + 1) * nd] * signe;
+  if (c->typ == 2) {
+    double q2 = .5 * (u * u + v * v + w * w);
+    double h = c->cp * t + q2;
+    double ph2 = gamm1 * q2;
+    if (d == 0) { /* lu_i_3dcart.for */
+      double qn = tcx * u;
+      double b11 = cs, b12 = tcx;
+      double b21 = (tcx * ph2 - u * qn), b22 = (qn - tcx * gam2 * u) + cs, b23 = (-tcx * gamm1 * v), b24 = (-tcx * gamm1 * w), b25 = tcx * gamm1;
+      double b31 = (-v * qn), b32 = (tcx * v), b33 = (qn) + cs;
+      double b41 = (-w * qn), b42 = (tcx * w), b44 = (qn) + cs;
+      double b51 = qn * (ph2 - h), b52 = (tcx * h - gamm1 * u * qn), b53 = (-gamm1 * v * qn), b54 = (-gamm1 * w * qn), b55 = (gam1 * qn) + cs;
+      b[0] = b11 * o1 + b12 * o2;
+      b[1] = b21 * o1 + b22 * o2 + b23 * o3 + b24 * o4 + b25 * o5;
+      b[2] = b31 * o1 + b32 * o2 + b33 * o3;
+      b[3] = b41 * o1 + b42 * o2 + b44 * o4;
+      b[4] = b51 * o1 + b52 * o2 + b53 * o3 + b54 * o4 + b55 * o5;
+    } else if (d == 1) { /* lu_j_3dcart.for */
+      double qn = tcy * v;
+      double b11 = cs, b13 = tcy;
+      double b21 = (-u * qn), b22 = qn + cs, b23 = tcy * u;
+      double b31 = (tcy * ph2 - v * qn), b32 = (-tcy * gamm1 * u), b33 = (qn - tcy * gam2 * v) + cs, b34 = (-tcy * gamm1 * w), b35 = tcy * gamm1;
+      double b41 = (-w * qn), b43 = (tcy * w), b44 = (qn) + cs;
+      double b51 = qn * (ph2 - h), b52 = (-gamm1 * u * qn), b53 = (tcy * h - gamm1 * v * qn), b54 = (-gamm1 * w * qn), b55 = (gam1 * qn) + cs;
+      b[0] = b11 * o1 + b13 * o3;
+      b[1] = b21 * o1 + b22 * o2 + b23 * o3;
+      b[2] = b31 * o1 + b32 * o2 + b33 * o3 + b34 * o4 + b35 * o5;
+      b[3] = b41 * o1 + b43 * o3 + b44 * o4;
+      b[4] = b51 * o1 + b52 * o2 + b53 * o3 + b54 * o4 + b55 * o5;
+    } else { /* lu_k_3dcart.for */
+      double qn = tcz * w;
+      double b11 = cs, b14 = tcz;
+      double b21 = -u * qn, b22 = qn + cs, b24 = tcz * u;
+      double b31 = -v * qn, b33 = qn + cs, b34 = tcz * v;
+      double b41 = tcz * ph2 - w * qn, b42 = -tcz * gamm1 * u, b43 = -tcz * gamm1 * v, b44 = (qn - tcz * gam2 * w) + cs, b45 = tcz * gamm1;
+      double b51 = qn * (ph2 - h), b52 = -gamm1 * u * qn, b53 = -gamm1 * v * qn, b54 = tcz * h - gamm1 * w * qn, b55 = gam1 * qn + cs;
+      b[0] = b11 * o1 + b14 * o4;
+      b[1] = b21 * o1 + b22 * o2 + b24 * o4;
+      b[2] = b31 * o1 + b33 * o3 + b34 * o4;
+      b[3] = b41 * o1 + b42 * o2 + b43 * o3 + b44 * o4 + b45 * o5;
+      b[4] = b51 * o1 + b52 * o2 + b53 * o3 + b54 * o4 + b55 * o5;
+    }
+    return;
+  }
+  if (c->typ == 0) { /* lu_{i,j,k}_3dfull.for */
+    double q2 = .5 * (u * u + v * v + w * w);
+    double h = c->cp * t + q2;
+    double ph2 = gamm1 * q2;
+    double qn = tcx * u + tcy * v + tcz * w;
+    double b11 = cs, b12 = tcx, b13 = tcy, b14 = tcz;
+    double b21 = (tcx * ph2 - u * qn), b22 = (qn - tcx * gam2 * u) + cs, b23 = (tcy * u - tcx * gamm1 * v), b24 = (tcz * u - tcx * gamm1 * w), b25 = tcx * gamm1;
+    double b31 = (tcy * ph2 - v * qn), b32 = (tcx * v - tcy * gamm1 * u), b33 = (qn - tcy * gam2 * v) + cs, b34 = (tcz * v - tcy * gamm1 * w), b35 = tcy * gamm1;
+    double b41 = (tcz * ph2 - w * qn), b42 = (tcx * w - tcz * gamm1 * u), b43 = (tcy * w - tcz * gamm1 * v), b44 = (qn - tcz * gam2 * w) + cs, b45 = tcz * gamm1;
+    double b51 = qn * (ph2 - h), b52 = (tcx * h - gamm1 * u * qn), b53 = (tcy * h - gamm1 * v * qn), b54 = (tcz * h - gamm1 * w * qn), b55 = (gam1 * qn) + cs;
+    b[0] = b11 * o1 + b12 * o2 + b13 * o3 + b14 * o4;
+    b[1] = b21 * o1 + b22 * o2 + b23 * o3 + b24 * o4 + b25 * o5;
+    b[2] = b31 * o1 + b32 * o2 + b33 * o3 + b34 * o4 + b35 * o5;
+    b[3] = b41 * o1 + b42 * o2 + b43 * o3 + b44 * o4 + b45 * o5;
+    b[4] = b51 * o1 + b52 * o2 + b53 * o3 + b54 * o4 + b55 * o5;
+    return;
+  }
+  { /* lu_{i,j}_2d.for */
+    double q2 = .5 * (u * u + v * v);
+    double h = c->cp * t + q2;
+    double ph2 = gamm1 * q2;
+    double qn = tcx * u + tcy * v;
+    double b11 = cs, b12 = tcx, b13 = tcy;
+    double b21 = (tcx * ph2 - u * qn), b22 = (qn - tcx * gam2 * u) + cs, b23 = (tcy * u - tcx * gamm1 * v), b25 = tcx * gamm1;
+    double b31 = (tcy * ph2 - v * qn), b32 = (tcx * v - tcy * gamm1 * u), b33 = (qn - tcy * gam2 * v) + cs, b35 = tcy * gamm1;
+    double b51 = qn * (ph2 - h), b52 = (tcx * h - gamm1 * u * qn), b53 = (tcy * h - gamm1 * v * qn), b55 = (gam1 * qn) + cs;
+    b[0] = b11 * o1 + b12 * o2 + b13 * o3;
+    b[1] = b21 * o1 + b22 * o2 + b23 * o3 + b25 * o5;
+    b[2] = b31 * o1 + b32 * o2 + b33 * o3 + b35 * o5;
+    b[3] = 0.;
+    b[4] = b51 * o1 + b52 * o2 + b53 * o3 + b55 * o5;
+  }
+}
+
+/* mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW) */
+static void mjr_newton(const int64_t* pi, const double* pr, int64_t l, const double* rop,
+                       double* rop_1, const double* out) {
+  int64_t nd = pi[NDIMDX];
+  double cvinv = 1. / pr[CVINF], cvinv2 = 0.5 * cvinv;
+  double ro_old = rop[l], u_old = rop[l + nd], v_old = rop[l + 2 * nd], w_old = rop[l + 3 * nd], t_old = rop[l + 4 * nd];
+  double n1 = rop[l] + out[l];
+  double r_1 = 1. / n1;
+  double n2 = (ro_old * u_old + out[l + nd]) * r_1;
+  double n3 = (ro_old * v_old + out[l + 2 * nd]) * r_1;
+  if (pi[ITYPZONE] == 3) {
+    double roe_old = ro_old * (pr[CVINF] * t_old + 0.5 * (u_old * u_old + v_old * v_old));
+    double n5 = (roe_old + out[l + 4 * nd]) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3);
+    rop_1[l] = n1; rop_1[l + nd] = n2; rop_1[l + 2 * nd] = n3; rop_1[l + 3 * nd] = 0.; rop_1[l + 4 * nd] = n5;
+    return;
+  }
+  double n4 = (ro_old * w_old + out[l + 3 * nd]) * r_1;
+  double roe_old = ro_old * (pr[CVINF] * t_old + 0.5 * (u_old * u_old + v_old * v_old + w_old * w_old));
+  double n5 = (roe_old + out[l + 4 * nd]) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
+  rop_1[l] = n1; rop_1[l + nd] = n2; rop_1[l + 2 * nd] = n3; rop_1[l + 3 * nd] = n4; rop_1[l + 4 * nd] = n5;
+}
+
+void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind,
+              double* rotmp, double* rop_ssiter, const double* drodm_in,
+              double* drodm_out, const double* ti, const double* tj, const double* tk,
+              const double* coe, int mjrnewton) {
+  if (ind[1] < ind[0]) return;
+  luctx c;
+  c.pi = pi; c.rop = rop_ssiter; c.coe = coe; c.ti = ti; c.tj = tj; c.tk = tk;
+  c.nd = pi[NDIMDX]; c.ndm = pi[NDIMDX_MTR]; c.typ = (int)pi[ITYPZONE];
+  c.inc[0] = 1; c.inc[1] = pi[NIJK]; c.inc[2] = pi[NIJK] * pi[NIJK + 1];
+  c.inc_mtr[0] = pi[NIJK_MTR]; c.inc_mtr[1] = pi[NIJK_MTR + 1]; c.inc_mtr[2] = pi[NIJK_MTR + 2];
+  c.gam1 = pr[GAMMA]; c.gamm1 = c.gam1 - 1.; c.cp = pr[GAMMA] * pr[CVINF]; c.gam2 = c.gamm1 - 1.;
+  int64_t nd = c.nd;
+  int neq = 5;
+  int two_d = c.typ == 3;
+  /* lower sweep: invlu_l.for, lexicographic k, j, i.  The neighbour terms
+   * present at a cell are those whose neighbour lies inside the LU range;
+   * their order is j, k, i on a 3d cartesian zone (invlu_l.for 3dcart
+   * section) and k, j, i otherwise. */
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k), lt = indmtr(pi, i, j, k);
+        double xal = coe[l] * 0.5;
+        double x[5], b[5];
+        int first = 1;
+        int hasj = j > ind[2], hask = (!two_d) && k > ind[4], hasi = i > ind[0];
+        int order[2] = {2, 1};
+        if (c.typ == 2) { order[0] = 1; order[1] = 2; }
+        for (int v = 0; v < neq; v++) x[v] = drodm_in[l + v * nd];
+        for (int o = 0; o < 2; o++) {
+          int d = order[o];
+          if ((d == 1 && !hasj) || (d == 2 && !hask)) continue;
+          lu_nb(&c, d, l - c.inc[d], lt - c.inc_mtr[d], lt, 0.5, drodm_out, b);
+          for (int v = 0; v < neq; v++) x[v] = x[v] + b[v] * xal;
+          first = 0;
+        }
+        if (hasi) {
+          lu_nb(&c, 0, l - 1, lt - c.inc_mtr[0], lt, 0.5, drodm_out, b);
+          for (int v = 0; v < neq; v++) x[v] = x[v] + b[v] * xal;
+        }
+        (void)first;
+        double diag = 1. / coe[l + 4 * nd];
+        for (int v = 0; v < neq; v++) drodm_out[l + v * nd] = x[v] * diag;
+        if (two_d) drodm_out[l + 3 * nd] = drodm_in[l + 3 * nd] * diag;
+      }
+  /* upper sweep: invlu_u.for, reverse lexicographic; out = D^-1 (D out_L
+   * + terms k, j, i), then mjr_newton plane by plane (k descending).  When
+   * rotmp and rop_ssiter are the same array the k+1 neighbour is read after
+   * its plane has been Newton-updated, as in the reference. */
+  for (int64_t k = ind[5]; k >= ind[4]; k--) {
+    for (int64_t j = ind[3]; j >= ind[2]; j--)
+      for (int64_t i = ind[1]; i >= ind[0]; i--) {
+        int64_t l = inddm(pi, i, j, k), lt = indmtr(pi, i, j, k);
+        double xal = coe[l] * (-0.5);
+        double x[5], b[5];
+        double dg = coe[l + 4 * nd];
+        for (int v = 0; v < neq; v++) x[v] = drodm_out[l + v * nd] * dg;
+        int hasj = j < ind[3], hask = (!two_d) && k < ind[5], hasi = i < ind[1];
+        if (hask) {
+          lu_nb(&c, 2, l + c.inc[2], lt + c.inc_mtr[2], lt + 2 * c.inc_mtr[2], -0.5, drodm_out, b);
+          for (int v = 0; v < neq; v++) x[v] = x[v] + b[v] * xal;
+        }
+        if (hasj) {
+          lu_nb(&c, 1, l + c.inc[1], lt + c.inc_mtr[1], lt + 2 * c.inc_mtr[1], -0.5, drodm_out, b);
+          for (int v = 0; v < neq; v++) x[v] = x[v] + b[v] * xal;
+        }
+        if (hasi) {
+          lu_nb(&c, 0, l + 1, lt + c.inc_mtr[0], lt + 2 * c.inc_mtr[0], -0.5, drodm_out, b);
+          for (int v = 0; v < neq; v++) x[v] = x[v] + b[v] * xal;
+        }
+        double diag = 1. / coe[l + 4 * nd];
+        for (int v = 0; v < neq; v++) drodm_out[l + v * nd] = x[v] * diag;
+      }
+    if (mjrnewton == 1)
+      for (int64_t j = ind[2]; j <= ind[3]; j++)
+        for (int64_t i = ind[0]; i <= ind[1]; i++)
+          mjr_newton(pi, pr, inddm(pi, i, j, k), rop_ssiter, rotmp, drodm_out);
+  }
+}
+
+/* ======================================================================
+ * cprdu3s1 -- FastS/FastS/Compute/cprdu3s1_incl.for:14-135: per LU block
+ * (SIZE_SSDOM cells, the last block of a direction takes the remainder)
+ * sum of squares and max |drodm| for each equation, stored at sub-iteration
+ * it_bloc: rdm(it_bloc, ne, 1:2, no_rdm) (Fortran order).
+ * ====================================================================== */
+void or_cprdu3s1(const int64_t* pi, int it_bloc, int nssiter, const double* drodm, double* rdm) {
+  int64_t ijkv_lu[3];
+  for (int d = 0; d < 3; d++) {
+    int64_t q = pi[IJKV + d] / pi[SIZE_SSDOM + d];
+    ijkv_lu[d] = q > 1 ? q : 1;
+  }
+  int64_t neq = pi[NEQ], nd = pi[NDIMDX];
+  int64_t nrdm = ijkv_lu[0] * ijkv_lu[1] * ijkv_lu[2];
+  for (int64_t no = 0; no < nrdm; no++) {
+    int64_t k_lu = no / (ijkv_lu[0] * ijkv_lu[1]);
+    int64_t j_lu = (no - ijkv_lu[0] * ijkv_lu[1] * k_lu) / ijkv_lu[0];
+    int64_t i_lu = no - j_lu * ijkv_lu[0] - k_lu * ijkv_lu[0] * ijkv_lu[1];
+    int64_t lo[3] = {i_lu, j_lu, k_lu}, a[3], b[3];
+    for (int d = 0; d < 3; d++) {
+      a[d] = 1 + lo[d] * pi[SIZE_SSDOM + d];
+      b[d] = (lo[d] + 1) * pi[SIZE_SSDOM + d];
+      if (lo[d] == ijkv_lu[d] - 1) b[d] = pi[IJKV + d];
+    }
+    double xs[6] = {0, 0, 0, 0, 0, 0}, xm[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t k = a[2]; k <= b[2]; k++)
+      for (int64_t j = a[1]; j <= b[1]; j++)
+        for (int64_t i = a[0]; i <= b[0]; i++) {
+          int64_t l = inddm(pi, i, j, k);
+          for (int64_t ne = 0; ne < neq; ne++) {
+            double dv = drodm[l + ne * nd];
+            double xp = fabs(dv);
+            if (xp > xm[ne]) xm[ne] = xp;
+            xs[ne] = xs[ne] + dv * dv;
+          }
+        }
+    for (int64_t ne = 0; ne < neq; ne++) {
+      rdm[(it_bloc - 1) + ne * nssiter + 0 * neq * nssiter + no * neq * 2 * nssiter] = xs[ne];
+      rdm[(it_bloc - 1) + ne * nssiter + 1 * neq * nssiter + no * neq * 2 * nssiter] = xm[ne];
+    }
+  }
+}
+
+/* display_ss_iteration.cpp:112-145 */
+void or_residual_norms(const int64_t* pi, const double* pr, const double* rdm,
+                       int nssiter, int it_bloc, double* out) {
+  int64_t ijkv_lu[3];
+  for (int d = 0; d < 3; d++) {
+    int64_t q = pi[IJKV + d] / pi[SIZE_SSDOM + d];
+    ijkv_lu[d] = q > 1 ? q : 1;
+  }
+  int64_t neq = pi[NEQ];
+  double xpt_1 = 1. / (double)(pi[IJKV] * pi[IJKV + 1] * pi[IJKV + 2]);
+  for (int64_t ne = 0; ne < neq; ne++)
+    for (int i = 0; i < it_bloc; i++) {
+      double rmax = 0., rmoy = 0.;
+      for (int64_t k_lu = 0; k_lu < ijkv_lu[2]; k_lu++)
+        for (int64_t j_lu = 0; j_lu < ijkv_lu[1]; j_lu++)
+          for (int64_t i_lu = 0; i_lu < ijkv_lu[0]; i_lu++) {
+            int64_t no = i_lu + j_lu * ijkv_lu[0] + k_lu * ijkv_lu[0] * ijkv_lu[1];
+            int64_t ind1 = i + ne * nssiter + no * neq * 2 * nssiter;
+            int64_t ind2 = i + (ne + neq) * nssiter + no * neq * 2 * nssiter;
+            rmax = OMAX(rmax, rdm[ind2]);
+            rmoy = rmoy + rdm[ind1];
+          }
+      out[it_bloc * ne + i] = sqrt(rmoy * xpt_1) / pr[DTC];
+      out[it_bloc * (ne + neq) + i] = rmax / pr[DTC];
+    }
+}
+
+/* ======================================================================
+ * Ghost cells: BC/BCzone.cpp:60-865 dispatch with FastC/FastC/BC/
+ * indice_cl_sdm.for windows (npass = 0), bvbs_periodique.for (tag 11,
+ * ghost <- cell shifted by the zone size), bvbs_extrapolate.for (tag 0,
+ * zeroth order); then correct_coins.for for edges and corners.
+ * ====================================================================== */
+static void bc_window(const int64_t* pi, const int64_t* fen, int idir, int64_t* cl) {
+  int64_t ng = pi[NIJK + 3], ngk = pi[NIJK + 4];
+  int64_t sdm[6] = {1, pi[IJKV], 1, pi[IJKV + 1], 1, pi[IJKV + 2]};
+  for (int d = 0; d < 3; d++) {
+    cl[2 * d] = OMAX(fen[2 * d], sdm[2 * d]);
+    cl[2 * d + 1] = OMIN(fen[2 * d + 1], sdm[2 * d + 1]);
+  }
+  if (idir == 1) { cl[1] = cl[0] - 1; cl[0] = cl[0] - ng; }
+  else if (idir == 2) { cl[1] = cl[0] + ng; cl[0] = cl[0] + 1; }
+  else if (idir == 3) { cl[3] = cl[2] - 1; cl[2] = cl[2] - ng; }
+  else if (idir == 4) { cl[3] = cl[2] + ng; cl[2] = cl[2] + 1; }
+  else if (idir == 5) { cl[5] = cl[4] - 1; cl[4] = cl[4] - ngk; }
+  else { cl[5] = cl[4] + ngk; cl[4] = cl[4] + 1; }
+}
+
+void or_bc_zone(const int64_t* pi, const double* pr, int lrhs, double* rop) {
+  (void)pr;
+  int64_t pt_bcs = pi[PT_BC];
+  if (pt_bcs <= 0) goto coins;
+  {
+    int64_t nb_bc = pi[pt_bcs];
+    int64_t nd = pi[NDIMDX], neq = pi[NEQ];
+    double c1 = lrhs == 1 ? 0. : 1.;
+    for (int64_t n = 0; n < nb_bc; n++) {
+      int64_t pt = pi[pt_bcs + 1 + n];
+      int64_t type = pi[pt + BC_TYPE];
+      int idir = (int)pi[pt + BC_IDIR];
+      int64_t cl[6];
+      bc_window(pi, pi + pt + BC_FEN, idir, cl);
+      int d = (idir - 1) / 2;
+      int low = (idir % 2) == 1;
+      int64_t n_d = pi[IJKV + d];
+      for (int64_t k = cl[4]; k <= cl[5]; k++)
+        for (int64_t j = cl[2]; j <= cl[3]; j++)
+          for (int64_t i = cl[0]; i <= cl[1]; i++) {
+            int64_t idx[3] = {i, j, k};
+            int64_t l = inddm(pi, i, j, k);
+            int64_t src[3] = {i, j, k};
+            if (type == 11) { src[d] = low ? idx[d] + n_d : idx[d] - n_d; }
+            else if (type == 0) { src[d] = low ? cl[2 * d + 1] + 1 : cl[2 * d] - 1; }
+            else continue;
+            int64_t l1 = inddm(pi, src[0], src[1], src[2]);
+            for (int64_t v = 0; v < neq; v++) {
+              if (type == 11) rop[l + v * nd] = rop[l1 + v * nd] * c1;
+              else rop[l + v * nd] = OMAX(-1.e30, rop[l1 + v * nd]) * c1;
+            }
+          }
+    }
+  }
+coins:
+  if (lrhs == 0) {
+    int64_t ind[6] = {1, pi[IJKV], 1, pi[IJKV + 1], 1, pi[IJKV + 2]};
+    or_correct_coins(pi, ind, rop);
+  }
+}
+
+/* correct_coins.for: edges = mean of the two adjacent face ghosts, corners
+ * = mean of the three. */
+void or_correct_coins(const int64_t* pi, const int64_t* ind_loop, double* rop) {
+  int64_t ng = pi[NIJK + 3], ngk = pi[NIJK + 4], nd = pi[NDIMDX], neq = pi[NEQ];
+  int64_t il[6];
+  il[0] = OMAX(1, ind_loop[0]); il[2] = OMAX(1, ind_loop[2]); il[4] = OMAX(1, ind_loop[4]);
+  il[1] = OMIN(pi[IJKV], ind_loop[1]); il[3] = OMIN(pi[IJKV + 1], ind_loop[3]); il[5] = OMIN(pi[IJKV + 2], ind_loop[5]);
+  int64_t itest[4] = {1, pi[IJKV], 1, pi[IJKV + 1]};
+  /* faces I: edges along j and k */
+  for (int idir = 1; idir <= 2; idir++) {
+    int64_t is = idir == 1 ? -1 : 1;
+    int64_t i0 = il[idir - 1];
+    if (i0 != itest[idir - 1]) continue;
+    if (il[2] == 1)
+      for (int64_t ne = 0; ne < neq; ne++) for (int64_t k = il[4]; k <= il[5]; k++)
+        for (int64_t j = 1; j <= ng; j++) for (int64_t i = 1; i <= ng; i++) {
+          int64_t i1 = OMIN(ng, i + 1), j1 = OMIN(ng, j + 1);
+          int64_t l1 = inddm(pi, i0 + i * is, il[2] - j, k);
+          int64_t l11 = inddm(pi, i0 + i1 * is, il[2], k), l12 = inddm(pi, i0, il[2] - j1, k);
+          rop[l1 + ne * nd] = (rop[l11 + ne * nd] + rop[l12 + ne * nd]) * 0.5;
+        }
+    if (il[3] == pi[IJKV + 1])
+      for (int64_t ne = 0; ne < neq; ne++) for (int64_t k = il[4]; k <= il[5]; k++)
+        for (int64_t j = 1; j <= ng; j++) for (int64_t i = 1; i <= ng; i++) {
+          int64_t i1 = OMIN(ng, i + 1), j1 = OMIN(ng, j + 1);
+          int64_t l1 = inddm(pi, i0 + i * is, il[3] + j, k);
+          int64_t l11 = inddm(pi, i0 + i1 * is, il[3], k), l12 = inddm(pi, i0, il[3] + j1, k);
+          rop[l1 + ne * nd] = (rop[l11 + ne * nd] + rop[l12 + ne * nd]) * 0.5;
+        }
+    if (il[4] == 1)
+      for (int64_t ne = 0; ne < neq; ne++) for (int64_t k = 1; k <= ngk; k++)
+        for (int64_t j = il[2]; j <= il[3]; j++) for (int64_t i = 1; i <= ng; i++) {
+          int64_t k1 = OMIN(ngk, k + 1), i1 = OMIN(ng, i + 1);
+          int64_t l1 = inddm(pi, i0 + i * is, j, il[4] - k);
+          int64_t l11 = inddm(pi, i0, j, il[4] - k1), l12 = inddm(pi, i0 + i1 * is, j, il[4]);
+          rop[l1 + ne * nd] = (rop[l11 + ne * nd] + rop[l12 + ne * nd]) * 0.5;
+        }
+    if (il[5] == pi[IJKV + 2])
+      for (int64_t ne = 0; ne < neq; ne++) for (int64_t k = 1; k <= ngk; k++)
+        for (int64_t j = il[2]; j <= il[3]; j++) for (int64_t i = 1; i <= ng; i++) {
+          int64_t k1 = OMIN(ngk, k + 1), i1 = OMIN(ng, i + 1);
+          int64_t l1 = inddm(pi, i0 + i * is, j, il[5] + k);
+          int64_t l11 = inddm(pi, i0, j, il[5] + k1), l12 = inddm(pi, i0 + i1 * is, j, il[5]);
+          rop[l1 + ne * nd] = (rop[l11 + ne * nd] + rop[l12 + ne * nd]) * 0.5;
+        }
+  }
+  /* faces J: edges along k */
+  for (int idir = 3; idir <= 4; idir++) {
+    int64_t is = idir == 3 ? -1 : 1;
+    int64_t j0 = il[idir - 1];
+    if (j0 != itest[idir - 1]) continue;
+    if (il[4] == 1)
+      for (int64_t ne = 0; ne < neq; ne++) for (int64_t k = 1; k <= ngk; k++)
+        for (int64_t j = 1; j <= ng; j++) for (int64_t i = il[0]; i <= il[1]; i++) {
+          int64_t k1 = OMIN(ngk, k + 1), j1 = OMIN(ng, j + 1);
+          int64_t l1 = inddm(pi, i, j0 + j * is, il[4] - k);
+          int64_t l11 = inddm(pi, i, j0, il[4] - k1), l12 = inddm(pi, i, j0 + j1 * is, il[4]);
+          rop[l1 + ne * nd] = (rop[l11 + ne * nd] + rop[l12 + ne * nd]) * 0.5;
+        }
+    if (il[5] == pi[IJKV + 2])
+      for (int64_t ne = 0; ne < neq; ne++) for (int64_t k = 1; k <= ngk; k++)
+        for (int64_t j = 1; j <= ng; j++) for (int64_t i = il[0]; i <= il[1]; i++) {
+          int64_t k1 = OMIN(ngk, k + 1), j1 = OMIN(ng, j + 1);
+          int64_t l1 = inddm(pi, i, j0 + j * is, il[5] + k);
+          int64_t l11 = inddm(pi, i, j0, il[5] + k1), l12 = inddm(pi, i, j0 + j1 * is, il[5]);
+          rop[l1 + ne * nd] = (rop[l11 + ne * nd] + rop[l12 + ne * nd]) * 0.5;
+        }
+  }
+  /* corners */
+  double c3 = 1. / 3.;
+  for (int corner = 0; corner < 8; corner++) {
+    int hi_i = corner & 1, hi_j = (corner >> 1) & 1, hi_k = (corner >> 2) & 1;
+    int64_t i0 = hi_i ? il[1] : il[0], j0 = hi_j ? il[3] : il[2], k0 = hi_k ? il[5] : il[4];
+    int64_t ti_ = hi_i ? pi[IJKV] : 1, tj_ = hi_j ? pi[IJKV + 1] : 1, tk_ = hi_k ? pi[IJKV + 2] : 1;
+    if (i0 != ti_ || j0 != tj_ || k0 != tk_) continue;
+    int64_t si = hi_i ? 1 : -1, sj = hi_j ? 1 : -1, sk = hi_k ? 1 : -1;
+    for (int64_t ne = 0; ne < neq; ne++) for (int64_t k = 1; k <= ngk; k++)
+      for (int64_t j = 1; j <= ng; j++) for (int64_t i = 1; i <= ng; i++) {
+        int64_t i1 = OMIN(ng, i + 1), j1 = OMIN(ng, j + 1), k1 = OMIN(ngk, k + 1);
+        int64_t l = inddm(pi, i0 + si * i, j0 + sj * j, k0 + sk * k);
+        int64_t l11 = inddm(pi, i0, j0, k0 + sk * k1);
+        int64_t l12 = inddm(pi, i0 + si * i1, j0, k0);
+        int64_t l13 = inddm(pi, i0, j0 + sj * j1, k0);
+        rop[l + ne * nd] = (rop[l11 + ne * nd] + rop[l12 + ne * nd] + rop[l13 + ne * nd]) * c3;
+      }
+  }
+}
+
+/* FastC/FastC/Com/setInterpTransfersFast.cpp:852-883, interpolation type 0
+ * (1-to-1 match): receiver ghost cell <- donor cell, every variable. */
+void or_transfers(or_zone* zones, const or_transfer* tr, int ntr, int use_p1) {
+  for (int t = 0; t < ntr; t++) {
+    or_zone* dz = &zones[tr[t].dnr_zone];
+    or_zone* rz = &zones[tr[t].rcv_zone];
+    const double* src = use_p1 ? dz->ro_p1 : dz->ro;
+    double* dst = use_p1 ? rz->ro_p1 : rz->ro;
+    int64_t ndd = dz->param_int[NDIMDX], ndr = rz->param_int[NDIMDX];
+    int64_t neq = rz->param_int[NEQ];
+    for (int64_t n = 0; n < tr[t].n; n++)
+      for (int64_t v = 0; v < neq; v++)
+        dst[tr[t].rcv_idx[n] + v * ndr] = src[tr[t].dnr_idx[n] + v * ndd];
+  }
+}
+
+/* cpcfl3.for (non-ALE branches): the largest stable dt for the given CFL,
+ * i.e. cfl * min over interior cells of comp = min(vis, conv). */
+double or_cfl_dt(const int64_t* pi, const double* pr, const double* rop,
+                 const double* xmut, const double* ti, const double* tj,
+                 const double* tk, const double* vol, double cfl) {
+  int64_t nd = pi[NDIMDX];
+  double gam = pr[GAMMA], rgp = pr[CVINF] * (gam - 1.);
+  double gam1 = gam / pr[PRANDT], gam2 = gam * rgp;
+  double best = 1e300;
+  for (int64_t k = 1; k <= pi[IJKV + 2]; k++)
+    for (int64_t j = 1; j <= pi[IJKV + 1]; j++)
+      for (int64_t i = 1; i <= pi[IJKV]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        double surf, vv;
+        if (pi[ITYPZONE] == 2) {
+          double ddi = 2. * sqrt(ti[0] * ti[0]), ddj = 2. * sqrt(tj[0] * tj[0]), ddk = 2. * sqrt(tk[0] * tk[0]);
+          surf = 1. / OMAX(OMAX(ddi, ddj), ddk);
+          vv = vol[0];
+        } else {
+          int64_t lt = indmtr(pi, i, j, k);
+          int64_t ndm = pi[NDIMDX_MTR];
+          double dd[3];
+          const double* t3[3] = {ti, tj, tk};
+          for (int d = 0; d < 3; d++) {
+            int64_t lo = lt, hi = lt + pi[NIJK_MTR + d];
+            const double* t = t3[d];
+            if (pi[ITYPZONE] == 3 && d == 2) { dd[d] = 0.; continue; }
+            double a = sqrt(t[hi] * t[hi] + t[hi + ndm] * t[hi + ndm] + (pi[ITYPZONE] == 3 ? 0. : t[hi + 2 * ndm] * t[hi + 2 * ndm]));
+            double b = sqrt(t[lo] * t[lo] + t[lo + ndm] * t[lo + ndm] + (pi[ITYPZONE] == 3 ? 0. : t[lo + 2 * ndm] * t[lo + 2 * ndm]));
+            dd[d] = a + b;
+          }
+          surf = 1. / OMAX(OMAX(dd[0], dd[1]), dd[2]);
+          vv = vol[lt];
+        }
+        double u = rop[l + nd], v = rop[l + 2 * nd], w = rop[l + 3 * nd], r = rop[l];
+        double c = sqrt(gam2 * rop[l + 4 * nd]);
+        double sp = sqrt(u * u + v * v + w * w);
+        double conv = 2. * vv * surf / (sp + c);
+        double comp = conv;
+        if (pi[IFLOW] >= 2) {
+          double vis = 2. * r * vv * vv * surf * surf * (gam1 / xmut[l]);
+          comp = OMIN(vis, conv);
+        }
+        if (comp < best) best = comp;
+      }
+  return cfl * best;
+}
+
+/* ======================================================================
+ * The solve step -- computePT.cpp:534-680 with gsdr3.cpp:152-173 (choice
+ * of the sub-step arrays), souszones_list.cpp:31-97 (verification flags),
+ * navier_stokes_struct.for:6 (per-zone sub-step), lhs.cpp (residual + LU),
+ * transfert_multiblock.cpp / bcs.cpp (ghost fill), computePT.cpp:675-679
+ * (time-level rotation M1 <- N <- P1).
+ * ====================================================================== */
+int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
+               int nitrun, int nstep_deb, int nstep_fin, int nit_c,
+               int modulo_verif, int* first_it) {
+  if (nzones < 1) return 1;
+  const int64_t* p0 = zones[0].param_int;
+  int64_t nssiter = p0[NSSITER];
+  int implicit = p0[ITYPCP] <= 1;
+  for (int it = 0; it < nit_c; it++) {
+    int64_t nitrun_loc = (int64_t)nitrun * nit_c + it;
+    for (int nstep = nstep_deb; nstep <= nstep_fin; nstep++) {
+      int lssiter_verif = 0, lexit_lu = 0;
+      if (modulo_verif > 0 && nitrun_loc % modulo_verif == 0) {
+        lssiter_verif = 1;
+        if (nstep == nssiter && implicit) lexit_lu = 1;
+      }
+      int skip = (lssiter_verif == 0 && nstep == nssiter && p0[ITYPCP] == 1);
+      if (skip) continue;
+      for (int z = 0; z < nzones; z++) {
+        or_zone* Z = &zones[z];
+        const int64_t* pi = Z->param_int;
+        const double* pr = Z->param_real;
+        int64_t ni = pi[IJKV], nj = pi[IJKV + 1], nk = pi[IJKV + 2];
+        int64_t ng = pi[NIJK + 3], ngk = pi[NIJK + 4];
+        int64_t sdm[6] = {1, ni, 1, nj, 1, nk};
+        int64_t coe_r[6] = {1 - ng, ni + ng, 1 - ng, nj + ng, 1 - ngk, nk + ngk};
+        int64_t grad_r[6] = {0, ni + 1, 0, nj + 1, 1 - (ngk ? 1 : 0), nk + (ngk ? 1 : 0)};
+        double *ssiter, *out;
+        if (nstep == 1) { ssiter = Z->ro; out = Z->ro_p1; }
+        else if (implicit) { ssiter = Z->ro_p1; out = Z->ro_p1; }
+        else if (nstep % 2 == 0) { ssiter = Z->ro_p1; out = Z->ro; }
+        else { ssiter = Z->ro; out = Z->ro_p1; }
+        if (nstep == 1) {
+          if (pi[IFLOW] == 2) or_invist(pi, pr, implicit ? coe_r : grad_r, ssiter, Z->xmut);
+          if (implicit) {
+            or_tstb3_global(pi, pr, coe_r, Z->coe, Z->vol);
+            or_tstb3c(pi, pr, *first_it, coe_r, ssiter, Z->coe, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
+          } else {
+            or_tstb3_global(pi, pr, sdm, Z->coe, Z->vol);
+          }
+        }
+        or_init_rhs(pi, nstep, sdm, Z->drodm);
+        or_flux(pi, pr, sdm, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
+        if (implicit) {
+          or_core3as2(pi, pr, nstep, *first_it, sdm, ssiter, Z->ro, Z->ro_m1, Z->drodm, Z->coe);
+          if (lssiter_verif) or_cprdu3s1(pi, nstep, (int)nssiter, Z->drodm, Z->rdm);
+          if (!lexit_lu) {
+            int nt = g_lu_tiles;
+            if (nt <= 1) {
+              or_invlu(pi, pr, sdm, Z->ro_p1, ssiter, Z->drodm, Z->drodm, Z->ti, Z->tj, Z->tk, Z->coe, 1);
+            } else {
+              /* k-slab tiles; a tile never reads outside its own range */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+              for (int tt = 0; tt < nt; tt++) {
+                int64_t k0 = 1 + (nk * tt) / nt, k1 = (nk * (tt + 1)) / nt;
+                int64_t tl[6] = {1, ni, 1, nj, k0, k1};
+                if (k1 >= k0)
+                  or_invlu(pi, pr, tl, Z->ro_p1, ssiter, Z->drodm, Z->drodm, Z->ti, Z->tj, Z->tk, Z->coe, 1);
+              }
+            }
+          }
+        } else {
+          or_core3ark3(pi, pr, nstep, sdm, out, ssiter, Z->drodm, Z->coe);
+        }
+      }
+      /* ghost fill of the array just written: 1-to-1 transfers, then BCs */
+      int use_p1 = implicit || (nstep % 2 == 1);
+      if (ntr > 0) or_transfers(zones, tr, ntr, use_p1);
+      for (int z = 0; z < nzones; z++) {
+        or_zone* Z = &zones[z];
+        or_bc_zone(Z->param_int, Z->param_real, 0, use_p1 ? Z->ro_p1 : Z->ro);
+      }
+    }
+    *first_it = 1;
+    for (int z = 0; z < nzones; z++) {
+      double* save = zones[z].ro_m1;
+      zones[z].ro_m1 = zones[z].ro;
+      zones[z].ro = zones[z].ro_p1;
+      zones[z].ro_p1 = save;
+    }
+  }
+  return 0;
+}

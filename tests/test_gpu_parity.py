@@ -1,0 +1,146 @@
+"""GPU parity: the sm_103a solve step, called through the C ABI, against the
+CPU oracle on the same seeded inputs.  Bar: 1e-12 relative per cell (the
+FP64 kernels are built without contraction and follow the reference's
+operation order, so in practice the results are bit-identical); residual
+norms, which the GPU reduces with a different summation order, to 1e-12."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from fast_gb300 import cases, fasts
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _pair(t, oracle_mod, modulo_verif):
+    from fast_gb300._native import Solver
+    m = fasts.prepare(t)
+    zd = fasts.zone_data(t, m)
+    ref = oracle_mod.Case(zd)
+    ref.apply_bc(0)
+    ref.apply_bc(1)
+    s = Solver(0)
+    for z in zd:
+        s.add_zone(z["pi"], z["pr"], z["ti"], z["tj"], z["tk"], z["vol"])
+    s.set_option("modulo_verif", modulo_verif)
+    for n, z in enumerate(zd):
+        for lvl, key in enumerate(("ro", "ro_m1", "ro_p1")):
+            s.upload(n, lvl, z[key])
+    s.apply_bc(0)
+    s.apply_bc(1)
+    return zd, ref, s
+
+
+def _check_levels(ref, s, zone=0, tol=TOL):
+    s.synchronize()
+    for lvl in range(3):
+        got = s.download(zone, lvl)
+        exp = ref.z[zone]["lv"][lvl]
+        err = rel_err(got, exp)
+        assert err <= tol, f"level {lvl}: rel err {err:.3e}"
+
+
+def _interior_mask(pi):
+    ni, nj, nk = (int(pi[0]), int(pi[1]), int(pi[2]))
+    m = np.zeros((nk, nj, ni), dtype=bool)
+    m[2:nk - 2, 2:nj - 2, 2:ni - 2] = True
+    return m.reshape(-1)
+
+
+@pytest.mark.parametrize("scheme,slope", [("roe_min", "minmod"), ("roe", "o3"), ("roe", "o1"),
+                                          ("ausmpred", "o3")])
+def test_explicit_rk3_step(oracle_mod, scheme, slope):
+    t = cases.isentropic_vortex(n=(24, 20, 6),
+                                numz={"scheme": scheme, "slope": slope, "time_step": 0.05})
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    # the stage-3 residual as well (interior cells)
+    pi = zd[0]["pi"]
+    nd = int(pi[41])
+    mask = np.tile(_interior_mask(pi), 5)
+    got = s.work(0, "drodm", 5 * nd)
+    exp = ref.z[0]["drodm"]
+    assert rel_err(got[mask], exp[mask]) <= TOL
+    s.close()
+
+
+@pytest.mark.parametrize("scheme,slope,n", [("ausmpred", "o3", (12, 10, 8)),
+                                            ("roe_min", "minmod", (9, 11, 7)),
+                                            ("roe", "o3", (10, 10, 10))])
+def test_implicit_lusgs_step(oracle_mod, scheme, slope, n):
+    t = cases.taylor_green(n=n, ss_iteration=3, scheme=scheme, slope=slope)
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
+    pi = zd[0]["pi"]
+    nd = int(pi[41])
+    mask = _interior_mask(pi)
+    coe = s.work(0, "coe", 5 * nd).reshape(5, nd)
+    assert rel_err(coe[:, mask], ref.z[0]["coe"].reshape(5, nd)[:, mask]) <= TOL
+    xm = s.work(0, "xmut", nd)
+    assert rel_err(xm[mask], ref.z[0]["xmut"][mask]) <= TOL
+    nss = int(pi[58])
+    got = s.residuals(0)
+    exp = ref.residual_norms(0, nss)
+    assert got.shape == exp.shape
+    assert rel_err(got, exp) <= TOL
+    s.close()
+
+
+def test_implicit_skipped_last_subiteration(oracle_mod):
+    """Steps without verification skip the residual-only last sub-iteration
+    (computePT.cpp:581-582)."""
+    t = cases.taylor_green(n=(8, 8, 8), ss_iteration=2)
+    zd, ref, s = _pair(t, oracle_mod, 3)
+    for it in range(1, 5):
+        ref.compute(it, 1, 3, 1, modulo_verif=3)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
+def test_nit_c_loop(oracle_mod):
+    t = cases.isentropic_vortex(n=(16, 16, 4))
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    ref.compute(0, 1, 3, 4, modulo_verif=1000)
+    s.compute(0, 1, 3, 1, 4)
+    _check_levels(ref, s)
+    s.close()
+
+
+def test_fasts_api_roundtrip(oracle_mod):
+    """warmup / _compute / display_temporal_criteria / convergence history
+    through the FastS-style API, against the oracle."""
+    t = cases.taylor_green(n=(10, 8, 6), ss_iteration=2)
+    t2 = cases.taylor_green(n=(10, 8, 6), ss_iteration=2)
+    zd, ref, _ = _pair(t2, oracle_mod, 1)
+    t, tc, metrics = fasts.warmup(t, None)
+    fasts._createConvergenceHistory(t, 5)
+    for it in range(1, 4):
+        fasts._compute(t, metrics, it)
+        ref.compute(it, 1, 3, 1, modulo_verif=1)
+        fasts.display_temporal_criteria(t, metrics, it, format="store")
+    from fast_gb300 import fastc, pytree as I
+    z = I.getZones(t)[0]
+    assert rel_err(fastc.compactArray(z, "").reshape(-1), ref.z[0]["lv"][0]) <= TOL
+    ch = I.getNodeFromName1(z, "ZoneConvergenceHistory")
+    assert int(I.getValue(ch)) == 3
+
+
+def test_errors_are_reported_not_fatal():
+    from fast_gb300._native import FastGB300Error, Solver
+    s = Solver(0)
+    with pytest.raises(FastGB300Error):
+        s.compute(1, 1, 3, 1, 1)          # no zone yet
+    with pytest.raises(FastGB300Error):
+        s.set_option("lu_precision", 16)
+    with pytest.raises(FastGB300Error):
+        s.set_option("no_such_option", 1)
+    s.close()
