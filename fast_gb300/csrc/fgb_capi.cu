@@ -52,6 +52,7 @@ struct ZoneData {
   double *drodm = nullptr, *coe = nullptr, *xmut = nullptr, *rdm = nullptr;
   double *ti = nullptr, *tj = nullptr, *tk = nullptr, *vol = nullptr;
   double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
+  float *st32 = nullptr, *coe32 = nullptr, *d32 = nullptr;  // mixed-precision LU work
   int64_t n_rdm = 0, ijkv_lu[3] = {1, 1, 1};
   std::vector<GatherList> bcs;
   int32_t *co_dst = nullptr, *co_a = nullptr, *co_b = nullptr, *co_c = nullptr;
@@ -70,6 +71,9 @@ struct fgb_solver {
   int first_it = 0;
   int modulo_verif = 200;
   int lu_precision = 64;
+  int lu_mode = 1;                 // 1 persistent cooperative sweeps, 0 one launch per plane
+  unsigned int* bar = nullptr;     // grid-barrier words
+  int* derr = nullptr;             // device error word
   int nit_recorded = 0;
   int64_t launches = 0;
   // optional per-kernel timing with CUDA events on the solver stream
@@ -292,6 +296,9 @@ int fgb_create(int device, fgb_solver** out) {
   fgb_solver* s = new fgb_solver();
   s->device = device;
   cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&s->bar, 4 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&s->derr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(s->derr, 0, sizeof(int));
   if (e != cudaSuccess) { delete s; return fail(FGB_ERR_CUDA, cudaGetErrorString(e)); }
   *out = s;
   return FGB_OK;
@@ -306,10 +313,13 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.scratch); cudaFree(Z.drodm); cudaFree(Z.coe); cudaFree(Z.xmut); cudaFree(Z.rdm);
     cudaFree(Z.ti); cudaFree(Z.tj); cudaFree(Z.tk); cudaFree(Z.vol);
     cudaFree(Z.Fi); cudaFree(Z.Fj); cudaFree(Z.Fk);
+    cudaFree(Z.st32); cudaFree(Z.coe32); cudaFree(Z.d32);
     for (GatherList& g : Z.bcs) { cudaFree(g.dst); cudaFree(g.src); }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
   for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
+  cudaFree(s->bar);
+  cudaFree(s->derr);
   for (auto& e : s->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
   for (auto e : s->pool) cudaEventDestroy(e);
   if (s->t0) cudaEventDestroy(s->t0);
@@ -411,6 +421,9 @@ int fgb_set_option(fgb_solver* s, const char* key, double value) {
   if (k == "lu_precision") {
     if (value != 64. && value != 32.) return fail(FGB_ERR_ARG, "lu_precision must be 64 or 32");
     s->lu_precision = (int)value;
+  } else if (k == "lu_mode") {
+    if (value != 0. && value != 1.) return fail(FGB_ERR_ARG, "lu_mode must be 0 or 1");
+    s->lu_mode = (int)value;
   } else if (k == "modulo_verif") {
     if (value < 1) return fail(FGB_ERR_ARG, "modulo_verif must be >= 1");
     s->modulo_verif = (int)value;
@@ -428,6 +441,7 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value) {
   if (!s || !key || !value) return fail(FGB_ERR_ARG, "null argument");
   std::string k(key);
   if (k == "lu_precision") *value = s->lu_precision;
+  else if (k == "lu_mode") *value = s->lu_mode;
   else if (k == "modulo_verif") *value = s->modulo_verif;
   else if (k == "first_it") *value = s->first_it;
   else if (k == "profile") *value = s->profile;
@@ -520,7 +534,6 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
   if (s->zones.empty()) return fail(FGB_ERR_STATE, "no zone");
   if (layer_mode != 1) return fail(FGB_ERR_ARG, "only layer_mode=1 (the C layer) is supported");
   if (nstep_deb < 1 || nstep_fin < nstep_deb || nit_c < 1) return fail(FGB_ERR_ARG, "bad step range");
-  if (s->lu_precision != 64) return fail(FGB_ERR_ARG, "FP32 LU sweeps are not available");
   CK(cudaSetDevice(s->device));
   const std::vector<int64_t>& p0 = s->zones[0].pi;
   const int64_t nssiter = p0[NSSITER];
@@ -610,11 +623,25 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             la.rop_new = inplace ? Z.scratch : out;
             la.rop_knb = inplace ? Z.scratch : ssiter;
             la.coe = Z.coe; la.din = Z.drodm; la.dout = Z.drodm;
+            LuLaunch L{};
+            L.persistent = s->lu_mode;
+            L.fp32 = s->lu_precision == 32;
+            L.bar = s->bar;
+            L.err = s->derr;
+            if (L.fp32) {
+              if (!Z.st32) {
+                size_t nb = sizeof(float) * 5 * z.nd;
+                CK(cudaMalloc(&Z.st32, nb));
+                CK(cudaMalloc(&Z.coe32, nb));
+                CK(cudaMalloc(&Z.d32, nb));
+              }
+              L.st32 = Z.st32; L.coe32 = Z.coe32; L.d32 = Z.d32;
+            }
             {
               ProfScope ps(s, "lu_sgs");
-              CK(launch_lusgs(z, la, s->st));
+              CK(launch_lusgs(z, la, L, s->st));
             }
-            s->launches += 2 * (z.ni + z.nj + z.nk - 2);
+            s->launches += (L.persistent ? 1 : 2 * (z.ni + z.nj + z.nk - 2)) + (L.fp32 ? 3 : 0);
             if (inplace) std::swap(Z.lvl[2], Z.scratch);
           }
         }
@@ -671,6 +698,12 @@ int fgb_synchronize(fgb_solver* s) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
   CK(cudaSetDevice(s->device));
   CK(cudaStreamSynchronize(s->st));
+  int h = 0;
+  CK(cudaMemcpy(&h, s->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h != 0) {
+    CK(cudaMemset(s->derr, 0, sizeof(int)));
+    return fail(FGB_ERR_DEVICE, "a grid barrier of the LU-SGS kernel timed out");
+  }
   return FGB_OK;
 }
 

@@ -39,8 +39,18 @@ struct LuArgs {
   int64_t s;              // hyperplane index (i-1)+(j-1)+(k-1)
   int64_t jlo, klo, nbj, nbk;  // (j,k) box holding the hyperplane
 };
+// how the sweeps run: persistent cooperative kernel (one launch per solve,
+// bounded grid barrier between hyperplanes) or one launch per hyperplane;
+// FP64 or FP32 (mixed precision, needs the three FP32 work arrays)
+struct LuLaunch {
+  int persistent;
+  int fp32;
+  unsigned int* bar;   // 2 words of barrier state (zeroed by the launcher)
+  int* err;            // device error word (barrier time-out)
+  float* st32; float* coe32; float* d32;
+};
 cudaError_t launch_coefficients(const Zone& z, const CoeArgs& a, cudaStream_t st);
-cudaError_t launch_lusgs(const Zone& z, LuArgs a, cudaStream_t st);
+cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st);
 
 // fgb_ghost.cu: ghost fill and residual norms
 struct NormArgs {

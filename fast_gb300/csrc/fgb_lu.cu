@@ -103,13 +103,11 @@ cudaError_t launch_coefficients(const Zone& z, const CoeArgs& a, cudaStream_t st
 
 // ------------------------------------------------------- neighbour term
 // b = B_d(W_nb) . dW_nb  (LU/lu_{i,j,k}_3dcart.for, lu_{i,j,k}_3dfull.for).
-// signe = +0.5 (lower) / -0.5 (upper); cs = coe_{d+2}(nb) * signe.
+// (u,v,w,t) = neighbour state, cs = coe_{d+2}(nb) * signe with signe = +0.5
+// in the lower sweep and -0.5 in the upper sweep.
 template <int TYP, int D, typename T>
-__device__ __forceinline__ void nb_term(const Zone& z, const T* __restrict__ R, int64_t l1,
-                                        T tcx, T tcy, T tcz, T cs, const T o[5], T b[5],
-                                        T gam1, T gamm1, T gam2, T cp) {
-  const int64_t nd = z.nd;
-  T u = R[l1 + nd], v = R[l1 + 2 * nd], w = R[l1 + 3 * nd], t = R[l1 + 4 * nd];
+__device__ __forceinline__ void nb_term(T u, T v, T w, T t, T tcx, T tcy, T tcz, T cs,
+                                        const T o[5], T b[5], T gam1, T gamm1, T gam2, T cp) {
   T q2 = T(.5) * (u * u + v * v + w * w);
   T h = cp * t + q2;
   T ph2 = gamm1 * q2;
@@ -189,31 +187,46 @@ __device__ __forceinline__ void nb_normal(const Zone& z, int d, int64_t lta, int
   }
 }
 
+// Loads of values that other CTAs of the same launch write (increments, the
+// updated state) bypass L1 (ld.global.cg): L1 is not coherent across SMs.
+template <typename T> __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
+
 template <int D> struct DirT { static constexpr int value = D; };
 
-template <int TYP>
-__global__ void __launch_bounds__(128) lu_lower(Zone z, LuArgs a) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= a.nbj * a.nbk) return;
-  const int64_t jj = a.jlo + t % a.nbj, kk = a.klo + t / a.nbj;
-  const int64_t ii = a.s - jj - kk;
-  if (ii < 0 || ii >= z.ni) return;
+// ---------------------------------------------------------------- cells
+// Precision T: double for the plain FP64 path; float for the mixed path
+// (FP32 sweeps and approximate Jacobians; the Newton update stays FP64).
+template <typename T>
+struct LuCellArgs {
+  const T* st;            // W^p in precision T (B matrices)
+  const T* coe;           // coe in precision T
+  T* dio;                 // increment, in place over the residual
+  const double* rop_old;  // FP64 W^p (Newton update)
+  double* rop_new;        // FP64 W^{p+1}
+  int knb_new;            // upper sweep: k+1 neighbour state from rop_new
+};
+
+template <int TYP, typename T>
+__device__ __forceinline__ void lower_cell(const Zone& z, const LuCellArgs<T>& a, int64_t ii,
+                                           int64_t jj, int64_t kk) {
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
   const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
   const int64_t nd = z.nd;
-  const double gam1 = z.gam, gamm1 = gam1 - 1., cp = z.gam * z.cv, gam2 = gamm1 - 1.;
-  const double xal = a.coe[l] * 0.5;
-  double x[5], o[5], b[5];
+  const T gam1 = T(z.gam), gamm1 = T(z.gam - 1.), cp = T(z.gam * z.cv),
+          gam2 = T((z.gam - 1.) - 1.);
+  const T xal = a.coe[l] * T(0.5);
+  T x[5], o[5], b[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = a.din[l + v * nd];
+  for (int v = 0; v < 5; v++) x[v] = ldcg(a.dio + l + v * nd);
   auto term = [&](auto dc, int64_t l1) {
     constexpr int D = decltype(dc)::value;
-    double tx, ty, tz;
-    nb_normal<TYP, double>(z, D, lt - z.minc[D], lt, tx, ty, tz);
+    T tx, ty, tz;
+    nb_normal<TYP, T>(z, D, lt - z.minc[D], lt, tx, ty, tz);
 #pragma unroll
-    for (int v = 0; v < 5; v++) o[v] = a.dout[l1 + v * nd];
-    double cs = a.coe[l1 + (D + 1) * nd] * 0.5;
-    nb_term<TYP, D, double>(z, a.rop_old, l1, tx, ty, tz, cs, o, b, gam1, gamm1, gam2, cp);
+    for (int v = 0; v < 5; v++) o[v] = ldcg(a.dio + l1 + v * nd);
+    T cs = a.coe[l1 + (D + 1) * nd] * T(0.5);
+    nb_term<TYP, D, T>(a.st[l1 + nd], a.st[l1 + 2 * nd], a.st[l1 + 3 * nd], a.st[l1 + 4 * nd],
+                       tx, ty, tz, cs, o, b, gam1, gamm1, gam2, cp);
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
   };
@@ -225,88 +238,207 @@ __global__ void __launch_bounds__(128) lu_lower(Zone z, LuArgs a) {
     if (jj > 0) term(DirT<1>{}, l - z.inc[1]);
   }
   if (ii > 0) term(DirT<0>{}, l - 1);
-  const double diag = 1. / a.coe[l + 4 * nd];
+  const T diag = T(1.) / a.coe[l + 4 * nd];
 #pragma unroll
-  for (int v = 0; v < 5; v++) a.dout[l + v * nd] = x[v] * diag;
+  for (int v = 0; v < 5; v++) a.dio[l + v * nd] = x[v] * diag;
 }
 
-template <int TYP>
-__global__ void __launch_bounds__(128) lu_upper(Zone z, LuArgs a) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= a.nbj * a.nbk) return;
-  const int64_t jj = a.jlo + t % a.nbj, kk = a.klo + t / a.nbj;
-  const int64_t ii = a.s - jj - kk;
-  if (ii < 0 || ii >= z.ni) return;
+template <int TYP, typename T>
+__device__ __forceinline__ void upper_cell(const Zone& z, const LuCellArgs<T>& a, int64_t ii,
+                                           int64_t jj, int64_t kk) {
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
   const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
   const int64_t nd = z.nd;
-  const double gam1 = z.gam, gamm1 = gam1 - 1., cp = z.gam * z.cv, gam2 = gamm1 - 1.;
-  const double xal = a.coe[l] * (-0.5);
-  const double dg = a.coe[l + 4 * nd];
-  double x[5], o[5], b[5];
+  const T gam1 = T(z.gam), gamm1 = T(z.gam - 1.), cp = T(z.gam * z.cv),
+          gam2 = T((z.gam - 1.) - 1.);
+  const T xal = a.coe[l] * T(-0.5);
+  const T dg = a.coe[l + 4 * nd];
+  T x[5], o[5], b[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = a.dout[l + v * nd] * dg;  // lu_d.for
-  auto term = [&](auto dc, int64_t l1, const double* R) {
+  for (int v = 0; v < 5; v++) x[v] = ldcg(a.dio + l + v * nd) * dg;  // lu_d.for
+  auto term = [&](auto dc, int64_t l1, bool from_new) {
     constexpr int D = decltype(dc)::value;
-    double tx, ty, tz;
-    nb_normal<TYP, double>(z, D, lt + z.minc[D], lt + 2 * z.minc[D], tx, ty, tz);
+    T tx, ty, tz;
+    nb_normal<TYP, T>(z, D, lt + z.minc[D], lt + 2 * z.minc[D], tx, ty, tz);
 #pragma unroll
-    for (int v = 0; v < 5; v++) o[v] = a.dout[l1 + v * nd];
-    double cs = a.coe[l1 + (D + 1) * nd] * (-0.5);
-    nb_term<TYP, D, double>(z, R, l1, tx, ty, tz, cs, o, b, gam1, gamm1, gam2, cp);
+    for (int v = 0; v < 5; v++) o[v] = ldcg(a.dio + l1 + v * nd);
+    T cs = a.coe[l1 + (D + 1) * nd] * T(-0.5);
+    T u, vv, w, t;
+    if (from_new) {
+      u = T(ldcg(a.rop_new + l1 + nd)); vv = T(ldcg(a.rop_new + l1 + 2 * nd));
+      w = T(ldcg(a.rop_new + l1 + 3 * nd)); t = T(ldcg(a.rop_new + l1 + 4 * nd));
+    } else {
+      u = a.st[l1 + nd]; vv = a.st[l1 + 2 * nd]; w = a.st[l1 + 3 * nd]; t = a.st[l1 + 4 * nd];
+    }
+    nb_term<TYP, D, T>(u, vv, w, t, tx, ty, tz, cs, o, b, gam1, gamm1, gam2, cp);
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
   };
-  if (kk < z.nk - 1) term(DirT<2>{}, l + z.inc[2], a.rop_knb);
-  if (jj < z.nj - 1) term(DirT<1>{}, l + z.inc[1], a.rop_old);
-  if (ii < z.ni - 1) term(DirT<0>{}, l + 1, a.rop_old);
-  const double diag = 1. / a.coe[l + 4 * nd];
+  if (kk < z.nk - 1) term(DirT<2>{}, l + z.inc[2], a.knb_new != 0);
+  if (jj < z.nj - 1) term(DirT<1>{}, l + z.inc[1], false);
+  if (ii < z.ni - 1) term(DirT<0>{}, l + 1, false);
+  const T diag = T(1.) / a.coe[l + 4 * nd];
 #pragma unroll
   for (int v = 0; v < 5; v++) x[v] = x[v] * diag;
 #pragma unroll
-  for (int v = 0; v < 5; v++) a.dout[l + v * nd] = x[v];
-  // mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW)
+  for (int v = 0; v < 5; v++) a.dio[l + v * nd] = x[v];
+  // mjr_newton.for (FP64): W^{p+1} = prim(cons(W^p) + dW)
   const double* R = a.rop_old;
   const double cv = z.cv, cvinv = 1. / cv, cvinv2 = 0.5 * cvinv;
   double ro = R[l], u = R[l + nd], v = R[l + 2 * nd], w = R[l + 3 * nd], tt = R[l + 4 * nd];
-  double n1 = ro + x[0];
+  double n1 = ro + double(x[0]);
   double r_1 = 1. / n1;
-  double n2 = (ro * u + x[1]) * r_1;
-  double n3 = (ro * v + x[2]) * r_1;
-  double n4 = (ro * w + x[3]) * r_1;
+  double n2 = (ro * u + double(x[1])) * r_1;
+  double n3 = (ro * v + double(x[2])) * r_1;
+  double n4 = (ro * w + double(x[3])) * r_1;
   double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v + w * w));
-  double n5 = (roe_old + x[4]) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
+  double n5 = (roe_old + double(x[4])) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
   double* O = a.rop_new;
   O[l] = n1; O[l + nd] = n2; O[l + 2 * nd] = n3; O[l + 3 * nd] = n4; O[l + 4 * nd] = n5;
 }
 
-// One full LU-SGS solve (lower, then upper + Newton update) as a sequence of
-// hyperplane launches on stream st.
-cudaError_t launch_lusgs(const Zone& z, LuArgs a, cudaStream_t st) {
+// (j,k) box of hyperplane s: cells (i,j,k) with i+j+k = s, all 0-based
+__device__ __forceinline__ void plane_box(const Zone& z, int64_t s, int64_t& jlo, int64_t& klo,
+                                          int64_t& nbj, int64_t& nbk) {
+  jlo = s - (z.ni - 1) - (z.nk - 1); if (jlo < 0) jlo = 0;
+  int64_t jhi = s < z.nj - 1 ? s : z.nj - 1;
+  klo = s - (z.ni - 1) - (z.nj - 1); if (klo < 0) klo = 0;
+  int64_t khi = s < z.nk - 1 ? s : z.nk - 1;
+  nbj = jhi - jlo + 1; nbk = khi - klo + 1;
+}
+
+// ------------------------------------------------------- grid barrier
+// Cooperative launch guarantees that every CTA is resident.  The wait is
+// bounded: past ~1 s it sets the error word, leaves the barrier and the
+// kernel returns; the host reports FGB_ERR_DEVICE.
+struct GridBar { unsigned int* count; unsigned int* gen; int* err; };
+
+__device__ __forceinline__ bool grid_sync(const GridBar& g, unsigned int nblocks,
+                                          unsigned int& my_gen) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int target = my_gen + 1;
+    __threadfence();
+    unsigned int arrived = atomicAdd(g.count, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(g.count, 0u);
+      __threadfence();
+      atomicExch(g.gen, target);
+    } else {
+      long long spins = 0;
+      while (true) {
+        unsigned int cur;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(g.gen) : "memory");
+        if (cur == target) break;
+        if (*(volatile int*)g.err) break;
+        if (++spins > (1ll << 24)) { atomicExch(g.err, 1); break; }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    my_gen = target;
+  }
+  __syncthreads();
+  return *(volatile int*)g.err == 0;
+}
+
+template <int TYP, typename T>
+__global__ void __launch_bounds__(256) lusgs_persistent(Zone z, LuCellArgs<T> a, GridBar g) {
+  const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned int my_gen = 0;
+  for (int64_t s = 0; s <= smax; s++) {   // lower sweep, ascending hyperplanes
+    int64_t jlo, klo, nbj, nbk;
+    plane_box(z, s, jlo, klo, nbj, nbk);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nbj * nbk; t += stride) {
+      const int64_t jj = jlo + t % nbj, kk = klo + t / nbj, ii = s - jj - kk;
+      if (ii >= 0 && ii < z.ni) lower_cell<TYP, T>(z, a, ii, jj, kk);
+    }
+    if (!grid_sync(g, gridDim.x, my_gen)) return;
+  }
+  for (int64_t s = smax; s >= 0; s--) {   // upper sweep + Newton update
+    int64_t jlo, klo, nbj, nbk;
+    plane_box(z, s, jlo, klo, nbj, nbk);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nbj * nbk; t += stride) {
+      const int64_t jj = jlo + t % nbj, kk = klo + t / nbj, ii = s - jj - kk;
+      if (ii >= 0 && ii < z.ni) upper_cell<TYP, T>(z, a, ii, jj, kk);
+    }
+    if (s > 0 && !grid_sync(g, gridDim.x, my_gen)) return;
+  }
+}
+
+// one launch per hyperplane (no inter-CTA waits); kept as a cross-check of
+// the persistent kernel and for streams where cooperative launch is absent
+template <int TYP, typename T, bool UPPER>
+__global__ void __launch_bounds__(128) lusgs_plane(Zone z, LuCellArgs<T> a, int64_t s) {
+  int64_t jlo, klo, nbj, nbk;
+  plane_box(z, s, jlo, klo, nbj, nbk);
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nbj * nbk) return;
+  const int64_t jj = jlo + t % nbj, kk = klo + t / nbj, ii = s - jj - kk;
+  if (ii < 0 || ii >= z.ni) return;
+  if (UPPER) upper_cell<TYP, T>(z, a, ii, jj, kk);
+  else lower_cell<TYP, T>(z, a, ii, jj, kk);
+}
+
+// FP32 copies of the state, the coefficients and the residual for the
+// mixed-precision sweeps (one pass per sub-iteration)
+__global__ void __launch_bounds__(256) to_float(int64_t n, const double* __restrict__ a,
+                                                float* __restrict__ b) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) b[t] = (float)a[t];
+}
+
+template <int TYP, typename T>
+static cudaError_t launch_t(const Zone& z, const LuCellArgs<T>& a, const LuLaunch& L,
+                            cudaStream_t st) {
+  if (L.persistent) {
+    static int grid_cache[2][2] = {{0, 0}, {0, 0}};
+    int& grid = grid_cache[TYP == Z3DCART][sizeof(T) == 4];
+    if (grid == 0) {
+      int dev = 0, nsm = 0, per = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T>, 256, 0);
+      grid = nsm * (per > 0 ? per : 1);
+    }
+    cudaError_t e = cudaMemsetAsync(L.bar, 0, 2 * sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+    GridBar g{L.bar, L.bar + 1, L.err};
+    void* args[] = {(void*)&z, (void*)&a, (void*)&g};
+    return cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(256),
+                                       args, 0, st);
+  }
   const int B = 128;
   const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
-  auto box = [&](int64_t s) {
-    int64_t jlo = s - (z.ni - 1) - (z.nk - 1); if (jlo < 0) jlo = 0;
-    int64_t jhi = s < z.nj - 1 ? s : z.nj - 1;
-    int64_t klo = s - (z.ni - 1) - (z.nj - 1); if (klo < 0) klo = 0;
-    int64_t khi = s < z.nk - 1 ? s : z.nk - 1;
-    a.s = s; a.jlo = jlo; a.klo = klo; a.nbj = jhi - jlo + 1; a.nbk = khi - klo + 1;
-  };
   for (int64_t s = 0; s <= smax; s++) {
-    box(s);
-    unsigned g = (unsigned)((a.nbj * a.nbk + B - 1) / B);
-    if (z.typ == Z3DCART) lu_lower<Z3DCART><<<g, B, 0, st>>>(z, a);
-    else lu_lower<Z3DFULL><<<g, B, 0, st>>>(z, a);
+    int64_t n = (int64_t)z.nj * z.nk;
+    lusgs_plane<TYP, T, false><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a, s);
   }
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
   for (int64_t s = smax; s >= 0; s--) {
-    box(s);
-    unsigned g = (unsigned)((a.nbj * a.nbk + B - 1) / B);
-    if (z.typ == Z3DCART) lu_upper<Z3DCART><<<g, B, 0, st>>>(z, a);
-    else lu_upper<Z3DFULL><<<g, B, 0, st>>>(z, a);
+    int64_t n = (int64_t)z.nj * z.nk;
+    lusgs_plane<TYP, T, true><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a, s);
   }
   return cudaGetLastError();
+}
+
+// One LU-SGS solve (lower, upper + Newton update) of one zone.
+cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st) {
+  if (L.fp32) {
+    const int64_t n = 5 * z.nd;
+    const unsigned g = (unsigned)((n + 255) / 256);
+    to_float<<<g, 256, 0, st>>>(n, a.rop_old, L.st32);
+    to_float<<<g, 256, 0, st>>>(n, a.coe, L.coe32);
+    to_float<<<g, 256, 0, st>>>(n, a.din, L.d32);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    LuCellArgs<float> c{L.st32, L.coe32, L.d32, a.rop_old, a.rop_new, a.rop_knb == a.rop_new};
+    return z.typ == Z3DCART ? launch_t<Z3DCART, float>(z, c, L, st)
+                            : launch_t<Z3DFULL, float>(z, c, L, st);
+  }
+  LuCellArgs<double> c{a.rop_old, a.coe, a.dout, a.rop_old, a.rop_new, a.rop_knb == a.rop_new};
+  return z.typ == Z3DCART ? launch_t<Z3DCART, double>(z, c, L, st)
+                          : launch_t<Z3DFULL, double>(z, c, L, st);
 }
 
 }  // namespace fgb
