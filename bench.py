@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--cpu-n", type=int, default=96, help="CPU sample size (cells per side)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
+                   help="64: plain FP64 path; 32: FP32 LU-SGS sweeps (mixed precision)")
     return p.parse_args()
 
 
@@ -209,9 +211,13 @@ def run_ours(args, d: Dist):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
 
-    t = cases.taylor_green(n=n, ss_iteration=ss)
+    # FastS defaults: residual check every 200 steps (modulo_verif)
+    t = cases.taylor_green(n=n, ss_iteration=ss,
+                           numb={"temporal_scheme": "implicit", "ss_iteration": ss,
+                                 "modulo_verif": 200})
     t, tc, metrics = fasts.warmup(t, None, device=dev, gpu_resident=True)
     s = fasts.HOOK["solver"]
+    s.set_option("lu_precision", args.lu_precision)
     it = 1
     for _ in range(args.warmup):
         fasts._compute(t, metrics, it)
@@ -295,8 +301,10 @@ def run_ours(args, d: Dist):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.lu_precision == 64 else "f64+f32-sweeps",
+            "data": "synthetic",
             "config": {"workload": f"taylor_green_{n}^3_ausmpred_o3_implicit_lusgs_ss{ss}",
+                       "lu_precision": args.lu_precision,
                        "cells": cells, "global_batch": d.world, "sub_iterations": ss,
                        "parallelism": f"replicas x{d.world}",
                        "l2": "state (>=700 MB) larger than L2; no flush"},
