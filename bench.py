@@ -50,6 +50,10 @@ def parse():
     p.add_argument("--cpu-n", type=int, default=96, help="CPU sample size (cells per side)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--ttc", action="store_true",
+                   help="time to a 1e-10 Newton residual drop, FP64 vs mixed sweeps")
+    p.add_argument("--ttc-n", type=int, default=256)
+    p.add_argument("--ttc-max", type=int, default=80, help="max sub-iterations per step")
     p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
                    help="64: plain FP64 path; 32: FP32 LU-SGS sweeps (mixed precision)")
     return p.parse_args()
@@ -315,8 +319,63 @@ def run_ours(args, d: Dist):
         print(json.dumps(line), flush=True)
 
 
+def run_ttc(args):
+    """Time to a 1e-10 drop of the Newton residual within one physical step.
+
+    One BDF2 step (after one BDF1 step) of the 256^3 Taylor-Green case with
+    up to --ttc-max LU-SGS sub-iterations, residual norms (FP64, computed by
+    the GPU as cprdu3s1 does) recorded at every sub-iteration.  The drop is
+    the max over the 5 equations of L2(k)/L2(1); time = sub-iterations to
+    reach 1e-10 x measured time per sub-iteration.  FP64 sweeps vs FP32
+    sweeps (the residual, the update and the norms stay FP64)."""
+    from fast_gb300 import cases, fasts
+    import numpy as np
+    out = {}
+    for prec in (64, 32):
+        t = cases.taylor_green(n=args.ttc_n, ss_iteration=args.ttc_max,
+                               numb={"temporal_scheme": "implicit",
+                                     "ss_iteration": args.ttc_max, "modulo_verif": 1})
+        t, tc, metrics = fasts.warmup(t, None, gpu_resident=True)
+        s = fasts.HOOK["solver"]
+        s.set_option("lu_precision", prec)
+        fasts._compute(t, metrics, 1)          # BDF1 step
+        s.synchronize()
+        s.timer_start()
+        fasts._compute(t, metrics, 2)          # BDF2 step, timed
+        ms = s.timer_stop()
+        r = s.residuals(0)                     # (2*neq, nit)
+        l2 = r[:5]
+        drop = np.max(l2 / l2[:, :1], axis=0)
+        nit = l2.shape[1]
+        ms_it = ms / nit
+        hit = np.nonzero(drop <= 1e-10)[0]
+        k = int(hit[0]) + 1 if hit.size else None
+        fasts._syncHost(t)
+        out[prec] = {"sub_iterations_to_1e-10": k, "ms_per_sub_iteration": ms_it,
+                     "time_to_1e-10_ms": (k * ms_it) if k else None,
+                     "best_drop": float(drop.min()), "drop_history": [float(x) for x in drop],
+                     "final_state_checksum": None}
+        from fast_gb300 import fastc, pytree as I
+        z = I.getZones(t)[0]
+        out[prec]["_state"] = fastc.compactArray(z, "").copy()
+        s.close()
+        fasts.HOOK = None
+    a, b = out[64].pop("_state"), out[32].pop("_state")
+    diff = float(np.max(np.abs(a - b) / (np.abs(a) + 1e-300)))
+    t64, t32 = out[64]["time_to_1e-10_ms"], out[32]["time_to_1e-10_ms"]
+    line = {"metric": "time to 1e-10 residual drop (one BDF2 step)", "unit": "ms",
+            "higher_is_better": False, "config": {"workload": f"taylor_green_{args.ttc_n}^3_ausmpred_o3_bdf2"},
+            "fp64": out[64], "mixed": out[32],
+            "speedup_mixed_vs_fp64": (t64 / t32) if (t64 and t32) else None,
+            "final_state_max_rel_diff_mixed_vs_fp64": diff}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.ttc:
+        run_ttc(args)
+        return
     d = Dist()
     try:
         if args.impl == "reference":

@@ -140,7 +140,7 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
     for f in ("imin", "imax", "jmin", "jmax", "kmin", "kmax"):
         add_bc(z, "per_" + f, "BCautoperiod", f)
     if dt is None:
-        dt = 0.1 * h[0] / (U0 + 1.0) * 5.0   # acoustic CFL ~ 5 (implicit)
+        dt = 2.0 * h[0] / (U0 + 1.0)   # acoustic CFL 2 (implicit dual time)
     numb = numb or {"temporal_scheme": "implicit", "ss_iteration": ss_iteration,
                     "modulo_verif": 1}
     numz = numz or {"scheme": scheme, "slope": slope, "time_step": dt,

@@ -52,7 +52,11 @@ struct ZoneData {
   double *drodm = nullptr, *coe = nullptr, *xmut = nullptr, *rdm = nullptr;
   double *ti = nullptr, *tj = nullptr, *tk = nullptr, *vol = nullptr;
   double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
-  float *st32 = nullptr, *coe32 = nullptr, *d32 = nullptr;  // mixed-precision LU work
+  float *st32 = nullptr, *coe32 = nullptr, *d32 = nullptr, *stn32 = nullptr;  // mixed LU work
+  void* bt = nullptr;               // LU B-coefficient table
+  uint32_t* cells = nullptr;        // interior cells by hyperplane
+  int64_t* plane = nullptr;         // plane offsets (device)
+  std::vector<int64_t> plane_host;  // plane offsets (host)
   int64_t n_rdm = 0, ijkv_lu[3] = {1, 1, 1};
   std::vector<GatherList> bcs;
   int32_t *co_dst = nullptr, *co_a = nullptr, *co_b = nullptr, *co_c = nullptr;
@@ -313,7 +317,8 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.scratch); cudaFree(Z.drodm); cudaFree(Z.coe); cudaFree(Z.xmut); cudaFree(Z.rdm);
     cudaFree(Z.ti); cudaFree(Z.tj); cudaFree(Z.tk); cudaFree(Z.vol);
     cudaFree(Z.Fi); cudaFree(Z.Fj); cudaFree(Z.Fk);
-    cudaFree(Z.st32); cudaFree(Z.coe32); cudaFree(Z.d32);
+    cudaFree(Z.st32); cudaFree(Z.coe32); cudaFree(Z.d32); cudaFree(Z.stn32);
+    cudaFree(Z.bt); cudaFree(Z.cells); cudaFree(Z.plane);
     for (GatherList& g : Z.bcs) { cudaFree(g.dst); cudaFree(g.src); }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
@@ -387,6 +392,28 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   CK(cudaMemset(Z.rdm, 0, sizeof(double) * Z.n_rdm));
   int rc = build_ghost_lists(Z);
   if (rc != FGB_OK) return rc;
+  if (p[ITYPCP] <= 1) {
+    // LU-SGS: cells ordered by hyperplane i+j+k (counting sort), B table
+    if (ni >= 2048 || nj >= 2048 || nk >= 1024)
+      return fail(FGB_ERR_ARG, "zone too large for the LU plane table (ni,nj < 2048, nk < 1024)");
+    const int64_t np = ni + nj + nk - 2;
+    std::vector<int64_t> off(np + 1, 0);
+    for (int64_t k = 0; k < nk; k++)
+      for (int64_t j = 0; j < nj; j++)
+        for (int64_t i = 0; i < ni; i++) off[i + j + k + 1]++;
+    for (int64_t q = 0; q < np; q++) off[q + 1] += off[q];
+    std::vector<uint32_t> cells(ni * nj * nk);
+    std::vector<int64_t> pos(off.begin(), off.end() - 1);
+    for (int64_t k = 0; k < nk; k++)
+      for (int64_t j = 0; j < nj; j++)
+        for (int64_t i = 0; i < ni; i++)
+          cells[pos[i + j + k]++] = (uint32_t)(i | (j << 11) | (k << 22));
+    CK(dev_upload(&Z.cells, cells));
+    CK(dev_upload(&Z.plane, off));
+    Z.plane_host = off;
+    const int64_t nb = Z.z.typ == Z3DCART ? 14 : 25;
+    CK(cudaMalloc(&Z.bt, sizeof(double) * 3 * nb * nd));
+  }
   s->zones.push_back(Z);
   if (zone_id) *zone_id = (int)s->zones.size() - 1;
   return FGB_OK;
@@ -634,14 +661,17 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
                 CK(cudaMalloc(&Z.st32, nb));
                 CK(cudaMalloc(&Z.coe32, nb));
                 CK(cudaMalloc(&Z.d32, nb));
+                CK(cudaMalloc(&Z.stn32, nb));
               }
-              L.st32 = Z.st32; L.coe32 = Z.coe32; L.d32 = Z.d32;
+              L.st32 = Z.st32; L.coe32 = Z.coe32; L.d32 = Z.d32; L.stn32 = Z.stn32;
             }
+            L.bt = Z.bt; L.cells = Z.cells; L.plane = Z.plane; L.plane_host = Z.plane_host.data();
             {
               ProfScope ps(s, "lu_sgs");
               CK(launch_lusgs(z, la, L, s->st));
             }
-            s->launches += (L.persistent ? 1 : 2 * (z.ni + z.nj + z.nk - 2)) + (L.fp32 ? 3 : 0);
+            s->launches += 1 + (L.persistent ? 1 : 2 * (z.ni + z.nj + z.nk - 2)) + (L.fp32 ? 3 : 0) +
+                           ((!inplace || L.fp32) ? 1 : 0);
             if (inplace) std::swap(Z.lvl[2], Z.scratch);
           }
         }

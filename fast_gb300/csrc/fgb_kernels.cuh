@@ -47,7 +47,11 @@ struct LuLaunch {
   int fp32;
   unsigned int* bar;   // 2 words of barrier state (zeroed by the launcher)
   int* err;            // device error word (barrier time-out)
-  float* st32; float* coe32; float* d32;
+  float* st32; float* coe32; float* d32; float* stn32;
+  void* bt;                 // B-coefficient table (3 * entries * NDIMDX of the sweep precision)
+  const uint32_t* cells;    // interior cells ordered by hyperplane (packed i | j<<11 | k<<22)
+  const int64_t* plane;     // device offsets of each hyperplane in `cells`
+  const int64_t* plane_host;  // the same offsets on the host
 };
 cudaError_t launch_coefficients(const Zone& z, const CoeArgs& a, cudaStream_t st);
 cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st);

@@ -191,6 +191,98 @@ __device__ __forceinline__ void nb_normal(const Zone& z, int d, int64_t lta, int
 // updated state) bypass L1 (ld.global.cg): L1 is not coherent across SMs.
 template <typename T> __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 
+
+// ------------------------------------------------------ B-coefficient table
+// The neighbour terms of a sweep are B_d(W_nb) . dW_nb.  B_d(W_nb) depends on
+// the neighbour's state and metric only, which are known before the sweep,
+// so a fully parallel pre-pass evaluates every entry (the same expressions
+// in the same order as lu_{i,j,k}_*.for) and the sweep keeps only the
+// matrix-vector product on its critical path.  Entries that carry the
+// spectral radius (b11, b22, b33, b44, b55) are stored without it; the sweep
+// adds coe_{d+2}(nb)*signe exactly as the reference expression does.
+constexpr int NB_CART = 14;   // entries per direction, 3d cartesian zone
+constexpr int NB_FULL = 25;   // entries per direction, 3d general zone
+template <int TYP> struct NBE { static constexpr int n = TYP == Z3DCART ? NB_CART : NB_FULL; };
+
+template <int TYP, typename T>
+__device__ __forceinline__ void bentries(const Zone& z, int d, T u, T v, T w, T t, T tcx, T tcy,
+                                         T tcz, T* e) {
+  const T gam1 = T(z.gam), gamm1 = T(z.gam - 1.), cp = T(z.gam * z.cv),
+          gam2 = T((z.gam - 1.) - 1.);
+  T q2 = T(.5) * (u * u + v * v + w * w);
+  T h = cp * t + q2;
+  T ph2 = gamm1 * q2;
+  if (TYP == Z3DCART) {
+    if (d == 0) {
+      T qn = tcx * u;
+      e[0] = (tcx * ph2 - u * qn); e[1] = (qn - tcx * gam2 * u); e[2] = (-tcx * gamm1 * v);
+      e[3] = (-tcx * gamm1 * w); e[4] = (-v * qn); e[5] = (tcx * v); e[6] = qn;
+      e[7] = (-w * qn); e[8] = (tcx * w); e[9] = qn * (ph2 - h);
+      e[10] = (tcx * h - gamm1 * u * qn); e[11] = (-gamm1 * v * qn);
+      e[12] = (-gamm1 * w * qn); e[13] = (gam1 * qn);
+    } else if (d == 1) {
+      T qn = tcy * v;
+      e[0] = (-u * qn); e[1] = qn; e[2] = tcy * u; e[3] = (tcy * ph2 - v * qn);
+      e[4] = (-tcy * gamm1 * u); e[5] = (qn - tcy * gam2 * v); e[6] = (-tcy * gamm1 * w);
+      e[7] = (-w * qn); e[8] = (tcy * w); e[9] = qn * (ph2 - h); e[10] = (-gamm1 * u * qn);
+      e[11] = (tcy * h - gamm1 * v * qn); e[12] = (-gamm1 * w * qn); e[13] = (gam1 * qn);
+    } else {
+      T qn = tcz * w;
+      e[0] = -u * qn; e[1] = qn; e[2] = tcz * u; e[3] = -v * qn; e[4] = tcz * v;
+      e[5] = tcz * ph2 - w * qn; e[6] = -tcz * gamm1 * u; e[7] = -tcz * gamm1 * v;
+      e[8] = (qn - tcz * gam2 * w); e[9] = qn * (ph2 - h); e[10] = -gamm1 * u * qn;
+      e[11] = -gamm1 * v * qn; e[12] = tcz * h - gamm1 * w * qn; e[13] = gam1 * qn;
+    }
+  } else {
+    T qn = tcx * u + tcy * v + tcz * w;
+    e[0] = tcx; e[1] = tcy; e[2] = tcz;
+    e[3] = (tcx * ph2 - u * qn); e[4] = (qn - tcx * gam2 * u);
+    e[5] = (tcy * u - tcx * gamm1 * v); e[6] = (tcz * u - tcx * gamm1 * w); e[7] = tcx * gamm1;
+    e[8] = (tcy * ph2 - v * qn); e[9] = (tcx * v - tcy * gamm1 * u);
+    e[10] = (qn - tcy * gam2 * v); e[11] = (tcz * v - tcy * gamm1 * w); e[12] = tcy * gamm1;
+    e[13] = (tcz * ph2 - w * qn); e[14] = (tcx * w - tcz * gamm1 * u);
+    e[15] = (tcy * w - tcz * gamm1 * v); e[16] = (qn - tcz * gam2 * w); e[17] = tcz * gamm1;
+    e[18] = qn * (ph2 - h); e[19] = (tcx * h - gamm1 * u * qn);
+    e[20] = (tcy * h - gamm1 * v * qn); e[21] = (tcz * h - gamm1 * w * qn); e[22] = (gam1 * qn);
+  }
+}
+
+// b = B . o from the stored entries (cs = coe_{d+2}(nb) * signe)
+template <int TYP, int D, typename T>
+__device__ __forceinline__ void bmatvec(const Zone& z, const T* e, T cs, const T o[5], T b[5]) {
+  const T gamm1 = T(z.gam - 1.);
+  if (TYP == Z3DCART) {
+    if (D == 0) {
+      const T tcx = T(z.tcx), b25 = tcx * gamm1;
+      b[0] = cs * o[0] + tcx * o[1];
+      b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[2] + e[3] * o[3] + b25 * o[4];
+      b[2] = e[4] * o[0] + e[5] * o[1] + ((e[6]) + cs) * o[2];
+      b[3] = e[7] * o[0] + e[8] * o[1] + ((e[6]) + cs) * o[3];
+      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
+    } else if (D == 1) {
+      const T tcy = T(z.tcy), b35 = tcy * gamm1;
+      b[0] = cs * o[0] + tcy * o[2];
+      b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[2];
+      b[2] = e[3] * o[0] + e[4] * o[1] + (e[5] + cs) * o[2] + e[6] * o[3] + b35 * o[4];
+      b[3] = e[7] * o[0] + e[8] * o[2] + ((e[1]) + cs) * o[3];
+      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
+    } else {
+      const T tcz = T(z.tcz), b45 = tcz * gamm1;
+      b[0] = cs * o[0] + tcz * o[3];
+      b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[3];
+      b[2] = e[3] * o[0] + (e[1] + cs) * o[2] + e[4] * o[3];
+      b[3] = e[5] * o[0] + e[6] * o[1] + e[7] * o[2] + (e[8] + cs) * o[3] + b45 * o[4];
+      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
+    }
+  } else {
+    b[0] = cs * o[0] + e[0] * o[1] + e[1] * o[2] + e[2] * o[3];
+    b[1] = e[3] * o[0] + (e[4] + cs) * o[1] + e[5] * o[2] + e[6] * o[3] + e[7] * o[4];
+    b[2] = e[8] * o[0] + e[9] * o[1] + (e[10] + cs) * o[2] + e[11] * o[3] + e[12] * o[4];
+    b[3] = e[13] * o[0] + e[14] * o[1] + e[15] * o[2] + (e[16] + cs) * o[3] + e[17] * o[4];
+    b[4] = e[18] * o[0] + e[19] * o[1] + e[20] * o[2] + e[21] * o[3] + (e[22] + cs) * o[4];
+  }
+}
+
 template <int D> struct DirT { static constexpr int value = D; };
 
 // ---------------------------------------------------------------- cells
@@ -198,35 +290,40 @@ template <int D> struct DirT { static constexpr int value = D; };
 // (FP32 sweeps and approximate Jacobians; the Newton update stays FP64).
 template <typename T>
 struct LuCellArgs {
-  const T* st;            // W^p in precision T (B matrices)
+  const T* st;            // W^p in precision T
   const T* coe;           // coe in precision T
   T* dio;                 // increment, in place over the residual
+  const T* bt;            // B entries: bt[(d*NB + m)*nd + l]
   const double* rop_old;  // FP64 W^p (Newton update)
   double* rop_new;        // FP64 W^{p+1}
-  int knb_new;            // upper sweep: k+1 neighbour state from rop_new
+  T* stn;                 // mixed path, in place: W^{p+1} in precision T (k+1 neighbours)
+  int inplace;            // upper sweep: k+1 neighbour taken after its update
+  const uint32_t* cells;  // cells ordered by hyperplane, packed i | j<<11 | k<<22
+  const int64_t* plane;   // plane s holds cells[plane[s] .. plane[s+1])
 };
+
+__device__ __forceinline__ void unpack(uint32_t c, int64_t& ii, int64_t& jj, int64_t& kk) {
+  ii = c & 2047u; jj = (c >> 11) & 2047u; kk = c >> 22;
+}
 
 template <int TYP, typename T>
 __device__ __forceinline__ void lower_cell(const Zone& z, const LuCellArgs<T>& a, int64_t ii,
                                            int64_t jj, int64_t kk) {
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
-  const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
   const int64_t nd = z.nd;
-  const T gam1 = T(z.gam), gamm1 = T(z.gam - 1.), cp = T(z.gam * z.cv),
-          gam2 = T((z.gam - 1.) - 1.);
+  constexpr int NB = NBE<TYP>::n;
   const T xal = a.coe[l] * T(0.5);
-  T x[5], o[5], b[5];
+  T x[5], o[5], b[5], e[NB];
 #pragma unroll
   for (int v = 0; v < 5; v++) x[v] = ldcg(a.dio + l + v * nd);
   auto term = [&](auto dc, int64_t l1) {
     constexpr int D = decltype(dc)::value;
-    T tx, ty, tz;
-    nb_normal<TYP, T>(z, D, lt - z.minc[D], lt, tx, ty, tz);
 #pragma unroll
     for (int v = 0; v < 5; v++) o[v] = ldcg(a.dio + l1 + v * nd);
+#pragma unroll
+    for (int m = 0; m < NB; m++) e[m] = a.bt[(D * NB + m) * nd + l1];
     T cs = a.coe[l1 + (D + 1) * nd] * T(0.5);
-    nb_term<TYP, D, T>(a.st[l1 + nd], a.st[l1 + 2 * nd], a.st[l1 + 3 * nd], a.st[l1 + 4 * nd],
-                       tx, ty, tz, cs, o, b, gam1, gamm1, gam2, cp);
+    bmatvec<TYP, D, T>(z, e, cs, o, b);
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
   };
@@ -243,38 +340,60 @@ __device__ __forceinline__ void lower_cell(const Zone& z, const LuCellArgs<T>& a
   for (int v = 0; v < 5; v++) a.dio[l + v * nd] = x[v] * diag;
 }
 
+// mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW), FP64
+__device__ __forceinline__ void newton64(const Zone& z, const double* R, double* O, int64_t l,
+                                         double d0, double d1, double d2, double d3, double d4) {
+  const int64_t nd = z.nd;
+  const double cv = z.cv, cvinv = 1. / cv, cvinv2 = 0.5 * cvinv;
+  double ro = R[l], u = R[l + nd], v = R[l + 2 * nd], w = R[l + 3 * nd], tt = R[l + 4 * nd];
+  double n1 = ro + d0;
+  double r_1 = 1. / n1;
+  double n2 = (ro * u + d1) * r_1;
+  double n3 = (ro * v + d2) * r_1;
+  double n4 = (ro * w + d3) * r_1;
+  double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v + w * w));
+  double n5 = (roe_old + d4) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
+  O[l] = n1; O[l + nd] = n2; O[l + 2 * nd] = n3; O[l + 3 * nd] = n4; O[l + 4 * nd] = n5;
+}
+
 template <int TYP, typename T>
 __device__ __forceinline__ void upper_cell(const Zone& z, const LuCellArgs<T>& a, int64_t ii,
                                            int64_t jj, int64_t kk) {
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
   const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
   const int64_t nd = z.nd;
-  const T gam1 = T(z.gam), gamm1 = T(z.gam - 1.), cp = T(z.gam * z.cv),
-          gam2 = T((z.gam - 1.) - 1.);
+  constexpr int NB = NBE<TYP>::n;
   const T xal = a.coe[l] * T(-0.5);
   const T dg = a.coe[l + 4 * nd];
-  T x[5], o[5], b[5];
+  T x[5], o[5], b[5], e[NB];
 #pragma unroll
   for (int v = 0; v < 5; v++) x[v] = ldcg(a.dio + l + v * nd) * dg;  // lu_d.for
-  auto term = [&](auto dc, int64_t l1, bool from_new) {
+  auto term = [&](auto dc, int64_t l1, bool fresh) {
     constexpr int D = decltype(dc)::value;
-    T tx, ty, tz;
-    nb_normal<TYP, T>(z, D, lt + z.minc[D], lt + 2 * z.minc[D], tx, ty, tz);
 #pragma unroll
     for (int v = 0; v < 5; v++) o[v] = ldcg(a.dio + l1 + v * nd);
     T cs = a.coe[l1 + (D + 1) * nd] * T(-0.5);
-    T u, vv, w, t;
-    if (from_new) {
-      u = T(ldcg(a.rop_new + l1 + nd)); vv = T(ldcg(a.rop_new + l1 + 2 * nd));
-      w = T(ldcg(a.rop_new + l1 + 3 * nd)); t = T(ldcg(a.rop_new + l1 + 4 * nd));
+    if (fresh) {  // neighbour already updated: B from its new state
+      T u, vv, w, t;
+      if (sizeof(T) == 8) {
+        u = T(ldcg(a.rop_new + l1 + nd)); vv = T(ldcg(a.rop_new + l1 + 2 * nd));
+        w = T(ldcg(a.rop_new + l1 + 3 * nd)); t = T(ldcg(a.rop_new + l1 + 4 * nd));
+      } else {
+        u = ldcg(a.stn + l1 + nd); vv = ldcg(a.stn + l1 + 2 * nd);
+        w = ldcg(a.stn + l1 + 3 * nd); t = ldcg(a.stn + l1 + 4 * nd);
+      }
+      T tx, ty, tz;
+      nb_normal<TYP, T>(z, D, lt + z.minc[D], lt + 2 * z.minc[D], tx, ty, tz);
+      bentries<TYP, T>(z, D, u, vv, w, t, tx, ty, tz, e);
     } else {
-      u = a.st[l1 + nd]; vv = a.st[l1 + 2 * nd]; w = a.st[l1 + 3 * nd]; t = a.st[l1 + 4 * nd];
+#pragma unroll
+      for (int m = 0; m < NB; m++) e[m] = a.bt[(D * NB + m) * nd + l1];
     }
-    nb_term<TYP, D, T>(u, vv, w, t, tx, ty, tz, cs, o, b, gam1, gamm1, gam2, cp);
+    bmatvec<TYP, D, T>(z, e, cs, o, b);
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
   };
-  if (kk < z.nk - 1) term(DirT<2>{}, l + z.inc[2], a.knb_new != 0);
+  if (kk < z.nk - 1) term(DirT<2>{}, l + z.inc[2], a.inplace != 0);
   if (jj < z.nj - 1) term(DirT<1>{}, l + z.inc[1], false);
   if (ii < z.ni - 1) term(DirT<0>{}, l + 1, false);
   const T diag = T(1.) / a.coe[l + 4 * nd];
@@ -282,29 +401,23 @@ __device__ __forceinline__ void upper_cell(const Zone& z, const LuCellArgs<T>& a
   for (int v = 0; v < 5; v++) x[v] = x[v] * diag;
 #pragma unroll
   for (int v = 0; v < 5; v++) a.dio[l + v * nd] = x[v];
-  // mjr_newton.for (FP64): W^{p+1} = prim(cons(W^p) + dW)
-  const double* R = a.rop_old;
-  const double cv = z.cv, cvinv = 1. / cv, cvinv2 = 0.5 * cvinv;
-  double ro = R[l], u = R[l + nd], v = R[l + 2 * nd], w = R[l + 3 * nd], tt = R[l + 4 * nd];
-  double n1 = ro + double(x[0]);
-  double r_1 = 1. / n1;
-  double n2 = (ro * u + double(x[1])) * r_1;
-  double n3 = (ro * v + double(x[2])) * r_1;
-  double n4 = (ro * w + double(x[3])) * r_1;
-  double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v + w * w));
-  double n5 = (roe_old + double(x[4])) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
-  double* O = a.rop_new;
-  O[l] = n1; O[l + nd] = n2; O[l + 2 * nd] = n3; O[l + 3 * nd] = n4; O[l + 4 * nd] = n5;
-}
-
-// (j,k) box of hyperplane s: cells (i,j,k) with i+j+k = s, all 0-based
-__device__ __forceinline__ void plane_box(const Zone& z, int64_t s, int64_t& jlo, int64_t& klo,
-                                          int64_t& nbj, int64_t& nbk) {
-  jlo = s - (z.ni - 1) - (z.nk - 1); if (jlo < 0) jlo = 0;
-  int64_t jhi = s < z.nj - 1 ? s : z.nj - 1;
-  klo = s - (z.ni - 1) - (z.nj - 1); if (klo < 0) klo = 0;
-  int64_t khi = s < z.nk - 1 ? s : z.nk - 1;
-  nbj = jhi - jlo + 1; nbk = khi - klo + 1;
+  if (!a.inplace) return;  // the Newton update runs after the sweep
+  if (sizeof(T) == 8) {
+    // the k-1 neighbour reads this cell's new state in the next plane
+    newton64(z, a.rop_old, a.rop_new, l, double(x[0]), double(x[1]), double(x[2]),
+             double(x[3]), double(x[4]));
+  } else {
+    // mixed path: the new state in precision T for the neighbour's Jacobian;
+    // the FP64 update itself runs after the sweep
+    const T* R = a.st;
+    const T cv = T(z.cv), cvinv = T(1.) / cv, cvinv2 = T(0.5) * cvinv;
+    T ro = R[l], u = R[l + nd], v = R[l + 2 * nd], w = R[l + 3 * nd], tt = R[l + 4 * nd];
+    T n1 = ro + x[0], r_1 = T(1.) / n1;
+    T n2 = (ro * u + x[1]) * r_1, n3 = (ro * v + x[2]) * r_1, n4 = (ro * w + x[3]) * r_1;
+    T roe_old = ro * (cv * tt + T(0.5) * (u * u + v * v + w * w));
+    T n5 = (roe_old + x[4]) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
+    a.stn[l + nd] = n2; a.stn[l + 2 * nd] = n3; a.stn[l + 3 * nd] = n4; a.stn[l + 4 * nd] = n5;
+  }
 }
 
 // ------------------------------------------------------- grid barrier
@@ -332,7 +445,7 @@ __device__ __forceinline__ bool grid_sync(const GridBar& g, unsigned int nblocks
         if (cur == target) break;
         if (*(volatile int*)g.err) break;
         if (++spins > (1ll << 24)) { atomicExch(g.err, 1); break; }
-        __nanosleep(64);
+        __nanosleep(32);
       }
     }
     __threadfence();
@@ -342,43 +455,82 @@ __device__ __forceinline__ bool grid_sync(const GridBar& g, unsigned int nblocks
   return *(volatile int*)g.err == 0;
 }
 
+// cells of plane s spread over every CTA: cell c of the plane goes to CTA
+// c mod gridDim, so each CTA's share is packed into its first warps
+template <int TYP, typename T, bool UPPER>
+__device__ __forceinline__ void do_plane(const Zone& z, const LuCellArgs<T>& a, int64_t s) {
+  const int64_t c0 = a.plane[s], n = a.plane[s + 1] - c0;
+  for (int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ii, jj, kk;
+    unpack(a.cells[c0 + c], ii, jj, kk);
+    if (UPPER) upper_cell<TYP, T>(z, a, ii, jj, kk);
+    else lower_cell<TYP, T>(z, a, ii, jj, kk);
+  }
+}
+
 template <int TYP, typename T>
 __global__ void __launch_bounds__(256) lusgs_persistent(Zone z, LuCellArgs<T> a, GridBar g) {
   const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   unsigned int my_gen = 0;
   for (int64_t s = 0; s <= smax; s++) {   // lower sweep, ascending hyperplanes
-    int64_t jlo, klo, nbj, nbk;
-    plane_box(z, s, jlo, klo, nbj, nbk);
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nbj * nbk; t += stride) {
-      const int64_t jj = jlo + t % nbj, kk = klo + t / nbj, ii = s - jj - kk;
-      if (ii >= 0 && ii < z.ni) lower_cell<TYP, T>(z, a, ii, jj, kk);
-    }
+    do_plane<TYP, T, false>(z, a, s);
     if (!grid_sync(g, gridDim.x, my_gen)) return;
   }
-  for (int64_t s = smax; s >= 0; s--) {   // upper sweep + Newton update
-    int64_t jlo, klo, nbj, nbk;
-    plane_box(z, s, jlo, klo, nbj, nbk);
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nbj * nbk; t += stride) {
-      const int64_t jj = jlo + t % nbj, kk = klo + t / nbj, ii = s - jj - kk;
-      if (ii >= 0 && ii < z.ni) upper_cell<TYP, T>(z, a, ii, jj, kk);
-    }
+  for (int64_t s = smax; s >= 0; s--) {   // upper sweep
+    do_plane<TYP, T, true>(z, a, s);
     if (s > 0 && !grid_sync(g, gridDim.x, my_gen)) return;
   }
 }
 
-// one launch per hyperplane (no inter-CTA waits); kept as a cross-check of
-// the persistent kernel and for streams where cooperative launch is absent
+// one launch per hyperplane (no inter-CTA waits): cross-check of the
+// persistent kernel
 template <int TYP, typename T, bool UPPER>
 __global__ void __launch_bounds__(128) lusgs_plane(Zone z, LuCellArgs<T> a, int64_t s) {
-  int64_t jlo, klo, nbj, nbk;
-  plane_box(z, s, jlo, klo, nbj, nbk);
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nbj * nbk) return;
-  const int64_t jj = jlo + t % nbj, kk = klo + t / nbj, ii = s - jj - kk;
-  if (ii < 0 || ii >= z.ni) return;
+  const int64_t c0 = a.plane[s], n = a.plane[s + 1] - c0;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  int64_t ii, jj, kk;
+  unpack(a.cells[c0 + c], ii, jj, kk);
   if (UPPER) upper_cell<TYP, T>(z, a, ii, jj, kk);
   else lower_cell<TYP, T>(z, a, ii, jj, kk);
+}
+
+// B-coefficient pre-pass over every interior cell
+template <int TYP, typename T>
+__global__ void __launch_bounds__(256) lu_bprep(Zone z, const T* __restrict__ st,
+                                                T* __restrict__ bt) {
+  const int64_t n = z.ni * z.nj * z.nk;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int64_t ii = t % z.ni, r = t / z.ni, jj = r % z.nj, kk = r / z.nj;
+  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
+  const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
+  const int64_t nd = z.nd;
+  constexpr int NB = NBE<TYP>::n;
+  T u = st[l + nd], v = st[l + 2 * nd], w = st[l + 3 * nd], tt = st[l + 4 * nd];
+  T e[NB];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    T tx, ty, tz;
+    nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
+    bentries<TYP, T>(z, d, u, v, w, tt, tx, ty, tz, e);
+#pragma unroll
+    for (int m = 0; m < NB; m++) bt[(d * NB + m) * nd + l] = e[m];
+  }
+}
+
+// FP64 Newton update of every interior cell after the sweeps
+template <typename T>
+__global__ void __launch_bounds__(256) lu_newton(Zone z, const double* __restrict__ R,
+                                                 double* __restrict__ O, const T* __restrict__ d) {
+  const int64_t n = z.ni * z.nj * z.nk;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int64_t ii = t % z.ni, r = t / z.ni, jj = r % z.nj, kk = r / z.nj;
+  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1), nd = z.nd;
+  newton64(z, R, O, l, double(d[l]), double(d[l + nd]), double(d[l + 2 * nd]),
+           double(d[l + 3 * nd]), double(d[l + 4 * nd]));
 }
 
 // FP32 copies of the state, the coefficients and the residual for the
@@ -392,6 +544,11 @@ __global__ void __launch_bounds__(256) to_float(int64_t n, const double* __restr
 template <int TYP, typename T>
 static cudaError_t launch_t(const Zone& z, const LuCellArgs<T>& a, const LuLaunch& L,
                             cudaStream_t st) {
+  const int64_t ncell = z.ni * z.nj * z.nk;
+  const unsigned gc = (unsigned)((ncell + 255) / 256);
+  lu_bprep<TYP, T><<<gc, 256, 0, st>>>(z, a.st, const_cast<T*>(a.bt));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
   if (L.persistent) {
     static int grid_cache[2][2] = {{0, 0}, {0, 0}};
     int& grid = grid_cache[TYP == Z3DCART][sizeof(T) == 4];
@@ -402,28 +559,36 @@ static cudaError_t launch_t(const Zone& z, const LuCellArgs<T>& a, const LuLaunc
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T>, 256, 0);
       grid = nsm * (per > 0 ? per : 1);
     }
-    cudaError_t e = cudaMemsetAsync(L.bar, 0, 2 * sizeof(unsigned int), st);
+    e = cudaMemsetAsync(L.bar, 0, 2 * sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     GridBar g{L.bar, L.bar + 1, L.err};
     void* args[] = {(void*)&z, (void*)&a, (void*)&g};
-    return cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(256),
-                                       args, 0, st);
+    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(256), args,
+                                    0, st);
+  } else {
+    const int B = 128;
+    const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
+    for (int64_t s = 0; s <= smax; s++) {
+      int64_t n = L.plane_host[s + 1] - L.plane_host[s];
+      lusgs_plane<TYP, T, false><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a, s);
+    }
+    for (int64_t s = smax; s >= 0; s--) {
+      int64_t n = L.plane_host[s + 1] - L.plane_host[s];
+      lusgs_plane<TYP, T, true><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a, s);
+    }
+    e = cudaGetLastError();
   }
-  const int B = 128;
-  const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
-  for (int64_t s = 0; s <= smax; s++) {
-    int64_t n = (int64_t)z.nj * z.nk;
-    lusgs_plane<TYP, T, false><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a, s);
+  if (e != cudaSuccess) return e;
+  if (!a.inplace || sizeof(T) == 4) {
+    lu_newton<T><<<gc, 256, 0, st>>>(z, a.rop_old, a.rop_new, a.dio);
+    e = cudaGetLastError();
   }
-  for (int64_t s = smax; s >= 0; s--) {
-    int64_t n = (int64_t)z.nj * z.nk;
-    lusgs_plane<TYP, T, true><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a, s);
-  }
-  return cudaGetLastError();
+  return e;
 }
 
-// One LU-SGS solve (lower, upper + Newton update) of one zone.
+// One LU-SGS solve (lower, upper, Newton update) of one zone.
 cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st) {
+  const int inplace = a.rop_knb == a.rop_new;
   if (L.fp32) {
     const int64_t n = 5 * z.nd;
     const unsigned g = (unsigned)((n + 255) / 256);
@@ -432,11 +597,13 @@ cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cuda
     to_float<<<g, 256, 0, st>>>(n, a.din, L.d32);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    LuCellArgs<float> c{L.st32, L.coe32, L.d32, a.rop_old, a.rop_new, a.rop_knb == a.rop_new};
+    LuCellArgs<float> c{L.st32, L.coe32, L.d32, (const float*)L.bt, a.rop_old, a.rop_new,
+                        L.stn32, inplace, L.cells, L.plane};
     return z.typ == Z3DCART ? launch_t<Z3DCART, float>(z, c, L, st)
                             : launch_t<Z3DFULL, float>(z, c, L, st);
   }
-  LuCellArgs<double> c{a.rop_old, a.coe, a.dout, a.rop_old, a.rop_new, a.rop_knb == a.rop_new};
+  LuCellArgs<double> c{a.rop_old, a.coe, a.dout, (const double*)L.bt, a.rop_old, a.rop_new,
+                       nullptr, inplace, L.cells, L.plane};
   return z.typ == Z3DCART ? launch_t<Z3DCART, double>(z, c, L, st)
                           : launch_t<Z3DFULL, double>(z, c, L, st);
 }
