@@ -52,10 +52,12 @@ struct ZoneData {
   double *drodm = nullptr, *coe = nullptr, *xmut = nullptr, *rdm = nullptr;
   double *ti = nullptr, *tj = nullptr, *tk = nullptr, *vol = nullptr;
   double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
-  float *st32 = nullptr, *coe32 = nullptr, *d32 = nullptr, *stn32 = nullptr;  // mixed LU work
-  void* bt = nullptr;               // LU B-coefficient table
+  void* luwork = nullptr;           // plane-ordered LU work (FP64-sized)
   uint32_t* cells = nullptr;        // interior cells by hyperplane
   int64_t* plane = nullptr;         // plane offsets (device)
+  int32_t* posmap = nullptr;        // natural index -> plane index
+  int32_t* nbl = nullptr;           // lower neighbours in plane order
+  int32_t* nbu = nullptr;           // upper neighbours in plane order
   std::vector<int64_t> plane_host;  // plane offsets (host)
   int64_t n_rdm = 0, ijkv_lu[3] = {1, 1, 1};
   std::vector<GatherList> bcs;
@@ -317,8 +319,8 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.scratch); cudaFree(Z.drodm); cudaFree(Z.coe); cudaFree(Z.xmut); cudaFree(Z.rdm);
     cudaFree(Z.ti); cudaFree(Z.tj); cudaFree(Z.tk); cudaFree(Z.vol);
     cudaFree(Z.Fi); cudaFree(Z.Fj); cudaFree(Z.Fk);
-    cudaFree(Z.st32); cudaFree(Z.coe32); cudaFree(Z.d32); cudaFree(Z.stn32);
-    cudaFree(Z.bt); cudaFree(Z.cells); cudaFree(Z.plane);
+    cudaFree(Z.luwork); cudaFree(Z.cells); cudaFree(Z.plane); cudaFree(Z.posmap);
+    cudaFree(Z.nbl); cudaFree(Z.nbu);
     for (GatherList& g : Z.bcs) { cudaFree(g.dst); cudaFree(g.src); }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
@@ -402,17 +404,28 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
       for (int64_t j = 0; j < nj; j++)
         for (int64_t i = 0; i < ni; i++) off[i + j + k + 1]++;
     for (int64_t q = 0; q < np; q++) off[q + 1] += off[q];
-    std::vector<uint32_t> cells(ni * nj * nk);
+    const int64_t G = ni * nj * nk;
+    std::vector<uint32_t> cells(G);
+    std::vector<int32_t> posmap(nd, -1);
     std::vector<int64_t> pos(off.begin(), off.end() - 1);
     for (int64_t k = 0; k < nk; k++)
       for (int64_t j = 0; j < nj; j++)
-        for (int64_t i = 0; i < ni; i++)
-          cells[pos[i + j + k]++] = (uint32_t)(i | (j << 11) | (k << 22));
+        for (int64_t i = 0; i < ni; i++) {
+          int64_t g = pos[i + j + k]++;
+          cells[g] = (uint32_t)(i | (j << 11) | (k << 22));
+          posmap[idx(p, i + 1, j + 1, k + 1)] = (int32_t)g;
+        }
     CK(dev_upload(&Z.cells, cells));
     CK(dev_upload(&Z.plane, off));
+    CK(dev_upload(&Z.posmap, posmap));
     Z.plane_host = off;
-    const int64_t nb = Z.z.typ == Z3DCART ? 14 : 25;
-    CK(cudaMalloc(&Z.bt, sizeof(double) * 3 * nb * nd));
+    CK(cudaMalloc(&Z.nbl, sizeof(int32_t) * 3 * G));
+    CK(cudaMalloc(&Z.nbu, sizeof(int32_t) * 3 * G));
+    CK(cudaMalloc(&Z.luwork, sizeof(double) * G * lusgs_work_words(Z.z.typ)));
+    LuLaunch L0{};
+    L0.G = G; L0.cells = Z.cells; L0.posmap = Z.posmap;
+    CK(launch_lu_neighbours(Z.z, L0, Z.nbl, Z.nbu, s->st));
+    CK(cudaStreamSynchronize(s->st));
   }
   s->zones.push_back(Z);
   if (zone_id) *zone_id = (int)s->zones.size() - 1;
@@ -655,22 +668,14 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             L.fp32 = s->lu_precision == 32;
             L.bar = s->bar;
             L.err = s->derr;
-            if (L.fp32) {
-              if (!Z.st32) {
-                size_t nb = sizeof(float) * 5 * z.nd;
-                CK(cudaMalloc(&Z.st32, nb));
-                CK(cudaMalloc(&Z.coe32, nb));
-                CK(cudaMalloc(&Z.d32, nb));
-                CK(cudaMalloc(&Z.stn32, nb));
-              }
-              L.st32 = Z.st32; L.coe32 = Z.coe32; L.d32 = Z.d32; L.stn32 = Z.stn32;
-            }
-            L.bt = Z.bt; L.cells = Z.cells; L.plane = Z.plane; L.plane_host = Z.plane_host.data();
+            L.work = Z.luwork; L.G = z.ni * z.nj * z.nk;
+            L.cells = Z.cells; L.plane = Z.plane; L.plane_host = Z.plane_host.data();
+            L.posmap = Z.posmap; L.nbl = Z.nbl; L.nbu = Z.nbu;
             {
               ProfScope ps(s, "lu_sgs");
               CK(launch_lusgs(z, la, L, s->st));
             }
-            s->launches += 1 + (L.persistent ? 1 : 2 * (z.ni + z.nj + z.nk - 2)) + (L.fp32 ? 3 : 0) +
+            s->launches += 1 + (L.persistent ? 1 : 2 * (z.ni + z.nj + z.nk - 2)) +
                            ((!inplace || L.fp32) ? 1 : 0);
             if (inplace) std::swap(Z.lvl[2], Z.scratch);
           }

@@ -47,12 +47,18 @@ struct LuLaunch {
   int fp32;
   unsigned int* bar;   // 2 words of barrier state (zeroed by the launcher)
   int* err;            // device error word (barrier time-out)
-  float* st32; float* coe32; float* d32; float* stn32;
-  void* bt;                 // B-coefficient table (3 * entries * NDIMDX of the sweep precision)
+  void* work;          // plane-ordered work: G * lusgs_work_words(typ) words of the sweep precision
+  int64_t G;           // interior cells
   const uint32_t* cells;    // interior cells ordered by hyperplane (packed i | j<<11 | k<<22)
   const int64_t* plane;     // device offsets of each hyperplane in `cells`
   const int64_t* plane_host;  // the same offsets on the host
+  const int32_t* posmap;    // natural cell index -> plane index
+  const int32_t* nbl;       // [3][G] lower neighbours (plane index or -1)
+  const int32_t* nbu;       // [3][G] upper neighbours
 };
+int64_t lusgs_work_words(int typ);
+cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl, int32_t* nbu,
+                                 cudaStream_t st);
 cudaError_t launch_coefficients(const Zone& z, const CoeArgs& a, cudaStream_t st);
 cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st);
 

@@ -285,138 +285,227 @@ __device__ __forceinline__ void bmatvec(const Zone& z, const T* e, T cs, const T
 
 template <int D> struct DirT { static constexpr int value = D; };
 
-// ---------------------------------------------------------------- cells
-// Precision T: double for the plain FP64 path; float for the mixed path
-// (FP32 sweeps and approximate Jacobians; the Newton update stays FP64).
+// ------------------------------------------------------- plane-ordered data
+// The sweeps visit cells hyperplane by hyperplane, which has no locality in
+// the natural (i,j,k) layout.  Every array the sweeps read is therefore
+// gathered once per solve into hyperplane order (index g = position in the
+// plane table): consecutive cells of a plane, and their neighbours on the
+// previous plane, are then consecutive in memory.
 template <typename T>
-struct LuCellArgs {
-  const T* st;            // W^p in precision T
-  const T* coe;           // coe in precision T
-  T* dio;                 // increment, in place over the residual
-  const T* bt;            // B entries: bt[(d*NB + m)*nd + l]
-  const double* rop_old;  // FP64 W^p (Newton update)
-  double* rop_new;        // FP64 W^{p+1}
-  T* stn;                 // mixed path, in place: W^{p+1} in precision T (k+1 neighbours)
-  int inplace;            // upper sweep: k+1 neighbour taken after its update
-  const uint32_t* cells;  // cells ordered by hyperplane, packed i | j<<11 | k<<22
-  const int64_t* plane;   // plane s holds cells[plane[s] .. plane[s+1])
+struct PlaneData {
+  T* dio;            // [5][G]  residual in, increment out (in place)
+  T* coe1;           // [G]     dt/vol
+  T* coe5;           // [G]     LU diagonal
+  T* diag;           // [G]     1 / coe5 (taken off the sweep's critical path)
+  T* coen;           // [3][G]  coe_{d+2} (spectral radius of direction d)
+  T* st;             // [5][G]  W^p (Newton update of the in-place upper sweep)
+  T* bt;             // [3][NB][G] B-matrix entries of each cell
+  T* newst;          // [4][G]  W^{p+1} (u,v,w,T) of the in-place upper sweep
+  const int32_t* nbl;  // [3][G] plane index of the i-1 / j-1 / k-1 neighbour, -1 if none
+  const int32_t* nbu;  // [3][G] plane index of the i+1 / j+1 / k+1 neighbour, -1 if none
+  const uint32_t* cells;  // [G] packed (i, j, k) of each plane index
+  const int64_t* plane;   // plane s = [plane[s], plane[s+1])
+  int64_t G;
+};
+
+struct LuFields {           // natural-order FP64 fields of one LU solve
+  const double* rop_old;    // W^p
+  double* rop_new;          // W^{p+1}
+  const double* coe;        // coefficients
+  const double* din;        // Newton residual
+  const int32_t* posmap;    // natural index -> plane index (-1 outside the LU range)
+  int inplace;              // upper sweep reads the k+1 neighbour after its update
 };
 
 __device__ __forceinline__ void unpack(uint32_t c, int64_t& ii, int64_t& jj, int64_t& kk) {
   ii = c & 2047u; jj = (c >> 11) & 2047u; kk = c >> 22;
 }
 
-template <int TYP, typename T>
-__device__ __forceinline__ void lower_cell(const Zone& z, const LuCellArgs<T>& a, int64_t ii,
-                                           int64_t jj, int64_t kk) {
+// neighbour tables (static per zone)
+__global__ void __launch_bounds__(256) lu_neighbours(Zone z, const uint32_t* __restrict__ cells,
+                                                     const int32_t* __restrict__ posmap,
+                                                     int32_t* __restrict__ nbl,
+                                                     int32_t* __restrict__ nbu, int64_t G) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= G) return;
+  int64_t ii, jj, kk;
+  unpack(cells[g], ii, jj, kk);
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
-  const int64_t nd = z.nd;
+  const int64_t idx[3] = {ii, jj, kk}, n[3] = {z.ni, z.nj, z.nk};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    nbl[d * G + g] = idx[d] > 0 ? posmap[l - z.inc[d]] : -1;
+    nbu[d * G + g] = idx[d] < n[d] - 1 ? posmap[l + z.inc[d]] : -1;
+  }
+}
+
+// per-solve gather into plane order + B entries (fully parallel)
+template <int TYP, typename T>
+__global__ void __launch_bounds__(256) lu_gather(Zone z, LuFields f, PlaneData<T> p) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= p.G) return;
+  int64_t ii, jj, kk;
+  unpack(p.cells[g], ii, jj, kk);
+  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
+  const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
+  const int64_t nd = z.nd, G = p.G;
   constexpr int NB = NBE<TYP>::n;
-  const T xal = a.coe[l] * T(0.5);
+#pragma unroll
+  for (int v = 0; v < 5; v++) p.dio[v * G + g] = T(f.din[l + v * nd]);
+  const T c5 = T(f.coe[l + 4 * nd]);
+  p.coe1[g] = T(f.coe[l]);
+  p.coe5[g] = c5;
+  p.diag[g] = T(1.) / c5;
+#pragma unroll
+  for (int d = 0; d < 3; d++) p.coen[d * G + g] = T(f.coe[l + (d + 1) * nd]);
+  T w5[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    w5[v] = T(f.rop_old[l + v * nd]);
+    p.st[v * G + g] = w5[v];
+  }
+  T e[NB];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    T tx, ty, tz;
+    nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
+    bentries<TYP, T>(z, d, w5[1], w5[2], w5[3], w5[4], tx, ty, tz, e);
+#pragma unroll
+    for (int m = 0; m < NB; m++) p.bt[(d * NB + m) * G + g] = e[m];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void prefetch_l1(const T* ptr) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
+}
+
+// static data of cell g for one sweep (prefetched before the plane barrier)
+template <int TYP, typename T, bool UPPER>
+__device__ __forceinline__ void prefetch_cell(const PlaneData<T>& p, int64_t g) {
+  constexpr int NB = NBE<TYP>::n;
+  const int32_t* nb = UPPER ? p.nbu : p.nbl;
+  prefetch_l1(p.coe1 + g);
+  prefetch_l1(p.diag + g);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int32_t n = nb[d * p.G + g];
+    if (n < 0) continue;
+    prefetch_l1(p.coen + d * p.G + n);
+#pragma unroll
+    for (int m = 0; m < NB; m++) prefetch_l1(p.bt + (d * NB + m) * p.G + n);
+  }
+}
+
+// ---------------------------------------------------------------- cells
+// Precision T: double for the plain FP64 path; float for the mixed path
+// (FP32 sweeps and approximate Jacobians; the Newton update stays FP64).
+template <int TYP, typename T>
+__device__ __forceinline__ void lower_cell(const Zone& z, const PlaneData<T>& p, int64_t g) {
+  constexpr int NB = NBE<TYP>::n;
+  const int64_t G = p.G;
+  const T xal = p.coe1[g] * T(0.5);
   T x[5], o[5], b[5], e[NB];
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = ldcg(a.dio + l + v * nd);
-  auto term = [&](auto dc, int64_t l1) {
+  for (int v = 0; v < 5; v++) x[v] = __ldcg(p.dio + v * G + g);
+  auto term = [&](auto dc) {
     constexpr int D = decltype(dc)::value;
+    const int32_t n = p.nbl[D * G + g];
+    if (n < 0) return;
 #pragma unroll
-    for (int v = 0; v < 5; v++) o[v] = ldcg(a.dio + l1 + v * nd);
+    for (int v = 0; v < 5; v++) o[v] = __ldcg(p.dio + v * G + n);
 #pragma unroll
-    for (int m = 0; m < NB; m++) e[m] = a.bt[(D * NB + m) * nd + l1];
-    T cs = a.coe[l1 + (D + 1) * nd] * T(0.5);
+    for (int m = 0; m < NB; m++) e[m] = p.bt[(D * NB + m) * G + n];
+    T cs = p.coen[D * G + n] * T(0.5);
     bmatvec<TYP, D, T>(z, e, cs, o, b);
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
   };
   if (TYP == Z3DCART) {  // invlu_l.for cartesian section: j, then k, then i
-    if (jj > 0) term(DirT<1>{}, l - z.inc[1]);
-    if (kk > 0) term(DirT<2>{}, l - z.inc[2]);
+    term(DirT<1>{});
+    term(DirT<2>{});
   } else {               // general section: k, then j, then i
-    if (kk > 0) term(DirT<2>{}, l - z.inc[2]);
-    if (jj > 0) term(DirT<1>{}, l - z.inc[1]);
+    term(DirT<2>{});
+    term(DirT<1>{});
   }
-  if (ii > 0) term(DirT<0>{}, l - 1);
-  const T diag = T(1.) / a.coe[l + 4 * nd];
+  term(DirT<0>{});
+  const T diag = p.diag[g];
 #pragma unroll
-  for (int v = 0; v < 5; v++) a.dio[l + v * nd] = x[v] * diag;
+  for (int v = 0; v < 5; v++) p.dio[v * G + g] = x[v] * diag;
 }
 
-// mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW), FP64
-__device__ __forceinline__ void newton64(const Zone& z, const double* R, double* O, int64_t l,
-                                         double d0, double d1, double d2, double d3, double d4) {
-  const int64_t nd = z.nd;
-  const double cv = z.cv, cvinv = 1. / cv, cvinv2 = 0.5 * cvinv;
-  double ro = R[l], u = R[l + nd], v = R[l + 2 * nd], w = R[l + 3 * nd], tt = R[l + 4 * nd];
-  double n1 = ro + d0;
-  double r_1 = 1. / n1;
-  double n2 = (ro * u + d1) * r_1;
-  double n3 = (ro * v + d2) * r_1;
-  double n4 = (ro * w + d3) * r_1;
-  double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v + w * w));
-  double n5 = (roe_old + d4) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
-  O[l] = n1; O[l + nd] = n2; O[l + 2 * nd] = n3; O[l + 3 * nd] = n4; O[l + 4 * nd] = n5;
+// mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW) in precision T
+template <typename T>
+__device__ __forceinline__ void newton(T cv, T ro, T u, T v, T w, T tt, const T d[5], T n[5]) {
+  const T cvinv = T(1.) / cv, cvinv2 = T(0.5) * cvinv;
+  n[0] = ro + d[0];
+  const T r_1 = T(1.) / n[0];
+  n[1] = (ro * u + d[1]) * r_1;
+  n[2] = (ro * v + d[2]) * r_1;
+  n[3] = (ro * w + d[3]) * r_1;
+  const T roe_old = ro * (cv * tt + T(0.5) * (u * u + v * v + w * w));
+  n[4] = (roe_old + d[4]) * r_1 * cvinv - cvinv2 * (n[1] * n[1] + n[2] * n[2] + n[3] * n[3]);
 }
 
 template <int TYP, typename T>
-__device__ __forceinline__ void upper_cell(const Zone& z, const LuCellArgs<T>& a, int64_t ii,
-                                           int64_t jj, int64_t kk) {
-  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
-  const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
-  const int64_t nd = z.nd;
+__device__ __forceinline__ void upper_cell(const Zone& z, const PlaneData<T>& p,
+                                           const LuFields& f, int64_t g) {
   constexpr int NB = NBE<TYP>::n;
-  const T xal = a.coe[l] * T(-0.5);
-  const T dg = a.coe[l + 4 * nd];
+  const int64_t G = p.G;
+  const T xal = p.coe1[g] * T(-0.5);
+  const T dg = p.coe5[g];
   T x[5], o[5], b[5], e[NB];
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = ldcg(a.dio + l + v * nd) * dg;  // lu_d.for
-  auto term = [&](auto dc, int64_t l1, bool fresh) {
+  for (int v = 0; v < 5; v++) x[v] = __ldcg(p.dio + v * G + g) * dg;  // lu_d.for
+  auto term = [&](auto dc, bool fresh) {
     constexpr int D = decltype(dc)::value;
+    const int32_t n = p.nbu[D * G + g];
+    if (n < 0) return;
 #pragma unroll
-    for (int v = 0; v < 5; v++) o[v] = ldcg(a.dio + l1 + v * nd);
-    T cs = a.coe[l1 + (D + 1) * nd] * T(-0.5);
-    if (fresh) {  // neighbour already updated: B from its new state
-      T u, vv, w, t;
-      if (sizeof(T) == 8) {
-        u = T(ldcg(a.rop_new + l1 + nd)); vv = T(ldcg(a.rop_new + l1 + 2 * nd));
-        w = T(ldcg(a.rop_new + l1 + 3 * nd)); t = T(ldcg(a.rop_new + l1 + 4 * nd));
-      } else {
-        u = ldcg(a.stn + l1 + nd); vv = ldcg(a.stn + l1 + 2 * nd);
-        w = ldcg(a.stn + l1 + 3 * nd); t = ldcg(a.stn + l1 + 4 * nd);
-      }
+    for (int v = 0; v < 5; v++) o[v] = __ldcg(p.dio + v * G + n);
+    T cs = p.coen[D * G + n] * T(-0.5);
+    if (fresh) {  // k+1 neighbour updated in place: B from its new state
+      T u = __ldcg(p.newst + n), vv = __ldcg(p.newst + G + n);
+      T w = __ldcg(p.newst + 2 * G + n), t = __ldcg(p.newst + 3 * G + n);
       T tx, ty, tz;
-      nb_normal<TYP, T>(z, D, lt + z.minc[D], lt + 2 * z.minc[D], tx, ty, tz);
+      if (TYP == Z3DCART) {
+        tx = T(0); ty = T(0); tz = T(z.tcz);
+      } else {
+        int64_t ii, jj, kk;
+        unpack(p.cells[n], ii, jj, kk);
+        const int64_t lt = indmtr(z, ii + 1, jj + 1, kk + 1);
+        nb_normal<TYP, T>(z, D, lt, lt + z.minc[D], tx, ty, tz);
+      }
       bentries<TYP, T>(z, D, u, vv, w, t, tx, ty, tz, e);
     } else {
 #pragma unroll
-      for (int m = 0; m < NB; m++) e[m] = a.bt[(D * NB + m) * nd + l1];
+      for (int m = 0; m < NB; m++) e[m] = p.bt[(D * NB + m) * G + n];
     }
     bmatvec<TYP, D, T>(z, e, cs, o, b);
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
   };
-  if (kk < z.nk - 1) term(DirT<2>{}, l + z.inc[2], a.inplace != 0);
-  if (jj < z.nj - 1) term(DirT<1>{}, l + z.inc[1], false);
-  if (ii < z.ni - 1) term(DirT<0>{}, l + 1, false);
-  const T diag = T(1.) / a.coe[l + 4 * nd];
+  term(DirT<2>{}, f.inplace != 0);
+  term(DirT<1>{}, false);
+  term(DirT<0>{}, false);
+  const T diag = p.diag[g];
 #pragma unroll
   for (int v = 0; v < 5; v++) x[v] = x[v] * diag;
 #pragma unroll
-  for (int v = 0; v < 5; v++) a.dio[l + v * nd] = x[v];
-  if (!a.inplace) return;  // the Newton update runs after the sweep
-  if (sizeof(T) == 8) {
-    // the k-1 neighbour reads this cell's new state in the next plane
-    newton64(z, a.rop_old, a.rop_new, l, double(x[0]), double(x[1]), double(x[2]),
-             double(x[3]), double(x[4]));
-  } else {
-    // mixed path: the new state in precision T for the neighbour's Jacobian;
-    // the FP64 update itself runs after the sweep
-    const T* R = a.st;
-    const T cv = T(z.cv), cvinv = T(1.) / cv, cvinv2 = T(0.5) * cvinv;
-    T ro = R[l], u = R[l + nd], v = R[l + 2 * nd], w = R[l + 3 * nd], tt = R[l + 4 * nd];
-    T n1 = ro + x[0], r_1 = T(1.) / n1;
-    T n2 = (ro * u + x[1]) * r_1, n3 = (ro * v + x[2]) * r_1, n4 = (ro * w + x[3]) * r_1;
-    T roe_old = ro * (cv * tt + T(0.5) * (u * u + v * v + w * w));
-    T n5 = (roe_old + x[4]) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
-    a.stn[l + nd] = n2; a.stn[l + 2 * nd] = n3; a.stn[l + 3 * nd] = n4; a.stn[l + 4 * nd] = n5;
+  for (int v = 0; v < 5; v++) p.dio[v * G + g] = x[v];
+  if (!f.inplace) return;  // the Newton update runs after the sweep
+  // in place: the k-1 neighbour needs this cell's new state in the next plane
+  T nw[5];
+  newton<T>(T(z.cv), p.st[g], p.st[G + g], p.st[2 * G + g], p.st[3 * G + g], p.st[4 * G + g], x,
+            nw);
+#pragma unroll
+  for (int v = 0; v < 4; v++) p.newst[v * G + g] = nw[v + 1];
+  if (sizeof(T) == 8) {  // FP64 path: this is the update itself
+    int64_t ii, jj, kk;
+    unpack(p.cells[g], ii, jj, kk);
+    const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
+#pragma unroll
+    for (int v = 0; v < 5; v++) f.rop_new[l + v * z.nd] = double(nw[v]);
   }
 }
 
@@ -445,7 +534,7 @@ __device__ __forceinline__ bool grid_sync(const GridBar& g, unsigned int nblocks
         if (cur == target) break;
         if (*(volatile int*)g.err) break;
         if (++spins > (1ll << 24)) { atomicExch(g.err, 1); break; }
-        __nanosleep(32);
+        __nanosleep(20);
       }
     }
     __threadfence();
@@ -458,95 +547,79 @@ __device__ __forceinline__ bool grid_sync(const GridBar& g, unsigned int nblocks
 // cells of plane s spread over every CTA: cell c of the plane goes to CTA
 // c mod gridDim, so each CTA's share is packed into its first warps
 template <int TYP, typename T, bool UPPER>
-__device__ __forceinline__ void do_plane(const Zone& z, const LuCellArgs<T>& a, int64_t s) {
-  const int64_t c0 = a.plane[s], n = a.plane[s + 1] - c0;
+__device__ __forceinline__ void do_plane(const Zone& z, const PlaneData<T>& p, const LuFields& f,
+                                         int64_t s) {
+  const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
   for (int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x) {
-    int64_t ii, jj, kk;
-    unpack(a.cells[c0 + c], ii, jj, kk);
-    if (UPPER) upper_cell<TYP, T>(z, a, ii, jj, kk);
-    else lower_cell<TYP, T>(z, a, ii, jj, kk);
+    if (UPPER) upper_cell<TYP, T>(z, p, f, c0 + c);
+    else lower_cell<TYP, T>(z, p, c0 + c);
   }
 }
 
+template <int TYP, typename T, bool UPPER>
+__device__ __forceinline__ void prefetch_plane(const PlaneData<T>& p, int64_t s) {
+  const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
+  const int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
+  if (c < n) prefetch_cell<TYP, T, UPPER>(p, c0 + c);
+}
+
 template <int TYP, typename T>
-__global__ void __launch_bounds__(256) lusgs_persistent(Zone z, LuCellArgs<T> a, GridBar g) {
+__global__ void __launch_bounds__(512) lusgs_persistent(Zone z, PlaneData<T> p, LuFields f,
+                                                        GridBar gb) {
   const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
   unsigned int my_gen = 0;
+  prefetch_plane<TYP, T, false>(p, 0);
   for (int64_t s = 0; s <= smax; s++) {   // lower sweep, ascending hyperplanes
-    do_plane<TYP, T, false>(z, a, s);
-    if (!grid_sync(g, gridDim.x, my_gen)) return;
+    do_plane<TYP, T, false>(z, p, f, s);
+    if (s < smax) prefetch_plane<TYP, T, false>(p, s + 1);
+    else prefetch_plane<TYP, T, true>(p, smax);
+    if (!grid_sync(gb, gridDim.x, my_gen)) return;
   }
   for (int64_t s = smax; s >= 0; s--) {   // upper sweep
-    do_plane<TYP, T, true>(z, a, s);
-    if (s > 0 && !grid_sync(g, gridDim.x, my_gen)) return;
+    do_plane<TYP, T, true>(z, p, f, s);
+    if (s > 0) {
+      prefetch_plane<TYP, T, true>(p, s - 1);
+      if (!grid_sync(gb, gridDim.x, my_gen)) return;
+    }
   }
 }
 
 // one launch per hyperplane (no inter-CTA waits): cross-check of the
 // persistent kernel
 template <int TYP, typename T, bool UPPER>
-__global__ void __launch_bounds__(128) lusgs_plane(Zone z, LuCellArgs<T> a, int64_t s) {
-  const int64_t c0 = a.plane[s], n = a.plane[s + 1] - c0;
+__global__ void __launch_bounds__(128) lusgs_plane(Zone z, PlaneData<T> p, LuFields f, int64_t s) {
+  const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
-  int64_t ii, jj, kk;
-  unpack(a.cells[c0 + c], ii, jj, kk);
-  if (UPPER) upper_cell<TYP, T>(z, a, ii, jj, kk);
-  else lower_cell<TYP, T>(z, a, ii, jj, kk);
+  if (UPPER) upper_cell<TYP, T>(z, p, f, c0 + c);
+  else lower_cell<TYP, T>(z, p, c0 + c);
 }
 
-// B-coefficient pre-pass over every interior cell
-template <int TYP, typename T>
-__global__ void __launch_bounds__(256) lu_bprep(Zone z, const T* __restrict__ st,
-                                                T* __restrict__ bt) {
-  const int64_t n = z.ni * z.nj * z.nk;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int64_t ii = t % z.ni, r = t / z.ni, jj = r % z.nj, kk = r / z.nj;
-  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
-  const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
-  const int64_t nd = z.nd;
-  constexpr int NB = NBE<TYP>::n;
-  T u = st[l + nd], v = st[l + 2 * nd], w = st[l + 3 * nd], tt = st[l + 4 * nd];
-  T e[NB];
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    T tx, ty, tz;
-    nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
-    bentries<TYP, T>(z, d, u, v, w, tt, tx, ty, tz, e);
-#pragma unroll
-    for (int m = 0; m < NB; m++) bt[(d * NB + m) * nd + l] = e[m];
-  }
-}
-
-// FP64 Newton update of every interior cell after the sweeps
+// FP64 Newton update of every interior cell after the sweeps (natural order)
 template <typename T>
-__global__ void __launch_bounds__(256) lu_newton(Zone z, const double* __restrict__ R,
-                                                 double* __restrict__ O, const T* __restrict__ d) {
+__global__ void __launch_bounds__(256) lu_newton(Zone z, LuFields f, const T* __restrict__ dio,
+                                                 int64_t G) {
   const int64_t n = z.ni * z.nj * z.nk;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int64_t ii = t % z.ni, r = t / z.ni, jj = r % z.nj, kk = r / z.nj;
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1), nd = z.nd;
-  newton64(z, R, O, l, double(d[l]), double(d[l + nd]), double(d[l + 2 * nd]),
-           double(d[l + 3 * nd]), double(d[l + 4 * nd]));
-}
-
-// FP32 copies of the state, the coefficients and the residual for the
-// mixed-precision sweeps (one pass per sub-iteration)
-__global__ void __launch_bounds__(256) to_float(int64_t n, const double* __restrict__ a,
-                                                float* __restrict__ b) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) b[t] = (float)a[t];
+  const int64_t g = f.posmap[l];
+  const double* R = f.rop_old;
+  double d[5], nw[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) d[v] = double(dio[v * G + g]);
+  newton<double>(z.cv, R[l], R[l + nd], R[l + 2 * nd], R[l + 3 * nd], R[l + 4 * nd], d, nw);
+#pragma unroll
+  for (int v = 0; v < 5; v++) f.rop_new[l + v * nd] = nw[v];
 }
 
 template <int TYP, typename T>
-static cudaError_t launch_t(const Zone& z, const LuCellArgs<T>& a, const LuLaunch& L,
-                            cudaStream_t st) {
-  const int64_t ncell = z.ni * z.nj * z.nk;
-  const unsigned gc = (unsigned)((ncell + 255) / 256);
-  lu_bprep<TYP, T><<<gc, 256, 0, st>>>(z, a.st, const_cast<T*>(a.bt));
+static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>& p,
+                            const LuLaunch& L, cudaStream_t st) {
+  const unsigned gc = (unsigned)((p.G + 255) / 256);
+  lu_gather<TYP, T><<<gc, 256, 0, st>>>(z, f, p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (L.persistent) {
@@ -556,56 +629,74 @@ static cudaError_t launch_t(const Zone& z, const LuCellArgs<T>& a, const LuLaunc
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T>, 256, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T>, 512, 0);
       grid = nsm * (per > 0 ? per : 1);
     }
     e = cudaMemsetAsync(L.bar, 0, 2 * sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
-    GridBar g{L.bar, L.bar + 1, L.err};
-    void* args[] = {(void*)&z, (void*)&a, (void*)&g};
-    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(256), args,
+    GridBar gb{L.bar, L.bar + 1, L.err};
+    void* args[] = {(void*)&z, (void*)&p, (void*)&f, (void*)&gb};
+    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(512), args,
                                     0, st);
   } else {
     const int B = 128;
     const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
     for (int64_t s = 0; s <= smax; s++) {
       int64_t n = L.plane_host[s + 1] - L.plane_host[s];
-      lusgs_plane<TYP, T, false><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a, s);
+      lusgs_plane<TYP, T, false><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
     }
     for (int64_t s = smax; s >= 0; s--) {
       int64_t n = L.plane_host[s + 1] - L.plane_host[s];
-      lusgs_plane<TYP, T, true><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a, s);
+      lusgs_plane<TYP, T, true><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
     }
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) return e;
-  if (!a.inplace || sizeof(T) == 4) {
-    lu_newton<T><<<gc, 256, 0, st>>>(z, a.rop_old, a.rop_new, a.dio);
+  if (!f.inplace || sizeof(T) == 4) {
+    lu_newton<T><<<gc, 256, 0, st>>>(z, f, p.dio, p.G);
     e = cudaGetLastError();
   }
   return e;
 }
 
+template <typename T>
+static PlaneData<T> plane_data(const LuLaunch& L, int nb) {
+  PlaneData<T> p;
+  const int64_t G = L.G;
+  T* w = (T*)L.work;
+  p.dio = w; w += 5 * G;
+  p.coe1 = w; w += G;
+  p.coe5 = w; w += G;
+  p.diag = w; w += G;
+  p.coen = w; w += 3 * G;
+  p.st = w; w += 5 * G;
+  p.newst = w; w += 4 * G;
+  p.bt = w; w += 3 * (int64_t)nb * G;
+  p.nbl = L.nbl; p.nbu = L.nbu; p.cells = L.cells; p.plane = L.plane; p.G = G;
+  return p;
+}
+
+// words of LU work per interior cell (the caller allocates G * this * 8 bytes)
+int64_t lusgs_work_words(int typ) { return 5 + 1 + 1 + 1 + 3 + 5 + 4 + 3 * (typ == Z3DCART ? NB_CART : NB_FULL); }
+
+cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl, int32_t* nbu,
+                                 cudaStream_t st) {
+  lu_neighbours<<<(unsigned)((L.G + 255) / 256), 256, 0, st>>>(z, L.cells, L.posmap, nbl, nbu, L.G);
+  return cudaGetLastError();
+}
+
 // One LU-SGS solve (lower, upper, Newton update) of one zone.
 cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st) {
-  const int inplace = a.rop_knb == a.rop_new;
+  LuFields f{a.rop_old, a.rop_new, a.coe, a.din, L.posmap, a.rop_knb == a.rop_new};
+  const int nb = z.typ == Z3DCART ? NB_CART : NB_FULL;
   if (L.fp32) {
-    const int64_t n = 5 * z.nd;
-    const unsigned g = (unsigned)((n + 255) / 256);
-    to_float<<<g, 256, 0, st>>>(n, a.rop_old, L.st32);
-    to_float<<<g, 256, 0, st>>>(n, a.coe, L.coe32);
-    to_float<<<g, 256, 0, st>>>(n, a.din, L.d32);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    LuCellArgs<float> c{L.st32, L.coe32, L.d32, (const float*)L.bt, a.rop_old, a.rop_new,
-                        L.stn32, inplace, L.cells, L.plane};
-    return z.typ == Z3DCART ? launch_t<Z3DCART, float>(z, c, L, st)
-                            : launch_t<Z3DFULL, float>(z, c, L, st);
+    PlaneData<float> p = plane_data<float>(L, nb);
+    return z.typ == Z3DCART ? launch_t<Z3DCART, float>(z, f, p, L, st)
+                            : launch_t<Z3DFULL, float>(z, f, p, L, st);
   }
-  LuCellArgs<double> c{a.rop_old, a.coe, a.dout, (const double*)L.bt, a.rop_old, a.rop_new,
-                       nullptr, inplace, L.cells, L.plane};
-  return z.typ == Z3DCART ? launch_t<Z3DCART, double>(z, c, L, st)
-                          : launch_t<Z3DFULL, double>(z, c, L, st);
+  PlaneData<double> p = plane_data<double>(L, nb);
+  return z.typ == Z3DCART ? launch_t<Z3DCART, double>(z, f, p, L, st)
+                          : launch_t<Z3DFULL, double>(z, f, p, L, st);
 }
 
 }  // namespace fgb
