@@ -287,20 +287,27 @@ template <int D> struct DirT { static constexpr int value = D; };
 
 // ------------------------------------------------------- plane-ordered data
 // The sweeps visit cells hyperplane by hyperplane, which has no locality in
-// the natural (i,j,k) layout.  Every array the sweeps read is therefore
+// the natural (i,j,k) layout.  Every value the sweeps read is therefore
 // gathered once per solve into hyperplane order (index g = position in the
-// plane table): consecutive cells of a plane, and their neighbours on the
-// previous plane, are then consecutive in memory.
+// plane table), as one contiguous record per cell: a warp working on
+// consecutive cells of a plane, and on their neighbours in the previous
+// plane, then reads a few contiguous spans instead of one scattered word per
+// array (which thrashed the TLB and sector caches).
+//   rec[g] : coe1, 1/coe5, coe5, -, coe_{2..4}, W^p (5), B entries (3 x NB)
+//   dio[g] : residual in / increment out (5 words, stride 6)
+//   nst[g] : in-place upper sweep: W^{p+1} u, v, w, T (stride 4)
+template <int TYP> struct Rec {
+  static constexpr int NB = NBE<TYP>::n;
+  static constexpr int COE1 = 0, DIAG = 1, COE5 = 2, COEN = 4, ST = 7, B = 12;
+  static constexpr int SIZE = ((B + 3 * NB) + 1) / 2 * 2;   // even: 16-byte records
+};
+constexpr int DIO = 6;
+
 template <typename T>
 struct PlaneData {
-  T* dio;            // [5][G]  residual in, increment out (in place)
-  T* coe1;           // [G]     dt/vol
-  T* coe5;           // [G]     LU diagonal
-  T* diag;           // [G]     1 / coe5 (taken off the sweep's critical path)
-  T* coen;           // [3][G]  coe_{d+2} (spectral radius of direction d)
-  T* st;             // [5][G]  W^p (Newton update of the in-place upper sweep)
-  T* bt;             // [3][NB][G] B-matrix entries of each cell
-  T* newst;          // [4][G]  W^{p+1} (u,v,w,T) of the in-place upper sweep
+  T* rec;              // [G][Rec::SIZE]
+  T* dio;              // [G][DIO]
+  T* nst;              // [G][4]
   const int32_t* nbl;  // [3][G] plane index of the i-1 / j-1 / k-1 neighbour, -1 if none
   const int32_t* nbu;  // [3][G] plane index of the i+1 / j+1 / k+1 neighbour, -1 if none
   const uint32_t* cells;  // [G] packed (i, j, k) of each plane index
@@ -339,85 +346,71 @@ __global__ void __launch_bounds__(256) lu_neighbours(Zone z, const uint32_t* __r
   }
 }
 
-// per-solve gather into plane order + B entries (fully parallel)
+// per-solve gather into plane-ordered records + B entries (fully parallel)
 template <int TYP, typename T>
 __global__ void __launch_bounds__(256) lu_gather(Zone z, LuFields f, PlaneData<T> p) {
+  using R = Rec<TYP>;
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= p.G) return;
   int64_t ii, jj, kk;
   unpack(p.cells[g], ii, jj, kk);
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
   const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
-  const int64_t nd = z.nd, G = p.G;
-  constexpr int NB = NBE<TYP>::n;
+  const int64_t nd = z.nd;
+  T* r = p.rec + g * R::SIZE;
+  T* io = p.dio + g * DIO;
 #pragma unroll
-  for (int v = 0; v < 5; v++) p.dio[v * G + g] = T(f.din[l + v * nd]);
+  for (int v = 0; v < 5; v++) io[v] = T(f.din[l + v * nd]);
   const T c5 = T(f.coe[l + 4 * nd]);
-  p.coe1[g] = T(f.coe[l]);
-  p.coe5[g] = c5;
-  p.diag[g] = T(1.) / c5;
+  r[R::COE1] = T(f.coe[l]);
+  r[R::DIAG] = T(1.) / c5;
+  r[R::COE5] = c5;
 #pragma unroll
-  for (int d = 0; d < 3; d++) p.coen[d * G + g] = T(f.coe[l + (d + 1) * nd]);
+  for (int d = 0; d < 3; d++) r[R::COEN + d] = T(f.coe[l + (d + 1) * nd]);
   T w5[5];
 #pragma unroll
   for (int v = 0; v < 5; v++) {
     w5[v] = T(f.rop_old[l + v * nd]);
-    p.st[v * G + g] = w5[v];
+    r[R::ST + v] = w5[v];
   }
-  T e[NB];
+  T e[R::NB];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     T tx, ty, tz;
     nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
     bentries<TYP, T>(z, d, w5[1], w5[2], w5[3], w5[4], tx, ty, tz, e);
 #pragma unroll
-    for (int m = 0; m < NB; m++) p.bt[(d * NB + m) * G + g] = e[m];
-  }
-}
-
-template <typename T>
-__device__ __forceinline__ void prefetch_l1(const T* ptr) {
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
-}
-
-// static data of cell g for one sweep (prefetched before the plane barrier)
-template <int TYP, typename T, bool UPPER>
-__device__ __forceinline__ void prefetch_cell(const PlaneData<T>& p, int64_t g) {
-  constexpr int NB = NBE<TYP>::n;
-  const int32_t* nb = UPPER ? p.nbu : p.nbl;
-  prefetch_l1(p.coe1 + g);
-  prefetch_l1(p.diag + g);
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const int32_t n = nb[d * p.G + g];
-    if (n < 0) continue;
-    prefetch_l1(p.coen + d * p.G + n);
-#pragma unroll
-    for (int m = 0; m < NB; m++) prefetch_l1(p.bt + (d * NB + m) * p.G + n);
+    for (int m = 0; m < R::NB; m++) r[R::B + d * R::NB + m] = e[m];
   }
 }
 
 // ---------------------------------------------------------------- cells
 // Precision T: double for the plain FP64 path; float for the mixed path
 // (FP32 sweeps and approximate Jacobians; the Newton update stays FP64).
+template <typename T>
+__device__ __forceinline__ void load_dio(const T* __restrict__ dio, int64_t g, T o[5]) {
+  const T* q = dio + g * DIO;
+#pragma unroll
+  for (int v = 0; v < 5; v++) o[v] = __ldcg(q + v);
+}
+
 template <int TYP, typename T>
 __device__ __forceinline__ void lower_cell(const Zone& z, const PlaneData<T>& p, int64_t g) {
-  constexpr int NB = NBE<TYP>::n;
+  using R = Rec<TYP>;
+  constexpr int NB = R::NB;
   const int64_t G = p.G;
-  const T xal = p.coe1[g] * T(0.5);
-  T x[5], o[5], b[5], e[NB];
-#pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = __ldcg(p.dio + v * G + g);
+  const T* me = p.rec + g * R::SIZE;
+  const T xal = me[R::COE1] * T(0.5);
+  T x[5], o[5], b[5];
+  load_dio(p.dio, g, x);
   auto term = [&](auto dc) {
     constexpr int D = decltype(dc)::value;
     const int32_t n = p.nbl[D * G + g];
     if (n < 0) return;
-#pragma unroll
-    for (int v = 0; v < 5; v++) o[v] = __ldcg(p.dio + v * G + n);
-#pragma unroll
-    for (int m = 0; m < NB; m++) e[m] = p.bt[(D * NB + m) * G + n];
-    T cs = p.coen[D * G + n] * T(0.5);
-    bmatvec<TYP, D, T>(z, e, cs, o, b);
+    load_dio(p.dio, n, o);
+    const T* rn = p.rec + (int64_t)n * R::SIZE;
+    T cs = rn[R::COEN + D] * T(0.5);
+    bmatvec<TYP, D, T>(z, rn + R::B + D * NB, cs, o, b);
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
   };
@@ -429,9 +422,10 @@ __device__ __forceinline__ void lower_cell(const Zone& z, const PlaneData<T>& p,
     term(DirT<1>{});
   }
   term(DirT<0>{});
-  const T diag = p.diag[g];
+  const T diag = me[R::DIAG];
+  T* io = p.dio + g * DIO;
 #pragma unroll
-  for (int v = 0; v < 5; v++) p.dio[v * G + g] = x[v] * diag;
+  for (int v = 0; v < 5; v++) io[v] = x[v] * diag;
 }
 
 // mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW) in precision T
@@ -450,23 +444,26 @@ __device__ __forceinline__ void newton(T cv, T ro, T u, T v, T w, T tt, const T 
 template <int TYP, typename T>
 __device__ __forceinline__ void upper_cell(const Zone& z, const PlaneData<T>& p,
                                            const LuFields& f, int64_t g) {
-  constexpr int NB = NBE<TYP>::n;
+  using R = Rec<TYP>;
+  constexpr int NB = R::NB;
   const int64_t G = p.G;
-  const T xal = p.coe1[g] * T(-0.5);
-  const T dg = p.coe5[g];
+  const T* me = p.rec + g * R::SIZE;
+  const T xal = me[R::COE1] * T(-0.5);
+  const T dg = me[R::COE5];
   T x[5], o[5], b[5], e[NB];
+  load_dio(p.dio, g, x);
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = __ldcg(p.dio + v * G + g) * dg;  // lu_d.for
+  for (int v = 0; v < 5; v++) x[v] = x[v] * dg;  // lu_d.for
   auto term = [&](auto dc, bool fresh) {
     constexpr int D = decltype(dc)::value;
     const int32_t n = p.nbu[D * G + g];
     if (n < 0) return;
-#pragma unroll
-    for (int v = 0; v < 5; v++) o[v] = __ldcg(p.dio + v * G + n);
-    T cs = p.coen[D * G + n] * T(-0.5);
+    load_dio(p.dio, n, o);
+    const T* rn = p.rec + (int64_t)n * R::SIZE;
+    T cs = rn[R::COEN + D] * T(-0.5);
     if (fresh) {  // k+1 neighbour updated in place: B from its new state
-      T u = __ldcg(p.newst + n), vv = __ldcg(p.newst + G + n);
-      T w = __ldcg(p.newst + 2 * G + n), t = __ldcg(p.newst + 3 * G + n);
+      const T* q = p.nst + (int64_t)n * 4;
+      T u = __ldcg(q), vv = __ldcg(q + 1), w = __ldcg(q + 2), t = __ldcg(q + 3);
       T tx, ty, tz;
       if (TYP == Z3DCART) {
         tx = T(0); ty = T(0); tz = T(z.tcz);
@@ -477,29 +474,30 @@ __device__ __forceinline__ void upper_cell(const Zone& z, const PlaneData<T>& p,
         nb_normal<TYP, T>(z, D, lt, lt + z.minc[D], tx, ty, tz);
       }
       bentries<TYP, T>(z, D, u, vv, w, t, tx, ty, tz, e);
+      bmatvec<TYP, D, T>(z, e, cs, o, b);
     } else {
-#pragma unroll
-      for (int m = 0; m < NB; m++) e[m] = p.bt[(D * NB + m) * G + n];
+      bmatvec<TYP, D, T>(z, rn + R::B + D * NB, cs, o, b);
     }
-    bmatvec<TYP, D, T>(z, e, cs, o, b);
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
   };
   term(DirT<2>{}, f.inplace != 0);
   term(DirT<1>{}, false);
   term(DirT<0>{}, false);
-  const T diag = p.diag[g];
+  const T diag = me[R::DIAG];
 #pragma unroll
   for (int v = 0; v < 5; v++) x[v] = x[v] * diag;
+  T* io = p.dio + g * DIO;
 #pragma unroll
-  for (int v = 0; v < 5; v++) p.dio[v * G + g] = x[v];
+  for (int v = 0; v < 5; v++) io[v] = x[v];
   if (!f.inplace) return;  // the Newton update runs after the sweep
   // in place: the k-1 neighbour needs this cell's new state in the next plane
   T nw[5];
-  newton<T>(T(z.cv), p.st[g], p.st[G + g], p.st[2 * G + g], p.st[3 * G + g], p.st[4 * G + g], x,
+  newton<T>(T(z.cv), me[R::ST], me[R::ST + 1], me[R::ST + 2], me[R::ST + 3], me[R::ST + 4], x,
             nw);
+  T* q = p.nst + g * 4;
 #pragma unroll
-  for (int v = 0; v < 4; v++) p.newst[v * G + g] = nw[v + 1];
+  for (int v = 0; v < 4; v++) q[v] = nw[v + 1];
   if (sizeof(T) == 8) {  // FP64 path: this is the update itself
     int64_t ii, jj, kk;
     unpack(p.cells[g], ii, jj, kk);
@@ -557,31 +555,18 @@ __device__ __forceinline__ void do_plane(const Zone& z, const PlaneData<T>& p, c
   }
 }
 
-template <int TYP, typename T, bool UPPER>
-__device__ __forceinline__ void prefetch_plane(const PlaneData<T>& p, int64_t s) {
-  const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
-  const int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
-  if (c < n) prefetch_cell<TYP, T, UPPER>(p, c0 + c);
-}
-
 template <int TYP, typename T>
 __global__ void __launch_bounds__(512) lusgs_persistent(Zone z, PlaneData<T> p, LuFields f,
                                                         GridBar gb) {
   const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
   unsigned int my_gen = 0;
-  prefetch_plane<TYP, T, false>(p, 0);
   for (int64_t s = 0; s <= smax; s++) {   // lower sweep, ascending hyperplanes
     do_plane<TYP, T, false>(z, p, f, s);
-    if (s < smax) prefetch_plane<TYP, T, false>(p, s + 1);
-    else prefetch_plane<TYP, T, true>(p, smax);
     if (!grid_sync(gb, gridDim.x, my_gen)) return;
   }
   for (int64_t s = smax; s >= 0; s--) {   // upper sweep
     do_plane<TYP, T, true>(z, p, f, s);
-    if (s > 0) {
-      prefetch_plane<TYP, T, true>(p, s - 1);
-      if (!grid_sync(gb, gridDim.x, my_gen)) return;
-    }
+    if (s > 0 && !grid_sync(gb, gridDim.x, my_gen)) return;
   }
 }
 
@@ -598,8 +583,7 @@ __global__ void __launch_bounds__(128) lusgs_plane(Zone z, PlaneData<T> p, LuFie
 
 // FP64 Newton update of every interior cell after the sweeps (natural order)
 template <typename T>
-__global__ void __launch_bounds__(256) lu_newton(Zone z, LuFields f, const T* __restrict__ dio,
-                                                 int64_t G) {
+__global__ void __launch_bounds__(256) lu_newton(Zone z, LuFields f, const T* __restrict__ dio) {
   const int64_t n = z.ni * z.nj * z.nk;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
@@ -609,7 +593,7 @@ __global__ void __launch_bounds__(256) lu_newton(Zone z, LuFields f, const T* __
   const double* R = f.rop_old;
   double d[5], nw[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) d[v] = double(dio[v * G + g]);
+  for (int v = 0; v < 5; v++) d[v] = double(dio[g * DIO + v]);
   newton<double>(z.cv, R[l], R[l + nd], R[l + 2 * nd], R[l + 3 * nd], R[l + 4 * nd], d, nw);
 #pragma unroll
   for (int v = 0; v < 5; v++) f.rop_new[l + v * nd] = nw[v];
@@ -653,31 +637,28 @@ static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>
   }
   if (e != cudaSuccess) return e;
   if (!f.inplace || sizeof(T) == 4) {
-    lu_newton<T><<<gc, 256, 0, st>>>(z, f, p.dio, p.G);
+    lu_newton<T><<<gc, 256, 0, st>>>(z, f, p.dio);
     e = cudaGetLastError();
   }
   return e;
 }
 
 template <typename T>
-static PlaneData<T> plane_data(const LuLaunch& L, int nb) {
+static PlaneData<T> plane_data(const LuLaunch& L, int rec_size) {
   PlaneData<T> p;
   const int64_t G = L.G;
   T* w = (T*)L.work;
-  p.dio = w; w += 5 * G;
-  p.coe1 = w; w += G;
-  p.coe5 = w; w += G;
-  p.diag = w; w += G;
-  p.coen = w; w += 3 * G;
-  p.st = w; w += 5 * G;
-  p.newst = w; w += 4 * G;
-  p.bt = w; w += 3 * (int64_t)nb * G;
+  p.rec = w; w += (int64_t)rec_size * G;
+  p.dio = w; w += (int64_t)DIO * G;
+  p.nst = w; w += 4 * G;
   p.nbl = L.nbl; p.nbu = L.nbu; p.cells = L.cells; p.plane = L.plane; p.G = G;
   return p;
 }
 
 // words of LU work per interior cell (the caller allocates G * this * 8 bytes)
-int64_t lusgs_work_words(int typ) { return 5 + 1 + 1 + 1 + 3 + 5 + 4 + 3 * (typ == Z3DCART ? NB_CART : NB_FULL); }
+int64_t lusgs_work_words(int typ) {
+  return (typ == Z3DCART ? Rec<Z3DCART>::SIZE : Rec<Z3DFULL>::SIZE) + DIO + 4;
+}
 
 cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl, int32_t* nbu,
                                  cudaStream_t st) {
@@ -688,13 +669,13 @@ cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl,
 // One LU-SGS solve (lower, upper, Newton update) of one zone.
 cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st) {
   LuFields f{a.rop_old, a.rop_new, a.coe, a.din, L.posmap, a.rop_knb == a.rop_new};
-  const int nb = z.typ == Z3DCART ? NB_CART : NB_FULL;
+  const int rs = z.typ == Z3DCART ? Rec<Z3DCART>::SIZE : Rec<Z3DFULL>::SIZE;
   if (L.fp32) {
-    PlaneData<float> p = plane_data<float>(L, nb);
+    PlaneData<float> p = plane_data<float>(L, rs);
     return z.typ == Z3DCART ? launch_t<Z3DCART, float>(z, f, p, L, st)
                             : launch_t<Z3DFULL, float>(z, f, p, L, st);
   }
-  PlaneData<double> p = plane_data<double>(L, nb);
+  PlaneData<double> p = plane_data<double>(L, rs);
   return z.typ == Z3DCART ? launch_t<Z3DCART, double>(z, f, p, L, st)
                           : launch_t<Z3DFULL, double>(z, f, p, L, st);
 }
