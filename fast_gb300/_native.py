@@ -35,6 +35,7 @@ SIGNATURES = {
     "fgb_compute": ([_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
     "fgb_apply_bc": ([_P, C.c_int], C.c_int),
     "fgb_residuals": ([_P, C.c_int, _DP, C.c_int64, C.POINTER(C.c_int)], C.c_int),
+    "fgb_residual_norms_noalloc": ([_P, C.c_int, _P], C.c_int),
     "fgb_synchronize": ([_P], C.c_int),
     "fgb_kernel_stats": ([_P, C.c_int, C.c_char_p, C.c_int, _I64P, _DP], C.c_int),
     "fgb_launch_count": ([_P, _I64P], C.c_int),
@@ -162,6 +163,11 @@ class Solver:
         _check(self._lib.fgb_residuals(self._h, zone, _dp(out), out.size, C.byref(nit)))
         k = nit.value
         return out[:2 * neq * k].reshape(2 * neq, k) if k else np.zeros((2 * neq, 0))
+
+    def residual_norms_noalloc(self, zone: int, out_ptr: int):
+        """Enqueue fgb_residual_norms_noalloc: 2*neq doubles (L2 then Loo)
+        written to the device address out_ptr; fgb_synchronize waits."""
+        _check(self._lib.fgb_residual_norms_noalloc(self._h, int(zone), C.c_void_p(int(out_ptr))))
 
     def synchronize(self):
         _check(self._lib.fgb_synchronize(self._h))

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 #include "../../include/fast_gb300.h"
 #include "fgb_kernels.cuh"
 
@@ -726,6 +727,48 @@ int fgb_residuals(fgb_solver* s, int zone, double* out, int64_t n, int* nit_out)
       out[nit * ne + i] = std::sqrt(rmoy * xpt_1) / Z.pr[DTC];
       out[nit * (ne + neq) + i] = rmax / Z.pr[DTC];
     }
+  return FGB_OK;
+}
+
+// The fixed partials array of each device, looked up once per device (with
+// that device current) by the first fgb_residual_norms_noalloc call on it.
+static constexpr int kMaxDevices = 64;
+static std::mutex g_partials_mu;
+static double* g_partials[kMaxDevices] = {};
+
+int fgb_residual_norms_noalloc(fgb_solver* s, int zone, double* out_dev) {
+  int rc = check_zone(s, zone);
+  if (rc) return rc;
+  if (!out_dev) return fail(FGB_ERR_ARG, "null output pointer");
+  if (s->device < 0 || s->device >= kMaxDevices) return fail(FGB_ERR_ARG, "device index out of range");
+  ZoneData& Z = s->zones[zone];
+  const int neq = Z.z.neq;
+  const int64_t nblocks = Z.ijkv_lu[0] * Z.ijkv_lu[1] * Z.ijkv_lu[2];
+  if (nblocks * 2 * neq > FGB_NORM_PARTIALS_MAX)
+    return fail(FGB_ERR_ARG, "zone has too many LU blocks for the fixed norm scratch "
+                             "(2 * neq * blocks > FGB_NORM_PARTIALS_MAX)");
+  CK(cudaSetDevice(s->device));
+  cudaPointerAttributes pa{};
+  CK(cudaPointerGetAttributes(&pa, out_dev));
+  if ((pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged) || pa.device != s->device)
+    return fail(FGB_ERR_ARG, "out_dev is not device memory of the solver's device");
+  double* part = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_partials_mu);
+    if (!g_partials[s->device]) {
+      double* p = nullptr;
+      CK(norm_partials_address(&p));
+      g_partials[s->device] = p;
+    }
+    part = g_partials[s->device];
+  }
+  NormArgs na{};
+  na.drodm = Z.drodm; na.rdm = part; na.nssiter = 1; na.it_bloc = 1; na.neq = neq;
+  for (int d = 0; d < 3; d++) { na.ijkv_lu[d] = Z.ijkv_lu[d]; na.size[d] = Z.pi[SIZE_SSDOM + d]; }
+  CK(launch_norms(Z.z, na, s->st));
+  const double xpt_1 = 1. / (double)(Z.z.ni * Z.z.nj * Z.z.nk);
+  CK(launch_norms_finish(part, nblocks, neq, xpt_1, Z.pr[DTC], out_dev, s->st));
+  s->launches += 2;
   return FGB_OK;
 }
 

@@ -14,6 +14,7 @@
 // The residual norms replace FastS/FastS/Compute/cprdu3s1_incl.for: one CTA
 // per LU block reduces sum(drodm^2) and max|drodm| per equation with warp
 // shuffles.
+#include "../../include/fast_gb300.h"
 #include "fgb_kernels.cuh"
 
 namespace fgb {
@@ -128,6 +129,44 @@ __global__ void __launch_bounds__(256) block_norms(Zone z, NormArgs a) {
 cudaError_t launch_norms(const Zone& z, const NormArgs& a, cudaStream_t st) {
   unsigned nb = (unsigned)(a.ijkv_lu[0] * a.ijkv_lu[1] * a.ijkv_lu[2]);
   block_norms<<<nb, 256, 0, st>>>(z, a);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------- norms into a fixed scratch
+// fgb_residual_norms_noalloc keeps its per-block partials here instead of in
+// an allocation: a module global, so one array per device, created with the
+// library's device image.  Slots [no * 2 * neq, (no + 1) * 2 * neq) belong to
+// LU block no; block_norms writes all of them before norms_finish reads them,
+// so nothing has to start at zero.
+static __device__ __align__(256) double g_norm_partials[FGB_NORM_PARTIALS_MAX];
+
+cudaError_t norm_partials_address(double** p) {
+  return cudaGetSymbolAddress((void**)p, g_norm_partials);
+}
+
+// Sum (L2^2) and maximum (Loo) of the partials over the blocks, in block
+// order, then the scaling of display_ss_iteration.cpp:112-145: one thread
+// per equation, the same operations in the same order as fgb_residuals'
+// host loop.
+__global__ void __launch_bounds__(32) norms_finish(const double* __restrict__ part, int64_t nblocks,
+                                                   int neq, double xpt_1, double dtc,
+                                                   double* __restrict__ out) {
+  const int ne = threadIdx.x;
+  if (ne >= neq) return;
+  double rmoy = 0., rmax = 0.;
+  for (int64_t no = 0; no < nblocks; no++) {
+    const double* q = part + no * 2 * neq;
+    const double m = q[neq + ne];
+    rmax = rmax < m ? m : rmax;
+    rmoy = rmoy + q[ne];
+  }
+  out[ne] = sqrt(rmoy * xpt_1) / dtc;
+  out[neq + ne] = rmax / dtc;
+}
+
+cudaError_t launch_norms_finish(const double* part, int64_t nblocks, int neq, double xpt_1,
+                                double dtc, double* out, cudaStream_t st) {
+  norms_finish<<<1, 32, 0, st>>>(part, nblocks, neq, xpt_1, dtc, out);
   return cudaGetLastError();
 }
 

@@ -79,6 +79,9 @@ cudaError_t launch_coins(double* q, int64_t nd, const int32_t* dst, const int32_
                          const int32_t* b, const int32_t* c, int64_t n_edge, int64_t n, int neq,
                          cudaStream_t st);
 cudaError_t launch_norms(const Zone& z, const NormArgs& a, cudaStream_t st);
+cudaError_t norm_partials_address(double** p);   // the fixed partials array of this device
+cudaError_t launch_norms_finish(const double* part, int64_t nblocks, int neq, double xpt_1,
+                                double dtc, double* out, cudaStream_t st);
 cudaError_t run_fp64_probe(int nsm, int iters, double* out, cudaStream_t st);
 
 }  // namespace fgb

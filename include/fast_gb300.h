@@ -104,6 +104,41 @@ int fgb_apply_bc(fgb_solver* s, int level);
  * recorded); returns nit through *nit_out. */
 int fgb_residuals(fgb_solver* s, int zone, double* out, int64_t n, int* nit_out);
 
+/* Size, in doubles, of the fixed device array that holds the per-block
+ * partials of fgb_residual_norms_noalloc (256 KB): a zone qualifies when
+ * 2 * neq * (its number of LU blocks) <= FGB_NORM_PARTIALS_MAX, i.e. up to
+ * 3276 blocks of SIZE_SSDOM cells for neq = 5. */
+#define FGB_NORM_PARTIALS_MAX 32768
+
+/* Residual norms of a zone's current right-hand side, reduced on the device
+ * into the caller's device buffer, with no memory allocated:
+ *   out_dev[ne] = L2,  out_dev[neq + ne] = Loo   (ne < neq)
+ * with the LU-block decomposition, summation order and 1/DTC scaling of
+ * fgb_residuals, so on the same state the values equal the last column that
+ * entry reports.  out_dev: 2*neq doubles of device memory on the solver's
+ * device.  Asynchronous on the solver stream; fgb_synchronize waits for it.
+ *
+ * For callers that cannot allocate: a convergence monitor that runs between
+ * solves on a stream shared with other work (a device allocation or free can
+ * synchronize the whole device, and fgb_residuals also allocates host memory,
+ * copies the full block table back and waits for the stream), or a process
+ * that reserved all of its device memory up front.  No device memory and, on
+ * success, no host memory is allocated; the per-block partials go to one
+ * fixed array per device of FGB_NORM_PARTIALS_MAX doubles that is part of the
+ * library's device image.  Zones that need more are rejected with
+ * FGB_ERR_ARG.  Nothing in that array has to start at zero: each call writes
+ * every slot it reads.
+ *
+ * The first call on a device does a one-time set-up (it looks up the array's
+ * device address, which may load the library's device code); make that first
+ * call before any stream capture.  The array is shared by every solver on the
+ * device, so calls whose work can overlap in time (solvers on different
+ * streams, calls from several host threads) race on it: serialize them.
+ *
+ * No counterpart in the reference (its norms are reduced on the host, in
+ * display_ss_iteration.cpp). */
+int fgb_residual_norms_noalloc(fgb_solver* s, int zone, double* out_dev);
+
 /* Wait for the solver stream and report any kernel error. */
 int fgb_synchronize(fgb_solver* s);
 
