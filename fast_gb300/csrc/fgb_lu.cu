@@ -299,7 +299,7 @@ template <int D> struct DirT { static constexpr int value = D; };
 template <int TYP> struct Rec {
   static constexpr int NB = NBE<TYP>::n;
   static constexpr int COE1 = 0, DIAG = 1, COE5 = 2, COEN = 4, ST = 7, B = 12;
-  static constexpr int SIZE = ((B + 3 * NB) + 1) / 2 * 2;   // even: 16-byte records
+  static constexpr int SIZE = ((B + 3 * NB) + 3) / 4 * 4;   // whole 16-byte vectors in FP32 too
 };
 constexpr int DIO = 6;
 
@@ -346,42 +346,69 @@ __global__ void __launch_bounds__(256) lu_neighbours(Zone z, const uint32_t* __r
   }
 }
 
-// per-solve gather into plane-ordered records + B entries (fully parallel)
+// Record stores: whole 16-byte vectors, so that a thread fills its record
+// with SIZE/2 (FP64) or SIZE/4 (FP32) stores instead of SIZE scalar ones.
+template <int N>
+__device__ __forceinline__ void store_rec(double* dst, const double (&r)[N]) {
+  static_assert(N % 2 == 0, "FP64 records are whole double2 vectors");
+  double2* d = reinterpret_cast<double2*>(dst);
+#pragma unroll
+  for (int m = 0; m < N / 2; m++) d[m] = make_double2(r[2 * m], r[2 * m + 1]);
+}
+template <int N>
+__device__ __forceinline__ void store_rec(float* dst, const float (&r)[N]) {
+  static_assert(N % 4 == 0, "FP32 records are whole float4 vectors");
+  float4* d = reinterpret_cast<float4*>(dst);
+#pragma unroll
+  for (int m = 0; m < N / 4; m++) d[m] = make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+}
+__device__ __forceinline__ void store_dio(double* dst, const double (&x)[5]) {
+  double2* d = reinterpret_cast<double2*>(dst);   // DIO = 6 words: 48-byte slots
+  d[0] = make_double2(x[0], x[1]); d[1] = make_double2(x[2], x[3]); d[2] = make_double2(x[4], 0.);
+}
+__device__ __forceinline__ void store_dio(float* dst, const float (&x)[5]) {
+  float2* d = reinterpret_cast<float2*>(dst);     // 24-byte slots
+  d[0] = make_float2(x[0], x[1]); d[1] = make_float2(x[2], x[3]); d[2] = make_float2(x[4], 0.f);
+}
+
+// Per-solve gather into plane-ordered records + B entries (fully parallel).
+// Threads run in natural (i fastest) order, so the reads of din / coe / W^p
+// are coalesced; each thread then writes its own record (posmap[l]) with
+// vector stores.  Grid: (ceil(ni/128), nj, nk) x 128 threads.
 template <int TYP, typename T>
-__global__ void __launch_bounds__(256) lu_gather(Zone z, LuFields f, PlaneData<T> p) {
+__global__ void __launch_bounds__(128) lu_gather(Zone z, LuFields f, PlaneData<T> p) {
   using R = Rec<TYP>;
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= p.G) return;
-  int64_t ii, jj, kk;
-  unpack(p.cells[g], ii, jj, kk);
+  const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= z.ni) return;
+  const int64_t jj = blockIdx.y, kk = blockIdx.z;
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
   const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
   const int64_t nd = z.nd;
-  T* r = p.rec + g * R::SIZE;
-  T* io = p.dio + g * DIO;
+  const int64_t g = f.posmap[l];
+  T x[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) io[v] = T(f.din[l + v * nd]);
+  for (int v = 0; v < 5; v++) x[v] = T(f.din[l + v * nd]);
+  store_dio(p.dio + g * DIO, x);
+  T r[R::SIZE];
   const T c5 = T(f.coe[l + 4 * nd]);
   r[R::COE1] = T(f.coe[l]);
   r[R::DIAG] = T(1.) / c5;
   r[R::COE5] = c5;
+  r[3] = T(0);
 #pragma unroll
   for (int d = 0; d < 3; d++) r[R::COEN + d] = T(f.coe[l + (d + 1) * nd]);
-  T w5[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) {
-    w5[v] = T(f.rop_old[l + v * nd]);
-    r[R::ST + v] = w5[v];
-  }
-  T e[R::NB];
+  for (int v = 0; v < 5; v++) r[R::ST + v] = T(f.rop_old[l + v * nd]);
+#pragma unroll
+  for (int m = R::B; m < R::SIZE; m++) r[m] = T(0);   // padding and unused entries
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     T tx, ty, tz;
     nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
-    bentries<TYP, T>(z, d, w5[1], w5[2], w5[3], w5[4], tx, ty, tz, e);
-#pragma unroll
-    for (int m = 0; m < R::NB; m++) r[R::B + d * R::NB + m] = e[m];
+    bentries<TYP, T>(z, d, r[R::ST + 1], r[R::ST + 2], r[R::ST + 3], r[R::ST + 4], tx, ty, tz,
+                     r + R::B + d * R::NB);
   }
+  store_rec(p.rec + g * R::SIZE, r);
 }
 
 // ---------------------------------------------------------------- cells
@@ -603,7 +630,8 @@ template <int TYP, typename T>
 static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>& p,
                             const LuLaunch& L, cudaStream_t st) {
   const unsigned gc = (unsigned)((p.G + 255) / 256);
-  lu_gather<TYP, T><<<gc, 256, 0, st>>>(z, f, p);
+  lu_gather<TYP, T><<<dim3((unsigned)((z.ni + 127) / 128), (unsigned)z.nj, (unsigned)z.nk), 128, 0,
+                      st>>>(z, f, p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (L.persistent) {
