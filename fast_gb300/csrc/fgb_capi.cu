@@ -397,8 +397,9 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   if (rc != FGB_OK) return rc;
   if (p[ITYPCP] <= 1) {
     // LU-SGS: cells ordered by hyperplane i+j+k (counting sort), B table
-    if (ni >= 2048 || nj >= 2048 || nk >= 1024)
-      return fail(FGB_ERR_ARG, "zone too large for the LU plane table (ni,nj < 2048, nk < 1024)");
+    if (ni >= 2048 || nj >= 2048 || nk >= 1024 || ni * nj * nk >= (int64_t(1) << 31))
+      return fail(FGB_ERR_ARG, "zone too large for the LU plane table "
+                               "(ni,nj < 2048, nk < 1024, ni*nj*nk < 2^31)");
     const int64_t np = ni + nj + nk - 2;
     std::vector<int64_t> off(np + 1, 0);
     for (int64_t k = 0; k < nk; k++)

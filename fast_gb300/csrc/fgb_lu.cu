@@ -372,43 +372,93 @@ __device__ __forceinline__ void store_dio(float* dst, const float (&x)[5]) {
 }
 
 // Per-solve gather into plane-ordered records + B entries (fully parallel).
-// Threads run in natural (i fastest) order, so the reads of din / coe / W^p
-// are coalesced; each thread then writes its own record (posmap[l]) with
-// vector stores.  Grid: (ceil(ni/128), nj, nk) x 128 threads.
+// A CTA takes a tile of GT_I x GT_J cells (i, j) at one k.  Reads of
+// din / coe / W^p run along i (coalesced).  In the plane table, cells of
+// one plane and one k follow each other by increasing j, so the cells of a
+// tile anti-diagonal (i + j constant) have consecutive plane indices: the
+// CTA stages its records in shared memory ordered by anti-diagonal and then
+// writes each anti-diagonal as one contiguous span of records.
+constexpr int GT_I = 16, GT_J = 8, GT_N = GT_I * GT_J;
+
 template <int TYP, typename T>
-__global__ void __launch_bounds__(128) lu_gather(Zone z, LuFields f, PlaneData<T> p) {
+struct GatherSmem {
+  static constexpr int CH = Rec<TYP>::SIZE * (int)sizeof(T) / 16;   // 16-byte chunks per record
+  static constexpr int STRIDE = (CH | 1) * (16 / (int)sizeof(T));   // odd chunk stride: no bank conflicts
+  static constexpr size_t bytes = sizeof(T) * (size_t)GT_N * (STRIDE + DIO) + 4 * GT_N;
+};
+
+// slot of tile cell (ti, tj): anti-diagonal a = ti + tj first, then tj
+__device__ __forceinline__ int tile_slot(int ti, int tj) {
+  const int a = ti + tj;
+  int q = 0;
+  for (int b = 0; b < a; b++) q += min(min(b + 1, GT_J), GT_I + GT_J - 1 - b);
+  return q + tj - max(0, a - (GT_I - 1));
+}
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { using t = double2; };
+template <> struct Vec2<float> { using t = float2; };
+
+template <int TYP, typename T>
+__global__ void __launch_bounds__(GT_N) lu_gather(Zone z, LuFields f, PlaneData<T> p) {
   using R = Rec<TYP>;
-  const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (ii >= z.ni) return;
-  const int64_t jj = blockIdx.y, kk = blockIdx.z;
-  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
-  const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
-  const int64_t nd = z.nd;
-  const int64_t g = f.posmap[l];
-  T x[5];
+  using S = GatherSmem<TYP, T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* s_rec = reinterpret_cast<T*>(smem);
+  T* s_dio = s_rec + GT_N * S::STRIDE;
+  int32_t* s_g = reinterpret_cast<int32_t*>(s_dio + GT_N * DIO);
+  const int ti = threadIdx.x % GT_I, tj = threadIdx.x / GT_I;
+  const int64_t ii = (int64_t)blockIdx.x * GT_I + ti, jj = (int64_t)blockIdx.y * GT_J + tj;
+  const int64_t kk = blockIdx.z;
+  const int q = tile_slot(ti, tj);
+  if (ii < z.ni && jj < z.nj) {
+    const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
+    const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
+    const int64_t nd = z.nd;
+    T x[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = T(f.din[l + v * nd]);
-  store_dio(p.dio + g * DIO, x);
-  T r[R::SIZE];
-  const T c5 = T(f.coe[l + 4 * nd]);
-  r[R::COE1] = T(f.coe[l]);
-  r[R::DIAG] = T(1.) / c5;
-  r[R::COE5] = c5;
-  r[3] = T(0);
+    for (int v = 0; v < 5; v++) x[v] = T(f.din[l + v * nd]);
+    T r[R::SIZE];
+    const T c5 = T(f.coe[l + 4 * nd]);
+    r[R::COE1] = T(f.coe[l]);
+    r[R::DIAG] = T(1.) / c5;
+    r[R::COE5] = c5;
+    r[3] = T(0);
 #pragma unroll
-  for (int d = 0; d < 3; d++) r[R::COEN + d] = T(f.coe[l + (d + 1) * nd]);
+    for (int d = 0; d < 3; d++) r[R::COEN + d] = T(f.coe[l + (d + 1) * nd]);
 #pragma unroll
-  for (int v = 0; v < 5; v++) r[R::ST + v] = T(f.rop_old[l + v * nd]);
+    for (int v = 0; v < 5; v++) r[R::ST + v] = T(f.rop_old[l + v * nd]);
 #pragma unroll
-  for (int m = R::B; m < R::SIZE; m++) r[m] = T(0);   // padding and unused entries
+    for (int m = R::B; m < R::SIZE; m++) r[m] = T(0);   // padding and unused entries
 #pragma unroll
-  for (int d = 0; d < 3; d++) {
-    T tx, ty, tz;
-    nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
-    bentries<TYP, T>(z, d, r[R::ST + 1], r[R::ST + 2], r[R::ST + 3], r[R::ST + 4], tx, ty, tz,
-                     r + R::B + d * R::NB);
+    for (int d = 0; d < 3; d++) {
+      T tx, ty, tz;
+      nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
+      bentries<TYP, T>(z, d, r[R::ST + 1], r[R::ST + 2], r[R::ST + 3], r[R::ST + 4], tx, ty, tz,
+                       r + R::B + d * R::NB);
+    }
+    s_g[q] = f.posmap[l];
+    store_rec(s_rec + q * S::STRIDE, r);
+    store_dio(s_dio + q * DIO, x);
+  } else {
+    s_g[q] = -1;
   }
-  store_rec(p.rec + g * R::SIZE, r);
+  __syncthreads();
+  for (int c = threadIdx.x; c < GT_N * S::CH; c += GT_N) {
+    const int qq = c / S::CH, m = c - qq * S::CH;
+    const int32_t g = s_g[qq];
+    if (g < 0) continue;
+    reinterpret_cast<int4*>(p.rec + (int64_t)g * R::SIZE)[m] =
+        reinterpret_cast<const int4*>(s_rec + qq * S::STRIDE)[m];
+  }
+  using V2 = typename Vec2<T>::t;
+  for (int c = threadIdx.x; c < GT_N * (DIO / 2); c += GT_N) {
+    const int qq = c / (DIO / 2), m = c - qq * (DIO / 2);
+    const int32_t g = s_g[qq];
+    if (g < 0) continue;
+    reinterpret_cast<V2*>(p.dio + (int64_t)g * DIO)[m] =
+        reinterpret_cast<const V2*>(s_dio + qq * DIO)[m];
+  }
 }
 
 // ---------------------------------------------------------------- cells
@@ -630,8 +680,19 @@ template <int TYP, typename T>
 static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>& p,
                             const LuLaunch& L, cudaStream_t st) {
   const unsigned gc = (unsigned)((p.G + 255) / 256);
-  lu_gather<TYP, T><<<dim3((unsigned)((z.ni + 127) / 128), (unsigned)z.nj, (unsigned)z.nk), 128, 0,
-                      st>>>(z, f, p);
+  using S = GatherSmem<TYP, T>;
+  static bool smem_set[64] = {};   // per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!smem_set[dev]) {
+    cudaError_t e0 = cudaFuncSetAttribute(lu_gather<TYP, T>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes);
+    if (e0 != cudaSuccess) return e0;
+    smem_set[dev] = true;
+  }
+  lu_gather<TYP, T><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I), (unsigned)((z.nj + GT_J - 1) / GT_J),
+                       (unsigned)z.nk), GT_N, S::bytes, st>>>(z, f, p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (L.persistent) {
