@@ -585,38 +585,55 @@ __device__ __forceinline__ void upper_cell(const Zone& z, const PlaneData<T>& p,
 }
 
 // ------------------------------------------------------- grid barrier
-// Cooperative launch guarantees that every CTA is resident.  The wait is
-// bounded: past ~1 s it sets the error word, leaves the barrier and the
-// kernel returns; the host reports FGB_ERR_DEVICE.
-struct GridBar { unsigned int* count; unsigned int* gen; int* err; };
+// Cooperative launch guarantees that every CTA is resident.  One monotone
+// counter per launch (zeroed before it): round r is complete when the
+// counter reaches (r + 1) * gridDim.x.  Arrive (after the CTA's writes) is a
+// release add by thread 0; wait is an acquire poll by thread 0 followed by a
+// CTA barrier, so the CTA can do independent work in between.  The wait is
+// bounded: past 2^24 polls it sets the error word and the kernel returns;
+// the host reports FGB_ERR_DEVICE.
+struct GridBar { unsigned int* count; int* err; };
 
-__device__ __forceinline__ bool grid_sync(const GridBar& g, unsigned int nblocks,
-                                          unsigned int& my_gen) {
+__device__ __forceinline__ void bar_arrive(const GridBar& g) {
   __syncthreads();
+  if (threadIdx.x == 0)
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(g.count), "r"(1u) : "memory");
+}
+
+__device__ __forceinline__ bool bar_wait(const GridBar& g, unsigned int target) {
   if (threadIdx.x == 0) {
-    const unsigned int target = my_gen + 1;
-    __threadfence();
-    unsigned int arrived = atomicAdd(g.count, 1u);
-    if (arrived == nblocks - 1) {
-      atomicExch(g.count, 0u);
-      __threadfence();
-      atomicExch(g.gen, target);
-    } else {
-      long long spins = 0;
-      while (true) {
-        unsigned int cur;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(g.gen) : "memory");
-        if (cur == target) break;
+    long long spins = 0;
+    while (true) {
+      unsigned int cur;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(g.count) : "memory");
+      if ((int)(cur - target) >= 0) break;
+      if ((++spins & 63) == 0) {
         if (*(volatile int*)g.err) break;
-        if (++spins > (1ll << 24)) { atomicExch(g.err, 1); break; }
-        __nanosleep(20);
+        if (spins > (1ll << 24)) { atomicExch(g.err, 1); break; }
       }
     }
-    __threadfence();
-    my_gen = target;
   }
   __syncthreads();
   return *(volatile int*)g.err == 0;
+}
+
+// L2 prefetch of everything plane s keeps in plane order (records,
+// increments, neighbour tables): contiguous spans, spread over the grid.
+__device__ __forceinline__ void prefetch_span_l2(const void* base, int64_t bytes) {
+  const char* b = static_cast<const char*>(base);
+  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t o = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 128; o < bytes; o += nt * 128)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(b + o));
+}
+
+template <int TYP, typename T>
+__device__ __forceinline__ void prefetch_plane(const PlaneData<T>& p, int64_t s, bool upper) {
+  const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
+  prefetch_span_l2(p.rec + c0 * Rec<TYP>::SIZE, n * Rec<TYP>::SIZE * (int64_t)sizeof(T));
+  prefetch_span_l2(p.dio + c0 * DIO, n * DIO * (int64_t)sizeof(T));
+  const int32_t* nb = upper ? p.nbu : p.nbl;
+#pragma unroll
+  for (int d = 0; d < 3; d++) prefetch_span_l2(nb + d * p.G + c0, n * 4);
 }
 
 // cells of plane s spread over every CTA: cell c of the plane goes to CTA
@@ -636,14 +653,21 @@ template <int TYP, typename T>
 __global__ void __launch_bounds__(512) lusgs_persistent(Zone z, PlaneData<T> p, LuFields f,
                                                         GridBar gb) {
   const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
-  unsigned int my_gen = 0;
-  for (int64_t s = 0; s <= smax; s++) {   // lower sweep, ascending hyperplanes
-    do_plane<TYP, T, false>(z, p, f, s);
-    if (!grid_sync(gb, gridDim.x, my_gen)) return;
-  }
-  for (int64_t s = smax; s >= 0; s--) {   // upper sweep
-    do_plane<TYP, T, true>(z, p, f, s);
-    if (s > 0 && !grid_sync(gb, gridDim.x, my_gen)) return;
+  // traversal step t: lower planes 0..smax, then upper planes smax..0
+  auto plane_of = [&](int64_t t) { return t <= smax ? t : 2 * smax + 1 - t; };
+  const int64_t nsteps = 2 * smax + 2;
+  prefetch_plane<TYP, T>(p, 0, false);
+  if (nsteps > 1) prefetch_plane<TYP, T>(p, plane_of(1), 1 > smax);
+  unsigned int round = 0;
+  for (int64_t t = 0; t < nsteps; t++) {
+    const int64_t s = plane_of(t);
+    if (t <= smax) do_plane<TYP, T, false>(z, p, f, s);
+    else do_plane<TYP, T, true>(z, p, f, s);
+    if (t == nsteps - 1) break;
+    bar_arrive(gb);
+    if (t + 2 < nsteps) prefetch_plane<TYP, T>(p, plane_of(t + 2), t + 2 > smax);
+    round++;
+    if (!bar_wait(gb, round * gridDim.x)) return;
   }
 }
 
@@ -705,9 +729,9 @@ static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T>, 512, 0);
       grid = nsm * (per > 0 ? per : 1);
     }
-    e = cudaMemsetAsync(L.bar, 0, 2 * sizeof(unsigned int), st);
+    e = cudaMemsetAsync(L.bar, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
-    GridBar gb{L.bar, L.bar + 1, L.err};
+    GridBar gb{L.bar, L.err};
     void* args[] = {(void*)&z, (void*)&p, (void*)&f, (void*)&gb};
     e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(512), args,
                                     0, st);
