@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--ttc", action="store_true",
                    help="time to a 1e-10 Newton residual drop, FP64 vs mixed sweeps")
     p.add_argument("--ttc-n", type=int, default=256)
-    p.add_argument("--ttc-max", type=int, default=80, help="max sub-iterations per step")
+    p.add_argument("--ttc-max", type=int, default=100, help="max sub-iterations per step")
     p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
                    help="64: plain FP64 path; 32: FP32 LU-SGS sweeps (mixed precision)")
     return p.parse_args()
@@ -325,8 +325,11 @@ def run_ttc(args):
     One BDF2 step (after one BDF1 step) of the 256^3 Taylor-Green case with
     up to --ttc-max LU-SGS sub-iterations, residual norms (FP64, computed by
     the GPU as cprdu3s1 does) recorded at every sub-iteration.  The drop is
-    the max over the 5 equations of L2(k)/L2(1); time = sub-iterations to
-    reach 1e-10 x measured time per sub-iteration.  FP64 sweeps vs FP32
+    that of the system residual, sqrt(sum_e L2_e(k)^2) / sqrt(sum_e L2_e(1)^2)
+    over the 5 equations (the w-momentum residual of the Taylor-Green vortex
+    starts at round-off level, so a per-equation maximum can never reach
+    1e-10; the per-equation drops are reported as well); time = sub-iterations
+    to reach 1e-10 x measured time per sub-iteration.  FP64 sweeps vs FP32
     sweeps (the residual, the update and the norms stay FP64)."""
     from fast_gb300 import cases, fasts
     import numpy as np
@@ -345,7 +348,9 @@ def run_ttc(args):
         ms = s.timer_stop()
         r = s.residuals(0)                     # (2*neq, nit)
         l2 = r[:5]
-        drop = np.max(l2 / l2[:, :1], axis=0)
+        tot = np.sqrt(np.sum(l2 * l2, axis=0))
+        drop = tot / tot[0]
+        per_eq = l2 / np.where(l2[:, :1] > 0, l2[:, :1], 1.0)
         nit = l2.shape[1]
         ms_it = ms / nit
         hit = np.nonzero(drop <= 1e-10)[0]
@@ -354,6 +359,8 @@ def run_ttc(args):
         out[prec] = {"sub_iterations_to_1e-10": k, "ms_per_sub_iteration": ms_it,
                      "time_to_1e-10_ms": (k * ms_it) if k else None,
                      "best_drop": float(drop.min()), "drop_history": [float(x) for x in drop],
+                     "initial_l2_per_equation": [float(x) for x in l2[:, 0]],
+                     "final_drop_per_equation": [float(x) for x in per_eq[:, -1]],
                      "final_state_checksum": None}
         from fast_gb300 import fastc, pytree as I
         z = I.getZones(t)[0]

@@ -296,10 +296,14 @@ template <int D> struct DirT { static constexpr int value = D; };
 //   rec[g] : coe1, 1/coe5, coe5, -, coe_{2..4}, W^p (5), B entries (3 x NB)
 //   dio[g] : residual in / increment out (5 words, stride 6)
 //   nst[g] : in-place upper sweep: W^{p+1} u, v, w, T (stride 4)
-template <int TYP> struct Rec {
+template <int TYP, typename T> struct Rec {
+  // FP32 sweeps in cartesian zones rebuild B from the neighbour's state
+  // instead of reading a stored table: the same float arithmetic on the same
+  // float inputs as the pre-pass, so the same values, in 12 words a cell.
+  static constexpr bool HAS_B = !(TYP == Z3DCART && sizeof(T) == 4);
   static constexpr int NB = NBE<TYP>::n;
   static constexpr int COE1 = 0, DIAG = 1, COE5 = 2, COEN = 4, ST = 7, B = 12;
-  static constexpr int SIZE = ((B + 3 * NB) + 3) / 4 * 4;   // whole 16-byte vectors in FP32 too
+  static constexpr int SIZE = HAS_B ? ((B + 3 * NB) + 3) / 4 * 4 : B;   // whole 16-byte vectors
 };
 constexpr int DIO = 6;
 
@@ -382,7 +386,7 @@ constexpr int GT_I = 16, GT_J = 8, GT_N = GT_I * GT_J;
 
 template <int TYP, typename T>
 struct GatherSmem {
-  static constexpr int CH = Rec<TYP>::SIZE * (int)sizeof(T) / 16;   // 16-byte chunks per record
+  static constexpr int CH = Rec<TYP, T>::SIZE * (int)sizeof(T) / 16;   // 16-byte chunks per record
   static constexpr int STRIDE = (CH | 1) * (16 / (int)sizeof(T));   // odd chunk stride: no bank conflicts
   static constexpr size_t bytes = sizeof(T) * (size_t)GT_N * (STRIDE + DIO) + 4 * GT_N;
 };
@@ -401,7 +405,7 @@ template <> struct Vec2<float> { using t = float2; };
 
 template <int TYP, typename T>
 __global__ void __launch_bounds__(GT_N) lu_gather(Zone z, LuFields f, PlaneData<T> p) {
-  using R = Rec<TYP>;
+  using R = Rec<TYP, T>;
   using S = GatherSmem<TYP, T>;
   extern __shared__ __align__(16) unsigned char smem[];
   T* s_rec = reinterpret_cast<T*>(smem);
@@ -430,12 +434,14 @@ __global__ void __launch_bounds__(GT_N) lu_gather(Zone z, LuFields f, PlaneData<
     for (int v = 0; v < 5; v++) r[R::ST + v] = T(f.rop_old[l + v * nd]);
 #pragma unroll
     for (int m = R::B; m < R::SIZE; m++) r[m] = T(0);   // padding and unused entries
+    if (R::HAS_B) {
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      T tx, ty, tz;
-      nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
-      bentries<TYP, T>(z, d, r[R::ST + 1], r[R::ST + 2], r[R::ST + 3], r[R::ST + 4], tx, ty, tz,
-                       r + R::B + d * R::NB);
+      for (int d = 0; d < 3; d++) {
+        T tx, ty, tz;
+        nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
+        bentries<TYP, T>(z, d, r[R::ST + 1], r[R::ST + 2], r[R::ST + 3], r[R::ST + 4], tx, ty, tz,
+                         r + R::B + d * R::NB);
+      }
     }
     s_g[q] = f.posmap[l];
     store_rec(s_rec + q * S::STRIDE, r);
@@ -471,40 +477,6 @@ __device__ __forceinline__ void load_dio(const T* __restrict__ dio, int64_t g, T
   for (int v = 0; v < 5; v++) o[v] = __ldcg(q + v);
 }
 
-template <int TYP, typename T>
-__device__ __forceinline__ void lower_cell(const Zone& z, const PlaneData<T>& p, int64_t g) {
-  using R = Rec<TYP>;
-  constexpr int NB = R::NB;
-  const int64_t G = p.G;
-  const T* me = p.rec + g * R::SIZE;
-  const T xal = me[R::COE1] * T(0.5);
-  T x[5], o[5], b[5];
-  load_dio(p.dio, g, x);
-  auto term = [&](auto dc) {
-    constexpr int D = decltype(dc)::value;
-    const int32_t n = p.nbl[D * G + g];
-    if (n < 0) return;
-    load_dio(p.dio, n, o);
-    const T* rn = p.rec + (int64_t)n * R::SIZE;
-    T cs = rn[R::COEN + D] * T(0.5);
-    bmatvec<TYP, D, T>(z, rn + R::B + D * NB, cs, o, b);
-#pragma unroll
-    for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
-  };
-  if (TYP == Z3DCART) {  // invlu_l.for cartesian section: j, then k, then i
-    term(DirT<1>{});
-    term(DirT<2>{});
-  } else {               // general section: k, then j, then i
-    term(DirT<2>{});
-    term(DirT<1>{});
-  }
-  term(DirT<0>{});
-  const T diag = me[R::DIAG];
-  T* io = p.dio + g * DIO;
-#pragma unroll
-  for (int v = 0; v < 5; v++) io[v] = x[v] * diag;
-}
-
 // mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW) in precision T
 template <typename T>
 __device__ __forceinline__ void newton(T cv, T ro, T u, T v, T w, T tt, const T d[5], T n[5]) {
@@ -518,27 +490,76 @@ __device__ __forceinline__ void newton(T cv, T ro, T u, T v, T w, T tt, const T 
   n[4] = (roe_old + d[4]) * r_1 * cvinv - cvinv2 * (n[1] * n[1] + n[2] * n[2] + n[3] * n[3]);
 }
 
+// ------------------------------------------------------------ cell operands
+// Everything a cell of a sweep reads except what the previous hyperplane
+// produces (the neighbours' increments and, in place, the k+1 neighbour's
+// new state).  FP32 sweeps load these for the next cell between arriving at
+// the grid barrier and waiting on it, so only the increments' loads stay
+// between two hyperplanes; without a stored B table (FP32, cartesian) the
+// neighbours' states are held instead (3 x 4 values).
 template <int TYP, typename T>
-__device__ __forceinline__ void upper_cell(const Zone& z, const PlaneData<T>& p,
-                                           const LuFields& f, int64_t g) {
-  using R = Rec<TYP>;
-  constexpr int NB = R::NB;
-  const int64_t G = p.G;
+struct CellOps {
+  static constexpr bool HOLD_W = !Rec<TYP, T>::HAS_B;
+  static constexpr int NW = HOLD_W ? 4 : 1;
+  int32_t n[3];   // neighbour plane indices (-1: none)
+  T x[5];         // lower: residual; upper: lower result x coe5 (lu_d.for)
+  T xal, diag;
+  T cs[3];        // coe_{d+2}(neighbour) x (+-1/2)
+  T wn[3][NW];    // neighbours' u, v, w, T (no stored B table)
+  T st[5];        // upper: W^p of the cell (in-place Newton)
+};
+
+template <int TYP, typename T, bool UPPER>
+__device__ __forceinline__ void load_ops(const PlaneData<T>& p, bool inplace, int64_t g,
+                                         CellOps<TYP, T>& o) {
+  using R = Rec<TYP, T>;
   const T* me = p.rec + g * R::SIZE;
-  const T xal = me[R::COE1] * T(-0.5);
-  const T dg = me[R::COE5];
-  T x[5], o[5], b[5], e[NB];
-  load_dio(p.dio, g, x);
+  const int32_t* nbt = UPPER ? p.nbu : p.nbl;
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = x[v] * dg;  // lu_d.for
+  for (int d = 0; d < 3; d++) o.n[d] = nbt[d * p.G + g];
+  load_dio(p.dio, g, o.x);
+  if (UPPER) {
+    const T dg = me[R::COE5];
+#pragma unroll
+    for (int v = 0; v < 5; v++) o.x[v] = o.x[v] * dg;
+    o.xal = me[R::COE1] * T(-0.5);
+#pragma unroll
+    for (int v = 0; v < 5; v++) o.st[v] = me[R::ST + v];
+  } else {
+    o.xal = me[R::COE1] * T(0.5);
+  }
+  o.diag = me[R::DIAG];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (o.n[d] < 0) continue;
+    const T* rn = p.rec + (int64_t)o.n[d] * R::SIZE;
+    o.cs[d] = rn[R::COEN + d] * T(UPPER ? -0.5 : 0.5);
+    if (CellOps<TYP, T>::HOLD_W && !(UPPER && d == 2 && inplace)) {
+#pragma unroll
+      for (int m = 0; m < CellOps<TYP, T>::NW; m++) o.wn[d][m] = rn[R::ST + 1 + m];
+    }
+  }
+}
+
+// invlu_l.for / invlu_u.for for one cell: out = (x + sum_d B_d(nb).out_nb *
+// (+-coe1/2)) / coe5 in the reference's direction order; in place (upper
+// sweep of a sub-iteration that updates W^{p+1} over W^p) the k+1 term uses
+// the neighbour's new state and the cell's own Newton update follows.
+template <int TYP, typename T, bool UPPER>
+__device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, const LuFields& f,
+                                         int64_t g, const CellOps<TYP, T>& o) {
+  using R = Rec<TYP, T>;
+  constexpr int NB = R::NB;
+  T x[5], od[5], b[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) x[v] = o.x[v];
   auto term = [&](auto dc, bool fresh) {
     constexpr int D = decltype(dc)::value;
-    const int32_t n = p.nbu[D * G + g];
+    const int32_t n = o.n[D];
     if (n < 0) return;
-    load_dio(p.dio, n, o);
-    const T* rn = p.rec + (int64_t)n * R::SIZE;
-    T cs = rn[R::COEN + D] * T(-0.5);
+    load_dio(p.dio, n, od);
     if (fresh) {  // k+1 neighbour updated in place: B from its new state
+      T e[NB];
       const T* q = p.nst + (int64_t)n * 4;
       T u = __ldcg(q), vv = __ldcg(q + 1), w = __ldcg(q + 2), t = __ldcg(q + 3);
       T tx, ty, tz;
@@ -551,27 +572,43 @@ __device__ __forceinline__ void upper_cell(const Zone& z, const PlaneData<T>& p,
         nb_normal<TYP, T>(z, D, lt, lt + z.minc[D], tx, ty, tz);
       }
       bentries<TYP, T>(z, D, u, vv, w, t, tx, ty, tz, e);
-      bmatvec<TYP, D, T>(z, e, cs, o, b);
+      bmatvec<TYP, D, T>(z, e, o.cs[D], od, b);
+    } else if (CellOps<TYP, T>::HOLD_W) {  // cartesian: B from the held state
+      T e[NB];
+      T tx, ty, tz;
+      nb_normal<TYP, T>(z, D, 0, 0, tx, ty, tz);
+      bentries<TYP, T>(z, D, o.wn[D][0], o.wn[D][CellOps<TYP, T>::NW > 1 ? 1 : 0],
+                       o.wn[D][CellOps<TYP, T>::NW > 2 ? 2 : 0], o.wn[D][CellOps<TYP, T>::NW > 3 ? 3 : 0],
+                       tx, ty, tz, e);
+      bmatvec<TYP, D, T>(z, e, o.cs[D], od, b);
     } else {
-      bmatvec<TYP, D, T>(z, rn + R::B + D * NB, cs, o, b);
+      bmatvec<TYP, D, T>(z, p.rec + (int64_t)n * R::SIZE + R::B + D * NB, o.cs[D], od, b);
     }
 #pragma unroll
-    for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * xal;
+    for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * o.xal;
   };
-  term(DirT<2>{}, f.inplace != 0);
-  term(DirT<1>{}, false);
-  term(DirT<0>{}, false);
-  const T diag = me[R::DIAG];
+  if (UPPER) {                 // invlu_u.for: k, then j, then i
+    term(DirT<2>{}, f.inplace != 0);
+    term(DirT<1>{}, false);
+    term(DirT<0>{}, false);
+  } else if (TYP == Z3DCART) { // invlu_l.for cartesian section: j, then k, then i
+    term(DirT<1>{}, false);
+    term(DirT<2>{}, false);
+    term(DirT<0>{}, false);
+  } else {                     // general section: k, then j, then i
+    term(DirT<2>{}, false);
+    term(DirT<1>{}, false);
+    term(DirT<0>{}, false);
+  }
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = x[v] * diag;
+  for (int v = 0; v < 5; v++) x[v] = x[v] * o.diag;
   T* io = p.dio + g * DIO;
 #pragma unroll
   for (int v = 0; v < 5; v++) io[v] = x[v];
-  if (!f.inplace) return;  // the Newton update runs after the sweep
+  if (!UPPER || !f.inplace) return;  // otherwise the Newton update runs after the sweep
   // in place: the k-1 neighbour needs this cell's new state in the next plane
   T nw[5];
-  newton<T>(T(z.cv), me[R::ST], me[R::ST + 1], me[R::ST + 2], me[R::ST + 3], me[R::ST + 4], x,
-            nw);
+  newton<T>(T(z.cv), o.st[0], o.st[1], o.st[2], o.st[3], o.st[4], x, nw);
   T* q = p.nst + g * 4;
 #pragma unroll
   for (int v = 0; v < 4; v++) q[v] = nw[v + 1];
@@ -588,8 +625,10 @@ __device__ __forceinline__ void upper_cell(const Zone& z, const PlaneData<T>& p,
 // Cooperative launch guarantees that every CTA is resident.  One monotone
 // counter per launch (zeroed before it): round r is complete when the
 // counter reaches (r + 1) * gridDim.x.  Arrive (after the CTA's writes) is a
-// release add by thread 0; wait is an acquire poll by thread 0 followed by a
-// CTA barrier, so the CTA can do independent work in between.  The wait is
+// release add by thread 0; wait is an acquire poll by the CTA's last thread
+// (the one least likely to own a cell of the next plane, so its poll does
+// not queue behind operand loads) followed by a CTA barrier, so the CTA can
+// do independent work in between.  The wait is
 // bounded: past 2^24 polls it sets the error word and the kernel returns;
 // the host reports FGB_ERR_DEVICE.
 struct GridBar { unsigned int* count; int* err; };
@@ -601,7 +640,7 @@ __device__ __forceinline__ void bar_arrive(const GridBar& g) {
 }
 
 __device__ __forceinline__ bool bar_wait(const GridBar& g, unsigned int target) {
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == blockDim.x - 1) {
     long long spins = 0;
     while (true) {
       unsigned int cur;
@@ -629,43 +668,67 @@ __device__ __forceinline__ void prefetch_span_l2(const void* base, int64_t bytes
 template <int TYP, typename T>
 __device__ __forceinline__ void prefetch_plane(const PlaneData<T>& p, int64_t s, bool upper) {
   const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
-  prefetch_span_l2(p.rec + c0 * Rec<TYP>::SIZE, n * Rec<TYP>::SIZE * (int64_t)sizeof(T));
+  prefetch_span_l2(p.rec + c0 * Rec<TYP, T>::SIZE, n * Rec<TYP, T>::SIZE * (int64_t)sizeof(T));
   prefetch_span_l2(p.dio + c0 * DIO, n * DIO * (int64_t)sizeof(T));
   const int32_t* nb = upper ? p.nbu : p.nbl;
 #pragma unroll
   for (int d = 0; d < 3; d++) prefetch_span_l2(nb + d * p.G + c0, n * 4);
 }
 
-// cells of plane s spread over every CTA: cell c of the plane goes to CTA
-// c mod gridDim, so each CTA's share is packed into its first warps
-template <int TYP, typename T, bool UPPER>
+// Cells of plane s spread over every CTA: cell c of the plane goes to CTA
+// c mod gridDim, so each CTA's share is packed into its first warps.  With
+// PRE, a thread's first cell of the plane comes with its operands already
+// loaded (FP32 sweeps: they are latency-bound); FP64 sweeps, bound by the
+// FP64 pipe, load them here.
+template <int TYP, typename T, bool UPPER, bool PRE>
 __device__ __forceinline__ void do_plane(const Zone& z, const PlaneData<T>& p, const LuFields& f,
-                                         int64_t s) {
+                                         int64_t s, CellOps<TYP, T>& first) {
   const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
-  for (int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    if (UPPER) upper_cell<TYP, T>(z, p, f, c0 + c);
-    else lower_cell<TYP, T>(z, p, c0 + c);
+  int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
+  if (c >= n) return;
+  if (!PRE) load_ops<TYP, T, UPPER>(p, f.inplace != 0, c0 + c, first);
+  run_cell<TYP, T, UPPER>(z, p, f, c0 + c, first);
+  for (c += (int64_t)gridDim.x * blockDim.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    CellOps<TYP, T> o;
+    load_ops<TYP, T, UPPER>(p, f.inplace != 0, c0 + c, o);
+    run_cell<TYP, T, UPPER>(z, p, f, c0 + c, o);
   }
 }
 
+template <int TYP, typename T, bool UPPER>
+__device__ __forceinline__ void load_first(const PlaneData<T>& p, const LuFields& f, int64_t s,
+                                           CellOps<TYP, T>& o) {
+  const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
+  const int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
+  if (c < n) load_ops<TYP, T, UPPER>(p, f.inplace != 0, c0 + c, o);
+}
+
+template <typename T> struct LuThreads { static constexpr int n = 512; };
+
 template <int TYP, typename T>
-__global__ void __launch_bounds__(512) lusgs_persistent(Zone z, PlaneData<T> p, LuFields f,
-                                                        GridBar gb) {
+__global__ void __launch_bounds__(LuThreads<T>::n, 1)
+    lusgs_persistent(Zone z, PlaneData<T> p, LuFields f, GridBar gb) {
   const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
   // traversal step t: lower planes 0..smax, then upper planes smax..0
   auto plane_of = [&](int64_t t) { return t <= smax ? t : 2 * smax + 1 - t; };
   const int64_t nsteps = 2 * smax + 2;
   prefetch_plane<TYP, T>(p, 0, false);
   if (nsteps > 1) prefetch_plane<TYP, T>(p, plane_of(1), 1 > smax);
+  constexpr bool PRE = sizeof(T) == 4;
+  CellOps<TYP, T> o;
+  if (PRE) load_first<TYP, T, false>(p, f, 0, o);
   unsigned int round = 0;
   for (int64_t t = 0; t < nsteps; t++) {
     const int64_t s = plane_of(t);
-    if (t <= smax) do_plane<TYP, T, false>(z, p, f, s);
-    else do_plane<TYP, T, true>(z, p, f, s);
+    if (t <= smax) do_plane<TYP, T, false, PRE>(z, p, f, s, o);
+    else do_plane<TYP, T, true, PRE>(z, p, f, s, o);
     if (t == nsteps - 1) break;
     bar_arrive(gb);
     if (t + 2 < nsteps) prefetch_plane<TYP, T>(p, plane_of(t + 2), t + 2 > smax);
+    if (PRE) {
+      if (t + 1 <= smax) load_first<TYP, T, false>(p, f, plane_of(t + 1), o);
+      else load_first<TYP, T, true>(p, f, plane_of(t + 1), o);
+    }
     round++;
     if (!bar_wait(gb, round * gridDim.x)) return;
   }
@@ -678,23 +741,41 @@ __global__ void __launch_bounds__(128) lusgs_plane(Zone z, PlaneData<T> p, LuFie
   const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
-  if (UPPER) upper_cell<TYP, T>(z, p, f, c0 + c);
-  else lower_cell<TYP, T>(z, p, c0 + c);
+  CellOps<TYP, T> o;
+  load_ops<TYP, T, UPPER>(p, f.inplace != 0, c0 + c, o);
+  run_cell<TYP, T, UPPER>(z, p, f, c0 + c, o);
 }
 
-// FP64 Newton update of every interior cell after the sweeps (natural order)
+// FP64 Newton update of every interior cell after the sweeps.  Tiles of
+// GT_I x GT_J cells at one k as in lu_gather: the increments of a tile
+// anti-diagonal are contiguous in plane order, so the CTA reads them as
+// spans into shared memory, then updates its cells in natural order.
 template <typename T>
-__global__ void __launch_bounds__(256) lu_newton(Zone z, LuFields f, const T* __restrict__ dio) {
-  const int64_t n = z.ni * z.nj * z.nk;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int64_t ii = t % z.ni, r = t / z.ni, jj = r % z.nj, kk = r / z.nj;
-  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1), nd = z.nd;
-  const int64_t g = f.posmap[l];
+__global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* __restrict__ dio) {
+  __shared__ __align__(16) T s_dio[GT_N * DIO];
+  __shared__ int32_t s_g[GT_N];
+  const int ti = threadIdx.x % GT_I, tj = threadIdx.x / GT_I;
+  const int64_t ii = (int64_t)blockIdx.x * GT_I + ti, jj = (int64_t)blockIdx.y * GT_J + tj;
+  const int64_t kk = blockIdx.z;
+  const int q = tile_slot(ti, tj);
+  const bool in = ii < z.ni && jj < z.nj;
+  const int64_t l = in ? inddm(z, ii + 1, jj + 1, kk + 1) : 0;
+  s_g[q] = in ? f.posmap[l] : -1;
+  __syncthreads();
+  using V2 = typename Vec2<T>::t;
+  for (int c = threadIdx.x; c < GT_N * (DIO / 2); c += GT_N) {
+    const int qq = c / (DIO / 2), m = c - qq * (DIO / 2);
+    const int32_t g = s_g[qq];
+    if (g < 0) continue;
+    reinterpret_cast<V2*>(s_dio + qq * DIO)[m] = reinterpret_cast<const V2*>(dio + (int64_t)g * DIO)[m];
+  }
+  __syncthreads();
+  if (!in) return;
+  const int64_t nd = z.nd;
   const double* R = f.rop_old;
   double d[5], nw[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) d[v] = double(dio[g * DIO + v]);
+  for (int v = 0; v < 5; v++) d[v] = double(s_dio[q * DIO + v]);
   newton<double>(z.cv, R[l], R[l + nd], R[l + 2 * nd], R[l + 3 * nd], R[l + 4 * nd], d, nw);
 #pragma unroll
   for (int v = 0; v < 5; v++) f.rop_new[l + v * nd] = nw[v];
@@ -703,7 +784,6 @@ __global__ void __launch_bounds__(256) lu_newton(Zone z, LuFields f, const T* __
 template <int TYP, typename T>
 static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>& p,
                             const LuLaunch& L, cudaStream_t st) {
-  const unsigned gc = (unsigned)((p.G + 255) / 256);
   using S = GatherSmem<TYP, T>;
   static bool smem_set[64] = {};   // per device
   int dev = 0;
@@ -726,15 +806,15 @@ static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T>, 512, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T>, LuThreads<T>::n, 0);
       grid = nsm * (per > 0 ? per : 1);
     }
     e = cudaMemsetAsync(L.bar, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     GridBar gb{L.bar, L.err};
     void* args[] = {(void*)&z, (void*)&p, (void*)&f, (void*)&gb};
-    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(512), args,
-                                    0, st);
+    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(LuThreads<T>::n),
+                                    args, 0, st);
   } else {
     const int B = 128;
     const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
@@ -750,7 +830,8 @@ static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>
   }
   if (e != cudaSuccess) return e;
   if (!f.inplace || sizeof(T) == 4) {
-    lu_newton<T><<<gc, 256, 0, st>>>(z, f, p.dio);
+    lu_newton<T><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I), (unsigned)((z.nj + GT_J - 1) / GT_J),
+                        (unsigned)z.nk), GT_N, 0, st>>>(z, f, p.dio);
     e = cudaGetLastError();
   }
   return e;
@@ -770,7 +851,7 @@ static PlaneData<T> plane_data(const LuLaunch& L, int rec_size) {
 
 // words of LU work per interior cell (the caller allocates G * this * 8 bytes)
 int64_t lusgs_work_words(int typ) {
-  return (typ == Z3DCART ? Rec<Z3DCART>::SIZE : Rec<Z3DFULL>::SIZE) + DIO + 4;
+  return (typ == Z3DCART ? Rec<Z3DCART, double>::SIZE : Rec<Z3DFULL, double>::SIZE) + DIO + 4;
 }
 
 cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl, int32_t* nbu,
@@ -782,12 +863,13 @@ cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl,
 // One LU-SGS solve (lower, upper, Newton update) of one zone.
 cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st) {
   LuFields f{a.rop_old, a.rop_new, a.coe, a.din, L.posmap, a.rop_knb == a.rop_new};
-  const int rs = z.typ == Z3DCART ? Rec<Z3DCART>::SIZE : Rec<Z3DFULL>::SIZE;
   if (L.fp32) {
+    const int rs = z.typ == Z3DCART ? Rec<Z3DCART, float>::SIZE : Rec<Z3DFULL, float>::SIZE;
     PlaneData<float> p = plane_data<float>(L, rs);
     return z.typ == Z3DCART ? launch_t<Z3DCART, float>(z, f, p, L, st)
                             : launch_t<Z3DFULL, float>(z, f, p, L, st);
   }
+  const int rs = z.typ == Z3DCART ? Rec<Z3DCART, double>::SIZE : Rec<Z3DFULL, double>::SIZE;
   PlaneData<double> p = plane_data<double>(L, rs);
   return z.typ == Z3DCART ? launch_t<Z3DCART, double>(z, f, p, L, st)
                           : launch_t<Z3DFULL, double>(z, f, p, L, st);
