@@ -257,6 +257,7 @@ static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const dou
   z.rk = (int)p[RK]; z.dtloc = (int)p[DTLOC];
   z.gam = r[GAMMA];
   z.cv = r[CVINF];
+  z.cvinv = 1. / z.cv;
   z.rgp = r[CVINF] * (z.gam - 1.);
   z.gam1 = z.gam / (z.gam - 1.);
   z.gam3 = z.gam1 / r[PRANDT] * z.rgp;

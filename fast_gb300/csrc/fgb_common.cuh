@@ -46,6 +46,7 @@ struct Zone {
   int typ, iflow, kflu, slope, neq, itypcp, rk, dtloc;
   // constants of template_FluxAndBalance.for:108-156 and friends
   double gam, rgp, gam1, gam3, cv, dtc, psiroe, wig_cte, tmin_1;
+  double cvinv;   // 1/cv (mjr_newton.for computes it once per call)
   double c1, c2, c3, c4, c5, c6, cvisq;
   double tcx, tcy, tcz, si, sj, sk, volinv;  // 3d cartesian metric
   double prandt, xmul0, temp0, cs;

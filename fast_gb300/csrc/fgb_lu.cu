@@ -477,10 +477,12 @@ __device__ __forceinline__ void load_dio(const T* __restrict__ dio, int64_t g, T
   for (int v = 0; v < 5; v++) o[v] = __ldcg(q + v);
 }
 
-// mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW) in precision T
+// mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW) in precision T; cvinv =
+// 1/cv in precision T (the FP64 quotient is the host's: the same IEEE value)
 template <typename T>
-__device__ __forceinline__ void newton(T cv, T ro, T u, T v, T w, T tt, const T d[5], T n[5]) {
-  const T cvinv = T(1.) / cv, cvinv2 = T(0.5) * cvinv;
+__device__ __forceinline__ void newton(T cv, T cvinv, T ro, T u, T v, T w, T tt, const T d[5],
+                                       T n[5]) {
+  const T cvinv2 = T(0.5) * cvinv;
   n[0] = ro + d[0];
   const T r_1 = T(1.) / n[0];
   n[1] = (ro * u + d[1]) * r_1;
@@ -608,7 +610,8 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
   if (!UPPER || !f.inplace) return;  // otherwise the Newton update runs after the sweep
   // in place: the k-1 neighbour needs this cell's new state in the next plane
   T nw[5];
-  newton<T>(T(z.cv), o.st[0], o.st[1], o.st[2], o.st[3], o.st[4], x, nw);
+  const T cvinv = sizeof(T) == 8 ? T(z.cvinv) : T(1.) / T(z.cv);
+  newton<T>(T(z.cv), cvinv, o.st[0], o.st[1], o.st[2], o.st[3], o.st[4], x, nw);
   T* q = p.nst + g * 4;
 #pragma unroll
   for (int v = 0; v < 4; v++) q[v] = nw[v + 1];
@@ -773,12 +776,39 @@ __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* _
   if (!in) return;
   const int64_t nd = z.nd;
   const double* R = f.rop_old;
-  double d[5], nw[5];
+  if (sizeof(T) == 8) {  // mjr_newton.for, FP64
+    double d[5], nw[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) d[v] = double(s_dio[q * DIO + v]);
-  newton<double>(z.cv, R[l], R[l + nd], R[l + 2 * nd], R[l + 3 * nd], R[l + 4 * nd], d, nw);
+    for (int v = 0; v < 5; v++) d[v] = double(s_dio[q * DIO + v]);
+    newton<double>(z.cv, z.cvinv, R[l], R[l + nd], R[l + 2 * nd], R[l + 3 * nd], R[l + 4 * nd], d,
+                   nw);
 #pragma unroll
-  for (int v = 0; v < 5; v++) f.rop_new[l + v * nd] = nw[v];
+    for (int v = 0; v < 5; v++) f.rop_new[l + v * nd] = nw[v];
+    return;
+  }
+  // Mixed precision: the same map written as W^{p+1} = W^p + delta with the
+  // increments in cancellation-free form,
+  //   ro' = ro + d0,  du = (d1 - u d0) / ro'  (likewise v, w),
+  //   de = (d4 - e d0) / ro'  with e = cv T + |u|^2 / 2,
+  //   dT = (de - (du (2u + du) + dv (2v + dv) + dw (2w + dw)) / 2) / cv,
+  // evaluated in FP32 (their relative FP32 error vanishes with delta) and
+  // added to the FP64 state.
+  const double ro = R[l], u = R[l + nd], v = R[l + 2 * nd], w = R[l + 3 * nd], tt = R[l + 4 * nd];
+  const float d0 = float(s_dio[q * DIO]), d1 = float(s_dio[q * DIO + 1]),
+              d2 = float(s_dio[q * DIO + 2]), d3 = float(s_dio[q * DIO + 3]),
+              d4 = float(s_dio[q * DIO + 4]);
+  const double ron = ro + double(d0);
+  const float r1 = 1.f / float(ron);
+  const float fu = float(u), fv = float(v), fw = float(w), cv = float(z.cv);
+  const float e = cv * float(tt) + 0.5f * (fu * fu + fv * fv + fw * fw);
+  const float du = (d1 - fu * d0) * r1, dv = (d2 - fv * d0) * r1, dw = (d3 - fw * d0) * r1;
+  const float de = (d4 - e * d0) * r1;
+  const float dT = (de - 0.5f * (du * (2.f * fu + du) + dv * (2.f * fv + dv) + dw * (2.f * fw + dw))) / cv;
+  f.rop_new[l] = ron;
+  f.rop_new[l + nd] = u + double(du);
+  f.rop_new[l + 2 * nd] = v + double(dv);
+  f.rop_new[l + 3 * nd] = w + double(dw);
+  f.rop_new[l + 4 * nd] = tt + double(dT);
 }
 
 template <int TYP, typename T>
