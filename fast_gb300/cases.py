@@ -45,6 +45,26 @@ def cart_zone(name, x0, h, n, ng=NG):
     return z
 
 
+def wave(z, amp, x0, L):
+    """Periodic curvilinear mesh: displace every vertex of a uniform box by
+    amp x (local step) x a product of sines of the other two coordinates,
+    with the box lengths L as periods, so the mesh stays periodic (ghost
+    vertices coincide with the shifted interior ones) and is a general
+    3-d zone (no direction stays cartesian)."""
+    gc = I.getNodeFromName1(z, "GridCoordinates")
+    X, Y, Z = (I.getNodeFromName1(gc, n)[1].copy() for n in
+               ("CoordinateX", "CoordinateY", "CoordinateZ"))
+    hx, hy, hz = X[1, 0, 0] - X[0, 0, 0], Y[0, 1, 0] - Y[0, 0, 0], Z[0, 0, 1] - Z[0, 0, 0]
+    sx, sy, sz = (2 * math.pi * (A - a0) / l for A, a0, l in ((X, x0[0], L[0]), (Y, x0[1], L[1]),
+                                                              (Z, x0[2], L[2])))
+    new = (X + amp * hx * np.sin(sy) * np.sin(sz),
+           Y + amp * hy * np.sin(sx) * np.sin(sz),
+           Z + amp * hz * np.sin(sx) * np.sin(sy))
+    for nm, arr in zip(("CoordinateX", "CoordinateY", "CoordinateZ"), new):
+        I.getNodeFromName1(gc, nm)[1] = np.asfortranarray(arr)
+    return z
+
+
 def cell_centers(z):
     gc = I.getNodeFromName1(z, "GridCoordinates")
     out = []
@@ -92,12 +112,15 @@ def _tree(zones, model, numb, numz, mach, reynolds, gamma=1.4, prandtl=0.72, sut
 
 
 def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0, gamma=1.4,
-                      numb=None, numz=None):
+                      numb=None, numz=None, wavy=0.0):
     """Config: plain FP64, 128x128x4 periodic box [-box, box]^2, Euler vortex
-    (Mach 0.5, strength 5, core radius 1), Roe + minmod, explicit RK3."""
+    (Mach 0.5, strength 5, core radius 1), Roe + minmod, explicit RK3.
+    wavy > 0: the same box on a periodic curvilinear mesh (see wave)."""
     ni, nj, nk = n
     h = (2 * box / ni, 2 * box / nj, 2 * box / ni)
     z = cart_zone("vortex", (-box, -box, 0.0), h, n)
+    if wavy:
+        wave(z, wavy, (-box, -box, 0.0), (2 * box, 2 * box, h[2] * nk))
     xc, yc, _ = cell_centers(z)
     x = xc / radius
     y = yc / radius
@@ -119,7 +142,8 @@ def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0,
 
 
 def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_iteration=4,
-                 dt=None, scheme="ausmpred", slope="o3", numb=None, numz=None, name="tgv"):
+                 dt=None, scheme="ausmpred", slope="o3", numb=None, numz=None, name="tgv",
+                 wavy=0.0, model="NSLaminar"):
     """Config: laminar Taylor-Green vortex on the periodic box [0, 2 pi]^3,
     Re = 1600, Mach 0.1, Pr 0.71, mu ~ sqrt(T) (FastS Sutherland form with
     Cs = 0), AUSM+(P) o3, implicit LU-SGS dual time stepping."""
@@ -127,6 +151,8 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
     L = 1.0
     h = tuple(2 * math.pi * L / k for k in N)
     z = cart_zone(name, (0.0, 0.0, 0.0), h, N)
+    if wavy:
+        wave(z, wavy, (0.0, 0.0, 0.0), tuple(2 * math.pi * L for _ in range(3)))
     xc, yc, zc = cell_centers(z)
     U0 = mach
     ro0, T0 = 1.0, 1.0
@@ -146,5 +172,5 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
     numz = numz or {"scheme": scheme, "slope": slope, "time_step": dt,
                     "cache_blocking_I": 1000000, "cache_blocking_J": 1000000,
                     "cache_blocking_K": 1000000}
-    return _tree([z], "NSLaminar", numb, numz, mach, reynolds, gamma=gamma, prandtl=prandtl,
+    return _tree([z], model, numb, numz, mach, reynolds, gamma=gamma, prandtl=prandtl,
                  sutherland=False)

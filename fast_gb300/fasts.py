@@ -17,6 +17,7 @@ import sys
 import numpy as np
 
 from . import fastc as FastC
+from . import metric
 from . import pytree as I
 from ._native import Solver
 
@@ -48,24 +49,20 @@ def allocate_metric(z, nssiter, verbose=0):
     x, y, z_ = _coords(z)
     typ = _zone_type(x, y, z_, nk)
     pi[FastC.ITYPZONE] = typ
-    if typ == 2:
-        pi[FastC.NIJK_MTR:FastC.NIJK_MTR + 5] = 0
-        pi[FastC.NDIMDX_MTR] = 1
-        pi[FastC.NEQ_IJ] = 1
-        pi[FastC.NEQ_K] = 1
-    else:
-        raise NotImplementedError("curvilinear metrics are computed by fast_gb300.metric")
+    nijk_mtr, ndm, neq_ij, neq_k = metric.dims(pi[FastC.NIJK_XYZ:FastC.NIJK_XYZ + 5], typ)
+    pi[FastC.NIJK_MTR:FastC.NIJK_MTR + 5] = nijk_mtr
+    pi[FastC.NDIMDX_MTR] = ndm
+    pi[FastC.NEQ_IJ] = neq_ij
+    pi[FastC.NEQ_K] = neq_k
     itypcp = pi[FastC.ITYPCP]
     pi[FastC.NEQ] = 6 if pi[FastC.IFLOW] == 3 else 5
     pi[FastC.NEQ_COE] = (6 if pi[FastC.IFLOW] == 3 else 5) if itypcp <= 1 else 1
     pi[FastC.ITYPVENT] = 2
     pi[FastC.NEQ_VENT] = 3
     pi[FastC.NDIMDX_VENT] = 1
-    # 3d cartesian metric: face areas and cell volume of a uniform box
-    dx = float(x[ific + 1, ific, ific] - x[ific, ific, ific])
-    dy = float(y[ific, ific + 1, ific] - y[ific, ific, ific])
-    dz = float(z_[ific, ific, ific + 1] - z_[ific, ific, ific])
-    mtr = np.array([dy * dz, dx * dz, dx * dy, dx * dy * dz], dtype=np.float64)
+    # cp_tijk.for / cp_vol.for
+    ti, tj, tk, vol = metric.compute(x, y, z_, typ, ng=ific, ngk=int(pi[FastC.NIJK + 4]))
+    mtr = np.concatenate([ti, tj, tk, vol])
     ijkv_lu = [max(1, int(pi[FastC.IJKV + d]) // int(pi[FastC.SIZE_SSDOM + d])) for d in range(3)]
     rdm = np.zeros(int(nssiter) * int(pi[FastC.NEQ]) * 2 * ijkv_lu[0] * ijkv_lu[1] * ijkv_lu[2])
     return [mtr, None, None, None, rdm, None, None, None]
@@ -73,7 +70,9 @@ def allocate_metric(z, nssiter, verbose=0):
 
 def _zone_type(x, y, z, nk, tol=2.0e-8):
     """FastC/FastC/Metric/nature_geom_dom.for: 3 = 2d (nk = 2 vertices),
-    2 = 3d cartesian with constant steps, 0 = general."""
+    2 = 3d cartesian with constant steps, 1 = 3d with a homogeneous k
+    direction (z = z(k) with a constant step, x and y independent of k),
+    0 = general."""
     if nk == 2:
         return 3
     dx = np.diff(x, axis=0)
@@ -83,7 +82,13 @@ def _zone_type(x, y, z, nk, tol=2.0e-8):
             np.ptp(np.diff(y, axis=0)) < tol and np.ptp(np.diff(y, axis=2)) < tol and
             np.ptp(np.diff(z, axis=0)) < tol and np.ptp(np.diff(z, axis=1)) < tol)
     cte = np.ptp(dx) < tol and np.ptp(dy) < tol and np.ptp(dz) < tol
-    return 2 if (cart and cte) else 0
+    if cart and cte:
+        return 2
+    zcart = np.ptp(np.diff(z, axis=0)) < tol and np.ptp(np.diff(z, axis=1)) < tol
+    if zcart and np.ptp(dz) < tol and np.ptp(np.diff(x, axis=2)) < tol and \
+            np.ptp(np.diff(y, axis=2)) < tol:
+        return 1
+    return 0
 
 
 def metric_arrays(pi, mtr):

@@ -24,7 +24,7 @@
 #endif
 
 /* ---- FastS/FastS/param_solver.h index map (the subset used here) ---- */
-enum { NIJK = 0, NIJK_MTR = 5, IJKV = 20, ITYPZONE = 25, IFLOW = 27, ILES = 28,
+enum { NIJK = 0, NIJK_MTR = 5, NIJK_XYZ = 10, IJKV = 20, ITYPZONE = 25, IFLOW = 27, ILES = 28,
        ITYPCP = 29, SIZE_SSDOM = 30, KFLUDOM = 33, LALE = 34, NEQ = 36,
        NEQ_IJ = 37, NEQ_K = 38, NEQ_COE = 39, NDIMDX = 41, NDIMDX_MTR = 43,
        DTLOC = 46, RK = 52, LEVEL = 53, EXPLOC = 54, NSSITER = 58, SLOPE = 64,
@@ -1022,6 +1022,116 @@ void or_residual_norms(const int64_t* pi, const double* pr, const double* rdm,
  * ghost <- cell shifted by the zone size), bvbs_extrapolate.for (tag 0,
  * zeroth order); then correct_coins.for for edges and corners.
  * ====================================================================== */
+/* ----------------------------------------------------------- metrics
+ * FastC/FastC/Metric/cp_tijk.for (faces: normal * area) and cp_vol.for
+ * (volumes) for 3-d general (ITYPZONE 0) and 3-d cartesian (2) zones, over
+ * every cell including ghosts (indice_omp1.h ind_mtr), plus the last
+ * imax+1 / jmax+1 / kmax+1 faces.  x, y, z: vertex coordinates, Fortran
+ * order, NIJK_XYZ dimensions.  General zones index the metric on the
+ * vertex grid (NIJK_MTR strides 1, nvi, nvi*nvj). */
+static void face_i(const double* x, const double* y, const double* z, int64_t l0, int64_t l1,
+                   int64_t l2, int64_t l3, double t[3]) {
+  double tix10 = (y[l1] - y[l0]) * (z[l3] - z[l0]) - (z[l1] - z[l0]) * (y[l3] - y[l0]);
+  double tiy10 = (z[l1] - z[l0]) * (x[l3] - x[l0]) - (x[l1] - x[l0]) * (z[l3] - z[l0]);
+  double tiz10 = (x[l1] - x[l0]) * (y[l3] - y[l0]) - (y[l1] - y[l0]) * (x[l3] - x[l0]);
+  double tix11 = (y[l2] - y[l3]) * (z[l0] - z[l2]) - (z[l2] - z[l3]) * (y[l0] - y[l2]);
+  double tiy11 = (z[l2] - z[l3]) * (x[l0] - x[l2]) - (x[l2] - x[l3]) * (z[l0] - z[l2]);
+  double tiz11 = (x[l2] - x[l3]) * (y[l0] - y[l2]) - (y[l2] - y[l3]) * (x[l0] - x[l2]);
+  t[0] = .5 * (tix10 + tix11); t[1] = .5 * (tiy10 + tiy11); t[2] = .5 * (tiz10 + tiz11);
+}
+static void face_j(const double* x, const double* y, const double* z, int64_t l0, int64_t l4,
+                   int64_t l2, int64_t l6, double t[3]) {
+  double tjx10 = (y[l0] - y[l4]) * (z[l2] - z[l0]) - (z[l0] - z[l4]) * (y[l2] - y[l0]);
+  double tjy10 = (z[l0] - z[l4]) * (x[l2] - x[l0]) - (x[l0] - x[l4]) * (z[l2] - z[l0]);
+  double tjz10 = (x[l0] - x[l4]) * (y[l2] - y[l0]) - (y[l0] - y[l4]) * (x[l2] - x[l0]);
+  double tjx11 = (y[l6] - y[l2]) * (z[l4] - z[l6]) - (z[l6] - z[l2]) * (y[l4] - y[l6]);
+  double tjy11 = (z[l6] - z[l2]) * (x[l4] - x[l6]) - (x[l6] - x[l2]) * (z[l4] - z[l6]);
+  double tjz11 = (x[l6] - x[l2]) * (y[l4] - y[l6]) - (y[l6] - y[l2]) * (x[l4] - x[l6]);
+  t[0] = .5 * (tjx10 + tjx11); t[1] = .5 * (tjy10 + tjy11); t[2] = .5 * (tjz10 + tjz11);
+}
+static void face_k(const double* x, const double* y, const double* z, int64_t l0, int64_t l4,
+                   int64_t l1, int64_t l5, double t[3]) {
+  double tkx10 = (y[l4] - y[l0]) * (z[l5] - z[l4]) - (z[l4] - z[l0]) * (y[l5] - y[l4]);
+  double tky10 = (z[l4] - z[l0]) * (x[l5] - x[l4]) - (x[l4] - x[l0]) * (z[l5] - z[l4]);
+  double tkz10 = (x[l4] - x[l0]) * (y[l5] - y[l4]) - (y[l4] - y[l0]) * (x[l5] - x[l4]);
+  double tkx11 = (y[l1] - y[l5]) * (z[l0] - z[l1]) - (z[l1] - z[l5]) * (y[l0] - y[l1]);
+  double tky11 = (z[l1] - z[l5]) * (x[l0] - x[l1]) - (x[l1] - x[l5]) * (z[l0] - z[l1]);
+  double tkz11 = (x[l1] - x[l5]) * (y[l0] - y[l1]) - (y[l1] - y[l5]) * (x[l0] - x[l1]);
+  t[0] = .5 * (tkx10 + tkx11); t[1] = .5 * (tky10 + tky11); t[2] = .5 * (tkz10 + tkz11);
+}
+
+void or_metric(const int64_t* pi, const double* x, const double* y, const double* z, double* ti,
+               double* tj, double* tk, double* vol) {
+  const int64_t nvi = pi[NIJK_XYZ], nvj = pi[NIJK_XYZ + 1], nvk = pi[NIJK_XYZ + 2];
+  const int64_t ng = pi[NIJK_XYZ + 3], ngk = pi[NIJK_XYZ + 4];
+  const int64_t inci = 1, incj = nvi, inck = nvi * nvj;
+#define VX(i, j, k) (((i) + ng - 1) + ((j) + ng - 1) * nvi + ((k) + ngk - 1) * nvi * nvj)
+  double t[3];
+  if (pi[ITYPZONE] == 2) {
+    const int64_t l0 = VX(1, 1, 1), l1 = l0 + incj, l2 = l0 + inck, l3 = l1 + inck;
+    const int64_t l4 = l0 + inci, l5 = l1 + inci, l6 = l2 + inci, l7 = l3 + inci;
+    face_i(x, y, z, l0, l1, l2, l3, t); ti[0] = t[0];
+    face_j(x, y, z, l0, l4, l2, l6, t); tj[0] = t[1];
+    face_k(x, y, z, l0, l4, l1, l5, t); tk[0] = t[2];
+    double ax = .25 * ((x[l4] + x[l5] + x[l7] + x[l6]) * ti[0] - (x[l0] + x[l1] + x[l3] + x[l2]) * ti[0]);
+    double ay = .25 * ((y[l1] + y[l3] + y[l5] + y[l7]) * tj[0] - (y[l0] + y[l2] + y[l4] + y[l6]) * tj[0]);
+    double az = .25 * ((z[l2] + z[l3] + z[l6] + z[l7]) * tk[0] - (z[l0] + z[l1] + z[l4] + z[l5]) * tk[0]);
+    vol[0] = OMAX((ax + ay + az) / 3., 1.e-30);
+    return;
+  }
+  const int64_t ndm = nvi * nvj * nvk;
+  const int64_t iv = pi[IJKV], jv = pi[IJKV + 1], kv = pi[IJKV + 2];
+  const int64_t ngc = pi[NIJK + 3], ngkc = pi[NIJK + 4];
+  for (int64_t k = 1 - ngkc; k <= kv + ngkc; k++)
+    for (int64_t j = 1 - ngc; j <= jv + ngc; j++)
+      for (int64_t i = 1 - ngc; i <= iv + ngc; i++) {
+        const int64_t lt = VX(i, j, k), l0 = lt, l1 = l0 + incj, l2 = l0 + inck, l3 = l1 + inck;
+        const int64_t l4 = l0 + inci, l5 = l1 + inci, l6 = l2 + inci;
+        face_i(x, y, z, l0, l1, l2, l3, t);
+        for (int c = 0; c < 3; c++) ti[lt + c * ndm] = t[c];
+        face_j(x, y, z, l0, l4, l2, l6, t);
+        for (int c = 0; c < 3; c++) tj[lt + c * ndm] = t[c];
+        face_k(x, y, z, l0, l4, l1, l5, t);
+        for (int c = 0; c < 3; c++) tk[lt + c * ndm] = t[c];
+      }
+  for (int64_t k = 1 - ngkc; k <= kv + ngkc; k++)   /* i = imax + 1 faces */
+    for (int64_t j = 1 - ngc; j <= jv + ngc; j++) {
+      const int64_t lt = VX(iv + ngc + 1, j, k), l1 = lt + incj, l2 = lt + inck, l3 = l1 + inck;
+      face_i(x, y, z, lt, l1, l2, l3, t);
+      for (int c = 0; c < 3; c++) ti[lt + c * ndm] = t[c];
+    }
+  for (int64_t k = 1 - ngkc; k <= kv + ngkc; k++)   /* j = jmax + 1 faces */
+    for (int64_t i = 1 - ngc; i <= iv + ngc; i++) {
+      const int64_t lt = VX(i, jv + ngc + 1, k), l2 = lt + inck, l4 = lt + inci, l6 = l2 + inci;
+      face_j(x, y, z, lt, l4, l2, l6, t);
+      for (int c = 0; c < 3; c++) tj[lt + c * ndm] = t[c];
+    }
+  for (int64_t j = 1 - ngc; j <= jv + ngc; j++)     /* k = kmax + 1 faces */
+    for (int64_t i = 1 - ngc; i <= iv + ngc; i++) {
+      const int64_t lt = VX(i, j, kv + ngkc + 1), l1 = lt + incj, l4 = lt + inci, l5 = l1 + inci;
+      face_k(x, y, z, lt, l4, l1, l5, t);
+      for (int c = 0; c < 3; c++) tk[lt + c * ndm] = t[c];
+    }
+  for (int64_t k = 1 - ngkc; k <= kv + ngkc; k++)
+    for (int64_t j = 1 - ngc; j <= jv + ngc; j++)
+      for (int64_t i = 1 - ngc; i <= iv + ngc; i++) {
+        const int64_t lt = VX(i, j, k), l0 = lt, l1 = l0 + incj, l2 = l0 + inck, l3 = l1 + inck;
+        const int64_t l4 = l0 + inci, l5 = l1 + inci, l6 = l2 + inci, l7 = l3 + inci;
+        const int64_t lip = lt + inci, ljp = lt + incj, lkp = lt + inck;
+        const double* c3[3] = {x, y, z};
+        double a[3];
+        for (int c = 0; c < 3; c++) {
+          const double* q = c3[c];
+          const int64_t o = c * ndm;
+          a[c] = .25 * ((q[l4] + q[l5] + q[l7] + q[l6]) * ti[lip + o] - (q[l0] + q[l1] + q[l3] + q[l2]) * ti[lt + o] +
+                        (q[l1] + q[l3] + q[l5] + q[l7]) * tj[ljp + o] - (q[l0] + q[l2] + q[l4] + q[l6]) * tj[lt + o] +
+                        (q[l2] + q[l3] + q[l6] + q[l7]) * tk[lkp + o] - (q[l0] + q[l1] + q[l4] + q[l5]) * tk[lt + o]);
+        }
+        vol[lt] = OMAX((a[0] + a[1] + a[2]) / 3., 1.e-30);
+      }
+#undef VX
+}
+
 static void bc_window(const int64_t* pi, const int64_t* fen, int idir, int64_t* cl) {
   int64_t ng = pi[NIJK + 3], ngk = pi[NIJK + 4];
   int64_t sdm[6] = {1, pi[IJKV], 1, pi[IJKV + 1], 1, pi[IJKV + 2]};

@@ -77,6 +77,9 @@ void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind_lu,
 void or_cprdu3s1(const int64_t* pi, int it_bloc, int nssiter,
                  const double* drodm, double* rdm);
 void or_bc_zone(const int64_t* pi, const double* pr, int lrhs, double* rop);
+/* cp_tijk.for + cp_vol.for: face normals * areas and volumes of a zone */
+void or_metric(const int64_t* pi, const double* x, const double* y, const double* z, double* ti,
+               double* tj, double* tk, double* vol);
 void or_correct_coins(const int64_t* pi, const int64_t* ind, double* rop);
 void or_transfers(or_zone* zones, const or_transfer* tr, int ntr, int use_p1);
 double or_cfl_dt(const int64_t* pi, const double* pr, const double* rop,

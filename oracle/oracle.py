@@ -158,3 +158,16 @@ def cfl_dt(zd, cfl):
     xmut = np.zeros(int(pi[41]))
     ar = [np.ascontiguousarray(zd[k], dtype=np.float64) for k in ("ti", "tj", "tk", "vol")]
     return lib.or_cfl_dt(_i(pi), _d(pr), _d(ro), _d(xmut), *(_d(a) for a in ar), C.c_double(cfl))
+
+
+def metric(pi, x, y, z):
+    """cp_tijk.for + cp_vol.for restated in C: (ti, tj, tk, vol) for vertex
+    coordinates of shape (nvi, nvj, nvk) (ghosts included)."""
+    lib = load()
+    pi = np.ascontiguousarray(pi, dtype=np.int64)
+    ndm, nij, nk_ = int(pi[43]), int(pi[37]), int(pi[38])
+    ti, tj = np.zeros(ndm * nij), np.zeros(ndm * nij)
+    tk, vol = np.zeros(ndm * nk_), np.zeros(ndm)
+    xs = [np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, order="F")) for a in (x, y, z)]
+    lib.or_metric(_i(pi), *(_d(a) for a in xs), _d(ti), _d(tj), _d(tk), _d(vol))
+    return ti, tj, tk, vol

@@ -183,3 +183,36 @@ def test_mixed_precision_sweeps(oracle_mod):
     scale = np.max(np.abs(exp), axis=1, keepdims=True)
     assert np.max(np.abs(got - exp) / scale) < 1e-5
     s.close()
+
+
+@pytest.mark.parametrize("scheme,slope", [("roe_min", "minmod"), ("roe", "o3"), ("roe", "o1"),
+                                          ("ausmpred", "o3")])
+def test_curvilinear_explicit_rk3(oracle_mod, scheme, slope):
+    """3-d general zone (periodic curvilinear mesh): face normals from the
+    metric arrays, general Roe / AUSM+(P) faces."""
+    t = cases.isentropic_vortex(n=(20, 16, 6), wavy=0.3,
+                                numz={"scheme": scheme, "slope": slope, "time_step": 0.05})
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    assert int(zd[0]["pi"][25]) == 0
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
+@pytest.mark.parametrize("scheme,slope", [("ausmpred", "o3"), ("roe_min", "minmod")])
+def test_curvilinear_implicit_lusgs(oracle_mod, scheme, slope):
+    """LU-SGS on a 3-d general zone: B matrices from the cell normals,
+    in-place upper sweep with the metric of the k+1 neighbour."""
+    t = cases.taylor_green(n=(12, 10, 8), ss_iteration=3, scheme=scheme, slope=slope, wavy=0.3,
+                           model="Euler")
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    assert int(zd[0]["pi"][25]) == 0
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
+    nss = int(zd[0]["pi"][58])
+    assert rel_err(s.residuals(0), ref.residual_norms(0, nss)) <= TOL
+    s.close()
