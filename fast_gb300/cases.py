@@ -174,3 +174,38 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
                     "cache_blocking_K": 1000000}
     return _tree([z], model, numb, numz, mach, reynolds, gamma=gamma, prandtl=prandtl,
                  sutherland=False)
+
+
+def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model="NSLaminar",
+           wavy=0.0, perturb=0.05, temporal="explicit", ss_iteration=3, scheme="roe_min",
+           slope="minmod", time_step=0.02, gamma=1.4):
+    """Box [0,1]x[0,1]x[0,dz] exercising the non-periodic BCs of the path:
+    inflow at imin (BCInflow), outflow at imax (BCOutflow), a wall at jmin
+    (``wall``), farfield at jmax (BCFarfield), periodic in k.  The initial
+    field is the free stream with a smooth perturbation of relative size
+    ``perturb`` (0 gives the free stream itself).  wavy > 0 displaces the
+    vertices as in ``wave`` (periods = box lengths)."""
+    ni, nj, nk = n
+    h = (1.0 / ni, 1.0 / nj, 1.0 / ni)
+    z = cart_zone("box", (0.0, 0.0, 0.0), h, n)
+    if wavy:
+        wave(z, wavy, (0.0, 0.0, 0.0), (1.0, 1.0, h[2] * nk))
+    xc, yc, zc = cell_centers(z)
+    a = perturb
+    s = np.sin(2 * math.pi * xc) * np.sin(2 * math.pi * yc) * np.cos(2 * math.pi * zc / (h[2] * nk))
+    ro = 1.0 + a * s
+    u = mach * (1.0 + a * np.cos(2 * math.pi * yc) * np.sin(2 * math.pi * xc))
+    v = mach * a * s
+    w = mach * a * np.sin(2 * math.pi * xc) * np.cos(2 * math.pi * yc)
+    p = (1.0 + a * 0.5 * s) / gamma
+    set_conservative(z, ro, u, v, w, p, gamma)
+    add_bc(z, "in", "BCInflow", "imin")
+    add_bc(z, "out", "BCOutflow", "imax")
+    add_bc(z, "wall", wall, "jmin")
+    add_bc(z, "far", "BCFarfield", "jmax")
+    add_bc(z, "per_kmin", "BCautoperiod", "kmin")
+    add_bc(z, "per_kmax", "BCautoperiod", "kmax")
+    numb = {"temporal_scheme": temporal, "ss_iteration": ss_iteration, "modulo_verif": 1}
+    numz = {"scheme": scheme, "slope": slope, "time_step": time_step,
+            "cache_blocking_I": 1000000, "cache_blocking_J": 1000000, "cache_blocking_K": 1000000}
+    return _tree([z], model, numb, numz, mach, reynolds if model != "Euler" else 0.0, gamma=gamma)

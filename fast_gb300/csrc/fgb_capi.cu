@@ -41,8 +41,16 @@ static cudaError_t dev_upload(T** d, const std::vector<T>& h) {
   return cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
+// One BC window's ghost-fill step, run in BC order: a gather (kind 0: copy
+// or extrapolation from a donor cell), a face formula (kind 1: walls,
+// farfield / inflow / outflow first rank) or the farfield / inflow next
+// ranks (kind 2).
 struct GatherList {
+  int kind = 0;
   int32_t* dst = nullptr; int32_t* src = nullptr; int64_t n = 0; int op = 0;
+  int32_t *q0 = nullptr, *q1 = nullptr, *q2 = nullptr;
+  double* nrm = nullptr;
+  double st[5] = {0, 0, 0, 0, 0};
 };
 struct ZoneData {
   std::vector<int64_t> pi;
@@ -136,8 +144,10 @@ static void bc_window(const std::vector<int64_t>& p, const int64_t* fen, int idi
   else { cl[5] = cl[4] + ngk; cl[4] = cl[4] + 1; }
 }
 
-static int build_ghost_lists(ZoneData& Z) {
+static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
+                             const std::vector<double>& htj, const std::vector<double>& htk) {
   const std::vector<int64_t>& p = Z.pi;
+  const std::vector<double>& pr = Z.pr;
   int64_t pt_bcs = p[PT_BC];
   if (pt_bcs > 0 && pt_bcs < (int64_t)p.size()) {
     int64_t nb = p[pt_bcs];
@@ -145,30 +155,124 @@ static int build_ghost_lists(ZoneData& Z) {
       int64_t pt = p[pt_bcs + 1 + n];
       int64_t type = p[pt + 0];
       int idir = (int)p[pt + 1];
-      if (type != 11 && type != 0)
+      const bool slip = type == 3 || type == 5 || (type == 4 && p[IFLOW] == 1);
+      const bool noslip = (type == 6 || type == 4) && p[IFLOW] > 1;
+      const bool charac = type == 1 || type == 13 || type == 10;
+      if (type != 11 && type != 0 && !slip && !noslip && !charac)
         return fail(FGB_ERR_ARG, "boundary condition type " + std::to_string(type) +
                                      " is not implemented on the GPU path");
+      if (p[pt + 8] != 0)
+        return fail(FGB_ERR_ARG, "boundary data (nbdata > 0) is not supported on the GPU path");
       int64_t cl[6];
       bc_window(p, &p[pt + 2], idir, cl);
       int d = (idir - 1) / 2;
       bool low = (idir % 2) == 1;
       int64_t nD = p[IJKV + d];
-      std::vector<int32_t> dst, src;
-      for (int64_t k = cl[4]; k <= cl[5]; k++)
-        for (int64_t j = cl[2]; j <= cl[3]; j++)
-          for (int64_t i = cl[0]; i <= cl[1]; i++) {
-            int64_t c[3] = {i, j, k}, s[3] = {i, j, k};
-            if (type == 11) s[d] = low ? c[d] + nD : c[d] - nD;
-            else s[d] = low ? cl[2 * d + 1] + 1 : cl[2 * d] - 1;
-            dst.push_back((int32_t)idx(p, i, j, k));
-            src.push_back((int32_t)idx(p, s[0], s[1], s[2]));
+      if (type == 11 || type == 0) {
+        std::vector<int32_t> dst, src;
+        for (int64_t k = cl[4]; k <= cl[5]; k++)
+          for (int64_t j = cl[2]; j <= cl[3]; j++)
+            for (int64_t i = cl[0]; i <= cl[1]; i++) {
+              int64_t c[3] = {i, j, k}, s[3] = {i, j, k};
+              if (type == 11) s[d] = low ? c[d] + nD : c[d] - nD;
+              else s[d] = low ? cl[2 * d + 1] + 1 : cl[2 * d] - 1;
+              dst.push_back((int32_t)idx(p, i, j, k));
+              src.push_back((int32_t)idx(p, s[0], s[1], s[2]));
+            }
+        GatherList g;
+        g.n = (int64_t)dst.size();
+        g.op = type == 11 ? 0 : 1;
+        if (dev_upload(&g.dst, dst) != cudaSuccess || dev_upload(&g.src, src) != cudaSuccess)
+          return fail(FGB_ERR_CUDA, "cannot upload BC lists");
+        Z.bcs.push_back(g);
+        continue;
+      }
+      // ghost lines normal to the face (bvbs_*.for): rank 0 next to the face
+      const int64_t first = low ? cl[2 * d + 1] : cl[2 * d], step = low ? -1 : 1;
+      const int64_t ir = low ? first + 1 : first - 1;          // first interior cell
+      const int64_t iref = low ? 2 * first + 1 : 2 * first - 1; // mirror: iref - i
+      const int64_t nrank = d == 2 ? p[NIJK + 4] : p[NIJK + 3];
+      const int ta = d == 0 ? 1 : 0, tb = d == 2 ? 1 : 2;
+      const double snorm = low ? -1. : 1.;
+      // raw face normal tijk(lmtr) * c_mtr (shape_tab_mtr.for)
+      const std::vector<double>& T = d == 0 ? hti : (d == 1 ? htj : htk);
+      const int64_t neq_mtr = d < 2 ? p[NEQ_IJ] : p[NEQ_K], ndm = p[NDIMDX_MTR];
+      auto normal = [&](int64_t c0, int64_t c1, int64_t c2, double t[3]) {
+        int64_t c[3] = {c0, c1, c2};
+        c[d] = low ? 1 : nD + 1;
+        const int64_t lm = (c[0] + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR] +
+                           (c[1] + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR + 1] +
+                           (c[2] + p[NIJK_MTR + 4] - 1) * p[NIJK_MTR + 2];
+        if (neq_mtr == 3) {
+          t[0] = T[lm] * 1.; t[1] = T[lm + ndm] * 1.; t[2] = T[lm + 2 * ndm] * 1.;
+        } else {
+          t[0] = T[lm] * (d == 0 ? 1. : 0.); t[1] = T[lm] * (d == 1 ? 1. : 0.);
+          t[2] = T[lm] * (d == 2 ? 1. : 0.);
+        }
+      };
+      std::vector<int32_t> fdst, fsrc, ndst, n0, n1, n2, cdst, csrc;
+      std::vector<double> nrm;
+      const int64_t inc = d == 0 ? 1 : (d == 1 ? p[NIJK] : p[NIJK] * p[NIJK + 1]);
+      for (int64_t b = cl[2 * tb]; b <= cl[2 * tb + 1]; b++)
+        for (int64_t a = cl[2 * ta]; a <= cl[2 * ta + 1]; a++) {
+          int64_t c[3];
+          c[ta] = a; c[tb] = b; c[d] = first;
+          double t[3];
+          normal(c[0], c[1], c[2], t);
+          for (int64_t rank = 0; rank < nrank; rank++) {
+            c[d] = first + step * rank;
+            const int64_t l = idx(p, c[0], c[1], c[2]);
+            int64_t m[3] = {c[0], c[1], c[2]};
+            if (slip || noslip) {
+              m[d] = iref - c[d];
+              fdst.push_back((int32_t)l); fsrc.push_back((int32_t)idx(p, m[0], m[1], m[2]));
+              for (int q = 0; q < 3; q++) nrm.push_back(t[q]);
+            } else if (rank == 0) {
+              m[d] = ir;
+              fdst.push_back((int32_t)l); fsrc.push_back((int32_t)idx(p, m[0], m[1], m[2]));
+              for (int q = 0; q < 3; q++) nrm.push_back(t[q] * snorm);
+            } else if (type == 10) {     // BC_extrap.for: copy of the first ghost
+              m[d] = first;
+              cdst.push_back((int32_t)l); csrc.push_back((int32_t)idx(p, m[0], m[1], m[2]));
+            } else {                     // BC_nextrank.for
+              const int64_t dl = -step * inc;
+              ndst.push_back((int32_t)l); n0.push_back((int32_t)(l + dl));
+              n1.push_back((int32_t)(l + 2 * dl)); n2.push_back((int32_t)(l + 3 * dl));
+            }
           }
-      GatherList g;
-      g.n = (int64_t)dst.size();
-      g.op = type == 11 ? 0 : 1;
-      if (dev_upload(&g.dst, dst) != cudaSuccess || dev_upload(&g.src, src) != cudaSuccess)
+        }
+      GatherList f;
+      f.kind = 1;
+      f.op = slip ? BCF_SLIP : (noslip ? BCF_NOSLIP : (type == 10 ? BCF_OUTFLOW : BCF_FARFIELD));
+      f.n = (int64_t)fdst.size();
+      // BCzone.cpp DEFAULT_STATE, nbdata = 0: the free stream
+      f.st[0] = pr[ROINF];
+      f.st[1] = pr[VXINF] * pr[ROINF];
+      f.st[2] = pr[VYINF] * pr[ROINF];
+      f.st[3] = pr[VZINF] * pr[ROINF];
+      f.st[4] = pr[PINF] / (pr[GAMMA] - 1.) +
+                0.5 * (pr[VXINF] * f.st[1] + pr[VYINF] * f.st[2] + pr[VZINF] * f.st[3]);
+      if (dev_upload(&f.dst, fdst) != cudaSuccess || dev_upload(&f.src, fsrc) != cudaSuccess ||
+          dev_upload(&f.nrm, nrm) != cudaSuccess)
         return fail(FGB_ERR_CUDA, "cannot upload BC lists");
-      Z.bcs.push_back(g);
+      Z.bcs.push_back(f);
+      if (!cdst.empty()) {
+        GatherList g;
+        g.n = (int64_t)cdst.size();
+        g.op = 0;
+        if (dev_upload(&g.dst, cdst) != cudaSuccess || dev_upload(&g.src, csrc) != cudaSuccess)
+          return fail(FGB_ERR_CUDA, "cannot upload BC lists");
+        Z.bcs.push_back(g);
+      }
+      if (!ndst.empty()) {
+        GatherList g;
+        g.kind = 2;
+        g.n = (int64_t)ndst.size();
+        if (dev_upload(&g.dst, ndst) != cudaSuccess || dev_upload(&g.q0, n0) != cudaSuccess ||
+            dev_upload(&g.q1, n1) != cudaSuccess || dev_upload(&g.q2, n2) != cudaSuccess)
+          return fail(FGB_ERR_CUDA, "cannot upload BC lists");
+        Z.bcs.push_back(g);
+      }
     }
   }
   // correct_coins.for lists (edges first, then corners)
@@ -323,7 +427,10 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.Fi); cudaFree(Z.Fj); cudaFree(Z.Fk);
     cudaFree(Z.luwork); cudaFree(Z.cells); cudaFree(Z.plane); cudaFree(Z.posmap);
     cudaFree(Z.nbl); cudaFree(Z.nbu);
-    for (GatherList& g : Z.bcs) { cudaFree(g.dst); cudaFree(g.src); }
+    for (GatherList& g : Z.bcs) {
+      cudaFree(g.dst); cudaFree(g.src); cudaFree(g.q0); cudaFree(g.q1); cudaFree(g.q2);
+      cudaFree(g.nrm);
+    }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
   for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
@@ -394,7 +501,7 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   Z.n_rdm = p[NSSITER] * neq * 2 * Z.ijkv_lu[0] * Z.ijkv_lu[1] * Z.ijkv_lu[2];
   CK(cudaMalloc(&Z.rdm, sizeof(double) * Z.n_rdm));
   CK(cudaMemset(Z.rdm, 0, sizeof(double) * Z.n_rdm));
-  int rc = build_ghost_lists(Z);
+  int rc = build_ghost_lists(Z, hti, htj, htk);
   if (rc != FGB_OK) return rc;
   if (p[ITYPCP] <= 1) {
     // LU-SGS: cells ordered by hyperplane i+j+k (counting sort), B table
@@ -553,8 +660,25 @@ static int ghost_fill(fgb_solver* s, int level) {
   }
   for (ZoneData& Z : s->zones) {
     for (GatherList& g : Z.bcs) {
-      CK(launch_gather(Z.lvl[level], Z.z.nd, Z.lvl[level], Z.z.nd, g.dst, g.src, g.n, Z.z.neq,
-                       g.op, 1., s->st));
+      if (g.kind == 0) {
+        CK(launch_gather(Z.lvl[level], Z.z.nd, Z.lvl[level], Z.z.nd, g.dst, g.src, g.n, Z.z.neq,
+                         g.op, 1., s->st));
+      } else if (g.kind == 1) {
+        BcFaceArgs a{};
+        a.dst = g.dst; a.src = g.src; a.nrm = g.nrm; a.n = g.n; a.nd = Z.z.nd; a.op = g.op;
+        a.gam = Z.pr[GAMMA]; a.gam1 = Z.pr[GAMMA] - 1.; a.gam1_1 = 1. / a.gam1;
+        a.cv = Z.pr[CVINF]; a.cvinv = 1. / Z.pr[CVINF];
+        for (int m = 0; m < 5; m++) a.st[m] = g.st[m];
+        CK(launch_bc_face(Z.lvl[level], a, s->st));
+      } else {
+        // BC_nextrank.for with the MUSCL constants of BCzone.cpp (c4, c5, c6)
+        const double c4 = 5. / 6., c5 = 2. / 6., c6 = -1. / 6.;
+        const double k0 = 1. / c6;
+        BcNextArgs a{};
+        a.dst = g.dst; a.q0 = g.q0; a.q1 = g.q1; a.q2 = g.q2; a.n = g.n; a.nd = Z.z.nd;
+        a.k1 = -(c4 + c5) * k0; a.k2 = -c6 * k0; a.k3 = (2. - c5 - c4) * k0;
+        CK(launch_bc_next(Z.lvl[level], a, s->st));
+      }
       s->launches++;
     }
     CK(launch_coins(Z.lvl[level], Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n,

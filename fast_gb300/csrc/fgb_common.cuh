@@ -27,7 +27,8 @@ enum PI : int {
 };
 enum PR : int {
   DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6, MINF = 7,
-  PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14, PSIROE = 34, WIG_AMP = 72
+  PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14, VXINF = 19, VYINF = 20,
+  VZINF = 21, PSIROE = 34, WIG_AMP = 72
 };
 enum ZoneType : int { Z3DFULL = 0, Z3DHOMO = 1, Z3DCART = 2, Z2D = 3 };
 enum Scheme : int { AUSM = 1, SENSEUR = 2, ROE = 5 };

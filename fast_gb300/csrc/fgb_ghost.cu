@@ -73,6 +73,142 @@ cudaError_t launch_coins(double* q, int64_t nd, const int32_t* dst, const int32_
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------- face BC formulas
+// BC/BCWallInviscid.for, BCWallViscous.for (adiabatic), BCFarfield.for /
+// BCInflow_i.for (with BC/non_reflection.for), BCOutflow.for: one ghost
+// cell per thread, reading interior (or mirror) cells only.  nrm = the raw
+// face normal tijk * c_mtr, multiplied by snorm on the host for the
+// characteristic types.  No mesh motion: (vent . n) * c_ale = 0.
+struct NrOut { double r, u, v, w, qn, sn, svar[5], qvar5; };
+
+__device__ __forceinline__ void non_reflection(const BcFaceArgs& a, const double* __restrict__ q,
+                                               int64_t l1, const double t[3], const double ext[5],
+                                               NrOut& o) {
+  const int64_t nd = a.nd;
+  const double gam1 = a.gam1, gam1_1 = a.gam1_1;
+  const double tcx = t[0], tcy = t[1], tcz = t[2];
+  const double sn = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
+  const double roi = q[l1], rui = q[l1 + nd] * roi, rvi = q[l1 + 2 * nd] * roi, rwi = q[l1 + 3 * nd] * roi;
+  const double eti = q[l1 + 4 * nd] * a.cv * roi + .5 * (rui * rui + rvi * rvi + rwi * rwi) / roi;
+  const double qen = 0.;
+  const double qref1 = .5 * (ext[0] + roi), qref2 = .5 * (ext[1] + rui), qref3 = .5 * (ext[2] + rvi),
+               qref4 = .5 * (ext[3] + rwi), qref5 = .5 * (ext[4] + eti);
+  const double r = qref1, ri = 1. / r;
+  const double u = qref2 * ri, v = qref3 * ri, w = qref4 * ri;
+  const double p = gam1 * (qref5 - .5 * r * (u * u + v * v + w * w));
+  const double c = sqrt(a.gam * p * ri), ci = 1. / c, s_1 = 1. / sn;
+  const double qn = tcx * u + tcy * v + tcz * w - qen;
+  double tnx, tny;
+  if (sn == 0.) { tnx = 1.; tny = 0.; } else { tnx = tcx / sn; tny = tcy / sn; }
+  const double eig[5] = {qn, qn, qn, qn + sn * c, qn - sn * c};
+  double rv[2][5];
+  const double qv[2][5] = {{ext[0], ext[1], ext[2], ext[3], ext[4]}, {roi, rui, rvi, rwi, eti}};
+#pragma unroll
+  for (int side = 0; side < 2; side++) {
+    const double* x = qv[side];
+    const double sv1 = x[0], sv2 = (x[1] - u * x[0]) * ri, sv3 = (x[2] - v * x[0]) * ri,
+                 sv4 = (x[3] - w * x[0]) * ri;
+    const double sv5 = gam1 * (.5 * (u * u + v * v + w * w) * x[0] - u * x[1] - v * x[2] - w * x[3] + x[4]);
+    rv[side][0] = sv1 - ci * ci * sv5;
+    rv[side][1] = tcz * s_1 * (tnx * sv2 + tny * sv3) - sv4;
+    rv[side][2] = -tny * sv2 + tnx * sv3;
+    rv[side][3] = .5 * s_1 * (tcx * sv2 + tcy * sv3 + tcz * sv4) + .5 * ri * ci * sv5;
+    rv[side][4] = -.5 * s_1 * (tcx * sv2 + tcy * sv3 + tcz * sv4) + .5 * ri * ci * sv5;
+  }
+  double rvar[5];
+#pragma unroll
+  for (int m = 0; m < 5; m++) rvar[m] = eig[m] < 0. ? rv[0][m] : rv[1][m];
+  o.svar[0] = rvar[0] + r * ci * (rvar[3] + rvar[4]);
+  o.svar[1] = tcz * s_1 * tnx * rvar[1] - tny * rvar[2] + tcx * s_1 * (rvar[3] - rvar[4]);
+  o.svar[2] = tcz * s_1 * tny * rvar[1] + tnx * rvar[2] + tcy * s_1 * (rvar[3] - rvar[4]);
+  o.svar[3] = -rvar[1] + tcz * s_1 * (rvar[3] - rvar[4]);
+  o.svar[4] = r * c * (rvar[3] + rvar[4]);
+  o.qvar5 = .5 * (u * u + v * v + w * w) * o.svar[0] + r * (u * o.svar[1] + v * o.svar[2] + w * o.svar[3]) +
+            gam1_1 * o.svar[4];
+  o.r = r; o.u = u; o.v = v; o.w = w; o.qn = qn; o.sn = sn;
+}
+
+__global__ void __launch_bounds__(128) bc_face(double* __restrict__ q, BcFaceArgs a) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  const int64_t nd = a.nd, l = a.dst[e], s = a.src[e];
+  const double t[3] = {a.nrm[3 * e], a.nrm[3 * e + 1], a.nrm[3 * e + 2]};
+  if (a.op == BCF_SLIP) {
+    double tcx = t[0], tcy = t[1], tcz = t[2];
+    double surf = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
+    surf = fmaxF(surf, 1e-30);
+    const double s_1 = 1. / surf;
+    tcx = tcx * s_1; tcy = tcy * s_1; tcz = tcz * s_1;
+    const double u = q[s + nd] - 0., v = q[s + 2 * nd] - 0., w = q[s + 3 * nd] - 0.;
+    const double qn = u * tcx + v * tcy + w * tcz;
+    const double ut = u - qn * tcx, vt = v - qn * tcy, wt = w - qn * tcz;
+    const double ua = 2. * ut - u, va = 2. * vt - v, wa = 2. * wt - w;
+    q[l] = q[s];
+    q[l + nd] = 0. + ua; q[l + 2 * nd] = 0. + va; q[l + 3 * nd] = 0. + wa;
+    q[l + 4 * nd] = q[s + 4 * nd];
+  } else if (a.op == BCF_NOSLIP) {
+    const double u = q[s + nd], v = q[s + 2 * nd], w = q[s + 3 * nd];
+    q[l] = q[s];
+    q[l + nd] = 0. - u; q[l + 2 * nd] = 0. - v; q[l + 3 * nd] = 0. - w;
+    q[l + 4 * nd] = q[s + 4 * nd];
+  } else if (a.op == BCF_FARFIELD) {
+    NrOut o;
+    non_reflection(a, q, s, t, a.st, o);
+    const double roinv = 1. / o.svar[0];
+    const double u = o.u + o.r * o.svar[1] * roinv, v = o.v + o.r * o.svar[2] * roinv,
+                 w = o.w + o.r * o.svar[3] * roinv;
+    q[l] = o.svar[0];
+    q[l + nd] = u; q[l + 2 * nd] = v; q[l + 3 * nd] = w;
+    q[l + 4 * nd] = (o.qvar5 * roinv - .5 * (u * u + v * v + w * w)) * a.cvinv;
+  } else {  // BCF_OUTFLOW
+    const double roe = q[s], rue = q[s + nd] * roe, rve = q[s + 2 * nd] * roe, rwe = q[s + 3 * nd] * roe;
+    const double roe_inv = 1. / a.st[0];
+    const double ete = a.st[4] - 0.5 * (a.st[1] * a.st[1] + a.st[2] * a.st[2] + a.st[3] * a.st[3]) * roe_inv +
+                       0.5 * (rue * q[s + nd] + rve * q[s + 2 * nd] + rwe * q[s + 3 * nd]);
+    const double ext[5] = {roe, rue, rve, rwe, ete};
+    NrOut o;
+    non_reflection(a, q, s, t, ext, o);
+    q[l] = q[s];
+    const double roinv = 1. / q[l];
+    double vel[3];
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+      vel[m] = o.qn < 0. ? q[s + (m + 1) * nd] - o.qn / (o.sn * o.sn) * t[m] : q[s + (m + 1) * nd];
+#pragma unroll
+    for (int m = 0; m < 3; m++) q[l + (m + 1) * nd] = vel[m];
+    q[l + 4 * nd] = (o.qvar5 * roinv - .5 * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2])) * a.cvinv;
+  }
+}
+
+// BC/BC_nextrank.for: ghost ranks beyond the first of farfield / inflow BCs,
+// from the first ghost (q0) and the first two interior cells (q1, q2).
+__global__ void __launch_bounds__(128) bc_next(double* __restrict__ q, BcNextArgs a) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  const int64_t nd = a.nd, l = a.dst[e], q0 = a.q0[e], q1 = a.q1[e], q2 = a.q2[e];
+  const double r = q[q0] * a.k3 + q[q1] * a.k1 + q[q2] * a.k2;
+  if (fabs(r / q[q0] - 1.) >= 0.7) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) q[l + v * nd] = q[q0 + v * nd];
+  } else {
+    q[l] = r;
+#pragma unroll
+    for (int v = 1; v < 5; v++) q[l + v * nd] = q[q0 + v * nd] * a.k3 + q[q1 + v * nd] * a.k1 + q[q2 + v * nd] * a.k2;
+  }
+}
+
+cudaError_t launch_bc_face(double* q, const BcFaceArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return cudaSuccess;
+  bc_face<<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(q, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return cudaSuccess;
+  bc_next<<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(q, a);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ norms
 // One CTA per LU block (cprdu3s1_incl.for:14-135 block decomposition).
 __global__ void __launch_bounds__(256) block_norms(Zone z, NormArgs a) {

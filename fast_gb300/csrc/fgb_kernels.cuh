@@ -75,6 +75,23 @@ struct NormArgs {
 cudaError_t launch_gather(double* dst, int64_t nd_dst, const double* src, int64_t nd_src,
                           const int32_t* d_idx, const int32_t* s_idx, int64_t n, int neq,
                           int op, double c, cudaStream_t st);
+enum { BCF_SLIP = 0, BCF_NOSLIP = 1, BCF_FARFIELD = 2, BCF_OUTFLOW = 3 };
+struct BcFaceArgs {            // one face BC window (bc_face)
+  const int32_t* dst;          // ghost cells
+  const int32_t* src;          // mirror cell (walls) or first interior cell
+  const double* nrm;           // [n][3] raw face normal (x snorm for farfield / outflow)
+  int64_t n, nd;
+  int op;
+  double gam, gam1, gam1_1, cv, cvinv;
+  double st[5];                // exterior state (conservative)
+};
+struct BcNextArgs {            // farfield / inflow ghost ranks past the first
+  const int32_t *dst, *q0, *q1, *q2;
+  int64_t n, nd;
+  double k1, k2, k3;
+};
+cudaError_t launch_bc_face(double* q, const BcFaceArgs& a, cudaStream_t st);
+cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st);
 cudaError_t launch_coins(double* q, int64_t nd, const int32_t* dst, const int32_t* a,
                          const int32_t* b, const int32_t* c, int64_t n_edge, int64_t n, int neq,
                          cudaStream_t st);

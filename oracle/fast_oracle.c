@@ -31,7 +31,7 @@ enum { NIJK = 0, NIJK_MTR = 5, NIJK_XYZ = 10, IJKV = 20, ITYPZONE = 25, IFLOW = 
        PT_BC = 70, NB_RELAX = 71, LU_MATCH = 75 };
 enum { DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6,
        PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14,
-       PSIROE = 34, WIG_AMP = 72 };
+       PSIROE = 34, WIG_AMP = 72, VXINF = 19, VYINF = 20, VZINF = 21 };
 enum { BC_TYPE = 0, BC_IDIR = 1, BC_FEN = 2 };
 
 #define OMAX(a, b) ((a) > (b) ? (a) : (b))
@@ -1147,14 +1147,96 @@ static void bc_window(const int64_t* pi, const int64_t* fen, int idir, int64_t* 
   else { cl[5] = cl[4] + ngk; cl[4] = cl[4] + 1; }
 }
 
-void or_bc_zone(const int64_t* pi, const double* pr, int lrhs, double* rop) {
-  (void)pr;
+/* Raw face normal of a BC window at the boundary face of ghost line
+ * (i, j, k): tijk(lmtr, ic..kc) * c_mtr (shape_tab_mtr.for), lmtr at the
+ * first interior cell (low faces) or the first ghost (high faces). */
+static void bc_normal(const int64_t* pi, const double* ti, const double* tj, const double* tk,
+                      int idir, int64_t i, int64_t j, int64_t k, double t[3]) {
+  int d = (idir - 1) / 2, low = idir % 2;
+  int64_t c[3] = {i, j, k};
+  c[d] = low ? 1 : pi[IJKV + d] + 1;
+  const double* T = d == 0 ? ti : (d == 1 ? tj : tk);
+  const int64_t neq_mtr = d < 2 ? pi[NEQ_IJ] : pi[NEQ_K], ndm = pi[NDIMDX_MTR];
+  const int64_t lm = indmtr(pi, c[0], c[1], c[2]);
+  if (neq_mtr == 3) {
+    t[0] = T[lm] * 1.; t[1] = T[lm + ndm] * 1.; t[2] = T[lm + 2 * ndm] * 1.;
+  } else {
+    double ci = d == 0 ? 1. : 0., cj = d == 1 ? 1. : 0., ck = d == 2 ? 1. : 0.;
+    t[0] = T[lm] * ci; t[1] = T[lm] * cj; t[2] = T[lm] * ck;
+  }
+}
+
+/* BC/non_reflection.for: characteristic state between the exterior state
+ * (roe, rue, rve, rwe, ete) and interior cell l1; t = normal * snorm. */
+typedef struct { double r, u, v, w, qn, sn, svar[5], qvar5; } nr_out;
+static void non_reflection(const double* pr, const double t[3], const double* rop, int64_t nd,
+                           int64_t l1, const double ext[5], nr_out* o) {
+  const double gam = pr[GAMMA], gam1 = pr[GAMMA] - 1., gam1_1 = 1. / gam1;
+  const double tcx = t[0], tcy = t[1], tcz = t[2];
+  const double sn = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
+  const double roi = rop[l1], rui = rop[l1 + nd] * roi, rvi = rop[l1 + 2 * nd] * roi,
+               rwi = rop[l1 + 3 * nd] * roi;
+  const double eti = rop[l1 + 4 * nd] * pr[CVINF] * roi + .5 * (rui * rui + rvi * rvi + rwi * rwi) / roi;
+  const double qen = 0.;  /* (vent . n) * c_ale: no mesh motion */
+  const double qref1 = .5 * (ext[0] + roi), qref2 = .5 * (ext[1] + rui), qref3 = .5 * (ext[2] + rvi),
+               qref4 = .5 * (ext[3] + rwi), qref5 = .5 * (ext[4] + eti);
+  const double r = qref1, ri = 1. / r;
+  const double u = qref2 * ri, v = qref3 * ri, w = qref4 * ri;
+  const double p = gam1 * (qref5 - .5 * r * (u * u + v * v + w * w));
+  const double c = sqrt(gam * p * ri), ci = 1. / c, s_1 = 1. / sn;
+  const double qn = tcx * u + tcy * v + tcz * w - qen;
+  double tnx, tny;
+  if (sn == 0.) { tnx = 1.; tny = 0.; } else { tnx = tcx / sn; tny = tcy / sn; }
+  const double eig[5] = {qn, qn, qn, qn + sn * c, qn - sn * c};
+  double rv[2][5];
+  const double qv[2][5] = {{ext[0], ext[1], ext[2], ext[3], ext[4]}, {roi, rui, rvi, rwi, eti}};
+  for (int side = 0; side < 2; side++) {
+    const double* q = qv[side];
+    double sv1 = q[0], sv2 = (q[1] - u * q[0]) * ri, sv3 = (q[2] - v * q[0]) * ri,
+           sv4 = (q[3] - w * q[0]) * ri;
+    double sv5 = gam1 * (.5 * (u * u + v * v + w * w) * q[0] - u * q[1] - v * q[2] - w * q[3] + q[4]);
+    rv[side][0] = sv1 - ci * ci * sv5;
+    rv[side][1] = tcz * s_1 * (tnx * sv2 + tny * sv3) - sv4;
+    rv[side][2] = -tny * sv2 + tnx * sv3;
+    rv[side][3] = .5 * s_1 * (tcx * sv2 + tcy * sv3 + tcz * sv4) + .5 * ri * ci * sv5;
+    rv[side][4] = -.5 * s_1 * (tcx * sv2 + tcy * sv3 + tcz * sv4) + .5 * ri * ci * sv5;
+  }
+  double rvar[5];
+  for (int m = 0; m < 5; m++) rvar[m] = eig[m] < 0. ? rv[0][m] : rv[1][m];
+  o->svar[0] = rvar[0] + r * ci * (rvar[3] + rvar[4]);
+  o->svar[1] = tcz * s_1 * tnx * rvar[1] - tny * rvar[2] + tcx * s_1 * (rvar[3] - rvar[4]);
+  o->svar[2] = tcz * s_1 * tny * rvar[1] + tnx * rvar[2] + tcy * s_1 * (rvar[3] - rvar[4]);
+  o->svar[3] = -rvar[1] + tcz * s_1 * (rvar[3] - rvar[4]);
+  o->svar[4] = r * c * (rvar[3] + rvar[4]);
+  o->qvar5 = .5 * (u * u + v * v + w * w) * o->svar[0] + r * (u * o->svar[1] + v * o->svar[2] + w * o->svar[3]) +
+             gam1_1 * o->svar[4];
+  o->r = r; o->u = u; o->v = v; o->w = w; o->qn = qn; o->sn = sn;
+}
+
+/* BCzone.cpp DEFAULT_STATE with nbdata = 0: the free stream. */
+static void bc_default_state(const double* pr, double st[5]) {
+  st[0] = pr[ROINF];
+  st[1] = pr[VXINF] * pr[ROINF];
+  st[2] = pr[VYINF] * pr[ROINF];
+  st[3] = pr[VZINF] * pr[ROINF];
+  st[4] = pr[PINF] / (pr[GAMMA] - 1.) + 0.5 * (pr[VXINF] * st[1] + pr[VYINF] * st[2] + pr[VZINF] * st[3]);
+}
+
+/* BCzone.cpp:255-865 for the types of the path, with the ghost windows of
+ * indice_cl_sdm.for (npass = 0).  Ghost cells of the first rank (next to
+ * the face) are filled before the next ranks of the same line, which the
+ * farfield / inflow / outflow next ranks read. */
+void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const double* tj,
+                const double* tk, int lrhs, double* rop) {
   int64_t pt_bcs = pi[PT_BC];
   if (pt_bcs <= 0) goto coins;
   {
     int64_t nb_bc = pi[pt_bcs];
     int64_t nd = pi[NDIMDX], neq = pi[NEQ];
     double c1 = lrhs == 1 ? 0. : 1.;
+    const double cvinv = 1. / pr[CVINF];
+    const double c4 = 5. / 6., c5 = 2. / 6., c6 = -1. / 6.;
+    const double k0 = 1. / c6, k1 = -(c4 + c5) * k0, k2 = -c6 * k0, k3 = (2. - c5 - c4) * k0;
     for (int64_t n = 0; n < nb_bc; n++) {
       int64_t pt = pi[pt_bcs + 1 + n];
       int64_t type = pi[pt + BC_TYPE];
@@ -1164,21 +1246,119 @@ void or_bc_zone(const int64_t* pi, const double* pr, int lrhs, double* rop) {
       int d = (idir - 1) / 2;
       int low = (idir % 2) == 1;
       int64_t n_d = pi[IJKV + d];
-      for (int64_t k = cl[4]; k <= cl[5]; k++)
-        for (int64_t j = cl[2]; j <= cl[3]; j++)
-          for (int64_t i = cl[0]; i <= cl[1]; i++) {
-            int64_t idx[3] = {i, j, k};
-            int64_t l = inddm(pi, i, j, k);
-            int64_t src[3] = {i, j, k};
-            if (type == 11) { src[d] = low ? idx[d] + n_d : idx[d] - n_d; }
-            else if (type == 0) { src[d] = low ? cl[2 * d + 1] + 1 : cl[2 * d] - 1; }
-            else continue;
-            int64_t l1 = inddm(pi, src[0], src[1], src[2]);
-            for (int64_t v = 0; v < neq; v++) {
-              if (type == 11) rop[l + v * nd] = rop[l1 + v * nd] * c1;
-              else rop[l + v * nd] = OMAX(-1.e30, rop[l1 + v * nd]) * c1;
+      if (type == 11 || type == 0) {
+        for (int64_t k = cl[4]; k <= cl[5]; k++)
+          for (int64_t j = cl[2]; j <= cl[3]; j++)
+            for (int64_t i = cl[0]; i <= cl[1]; i++) {
+              int64_t idx[3] = {i, j, k};
+              int64_t l = inddm(pi, i, j, k);
+              int64_t src[3] = {i, j, k};
+              if (type == 11) { src[d] = low ? idx[d] + n_d : idx[d] - n_d; }
+              else { src[d] = low ? cl[2 * d + 1] + 1 : cl[2 * d] - 1; }
+              int64_t l1 = inddm(pi, src[0], src[1], src[2]);
+              for (int64_t v = 0; v < neq; v++) {
+                if (type == 11) rop[l + v * nd] = rop[l1 + v * nd] * c1;
+                else rop[l + v * nd] = OMAX(-1.e30, rop[l1 + v * nd]) * c1;
+              }
+            }
+        continue;
+      }
+      /* the other types: ghost lines normal to the face */
+      int64_t first = low ? cl[2 * d + 1] : cl[2 * d];       /* rank next to the face */
+      int64_t step = low ? -1 : 1;                            /* towards the next ranks */
+      int64_t ir = low ? first + 1 : first - 1;               /* first interior cell */
+      int64_t iref = low ? 2 * first + 1 : 2 * first - 1;     /* mirror: iref - i */
+      int64_t a0 = d == 0 ? 1 : 0, a1 = d == 2 ? 1 : 2;      /* tangential directions */
+      int64_t ta = a0, tb = a1;
+      if (d == 1) { ta = 0; tb = 2; }
+      double snorm = low ? -1. : 1.;
+      double st[5];
+      bc_default_state(pr, st);
+      for (int64_t b = cl[2 * tb]; b <= cl[2 * tb + 1]; b++)
+        for (int64_t a = cl[2 * ta]; a <= cl[2 * ta + 1]; a++) {
+          int64_t c[3];
+          c[ta] = a; c[tb] = b;
+          double t[3];
+          c[d] = first;
+          bc_normal(pi, ti, tj, tk, idir, c[0], c[1], c[2], t);
+          for (int64_t rank = 0; rank < (d == 2 ? pi[NIJK + 4] : pi[NIJK + 3]); rank++) {
+            c[d] = first + step * rank;
+            int64_t l = inddm(pi, c[0], c[1], c[2]);
+            int64_t cm[3] = {c[0], c[1], c[2]};
+            cm[d] = iref - c[d];
+            int64_t ldjr = inddm(pi, cm[0], cm[1], cm[2]);
+            int64_t ci1[3] = {c[0], c[1], c[2]};
+            ci1[d] = ir;
+            int64_t l1 = inddm(pi, ci1[0], ci1[1], ci1[2]);
+            int slip = type == 3 || type == 5 || (type == 4 && pi[IFLOW] == 1);
+            int noslip = (type == 6 || type == 4) && pi[IFLOW] > 1;
+            if (slip) {             /* BCWallInviscid.for */
+              double tcx = t[0], tcy = t[1], tcz = t[2];
+              double surf = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
+              surf = OMAX(surf, 1e-30);
+              double s_1 = 1. / surf;
+              tcx = tcx * s_1; tcy = tcy * s_1; tcz = tcz * s_1;
+              double u = rop[ldjr + nd] - 0., v = rop[ldjr + 2 * nd] - 0., w = rop[ldjr + 3 * nd] - 0.;
+              double qn = u * tcx + v * tcy + w * tcz;
+              double ut = u - qn * tcx, vt = v - qn * tcy, wt = w - qn * tcz;
+              double ua = 2. * ut - u, va = 2. * vt - v, wa = 2. * wt - w;
+              rop[l] = rop[ldjr];
+              rop[l + nd] = 0. + ua; rop[l + 2 * nd] = 0. + va; rop[l + 3 * nd] = 0. + wa;
+              rop[l + 4 * nd] = rop[ldjr + 4 * nd];
+            } else if (noslip) {    /* BCWallViscous.for (adiabatic) */
+              double u = rop[ldjr + nd], v = rop[ldjr + 2 * nd], w = rop[ldjr + 3 * nd];
+              rop[l] = rop[ldjr];
+              rop[l + nd] = 0. - u; rop[l + 2 * nd] = 0. - v; rop[l + 3 * nd] = 0. - w;
+              rop[l + 4 * nd] = rop[ldjr + 4 * nd];
+            } else if (rank == 0 && (type == 1 || type == 13)) {   /* BCFarfield.for / BCInflow_i.for */
+              double tn[3] = {t[0] * snorm, t[1] * snorm, t[2] * snorm};
+              nr_out o;
+              non_reflection(pr, tn, rop, nd, l1, st, &o);
+              double roinv = 1. / o.svar[0];
+              double u = o.u + o.r * o.svar[1] * roinv, v = o.v + o.r * o.svar[2] * roinv,
+                     w = o.w + o.r * o.svar[3] * roinv;
+              rop[l] = o.svar[0];
+              rop[l + nd] = u; rop[l + 2 * nd] = v; rop[l + 3 * nd] = w;
+              rop[l + 4 * nd] = (o.qvar5 * roinv - .5 * (u * u + v * v + w * w)) * cvinv;
+            } else if (rank == 0 && type == 10) {                  /* BCOutflow.for */
+              double roe = rop[l1], rue = rop[l1 + nd] * roe, rve = rop[l1 + 2 * nd] * roe,
+                     rwe = rop[l1 + 3 * nd] * roe;
+              double roe_inv = 1. / st[0];
+              double ete = st[4] - 0.5 * (st[1] * st[1] + st[2] * st[2] + st[3] * st[3]) * roe_inv +
+                           0.5 * (rue * rop[l1 + nd] + rve * rop[l1 + 2 * nd] + rwe * rop[l1 + 3 * nd]);
+              double ext[5] = {roe, rue, rve, rwe, ete};
+              double tn[3] = {t[0] * snorm, t[1] * snorm, t[2] * snorm};
+              nr_out o;
+              non_reflection(pr, tn, rop, nd, l1, ext, &o);
+              rop[l] = rop[l1];
+              double roinv = 1. / rop[l];
+              if (o.qn < 0.) {
+                for (int m = 0; m < 3; m++)
+                  rop[l + (m + 1) * nd] = rop[l1 + (m + 1) * nd] - o.qn / (o.sn * o.sn) * tn[m];
+              } else {
+                for (int m = 0; m < 3; m++) rop[l + (m + 1) * nd] = rop[l1 + (m + 1) * nd];
+              }
+              rop[l + 4 * nd] = (o.qvar5 * roinv - .5 * (rop[l + nd] * rop[l + nd] + rop[l + 2 * nd] * rop[l + 2 * nd] +
+                                                         rop[l + 3 * nd] * rop[l + 3 * nd])) * cvinv;
+            } else if (type == 1 || type == 13) {  /* BC_nextrank.for */
+              int64_t inc = d == 0 ? 1 : (d == 1 ? pi[NIJK] : pi[NIJK] * pi[NIJK + 1]);
+              int64_t dl = -step * inc;            /* towards the interior */
+              int64_t q0 = l + dl, q1 = l + 2 * dl, q2 = l + 3 * dl;
+              rop[l] = rop[q0] * k3 + rop[q1] * k1 + rop[q2] * k2;
+              if (fabs(rop[l] / rop[q0] - 1.) >= 0.7) {
+                for (int v = 0; v < 5; v++) rop[l + v * nd] = rop[q0 + v * nd];
+              } else {
+                for (int v = 1; v < 5; v++)
+                  rop[l + v * nd] = rop[q0 + v * nd] * k3 + rop[q1 + v * nd] * k1 + rop[q2 + v * nd] * k2;
+              }
+            } else if (type == 10) {                /* BC_extrap.for: copy of the first ghost */
+              int64_t cf[3] = {c[0], c[1], c[2]};
+              cf[d] = first;
+              int64_t q0 = inddm(pi, cf[0], cf[1], cf[2]);
+              for (int v = 0; v < 5; v++) rop[l + v * nd] = rop[q0 + v * nd];
             }
           }
+        }
     }
   }
 coins:
@@ -1416,7 +1596,7 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
       if (ntr > 0) or_transfers(zones, tr, ntr, use_p1);
       for (int z = 0; z < nzones; z++) {
         or_zone* Z = &zones[z];
-        or_bc_zone(Z->param_int, Z->param_real, 0, use_p1 ? Z->ro_p1 : Z->ro);
+        or_bc_zone(Z->param_int, Z->param_real, Z->ti, Z->tj, Z->tk, 0, use_p1 ? Z->ro_p1 : Z->ro);
       }
     }
     *first_it = 1;

@@ -76,7 +76,8 @@ void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind_lu,
               const double* coe, int mjrnewton);
 void or_cprdu3s1(const int64_t* pi, int it_bloc, int nssiter,
                  const double* drodm, double* rdm);
-void or_bc_zone(const int64_t* pi, const double* pr, int lrhs, double* rop);
+void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const double* tj,
+                const double* tk, int lrhs, double* rop);
 /* cp_tijk.for + cp_vol.for: face normals * areas and volumes of a zone */
 void or_metric(const int64_t* pi, const double* x, const double* y, const double* z, double* ti,
                double* tj, double* tk, double* vol);

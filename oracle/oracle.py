@@ -125,7 +125,8 @@ class Case:
                 raise ValueError("transfers on level M1 are not used")
             lib.or_transfers(arr, tr, len(self.tr), 1 if level == 2 else 0)
         for e in self.z:
-            lib.or_bc_zone(_i(e["pi"]), _d(e["pr"]), 0, _d(e["lv"][level]))
+            lib.or_bc_zone(_i(e["pi"]), _d(e["pr"]), _d(e["ti"]), _d(e["tj"]), _d(e["tk"]), 0,
+                           _d(e["lv"][level]))
 
     def compute(self, nitrun, nstep_deb, nstep_fin, nit_c=1, modulo_verif=200):
         lib = load()

@@ -216,3 +216,37 @@ def test_curvilinear_implicit_lusgs(oracle_mod, scheme, slope):
     nss = int(zd[0]["pi"][58])
     assert rel_err(s.residuals(0), ref.residual_norms(0, nss)) <= TOL
     s.close()
+
+
+@pytest.mark.parametrize("wall,model,scheme,slope,wavy", [
+    ("BCWallInviscid", "Euler", "roe_min", "minmod", 0.0),
+    ("BCWallViscous", "NSLaminar", "ausmpred", "o3", 0.0),
+    ("BCWallInviscid", "Euler", "roe", "o3", 0.3),
+])
+def test_bcs_explicit(oracle_mod, wall, model, scheme, slope, wavy):
+    """Inflow, outflow, wall, farfield and periodic BCs on one zone
+    (BCzone.cpp: bvbs_inflow / outflow / wall_* / farfield / periodique)."""
+    t = cases.bc_box(n=(16, 12, 6), wall=wall, model=model, scheme=scheme, slope=slope,
+                     wavy=wavy)
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    for lvl in range(2):   # ghost fill alone
+        got = s.download(0, lvl)
+        assert rel_err(got, ref.z[0]["lv"][lvl]) <= TOL
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
+@pytest.mark.parametrize("wall,model,wavy", [("BCWallViscous", "NSLaminar", 0.0),
+                                             ("BCWallInviscid", "Euler", 0.3)])
+def test_bcs_implicit(oracle_mod, wall, model, wavy):
+    t = cases.bc_box(n=(12, 10, 6), wall=wall, model=model, wavy=wavy, temporal="implicit",
+                     ss_iteration=3, scheme="ausmpred", slope="o3", time_step=0.05)
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
+    s.close()

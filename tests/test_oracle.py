@@ -125,3 +125,34 @@ def test_periodic_ghosts_and_corners(oracle_mod):
     a = q[:, 3, 2, 0]   # i0 + i1*is with i=1 -> i1=2: i index 2-2 = 0
     b = q[:, 3, 0, 2]
     assert np.array_equal(e, (a + b) * 0.5)
+
+
+def test_free_stream_with_characteristic_bcs(oracle_mod):
+    """The free stream is a solution with inflow, outflow, farfield and a
+    slip wall aligned with it: the characteristic BCs (non_reflection.for)
+    rebuild the free stream in the ghost cells."""
+    t = cases.bc_box(n=(12, 10, 6), perturb=0.0, wall="BCWallInviscid", model="Euler")
+    zd, c = _case(t, oracle_mod)
+    q0 = c.z[0]["lv"][0].copy()
+    for it in range(1, 4):
+        c.compute(it, 1, 3, 1, modulo_verif=1000)
+    assert np.max(np.abs(c.z[0]["lv"][0] - q0)) < 1e-14
+
+
+def test_wall_ghosts(oracle_mod):
+    """Slip wall: mirror state with the normal velocity reversed; no-slip
+    adiabatic wall: mirror state with the velocity reversed."""
+    for wall, model, flip in (("BCWallInviscid", "Euler", (1, -1, 1)),
+                              ("BCWallViscous", "NSLaminar", (-1, -1, -1))):
+        t = cases.bc_box(n=(8, 6, 4), wall=wall, model=model)
+        zd, c = _case(t, oracle_mod)
+        pi = zd[0]["pi"]
+        ni, nj, nk = (int(pi[0]), int(pi[1]), int(pi[2]))
+        q = c.z[0]["lv"][0].reshape(5, nk, nj, ni)
+        for g, m in ((1, 2), (0, 3)):          # ghost j index -> mirror j index
+            for v, sgn in zip((1, 2, 3), flip):
+                a = q[v, 2:nk - 2, g, 2:ni - 2]
+                b = q[v, 2:nk - 2, m, 2:ni - 2]
+                assert np.array_equal(a, sgn * b)
+            for v in (0, 4):
+                assert np.array_equal(q[v, 2:nk - 2, g, 2:ni - 2], q[v, 2:nk - 2, m, 2:ni - 2])
