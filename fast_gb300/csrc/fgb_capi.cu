@@ -473,8 +473,6 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   std::vector<double> hti(ti, ti + ndm * nmtr_ij), htj(tj, tj + ndm * nmtr_ij),
       htk(tk, tk + ndm * nmtr_ij), hvol(vol, vol + ndm);
   fill_zone(Z, ti, tj, tk, vol);
-  if (Z.z.iflow >= 2 && Z.z.typ != Z3DCART)
-    return fail(FGB_ERR_ARG, "viscous fluxes on curvilinear zones are not implemented on the GPU path");
   size_t st_bytes = sizeof(double) * neq * nd;
   for (int i = 0; i < 3; i++) {
     CK(cudaMalloc(&Z.lvl[i], st_bytes));

@@ -336,6 +336,70 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
   }
 }
 
+// ------------------------------------------------------ viscous (full)
+// fluvisq_3dfull_{i,j,k}.for + mut_interface.for on a 3d general zone, face
+// D of cell l: Green-Gauss gradient over the cell joining il = l - inc_D and
+// ir = l, with the transverse directions A = D+1, B = D+2 (mod 3) -- the
+// three reference files are this routine for (D, A, B) = (i,j,k), (j,k,i),
+// (k,i,j).
+template <int D>
+__device__ __forceinline__ void visc_full(const Zone& z, const double* __restrict__ q,
+                                          const double* __restrict__ xmut, int64_t l, int64_t lt,
+                                          double tcx, double tcy, double tcz, double F[5]) {
+  constexpr int A = (D + 1) % 3, B = (D + 2) % 3;
+  const int64_t nd = z.nd, ndm = z.ndm;
+  const double* TD = D == 0 ? z.ti : (D == 1 ? z.tj : z.tk);
+  const double* TA = A == 0 ? z.ti : (A == 1 ? z.tj : z.tk);
+  const double* TB = B == 0 ? z.ti : (B == 1 ? z.tj : z.tk);
+  const int64_t mD = z.minc[D], mA = z.minc[A], mB = z.minc[B];
+  const int64_t iA = z.inc[A], iB = z.inc[B];
+  const int64_t ltm = lt - mD, ltp = lt + mD, ltA = lt + mA, ltAm = lt + mA - mD, ltB = lt + mB,
+                ltBm = lt + mB - mD;
+  double t0[3], t1[3], ta0[3], ta1[3], tb0[3], tb1[3];
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    const int64_t o = m * ndm;
+    t0[m] = .5 * (TD[lt + o] + TD[ltm + o]);
+    t1[m] = .5 * (TD[lt + o] + TD[ltp + o]);
+    ta0[m] = .125 * (TA[lt + o] + TA[ltm + o]);
+    ta1[m] = .125 * (TA[ltA + o] + TA[ltAm + o]);
+    tb0[m] = .125 * (TB[lt + o] + TB[ltm + o]);
+    tb1[m] = .125 * (TB[ltB + o] + TB[ltBm + o]);
+  }
+  const int64_t il = l - z.inc[D], ir = l;
+  double g[4][3];
+#pragma unroll
+  for (int v = 0; v < 4; v++) {
+    const double* Q = q + (v + 1) * nd;
+    const double f1 = Q[il], f2 = Q[ir];
+    const double f3 = Q[ir] + Q[il] + Q[il - iA] + Q[ir - iA];
+    const double f4 = Q[ir] + Q[il] + Q[il + iA] + Q[ir + iA];
+    const double f5 = Q[ir] + Q[il] + Q[il - iB] + Q[ir - iB];
+    const double f6 = Q[ir] + Q[il] + Q[il + iB] + Q[ir + iB];
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+      g[v][m] = (f2 * t1[m] - f1 * t0[m]) + (f4 * ta1[m] - f3 * ta0[m]) + (f6 * tb1[m] - f5 * tb0[m]);
+  }
+  const double div = (g[0][0] + g[1][1] + g[2][2]) * z.cvisq;
+  const double e1 = g[0][0] - div, e2 = g[0][1] + g[1][0], e3 = g[0][2] + g[2][0];
+  const double e4 = g[1][1] - div, e5 = g[1][2] + g[2][1], e6 = g[2][2] - div;
+  const double volinv = 1. / (z.vol[lt] + z.vol[ltm]);
+  const double xmutvol = (xmut[ir] + xmut[il]) * volinv;
+  const double xktvol = xmutvol * z.gam3;
+  double fv, fv5;
+  fv = -(2. * e1 * tcx + e2 * tcy + e3 * tcz) * xmutvol;
+  fv5 = fv * (q[ir + nd] + q[il + nd]);
+  F[1] = F[1] + fv;
+  fv = -(e2 * tcx + 2. * e4 * tcy + e5 * tcz) * xmutvol;
+  fv5 = fv5 + fv * (q[ir + 2 * nd] + q[il + 2 * nd]);
+  F[2] = F[2] + fv;
+  fv = -(e3 * tcx + e5 * tcy + 2. * e6 * tcz) * xmutvol;
+  fv5 = fv5 + fv * (q[ir + 3 * nd] + q[il + 3 * nd]);
+  F[3] = F[3] + fv;
+  fv = fv5 * 0.5 - (g[3][0] * tcx + g[3][1] * tcy + g[3][2] * tcz) * xktvol;
+  F[4] = F[4] + fv;
+}
+
 // ------------------------------------------------------------- face kernel
 // One thread per face of direction D; faces of direction D are indexed
 // f = ii + NI*(jj + NJ*kk) over the interior face box (NI = ni+1 for D=0 ...).
@@ -377,6 +441,7 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     double s = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
     if (KF == ROE) roe_full(z, qm, qp, tcx, tcy, tcz, s, F);
     else ausm_face<D, false>(z, qm, qp, q[l + 4 * nd], tcx, tcy, tcz, s, F);
+    if (VISC) visc_full<D>(z, q, xmut, l, lt, tcx, tcy, tcz, F);
   }
 #pragma unroll
   for (int v = 0; v < 5; v++) Fo[v * nf + f] = F[v];
@@ -507,13 +572,17 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
       return visc ? launch_faces_t<Z3DCART, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z3DCART, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
-  } else if (z.typ == Z3DFULL && !visc) {
+  } else if (z.typ == Z3DFULL) {
     if (z.kflu == ROE) {
-      if (z.slope == O1) return launch_faces_t<Z3DFULL, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == O3) return launch_faces_t<Z3DFULL, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == MINMOD) return launch_faces_t<Z3DFULL, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O1) return visc ? launch_faces_t<Z3DFULL, ROE, O1, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                     : launch_faces_t<Z3DFULL, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O3) return visc ? launch_faces_t<Z3DFULL, ROE, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                     : launch_faces_t<Z3DFULL, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == MINMOD) return visc ? launch_faces_t<Z3DFULL, ROE, MINMOD, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                         : launch_faces_t<Z3DFULL, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
     } else if (z.kflu == AUSM && z.slope == O3) {
-      return launch_faces_t<Z3DFULL, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      return visc ? launch_faces_t<Z3DFULL, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DFULL, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
   }
   return cudaErrorNotSupported;

@@ -554,6 +554,65 @@ static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
   }
 }
 
+/* Viscous face flux on a 3d general zone: Compute/fluvisq_3dfull_{i,j,k}.for
+ * + mut_interface.for.  Green-Gauss gradient over the cell joining il =
+ * l - inc_d and ir = l: faces normal to d at the two cell centres (mean of
+ * two face vectors), faces along the transverse directions a = d+1, b = d+2
+ * (mod 3) from four-cell means (factor 1/8 = 1/4 x 1/2).  The three files
+ * are this routine with (d, a, b) = (i, j, k), (j, k, i), (k, i, j). */
+static void visc_full(const fctx* c, int d, int64_t l, int64_t lt, double tcx, double tcy,
+                      double tcz, double flu[5]) {
+  const double* rop = c->rop;
+  const int64_t nd = c->nd, ndm = c->ndm;
+  const int a = (d + 1) % 3, b = (d + 2) % 3;
+  const double* T3[3] = {c->ti, c->tj, c->tk};
+  const double *TD = T3[d], *TA = T3[a], *TB = T3[b];
+  const int64_t mD = c->inc_mtr[d], mA = c->inc_mtr[a], mB = c->inc_mtr[b];
+  const int64_t iA = c->inc[a], iB = c->inc[b];
+  const int64_t ltm = lt - mD, ltp = lt + mD, ltA = lt + mA, ltAm = lt + mA - mD,
+                ltB = lt + mB, ltBm = lt + mB - mD;
+  double t0[3], t1[3], ta0[3], ta1[3], tb0[3], tb1[3];
+  for (int m = 0; m < 3; m++) {
+    const int64_t o = m * ndm;
+    t0[m] = .5 * (TD[lt + o] + TD[ltm + o]);
+    t1[m] = .5 * (TD[lt + o] + TD[ltp + o]);
+    ta0[m] = .125 * (TA[lt + o] + TA[ltm + o]);
+    ta1[m] = .125 * (TA[ltA + o] + TA[ltAm + o]);
+    tb0[m] = .125 * (TB[lt + o] + TB[ltm + o]);
+    tb1[m] = .125 * (TB[ltB + o] + TB[ltBm + o]);
+  }
+  const int64_t il = l - c->inc[d], ir = l;
+  double g[4][3];
+  for (int v = 0; v < 4; v++) {
+    const double* q = rop + (v + 1) * nd;
+    double f1 = q[il], f2 = q[ir];
+    double f3 = q[ir] + q[il] + q[il - iA] + q[ir - iA];
+    double f4 = q[ir] + q[il] + q[il + iA] + q[ir + iA];
+    double f5 = q[ir] + q[il] + q[il - iB] + q[ir - iB];
+    double f6 = q[ir] + q[il] + q[il + iB] + q[ir + iB];
+    for (int m = 0; m < 3; m++)
+      g[v][m] = (f2 * t1[m] - f1 * t0[m]) + (f4 * ta1[m] - f3 * ta0[m]) + (f6 * tb1[m] - f5 * tb0[m]);
+  }
+  const double div = (g[0][0] + g[1][1] + g[2][2]) * c->cvisq;
+  const double f1 = g[0][0] - div, f2 = g[0][1] + g[1][0], f3 = g[0][2] + g[2][0];
+  const double f4 = g[1][1] - div, f5 = g[1][2] + g[2][1], f6 = g[2][2] - div;
+  const double volinv = 1. / (c->vol[lt] + c->vol[ltm]);
+  const double xmutvol = (c->xmut[ir] + c->xmut[il]) * volinv;
+  const double xktvol = xmutvol * c->gam3;
+  double fv, fv5;
+  fv = -(2. * f1 * tcx + f2 * tcy + f3 * tcz) * xmutvol;
+  fv5 = fv * (rop[ir + nd] + rop[il + nd]);
+  flu[1] = flu[1] + fv;
+  fv = -(f2 * tcx + 2. * f4 * tcy + f5 * tcz) * xmutvol;
+  fv5 = fv5 + fv * (rop[ir + 2 * nd] + rop[il + 2 * nd]);
+  flu[2] = flu[2] + fv;
+  fv = -(f3 * tcx + f5 * tcy + 2. * f6 * tcz) * xmutvol;
+  fv5 = fv5 + fv * (rop[ir + 3 * nd] + rop[il + 3 * nd]);
+  flu[3] = flu[3] + fv;
+  fv = fv5 * 0.5 - (g[3][0] * tcx + g[3][1] * tcy + g[3][2] * tcz) * xktvol;
+  flu[4] = flu[4] + fv;
+}
+
 /* One face flux (convective + viscous) of direction d at cell (i,j,k). */
 static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, double flu[5]) {
   int64_t l = inddm(c->pi, i, j, k);
@@ -568,7 +627,10 @@ static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, dou
   }
   if (c->kflu == 5) roe_face(c, qm, qp, tcx, tcy, tcz, s, flu);
   else ausm_face(c, qm, qp, c->rop[l + 4 * c->nd], tcx, tcy, tcz, s, flu);
-  if (c->iflow >= 2) visc_cart(c, d, l, flu);
+  if (c->iflow >= 2) {
+    if (c->typ == 2) visc_cart(c, d, l, flu);
+    else visc_full(c, d, l, lt, tcx, tcy, tcz, flu);
+  }
 }
 
 /* Flux balance of template_FluxAndBalance.for:192-271 for one zone: every

@@ -250,3 +250,32 @@ def test_bcs_implicit(oracle_mod, wall, model, wavy):
         s.compute(it, 1, 4, 1, 1)
     _check_levels(ref, s)
     s.close()
+
+
+@pytest.mark.parametrize("scheme,slope", [("roe", "o3"), ("ausmpred", "o3")])
+def test_curvilinear_viscous_explicit(oracle_mod, scheme, slope):
+    """fluvisq_3dfull_{i,j,k}.for on a periodic curvilinear mesh."""
+    t = cases.taylor_green(n=(12, 10, 8), wavy=0.3, reynolds=100.0, scheme=scheme, slope=slope,
+                           dt=0.02, numb={"temporal_scheme": "explicit", "ss_iteration": 1,
+                                          "modulo_verif": 1000})
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    assert int(zd[0]["pi"][25]) == 0 and int(zd[0]["pi"][27]) == 2
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
+def test_curvilinear_viscous_implicit_with_walls(oracle_mod):
+    """Implicit LU-SGS, Navier-Stokes, curvilinear mesh, no-slip wall,
+    inflow / outflow / farfield."""
+    t = cases.bc_box(n=(12, 10, 6), wall="BCWallViscous", model="NSLaminar", wavy=0.3,
+                     temporal="implicit", ss_iteration=3, scheme="ausmpred", slope="o3",
+                     time_step=0.05, reynolds=500.0)
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
+    s.close()

@@ -80,3 +80,25 @@ def test_conservation_curvilinear(oracle_mod):
     c.compute(1, 1, 3, 1, modulo_verif=1000)
     w1, scale = total(c.z[0]["lv"][0])
     assert np.all(np.abs(w1 - w0) <= 1e-13 * scale)
+
+
+def test_free_stream_preservation_curvilinear_viscous(oracle_mod):
+    """Navier-Stokes on the curvilinear mesh: the Green-Gauss cells of
+    fluvisq_3dfull_*.for are closed, so a uniform field has no gradient."""
+    t = cases.taylor_green(n=(10, 8, 6), wavy=0.3, mach=0.2, ss_iteration=2, dt=0.05,
+                           numb={"temporal_scheme": "explicit", "ss_iteration": 1,
+                                 "modulo_verif": 1000})
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    # uniform state (moving): ro = 1, u = (0.2, -0.1, 0.05), T = 1/(gamma cv)
+    nd = int(zd[0]["pi"][41])
+    for key in ("ro", "ro_m1", "ro_p1"):
+        q = zd[0][key].reshape(5, nd)
+        q[0], q[1], q[2], q[3] = 1.0, 0.2, -0.1, 0.05
+        q[4] = q[4].mean()
+    c = oracle_mod.Case(zd)
+    c.apply_bc(0)
+    c.apply_bc(1)
+    q0 = c.z[0]["lv"][0].copy()
+    for it in range(1, 3):
+        c.compute(it, 1, 3, 1, modulo_verif=1000)
+    assert np.max(np.abs(c.z[0]["lv"][0] - q0)) < 1e-13
