@@ -61,6 +61,7 @@ struct ZoneData {
   double *drodm = nullptr, *coe = nullptr, *xmut = nullptr, *rdm = nullptr;
   double *ti = nullptr, *tj = nullptr, *tk = nullptr, *vol = nullptr;
   double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
+  double* wig = nullptr;            // senseur wiggle flags (KFLUDOM = 2)
   void* luwork = nullptr;           // plane-ordered LU work (FP64-sized)
   uint32_t* cells = nullptr;        // interior cells by hyperplane
   int64_t* plane = nullptr;         // plane offsets (device)
@@ -431,6 +432,7 @@ int fgb_destroy(fgb_solver* s) {
       cudaFree(g.dst); cudaFree(g.src); cudaFree(g.q0); cudaFree(g.q1); cudaFree(g.q2);
       cudaFree(g.nrm);
     }
+    cudaFree(Z.wig);
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
   for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
@@ -489,6 +491,12 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   CK(dev_upload(&Z.tk, htk)); CK(dev_upload(&Z.vol, hvol));
   Z.z.ti = Z.ti; Z.z.tj = Z.tj; Z.z.tk = Z.tk; Z.z.vol = Z.vol;
   int64_t ni = Z.z.ni, nj = Z.z.nj, nk = Z.z.nk;
+  if (p[KFLUDOM] == SENSEUR) {
+    CK(cudaMalloc(&Z.wig, sizeof(double) * 3 * nd));
+    CK(cudaMemset(Z.wig, 0, sizeof(double) * 3 * nd));
+  }
+  Z.z.wig = Z.wig;
+  Z.z.opt0 = (double)p[SENSORTYPE];
   CK(cudaMalloc(&Z.Fi, sizeof(double) * 5 * (ni + 1) * nj * nk));
   CK(cudaMalloc(&Z.Fj, sizeof(double) * 5 * ni * (nj + 1) * nk));
   CK(cudaMalloc(&Z.Fk, sizeof(double) * 5 * ni * nj * (nk + 1)));
@@ -743,6 +751,11 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             CK(launch_coefficients(z, ca, s->st));
           }
           s->launches++;
+        }
+        if (nstep == 1 && z.kflu == SENSEUR) {  // src_term.for:257-266
+          ProfScope ps(s, "wiggle");
+          CK(launch_wiggle(z, ssiter, Z.wig, s->st));
+          s->launches += 3;
         }
         cudaError_t e;
         {

@@ -23,7 +23,7 @@ enum PI : int {
   IFLOW = 27, ILES = 28, ITYPCP = 29, SIZE_SSDOM = 30, KFLUDOM = 33, LALE = 34, NEQ = 36,
   NEQ_IJ = 37, NEQ_K = 38, NEQ_COE = 39, NDIMDX = 41, NDIMDX_MTR = 43, DTLOC = 46,
   RK = 52, LEVEL = 53, EXPLOC = 54, NSSITER = 58, SLOPE = 64, PT_BC = 70, NB_RELAX = 71,
-  LU_MATCH = 75
+  LU_MATCH = 75, SENSORTYPE = 85
 };
 enum PR : int {
   DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6, MINF = 7,
@@ -48,6 +48,8 @@ struct Zone {
   // constants of template_FluxAndBalance.for:108-156 and friends
   double gam, rgp, gam1, gam3, cv, dtc, psiroe, wig_cte, tmin_1;
   double cvinv;   // 1/cv (mjr_newton.for computes it once per call)
+  const double* wig;   // senseur wiggle flags, 3 x NDIMDX (KFLUDOM = 2)
+  double opt0;         // float(SENSORTYPE)
   double c1, c2, c3, c4, c5, c6, cvisq;
   double tcx, tcy, tcz, si, sj, sk, volinv;  // 3d cartesian metric
   double prandt, xmul0, temp0, cs;

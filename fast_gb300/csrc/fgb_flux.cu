@@ -178,10 +178,10 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
 // AUSM/fluFaceEuler.for:36-57 + etat_GD.for + Vit_ent/fluvector_*.for.
 // NX = number of non-zero normal components the face can have (1: cartesian
 // face of direction D, 3: general).
-template <int D, bool CART>
+template <int D, bool CART, bool SENS = false>
 __device__ __forceinline__ void ausm_face(const Zone& z, const double qm[5], const double qp[5],
                                           double tl, double tcx, double tcy, double tcz,
-                                          double s, double F[5]) {
+                                          double s, double F[5], double wg = 0.) {
   const double rgp = z.rgp, gam1 = z.gam1;
   double r1 = qp[0], rou1 = r1 * qp[1], rov1 = r1 * qp[2], row1 = r1 * qp[3];
   double p1 = r1 * qp[4] * rgp;
@@ -198,12 +198,18 @@ __device__ __forceinline__ void ausm_face(const Zone& z, const double qm[5], con
     qn1 = qp[1] * tcx + qp[2] * tcy + qp[3] * tcz;
     qn2 = qm[1] * tcx + qm[2] * tcy + qm[3] * tcz;
   }
-  double cc = rgp * z.gam * tl;  // c^2 from the temperature of cell l
-  double son = sqrt(qn1 * qn1 / cc);
-  double tam = z.c3 * son + s;
-  double tam1 = fmaxF(0., tam) * z.c2;
-  double u = 0.25 * (qn1 + qn2) - tam1 * (p2 - p1);
-  double tdu = fmaxF(fabs(u), z.c1 * s) * z.wig_cte;
+  double u, tdu;
+  if (SENS) {  // SENSOR/fluFaceEuler.for: Rhie-Chow term and dissipation switched by wig
+    u = 0.25 * (qn1 + qn2) - z.c2 * s * (p2 - p1) * (z.opt0 * wg + 1. - z.opt0);
+    tdu = fmaxF(fabs(u), z.c1 * s) * wg;
+  } else {
+    double cc = rgp * z.gam * tl;  // c^2 from the temperature of cell l
+    double son = sqrt(qn1 * qn1 / cc);
+    double tam = z.c3 * son + s;
+    double tam1 = fmaxF(0., tam) * z.c2;
+    u = 0.25 * (qn1 + qn2) - tam1 * (p2 - p1);
+    tdu = fmaxF(fabs(u), z.c1 * s) * z.wig_cte;
+  }
   double p1p2 = (p1 + p2) * 0.5;
   F[0] = u * (r1 + r2) - tdu * (r2 - r1);
   F[1] = u * (rou1 + rou2) - tdu * (rou2 - rou1);
@@ -431,8 +437,9 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
   double F[5];
   if (TYP == Z3DCART) {
     if (KF == ROE) roe_cart<D>(z, qm, qp, F);
-    else ausm_face<D, true>(z, qm, qp, q[l + 4 * nd], z.tcx, z.tcy, z.tcz,
-                            D == 0 ? z.si : (D == 1 ? z.sj : z.sk), F);
+    else ausm_face<D, true, KF == SENSEUR>(z, qm, qp, q[l + 4 * nd], z.tcx, z.tcy, z.tcz,
+                                          D == 0 ? z.si : (D == 1 ? z.sj : z.sk), F,
+                                          KF == SENSEUR ? z.wig[l + D * nd] : 0.);
     if (VISC) visc_cart<D>(z, q, xmut, l, F);
   } else {
     const int64_t lt = indmtr(z, ii + 1, jj + 1, kk + 1);
@@ -440,7 +447,8 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     double tcx = t[lt], tcy = t[lt + z.ndm], tcz = t[lt + 2 * z.ndm];
     double s = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
     if (KF == ROE) roe_full(z, qm, qp, tcx, tcy, tcz, s, F);
-    else ausm_face<D, false>(z, qm, qp, q[l + 4 * nd], tcx, tcy, tcz, s, F);
+    else ausm_face<D, false, KF == SENSEUR>(z, qm, qp, q[l + 4 * nd], tcx, tcy, tcz, s, F,
+                                           KF == SENSEUR ? z.wig[l + D * nd] : 0.);
     if (VISC) visc_full<D>(z, q, xmut, l, lt, tcx, tcy, tcz, F);
   }
 #pragma unroll
@@ -571,6 +579,9 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
     } else if (z.kflu == AUSM && z.slope == O3) {
       return visc ? launch_faces_t<Z3DCART, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z3DCART, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+    } else if (z.kflu == SENSEUR && z.slope == O3) {
+      return visc ? launch_faces_t<Z3DCART, SENSEUR, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DCART, SENSEUR, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
   } else if (z.typ == Z3DFULL) {
     if (z.kflu == ROE) {
@@ -583,9 +594,49 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
     } else if (z.kflu == AUSM && z.slope == O3) {
       return visc ? launch_faces_t<Z3DFULL, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z3DFULL, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+    } else if (z.kflu == SENSEUR && z.slope == O3) {
+      return visc ? launch_faces_t<Z3DFULL, SENSEUR, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DFULL, SENSEUR, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
   }
   return cudaErrorNotSupported;
+}
+
+// ------------------------------------------------------------ wiggle
+// SENSOR/wiggle2001.for + wiggle.for (3-d): flag of the D-face of cell l
+// (faces indexed like face_flux, so the last imax+1 / jmax+1 / kmax+1
+// planes are included): 1 if, for some variable, both slope products
+// (q_{l-1}-q_{l-2})(q_l-q_{l-1}) and (q_l-q_{l-1})(q_{l+1}-q_l) are
+// negative (min of sign sums < -1e-12), else 0.
+template <int D>
+__global__ void __launch_bounds__(128) wiggle(Zone z, const double* __restrict__ q,
+                                              double* __restrict__ wig) {
+  const int64_t NI = z.ni + (D == 0), NJ = z.nj + (D == 1), NK = z.nk + (D == 2);
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= NI * NJ * NK) return;
+  const int64_t ii = f % NI, r = f / NI, jj = r % NJ, kk = r / NJ;
+  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1), inc = z.inc[D], nd = z.nd;
+  const int64_t nm = l - inc, nm2 = l - 2 * inc, np = l + inc;
+  double test = 0.;
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    const double* Q = q + v * nd;
+    const double qm = (Q[nm] - Q[nm2]) * (Q[l] - Q[nm]);
+    const double qp = (Q[l] - Q[nm]) * (Q[np] - Q[l]);
+    const double fv = fsignF(1., qm) + fsignF(1., qp);
+    test = v == 0 ? fv : fminF(test, fv);
+  }
+  wig[l + D * nd] = test < -1e-12 ? 1. : 0.;
+}
+
+cudaError_t launch_wiggle(const Zone& z, const double* q, double* wig, cudaStream_t st) {
+  const int B = 128;
+  const int64_t nfi = (z.ni + 1) * z.nj * z.nk, nfj = z.ni * (z.nj + 1) * z.nk,
+                nfk = z.ni * z.nj * (z.nk + 1);
+  wiggle<0><<<(unsigned)((nfi + B - 1) / B), B, 0, st>>>(z, q, wig);
+  wiggle<1><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, wig);
+  wiggle<2><<<(unsigned)((nfk + B - 1) / B), B, 0, st>>>(z, q, wig);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_assemble(const Zone& z, const StageArgs& a, bool implicit, cudaStream_t st) {

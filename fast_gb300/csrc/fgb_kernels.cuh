@@ -20,6 +20,7 @@ struct StageArgs {
 };
 cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
                          double* Fj, double* Fk, cudaStream_t st);
+cudaError_t launch_wiggle(const Zone& z, const double* q, double* wig, cudaStream_t st);
 cudaError_t launch_assemble(const Zone& z, const StageArgs& a, bool implicit, cudaStream_t st);
 
 // fgb_lu.cu: coefficients and LU-SGS

@@ -28,7 +28,7 @@ enum { NIJK = 0, NIJK_MTR = 5, NIJK_XYZ = 10, IJKV = 20, ITYPZONE = 25, IFLOW = 
        ITYPCP = 29, SIZE_SSDOM = 30, KFLUDOM = 33, LALE = 34, NEQ = 36,
        NEQ_IJ = 37, NEQ_K = 38, NEQ_COE = 39, NDIMDX = 41, NDIMDX_MTR = 43,
        DTLOC = 46, RK = 52, LEVEL = 53, EXPLOC = 54, NSSITER = 58, SLOPE = 64,
-       PT_BC = 70, NB_RELAX = 71, LU_MATCH = 75 };
+       PT_BC = 70, NB_RELAX = 71, LU_MATCH = 75, SENSORTYPE = 85 };
 enum { DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6,
        PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14,
        PSIROE = 34, WIG_AMP = 72, VXINF = 19, VYINF = 20, VZINF = 21 };
@@ -247,6 +247,7 @@ typedef struct {
   int typ, iflow, kflu, slope;
   double gam, rgp, gam1, gam3, c1, c2, c3, c4, c5, c6, cvisq, psiroe, wig_cte, tmin_1;
   double tcx, tcy, tcz, si, sj, sk, volinv; /* 3d cartesian constants */
+  const double* wig; double opt0;           /* senseur (KFLUDOM = 2) */
 } fctx;
 
 static void fctx_init(fctx* c, const int64_t* pi, const double* pr, const double* rop,
@@ -278,6 +279,8 @@ static void fctx_init(fctx* c, const int64_t* pi, const double* pr, const double
   c->c5 = 2. * c6;
   c->c6 = -1. * c6;
   c->cvisq = 1. / 3;
+  c->wig = NULL;
+  c->opt0 = (double)pi[SENSORTYPE];
 }
 
 /* Slope/minmod_slope_var.for:1-17 limiter */
@@ -404,7 +407,7 @@ static void roe_face(const fctx* c, const double qm[5], const double qp[5],
  * Vit_ent/fluvector_3dfull_i.for:1-5.  Same general-form remark as Roe.
  * tl = temperature of cell l (the right cell), used for the sound speed. */
 static void ausm_face(const fctx* c, const double qm[5], const double qp[5], double tl,
-                      double tcx, double tcy, double tcz, double s, double flu[5]) {
+                      double tcx, double tcy, double tcz, double s, double wg, double flu[5]) {
   double rgp = c->rgp, gam1 = c->gam1;
   double r1 = qp[0], rou1 = r1 * qp[1], rov1 = r1 * qp[2], row1 = r1 * qp[3];
   double p1 = r1 * qp[4] * rgp;
@@ -415,11 +418,17 @@ static void ausm_face(const fctx* c, const double qm[5], const double qp[5], dou
   double qn1 = qp[1] * tcx + qp[2] * tcy + qp[3] * tcz;
   double qn2 = qm[1] * tcx + qm[2] * tcy + qm[3] * tcz;
   double cc = rgp * c->gam * tl;
-  double son = sqrt(qn1 * qn1 / cc);
-  double tam = c->c3 * son + s;
-  double tam1 = OMAX(0., tam) * c->c2;
-  double u = 0.25 * (qn1 + qn2) - tam1 * (p2 - p1);
-  double tdu = OMAX(fabs(u), c->c1 * s) * c->wig_cte;
+  double u, tdu;
+  if (c->kflu == 2) {  /* SENSOR/fluFaceEuler.for: Rhie-Chow term and dissipation switched by wig */
+    u = 0.25 * (qn1 + qn2) - c->c2 * s * (p2 - p1) * (c->opt0 * wg + 1. - c->opt0);
+    tdu = OMAX(fabs(u), c->c1 * s) * wg;
+  } else {
+    double son = sqrt(qn1 * qn1 / cc);
+    double tam = c->c3 * son + s;
+    double tam1 = OMAX(0., tam) * c->c2;
+    u = 0.25 * (qn1 + qn2) - tam1 * (p2 - p1);
+    tdu = OMAX(fabs(u), c->c1 * s) * c->wig_cte;
+  }
   double p1p2 = (p1 + p2) * 0.5;
   flu[0] = u * (r1 + r2) - tdu * (r2 - r1);
   flu[1] = u * (rou1 + rou2) - tdu * (rou2 - rou1) + tcx * p1p2;
@@ -626,7 +635,8 @@ static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, dou
     face_normal(c, d, lt, &tcx, &tcy, &tcz, &s);
   }
   if (c->kflu == 5) roe_face(c, qm, qp, tcx, tcy, tcz, s, flu);
-  else ausm_face(c, qm, qp, c->rop[l + 4 * c->nd], tcx, tcy, tcz, s, flu);
+  else ausm_face(c, qm, qp, c->rop[l + 4 * c->nd], tcx, tcy, tcz, s,
+                 c->wig ? c->wig[l + d * c->nd] : 0., flu);
   if (c->iflow >= 2) {
     if (c->typ == 2) visc_cart(c, d, l, flu);
     else visc_full(c, d, l, lt, tcx, tcy, tcz, flu);
@@ -637,11 +647,45 @@ static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, dou
  * face flux is computed once; each interior cell then receives, in the
  * order the reference's k/j/i loop nest produces, drodm + F_k(lo) + F_j(lo)
  * + F_i(lo) - F_i(hi) - F_j(hi) - F_k(hi). */
+/* SENSOR/wiggle2001.for + wiggle.for (3-d): for the d-face of cell l,
+ * f_v = sign(1, (q_{l-1}-q_{l-2})(q_l-q_{l-1})) + sign(1, (q_l-q_{l-1})(q_{l+1}-q_l))
+ * for the 5 variables; wig = 1 if min_v f_v < -1e-12.  Cells of ind plus
+ * the imax+1 / jmax+1 / kmax+1 planes of the last faces. */
+static double wig_face(const int64_t* pi, const double* rop, int64_t l, int64_t inc) {
+  const int64_t nd = pi[NDIMDX], nm = l - inc, nm2 = l - 2 * inc, np = l + inc;
+  double test = 0.;
+  for (int v = 0; v < 5; v++) {
+    const double* q = rop + v * nd;
+    double qm = (q[nm] - q[nm2]) * (q[l] - q[nm]);
+    double qp = (q[l] - q[nm]) * (q[np] - q[l]);
+    double f = fsign(1., qm) + fsign(1., qp);
+    test = v == 0 ? f : OMIN(test, f);
+  }
+  return test < -1e-12 ? 1. : 0.;
+}
+
+void or_wiggle(const int64_t* pi, const int64_t* ind, const double* rop, double* wig) {
+  const int64_t nd = pi[NDIMDX];
+  const int64_t inc[3] = {1, pi[NIJK], pi[NIJK] * pi[NIJK + 1]};
+  const int64_t hi[3] = {ind[1], ind[3], ind[5]};
+  const int64_t corr[3] = {ind[1] == pi[IJKV], ind[3] == pi[IJKV + 1], ind[5] == pi[IJKV + 2]};
+  for (int d = 0; d < 3; d++)
+    for (int64_t k = ind[4]; k <= ind[5] + (d == 2 ? corr[2] : 0); k++)
+      for (int64_t j = ind[2]; j <= ind[3] + (d == 1 ? corr[1] : 0); j++)
+        for (int64_t i = ind[0]; i <= ind[1] + (d == 0 ? corr[0] : 0); i++) {
+          const int64_t l = inddm(pi, i, j, k);
+          wig[l + d * nd] = wig_face(pi, rop, l, inc[d]);
+        }
+  (void)hi;
+}
+
 void or_flux(const int64_t* pi, const double* pr, const int64_t* ind,
              const double* rop, double* drodm, const double* xmut,
-             const double* ti, const double* tj, const double* tk, const double* vol) {
+             const double* ti, const double* tj, const double* tk, const double* vol,
+             const double* wig) {
   fctx c;
   fctx_init(&c, pi, pr, rop, xmut, ti, tj, tk, vol);
+  c.wig = wig;
   int64_t ni = ind[1] - ind[0] + 1, nj = ind[3] - ind[2] + 1, nk = ind[5] - ind[4] + 1;
   int two_d = (c.typ == 3);
   int64_t fi = (ni + 1) * nj * nk, fj = ni * (nj + 1) * nk, fk = ni * nj * (nk + 1);
@@ -1630,7 +1674,9 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
           }
         }
         or_init_rhs(pi, nstep, sdm, Z->drodm);
-        or_flux(pi, pr, sdm, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
+        /* src_term.for:257-266: senseur wiggle on the first sub-step */
+        if (pi[KFLUDOM] == 2 && nstep == 1) or_wiggle(pi, sdm, ssiter, Z->wig);
+        or_flux(pi, pr, sdm, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol, Z->wig);
         if (implicit) {
           or_core3as2(pi, pr, nstep, *first_it, sdm, ssiter, Z->ro, Z->ro_m1, Z->drodm, Z->coe);
           if (lssiter_verif) or_cprdu3s1(pi, nstep, (int)nssiter, Z->drodm, Z->rdm);

@@ -40,6 +40,7 @@ typedef struct {
   double* coe;    /* dt/vol, spectral radii, LU diagonal: NEQ_COE*NDIMDX   */
   const double* ti; const double* tj; const double* tk; const double* vol;
   double* rdm;    /* Newton residual per LU block: nssiter*neq*2*ndim_rdm  */
+  double* wig;    /* senseur wiggle flags, 3*NDIMDX (KFLUDOM = 2)           */
 } or_zone;
 
 /* 1-to-1 (type 0) interface copy: rcv_zone ghost cells <- dnr_zone cells. */
@@ -64,7 +65,11 @@ void or_tstb3c(const int64_t* pi, const double* pr, int first_it, const int64_t*
 void or_init_rhs(const int64_t* pi, int nitcfg, const int64_t* ind, double* drodm);
 void or_flux(const int64_t* pi, const double* pr, const int64_t* ind,
              const double* rop, double* drodm, const double* xmut,
-             const double* ti, const double* tj, const double* tk, const double* vol);
+             const double* ti, const double* tj, const double* tk, const double* vol,
+             const double* wig);
+/* SENSOR/wiggle2001.for: wig[d*NDIMDX + l] = 1 where a slope product of
+ * any variable changes sign across the d-face of cell l, else 0 */
+void or_wiggle(const int64_t* pi, const int64_t* ind, const double* rop, double* wig);
 void or_core3ark3(const int64_t* pi, const double* pr, int nitcfg, const int64_t* ind,
                   double* rop_1, const double* rop, const double* drodm, const double* coe);
 void or_core3as2(const int64_t* pi, const double* pr, int nitcfg, int first_it,

@@ -41,7 +41,7 @@ class OrZone(C.Structure):
                 ("drodm", C.POINTER(C.c_double)), ("coe", C.POINTER(C.c_double)),
                 ("ti", C.POINTER(C.c_double)), ("tj", C.POINTER(C.c_double)),
                 ("tk", C.POINTER(C.c_double)), ("vol", C.POINTER(C.c_double)),
-                ("rdm", C.POINTER(C.c_double))]
+                ("rdm", C.POINTER(C.c_double)), ("wig", C.POINTER(C.c_double))]
 
 
 class OrTransfer(C.Structure):
@@ -94,7 +94,7 @@ class Case:
                      vol=np.ascontiguousarray(zd["vol"], dtype=np.float64),
                      lv=[np.array(zd[k], dtype=np.float64).reshape(-1) for k in ("ro", "ro_m1", "ro_p1")],
                      xmut=np.zeros(nd), drodm=np.zeros(neq * nd), coe=np.zeros(5 * nd),
-                     rdm=np.zeros(nss * neq * 2 * nlu))
+                     rdm=np.zeros(nss * neq * 2 * nlu), wig=np.zeros(3 * nd))
             self.z.append(e)
         self.tr = [dict(dnr=int(t["dnr"]), rcv=int(t["rcv"]),
                         dnr_idx=np.ascontiguousarray(t["dnr_idx"], dtype=np.int64),
@@ -109,7 +109,7 @@ class Case:
             s.ro, s.ro_m1, s.ro_p1 = (_d(a) for a in e["lv"])
             s.xmut = _d(e["xmut"]); s.drodm = _d(e["drodm"]); s.coe = _d(e["coe"])
             s.ti = _d(e["ti"]); s.tj = _d(e["tj"]); s.tk = _d(e["tk"]); s.vol = _d(e["vol"])
-            s.rdm = _d(e["rdm"])
+            s.rdm = _d(e["rdm"]); s.wig = _d(e["wig"])
         tr = (OrTransfer * max(1, len(self.tr)))()
         for s, t in zip(tr, self.tr):
             s.dnr_zone, s.rcv_zone, s.n = t["dnr"], t["rcv"], t["dnr_idx"].size

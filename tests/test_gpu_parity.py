@@ -279,3 +279,29 @@ def test_curvilinear_viscous_implicit_with_walls(oracle_mod):
         s.compute(it, 1, 4, 1, 1)
     _check_levels(ref, s)
     s.close()
+
+
+@pytest.mark.parametrize("wavy", [0.0, 0.3])
+def test_senseur_explicit(oracle_mod, wavy):
+    """senseur scheme: wiggle sensor (wiggle2001.for) on the first sub-step,
+    AUSM faces with sensor-switched dissipation (SENSOR/fluFaceEuler.for)."""
+    t = cases.taylor_green(n=(12, 10, 8), wavy=wavy, reynolds=200.0, scheme="senseur", slope="o3",
+                           dt=0.02, numb={"temporal_scheme": "explicit", "ss_iteration": 1,
+                                          "modulo_verif": 1000})
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    assert int(zd[0]["pi"][33]) == 2
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
+def test_senseur_implicit(oracle_mod):
+    t = cases.taylor_green(n=(12, 10, 8), ss_iteration=3, scheme="senseur", slope="o3")
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
+    s.close()

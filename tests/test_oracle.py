@@ -31,7 +31,8 @@ def _interior(pi, a):
     return a[:, ngk:nk - ngk, ng:nj - ng, ng:ni - ng]
 
 
-@pytest.mark.parametrize("scheme,slope", [("roe", "o1"), ("roe_min", "minmod"), ("roe", "o3")])
+@pytest.mark.parametrize("scheme,slope", [("roe", "o1"), ("roe_min", "minmod"), ("roe", "o3"),
+                                          ("senseur", "o3")])
 def test_free_stream_preservation_explicit(oracle_mod, scheme, slope):
     t = cases.isentropic_vortex(n=(12, 10, 6), beta=0.0,
                                 numz={"scheme": scheme, "slope": slope, "time_step": 0.05})
@@ -55,7 +56,8 @@ def test_free_stream_preservation_implicit(oracle_mod, scheme, slope):
     assert np.max(np.abs(c.z[0]["lv"][0] - q0)) < 1e-13
 
 
-@pytest.mark.parametrize("scheme,slope", [("roe_min", "minmod"), ("ausmpred", "o3")])
+@pytest.mark.parametrize("scheme,slope", [("roe_min", "minmod"), ("ausmpred", "o3"),
+                                          ("senseur", "o3")])
 def test_conservation_periodic(oracle_mod, scheme, slope):
     """Sum over a periodic box of V*(W^{n+1}-W^n) in conservative variables
     vanishes: every face flux enters two cells with opposite signs."""
