@@ -177,8 +177,8 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
 
 
 def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model="NSLaminar",
-           wavy=0.0, perturb=0.05, temporal="explicit", ss_iteration=3, scheme="roe_min",
-           slope="minmod", time_step=0.02, gamma=1.4):
+           wavy=0.0, perturb=0.05, temporal="explicit", ss_iteration=3, scheme="ausmpred",
+           slope="o3", time_step=0.02, gamma=1.4):
     """Box [0,1]x[0,1]x[0,dz] exercising the non-periodic BCs of the path:
     inflow at imin (BCInflow), outflow at imax (BCOutflow), a wall at jmin
     (``wall``), farfield at jmax (BCFarfield), periodic in k.  The initial

@@ -164,6 +164,9 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
                                      " is not implemented on the GPU path");
       if (p[pt + 8] != 0)
         return fail(FGB_ERR_ARG, "boundary data (nbdata > 0) is not supported on the GPU path");
+      if (p[KFLUDOM] == ROE && (type == 3 || type == 4 || type == 5 || type == 6 || type == 7 || type == 12))
+        return fail(FGB_ERR_ARG, "wall BCs with the Roe scheme need the wall-face flux correction of "
+                                 "BC/correct_flux.for, which is not implemented on the GPU path");
       int64_t cl[6];
       bc_window(p, &p[pt + 2], idir, cl);
       int d = (idir - 1) / 2;

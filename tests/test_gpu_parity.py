@@ -219,9 +219,10 @@ def test_curvilinear_implicit_lusgs(oracle_mod, scheme, slope):
 
 
 @pytest.mark.parametrize("wall,model,scheme,slope,wavy", [
-    ("BCWallInviscid", "Euler", "roe_min", "minmod", 0.0),
+    ("BCWallInviscid", "Euler", "ausmpred", "o3", 0.0),
     ("BCWallViscous", "NSLaminar", "ausmpred", "o3", 0.0),
-    ("BCWallInviscid", "Euler", "roe", "o3", 0.3),
+    ("BCWallInviscid", "Euler", "senseur", "o3", 0.3),
+    ("BCWallViscous", "NSLaminar", "senseur", "o3", 0.3),
 ])
 def test_bcs_explicit(oracle_mod, wall, model, scheme, slope, wavy):
     """Inflow, outflow, wall, farfield and periodic BCs on one zone
@@ -304,4 +305,17 @@ def test_senseur_implicit(oracle_mod):
         ref.compute(it, 1, 4, 1, modulo_verif=1)
         s.compute(it, 1, 4, 1, 1)
     _check_levels(ref, s)
+    s.close()
+
+
+def test_roe_with_walls_is_refused():
+    """FastS corrects wall-face fluxes for the Roe scheme (correct_flux.for);
+    without that correction the GPU path refuses the combination."""
+    from fast_gb300._native import FastGB300Error, Solver
+    t = cases.bc_box(n=(8, 6, 4), wall="BCWallInviscid", model="Euler", scheme="roe", slope="o3")
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    s = Solver(0)
+    with pytest.raises(FastGB300Error, match="correct_flux"):
+        z = zd[0]
+        s.add_zone(z["pi"], z["pr"], z["ti"], z["tj"], z["tk"], z["vol"])
     s.close()

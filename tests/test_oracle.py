@@ -158,3 +158,10 @@ def test_wall_ghosts(oracle_mod):
                 assert np.array_equal(a, sgn * b)
             for v in (0, 4):
                 assert np.array_equal(q[v, 2:nk - 2, g, 2:ni - 2], q[v, 2:nk - 2, m, 2:ni - 2])
+
+
+def test_oracle_refuses_roe_with_walls(oracle_mod):
+    t = cases.bc_box(n=(8, 6, 4), wall="BCWallInviscid", model="Euler", scheme="roe", slope="o3")
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    with pytest.raises(NotImplementedError):
+        oracle_mod.Case(zd)
