@@ -52,6 +52,13 @@ struct GatherList {
   double* nrm = nullptr;
   double st[5] = {0, 0, 0, 0, 0};
 };
+struct WallCorrList {             // one wall BC window of a Roe zone (correct_flux.for)
+  int32_t *l = nullptr, *l0 = nullptr, *lt = nullptr;
+  double* nrm = nullptr;
+  int64_t n = 0;
+  int dir = 0, slip = 0;
+  double sens_c = 0., sens_w = 0.;
+};
 struct ZoneData {
   std::vector<int64_t> pi;
   std::vector<double> pr;
@@ -71,6 +78,7 @@ struct ZoneData {
   std::vector<int64_t> plane_host;  // plane offsets (host)
   int64_t n_rdm = 0, ijkv_lu[3] = {1, 1, 1};
   std::vector<GatherList> bcs;
+  std::vector<WallCorrList> walls;  // Roe wall-face corrections, in BC order
   int32_t *co_dst = nullptr, *co_a = nullptr, *co_b = nullptr, *co_c = nullptr;
   int64_t co_nedge = 0, co_n = 0;
   double coesut = 0., cmus1 = 0.;
@@ -164,9 +172,7 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
                                      " is not implemented on the GPU path");
       if (p[pt + 8] != 0)
         return fail(FGB_ERR_ARG, "boundary data (nbdata > 0) is not supported on the GPU path");
-      if (p[KFLUDOM] == ROE && (type == 3 || type == 4 || type == 5 || type == 6 || type == 7 || type == 12))
-        return fail(FGB_ERR_ARG, "wall BCs with the Roe scheme need the wall-face flux correction of "
-                                 "BC/correct_flux.for, which is not implemented on the GPU path");
+
       int64_t cl[6];
       bc_window(p, &p[pt + 2], idir, cl);
       int d = (idir - 1) / 2;
@@ -214,6 +220,35 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
           t[2] = T[lm] * (d == 2 ? 1. : 0.);
         }
       };
+      if (p[KFLUDOM] == ROE && (type == 3 || type == 4 || type == 6)) {
+        // correct_flux.for lapply = 4: faces between the first interior
+        // cell and its ghost, tangential range of the window
+        const int64_t fcell = low ? 1 : nD + 1;
+        std::vector<int32_t> wl, wl0, wlt;
+        std::vector<double> wn;
+        const int64_t incd = d == 0 ? 1 : (d == 1 ? p[NIJK] : p[NIJK] * p[NIJK + 1]);
+        for (int64_t b = cl[2 * tb]; b <= cl[2 * tb + 1]; b++)
+          for (int64_t a = cl[2 * ta]; a <= cl[2 * ta + 1]; a++) {
+            int64_t c[3];
+            c[ta] = a; c[tb] = b; c[d] = fcell;
+            const int64_t l = idx(p, c[0], c[1], c[2]);
+            wl.push_back((int32_t)l);
+            wl0.push_back((int32_t)(low ? l : l - incd));
+            wlt.push_back((int32_t)((c[0] + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR] +
+                                    (c[1] + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR + 1] +
+                                    (c[2] + p[NIJK_MTR + 4] - 1) * p[NIJK_MTR + 2]));
+            double t[3];
+            normal(c[0], c[1], c[2], t);
+            for (int q = 0; q < 3; q++) wn.push_back(t[q]);
+          }
+        WallCorrList w;
+        w.n = (int64_t)wl.size(); w.dir = d; w.slip = type == 3;
+        w.sens_c = low ? -1. : 1.; w.sens_w = low ? 1. : -1.;
+        if (dev_upload(&w.l, wl) != cudaSuccess || dev_upload(&w.l0, wl0) != cudaSuccess ||
+            dev_upload(&w.lt, wlt) != cudaSuccess || dev_upload(&w.nrm, wn) != cudaSuccess)
+          return fail(FGB_ERR_CUDA, "cannot upload wall correction lists");
+        Z.walls.push_back(w);
+      }
       std::vector<int32_t> fdst, fsrc, ndst, n0, n1, n2, cdst, csrc;
       std::vector<double> nrm;
       const int64_t inc = d == 0 ? 1 : (d == 1 ? p[NIJK] : p[NIJK] * p[NIJK + 1]);
@@ -436,6 +471,7 @@ int fgb_destroy(fgb_solver* s) {
       cudaFree(g.nrm);
     }
     cudaFree(Z.wig);
+    for (WallCorrList& w : Z.walls) { cudaFree(w.l); cudaFree(w.l0); cudaFree(w.lt); cudaFree(w.nrm); }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
   for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
@@ -784,9 +820,25 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
         }
         {
           ProfScope ps(s, implicit ? "assemble_bdf" : "assemble_rk3");
-          CK(launch_assemble(z, sa, implicit, s->st));
+          if (Z.walls.empty()) {
+            CK(launch_assemble(z, sa, implicit, s->st));
+            s->launches++;
+          } else {  // balance, wall-face corrections (correct_flux.for), update
+            sa.mode = 1;
+            CK(launch_assemble(z, sa, implicit, s->st));
+            for (WallCorrList& w : Z.walls) {
+              WallCorrArgs wa{};
+              wa.l = w.l; wa.l0 = w.l0; wa.lt = w.lt; wa.nrm = w.nrm; wa.n = w.n;
+              wa.dir = w.dir; wa.slip = w.slip; wa.sens_c = w.sens_c; wa.sens_w = w.sens_w;
+              wa.rgp = Z.pr[CVINF] * (Z.pr[GAMMA] - 1.);
+              wa.gam2 = Z.pr[GAMMA] / (Z.pr[GAMMA] - 1.);
+              CK(launch_wall_corr(z, ssiter, Z.drodm, wa, s->st));
+            }
+            sa.mode = 2;
+            CK(launch_assemble(z, sa, implicit, s->st));
+            s->launches += 2 + (int64_t)Z.walls.size();
+          }
         }
-        s->launches++;
         if (implicit) {
           if (verif) {  // lhs.cpp residus_navier.h -> cprdu3s1
             NormArgs na{};

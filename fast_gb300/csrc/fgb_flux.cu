@@ -478,16 +478,26 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
   const int64_t aj = ii + z.ni * (jj + (z.nj + 1) * kk);
   const int64_t ak = ii + z.ni * (jj + z.nj * kk);
   double x[5];
+  if (a.mode == 2) {  // balance already in drodm (corrected by wall_corr)
 #pragma unroll
-  for (int v = 0; v < 5; v++) {
-    double s = a.zero_init ? 0. : a.drodm[l + v * nd] * a.coefH;
-    s = s + a.Fk[v * nfk + ak];
-    s = s + a.Fj[v * nfj + aj];
-    s = s + a.Fi[v * nfi + ai];
-    s = s - a.Fi[v * nfi + ai + 1];
-    s = s - a.Fj[v * nfj + aj + z.ni];
-    s = s - a.Fk[v * nfk + ak + z.ni * z.nj];
-    x[v] = s;
+    for (int v = 0; v < 5; v++) x[v] = a.drodm[l + v * nd];
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+      double s = a.zero_init ? 0. : a.drodm[l + v * nd] * a.coefH;
+      s = s + a.Fk[v * nfk + ak];
+      s = s + a.Fj[v * nfj + aj];
+      s = s + a.Fi[v * nfi + ai];
+      s = s - a.Fi[v * nfi + ai + 1];
+      s = s - a.Fj[v * nfj + aj + z.ni];
+      s = s - a.Fk[v * nfk + ak + z.ni * z.nj];
+      x[v] = s;
+    }
+    if (a.mode == 1) {
+#pragma unroll
+      for (int v = 0; v < 5; v++) a.drodm[l + v * nd] = x[v];
+      return;
+    }
   }
   const double cv = z.cv;
   if (!IMPL) {
@@ -600,6 +610,93 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
     }
   }
   return cudaErrorNotSupported;
+}
+
+// --------------------------------------------------- wall correction (Roe)
+// BC/correct_flux.for, lapply = 4: for each face of a wall window, remove
+// the Euler Roe flux of the face from the balance of its interior cell
+// (corr_fluroe_euler_*: the same reconstruction and Roe flux as face_flux),
+// then add the wall flux (CL_correction_flu.for: bflwallslip.for /
+// bflwall.for) built from the face-averaged state.  One thread per face;
+// the windows of one BC have distinct cells, BCs run one after another.
+template <int D, int TYP, int SL>
+__global__ void __launch_bounds__(128) wall_corr(Zone z, const double* __restrict__ q,
+                                                 double* __restrict__ drodm, WallCorrArgs a) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  const int64_t l = a.l[e], l0 = a.l0[e], nd = z.nd, inc = z.inc[D];
+  double qm[5], qp[5];
+  double roff = 0.;
+  if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    const double* Q = q + v * nd;
+    double aa = (SL == O1) ? 0. : Q[l - 2 * inc];
+    double bb = Q[l - inc], cc = Q[l];
+    double dd = (SL == O1) ? 0. : Q[l + inc];
+    reconstruct<SL>(z, aa, bb, cc, dd, roff, qm[v], qp[v]);
+  }
+  double F[5];
+  if (TYP == Z3DCART) {
+    roe_cart<D>(z, qm, qp, F);
+  } else {
+    const int64_t lt = a.lt[e];
+    const double* t = D == 0 ? z.ti : (D == 1 ? z.tj : z.tk);
+    double tcx = t[lt], tcy = t[lt + z.ndm], tcz = t[lt + 2 * z.ndm];
+    double s = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
+    roe_full(z, qm, qp, tcx, tcy, tcz, s, F);
+  }
+  double x[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) x[v] = drodm[l0 + v * nd] + (F[v] * a.sens_c + 0.);
+  const int64_t ia = l - inc;   // iadrf
+  const double t0 = a.nrm[3 * e], t1 = a.nrm[3 * e + 1], t2 = a.nrm[3 * e + 2];
+  const double qen = 0.;
+  const double r = 0.5 * (q[l] + q[ia]);
+  const double u = 0.5 * (q[l + nd] + q[ia + nd]);
+  const double v = 0.5 * (q[l + 2 * nd] + q[ia + 2 * nd]);
+  const double w = 0.5 * (q[l + 3 * nd] + q[ia + 3 * nd]);
+  const double u_int = t0 * u + t1 * v + t2 * w - qen;
+  double fw[5];
+  if (a.slip) {
+    double p = q[ia + 4 * nd] * q[ia] * a.rgp;
+    const double h = a.gam2 * p + r * (u * u + v * v + w * w) * 0.5;
+    p = 0.5 * (q[l + 4 * nd] * q[l] + q[ia + 4 * nd] * q[ia]) * a.rgp;
+    fw[0] = u_int * r;
+    fw[1] = t0 * p + u_int * r * u;
+    fw[2] = t1 * p + u_int * r * v;
+    fw[3] = t2 * p + u_int * r * w;
+    fw[4] = u_int * h + p * qen;
+  } else {
+    const double p = 0.5 * (q[l + 4 * nd] * q[l] + q[ia + 4 * nd] * q[ia]) * a.rgp;
+    fw[0] = 0.;
+    fw[1] = t0 * p + u_int * u * r;
+    fw[2] = t1 * p + u_int * v * r;
+    fw[3] = t2 * p + u_int * w * r;
+    fw[4] = p * qen;
+  }
+#pragma unroll
+  for (int m = 0; m < 5; m++) drodm[l0 + m * nd] = x[m] + fw[m] * a.sens_w;
+}
+
+template <int D, int TYP>
+static void wall_corr_sl(const Zone& z, const double* q, double* drodm, const WallCorrArgs& a,
+                         cudaStream_t st) {
+  const unsigned g = (unsigned)((a.n + 127) / 128);
+  if (z.slope == O1) wall_corr<D, TYP, O1><<<g, 128, 0, st>>>(z, q, drodm, a);
+  else if (z.slope == O3) wall_corr<D, TYP, O3><<<g, 128, 0, st>>>(z, q, drodm, a);
+  else wall_corr<D, TYP, MINMOD><<<g, 128, 0, st>>>(z, q, drodm, a);
+}
+
+cudaError_t launch_wall_corr(const Zone& z, const double* q, double* drodm, const WallCorrArgs& a,
+                             cudaStream_t st) {
+  if (a.n <= 0) return cudaSuccess;
+  if (z.kflu != ROE || (z.typ != Z3DCART && z.typ != Z3DFULL)) return cudaErrorNotSupported;
+  const bool cart = z.typ == Z3DCART;
+  if (a.dir == 0) cart ? wall_corr_sl<0, Z3DCART>(z, q, drodm, a, st) : wall_corr_sl<0, Z3DFULL>(z, q, drodm, a, st);
+  else if (a.dir == 1) cart ? wall_corr_sl<1, Z3DCART>(z, q, drodm, a, st) : wall_corr_sl<1, Z3DFULL>(z, q, drodm, a, st);
+  else cart ? wall_corr_sl<2, Z3DCART>(z, q, drodm, a, st) : wall_corr_sl<2, Z3DFULL>(z, q, drodm, a, st);
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------ wiggle

@@ -17,7 +17,20 @@ struct StageArgs {
   double coefH; int zero_init;       // init_rhs.for
   double coefW;                      // core3ark3.for
   double c1, c2, c3; int first_sub;  // core3as2.for
+  int mode;   // 0: balance + update, 1: balance into drodm only, 2: update from drodm only
 };
+// BC/correct_flux.for, wall BCs with the Roe scheme: one wall BC window
+struct WallCorrArgs {
+  const int32_t* l;      // cell on the high side of the wall face
+  const int32_t* l0;     // interior cell receiving the correction
+  const int32_t* lt;     // metric index of the face
+  const double* nrm;     // [n][3] raw face normal (tijk * c_mtr)
+  int64_t n;
+  int dir, slip;         // face direction; bflwallslip (1) or bflwall (0)
+  double sens_c, sens_w, rgp, gam2;
+};
+cudaError_t launch_wall_corr(const Zone& z, const double* q, double* drodm, const WallCorrArgs& a,
+                             cudaStream_t st);
 cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
                          double* Fj, double* Fk, cudaStream_t st);
 cudaError_t launch_wiggle(const Zone& z, const double* q, double* wig, cudaStream_t st);

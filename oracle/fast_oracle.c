@@ -240,6 +240,10 @@ void or_init_rhs(const int64_t* pi, int nitcfg, const int64_t* ind, double* drod
  * face between l-inc and l; assemble_drodm_plus_vec1.for adds it to l and
  * subtracts it from l-inc.
  * ====================================================================== */
+static void bc_window(const int64_t* pi, const int64_t* fen, int idir, int64_t* cl);
+static void bc_normal(const int64_t* pi, const double* ti, const double* tj, const double* tk,
+                      int idir, int64_t i, int64_t j, int64_t k, double t[3]);
+
 typedef struct {
   const int64_t* pi; const double* pr;
   const double *rop, *xmut, *ti, *tj, *tk, *vol;
@@ -640,6 +644,74 @@ static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, dou
   if (c->iflow >= 2) {
     if (c->typ == 2) visc_cart(c, d, l, flu);
     else visc_full(c, d, l, lt, tcx, tcy, tcz, flu);
+  }
+}
+
+/* BC/correct_flux.for with lapply = 4 (wall BCs with the Roe scheme), in
+ * BC order, for each face of the wall window (the face between the first
+ * interior cell l0 and its ghost): drodm(l0) += F_roe * sens_c + 0 with the
+ * Euler Roe flux of that face (corr_fluroe_euler_*: the balance's flux
+ * removed), then drodm(l0) += F_wall * sens_w (CL_correction_flu.for:
+ * bflwallslip.for for BCWallInviscid / BCSymmetryPlane, bflwall.for for
+ * BCWall / BCWallViscous). */
+void or_correct_flux(const int64_t* pi, const double* pr, const double* rop, double* drodm,
+                     const double* xmut, const double* ti, const double* tj, const double* tk,
+                     const double* vol) {
+  if (pi[KFLUDOM] != 5) return;
+  int64_t pt_bcs = pi[PT_BC];
+  if (pt_bcs <= 0) return;
+  fctx c;
+  fctx_init(&c, pi, pr, rop, xmut, ti, tj, tk, vol);
+  c.iflow = 1;   /* Euler part only */
+  const int64_t nd = pi[NDIMDX];
+  const double rgp = pr[CVINF] * (pr[GAMMA] - 1.), gam2 = pr[GAMMA] / (pr[GAMMA] - 1.);
+  for (int64_t n = 0; n < pi[pt_bcs]; n++) {
+    const int64_t pt = pi[pt_bcs + 1 + n], type = pi[pt + BC_TYPE];
+    if (type != 3 && type != 4 && type != 6) continue;
+    const int idir = (int)pi[pt + BC_IDIR];
+    int64_t cl[6];
+    bc_window(pi, pi + pt + BC_FEN, idir, cl);
+    const int d = (idir - 1) / 2, low = idir % 2;
+    /* the face layer: cell 1 (low faces) or the first ghost n_d + 1 (high) */
+    const int64_t fc = low ? 1 : pi[IJKV + d] + 1;
+    cl[2 * d] = fc; cl[2 * d + 1] = fc;
+    const int64_t inc = c.inc[d];
+    const double sens_c = low ? -1. : 1., sens_w = low ? 1. : -1.;
+    for (int64_t k = cl[4]; k <= cl[5]; k++)
+      for (int64_t j = cl[2]; j <= cl[3]; j++)
+        for (int64_t i = cl[0]; i <= cl[1]; i++) {
+          const int64_t l = inddm(pi, i, j, k), iadrf = l - inc, l0 = low ? l : l - inc;
+          double flu[5];
+          face_flux(&c, d, i, j, k, flu);
+          for (int v = 0; v < 5; v++) drodm[l0 + v * nd] = drodm[l0 + v * nd] + (flu[v] * sens_c + 0.);
+          double t[3];
+          bc_normal(pi, ti, tj, tk, idir, i, j, k, t);
+          const double qen = 0.;
+          const double r = 0.5 * (rop[l] + rop[iadrf]);
+          const double u = 0.5 * (rop[l + nd] + rop[iadrf + nd]);
+          const double v = 0.5 * (rop[l + 2 * nd] + rop[iadrf + 2 * nd]);
+          const double w = 0.5 * (rop[l + 3 * nd] + rop[iadrf + 3 * nd]);
+          const double u_int = t[0] * u + t[1] * v + t[2] * w - qen;
+          double fw[5];
+          if (type == 3) {    /* bflwallslip.for */
+            double p = rop[iadrf + 4 * nd] * rop[iadrf] * rgp;
+            const double h = gam2 * p + r * (u * u + v * v + w * w) * 0.5;
+            p = 0.5 * (rop[l + 4 * nd] * rop[l] + rop[iadrf + 4 * nd] * rop[iadrf]) * rgp;
+            fw[0] = u_int * r;
+            fw[1] = t[0] * p + u_int * r * u;
+            fw[2] = t[1] * p + u_int * r * v;
+            fw[3] = t[2] * p + u_int * r * w;
+            fw[4] = u_int * h + p * qen;
+          } else {            /* bflwall.for */
+            const double p = 0.5 * (rop[l + 4 * nd] * rop[l] + rop[iadrf + 4 * nd] * rop[iadrf]) * rgp;
+            fw[0] = 0.;
+            fw[1] = t[0] * p + u_int * u * r;
+            fw[2] = t[1] * p + u_int * v * r;
+            fw[3] = t[2] * p + u_int * w * r;
+            fw[4] = p * qen;
+          }
+          for (int m = 0; m < 5; m++) drodm[l0 + m * nd] = drodm[l0 + m * nd] + fw[m] * sens_w;
+        }
   }
 }
 
@@ -1677,6 +1749,8 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
         /* src_term.for:257-266: senseur wiggle on the first sub-step */
         if (pi[KFLUDOM] == 2 && nstep == 1) or_wiggle(pi, sdm, ssiter, Z->wig);
         or_flux(pi, pr, sdm, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol, Z->wig);
+        /* navier_stokes_struct.for:378: wall-face correction (Roe) */
+        or_correct_flux(pi, pr, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
         if (implicit) {
           or_core3as2(pi, pr, nstep, *first_it, sdm, ssiter, Z->ro, Z->ro_m1, Z->drodm, Z->coe);
           if (lssiter_verif) or_cprdu3s1(pi, nstep, (int)nssiter, Z->drodm, Z->rdm);

@@ -67,6 +67,10 @@ void or_flux(const int64_t* pi, const double* pr, const int64_t* ind,
              const double* rop, double* drodm, const double* xmut,
              const double* ti, const double* tj, const double* tk, const double* vol,
              const double* wig);
+/* BC/correct_flux.for for wall BCs with the Roe scheme (lapply = 4) */
+void or_correct_flux(const int64_t* pi, const double* pr, const double* rop, double* drodm,
+                     const double* xmut, const double* ti, const double* tj, const double* tk,
+                     const double* vol);
 /* SENSOR/wiggle2001.for: wig[d*NDIMDX + l] = 1 where a slope product of
  * any variable changes sign across the d-face of cell l, else 0 */
 void or_wiggle(const int64_t* pi, const int64_t* ind, const double* rop, double* wig);

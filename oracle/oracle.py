@@ -73,19 +73,6 @@ def _i(a):
     return a.ctypes.data_as(C.POINTER(C.c_int64))
 
 
-def _check_supported(pi):
-    """The restatement covers the BC types of the path; with the Roe scheme,
-    FastS corrects wall-face fluxes after the balance (BC/correct_flux.for,
-    lapply = 4), which is not restated: refuse such cases."""
-    pt = int(pi[70])
-    if pt <= 0 or pt >= pi.size:
-        return
-    for n in range(int(pi[pt])):
-        b = int(pi[pt + 1 + n])
-        if int(pi[33]) == 5 and int(pi[b]) in (3, 4, 5, 6, 7, 12):
-            raise NotImplementedError("wall BC with the Roe scheme: correct_flux.for is not restated")
-
-
 class Case:
     """Host copies of every zone's arrays, advanced by the oracle."""
 
@@ -95,7 +82,6 @@ class Case:
         self.z = []
         for zd in zones:
             pi = np.ascontiguousarray(zd["pi"], dtype=np.int64)
-            _check_supported(pi)
             nd, neq = int(pi[41]), int(pi[36])
             nss = int(pi[58])
             nlu = 1

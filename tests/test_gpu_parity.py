@@ -308,14 +308,31 @@ def test_senseur_implicit(oracle_mod):
     s.close()
 
 
-def test_roe_with_walls_is_refused():
-    """FastS corrects wall-face fluxes for the Roe scheme (correct_flux.for);
-    without that correction the GPU path refuses the combination."""
-    from fast_gb300._native import FastGB300Error, Solver
-    t = cases.bc_box(n=(8, 6, 4), wall="BCWallInviscid", model="Euler", scheme="roe", slope="o3")
-    zd = fasts.zone_data(t, fasts.prepare(t))
-    s = Solver(0)
-    with pytest.raises(FastGB300Error, match="correct_flux"):
-        z = zd[0]
-        s.add_zone(z["pi"], z["pr"], z["ti"], z["tj"], z["tk"], z["vol"])
+@pytest.mark.parametrize("wall,model,slope,wavy", [
+    ("BCWallInviscid", "Euler", "minmod", 0.0),
+    ("BCWall", "Euler", "o3", 0.3),
+    ("BCWallViscous", "NSLaminar", "o3", 0.0),
+    ("BCWallViscous", "NSLaminar", "minmod", 0.3),
+])
+def test_roe_wall_flux_correction(oracle_mod, wall, model, slope, wavy):
+    """Roe with wall BCs: the balance's Euler flux at wall faces is replaced
+    by the wall flux (BC/correct_flux.for, bflwallslip.for / bflwall.for)."""
+    t = cases.bc_box(n=(14, 10, 6), wall=wall, model=model, scheme="roe", slope=slope, wavy=wavy)
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
+def test_roe_wall_flux_correction_implicit(oracle_mod):
+    t = cases.bc_box(n=(12, 10, 6), wall="BCWallViscous", model="NSLaminar", scheme="roe_min",
+                     slope="minmod", temporal="implicit", ss_iteration=3, time_step=0.05,
+                     reynolds=500.0)
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
     s.close()

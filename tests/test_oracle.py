@@ -160,8 +160,13 @@ def test_wall_ghosts(oracle_mod):
                 assert np.array_equal(q[v, 2:nk - 2, g, 2:ni - 2], q[v, 2:nk - 2, m, 2:ni - 2])
 
 
-def test_oracle_refuses_roe_with_walls(oracle_mod):
-    t = cases.bc_box(n=(8, 6, 4), wall="BCWallInviscid", model="Euler", scheme="roe", slope="o3")
-    zd = fasts.zone_data(t, fasts.prepare(t))
-    with pytest.raises(NotImplementedError):
-        oracle_mod.Case(zd)
+def test_roe_slip_wall_keeps_parallel_free_stream(oracle_mod):
+    """With the Roe wall-face correction (correct_flux.for) a free stream
+    parallel to a slip wall stays the free stream."""
+    t = cases.bc_box(n=(12, 10, 6), perturb=0.0, wall="BCWallInviscid", model="Euler",
+                     scheme="roe", slope="o3")
+    zd, c = _case(t, oracle_mod)
+    q0 = c.z[0]["lv"][0].copy()
+    for it in range(1, 4):
+        c.compute(it, 1, 3, 1, modulo_verif=1000)
+    assert np.max(np.abs(c.z[0]["lv"][0] - q0)) < 1e-14
