@@ -28,24 +28,26 @@ from . import pytree as I
 NG = 2
 
 
-def cart_zone(name, x0, h, n, ng=NG):
+def cart_zone(name, x0, h, n, ng=NG, ngk=None):
     """Uniform cartesian zone of n = (ni, nj, nk) interior cells, origin x0
-    (first interior vertex), steps h, with ng ghost layers on every side."""
+    (first interior vertex), steps h, with ng ghost layers on every side
+    (ngk in k; a 2-d zone has nk = 1 and ngk = 0)."""
     ni, nj, nk = n
-    nv = [ni + 1 + 2 * ng, nj + 1 + 2 * ng, nk + 1 + 2 * ng]
+    ngk = ng if ngk is None else ngk
+    nv = [ni + 1 + 2 * ng, nj + 1 + 2 * ng, nk + 1 + 2 * ngk]
     z = I.newZone(name, nv)
     ii = np.arange(nv[0]) - ng
     jj = np.arange(nv[1]) - ng
-    kk = np.arange(nv[2]) - ng
+    kk = np.arange(nv[2]) - ngk
     X, Y, Z = np.meshgrid(x0[0] + ii * h[0], x0[1] + jj * h[1], x0[2] + kk * h[2], indexing="ij")
     gc = I.createChild(z, "GridCoordinates", "GridCoordinates_t")
     for nm, arr in (("CoordinateX", X), ("CoordinateY", Y), ("CoordinateZ", Z)):
         I.createChild(gc, nm, "DataArray_t")[1] = np.asfortranarray(arr)
-    I.createChild(z, "Rind", "Rind_t", np.array([ng] * 6, dtype=np.int64))
+    I.createChild(z, "Rind", "Rind_t", np.array([ng, ng, ng, ng, ngk, ngk], dtype=np.int64))
     return z
 
 
-def wave(z, amp, x0, L):
+def wave(z, amp, x0, L, two_d=False):
     """Periodic curvilinear mesh: displace every vertex of a uniform box by
     amp x (local step) x a product of sines of the other two coordinates,
     with the box lengths L as periods, so the mesh stays periodic (ghost
@@ -57,9 +59,12 @@ def wave(z, amp, x0, L):
     hx, hy, hz = X[1, 0, 0] - X[0, 0, 0], Y[0, 1, 0] - Y[0, 0, 0], Z[0, 0, 1] - Z[0, 0, 0]
     sx, sy, sz = (2 * math.pi * (A - a0) / l for A, a0, l in ((X, x0[0], L[0]), (Y, x0[1], L[1]),
                                                               (Z, x0[2], L[2])))
-    new = (X + amp * hx * np.sin(sy) * np.sin(sz),
-           Y + amp * hy * np.sin(sx) * np.sin(sz),
-           Z + amp * hz * np.sin(sx) * np.sin(sy))
+    if two_d:   # in-plane displacement only: the zone stays a 2-d zone
+        new = (X + amp * hx * np.sin(sy), Y + amp * hy * np.sin(sx), Z)
+    else:
+        new = (X + amp * hx * np.sin(sy) * np.sin(sz),
+               Y + amp * hy * np.sin(sx) * np.sin(sz),
+               Z + amp * hz * np.sin(sx) * np.sin(sy))
     for nm, arr in zip(("CoordinateX", "CoordinateY", "CoordinateZ"), new):
         I.getNodeFromName1(gc, nm)[1] = np.asfortranarray(arr)
     return z
@@ -112,15 +117,18 @@ def _tree(zones, model, numb, numz, mach, reynolds, gamma=1.4, prandtl=0.72, sut
 
 
 def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0, gamma=1.4,
-                      numb=None, numz=None, wavy=0.0):
+                      numb=None, numz=None, wavy=0.0, two_d=False):
     """Config: plain FP64, 128x128x4 periodic box [-box, box]^2, Euler vortex
     (Mach 0.5, strength 5, core radius 1), Roe + minmod, explicit RK3.
     wavy > 0: the same box on a periodic curvilinear mesh (see wave)."""
     ni, nj, nk = n
+    if two_d:
+        nk = 1
+        n = (ni, nj, 1)
     h = (2 * box / ni, 2 * box / nj, 2 * box / ni)
-    z = cart_zone("vortex", (-box, -box, 0.0), h, n)
+    z = cart_zone("vortex", (-box, -box, 0.0), h, n, ngk=0 if two_d else None)
     if wavy:
-        wave(z, wavy, (-box, -box, 0.0), (2 * box, 2 * box, h[2] * nk))
+        wave(z, wavy, (-box, -box, 0.0), (2 * box, 2 * box, h[2] * nk), two_d=two_d)
     xc, yc, _ = cell_centers(z)
     x = xc / radius
     y = yc / radius
@@ -132,7 +140,7 @@ def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0,
     ro = T ** (1.0 / (gamma - 1.0))
     p = ro * T / gamma
     set_conservative(z, ro, mach + du, dv, np.zeros_like(ro), p, gamma)
-    for f in ("imin", "imax", "jmin", "jmax", "kmin", "kmax"):
+    for f in ("imin", "imax", "jmin", "jmax") + (() if two_d else ("kmin", "kmax")):
         add_bc(z, "per_" + f, "BCautoperiod", f)
     numb = numb or {"temporal_scheme": "explicit", "ss_iteration": 1, "modulo_verif": 1000000}
     numz = numz or {"scheme": "roe_min", "slope": "minmod", "time_step": 0.01,
@@ -178,7 +186,7 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
 
 def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model="NSLaminar",
            wavy=0.0, perturb=0.05, temporal="explicit", ss_iteration=3, scheme="ausmpred",
-           slope="o3", time_step=0.02, gamma=1.4):
+           slope="o3", time_step=0.02, gamma=1.4, two_d=False):
     """Box [0,1]x[0,1]x[0,dz] exercising the non-periodic BCs of the path:
     inflow at imin (BCInflow), outflow at imax (BCOutflow), a wall at jmin
     (``wall``), farfield at jmax (BCFarfield), periodic in k.  The initial
@@ -186,25 +194,29 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
     ``perturb`` (0 gives the free stream itself).  wavy > 0 displaces the
     vertices as in ``wave`` (periods = box lengths)."""
     ni, nj, nk = n
+    if two_d:
+        nk = 1
+        n = (ni, nj, 1)
     h = (1.0 / ni, 1.0 / nj, 1.0 / ni)
-    z = cart_zone("box", (0.0, 0.0, 0.0), h, n)
+    z = cart_zone("box", (0.0, 0.0, 0.0), h, n, ngk=0 if two_d else None)
     if wavy:
-        wave(z, wavy, (0.0, 0.0, 0.0), (1.0, 1.0, h[2] * nk))
+        wave(z, wavy, (0.0, 0.0, 0.0), (1.0, 1.0, h[2] * nk), two_d=two_d)
     xc, yc, zc = cell_centers(z)
     a = perturb
     s = np.sin(2 * math.pi * xc) * np.sin(2 * math.pi * yc) * np.cos(2 * math.pi * zc / (h[2] * nk))
     ro = 1.0 + a * s
     u = mach * (1.0 + a * np.cos(2 * math.pi * yc) * np.sin(2 * math.pi * xc))
     v = mach * a * s
-    w = mach * a * np.sin(2 * math.pi * xc) * np.cos(2 * math.pi * yc)
+    w = 0.0 * xc if two_d else mach * a * np.sin(2 * math.pi * xc) * np.cos(2 * math.pi * yc)
     p = (1.0 + a * 0.5 * s) / gamma
     set_conservative(z, ro, u, v, w, p, gamma)
     add_bc(z, "in", "BCInflow", "imin")
     add_bc(z, "out", "BCOutflow", "imax")
     add_bc(z, "wall", wall, "jmin")
     add_bc(z, "far", "BCFarfield", "jmax")
-    add_bc(z, "per_kmin", "BCautoperiod", "kmin")
-    add_bc(z, "per_kmax", "BCautoperiod", "kmax")
+    if not two_d:
+        add_bc(z, "per_kmin", "BCautoperiod", "kmin")
+        add_bc(z, "per_kmax", "BCautoperiod", "kmax")
     numb = {"temporal_scheme": temporal, "ss_iteration": ss_iteration, "modulo_verif": 1}
     numz = {"scheme": scheme, "slope": slope, "time_step": time_step,
             "cache_blocking_I": 1000000, "cache_blocking_J": 1000000, "cache_blocking_K": 1000000}

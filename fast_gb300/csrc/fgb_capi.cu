@@ -215,6 +215,8 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
                            (c[2] + p[NIJK_MTR + 4] - 1) * p[NIJK_MTR + 2];
         if (neq_mtr == 3) {
           t[0] = T[lm] * 1.; t[1] = T[lm + ndm] * 1.; t[2] = T[lm + 2 * ndm] * 1.;
+        } else if (neq_mtr == 2) {   // shape_tab_mtr.for: ic=1, jc=2, kc=2, ck_mtr=0
+          t[0] = T[lm] * 1.; t[1] = T[lm + ndm] * 1.; t[2] = T[lm + ndm] * 0.;
         } else {
           t[0] = T[lm] * (d == 0 ? 1. : 0.); t[1] = T[lm] * (d == 1 ? 1. : 0.);
           t[2] = T[lm] * (d == 2 ? 1. : 0.);
@@ -417,7 +419,7 @@ static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const dou
   z.c5 = 2. * c6;
   z.c6 = -1. * c6;
   z.cvisq = 1. / 3;
-  z.tcx = ti[0]; z.tcy = tj[0]; z.tcz = tk[0];
+  z.tcx = ti[0]; z.tcy = tj[0]; z.tcz = p[NEQ_K] > 0 ? tk[0] : 0.;  // a 2-d zone has no tk
   z.si = std::fabs(z.tcx); z.sj = std::fabs(z.tcy); z.sk = std::fabs(z.tcz);
   z.volinv = 0.5 / vol[0];
   z.prandt = r[PRANDT]; z.xmul0 = r[XMUL0]; z.temp0 = r[TEMP0]; z.cs = r[CS];
@@ -497,10 +499,14 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   Z.pi.assign(param_int, param_int + n_int);
   Z.pr.assign(param_real, param_real + n_real);
   const std::vector<int64_t>& p = Z.pi;
-  if (p[ITYPZONE] != Z3DCART && p[ITYPZONE] != Z3DFULL)
+  if (p[ITYPZONE] != Z3DCART && p[ITYPZONE] != Z3DFULL && p[ITYPZONE] != Z2D)
     return fail(FGB_ERR_ARG, "zone type " + std::to_string(p[ITYPZONE]) + " not supported on the GPU path");
+  if (p[ITYPZONE] == Z2D && (p[IFLOW] != 1 || p[KFLUDOM] == SENSEUR))
+    return fail(FGB_ERR_ARG, "2-d zones are supported for the Euler equations with the Roe and "
+                             "AUSM+(P) schemes on the GPU path");
   if (p[NEQ] != 5) return fail(FGB_ERR_ARG, "only 5-equation models are supported on the GPU path");
-  if (p[NIJK + 3] != 2 || p[NIJK + 4] != 2) return fail(FGB_ERR_ARG, "two ghost layers expected");
+  if (p[NIJK + 3] != 2 || p[NIJK + 4] != (p[ITYPZONE] == Z2D ? 0 : 2))
+    return fail(FGB_ERR_ARG, "two ghost layers expected (none in k for a 2-d zone)");
   if (p[NDIMDX] != p[NIJK] * p[NIJK + 1] * p[NIJK + 2])
     return fail(FGB_ERR_ARG, "NDIMDX inconsistent with NIJK (shiftvar must be 0)");
   if (p[NDIMDX] >= (int64_t)INT32_MAX / 2) return fail(FGB_ERR_ARG, "zone too large");

@@ -428,6 +428,7 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
   if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
 #pragma unroll
   for (int v = 0; v < 5; v++) {
+    if (TYP == Z2D && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }   // 2-d: no w slope
     const double* Q = q + v * nd;
     double a = (SL == O1) ? 0. : Q[l - 2 * inc];
     double b = Q[l - inc], c = Q[l];
@@ -435,7 +436,17 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     reconstruct<SL>(z, a, b, c, d, roff, qm[v], qp[v]);
   }
   double F[5];
-  if (TYP == Z3DCART) {
+  if (TYP == Z2D) {
+    // *_2d_{i,j}.for: the 3-d general face with tcz = 0 and w = 0 (the
+    // w terms vanish exactly), w flux = 0
+    const int64_t lt = indmtr(z, ii + 1, jj + 1, kk + 1);
+    const double* t = D == 0 ? z.ti : z.tj;
+    double tcx = t[lt], tcy = t[lt + z.ndm];
+    double s = sqrt(tcx * tcx + tcy * tcy);
+    if (KF == ROE) roe_full(z, qm, qp, tcx, tcy, 0., s, F);
+    else ausm_face<D, false>(z, qm, qp, q[l + 4 * nd], tcx, tcy, 0., s, F);
+    F[3] = 0.;
+  } else if (TYP == Z3DCART) {
     if (KF == ROE) roe_cart<D>(z, qm, qp, F);
     else ausm_face<D, true, KF == SENSEUR>(z, qm, qp, q[l + 4 * nd], z.tcx, z.tcy, z.tcz,
                                           D == 0 ? z.si : (D == 1 ? z.sj : z.sk), F,
@@ -483,14 +494,15 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
     for (int v = 0; v < 5; v++) x[v] = a.drodm[l + v * nd];
   } else {
 #pragma unroll
+    const bool two_d = z.typ == Z2D;   // no k faces
     for (int v = 0; v < 5; v++) {
       double s = a.zero_init ? 0. : a.drodm[l + v * nd] * a.coefH;
-      s = s + a.Fk[v * nfk + ak];
+      if (!two_d) s = s + a.Fk[v * nfk + ak];
       s = s + a.Fj[v * nfj + aj];
       s = s + a.Fi[v * nfi + ai];
       s = s - a.Fi[v * nfi + ai + 1];
       s = s - a.Fj[v * nfj + aj + z.ni];
-      s = s - a.Fk[v * nfk + ak + z.ni * z.nj];
+      if (!two_d) s = s - a.Fk[v * nfk + ak + z.ni * z.nj];
       x[v] = s;
     }
     if (a.mode == 1) {
@@ -513,10 +525,17 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
     double rr = 1. / n1;
     double n2 = (ro * u + tab2) * rr;
     double n3 = (ro * v + tab3) * rr;
-    double n4 = (ro * w + tab4) * rr;
-    double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v + w * w));
     double cvinv = 1. / cv, cvinv2 = 0.5 * cvinv;
-    double n5 = (roe_old + tab5) * rr * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
+    double n4, n5;
+    if (z.typ == Z2D) {  // core3ark3.for 2-d branch: w = 0
+      n4 = 0.;
+      double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v));
+      n5 = (roe_old + tab5) * rr * cvinv - cvinv2 * (n2 * n2 + n3 * n3);
+    } else {
+      n4 = (ro * w + tab4) * rr;
+      double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v + w * w));
+      n5 = (roe_old + tab5) * rr * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
+    }
     double* O = a.rop_out;
     O[l] = n1; O[l + nd] = n2; O[l + 2 * nd] = n3; O[l + 3 * nd] = n4; O[l + 4 * nd] = n5;
   } else {
@@ -548,6 +567,9 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
       double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
       y[4] = cf * x[4] + a.c1 * roe + a.c2 * roen + a.c3 * roe1;
     }
+    // core3as2.for 2-d branch: the w residual is left as the balance, and
+    // the energies have no w term (w = 0 in a 2-d state: the same values)
+    if (z.typ == Z2D) y[3] = x[3];
 #pragma unroll
     for (int v = 0; v < 5; v++) a.drodm[l + v * nd] = y[v];
   }
@@ -567,8 +589,10 @@ static cudaError_t launch_faces_t(const Zone& z, const double* q, const double* 
   FGB_CHECK_LAUNCH();
   face_flux<1, TYP, KF, SL, VISC><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, xmut, Fj);
   FGB_CHECK_LAUNCH();
-  face_flux<2, TYP, KF, SL, VISC><<<(unsigned)((nfk + B - 1) / B), B, 0, st>>>(z, q, xmut, Fk);
-  FGB_CHECK_LAUNCH();
+  if (TYP != Z2D) {
+    face_flux<2, TYP, KF, SL, VISC><<<(unsigned)((nfk + B - 1) / B), B, 0, st>>>(z, q, xmut, Fk);
+    FGB_CHECK_LAUNCH();
+  }
   return cudaSuccess;
 }
 
@@ -609,6 +633,15 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
                   : launch_faces_t<Z3DFULL, SENSEUR, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
   }
+  if (z.typ == Z2D && !visc) {   // 2-d zones: Euler, Roe o1 / o3 / minmod, AUSM+(P) o3
+    if (z.kflu == ROE) {
+      if (z.slope == O1) return launch_faces_t<Z2D, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O3) return launch_faces_t<Z2D, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == MINMOD) return launch_faces_t<Z2D, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
+    } else if (z.kflu == AUSM && z.slope == O3) {
+      return launch_faces_t<Z2D, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+    }
+  }
   return cudaErrorNotSupported;
 }
 
@@ -630,6 +663,7 @@ __global__ void __launch_bounds__(128) wall_corr(Zone z, const double* __restric
   if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
 #pragma unroll
   for (int v = 0; v < 5; v++) {
+    if (TYP == Z2D && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
     const double* Q = q + v * nd;
     double aa = (SL == O1) ? 0. : Q[l - 2 * inc];
     double bb = Q[l - inc], cc = Q[l];
@@ -639,6 +673,13 @@ __global__ void __launch_bounds__(128) wall_corr(Zone z, const double* __restric
   double F[5];
   if (TYP == Z3DCART) {
     roe_cart<D>(z, qm, qp, F);
+  } else if (TYP == Z2D) {
+    const int64_t lt = a.lt[e];
+    const double* t = D == 0 ? z.ti : z.tj;
+    double tcx = t[lt], tcy = t[lt + z.ndm];
+    double s = sqrt(tcx * tcx + tcy * tcy);
+    roe_full(z, qm, qp, tcx, tcy, 0., s, F);
+    F[3] = 0.;
   } else {
     const int64_t lt = a.lt[e];
     const double* t = D == 0 ? z.ti : (D == 1 ? z.tj : z.tk);
@@ -691,7 +732,14 @@ static void wall_corr_sl(const Zone& z, const double* q, double* drodm, const Wa
 cudaError_t launch_wall_corr(const Zone& z, const double* q, double* drodm, const WallCorrArgs& a,
                              cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
-  if (z.kflu != ROE || (z.typ != Z3DCART && z.typ != Z3DFULL)) return cudaErrorNotSupported;
+  if (z.kflu != ROE) return cudaErrorNotSupported;
+  if (z.typ == Z2D) {
+    if (a.dir == 0) wall_corr_sl<0, Z2D>(z, q, drodm, a, st);
+    else if (a.dir == 1) wall_corr_sl<1, Z2D>(z, q, drodm, a, st);
+    else return cudaErrorNotSupported;
+    return cudaGetLastError();
+  }
+  if (z.typ != Z3DCART && z.typ != Z3DFULL) return cudaErrorNotSupported;
   const bool cart = z.typ == Z3DCART;
   if (a.dir == 0) cart ? wall_corr_sl<0, Z3DCART>(z, q, drodm, a, st) : wall_corr_sl<0, Z3DFULL>(z, q, drodm, a, st);
   else if (a.dir == 1) cart ? wall_corr_sl<1, Z3DCART>(z, q, drodm, a, st) : wall_corr_sl<1, Z3DFULL>(z, q, drodm, a, st);

@@ -67,6 +67,28 @@ __global__ void __launch_bounds__(256) coefficients(Zone z, CoeArgs a) {
     c3 = vmj * 2. + xmvis * tc2j * tc2j * 4.;
     double vmk = fabs(tczk * w) + c * tc2k;
     c4 = vmk * 2. + xmvis * tc2k * tc2k * 4.;
+  } else if (z.typ == Z2D) {  // tstb3c.for 2-d branch: i and j only
+    const int64_t lt = indmtr(z, i, j, k), m = z.ndm;
+    double detj = fmaxF(z.vol[lt], cut0x);
+    double volu = detj * rr;
+    double xmvis = vmu / volu;
+    const double* T2[2] = {z.ti, z.tj};
+    double cc[2];
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+      const double* T = T2[d];
+      int64_t l2 = lt + z.minc[d];
+      double tx = .5 * (T[lt] + T[l2]);
+      double ty = .5 * (T[lt + m] + T[l2 + m]);
+      double tc2 = .5 * (sqrt(T[lt] * T[lt] + T[lt + m] * T[lt + m]) + sqrt(T[l2] * T[l2] + T[l2 + m] * T[l2 + m]));
+      double qn = tx * u + ty * v;
+      double vm = fabs(qn) + c * tc2;
+      cc[d] = vm * 2. + xmvis * tc2 * tc2 * 4.;
+    }
+    a.coe[l + nd] = cc[0];
+    a.coe[l + 2 * nd] = cc[1];
+    a.coe[l + 4 * nd] = xid + c1 * (cc[0] + cc[1]) * 0.5;
+    return;
   } else {
     const int64_t lt = indmtr(z, i, j, k), m = z.ndm;
     double detj = fmaxF(z.vol[lt], cut0x);
@@ -178,6 +200,12 @@ __device__ __forceinline__ void nb_normal(const Zone& z, int d, int64_t lta, int
     tx = d == 0 ? T(z.tcx) : T(0);
     ty = d == 1 ? T(z.tcy) : T(0);
     tz = d == 2 ? T(z.tcz) : T(0);
+  } else if (TYP == Z2D) {   // lu_{i,j}_2d.for: two components
+    const double* M = d == 0 ? z.ti : z.tj;
+    const int64_t m = z.ndm;
+    tx = T(0.5 * (M[ltb] + M[lta]));
+    ty = T(0.5 * (M[ltb + m] + M[lta + m]));
+    tz = T(0);
   } else {
     const double* M = d == 0 ? z.ti : (d == 1 ? z.tj : z.tk);
     const int64_t m = z.ndm;
@@ -203,6 +231,8 @@ template <typename T> __device__ __forceinline__ T ldcg(const T* p) { return __l
 constexpr int NB_CART = 14;   // entries per direction, 3d cartesian zone
 constexpr int NB_FULL = 25;   // entries per direction, 3d general zone
 template <int TYP> struct NBE { static constexpr int n = TYP == Z3DCART ? NB_CART : NB_FULL; };
+// 2-d zones use the general entries with tz = 0 and w = 0 (lu_{i,j}_2d.for
+// is lu_{i,j}_3dfull.for without the w / tz terms, which vanish exactly)
 
 template <int TYP, typename T>
 __device__ __forceinline__ void bentries(const Zone& z, int d, T u, T v, T w, T t, T tcx, T tcy,
@@ -274,6 +304,12 @@ __device__ __forceinline__ void bmatvec(const Zone& z, const T* e, T cs, const T
       b[3] = e[5] * o[0] + e[6] * o[1] + e[7] * o[2] + (e[8] + cs) * o[3] + b45 * o[4];
       b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
     }
+  } else if (TYP == Z2D) {   // lu_{i,j}_2d.for: no w row
+    b[0] = cs * o[0] + e[0] * o[1] + e[1] * o[2];
+    b[1] = e[3] * o[0] + (e[4] + cs) * o[1] + e[5] * o[2] + e[7] * o[4];
+    b[2] = e[8] * o[0] + e[9] * o[1] + (e[10] + cs) * o[2] + e[12] * o[4];
+    b[3] = T(0);
+    b[4] = e[18] * o[0] + e[19] * o[1] + e[20] * o[2] + (e[22] + cs) * o[4];
   } else {
     b[0] = cs * o[0] + e[0] * o[1] + e[1] * o[2] + e[2] * o[3];
     b[1] = e[3] * o[0] + (e[4] + cs) * o[1] + e[5] * o[2] + e[6] * o[3] + e[7] * o[4];
@@ -479,7 +515,7 @@ __device__ __forceinline__ void load_dio(const T* __restrict__ dio, int64_t g, T
 
 // mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW) in precision T; cvinv =
 // 1/cv in precision T (the FP64 quotient is the host's: the same IEEE value)
-template <typename T>
+template <typename T, bool TWO_D = false>
 __device__ __forceinline__ void newton(T cv, T cvinv, T ro, T u, T v, T w, T tt, const T d[5],
                                        T n[5]) {
   const T cvinv2 = T(0.5) * cvinv;
@@ -487,6 +523,12 @@ __device__ __forceinline__ void newton(T cv, T cvinv, T ro, T u, T v, T w, T tt,
   const T r_1 = T(1.) / n[0];
   n[1] = (ro * u + d[1]) * r_1;
   n[2] = (ro * v + d[2]) * r_1;
+  if (TWO_D) {  // mjr_newton.for 2-d branch: w = 0
+    n[3] = T(0);
+    const T roe_old = ro * (cv * tt + T(0.5) * (u * u + v * v));
+    n[4] = (roe_old + d[4]) * r_1 * cvinv - cvinv2 * (n[1] * n[1] + n[2] * n[2]);
+    return;
+  }
   n[3] = (ro * w + d[3]) * r_1;
   const T roe_old = ro * (cv * tt + T(0.5) * (u * u + v * v + w * w));
   n[4] = (roe_old + d[4]) * r_1 * cvinv - cvinv2 * (n[1] * n[1] + n[2] * n[2] + n[3] * n[3]);
@@ -611,7 +653,7 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
   // in place: the k-1 neighbour needs this cell's new state in the next plane
   T nw[5];
   const T cvinv = sizeof(T) == 8 ? T(z.cvinv) : T(1.) / T(z.cv);
-  newton<T>(T(z.cv), cvinv, o.st[0], o.st[1], o.st[2], o.st[3], o.st[4], x, nw);
+  newton<T, TYP == Z2D>(T(z.cv), cvinv, o.st[0], o.st[1], o.st[2], o.st[3], o.st[4], x, nw);
   T* q = p.nst + g * 4;
 #pragma unroll
   for (int v = 0; v < 4; v++) q[v] = nw[v + 1];
@@ -753,7 +795,7 @@ __global__ void __launch_bounds__(128) lusgs_plane(Zone z, PlaneData<T> p, LuFie
 // GT_I x GT_J cells at one k as in lu_gather: the increments of a tile
 // anti-diagonal are contiguous in plane order, so the CTA reads them as
 // spans into shared memory, then updates its cells in natural order.
-template <typename T>
+template <typename T, bool TWO_D>
 __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* __restrict__ dio) {
   __shared__ __align__(16) T s_dio[GT_N * DIO];
   __shared__ int32_t s_g[GT_N];
@@ -780,8 +822,8 @@ __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* _
     double d[5], nw[5];
 #pragma unroll
     for (int v = 0; v < 5; v++) d[v] = double(s_dio[q * DIO + v]);
-    newton<double>(z.cv, z.cvinv, R[l], R[l + nd], R[l + 2 * nd], R[l + 3 * nd], R[l + 4 * nd], d,
-                   nw);
+    newton<double, TWO_D>(z.cv, z.cvinv, R[l], R[l + nd], R[l + 2 * nd], R[l + 3 * nd], R[l + 4 * nd],
+                          d, nw);
 #pragma unroll
     for (int v = 0; v < 5; v++) f.rop_new[l + v * nd] = nw[v];
     return;
@@ -801,13 +843,14 @@ __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* _
   const float r1 = 1.f / float(ron);
   const float fu = float(u), fv = float(v), fw = float(w), cv = float(z.cv);
   const float e = cv * float(tt) + 0.5f * (fu * fu + fv * fv + fw * fw);
-  const float du = (d1 - fu * d0) * r1, dv = (d2 - fv * d0) * r1, dw = (d3 - fw * d0) * r1;
+  const float du = (d1 - fu * d0) * r1, dv = (d2 - fv * d0) * r1;
+  const float dw = TWO_D ? 0.f : (d3 - fw * d0) * r1;   // 2-d: w = 0
   const float de = (d4 - e * d0) * r1;
   const float dT = (de - 0.5f * (du * (2.f * fu + du) + dv * (2.f * fv + dv) + dw * (2.f * fw + dw))) / cv;
   f.rop_new[l] = ron;
   f.rop_new[l + nd] = u + double(du);
   f.rop_new[l + 2 * nd] = v + double(dv);
-  f.rop_new[l + 3 * nd] = w + double(dw);
+  f.rop_new[l + 3 * nd] = TWO_D ? 0. : w + double(dw);
   f.rop_new[l + 4 * nd] = tt + double(dT);
 }
 
@@ -830,8 +873,8 @@ static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (L.persistent) {
-    static int grid_cache[2][2] = {{0, 0}, {0, 0}};
-    int& grid = grid_cache[TYP == Z3DCART][sizeof(T) == 4];
+    static int grid_cache[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    int& grid = grid_cache[TYP == Z3DCART ? 0 : (TYP == Z2D ? 1 : 2)][sizeof(T) == 4];
     if (grid == 0) {
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
@@ -860,8 +903,9 @@ static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>
   }
   if (e != cudaSuccess) return e;
   if (!f.inplace || sizeof(T) == 4) {
-    lu_newton<T><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I), (unsigned)((z.nj + GT_J - 1) / GT_J),
-                        (unsigned)z.nk), GT_N, 0, st>>>(z, f, p.dio);
+    lu_newton<T, TYP == Z2D><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I),
+                                    (unsigned)((z.nj + GT_J - 1) / GT_J), (unsigned)z.nk),
+                               GT_N, 0, st>>>(z, f, p.dio);
     e = cudaGetLastError();
   }
   return e;
@@ -882,6 +926,7 @@ static PlaneData<T> plane_data(const LuLaunch& L, int rec_size) {
 // words of LU work per interior cell (the caller allocates G * this * 8 bytes)
 int64_t lusgs_work_words(int typ) {
   return (typ == Z3DCART ? Rec<Z3DCART, double>::SIZE : Rec<Z3DFULL, double>::SIZE) + DIO + 4;
+  // (2-d zones use the general record layout)
 }
 
 cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl, int32_t* nbu,
@@ -896,13 +941,15 @@ cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cuda
   if (L.fp32) {
     const int rs = z.typ == Z3DCART ? Rec<Z3DCART, float>::SIZE : Rec<Z3DFULL, float>::SIZE;
     PlaneData<float> p = plane_data<float>(L, rs);
-    return z.typ == Z3DCART ? launch_t<Z3DCART, float>(z, f, p, L, st)
-                            : launch_t<Z3DFULL, float>(z, f, p, L, st);
+    if (z.typ == Z3DCART) return launch_t<Z3DCART, float>(z, f, p, L, st);
+    if (z.typ == Z2D) return launch_t<Z2D, float>(z, f, p, L, st);
+    return launch_t<Z3DFULL, float>(z, f, p, L, st);
   }
   const int rs = z.typ == Z3DCART ? Rec<Z3DCART, double>::SIZE : Rec<Z3DFULL, double>::SIZE;
   PlaneData<double> p = plane_data<double>(L, rs);
-  return z.typ == Z3DCART ? launch_t<Z3DCART, double>(z, f, p, L, st)
-                          : launch_t<Z3DFULL, double>(z, f, p, L, st);
+  if (z.typ == Z3DCART) return launch_t<Z3DCART, double>(z, f, p, L, st);
+  if (z.typ == Z2D) return launch_t<Z2D, double>(z, f, p, L, st);
+  return launch_t<Z3DFULL, double>(z, f, p, L, st);
 }
 
 }  // namespace fgb

@@ -24,8 +24,10 @@ def dims(nijk_xyz, typ):
         return [0, 0, 0, 0, 0], 1, 1, 1
     if typ == 0:
         return [1, nvi, nvi * nvj, ng, ngk], nvi * nvj * nvk, 3, 3
-    raise NotImplementedError(f"zone type {typ} (1 = 3-d with a homogeneous k direction, 3 = 2-d) "
-                              "is not implemented: only 3-d general (0) and 3-d cartesian (2)")
+    if typ == 3:   # nature_geom_dom.for:117-126
+        return [1, nvi, 0, ng, ngk], nvi * nvj, 2, 0
+    raise NotImplementedError(f"zone type {typ} (3-d with a homogeneous k direction) "
+                              "is not implemented: only 3-d general (0), 3-d cartesian (2) and 2-d (3)")
 
 
 def _faces_i(x, y, z):
@@ -100,6 +102,8 @@ def compute(x, y, z, typ, ng=2, ngk=2):
         az = 0.25 * ((((Z[2] + Z[3]) + Z[6]) + Z[7]) * tk - (((Z[0] + Z[1]) + Z[4]) + Z[5]) * tk)
         vol = max(((ax + ay) + az) / 3.0, 1.0e-30)
         return (np.array([ti]), np.array([tj]), np.array([tk]), np.array([vol]))
+    if typ == 3:
+        return _compute_2d(x, y, z)
     if typ != 0:
         raise NotImplementedError(f"zone type {typ}")
     shape = (nvi, nvj, nvk)
@@ -179,3 +183,58 @@ def _corners_k(a, sl_i, sl_j, sl_k):
             a[sl_i.start + 1:sl_i.stop + 1, sl_j.start:sl_j.stop, k:k + 1],
             a[sl_i.start:sl_i.stop, sl_j.start + 1:sl_j.stop + 1, k:k + 1],
             a[sl_i.start + 1:sl_i.stop + 1, sl_j.start + 1:sl_j.stop + 1, k:k + 1])
+
+
+def _compute_2d(x, y, z):
+    """2-d zone (one cell in k, no k ghosts): cp_tijk.for 2-d branch (i and
+    j faces, x and y components) and cp_vol.for 2-d branch, on the vertex
+    grid of the k = 1 layer (lt = flat index of vertex (i, j))."""
+    nvi, nvj, _ = x.shape
+    ti = np.zeros((2, nvi, nvj))
+    tj = np.zeros((2, nvi, nvj))
+    cells = (slice(0, nvi - 1), slice(0, nvj - 1))
+    def v(a, di, dj, dk):
+        return a[di:nvi - 1 + di, dj:nvj - 1 + dj, dk]
+    X = [v(x, *o) for o in ((0, 0, 0), (0, 1, 0), (0, 0, 1), (0, 1, 1), (1, 0, 0), (1, 1, 0), (1, 0, 1), (1, 1, 1))]
+    Y = [v(y, *o) for o in ((0, 0, 0), (0, 1, 0), (0, 0, 1), (0, 1, 1), (1, 0, 0), (1, 1, 0), (1, 0, 1), (1, 1, 1))]
+    Z = [v(z, *o) for o in ((0, 0, 0), (0, 1, 0), (0, 0, 1), (0, 1, 1), (1, 0, 0), (1, 1, 0), (1, 0, 1), (1, 1, 1))]
+    r = _faces_i(X[:4], Y[:4], Z[:4])
+    ti[0][cells], ti[1][cells] = r[0], r[1]
+    sel = (0, 4, 2, 6)
+    r = _faces_j(tuple(X[q] for q in sel), tuple(Y[q] for q in sel), tuple(Z[q] for q in sel))
+    tj[0][cells], tj[1][cells] = r[0], r[1]
+    # last faces i = imax+1, j = jmax+1
+    fi = [a[nvi - 1:nvi, 0:nvj - 1, 0] for a in (x, y, z)]
+    fi1 = [a[nvi - 1:nvi, 1:nvj, 0] for a in (x, y, z)]
+    fi2 = [a[nvi - 1:nvi, 0:nvj - 1, 1] for a in (x, y, z)]
+    fi3 = [a[nvi - 1:nvi, 1:nvj, 1] for a in (x, y, z)]
+    r = _faces_i(*[(fi[c], fi1[c], fi2[c], fi3[c]) for c in range(3)])
+    ti[0][nvi - 1:nvi, 0:nvj - 1], ti[1][nvi - 1:nvi, 0:nvj - 1] = r[0], r[1]
+    fj = [a[0:nvi - 1, nvj - 1:nvj, 0] for a in (x, y, z)]
+    fj4 = [a[1:nvi, nvj - 1:nvj, 0] for a in (x, y, z)]
+    fj2 = [a[0:nvi - 1, nvj - 1:nvj, 1] for a in (x, y, z)]
+    fj6 = [a[1:nvi, nvj - 1:nvj, 1] for a in (x, y, z)]
+    r = _faces_j(*[(fj[c], fj4[c], fj2[c], fj6[c]) for c in range(3)])
+    tj[0][0:nvi - 1, nvj - 1:nvj], tj[1][0:nvi - 1, nvj - 1:nvj] = r[0], r[1]
+    i1 = (slice(1, nvi), slice(0, nvj - 1))
+    j1 = (slice(0, nvi - 1), slice(1, nvj))
+    comp = []
+    for c, A in enumerate((X, Y)):
+        s1 = ((A[4] + A[5]) + A[7]) + A[6]
+        s2 = ((A[0] + A[1]) + A[3]) + A[2]
+        s3 = ((A[1] + A[3]) + A[5]) + A[7]
+        s4 = ((A[0] + A[2]) + A[4]) + A[6]
+        acc = s1 * ti[c][i1] - s2 * ti[c][cells]
+        acc = acc + s3 * tj[c][j1]
+        acc = acc - s4 * tj[c][cells]
+        comp.append(0.25 * acc)
+    tkz10 = (X[4] - X[0]) * (Y[5] - Y[4]) - (Y[4] - Y[0]) * (X[5] - X[4])
+    tkz11 = (X[1] - X[5]) * (Y[0] - Y[1]) - (Y[1] - Y[5]) * (X[0] - X[1])
+    tk1 = 0.5 * (tkz10 + tkz11)
+    az = 0.25 * (((((((Z[2] + Z[3]) + Z[6]) + Z[7]) - Z[0]) - Z[1]) - Z[4]) - Z[5]) * tk1
+    vol = np.zeros((nvi, nvj))
+    vol[cells] = np.maximum(((comp[0] + comp[1]) + az) / 3.0, 1.0e-30)
+    return (np.concatenate([ti[c].reshape(-1, order="F") for c in range(2)]),
+            np.concatenate([tj[c].reshape(-1, order="F") for c in range(2)]),
+            np.zeros(0),
+            vol.reshape(-1, order="F"))

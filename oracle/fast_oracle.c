@@ -264,7 +264,7 @@ static void fctx_init(fctx* c, const int64_t* pi, const double* pr, const double
   c->typ = (int)pi[ITYPZONE]; c->iflow = (int)pi[IFLOW]; c->kflu = (int)pi[KFLUDOM];
   c->slope = (int)pi[SLOPE];
   /* template_FluxAndBalance.for:108-156 */
-  c->tcx = ti[0]; c->tcy = tj[0]; c->tcz = tk[0];
+  c->tcx = ti[0]; c->tcy = tj[0]; c->tcz = pi[NEQ_K] > 0 ? tk[0] : 0.;  /* a 2-d zone has no tk */
   c->si = fabs(c->tcx); c->sj = fabs(c->tcy); c->sk = fabs(c->tcz);
   c->volinv = 0.5 / vol[0];
   c->gam = pr[GAMMA];
@@ -1257,9 +1257,47 @@ void or_metric(const int64_t* pi, const double* x, const double* y, const double
     vol[0] = OMAX((ax + ay + az) / 3., 1.e-30);
     return;
   }
-  const int64_t ndm = nvi * nvj * nvk;
   const int64_t iv = pi[IJKV], jv = pi[IJKV + 1], kv = pi[IJKV + 2];
   const int64_t ngc = pi[NIJK + 3], ngkc = pi[NIJK + 4];
+  if (pi[ITYPZONE] == 3) {   /* 2-d: cp_tijk.for / cp_vol.for "Domaine 2D" branches, k = 1 */
+    const int64_t ndm2 = nvi * nvj;
+#define VT(i, j) (((i) + ng - 1) + ((j) + ng - 1) * nvi)
+    for (int64_t j = 1 - ngc; j <= jv + ngc + 1; j++)
+      for (int64_t i = 1 - ngc; i <= iv + ngc + 1; i++) {
+        const int64_t lt = VT(i, j), l0 = VX(i, j, 1), l1 = l0 + incj, l2 = l0 + inck, l3 = l1 + inck;
+        const int64_t l4 = l0 + inci, l6 = l2 + inci;
+        if (j <= jv + ngc) {
+          face_i(x, y, z, l0, l1, l2, l3, t);
+          ti[lt] = t[0]; ti[lt + ndm2] = t[1];
+        }
+        if (i <= iv + ngc) {
+          face_j(x, y, z, l0, l4, l2, l6, t);
+          tj[lt] = t[0]; tj[lt + ndm2] = t[1];
+        }
+      }
+    for (int64_t j = 1 - ngc; j <= jv + ngc; j++)
+      for (int64_t i = 1 - ngc; i <= iv + ngc; i++) {
+        const int64_t lt = VT(i, j), l0 = VX(i, j, 1), l1 = l0 + incj, l2 = l0 + inck, l3 = l1 + inck;
+        const int64_t l4 = l0 + inci, l5 = l1 + inci, l6 = l2 + inci, l7 = l3 + inci;
+        const int64_t lip = lt + 1, ljp = lt + nvi;
+        double a[2];
+        const double* c2[2] = {x, y};
+        for (int c = 0; c < 2; c++) {
+          const double* q = c2[c];
+          const int64_t o = c * ndm2;
+          a[c] = .25 * ((q[l4] + q[l5] + q[l7] + q[l6]) * ti[lip + o] - (q[l0] + q[l1] + q[l3] + q[l2]) * ti[lt + o] +
+                        (q[l1] + q[l3] + q[l5] + q[l7]) * tj[ljp + o] - (q[l0] + q[l2] + q[l4] + q[l6]) * tj[lt + o]);
+        }
+        double tkz10 = (x[l4] - x[l0]) * (y[l5] - y[l4]) - (y[l4] - y[l0]) * (x[l5] - x[l4]);
+        double tkz11 = (x[l1] - x[l5]) * (y[l0] - y[l1]) - (y[l1] - y[l5]) * (x[l0] - x[l1]);
+        double tk1 = .5 * (tkz10 + tkz11);
+        double az = .25 * (z[l2] + z[l3] + z[l6] + z[l7] - z[l0] - z[l1] - z[l4] - z[l5]) * tk1;
+        vol[lt] = OMAX((a[0] + a[1] + az) / 3., 1.e-30);
+      }
+#undef VT
+    return;
+  }
+  const int64_t ndm = nvi * nvj * nvk;
   for (int64_t k = 1 - ngkc; k <= kv + ngkc; k++)
     for (int64_t j = 1 - ngc; j <= jv + ngc; j++)
       for (int64_t i = 1 - ngc; i <= iv + ngc; i++) {
@@ -1338,6 +1376,8 @@ static void bc_normal(const int64_t* pi, const double* ti, const double* tj, con
   const int64_t lm = indmtr(pi, c[0], c[1], c[2]);
   if (neq_mtr == 3) {
     t[0] = T[lm] * 1.; t[1] = T[lm + ndm] * 1.; t[2] = T[lm + 2 * ndm] * 1.;
+  } else if (neq_mtr == 2) {   /* ic = 1, jc = 2, kc = 2, ck_mtr = 0 */
+    t[0] = T[lm] * 1.; t[1] = T[lm + ndm] * 1.; t[2] = T[lm + ndm] * 0.;
   } else {
     double ci = d == 0 ? 1. : 0., cj = d == 1 ? 1. : 0., ck = d == 2 ? 1. : 0.;
     t[0] = T[lm] * ci; t[1] = T[lm] * cj; t[2] = T[lm] * ck;

@@ -336,3 +336,54 @@ def test_roe_wall_flux_correction_implicit(oracle_mod):
         s.compute(it, 1, 4, 1, 1)
     _check_levels(ref, s)
     s.close()
+
+
+@pytest.mark.parametrize("scheme,slope,wavy", [("roe_min", "minmod", 0.0), ("roe", "o3", 0.3),
+                                               ("ausmpred", "o3", 0.3)])
+def test_2d_explicit(oracle_mod, scheme, slope, wavy):
+    """2-d zones (ITYPZONE 3): i and j faces only, no w."""
+    t = cases.isentropic_vortex(n=(24, 20, 1), two_d=True, wavy=wavy,
+                                numz={"scheme": scheme, "slope": slope, "time_step": 0.05})
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    assert int(zd[0]["pi"][25]) == 3
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
+@pytest.mark.parametrize("scheme,slope,wavy", [("ausmpred", "o3", 0.0), ("roe_min", "minmod", 0.3)])
+def test_2d_implicit(oracle_mod, scheme, slope, wavy):
+    """LU-SGS on 2-d zones (lu_{i,j}_2d.for, 2-d Newton update)."""
+    t = cases.isentropic_vortex(n=(20, 16, 1), two_d=True, wavy=wavy,
+                                numb={"temporal_scheme": "implicit", "ss_iteration": 3,
+                                      "modulo_verif": 1},
+                                numz={"scheme": scheme, "slope": slope, "time_step": 0.2})
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
+    nss = int(zd[0]["pi"][58])
+    assert rel_err(s.residuals(0), ref.residual_norms(0, nss)) <= TOL
+    s.close()
+
+
+@pytest.mark.parametrize("scheme,slope,temporal", [("ausmpred", "o3", "explicit"),
+                                                   ("roe", "o3", "explicit"),
+                                                   ("roe_min", "minmod", "implicit")])
+def test_2d_bcs(oracle_mod, scheme, slope, temporal):
+    """2-d zone with inflow, outflow, slip wall (Roe: wall-face correction)
+    and farfield on a curvilinear mesh."""
+    t = cases.bc_box(n=(16, 12, 1), two_d=True, wall="BCWallInviscid", model="Euler", scheme=scheme,
+                     slope=slope, wavy=0.3, temporal=temporal, ss_iteration=3,
+                     time_step=0.02 if temporal == "explicit" else 0.05)
+    mv = 1000 if temporal == "explicit" else 1
+    zd, ref, s = _pair(t, oracle_mod, mv)
+    nfin = 3 if temporal == "explicit" else 4
+    for it in range(1, 3):
+        ref.compute(it, 1, nfin, 1, modulo_verif=mv)
+        s.compute(it, 1, nfin, 1, 1)
+    _check_levels(ref, s)
+    s.close()

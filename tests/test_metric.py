@@ -102,3 +102,24 @@ def test_free_stream_preservation_curvilinear_viscous(oracle_mod):
     for it in range(1, 3):
         c.compute(it, 1, 3, 1, modulo_verif=1000)
     assert np.max(np.abs(c.z[0]["lv"][0] - q0)) < 1e-13
+
+
+@pytest.mark.parametrize("wavy", [0.0, 0.3])
+def test_metric_2d_equals_oracle_and_free_stream(oracle_mod, wavy):
+    """2-d zones (one cell in k, no k ghosts): cp_tijk / cp_vol 2-d branches
+    against the oracle, and a free stream that stays a free stream."""
+    t = cases.isentropic_vortex(n=(12, 10, 1), two_d=True, wavy=wavy, beta=0.0,
+                                numz={"scheme": "roe", "slope": "o3", "time_step": 0.05})
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    pi = zd[0]["pi"]
+    assert int(pi[25]) == 3 and int(pi[4]) == 0
+    o = oracle_mod.metric(pi, *_coords(t))
+    for a, b in zip(o, (zd[0]["ti"], zd[0]["tj"], zd[0]["tk"], zd[0]["vol"])):
+        assert np.array_equal(a, b)
+    c = oracle_mod.Case(zd)
+    c.apply_bc(0)
+    c.apply_bc(1)
+    q0 = c.z[0]["lv"][0].copy()
+    for it in range(1, 4):
+        c.compute(it, 1, 3, 1, modulo_verif=1000)
+    assert np.max(np.abs(c.z[0]["lv"][0] - q0)) < 1e-14
