@@ -27,6 +27,7 @@ SIGNATURES = {
     "fgb_add_zone": ([_P, _I64P, C.c_int64, _DP, C.c_int64, _DP, _DP, _DP, _DP,
                       C.POINTER(C.c_int)], C.c_int),
     "fgb_add_transfer": ([_P, C.c_int, C.c_int, C.c_int64, _I64P, _I64P], C.c_int),
+    "fgb_set_wall_distance": ([_P, C.c_int, _DP], C.c_int),
     "fgb_set_option": ([_P, C.c_char_p, C.c_double], C.c_int),
     "fgb_get_option": ([_P, C.c_char_p, _DP], C.c_int),
     "fgb_upload_state": ([_P, C.c_int, C.c_int, _DP], C.c_int),
@@ -121,6 +122,11 @@ class Solver:
         d = np.ascontiguousarray(dnr_idx, dtype=np.int64)
         r = np.ascontiguousarray(rcv_idx, dtype=np.int64)
         _check(self._lib.fgb_add_transfer(self._h, int(dnr), int(rcv), d.size, _ip(d), _ip(r)))
+
+    def set_wall_distance(self, zone: int, dist):
+        """TurbulentDistance of a Spalart-Allmaras zone (NDIMDX values)."""
+        d = np.ascontiguousarray(dist, dtype=np.float64).reshape(-1)
+        _check(self._lib.fgb_set_wall_distance(self._h, int(zone), _dp(d)))
 
     def set_option(self, key: str, value: float):
         _check(self._lib.fgb_set_option(self._h, key.encode(), float(value)))

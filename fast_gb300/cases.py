@@ -101,7 +101,16 @@ def set_conservative(z, ro, u, v, w, p, gamma):
         I.createUniqueChild(sol, nm, "DataArray_t")[1] = np.asfortranarray(arr)
 
 
-def _tree(zones, model, numb, numz, mach, reynolds, gamma=1.4, prandtl=0.72, sutherland=True):
+def set_spalart(z, nutilde, dist):
+    """Spalart-Allmaras fields at centers: nutilde (TurbulentSANuTilde) and
+    the wall distance (TurbulentDistance, which FastS requires as input)."""
+    sol = I.createUniqueChild(z, I.__FlowSolutionCenters__, "FlowSolution_t")
+    I.createUniqueChild(sol, "TurbulentSANuTilde", "DataArray_t")[1] = np.asfortranarray(nutilde)
+    I.createUniqueChild(sol, "TurbulentDistance", "DataArray_t")[1] = np.asfortranarray(dist)
+
+
+def _tree(zones, model, numb, numz, mach, reynolds, gamma=1.4, prandtl=0.72, sutherland=True,
+          nutilde_ratio=0.1):
     t = I.newCGNSTree()
     b = I.newCGNSBase("Base", 3, 3, t)
     for z in zones:
@@ -110,7 +119,7 @@ def _tree(zones, model, numb, numz, mach, reynolds, gamma=1.4, prandtl=0.72, sut
     I.createChild(I.getNodeFromName1(b, "FlowEquationSet"), "GoverningEquations",
                   "GoverningEquations_t", model)
     FastC.addReferenceState(t, mach=mach, reynolds=reynolds, gamma=gamma, prandtl=prandtl,
-                            sutherland=sutherland)
+                            sutherland=sutherland, nutilde_ratio=nutilde_ratio)
     FastC._setNum2Base(t, numb)
     FastC._setNum2Zones(t, numz)
     return t
@@ -151,10 +160,12 @@ def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0,
 
 def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_iteration=4,
                  dt=None, scheme="ausmpred", slope="o3", numb=None, numz=None, name="tgv",
-                 wavy=0.0, model="NSLaminar"):
+                 wavy=0.0, model="NSLaminar", nutilde_ratio=5.0, wall_distance=1.0e8):
     """Config: laminar Taylor-Green vortex on the periodic box [0, 2 pi]^3,
     Re = 1600, Mach 0.1, Pr 0.71, mu ~ sqrt(T) (FastS Sutherland form with
-    Cs = 0), AUSM+(P) o3, implicit LU-SGS dual time stepping."""
+    Cs = 0), AUSM+(P) o3, implicit LU-SGS dual time stepping.  model
+    "NSTurbulent" adds Spalart-Allmaras with ro nutilde = nutilde_ratio x mu
+    and a uniform wall distance (no wall in the periodic box)."""
     N = (n, n, n) if isinstance(n, int) else tuple(n)
     L = 1.0
     h = tuple(2 * math.pi * L / k for k in N)
@@ -171,6 +182,8 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
     p = p0 + ro0 * U0 ** 2 / 16.0 * (np.cos(2 * xc / L) + np.cos(2 * yc / L)) * (np.cos(2 * zc / L) + 2.0)
     ro = p * gamma / T0   # T = T0 everywhere (R = 1/gamma)
     set_conservative(z, ro, u, v, w, p, gamma)
+    if model == "NSTurbulent":
+        set_spalart(z, nutilde_ratio * (mach / reynolds) / ro, np.full_like(ro, wall_distance))
     for f in ("imin", "imax", "jmin", "jmax", "kmin", "kmax"):
         add_bc(z, "per_" + f, "BCautoperiod", f)
     if dt is None:
@@ -181,18 +194,20 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
                     "cache_blocking_I": 1000000, "cache_blocking_J": 1000000,
                     "cache_blocking_K": 1000000}
     return _tree([z], model, numb, numz, mach, reynolds, gamma=gamma, prandtl=prandtl,
-                 sutherland=False)
+                 sutherland=False, nutilde_ratio=nutilde_ratio)
 
 
 def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model="NSLaminar",
            wavy=0.0, perturb=0.05, temporal="explicit", ss_iteration=3, scheme="ausmpred",
-           slope="o3", time_step=0.02, gamma=1.4, two_d=False):
+           slope="o3", time_step=0.02, gamma=1.4, two_d=False, nutilde_ratio=5.0):
     """Box [0,1]x[0,1]x[0,dz] exercising the non-periodic BCs of the path:
     inflow at imin (BCInflow), outflow at imax (BCOutflow), a wall at jmin
     (``wall``), farfield at jmax (BCFarfield), periodic in k.  The initial
     field is the free stream with a smooth perturbation of relative size
     ``perturb`` (0 gives the free stream itself).  wavy > 0 displaces the
-    vertices as in ``wave`` (periods = box lengths)."""
+    vertices as in ``wave`` (periods = box lengths).  model "NSTurbulent"
+    adds Spalart-Allmaras: free-stream ro nutilde = nutilde_ratio x mu, the
+    same perturbation on nutilde, and the distance to the jmin wall."""
     ni, nj, nk = n
     if two_d:
         nk = 1
@@ -210,6 +225,10 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
     w = 0.0 * xc if two_d else mach * a * np.sin(2 * math.pi * xc) * np.cos(2 * math.pi * yc)
     p = (1.0 + a * 0.5 * s) / gamma
     set_conservative(z, ro, u, v, w, p, gamma)
+    if model == "NSTurbulent":
+        mu = mach / reynolds
+        set_spalart(z, nutilde_ratio * mu * (1.0 + a * np.cos(2 * math.pi * xc) * np.sin(math.pi * yc)) / ro,
+                    np.abs(yc))
     add_bc(z, "in", "BCInflow", "imin")
     add_bc(z, "out", "BCOutflow", "imax")
     add_bc(z, "wall", wall, "jmin")
@@ -220,4 +239,5 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
     numb = {"temporal_scheme": temporal, "ss_iteration": ss_iteration, "modulo_verif": 1}
     numz = {"scheme": scheme, "slope": slope, "time_step": time_step,
             "cache_blocking_I": 1000000, "cache_blocking_J": 1000000, "cache_blocking_K": 1000000}
-    return _tree([z], model, numb, numz, mach, reynolds if model != "Euler" else 0.0, gamma=gamma)
+    return _tree([z], model, numb, numz, mach, reynolds if model != "Euler" else 0.0, gamma=gamma,
+                 nutilde_ratio=nutilde_ratio)

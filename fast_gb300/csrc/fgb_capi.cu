@@ -51,6 +51,7 @@ struct GatherList {
   int32_t *q0 = nullptr, *q1 = nullptr, *q2 = nullptr;
   double* nrm = nullptr;
   double st[5] = {0, 0, 0, 0, 0};
+  int inflow = 0;                 // BCInflow: nutilde imposed (Spalart-Allmaras)
 };
 struct WallCorrList {             // one wall BC window of a Roe zone (correct_flux.for)
   int32_t *l = nullptr, *l0 = nullptr, *lt = nullptr;
@@ -69,6 +70,8 @@ struct ZoneData {
   double *ti = nullptr, *tj = nullptr, *tk = nullptr, *vol = nullptr;
   double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
   double* wig = nullptr;            // senseur wiggle flags (KFLUDOM = 2)
+  double* dist = nullptr;           // wall distance (Spalart-Allmaras)
+  bool dist_set = false;
   void* luwork = nullptr;           // plane-ordered LU work (FP64-sized)
   uint32_t* cells = nullptr;        // interior cells by hyperplane
   int64_t* plane = nullptr;         // plane offsets (device)
@@ -285,6 +288,7 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
       GatherList f;
       f.kind = 1;
       f.op = slip ? BCF_SLIP : (noslip ? BCF_NOSLIP : (type == 10 ? BCF_OUTFLOW : BCF_FARFIELD));
+      f.inflow = type == 13;
       f.n = (int64_t)fdst.size();
       // BCzone.cpp DEFAULT_STATE, nbdata = 0: the free stream
       f.st[0] = pr[ROINF];
@@ -426,6 +430,15 @@ static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const dou
   Z.cmus1 = r[CS];
   double temp01 = 1. / r[TEMP0];
   Z.coesut = r[XMUL0] * (1. + Z.cmus1 * temp01) * std::sqrt(temp01);
+  // Spalart-Allmaras (SA/vispalart.for, spsource_SA.for, fluausm_SA_*.for:114-127)
+  z.sa_cmus1 = r[CS];
+  z.sa_temp01 = 1. / r[TEMP0];
+  z.sa_coesut = r[XMUL0] * (1. + z.sa_cmus1 * z.sa_temp01);
+  z.gam4 = z.gam1 / r[PRANDT_TUR] * z.rgp;
+  z.sigma_1 = 1. / SA_SIGMA;
+  z.ratiom = r[SA_RATIOM];
+  z.sa_low_re = (double)p[SA_LOW_RE];
+  z.sa_rot = (double)p[SA_ROT_CORR];
 }
 
 // ------------------------------------------------------------- C ABI
@@ -473,6 +486,7 @@ int fgb_destroy(fgb_solver* s) {
       cudaFree(g.nrm);
     }
     cudaFree(Z.wig);
+    cudaFree(Z.dist);
     for (WallCorrList& w : Z.walls) { cudaFree(w.l); cudaFree(w.l0); cudaFree(w.lt); cudaFree(w.nrm); }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
@@ -504,7 +518,16 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   if (p[ITYPZONE] == Z2D && (p[IFLOW] != 1 || p[KFLUDOM] == SENSEUR))
     return fail(FGB_ERR_ARG, "2-d zones are supported for the Euler equations with the Roe and "
                              "AUSM+(P) schemes on the GPU path");
-  if (p[NEQ] != 5) return fail(FGB_ERR_ARG, "only 5-equation models are supported on the GPU path");
+  if (p[NEQ] != (p[IFLOW] == 3 ? 6 : 5))
+    return fail(FGB_ERR_ARG, "NEQ must be 5 (Euler, laminar) or 6 (Spalart-Allmaras)");
+  if (p[IFLOW] == 3) {
+    if (p[ITYPZONE] == Z2D || p[KFLUDOM] != AUSM || p[SLOPE] != O3 || p[ILES] != 0 ||
+        p[SA_INT] != 0)
+      return fail(FGB_ERR_ARG, "Spalart-Allmaras is supported on 3-d zones with the AUSM+(P) "
+                               "o3 scheme (SA, not ZDES) on the GPU path");
+    if (p[ITYPCP] <= 1 && p[NEQ_COE] < 6)
+      return fail(FGB_ERR_ARG, "implicit Spalart-Allmaras needs NEQ_COE = 6");
+  }
   if (p[NIJK + 3] != 2 || p[NIJK + 4] != (p[ITYPZONE] == Z2D ? 0 : 2))
     return fail(FGB_ERR_ARG, "two ghost layers expected (none in k for a 2-d zone)");
   if (p[NDIMDX] != p[NIJK] * p[NIJK + 1] * p[NIJK + 2])
@@ -528,10 +551,15 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   CK(cudaMalloc(&Z.scratch, st_bytes));
   CK(cudaMalloc(&Z.drodm, st_bytes));
   CK(cudaMemset(Z.drodm, 0, st_bytes));
-  CK(cudaMalloc(&Z.coe, sizeof(double) * 5 * nd));
-  CK(cudaMemset(Z.coe, 0, sizeof(double) * 5 * nd));
+  CK(cudaMalloc(&Z.coe, sizeof(double) * neq * nd));
+  CK(cudaMemset(Z.coe, 0, sizeof(double) * neq * nd));
   CK(cudaMalloc(&Z.xmut, sizeof(double) * nd));
   CK(cudaMemset(Z.xmut, 0, sizeof(double) * nd));
+  if (neq == 6) {
+    CK(cudaMalloc(&Z.dist, sizeof(double) * nd));
+    CK(cudaMemset(Z.dist, 0, sizeof(double) * nd));
+  }
+  Z.z.dist = Z.dist;
   CK(dev_upload(&Z.ti, hti)); CK(dev_upload(&Z.tj, htj));
   CK(dev_upload(&Z.tk, htk)); CK(dev_upload(&Z.vol, hvol));
   Z.z.ti = Z.ti; Z.z.tj = Z.tj; Z.z.tk = Z.tk; Z.z.vol = Z.vol;
@@ -542,9 +570,9 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   }
   Z.z.wig = Z.wig;
   Z.z.opt0 = (double)p[SENSORTYPE];
-  CK(cudaMalloc(&Z.Fi, sizeof(double) * 5 * (ni + 1) * nj * nk));
-  CK(cudaMalloc(&Z.Fj, sizeof(double) * 5 * ni * (nj + 1) * nk));
-  CK(cudaMalloc(&Z.Fk, sizeof(double) * 5 * ni * nj * (nk + 1)));
+  CK(cudaMalloc(&Z.Fi, sizeof(double) * neq * (ni + 1) * nj * nk));
+  CK(cudaMalloc(&Z.Fj, sizeof(double) * neq * ni * (nj + 1) * nk));
+  CK(cudaMalloc(&Z.Fk, sizeof(double) * neq * ni * nj * (nk + 1)));
   for (int d = 0; d < 3; d++) {
     int64_t q = p[IJKV + d] / p[SIZE_SSDOM + d];
     Z.ijkv_lu[d] = q > 1 ? q : 1;
@@ -613,6 +641,17 @@ int fgb_add_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
   CK(dev_upload(&T.dnr_idx, d));
   CK(dev_upload(&T.rcv_idx, r));
   s->tr.push_back(T);
+  return FGB_OK;
+}
+
+int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist) {
+  if (!s || !dist) return fail(FGB_ERR_ARG, "null argument");
+  if (zone < 0 || zone >= (int)s->zones.size()) return fail(FGB_ERR_ARG, "zone out of range");
+  ZoneData& Z = s->zones[zone];
+  if (Z.z.neq != 6) return fail(FGB_ERR_ARG, "the zone has no Spalart-Allmaras equation");
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpy(Z.dist, dist, sizeof(double) * Z.z.nd, cudaMemcpyHostToDevice));
+  Z.dist_set = true;
   return FGB_OK;
 }
 
@@ -689,8 +728,9 @@ int fgb_download_work(fgb_solver* s, int zone, const char* which, double* host, 
   const double* src = nullptr;
   int64_t need = 0;
   if (w == "drodm") { src = Z.drodm; need = Z.z.neq * Z.z.nd; }
-  else if (w == "coe") { src = Z.coe; need = 5 * Z.z.nd; }
+  else if (w == "coe") { src = Z.coe; need = Z.z.neq * Z.z.nd; }
   else if (w == "xmut") { src = Z.xmut; need = Z.z.nd; }
+  else if (w == "dist" && Z.dist) { src = Z.dist; need = Z.z.nd; }
   else if (w == "rdm") { src = Z.rdm; need = Z.n_rdm; }
   else return fail(FGB_ERR_ARG, "unknown work array " + w);
   if (n < need) return fail(FGB_ERR_ARG, "buffer too small for " + w);
@@ -720,6 +760,9 @@ static int ghost_fill(fgb_solver* s, int level) {
         a.gam = Z.pr[GAMMA]; a.gam1 = Z.pr[GAMMA] - 1.; a.gam1_1 = 1. / a.gam1;
         a.cv = Z.pr[CVINF]; a.cvinv = 1. / Z.pr[CVINF];
         for (int m = 0; m < 5; m++) a.st[m] = g.st[m];
+        a.sa = Z.z.neq == 6;
+        a.inflow = g.inflow;
+        a.nue = Z.pr[RONUTILDEINF] / Z.pr[ROINF];   // BCFarfield_init.for: state(6) / state(1)
         CK(launch_bc_face(Z.lvl[level], a, s->st));
       } else {
         // BC_nextrank.for with the MUSCL constants of BCzone.cpp (c4, c5, c6)
@@ -728,6 +771,7 @@ static int ghost_fill(fgb_solver* s, int level) {
         BcNextArgs a{};
         a.dst = g.dst; a.q0 = g.q0; a.q1 = g.q1; a.q2 = g.q2; a.n = g.n; a.nd = Z.z.nd;
         a.k1 = -(c4 + c5) * k0; a.k2 = -c6 * k0; a.k3 = (2. - c5 - c4) * k0;
+        a.sa = Z.z.neq == 6;
         CK(launch_bc_next(Z.lvl[level], a, s->st));
       }
       s->launches++;
@@ -756,9 +800,13 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
   const std::vector<int64_t>& p0 = s->zones[0].pi;
   const int64_t nssiter = p0[NSSITER];
   const bool implicit = p0[ITYPCP] <= 1;
-  for (ZoneData& Z : s->zones)
+  for (ZoneData& Z : s->zones) {
     if ((Z.pi[ITYPCP] <= 1) != implicit || Z.pi[NSSITER] != nssiter)
       return fail(FGB_ERR_ARG, "all zones must share the temporal scheme");
+    if (Z.z.neq == 6 && !Z.dist_set)
+      return fail(FGB_ERR_STATE, "Spalart-Allmaras zone without wall distance "
+                                 "(fgb_set_wall_distance)");
+  }
   const double cxsi1 = -0.6830127018922193, cxsi2 = -4. / 3.;
   const double cg[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
   for (int it = 0; it < nit_c; it++) {
@@ -782,12 +830,16 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
         if (nstep == 1) {  // navier_stokes_struct.for:226-296 (first sub-step only)
           CoeArgs ca{};
           ca.rop = ssiter; ca.xmut_in = Z.xmut; ca.xmut = Z.xmut; ca.coe = Z.coe;
-          int64_t g = implicit ? 2 : (z.iflow == 2 ? 1 : 0);
-          int64_t gk = implicit ? z.ngk : (z.iflow == 2 ? (z.ngk ? 1 : 0) : 0);
+          // ranges: ind_coe (implicit, and SA/vispalart.for always), ind_grad
+          // (explicit laminar viscosity), the interior otherwise
+          const bool wide = implicit || z.iflow == 3;
+          int64_t g = wide ? 2 : (z.iflow == 2 ? 1 : 0);
+          int64_t gk = wide ? z.ngk : (z.iflow == 2 ? (z.ngk ? 1 : 0) : 0);
           ca.lo[0] = 1 - g; ca.hi[0] = z.ni + g;
           ca.lo[1] = 1 - g; ca.hi[1] = z.nj + g;
           ca.lo[2] = 1 - gk; ca.hi[2] = z.nk + gk;
           ca.do_invist = z.iflow == 2;
+          ca.do_sa = z.iflow == 3;
           ca.do_lu = implicit;
           ca.first_it = s->first_it;
           ca.coesut = Z.coesut; ca.cmus1 = Z.cmus1;
@@ -801,6 +853,13 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
           ProfScope ps(s, "wiggle");
           CK(launch_wiggle(z, ssiter, Z.wig, s->st));
           s->launches += 3;
+        }
+        if (z.neq == 6) {  // src_term.for:86-97: SA source (equation 6 initialised here)
+          ProfScope ps(s, "sa_source");
+          const int zero6 = implicit ? 1 : nstep == 1;
+          const double coefH6 = implicit ? 0. : (nstep == 2 ? cxsi1 : (nstep == 3 ? cxsi2 : 0.));
+          CK(launch_sa_source(z, ssiter, Z.drodm, Z.coe, coefH6, zero6, implicit && nstep == 1, s->st));
+          s->launches++;
         }
         cudaError_t e;
         {

@@ -21,15 +21,16 @@ namespace fgb {
 enum PI : int {
   NIJK = 0, NIJK_MTR = 5, NIJK_XYZ = 10, IJKV = 20, MXSSDOM_LU = 24, ITYPZONE = 25,
   IFLOW = 27, ILES = 28, ITYPCP = 29, SIZE_SSDOM = 30, KFLUDOM = 33, LALE = 34, NEQ = 36,
-  NEQ_IJ = 37, NEQ_K = 38, NEQ_COE = 39, NDIMDX = 41, NDIMDX_MTR = 43, DTLOC = 46,
+  NEQ_IJ = 37, NEQ_K = 38, NEQ_COE = 39, NDIMDX = 41, NDIMDX_MTR = 43, DTLOC = 46, SA_INT = 47,
   RK = 52, LEVEL = 53, EXPLOC = 54, NSSITER = 58, SLOPE = 64, PT_BC = 70, NB_RELAX = 71,
   LU_MATCH = 75, SENSORTYPE = 85
 };
 enum PR : int {
   DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6, MINF = 7,
-  PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14, VXINF = 19, VYINF = 20,
-  VZINF = 21, PSIROE = 34, WIG_AMP = 72
+  RONUTILDEINF = 8, PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14,
+  SA_RATIOM = 18, VXINF = 19, VYINF = 20, VZINF = 21, PSIROE = 34, PRANDT_TUR = 38, WIG_AMP = 72
 };
+enum PI_SA : int { SA_LOW_RE = 130, SA_ROT_CORR = 131 };
 enum ZoneType : int { Z3DFULL = 0, Z3DHOMO = 1, Z3DCART = 2, Z2D = 3 };
 enum Scheme : int { AUSM = 1, SENSEUR = 2, ROE = 5 };
 enum Slope : int { O1 = 1, O3 = 2, MINMOD = 3 };
@@ -54,7 +55,30 @@ struct Zone {
   double tcx, tcy, tcz, si, sj, sk, volinv;  // 3d cartesian metric
   double prandt, xmul0, temp0, cs;
   const double *ti, *tj, *tk, *vol;
+  // Spalart-Allmaras (IFLOW 3, neq 6): Sutherland constants in the form of
+  // the SA routines (coesut without sqrt(temp01)), turbulent conductivity,
+  // 1/sigma, the mu_t / mu clip, the rotation / low-Re switches and the wall
+  // distance (NDIMDX, natural layout)
+  double sa_coesut, sa_temp01, sa_cmus1, gam4, sigma_1, ratiom, sa_rot, sa_low_re;
+  const double* dist;
 };
+
+// Spalart-Allmaras constants (FastS/FastS/param_solver.h:315-327)
+#define SA_CKARM 0.41
+#define SA_CB1 0.1355
+#define SA_CB2 0.622
+#define SA_CV1 357.911
+#define SA_CW2 0.3
+#define SA_CW3 64.
+#define SA_CW4 0.21
+#define SA_CW5 1.5
+#define SA_SIGMA (2. / 3.)
+#define SA_CROT 2.0
+
+// mulam.for: laminar viscosity as the SA routines write it
+__device__ __forceinline__ double sa_mulam(const Zone& z, double t) {
+  return z.sa_coesut * sqrt(t * z.sa_temp01) / (1. + z.sa_cmus1 / t);
+}
 
 __host__ __device__ inline int64_t inddm(const Zone& z, int64_t i, int64_t j, int64_t k) {
   return (i + z.ng - 1) + (j + z.ng - 1) * z.nip + (k + z.ngk - 1) * z.nip * z.njp;

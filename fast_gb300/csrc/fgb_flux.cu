@@ -178,10 +178,12 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
 // AUSM/fluFaceEuler.for:36-57 + etat_GD.for + Vit_ent/fluvector_*.for.
 // NX = number of non-zero normal components the face can have (1: cartesian
 // face of direction D, 3: general).
-template <int D, bool CART, bool SENS = false>
-__device__ __forceinline__ void ausm_face(const Zone& z, const double qm[5], const double qp[5],
+// NV = 6: Spalart-Allmaras, the ro nutilde flux of AUSM/fluFaceSA.for with
+// the same interface velocity and dissipation.
+template <int D, bool CART, bool SENS = false, int NV = 5>
+__device__ __forceinline__ void ausm_face(const Zone& z, const double qm[NV], const double qp[NV],
                                           double tl, double tcx, double tcy, double tcz,
-                                          double s, double F[5], double wg = 0.) {
+                                          double s, double F[NV], double wg = 0.) {
   const double rgp = z.rgp, gam1 = z.gam1;
   double r1 = qp[0], rou1 = r1 * qp[1], rov1 = r1 * qp[2], row1 = r1 * qp[3];
   double p1 = r1 * qp[4] * rgp;
@@ -216,6 +218,10 @@ __device__ __forceinline__ void ausm_face(const Zone& z, const double qm[5], con
   F[2] = u * (rov1 + rov2) - tdu * (rov2 - rov1);
   F[3] = u * (row1 + row2) - tdu * (row2 - row1);
   F[4] = u * (h1 + h2) - tdu * (h2 - h1);
+  if (NV == 6) {
+    const double qm6 = qm[NV - 1] * qm[0], qp6 = qp[NV - 1] * qp[0];
+    F[NV - 1] = u * (qm6 + qp6) - tdu * (qm6 - qp6);
+  }
   if (CART) {
     const double tc = D == 0 ? tcx : (D == 1 ? tcy : tcz);
     F[D + 1] = F[D + 1] + tc * p1p2;
@@ -226,11 +232,39 @@ __device__ __forceinline__ void ausm_face(const Zone& z, const double qm[5], con
   }
 }
 
+// ------------------------------------------------- viscosity at a face
+// mut_interface.for (laminar: xmutvol = (mu_r + mu_l) volinv, xktvol =
+// xmutvol gam3) or, with Spalart-Allmaras, mut_prandtltb_interface.for
+// (laminar and turbulent conductivities apart) and SA/mut_interface.for
+// (xsa: diffusion coefficient of nutilde).
+template <int NV>
+__device__ __forceinline__ void mut_face(const Zone& z, const double* __restrict__ q,
+                                         const double* __restrict__ xmut, int64_t il, int64_t ir,
+                                         double volinv, double& xmutvol, double& xktvol,
+                                         double& xsa) {
+  if (NV == 6) {
+    const int64_t nd = z.nd;
+    double xmulam = sa_mulam(z, q[il + 4 * nd]);
+    xmulam = xmulam + sa_mulam(z, q[ir + 4 * nd]);
+    const double xmutot = xmut[ir] + xmut[il];
+    const double xmutur = xmutot - xmulam;
+    xktvol = (xmulam * z.gam3 + xmutur * z.gam4) * volinv;
+    xmutvol = xmutot * volinv;
+    const double x = xmulam + q[il + 5 * nd] * q[il] + q[ir + 5 * nd] * q[ir];
+    xsa = x * volinv * z.sigma_1;
+  } else {
+    xmutvol = (xmut[ir] + xmut[il]) * volinv;
+    xktvol = xmutvol * z.gam3;
+    xsa = 0.;
+  }
+}
+
 // ------------------------------------------------------ viscous (cart)
-// fluvisq_3dcart_{i,j,k}.for + mut_interface.for.  Face D of cell l.
-template <int D>
+// fluvisq_3dcart_{i,j,k}.for + mut_interface.for (SA: fluvisq_SA_3dcart_*,
+// nutilde diffusion).  Face D of cell l.
+template <int D, int NV = 5>
 __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restrict__ q,
-                                          const double* __restrict__ xmut, int64_t l, double F[5]) {
+                                          const double* __restrict__ xmut, int64_t l, double F[NV]) {
   const int64_t nd = z.nd;
   const double* U = q + nd;
   const double* V = q + 2 * nd;
@@ -262,8 +296,8 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     double gTx = (T[ir] - T[il]) * tix;
     double div = (gUx + gVy + gWz) * cvisq;
     double e1 = gUx - div, e2 = gUy + gVx, e3 = gUz + gWx;
-    double xmutvol = (xmut[ir] + xmut[il]) * z.volinv;
-    double xktvol = xmutvol * z.gam3;
+    double xmutvol, xktvol, xsa;
+    mut_face<NV>(z, q, xmut, il, ir, z.volinv, xmutvol, xktvol, xsa);
     fv = -(2. * e1 * tcx) * xmutvol;
     fv5 = fv * (U[ir] + U[il]);
     F[1] = F[1] + fv;
@@ -275,6 +309,10 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     F[3] = F[3] + fv;
     fv = fv5 * 0.5 - (gTx * tcx) * xktvol;
     F[4] = F[4] + fv;
+    if (NV == 6) {
+      const double gn = (q[ir + 5 * nd] - q[il + 5 * nd]) * tix;
+      F[NV - 1] = F[NV - 1] - xsa * gn * tcx;
+    }
   } else if (D == 1) {
     const double tiy = tcy, tjz = .25 * tcz, tkx = .25 * tcx;
     double f1 = U[il], f2 = U[ir], s = f1 + f2;
@@ -294,8 +332,8 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     double gTy = (T[ir] - T[il]) * tiy;
     double div = (gUx + gVy + gWz) * cvisq;
     double e2 = gUy + gVx, e4 = gVy - div, e5 = gVz + gWy;
-    double xmutvol = (xmut[ir] + xmut[il]) * z.volinv;
-    double xktvol = xmutvol * z.gam3;
+    double xmutvol, xktvol, xsa;
+    mut_face<NV>(z, q, xmut, il, ir, z.volinv, xmutvol, xktvol, xsa);
     fv = -(e2 * tcy) * xmutvol;
     fv5 = fv * (U[ir] + U[il]);
     F[1] = F[1] + fv;
@@ -307,6 +345,10 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     F[3] = F[3] + fv;
     fv = fv5 * 0.5 - (gTy * tcy) * xktvol;
     F[4] = F[4] + fv;
+    if (NV == 6) {
+      const double gn = (q[ir + 5 * nd] - q[il + 5 * nd]) * tiy;
+      F[NV - 1] = F[NV - 1] - xsa * (gn * tcy);
+    }
   } else {
     const double tiz = tcz, tky = 0.25 * tcy, tjx = 0.25 * tcx;
     double f1 = U[il], f2 = U[ir], s = f1 + f2;
@@ -326,8 +368,8 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     double gTz = (T[ir] - T[il]) * tiz;
     double div = (gUx + gVy + gWz) * cvisq;
     double e3 = gUz + gWx, e5 = gVz + gWy, e6 = gWz - div;
-    double xmutvol = (xmut[ir] + xmut[il]) * z.volinv;
-    double xktvol = xmutvol * z.gam3;
+    double xmutvol, xktvol, xsa;
+    mut_face<NV>(z, q, xmut, il, ir, z.volinv, xmutvol, xktvol, xsa);
     fv = -e3 * tcz * xmutvol;
     fv5 = fv * (U[ir] + U[il]);
     F[1] = F[1] + fv;
@@ -339,6 +381,10 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     F[3] = F[3] + fv;
     fv = fv5 * 0.5 - gTz * tcz * xktvol;
     F[4] = F[4] + fv;
+    if (NV == 6) {
+      const double gn = (q[ir + 5 * nd] - q[il + 5 * nd]) * tiz;
+      F[NV - 1] = F[NV - 1] - xsa * gn * tcz;
+    }
   }
 }
 
@@ -348,10 +394,10 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
 // ir = l, with the transverse directions A = D+1, B = D+2 (mod 3) -- the
 // three reference files are this routine for (D, A, B) = (i,j,k), (j,k,i),
 // (k,i,j).
-template <int D>
+template <int D, int NV = 5>
 __device__ __forceinline__ void visc_full(const Zone& z, const double* __restrict__ q,
                                           const double* __restrict__ xmut, int64_t l, int64_t lt,
-                                          double tcx, double tcy, double tcz, double F[5]) {
+                                          double tcx, double tcy, double tcz, double F[NV]) {
   constexpr int A = (D + 1) % 3, B = (D + 2) % 3;
   const int64_t nd = z.nd, ndm = z.ndm;
   const double* TD = D == 0 ? z.ti : (D == 1 ? z.tj : z.tk);
@@ -373,9 +419,10 @@ __device__ __forceinline__ void visc_full(const Zone& z, const double* __restric
     tb1[m] = .125 * (TB[ltB + o] + TB[ltBm + o]);
   }
   const int64_t il = l - z.inc[D], ir = l;
-  double g[4][3];
+  constexpr int NG = NV == 6 ? 5 : 4;   // u, v, w, T (, nutilde: fluvisq_SA_3dfull_*)
+  double g[NG][3];
 #pragma unroll
-  for (int v = 0; v < 4; v++) {
+  for (int v = 0; v < NG; v++) {
     const double* Q = q + (v + 1) * nd;
     const double f1 = Q[il], f2 = Q[ir];
     const double f3 = Q[ir] + Q[il] + Q[il - iA] + Q[ir - iA];
@@ -390,8 +437,8 @@ __device__ __forceinline__ void visc_full(const Zone& z, const double* __restric
   const double e1 = g[0][0] - div, e2 = g[0][1] + g[1][0], e3 = g[0][2] + g[2][0];
   const double e4 = g[1][1] - div, e5 = g[1][2] + g[2][1], e6 = g[2][2] - div;
   const double volinv = 1. / (z.vol[lt] + z.vol[ltm]);
-  const double xmutvol = (xmut[ir] + xmut[il]) * volinv;
-  const double xktvol = xmutvol * z.gam3;
+  double xmutvol, xktvol, xsa;
+  mut_face<NV>(z, q, xmut, il, ir, volinv, xmutvol, xktvol, xsa);
   double fv, fv5;
   fv = -(2. * e1 * tcx + e2 * tcy + e3 * tcz) * xmutvol;
   fv5 = fv * (q[ir + nd] + q[il + nd]);
@@ -404,12 +451,15 @@ __device__ __forceinline__ void visc_full(const Zone& z, const double* __restric
   F[3] = F[3] + fv;
   fv = fv5 * 0.5 - (g[3][0] * tcx + g[3][1] * tcy + g[3][2] * tcz) * xktvol;
   F[4] = F[4] + fv;
+  if (NV == 6)   // SA/assemble_tauij_3dfull.for
+    F[NV - 1] = F[NV - 1] - xsa * (g[NG - 1][0] * tcx + g[NG - 1][1] * tcy + g[NG - 1][2] * tcz);
 }
 
 // ------------------------------------------------------------- face kernel
 // One thread per face of direction D; faces of direction D are indexed
 // f = ii + NI*(jj + NJ*kk) over the interior face box (NI = ni+1 for D=0 ...).
-template <int D, int TYP, int KF, int SL, bool VISC>
+// NV = 6: Spalart-Allmaras (AUSM+(P) faces; nutilde takes the o3 slope).
+template <int D, int TYP, int KF, int SL, bool VISC, int NV = 5>
 __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restrict__ q,
                                                  const double* __restrict__ xmut,
                                                  double* __restrict__ Fo) {
@@ -423,11 +473,11 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
   const int64_t inc = z.inc[D];
   const int64_t nd = z.nd;
-  double qm[5], qp[5];
+  double qm[NV], qp[NV];
   double roff = 0.;
   if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
 #pragma unroll
-  for (int v = 0; v < 5; v++) {
+  for (int v = 0; v < NV; v++) {
     if (TYP == Z2D && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }   // 2-d: no w slope
     const double* Q = q + v * nd;
     double a = (SL == O1) ? 0. : Q[l - 2 * inc];
@@ -435,7 +485,7 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     double d = (SL == O1) ? 0. : Q[l + inc];
     reconstruct<SL>(z, a, b, c, d, roff, qm[v], qp[v]);
   }
-  double F[5];
+  double F[NV];
   if (TYP == Z2D) {
     // *_2d_{i,j}.for: the 3-d general face with tcz = 0 and w = 0 (the
     // w terms vanish exactly), w flux = 0
@@ -448,22 +498,22 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     F[3] = 0.;
   } else if (TYP == Z3DCART) {
     if (KF == ROE) roe_cart<D>(z, qm, qp, F);
-    else ausm_face<D, true, KF == SENSEUR>(z, qm, qp, q[l + 4 * nd], z.tcx, z.tcy, z.tcz,
-                                          D == 0 ? z.si : (D == 1 ? z.sj : z.sk), F,
-                                          KF == SENSEUR ? z.wig[l + D * nd] : 0.);
-    if (VISC) visc_cart<D>(z, q, xmut, l, F);
+    else ausm_face<D, true, KF == SENSEUR, NV>(z, qm, qp, q[l + 4 * nd], z.tcx, z.tcy, z.tcz,
+                                              D == 0 ? z.si : (D == 1 ? z.sj : z.sk), F,
+                                              KF == SENSEUR ? z.wig[l + D * nd] : 0.);
+    if (VISC) visc_cart<D, NV>(z, q, xmut, l, F);
   } else {
     const int64_t lt = indmtr(z, ii + 1, jj + 1, kk + 1);
     const double* t = D == 0 ? z.ti : (D == 1 ? z.tj : z.tk);
     double tcx = t[lt], tcy = t[lt + z.ndm], tcz = t[lt + 2 * z.ndm];
     double s = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
     if (KF == ROE) roe_full(z, qm, qp, tcx, tcy, tcz, s, F);
-    else ausm_face<D, false, KF == SENSEUR>(z, qm, qp, q[l + 4 * nd], tcx, tcy, tcz, s, F,
-                                           KF == SENSEUR ? z.wig[l + D * nd] : 0.);
-    if (VISC) visc_full<D>(z, q, xmut, l, lt, tcx, tcy, tcz, F);
+    else ausm_face<D, false, KF == SENSEUR, NV>(z, qm, qp, q[l + 4 * nd], tcx, tcy, tcz, s, F,
+                                               KF == SENSEUR ? z.wig[l + D * nd] : 0.);
+    if (VISC) visc_full<D, NV>(z, q, xmut, l, lt, tcx, tcy, tcz, F);
   }
 #pragma unroll
-  for (int v = 0; v < 5; v++) Fo[v * nf + f] = F[v];
+  for (int v = 0; v < NV; v++) Fo[v * nf + f] = F[v];
 }
 
 // --------------------------------------------------------- assemble+update
@@ -473,7 +523,11 @@ __device__ __forceinline__ double roe_of(double cv, double r, double u, double v
   return r * (cv * t + 0.5 * (u * u + v * v + w * w));
 }
 
-template <bool IMPL>
+// NV = 6 (Spalart-Allmaras): the ro nutilde balance starts from drodm(:,6),
+// which sa_source has initialised and given the source term; the updates
+// are core3ark3.for's nutilde branch (clipped to [0, ratiom nu_lam]) and
+// core3as2.for's sixth residual.
+template <bool IMPL, int NV = 5>
 __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
   const int64_t n = z.ni * z.nj * z.nk;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -488,15 +542,15 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
   const int64_t ai = ii + (z.ni + 1) * (jj + z.nj * kk);
   const int64_t aj = ii + z.ni * (jj + (z.nj + 1) * kk);
   const int64_t ak = ii + z.ni * (jj + z.nj * kk);
-  double x[5];
+  double x[NV];
   if (a.mode == 2) {  // balance already in drodm (corrected by wall_corr)
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = a.drodm[l + v * nd];
   } else {
 #pragma unroll
     const bool two_d = z.typ == Z2D;   // no k faces
-    for (int v = 0; v < 5; v++) {
-      double s = a.zero_init ? 0. : a.drodm[l + v * nd] * a.coefH;
+    for (int v = 0; v < NV; v++) {
+      double s = v == 5 ? a.drodm[l + v * nd] : (a.zero_init ? 0. : a.drodm[l + v * nd] * a.coefH);
       if (!two_d) s = s + a.Fk[v * nfk + ak];
       s = s + a.Fj[v * nfj + aj];
       s = s + a.Fi[v * nfi + ai];
@@ -514,7 +568,7 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
   const double cv = z.cv;
   if (!IMPL) {
 #pragma unroll
-    for (int v = 0; v < 5; v++) a.drodm[l + v * nd] = x[v];
+    for (int v = 0; v < NV; v++) a.drodm[l + v * nd] = x[v];
     // core3ark3.for:99-125
     const double* R = a.rop_in;
     double r_1 = a.coefW * a.coe[l];
@@ -538,6 +592,14 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
     }
     double* O = a.rop_out;
     O[l] = n1; O[l + nd] = n2; O[l + 2 * nd] = n3; O[l + 3 * nd] = n4; O[l + 4 * nd] = n5;
+    if (NV == 6) {   // core3ark3.for:188-236
+      const double tab6 = x[NV - 1] * r_1;
+      double anulam = sa_mulam(z, n5);
+      anulam = anulam * rr * z.ratiom;
+      double t6 = (ro * R[l + 5 * nd] + tab6) * rr;
+      t6 = fminF(t6, anulam);
+      O[l + 5 * nd] = fmaxF(t6, 0.);
+    }
   } else {
     // core3as2.for:233-330 (5 equations, 3d)
     const double* P = a.rop_in;   // W^p (rop_ssiter)
@@ -546,7 +608,7 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
     const double cf = a.coe[l];
     double pr_ = P[l], pu = P[l + nd], pv = P[l + 2 * nd], pw = P[l + 3 * nd], pt = P[l + 4 * nd];
     double mr = M[l], mu = M[l + nd], mv = M[l + 2 * nd], mw = M[l + 3 * nd], mt = M[l + 4 * nd];
-    double y[5];
+    double y[NV];
     if (a.first_sub) {
       double c4 = a.c1 + a.c2;
       y[0] = cf * x[0] + c4 * pr_ + a.c3 * mr;
@@ -556,6 +618,8 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
       double roe = roe_of(cv, pr_, pu, pv, pw, pt);
       double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
       y[4] = cf * x[4] + c4 * roe + a.c3 * roe1;
+      if (NV == 6)   // core3as2.for:97-99
+        y[NV - 1] = cf * x[NV - 1] + c4 * P[l + 5 * nd] * pr_ + a.c3 * M[l + 5 * nd] * mr;
     } else {
       double nr = N[l], nu = N[l + nd], nv = N[l + 2 * nd], nw = N[l + 3 * nd], nt = N[l + 4 * nd];
       y[0] = cf * x[0] + a.c1 * pr_ + a.c2 * nr + a.c3 * mr;
@@ -566,31 +630,164 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
       double roen = roe_of(cv, nr, nu, nv, nw, nt);
       double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
       y[4] = cf * x[4] + a.c1 * roe + a.c2 * roen + a.c3 * roe1;
+      if (NV == 6)   // core3as2.for:187-190
+        y[NV - 1] = cf * x[NV - 1] + a.c1 * P[l + 5 * nd] * pr_ + a.c2 * N[l + 5 * nd] * nr +
+                    a.c3 * M[l + 5 * nd] * mr;
     }
     // core3as2.for 2-d branch: the w residual is left as the balance, and
     // the energies have no w term (w = 0 in a 2-d state: the same values)
     if (z.typ == Z2D) y[3] = x[3];
 #pragma unroll
-    for (int v = 0; v < 5; v++) a.drodm[l + v * nd] = y[v];
+    for (int v = 0; v < NV; v++) a.drodm[l + v * nd] = y[v];
   }
+}
+
+// -------------------------------------------------- Spalart-Allmaras source
+// SA/spsource_SA.for with sourceSA_grad_3dcart.for / sourceSA_grad_3d.for,
+// sourceSA_prod_dest.for and sourceSA_LU.for, fused with init_rhs.for for
+// the sixth equation: drodm(l,6) = init + vol * (production + cross
+// diffusion - destruction); on the first implicit sub-step also
+// coe(l,6) = coe(l,5) - min(d source / d(ro nutilde), 0) coe(l,1).  One
+// thread per interior cell (the reference's first ghost ring is never read).
+template <int TYP>
+__global__ void __launch_bounds__(256) sa_source(Zone z, const double* __restrict__ q,
+                                                 double* __restrict__ drodm, double* __restrict__ coe,
+                                                 double coefH, int zero_init, int lu) {
+  const int64_t n = z.ni * z.nj * z.nk;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int64_t ii = t % z.ni, r0 = t / z.ni, jj = r0 % z.nj, kk = r0 / z.nj;
+  const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
+  const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
+  const int64_t nd = z.nd, ndm = z.ndm;
+  const int64_t l1 = l + 1, l2 = l - 1, l3 = l + z.inc[1], l4 = l - z.inc[1], l5 = l + z.inc[2],
+                l6 = l - z.inc[2];
+  const double* Rr = q;
+  const double* Nu = q + 5 * nd;
+  const double vol = z.vol[lt];
+  const double xvol = 0.5 / vol;
+  double g[3][3], gn[3], gr[3];
+  if (TYP == Z3DCART) {   // sourceSA_grad_3dcart.for
+    const double tix = z.ti[0], tjy = z.tj[0], tkz = z.tk[0];
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const double* Q = v < 3 ? q + (v + 1) * nd : Nu;
+      const double u1 = (Q[l] + Q[l2]), u2 = (Q[l] + Q[l3]), u3 = (Q[l] + Q[l1]);
+      const double u4 = (Q[l] + Q[l4]), u5 = (Q[l] + Q[l5]), u6 = (Q[l] + Q[l6]);
+      double* o = v < 3 ? g[v] : gn;
+      o[0] = (u3 - u1) * tix;
+      o[1] = (u2 - u4) * tjy;
+      o[2] = (u5 - u6) * tkz;
+    }
+    const double a = Nu[l] * Rr[l];
+    const double u1 = a + Nu[l2] * Rr[l2], u2 = a + Nu[l3] * Rr[l3], u3 = a + Nu[l1] * Rr[l1];
+    const double u4 = a + Nu[l4] * Rr[l4], u5 = a + Nu[l5] * Rr[l5], u6 = a + Nu[l6] * Rr[l6];
+    gr[0] = (u3 - u1) * tix;
+    gr[1] = (u2 - u4) * tjy;
+    gr[2] = (u5 - u6) * tkz;
+  } else {                // sourceSA_grad_3d.for
+    const double* TT[3] = {z.ti, z.tj, z.tk};
+    double t0[3][3], t1[3][3];   // [component][face family]: faces lt and lt + inc_d
+#pragma unroll
+    for (int x = 0; x < 3; x++)
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        t0[x][d] = TT[d][lt + x * ndm];
+        t1[x][d] = TT[d][lt + z.minc[d] + x * ndm];
+      }
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const double* Q = v < 3 ? q + (v + 1) * nd : Nu;
+      const double u1 = (Q[l] + Q[l2]), u2 = (Q[l] + Q[l3]), u3 = (Q[l] + Q[l1]);
+      const double u4 = (Q[l] + Q[l4]), u5 = (Q[l] + Q[l5]), u6 = (Q[l] + Q[l6]);
+      double* o = v < 3 ? g[v] : gn;
+#pragma unroll
+      for (int x = 0; x < 3; x++)
+        o[x] = (u3 * t1[x][0] - u1 * t0[x][0] + u2 * t1[x][1] - u4 * t0[x][1] +
+                u5 * t1[x][2] - u6 * t0[x][2]);
+    }
+    const double a = Nu[l] * Rr[l];
+    const double u1 = a + Nu[l2] * Rr[l2], u2 = a + Nu[l3] * Rr[l3], u3 = a + Nu[l1] * Rr[l1];
+    const double u4 = a + Nu[l4] * Rr[l4], u5 = a + Nu[l5] * Rr[l5], u6 = a + Nu[l6] * Rr[l6];
+#pragma unroll
+    for (int x = 0; x < 3; x++)
+      gr[x] = (u3 * t1[x][0] - u1 * t0[x][0] + u2 * t1[x][1] - u4 * t0[x][1] +
+               u5 * t1[x][2] - u6 * t0[x][2]);
+  }
+  // vorticity and strain magnitudes
+  const double rotx = g[2][1] - g[1][2], roty = g[0][2] - g[2][0], rotz = g[1][0] - g[0][1];
+  const double rot = sqrt(rotx * rotx + roty * roty + rotz * rotz) * xvol;
+  const double S11 = g[0][0], S22 = g[1][1], S33 = g[2][2];
+  const double S12 = 0.5 * (g[0][1] + g[1][0]), S13 = 0.5 * (g[0][2] + g[2][0]),
+               S23 = 0.5 * (g[1][2] + g[2][1]);
+  double St = S11 * S11 + S22 * S22 + S33 * S33 + 2. * (S12 * S12) + 2. * (S13 * S13) +
+              2. * (S23 * S23);
+  St = sqrt(2. * St) * xvol;
+  const double c1 = SA_CB2 / SA_SIGMA;
+  const double cw1 = (SA_CB1 / SA_CKARM / SA_CKARM) + (1. + SA_CB2) / SA_SIGMA;
+  const double anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1] + gn[2] * gr[2]) * xvol * xvol;
+  // mulam.for, SA/chi.for
+  const double amulam = sa_mulam(z, q[l + 4 * nd]);
+  const double anulam = Rr[l] / amulam;
+  const double anutild = fmaxF(Nu[l], 1.e-27);
+  const double chi = fmaxF(anutild * anulam, 1.e-7);
+  // sourceSA_prod_dest.for
+  const double f1 = 1. / (1. + SA_CV1 / (chi * chi * chi));
+  const double f2 = 1. - chi / (1. + chi * f1);
+  const double dist = fmaxF(z.dist[l], 1.e-27);
+  double stild = rot + (anutild * f2) / (SA_CKARM * SA_CKARM * dist * dist);
+  stild = stild + z.sa_rot * SA_CROT * fminF(0.00000000000000000001, St - rot);
+  const double prod = Rr[l] * SA_CB1 * stild * anutild;
+  stild = fmaxF(stild, 0.00000000000000000001);
+  double rr = anutild / (stild * SA_CKARM * SA_CKARM * dist * dist);
+  rr = fminF(rr, 10.);
+  const double r5 = rr * rr * rr * rr * rr - 1.;
+  double gg = rr * (1. + SA_CW2 * r5);
+  const double lre = 1. + chi / 40.;
+  const double cw2_lre = SA_CW4 + SA_CW5 / (lre * lre);
+  gg = z.sa_low_re * rr * (1. + cw2_lre * r5) + (1. - z.sa_low_re) * gg;
+  const double g3 = gg * gg * gg, g6 = g3 * g3;   // g**6 as the Fortran compiler expands it
+  const double fwg = gg * pow((1. + SA_CW3) / (g6 + SA_CW3), 1. / 6.);
+  const double destruc = Rr[l] * cw1 * fwg * (anutild / dist) * (anutild / dist);
+  const double tsource = (prod + anvisc - destruc);
+  if (lu) {   // sourceSA_LU.for
+    const double tsourceb = prod - destruc;
+    double amutild = anutild * Rr[l];
+    amutild = fmaxF(amutild, 0.0000000000000001);
+    const double tsourcenu = vol * tsourceb / amutild;
+    coe[l + 5 * nd] = coe[l + 4 * nd] - fminF(tsourcenu, 0.) * coe[l];
+  }
+  const double init = zero_init ? 0. : drodm[l + 5 * nd] * coefH;
+  drodm[l + 5 * nd] = init + vol * tsource;
+}
+
+cudaError_t launch_sa_source(const Zone& z, const double* q, double* drodm, double* coe,
+                             double coefH, int zero_init, int lu, cudaStream_t st) {
+  const int B = 256;
+  const int64_t n = z.ni * z.nj * z.nk;
+  const unsigned g = (unsigned)((n + B - 1) / B);
+  if (z.typ == Z3DCART) sa_source<Z3DCART><<<g, B, 0, st>>>(z, q, drodm, coe, coefH, zero_init, lu);
+  else if (z.typ == Z3DFULL) sa_source<Z3DFULL><<<g, B, 0, st>>>(z, q, drodm, coe, coefH, zero_init, lu);
+  else return cudaErrorNotSupported;
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------ host glue
 #define FGB_CHECK_LAUNCH() \
   do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) return e_; } while (0)
 
-template <int TYP, int KF, int SL, bool VISC>
+template <int TYP, int KF, int SL, bool VISC, int NV = 5>
 static cudaError_t launch_faces_t(const Zone& z, const double* q, const double* xmut, double* Fi,
                                   double* Fj, double* Fk, cudaStream_t st) {
   const int B = 128;
   int64_t nfi = (z.ni + 1) * z.nj * z.nk, nfj = z.ni * (z.nj + 1) * z.nk,
           nfk = z.ni * z.nj * (z.nk + 1);
-  face_flux<0, TYP, KF, SL, VISC><<<(unsigned)((nfi + B - 1) / B), B, 0, st>>>(z, q, xmut, Fi);
+  face_flux<0, TYP, KF, SL, VISC, NV><<<(unsigned)((nfi + B - 1) / B), B, 0, st>>>(z, q, xmut, Fi);
   FGB_CHECK_LAUNCH();
-  face_flux<1, TYP, KF, SL, VISC><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, xmut, Fj);
+  face_flux<1, TYP, KF, SL, VISC, NV><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, xmut, Fj);
   FGB_CHECK_LAUNCH();
   if (TYP != Z2D) {
-    face_flux<2, TYP, KF, SL, VISC><<<(unsigned)((nfk + B - 1) / B), B, 0, st>>>(z, q, xmut, Fk);
+    face_flux<2, TYP, KF, SL, VISC, NV><<<(unsigned)((nfk + B - 1) / B), B, 0, st>>>(z, q, xmut, Fk);
     FGB_CHECK_LAUNCH();
   }
   return cudaSuccess;
@@ -602,6 +799,12 @@ static cudaError_t launch_faces_t(const Zone& z, const double* q, const double* 
 cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
                          double* Fj, double* Fk, cudaStream_t st) {
   const bool visc = z.iflow >= 2;
+  if (z.neq == 6) {   // Spalart-Allmaras: AUSM+(P) o3, 3d zones
+    if (z.kflu != AUSM || z.slope != O3) return cudaErrorNotSupported;
+    if (z.typ == Z3DCART) return launch_faces_t<Z3DCART, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.typ == Z3DFULL) return launch_faces_t<Z3DFULL, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    return cudaErrorNotSupported;
+  }
   if (z.typ == Z3DCART) {
     if (z.kflu == ROE) {
       if (z.slope == O1) return visc ? launch_faces_t<Z3DCART, ROE, O1, true>(z, q, xmut, Fi, Fj, Fk, st)
@@ -787,8 +990,15 @@ cudaError_t launch_wiggle(const Zone& z, const double* q, double* wig, cudaStrea
 cudaError_t launch_assemble(const Zone& z, const StageArgs& a, bool implicit, cudaStream_t st) {
   const int B = 256;
   int64_t n = z.ni * z.nj * z.nk;
-  if (implicit) assemble<true><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a);
-  else assemble<false><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, a);
+  const unsigned g = (unsigned)((n + B - 1) / B);
+  if (z.neq == 6) {
+    if (a.mode != 0) return cudaErrorNotSupported;
+    if (implicit) assemble<true, 6><<<g, B, 0, st>>>(z, a);
+    else assemble<false, 6><<<g, B, 0, st>>>(z, a);
+  } else {
+    if (implicit) assemble<true><<<g, B, 0, st>>>(z, a);
+    else assemble<false><<<g, B, 0, st>>>(z, a);
+  }
   return cudaGetLastError();
 }
 

@@ -146,11 +146,13 @@ __global__ void __launch_bounds__(128) bc_face(double* __restrict__ q, BcFaceArg
     q[l] = q[s];
     q[l + nd] = 0. + ua; q[l + 2 * nd] = 0. + va; q[l + 3 * nd] = 0. + wa;
     q[l + 4 * nd] = q[s + 4 * nd];
+    if (a.sa) q[l + 5 * nd] = q[s + 5 * nd];          // BCWallInviscidSA_*.for
   } else if (a.op == BCF_NOSLIP) {
     const double u = q[s + nd], v = q[s + 2 * nd], w = q[s + 3 * nd];
     q[l] = q[s];
     q[l + nd] = 0. - u; q[l + 2 * nd] = 0. - v; q[l + 3 * nd] = 0. - w;
     q[l + 4 * nd] = q[s + 4 * nd];
+    if (a.sa) q[l + 5 * nd] = -q[s + 5 * nd];         // BCWallViscous_SA.for
   } else if (a.op == BCF_FARFIELD) {
     NrOut o;
     non_reflection(a, q, s, t, a.st, o);
@@ -160,6 +162,8 @@ __global__ void __launch_bounds__(128) bc_face(double* __restrict__ q, BcFaceArg
     q[l] = o.svar[0];
     q[l + nd] = u; q[l + 2 * nd] = v; q[l + 3 * nd] = w;
     q[l + 4 * nd] = (o.qvar5 * roinv - .5 * (u * u + v * v + w * w)) * a.cvinv;
+    // BCFarfield_firstrank_SA.for (inflow for eigv1 = qn < 0) / BCInflow_firstrank_SA.for
+    if (a.sa) q[l + 5 * nd] = (a.inflow || o.qn < 0.) ? a.nue : q[s + 5 * nd];
   } else {  // BCF_OUTFLOW
     const double roe = q[s], rue = q[s + nd] * roe, rve = q[s + 2 * nd] * roe, rwe = q[s + 3 * nd] * roe;
     const double roe_inv = 1. / a.st[0];
@@ -177,23 +181,26 @@ __global__ void __launch_bounds__(128) bc_face(double* __restrict__ q, BcFaceArg
 #pragma unroll
     for (int m = 0; m < 3; m++) q[l + (m + 1) * nd] = vel[m];
     q[l + 4 * nd] = (o.qvar5 * roinv - .5 * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2])) * a.cvinv;
+    if (a.sa) q[l + 5 * nd] = q[s + 5 * nd];          // BCOutflow_firstrank_SA.for
   }
 }
 
 // BC/BC_nextrank.for: ghost ranks beyond the first of farfield / inflow BCs,
 // from the first ghost (q0) and the first two interior cells (q1, q2).
+// BC_nextrankSA.for (six variables) keeps the first ghost when the
+// extrapolated density falls to 0.3 of it instead.
 __global__ void __launch_bounds__(128) bc_next(double* __restrict__ q, BcNextArgs a) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
   const int64_t nd = a.nd, l = a.dst[e], q0 = a.q0[e], q1 = a.q1[e], q2 = a.q2[e];
+  const int nv = a.sa ? 6 : 5;
   const double r = q[q0] * a.k3 + q[q1] * a.k1 + q[q2] * a.k2;
-  if (fabs(r / q[q0] - 1.) >= 0.7) {
-#pragma unroll
-    for (int v = 0; v < 5; v++) q[l + v * nd] = q[q0 + v * nd];
+  const bool keep = a.sa ? r <= 0.3 * q[q0] : fabs(r / q[q0] - 1.) >= 0.7;
+  if (keep) {
+    for (int v = 0; v < nv; v++) q[l + v * nd] = q[q0 + v * nd];
   } else {
     q[l] = r;
-#pragma unroll
-    for (int v = 1; v < 5; v++) q[l + v * nd] = q[q0 + v * nd] * a.k3 + q[q1 + v * nd] * a.k1 + q[q2 + v * nd] * a.k2;
+    for (int v = 1; v < nv; v++) q[l + v * nd] = q[q0 + v * nd] * a.k3 + q[q1 + v * nd] * a.k1 + q[q2 + v * nd] * a.k2;
   }
 }
 

@@ -35,12 +35,17 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
                          double* Fj, double* Fk, cudaStream_t st);
 cudaError_t launch_wiggle(const Zone& z, const double* q, double* wig, cudaStream_t st);
 cudaError_t launch_assemble(const Zone& z, const StageArgs& a, bool implicit, cudaStream_t st);
+// Spalart-Allmaras source of the sub-step (init_rhs of equation 6 fused in);
+// lu: also coe(:,6) for the LU-SGS sweeps (first implicit sub-step)
+cudaError_t launch_sa_source(const Zone& z, const double* q, double* drodm, double* coe,
+                             double coefH, int zero_init, int lu, cudaStream_t st);
 
 // fgb_lu.cu: coefficients and LU-SGS
 struct CoeArgs {
   const double* rop; const double* xmut_in; double* xmut; double* coe;
   int64_t lo[3], hi[3];      // Fortran index range (may include ghosts)
   int do_invist, do_lu, first_it;
+  int do_sa;                 // SA/vispalart.for instead of invist.for
   double coesut, cmus1;      // invist.for constants
 };
 struct LuArgs {
@@ -98,11 +103,14 @@ struct BcFaceArgs {            // one face BC window (bc_face)
   int op;
   double gam, gam1, gam1_1, cv, cvinv;
   double st[5];                // exterior state (conservative)
+  int sa, inflow;              // Spalart-Allmaras zone; BCInflow (nutilde imposed)
+  double nue;                  // exterior nutilde (state(6) / state(1))
 };
 struct BcNextArgs {            // farfield / inflow ghost ranks past the first
   const int32_t *dst, *q0, *q1, *q2;
   int64_t n, nd;
   double k1, k2, k3;
+  int sa;
 };
 cudaError_t launch_bc_face(double* q, const BcFaceArgs& a, cudaStream_t st);
 cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st);

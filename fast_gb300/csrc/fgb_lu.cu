@@ -30,7 +30,17 @@ __global__ void __launch_bounds__(256) coefficients(Zone z, CoeArgs a) {
   const int64_t nd = z.nd;
   const double* R = a.rop;
   double xm = 0.;
-  if (a.do_invist) {  // invist.for:33-35
+  if (a.do_sa) {      // SA/vispalart.for with mulam.for, chi.for, xmut.for
+    const double amulam = sa_mulam(z, R[l + 4 * nd]);
+    const double anulam = R[l] / amulam;
+    const double anutild = fmaxF(R[l + 5 * nd], 1.e-27);
+    const double chi = fmaxF(anutild * anulam, 1.e-7);
+    const double fvv1 = 1. / (1. + SA_CV1 / (chi * chi * chi));
+    const double amut = R[l] * anutild * fvv1;
+    const double xmuprov = fmaxF(amut, 0.);
+    xm = amulam + fminF(xmuprov, z.ratiom * amulam);
+    a.xmut[l] = xm;
+  } else if (a.do_invist) {  // invist.for:33-35
     double t1 = R[l + 4 * nd];
     xm = a.coesut * sqrt(t1) * t1 / (t1 + a.cmus1);
     a.xmut[l] = xm;
@@ -230,6 +240,7 @@ template <typename T> __device__ __forceinline__ T ldcg(const T* p) { return __l
 // adds coe_{d+2}(nb)*signe exactly as the reference expression does.
 constexpr int NB_CART = 14;   // entries per direction, 3d cartesian zone
 constexpr int NB_FULL = 25;   // entries per direction, 3d general zone
+constexpr int QN_FULL = 23;   // general layout: qn (entries 0..22 are the B matrix)
 template <int TYP> struct NBE { static constexpr int n = TYP == Z3DCART ? NB_CART : NB_FULL; };
 // 2-d zones use the general entries with tz = 0 and w = 0 (lu_{i,j}_2d.for
 // is lu_{i,j}_3dfull.for without the w / tz terms, which vanish exactly)
@@ -274,7 +285,16 @@ __device__ __forceinline__ void bentries(const Zone& z, int d, T u, T v, T w, T 
     e[15] = (tcy * w - tcz * gamm1 * v); e[16] = (qn - tcz * gam2 * w); e[17] = tcz * gamm1;
     e[18] = qn * (ph2 - h); e[19] = (tcx * h - gamm1 * u * qn);
     e[20] = (tcy * h - gamm1 * v * qn); e[21] = (tcz * h - gamm1 * w * qn); e[22] = (gam1 * qn);
+    e[QN_FULL] = qn;   // read by the Spalart-Allmaras row only
   }
+}
+
+// the normal velocity qn of the entries of direction D (the B_66 entry of
+// the Spalart-Allmaras row is qn + cs, LU/lu_*_SA.for)
+template <int TYP, int D, typename T>
+__device__ __forceinline__ T qn_entry(const T* e) {
+  if (TYP == Z3DCART) return D == 0 ? e[6] : e[1];
+  return e[QN_FULL];
 }
 
 // b = B . o from the stored entries (cs = coe_{d+2}(nb) * signe)
@@ -329,8 +349,8 @@ template <int D> struct DirT { static constexpr int value = D; };
 // consecutive cells of a plane, and on their neighbours in the previous
 // plane, then reads a few contiguous spans instead of one scattered word per
 // array (which thrashed the TLB and sector caches).
-//   rec[g] : coe1, 1/coe5, coe5, -, coe_{2..4}, W^p (5), B entries (3 x NB)
-//   dio[g] : residual in / increment out (5 words, stride 6)
+//   rec[g] : coe1, 1/coe5, coe5, coe6 (SA), coe_{2..4}, W^p (5), B entries (3 x NB)
+//   dio[g] : residual in / increment out (5 words, 6 with SA, stride 6)
 //   nst[g] : in-place upper sweep: W^{p+1} u, v, w, T (stride 4)
 template <int TYP, typename T> struct Rec {
   // FP32 sweeps in cartesian zones rebuild B from the neighbour's state
@@ -338,7 +358,7 @@ template <int TYP, typename T> struct Rec {
   // float inputs as the pre-pass, so the same values, in 12 words a cell.
   static constexpr bool HAS_B = !(TYP == Z3DCART && sizeof(T) == 4);
   static constexpr int NB = NBE<TYP>::n;
-  static constexpr int COE1 = 0, DIAG = 1, COE5 = 2, COEN = 4, ST = 7, B = 12;
+  static constexpr int COE1 = 0, DIAG = 1, COE5 = 2, COE6 = 3, COEN = 4, ST = 7, B = 12;
   static constexpr int SIZE = HAS_B ? ((B + 3 * NB) + 3) / 4 * 4 : B;   // whole 16-byte vectors
 };
 constexpr int DIO = 6;
@@ -402,13 +422,17 @@ __device__ __forceinline__ void store_rec(float* dst, const float (&r)[N]) {
 #pragma unroll
   for (int m = 0; m < N / 4; m++) d[m] = make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
 }
-__device__ __forceinline__ void store_dio(double* dst, const double (&x)[5]) {
+template <int NV>
+__device__ __forceinline__ void store_dio(double* dst, const double (&x)[NV]) {
   double2* d = reinterpret_cast<double2*>(dst);   // DIO = 6 words: 48-byte slots
-  d[0] = make_double2(x[0], x[1]); d[1] = make_double2(x[2], x[3]); d[2] = make_double2(x[4], 0.);
+  d[0] = make_double2(x[0], x[1]); d[1] = make_double2(x[2], x[3]);
+  d[2] = make_double2(x[4], NV == 6 ? x[NV - 1] : 0.);
 }
-__device__ __forceinline__ void store_dio(float* dst, const float (&x)[5]) {
+template <int NV>
+__device__ __forceinline__ void store_dio(float* dst, const float (&x)[NV]) {
   float2* d = reinterpret_cast<float2*>(dst);     // 24-byte slots
-  d[0] = make_float2(x[0], x[1]); d[1] = make_float2(x[2], x[3]); d[2] = make_float2(x[4], 0.f);
+  d[0] = make_float2(x[0], x[1]); d[1] = make_float2(x[2], x[3]);
+  d[2] = make_float2(x[4], NV == 6 ? x[NV - 1] : 0.f);
 }
 
 // Per-solve gather into plane-ordered records + B entries (fully parallel).
@@ -439,7 +463,7 @@ template <typename T> struct Vec2;
 template <> struct Vec2<double> { using t = double2; };
 template <> struct Vec2<float> { using t = float2; };
 
-template <int TYP, typename T>
+template <int TYP, typename T, int NV>
 __global__ void __launch_bounds__(GT_N) lu_gather(Zone z, LuFields f, PlaneData<T> p) {
   using R = Rec<TYP, T>;
   using S = GatherSmem<TYP, T>;
@@ -455,15 +479,15 @@ __global__ void __launch_bounds__(GT_N) lu_gather(Zone z, LuFields f, PlaneData<
     const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
     const int64_t lt = TYP == Z3DCART ? 0 : indmtr(z, ii + 1, jj + 1, kk + 1);
     const int64_t nd = z.nd;
-    T x[5];
+    T x[NV];
 #pragma unroll
-    for (int v = 0; v < 5; v++) x[v] = T(f.din[l + v * nd]);
+    for (int v = 0; v < NV; v++) x[v] = T(f.din[l + v * nd]);
     T r[R::SIZE];
     const T c5 = T(f.coe[l + 4 * nd]);
     r[R::COE1] = T(f.coe[l]);
     r[R::DIAG] = T(1.) / c5;
     r[R::COE5] = c5;
-    r[3] = T(0);
+    r[R::COE6] = NV == 6 ? T(f.coe[l + 5 * nd]) : T(0);
 #pragma unroll
     for (int d = 0; d < 3; d++) r[R::COEN + d] = T(f.coe[l + (d + 1) * nd]);
 #pragma unroll
@@ -506,11 +530,22 @@ __global__ void __launch_bounds__(GT_N) lu_gather(Zone z, LuFields f, PlaneData<
 // ---------------------------------------------------------------- cells
 // Precision T: double for the plain FP64 path; float for the mixed path
 // (FP32 sweeps and approximate Jacobians; the Newton update stays FP64).
-template <typename T>
-__device__ __forceinline__ void load_dio(const T* __restrict__ dio, int64_t g, T o[5]) {
+template <int NV, typename T>
+__device__ __forceinline__ void load_dio(const T* __restrict__ dio, int64_t g, T o[NV]) {
   const T* q = dio + g * DIO;
 #pragma unroll
-  for (int v = 0; v < 5; v++) o[v] = __ldcg(q + v);
+  for (int v = 0; v < NV; v++) o[v] = __ldcg(q + v);
+}
+
+// mjr_newton_SA.for: ro nutilde updated, nutilde clipped to
+// [0, ratiom nu_lam(T^{p+1})]; r_1 = 1 / ro^{p+1}, t_new = T^{p+1}
+__device__ __forceinline__ double newton_sa(const Zone& z, double ro_old, double nu_old, double d6,
+                                            double r_1, double t_new) {
+  double anulam = sa_mulam(z, t_new);
+  anulam = anulam * r_1 * z.ratiom;
+  double t6 = (ro_old * nu_old + d6) * r_1;
+  t6 = fminF(t6, anulam);
+  return fmaxF(t6, 0.);
 }
 
 // mjr_newton.for: W^{p+1} = prim(cons(W^p) + dW) in precision T; cvinv =
@@ -541,31 +576,34 @@ __device__ __forceinline__ void newton(T cv, T cvinv, T ro, T u, T v, T w, T tt,
 // the grid barrier and waiting on it, so only the increments' loads stay
 // between two hyperplanes; without a stored B table (FP32, cartesian) the
 // neighbours' states are held instead (3 x 4 values).
-template <int TYP, typename T>
+template <int TYP, typename T, int NV = 5>
 struct CellOps {
   static constexpr bool HOLD_W = !Rec<TYP, T>::HAS_B;
   static constexpr int NW = HOLD_W ? 4 : 1;
   int32_t n[3];   // neighbour plane indices (-1: none)
-  T x[5];         // lower: residual; upper: lower result x coe5 (lu_d.for)
+  T x[NV];        // lower: residual; upper: lower result x coe5 (lu_d.for; x coe6 for SA)
   T xal, diag;
+  T c6;           // SA: coe6 of the cell (its sixth diagonal, divided by)
   T cs[3];        // coe_{d+2}(neighbour) x (+-1/2)
   T wn[3][NW];    // neighbours' u, v, w, T (no stored B table)
   T st[5];        // upper: W^p of the cell (in-place Newton)
 };
 
-template <int TYP, typename T, bool UPPER>
+template <int TYP, typename T, bool UPPER, int NV>
 __device__ __forceinline__ void load_ops(const PlaneData<T>& p, bool inplace, int64_t g,
-                                         CellOps<TYP, T>& o) {
+                                         CellOps<TYP, T, NV>& o) {
   using R = Rec<TYP, T>;
   const T* me = p.rec + g * R::SIZE;
   const int32_t* nbt = UPPER ? p.nbu : p.nbl;
 #pragma unroll
   for (int d = 0; d < 3; d++) o.n[d] = nbt[d * p.G + g];
-  load_dio(p.dio, g, o.x);
+  load_dio<NV>(p.dio, g, o.x);
+  if (NV == 6) o.c6 = me[R::COE6];
   if (UPPER) {
     const T dg = me[R::COE5];
 #pragma unroll
     for (int v = 0; v < 5; v++) o.x[v] = o.x[v] * dg;
+    if (NV == 6) o.x[NV - 1] = o.x[NV - 1] * o.c6;   // lu_d_SA.for
     o.xal = me[R::COE1] * T(-0.5);
 #pragma unroll
     for (int v = 0; v < 5; v++) o.st[v] = me[R::ST + v];
@@ -578,9 +616,9 @@ __device__ __forceinline__ void load_ops(const PlaneData<T>& p, bool inplace, in
     if (o.n[d] < 0) continue;
     const T* rn = p.rec + (int64_t)o.n[d] * R::SIZE;
     o.cs[d] = rn[R::COEN + d] * T(UPPER ? -0.5 : 0.5);
-    if (CellOps<TYP, T>::HOLD_W && !(UPPER && d == 2 && inplace)) {
+    if (CellOps<TYP, T, NV>::HOLD_W && !(UPPER && d == 2 && inplace)) {
 #pragma unroll
-      for (int m = 0; m < CellOps<TYP, T>::NW; m++) o.wn[d][m] = rn[R::ST + 1 + m];
+      for (int m = 0; m < CellOps<TYP, T, NV>::NW; m++) o.wn[d][m] = rn[R::ST + 1 + m];
     }
   }
 }
@@ -589,19 +627,21 @@ __device__ __forceinline__ void load_ops(const PlaneData<T>& p, bool inplace, in
 // (+-coe1/2)) / coe5 in the reference's direction order; in place (upper
 // sweep of a sub-iteration that updates W^{p+1} over W^p) the k+1 term uses
 // the neighbour's new state and the cell's own Newton update follows.
-template <int TYP, typename T, bool UPPER>
+template <int TYP, typename T, bool UPPER, int NV>
 __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, const LuFields& f,
-                                         int64_t g, const CellOps<TYP, T>& o) {
+                                         int64_t g, const CellOps<TYP, T, NV>& o) {
   using R = Rec<TYP, T>;
+  using C = CellOps<TYP, T, NV>;
   constexpr int NB = R::NB;
-  T x[5], od[5], b[5];
+  T x[NV], od[NV], b[5];
 #pragma unroll
-  for (int v = 0; v < 5; v++) x[v] = o.x[v];
+  for (int v = 0; v < NV; v++) x[v] = o.x[v];
   auto term = [&](auto dc, bool fresh) {
     constexpr int D = decltype(dc)::value;
     const int32_t n = o.n[D];
     if (n < 0) return;
-    load_dio(p.dio, n, od);
+    load_dio<NV>(p.dio, n, od);
+    T qn = T(0);   // SA row: normal velocity of the neighbour
     if (fresh) {  // k+1 neighbour updated in place: B from its new state
       T e[NB];
       const T* q = p.nst + (int64_t)n * 4;
@@ -617,19 +657,27 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
       }
       bentries<TYP, T>(z, D, u, vv, w, t, tx, ty, tz, e);
       bmatvec<TYP, D, T>(z, e, o.cs[D], od, b);
-    } else if (CellOps<TYP, T>::HOLD_W) {  // cartesian: B from the held state
+      if (NV == 6) qn = qn_entry<TYP, D, T>(e);
+    } else if (C::HOLD_W) {  // cartesian: B from the held state
       T e[NB];
       T tx, ty, tz;
       nb_normal<TYP, T>(z, D, 0, 0, tx, ty, tz);
-      bentries<TYP, T>(z, D, o.wn[D][0], o.wn[D][CellOps<TYP, T>::NW > 1 ? 1 : 0],
-                       o.wn[D][CellOps<TYP, T>::NW > 2 ? 2 : 0], o.wn[D][CellOps<TYP, T>::NW > 3 ? 3 : 0],
+      bentries<TYP, T>(z, D, o.wn[D][0], o.wn[D][C::NW > 1 ? 1 : 0],
+                       o.wn[D][C::NW > 2 ? 2 : 0], o.wn[D][C::NW > 3 ? 3 : 0],
                        tx, ty, tz, e);
       bmatvec<TYP, D, T>(z, e, o.cs[D], od, b);
+      if (NV == 6) qn = qn_entry<TYP, D, T>(e);
     } else {
-      bmatvec<TYP, D, T>(z, p.rec + (int64_t)n * R::SIZE + R::B + D * NB, o.cs[D], od, b);
+      const T* e = p.rec + (int64_t)n * R::SIZE + R::B + D * NB;
+      bmatvec<TYP, D, T>(z, e, o.cs[D], od, b);
+      if (NV == 6) qn = qn_entry<TYP, D, T>(e);
     }
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * o.xal;
+    if (NV == 6) {   // lu_*_SA.for: b6 = (qn + coe_{d+2}(nb) signe) dW6_nb
+      const T b6 = (qn + o.cs[D]) * od[NV - 1];
+      x[NV - 1] = x[NV - 1] + b6 * o.xal;
+    }
   };
   if (UPPER) {                 // invlu_u.for: k, then j, then i
     term(DirT<2>{}, f.inplace != 0);
@@ -646,9 +694,10 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
   }
 #pragma unroll
   for (int v = 0; v < 5; v++) x[v] = x[v] * o.diag;
+  if (NV == 6) x[NV - 1] = x[NV - 1] / o.c6;   // lu_dinv_SA.for
   T* io = p.dio + g * DIO;
 #pragma unroll
-  for (int v = 0; v < 5; v++) io[v] = x[v];
+  for (int v = 0; v < NV; v++) io[v] = x[v];
   if (!UPPER || !f.inplace) return;  // otherwise the Newton update runs after the sweep
   // in place: the k-1 neighbour needs this cell's new state in the next plane
   T nw[5];
@@ -663,6 +712,9 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
     const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
 #pragma unroll
     for (int v = 0; v < 5; v++) f.rop_new[l + v * z.nd] = double(nw[v]);
+    if (NV == 6)
+      f.rop_new[l + 5 * z.nd] = newton_sa(z, double(o.st[0]), f.rop_old[l + 5 * z.nd],
+                                          double(x[NV - 1]), 1. / double(nw[0]), double(nw[4]));
   }
 }
 
@@ -725,32 +777,32 @@ __device__ __forceinline__ void prefetch_plane(const PlaneData<T>& p, int64_t s,
 // PRE, a thread's first cell of the plane comes with its operands already
 // loaded (FP32 sweeps: they are latency-bound); FP64 sweeps, bound by the
 // FP64 pipe, load them here.
-template <int TYP, typename T, bool UPPER, bool PRE>
+template <int TYP, typename T, bool UPPER, bool PRE, int NV>
 __device__ __forceinline__ void do_plane(const Zone& z, const PlaneData<T>& p, const LuFields& f,
-                                         int64_t s, CellOps<TYP, T>& first) {
+                                         int64_t s, CellOps<TYP, T, NV>& first) {
   const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
   int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
   if (c >= n) return;
-  if (!PRE) load_ops<TYP, T, UPPER>(p, f.inplace != 0, c0 + c, first);
-  run_cell<TYP, T, UPPER>(z, p, f, c0 + c, first);
+  if (!PRE) load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, c0 + c, first);
+  run_cell<TYP, T, UPPER, NV>(z, p, f, c0 + c, first);
   for (c += (int64_t)gridDim.x * blockDim.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-    CellOps<TYP, T> o;
-    load_ops<TYP, T, UPPER>(p, f.inplace != 0, c0 + c, o);
-    run_cell<TYP, T, UPPER>(z, p, f, c0 + c, o);
+    CellOps<TYP, T, NV> o;
+    load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, c0 + c, o);
+    run_cell<TYP, T, UPPER, NV>(z, p, f, c0 + c, o);
   }
 }
 
-template <int TYP, typename T, bool UPPER>
+template <int TYP, typename T, bool UPPER, int NV>
 __device__ __forceinline__ void load_first(const PlaneData<T>& p, const LuFields& f, int64_t s,
-                                           CellOps<TYP, T>& o) {
+                                           CellOps<TYP, T, NV>& o) {
   const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
   const int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
-  if (c < n) load_ops<TYP, T, UPPER>(p, f.inplace != 0, c0 + c, o);
+  if (c < n) load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, c0 + c, o);
 }
 
 template <typename T> struct LuThreads { static constexpr int n = 512; };
 
-template <int TYP, typename T>
+template <int TYP, typename T, int NV>
 __global__ void __launch_bounds__(LuThreads<T>::n, 1)
     lusgs_persistent(Zone z, PlaneData<T> p, LuFields f, GridBar gb) {
   const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
@@ -760,19 +812,19 @@ __global__ void __launch_bounds__(LuThreads<T>::n, 1)
   prefetch_plane<TYP, T>(p, 0, false);
   if (nsteps > 1) prefetch_plane<TYP, T>(p, plane_of(1), 1 > smax);
   constexpr bool PRE = sizeof(T) == 4;
-  CellOps<TYP, T> o;
-  if (PRE) load_first<TYP, T, false>(p, f, 0, o);
+  CellOps<TYP, T, NV> o;
+  if (PRE) load_first<TYP, T, false, NV>(p, f, 0, o);
   unsigned int round = 0;
   for (int64_t t = 0; t < nsteps; t++) {
     const int64_t s = plane_of(t);
-    if (t <= smax) do_plane<TYP, T, false, PRE>(z, p, f, s, o);
-    else do_plane<TYP, T, true, PRE>(z, p, f, s, o);
+    if (t <= smax) do_plane<TYP, T, false, PRE, NV>(z, p, f, s, o);
+    else do_plane<TYP, T, true, PRE, NV>(z, p, f, s, o);
     if (t == nsteps - 1) break;
     bar_arrive(gb);
     if (t + 2 < nsteps) prefetch_plane<TYP, T>(p, plane_of(t + 2), t + 2 > smax);
     if (PRE) {
-      if (t + 1 <= smax) load_first<TYP, T, false>(p, f, plane_of(t + 1), o);
-      else load_first<TYP, T, true>(p, f, plane_of(t + 1), o);
+      if (t + 1 <= smax) load_first<TYP, T, false, NV>(p, f, plane_of(t + 1), o);
+      else load_first<TYP, T, true, NV>(p, f, plane_of(t + 1), o);
     }
     round++;
     if (!bar_wait(gb, round * gridDim.x)) return;
@@ -781,21 +833,21 @@ __global__ void __launch_bounds__(LuThreads<T>::n, 1)
 
 // one launch per hyperplane (no inter-CTA waits): cross-check of the
 // persistent kernel
-template <int TYP, typename T, bool UPPER>
+template <int TYP, typename T, bool UPPER, int NV>
 __global__ void __launch_bounds__(128) lusgs_plane(Zone z, PlaneData<T> p, LuFields f, int64_t s) {
   const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
-  CellOps<TYP, T> o;
-  load_ops<TYP, T, UPPER>(p, f.inplace != 0, c0 + c, o);
-  run_cell<TYP, T, UPPER>(z, p, f, c0 + c, o);
+  CellOps<TYP, T, NV> o;
+  load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, c0 + c, o);
+  run_cell<TYP, T, UPPER, NV>(z, p, f, c0 + c, o);
 }
 
 // FP64 Newton update of every interior cell after the sweeps.  Tiles of
 // GT_I x GT_J cells at one k as in lu_gather: the increments of a tile
 // anti-diagonal are contiguous in plane order, so the CTA reads them as
 // spans into shared memory, then updates its cells in natural order.
-template <typename T, bool TWO_D>
+template <typename T, bool TWO_D, int NV>
 __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* __restrict__ dio) {
   __shared__ __align__(16) T s_dio[GT_N * DIO];
   __shared__ int32_t s_g[GT_N];
@@ -826,6 +878,9 @@ __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* _
                           d, nw);
 #pragma unroll
     for (int v = 0; v < 5; v++) f.rop_new[l + v * nd] = nw[v];
+    if (NV == 6)
+      f.rop_new[l + 5 * nd] = newton_sa(z, R[l], R[l + 5 * nd], double(s_dio[q * DIO + NV - 1]),
+                                        1. / nw[0], nw[4]);
     return;
   }
   // Mixed precision: the same map written as W^{p+1} = W^p + delta with the
@@ -852,9 +907,12 @@ __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* _
   f.rop_new[l + 2 * nd] = v + double(dv);
   f.rop_new[l + 3 * nd] = TWO_D ? 0. : w + double(dw);
   f.rop_new[l + 4 * nd] = tt + double(dT);
+  if (NV == 6)   // the SA update (mjr_newton_SA.for) on the FP64 state
+    f.rop_new[l + 5 * nd] = newton_sa(z, ro, R[l + 5 * nd], double(s_dio[q * DIO + NV - 1]), 1. / ron,
+                                      tt + double(dT));
 }
 
-template <int TYP, typename T>
+template <int TYP, typename T, int NV = 5>
 static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>& p,
                             const LuLaunch& L, cudaStream_t st) {
   using S = GatherSmem<TYP, T>;
@@ -863,49 +921,48 @@ static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (!smem_set[dev]) {
-    cudaError_t e0 = cudaFuncSetAttribute(lu_gather<TYP, T>,
+    cudaError_t e0 = cudaFuncSetAttribute(lu_gather<TYP, T, NV>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes);
     if (e0 != cudaSuccess) return e0;
     smem_set[dev] = true;
   }
-  lu_gather<TYP, T><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I), (unsigned)((z.nj + GT_J - 1) / GT_J),
-                       (unsigned)z.nk), GT_N, S::bytes, st>>>(z, f, p);
+  lu_gather<TYP, T, NV><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I), (unsigned)((z.nj + GT_J - 1) / GT_J),
+                           (unsigned)z.nk), GT_N, S::bytes, st>>>(z, f, p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (L.persistent) {
-    static int grid_cache[3][2] = {{0, 0}, {0, 0}, {0, 0}};
-    int& grid = grid_cache[TYP == Z3DCART ? 0 : (TYP == Z2D ? 1 : 2)][sizeof(T) == 4];
+    static int grid = 0;   // per instantiation (one device per process in practice)
     if (grid == 0) {
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T>, LuThreads<T>::n, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T, NV>, LuThreads<T>::n, 0);
       grid = nsm * (per > 0 ? per : 1);
     }
     e = cudaMemsetAsync(L.bar, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     GridBar gb{L.bar, L.err};
     void* args[] = {(void*)&z, (void*)&p, (void*)&f, (void*)&gb};
-    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T>, dim3(grid), dim3(LuThreads<T>::n),
+    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T, NV>, dim3(grid), dim3(LuThreads<T>::n),
                                     args, 0, st);
   } else {
     const int B = 128;
     const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
     for (int64_t s = 0; s <= smax; s++) {
       int64_t n = L.plane_host[s + 1] - L.plane_host[s];
-      lusgs_plane<TYP, T, false><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
+      lusgs_plane<TYP, T, false, NV><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
     }
     for (int64_t s = smax; s >= 0; s--) {
       int64_t n = L.plane_host[s + 1] - L.plane_host[s];
-      lusgs_plane<TYP, T, true><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
+      lusgs_plane<TYP, T, true, NV><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
     }
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) return e;
   if (!f.inplace || sizeof(T) == 4) {
-    lu_newton<T, TYP == Z2D><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I),
-                                    (unsigned)((z.nj + GT_J - 1) / GT_J), (unsigned)z.nk),
-                               GT_N, 0, st>>>(z, f, p.dio);
+    lu_newton<T, TYP == Z2D, NV><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I),
+                                        (unsigned)((z.nj + GT_J - 1) / GT_J), (unsigned)z.nk),
+                                   GT_N, 0, st>>>(z, f, p.dio);
     e = cudaGetLastError();
   }
   return e;
@@ -938,18 +995,22 @@ cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl,
 // One LU-SGS solve (lower, upper, Newton update) of one zone.
 cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st) {
   LuFields f{a.rop_old, a.rop_new, a.coe, a.din, L.posmap, a.rop_knb == a.rop_new};
+  const bool sa = z.neq == 6;   // Spalart-Allmaras: 3d zones
+  if (sa && z.typ == Z2D) return cudaErrorNotSupported;
   if (L.fp32) {
     const int rs = z.typ == Z3DCART ? Rec<Z3DCART, float>::SIZE : Rec<Z3DFULL, float>::SIZE;
     PlaneData<float> p = plane_data<float>(L, rs);
-    if (z.typ == Z3DCART) return launch_t<Z3DCART, float>(z, f, p, L, st);
+    if (z.typ == Z3DCART)
+      return sa ? launch_t<Z3DCART, float, 6>(z, f, p, L, st) : launch_t<Z3DCART, float>(z, f, p, L, st);
     if (z.typ == Z2D) return launch_t<Z2D, float>(z, f, p, L, st);
-    return launch_t<Z3DFULL, float>(z, f, p, L, st);
+    return sa ? launch_t<Z3DFULL, float, 6>(z, f, p, L, st) : launch_t<Z3DFULL, float>(z, f, p, L, st);
   }
   const int rs = z.typ == Z3DCART ? Rec<Z3DCART, double>::SIZE : Rec<Z3DFULL, double>::SIZE;
   PlaneData<double> p = plane_data<double>(L, rs);
-  if (z.typ == Z3DCART) return launch_t<Z3DCART, double>(z, f, p, L, st);
+  if (z.typ == Z3DCART)
+    return sa ? launch_t<Z3DCART, double, 6>(z, f, p, L, st) : launch_t<Z3DCART, double>(z, f, p, L, st);
   if (z.typ == Z2D) return launch_t<Z2D, double>(z, f, p, L, st);
-  return launch_t<Z3DFULL, double>(z, f, p, L, st);
+  return sa ? launch_t<Z3DFULL, double, 6>(z, f, p, L, st) : launch_t<Z3DFULL, double>(z, f, p, L, st);
 }
 
 }  // namespace fgb

@@ -381,8 +381,17 @@ def _BCcompact(t):
 
 
 # ---------------------------------------------------------- prim vars
-CONS = ["Density", "MomentumX", "MomentumY", "MomentumZ", "EnergyStagnationDensity"]
+CONS = ["Density", "MomentumX", "MomentumY", "MomentumZ", "EnergyStagnationDensity",
+        "TurbulentSANuTildeDensity"]
 PRIM = ["Density", "VelocityX", "VelocityY", "VelocityZ", "Temperature"]
+PRIM_SA = PRIM + ["TurbulentSANuTilde"]
+
+
+def _prim_names(z):
+    """Primitive variables of a zone: 5, or 6 with Spalart-Allmaras."""
+    o = I.getNodeFromName1(z, ".Solver#ownData")
+    pi = I.getNodeFromName1(o, "Parameter_int")[1]
+    return PRIM_SA if int(pi[IFLOW]) == 3 else PRIM
 
 
 def createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
@@ -393,6 +402,10 @@ def createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
         sol = I.getNodeFromName1(z, I.__FlowSolutionCenters__)
         o = I.getNodeFromName1(z, ".Solver#ownData")
         cv = float(I.getNodeFromName1(o, "Parameter_real")[1][CVINF])
+        names = _prim_names(z)
+        if len(names) == 6 and I.getNodeFromName1(sol, "TurbulentDistance") is None:
+            raise ValueError("createPrimVars: TurbulentDistance field required at cell "
+                             "centers for RANS computations.")
         if I.getNodeFromName1(sol, "VelocityX") is None:
             ro = I.getNodeFromName1(sol, "Density")[1]
             rou = I.getNodeFromName1(sol, "MomentumX")[1]
@@ -404,13 +417,23 @@ def createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
             prim = [ro, u, v, w, temp]
         else:
             prim = [I.getNodeFromName1(sol, n)[1] for n in PRIM]
+        if len(names) == 6:
+            # FastC/FastC/PyTree.py:484-486: nutilde from ro nutilde, else
+            # the free-stream ro nutilde over the density
+            nu = I.getNodeFromName1(sol, "TurbulentSANuTilde")
+            if nu is not None:
+                prim.append(nu[1])
+            else:
+                rnu = I.getNodeFromName1(sol, "TurbulentSANuTildeDensity")
+                ronut_inf = float(I.getNodeFromName1(o, "Parameter_real")[1][8])
+                prim.append((rnu[1] if rnu is not None else ronut_inf) / prim[0])
         shape = prim[0].shape
         n = prim[0].size
         for suffix in ("", "_M1", "_P1"):
-            buf = np.empty((5, n), dtype=np.float64)
+            buf = np.empty((len(names), n), dtype=np.float64)
             for v_, arr in enumerate(prim):
                 buf[v_] = np.asarray(arr, dtype=np.float64).ravel(order="F")
-            for v_, name in enumerate(PRIM):
+            for v_, name in enumerate(names):
                 view = buf[v_].reshape(shape, order="F")
                 I.createUniqueChild(sol, name + suffix, "DataArray_t")
                 I.getNodeFromName1(sol, name + suffix)[1] = view
@@ -436,6 +459,6 @@ def switchPointers__(zones, case=3):
         o = I.getNodeFromName1(z, ".Solver#ownData")
         cn, cm, cp = (I.getNodeFromName1(o, "compact" + s) for s in ("", "_M1", "_P1"))
         cn[1], cm[1], cp[1] = cp[1], cn[1], cm[1]
-        for name in PRIM:
+        for name in _prim_names(z):
             a, b, c = (I.getNodeFromName1(sol, name + s) for s in ("", "_M1", "_P1"))
             a[1], b[1], c[1] = c[1], a[1], b[1]

@@ -125,10 +125,15 @@ def zone_data(t, metrics):
         pi = I.getNodeFromName1(o, "Parameter_int")[1]
         pr = I.getNodeFromName1(o, "Parameter_real")[1]
         ti, tj, tk, vol = metric_arrays(pi, m[0])
-        out.append(dict(pi=pi, pr=pr, ti=ti, tj=tj, tk=tk, vol=vol,
-                        ro=FastC.compactArray(z, "").reshape(-1),
-                        ro_m1=FastC.compactArray(z, "_M1").reshape(-1),
-                        ro_p1=FastC.compactArray(z, "_P1").reshape(-1)))
+        d = dict(pi=pi, pr=pr, ti=ti, tj=tj, tk=tk, vol=vol,
+                 ro=FastC.compactArray(z, "").reshape(-1),
+                 ro_m1=FastC.compactArray(z, "_M1").reshape(-1),
+                 ro_p1=FastC.compactArray(z, "_P1").reshape(-1))
+        if int(pi[FastC.NEQ]) == 6:
+            sol = I.getNodeFromName1(z, I.__FlowSolutionCenters__)
+            d["dist"] = np.ascontiguousarray(
+                I.getNodeFromName1(sol, "TurbulentDistance")[1].ravel(order="F"), dtype=np.float64)
+        out.append(d)
     return out
 
 
@@ -146,8 +151,10 @@ def warmup(t, tc=None, graph=None, infos_ale=None, Adjoint=False, tmy=None, list
     dtloc = I.getNodeFromName1(I.getNodeFromName1(t, ".Solver#ownData"), ".Solver#dtloc")[1]
     nssiter = int(dtloc[0])
     solver = Solver(device)
-    for zd in zone_data(t, metrics):
+    for n, zd in enumerate(zone_data(t, metrics)):
         solver.add_zone(zd["pi"], zd["pr"], zd["ti"], zd["tj"], zd["tk"], zd["vol"])
+        if "dist" in zd:
+            solver.set_wall_distance(n, zd["dist"])
     for tr in (tc or []):
         solver.add_transfer(tr["dnr"], tr["rcv"], tr["dnr_idx"], tr["rcv_idx"])
     solver.set_option("modulo_verif", int(dtloc[1]))

@@ -61,6 +61,13 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
 int fgb_add_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
                      const int64_t* dnr_idx, const int64_t* rcv_idx);
 
+/* Wall distance of a Spalart-Allmaras zone (IFLOW 3, NEQ 6): NDIMDX doubles
+ * at cell centres, ghosts included -- the FlowSolution#Centers
+ * "TurbulentDistance" field that FastS reads behind the viscosity array
+ * (navier_stokes_struct.for passes xmut(1+NDIMDX) to spsource_SA.for).
+ * Required before the first fgb_compute of such a zone. */
+int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
+
 /* Solver options.  "lu_precision": 64 (default) or 32 -- FP32 LU-SGS sweeps
  * inside the FP64 defect-correction loop; "modulo_verif": residual check
  * period (FastC numerics key modulo_verif, default 200); "first_it": the
@@ -78,7 +85,8 @@ int fgb_upload_state(fgb_solver* s, int zone, int level, const double* host);
 int fgb_download_state(fgb_solver* s, int zone, int level, double* host);
 
 /* Work arrays for inspection: which = "drodm" (NEQ*NDIMDX), "coe"
- * (NEQ_COE*NDIMDX), "xmut" (NDIMDX), "rdm" (nssiter*NEQ*2*n_lu_blocks). */
+ * (NEQ*NDIMDX), "xmut" (NDIMDX), "dist" (NDIMDX, Spalart-Allmaras zones),
+ * "rdm" (nssiter*NEQ*2*n_lu_blocks). */
 int fgb_download_work(fgb_solver* s, int zone, const char* which, double* host,
                       int64_t n);
 

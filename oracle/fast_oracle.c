@@ -31,7 +31,8 @@ enum { NIJK = 0, NIJK_MTR = 5, NIJK_XYZ = 10, IJKV = 20, ITYPZONE = 25, IFLOW = 
        PT_BC = 70, NB_RELAX = 71, LU_MATCH = 75, SENSORTYPE = 85 };
 enum { DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6,
        PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14,
-       PSIROE = 34, WIG_AMP = 72, VXINF = 19, VYINF = 20, VZINF = 21 };
+       PSIROE = 34, WIG_AMP = 72, VXINF = 19, VYINF = 20, VZINF = 21,
+       RONUTILDEINF = 8, SA_RATIOM_R = 18, PRANDT_TUR = 38 };
 enum { BC_TYPE = 0, BC_IDIR = 1, BC_FEN = 2 };
 
 #define OMAX(a, b) ((a) > (b) ? (a) : (b))
@@ -74,6 +75,181 @@ void or_invist(const int64_t* pi, const double* pr, const int64_t* ind,
         int64_t l = inddm(pi, i, j, k);
         double t1 = rop[l + v5];
         xmut[l] = coesut * sqrt(t1) * t1 / (t1 + cmus1);
+      }
+}
+
+/* ======================================================================
+ * Spalart-Allmaras -- constants of FastS/FastS/param_solver.h:315-327
+ * ====================================================================== */
+#define SA_CKARM 0.41
+#define SA_CB1 0.1355
+#define SA_CB2 0.622
+#define SA_CV1 357.911
+#define SA_CW2 0.3
+#define SA_CW3 64.
+#define SA_CW4 0.21
+#define SA_CW5 1.5
+#define SA_SIGMA (2. / 3.)
+#define SA_CROT 2.0
+
+/* mulam.for: Sutherland law in the form the SA routines use */
+static inline double sa_mulam(double coesut, double temp01, double cmus1, double t) {
+  return coesut * sqrt(t * temp01) / (1. + cmus1 / t);
+}
+/* SA/chi.for (anutild = max(nutilde, 1e-27), chi = max(anutild*ro/mu, 1e-7)) */
+static inline double sa_fv1(double s) { return 1. / (1. + SA_CV1 / (s * s * s)); }
+
+/* SA/vispalart.for (SA branch, SA_IDES <= 1) with mulam.for, chi.for and
+ * xmut.for: mu_t = ro nutilde fv1(chi), clipped to [0, ratiom mu]. */
+void or_vispalart(const int64_t* pi, const double* pr, const int64_t* ind,
+                  const double* rop, double* xmut) {
+  const double cmus1 = pr[CS], temp01 = 1. / pr[TEMP0];
+  const double coesut = pr[XMUL0] * (1. + cmus1 * temp01);
+  const int64_t nd = pi[NDIMDX];
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        double amulam = sa_mulam(coesut, temp01, cmus1, rop[l + 4 * nd]);
+        double anulam = rop[l] / amulam;
+        double anutild = OMAX(rop[l + 5 * nd], 1.e-27);
+        double chi = OMAX(anutild * anulam, 1.e-7);
+        double fvv1 = sa_fv1(chi);
+        double amut = rop[l] * anutild * fvv1;
+        double xmuprov = OMAX(amut, 0.);
+        xmut[l] = amulam + OMIN(xmuprov, pr[SA_RATIOM_R] * amulam);
+      }
+}
+
+/* SA/spsource_SA.for with sourceSA_grad_3dcart.for / sourceSA_grad_3d.for
+ * (velocity and nutilde gradients from face sums), sourceSA_prod_dest.for
+ * (production, destruction, cross-diffusion) and sourceSA_LU.for (implicit:
+ * coe6 = coe5 - min(dS/d(ro nutilde), 0) coe1 on the first sub-step).
+ * The reference also evaluates the term on the first ghost ring
+ * (ind_ssa = [0, n+1]); those ghost residuals are never read, so the
+ * interior range is enough.  dist = wall distance (xmut(1+NDIMDX) there).
+ * rot_corr / low_re = param_int SA_ROT_CORR / SA_LOW_RE. */
+void or_spsource(const int64_t* pi, const double* pr, int nitcfg, const int64_t* ind,
+                 const double* rop, double* coe, const double* ti, const double* tj,
+                 const double* tk, const double* vol, const double* dist_in, double* drodm) {
+  const int64_t nd = pi[NDIMDX], ndm = pi[NDIMDX_MTR];
+  const double sw_low_re = (double)pi[130], sw_rot = (double)pi[131];
+  const double cmus1 = pr[CS], temp01 = 1. / pr[TEMP0];
+  const double coesut = pr[XMUL0] * (1. + cmus1 * temp01);
+  const double c1 = SA_CB2 / SA_SIGMA;
+  const double cw1 = (SA_CB1 / SA_CKARM / SA_CKARM) + (1. + SA_CB2) / SA_SIGMA;
+  const int typ = (int)pi[ITYPZONE];
+  const int lu = pi[ITYPCP] <= 1 && nitcfg <= 1;
+  const int64_t incj = pi[NIJK], inck = pi[NIJK] * pi[NIJK + 1];
+  const int64_t mi = pi[NIJK_MTR], mj = pi[NIJK_MTR + 1], mk = pi[NIJK_MTR + 2];
+  const double *r_ = rop, *nu_ = rop + 5 * nd;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        const int64_t l = inddm(pi, i, j, k);
+        const int64_t lt = typ == 2 ? 0 : indmtr(pi, i, j, k);
+        const int64_t l1 = l + 1, l2 = l - 1, l3 = l + incj, l4 = l - incj, l5 = l + inck, l6 = l - inck;
+        const double xvol = 0.5 / vol[lt];
+        double g[3][3], gn[3], gr[3];   /* g[v][x]: d(u,v,w)/dx, gn: d nutilde, gr: d ro nutilde */
+        if (typ == 2) {   /* sourceSA_grad_3dcart.for */
+          const double tix = ti[0], tjy = tj[0], tkz = tk[0];
+          for (int v = 0; v < 3; v++) {
+            const double* q = rop + (v + 1) * nd;
+            double u1 = (q[l] + q[l2]), u2 = (q[l] + q[l3]), u3 = (q[l] + q[l1]);
+            double u4 = (q[l] + q[l4]), u5 = (q[l] + q[l5]), u6 = (q[l] + q[l6]);
+            g[v][0] = (u3 - u1) * tix;
+            g[v][1] = (u2 - u4) * tjy;
+            g[v][2] = (u5 - u6) * tkz;
+          }
+          {
+            const double* q = nu_;
+            double u1 = (q[l] + q[l2]), u2 = (q[l] + q[l3]), u3 = (q[l] + q[l1]);
+            double u4 = (q[l] + q[l4]), u5 = (q[l] + q[l5]), u6 = (q[l] + q[l6]);
+            gn[0] = (u3 - u1) * tix;
+            gn[1] = (u2 - u4) * tjy;
+            gn[2] = (u5 - u6) * tkz;
+          }
+          {
+            double a = nu_[l] * r_[l];
+            double u1 = a + nu_[l2] * r_[l2], u2 = a + nu_[l3] * r_[l3], u3 = a + nu_[l1] * r_[l1];
+            double u4 = a + nu_[l4] * r_[l4], u5 = a + nu_[l5] * r_[l5], u6 = a + nu_[l6] * r_[l6];
+            gr[0] = (u3 - u1) * tix;
+            gr[1] = (u2 - u4) * tjy;
+            gr[2] = (u5 - u6) * tkz;
+          }
+        } else {          /* sourceSA_grad_3d.for */
+          const double* T[3] = {ti, tj, tk};
+          const int64_t lt1[3] = {lt + mi, lt + mj, lt + mk};
+          /* t0[x][d] = t_d(lt, x), t1[x][d] = t_d(lt + inc_d, x) */
+          double t0[3][3], t1[3][3];
+          for (int x = 0; x < 3; x++)
+            for (int d = 0; d < 3; d++) {
+              t0[x][d] = T[d][lt + x * ndm];
+              t1[x][d] = T[d][lt1[d] + x * ndm];
+            }
+          for (int v = 0; v < 4; v++) {
+            const double* q = v < 3 ? rop + (v + 1) * nd : nu_;
+            double u1 = (q[l] + q[l2]), u2 = (q[l] + q[l3]), u3 = (q[l] + q[l1]);
+            double u4 = (q[l] + q[l4]), u5 = (q[l] + q[l5]), u6 = (q[l] + q[l6]);
+            double* o = v < 3 ? g[v] : gn;
+            for (int x = 0; x < 3; x++)
+              o[x] = (u3 * t1[x][0] - u1 * t0[x][0] + u2 * t1[x][1] - u4 * t0[x][1] +
+                      u5 * t1[x][2] - u6 * t0[x][2]);
+          }
+          double a = nu_[l] * r_[l];
+          double u1 = a + nu_[l2] * r_[l2], u2 = a + nu_[l3] * r_[l3], u3 = a + nu_[l1] * r_[l1];
+          double u4 = a + nu_[l4] * r_[l4], u5 = a + nu_[l5] * r_[l5], u6 = a + nu_[l6] * r_[l6];
+          for (int x = 0; x < 3; x++)
+            gr[x] = (u3 * t1[x][0] - u1 * t0[x][0] + u2 * t1[x][1] - u4 * t0[x][1] +
+                     u5 * t1[x][2] - u6 * t0[x][2]);
+        }
+        const double dudx = g[0][0], dudy = g[0][1], dudz = g[0][2];
+        const double dvdx = g[1][0], dvdy = g[1][1], dvdz = g[1][2];
+        const double dwdx = g[2][0], dwdy = g[2][1], dwdz = g[2][2];
+        const double rotx = dwdy - dvdz, roty = dudz - dwdx, rotz = dvdx - dudy;
+        const double rot = sqrt(rotx * rotx + roty * roty + rotz * rotz) * xvol;
+        const double S11 = dudx, S22 = dvdy, S33 = dwdz;
+        const double S12 = 0.5 * (dudy + dvdx), S13 = 0.5 * (dudz + dwdx), S23 = 0.5 * (dvdz + dwdy);
+        double St = S11 * S11 + S22 * S22 + S33 * S33 + 2. * (S12 * S12) + 2. * (S13 * S13) +
+                    2. * (S23 * S23);
+        St = sqrt(2. * St) * xvol;
+        const double anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1] + gn[2] * gr[2]) * xvol * xvol;
+        /* mulam.for, chi.for */
+        const double amulam = sa_mulam(coesut, temp01, cmus1, rop[l + 4 * nd]);
+        const double anulam = r_[l] / amulam;
+        const double anutild = OMAX(nu_[l], 1.e-27);
+        const double chi = OMAX(anutild * anulam, 1.e-7);
+        /* sourceSA_prod_dest.for */
+        const double f1 = sa_fv1(chi);
+        const double f2 = 1. - chi / (1. + chi * f1);
+        const double dist = OMAX(dist_in[l], 1.e-27);
+        double stild = rot + (anutild * f2) / (SA_CKARM * SA_CKARM * dist * dist);
+        stild = stild + sw_rot * SA_CROT * OMIN(0.00000000000000000001, St - rot);
+        const double prod = r_[l] * SA_CB1 * stild * anutild;
+        stild = OMAX(stild, 0.00000000000000000001);
+        double r = anutild / (stild * SA_CKARM * SA_CKARM * dist * dist);
+        r = OMIN(r, 10.);
+        const double r5 = r * r * r * r * r - 1.;
+        double gg = r * (1. + SA_CW2 * r5);
+        const double lre = 1. + chi / 40.;
+        const double cw2_lre = SA_CW4 + SA_CW5 / (lre * lre);
+        gg = sw_low_re * r * (1. + cw2_lre * r5) + (1. - sw_low_re) * gg;
+        /* fw(g) = g ((1 + cw3) / (g^6 + cw3))^(1/6); g**6 is expanded by
+         * the Fortran compiler as (g^3)^2 with g^3 = g^2 g */
+        const double g3 = gg * gg * gg, g6 = g3 * g3;
+        const double fwg = gg * pow((1. + SA_CW3) / (g6 + SA_CW3), 1. / 6.);
+        const double destruc = r_[l] * cw1 * fwg * (anutild / dist) * (anutild / dist);
+        const double tsource = (prod + anvisc - destruc);
+        if (lu) {         /* sourceSA_LU.for */
+          const double tsourceb = prod - destruc;
+          double amutild = anutild * r_[l];
+          amutild = OMAX(amutild, 0.0000000000000001);
+          const double tsourcenu = vol[lt] * tsourceb / amutild;
+          coe[l + 5 * nd] = coe[l + 4 * nd] - OMIN(tsourcenu, 0.) * coe[l];
+        }
+        drodm[l + 5 * nd] = drodm[l + 5 * nd] + vol[lt] * tsource;
       }
 }
 
@@ -252,6 +428,8 @@ typedef struct {
   double gam, rgp, gam1, gam3, c1, c2, c3, c4, c5, c6, cvisq, psiroe, wig_cte, tmin_1;
   double tcx, tcy, tcz, si, sj, sk, volinv; /* 3d cartesian constants */
   const double* wig; double opt0;           /* senseur (KFLUDOM = 2) */
+  int neq;                                  /* 6: Spalart-Allmaras (IFLOW = 3) */
+  double gam4, coesut_sa, temp01, cmus1, sigma_1;
 } fctx;
 
 static void fctx_init(fctx* c, const int64_t* pi, const double* pr, const double* rop,
@@ -285,6 +463,13 @@ static void fctx_init(fctx* c, const int64_t* pi, const double* pr, const double
   c->cvisq = 1. / 3;
   c->wig = NULL;
   c->opt0 = (double)pi[SENSORTYPE];
+  /* SA drivers (e.g. AUSM/3dcart/fluausm_SA_o3_3dcart.for:114-127) */
+  c->neq = (int)pi[NEQ];
+  c->gam4 = c->gam1 / pr[PRANDT_TUR] * c->rgp;
+  c->cmus1 = pr[CS];
+  c->temp01 = 1. / pr[TEMP0];
+  c->coesut_sa = pr[XMUL0] * (1. + c->cmus1 * c->temp01);
+  c->sigma_1 = 1. / (2. / 3.);
 }
 
 /* Slope/minmod_slope_var.for:1-17 limiter */
@@ -293,10 +478,10 @@ static inline double avmin(double c, double r) {
 }
 
 /* Slope/{o1,o3,minmod}_slope_var.for: qm = right state, qp = left state */
-static void slopes(const fctx* c, int64_t l, int64_t inc, double qm[5], double qp[5]) {
+static void slopes(const fctx* c, int64_t l, int64_t inc, double qm[6], double qp[6]) {
   const double* rop = c->rop;
   int64_t nd = c->nd, nm = l - inc, nm2 = l - 2 * inc, np = l + inc;
-  for (int v = 0; v < 5; v++) {
+  for (int v = 0; v < c->neq; v++) {
     if (c->typ == 3 && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
     int64_t vs = v * nd;
     if (c->slope == 1) {
@@ -410,8 +595,8 @@ static void roe_face(const fctx* c, const double qm[5], const double qp[5],
 /* AUSM+(P) -- etat_GD.for:1-15, AUSM/fluFaceEuler.for:36-57,
  * Vit_ent/fluvector_3dfull_i.for:1-5.  Same general-form remark as Roe.
  * tl = temperature of cell l (the right cell), used for the sound speed. */
-static void ausm_face(const fctx* c, const double qm[5], const double qp[5], double tl,
-                      double tcx, double tcy, double tcz, double s, double wg, double flu[5]) {
+static void ausm_face(const fctx* c, const double qm[6], const double qp[6], double tl,
+                      double tcx, double tcy, double tcz, double s, double wg, double flu[6]) {
   double rgp = c->rgp, gam1 = c->gam1;
   double r1 = qp[0], rou1 = r1 * qp[1], rov1 = r1 * qp[2], row1 = r1 * qp[3];
   double p1 = r1 * qp[4] * rgp;
@@ -439,11 +624,32 @@ static void ausm_face(const fctx* c, const double qm[5], const double qp[5], dou
   flu[2] = u * (rov1 + rov2) - tdu * (rov2 - rov1) + tcy * p1p2;
   flu[3] = u * (row1 + row2) - tdu * (row2 - row1) + tcz * p1p2;
   flu[4] = u * (h1 + h2) - tdu * (h2 - h1);
+  if (c->neq == 6) {   /* AUSM/fluFaceSA.for: flux of ro * nutilde */
+    double qm6 = qm[5] * qm[0], qp6 = qp[5] * qp[0];
+    flu[5] = u * (qm6 + qp6) - tdu * (qm6 - qp6);
+  }
+}
+
+/* SA/mut_prandtltb_interface.for: laminar viscosity of the two cells (their
+ * sum), total mu and the laminar + turbulent conductivity; SA/mut_interface:
+ * nutilde diffusion coefficient. */
+static void sa_mut(const fctx* c, int64_t il, int64_t ir, double volinv, double* xmutvol,
+                   double* xktvol, double* xmutvol_sa) {
+  const double* rop = c->rop;
+  const int64_t nd = c->nd;
+  double xmulam = c->coesut_sa * sqrt(rop[il + 4 * nd] * c->temp01) / (1. + c->cmus1 / rop[il + 4 * nd]);
+  xmulam = xmulam + c->coesut_sa * sqrt(rop[ir + 4 * nd] * c->temp01) / (1. + c->cmus1 / rop[ir + 4 * nd]);
+  double xmutot = c->xmut[ir] + c->xmut[il];
+  double xmutur = xmutot - xmulam;
+  *xktvol = (xmulam * c->gam3 + xmutur * c->gam4) * volinv;
+  *xmutvol = xmutot * volinv;
+  double x = xmulam + rop[il + 5 * nd] * rop[il] + rop[ir + 5 * nd] * rop[ir];
+  *xmutvol_sa = x * volinv * c->sigma_1;
 }
 
 /* Viscous face flux on a 3d cartesian zone: fluvisq_3dcart_{i,j,k}.for and
  * mut_interface.for (xmutvol = (mu_r + mu_l) * 0.5/vol, xktvol = xmutvol*gam3). */
-static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
+static void visc_cart(const fctx* c, int d, int64_t l, double flu[6]) {
   const double* rop = c->rop;
   int64_t nd = c->nd, inci = c->inc[0], incj = c->inc[1], inck = c->inc[2];
   int64_t v2 = nd, v3 = 2 * nd, v4 = 3 * nd, v5 = 4 * nd;
@@ -475,8 +681,13 @@ static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
     f1 = gradU_nx - div;
     f2 = gradU_ny + gradV_nx;
     f3 = gradU_nz + gradW_nx;
-    double xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
-    double xktvol = xmutvol * c->gam3;
+    double xmutvol, xktvol, xmutvol_sa = 0.;
+    if (c->neq == 6) {
+      sa_mut(c, il, ir, c->volinv, &xmutvol, &xktvol, &xmutvol_sa);
+    } else {
+      xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
+      xktvol = xmutvol * c->gam3;
+    }
     fv = -(2. * f1 * tcx) * xmutvol;
     fv5 = fv * (rop[ir + v2] + rop[il + v2]);
     flu[1] = flu[1] + fv;
@@ -488,6 +699,10 @@ static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
     flu[3] = flu[3] + fv;
     fv = fv5 * 0.5 - (gradT_nx * tcx) * xktvol;
     flu[4] = flu[4] + fv;
+    if (c->neq == 6) {   /* SA/fluvisq_SA_3dcart_i.for */
+      double gn = (rop[ir + 5 * nd] - rop[il + 5 * nd]) * tix;
+      flu[5] = flu[5] - xmutvol_sa * gn * tcx;
+    }
   } else if (d == 1) {
     il = l - incj;
     int64_t l022 = l - incj - inck, l002 = l - inck, l021 = l - incj + inck, l001 = l + inck;
@@ -513,8 +728,13 @@ static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
     f2 = gradU_ny + gradV_nx;
     f4 = gradV_ny - div;
     f5 = gradV_nz + gradW_ny;
-    double xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
-    double xktvol = xmutvol * c->gam3;
+    double xmutvol, xktvol, xmutvol_sa = 0.;
+    if (c->neq == 6) {
+      sa_mut(c, il, ir, c->volinv, &xmutvol, &xktvol, &xmutvol_sa);
+    } else {
+      xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
+      xktvol = xmutvol * c->gam3;
+    }
     fv = -(f2 * tcy) * xmutvol;
     fv5 = fv * (rop[ir + v2] + rop[il + v2]);
     flu[1] = flu[1] + fv;
@@ -526,6 +746,10 @@ static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
     flu[3] = flu[3] + fv;
     fv = fv5 * 0.5 - (gradT_ny * tcy) * xktvol;
     flu[4] = flu[4] + fv;
+    if (c->neq == 6) {   /* SA/fluvisq_SA_3dcart_j.for */
+      double gn = (rop[ir + 5 * nd] - rop[il + 5 * nd]) * tiy;
+      flu[5] = flu[5] - xmutvol_sa * (gn * tcy);
+    }
   } else {
     il = l - inck;
     int64_t l200 = l - inci, l202 = l - inci - inck, l102 = l + inci - inck, l100 = l + inci;
@@ -551,8 +775,13 @@ static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
     f3 = gradU_nz + gradW_nx;
     f5 = gradV_nz + gradW_ny;
     f6 = gradW_nz - div;
-    double xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
-    double xktvol = xmutvol * c->gam3;
+    double xmutvol, xktvol, xmutvol_sa = 0.;
+    if (c->neq == 6) {
+      sa_mut(c, il, ir, c->volinv, &xmutvol, &xktvol, &xmutvol_sa);
+    } else {
+      xmutvol = (c->xmut[ir] + c->xmut[il]) * c->volinv;
+      xktvol = xmutvol * c->gam3;
+    }
     fv = -f3 * tcz * xmutvol;
     fv5 = fv * (rop[ir + v2] + rop[il + v2]);
     flu[1] = flu[1] + fv;
@@ -564,6 +793,10 @@ static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
     flu[3] = flu[3] + fv;
     fv = fv5 * 0.5 - gradT_nz * tcz * xktvol;
     flu[4] = flu[4] + fv;
+    if (c->neq == 6) {   /* SA/fluvisq_SA_3dcart_k.for */
+      double gn = (rop[ir + 5 * nd] - rop[il + 5 * nd]) * tiz;
+      flu[5] = flu[5] - xmutvol_sa * gn * tcz;
+    }
   }
 }
 
@@ -574,7 +807,7 @@ static void visc_cart(const fctx* c, int d, int64_t l, double flu[5]) {
  * (mod 3) from four-cell means (factor 1/8 = 1/4 x 1/2).  The three files
  * are this routine with (d, a, b) = (i, j, k), (j, k, i), (k, i, j). */
 static void visc_full(const fctx* c, int d, int64_t l, int64_t lt, double tcx, double tcy,
-                      double tcz, double flu[5]) {
+                      double tcz, double flu[6]) {
   const double* rop = c->rop;
   const int64_t nd = c->nd, ndm = c->ndm;
   const int a = (d + 1) % 3, b = (d + 2) % 3;
@@ -595,8 +828,9 @@ static void visc_full(const fctx* c, int d, int64_t l, int64_t lt, double tcx, d
     tb1[m] = .125 * (TB[ltB + o] + TB[ltBm + o]);
   }
   const int64_t il = l - c->inc[d], ir = l;
-  double g[4][3];
-  for (int v = 0; v < 4; v++) {
+  double g[5][3];
+  const int ng = c->neq == 6 ? 5 : 4;    /* u, v, w, T (, nutilde) */
+  for (int v = 0; v < ng; v++) {
     const double* q = rop + (v + 1) * nd;
     double f1 = q[il], f2 = q[ir];
     double f3 = q[ir] + q[il] + q[il - iA] + q[ir - iA];
@@ -610,8 +844,13 @@ static void visc_full(const fctx* c, int d, int64_t l, int64_t lt, double tcx, d
   const double f1 = g[0][0] - div, f2 = g[0][1] + g[1][0], f3 = g[0][2] + g[2][0];
   const double f4 = g[1][1] - div, f5 = g[1][2] + g[2][1], f6 = g[2][2] - div;
   const double volinv = 1. / (c->vol[lt] + c->vol[ltm]);
-  const double xmutvol = (c->xmut[ir] + c->xmut[il]) * volinv;
-  const double xktvol = xmutvol * c->gam3;
+  double xmutvol, xktvol, xmutvol_sa = 0.;
+  if (c->neq == 6) {
+    sa_mut(c, il, ir, volinv, &xmutvol, &xktvol, &xmutvol_sa);
+  } else {
+    xmutvol = (c->xmut[ir] + c->xmut[il]) * volinv;
+    xktvol = xmutvol * c->gam3;
+  }
   double fv, fv5;
   fv = -(2. * f1 * tcx + f2 * tcy + f3 * tcz) * xmutvol;
   fv5 = fv * (rop[ir + nd] + rop[il + nd]);
@@ -624,13 +863,15 @@ static void visc_full(const fctx* c, int d, int64_t l, int64_t lt, double tcx, d
   flu[3] = flu[3] + fv;
   fv = fv5 * 0.5 - (g[3][0] * tcx + g[3][1] * tcy + g[3][2] * tcz) * xktvol;
   flu[4] = flu[4] + fv;
+  if (c->neq == 6)   /* SA/fluvisq_SA_3dfull_*.for + assemble_tauij_3dfull.for */
+    flu[5] = flu[5] - xmutvol_sa * (g[4][0] * tcx + g[4][1] * tcy + g[4][2] * tcz);
 }
 
 /* One face flux (convective + viscous) of direction d at cell (i,j,k). */
-static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, double flu[5]) {
+static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, double flu[6]) {
   int64_t l = inddm(c->pi, i, j, k);
   int64_t lt = indmtr(c->pi, i, j, k);
-  double qm[5], qp[5], tcx, tcy, tcz, s;
+  double qm[6], qp[6], tcx, tcy, tcz, s;
   slopes(c, l, c->inc[d], qm, qp);
   if (c->typ == 2) {
     tcx = d == 0 ? c->tcx : 0.; tcy = d == 1 ? c->tcy : 0.; tcz = d == 2 ? c->tcz : 0.;
@@ -681,7 +922,7 @@ void or_correct_flux(const int64_t* pi, const double* pr, const double* rop, dou
       for (int64_t j = cl[2]; j <= cl[3]; j++)
         for (int64_t i = cl[0]; i <= cl[1]; i++) {
           const int64_t l = inddm(pi, i, j, k), iadrf = l - inc, l0 = low ? l : l - inc;
-          double flu[5];
+          double flu[6];
           face_flux(&c, d, i, j, k, flu);
           for (int v = 0; v < 5; v++) drodm[l0 + v * nd] = drodm[l0 + v * nd] + (flu[v] * sens_c + 0.);
           double t[3];
@@ -761,27 +1002,28 @@ void or_flux(const int64_t* pi, const double* pr, const int64_t* ind,
   int64_t ni = ind[1] - ind[0] + 1, nj = ind[3] - ind[2] + 1, nk = ind[5] - ind[4] + 1;
   int two_d = (c.typ == 3);
   int64_t fi = (ni + 1) * nj * nk, fj = ni * (nj + 1) * nk, fk = ni * nj * (nk + 1);
-  double* Fi = (double*)malloc(sizeof(double) * 5 * fi);
-  double* Fj = (double*)malloc(sizeof(double) * 5 * fj);
-  double* Fk = two_d ? NULL : (double*)malloc(sizeof(double) * 5 * fk);
+  const int neq = c.neq;
+  double* Fi = (double*)malloc(sizeof(double) * neq * fi);
+  double* Fj = (double*)malloc(sizeof(double) * neq * fj);
+  double* Fk = two_d ? NULL : (double*)malloc(sizeof(double) * neq * fk);
 #pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int64_t kk = 0; kk < nk + 1; kk++) {
-    double flu[5];
+    double flu[6];
     int64_t k = ind[4] + kk;
     for (int64_t jj = 0; jj < nj + 1; jj++)
       for (int64_t ii = 0; ii < ni + 1; ii++) {
         int64_t i = ind[0] + ii, j = ind[2] + jj;
         if (kk < nk && jj < nj) {
           face_flux(&c, 0, i, j, k, flu);
-          for (int v = 0; v < 5; v++) Fi[v * fi + ii + (ni + 1) * (jj + nj * kk)] = flu[v];
+          for (int v = 0; v < neq; v++) Fi[v * fi + ii + (ni + 1) * (jj + nj * kk)] = flu[v];
         }
         if (kk < nk && ii < ni) {
           face_flux(&c, 1, i, j, k, flu);
-          for (int v = 0; v < 5; v++) Fj[v * fj + ii + ni * (jj + (nj + 1) * kk)] = flu[v];
+          for (int v = 0; v < neq; v++) Fj[v * fj + ii + ni * (jj + (nj + 1) * kk)] = flu[v];
         }
         if (!two_d && jj < nj && ii < ni) {
           face_flux(&c, 2, i, j, k, flu);
-          for (int v = 0; v < 5; v++) Fk[v * fk + ii + ni * (jj + nj * kk)] = flu[v];
+          for (int v = 0; v < neq; v++) Fk[v * fk + ii + ni * (jj + nj * kk)] = flu[v];
         }
       }
   }
@@ -794,7 +1036,7 @@ void or_flux(const int64_t* pi, const double* pr, const int64_t* ind,
         int64_t ai = ii + (ni + 1) * (jj + nj * kk);
         int64_t aj = ii + ni * (jj + (nj + 1) * kk);
         int64_t ak = ii + ni * (jj + nj * kk);
-        for (int v = 0; v < 5; v++) {
+        for (int v = 0; v < neq; v++) {
           double x = drodm[l + v * nd];
           if (!two_d) x = x + Fk[v * fk + ak];
           x = x + Fj[v * fj + aj];
@@ -827,6 +1069,9 @@ void or_core3ark3(const int64_t* pi, const double* pr, int nitcfg, const int64_t
     else if (nitcfg == 3) coefW = cgamma3;
   }
   int two_d = pi[ITYPZONE] == 3;
+  const int sa = pi[NEQ] == 6;
+  const double cmus1 = pr[CS], temp01 = 1. / pr[TEMP0];
+  const double coesut = pr[XMUL0] * (1. + cmus1 * temp01);
 #pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int64_t k = ind[4]; k <= ind[5]; k++)
     for (int64_t j = ind[2]; j <= ind[3]; j++)
@@ -847,6 +1092,14 @@ void or_core3ark3(const int64_t* pi, const double* pr, int nitcfg, const int64_t
           rop_1[l + 4 * nd] = (roe_old + tab5) * r_1 * cvinv -
               cvinv2 * (rop_1[l + nd] * rop_1[l + nd] + rop_1[l + 2 * nd] * rop_1[l + 2 * nd] +
                         rop_1[l + 3 * nd] * rop_1[l + 3 * nd]);
+          if (sa) {   /* core3ark3.for:188-236: nutilde limited to [0, ratiom nu_lam] */
+            double tab6 = drodm[l + 5 * nd] * (coefW * coe[l]);
+            double anulam = sa_mulam(coesut, temp01, cmus1, rop_1[l + 4 * nd]);
+            anulam = anulam * r_1 * pr[SA_RATIOM_R];
+            double t6 = (ro_old * rop[l + 5 * nd] + tab6) * r_1;
+            t6 = OMIN(t6, anulam);
+            rop_1[l + 5 * nd] = OMAX(t6, 0.);
+          }
         } else {
           rop_1[l + 3 * nd] = 0.;
           double roe_old = ro_old * (cv * t_old + 0.5 * (u_old * u_old + v_old * v_old));
@@ -869,6 +1122,7 @@ void or_core3as2(const int64_t* pi, const double* pr, int nitcfg, int first_it,
   if (first_it == 0 || pi[DTLOC] == 1) { c1 = -1.; c2 = 1.; c3 = 0.; }
   else { c1 = -1.5; c2 = 2.; c3 = -0.5; }
   int two_d = pi[ITYPZONE] == 3;
+  const int sa = pi[NEQ] == 6;
   double c4 = c1 + c2;
 #pragma omp parallel for num_threads(g_threads) schedule(static)
   for (int64_t k = ind[4]; k <= ind[5]; k++)
@@ -893,6 +1147,10 @@ void or_core3as2(const int64_t* pi, const double* pr, int nitcfg, int first_it,
             roe_n1 = m[l] * (cv * m[l + 4 * nd] + 0.5 * (m[l + nd] * m[l + nd] + m[l + 2 * nd] * m[l + 2 * nd]));
           }
           drodm[l + 4 * nd] = cf * drodm[l + 4 * nd] + c4 * roe + c3 * roe_n1;
+          if (sa) {   /* core3as2.for:97-99 */
+            int64_t o = 5 * nd;
+            drodm[l + o] = cf * drodm[l + o] + c4 * a[l + o] * a[l] + c3 * m[l + o] * m[l];
+          }
         } else {
           drodm[l] = cf * drodm[l] + c1 * a[l] + c2 * b[l] + c3 * m[l];
           for (int v = 1; v <= 3; v++) {
@@ -911,6 +1169,10 @@ void or_core3as2(const int64_t* pi, const double* pr, int nitcfg, int first_it,
             roe_n1 = m[l] * (cv * m[l + 4 * nd] + 0.5 * (m[l + nd] * m[l + nd] + m[l + 2 * nd] * m[l + 2 * nd]));
           }
           drodm[l + 4 * nd] = cf * drodm[l + 4 * nd] + c1 * roe + c2 * roe_n + c3 * roe_n1;
+          if (sa) {   /* core3as2.for:187-190 */
+            int64_t o = 5 * nd;
+            drodm[l + o] = cf * drodm[l + o] + c1 * a[l + o] * a[l] + c2 * b[l + o] * b[l] + c3 * m[l + o] * m[l];
+          }
         }
       }
 }
@@ -922,7 +1184,7 @@ void or_core3as2(const int64_t* pi, const double* pr, int nitcfg, int first_it,
 typedef struct {
   const int64_t* pi; const double *rop, *coe, *ti, *tj, *tk;
   int64_t nd, ndm, inc[3], inc_mtr[3];
-  int typ;
+  int typ, neq;
   double gam1, gamm1, cp, gam2;
 } luctx;
 
@@ -930,7 +1192,7 @@ typedef struct {
  * lower sweep, l + inc for the upper).  signe = +-0.5.  For the 3d full /
  * 2d zones the normal is the mean of the neighbour's two faces in d. */
 static void lu_nb(const luctx* c, int d, int64_t l1, int64_t ltnb1, int64_t ltnb2,
-                  double signe, const double* out, double b[5]) {
+                  double signe, const double* out, double b[6]) {
   int64_t nd = c->nd;
   double tcx = 0., tcy = 0., tcz = 0.;
   if (c->typ == 2) {
@@ -945,6 +1207,7 @@ static void lu_nb(const luctx* c, int d, int64_t l1, int64_t ltnb1, int64_t ltnb
   double gam1 = c->gam1, gamm1 = c->gamm1, gam2 = c->gam2;
   double o1 = out[l1], o2 = out[l1 + nd], o3 = out[l1 + 2 * nd], o4 = out[l1 + 3 * nd], o5 = out[l1 + 4 * nd];
   double cs = c->coe[l1 + (d + 1) * nd] * signe;
+  const double o6 = c->neq == 6 ? out[l1 + 5 * nd] : 0.;
   if (c->typ == 2) {
     double q2 = .5 * (u * u + v * v + w * w);
     double h = c->cp * t + q2;
@@ -986,6 +1249,11 @@ static void lu_nb(const luctx* c, int d, int64_t l1, int64_t ltnb1, int64_t ltnb
       b[3] = b41 * o1 + b42 * o2 + b43 * o3 + b44 * o4 + b45 * o5;
       b[4] = b51 * o1 + b52 * o2 + b53 * o3 + b54 * o4 + b55 * o5;
     }
+    /* lu_{i,j,k}_3dcart_SA.for: scalar convection of ro nutilde */
+    if (c->neq == 6) {
+      double qn = d == 0 ? tcx * u : (d == 1 ? tcy * v : tcz * w);
+      b[5] = (qn + cs) * o6;
+    }
     return;
   }
   if (c->typ == 0) { /* lu_{i,j,k}_3dfull.for */
@@ -1003,6 +1271,7 @@ static void lu_nb(const luctx* c, int d, int64_t l1, int64_t ltnb1, int64_t ltnb
     b[2] = b31 * o1 + b32 * o2 + b33 * o3 + b34 * o4 + b35 * o5;
     b[3] = b41 * o1 + b42 * o2 + b43 * o3 + b44 * o4 + b45 * o5;
     b[4] = b51 * o1 + b52 * o2 + b53 * o3 + b54 * o4 + b55 * o5;
+    if (c->neq == 6) b[5] = (qn + cs) * o6;   /* lu_{i,j,k}_3dfull_SA.for */
     return;
   }
   { /* lu_{i,j}_2d.for */
@@ -1032,6 +1301,7 @@ static void mjr_newton(const int64_t* pi, const double* pr, int64_t l, const dou
   double r_1 = 1. / n1;
   double n2 = (ro_old * u_old + out[l + nd]) * r_1;
   double n3 = (ro_old * v_old + out[l + 2 * nd]) * r_1;
+  const double nu_old = pi[NEQ] == 6 ? rop[l + 5 * nd] : 0.;
   if (pi[ITYPZONE] == 3) {
     double roe_old = ro_old * (pr[CVINF] * t_old + 0.5 * (u_old * u_old + v_old * v_old));
     double n5 = (roe_old + out[l + 4 * nd]) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3);
@@ -1042,6 +1312,15 @@ static void mjr_newton(const int64_t* pi, const double* pr, int64_t l, const dou
   double roe_old = ro_old * (pr[CVINF] * t_old + 0.5 * (u_old * u_old + v_old * v_old + w_old * w_old));
   double n5 = (roe_old + out[l + 4 * nd]) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
   rop_1[l] = n1; rop_1[l + nd] = n2; rop_1[l + 2 * nd] = n3; rop_1[l + 3 * nd] = n4; rop_1[l + 4 * nd] = n5;
+  if (pi[NEQ] == 6) {   /* mjr_newton_SA.for */
+    const double cmus1 = pr[CS], temp01 = 1. / pr[TEMP0];
+    const double coesut = pr[XMUL0] * (1. + cmus1 * temp01);
+    double anulam = sa_mulam(coesut, temp01, cmus1, n5);
+    anulam = anulam * r_1 * pr[SA_RATIOM_R];
+    double t6 = (ro_old * nu_old + out[l + 5 * nd]) * r_1;
+    t6 = OMIN(t6, anulam);
+    rop_1[l + 5 * nd] = OMAX(t6, 0.);
+  }
 }
 
 void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind,
@@ -1056,7 +1335,8 @@ void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind,
   c.inc_mtr[0] = pi[NIJK_MTR]; c.inc_mtr[1] = pi[NIJK_MTR + 1]; c.inc_mtr[2] = pi[NIJK_MTR + 2];
   c.gam1 = pr[GAMMA]; c.gamm1 = c.gam1 - 1.; c.cp = pr[GAMMA] * pr[CVINF]; c.gam2 = c.gamm1 - 1.;
   int64_t nd = c.nd;
-  int neq = 5;
+  int neq = (int)pi[NEQ];
+  c.neq = neq;
   int two_d = c.typ == 3;
   /* lower sweep: invlu_l.for, lexicographic k, j, i.  The neighbour terms
    * present at a cell are those whose neighbour lies inside the LU range;
@@ -1067,7 +1347,7 @@ void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind,
       for (int64_t i = ind[0]; i <= ind[1]; i++) {
         int64_t l = inddm(pi, i, j, k), lt = indmtr(pi, i, j, k);
         double xal = coe[l] * 0.5;
-        double x[5], b[5];
+        double x[6], b[6];
         int first = 1;
         int hasj = j > ind[2], hask = (!two_d) && k > ind[4], hasi = i > ind[0];
         int order[2] = {2, 1};
@@ -1086,7 +1366,8 @@ void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind,
         }
         (void)first;
         double diag = 1. / coe[l + 4 * nd];
-        for (int v = 0; v < neq; v++) drodm_out[l + v * nd] = x[v] * diag;
+        for (int v = 0; v < 5; v++) drodm_out[l + v * nd] = x[v] * diag;
+        if (neq == 6) drodm_out[l + 5 * nd] = x[5] / coe[l + 5 * nd];   /* lu_dinv_SA.for */
         if (two_d) drodm_out[l + 3 * nd] = drodm_in[l + 3 * nd] * diag;
       }
   /* upper sweep: invlu_u.for, reverse lexicographic; out = D^-1 (D out_L
@@ -1098,9 +1379,10 @@ void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind,
       for (int64_t i = ind[1]; i >= ind[0]; i--) {
         int64_t l = inddm(pi, i, j, k), lt = indmtr(pi, i, j, k);
         double xal = coe[l] * (-0.5);
-        double x[5], b[5];
+        double x[6], b[6];
         double dg = coe[l + 4 * nd];
-        for (int v = 0; v < neq; v++) x[v] = drodm_out[l + v * nd] * dg;
+        for (int v = 0; v < 5; v++) x[v] = drodm_out[l + v * nd] * dg;
+        if (neq == 6) x[5] = drodm_out[l + 5 * nd] * coe[l + 5 * nd];   /* lu_d_SA.for */
         int hasj = j < ind[3], hask = (!two_d) && k < ind[5], hasi = i < ind[1];
         if (hask) {
           lu_nb(&c, 2, l + c.inc[2], lt + c.inc_mtr[2], lt + 2 * c.inc_mtr[2], -0.5, drodm_out, b);
@@ -1115,7 +1397,8 @@ void or_invlu(const int64_t* pi, const double* pr, const int64_t* ind,
           for (int v = 0; v < neq; v++) x[v] = x[v] + b[v] * xal;
         }
         double diag = 1. / coe[l + 4 * nd];
-        for (int v = 0; v < neq; v++) drodm_out[l + v * nd] = x[v] * diag;
+        for (int v = 0; v < 5; v++) drodm_out[l + v * nd] = x[v] * diag;
+        if (neq == 6) drodm_out[l + 5 * nd] = x[5] / coe[l + 5 * nd];
       }
     if (mjrnewton == 1)
       for (int64_t j = ind[2]; j <= ind[3]; j++)
@@ -1455,6 +1738,8 @@ void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const dou
     const double cvinv = 1. / pr[CVINF];
     const double c4 = 5. / 6., c5 = 2. / 6., c6 = -1. / 6.;
     const double k0 = 1. / c6, k1 = -(c4 + c5) * k0, k2 = -c6 * k0, k3 = (2. - c5 - c4) * k0;
+    const int sa = neq == 6;
+    const double nue = pr[RONUTILDEINF] / pr[ROINF];   /* BCFarfield_init.for: state(6)/state(1) */
     for (int64_t n = 0; n < nb_bc; n++) {
       int64_t pt = pi[pt_bcs + 1 + n];
       int64_t type = pi[pt + BC_TYPE];
@@ -1523,11 +1808,13 @@ void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const dou
               rop[l] = rop[ldjr];
               rop[l + nd] = 0. + ua; rop[l + 2 * nd] = 0. + va; rop[l + 3 * nd] = 0. + wa;
               rop[l + 4 * nd] = rop[ldjr + 4 * nd];
+              if (sa) rop[l + 5 * nd] = rop[ldjr + 5 * nd];   /* BCWallInviscidSA_*.for */
             } else if (noslip) {    /* BCWallViscous.for (adiabatic) */
               double u = rop[ldjr + nd], v = rop[ldjr + 2 * nd], w = rop[ldjr + 3 * nd];
               rop[l] = rop[ldjr];
               rop[l + nd] = 0. - u; rop[l + 2 * nd] = 0. - v; rop[l + 3 * nd] = 0. - w;
               rop[l + 4 * nd] = rop[ldjr + 4 * nd];
+              if (sa) rop[l + 5 * nd] = -rop[ldjr + 5 * nd];  /* BCWallViscous_SA.for */
             } else if (rank == 0 && (type == 1 || type == 13)) {   /* BCFarfield.for / BCInflow_i.for */
               double tn[3] = {t[0] * snorm, t[1] * snorm, t[2] * snorm};
               nr_out o;
@@ -1538,6 +1825,8 @@ void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const dou
               rop[l] = o.svar[0];
               rop[l + nd] = u; rop[l + 2 * nd] = v; rop[l + 3 * nd] = w;
               rop[l + 4 * nd] = (o.qvar5 * roinv - .5 * (u * u + v * v + w * w)) * cvinv;
+              /* BCFarfield_firstrank_SA.for (eigv1 = qn) / BCInflow_firstrank_SA.for */
+              if (sa) rop[l + 5 * nd] = (type == 13 || o.qn < 0.) ? nue : rop[l1 + 5 * nd];
             } else if (rank == 0 && type == 10) {                  /* BCOutflow.for */
               double roe = rop[l1], rue = rop[l1 + nd] * roe, rve = rop[l1 + 2 * nd] * roe,
                      rwe = rop[l1 + 3 * nd] * roe;
@@ -1558,22 +1847,25 @@ void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const dou
               }
               rop[l + 4 * nd] = (o.qvar5 * roinv - .5 * (rop[l + nd] * rop[l + nd] + rop[l + 2 * nd] * rop[l + 2 * nd] +
                                                          rop[l + 3 * nd] * rop[l + 3 * nd])) * cvinv;
+              if (sa) rop[l + 5 * nd] = rop[l1 + 5 * nd];   /* BCOutflow_firstrank_SA.for */
             } else if (type == 1 || type == 13) {  /* BC_nextrank.for */
               int64_t inc = d == 0 ? 1 : (d == 1 ? pi[NIJK] : pi[NIJK] * pi[NIJK + 1]);
               int64_t dl = -step * inc;            /* towards the interior */
               int64_t q0 = l + dl, q1 = l + 2 * dl, q2 = l + 3 * dl;
               rop[l] = rop[q0] * k3 + rop[q1] * k1 + rop[q2] * k2;
-              if (fabs(rop[l] / rop[q0] - 1.) >= 0.7) {
-                for (int v = 0; v < 5; v++) rop[l + v * nd] = rop[q0 + v * nd];
+              /* BC_nextrankSA.for tests ro <= 0.3 ro0 instead */
+              int keep = sa ? rop[l] <= 0.3 * rop[q0] : fabs(rop[l] / rop[q0] - 1.) >= 0.7;
+              if (keep) {
+                for (int v = 0; v < neq; v++) rop[l + v * nd] = rop[q0 + v * nd];
               } else {
-                for (int v = 1; v < 5; v++)
+                for (int v = 1; v < neq; v++)
                   rop[l + v * nd] = rop[q0 + v * nd] * k3 + rop[q1 + v * nd] * k1 + rop[q2 + v * nd] * k2;
               }
             } else if (type == 10) {                /* BC_extrap.for: copy of the first ghost */
               int64_t cf[3] = {c[0], c[1], c[2]};
               cf[d] = first;
               int64_t q0 = inddm(pi, cf[0], cf[1], cf[2]);
-              for (int v = 0; v < 5; v++) rop[l + v * nd] = rop[q0 + v * nd];
+              for (int v = 0; v < neq; v++) rop[l + v * nd] = rop[q0 + v * nd];   /* BC_extrap(SA) */
             }
           }
         }
@@ -1778,6 +2070,8 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
         else { ssiter = Z->ro; out = Z->ro_p1; }
         if (nstep == 1) {
           if (pi[IFLOW] == 2) or_invist(pi, pr, implicit ? coe_r : grad_r, ssiter, Z->xmut);
+          /* navier_stokes_struct.for:258-266: SA viscosity on ind_coe */
+          if (pi[IFLOW] == 3) or_vispalart(pi, pr, coe_r, ssiter, Z->xmut);
           if (implicit) {
             or_tstb3_global(pi, pr, coe_r, Z->coe, Z->vol);
             or_tstb3c(pi, pr, *first_it, coe_r, ssiter, Z->coe, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
@@ -1786,6 +2080,11 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
           }
         }
         or_init_rhs(pi, nstep, sdm, Z->drodm);
+        /* src_term.for:86-97: SA source (after the coefficients of the
+         * first sub-step, which coe6 reads) */
+        if (pi[IFLOW] == 3)
+          or_spsource(pi, pr, nstep, sdm, ssiter, Z->coe, Z->ti, Z->tj, Z->tk, Z->vol,
+                      Z->xmut + pi[NDIMDX], Z->drodm);
         /* src_term.for:257-266: senseur wiggle on the first sub-step */
         if (pi[KFLUDOM] == 2 && nstep == 1) or_wiggle(pi, sdm, ssiter, Z->wig);
         or_flux(pi, pr, sdm, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol, Z->wig);

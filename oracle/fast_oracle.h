@@ -35,7 +35,8 @@ typedef struct {
   double* ro;     /* time level n   (primitive: ro,u,v,w,T[,nutilde])     */
   double* ro_m1;  /* time level n-1                                        */
   double* ro_p1;  /* time level n+1 / RK work array (rop_tmp)              */
-  double* xmut;   /* laminar (+turbulent) viscosity, NDIMDX                */
+  double* xmut;   /* laminar (+turbulent) viscosity, NDIMDX; with SA        */
+                  /* (IFLOW 3) followed by the wall distance, 2*NDIMDX     */
   double* drodm;  /* residual / increment, NEQ*NDIMDX                      */
   double* coe;    /* dt/vol, spectral radii, LU diagonal: NEQ_COE*NDIMDX   */
   const double* ti; const double* tj; const double* tk; const double* vol;
@@ -57,6 +58,14 @@ void or_set_lu_tiles(int n);
 /* individual kernels (ind = 6 Fortran indices imin,imax,jmin,jmax,kmin,kmax) */
 void or_invist(const int64_t* pi, const double* pr, const int64_t* ind,
                const double* rop, double* xmut);
+/* SA/vispalart.for: SA eddy viscosity (IFLOW 3) */
+void or_vispalart(const int64_t* pi, const double* pr, const int64_t* ind,
+                  const double* rop, double* xmut);
+/* SA/spsource_SA.for: SA source term into drodm(:,6), coe(:,6) when
+ * implicit on the first sub-step; dist = wall distance (NDIMDX) */
+void or_spsource(const int64_t* pi, const double* pr, int nitcfg, const int64_t* ind,
+                 const double* rop, double* coe, const double* ti, const double* tj,
+                 const double* tk, const double* vol, const double* dist, double* drodm);
 void or_tstb3_global(const int64_t* pi, const double* pr, const int64_t* ind,
                      double* coe, const double* vol);
 void or_tstb3c(const int64_t* pi, const double* pr, int first_it, const int64_t* ind,

@@ -93,8 +93,12 @@ class Case:
                      tk=np.ascontiguousarray(zd["tk"], dtype=np.float64),
                      vol=np.ascontiguousarray(zd["vol"], dtype=np.float64),
                      lv=[np.array(zd[k], dtype=np.float64).reshape(-1) for k in ("ro", "ro_m1", "ro_p1")],
-                     xmut=np.zeros(nd), drodm=np.zeros(neq * nd), coe=np.zeros(5 * nd),
+                     xmut=np.zeros(2 * nd), drodm=np.zeros(neq * nd), coe=np.zeros(neq * nd),
                      rdm=np.zeros(nss * neq * 2 * nlu), wig=np.zeros(3 * nd))
+            if neq == 6:
+                # Spalart-Allmaras: the wall distance follows the viscosity
+                # (navier_stokes_struct passes xmut(1+NDIMDX) as dist)
+                e["xmut"][nd:] = np.asarray(zd["dist"], dtype=np.float64).reshape(-1)
             self.z.append(e)
         self.tr = [dict(dnr=int(t["dnr"]), rcv=int(t["rcv"]),
                         dnr_idx=np.ascontiguousarray(t["dnr_idx"], dtype=np.int64),

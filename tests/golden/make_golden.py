@@ -49,6 +49,13 @@ def specs():
             lambda: cases.bc_box(n=(12, 10, 6), wall="BCWallViscous", model="NSLaminar", wavy=0.3,
                                  temporal="implicit", ss_iteration=3, time_step=0.05,
                                  reynolds=500.0), 2, 4, 1),
+        "bcbox_sa_rk3": (
+            lambda: cases.bc_box(n=(12, 10, 6), wall="BCWallViscous", model="NSTurbulent",
+                                 temporal="explicit", time_step=0.02, reynolds=500.0), 3, 3, 1000),
+        "bcbox_sa_wavy_lusgs": (
+            lambda: cases.bc_box(n=(12, 10, 6), wall="BCWallViscous", model="NSTurbulent", wavy=0.3,
+                                 temporal="implicit", ss_iteration=3, time_step=0.05,
+                                 reynolds=500.0), 2, 4, 1),
     }
 
 
@@ -87,7 +94,7 @@ def positions(size, seed):
 def interior_sums(pi, q):
     ni, nj, nk = (int(pi[0]), int(pi[1]), int(pi[2]))
     ng, ngk = int(pi[3]), int(pi[4])
-    a = q.reshape(5, nk, nj, ni)[:, ngk:nk - ngk, ng:nj - ng, ng:ni - ng]
+    a = q.reshape(int(pi[36]), nk, nj, ni)[:, ngk:nk - ngk, ng:nj - ng, ng:ni - ng]
     return a.sum(axis=(1, 2, 3))
 
 

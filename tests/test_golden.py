@@ -51,6 +51,8 @@ def test_gpu_reproduces_golden(golden, name):
     s = Solver(0)
     z = zd[0]
     s.add_zone(z["pi"], z["pr"], z["ti"], z["tj"], z["tk"], z["vol"])
+    if "dist" in z:
+        s.set_wall_distance(0, z["dist"])
     s.set_option("modulo_verif", mv)
     for lvl, key in enumerate(("ro", "ro_m1", "ro_p1")):
         s.upload(0, lvl, z[key])

@@ -22,8 +22,10 @@ def _pair(t, oracle_mod, modulo_verif):
     ref.apply_bc(0)
     ref.apply_bc(1)
     s = Solver(0)
-    for z in zd:
+    for n, z in enumerate(zd):
         s.add_zone(z["pi"], z["pr"], z["ti"], z["tj"], z["tk"], z["vol"])
+        if "dist" in z:
+            s.set_wall_distance(n, z["dist"])
     s.set_option("modulo_verif", modulo_verif)
     for n, z in enumerate(zd):
         for lvl, key in enumerate(("ro", "ro_m1", "ro_p1")):
@@ -85,7 +87,7 @@ def test_implicit_lusgs_step(oracle_mod, scheme, slope, n):
     coe = s.work(0, "coe", 5 * nd).reshape(5, nd)
     assert rel_err(coe[:, mask], ref.z[0]["coe"].reshape(5, nd)[:, mask]) <= TOL
     xm = s.work(0, "xmut", nd)
-    assert rel_err(xm[mask], ref.z[0]["xmut"][mask]) <= TOL
+    assert rel_err(xm[mask], ref.z[0]["xmut"][:nd][mask]) <= TOL
     nss = int(pi[58])
     got = s.residuals(0)
     exp = ref.residual_norms(0, nss)
@@ -386,4 +388,98 @@ def test_2d_bcs(oracle_mod, scheme, slope, temporal):
         ref.compute(it, 1, nfin, 1, modulo_verif=mv)
         s.compute(it, 1, nfin, 1, 1)
     _check_levels(ref, s)
+    s.close()
+
+
+@pytest.mark.parametrize("wall,wavy", [("BCWallViscous", 0.0), ("BCWallViscous", 0.3),
+                                       ("BCWallInviscid", 0.3)])
+def test_spalart_allmaras_explicit(oracle_mod, wall, wavy):
+    """Spalart-Allmaras RK3 steps with inflow / outflow / wall / farfield:
+    AUSM+(P) flux of ro nutilde, nutilde diffusion, the source term of
+    spsource_SA.for, the clipped update and the SA ghost fill."""
+    t = cases.bc_box(n=(16, 12, 6), model="NSTurbulent", wall=wall, wavy=wavy,
+                     temporal="explicit", reynolds=500.0, time_step=0.02)
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    pi = zd[0]["pi"]
+    assert int(pi[36]) == 6
+    for lvl in range(2):
+        assert rel_err(s.download(0, lvl), ref.z[0]["lv"][lvl]) <= TOL
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    nd = int(pi[41])
+    mask = _interior_mask(pi)
+    xm = s.work(0, "xmut", nd)
+    assert rel_err(xm[mask], ref.z[0]["xmut"][:nd][mask]) <= TOL
+    s.close()
+
+
+@pytest.mark.parametrize("wavy", [0.0, 0.3])
+def test_spalart_allmaras_implicit(oracle_mod, wavy):
+    """Spalart-Allmaras with LU-SGS: coe6 from the source Jacobian, the
+    sixth row of the sweeps (lu_*_SA.for), mjr_newton_SA.for."""
+    t = cases.bc_box(n=(12, 10, 6), model="NSTurbulent", wavy=wavy, temporal="implicit",
+                     ss_iteration=3, reynolds=500.0, time_step=0.05)
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
+    pi = zd[0]["pi"]
+    nd = int(pi[41])
+    mask = _interior_mask(pi)
+    coe = s.work(0, "coe", 6 * nd).reshape(6, nd)
+    assert rel_err(coe[:, mask], ref.z[0]["coe"].reshape(6, nd)[:, mask]) <= TOL
+    nss = int(pi[58])
+    assert rel_err(s.residuals(0), ref.residual_norms(0, nss)) <= TOL
+    s.close()
+
+
+def test_spalart_allmaras_periodic_lusgs_plane_launches(oracle_mod):
+    """Periodic SA box, persistent sweeps and one launch per hyperplane."""
+    t = cases.taylor_green(n=(10, 9, 8), ss_iteration=3, model="NSTurbulent", wall_distance=2.0)
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    s.set_option("lu_mode", 0)
+    for it in range(1, 3):
+        ref.compute(it, 1, 4, 1, modulo_verif=1)
+        s.compute(it, 1, 4, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
+def test_spalart_allmaras_mixed_precision(oracle_mod):
+    """FP32 sweeps with the sixth equation: contraction and FP32-level error."""
+    t = cases.bc_box(n=(16, 12, 8), model="NSTurbulent", temporal="implicit", ss_iteration=5,
+                     reynolds=500.0, time_step=0.05)
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    s.set_option("lu_precision", 32)
+    ref.compute(1, 1, 6, 1, modulo_verif=1)
+    s.compute(1, 1, 6, 1, 1)
+    s.synchronize()
+    r = s.residuals(0)
+    assert np.all(r[:6, -1] < r[:6, 0])
+    nd = int(zd[0]["pi"][41])
+    mask = _interior_mask(zd[0]["pi"])
+    got = s.download(0, 0).reshape(6, nd)[:, mask]
+    exp = ref.z[0]["lv"][0].reshape(6, nd)[:, mask]
+    scale = np.max(np.abs(exp), axis=1, keepdims=True)
+    assert np.max(np.abs(got - exp) / scale) < 1e-5
+    s.close()
+
+
+def test_spalart_allmaras_refusals():
+    """Unsupported SA combinations are reported, never run: Roe + SA, and a
+    compute before the wall distance is given."""
+    from fast_gb300._native import Solver, FastGB300Error
+    t = cases.bc_box(n=(8, 8, 6), model="NSTurbulent", scheme="roe", temporal="explicit")
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    s = Solver(0)
+    with pytest.raises(FastGB300Error, match="AUSM"):
+        s.add_zone(zd[0]["pi"], zd[0]["pr"], zd[0]["ti"], zd[0]["tj"], zd[0]["tk"], zd[0]["vol"])
+    t = cases.bc_box(n=(8, 8, 6), model="NSTurbulent", temporal="explicit")
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    s.add_zone(zd[0]["pi"], zd[0]["pr"], zd[0]["ti"], zd[0]["tj"], zd[0]["tk"], zd[0]["vol"])
+    with pytest.raises(FastGB300Error, match="wall distance"):
+        s.compute(1, 1, 3, 1, 1)
     s.close()
