@@ -54,6 +54,9 @@ def parse():
                    help="time to a 1e-10 Newton residual drop, FP64 vs mixed sweeps")
     p.add_argument("--ttc-n", type=int, default=256)
     p.add_argument("--ttc-max", type=int, default=100, help="max sub-iterations per step")
+    p.add_argument("--workload", default="tgv", choices=["tgv", "channel", "batch"],
+                   help="tgv: the headline 256^3 case; channel: 48-block SA channel; "
+                        "batch: 64 independent Taylor-Green cases")
     p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
                    help="64: plain FP64 path; 32: FP32 LU-SGS sweeps (mixed precision)")
     return p.parse_args()
@@ -326,6 +329,57 @@ def run_ours(args, d: Dist):
         print(json.dumps(line), flush=True)
 
 
+def run_multizone(args):
+    """Multi-zone workloads on one GPU, one solver: the 48-block Spalart-
+    Allmaras channel (2.1 M cells, 1-to-1 interfaces) or 64 independent
+    Taylor-Green cases (48^3..96^3).  Zones run one after another within each
+    sub-step; interfaces and BCs are filled after every sub-step.  Value =
+    interior cells of all zones x physical steps / device time."""
+    import numpy as np
+    from fast_gb300 import cases, fasts
+    if args.workload == "channel":
+        t, tc = cases.sa_channel(ss_iteration=args.ss, modulo_verif=200)
+        name = f"sa_channel_48_blocks_ausmpred_o3_implicit_lusgs_ss{args.ss}"
+    else:
+        t, _ = cases.tgv_batch(ss_iteration=args.ss, modulo_verif=200)
+        tc = None
+        name = f"tgv_batch_64_cases_ausmpred_o3_implicit_lusgs_ss{args.ss}"
+    t, tc, metrics = fasts.warmup(t, tc, gpu_resident=True)
+    s = fasts.HOOK["solver"]
+    s.set_option("lu_precision", args.lu_precision)
+    cells = sum(int(np.prod(z[1][:, 0] - 1 - 4)) for z in fasts.HOOK["zones"])
+    it = 1
+    for _ in range(args.warmup):
+        fasts._compute(t, metrics, it)
+        it += 1
+    s.synchronize()
+    clocks = Clocks(0)
+    l0 = s.launch_count()
+    clocks.start()
+    s.timer_start()
+    for _ in range(args.steps):
+        fasts._compute(t, metrics, it)
+        it += 1
+    ms = s.timer_stop()
+    clk = clocks.stop()
+    launches = s.launch_count() - l0
+    s.set_option("profile", 1)
+    s.kernel_stats(reset=True)
+    fasts._compute(t, metrics, it)
+    stats = s.kernel_stats(reset=True)
+    s.set_option("profile", 0)
+    line = {"metric": METRIC, "value": cells * args.steps / (ms * 1e-3) / 1e6, "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64" if args.lu_precision == 64 else "f64+f32-sweeps", "data": "synthetic",
+            "config": {"workload": name, "zones": len(fasts.HOOK["zones"]), "cells": cells,
+                       "lu_precision": args.lu_precision, "sub_iterations": args.ss},
+            "clocks": clk, "gpu_launches": launches,
+            "kernel_ms_per_step": {k: v[1] for k, v in stats.items()}}
+    print(json.dumps(line), flush=True)
+
+
 def run_ttc(args):
     """Time to a 1e-10 drop of the Newton residual within one physical step.
 
@@ -389,6 +443,9 @@ def main():
     args = parse()
     if args.ttc:
         run_ttc(args)
+        return
+    if args.workload != "tgv" and args.impl == "ours":
+        run_multizone(args)
         return
     d = Dist()
     try:

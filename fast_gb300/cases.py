@@ -241,3 +241,227 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
             "cache_blocking_I": 1000000, "cache_blocking_J": 1000000, "cache_blocking_K": 1000000}
     return _tree([z], model, numb, numz, mach, reynolds if model != "Euler" else 0.0, gamma=gamma,
                  nutilde_ratio=nutilde_ratio)
+
+
+# ------------------------------------------------- multi-block SA channel
+def _tanh_both_ends(n, first):
+    """Vertex parameters s_0..s_n of [0, 1] clustered at both ends by
+    s = (1 + tanh(d (eta - 1/2)) / tanh(d / 2)) / 2, d chosen (bisection) so
+    that the first spacing s_1 equals `first` (uniform if that needs d <= 0)."""
+    def s1(d):
+        return 0.5 * (1.0 + math.tanh(d * (1.0 / n - 0.5)) / math.tanh(0.5 * d))
+    eta = np.arange(n + 1) / n
+    lo, hi = 1e-9, 200.0
+    if s1(lo) <= first:
+        return eta
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if s1(mid) > first:
+            lo = mid
+        else:
+            hi = mid
+    d = 0.5 * (lo + hi)
+    return 0.5 * (1.0 + np.tanh(d * (eta - 0.5)) / math.tanh(0.5 * d))
+
+
+def sa_channel(nblocks=(4, 3, 4), sizes=((16, 96), (16, 64), (16, 32)), seed=2024, mach=0.3,
+               reynolds=1.0e5, bump=0.1, first_cell=1.0e-4, length=(4.0, 1.0, 1.0),
+               nutilde_ratio=3.0, perturb=1.0e-3, temporal="implicit", ss_iteration=4,
+               time_step=0.01, modulo_verif=1, skew=0.2, parts=None, model="NSTurbulent",
+               wall="BCWallViscous"):
+    """Multi-block Spalart-Allmaras channel: a seeded random box decomposition
+    (nblocks = blocks per direction, 4 x 3 x 4 = 48; block sizes drawn
+    uniformly in `sizes` per direction) of a channel [0, Lx] x [y_w, H]
+    x [0, Lz], H = 1, with a sin^2 bump y_w = bump H sin^2(pi (x - 1))
+    (3/4 + cos(2 pi z / Lz) / 4) on x in [1, 2], wall-normal tanh stretching
+    at both walls (first cell
+    first_cell x H), uniform in x and z.  Inflow (BCInflow) at imin, outflow
+    (BCOutflow) at imax, no-slip walls (BCWallViscous) at jmin / jmax,
+    periodic in z; every block face inside the channel (and the z period) is
+    a 1-to-1 matching interface.  Free stream Mach `mach`, Re_H = reynolds,
+    AUSM+(P) o3, ro nutilde = nutilde_ratio x mu, plus a seeded density
+    perturbation of relative size `perturb`.  The x of every vertex is
+    shifted by skew x (x step) x sin(2 pi z / Lz), so that no block is
+    homogeneous in k (all are general 3-d zones).  The wall distance is the
+    vertical distance to the nearer wall.
+
+    `parts` (three lists of block sizes) overrides the random decomposition,
+    e.g. one block per direction for the single-block version of the same
+    mesh and initial field; `model` / `wall` select Euler with slip walls.
+
+    Returns (t, tc): tc = 1-to-1 transfer lists (dicts dnr, rcv, dnr_idx,
+    rcv_idx; receiver ghost cells of the face bands <- donor interior cells)."""
+    rng = np.random.default_rng(seed)
+    if parts is None:
+        parts = [rng.integers(lo, hi + 1, size=nb) for nb, (lo, hi) in zip(nblocks, sizes)]
+    parts = [np.asarray(q, dtype=np.int64) for q in parts]
+    nblocks = tuple(len(q) for q in parts)
+    offs = [np.concatenate([[0], np.cumsum(p)]) for p in parts]
+    NI, NJ, NK = (int(o[-1]) for o in offs)
+    Lx, H, Lz = length
+    ng = NG
+    s = _tanh_both_ends(NJ, first_cell)
+    # ghost vertices: linear extrapolation in i (uniform x) and j, periodic in k
+    jj = np.arange(-ng, NJ + ng + 1)
+    sj = np.empty(jj.size)
+    inner = (jj >= 0) & (jj <= NJ)
+    sj[inner] = s[jj[inner]]
+    lowj, highj = jj < 0, jj > NJ
+    sj[lowj] = s[0] + jj[lowj] * (s[1] - s[0])
+    sj[highj] = s[NJ] + (jj[highj] - NJ) * (s[NJ] - s[NJ - 1])
+
+    def ywall(x, z):
+        span = 0.75 + 0.25 * np.cos(2.0 * math.pi * z / Lz)
+        return np.where((x >= 1.0) & (x <= 2.0),
+                        bump * H * np.sin(math.pi * (x - 1.0)) ** 2 * span, 0.0)
+
+    gamma = 1.4
+    mu = mach / reynolds
+    # density perturbation on the global cell grid (ghosts included), so that
+    # every decomposition of the same mesh starts from the same field
+    noise = np.random.default_rng(seed + 1).standard_normal((NI + 2 * ng, NJ + 2 * ng, NK + 2 * ng))
+    zones, tc = [], []
+    for c in range(nblocks[2]):
+        for b in range(nblocks[1]):
+            for a in range(nblocks[0]):
+                n = (int(parts[0][a]), int(parts[1][b]), int(parts[2][c]))
+                o = (int(offs[0][a]), int(offs[1][b]), int(offs[2][c]))
+                ii = o[0] + np.arange(-ng, n[0] + ng + 1)
+                kk = o[2] + np.arange(-ng, n[2] + ng + 1)
+                x1 = Lx * ii / NI
+                s1 = sj[o[1]:o[1] + n[1] + 2 * ng + 1]
+                z1 = Lz * kk / NK
+                shape = (ii.size, s1.size, kk.size)
+                X = np.broadcast_to(x1[:, None, None] + skew * (Lx / NI) *
+                                    np.sin(2.0 * math.pi * z1 / Lz)[None, None, :], shape)
+                yw = ywall(X, z1[None, None, :])   # the wall under the vertices' own x
+                Y = np.broadcast_to(yw + (H - yw) * s1[None, :, None], shape)
+                Z = np.broadcast_to(z1[None, None, :], shape)
+                z = I.newZone("blk%02d_%d_%d_%d" % (len(zones), a, b, c), list(X.shape))
+                gc = I.createChild(z, "GridCoordinates", "GridCoordinates_t")
+                for nm, arr in (("CoordinateX", X), ("CoordinateY", Y), ("CoordinateZ", Z)):
+                    I.createChild(gc, nm, "DataArray_t")[1] = np.asfortranarray(arr)
+                I.createChild(z, "Rind", "Rind_t", np.array([ng] * 6, dtype=np.int64))
+                xc, yc, zc = cell_centers(z)
+                ro = 1.0 + perturb * noise[o[0]:o[0] + n[0] + 2 * ng, o[1]:o[1] + n[1] + 2 * ng,
+                                           o[2]:o[2] + n[2] + 2 * ng]
+                u = mach + 0.0 * xc
+                p = 1.0 / gamma + 0.0 * xc
+                set_conservative(z, ro, u, 0.0 * xc, 0.0 * xc, p, gamma)
+                if model == "NSTurbulent":
+                    dist = np.minimum(np.abs(yc - ywall(xc, zc)), np.abs(H - yc))
+                    set_spalart(z, nutilde_ratio * mu / ro, dist)
+                if a == 0:
+                    add_bc(z, "in", "BCInflow", "imin")
+                if a == nblocks[0] - 1:
+                    add_bc(z, "out", "BCOutflow", "imax")
+                if b == 0:
+                    add_bc(z, "wall_lo", wall, "jmin")
+                if b == nblocks[1] - 1:
+                    add_bc(z, "wall_hi", wall, "jmax")
+                zones.append((z, (a, b, c), n, o))
+    # 1-to-1 interfaces: the two ghost layers of every inner face (and the z
+    # period) from the neighbour block's interior cells
+    index = {blk: m for m, (_, blk, _, _) in enumerate(zones)}
+
+    def inddm0(n, i, j, k):   # 0-based natural index of Fortran cell (i, j, k)
+        nip, njp = n[0] + 2 * ng, n[1] + 2 * ng
+        return (i + ng - 1) + (j + ng - 1) * nip + (k + ng - 1) * nip * njp
+
+    for r, (_, blk, n, o) in enumerate(zones):
+        for d in range(3):
+            for side in (-1, 1):
+                nb = list(blk)
+                nb[d] += side
+                if d == 2:
+                    nb[2] %= nblocks[2]
+                elif not 0 <= nb[d] < nblocks[d]:
+                    continue   # physical boundary
+                dn = zones[index[tuple(nb)]][2]
+                rcv, dnr = [], []
+                t1, t2 = [e for e in range(3) if e != d]
+                for m in (1, 2):
+                    for q2 in range(1, n[t2] + 1):
+                        for q1 in range(1, n[t1] + 1):
+                            cr = [0, 0, 0]
+                            cr[t1], cr[t2] = q1, q2
+                            cr[d] = 1 - m if side < 0 else n[d] + m
+                            cd = list(cr)
+                            cd[d] = dn[d] + 1 - m if side < 0 else m
+                            rcv.append(inddm0(n, *cr))
+                            dnr.append(inddm0(dn, *cd))
+                tc.append(dict(dnr=index[tuple(nb)], rcv=r, dnr_idx=np.array(dnr, dtype=np.int64),
+                               rcv_idx=np.array(rcv, dtype=np.int64)))
+    numb = {"temporal_scheme": temporal, "ss_iteration": ss_iteration,
+            "modulo_verif": modulo_verif}
+    numz = {"scheme": "ausmpred", "slope": "o3", "time_step": time_step,
+            "cache_blocking_I": 1000000, "cache_blocking_J": 1000000, "cache_blocking_K": 1000000}
+    t = _tree([z for z, _, _, _ in zones], model, numb, numz, mach,
+              reynolds if model != "Euler" else 0.0, gamma=gamma, nutilde_ratio=nutilde_ratio)
+    return t, tc
+
+
+def channel_blocks(t):
+    """(zone index, (i0, j0, k0) global offset, (ni, nj, nk)) of the blocks
+    of a sa_channel tree, in zone order, from the zone names and sizes."""
+    out = []
+    zs = I.getZones(t)
+    dims = [tuple(int(v) - 1 - 2 * NG for v in z[1][:, 0]) for z in zs]
+    pos = [tuple(int(q) for q in z[0].split("_")[1:]) for z in zs]
+    nb = [max(p[d] for p in pos) + 1 for d in range(3)]
+    size = [[0] * nb[d] for d in range(3)]
+    for p, n in zip(pos, dims):
+        for d in range(3):
+            size[d][p[d]] = n[d]
+    offs = [np.concatenate([[0], np.cumsum(sz)]) for sz in size]
+    for m, (p, n) in enumerate(zip(pos, dims)):
+        out.append((m, tuple(int(offs[d][p[d]]) for d in range(3)), n))
+    return out
+
+
+# ------------------------------------------- many independent Taylor-Green
+def tgv_batch(ncases=64, sizes=(48, 64, 80, 96), mach=(0.05, 0.3), reynolds=(400.0, 3200.0),
+              perturb=1.0e-3, seed=7, ss_iteration=4, modulo_verif=200, prandtl=0.71):
+    """`ncases` independent Taylor-Green vortices in one tree (one zone each,
+    periodic through BCautoperiod): sizes drawn from `sizes` (cells per side),
+    Mach uniform in `mach`, Re log-uniform in `reynolds`, and seeded
+    initial-phase perturbations (x, y, z phases shifted by perturb x U(-1, 1)
+    times the box length / 2 pi).  Each zone carries its own ReferenceState
+    and time step (acoustic CFL 2); implicit LU-SGS with ss_iteration
+    sub-iterations."""
+    rng = np.random.default_rng(seed)
+    t = I.newCGNSTree()
+    b = I.newCGNSBase("Base", 3, 3, t)
+    I.createChild(b, "FlowEquationSet", "FlowEquationSet_t")
+    I.createChild(I.getNodeFromName1(b, "FlowEquationSet"), "GoverningEquations",
+                  "GoverningEquations_t", "NSLaminar")
+    params = []
+    for c in range(ncases):
+        n = int(rng.choice(sizes))
+        m = float(rng.uniform(*mach))
+        re = float(np.exp(rng.uniform(np.log(reynolds[0]), np.log(reynolds[1]))))
+        ph = perturb * rng.uniform(-1.0, 1.0, size=3)
+        one = taylor_green(n=n, mach=m, reynolds=re, prandtl=prandtl, ss_iteration=ss_iteration,
+                           name="tgv%02d" % c)
+        z = I.getZones(one)[0]
+        if np.any(ph):
+            # shift the initial field's phases (the cell-centred formula of
+            # taylor_green evaluated at x + phase)
+            xc, yc, zc = cell_centers(z)
+            gamma = 1.4
+            xs, ys, zs = xc + ph[0], yc + ph[1], zc + ph[2]
+            u = m * np.sin(xs) * np.cos(ys) * np.cos(zs)
+            v = -m * np.cos(xs) * np.sin(ys) * np.cos(zs)
+            p = 1.0 / gamma + m * m / 16.0 * (np.cos(2 * xs) + np.cos(2 * ys)) * (np.cos(2 * zs) + 2.0)
+            set_conservative(z, p * gamma, u, 0.0 * u, 0.0 * u, p, gamma)
+            sol = I.getNodeFromName1(z, I.__FlowSolutionCenters__)
+            I.getNodeFromName1(sol, "MomentumY")[1] = np.asfortranarray(p * gamma * v)
+            roe = p / (gamma - 1.0) + 0.5 * p * gamma * (u * u + v * v)
+            I.getNodeFromName1(sol, "EnergyStagnationDensity")[1] = np.asfortranarray(roe)
+        ref = I.getNodeFromName1(I.getBases(one)[0], "ReferenceState")
+        z[2].append(ref)
+        b[2].append(z)
+        params.append({"n": n, "mach": m, "reynolds": re, "phase": ph.tolist()})
+    FastC._setNum2Base(t, {"temporal_scheme": "implicit", "ss_iteration": ss_iteration,
+                           "modulo_verif": modulo_verif})
+    return t, params

@@ -124,9 +124,11 @@ class Case:
         lib = load()
         arr, tr = self._structs()
         if self.tr:
-            # transfers act on ro (use_p1=0) or ro_p1 (use_p1=1)
+            # transfers act on ro (use_p1=0) or ro_p1 (use_p1=1); for level
+            # M1 the ro slot is pointed at ro_m1 for the call
             if level == 1:
-                raise ValueError("transfers on level M1 are not used")
+                for s in arr:
+                    s.ro = s.ro_m1
             lib.or_transfers(arr, tr, len(self.tr), 1 if level == 2 else 0)
         for e in self.z:
             lib.or_bc_zone(_i(e["pi"]), _d(e["pr"]), _d(e["ti"]), _d(e["tj"]), _d(e["tk"]), 0,

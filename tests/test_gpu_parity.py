@@ -14,11 +14,11 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-12
 
 
-def _pair(t, oracle_mod, modulo_verif):
+def _pair(t, oracle_mod, modulo_verif, tc=()):
     from fast_gb300._native import Solver
     m = fasts.prepare(t)
     zd = fasts.zone_data(t, m)
-    ref = oracle_mod.Case(zd)
+    ref = oracle_mod.Case(zd, tc)
     ref.apply_bc(0)
     ref.apply_bc(1)
     s = Solver(0)
@@ -26,6 +26,8 @@ def _pair(t, oracle_mod, modulo_verif):
         s.add_zone(z["pi"], z["pr"], z["ti"], z["tj"], z["tk"], z["vol"])
         if "dist" in z:
             s.set_wall_distance(n, z["dist"])
+    for tr in tc:
+        s.add_transfer(tr["dnr"], tr["rcv"], tr["dnr_idx"], tr["rcv_idx"])
     s.set_option("modulo_verif", modulo_verif)
     for n, z in enumerate(zd):
         for lvl, key in enumerate(("ro", "ro_m1", "ro_p1")):
@@ -483,3 +485,65 @@ def test_spalart_allmaras_refusals():
     with pytest.raises(FastGB300Error, match="wall distance"):
         s.compute(1, 1, 3, 1, 1)
     s.close()
+
+
+CHANNEL = dict(sizes=((4, 9), (4, 7), (4, 6)), first_cell=2e-2, reynolds=2000.0)
+
+
+@pytest.mark.parametrize("temporal", ["explicit", "implicit"])
+def test_channel_sa_multiblock(oracle_mod, temporal):
+    """48-block SA channel (uneven general 3-d blocks, 1-to-1 interfaces
+    including the z period, inflow / outflow / no-slip walls)."""
+    kw = dict(CHANNEL, temporal=temporal, ss_iteration=3,
+              time_step=0.004 if temporal == "explicit" else 0.02,
+              modulo_verif=1000 if temporal == "explicit" else 1)
+    t, tc = cases.sa_channel(**kw)
+    zd, ref, s = _pair(t, oracle_mod, kw["modulo_verif"], tc)
+    assert len(zd) == 48
+    nfin = 3 if temporal == "explicit" else 4
+    for it in range(1, 3):
+        ref.compute(it, 1, nfin, 1, modulo_verif=kw["modulo_verif"])
+        s.compute(it, 1, nfin, 1, 1)
+    for m in range(len(zd)):
+        _check_levels(ref, s, zone=m)
+        if temporal == "implicit":
+            nss = int(zd[m]["pi"][58])
+            assert rel_err(s.residuals(m), ref.residual_norms(m, nss)) <= TOL
+    s.close()
+
+
+def test_channel_inviscid_multiblock_equals_single_block():
+    """On the GPU: the 48-block inviscid channel step equals the single-block
+    step of the same mesh, cell for cell."""
+    from fast_gb300._native import Solver
+    kw = dict(CHANNEL, model="Euler", wall="BCWallInviscid", temporal="explicit",
+              time_step=0.004, modulo_verif=1000)
+    t, tc = cases.sa_channel(**kw)
+    blocks = cases.channel_blocks(t)
+    N = [max(o[d] + n[d] for _, o, n in blocks) for d in range(3)]
+    t1, tc1 = cases.sa_channel(parts=[[N[0]], [N[1]], [N[2]]], **kw)
+    out = []
+    for tt, cc in ((t, tc), (t1, tc1)):
+        zd = fasts.zone_data(tt, fasts.prepare(tt))
+        s = Solver(0)
+        for n, z in enumerate(zd):
+            s.add_zone(z["pi"], z["pr"], z["ti"], z["tj"], z["tk"], z["vol"])
+            for lvl, key in enumerate(("ro", "ro_m1", "ro_p1")):
+                s.upload(n, lvl, z[key])
+        for tr in cc:
+            s.add_transfer(tr["dnr"], tr["rcv"], tr["dnr_idx"], tr["rcv_idx"])
+        s.set_option("modulo_verif", 1000)
+        s.apply_bc(0)
+        s.apply_bc(1)
+        for it in range(1, 4):
+            s.compute(it, 1, 3, 1, 1)
+        s.synchronize()
+        G = np.zeros((5, N[2], N[1], N[0]))
+        for m, o, n in cases.channel_blocks(tt):
+            pi = zd[m]["pi"]
+            ni, nj, nk = int(pi[0]), int(pi[1]), int(pi[2])
+            q = s.download(m, 0).reshape(5, nk, nj, ni)[:, 2:-2, 2:-2, 2:-2]
+            G[:, o[2]:o[2] + n[2], o[1]:o[1] + n[1], o[0]:o[0] + n[0]] = q
+        out.append(G)
+        s.close()
+    assert np.array_equal(out[0], out[1])
