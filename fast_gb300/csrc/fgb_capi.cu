@@ -72,13 +72,7 @@ struct ZoneData {
   double* wig = nullptr;            // senseur wiggle flags (KFLUDOM = 2)
   double* dist = nullptr;           // wall distance (Spalart-Allmaras)
   bool dist_set = false;
-  void* luwork = nullptr;           // plane-ordered LU work (FP64-sized)
-  uint32_t* cells = nullptr;        // interior cells by hyperplane
-  int64_t* plane = nullptr;         // plane offsets (device)
-  int32_t* posmap = nullptr;        // natural index -> plane index
-  int32_t* nbl = nullptr;           // lower neighbours in plane order
-  int32_t* nbu = nullptr;           // upper neighbours in plane order
-  std::vector<int64_t> plane_host;  // plane offsets (host)
+  int32_t* posmap = nullptr;        // natural index -> plane index in the zone's LU group
   int64_t n_rdm = 0, ijkv_lu[3] = {1, 1, 1};
   std::vector<GatherList> bcs;
   std::vector<WallCorrList> walls;  // Roe wall-face corrections, in BC order
@@ -89,12 +83,33 @@ struct ZoneData {
 struct Transfer {
   int dnr, rcv; int64_t n; int32_t* dnr_idx; int32_t* rcv_idx;
 };
+// Zones solved by one LU-SGS launch (same zone type and equation count): the
+// plane table over all of them and a ring of zone tables (the state pointers
+// of a solve change every sub-step), copied from pinned host slots.
+struct LuGroupData {
+  std::vector<int> zones;
+  int64_t GG = 0, smax = 0;
+  uint32_t* cells = nullptr;
+  int32_t* zid = nullptr;
+  int64_t* plane = nullptr;
+  std::vector<int64_t> plane_host;
+  int32_t *nbl = nullptr, *nbu = nullptr;
+  void* work = nullptr;
+  static constexpr int NSLOT = 16;
+  LuZone* tab_dev = nullptr;        // NSLOT x nz entries
+  LuZone* tab_host = nullptr;       // pinned, NSLOT x nz entries
+  cudaEvent_t ev[NSLOT] = {};
+  bool ev_used[NSLOT] = {};
+  int slot = 0;
+};
 
 struct fgb_solver {
   int device = 0;
   cudaStream_t st = nullptr;
   std::vector<ZoneData> zones;
   std::vector<Transfer> tr;
+  std::vector<LuGroupData> lu_groups;
+  bool lu_built = false;
   int first_it = 0;
   int modulo_verif = 200;
   int lu_precision = 64;
@@ -479,8 +494,7 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.scratch); cudaFree(Z.drodm); cudaFree(Z.coe); cudaFree(Z.xmut); cudaFree(Z.rdm);
     cudaFree(Z.ti); cudaFree(Z.tj); cudaFree(Z.tk); cudaFree(Z.vol);
     cudaFree(Z.Fi); cudaFree(Z.Fj); cudaFree(Z.Fk);
-    cudaFree(Z.luwork); cudaFree(Z.cells); cudaFree(Z.plane); cudaFree(Z.posmap);
-    cudaFree(Z.nbl); cudaFree(Z.nbu);
+    cudaFree(Z.posmap);
     for (GatherList& g : Z.bcs) {
       cudaFree(g.dst); cudaFree(g.src); cudaFree(g.q0); cudaFree(g.q1); cudaFree(g.q2);
       cudaFree(g.nrm);
@@ -491,6 +505,11 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
   for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
+  for (LuGroupData& g : s->lu_groups) {
+    cudaFree(g.cells); cudaFree(g.zid); cudaFree(g.plane); cudaFree(g.nbl); cudaFree(g.nbu);
+    cudaFree(g.work); cudaFree(g.tab_dev); cudaFreeHost(g.tab_host);
+    for (int i = 0; i < LuGroupData::NSLOT; i++) if (g.ev[i]) cudaEventDestroy(g.ev[i]);
+  }
   cudaFree(s->bar);
   cudaFree(s->derr);
   for (auto& e : s->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
@@ -582,40 +601,10 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   CK(cudaMemset(Z.rdm, 0, sizeof(double) * Z.n_rdm));
   int rc = build_ghost_lists(Z, hti, htj, htk);
   if (rc != FGB_OK) return rc;
-  if (p[ITYPCP] <= 1) {
-    // LU-SGS: cells ordered by hyperplane i+j+k (counting sort), B table
-    if (ni >= 2048 || nj >= 2048 || nk >= 1024 || ni * nj * nk >= (int64_t(1) << 31))
-      return fail(FGB_ERR_ARG, "zone too large for the LU plane table "
-                               "(ni,nj < 2048, nk < 1024, ni*nj*nk < 2^31)");
-    const int64_t np = ni + nj + nk - 2;
-    std::vector<int64_t> off(np + 1, 0);
-    for (int64_t k = 0; k < nk; k++)
-      for (int64_t j = 0; j < nj; j++)
-        for (int64_t i = 0; i < ni; i++) off[i + j + k + 1]++;
-    for (int64_t q = 0; q < np; q++) off[q + 1] += off[q];
-    const int64_t G = ni * nj * nk;
-    std::vector<uint32_t> cells(G);
-    std::vector<int32_t> posmap(nd, -1);
-    std::vector<int64_t> pos(off.begin(), off.end() - 1);
-    for (int64_t k = 0; k < nk; k++)
-      for (int64_t j = 0; j < nj; j++)
-        for (int64_t i = 0; i < ni; i++) {
-          int64_t g = pos[i + j + k]++;
-          cells[g] = (uint32_t)(i | (j << 11) | (k << 22));
-          posmap[idx(p, i + 1, j + 1, k + 1)] = (int32_t)g;
-        }
-    CK(dev_upload(&Z.cells, cells));
-    CK(dev_upload(&Z.plane, off));
-    CK(dev_upload(&Z.posmap, posmap));
-    Z.plane_host = off;
-    CK(cudaMalloc(&Z.nbl, sizeof(int32_t) * 3 * G));
-    CK(cudaMalloc(&Z.nbu, sizeof(int32_t) * 3 * G));
-    CK(cudaMalloc(&Z.luwork, sizeof(double) * G * lusgs_work_words(Z.z.typ)));
-    LuLaunch L0{};
-    L0.G = G; L0.cells = Z.cells; L0.posmap = Z.posmap;
-    CK(launch_lu_neighbours(Z.z, L0, Z.nbl, Z.nbu, s->st));
-    CK(cudaStreamSynchronize(s->st));
-  }
+  if (p[ITYPCP] <= 1 && (ni >= 2048 || nj >= 2048 || nk >= 1024 || ni * nj * nk >= (int64_t(1) << 31)))
+    return fail(FGB_ERR_ARG, "zone too large for the LU plane table "
+                             "(ni,nj < 2048, nk < 1024, ni*nj*nk < 2^31)");
+  s->lu_built = false;   // LU groups are (re)built by the next fgb_compute
   s->zones.push_back(Z);
   if (zone_id) *zone_id = (int)s->zones.size() - 1;
   return FGB_OK;
@@ -790,6 +779,110 @@ int fgb_apply_bc(fgb_solver* s, int level) {
   return ghost_fill(s, level);
 }
 
+static void free_lu_groups(fgb_solver* s) {
+  for (LuGroupData& g : s->lu_groups) {
+    cudaFree(g.cells); cudaFree(g.zid); cudaFree(g.plane); cudaFree(g.nbl); cudaFree(g.nbu);
+    cudaFree(g.work); cudaFree(g.tab_dev); cudaFreeHost(g.tab_host);
+    for (int i = 0; i < LuGroupData::NSLOT; i++) if (g.ev[i]) cudaEventDestroy(g.ev[i]);
+  }
+  s->lu_groups.clear();
+  for (ZoneData& Z : s->zones) { cudaFree(Z.posmap); Z.posmap = nullptr; }
+}
+
+static LuGroup group_launch(fgb_solver* s, LuGroupData& g, LuZone* tab) {
+  LuGroup L{};
+  L.persistent = s->lu_mode;
+  L.fp32 = s->lu_precision == 32;
+  L.bar = s->bar; L.err = s->derr;
+  L.work = g.work; L.GG = g.GG; L.smax = g.smax;
+  L.cells = g.cells; L.zid = g.zid; L.plane = g.plane; L.plane_host = g.plane_host.data();
+  L.nbl = g.nbl; L.nbu = g.nbu; L.ztab = tab; L.nz = (int)g.zones.size();
+  return L;
+}
+
+// LU-SGS groups: the implicit zones of one kind (zone type, equation count)
+// in order of creation.  The group's plane table orders its cells by
+// hyperplane, then zone, then (k, j) -- within one zone and one plane the
+// order in which invlu_l.for meets them.
+static int build_lu_groups(fgb_solver* s) {
+  CK(cudaStreamSynchronize(s->st));
+  free_lu_groups(s);
+  for (int m = 0; m < (int)s->zones.size(); m++) {
+    ZoneData& Z = s->zones[m];
+    if (Z.pi[ITYPCP] > 1) continue;
+    LuGroupData* g = nullptr;
+    for (LuGroupData& h : s->lu_groups) {
+      const Zone& z0 = s->zones[h.zones[0]].z;
+      if (z0.typ == Z.z.typ && z0.neq == Z.z.neq) g = &h;
+    }
+    if (!g) { s->lu_groups.emplace_back(); g = &s->lu_groups.back(); }
+    g->zones.push_back(m);
+  }
+  for (LuGroupData& g : s->lu_groups) {
+    const int nz = (int)g.zones.size();
+    g.smax = 0;
+    for (int q : g.zones) {
+      const Zone& z = s->zones[q].z;
+      g.smax = std::max<int64_t>(g.smax, z.ni + z.nj + z.nk - 3);
+    }
+    const int64_t np = g.smax + 1;
+    std::vector<int64_t> cnt((size_t)(np * nz), 0);
+    for (int q = 0; q < nz; q++) {
+      const Zone& z = s->zones[g.zones[q]].z;
+      for (int64_t k = 0; k < z.nk; k++)
+        for (int64_t j = 0; j < z.nj; j++)
+          for (int64_t i = 0; i < z.ni; i++) cnt[(size_t)((i + j + k) * nz + q)]++;
+    }
+    std::vector<int64_t> pos((size_t)(np * nz));
+    g.plane_host.assign((size_t)(np + 1), 0);
+    int64_t acc = 0;
+    for (int64_t t = 0; t < np; t++) {
+      g.plane_host[(size_t)t] = acc;
+      for (int q = 0; q < nz; q++) { pos[(size_t)(t * nz + q)] = acc; acc += cnt[(size_t)(t * nz + q)]; }
+    }
+    g.plane_host[(size_t)np] = acc;
+    g.GG = acc;
+    if (g.GG >= (int64_t)INT32_MAX) return fail(FGB_ERR_ARG, "LU group larger than 2^31 cells");
+    std::vector<uint32_t> cells((size_t)g.GG);
+    std::vector<int32_t> zid((size_t)g.GG);
+    for (int q = 0; q < nz; q++) {
+      ZoneData& Z = s->zones[g.zones[q]];
+      const Zone& z = Z.z;
+      std::vector<int32_t> posmap((size_t)z.nd, -1);
+      for (int64_t k = 0; k < z.nk; k++)
+        for (int64_t j = 0; j < z.nj; j++)
+          for (int64_t i = 0; i < z.ni; i++) {
+            const int64_t gg = pos[(size_t)((i + j + k) * nz + q)]++;
+            cells[(size_t)gg] = (uint32_t)(i | (j << 11) | (k << 22));
+            zid[(size_t)gg] = q;
+            posmap[(size_t)idx(Z.pi, i + 1, j + 1, k + 1)] = (int32_t)gg;
+          }
+      CK(dev_upload(&Z.posmap, posmap));
+    }
+    CK(dev_upload(&g.cells, cells));
+    CK(dev_upload(&g.zid, zid));
+    CK(dev_upload(&g.plane, g.plane_host));
+    CK(cudaMalloc(&g.nbl, sizeof(int32_t) * 3 * g.GG));
+    CK(cudaMalloc(&g.nbu, sizeof(int32_t) * 3 * g.GG));
+    CK(cudaMalloc(&g.work, sizeof(double) * g.GG * lusgs_work_words(s->zones[g.zones[0]].z.typ)));
+    const size_t tb = sizeof(LuZone) * (size_t)nz;
+    CK(cudaMalloc(&g.tab_dev, tb * LuGroupData::NSLOT));
+    CK(cudaMallocHost(&g.tab_host, tb * LuGroupData::NSLOT));
+    for (int i = 0; i < LuGroupData::NSLOT; i++) CK(cudaEventCreateWithFlags(&g.ev[i], cudaEventDisableTiming));
+    for (int q = 0; q < nz; q++) {
+      ZoneData& Z = s->zones[g.zones[q]];
+      g.tab_host[q].z = Z.z;
+      g.tab_host[q].f = LuFields{nullptr, nullptr, nullptr, nullptr, Z.posmap, 0};
+    }
+    CK(cudaMemcpy(g.tab_dev, g.tab_host, tb, cudaMemcpyHostToDevice));
+    LuGroup L = group_launch(s, g, g.tab_dev);
+    CK(launch_lu_neighbours(L, s->st));
+    CK(cudaStreamSynchronize(s->st));
+  }
+  s->lu_built = true;
+  return FGB_OK;
+}
+
 int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int layer_mode,
                 int nit_c) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
@@ -807,8 +900,13 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       return fail(FGB_ERR_STATE, "Spalart-Allmaras zone without wall distance "
                                  "(fgb_set_wall_distance)");
   }
+  if (implicit && !s->lu_built) {
+    int rc = build_lu_groups(s);
+    if (rc) return rc;
+  }
   const double cxsi1 = -0.6830127018922193, cxsi2 = -4. / 3.;
   const double cg[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
+  std::vector<LuFields> lu_fields(s->zones.size());
   for (int it = 0; it < nit_c; it++) {
     int64_t nitrun_loc = (int64_t)nitrun * nit_c + it;
     for (int nstep = nstep_deb; nstep <= nstep_fin; nstep++) {
@@ -914,29 +1012,38 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             CK(launch_norms(z, na, s->st));
             s->launches++;
           }
-          if (!lexit_lu) {  // lhs.cpp -> invlu (lower, upper + mjr_newton)
-            LuArgs la{};
-            bool inplace = ssiter == out;
-            la.rop_old = ssiter;
-            la.rop_new = inplace ? Z.scratch : out;
-            la.rop_knb = inplace ? Z.scratch : ssiter;
-            la.coe = Z.coe; la.din = Z.drodm; la.dout = Z.drodm;
-            LuLaunch L{};
-            L.persistent = s->lu_mode;
-            L.fp32 = s->lu_precision == 32;
-            L.bar = s->bar;
-            L.err = s->derr;
-            L.work = Z.luwork; L.G = z.ni * z.nj * z.nk;
-            L.cells = Z.cells; L.plane = Z.plane; L.plane_host = Z.plane_host.data();
-            L.posmap = Z.posmap; L.nbl = Z.nbl; L.nbu = Z.nbu;
-            {
-              ProfScope ps(s, "lu_sgs");
-              CK(launch_lusgs(z, la, L, s->st));
-            }
-            s->launches += 1 + (L.persistent ? 1 : 2 * (z.ni + z.nj + z.nk - 2)) +
-                           ((!inplace || L.fp32) ? 1 : 0);
-            if (inplace) std::swap(Z.lvl[2], Z.scratch);
+          if (!lexit_lu) {  // lhs.cpp -> invlu (lower, upper + mjr_newton), after every zone's residual
+            const bool inplace = ssiter == out;
+            int m = (int)(&Z - s->zones.data());
+            lu_fields[(size_t)m] = LuFields{ssiter, inplace ? Z.scratch : out, Z.coe, Z.drodm, Z.posmap,
+                                            inplace ? 1 : 0};
           }
+        }
+      }
+      if (implicit && !lexit_lu) {
+        for (LuGroupData& g : s->lu_groups) {
+          const int nz = (int)g.zones.size();
+          const int slot = g.slot;
+          g.slot = (g.slot + 1) % LuGroupData::NSLOT;
+          if (g.ev_used[slot]) CK(cudaEventSynchronize(g.ev[slot]));   // slot's last copy done
+          LuZone* th = g.tab_host + (size_t)slot * nz;
+          LuZone* td = g.tab_dev + (size_t)slot * nz;
+          for (int q = 0; q < nz; q++) {
+            th[q].z = s->zones[g.zones[q]].z;
+            th[q].f = lu_fields[(size_t)g.zones[q]];
+          }
+          CK(cudaMemcpyAsync(td, th, sizeof(LuZone) * nz, cudaMemcpyHostToDevice, s->st));
+          CK(cudaEventRecord(g.ev[slot], s->st));
+          g.ev_used[slot] = true;
+          LuGroup L = group_launch(s, g, td);
+          {
+            ProfScope ps(s, "lu_sgs");
+            CK(launch_lusgs(th, L, s->st));
+          }
+          const bool inplace = th[0].f.inplace != 0;
+          s->launches += nz + (L.persistent ? 1 : 2 * (g.smax + 1)) + ((!inplace || L.fp32) ? nz : 0);
+          if (inplace)
+            for (int q : g.zones) std::swap(s->zones[q].lvl[2], s->zones[q].scratch);
         }
       }
       int wl = (implicit || nstep % 2 == 1) ? 2 : 0;

@@ -48,38 +48,49 @@ struct CoeArgs {
   int do_sa;                 // SA/vispalart.for instead of invist.for
   double coesut, cmus1;      // invist.for constants
 };
-struct LuArgs {
-  const double* rop_old;  // W^p for the B matrices and the Newton update
-  const double* rop_knb;  // state read for the k+1 neighbour in the upper sweep
-  double* rop_new;        // W^{p+1}
-  const double* coe;
-  const double* din;      // Newton residual (lower sweep input)
-  double* dout;           // increment, in place over din is allowed
-  int64_t s;              // hyperplane index (i-1)+(j-1)+(k-1)
-  int64_t jlo, klo, nbj, nbk;  // (j,k) box holding the hyperplane
+// natural-order fields of one zone's LU solve
+struct LuFields {
+  const double* rop_old;    // W^p
+  double* rop_new;          // W^{p+1}
+  const double* coe;        // coefficients
+  const double* din;        // Newton residual
+  const int32_t* posmap;    // natural index -> group plane index (-1 outside the LU range)
+  int inplace;              // upper sweep reads the k+1 neighbour after its update
 };
-// how the sweeps run: persistent cooperative kernel (one launch per solve,
-// bounded grid barrier between hyperplanes) or one launch per hyperplane;
-// FP64 or FP32 (mixed precision, needs the three FP32 work arrays)
-struct LuLaunch {
+// one zone of an LU group as the sweep kernels see it
+struct LuZone { Zone z; LuFields f; };
+
+// One LU-SGS solve of a group of zones of one kind (zone type, equation
+// count).  The plane-ordered arrays hold every interior cell of every zone
+// of the group: plane s = the cells with i+j+k = s of zone 0, then of zone 1,
+// ...  One persistent cooperative launch (one bounded grid barrier per
+// plane) or one launch per plane sweeps all zones together, so a group of
+// small blocks costs the barriers of its largest block, not of their sum.
+// FP64 or FP32 sweeps (mixed precision; the Newton update stays FP64).
+struct LuGroup {
   int persistent;
   int fp32;
-  unsigned int* bar;   // 2 words of barrier state (zeroed by the launcher)
-  int* err;            // device error word (barrier time-out)
-  void* work;          // plane-ordered work: G * lusgs_work_words(typ) words of the sweep precision
-  int64_t G;           // interior cells
-  const uint32_t* cells;    // interior cells ordered by hyperplane (packed i | j<<11 | k<<22)
-  const int64_t* plane;     // device offsets of each hyperplane in `cells`
-  const int64_t* plane_host;  // the same offsets on the host
-  const int32_t* posmap;    // natural cell index -> plane index
-  const int32_t* nbl;       // [3][G] lower neighbours (plane index or -1)
-  const int32_t* nbu;       // [3][G] upper neighbours
+  unsigned int* bar;        // barrier counter (zeroed by the launcher)
+  int* err;                 // device error word (barrier time-out)
+  void* work;               // GG * lusgs_work_words(typ) words of the sweep precision
+  int64_t GG;               // interior cells of the group
+  int64_t smax;             // last hyperplane over the group
+  const uint32_t* cells;    // packed i | j<<11 | k<<22 per group plane index
+  const int32_t* zid;       // zone (position in the group) per group plane index
+  const int64_t* plane;     // device plane offsets (smax + 2)
+  const int64_t* plane_host;
+  int32_t* nbl;             // [3][GG] lower neighbours (group plane index or -1)
+  int32_t* nbu;             // [3][GG] upper neighbours
+  LuZone* ztab;             // device zone table of this solve (nz entries)
+  int nz;
 };
 int64_t lusgs_work_words(int typ);
-cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl, int32_t* nbu,
-                                 cudaStream_t st);
+// neighbour tables of a group (ztab must hold every zone's z and f.posmap)
+cudaError_t launch_lu_neighbours(const LuGroup& G, cudaStream_t st);
 cudaError_t launch_coefficients(const Zone& z, const CoeArgs& a, cudaStream_t st);
-cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st);
+// gather of every zone, sweeps, Newton update; ztab_host = the nz entries
+// already copied to G.ztab on the stream
+cudaError_t launch_lusgs(const LuZone* ztab_host, const LuGroup& G, cudaStream_t st);
 
 // fgb_ghost.cu: ghost fill and residual norms
 struct NormArgs {

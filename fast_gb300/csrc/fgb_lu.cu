@@ -373,36 +373,34 @@ struct PlaneData {
   const uint32_t* cells;  // [G] packed (i, j, k) of each plane index
   const int64_t* plane;   // plane s = [plane[s], plane[s+1])
   int64_t G;
-};
-
-struct LuFields {           // natural-order FP64 fields of one LU solve
-  const double* rop_old;    // W^p
-  double* rop_new;          // W^{p+1}
-  const double* coe;        // coefficients
-  const double* din;        // Newton residual
-  const int32_t* posmap;    // natural index -> plane index (-1 outside the LU range)
-  int inplace;              // upper sweep reads the k+1 neighbour after its update
+  int64_t smax;           // last plane
+  const int32_t* zid;     // [G] zone of each plane index (several zones)
+  const LuZone* zt;       // zone table
 };
 
 __device__ __forceinline__ void unpack(uint32_t c, int64_t& ii, int64_t& jj, int64_t& kk) {
   ii = c & 2047u; jj = (c >> 11) & 2047u; kk = c >> 22;
 }
 
-// neighbour tables (static per zone)
-__global__ void __launch_bounds__(256) lu_neighbours(Zone z, const uint32_t* __restrict__ cells,
-                                                     const int32_t* __restrict__ posmap,
+// neighbour tables of a group (static): the neighbours of a cell are in
+// its own zone
+__global__ void __launch_bounds__(256) lu_neighbours(const LuZone* __restrict__ zt,
+                                                     const int32_t* __restrict__ zid,
+                                                     const uint32_t* __restrict__ cells,
                                                      int32_t* __restrict__ nbl,
                                                      int32_t* __restrict__ nbu, int64_t G) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= G) return;
+  const LuZone& Z = zt[zid[g]];
+  const Zone& z = Z.z;
   int64_t ii, jj, kk;
   unpack(cells[g], ii, jj, kk);
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
   const int64_t idx[3] = {ii, jj, kk}, n[3] = {z.ni, z.nj, z.nk};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    nbl[d * G + g] = idx[d] > 0 ? posmap[l - z.inc[d]] : -1;
-    nbu[d * G + g] = idx[d] < n[d] - 1 ? posmap[l + z.inc[d]] : -1;
+    nbl[d * G + g] = idx[d] > 0 ? Z.f.posmap[l - z.inc[d]] : -1;
+    nbu[d * G + g] = idx[d] < n[d] - 1 ? Z.f.posmap[l + z.inc[d]] : -1;
   }
 }
 
@@ -777,18 +775,31 @@ __device__ __forceinline__ void prefetch_plane(const PlaneData<T>& p, int64_t s,
 // PRE, a thread's first cell of the plane comes with its operands already
 // loaded (FP32 sweeps: they are latency-bound); FP64 sweeps, bound by the
 // FP64 pipe, load them here.
-template <int TYP, typename T, bool UPPER, bool PRE, int NV>
+// MULTI: the cells of a plane belong to several zones, whose descriptor and
+// fields come from the group's zone table
+template <int TYP, typename T, bool UPPER, int NV, bool MULTI>
+__device__ __forceinline__ void run_cell_of(const Zone& z, const PlaneData<T>& p, const LuFields& f,
+                                            int64_t g, const CellOps<TYP, T, NV>& o) {
+  if (MULTI) {
+    const LuZone& Z = p.zt[p.zid[g]];
+    run_cell<TYP, T, UPPER, NV>(Z.z, p, Z.f, g, o);
+  } else {
+    run_cell<TYP, T, UPPER, NV>(z, p, f, g, o);
+  }
+}
+
+template <int TYP, typename T, bool UPPER, bool PRE, int NV, bool MULTI>
 __device__ __forceinline__ void do_plane(const Zone& z, const PlaneData<T>& p, const LuFields& f,
                                          int64_t s, CellOps<TYP, T, NV>& first) {
   const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
   int64_t c = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
   if (c >= n) return;
   if (!PRE) load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, c0 + c, first);
-  run_cell<TYP, T, UPPER, NV>(z, p, f, c0 + c, first);
+  run_cell_of<TYP, T, UPPER, NV, MULTI>(z, p, f, c0 + c, first);
   for (c += (int64_t)gridDim.x * blockDim.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     CellOps<TYP, T, NV> o;
     load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, c0 + c, o);
-    run_cell<TYP, T, UPPER, NV>(z, p, f, c0 + c, o);
+    run_cell_of<TYP, T, UPPER, NV, MULTI>(z, p, f, c0 + c, o);
   }
 }
 
@@ -802,10 +813,10 @@ __device__ __forceinline__ void load_first(const PlaneData<T>& p, const LuFields
 
 template <typename T> struct LuThreads { static constexpr int n = 512; };
 
-template <int TYP, typename T, int NV>
+template <int TYP, typename T, int NV, bool MULTI>
 __global__ void __launch_bounds__(LuThreads<T>::n, 1)
     lusgs_persistent(Zone z, PlaneData<T> p, LuFields f, GridBar gb) {
-  const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
+  const int64_t smax = p.smax;
   // traversal step t: lower planes 0..smax, then upper planes smax..0
   auto plane_of = [&](int64_t t) { return t <= smax ? t : 2 * smax + 1 - t; };
   const int64_t nsteps = 2 * smax + 2;
@@ -817,8 +828,8 @@ __global__ void __launch_bounds__(LuThreads<T>::n, 1)
   unsigned int round = 0;
   for (int64_t t = 0; t < nsteps; t++) {
     const int64_t s = plane_of(t);
-    if (t <= smax) do_plane<TYP, T, false, PRE, NV>(z, p, f, s, o);
-    else do_plane<TYP, T, true, PRE, NV>(z, p, f, s, o);
+    if (t <= smax) do_plane<TYP, T, false, PRE, NV, MULTI>(z, p, f, s, o);
+    else do_plane<TYP, T, true, PRE, NV, MULTI>(z, p, f, s, o);
     if (t == nsteps - 1) break;
     bar_arrive(gb);
     if (t + 2 < nsteps) prefetch_plane<TYP, T>(p, plane_of(t + 2), t + 2 > smax);
@@ -833,14 +844,14 @@ __global__ void __launch_bounds__(LuThreads<T>::n, 1)
 
 // one launch per hyperplane (no inter-CTA waits): cross-check of the
 // persistent kernel
-template <int TYP, typename T, bool UPPER, int NV>
+template <int TYP, typename T, bool UPPER, int NV, bool MULTI>
 __global__ void __launch_bounds__(128) lusgs_plane(Zone z, PlaneData<T> p, LuFields f, int64_t s) {
   const int64_t c0 = p.plane[s], n = p.plane[s + 1] - c0;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
   CellOps<TYP, T, NV> o;
   load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, c0 + c, o);
-  run_cell<TYP, T, UPPER, NV>(z, p, f, c0 + c, o);
+  run_cell_of<TYP, T, UPPER, NV, MULTI>(z, p, f, c0 + c, o);
 }
 
 // FP64 Newton update of every interior cell after the sweeps.  Tiles of
@@ -912,9 +923,8 @@ __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* _
                                       tt + double(dT));
 }
 
-template <int TYP, typename T, int NV = 5>
-static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>& p,
-                            const LuLaunch& L, cudaStream_t st) {
+template <int TYP, typename T, int NV>
+static cudaError_t gather_t(const Zone& z, const LuFields& f, const PlaneData<T>& p, cudaStream_t st) {
   using S = GatherSmem<TYP, T>;
   static bool smem_set[64] = {};   // per device
   int dev = 0;
@@ -928,55 +938,83 @@ static cudaError_t launch_t(const Zone& z, const LuFields& f, const PlaneData<T>
   }
   lu_gather<TYP, T, NV><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I), (unsigned)((z.nj + GT_J - 1) / GT_J),
                            (unsigned)z.nk), GT_N, S::bytes, st>>>(z, f, p);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+template <int TYP, typename T, int NV, bool MULTI>
+static cudaError_t sweep_t(const Zone& z, const LuFields& f, const PlaneData<T>& p, const LuGroup& L,
+                           cudaStream_t st) {
+  cudaError_t e;
   if (L.persistent) {
     static int grid = 0;   // per instantiation (one device per process in practice)
     if (grid == 0) {
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T, NV>, LuThreads<T>::n, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T, NV, MULTI>,
+                                                    LuThreads<T>::n, 0);
       grid = nsm * (per > 0 ? per : 1);
     }
     e = cudaMemsetAsync(L.bar, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     GridBar gb{L.bar, L.err};
-    void* args[] = {(void*)&z, (void*)&p, (void*)&f, (void*)&gb};
-    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T, NV>, dim3(grid), dim3(LuThreads<T>::n),
-                                    args, 0, st);
+    Zone zz = z;
+    LuFields ff = f;
+    PlaneData<T> pp = p;
+    void* args[] = {(void*)&zz, (void*)&pp, (void*)&ff, (void*)&gb};
+    e = cudaLaunchCooperativeKernel((void*)lusgs_persistent<TYP, T, NV, MULTI>, dim3(grid),
+                                    dim3(LuThreads<T>::n), args, 0, st);
   } else {
     const int B = 128;
-    const int64_t smax = (z.ni - 1) + (z.nj - 1) + (z.nk - 1);
-    for (int64_t s = 0; s <= smax; s++) {
+    for (int64_t s = 0; s <= p.smax; s++) {
       int64_t n = L.plane_host[s + 1] - L.plane_host[s];
-      lusgs_plane<TYP, T, false, NV><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
+      if (n > 0)
+        lusgs_plane<TYP, T, false, NV, MULTI><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
     }
-    for (int64_t s = smax; s >= 0; s--) {
+    for (int64_t s = p.smax; s >= 0; s--) {
       int64_t n = L.plane_host[s + 1] - L.plane_host[s];
-      lusgs_plane<TYP, T, true, NV><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
+      if (n > 0)
+        lusgs_plane<TYP, T, true, NV, MULTI><<<(unsigned)((n + B - 1) / B), B, 0, st>>>(z, p, f, s);
     }
-    e = cudaGetLastError();
-  }
-  if (e != cudaSuccess) return e;
-  if (!f.inplace || sizeof(T) == 4) {
-    lu_newton<T, TYP == Z2D, NV><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I),
-                                        (unsigned)((z.nj + GT_J - 1) / GT_J), (unsigned)z.nk),
-                                   GT_N, 0, st>>>(z, f, p.dio);
     e = cudaGetLastError();
   }
   return e;
 }
 
+template <int TYP, typename T, int NV>
+static cudaError_t group_t(const LuZone* zh, const PlaneData<T>& p, const LuGroup& L, cudaStream_t st) {
+  cudaError_t e;
+  for (int m = 0; m < L.nz; m++) {
+    e = gather_t<TYP, T, NV>(zh[m].z, zh[m].f, p, st);
+    if (e != cudaSuccess) return e;
+  }
+  // a single zone runs with its descriptor as a kernel parameter; several
+  // zones read theirs from the table (per cell)
+  e = L.nz == 1 ? sweep_t<TYP, T, NV, false>(zh[0].z, zh[0].f, p, L, st)
+                : sweep_t<TYP, T, NV, true>(zh[0].z, zh[0].f, p, L, st);
+  if (e != cudaSuccess) return e;
+  for (int m = 0; m < L.nz; m++) {
+    const Zone& z = zh[m].z;
+    if (zh[m].f.inplace && sizeof(T) == 8) continue;   // updated by the upper sweep
+    lu_newton<T, TYP == Z2D, NV><<<dim3((unsigned)((z.ni + GT_I - 1) / GT_I),
+                                        (unsigned)((z.nj + GT_J - 1) / GT_J), (unsigned)z.nk),
+                                   GT_N, 0, st>>>(z, zh[m].f, p.dio);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 template <typename T>
-static PlaneData<T> plane_data(const LuLaunch& L, int rec_size) {
+static PlaneData<T> plane_data(const LuGroup& L, int rec_size) {
   PlaneData<T> p;
-  const int64_t G = L.G;
+  const int64_t G = L.GG;
   T* w = (T*)L.work;
   p.rec = w; w += (int64_t)rec_size * G;
   p.dio = w; w += (int64_t)DIO * G;
   p.nst = w; w += 4 * G;
   p.nbl = L.nbl; p.nbu = L.nbu; p.cells = L.cells; p.plane = L.plane; p.G = G;
+  p.smax = L.smax; p.zid = L.zid; p.zt = L.ztab;
   return p;
 }
 
@@ -986,31 +1024,33 @@ int64_t lusgs_work_words(int typ) {
   // (2-d zones use the general record layout)
 }
 
-cudaError_t launch_lu_neighbours(const Zone& z, const LuLaunch& L, int32_t* nbl, int32_t* nbu,
-                                 cudaStream_t st) {
-  lu_neighbours<<<(unsigned)((L.G + 255) / 256), 256, 0, st>>>(z, L.cells, L.posmap, nbl, nbu, L.G);
+cudaError_t launch_lu_neighbours(const LuGroup& L, cudaStream_t st) {
+  lu_neighbours<<<(unsigned)((L.GG + 255) / 256), 256, 0, st>>>(L.ztab, L.zid, L.cells, L.nbl, L.nbu,
+                                                                L.GG);
   return cudaGetLastError();
 }
 
-// One LU-SGS solve (lower, upper, Newton update) of one zone.
-cudaError_t launch_lusgs(const Zone& z, const LuArgs& a, const LuLaunch& L, cudaStream_t st) {
-  LuFields f{a.rop_old, a.rop_new, a.coe, a.din, L.posmap, a.rop_knb == a.rop_new};
+// One LU-SGS solve (lower, upper, Newton update) of a group of zones of one
+// kind (zone type, equation count, sweep precision).
+cudaError_t launch_lusgs(const LuZone* zh, const LuGroup& L, cudaStream_t st) {
+  if (L.nz < 1) return cudaSuccess;
+  const Zone& z = zh[0].z;
   const bool sa = z.neq == 6;   // Spalart-Allmaras: 3d zones
   if (sa && z.typ == Z2D) return cudaErrorNotSupported;
   if (L.fp32) {
     const int rs = z.typ == Z3DCART ? Rec<Z3DCART, float>::SIZE : Rec<Z3DFULL, float>::SIZE;
     PlaneData<float> p = plane_data<float>(L, rs);
     if (z.typ == Z3DCART)
-      return sa ? launch_t<Z3DCART, float, 6>(z, f, p, L, st) : launch_t<Z3DCART, float>(z, f, p, L, st);
-    if (z.typ == Z2D) return launch_t<Z2D, float>(z, f, p, L, st);
-    return sa ? launch_t<Z3DFULL, float, 6>(z, f, p, L, st) : launch_t<Z3DFULL, float>(z, f, p, L, st);
+      return sa ? group_t<Z3DCART, float, 6>(zh, p, L, st) : group_t<Z3DCART, float, 5>(zh, p, L, st);
+    if (z.typ == Z2D) return group_t<Z2D, float, 5>(zh, p, L, st);
+    return sa ? group_t<Z3DFULL, float, 6>(zh, p, L, st) : group_t<Z3DFULL, float, 5>(zh, p, L, st);
   }
   const int rs = z.typ == Z3DCART ? Rec<Z3DCART, double>::SIZE : Rec<Z3DFULL, double>::SIZE;
   PlaneData<double> p = plane_data<double>(L, rs);
   if (z.typ == Z3DCART)
-    return sa ? launch_t<Z3DCART, double, 6>(z, f, p, L, st) : launch_t<Z3DCART, double>(z, f, p, L, st);
-  if (z.typ == Z2D) return launch_t<Z2D, double>(z, f, p, L, st);
-  return sa ? launch_t<Z3DFULL, double, 6>(z, f, p, L, st) : launch_t<Z3DFULL, double>(z, f, p, L, st);
+    return sa ? group_t<Z3DCART, double, 6>(zh, p, L, st) : group_t<Z3DCART, double, 5>(zh, p, L, st);
+  if (z.typ == Z2D) return group_t<Z2D, double, 5>(zh, p, L, st);
+  return sa ? group_t<Z3DFULL, double, 6>(zh, p, L, st) : group_t<Z3DFULL, double, 5>(zh, p, L, st);
 }
 
 }  // namespace fgb
