@@ -37,6 +37,10 @@ SIGNATURES = {
     "fgb_apply_bc": ([_P, C.c_int], C.c_int),
     "fgb_residuals": ([_P, C.c_int, _DP, C.c_int64, C.POINTER(C.c_int)], C.c_int),
     "fgb_residual_norms_noalloc": ([_P, C.c_int, _P], C.c_int),
+    "fgb_set_bc_state": ([_P, C.c_int, _DP], C.c_int),
+    "fgb_adjoint_forward": ([_P, C.c_int, C.c_int, C.c_int], C.c_int),
+    "fgb_adjoint_backward": ([_P, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP], C.c_int),
+    "fgb_tangent": ([_P, C.c_int, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP], C.c_int),
     "fgb_synchronize": ([_P], C.c_int),
     "fgb_kernel_stats": ([_P, C.c_int, C.c_char_p, C.c_int, _I64P, _DP], C.c_int),
     "fgb_launch_count": ([_P, _I64P], C.c_int),
@@ -174,6 +178,29 @@ class Solver:
         """Enqueue fgb_residual_norms_noalloc: 2*neq doubles (L2 then Loo)
         written to the device address out_ptr; fgb_synchronize waits."""
         _check(self._lib.fgb_residual_norms_noalloc(self._h, int(zone), C.c_void_p(int(out_ptr))))
+
+    def set_bc_state(self, zone: int, st):
+        a = np.ascontiguousarray(st, dtype=np.float64)
+        _check(self._lib.fgb_set_bc_state(self._h, int(zone), _dp(a)))
+
+    def adjoint_forward(self, zone: int, nsteps: int, ckpt: int):
+        _check(self._lib.fgb_adjoint_forward(self._h, int(zone), int(nsteps), int(ckpt)))
+
+    def adjoint_backward(self, zone: int, lam_final):
+        """(dJ/dW0, dJ/dti, dJ/dtj, dJ/dvol, dJ/dst) of the last forward run."""
+        pi = self.zones[zone][0]
+        nq, nm = int(pi[36] * pi[41]), int(pi[43])
+        lf = np.ascontiguousarray(lam_final, dtype=np.float64)
+        out = [np.zeros(nq), np.zeros(2 * nm), np.zeros(2 * nm), np.zeros(nm), np.zeros(5)]
+        _check(self._lib.fgb_adjoint_backward(self._h, int(zone), _dp(lf), *(_dp(o) for o in out)))
+        return out
+
+    def tangent(self, zone: int, nsteps: int, dw0, dti, dtj, dvol, dst):
+        pi = self.zones[zone][0]
+        out = np.zeros(int(pi[36] * pi[41]))
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (dw0, dti, dtj, dvol, dst)]
+        _check(self._lib.fgb_tangent(self._h, int(zone), int(nsteps), *(_dp(x) for x in a), _dp(out)))
+        return out
 
     def synchronize(self):
         _check(self._lib.fgb_synchronize(self._h))

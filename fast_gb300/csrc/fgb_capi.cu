@@ -50,6 +50,8 @@ struct GatherList {
   int32_t* dst = nullptr; int32_t* src = nullptr; int64_t n = 0; int op = 0;
   int32_t *q0 = nullptr, *q1 = nullptr, *q2 = nullptr;
   double* nrm = nullptr;
+  int32_t* mt = nullptr;          // metric index of the face of each entry (face formulas)
+  int dir = 0;                    // face direction (0 i, 1 j, 2 k)
   double st[5] = {0, 0, 0, 0, 0};
   int inflow = 0;                 // BCInflow: nutilde imposed (Spalart-Allmaras)
 };
@@ -110,6 +112,18 @@ struct fgb_solver {
   std::vector<Transfer> tr;
   std::vector<LuGroupData> lu_groups;
   bool lu_built = false;
+  // explicit 2-d adjoint (fgb_adjoint_forward / _backward): checkpoints of
+  // the forward run and the recomputation buffers of one segment
+  struct Adj {
+    int zone = -1, nsteps = 0, ckpt = 0;
+    std::vector<double*> ck;       // full states at steps 0, ckpt, 2 ckpt, ... and the last
+    double* W = nullptr;           // (3 ckpt + 1) full states of a segment's stages
+    double* D = nullptr;           // 3 ckpt stage residuals of a segment
+    double *lamW = nullptr, *lamIn = nullptr, *lamD = nullptr;
+    double *lamTi = nullptr, *lamTj = nullptr, *lamVol = nullptr, *lamSt = nullptr;
+    double *dW = nullptr, *dWn = nullptr, *dD = nullptr, *dFi = nullptr, *dFj = nullptr;
+    double *dTi = nullptr, *dTj = nullptr, *dVol = nullptr, *dSt = nullptr;
+  } adj;
   int first_it = 0;
   int modulo_verif = 200;
   int lu_precision = 64;
@@ -125,6 +139,10 @@ struct fgb_solver {
   std::vector<cudaEvent_t> pool;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
 };
+
+extern "C" {
+static void adj_free(fgb_solver* s);   // defined with the C ABI below
+}
 
 static cudaEvent_t ev_get(fgb_solver* s) {
   if (!s->pool.empty()) { cudaEvent_t e = s->pool.back(); s->pool.pop_back(); return e; }
@@ -225,12 +243,13 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
       // raw face normal tijk(lmtr) * c_mtr (shape_tab_mtr.for)
       const std::vector<double>& T = d == 0 ? hti : (d == 1 ? htj : htk);
       const int64_t neq_mtr = d < 2 ? p[NEQ_IJ] : p[NEQ_K], ndm = p[NDIMDX_MTR];
+      int64_t lm = 0;   // metric index of the last face normal
       auto normal = [&](int64_t c0, int64_t c1, int64_t c2, double t[3]) {
         int64_t c[3] = {c0, c1, c2};
         c[d] = low ? 1 : nD + 1;
-        const int64_t lm = (c[0] + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR] +
-                           (c[1] + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR + 1] +
-                           (c[2] + p[NIJK_MTR + 4] - 1) * p[NIJK_MTR + 2];
+        lm = (c[0] + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR] +
+             (c[1] + p[NIJK_MTR + 3] - 1) * p[NIJK_MTR + 1] +
+             (c[2] + p[NIJK_MTR + 4] - 1) * p[NIJK_MTR + 2];
         if (neq_mtr == 3) {
           t[0] = T[lm] * 1.; t[1] = T[lm + ndm] * 1.; t[2] = T[lm + 2 * ndm] * 1.;
         } else if (neq_mtr == 2) {   // shape_tab_mtr.for: ic=1, jc=2, kc=2, ck_mtr=0
@@ -269,7 +288,7 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
           return fail(FGB_ERR_CUDA, "cannot upload wall correction lists");
         Z.walls.push_back(w);
       }
-      std::vector<int32_t> fdst, fsrc, ndst, n0, n1, n2, cdst, csrc;
+      std::vector<int32_t> fdst, fsrc, fmt, ndst, n0, n1, n2, cdst, csrc;
       std::vector<double> nrm;
       const int64_t inc = d == 0 ? 1 : (d == 1 ? p[NIJK] : p[NIJK] * p[NIJK + 1]);
       for (int64_t b = cl[2 * tb]; b <= cl[2 * tb + 1]; b++)
@@ -285,10 +304,12 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
             if (slip || noslip) {
               m[d] = iref - c[d];
               fdst.push_back((int32_t)l); fsrc.push_back((int32_t)idx(p, m[0], m[1], m[2]));
+              fmt.push_back((int32_t)lm);
               for (int q = 0; q < 3; q++) nrm.push_back(t[q]);
             } else if (rank == 0) {
               m[d] = ir;
               fdst.push_back((int32_t)l); fsrc.push_back((int32_t)idx(p, m[0], m[1], m[2]));
+              fmt.push_back((int32_t)lm);
               for (int q = 0; q < 3; q++) nrm.push_back(t[q] * snorm);
             } else if (type == 10) {     // BC_extrap.for: copy of the first ghost
               m[d] = first;
@@ -304,6 +325,7 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
       f.kind = 1;
       f.op = slip ? BCF_SLIP : (noslip ? BCF_NOSLIP : (type == 10 ? BCF_OUTFLOW : BCF_FARFIELD));
       f.inflow = type == 13;
+      f.dir = d;
       f.n = (int64_t)fdst.size();
       // BCzone.cpp DEFAULT_STATE, nbdata = 0: the free stream
       f.st[0] = pr[ROINF];
@@ -313,7 +335,7 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
       f.st[4] = pr[PINF] / (pr[GAMMA] - 1.) +
                 0.5 * (pr[VXINF] * f.st[1] + pr[VYINF] * f.st[2] + pr[VZINF] * f.st[3]);
       if (dev_upload(&f.dst, fdst) != cudaSuccess || dev_upload(&f.src, fsrc) != cudaSuccess ||
-          dev_upload(&f.nrm, nrm) != cudaSuccess)
+          dev_upload(&f.nrm, nrm) != cudaSuccess || dev_upload(&f.mt, fmt) != cudaSuccess)
         return fail(FGB_ERR_CUDA, "cannot upload BC lists");
       Z.bcs.push_back(f);
       if (!cdst.empty()) {
@@ -497,7 +519,7 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.posmap);
     for (GatherList& g : Z.bcs) {
       cudaFree(g.dst); cudaFree(g.src); cudaFree(g.q0); cudaFree(g.q1); cudaFree(g.q2);
-      cudaFree(g.nrm);
+      cudaFree(g.nrm); cudaFree(g.mt);
     }
     cudaFree(Z.wig);
     cudaFree(Z.dist);
@@ -510,6 +532,7 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(g.work); cudaFree(g.tab_dev); cudaFreeHost(g.tab_host);
     for (int i = 0; i < LuGroupData::NSLOT; i++) if (g.ev[i]) cudaEventDestroy(g.ev[i]);
   }
+  adj_free(s);
   cudaFree(s->bar);
   cudaFree(s->derr);
   for (auto& e : s->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
@@ -558,9 +581,14 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   if (p[EXPLOC] != 0 || p[DTLOC] != 0 || p[LALE] != 0)
     return fail(FGB_ERR_ARG, "local time stepping and moving meshes are not supported");
   int64_t nd = p[NDIMDX], neq = p[NEQ], ndm = p[NDIMDX_MTR];
-  int64_t nmtr_ij = p[ITYPZONE] == Z3DCART ? 1 : 3;
+  // metric components per face family: NEQ_IJ for ti / tj, NEQ_K for tk
+  // (3d cartesian 1 / 1, 3d general 3 / 3, 2d 2 / 0 -- a 2-d zone has no tk)
+  const int64_t nmtr_ij = p[NEQ_IJ], nmtr_k = p[NEQ_K];
+  if (nmtr_ij != (p[ITYPZONE] == Z3DCART ? 1 : (p[ITYPZONE] == Z2D ? 2 : 3)) ||
+      nmtr_k != (p[ITYPZONE] == Z3DCART ? 1 : (p[ITYPZONE] == Z2D ? 0 : 3)))
+    return fail(FGB_ERR_ARG, "NEQ_IJ / NEQ_K inconsistent with the zone type");
   std::vector<double> hti(ti, ti + ndm * nmtr_ij), htj(tj, tj + ndm * nmtr_ij),
-      htk(tk, tk + ndm * nmtr_ij), hvol(vol, vol + ndm);
+      htk(tk, tk + ndm * nmtr_k), hvol(vol, vol + ndm);
   fill_zone(Z, ti, tj, tk, vol);
   size_t st_bytes = sizeof(double) * neq * nd;
   for (int i = 0; i < 3; i++) {
@@ -779,6 +807,168 @@ int fgb_apply_bc(fgb_solver* s, int level) {
   return ghost_fill(s, level);
 }
 
+// ----------------------------------------------------------- adjoint
+// Explicit 2-d Euler (Roe + van Albada) zones: the primal runs the product
+// kernels (faces, assemble, ghost fill) on the adjoint's own buffers; the
+// tangent and adjoint apply the local Jacobians of fgb_adjoint.cu in the
+// same / reverse order.
+static void adj_free(fgb_solver* s) {
+  fgb_solver::Adj& A = s->adj;
+  for (double* p : A.ck) cudaFree(p);
+  A.ck.clear();
+  double** bufs[] = {&A.W, &A.D, &A.lamW, &A.lamIn, &A.lamD, &A.lamTi, &A.lamTj, &A.lamVol,
+                     &A.lamSt, &A.dW, &A.dWn, &A.dD, &A.dFi, &A.dFj, &A.dTi, &A.dTj, &A.dVol,
+                     &A.dSt};
+  for (double** b : bufs) { cudaFree(*b); *b = nullptr; }
+  A.zone = -1;
+}
+
+static int adj_check(fgb_solver* s, int zone) {
+  if (!s) return fail(FGB_ERR_ARG, "null solver");
+  if (zone < 0 || zone >= (int)s->zones.size()) return fail(FGB_ERR_ARG, "zone out of range");
+  ZoneData& Z = s->zones[zone];
+  const Zone& z = Z.z;
+  if (z.typ != Z2D || z.iflow != 1 || z.kflu != ROE || z.slope != VANALBADA || z.itypcp <= 1 ||
+      z.rk != 3)
+    return fail(FGB_ERR_ARG, "the adjoint covers explicit RK3, Euler, Roe + van Albada, 2-d zones");
+  for (GatherList& g : Z.bcs)
+    if (g.kind == 1 && g.op != BCF_SLIP && g.op != BCF_FARFIELD)
+      return fail(FGB_ERR_ARG, "the adjoint covers slip-wall and farfield / inflow BCs");
+  for (Transfer& T : s->tr)
+    if (T.rcv == zone && T.dnr != zone)
+      return fail(FGB_ERR_ARG, "the adjoint covers one zone (self 1-to-1 interfaces only)");
+  for (WallCorrList& w : Z.walls)
+    if (!w.slip) return fail(FGB_ERR_ARG, "the adjoint covers slip walls");
+  return FGB_OK;
+}
+
+static BcFaceArgs face_args(ZoneData& Z, GatherList& g) {
+  BcFaceArgs a{};
+  a.dst = g.dst; a.src = g.src; a.nrm = g.nrm; a.n = g.n; a.nd = Z.z.nd; a.op = g.op;
+  a.gam = Z.pr[GAMMA]; a.gam1 = Z.pr[GAMMA] - 1.; a.gam1_1 = 1. / a.gam1;
+  a.cv = Z.pr[CVINF]; a.cvinv = 1. / Z.pr[CVINF];
+  for (int m = 0; m < 5; m++) a.st[m] = g.st[m];
+  a.sa = Z.z.neq == 6; a.inflow = g.inflow;
+  a.nue = Z.pr[RONUTILDEINF] / Z.pr[ROINF];
+  return a;
+}
+
+static BcNextArgs next_args(ZoneData& Z, GatherList& g) {
+  const double c4 = 5. / 6., c5 = 2. / 6., c6 = -1. / 6.;
+  const double k0 = 1. / c6;
+  BcNextArgs a{};
+  a.dst = g.dst; a.q0 = g.q0; a.q1 = g.q1; a.q2 = g.q2; a.n = g.n; a.nd = Z.z.nd;
+  a.k1 = -(c4 + c5) * k0; a.k2 = -c6 * k0; a.k3 = (2. - c5 - c4) * k0;
+  a.sa = Z.z.neq == 6;
+  return a;
+}
+
+// ghost fill of zone m on buffer q (self interfaces, BCs, corners): the
+// order of ghost_fill
+static int zone_fill(fgb_solver* s, int m, double* q) {
+  ZoneData& Z = s->zones[m];
+  for (Transfer& T : s->tr)
+    if (T.rcv == m) CK(launch_gather(q, Z.z.nd, q, Z.z.nd, T.rcv_idx, T.dnr_idx, T.n, Z.z.neq, 0, 1., s->st));
+  for (GatherList& g : Z.bcs) {
+    if (g.kind == 0) CK(launch_gather(q, Z.z.nd, q, Z.z.nd, g.dst, g.src, g.n, Z.z.neq, g.op, 1., s->st));
+    else if (g.kind == 1) CK(launch_bc_face(q, face_args(Z, g), s->st));
+    else CK(launch_bc_next(q, next_args(Z, g), s->st));
+  }
+  CK(launch_coins(q, Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n, Z.z.neq, s->st));
+  return FGB_OK;
+}
+
+// tangent of the fill at the filled state q: dq's ghosts from its interior
+static int zone_fill_tan(fgb_solver* s, int m, const double* q, double* dq) {
+  ZoneData& Z = s->zones[m];
+  fgb_solver::Adj& A = s->adj;
+  for (Transfer& T : s->tr)
+    if (T.rcv == m) CK(launch_gather(dq, Z.z.nd, dq, Z.z.nd, T.rcv_idx, T.dnr_idx, T.n, Z.z.neq, 0, 1., s->st));
+  for (GatherList& g : Z.bcs) {
+    if (g.kind == 0) CK(launch_gather(dq, Z.z.nd, dq, Z.z.nd, g.dst, g.src, g.n, Z.z.neq, 0, 1., s->st));
+    else if (g.kind == 1)
+      CK(launch_tan_bc_face(q, dq, face_args(Z, g), g.mt, Z.z.ndm, g.dir == 0 ? A.dTi : A.dTj, A.dSt, s->st));
+    else CK(launch_lin_bc_next(q, dq, next_args(Z, g), 0, Z.z.neq, s->st));
+  }
+  CK(launch_coins(dq, Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n, Z.z.neq, s->st));
+  return FGB_OK;
+}
+
+// adjoint of the fill at the filled state q: ghost adjoints of lam moved to
+// the interior (and to the wall normals / farfield state)
+static int zone_fill_adj(fgb_solver* s, int m, const double* q, double* lam) {
+  ZoneData& Z = s->zones[m];
+  fgb_solver::Adj& A = s->adj;
+  CK(launch_adj_coins(lam, Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n, Z.z.neq, s->st));
+  for (int i = (int)Z.bcs.size() - 1; i >= 0; i--) {
+    GatherList& g = Z.bcs[(size_t)i];
+    if (g.kind == 0) CK(launch_adj_gather(lam, Z.z.nd, g.dst, g.src, g.n, Z.z.neq, s->st));
+    else if (g.kind == 1)
+      CK(launch_adj_bc_face(q, lam, face_args(Z, g), g.mt, Z.z.ndm, g.dir == 0 ? A.lamTi : A.lamTj,
+                            A.lamSt, s->st));
+    else CK(launch_lin_bc_next(q, lam, next_args(Z, g), 1, Z.z.neq, s->st));
+  }
+  for (int i = (int)s->tr.size() - 1; i >= 0; i--) {
+    Transfer& T = s->tr[(size_t)i];
+    if (T.rcv == m) CK(launch_adj_gather(lam, Z.z.nd, T.rcv_idx, T.dnr_idx, T.n, Z.z.neq, s->st));
+  }
+  return FGB_OK;
+}
+
+// wall-correction arguments of one Roe wall list (correct_flux.for)
+static WallCorrArgs wall_args(ZoneData& Z, WallCorrList& w) {
+  WallCorrArgs wa{};
+  wa.l = w.l; wa.l0 = w.l0; wa.lt = w.lt; wa.nrm = w.nrm; wa.n = w.n;
+  wa.dir = w.dir; wa.slip = w.slip; wa.sens_c = w.sens_c; wa.sens_w = w.sens_w;
+  wa.rgp = Z.pr[CVINF] * (Z.pr[GAMMA] - 1.);
+  wa.gam2 = Z.pr[GAMMA] / (Z.pr[GAMMA] - 1.);
+  return wa;
+}
+
+// balance + update of one sub-step: fused, or -- zones with Roe walls --
+// balance, wall-face corrections (correct_flux.for), update
+static int assemble_stage(fgb_solver* s, ZoneData& Z, StageArgs sa, const double* ssiter,
+                          bool implicit) {
+  if (Z.walls.empty()) {
+    CK(launch_assemble(Z.z, sa, implicit, s->st));
+    s->launches++;
+    return FGB_OK;
+  }
+  sa.mode = 1;
+  CK(launch_assemble(Z.z, sa, implicit, s->st));
+  for (WallCorrList& w : Z.walls) CK(launch_wall_corr(Z.z, ssiter, sa.drodm, wall_args(Z, w), s->st));
+  sa.mode = 2;
+  CK(launch_assemble(Z.z, sa, implicit, s->st));
+  s->launches += 2 + (int64_t)Z.walls.size();
+  return FGB_OK;
+}
+
+static const double kCoefH[4] = {0., 0., -0.6830127018922193, -4. / 3.};
+static const double kCoefW[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
+
+// one RK3 stage of fgb_compute's explicit path on explicit buffers
+static int explicit_stage(fgb_solver* s, int m, int nstep, const double* in, double* out, double* D) {
+  ZoneData& Z = s->zones[m];
+  cudaError_t e = launch_faces(Z.z, in, Z.xmut, Z.Fi, Z.Fj, Z.Fk, s->st);
+  if (e == cudaErrorNotSupported) return fail(FGB_ERR_ARG, "scheme not implemented");
+  CK(e);
+  StageArgs sa{};
+  sa.Fi = Z.Fi; sa.Fj = Z.Fj; sa.Fk = Z.Fk; sa.drodm = D; sa.coe = Z.coe;
+  sa.rop_in = in; sa.rop_out = out;
+  sa.zero_init = nstep == 1;
+  sa.coefH = kCoefH[nstep];
+  sa.coefW = kCoefW[nstep];
+  int rc = assemble_stage(s, Z, sa, in, false);
+  if (rc) return rc;
+  return zone_fill(s, m, out);
+}
+
+static int adj_alloc(double** p, size_t n) {
+  CK(cudaMalloc(p, sizeof(double) * n));
+  CK(cudaMemset(*p, 0, sizeof(double) * n));
+  return FGB_OK;
+}
+
 static void free_lu_groups(fgb_solver* s) {
   for (LuGroupData& g : s->lu_groups) {
     cudaFree(g.cells); cudaFree(g.zid); cudaFree(g.plane); cudaFree(g.nbl); cudaFree(g.nbu);
@@ -983,24 +1173,8 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
         }
         {
           ProfScope ps(s, implicit ? "assemble_bdf" : "assemble_rk3");
-          if (Z.walls.empty()) {
-            CK(launch_assemble(z, sa, implicit, s->st));
-            s->launches++;
-          } else {  // balance, wall-face corrections (correct_flux.for), update
-            sa.mode = 1;
-            CK(launch_assemble(z, sa, implicit, s->st));
-            for (WallCorrList& w : Z.walls) {
-              WallCorrArgs wa{};
-              wa.l = w.l; wa.l0 = w.l0; wa.lt = w.lt; wa.nrm = w.nrm; wa.n = w.n;
-              wa.dir = w.dir; wa.slip = w.slip; wa.sens_c = w.sens_c; wa.sens_w = w.sens_w;
-              wa.rgp = Z.pr[CVINF] * (Z.pr[GAMMA] - 1.);
-              wa.gam2 = Z.pr[GAMMA] / (Z.pr[GAMMA] - 1.);
-              CK(launch_wall_corr(z, ssiter, Z.drodm, wa, s->st));
-            }
-            sa.mode = 2;
-            CK(launch_assemble(z, sa, implicit, s->st));
-            s->launches += 2 + (int64_t)Z.walls.size();
-          }
+          int rc = assemble_stage(s, Z, sa, ssiter, implicit);
+          if (rc) return rc;
         }
         if (implicit) {
           if (verif) {  // lhs.cpp residus_navier.h -> cprdu3s1
@@ -1062,6 +1236,178 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       Z.lvl[2] = save;
     }
   }
+  return FGB_OK;
+}
+
+int fgb_set_bc_state(fgb_solver* s, int zone, const double* st) {
+  if (!s || !st) return fail(FGB_ERR_ARG, "null argument");
+  if (zone < 0 || zone >= (int)s->zones.size()) return fail(FGB_ERR_ARG, "zone out of range");
+  for (GatherList& g : s->zones[zone].bcs)
+    if (g.kind == 1 && (g.op == BCF_FARFIELD || g.op == BCF_OUTFLOW))
+      for (int m = 0; m < 5; m++) g.st[m] = st[m];
+  return FGB_OK;
+}
+
+int fgb_adjoint_forward(fgb_solver* s, int zone, int nsteps, int ckpt) {
+  int rc = adj_check(s, zone);
+  if (rc) return rc;
+  if (nsteps < 1 || ckpt < 1) return fail(FGB_ERR_ARG, "nsteps and ckpt must be >= 1");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->st));
+  adj_free(s);
+  fgb_solver::Adj& A = s->adj;
+  ZoneData& Z = s->zones[zone];
+  const Zone& z = Z.z;
+  const size_t nq = (size_t)z.neq * z.nd;
+  A.zone = zone; A.nsteps = nsteps; A.ckpt = ckpt;
+  const int nseg = (nsteps + ckpt - 1) / ckpt;
+  A.ck.assign((size_t)nseg + 1, nullptr);
+  for (double*& c : A.ck) if ((rc = adj_alloc(&c, nq))) return rc;
+  if ((rc = adj_alloc(&A.W, nq * (3 * (size_t)ckpt + 1))) || (rc = adj_alloc(&A.D, nq * 3 * (size_t)ckpt)))
+    return rc;
+  // coefficients (coe1 = dtc / vol) as on the first sub-step
+  CoeArgs ca{};
+  ca.rop = Z.lvl[0]; ca.xmut_in = Z.xmut; ca.xmut = Z.xmut; ca.coe = Z.coe;
+  ca.lo[0] = 1; ca.hi[0] = z.ni; ca.lo[1] = 1; ca.hi[1] = z.nj; ca.lo[2] = 1; ca.hi[2] = z.nk;
+  CK(launch_coefficients(z, ca, s->st));
+  // initial state: level 0 with its ghosts filled
+  double* cur = A.W;
+  double* nxt = A.W + nq;
+  CK(cudaMemcpyAsync(cur, Z.lvl[0], sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
+  if ((rc = zone_fill(s, zone, cur))) return rc;
+  CK(cudaMemcpyAsync(A.ck[0], cur, sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
+  for (int n = 0; n < nsteps; n++) {
+    for (int st_ = 1; st_ <= 3; st_++) {
+      if ((rc = explicit_stage(s, zone, st_, cur, nxt, A.D))) return rc;
+      std::swap(cur, nxt);
+    }
+    if ((n + 1) % ckpt == 0 || n + 1 == nsteps)
+      CK(cudaMemcpyAsync(A.ck[(size_t)((n + 1 + ckpt - 1) / ckpt)], cur, sizeof(double) * nq,
+                         cudaMemcpyDeviceToDevice, s->st));
+  }
+  CK(cudaMemcpyAsync(Z.lvl[0], cur, sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return FGB_OK;
+}
+
+int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, double* lam_w0,
+                         double* lam_ti, double* lam_tj, double* lam_vol, double* lam_st) {
+  int rc = adj_check(s, zone);
+  if (rc) return rc;
+  fgb_solver::Adj& A = s->adj;
+  if (A.zone != zone || A.ck.empty()) return fail(FGB_ERR_STATE, "fgb_adjoint_forward first");
+  if (!lam_final || !lam_w0 || !lam_ti || !lam_tj || !lam_vol || !lam_st)
+    return fail(FGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  ZoneData& Z = s->zones[zone];
+  const Zone& z = Z.z;
+  const size_t nq = (size_t)z.neq * z.nd, nm = (size_t)z.ndm * 2;
+  const int ckpt = A.ckpt, nseg = (int)A.ck.size() - 1;
+  if (!A.lamW) {
+    if ((rc = adj_alloc(&A.lamW, nq)) || (rc = adj_alloc(&A.lamIn, nq)) || (rc = adj_alloc(&A.lamD, nq)) ||
+        (rc = adj_alloc(&A.lamTi, nm)) || (rc = adj_alloc(&A.lamTj, nm)) ||
+        (rc = adj_alloc(&A.lamVol, (size_t)z.ndm)) || (rc = adj_alloc(&A.lamSt, 5)))
+      return rc;
+  }
+  CK(cudaMemcpyAsync(A.lamW, lam_final, sizeof(double) * nq, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemsetAsync(A.lamD, 0, sizeof(double) * nq, s->st));
+  CK(cudaMemsetAsync(A.lamTi, 0, sizeof(double) * nm, s->st));
+  CK(cudaMemsetAsync(A.lamTj, 0, sizeof(double) * nm, s->st));
+  CK(cudaMemsetAsync(A.lamVol, 0, sizeof(double) * z.ndm, s->st));
+  CK(cudaMemsetAsync(A.lamSt, 0, sizeof(double) * 5, s->st));
+  for (int seg = nseg - 1; seg >= 0; seg--) {
+    const int n0 = seg * ckpt, steps = std::min(ckpt, A.nsteps - n0);
+    // recompute the segment: W[3t + st - 1] = input of stage st of step t
+    CK(cudaMemcpyAsync(A.W, A.ck[(size_t)seg], sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
+    for (int t = 0; t < steps; t++)
+      for (int st_ = 1; st_ <= 3; st_++) {
+        const size_t i = 3 * (size_t)t + st_ - 1;
+        // low-storage RK3: stages 2 and 3 start from coefH x the previous residual
+        if (st_ > 1)
+          CK(cudaMemcpyAsync(A.D + i * nq, A.D + (i - 1) * nq, sizeof(double) * nq,
+                             cudaMemcpyDeviceToDevice, s->st));
+        if ((rc = explicit_stage(s, zone, st_, A.W + i * nq, A.W + (i + 1) * nq, A.D + i * nq))) return rc;
+      }
+    for (int t = steps - 1; t >= 0; t--)
+      for (int st_ = 3; st_ >= 1; st_--) {
+        const size_t i = 3 * (size_t)t + st_ - 1;
+        // the stage output's ghost fill, the update, the face fluxes
+        if ((rc = zone_fill_adj(s, zone, A.W + (i + 1) * nq, A.lamW))) return rc;
+        CK(cudaMemsetAsync(A.lamIn, 0, sizeof(double) * nq, s->st));
+        CK(launch_adj_update(z, A.W + i * nq, A.D + i * nq, kCoefW[st_], A.lamW, A.lamIn, A.lamD,
+                             A.lamVol, s->st));
+        CK(launch_adj_faces(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, s->st));
+        for (WallCorrList& w : Z.walls)
+          CK(launch_adj_wall(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, wall_args(Z, w), s->st));
+        // D_st = coefH_st D_{st-1} + R: the earlier residual's adjoint
+        std::swap(A.lamW, A.lamIn);
+        if (st_ == 1) CK(cudaMemsetAsync(A.lamD, 0, sizeof(double) * nq, s->st));
+        else {
+          // scale lamD by coefH_st (a plain kernel over the array)
+          CK(launch_scale(A.lamD, (int64_t)nq, kCoefH[st_], s->st));
+        }
+      }
+  }
+  // the initial ghost fill
+  if ((rc = zone_fill_adj(s, zone, A.ck[0], A.lamW))) return rc;
+  CK(cudaMemcpyAsync(lam_w0, A.lamW, sizeof(double) * nq, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(lam_ti, A.lamTi, sizeof(double) * nm, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(lam_tj, A.lamTj, sizeof(double) * nm, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(lam_vol, A.lamVol, sizeof(double) * z.ndm, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(lam_st, A.lamSt, sizeof(double) * 5, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return FGB_OK;
+}
+
+int fgb_tangent(fgb_solver* s, int zone, int nsteps, const double* dw0, const double* dti,
+                const double* dtj, const double* dvol, const double* dst, double* dw_final) {
+  int rc = adj_check(s, zone);
+  if (rc) return rc;
+  if (!dw0 || !dti || !dtj || !dvol || !dst || !dw_final) return fail(FGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->st));
+  fgb_solver::Adj& A = s->adj;
+  ZoneData& Z = s->zones[zone];
+  const Zone& z = Z.z;
+  const size_t nq = (size_t)z.neq * z.nd, nm = (size_t)z.ndm * 2;
+  const size_t nf = (size_t)z.neq * (size_t)(std::max(z.ni + 1, (int64_t)1) * (z.nj + 1));
+  if (!A.dW) {
+    if ((rc = adj_alloc(&A.dW, nq)) || (rc = adj_alloc(&A.dWn, nq)) || (rc = adj_alloc(&A.dD, nq)) ||
+        (rc = adj_alloc(&A.dFi, nf)) || (rc = adj_alloc(&A.dFj, nf)) || (rc = adj_alloc(&A.dTi, nm)) ||
+        (rc = adj_alloc(&A.dTj, nm)) || (rc = adj_alloc(&A.dVol, (size_t)z.ndm)) ||
+        (rc = adj_alloc(&A.dSt, 5)))
+      return rc;
+  }
+  double *W = nullptr, *Wn = nullptr, *D = nullptr;
+  if ((rc = adj_alloc(&W, nq)) || (rc = adj_alloc(&Wn, nq)) || (rc = adj_alloc(&D, nq))) return rc;
+  CK(cudaMemcpyAsync(A.dW, dw0, sizeof(double) * nq, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(A.dTi, dti, sizeof(double) * nm, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(A.dTj, dtj, sizeof(double) * nm, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(A.dVol, dvol, sizeof(double) * z.ndm, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(A.dSt, dst, sizeof(double) * 5, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemsetAsync(A.dD, 0, sizeof(double) * nq, s->st));
+  CoeArgs ca{};
+  ca.rop = Z.lvl[0]; ca.xmut_in = Z.xmut; ca.xmut = Z.xmut; ca.coe = Z.coe;
+  ca.lo[0] = 1; ca.hi[0] = z.ni; ca.lo[1] = 1; ca.hi[1] = z.nj; ca.lo[2] = 1; ca.hi[2] = z.nk;
+  CK(launch_coefficients(z, ca, s->st));
+  CK(cudaMemcpyAsync(W, Z.lvl[0], sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
+  if ((rc = zone_fill(s, zone, W))) return rc;
+  if ((rc = zone_fill_tan(s, zone, W, A.dW))) return rc;
+  for (int n = 0; n < nsteps; n++)
+    for (int st_ = 1; st_ <= 3; st_++) {
+      CK(launch_tan_faces(z, W, A.dW, A.dTi, A.dTj, A.dFi, A.dFj, s->st));
+      if ((rc = explicit_stage(s, zone, st_, W, Wn, D))) return rc;
+      CK(launch_tan_balance(z, kCoefH[st_], st_ == 1, A.dFi, A.dFj, A.dD, s->st));
+      for (WallCorrList& w : Z.walls)
+        CK(launch_tan_wall(z, W, A.dW, A.dTi, A.dTj, A.dD, wall_args(Z, w), s->st));
+      CK(launch_tan_apply(z, W, D, kCoefW[st_], A.dW, A.dD, A.dVol, A.dWn, s->st));
+      if ((rc = zone_fill_tan(s, zone, Wn, A.dWn))) return rc;
+      std::swap(W, Wn);
+      std::swap(A.dW, A.dWn);
+    }
+  CK(cudaMemcpyAsync(dw_final, A.dW, sizeof(double) * nq, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  cudaFree(W); cudaFree(Wn); cudaFree(D);
   return FGB_OK;
 }
 

@@ -24,10 +24,20 @@ namespace fgb {
 // Slope/o1_slope_var.for, o3_slope_var.for, minmod_slope_var.for.
 // a = q(l-2*inc), b = q(l-inc), c = q(l), d = q(l+inc); qm = right state of
 // the face (cell l side), qp = left state.
+// van Albada's smooth averaged slope of the differences x, y (VANALBADA;
+// differentiable, for the adjoint): ((y^2 + e) x + (x^2 + e) y) / (x^2 + y^2 + 2e)
+__device__ __forceinline__ double vanalbada(double x, double y) {
+  const double e2 = 1e-12;
+  return ((y * y + e2) * x + (x * x + e2) * y) / (x * x + y * y + 2. * e2);
+}
+
 template <int SL>
 __device__ __forceinline__ void reconstruct(const Zone& z, double a, double b, double c, double d,
                                             double roff, double& qm, double& qp) {
-  if (SL == O1) {
+  if (SL == VANALBADA) {
+    qm = c - 0.5 * vanalbada(c - b, d - c);
+    qp = b + 0.5 * vanalbada(b - a, c - b);
+  } else if (SL == O1) {
     qm = c;
     qp = b;
   } else if (SL == O3) {
@@ -813,6 +823,7 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
                                      : launch_faces_t<Z3DCART, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
       if (z.slope == MINMOD) return visc ? launch_faces_t<Z3DCART, ROE, MINMOD, true>(z, q, xmut, Fi, Fj, Fk, st)
                                          : launch_faces_t<Z3DCART, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == VANALBADA && !visc) return launch_faces_t<Z3DCART, ROE, VANALBADA, false>(z, q, xmut, Fi, Fj, Fk, st);
     } else if (z.kflu == AUSM && z.slope == O3) {
       return visc ? launch_faces_t<Z3DCART, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z3DCART, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
@@ -828,6 +839,7 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
                                      : launch_faces_t<Z3DFULL, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
       if (z.slope == MINMOD) return visc ? launch_faces_t<Z3DFULL, ROE, MINMOD, true>(z, q, xmut, Fi, Fj, Fk, st)
                                          : launch_faces_t<Z3DFULL, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == VANALBADA && !visc) return launch_faces_t<Z3DFULL, ROE, VANALBADA, false>(z, q, xmut, Fi, Fj, Fk, st);
     } else if (z.kflu == AUSM && z.slope == O3) {
       return visc ? launch_faces_t<Z3DFULL, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z3DFULL, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
@@ -841,6 +853,7 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
       if (z.slope == O1) return launch_faces_t<Z2D, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
       if (z.slope == O3) return launch_faces_t<Z2D, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
       if (z.slope == MINMOD) return launch_faces_t<Z2D, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == VANALBADA) return launch_faces_t<Z2D, ROE, VANALBADA, false>(z, q, xmut, Fi, Fj, Fk, st);
     } else if (z.kflu == AUSM && z.slope == O3) {
       return launch_faces_t<Z2D, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
@@ -929,6 +942,7 @@ static void wall_corr_sl(const Zone& z, const double* q, double* drodm, const Wa
   const unsigned g = (unsigned)((a.n + 127) / 128);
   if (z.slope == O1) wall_corr<D, TYP, O1><<<g, 128, 0, st>>>(z, q, drodm, a);
   else if (z.slope == O3) wall_corr<D, TYP, O3><<<g, 128, 0, st>>>(z, q, drodm, a);
+  else if (z.slope == VANALBADA) wall_corr<D, TYP, VANALBADA><<<g, 128, 0, st>>>(z, q, drodm, a);
   else wall_corr<D, TYP, MINMOD><<<g, 128, 0, st>>>(z, q, drodm, a);
 }
 

@@ -134,4 +134,35 @@ cudaError_t launch_norms_finish(const double* part, int64_t nblocks, int neq, do
                                 double dtc, double* out, cudaStream_t st);
 cudaError_t run_fp64_probe(int nsm, int iters, double* out, cudaStream_t st);
 
+// fgb_adjoint.cu: tangent / adjoint of the explicit 2-d Euler step (Roe +
+// van Albada), from local Jacobians of the face flux, BC and update formulas
+cudaError_t launch_adj_faces(const Zone& z, const double* q, const double* lamD, double* lamQ,
+                             double* lamTi, double* lamTj, cudaStream_t st);
+cudaError_t launch_tan_faces(const Zone& z, const double* q, const double* dq, const double* dTi,
+                             const double* dTj, double* dFi, double* dFj, cudaStream_t st);
+cudaError_t launch_adj_update(const Zone& z, const double* q, const double* D, double coefW,
+                              double* lamOut, double* lamIn, double* lamD, double* lamVol,
+                              cudaStream_t st);
+cudaError_t launch_tan_balance(const Zone& z, double coefH, int zero, const double* dFi,
+                               const double* dFj, double* dD, cudaStream_t st);
+cudaError_t launch_tan_apply(const Zone& z, const double* q, const double* D, double coefW,
+                             const double* dIn, const double* dD, const double* dVol, double* dOut,
+                             cudaStream_t st);
+cudaError_t launch_adj_wall(const Zone& z, const double* q, const double* lamD, double* lamQ,
+                            double* lamTi, double* lamTj, const WallCorrArgs& a, cudaStream_t st);
+cudaError_t launch_tan_wall(const Zone& z, const double* q, const double* dq, const double* dTi,
+                            const double* dTj, double* dD, const WallCorrArgs& a, cudaStream_t st);
+cudaError_t launch_adj_bc_face(const double* q, double* lam, const BcFaceArgs& a, const int32_t* mt,
+                               int64_t ndm, double* lamT, double* lamSt, cudaStream_t st);
+cudaError_t launch_tan_bc_face(const double* q, double* dq, const BcFaceArgs& a, const int32_t* mt,
+                               int64_t ndm, const double* dT, const double* dSt, cudaStream_t st);
+cudaError_t launch_lin_bc_next(const double* q, double* x, const BcNextArgs& a, int adjoint, int nv,
+                               cudaStream_t st);
+cudaError_t launch_adj_gather(double* lam, int64_t nd, const int32_t* d_idx, const int32_t* s_idx,
+                              int64_t n, int nv, cudaStream_t st);
+cudaError_t launch_scale(double* x, int64_t n, double c, cudaStream_t st);
+cudaError_t launch_adj_coins(double* lam, int64_t nd, const int32_t* dst, const int32_t* a,
+                             const int32_t* b, const int32_t* c, int64_t n_edge, int64_t n, int nv,
+                             cudaStream_t st);
+
 }  // namespace fgb

@@ -58,7 +58,7 @@ keys4Zone = {
     "epsi_linear": 1, "nudging_ampli": 1, "nudging_vector": 3, "inj1_newton_tol": 1,
     "inj1_newton_nit": 0, "cfl": 1, "niveaux_temps": 0, "psiroe": 1, "ausmDamping": 1,
     "coef_hyper": 4, "prandtltb": 1, "sfd": 0, "sfd_chi": 1, "sfd_delta": 1, "sfd_init_iter": 0,
-    "slope": ["o1", "o3", "o5", "minmod", "o3sc", "o5sc"],
+    "slope": ["o1", "o3", "o5", "minmod", "o3sc", "o5sc", "vanalbada"],
     "DES": ["zdes1", "zdes1_w", "zdes2", "zdes2_w", "zdes3", "zdes3_w"], "SA_add_LowRe": 0,
     "SA_add_RotCorr": 0, "snear": 1, "DES_debug": 0, "extract_res": 0, "IBC": 3, "source": 0,
     "Cups": 4, "senseurType": 0, "ratiom": 1,
@@ -195,7 +195,9 @@ def _buildOwnData(t):
             raise ValueError(f"Fast: model {model} is invalid.")
         itypcp = 2 if temporal == "explicit" else 1
         slope = zn["slope"]
-        islope = {"o1": 1, "o2": 4, "o3": 2, "o5": 5, "minmod": 3, "o3sc": 6, "o5sc": 7}[slope]
+        # "vanalbada" (8) is not a FastS slope: a smooth limiter for the adjoint
+        islope = {"o1": 1, "o2": 4, "o3": 2, "o5": 5, "minmod": 3, "o3sc": 6, "o5sc": 7,
+                  "vanalbada": 8}[slope]
         scheme = zn["scheme"]
         kfludom = {"ausmpred": 1, "senseur": 2, "dfcentre6": 3, "roe_kap": 5, "roe_min": 5,
                    "roe_nul": 5, "roe": 5, "senseur_hyper": 8}[scheme]

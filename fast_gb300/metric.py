@@ -185,13 +185,31 @@ def _corners_k(a, sl_i, sl_j, sl_k):
             a[sl_i.start + 1:sl_i.stop + 1, sl_j.start + 1:sl_j.stop + 1, k:k + 1])
 
 
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def _zeros(shape, like):
+    if _is_torch(like):
+        import torch
+        return torch.zeros(shape, dtype=like.dtype, device=like.device)
+    return np.zeros(shape)
+
+
+def _flat_f(a):
+    """Fortran-order flattening of a 2-d array (numpy or torch)."""
+    return a.t().reshape(-1) if _is_torch(a) else a.reshape(-1, order="F")
+
+
 def _compute_2d(x, y, z):
     """2-d zone (one cell in k, no k ghosts): cp_tijk.for 2-d branch (i and
     j faces, x and y components) and cp_vol.for 2-d branch, on the vertex
-    grid of the k = 1 layer (lt = flat index of vertex (i, j))."""
+    grid of the k = 1 layer (lt = flat index of vertex (i, j)).  Takes numpy
+    or torch arrays (the same operations in the same order, so the same
+    values; torch arrays keep the autograd graph from the coordinates)."""
     nvi, nvj, _ = x.shape
-    ti = np.zeros((2, nvi, nvj))
-    tj = np.zeros((2, nvi, nvj))
+    ti = _zeros((2, nvi, nvj), x)
+    tj = _zeros((2, nvi, nvj), x)
     cells = (slice(0, nvi - 1), slice(0, nvj - 1))
     def v(a, di, dj, dk):
         return a[di:nvi - 1 + di, dj:nvj - 1 + dj, dk]
@@ -232,8 +250,14 @@ def _compute_2d(x, y, z):
     tkz11 = (X[1] - X[5]) * (Y[0] - Y[1]) - (Y[1] - Y[5]) * (X[0] - X[1])
     tk1 = 0.5 * (tkz10 + tkz11)
     az = 0.25 * (((((((Z[2] + Z[3]) + Z[6]) + Z[7]) - Z[0]) - Z[1]) - Z[4]) - Z[5]) * tk1
-    vol = np.zeros((nvi, nvj))
-    vol[cells] = np.maximum(((comp[0] + comp[1]) + az) / 3.0, 1.0e-30)
+    vol = _zeros((nvi, nvj), x)
+    v = ((comp[0] + comp[1]) + az) / 3.0
+    vol[cells] = v.clamp_min(1.0e-30) if _is_torch(v) else np.maximum(v, 1.0e-30)
+    if _is_torch(x):
+        import torch
+        return (torch.cat([_flat_f(ti[c]) for c in range(2)]),
+                torch.cat([_flat_f(tj[c]) for c in range(2)]),
+                _zeros((0,), x), _flat_f(vol))
     return (np.concatenate([ti[c].reshape(-1, order="F") for c in range(2)]),
             np.concatenate([tj[c].reshape(-1, order="F") for c in range(2)]),
             np.zeros(0),

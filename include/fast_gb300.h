@@ -112,6 +112,30 @@ int fgb_apply_bc(fgb_solver* s, int level);
  * recorded); returns nit through *nit_out. */
 int fgb_residuals(fgb_solver* s, int zone, double* out, int64_t n, int* nit_out);
 
+/* Exterior state (conservative ro, ro u, ro v, ro w, ro E) of every farfield
+ * / inflow / outflow BC of a zone, replacing the free stream (BCzone.cpp
+ * DEFAULT_STATE, or the nbdata = 21 per-BC state). */
+int fgb_set_bc_state(fgb_solver* s, int zone, const double* st);
+
+/* Differentiation of the explicit solve of a 2-d Euler zone (RK3, Roe +
+ * van Albada MUSCL, slip walls, characteristic farfield, self 1-to-1
+ * interfaces); no reference counterpart.
+ * fgb_adjoint_forward: from the state at level 0 (its ghosts filled here),
+ *   nsteps RK3 steps, keeping every ckpt-th state; the final state replaces
+ *   level 0.
+ * fgb_adjoint_backward: given dJ/dW_final (NEQ*NDIMDX, host), the gradient
+ *   of J with respect to the initial state (NEQ*NDIMDX), the metric arrays ti
+ *   and tj (2*NDIMDX_MTR each), vol (NDIMDX_MTR) and the farfield state (5),
+ *   by the discrete adjoint of every stage (segments recomputed from their
+ *   checkpoints, then swept in reverse).
+ * fgb_tangent: the forward-mode derivative dW_final of the same run for
+ *   perturbations of the initial state, ti, tj, vol and the farfield state. */
+int fgb_adjoint_forward(fgb_solver* s, int zone, int nsteps, int ckpt);
+int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, double* lam_w0,
+                         double* lam_ti, double* lam_tj, double* lam_vol, double* lam_st);
+int fgb_tangent(fgb_solver* s, int zone, int nsteps, const double* dw0, const double* dti,
+                const double* dtj, const double* dvol, const double* dst, double* dw_final);
+
 /* Size, in doubles, of the fixed device array that holds the per-block
  * partials of fgb_residual_norms_noalloc (256 KB): a zone qualifies when
  * 2 * neq * (its number of LU blocks) <= FGB_NORM_PARTIALS_MAX, i.e. up to

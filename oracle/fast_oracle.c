@@ -477,6 +477,15 @@ static inline double avmin(double c, double r) {
   return fsign(1., c) * OMAX(0., OMIN(fabs(c), fsign(1., c) * r));
 }
 
+/* van Albada's smooth limiter (slope = 8; not a FastS slope): the averaged
+ * slope ((y^2 + e) x + (x^2 + e) y) / (x^2 + y^2 + 2 e), e = 1e-12, of the
+ * backward / forward differences x, y (van Albada, van Leer & Roberts,
+ * Astron. Astrophys. 108, 1982); differentiable everywhere. */
+static inline double vanalbada(double x, double y) {
+  const double e2 = 1e-12;
+  return ((y * y + e2) * x + (x * x + e2) * y) / (x * x + y * y + 2. * e2);
+}
+
 /* Slope/{o1,o3,minmod}_slope_var.for: qm = right state, qp = left state */
 static void slopes(const fctx* c, int64_t l, int64_t inc, double qm[6], double qp[6]) {
   const double* rop = c->rop;
@@ -490,6 +499,11 @@ static void slopes(const fctx* c, int64_t l, int64_t inc, double qm[6], double q
     } else if (c->slope == 2) {
       qm[v] = c->c4 * rop[l + vs] + c->c5 * rop[nm + vs] + c->c6 * rop[np + vs];
       qp[v] = c->c4 * rop[nm + vs] + c->c6 * rop[nm2 + vs] + c->c5 * rop[l + vs];
+    } else if (c->slope == 8) { /* van Albada MUSCL */
+      double d1 = rop[nm + vs] - rop[nm2 + vs], d2 = rop[l + vs] - rop[nm + vs];
+      double d3 = rop[np + vs] - rop[l + vs];
+      qm[v] = rop[l + vs] - 0.5 * vanalbada(d2, d3);
+      qp[v] = rop[nm + vs] + 0.5 * vanalbada(d1, d2);
     } else { /* minmod */
       double roff = .5 * OMAX(0., OMIN(rop[l + 4 * nd] * c->tmin_1 - .5, 1.));
       double delm = rop[l + vs] - rop[nm + vs];

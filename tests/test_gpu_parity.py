@@ -547,3 +547,19 @@ def test_channel_inviscid_multiblock_equals_single_block():
         out.append(G)
         s.close()
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("wavy,two_d", [(0.0, False), (0.3, False), (0.3, True)])
+def test_roe_vanalbada_explicit(oracle_mod, wavy, two_d):
+    """Roe + van Albada MUSCL (slope 8, the smooth limiter of the adjoint
+    path) on cartesian, curvilinear and 2-d zones."""
+    n = (20, 16, 1) if two_d else (20, 16, 6)
+    t = cases.isentropic_vortex(n=n, wavy=wavy, two_d=two_d,
+                                numz={"scheme": "roe", "slope": "vanalbada", "time_step": 0.05})
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    assert int(zd[0]["pi"][64]) == 8
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
