@@ -54,9 +54,10 @@ def parse():
                    help="time to a 1e-10 Newton residual drop, FP64 vs mixed sweeps")
     p.add_argument("--ttc-n", type=int, default=256)
     p.add_argument("--ttc-max", type=int, default=100, help="max sub-iterations per step")
-    p.add_argument("--workload", default="tgv", choices=["tgv", "channel", "batch"],
+    p.add_argument("--workload", default="tgv", choices=["tgv", "channel", "batch", "adjoint"],
                    help="tgv: the headline 256^3 case; channel: 48-block SA channel; "
-                        "batch: 64 independent Taylor-Green cases")
+                        "batch: 64 independent Taylor-Green cases; adjoint: gradient of the "
+                        "C-grid wall force (cost against the primal, tangent and FD checks)")
     p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
                    help="64: plain FP64 path; 32: FP32 LU-SGS sweeps (mixed precision)")
     return p.parse_args()
@@ -380,6 +381,49 @@ def run_multizone(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args):
+    """Adjoint / primal cost on the differentiation case: C-grid 385 x 129,
+    8 Hicks-Henne amplitudes + M_inf, Roe + van Albada, RK3, 400 steps,
+    checkpoints every 20.  Times (CUDA-synchronised wall clock of the
+    device work) of the primal run and of the adjoint (recomputation +
+    reverse sweep), the gradient, its agreement with the forward-mode tangent
+    along two directions and with central differences (h = 1e-6, 1e-7)."""
+    import numpy as np
+    import torch
+    from fast_gb300 import adjoint as A
+    case = A.CGridCase()
+    alpha = torch.from_numpy(np.random.default_rng(4).uniform(-0.005, 0.005, 8))
+    mach = torch.tensor(0.7, dtype=torch.float64)
+    for _ in range(max(1, args.warmup)):
+        A.gradient(case, alpha, mach)
+    prim, adj = [], []
+    for _ in range(max(1, args.steps)):
+        J, ga, gm = A.gradient(case, alpha, mach)
+        prim.append(case.timing["primal_s"])
+        adj.append(case.timing["adjoint_s"])
+    grad = np.concatenate([ga, [gm]])
+    rng = np.random.default_rng(5)
+    tang = []
+    for _ in range(2):
+        d = rng.standard_normal(9)
+        dJ = A.tangent(case, alpha, mach, torch.from_numpy(d[:8]), torch.tensor(d[8], dtype=torch.float64))
+        tang.append(abs(dJ - grad @ d) / abs(dJ))
+    scale = float(np.max(np.abs(grad)))
+    fd6 = A.fd_gradient(case, alpha, mach, h=1e-6)
+    fd7 = A.fd_gradient(case, alpha, mach, h=1e-7)
+    tp, ta = float(np.median(prim)), float(np.median(adj))
+    line = {"metric": "adjoint/primal cost", "value": ta / tp, "unit": "x primal",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "cgrid_385x129_roe_vanalbada_rk3_400_steps_ckpt20",
+                       "parameters": "8 Hicks-Henne amplitudes + M_inf", "mach": 0.7},
+            "primal_s": tp, "adjoint_s": ta, "J": J, "gradient": grad.tolist(),
+            "tangent_rel_err": tang,
+            "fd_rel_err_h1e-6": float(np.max(np.abs(fd6 - grad)) / scale),
+            "fd_rel_err_h1e-7": float(np.max(np.abs(fd7 - grad)) / scale)}
+    print(json.dumps(line), flush=True)
+
+
 def run_ttc(args):
     """Time to a 1e-10 drop of the Newton residual within one physical step.
 
@@ -443,6 +487,9 @@ def main():
     args = parse()
     if args.ttc:
         run_ttc(args)
+        return
+    if args.workload == "adjoint" and args.impl == "ours":
+        run_adjoint(args)
         return
     if args.workload != "tgv" and args.impl == "ours":
         run_multizone(args)

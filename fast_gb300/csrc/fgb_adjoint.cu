@@ -83,6 +83,20 @@ template <typename T> __device__ __forceinline__ double tsign(double c, const T&
   return copysign(::fabs(c), val(x));
 }
 
+// Input seeding of a local Jacobian: N > 1 -- input idx is direction idx
+// (the whole Jacobian); N == 1 -- only input col is seeded (its column, one
+// lane per column)
+template <int N>
+__device__ __forceinline__ Dual<N> seed(double x, int idx, int col) {
+  Dual<N> r(x);
+  if (N == 1) {
+    if (idx == col) r.d[0] = 1.;
+  } else {
+    r.d[idx] = 1.;
+  }
+  return r;
+}
+
 // ------------------------------------------------------ restated formulas
 template <typename T>
 __device__ __forceinline__ T vanalbada_t(const T& x, const T& y) {
@@ -148,6 +162,200 @@ __device__ __forceinline__ void roe2d(const Zone& z, const T qm[5], const T qp[5
   F[4] = (fl5 + rou1 * h1 + rou2 * h2) * 0.5;
 }
 
+// Reverse mode of roe2d, written out: given the output adjoints Fb (F[3]
+// unused), adds d(Fb . F)/d(input) to qmb, qpb (variables 0, 1, 2, 4) and
+// tb[0..1] (tcx, tcy).  Forward pass with every intermediate kept, then the
+// chain rule in reverse order; |x| and the entropy-fix switches take the
+// derivative of the branch the value selects (the dual numbers' rule).
+__device__ __forceinline__ double sgn1(double x) { return x < 0. ? -1. : 1.; }
+
+__device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5], double tcx,
+                          double tcy, const double Fb[5], double qmb[5], double qpb[5], double tb[2]) {
+  const double rgp = z.rgp, gam1 = z.gam1, g_ = z.gam - 1., psi = z.psiroe;
+  // ---- forward
+  const double ss = tcx * tcx + tcy * tcy, s = ::sqrt(ss);
+  const double r1 = qp[0], p1 = r1 * qp[4] * rgp;
+  const double h1 = gam1 * qp[4] * rgp + .5 * (qp[1] * qp[1] + qp[2] * qp[2]);
+  const double r2 = qm[0], p2 = r2 * qm[4] * rgp;
+  const double h2 = gam1 * qm[4] * rgp + .5 * (qm[1] * qm[1] + qm[2] * qm[2]);
+  const double s1 = ::sqrt(r1), s2 = ::sqrt(r2);
+  const double r = s1 * s2, r_1 = 1. / (s1 + s2);
+  const double t7u = s1 * qp[1] + s2 * qm[1], t7v = s1 * qp[2] + s2 * qm[2];
+  const double u = t7u * r_1, v = t7v * r_1;
+  const double t8 = s1 * h1 + s2 * h2, h = t8 * r_1;
+  const double q = .5 * (u * u + v * v);
+  const double hq = h - q, c = ::sqrt(g_ * ::fabs(hq));
+  const double qn1 = qp[1] * tcx + qp[2] * tcy, qn2 = qm[1] * tcx + qm[2] * tcy;
+  const double du = (qm[1] - qp[1]) * s, dv = (qm[2] - qp[2]) * s;
+  const double dp = p2 - p1, dqn = qn2 - qn1;
+  const bool smax_on = s > 1.E-30;
+  const double s_1 = 1.0 / (smax_on ? s : 1.E-30);
+  const double nx = tcx * s_1, ny = tcy * s_1;
+  const double qn = u * nx + v * ny;
+  const double A1 = ::fabs(qn), f4 = psi * (A1 + c);
+  const double f2a = 0.5 + copysign(0.5, A1 - f4);
+  const double f3a = (f2a - 1.0) * (qn * qn / f4 + f4) * 0.5 - f2a * A1;
+  const double c2 = c * c;
+  const double Z = r2 - r1 - dp / c2, f1a = Z * s;
+  const double X2 = f1a * u + r * (du - nx * dqn), X3 = f1a * v + r * (dv - ny * dqn);
+  const double Y5 = u * du + v * dv - qn * dqn, X5 = f1a * q + r * Y5;
+  const double l4 = qn + c, A4 = ::fabs(l4);
+  const double f2b = 0.5 + copysign(0.5, A4 - f4);
+  const double f3b = (f2b - 1.) * (l4 * l4 / f4 + f4) * 0.5 - f2b * A4;
+  const double N4 = dp + r * c * dqn * s_1, K4 = N4 / (2. * c2), f1b = K4 * s * f3b;
+  const double l5 = qn - c, A5 = ::fabs(l5);
+  const double f2c = 0.5 + copysign(0.5, A5 - f4);
+  const double f3c = (f2c - 1.) * (l5 * l5 / f4 + f4) * 0.5 - f2c * A5;
+  const double N5 = dp - r * c * dqn * s_1, K5 = N5 / (2. * c2), f1c = K5 * f3c * s;
+  const double rou1 = r1 * qn1, rou2 = r2 * qn2, p1p2 = p1 + p2;
+  // ---- reverse
+  double r1b = 0., r2b = 0., qn1b = 0., qn2b = 0., p1b = 0., p2b = 0., h1b = 0., h2b = 0.;
+  double ub = 0., vb = 0., hb = 0., qb = 0., cb = 0., rb = 0., nxb = 0., nyb = 0., qnb = 0.;
+  double dub = 0., dvb = 0., dpb = 0., dqnb = 0., sb = 0., s_1b = 0., f4b = 0., c2b = 0.;
+  double tcxb = 0., tcyb = 0.;
+  const double b0 = 0.5 * Fb[0], b1 = 0.5 * Fb[1], b2 = 0.5 * Fb[2], b4 = 0.5 * Fb[4];
+  const double fl1b = b0, fl2b = b1, fl3b = b2, fl5b = b4;
+  const double rou1b = b0 + b1 * qp[1] + b2 * qp[2] + b4 * h1;
+  const double rou2b = b0 + b1 * qm[1] + b2 * qm[2] + b4 * h2;
+  qpb[1] += b1 * rou1; qmb[1] += b1 * rou2; qpb[2] += b2 * rou1; qmb[2] += b2 * rou2;
+  tcxb += b1 * p1p2; tcyb += b2 * p1p2;
+  const double p1p2b = b1 * tcx + b2 * tcy;
+  h1b += b4 * rou1; h2b += b4 * rou2;
+  r1b += rou1b * qn1; qn1b += rou1b * r1; r2b += rou2b * qn2; qn2b += rou2b * r2;
+  p1b += p1p2b; p2b += p1p2b;
+  // wave 5 (qn - c)
+  {
+    const double f1cb = fl1b + fl2b * (u - nx * c) + fl3b * (v - ny * c) + fl5b * (h - qn * c);
+    ub += fl2b * f1c; nxb -= fl2b * f1c * c; cb -= fl2b * f1c * nx;
+    vb += fl3b * f1c; nyb -= fl3b * f1c * c; cb -= fl3b * f1c * ny;
+    hb += fl5b * f1c; qnb -= fl5b * f1c * c; cb -= fl5b * f1c * qn;
+    const double K5b = f1cb * f3c * s, f3cb = f1cb * K5 * s;
+    sb += f1cb * K5 * f3c;
+    const double N5b = K5b / (2. * c2);
+    c2b -= K5b * K5 / c2;
+    dpb += N5b; rb -= N5b * c * dqn * s_1; cb -= N5b * r * dqn * s_1;
+    dqnb -= N5b * r * c * s_1; s_1b -= N5b * r * c * dqn;
+    double l5b = f3cb * (f2c - 1.) * l5 / f4;
+    f4b += f3cb * (f2c - 1.) * 0.5 * (1. - l5 * l5 / (f4 * f4));
+    l5b += -f3cb * f2c * sgn1(l5);
+    qnb += l5b; cb -= l5b;
+  }
+  // wave 4 (qn + c)
+  {
+    const double f1bb = fl1b + fl2b * (u + nx * c) + fl3b * (v + ny * c) + fl5b * (h + qn * c);
+    ub += fl2b * f1b; nxb += fl2b * f1b * c; cb += fl2b * f1b * nx;
+    vb += fl3b * f1b; nyb += fl3b * f1b * c; cb += fl3b * f1b * ny;
+    hb += fl5b * f1b; qnb += fl5b * f1b * c; cb += fl5b * f1b * qn;
+    const double K4b = f1bb * s * f3b, f3bb = f1bb * K4 * s;
+    sb += f1bb * K4 * f3b;
+    const double N4b = K4b / (2. * c2);
+    c2b -= K4b * K4 / c2;
+    dpb += N4b; rb += N4b * c * dqn * s_1; cb += N4b * r * dqn * s_1;
+    dqnb += N4b * r * c * s_1; s_1b += N4b * r * c * dqn;
+    double l4b = f3bb * (f2b - 1.) * l4 / f4;
+    f4b += f3bb * (f2b - 1.) * 0.5 * (1. - l4 * l4 / (f4 * f4));
+    l4b += -f3bb * f2b * sgn1(l4);
+    qnb += l4b; cb += l4b;
+  }
+  // wave 1 (qn)
+  {
+    const double f3ab = fl1b * f1a + fl2b * X2 + fl3b * X3 + fl5b * X5;
+    double f1ab = fl1b * f3a;
+    const double X2b = fl2b * f3a, X3b = fl3b * f3a, X5b = fl5b * f3a;
+    f1ab += X2b * u; ub += X2b * f1a; rb += X2b * (du - nx * dqn); dub += X2b * r;
+    nxb -= X2b * r * dqn; dqnb -= X2b * r * nx;
+    f1ab += X3b * v; vb += X3b * f1a; rb += X3b * (dv - ny * dqn); dvb += X3b * r;
+    nyb -= X3b * r * dqn; dqnb -= X3b * r * ny;
+    f1ab += X5b * q; qb += X5b * f1a; rb += X5b * Y5;
+    ub += X5b * r * du; dub += X5b * r * u; vb += X5b * r * dv; dvb += X5b * r * v;
+    qnb -= X5b * r * dqn; dqnb -= X5b * r * qn;
+    const double Zb = f1ab * s;
+    sb += f1ab * Z;
+    r2b += Zb; r1b -= Zb; dpb -= Zb / c2; c2b += Zb * dp / (c2 * c2);
+    qnb += f3ab * (f2a - 1.) * qn / f4;
+    f4b += f3ab * (f2a - 1.) * 0.5 * (1. - qn * qn / (f4 * f4));
+    const double A1b = -f3ab * f2a + f4b * psi;
+    cb += f4b * psi;
+    qnb += A1b * sgn1(qn);
+  }
+  cb += 2. * c * c2b;
+  ub += qnb * nx; nxb += qnb * u; vb += qnb * ny; nyb += qnb * v;
+  tcxb += nxb * s_1; s_1b += nxb * tcx; tcyb += nyb * s_1; s_1b += nyb * tcy;
+  if (smax_on) sb += -s_1b * s_1 * s_1;
+  p2b += dpb; p1b -= dpb; qn2b += dqnb; qn1b -= dqnb;
+  qmb[1] += dub * s; qpb[1] -= dub * s; sb += dub * (qm[1] - qp[1]);
+  qmb[2] += dvb * s; qpb[2] -= dvb * s; sb += dvb * (qm[2] - qp[2]);
+  qpb[1] += qn1b * tcx; tcxb += qn1b * qp[1]; qpb[2] += qn1b * tcy; tcyb += qn1b * qp[2];
+  qmb[1] += qn2b * tcx; tcxb += qn2b * qm[1]; qmb[2] += qn2b * tcy; tcyb += qn2b * qm[2];
+  {
+    const double gb = cb * 0.5 / c;          // d / d(g_ |hq|)
+    const double hqb = gb * g_ * sgn1(hq);
+    hb += hqb; qb -= hqb;
+  }
+  ub += qb * u; vb += qb * v;
+  const double t8b = hb * r_1;
+  double r_1b = hb * t8;
+  double s1b = t8b * h1, s2b = t8b * h2;
+  h1b += t8b * s1; h2b += t8b * s2;
+  const double t7ub = ub * r_1, t7vb = vb * r_1;
+  r_1b += ub * t7u + vb * t7v;
+  s1b += t7ub * qp[1] + t7vb * qp[2]; s2b += t7ub * qm[1] + t7vb * qm[2];
+  qpb[1] += t7ub * s1; qmb[1] += t7ub * s2; qpb[2] += t7vb * s1; qmb[2] += t7vb * s2;
+  s1b += rb * s2; s2b += rb * s1;
+  const double denb = -r_1b * r_1 * r_1;
+  s1b += denb; s2b += denb;
+  r1b += s1b * 0.5 / s1; r2b += s2b * 0.5 / s2;
+  qmb[4] += h2b * gam1 * rgp; qmb[1] += h2b * qm[1]; qmb[2] += h2b * qm[2];
+  r2b += p2b * qm[4] * rgp; qmb[4] += p2b * r2 * rgp;
+  qpb[4] += h1b * gam1 * rgp; qpb[1] += h1b * qp[1]; qpb[2] += h1b * qp[2];
+  r1b += p1b * qp[4] * rgp; qpb[4] += p1b * r1 * rgp;
+  qpb[0] += r1b; qmb[0] += r2b;
+  const double ssb = sb * 0.5 / s;
+  tcxb += 2. * tcx * ssb; tcyb += 2. * tcy * ssb;
+  tb[0] += tcxb; tb[1] += tcyb;
+}
+
+// adjoint of one face: mu = d J / d F (per component) -> cells and normal.
+// The reconstructed states first (values only), the reverse Roe pass, then
+// per variable the reconstruction derivatives (recomputed, 3 duals) and the
+// scatter: the derivatives are not live across the Roe pass.
+template <int D>
+__device__ __forceinline__ void face_adjoint(const Zone& z, const double* __restrict__ q,
+                                             int64_t l, int64_t lt, const double mu[5],
+                                             double* __restrict__ lamQ, double* __restrict__ lamT) {
+  const int64_t inc = z.inc[D], nd = z.nd;
+  double qm[5], qp[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    if (v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
+    const double* Q = q + v * nd;
+    const double a = Q[l - 2 * inc], b = Q[l - inc], c = Q[l], d = Q[l + inc];
+    qm[v] = c - 0.5 * vanalbada_t(c - b, d - c);
+    qp[v] = b + 0.5 * vanalbada_t(b - a, c - b);
+  }
+  const double* M = D == 0 ? z.ti : z.tj;
+  double qmb[5] = {0, 0, 0, 0, 0}, qpb[5] = {0, 0, 0, 0, 0}, tb[2] = {0, 0};
+  roe2d_rev(z, qm, qp, M[lt], M[lt + z.ndm], mu, qmb, qpb, tb);
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    const int v = m == 3 ? 4 : m;
+    const double* Q = q + v * nd;
+    const double a = Q[l - 2 * inc], b = Q[l - inc], c = Q[l], d = Q[l + inc];
+    Dual<3> B = var<3>(b, 0), C = var<3>(c, 1), Dd = var<3>(d, 2);
+    Dual<3> rm = C - 0.5 * vanalbada_t(C - B, Dd - C);
+    Dual<3> A = var<3>(a, 0), B2 = var<3>(b, 1), C2 = var<3>(c, 2);
+    Dual<3> rp = B2 + 0.5 * vanalbada_t(B2 - A, C2 - B2);
+    const int64_t o = v * nd;
+    const double gm = qmb[v], gp = qpb[v];
+    atomicAdd(lamQ + l - 2 * inc + o, gp * rp.d[0]);
+    atomicAdd(lamQ + l - inc + o, gm * rm.d[0] + gp * rp.d[1]);
+    atomicAdd(lamQ + l + o, gm * rm.d[1] + gp * rp.d[2]);
+    atomicAdd(lamQ + l + inc + o, gm * rm.d[2]);
+  }
+  atomicAdd(lamT + lt, tb[0]);
+  atomicAdd(lamT + lt + z.ndm, tb[1]);
+}
+
 // the four primitive variables of a 2-d state (w = 0 throughout)
 __device__ __constant__ const int V4[4] = {0, 1, 2, 4};
 
@@ -200,8 +408,10 @@ __device__ __forceinline__ void face_lin(const Zone& z, const double* __restrict
 }
 
 // adjoint: mu = lamD(l) [l interior] - lamD(l - inc) [l - inc interior]
+// (register-bounded to 3 blocks of 128 per SM: faster than the unbounded
+// 255-register build, measured on GB300)
 template <int D>
-__global__ void __launch_bounds__(128) adj_faces(Zone z, const double* __restrict__ q,
+__global__ void __launch_bounds__(128, 3) adj_faces(Zone z, const double* __restrict__ q,
                                                  const double* __restrict__ lamD,
                                                  double* __restrict__ lamQ,
                                                  double* __restrict__ lamT) {
@@ -217,27 +427,7 @@ __global__ void __launch_bounds__(128) adj_faces(Zone z, const double* __restric
 #pragma unroll
   for (int v = 0; v < 5; v++)
     mu[v] = (hi_in ? lamD[l + v * nd] : 0.) - (lo_in ? lamD[l - inc + v * nd] : 0.);
-  FaceLin L;
-  face_lin<D>(z, q, l, lt, L);
-  double g[10];
-#pragma unroll
-  for (int k = 0; k < 10; k++) {
-    double s = 0.;
-#pragma unroll
-    for (int v = 0; v < 5; v++) s += mu[v] * L.JF[v][k];
-    g[k] = s;
-  }
-#pragma unroll
-  for (int m = 0; m < 4; m++) {
-    const int64_t o = V4[m] * nd;
-    const double gm = g[m], gp = g[4 + m];
-    atomicAdd(lamQ + l - 2 * inc + o, gp * L.gp[m][0]);
-    atomicAdd(lamQ + l - inc + o, gm * L.gm[m][0] + gp * L.gp[m][1]);
-    atomicAdd(lamQ + l + o, gm * L.gm[m][1] + gp * L.gp[m][2]);
-    atomicAdd(lamQ + l + inc + o, gm * L.gm[m][2]);
-  }
-  atomicAdd(lamT + lt, g[8]);
-  atomicAdd(lamT + lt + z.ndm, g[9]);
+  face_adjoint<D>(z, q, l, lt, mu, lamQ, lamT);
 }
 
 // tangent: dF = J (dq, dt) into the face array (SoA, 5 x faces)
@@ -434,15 +624,16 @@ cudaError_t launch_tan_apply(const Zone& z, const double* q, const double* D, do
 // (t0, t1; t2 = 0 in 2-d) -- 10 duals over (l: ro, u, v, T; ia: ro, u, v,
 // T; t0, t1).  The Roe term is the face flux of face_lin with the sign
 // sens_c: it cancels the face's contribution to D(l0) of the balance.
-__device__ __forceinline__ void wallslip_lin(const double* __restrict__ q, int64_t nd, int64_t l,
-                                             int64_t ia, double t0v, double t1v, double rgp,
-                                             double gam2, double J[4][10]) {
-  typedef Dual<10> T;
-  const T rl = var<10>(q[l], 0), ul = var<10>(q[l + nd], 1), vl = var<10>(q[l + 2 * nd], 2),
-          Tl = var<10>(q[l + 4 * nd], 3);
-  const T ra = var<10>(q[ia], 4), ua = var<10>(q[ia + nd], 5), va = var<10>(q[ia + 2 * nd], 6),
-          Ta = var<10>(q[ia + 4 * nd], 7);
-  const T t0 = var<10>(t0v, 8), t1 = var<10>(t1v, 9);
+template <int N>
+__device__ __forceinline__ void wallslip_eval(const double* __restrict__ q, int64_t nd, int64_t l,
+                                              int64_t ia, double t0v, double t1v, double rgp,
+                                              double gam2, int col, double J[4][N]) {
+  typedef Dual<N> T;
+  const T rl = seed<N>(q[l], 0, col), ul = seed<N>(q[l + nd], 1, col),
+          vl = seed<N>(q[l + 2 * nd], 2, col), Tl = seed<N>(q[l + 4 * nd], 3, col);
+  const T ra = seed<N>(q[ia], 4, col), ua = seed<N>(q[ia + nd], 5, col),
+          va = seed<N>(q[ia + 2 * nd], 6, col), Ta = seed<N>(q[ia + 4 * nd], 7, col);
+  const T t0 = seed<N>(t0v, 8, col), t1 = seed<N>(t1v, 9, col);
   const T r = 0.5 * (rl + ra), u = 0.5 * (ul + ua), v = 0.5 * (vl + va);
   const T u_int = t0 * u + t1 * v - 0.;
   T p = Ta * ra * rgp;
@@ -454,59 +645,48 @@ __device__ __forceinline__ void wallslip_lin(const double* __restrict__ q, int64
 #pragma unroll
   for (int m = 0; m < 4; m++)
 #pragma unroll
-    for (int k = 0; k < 10; k++) J[m][k] = o[m]->d[k];
+    for (int k = 0; k < N; k++) J[m][k] = o[m]->d[k];
+}
+__device__ __forceinline__ void wallslip_lin(const double* __restrict__ q, int64_t nd, int64_t l,
+                                             int64_t ia, double t0v, double t1v, double rgp,
+                                             double gam2, double J[4][10]) {
+  wallslip_eval<10>(q, nd, l, ia, t0v, t1v, rgp, gam2, -1, J);
 }
 
+// the Roe part of the wall correction: the face adjoint with mu = sens_c lamD(l0)
 template <int D>
-__global__ void __launch_bounds__(128) adj_wall(Zone z, const double* __restrict__ q,
-                                                const double* __restrict__ lamD,
-                                                double* __restrict__ lamQ,
-                                                double* __restrict__ lamT, WallCorrArgs a) {
+__global__ void __launch_bounds__(128) adj_wall_roe(Zone z, const double* __restrict__ q,
+                                                    const double* __restrict__ lamD,
+                                                    double* __restrict__ lamQ,
+                                                    double* __restrict__ lamT, WallCorrArgs a) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
-  const int64_t l = a.l[e], l0 = a.l0[e], lt = a.lt[e], nd = z.nd, inc = z.inc[D];
+  const int64_t l = a.l[e], l0 = a.l0[e], lt = a.lt[e], nd = z.nd;
   double mu[5];
 #pragma unroll
   for (int v = 0; v < 5; v++) mu[v] = lamD[l0 + v * nd] * a.sens_c;
-  FaceLin L;
-  face_lin<D>(z, q, l, lt, L);
-  double g[10];
+  face_adjoint<D>(z, q, l, lt, mu, lamQ, lamT);
+}
+
+// the wall-flux part: sixteen lanes per face, lane k < 10 the column of input k
+template <int D>
+__global__ void __launch_bounds__(128) adj_wall_flux(Zone z, const double* __restrict__ q,
+                                                     const double* __restrict__ lamD,
+                                                     double* __restrict__ lamQ,
+                                                     double* __restrict__ lamT, WallCorrArgs a) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t e = gid >> 4;
+  const int k = (int)(gid & 15);
+  if (e >= a.n || k >= 10) return;
+  const int64_t l = a.l[e], l0 = a.l0[e], lt = a.lt[e], nd = z.nd, inc = z.inc[D];
+  double J[4][1];
+  wallslip_eval<1>(q, nd, l, l - inc, a.nrm[3 * e], a.nrm[3 * e + 1], a.rgp, a.gam2, k, J);
+  double w = 0.;
 #pragma unroll
-  for (int k = 0; k < 10; k++) {
-    double s = 0.;
-#pragma unroll
-    for (int v = 0; v < 5; v++) s += mu[v] * L.JF[v][k];
-    g[k] = s;
-  }
-#pragma unroll
-  for (int m = 0; m < 4; m++) {
-    const int64_t o = V4[m] * nd;
-    const double gm = g[m], gp = g[4 + m];
-    atomicAdd(lamQ + l - 2 * inc + o, gp * L.gp[m][0]);
-    atomicAdd(lamQ + l - inc + o, gm * L.gm[m][0] + gp * L.gp[m][1]);
-    atomicAdd(lamQ + l + o, gm * L.gm[m][1] + gp * L.gp[m][2]);
-    atomicAdd(lamQ + l + inc + o, gm * L.gm[m][2]);
-  }
-  atomicAdd(lamT + lt, g[8]);
-  atomicAdd(lamT + lt + z.ndm, g[9]);
-  // the wall flux
-  double J[4][10];
-  wallslip_lin(q, nd, l, l - inc, a.nrm[3 * e], a.nrm[3 * e + 1], a.rgp, a.gam2, J);
-  double w[10];
-#pragma unroll
-  for (int k = 0; k < 10; k++) {
-    double s = 0.;
-#pragma unroll
-    for (int m = 0; m < 4; m++) s += lamD[l0 + V4[m] * nd] * a.sens_w * J[m][k];
-    w[k] = s;
-  }
-#pragma unroll
-  for (int m = 0; m < 4; m++) {
-    atomicAdd(lamQ + l + V4[m] * nd, w[m]);
-    atomicAdd(lamQ + l - inc + V4[m] * nd, w[4 + m]);
-  }
-  atomicAdd(lamT + lt, w[8]);
-  atomicAdd(lamT + lt + z.ndm, w[9]);
+  for (int m = 0; m < 4; m++) w += lamD[l0 + V4[m] * nd] * a.sens_w * J[m][0];
+  if (k < 4) atomicAdd(lamQ + l + V4[k] * nd, w);
+  else if (k < 8) atomicAdd(lamQ + l - inc + V4[k - 4] * nd, w);
+  else atomicAdd(lamT + lt + (k == 8 ? 0 : z.ndm), w);
 }
 
 template <int D>
@@ -554,9 +734,14 @@ cudaError_t launch_adj_wall(const Zone& z, const double* q, const double* lamD, 
                             double* lamTi, double* lamTj, const WallCorrArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
   if (z.typ != Z2D || !a.slip || a.dir > 1) return cudaErrorNotSupported;
-  const unsigned g = (unsigned)((a.n + 127) / 128);
-  if (a.dir == 0) adj_wall<0><<<g, 128, 0, st>>>(z, q, lamD, lamQ, lamTi, a);
-  else adj_wall<1><<<g, 128, 0, st>>>(z, q, lamD, lamQ, lamTj, a);
+  const unsigned g = (unsigned)((a.n + 127) / 128), g16 = (unsigned)((16 * a.n + 127) / 128);
+  if (a.dir == 0) {
+    adj_wall_roe<0><<<g, 128, 0, st>>>(z, q, lamD, lamQ, lamTi, a);
+    adj_wall_flux<0><<<g16, 128, 0, st>>>(z, q, lamD, lamQ, lamTi, a);
+  } else {
+    adj_wall_roe<1><<<g, 128, 0, st>>>(z, q, lamD, lamQ, lamTj, a);
+    adj_wall_flux<1><<<g16, 128, 0, st>>>(z, q, lamD, lamQ, lamTj, a);
+  }
   return cudaGetLastError();
 }
 
@@ -572,39 +757,47 @@ cudaError_t launch_tan_wall(const Zone& z, const double* q, const double* dq, co
 
 // ------------------------------------------------------------ ghost cells
 // bc_face BCF_SLIP: ghost(ro, u, v, T) of mirror cell s and face normal
-// (tcx, tcy) -- 6 duals
-__device__ __forceinline__ void slip_lin(const double* __restrict__ q, int64_t nd, int64_t s,
-                                         double t0, double t1, double J[4][6]) {
-  Dual<6> ro = var<6>(q[s], 0), u = var<6>(q[s + nd], 1), v = var<6>(q[s + 2 * nd], 2),
-          tt = var<6>(q[s + 4 * nd], 3), tcx = var<6>(t0, 4), tcy = var<6>(t1, 5);
-  Dual<6> surf = sqrt(tcx * tcx + tcy * tcy);
+// (tcx, tcy) -- 6 inputs
+template <int N>
+__device__ __forceinline__ void slip_eval(const double* __restrict__ q, int64_t nd, int64_t s,
+                                          double t0, double t1, int col, double J[4][N]) {
+  Dual<N> ro = seed<N>(q[s], 0, col), u = seed<N>(q[s + nd], 1, col),
+          v = seed<N>(q[s + 2 * nd], 2, col), tt = seed<N>(q[s + 4 * nd], 3, col),
+          tcx = seed<N>(t0, 4, col), tcy = seed<N>(t1, 5, col);
+  Dual<N> surf = sqrt(tcx * tcx + tcy * tcy);
   surf = tmax(surf, 1e-30);
-  Dual<6> s_1 = 1. / surf;
+  Dual<N> s_1 = 1. / surf;
   tcx = tcx * s_1;
   tcy = tcy * s_1;
-  Dual<6> uu = u - 0., vv = v - 0.;
-  Dual<6> qn = uu * tcx + vv * tcy;
-  Dual<6> ut = uu - qn * tcx, vt = vv - qn * tcy;
-  Dual<6> ua = 2. * ut - uu, va = 2. * vt - vv;
-  Dual<6> o1 = 0. + ua, o2 = 0. + va;
-  const Dual<6>* o[4] = {&ro, &o1, &o2, &tt};
+  Dual<N> uu = u - 0., vv = v - 0.;
+  Dual<N> qn = uu * tcx + vv * tcy;
+  Dual<N> ut = uu - qn * tcx, vt = vv - qn * tcy;
+  Dual<N> ua = 2. * ut - uu, va = 2. * vt - vv;
+  Dual<N> o1 = 0. + ua, o2 = 0. + va;
+  const Dual<N>* o[4] = {&ro, &o1, &o2, &tt};
 #pragma unroll
   for (int m = 0; m < 4; m++)
 #pragma unroll
-    for (int k = 0; k < 6; k++) J[m][k] = o[m]->d[k];
+    for (int k = 0; k < N; k++) J[m][k] = o[m]->d[k];
+}
+__device__ __forceinline__ void slip_lin(const double* __restrict__ q, int64_t nd, int64_t s,
+                                         double t0, double t1, double J[4][6]) {
+  slip_eval<6>(q, nd, s, t0, t1, -1, J);
 }
 
 // bc_face BCF_FARFIELD (non_reflection.for, 2-d: t[2] = 0): ghost(ro, u, v,
 // T) of interior cell s (ro, u, v, T) and the exterior state (st0, st1, st2,
 // st4; st3 = 0) -- 8 duals; the normal t (x snorm) is held fixed
-__device__ __forceinline__ void farfield_lin(const BcFaceArgs& a, const double* __restrict__ q,
-                                             int64_t s, const double t[3], double J[4][8]) {
+template <int N>
+__device__ __forceinline__ void farfield_eval(const BcFaceArgs& a, const double* __restrict__ q,
+                                              int64_t s, const double t[3], int col,
+                                              double J[4][N]) {
   const int64_t nd = a.nd;
-  typedef Dual<8> T;
-  const T roi = var<8>(q[s], 0), ui = var<8>(q[s + nd], 1), vi = var<8>(q[s + 2 * nd], 2),
-          ti = var<8>(q[s + 4 * nd], 3);
-  const T e0 = var<8>(a.st[0], 4), e1 = var<8>(a.st[1], 5), e2 = var<8>(a.st[2], 6), e3 = T(0.),
-          e4 = var<8>(a.st[4], 7);
+  typedef Dual<N> T;
+  const T roi = seed<N>(q[s], 0, col), ui = seed<N>(q[s + nd], 1, col),
+          vi = seed<N>(q[s + 2 * nd], 2, col), ti = seed<N>(q[s + 4 * nd], 3, col);
+  const T e0 = seed<N>(a.st[0], 4, col), e1 = seed<N>(a.st[1], 5, col),
+          e2 = seed<N>(a.st[2], 6, col), e3 = T(0.), e4 = seed<N>(a.st[4], 7, col);
   const double gam1 = a.gam1, gam1_1 = a.gam1_1;
   const double tcx = t[0], tcy = t[1], tcz = 0.;
   const double sn = ::sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
@@ -653,57 +846,56 @@ __device__ __forceinline__ void farfield_lin(const BcFaceArgs& a, const double* 
 #pragma unroll
   for (int m = 0; m < 4; m++)
 #pragma unroll
-    for (int k = 0; k < 8; k++) J[m][k] = o[m]->d[k];
+    for (int k = 0; k < N; k++) J[m][k] = o[m]->d[k];
+}
+__device__ __forceinline__ void farfield_lin(const BcFaceArgs& a, const double* __restrict__ q,
+                                             int64_t s, const double t[3], double J[4][8]) {
+  farfield_eval<8>(a, q, s, t, -1, J);
 }
 
 // adjoint of one face-BC list: lam[src] += J^T lam[dst], lam[dst] = 0;
-// slip: lamT[mt] (metric of the face) += d/d normal; farfield: lamSt += d/d st
+// slip: lamT[mt] (metric of the face) += d/d normal; farfield: lamSt += d/d st.
+// Eight lanes per ghost cell, lane k the Jacobian column of input k (one
+// seeded input each, the columns run in parallel); no lane leaves before the
+// warp barrier that orders the reads of lam[dst] before its reset.
 __global__ void __launch_bounds__(128) adj_bc_face(const double* __restrict__ q,
                                                    double* __restrict__ lam, BcFaceArgs a,
                                                    const int32_t* __restrict__ mt, int64_t ndm,
                                                    double* __restrict__ lamT,
                                                    double* __restrict__ lamSt) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
-  const int64_t nd = a.nd, l = a.dst[e], s = a.src[e];
-  double lo[4];
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t e = gid >> 3;
+  const int k = (int)(gid & 7);
+  const bool act = e < a.n;
+  const int64_t nd = a.nd;
+  int64_t l = 0, s = 0;
+  double lo[4] = {0., 0., 0., 0.};
+  if (act) {
+    l = a.dst[e];
+    s = a.src[e];
 #pragma unroll
-  for (int m = 0; m < 4; m++) { lo[m] = lam[l + V4[m] * nd]; lam[l + V4[m] * nd] = 0.; }
-  lam[l + 3 * nd] = 0.;
-  if (a.op == BCF_SLIP) {
-    double J[4][6];
-    slip_lin(q, nd, s, a.nrm[3 * e], a.nrm[3 * e + 1], J);
-    double g[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-      double x = 0.;
-#pragma unroll
-      for (int m = 0; m < 4; m++) x += lo[m] * J[m][k];
-      g[k] = x;
-    }
-#pragma unroll
-    for (int m = 0; m < 4; m++) atomicAdd(lam + s + V4[m] * nd, g[m]);
-    atomicAdd(lamT + mt[e], g[4]);
-    atomicAdd(lamT + mt[e] + ndm, g[5]);
-  } else {   // BCF_FARFIELD
-    const double t[3] = {a.nrm[3 * e], a.nrm[3 * e + 1], a.nrm[3 * e + 2]};
-    double J[4][8];
-    farfield_lin(a, q, s, t, J);
-    double g[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      double x = 0.;
-#pragma unroll
-      for (int m = 0; m < 4; m++) x += lo[m] * J[m][k];
-      g[k] = x;
-    }
-#pragma unroll
-    for (int m = 0; m < 4; m++) atomicAdd(lam + s + V4[m] * nd, g[m]);
-    atomicAdd(lamSt + 0, g[4]);
-    atomicAdd(lamSt + 1, g[5]);
-    atomicAdd(lamSt + 2, g[6]);
-    atomicAdd(lamSt + 4, g[7]);
+    for (int m = 0; m < 4; m++) lo[m] = lam[l + V4[m] * nd];
   }
+  __syncwarp();
+  if (act && k == 0) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) lam[l + v * nd] = 0.;
+  }
+  if (!act) return;
+  double J[4][1];
+  if (a.op == BCF_SLIP) {
+    if (k >= 6) return;
+    slip_eval<1>(q, nd, s, a.nrm[3 * e], a.nrm[3 * e + 1], k, J);
+  } else {
+    const double t[3] = {a.nrm[3 * e], a.nrm[3 * e + 1], a.nrm[3 * e + 2]};
+    farfield_eval<1>(a, q, s, t, k, J);
+  }
+  double g = 0.;
+#pragma unroll
+  for (int m = 0; m < 4; m++) g += lo[m] * J[m][0];
+  if (k < 4) atomicAdd(lam + s + V4[k] * nd, g);
+  else if (a.op == BCF_SLIP) atomicAdd(lamT + mt[e] + (k == 4 ? 0 : ndm), g);
+  else atomicAdd(lamSt + (k == 7 ? 4 : k - 4), g);
 }
 
 // tangent of one face-BC list: dq[dst] = J (dq[src], dnormal | dst)
@@ -751,7 +943,7 @@ cudaError_t launch_adj_bc_face(const double* q, double* lam, const BcFaceArgs& a
                                int64_t ndm, double* lamT, double* lamSt, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
   if (a.op != BCF_SLIP && a.op != BCF_FARFIELD) return cudaErrorNotSupported;
-  adj_bc_face<<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(q, lam, a, mt, ndm, lamT, lamSt);
+  adj_bc_face<<<(unsigned)((8 * a.n + 127) / 128), 128, 0, st>>>(q, lam, a, mt, ndm, lamT, lamSt);
   return cudaGetLastError();
 }
 

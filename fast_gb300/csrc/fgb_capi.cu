@@ -1319,26 +1319,38 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
     const int n0 = seg * ckpt, steps = std::min(ckpt, A.nsteps - n0);
     // recompute the segment: W[3t + st - 1] = input of stage st of step t
     CK(cudaMemcpyAsync(A.W, A.ck[(size_t)seg], sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
-    for (int t = 0; t < steps; t++)
-      for (int st_ = 1; st_ <= 3; st_++) {
-        const size_t i = 3 * (size_t)t + st_ - 1;
-        // low-storage RK3: stages 2 and 3 start from coefH x the previous residual
-        if (st_ > 1)
-          CK(cudaMemcpyAsync(A.D + i * nq, A.D + (i - 1) * nq, sizeof(double) * nq,
-                             cudaMemcpyDeviceToDevice, s->st));
-        if ((rc = explicit_stage(s, zone, st_, A.W + i * nq, A.W + (i + 1) * nq, A.D + i * nq))) return rc;
-      }
+    {
+      ProfScope ps_re(s, "adj_recompute");
+      for (int t = 0; t < steps; t++)
+        for (int st_ = 1; st_ <= 3; st_++) {
+          const size_t i = 3 * (size_t)t + st_ - 1;
+          // low-storage RK3: stages 2 and 3 start from coefH x the previous residual
+          if (st_ > 1)
+            CK(cudaMemcpyAsync(A.D + i * nq, A.D + (i - 1) * nq, sizeof(double) * nq,
+                               cudaMemcpyDeviceToDevice, s->st));
+          if ((rc = explicit_stage(s, zone, st_, A.W + i * nq, A.W + (i + 1) * nq, A.D + i * nq))) return rc;
+        }
+    }
     for (int t = steps - 1; t >= 0; t--)
       for (int st_ = 3; st_ >= 1; st_--) {
         const size_t i = 3 * (size_t)t + st_ - 1;
         // the stage output's ghost fill, the update, the face fluxes
-        if ((rc = zone_fill_adj(s, zone, A.W + (i + 1) * nq, A.lamW))) return rc;
-        CK(cudaMemsetAsync(A.lamIn, 0, sizeof(double) * nq, s->st));
-        CK(launch_adj_update(z, A.W + i * nq, A.D + i * nq, kCoefW[st_], A.lamW, A.lamIn, A.lamD,
-                             A.lamVol, s->st));
-        CK(launch_adj_faces(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, s->st));
-        for (WallCorrList& w : Z.walls)
-          CK(launch_adj_wall(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, wall_args(Z, w), s->st));
+        {
+          ProfScope ps(s, "adj_fill");
+          if ((rc = zone_fill_adj(s, zone, A.W + (i + 1) * nq, A.lamW))) return rc;
+        }
+        {
+          ProfScope ps(s, "adj_update");
+          CK(cudaMemsetAsync(A.lamIn, 0, sizeof(double) * nq, s->st));
+          CK(launch_adj_update(z, A.W + i * nq, A.D + i * nq, kCoefW[st_], A.lamW, A.lamIn, A.lamD,
+                               A.lamVol, s->st));
+        }
+        {
+          ProfScope ps(s, "adj_faces");
+          CK(launch_adj_faces(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, s->st));
+          for (WallCorrList& w : Z.walls)
+            CK(launch_adj_wall(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, wall_args(Z, w), s->st));
+        }
         // D_st = coefH_st D_{st-1} + R: the earlier residual's adjoint
         std::swap(A.lamW, A.lamIn);
         if (st_ == 1) CK(cudaMemsetAsync(A.lamD, 0, sizeof(double) * nq, s->st));
