@@ -58,6 +58,12 @@ def parse():
                    help="tgv: the headline 256^3 case; channel: 48-block SA channel; "
                         "batch: 64 independent Taylor-Green cases; adjoint: gradient of the "
                         "C-grid wall force (cost against the primal, tangent and FD checks)")
+    p.add_argument("--adj-nsteps", type=int, default=400, help="adjoint workload: RK3 steps")
+    p.add_argument("--adj-ckpt", type=int, default=20, help="adjoint workload: checkpoint period")
+    p.add_argument("--adj-graph", type=int, default=1, choices=[0, 1],
+                   help="adjoint workload: replay the driver loops as CUDA graphs")
+    p.add_argument("--adj-checks", type=int, default=1, choices=[0, 1],
+                   help="adjoint workload: tangent / FD checks and the per-group breakdown")
     p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
                    help="64: plain FP64 path; 32: FP32 LU-SGS sweeps (mixed precision)")
     return p.parse_args()
@@ -391,7 +397,8 @@ def run_adjoint(args):
     import numpy as np
     import torch
     from fast_gb300 import adjoint as A
-    case = A.CGridCase()
+    case = A.CGridCase(nsteps=args.adj_nsteps, ckpt=args.adj_ckpt)
+    case.graph = bool(args.adj_graph)
     alpha = torch.from_numpy(np.random.default_rng(4).uniform(-0.005, 0.005, 8))
     mach = torch.tensor(0.7, dtype=torch.float64)
     for _ in range(max(1, args.warmup)):
@@ -402,25 +409,34 @@ def run_adjoint(args):
         prim.append(case.timing["primal_s"])
         adj.append(case.timing["adjoint_s"])
     grad = np.concatenate([ga, [gm]])
-    rng = np.random.default_rng(5)
-    tang = []
-    for _ in range(2):
-        d = rng.standard_normal(9)
-        dJ = A.tangent(case, alpha, mach, torch.from_numpy(d[:8]), torch.tensor(d[8], dtype=torch.float64))
-        tang.append(abs(dJ - grad @ d) / abs(dJ))
-    scale = float(np.max(np.abs(grad)))
-    fd6 = A.fd_gradient(case, alpha, mach, h=1e-6)
-    fd7 = A.fd_gradient(case, alpha, mach, h=1e-7)
     tp, ta = float(np.median(prim)), float(np.median(adj))
+    checks = {}
+    if args.adj_checks:
+        rng = np.random.default_rng(5)
+        tang = []
+        for _ in range(2):
+            d = rng.standard_normal(9)
+            dJ = A.tangent(case, alpha, mach, torch.from_numpy(d[:8]),
+                           torch.tensor(d[8], dtype=torch.float64))
+            tang.append(abs(dJ - grad @ d) / abs(dJ))
+        scale = float(np.max(np.abs(grad)))
+        fd6 = A.fd_gradient(case, alpha, mach, h=1e-6)
+        fd7 = A.fd_gradient(case, alpha, mach, h=1e-7)
+        checks = {"tangent_rel_err": tang,
+                  "fd_rel_err_h1e-6": float(np.max(np.abs(fd6 - grad)) / scale),
+                  "fd_rel_err_h1e-7": float(np.max(np.abs(fd7 - grad)) / scale)}
+        # per-group device time of one adjoint with stream launches and CUDA events
+        case.profile = True
+        A.gradient(case, alpha, mach)
+        checks["eager_profiled_groups_ms"] = case.timing.get("groups_ms", {})
+        case.profile = False
     line = {"metric": "adjoint/primal cost", "value": ta / tp, "unit": "x primal",
             "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "cgrid_385x129_roe_vanalbada_rk3_400_steps_ckpt20",
-                       "parameters": "8 Hicks-Henne amplitudes + M_inf", "mach": 0.7},
-            "primal_s": tp, "adjoint_s": ta, "J": J, "gradient": grad.tolist(),
-            "tangent_rel_err": tang,
-            "fd_rel_err_h1e-6": float(np.max(np.abs(fd6 - grad)) / scale),
-            "fd_rel_err_h1e-7": float(np.max(np.abs(fd7 - grad)) / scale)}
+            "config": {"workload": f"cgrid_385x129_roe_vanalbada_rk3_{case.nsteps}_steps_ckpt{case.ckpt}",
+                       "parameters": "8 Hicks-Henne amplitudes + M_inf", "mach": 0.7,
+                       "cuda_graphs": case.graph},
+            "primal_s": tp, "adjoint_s": ta, "J": J, "gradient": grad.tolist(), **checks}
     print(json.dumps(line), flush=True)
 
 

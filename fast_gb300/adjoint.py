@@ -191,12 +191,16 @@ class CGridCase:
         self.cut = (np.array(dnr, dtype=np.int64), np.array(rcv, dtype=np.int64))
         self.wall_i = np.arange(nw + 1, nw + na + 1)
         self.timing = {}
+        self.graph = True       # replay the driver loops as CUDA graphs
+        self.profile = False    # per-group CUDA-event timing (stream launches)
 
     def inddm(self, i, j):
         return (i + NG - 1) + (j + NG - 1) * self.nip
 
     def solver(self, ti, tj, vol, w0, st):
         s = Solver(0)
+        s.set_option("graph", int(self.graph))
+        s.set_option("profile", int(self.profile))
         s.add_zone(self.pi, self.pr, ti, tj, np.zeros(0), vol)
         s.add_transfer(0, 0, *self.cut)
         s.set_bc_state(0, st)
@@ -238,6 +242,8 @@ class _Solve(torch.autograd.Function):
         t0 = time.perf_counter()
         gw0, gti, gtj, gvol, gst = s.adjoint_backward(0, gW.detach().contiguous().numpy())
         case.timing["adjoint_s"] = time.perf_counter() - t0
+        if case.profile:
+            case.timing["groups_ms"] = {k: v[1] for k, v in s.kernel_stats().items()}
         s.close()
         return (torch.from_numpy(gti), torch.from_numpy(gtj), torch.from_numpy(gvol),
                 torch.from_numpy(gw0), torch.from_numpy(gst), None)

@@ -54,8 +54,26 @@ __device__ __forceinline__ Dual<N> var(double x, int k) {
 DUAL_BIN(+, a.d[k] + b.d[k], , )
 DUAL_BIN(-, a.d[k] - b.d[k], , )
 DUAL_BIN(*, a.d[k] * b.v + a.v * b.d[k], , )
-DUAL_BIN(/, (a.d[k] - r.v * b.d[k]) / b.v, , )
 #undef DUAL_BIN
+// quotient: the value as the primal computes it, the derivatives through one
+// reciprocal (N + 1 divisions -> 2)
+template <int N>
+__device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a.v / b.v;
+  const double ib = 1. / b.v;
+#pragma unroll
+  for (int k = 0; k < N; k++) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, double b) {
+  return a / Dual<N>(b);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator/(double a, const Dual<N>& b) {
+  return Dual<N>(a) / b;
+}
 template <int N> __device__ __forceinline__ Dual<N> operator-(const Dual<N>& a) {
   Dual<N> r;
   r.v = -a.v;
@@ -102,6 +120,18 @@ template <typename T>
 __device__ __forceinline__ T vanalbada_t(const T& x, const T& y) {
   const double e2 = 1e-12;
   return ((y * y + e2) * x + (x * x + e2) * y) / (x * x + y * y + 2. * e2);
+}
+
+// gradient of vanalbada_t: va = N / Dn, N = (y^2 + e) x + (x^2 + e) y,
+// Dn = x^2 + y^2 + 2e; d va / dx = (y^2 + e + 2xy - 2x va) / Dn and
+// symmetrically in y (one reciprocal)
+__device__ __forceinline__ void vanalbada_grad(double x, double y, double& gx, double& gy) {
+  const double e2 = 1e-12;
+  const double xx = x * x, yy = y * y, xy2 = 2. * x * y;
+  const double iD = 1. / (xx + yy + 2. * e2);
+  const double va = ((yy + e2) * x + (xx + e2) * y) * iD;
+  gx = (yy + e2 + xy2 - 2. * x * va) * iD;
+  gy = (xx + e2 + xy2 - 2. * y * va) * iD;
 }
 
 // roe_full (fgb_flux.cu) for a 2-d face: tcz = 0, w = 0 (those terms vanish
@@ -179,7 +209,7 @@ __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5],
   const double r2 = qm[0], p2 = r2 * qm[4] * rgp;
   const double h2 = gam1 * qm[4] * rgp + .5 * (qm[1] * qm[1] + qm[2] * qm[2]);
   const double s1 = ::sqrt(r1), s2 = ::sqrt(r2);
-  const double r = s1 * s2, r_1 = 1. / (s1 + s2);
+  const double r = s1 * s2, r_1 = 1. / (s1 + s2), i_r = 1. / r;
   const double t7u = s1 * qp[1] + s2 * qm[1], t7v = s1 * qp[2] + s2 * qm[2];
   const double u = t7u * r_1, v = t7v * r_1;
   const double t8 = s1 * h1 + s2 * h2, h = t8 * r_1;
@@ -192,21 +222,21 @@ __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5],
   const double s_1 = 1.0 / (smax_on ? s : 1.E-30);
   const double nx = tcx * s_1, ny = tcy * s_1;
   const double qn = u * nx + v * ny;
-  const double A1 = ::fabs(qn), f4 = psi * (A1 + c);
+  const double A1 = ::fabs(qn), f4 = psi * (A1 + c), i_f4 = 1. / f4;
   const double f2a = 0.5 + copysign(0.5, A1 - f4);
-  const double f3a = (f2a - 1.0) * (qn * qn / f4 + f4) * 0.5 - f2a * A1;
-  const double c2 = c * c;
-  const double Z = r2 - r1 - dp / c2, f1a = Z * s;
+  const double f3a = (f2a - 1.0) * (qn * qn * i_f4 + f4) * 0.5 - f2a * A1;
+  const double c2 = c * c, i_c2 = 1. / c2;
+  const double Z = r2 - r1 - dp * i_c2, f1a = Z * s;
   const double X2 = f1a * u + r * (du - nx * dqn), X3 = f1a * v + r * (dv - ny * dqn);
   const double Y5 = u * du + v * dv - qn * dqn, X5 = f1a * q + r * Y5;
   const double l4 = qn + c, A4 = ::fabs(l4);
   const double f2b = 0.5 + copysign(0.5, A4 - f4);
-  const double f3b = (f2b - 1.) * (l4 * l4 / f4 + f4) * 0.5 - f2b * A4;
-  const double N4 = dp + r * c * dqn * s_1, K4 = N4 / (2. * c2), f1b = K4 * s * f3b;
+  const double f3b = (f2b - 1.) * (l4 * l4 * i_f4 + f4) * 0.5 - f2b * A4;
+  const double N4 = dp + r * c * dqn * s_1, K4 = N4 * 0.5 * i_c2, f1b = K4 * s * f3b;
   const double l5 = qn - c, A5 = ::fabs(l5);
   const double f2c = 0.5 + copysign(0.5, A5 - f4);
-  const double f3c = (f2c - 1.) * (l5 * l5 / f4 + f4) * 0.5 - f2c * A5;
-  const double N5 = dp - r * c * dqn * s_1, K5 = N5 / (2. * c2), f1c = K5 * f3c * s;
+  const double f3c = (f2c - 1.) * (l5 * l5 * i_f4 + f4) * 0.5 - f2c * A5;
+  const double N5 = dp - r * c * dqn * s_1, K5 = N5 * 0.5 * i_c2, f1c = K5 * f3c * s;
   const double rou1 = r1 * qn1, rou2 = r2 * qn2, p1p2 = p1 + p2;
   // ---- reverse
   double r1b = 0., r2b = 0., qn1b = 0., qn2b = 0., p1b = 0., p2b = 0., h1b = 0., h2b = 0.;
@@ -231,12 +261,12 @@ __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5],
     hb += fl5b * f1c; qnb -= fl5b * f1c * c; cb -= fl5b * f1c * qn;
     const double K5b = f1cb * f3c * s, f3cb = f1cb * K5 * s;
     sb += f1cb * K5 * f3c;
-    const double N5b = K5b / (2. * c2);
-    c2b -= K5b * K5 / c2;
+    const double N5b = K5b * 0.5 * i_c2;
+    c2b -= K5b * K5 * i_c2;
     dpb += N5b; rb -= N5b * c * dqn * s_1; cb -= N5b * r * dqn * s_1;
     dqnb -= N5b * r * c * s_1; s_1b -= N5b * r * c * dqn;
-    double l5b = f3cb * (f2c - 1.) * l5 / f4;
-    f4b += f3cb * (f2c - 1.) * 0.5 * (1. - l5 * l5 / (f4 * f4));
+    double l5b = f3cb * (f2c - 1.) * l5 * i_f4;
+    f4b += f3cb * (f2c - 1.) * 0.5 * (1. - l5 * l5 * i_f4 * i_f4);
     l5b += -f3cb * f2c * sgn1(l5);
     qnb += l5b; cb -= l5b;
   }
@@ -248,12 +278,12 @@ __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5],
     hb += fl5b * f1b; qnb += fl5b * f1b * c; cb += fl5b * f1b * qn;
     const double K4b = f1bb * s * f3b, f3bb = f1bb * K4 * s;
     sb += f1bb * K4 * f3b;
-    const double N4b = K4b / (2. * c2);
-    c2b -= K4b * K4 / c2;
+    const double N4b = K4b * 0.5 * i_c2;
+    c2b -= K4b * K4 * i_c2;
     dpb += N4b; rb += N4b * c * dqn * s_1; cb += N4b * r * dqn * s_1;
     dqnb += N4b * r * c * s_1; s_1b += N4b * r * c * dqn;
-    double l4b = f3bb * (f2b - 1.) * l4 / f4;
-    f4b += f3bb * (f2b - 1.) * 0.5 * (1. - l4 * l4 / (f4 * f4));
+    double l4b = f3bb * (f2b - 1.) * l4 * i_f4;
+    f4b += f3bb * (f2b - 1.) * 0.5 * (1. - l4 * l4 * i_f4 * i_f4);
     l4b += -f3bb * f2b * sgn1(l4);
     qnb += l4b; cb += l4b;
   }
@@ -271,9 +301,9 @@ __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5],
     qnb -= X5b * r * dqn; dqnb -= X5b * r * qn;
     const double Zb = f1ab * s;
     sb += f1ab * Z;
-    r2b += Zb; r1b -= Zb; dpb -= Zb / c2; c2b += Zb * dp / (c2 * c2);
-    qnb += f3ab * (f2a - 1.) * qn / f4;
-    f4b += f3ab * (f2a - 1.) * 0.5 * (1. - qn * qn / (f4 * f4));
+    r2b += Zb; r1b -= Zb; dpb -= Zb * i_c2; c2b += Zb * dp * i_c2 * i_c2;
+    qnb += f3ab * (f2a - 1.) * qn * i_f4;
+    f4b += f3ab * (f2a - 1.) * 0.5 * (1. - qn * qn * i_f4 * i_f4);
     const double A1b = -f3ab * f2a + f4b * psi;
     cb += f4b * psi;
     qnb += A1b * sgn1(qn);
@@ -288,7 +318,7 @@ __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5],
   qpb[1] += qn1b * tcx; tcxb += qn1b * qp[1]; qpb[2] += qn1b * tcy; tcyb += qn1b * qp[2];
   qmb[1] += qn2b * tcx; tcxb += qn2b * qm[1]; qmb[2] += qn2b * tcy; tcyb += qn2b * qm[2];
   {
-    const double gb = cb * 0.5 / c;          // d / d(g_ |hq|)
+    const double gb = cb * 0.5 * c * i_c2;   // d / d(g_ |hq|) = cb / (2c)
     const double hqb = gb * g_ * sgn1(hq);
     hb += hqb; qb -= hqb;
   }
@@ -304,21 +334,21 @@ __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5],
   s1b += rb * s2; s2b += rb * s1;
   const double denb = -r_1b * r_1 * r_1;
   s1b += denb; s2b += denb;
-  r1b += s1b * 0.5 / s1; r2b += s2b * 0.5 / s2;
+  r1b += s1b * 0.5 * s2 * i_r; r2b += s2b * 0.5 * s1 * i_r;   // 1 / s1 = s2 / r
   qmb[4] += h2b * gam1 * rgp; qmb[1] += h2b * qm[1]; qmb[2] += h2b * qm[2];
   r2b += p2b * qm[4] * rgp; qmb[4] += p2b * r2 * rgp;
   qpb[4] += h1b * gam1 * rgp; qpb[1] += h1b * qp[1]; qpb[2] += h1b * qp[2];
   r1b += p1b * qp[4] * rgp; qpb[4] += p1b * r1 * rgp;
   qpb[0] += r1b; qmb[0] += r2b;
-  const double ssb = sb * 0.5 / s;
+  const double ssb = sb * 0.5 * s_1;
   tcxb += 2. * tcx * ssb; tcyb += 2. * tcy * ssb;
   tb[0] += tcxb; tb[1] += tcyb;
 }
 
 // adjoint of one face: mu = d J / d F (per component) -> cells and normal.
 // The reconstructed states first (values only), the reverse Roe pass, then
-// per variable the reconstruction derivatives (recomputed, 3 duals) and the
-// scatter: the derivatives are not live across the Roe pass.
+// per variable the reconstruction derivatives (vanalbada_grad, recomputed:
+// they are not live across the Roe pass) and the scatter.
 template <int D>
 __device__ __forceinline__ void face_adjoint(const Zone& z, const double* __restrict__ q,
                                              int64_t l, int64_t lt, const double mu[5],
@@ -341,16 +371,16 @@ __device__ __forceinline__ void face_adjoint(const Zone& z, const double* __rest
     const int v = m == 3 ? 4 : m;
     const double* Q = q + v * nd;
     const double a = Q[l - 2 * inc], b = Q[l - inc], c = Q[l], d = Q[l + inc];
-    Dual<3> B = var<3>(b, 0), C = var<3>(c, 1), Dd = var<3>(d, 2);
-    Dual<3> rm = C - 0.5 * vanalbada_t(C - B, Dd - C);
-    Dual<3> A = var<3>(a, 0), B2 = var<3>(b, 1), C2 = var<3>(c, 2);
-    Dual<3> rp = B2 + 0.5 * vanalbada_t(B2 - A, C2 - B2);
+    // qm = c - va(c - b, d - c) / 2, qp = b + va(b - a, c - b) / 2
+    double mx, my, px, py;
+    vanalbada_grad(c - b, d - c, mx, my);
+    vanalbada_grad(b - a, c - b, px, py);
     const int64_t o = v * nd;
     const double gm = qmb[v], gp = qpb[v];
-    atomicAdd(lamQ + l - 2 * inc + o, gp * rp.d[0]);
-    atomicAdd(lamQ + l - inc + o, gm * rm.d[0] + gp * rp.d[1]);
-    atomicAdd(lamQ + l + o, gm * rm.d[1] + gp * rp.d[2]);
-    atomicAdd(lamQ + l + inc + o, gm * rm.d[2]);
+    atomicAdd(lamQ + l - 2 * inc + o, -0.5 * px * gp);
+    atomicAdd(lamQ + l - inc + o, 0.5 * mx * gm + (1. + 0.5 * (px - py)) * gp);
+    atomicAdd(lamQ + l + o, (1. - 0.5 * (mx - my)) * gm + 0.5 * py * gp);
+    atomicAdd(lamQ + l + inc + o, -0.5 * my * gm);
   }
   atomicAdd(lamT + lt, tb[0]);
   atomicAdd(lamT + lt + z.ndm, tb[1]);
@@ -527,20 +557,29 @@ __global__ void __launch_bounds__(128) adj_update(Zone z, const double* __restri
   if (t >= z.ni * z.nj) return;
   const int64_t ii = t % z.ni, jj = t / z.ni;
   const int64_t l = inddm(z, ii + 1, jj + 1, 1), lt = indmtr(z, ii + 1, jj + 1, 1), nd = z.nd;
-  double J[4][9];
-  update_lin(z, q, D, l, lt, coefW, J);
   double lo[4];
 #pragma unroll
   for (int m = 0; m < 4; m++) { lo[m] = lamOut[l + V4[m] * nd]; lamOut[l + V4[m] * nd] = 0.; }
   lamOut[l + 3 * nd] = 0.;
-  double g[9];
-#pragma unroll
-  for (int k = 0; k < 9; k++) {
-    double s = 0.;
-#pragma unroll
-    for (int m = 0; m < 4; m++) s += lo[m] * J[m][k];
-    g[k] = s;
-  }
+  // forward values of update_lin's formula, then its reverse pass
+  const double ro = q[l], u = q[l + nd], v = q[l + 2 * nd], tt = q[l + 4 * nd];
+  const double x0 = D[l], x1 = D[l + nd], x2 = D[l + 2 * nd], x4 = D[l + 4 * nd];
+  const double vol = z.vol[lt], cv = z.cv, cvinv = 1. / cv;
+  const double r_1 = coefW * (z.dtc / vol);
+  const double n1 = ro + x0 * r_1, rr = 1. / n1;
+  const double B2 = ro * u + x1 * r_1, B3 = ro * v + x2 * r_1;
+  const double n2 = B2 * rr, n3 = B3 * rr;
+  const double E = cv * tt + 0.5 * (u * u + v * v), A5 = ro * E + x4 * r_1;
+  // n5 = A5 rr / cv - (n2^2 + n3^2) / (2 cv)
+  const double A5b = lo[3] * rr * cvinv;
+  const double n2b = lo[1] - lo[3] * cvinv * n2, n3b = lo[2] - lo[3] * cvinv * n3;
+  const double B2b = n2b * rr, B3b = n3b * rr;
+  const double rrb = lo[3] * A5 * cvinv + n2b * B2 + n3b * B3;
+  const double n1b = lo[0] - rrb * rr * rr;
+  const double g[9] = {n1b + B2b * u + B3b * v + A5b * E, (B2b + A5b * u) * ro,
+                       (B3b + A5b * v) * ro, A5b * ro * cv,
+                       n1b * r_1, B2b * r_1, B3b * r_1, A5b * r_1,
+                       -(n1b * x0 + B2b * x1 + B3b * x2 + A5b * x4) * r_1 / vol};
 #pragma unroll
   for (int m = 0; m < 4; m++) {
     lamIn[l + V4[m] * nd] += g[m];       // one thread per cell: no race

@@ -123,7 +123,15 @@ struct fgb_solver {
     double *lamTi = nullptr, *lamTj = nullptr, *lamVol = nullptr, *lamSt = nullptr;
     double *dW = nullptr, *dWn = nullptr, *dD = nullptr, *dFi = nullptr, *dFj = nullptr;
     double *dTi = nullptr, *dTj = nullptr, *dVol = nullptr, *dSt = nullptr;
+    // CUDA graphs of the driver loops: one RK3 step from either ping-pong
+    // buffer; a full segment's recomputation; a full segment's reverse sweep
+    // for either assignment of the two lambda buffers
+    cudaGraphExec_t step[2] = {nullptr, nullptr};
+    cudaGraphExec_t rec = nullptr;
+    cudaGraphExec_t rev[2] = {nullptr, nullptr};
+    double* lam0 = nullptr;        // lamW as allocated (the parity of rev)
   } adj;
+  bool graph = true;               // replay the adjoint driver loops as CUDA graphs
   int first_it = 0;
   int modulo_verif = 200;
   int lu_precision = 64;
@@ -164,6 +172,22 @@ struct ProfScope {
     }
   }
 };
+
+// Record the launches of body() on the solver stream into an executable
+// graph (the stream is left out of capture mode on every path)
+template <class F>
+static int capture_graph(fgb_solver* s, cudaGraphExec_t* out, F&& body) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+  const int rc = body();
+  const cudaError_t e = cudaStreamEndCapture(s->st, &g);
+  if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+  CK(e);
+  const cudaError_t ei = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  CK(ei);
+  return FGB_OK;
+}
 
 // ------------------------------------------------------------- helpers
 static int64_t idx(const std::vector<int64_t>& p, int64_t i, int64_t j, int64_t k) {
@@ -688,6 +712,8 @@ int fgb_set_option(fgb_solver* s, const char* key, double value) {
     s->first_it = value != 0.;
   } else if (k == "profile") {
     s->profile = value != 0.;
+  } else if (k == "graph") {
+    s->graph = value != 0.;
   } else {
     return fail(FGB_ERR_ARG, "unknown option " + k);
   }
@@ -702,6 +728,7 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value) {
   else if (k == "modulo_verif") *value = s->modulo_verif;
   else if (k == "first_it") *value = s->first_it;
   else if (k == "profile") *value = s->profile;
+  else if (k == "graph") *value = s->graph;
   else return fail(FGB_ERR_ARG, "unknown option " + k);
   return FGB_OK;
 }
@@ -820,8 +847,12 @@ static void adj_free(fgb_solver* s) {
                      &A.lamSt, &A.dW, &A.dWn, &A.dD, &A.dFi, &A.dFj, &A.dTi, &A.dTj, &A.dVol,
                      &A.dSt};
   for (double** b : bufs) { cudaFree(*b); *b = nullptr; }
+  cudaGraphExec_t* gs[] = {&A.step[0], &A.step[1], &A.rec, &A.rev[0], &A.rev[1]};
+  for (cudaGraphExec_t* g : gs) { if (*g) cudaGraphExecDestroy(*g); *g = nullptr; }
+  A.lam0 = nullptr;
   A.zone = -1;
 }
+
 
 static int adj_check(fgb_solver* s, int zone) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
@@ -1276,10 +1307,29 @@ int fgb_adjoint_forward(fgb_solver* s, int zone, int nsteps, int ckpt) {
   CK(cudaMemcpyAsync(cur, Z.lvl[0], sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
   if ((rc = zone_fill(s, zone, cur))) return rc;
   CK(cudaMemcpyAsync(A.ck[0], cur, sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
+  const bool graph = s->graph && !s->profile;
   for (int n = 0; n < nsteps; n++) {
-    for (int st_ = 1; st_ <= 3; st_++) {
-      if ((rc = explicit_stage(s, zone, st_, cur, nxt, A.D))) return rc;
-      std::swap(cur, nxt);
+    if (graph) {
+      const int b = cur == A.W ? 0 : 1;
+      if (!A.step[b]) {
+        double *c0 = cur, *c1 = nxt;
+        rc = capture_graph(s, &A.step[b], [&]() {
+          for (int st_ = 1; st_ <= 3; st_++) {
+            const int r = explicit_stage(s, zone, st_, c0, c1, A.D);
+            if (r) return r;
+            std::swap(c0, c1);
+          }
+          return (int)FGB_OK;
+        });
+        if (rc) return rc;
+      }
+      CK(cudaGraphLaunch(A.step[b], s->st));
+      std::swap(cur, nxt);     // three stages: the step ends in the other buffer
+    } else {
+      for (int st_ = 1; st_ <= 3; st_++) {
+        if ((rc = explicit_stage(s, zone, st_, cur, nxt, A.D))) return rc;
+        std::swap(cur, nxt);
+      }
     }
     if ((n + 1) % ckpt == 0 || n + 1 == nsteps)
       CK(cudaMemcpyAsync(A.ck[(size_t)((n + 1 + ckpt - 1) / ckpt)], cur, sizeof(double) * nq,
@@ -1315,29 +1365,31 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
   CK(cudaMemsetAsync(A.lamTj, 0, sizeof(double) * nm, s->st));
   CK(cudaMemsetAsync(A.lamVol, 0, sizeof(double) * z.ndm, s->st));
   CK(cudaMemsetAsync(A.lamSt, 0, sizeof(double) * 5, s->st));
-  for (int seg = nseg - 1; seg >= 0; seg--) {
-    const int n0 = seg * ckpt, steps = std::min(ckpt, A.nsteps - n0);
-    // recompute the segment: W[3t + st - 1] = input of stage st of step t
-    CK(cudaMemcpyAsync(A.W, A.ck[(size_t)seg], sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
-    {
-      ProfScope ps_re(s, "adj_recompute");
-      for (int t = 0; t < steps; t++)
-        for (int st_ = 1; st_ <= 3; st_++) {
-          const size_t i = 3 * (size_t)t + st_ - 1;
-          // low-storage RK3: stages 2 and 3 start from coefH x the previous residual
-          if (st_ > 1)
-            CK(cudaMemcpyAsync(A.D + i * nq, A.D + (i - 1) * nq, sizeof(double) * nq,
-                               cudaMemcpyDeviceToDevice, s->st));
-          if ((rc = explicit_stage(s, zone, st_, A.W + i * nq, A.W + (i + 1) * nq, A.D + i * nq))) return rc;
-        }
-    }
+  if (!A.lam0) A.lam0 = A.lamW;
+  // recompute a segment: W[3t + st - 1] = input of stage st of step t
+  auto recompute = [&](int steps) -> int {
+    for (int t = 0; t < steps; t++)
+      for (int st_ = 1; st_ <= 3; st_++) {
+        const size_t i = 3 * (size_t)t + st_ - 1;
+        // low-storage RK3: stages 2 and 3 start from coefH x the previous residual
+        if (st_ > 1)
+          CK(cudaMemcpyAsync(A.D + i * nq, A.D + (i - 1) * nq, sizeof(double) * nq,
+                             cudaMemcpyDeviceToDevice, s->st));
+        const int r = explicit_stage(s, zone, st_, A.W + i * nq, A.W + (i + 1) * nq, A.D + i * nq);
+        if (r) return r;
+      }
+    return (int)FGB_OK;
+  };
+  // the reverse sweep of a segment (swaps lamW / lamIn once per stage)
+  auto reverse = [&](int steps) -> int {
     for (int t = steps - 1; t >= 0; t--)
       for (int st_ = 3; st_ >= 1; st_--) {
         const size_t i = 3 * (size_t)t + st_ - 1;
         // the stage output's ghost fill, the update, the face fluxes
         {
           ProfScope ps(s, "adj_fill");
-          if ((rc = zone_fill_adj(s, zone, A.W + (i + 1) * nq, A.lamW))) return rc;
+          const int r = zone_fill_adj(s, zone, A.W + (i + 1) * nq, A.lamW);
+          if (r) return r;
         }
         {
           ProfScope ps(s, "adj_update");
@@ -1354,11 +1406,35 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
         // D_st = coefH_st D_{st-1} + R: the earlier residual's adjoint
         std::swap(A.lamW, A.lamIn);
         if (st_ == 1) CK(cudaMemsetAsync(A.lamD, 0, sizeof(double) * nq, s->st));
-        else {
-          // scale lamD by coefH_st (a plain kernel over the array)
-          CK(launch_scale(A.lamD, (int64_t)nq, kCoefH[st_], s->st));
-        }
+        else CK(launch_scale(A.lamD, (int64_t)nq, kCoefH[st_], s->st));
       }
+    return (int)FGB_OK;
+  };
+  const bool graph = s->graph && !s->profile;
+  for (int seg = nseg - 1; seg >= 0; seg--) {
+    const int n0 = seg * ckpt, steps = std::min(ckpt, A.nsteps - n0);
+    const bool full = steps == ckpt;
+    CK(cudaMemcpyAsync(A.W, A.ck[(size_t)seg], sizeof(double) * nq, cudaMemcpyDeviceToDevice, s->st));
+    {
+      ProfScope ps_re(s, "adj_recompute");
+      if (graph && full) {
+        if (!A.rec && (rc = capture_graph(s, &A.rec, [&]() { return recompute(steps); }))) return rc;
+        CK(cudaGraphLaunch(A.rec, s->st));
+      } else if ((rc = recompute(steps))) {
+        return rc;
+      }
+    }
+    if (graph && full) {
+      const int b = A.lamW == A.lam0 ? 0 : 1;
+      double *w = A.lamW, *in = A.lamIn;
+      if (!A.rev[b] && (rc = capture_graph(s, &A.rev[b], [&]() { return reverse(steps); }))) return rc;
+      // the capture ran the host-side swaps: restore, then apply the replay's
+      A.lamW = w; A.lamIn = in;
+      CK(cudaGraphLaunch(A.rev[b], s->st));
+      if ((3 * steps) % 2) std::swap(A.lamW, A.lamIn);
+    } else if ((rc = reverse(steps))) {
+      return rc;
+    }
   }
   // the initial ghost fill
   if ((rc = zone_fill_adj(s, zone, A.ck[0], A.lamW))) return rc;

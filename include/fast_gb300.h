@@ -72,7 +72,9 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * inside the FP64 defect-correction loop; "modulo_verif": residual check
  * period (FastC numerics key modulo_verif, default 200); "first_it": the
  * HOOK["FIRST_IT"] flag (0 = BDF1 step); "profile": 1 to time every kernel
- * group with CUDA events (see fgb_kernel_stats). */
+ * group with CUDA events (see fgb_kernel_stats); "graph": 1 (default) to
+ * replay the loops of fgb_adjoint_forward / _backward as CUDA graphs, 0 for
+ * stream launches (profiling always uses stream launches). */
 int fgb_set_option(fgb_solver* s, const char* key, double value);
 int fgb_get_option(fgb_solver* s, const char* key, double* value);
 

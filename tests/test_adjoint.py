@@ -139,3 +139,29 @@ def test_gradient_tangent_and_fd(case):
     assert np.max(np.abs(fd6 - grad)) <= 2e-5 * scale, (fd6, grad)
     fd7 = A.fd_gradient(case, alpha, mach, h=1e-7)
     assert np.max(np.abs(fd7 - grad)) <= 1e-6 * scale, (fd7, grad)
+
+
+@pytest.mark.gpu
+def test_graph_replay_equals_stream_launches():
+    """The CUDA-graph replay of the driver loops (odd segment length: both
+    lambda-buffer parities, a partial last segment) against stream launches:
+    the same primal bit for bit, the same gradient to FP64-atomic reordering."""
+    c = A.CGridCase(ni=97, nj=33, nw=16, dt=4e-4, nsteps=40, ckpt=7)
+    ti, tj, vol, w0, st = (x.detach().numpy() for x in A.inputs(c, _alpha(),
+                                                              torch.tensor(0.7, dtype=torch.float64)))
+    lam = np.random.default_rng(3).standard_normal(w0.size)
+    out = []
+    for graph in (True, False):
+        c.graph = graph
+        s = c.solver(ti, tj, vol, w0, st)
+        s.adjoint_forward(0, c.nsteps, c.ckpt)
+        W = s.download(0, 0).copy()
+        g = s.adjoint_backward(0, lam)
+        g2 = s.adjoint_backward(0, lam)          # a second sweep over the same forward run
+        s.close()
+        out.append((W, g, g2))
+    (Wg, gg, gg2), (We, ge, _) = out
+    assert np.array_equal(Wg, We)
+    for a, b, b2 in zip(gg, ge, gg2):
+        tol = 1e-12 * max(np.max(np.abs(b)), 1e-300)
+        assert np.max(np.abs(a - b)) <= tol and np.max(np.abs(b2 - b)) <= tol
