@@ -37,6 +37,13 @@ UNIT = "Mcell-updates/s"
 # residual (W^p, W^n, W^{n-1} in, drodm out) = 160 B; LU-SGS lower + upper
 # (drodm, W^p, coe in / increment, W^{p+1} out) = 320 B per sub-iteration.
 ALG_BYTES = {"residual": 160.0, "lu_sgs": 320.0}
+# DRAM bytes per cell and launch group measured with ncu (dram__bytes_read.sum
+# + dram__bytes_write.sum of every kernel of the group, one sub-iteration of
+# the 160^3 case, FP64): LU-SGS = lu_gather (2.49 GB) + lusgs_persistent
+# (4.48 GB) over 4.10 M cells; the plane-ordered records are written once
+# and read by both sweeps, so the traffic scales with the cell count.
+# residual = three face_flux launches (1.01 GB) + assemble (1.03 GB).
+DRAM_BYTES = {"residual": 497.0, "lu_sgs": 1702.0}
 
 
 def parse():
@@ -50,6 +57,8 @@ def parse():
     p.add_argument("--cpu-n", type=int, default=96, help="CPU sample size (cells per side)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-mixed", action="store_true",
+                   help="skip the FP32-sweep steps reported beside the FP64 value")
     p.add_argument("--ttc", action="store_true",
                    help="time to a 1e-10 Newton residual drop, FP64 vs mixed sweeps")
     p.add_argument("--ttc-n", type=int, default=256)
@@ -167,10 +176,11 @@ class Clocks:
 
 
 # ------------------------------------------------------------- CPU side
-def cpu_sample(n, ss, steps=1):
+def cpu_sample(n, ss, steps=1, min_seconds=0.0):
     """The oracle (C restatement of the FastS kernels, OpenMP on every host
     core, one LU-SGS block per thread as FastS does) on an n^3 sample of the
-    workload.  Returns (Mcell-updates/s, threads, seconds)."""
+    workload: `steps` physical steps, continued until `min_seconds` of CPU
+    time have elapsed.  Returns (Mcell-updates/s, threads, seconds, steps)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     from fast_gb300 import cases, fasts
@@ -183,11 +193,13 @@ def cpu_sample(n, ss, steps=1):
     c.apply_bc(0)
     c.apply_bc(1)
     t0 = time.perf_counter()
-    for it in range(1, steps + 1):
+    it = 0
+    while it < steps or (time.perf_counter() - t0 < min_seconds and it < 10000):
+        it += 1
         c.compute(it, 1, ss + 1, 1, modulo_verif=200)
     dt = time.perf_counter() - t0
     oracle.load().or_set_lu_tiles(1)
-    return n ** 3 * steps / dt / 1e6, threads, dt
+    return n ** 3 * it / dt / 1e6, threads, dt, it
 
 
 def run_reference(args, d: Dist):
@@ -198,7 +210,7 @@ def run_reference(args, d: Dist):
         cpu_sample(n, args.ss, 1)
     vals, secs = [], 0.0
     for _ in range(args.steps):
-        v, threads, dt = cpu_sample(n, args.ss, 1)
+        v, threads, dt, _ = cpu_sample(n, args.ss, 1)
         vals.append(v)
         secs += dt
     value = args.steps * n ** 3 / secs / 1e6
@@ -262,6 +274,28 @@ def run_ours(args, d: Dist):
     d.barrier()
     value, ms_max = replica_throughput(d, cells, args.steps, ms)
 
+    # ---- the same steps with FP32 LU-SGS sweeps (FP64 residual, update and
+    # norms): reported beside the FP64 value, not part of it
+    mixed = None
+    if args.lu_precision == 64 and not args.no_mixed:
+        s.set_option("lu_precision", 32)
+        fasts._compute(t, metrics, it)   # untimed: first FP32 solve builds its work arrays
+        it += 1
+        d.barrier()
+        s.synchronize()
+        s.timer_start()
+        for _ in range(args.steps):
+            fasts._compute(t, metrics, it)
+            it += 1
+        ms32 = s.timer_stop()
+        d.barrier()
+        v32, ms32_max = replica_throughput(d, cells, args.steps, ms32)
+        mixed = {"value": v32, "unit": UNIT, "ms_per_step": ms32_max / args.steps,
+                 "dtype": "f64+f32-sweeps"}
+        s.set_option("lu_precision", 64)
+        fasts._compute(t, metrics, it)   # back on the FP64 path before the profiled step
+        it += 1
+
     # ---- per-kernel groups (separate profiled step; not part of `value`)
     s.set_option("profile", 1)
     s.kernel_stats(reset=True)
@@ -284,7 +318,10 @@ def run_ours(args, d: Dist):
     total_prof = sum(v[1] for v in stats.values())
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-        "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
+        "frac": achieved / hbm_peak,
+        "traffic": DRAM_BYTES[dom] * cells if args.lu_precision == 64 else None,
+        "traffic_source": "ncu at 160^3, bytes per cell scaled to this cell count",
+        "peak_source": peak_kind,
         "avg_launch_ms": avg_ms,
         "fp64_fma_peak_gflops_measured": fp64,
         "kernel_share": {k: round(v[1] / total_prof, 4) for k, v in stats.items()},
@@ -312,10 +349,10 @@ def run_ours(args, d: Dist):
 
     cpu = None
     if d.rank == 0 and not args.no_cpu:
-        v, threads, sec = cpu_sample(args.cpu_n, ss, 1)
+        v, threads, sec, nst = cpu_sample(args.cpu_n, ss, 1, min_seconds=10.0)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"taylor_green {args.cpu_n}^3, one physical step ({ss} LU-SGS "
-                         f"sub-iterations), {sec:.1f} s"}
+               "sample": f"taylor_green {args.cpu_n}^3, {nst} physical steps ({ss} LU-SGS "
+                         f"sub-iterations each), {sec:.1f} s"}
     d.barrier()
     if d.rank == 0:
         line = {
@@ -332,6 +369,7 @@ def run_ours(args, d: Dist):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches,
             "kernel_ms_per_step": {k: v[1] for k, v in stats.items()},
+            "mixed_precision": mixed,
         }
         print(json.dumps(line), flush=True)
 
