@@ -199,7 +199,8 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
 
 def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model="NSLaminar",
            wavy=0.0, perturb=0.05, temporal="explicit", ss_iteration=3, scheme="ausmpred",
-           slope="o3", time_step=0.02, gamma=1.4, two_d=False, nutilde_ratio=5.0):
+           slope="o3", time_step=0.02, gamma=1.4, two_d=False, nutilde_ratio=5.0,
+           extrude=False):
     """Box [0,1]x[0,1]x[0,dz] exercising the non-periodic BCs of the path:
     inflow at imin (BCInflow), outflow at imax (BCOutflow), a wall at jmin
     (``wall``), farfield at jmax (BCFarfield), periodic in k.  The initial
@@ -207,22 +208,27 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
     ``perturb`` (0 gives the free stream itself).  wavy > 0 displaces the
     vertices as in ``wave`` (periods = box lengths).  model "NSTurbulent"
     adds Spalart-Allmaras: free-stream ro nutilde = nutilde_ratio x mu, the
-    same perturbation on nutilde, and the distance to the jmin wall."""
+    same perturbation on nutilde, and the distance to the jmin wall.
+    extrude (3-d only): the 2-d case extruded in k -- in-plane displacement,
+    no k dependence of the initial field, w = 0."""
     ni, nj, nk = n
     if two_d:
         nk = 1
         n = (ni, nj, 1)
     h = (1.0 / ni, 1.0 / nj, 1.0 / ni)
     z = cart_zone("box", (0.0, 0.0, 0.0), h, n, ngk=0 if two_d else None)
+    flat = two_d or extrude
     if wavy:
-        wave(z, wavy, (0.0, 0.0, 0.0), (1.0, 1.0, h[2] * nk), two_d=two_d)
+        wave(z, wavy, (0.0, 0.0, 0.0), (1.0, 1.0, h[2] * nk), two_d=flat)
     xc, yc, zc = cell_centers(z)
     a = perturb
-    s = np.sin(2 * math.pi * xc) * np.sin(2 * math.pi * yc) * np.cos(2 * math.pi * zc / (h[2] * nk))
+    s = np.sin(2 * math.pi * xc) * np.sin(2 * math.pi * yc)
+    if not flat:
+        s = s * np.cos(2 * math.pi * zc / (h[2] * nk))
     ro = 1.0 + a * s
     u = mach * (1.0 + a * np.cos(2 * math.pi * yc) * np.sin(2 * math.pi * xc))
     v = mach * a * s
-    w = 0.0 * xc if two_d else mach * a * np.sin(2 * math.pi * xc) * np.cos(2 * math.pi * yc)
+    w = 0.0 * xc if flat else mach * a * np.sin(2 * math.pi * xc) * np.cos(2 * math.pi * yc)
     p = (1.0 + a * 0.5 * s) / gamma
     set_conservative(z, ro, u, v, w, p, gamma)
     if model == "NSTurbulent":

@@ -184,6 +184,34 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
   F[4] = (fl5 + rou1 * h1 + rou2 * h2) * 0.5;
 }
 
+// ---------------------------------------------------------- Roe (SA row)
+// ROE/3dfull/fluFaceSA_*_3dfull_{i,j,k}.for (3dcart: Vit_ent/qn_3dcart_*):
+// the ro nutilde flux from the first-order states of cells nm = l - inc and
+// l, upwinded by the Roe-averaged normal velocity with the floor c1 |S|.
+template <int D, bool CART>
+__device__ __forceinline__ double roe_sa_flux(const Zone& z, const double* __restrict__ q,
+                                              int64_t l, int64_t nm, double tcx, double tcy,
+                                              double tcz, double s) {
+  const int64_t nd = z.nd;
+  const double t[3] = {tcx, tcy, tcz};
+  double qp[3] = {q[nm + nd], q[nm + 2 * nd], q[nm + 3 * nd]};
+  const double qm[3] = {q[l + nd], q[l + 2 * nd], q[l + 3 * nd]};
+  double qn1 = CART ? qp[D] * t[D] : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz;
+  const double qn2 = CART ? qm[D] * t[D] : qm[0] * tcx + qm[1] * tcy + qm[2] * tcz;
+  double qp1 = q[nm], qm1 = q[l];
+  const double qm6 = q[l + 5 * nd] * qm1 * qn2;
+  const double qp6 = q[nm + 5 * nd] * qp1 * qn1;
+  qp1 = sqrt(qp1);
+  qm1 = sqrt(qm1);
+  const double r_1 = 1. / (qp1 + qm1);
+#pragma unroll
+  for (int m = 0; m < 3; m++) qp[m] = r_1 * (qp1 * qp[m] + qm1 * qm[m]);
+  qn1 = CART ? qp[D] * t[D] : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz;
+  const double s_1 = 1.0 / fmaxF(s, 1.E-30);
+  const double tdu = fmaxF(z.c1 / s_1, fabs(qn1));
+  return 0.5 * (qm6 + qp6 - tdu * (q[l + 5 * nd] * q[l] - q[nm + 5 * nd] * q[nm]));
+}
+
 // ------------------------------------------------------------- AUSM+(P)
 // AUSM/fluFaceEuler.for:36-57 + etat_GD.for + Vit_ent/fluvector_*.for.
 // NX = number of non-zero normal components the face can have (1: cartesian
@@ -465,10 +493,60 @@ __device__ __forceinline__ void visc_full(const Zone& z, const double* __restric
     F[NV - 1] = F[NV - 1] - xsa * (g[NG - 1][0] * tcx + g[NG - 1][1] * tcy + g[NG - 1][2] * tcz);
 }
 
+// ------------------------------------------------------- viscous (2-d)
+// fluvisq_2d_{i,j}.for + mut_interface.for: visc_full without the k faces,
+// one transverse direction A, two velocity components (no w row).
+template <int D>
+__device__ __forceinline__ void visc_2d(const Zone& z, const double* __restrict__ q,
+                                        const double* __restrict__ xmut, int64_t l, int64_t lt,
+                                        double tcx, double tcy, double F[5]) {
+  constexpr int A = 1 - D;
+  const int64_t nd = z.nd, ndm = z.ndm;
+  const double* TD = D == 0 ? z.ti : z.tj;
+  const double* TA = A == 0 ? z.ti : z.tj;
+  const int64_t mD = z.minc[D], mA = z.minc[A], iA = z.inc[A];
+  const int64_t ltm = lt - mD, ltp = lt + mD, ltA = lt + mA, ltAm = lt + mA - mD;
+  double t0[2], t1[2], ta0[2], ta1[2];
+#pragma unroll
+  for (int m = 0; m < 2; m++) {
+    const int64_t o = m * ndm;
+    t0[m] = .5 * (TD[lt + o] + TD[ltm + o]);
+    t1[m] = .5 * (TD[lt + o] + TD[ltp + o]);
+    ta0[m] = .125 * (TA[lt + o] + TA[ltm + o]);
+    ta1[m] = .125 * (TA[ltA + o] + TA[ltAm + o]);
+  }
+  const int64_t il = l - z.inc[D], ir = l;
+  double g[3][2];   // u, v, T
+#pragma unroll
+  for (int v = 0; v < 3; v++) {
+    const double* Q = q + (v == 2 ? 4 : v + 1) * nd;
+    const double f1 = Q[il], f2 = Q[ir];
+    const double f3 = Q[ir] + Q[il] + Q[il - iA] + Q[ir - iA];
+    const double f4 = Q[ir] + Q[il] + Q[il + iA] + Q[ir + iA];
+#pragma unroll
+    for (int m = 0; m < 2; m++) g[v][m] = (f2 * t1[m] - f1 * t0[m]) + (f4 * ta1[m] - f3 * ta0[m]);
+  }
+  const double div = (g[0][0] + g[1][1]) * z.cvisq;
+  const double e1 = g[0][0] - div, e2 = g[0][1] + g[1][0], e4 = g[1][1] - div;
+  const double volinv = 1. / (z.vol[lt] + z.vol[ltm]);
+  double xmutvol, xktvol, xsa;
+  mut_face<5>(z, q, xmut, il, ir, volinv, xmutvol, xktvol, xsa);
+  double fv, fv5;
+  fv = -(2. * e1 * tcx + e2 * tcy) * xmutvol;
+  fv5 = fv * (q[ir + nd] + q[il + nd]);
+  F[1] = F[1] + fv;
+  fv = -(e2 * tcx + 2. * e4 * tcy) * xmutvol;
+  fv5 = fv5 + fv * (q[ir + 2 * nd] + q[il + 2 * nd]);
+  F[2] = F[2] + fv;
+  fv = fv5 * 0.5 - (g[2][0] * tcx + g[2][1] * tcy) * xktvol;
+  F[4] = F[4] + fv;
+}
+
 // ------------------------------------------------------------- face kernel
 // One thread per face of direction D; faces of direction D are indexed
 // f = ii + NI*(jj + NJ*kk) over the interior face box (NI = ni+1 for D=0 ...).
-// NV = 6: Spalart-Allmaras (AUSM+(P) faces; nutilde takes the o3 slope).
+// NV = 6: Spalart-Allmaras (AUSM+(P): nutilde takes the o3 slope; Roe:
+// first-order nutilde flux, no reconstruction).
 template <int D, int TYP, int KF, int SL, bool VISC, int NV = 5>
 __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restrict__ q,
                                                  const double* __restrict__ xmut,
@@ -489,6 +567,7 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
 #pragma unroll
   for (int v = 0; v < NV; v++) {
     if (TYP == Z2D && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }   // 2-d: no w slope
+    if (KF == ROE && v == 5) { qm[v] = 0.; qp[v] = 0.; continue; }    // Roe SA: unreconstructed
     const double* Q = q + v * nd;
     double a = (SL == O1) ? 0. : Q[l - 2 * inc];
     double b = Q[l - inc], c = Q[l];
@@ -506,8 +585,14 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     if (KF == ROE) roe_full(z, qm, qp, tcx, tcy, 0., s, F);
     else ausm_face<D, false>(z, qm, qp, q[l + 4 * nd], tcx, tcy, 0., s, F);
     F[3] = 0.;
+    if (VISC) visc_2d<D>(z, q, xmut, l, lt, tcx, tcy, F);
   } else if (TYP == Z3DCART) {
-    if (KF == ROE) roe_cart<D>(z, qm, qp, F);
+    if (KF == ROE) {
+      roe_cart<D>(z, qm, qp, F);
+      if (NV == 6)
+        F[NV - 1] = roe_sa_flux<D, true>(z, q, l, l - inc, z.tcx, z.tcy, z.tcz,
+                                        D == 0 ? z.si : (D == 1 ? z.sj : z.sk));
+    }
     else ausm_face<D, true, KF == SENSEUR, NV>(z, qm, qp, q[l + 4 * nd], z.tcx, z.tcy, z.tcz,
                                               D == 0 ? z.si : (D == 1 ? z.sj : z.sk), F,
                                               KF == SENSEUR ? z.wig[l + D * nd] : 0.);
@@ -517,8 +602,10 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     const double* t = D == 0 ? z.ti : (D == 1 ? z.tj : z.tk);
     double tcx = t[lt], tcy = t[lt + z.ndm], tcz = t[lt + 2 * z.ndm];
     double s = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
-    if (KF == ROE) roe_full(z, qm, qp, tcx, tcy, tcz, s, F);
-    else ausm_face<D, false, KF == SENSEUR, NV>(z, qm, qp, q[l + 4 * nd], tcx, tcy, tcz, s, F,
+    if (KF == ROE) {
+      roe_full(z, qm, qp, tcx, tcy, tcz, s, F);
+      if (NV == 6) F[NV - 1] = roe_sa_flux<D, false>(z, q, l, l - inc, tcx, tcy, tcz, s);
+    } else ausm_face<D, false, KF == SENSEUR, NV>(z, qm, qp, q[l + 4 * nd], tcx, tcy, tcz, s, F,
                                                KF == SENSEUR ? z.wig[l + D * nd] : 0.);
     if (VISC) visc_full<D, NV>(z, q, xmut, l, lt, tcx, tcy, tcz, F);
   }
@@ -555,7 +642,7 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
   double x[NV];
   if (a.mode == 2) {  // balance already in drodm (corrected by wall_corr)
 #pragma unroll
-    for (int v = 0; v < 5; v++) x[v] = a.drodm[l + v * nd];
+    for (int v = 0; v < NV; v++) x[v] = a.drodm[l + v * nd];
   } else {
 #pragma unroll
     const bool two_d = z.typ == Z2D;   // no k faces
@@ -571,7 +658,7 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
     }
     if (a.mode == 1) {
 #pragma unroll
-      for (int v = 0; v < 5; v++) a.drodm[l + v * nd] = x[v];
+      for (int v = 0; v < NV; v++) a.drodm[l + v * nd] = x[v];
       return;
     }
   }
@@ -809,10 +896,21 @@ static cudaError_t launch_faces_t(const Zone& z, const double* q, const double* 
 cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
                          double* Fj, double* Fk, cudaStream_t st) {
   const bool visc = z.iflow >= 2;
-  if (z.neq == 6) {   // Spalart-Allmaras: AUSM+(P) o3, 3d zones
-    if (z.kflu != AUSM || z.slope != O3) return cudaErrorNotSupported;
-    if (z.typ == Z3DCART) return launch_faces_t<Z3DCART, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.typ == Z3DFULL) return launch_faces_t<Z3DFULL, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+  if (z.neq == 6) {   // Spalart-Allmaras: AUSM+(P) o3 or Roe o1 / o3 / minmod, 3d zones
+    const bool cart = z.typ == Z3DCART;
+    if (z.typ != Z3DCART && z.typ != Z3DFULL) return cudaErrorNotSupported;
+    if (z.kflu == AUSM && z.slope == O3)
+      return cart ? launch_faces_t<Z3DCART, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DFULL, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == ROE && z.slope == O1)
+      return cart ? launch_faces_t<Z3DCART, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DFULL, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == ROE && z.slope == O3)
+      return cart ? launch_faces_t<Z3DCART, ROE, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DFULL, ROE, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == ROE && z.slope == MINMOD)
+      return cart ? launch_faces_t<Z3DCART, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DFULL, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
     return cudaErrorNotSupported;
   }
   if (z.typ == Z3DCART) {
@@ -848,14 +946,18 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
                   : launch_faces_t<Z3DFULL, SENSEUR, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
   }
-  if (z.typ == Z2D && !visc) {   // 2-d zones: Euler, Roe o1 / o3 / minmod, AUSM+(P) o3
+  if (z.typ == Z2D) {   // 2-d zones: Euler / laminar, Roe o1 / o3 / minmod, AUSM+(P) o3
     if (z.kflu == ROE) {
-      if (z.slope == O1) return launch_faces_t<Z2D, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == O3) return launch_faces_t<Z2D, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == MINMOD) return launch_faces_t<Z2D, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == VANALBADA) return launch_faces_t<Z2D, ROE, VANALBADA, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O1) return visc ? launch_faces_t<Z2D, ROE, O1, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                     : launch_faces_t<Z2D, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O3) return visc ? launch_faces_t<Z2D, ROE, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                     : launch_faces_t<Z2D, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == MINMOD) return visc ? launch_faces_t<Z2D, ROE, MINMOD, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                         : launch_faces_t<Z2D, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == VANALBADA && !visc) return launch_faces_t<Z2D, ROE, VANALBADA, false>(z, q, xmut, Fi, Fj, Fk, st);
     } else if (z.kflu == AUSM && z.slope == O3) {
-      return launch_faces_t<Z2D, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      return visc ? launch_faces_t<Z2D, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z2D, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
   }
   return cudaErrorNotSupported;
@@ -1006,7 +1108,6 @@ cudaError_t launch_assemble(const Zone& z, const StageArgs& a, bool implicit, cu
   int64_t n = z.ni * z.nj * z.nk;
   const unsigned g = (unsigned)((n + B - 1) / B);
   if (z.neq == 6) {
-    if (a.mode != 0) return cudaErrorNotSupported;
     if (implicit) assemble<true, 6><<<g, B, 0, st>>>(z, a);
     else assemble<false, 6><<<g, B, 0, st>>>(z, a);
   } else {

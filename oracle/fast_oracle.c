@@ -881,6 +881,82 @@ static void visc_full(const fctx* c, int d, int64_t l, int64_t lt, double tcx, d
     flu[5] = flu[5] - xmutvol_sa * (g[4][0] * tcx + g[4][1] * tcy + g[4][2] * tcz);
 }
 
+/* Viscous face flux on a 2-d zone: Compute/fluvisq_2d_i.for and
+ * fluvisq_2d_j.for + mut_interface.for.  The 2-d Green-Gauss gradient of
+ * the 3-d general routine without its k faces: faces normal to d at the two
+ * cell centres (means of two face vectors) and the faces along the single
+ * transverse direction a (four-cell means, factor 1/8); two velocity
+ * components, no w row. */
+static void visc_2d(const fctx* c, int d, int64_t l, int64_t lt, double tcx, double tcy,
+                    double flu[6]) {
+  const double* rop = c->rop;
+  const int64_t nd = c->nd, ndm = c->ndm;
+  const int a = 1 - d;
+  const double *TD = d == 0 ? c->ti : c->tj, *TA = d == 0 ? c->tj : c->ti;
+  const int64_t mD = c->inc_mtr[d], mA = c->inc_mtr[a], iA = c->inc[a];
+  const int64_t ltm = lt - mD, ltp = lt + mD, ltA = lt + mA, ltAm = lt + mA - mD;
+  double t0[2], t1[2], ta0[2], ta1[2];
+  for (int m = 0; m < 2; m++) {
+    const int64_t o = m * ndm;
+    t0[m] = .5 * (TD[lt + o] + TD[ltm + o]);
+    t1[m] = .5 * (TD[lt + o] + TD[ltp + o]);
+    ta0[m] = .125 * (TA[lt + o] + TA[ltm + o]);
+    ta1[m] = .125 * (TA[ltA + o] + TA[ltAm + o]);
+  }
+  const int64_t il = l - c->inc[d], ir = l;
+  double g[3][2];                         /* u, v, T */
+  const int var[3] = {1, 2, 4};
+  for (int v = 0; v < 3; v++) {
+    const double* q = rop + var[v] * nd;
+    double f1 = q[il], f2 = q[ir];
+    double f3 = q[ir] + q[il] + q[il - iA] + q[ir - iA];
+    double f4 = q[ir] + q[il] + q[il + iA] + q[ir + iA];
+    for (int m = 0; m < 2; m++) g[v][m] = (f2 * t1[m] - f1 * t0[m]) + (f4 * ta1[m] - f3 * ta0[m]);
+  }
+  const double div = (g[0][0] + g[1][1]) * c->cvisq;
+  const double f1 = g[0][0] - div, f2 = g[0][1] + g[1][0], f4 = g[1][1] - div;
+  const double volinv = 1. / (c->vol[lt] + c->vol[ltm]);
+  const double xmutvol = (c->xmut[ir] + c->xmut[il]) * volinv;
+  const double xktvol = xmutvol * c->gam3;
+  double fv, fv5;
+  fv = -(2. * f1 * tcx + f2 * tcy) * xmutvol;
+  fv5 = fv * (rop[ir + nd] + rop[il + nd]);
+  flu[1] = flu[1] + fv;
+  fv = -(f2 * tcx + 2. * f4 * tcy) * xmutvol;
+  fv5 = fv5 + fv * (rop[ir + 2 * nd] + rop[il + 2 * nd]);
+  flu[2] = flu[2] + fv;
+  fv = fv5 * 0.5 - (g[2][0] * tcx + g[2][1] * tcy) * xktvol;
+  flu[4] = flu[4] + fv;
+}
+
+/* Roe flux of ro * nutilde (ROE/3dfull/fluFaceSA_*_3dfull_i.for and the
+ * 3dcart variants): first-order states (cells nm = l - inc and l, no slope),
+ * upwinding by the Roe-averaged normal velocity with the floor c1 |S|:
+ * flu6 = (qm6 + qp6 - tdu (nu_l ro_l - nu_nm ro_nm)) / 2.  Cartesian faces
+ * take the normal velocity from their one component (Vit_ent/qn_3dcart_*). */
+static double roe_sa_flux(const fctx* c, int d, int64_t l, int64_t nm, double tcx, double tcy,
+                          double tcz, double s) {
+  const double* rop = c->rop;
+  const int64_t nd = c->nd;
+  const double t[3] = {tcx, tcy, tcz};
+  double qp[3] = {rop[nm + nd], rop[nm + 2 * nd], rop[nm + 3 * nd]};
+  const double qm[3] = {rop[l + nd], rop[l + 2 * nd], rop[l + 3 * nd]};
+  const int cart = c->typ == 2;
+  double qn1 = cart ? qp[d] * t[d] : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz;
+  const double qn2 = cart ? qm[d] * t[d] : qm[0] * tcx + qm[1] * tcy + qm[2] * tcz;
+  double qp1 = rop[nm], qm1 = rop[l];
+  const double qm6 = rop[l + 5 * nd] * qm1 * qn2;
+  const double qp6 = rop[nm + 5 * nd] * qp1 * qn1;
+  qp1 = sqrt(qp1);
+  qm1 = sqrt(qm1);
+  const double r_1 = 1. / (qp1 + qm1);
+  for (int m = 0; m < 3; m++) qp[m] = r_1 * (qp1 * qp[m] + qm1 * qm[m]);
+  qn1 = cart ? qp[d] * t[d] : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz;
+  const double s_1 = 1.0 / OMAX(s, 1.e-30);
+  const double tdu = OMAX(c->c1 / s_1, fabs(qn1));
+  return 0.5 * (qm6 + qp6 - tdu * (rop[l + 5 * nd] * rop[l] - rop[nm + 5 * nd] * rop[nm]));
+}
+
 /* One face flux (convective + viscous) of direction d at cell (i,j,k). */
 static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, double flu[6]) {
   int64_t l = inddm(c->pi, i, j, k);
@@ -893,11 +969,14 @@ static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, dou
   } else {
     face_normal(c, d, lt, &tcx, &tcy, &tcz, &s);
   }
-  if (c->kflu == 5) roe_face(c, qm, qp, tcx, tcy, tcz, s, flu);
-  else ausm_face(c, qm, qp, c->rop[l + 4 * c->nd], tcx, tcy, tcz, s,
+  if (c->kflu == 5) {
+    roe_face(c, qm, qp, tcx, tcy, tcz, s, flu);
+    if (c->neq == 6) flu[5] = roe_sa_flux(c, d, l, l - c->inc[d], tcx, tcy, tcz, s);
+  } else ausm_face(c, qm, qp, c->rop[l + 4 * c->nd], tcx, tcy, tcz, s,
                  c->wig ? c->wig[l + d * c->nd] : 0., flu);
   if (c->iflow >= 2) {
     if (c->typ == 2) visc_cart(c, d, l, flu);
+    else if (c->typ == 3) visc_2d(c, d, l, lt, tcx, tcy, flu);
     else visc_full(c, d, l, lt, tcx, tcy, tcz, flu);
   }
 }

@@ -417,6 +417,27 @@ def test_spalart_allmaras_explicit(oracle_mod, wall, wavy):
     s.close()
 
 
+@pytest.mark.parametrize("scheme,slope,temporal,wavy", [
+    ("roe", "o3", "explicit", 0.0), ("roe_min", "minmod", "explicit", 0.3),
+    ("roe", "o1", "implicit", 0.3), ("roe", "o3", "implicit", 0.0)])
+def test_spalart_allmaras_roe(oracle_mod, scheme, slope, temporal, wavy):
+    """Roe with Spalart-Allmaras (ROE/*/fluFaceSA_*.for: first-order ro
+    nutilde flux upwinded by the Roe-averaged normal velocity), no-slip wall
+    with the Roe wall-face correction, inflow / outflow / farfield."""
+    t = cases.bc_box(n=(14, 10, 6), model="NSTurbulent", scheme=scheme, slope=slope, wavy=wavy,
+                     temporal=temporal, ss_iteration=3, reynolds=500.0,
+                     time_step=0.02 if temporal == "explicit" else 0.05)
+    mv = 1000 if temporal == "explicit" else 1
+    zd, ref, s = _pair(t, oracle_mod, mv)
+    assert int(zd[0]["pi"][36]) == 6 and int(zd[0]["pi"][33]) == 5
+    nfin = 3 if temporal == "explicit" else 4
+    for it in range(1, 4):
+        ref.compute(it, 1, nfin, 1, modulo_verif=mv)
+        s.compute(it, 1, nfin, 1, 1)
+    _check_levels(ref, s)
+    s.close()
+
+
 @pytest.mark.parametrize("wavy", [0.0, 0.3])
 def test_spalart_allmaras_implicit(oracle_mod, wavy):
     """Spalart-Allmaras with LU-SGS: coe6 from the source Jacobian, the
@@ -471,10 +492,10 @@ def test_spalart_allmaras_mixed_precision(oracle_mod):
 
 
 def test_spalart_allmaras_refusals():
-    """Unsupported SA combinations are reported, never run: Roe + SA, and a
-    compute before the wall distance is given."""
+    """Unsupported SA combinations are reported, never run: senseur + SA, and
+    a compute before the wall distance is given."""
     from fast_gb300._native import Solver, FastGB300Error
-    t = cases.bc_box(n=(8, 8, 6), model="NSTurbulent", scheme="roe", temporal="explicit")
+    t = cases.bc_box(n=(8, 8, 6), model="NSTurbulent", scheme="senseur", temporal="explicit")
     zd = fasts.zone_data(t, fasts.prepare(t))
     s = Solver(0)
     with pytest.raises(FastGB300Error, match="AUSM"):

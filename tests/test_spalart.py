@@ -2,8 +2,9 @@
 and internal consistency on the CPU.
 
 * a uniform flow with uniform nutilde and no wall nearby stays uniform on a
-  curvilinear periodic mesh (the SA fluxes and the source gradients of
-  sourceSA_grad_3d.for are closed, production / destruction vanish);
+  curvilinear periodic mesh, with the AUSM+(P) and the Roe SA fluxes (the SA
+  fluxes and the source gradients of sourceSA_grad_3d.for are closed,
+  production / destruction vanish);
 * nutilde stays in [0, ratiom nu_lam] (core3ark3.for / mjr_newton_SA.for
   clip it there);
 * the curvilinear restatements (fluvisq_SA_3dfull, sourceSA_grad_3d) agree
@@ -31,12 +32,13 @@ def _interior(pi, q, nv=6):
     return q.reshape(nv, nk, nj, ni)[:, 2:nk - 2, 2:nj - 2, 2:ni - 2]
 
 
-@pytest.mark.parametrize("temporal", ["explicit", "implicit"])
-def test_sa_free_stream_curvilinear(oracle_mod, temporal):
+@pytest.mark.parametrize("temporal,scheme", [("explicit", "ausmpred"), ("implicit", "ausmpred"),
+                                             ("explicit", "roe"), ("implicit", "roe")])
+def test_sa_free_stream_curvilinear(oracle_mod, temporal, scheme):
     numb = ({"temporal_scheme": "explicit", "ss_iteration": 1, "modulo_verif": 1000}
             if temporal == "explicit" else None)
     t = cases.taylor_green(n=(10, 8, 6), wavy=0.3, mach=0.2, model="NSTurbulent", dt=0.05,
-                           ss_iteration=2, numb=numb)
+                           ss_iteration=2, numb=numb, scheme=scheme)
     zd = fasts.zone_data(t, fasts.prepare(t))
     pi = zd[0]["pi"]
     assert int(pi[36]) == 6 and int(pi[25]) == 0
@@ -57,10 +59,12 @@ def test_sa_free_stream_curvilinear(oracle_mod, temporal):
     assert np.max(np.abs(q - q0).reshape(6, nd) / scale) < 1e-13
 
 
-@pytest.mark.parametrize("temporal,wavy", [("explicit", 0.0), ("implicit", 0.3)])
-def test_sa_nutilde_bounds(oracle_mod, temporal, wavy):
+@pytest.mark.parametrize("temporal,wavy,scheme", [("explicit", 0.0, "ausmpred"),
+                                                ("implicit", 0.3, "ausmpred"),
+                                                ("explicit", 0.3, "roe"), ("implicit", 0.0, "roe")])
+def test_sa_nutilde_bounds(oracle_mod, temporal, wavy, scheme):
     t = cases.bc_box(n=(12, 10, 6), model="NSTurbulent", temporal=temporal, ss_iteration=3,
-                     wavy=wavy, reynolds=500.0, time_step=0.02)
+                     wavy=wavy, reynolds=500.0, time_step=0.02, scheme=scheme)
     zd, c = _case(oracle_mod, t)
     pi, pr = zd[0]["pi"], zd[0]["pr"]
     for it in range(1, 5):
