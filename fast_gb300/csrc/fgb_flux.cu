@@ -188,7 +188,7 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
 // ROE/3dfull/fluFaceSA_*_3dfull_{i,j,k}.for (3dcart: Vit_ent/qn_3dcart_*):
 // the ro nutilde flux from the first-order states of cells nm = l - inc and
 // l, upwinded by the Roe-averaged normal velocity with the floor c1 |S|.
-template <int D, bool CART>
+template <int D, bool CART, bool TWO_D = false>
 __device__ __forceinline__ double roe_sa_flux(const Zone& z, const double* __restrict__ q,
                                               int64_t l, int64_t nm, double tcx, double tcy,
                                               double tcz, double s) {
@@ -196,8 +196,8 @@ __device__ __forceinline__ double roe_sa_flux(const Zone& z, const double* __res
   const double t[3] = {tcx, tcy, tcz};
   double qp[3] = {q[nm + nd], q[nm + 2 * nd], q[nm + 3 * nd]};
   const double qm[3] = {q[l + nd], q[l + 2 * nd], q[l + 3 * nd]};
-  double qn1 = CART ? qp[D] * t[D] : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz;
-  const double qn2 = CART ? qm[D] * t[D] : qm[0] * tcx + qm[1] * tcy + qm[2] * tcz;
+  double qn1 = CART ? qp[D] * t[D] : (TWO_D ? qp[0] * tcx + qp[1] * tcy : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz);
+  const double qn2 = CART ? qm[D] * t[D] : (TWO_D ? qm[0] * tcx + qm[1] * tcy : qm[0] * tcx + qm[1] * tcy + qm[2] * tcz);
   double qp1 = q[nm], qm1 = q[l];
   const double qm6 = q[l + 5 * nd] * qm1 * qn2;
   const double qp6 = q[nm + 5 * nd] * qp1 * qn1;
@@ -206,7 +206,7 @@ __device__ __forceinline__ double roe_sa_flux(const Zone& z, const double* __res
   const double r_1 = 1. / (qp1 + qm1);
 #pragma unroll
   for (int m = 0; m < 3; m++) qp[m] = r_1 * (qp1 * qp[m] + qm1 * qm[m]);
-  qn1 = CART ? qp[D] * t[D] : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz;
+  qn1 = CART ? qp[D] * t[D] : (TWO_D ? qp[0] * tcx + qp[1] * tcy : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz);
   const double s_1 = 1.0 / fmaxF(s, 1.E-30);
   const double tdu = fmaxF(z.c1 / s_1, fabs(qn1));
   return 0.5 * (qm6 + qp6 - tdu * (q[l + 5 * nd] * q[l] - q[nm + 5 * nd] * q[nm]));
@@ -495,11 +495,12 @@ __device__ __forceinline__ void visc_full(const Zone& z, const double* __restric
 
 // ------------------------------------------------------- viscous (2-d)
 // fluvisq_2d_{i,j}.for + mut_interface.for: visc_full without the k faces,
-// one transverse direction A, two velocity components (no w row).
-template <int D>
+// one transverse direction A, two velocity components (no w row).  NV = 6:
+// SA/fluvisq_2d_* (mut_prandtltb_interface.for) + SA/fluvisq_SA_2d_*.
+template <int D, int NV = 5>
 __device__ __forceinline__ void visc_2d(const Zone& z, const double* __restrict__ q,
                                         const double* __restrict__ xmut, int64_t l, int64_t lt,
-                                        double tcx, double tcy, double F[5]) {
+                                        double tcx, double tcy, double F[NV]) {
   constexpr int A = 1 - D;
   const int64_t nd = z.nd, ndm = z.ndm;
   const double* TD = D == 0 ? z.ti : z.tj;
@@ -530,7 +531,7 @@ __device__ __forceinline__ void visc_2d(const Zone& z, const double* __restrict_
   const double e1 = g[0][0] - div, e2 = g[0][1] + g[1][0], e4 = g[1][1] - div;
   const double volinv = 1. / (z.vol[lt] + z.vol[ltm]);
   double xmutvol, xktvol, xsa;
-  mut_face<5>(z, q, xmut, il, ir, volinv, xmutvol, xktvol, xsa);
+  mut_face<NV>(z, q, xmut, il, ir, volinv, xmutvol, xktvol, xsa);
   double fv, fv5;
   fv = -(2. * e1 * tcx + e2 * tcy) * xmutvol;
   fv5 = fv * (q[ir + nd] + q[il + nd]);
@@ -540,6 +541,15 @@ __device__ __forceinline__ void visc_2d(const Zone& z, const double* __restrict_
   F[2] = F[2] + fv;
   fv = fv5 * 0.5 - (g[2][0] * tcx + g[2][1] * tcy) * xktvol;
   F[4] = F[4] + fv;
+  if (NV == 6) {   // diffusion of nutilde
+    const double* Q = q + 5 * nd;
+    const double f1 = Q[il], f2 = Q[ir];
+    const double f3 = Q[ir] + Q[il] + Q[il - iA] + Q[ir - iA];
+    const double f4 = Q[ir] + Q[il] + Q[il + iA] + Q[ir + iA];
+    const double gx = (f2 * t1[0] - f1 * t0[0]) + (f4 * ta1[0] - f3 * ta0[0]);
+    const double gy = (f2 * t1[1] - f1 * t0[1]) + (f4 * ta1[1] - f3 * ta0[1]);
+    F[NV - 1] = F[NV - 1] - xsa * (gx * tcx + gy * tcy);
+  }
 }
 
 // ------------------------------------------------------------- face kernel
@@ -582,10 +592,14 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     const double* t = D == 0 ? z.ti : z.tj;
     double tcx = t[lt], tcy = t[lt + z.ndm];
     double s = sqrt(tcx * tcx + tcy * tcy);
-    if (KF == ROE) roe_full(z, qm, qp, tcx, tcy, 0., s, F);
-    else ausm_face<D, false>(z, qm, qp, q[l + 4 * nd], tcx, tcy, 0., s, F);
+    if (KF == ROE) {
+      roe_full(z, qm, qp, tcx, tcy, 0., s, F);
+      if (NV == 6) F[NV - 1] = roe_sa_flux<D, false, true>(z, q, l, l - inc, tcx, tcy, 0., s);
+    } else {
+      ausm_face<D, false, false, NV>(z, qm, qp, q[l + 4 * nd], tcx, tcy, 0., s, F);
+    }
     F[3] = 0.;
-    if (VISC) visc_2d<D>(z, q, xmut, l, lt, tcx, tcy, F);
+    if (VISC) visc_2d<D, NV>(z, q, xmut, l, lt, tcx, tcy, F);
   } else if (TYP == Z3DCART) {
     if (KF == ROE) {
       roe_cart<D>(z, qm, qp, F);
@@ -764,7 +778,31 @@ __global__ void __launch_bounds__(256) sa_source(Zone z, const double* __restric
   const double vol = z.vol[lt];
   const double xvol = 0.5 / vol;
   double g[3][3], gn[3], gr[3];
-  if (TYP == Z3DCART) {   // sourceSA_grad_3dcart.for
+  if (TYP == Z2D) {       // sourceSA_grad_2d.for: i and j faces, u and v
+    const double* TT[2] = {z.ti, z.tj};
+    double t0[2][2], t1[2][2];
+#pragma unroll
+    for (int x = 0; x < 2; x++)
+#pragma unroll
+      for (int d = 0; d < 2; d++) {
+        t0[x][d] = TT[d][lt + x * ndm];
+        t1[x][d] = TT[d][lt + z.minc[d] + x * ndm];
+      }
+#pragma unroll
+    for (int v = 0; v < 3; v++) {
+      const double* Q = v < 2 ? q + (v + 1) * nd : Nu;
+      const double u1 = (Q[l] + Q[l2]), u2 = (Q[l] + Q[l3]), u3 = (Q[l] + Q[l1]);
+      const double u4 = (Q[l] + Q[l4]);
+      double* o = v < 2 ? g[v] : gn;
+#pragma unroll
+      for (int x = 0; x < 2; x++) o[x] = (u3 * t1[x][0] - u1 * t0[x][0] + u2 * t1[x][1] - u4 * t0[x][1]);
+    }
+    const double a = Nu[l] * Rr[l];
+    const double u1 = a + Nu[l2] * Rr[l2], u2 = a + Nu[l3] * Rr[l3], u3 = a + Nu[l1] * Rr[l1];
+    const double u4 = a + Nu[l4] * Rr[l4];
+#pragma unroll
+    for (int x = 0; x < 2; x++) gr[x] = (u3 * t1[x][0] - u1 * t0[x][0] + u2 * t1[x][1] - u4 * t0[x][1]);
+  } else if (TYP == Z3DCART) {   // sourceSA_grad_3dcart.for
     const double tix = z.ti[0], tjy = z.tj[0], tkz = z.tk[0];
 #pragma unroll
     for (int v = 0; v < 4; v++) {
@@ -812,17 +850,27 @@ __global__ void __launch_bounds__(256) sa_source(Zone z, const double* __restric
                u5 * t1[x][2] - u6 * t0[x][2]);
   }
   // vorticity and strain magnitudes
-  const double rotx = g[2][1] - g[1][2], roty = g[0][2] - g[2][0], rotz = g[1][0] - g[0][1];
-  const double rot = sqrt(rotx * rotx + roty * roty + rotz * rotz) * xvol;
-  const double S11 = g[0][0], S22 = g[1][1], S33 = g[2][2];
-  const double S12 = 0.5 * (g[0][1] + g[1][0]), S13 = 0.5 * (g[0][2] + g[2][0]),
-               S23 = 0.5 * (g[1][2] + g[2][1]);
-  double St = S11 * S11 + S22 * S22 + S33 * S33 + 2. * (S12 * S12) + 2. * (S13 * S13) +
-              2. * (S23 * S23);
-  St = sqrt(2. * St) * xvol;
   const double c1 = SA_CB2 / SA_SIGMA;
   const double cw1 = (SA_CB1 / SA_CKARM / SA_CKARM) + (1. + SA_CB2) / SA_SIGMA;
-  const double anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1] + gn[2] * gr[2]) * xvol * xvol;
+  double rot, St, anvisc;
+  if (TYP == Z2D) {
+    const double rotz = g[1][0] - g[0][1];
+    rot = fabs(rotz) * xvol;
+    const double S11 = g[0][0], S22 = g[1][1], S12 = 0.5 * (g[0][1] + g[1][0]);
+    St = S11 * S11 + S22 * S22 + 2. * (S12 * S12);
+    St = sqrt(2. * St) * xvol;
+    anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1]) * xvol * xvol;
+  } else {
+    const double rotx = g[2][1] - g[1][2], roty = g[0][2] - g[2][0], rotz = g[1][0] - g[0][1];
+    rot = sqrt(rotx * rotx + roty * roty + rotz * rotz) * xvol;
+    const double S11 = g[0][0], S22 = g[1][1], S33 = g[2][2];
+    const double S12 = 0.5 * (g[0][1] + g[1][0]), S13 = 0.5 * (g[0][2] + g[2][0]),
+                 S23 = 0.5 * (g[1][2] + g[2][1]);
+    St = S11 * S11 + S22 * S22 + S33 * S33 + 2. * (S12 * S12) + 2. * (S13 * S13) +
+         2. * (S23 * S23);
+    St = sqrt(2. * St) * xvol;
+    anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1] + gn[2] * gr[2]) * xvol * xvol;
+  }
   // mulam.for, SA/chi.for
   const double amulam = sa_mulam(z, q[l + 4 * nd]);
   const double anulam = Rr[l] / amulam;
@@ -865,6 +913,7 @@ cudaError_t launch_sa_source(const Zone& z, const double* q, double* drodm, doub
   const unsigned g = (unsigned)((n + B - 1) / B);
   if (z.typ == Z3DCART) sa_source<Z3DCART><<<g, B, 0, st>>>(z, q, drodm, coe, coefH, zero_init, lu);
   else if (z.typ == Z3DFULL) sa_source<Z3DFULL><<<g, B, 0, st>>>(z, q, drodm, coe, coefH, zero_init, lu);
+  else if (z.typ == Z2D) sa_source<Z2D><<<g, B, 0, st>>>(z, q, drodm, coe, coefH, zero_init, lu);
   else return cudaErrorNotSupported;
   return cudaGetLastError();
 }
@@ -896,6 +945,13 @@ static cudaError_t launch_faces_t(const Zone& z, const double* q, const double* 
 cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
                          double* Fj, double* Fk, cudaStream_t st) {
   const bool visc = z.iflow >= 2;
+  if (z.neq == 6 && z.typ == Z2D) {   // Spalart-Allmaras on 2-d zones
+    if (z.kflu == AUSM && z.slope == O3) return launch_faces_t<Z2D, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == ROE && z.slope == O1) return launch_faces_t<Z2D, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == ROE && z.slope == O3) return launch_faces_t<Z2D, ROE, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == ROE && z.slope == MINMOD) return launch_faces_t<Z2D, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    return cudaErrorNotSupported;
+  }
   if (z.neq == 6) {   // Spalart-Allmaras: AUSM+(P) o3 or Roe o1 / o3 / minmod, 3d zones
     const bool cart = z.typ == Z3DCART;
     if (z.typ != Z3DCART && z.typ != Z3DFULL) return cudaErrorNotSupported;

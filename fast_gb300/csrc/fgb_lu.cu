@@ -1036,20 +1036,19 @@ cudaError_t launch_lusgs(const LuZone* zh, const LuGroup& L, cudaStream_t st) {
   if (L.nz < 1) return cudaSuccess;
   const Zone& z = zh[0].z;
   const bool sa = z.neq == 6;   // Spalart-Allmaras: 3d zones
-  if (sa && z.typ == Z2D) return cudaErrorNotSupported;
   if (L.fp32) {
     const int rs = z.typ == Z3DCART ? Rec<Z3DCART, float>::SIZE : Rec<Z3DFULL, float>::SIZE;
     PlaneData<float> p = plane_data<float>(L, rs);
     if (z.typ == Z3DCART)
       return sa ? group_t<Z3DCART, float, 6>(zh, p, L, st) : group_t<Z3DCART, float, 5>(zh, p, L, st);
-    if (z.typ == Z2D) return group_t<Z2D, float, 5>(zh, p, L, st);
+    if (z.typ == Z2D) return sa ? group_t<Z2D, float, 6>(zh, p, L, st) : group_t<Z2D, float, 5>(zh, p, L, st);
     return sa ? group_t<Z3DFULL, float, 6>(zh, p, L, st) : group_t<Z3DFULL, float, 5>(zh, p, L, st);
   }
   const int rs = z.typ == Z3DCART ? Rec<Z3DCART, double>::SIZE : Rec<Z3DFULL, double>::SIZE;
   PlaneData<double> p = plane_data<double>(L, rs);
   if (z.typ == Z3DCART)
     return sa ? group_t<Z3DCART, double, 6>(zh, p, L, st) : group_t<Z3DCART, double, 5>(zh, p, L, st);
-  if (z.typ == Z2D) return group_t<Z2D, double, 5>(zh, p, L, st);
+  if (z.typ == Z2D) return sa ? group_t<Z2D, double, 6>(zh, p, L, st) : group_t<Z2D, double, 5>(zh, p, L, st);
   return sa ? group_t<Z3DFULL, double, 6>(zh, p, L, st) : group_t<Z3DFULL, double, 5>(zh, p, L, st);
 }
 

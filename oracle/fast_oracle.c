@@ -153,6 +153,36 @@ void or_spsource(const int64_t* pi, const double* pr, int nitcfg, const int64_t*
         const int64_t l1 = l + 1, l2 = l - 1, l3 = l + incj, l4 = l - incj, l5 = l + inck, l6 = l - inck;
         const double xvol = 0.5 / vol[lt];
         double g[3][3], gn[3], gr[3];   /* g[v][x]: d(u,v,w)/dx, gn: d nutilde, gr: d ro nutilde */
+        double rot, St, anvisc;
+        if (typ == 3) {   /* sourceSA_grad_2d.for: i and j faces, u and v */
+          const double* T[2] = {ti, tj};
+          const int64_t lt1[2] = {lt + mi, lt + mj};
+          double t0[2][2], t1[2][2];
+          for (int x = 0; x < 2; x++)
+            for (int d = 0; d < 2; d++) {
+              t0[x][d] = T[d][lt + x * ndm];
+              t1[x][d] = T[d][lt1[d] + x * ndm];
+            }
+          for (int v = 0; v < 3; v++) {
+            const double* q = v < 2 ? rop + (v + 1) * nd : nu_;
+            double u1 = (q[l] + q[l2]), u2 = (q[l] + q[l3]), u3 = (q[l] + q[l1]);
+            double u4 = (q[l] + q[l4]);
+            double* o = v < 2 ? g[v] : gn;
+            for (int x = 0; x < 2; x++)
+              o[x] = (u3 * t1[x][0] - u1 * t0[x][0] + u2 * t1[x][1] - u4 * t0[x][1]);
+          }
+          double a = nu_[l] * r_[l];
+          double u1 = a + nu_[l2] * r_[l2], u2 = a + nu_[l3] * r_[l3], u3 = a + nu_[l1] * r_[l1];
+          double u4 = a + nu_[l4] * r_[l4];
+          for (int x = 0; x < 2; x++)
+            gr[x] = (u3 * t1[x][0] - u1 * t0[x][0] + u2 * t1[x][1] - u4 * t0[x][1]);
+          const double rotz = g[1][0] - g[0][1];
+          rot = fabs(rotz) * xvol;
+          const double S11 = g[0][0], S22 = g[1][1], S12 = 0.5 * (g[0][1] + g[1][0]);
+          St = S11 * S11 + S22 * S22 + 2. * (S12 * S12);
+          St = sqrt(2. * St) * xvol;
+          anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1]) * xvol * xvol;
+        } else {
         if (typ == 2) {   /* sourceSA_grad_3dcart.for */
           const double tix = ti[0], tjy = tj[0], tkz = tk[0];
           for (int v = 0; v < 3; v++) {
@@ -209,13 +239,14 @@ void or_spsource(const int64_t* pi, const double* pr, int nitcfg, const int64_t*
         const double dvdx = g[1][0], dvdy = g[1][1], dvdz = g[1][2];
         const double dwdx = g[2][0], dwdy = g[2][1], dwdz = g[2][2];
         const double rotx = dwdy - dvdz, roty = dudz - dwdx, rotz = dvdx - dudy;
-        const double rot = sqrt(rotx * rotx + roty * roty + rotz * rotz) * xvol;
+        rot = sqrt(rotx * rotx + roty * roty + rotz * rotz) * xvol;
         const double S11 = dudx, S22 = dvdy, S33 = dwdz;
         const double S12 = 0.5 * (dudy + dvdx), S13 = 0.5 * (dudz + dwdx), S23 = 0.5 * (dvdz + dwdy);
-        double St = S11 * S11 + S22 * S22 + S33 * S33 + 2. * (S12 * S12) + 2. * (S13 * S13) +
-                    2. * (S23 * S23);
+        St = S11 * S11 + S22 * S22 + S33 * S33 + 2. * (S12 * S12) + 2. * (S13 * S13) +
+             2. * (S23 * S23);
         St = sqrt(2. * St) * xvol;
-        const double anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1] + gn[2] * gr[2]) * xvol * xvol;
+        anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1] + gn[2] * gr[2]) * xvol * xvol;
+        }
         /* mulam.for, chi.for */
         const double amulam = sa_mulam(coesut, temp01, cmus1, rop[l + 4 * nd]);
         const double anulam = r_[l] / amulam;
@@ -916,8 +947,13 @@ static void visc_2d(const fctx* c, int d, int64_t l, int64_t lt, double tcx, dou
   const double div = (g[0][0] + g[1][1]) * c->cvisq;
   const double f1 = g[0][0] - div, f2 = g[0][1] + g[1][0], f4 = g[1][1] - div;
   const double volinv = 1. / (c->vol[lt] + c->vol[ltm]);
-  const double xmutvol = (c->xmut[ir] + c->xmut[il]) * volinv;
-  const double xktvol = xmutvol * c->gam3;
+  double xmutvol, xktvol, xmutvol_sa = 0.;
+  if (c->neq == 6) {   /* SA/fluvisq_2d_*.for: mut_prandtltb_interface.for */
+    sa_mut(c, il, ir, volinv, &xmutvol, &xktvol, &xmutvol_sa);
+  } else {
+    xmutvol = (c->xmut[ir] + c->xmut[il]) * volinv;
+    xktvol = xmutvol * c->gam3;
+  }
   double fv, fv5;
   fv = -(2. * f1 * tcx + f2 * tcy) * xmutvol;
   fv5 = fv * (rop[ir + nd] + rop[il + nd]);
@@ -927,6 +963,15 @@ static void visc_2d(const fctx* c, int d, int64_t l, int64_t lt, double tcx, dou
   flu[2] = flu[2] + fv;
   fv = fv5 * 0.5 - (g[2][0] * tcx + g[2][1] * tcy) * xktvol;
   flu[4] = flu[4] + fv;
+  if (c->neq == 6) {   /* SA/fluvisq_SA_2d_*.for: diffusion of nutilde */
+    const double* q = rop + 5 * nd;
+    double f1n = q[il], f2n = q[ir];
+    double f3n = q[ir] + q[il] + q[il - iA] + q[ir - iA];
+    double f4n = q[ir] + q[il] + q[il + iA] + q[ir + iA];
+    double gx = (f2n * t1[0] - f1n * t0[0]) + (f4n * ta1[0] - f3n * ta0[0]);
+    double gy = (f2n * t1[1] - f1n * t0[1]) + (f4n * ta1[1] - f3n * ta0[1]);
+    flu[5] = flu[5] - xmutvol_sa * (gx * tcx + gy * tcy);
+  }
 }
 
 /* Roe flux of ro * nutilde (ROE/3dfull/fluFaceSA_*_3dfull_i.for and the
@@ -941,9 +986,9 @@ static double roe_sa_flux(const fctx* c, int d, int64_t l, int64_t nm, double tc
   const double t[3] = {tcx, tcy, tcz};
   double qp[3] = {rop[nm + nd], rop[nm + 2 * nd], rop[nm + 3 * nd]};
   const double qm[3] = {rop[l + nd], rop[l + 2 * nd], rop[l + 3 * nd]};
-  const int cart = c->typ == 2;
-  double qn1 = cart ? qp[d] * t[d] : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz;
-  const double qn2 = cart ? qm[d] * t[d] : qm[0] * tcx + qm[1] * tcy + qm[2] * tcz;
+  const int cart = c->typ == 2, two_d = c->typ == 3;
+  double qn1 = cart ? qp[d] * t[d] : (two_d ? qp[0] * tcx + qp[1] * tcy : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz);
+  const double qn2 = cart ? qm[d] * t[d] : (two_d ? qm[0] * tcx + qm[1] * tcy : qm[0] * tcx + qm[1] * tcy + qm[2] * tcz);
   double qp1 = rop[nm], qm1 = rop[l];
   const double qm6 = rop[l + 5 * nd] * qm1 * qn2;
   const double qp6 = rop[nm + 5 * nd] * qp1 * qn1;
@@ -951,7 +996,7 @@ static double roe_sa_flux(const fctx* c, int d, int64_t l, int64_t nm, double tc
   qm1 = sqrt(qm1);
   const double r_1 = 1. / (qp1 + qm1);
   for (int m = 0; m < 3; m++) qp[m] = r_1 * (qp1 * qp[m] + qm1 * qm[m]);
-  qn1 = cart ? qp[d] * t[d] : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz;
+  qn1 = cart ? qp[d] * t[d] : (two_d ? qp[0] * tcx + qp[1] * tcy : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz);
   const double s_1 = 1.0 / OMAX(s, 1.e-30);
   const double tdu = OMAX(c->c1 / s_1, fabs(qn1));
   return 0.5 * (qm6 + qp6 - tdu * (rop[l + 5 * nd] * rop[l] - rop[nm + 5 * nd] * rop[nm]));
@@ -1198,6 +1243,14 @@ void or_core3ark3(const int64_t* pi, const double* pr, int nitcfg, const int64_t
           double roe_old = ro_old * (cv * t_old + 0.5 * (u_old * u_old + v_old * v_old));
           rop_1[l + 4 * nd] = (roe_old + tab5) * r_1 * cvinv -
               cvinv2 * (rop_1[l + nd] * rop_1[l + nd] + rop_1[l + 2 * nd] * rop_1[l + 2 * nd]);
+          if (sa) {   /* core3ark3.for:238-276 (2-d) */
+            double tab6 = drodm[l + 5 * nd] * (coefW * coe[l]);
+            double anulam = sa_mulam(coesut, temp01, cmus1, rop_1[l + 4 * nd]);
+            anulam = anulam * r_1 * pr[SA_RATIOM_R];
+            double t6 = (ro_old * rop[l + 5 * nd] + tab6) * r_1;
+            t6 = OMIN(t6, anulam);
+            rop_1[l + 5 * nd] = OMAX(t6, 0.);
+          }
         }
       }
 }
@@ -1381,6 +1434,7 @@ static void lu_nb(const luctx* c, int d, int64_t l1, int64_t ltnb1, int64_t ltnb
     b[2] = b31 * o1 + b32 * o2 + b33 * o3 + b35 * o5;
     b[3] = 0.;
     b[4] = b51 * o1 + b52 * o2 + b53 * o3 + b55 * o5;
+    if (c->neq == 6) b[5] = (qn + cs) * o6;   /* lu_{i,j}_2d_SA.for */
   }
 }
 
@@ -1399,6 +1453,15 @@ static void mjr_newton(const int64_t* pi, const double* pr, int64_t l, const dou
     double roe_old = ro_old * (pr[CVINF] * t_old + 0.5 * (u_old * u_old + v_old * v_old));
     double n5 = (roe_old + out[l + 4 * nd]) * r_1 * cvinv - cvinv2 * (n2 * n2 + n3 * n3);
     rop_1[l] = n1; rop_1[l + nd] = n2; rop_1[l + 2 * nd] = n3; rop_1[l + 3 * nd] = 0.; rop_1[l + 4 * nd] = n5;
+    if (pi[NEQ] == 6) {   /* mjr_newton_2d_SA.for */
+      const double cmus1 = pr[CS], temp01 = 1. / pr[TEMP0];
+      const double coesut = pr[XMUL0] * (1. + cmus1 * temp01);
+      double anulam = sa_mulam(coesut, temp01, cmus1, n5);
+      anulam = anulam * r_1 * pr[SA_RATIOM_R];
+      double t6 = (ro_old * nu_old + out[l + 5 * nd]) * r_1;
+      t6 = OMIN(t6, anulam);
+      rop_1[l + 5 * nd] = OMAX(t6, 0.);
+    }
     return;
   }
   double n4 = (ro_old * w_old + out[l + 3 * nd]) * r_1;
