@@ -38,6 +38,7 @@ SIGNATURES = {
     "fgb_residuals": ([_P, C.c_int, _DP, C.c_int64, C.POINTER(C.c_int)], C.c_int),
     "fgb_residual_norms_noalloc": ([_P, C.c_int, _P], C.c_int),
     "fgb_set_bc_state": ([_P, C.c_int, _DP], C.c_int),
+    "fgb_cfl": ([_P, C.c_int, _DP], C.c_int),
     "fgb_adjoint_forward": ([_P, C.c_int, C.c_int, C.c_int], C.c_int),
     "fgb_adjoint_backward": ([_P, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP], C.c_int),
     "fgb_tangent": ([_P, C.c_int, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP], C.c_int),
@@ -178,6 +179,12 @@ class Solver:
         """Enqueue fgb_residual_norms_noalloc: 2*neq doubles (L2 then Loo)
         written to the device address out_ptr; fgb_synchronize waits."""
         _check(self._lib.fgb_residual_norms_noalloc(self._h, int(zone), C.c_void_p(int(out_ptr))))
+
+    def cfl(self, zone: int) -> np.ndarray:
+        """(max, min, mean) CFL of the last verified iteration (cpcfl3.for)."""
+        out = np.zeros(3)
+        _check(self._lib.fgb_cfl(self._h, int(zone), _dp(out)))
+        return out
 
     def set_bc_state(self, zone: int, st):
         a = np.ascontiguousarray(st, dtype=np.float64)

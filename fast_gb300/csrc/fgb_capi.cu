@@ -73,6 +73,8 @@ struct ZoneData {
   double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
   double* wig = nullptr;            // senseur wiggle flags (KFLUDOM = 2)
   double* dist = nullptr;           // wall distance (Spalart-Allmaras)
+  double* cfl = nullptr;            // CFL max, min, mean of the last verified iteration
+  double* cfl_part = nullptr;       // per-CTA partials of the CFL reduction
   bool dist_set = false;
   int32_t* posmap = nullptr;        // natural index -> plane index in the zone's LU group
   int64_t n_rdm = 0, ijkv_lu[3] = {1, 1, 1};
@@ -547,6 +549,8 @@ int fgb_destroy(fgb_solver* s) {
     }
     cudaFree(Z.wig);
     cudaFree(Z.dist);
+    cudaFree(Z.cfl);
+    cudaFree(Z.cfl_part);
     for (WallCorrList& w : Z.walls) { cudaFree(w.l); cudaFree(w.l0); cudaFree(w.lt); cudaFree(w.nrm); }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
@@ -650,6 +654,9 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
     Z.ijkv_lu[d] = q > 1 ? q : 1;
   }
   Z.n_rdm = p[NSSITER] * neq * 2 * Z.ijkv_lu[0] * Z.ijkv_lu[1] * Z.ijkv_lu[2];
+  CK(cudaMalloc(&Z.cfl, sizeof(double) * 3));
+  CK(cudaMemset(Z.cfl, 0, sizeof(double) * 3));
+  CK(cudaMalloc(&Z.cfl_part, sizeof(double) * 3 * (size_t)cfl_partial_blocks(Z.z)));
   CK(cudaMalloc(&Z.rdm, sizeof(double) * Z.n_rdm));
   CK(cudaMemset(Z.rdm, 0, sizeof(double) * Z.n_rdm));
   int rc = build_ghost_lists(Z, hti, htj, htk);
@@ -1168,6 +1175,11 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             CK(launch_coefficients(z, ca, s->st));
           }
           s->launches++;
+          if (verif) {   // cptst3.for:115-120: CFL statistics of a verified iteration
+            ProfScope ps(s, "cfl");
+            CK(launch_cfl(z, ssiter, Z.xmut, Z.cfl_part, Z.cfl, s->st));
+            s->launches += 2;
+          }
         }
         if (nstep == 1 && z.kflu == SENSEUR) {  // src_term.for:257-266
           ProfScope ps(s, "wiggle");
@@ -1268,6 +1280,16 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       Z.lvl[2] = save;
     }
   }
+  return FGB_OK;
+}
+
+int fgb_cfl(fgb_solver* s, int zone, double* out) {
+  int rc = check_zone(s, zone);
+  if (rc) return rc;
+  if (!out) return fail(FGB_ERR_ARG, "null output pointer");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->st));
+  CK(cudaMemcpy(out, s->zones[zone].cfl, sizeof(double) * 3, cudaMemcpyDeviceToHost));
   return FGB_OK;
 }
 

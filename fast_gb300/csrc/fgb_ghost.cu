@@ -216,6 +216,128 @@ cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------- CFL numbers
+// cpcfl3.for (non-ALE branches): per interior cell dt / min(vis, conv)
+// (Navier-Stokes) or dt / conv (Euler) with the cell's face areas; each CTA
+// reduces its cells to (max, min, sum) partials, cfl_finish reduces the
+// partials in CTA order.
+template <int TYP>
+__device__ __forceinline__ double cfl_cell(const Zone& z, const double* __restrict__ q,
+                                           const double* __restrict__ xmut, int64_t i, int64_t j,
+                                           int64_t k, double surf_c, double dt, double gam1,
+                                           double gam2, int visc) {
+  const int64_t nd = z.nd, ndm = z.ndm;
+  const int64_t l = inddm(z, i, j, k);
+  const int64_t lvo = TYP == Z3DCART ? 0 : indmtr(z, i, j, k);
+  double surf = surf_c;
+  if (TYP == Z3DFULL) {
+    const double* T[3] = {z.ti, z.tj, z.tk};
+    double dd[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double* t = T[d];
+      const int64_t a = lvo + z.minc[d], b = lvo;
+      dd[d] = sqrt(t[a] * t[a] + t[a + ndm] * t[a + ndm] + t[a + 2 * ndm] * t[a + 2 * ndm]);
+      dd[d] = dd[d] + sqrt(t[b] * t[b] + t[b + ndm] * t[b + ndm] + t[b + 2 * ndm] * t[b + 2 * ndm]);
+    }
+    surf = 1. / fmaxF(fmaxF(dd[0], dd[1]), dd[2]);
+  } else if (TYP == Z2D) {
+    const double* T[2] = {z.ti, z.tj};
+    double dd[2];
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+      const double* t = T[d];
+      const int64_t a = lvo + z.minc[d], b = lvo;
+      dd[d] = sqrt(t[a] * t[a] + t[a + ndm] * t[a + ndm]);
+      dd[d] = dd[d] + sqrt(t[b] * t[b] + t[b + ndm] * t[b + ndm]);
+    }
+    surf = 1. / fmaxF(dd[0], dd[1]);
+  }
+  const double u = q[l + nd], v = q[l + 2 * nd], w = q[l + 3 * nd], r = q[l];
+  const double c = sqrt(gam2 * q[l + 4 * nd]);
+  const double ur2 = TYP == Z2D ? u * u + v * v : u * u + v * v + w * w;
+  const double sp = sqrt(ur2);
+  const double xinvspc = 1. / (sp + c);
+  const double vo = z.vol[lvo];
+  const double conv = 2. * vo * surf * xinvspc;
+  if (!visc) return dt / conv;
+  const double xinvkt = gam1 / xmut[l];
+  const double vis = 2. * r * vo * vo * surf * surf * xinvkt;
+  return dt / fminF(vis, conv);
+}
+
+template <int TYP>
+__global__ void __launch_bounds__(256) cfl_partial(Zone z, const double* __restrict__ q,
+                                                   const double* __restrict__ xmut, double surf_c,
+                                                   double dt, double gam1, double gam2, int visc,
+                                                   double* __restrict__ part) {
+  const int64_t n = z.ni * z.nj * z.nk;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double mx = 0., mn = 100000000., sm = 0.;
+  if (t < n) {
+    const int64_t ii = t % z.ni, r = t / z.ni;
+    const double x = cfl_cell<TYP>(z, q, xmut, ii + 1, r % z.nj + 1, r / z.nj + 1, surf_c, dt,
+                                   gam1, gam2, visc);
+    mx = x; mn = x; sm = x;
+  }
+  __shared__ double s_mx[256], s_mn[256], s_sm[256];
+  s_mx[threadIdx.x] = mx; s_mn[threadIdx.x] = mn; s_sm[threadIdx.x] = sm;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      s_mx[threadIdx.x] = fmaxF(s_mx[threadIdx.x], s_mx[threadIdx.x + o]);
+      s_mn[threadIdx.x] = fminF(s_mn[threadIdx.x], s_mn[threadIdx.x + o]);
+      s_sm[threadIdx.x] = s_sm[threadIdx.x] + s_sm[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[3 * blockIdx.x] = s_mx[0];
+    part[3 * blockIdx.x + 1] = s_mn[0];
+    part[3 * blockIdx.x + 2] = s_sm[0];
+  }
+}
+
+__global__ void __launch_bounds__(32) cfl_finish(const double* __restrict__ part, int64_t nb,
+                                                 double ncell, double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double mx = 0., mn = 100000000., sm = 0.;
+  for (int64_t b = 0; b < nb; b++) {
+    mx = fmaxF(mx, part[3 * b]);
+    mn = fminF(mn, part[3 * b + 1]);
+    sm = sm + part[3 * b + 2];
+  }
+  out[0] = mx; out[1] = mn; out[2] = sm / ncell;
+}
+
+int64_t cfl_partial_blocks(const Zone& z) { return (z.ni * z.nj * z.nk + 255) / 256; }
+
+cudaError_t launch_cfl(const Zone& z, const double* q, const double* xmut, double* part,
+                       double* out, cudaStream_t st) {
+  const double gam = z.gam, rgp = z.cv * (gam - 1.);
+  const double gam1 = gam / z.prandt, gam2 = gam * rgp;
+  const int visc = z.iflow >= 2;
+  const int64_t nb = cfl_partial_blocks(z);
+  double surf_c = 0.;
+  if (z.typ == Z3DCART) {
+    const double ddi = 2. * sqrt(z.tcx * z.tcx), ddj = 2. * sqrt(z.tcy * z.tcy),
+                 ddk = 2. * sqrt(z.tcz * z.tcz);
+    auto mx = [](double x, double y) { return x > y ? x : y; };   // Fortran max
+    surf_c = 1. / mx(mx(ddi, ddj), ddk);
+    cfl_partial<Z3DCART><<<(unsigned)nb, 256, 0, st>>>(z, q, xmut, surf_c, z.dtc, gam1, gam2, visc, part);
+  } else if (z.typ == Z3DFULL) {
+    cfl_partial<Z3DFULL><<<(unsigned)nb, 256, 0, st>>>(z, q, xmut, 0., z.dtc, gam1, gam2, visc, part);
+  } else if (z.typ == Z2D) {
+    cfl_partial<Z2D><<<(unsigned)nb, 256, 0, st>>>(z, q, xmut, 0., z.dtc, gam1, gam2, visc, part);
+  } else {
+    return cudaErrorNotSupported;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  cfl_finish<<<1, 32, 0, st>>>(part, nb, (double)(z.ni * z.nj * z.nk), out);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ norms
 // One CTA per LU block (cprdu3s1_incl.for:14-135 block decomposition).
 __global__ void __launch_bounds__(256) block_norms(Zone z, NormArgs a) {

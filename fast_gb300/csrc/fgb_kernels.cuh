@@ -128,6 +128,11 @@ cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st);
 cudaError_t launch_coins(double* q, int64_t nd, const int32_t* dst, const int32_t* a,
                          const int32_t* b, const int32_t* c, int64_t n_edge, int64_t n, int neq,
                          cudaStream_t st);
+// cpcfl3.for: (max, min, mean) CFL of a zone into out[3]; part holds
+// 3 * cfl_partial_blocks(z) doubles
+int64_t cfl_partial_blocks(const Zone& z);
+cudaError_t launch_cfl(const Zone& z, const double* q, const double* xmut, double* part,
+                       double* out, cudaStream_t st);
 cudaError_t launch_norms(const Zone& z, const NormArgs& a, cudaStream_t st);
 cudaError_t norm_partials_address(double** p);   // the fixed partials array of this device
 cudaError_t launch_norms_finish(const double* part, int64_t nblocks, int neq, double xpt_1,

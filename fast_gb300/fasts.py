@@ -248,6 +248,15 @@ def display_temporal_criteria(t, metrics, nitrun, format=None, gmres=None, verbo
         res = s.residuals(n)
         if res.shape[1] == 0:
             continue
+        # CFL_minmaxmoy of the zone's numerics (computePT.cpp:629-644),
+        # printed as display_ss_iteration.cpp:100-105 does
+        node = I.getNodeFromName2(z, "CFL_minmaxmoy")
+        if node is not None:
+            cfl = s.cfl(n)
+            node[1] = np.array(cfl, dtype=np.float64)
+            if (format is None or format == "double") and verbose != "none":
+                print("CFL_MOY_MAX_MIN(Zone= %32.32s, nitrun=%d) %f    %f    %f " % (
+                    z[0], nitrun, cfl[2], cfl[0], cfl[1]))
         neq = res.shape[0] // 2
         L2, Loo = res[:neq], res[neq:]
         resL2 += float(L2.sum())

@@ -114,6 +114,14 @@ int fgb_apply_bc(fgb_solver* s, int level);
  * recorded); returns nit through *nit_out. */
 int fgb_residuals(fgb_solver* s, int zone, double* out, int64_t n, int* nit_out);
 
+/* CFL statistics of the last verified iteration (the first sub-step of an
+ * iteration with nitrun % modulo_verif == 0), as cptst3.for -> cpcfl3.for
+ * computes them and FastS/FastS/Compute/computePT.cpp:629-644 reduces them
+ * into the zone's CFL_minmaxmoy node: out[0] = max, out[1] = min, out[2] =
+ * mean over the interior cells of dt / min(viscous, convective) time step
+ * (the convective one for Euler).  Waits for the solver stream. */
+int fgb_cfl(fgb_solver* s, int zone, double* out);
+
 /* Exterior state (conservative ro, ro u, ro v, ro w, ro E) of every farfield
  * / inflow / outflow BC of a zone, replacing the free stream (BCzone.cpp
  * DEFAULT_STATE, or the nbdata = 21 per-BC state). */

@@ -2138,6 +2138,74 @@ void or_transfers(or_zone* zones, const or_transfer* tr, int ntr, int use_p1) {
   }
 }
 
+/* cpcfl3.for (non-ALE branches, called by cptst3.for on the first
+ * sub-step of a verified iteration): per interior cell the CFL number
+ * dt / min(vis, conv) (Navier-Stokes) or dt / conv (Euler), with the face
+ * areas of the cell's faces; cfl = (max, min, sum) in the i-fastest loop
+ * order (the driver divides the sum by the cell count, computePT.cpp:643). */
+void or_cpcfl3(const int64_t* pi, const double* pr, const double* rop, const double* xmut,
+               const double* ti, const double* tj, const double* tk, const double* vol,
+               double cfl[3]) {
+  const int64_t nd = pi[NDIMDX], ndm = pi[NDIMDX_MTR];
+  const double rgp = pr[CVINF] * (pr[GAMMA] - 1.);
+  const double gam1 = pr[GAMMA] / pr[PRANDT], gam2 = pr[GAMMA] * rgp;
+  const double dt = pr[DTC];
+  const int typ = (int)pi[ITYPZONE], visc = pi[IFLOW] >= 2;
+  const int64_t inc[3] = {pi[NIJK_MTR], pi[NIJK_MTR + 1], pi[NIJK_MTR + 2]};
+  cfl[0] = 0.; cfl[1] = 100000000.; cfl[2] = 0.;
+  double surf_c = 0.;
+  if (typ == 2) {
+    const double ddi = 2. * sqrt(ti[0] * ti[0]), ddj = 2. * sqrt(tj[0] * tj[0]),
+                 ddk = 2. * sqrt(tk[0] * tk[0]);
+    surf_c = 1. / OMAX(OMAX(ddi, ddj), ddk);
+  }
+  for (int64_t k = 1; k <= pi[IJKV + 2]; k++)
+    for (int64_t j = 1; j <= pi[IJKV + 1]; j++)
+      for (int64_t i = 1; i <= pi[IJKV]; i++) {
+        const int64_t l = inddm(pi, i, j, k);
+        const int64_t lvo = typ == 2 ? 0 : indmtr(pi, i, j, k);
+        double surf = surf_c;
+        if (typ == 0) {
+          const double* T[3] = {ti, tj, tk};
+          double dd[3];
+          for (int d = 0; d < 3; d++) {
+            const double* t = T[d];
+            const int64_t a = lvo + inc[d], b = lvo;
+            dd[d] = sqrt(t[a] * t[a] + t[a + ndm] * t[a + ndm] + t[a + 2 * ndm] * t[a + 2 * ndm]);
+            dd[d] = dd[d] + sqrt(t[b] * t[b] + t[b + ndm] * t[b + ndm] + t[b + 2 * ndm] * t[b + 2 * ndm]);
+          }
+          surf = 1. / OMAX(OMAX(dd[0], dd[1]), dd[2]);
+        } else if (typ == 3) {
+          const double* T[2] = {ti, tj};
+          double dd[2];
+          for (int d = 0; d < 2; d++) {
+            const double* t = T[d];
+            const int64_t a = lvo + inc[d], b = lvo;
+            dd[d] = sqrt(t[a] * t[a] + t[a + ndm] * t[a + ndm]);
+            dd[d] = dd[d] + sqrt(t[b] * t[b] + t[b + ndm] * t[b + ndm]);
+          }
+          surf = 1. / OMAX(dd[0], dd[1]);
+        }
+        const double u = rop[l + nd], v = rop[l + 2 * nd], w = rop[l + 3 * nd], r = rop[l];
+        const double c = sqrt(gam2 * rop[l + 4 * nd]);
+        const double ur2 = typ == 3 ? u * u + v * v : u * u + v * v + w * w;
+        const double sp = sqrt(ur2);
+        const double xinvspc = 1. / (sp + c);
+        const double conv = 2. * vol[lvo] * surf * xinvspc;
+        double cfloc;
+        if (visc) {
+          const double xinvkt = gam1 / xmut[l];
+          const double vis = 2. * r * vol[lvo] * vol[lvo] * surf * surf * xinvkt;
+          cfloc = dt / OMIN(vis, conv);
+        } else {
+          cfloc = dt / conv;
+        }
+        cfl[0] = OMAX(cfl[0], cfloc);
+        cfl[1] = OMIN(cfl[1], cfloc);
+        cfl[2] = cfl[2] + cfloc;
+      }
+}
+
 /* cpcfl3.for (non-ALE branches): the largest stable dt for the given CFL,
  * i.e. cfl * min over interior cells of comp = min(vis, conv). */
 double or_cfl_dt(const int64_t* pi, const double* pr, const double* rop,
@@ -2233,6 +2301,11 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
             or_tstb3c(pi, pr, *first_it, coe_r, ssiter, Z->coe, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
           } else {
             or_tstb3_global(pi, pr, sdm, Z->coe, Z->vol);
+          }
+          /* cptst3.for:115-120: CFL statistics of a verified iteration */
+          if (lssiter_verif && Z->cfl) {
+            or_cpcfl3(pi, pr, ssiter, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol, Z->cfl);
+            Z->cfl[2] = Z->cfl[2] / (double)(pi[IJKV] * pi[IJKV + 1] * pi[IJKV + 2]);
           }
         }
         or_init_rhs(pi, nstep, sdm, Z->drodm);

@@ -42,6 +42,7 @@ typedef struct {
   const double* ti; const double* tj; const double* tk; const double* vol;
   double* rdm;    /* Newton residual per LU block: nssiter*neq*2*ndim_rdm  */
   double* wig;    /* senseur wiggle flags, 3*NDIMDX (KFLUDOM = 2)           */
+  double* cfl;    /* CFL max, min, mean of the last verified step (3)      */
 } or_zone;
 
 /* 1-to-1 (type 0) interface copy: rcv_zone ghost cells <- dnr_zone cells. */

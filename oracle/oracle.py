@@ -41,7 +41,8 @@ class OrZone(C.Structure):
                 ("drodm", C.POINTER(C.c_double)), ("coe", C.POINTER(C.c_double)),
                 ("ti", C.POINTER(C.c_double)), ("tj", C.POINTER(C.c_double)),
                 ("tk", C.POINTER(C.c_double)), ("vol", C.POINTER(C.c_double)),
-                ("rdm", C.POINTER(C.c_double)), ("wig", C.POINTER(C.c_double))]
+                ("rdm", C.POINTER(C.c_double)), ("wig", C.POINTER(C.c_double)),
+                ("cfl", C.POINTER(C.c_double))]
 
 
 class OrTransfer(C.Structure):
@@ -94,7 +95,7 @@ class Case:
                      vol=np.ascontiguousarray(zd["vol"], dtype=np.float64),
                      lv=[np.array(zd[k], dtype=np.float64).reshape(-1) for k in ("ro", "ro_m1", "ro_p1")],
                      xmut=np.zeros(2 * nd), drodm=np.zeros(neq * nd), coe=np.zeros(neq * nd),
-                     rdm=np.zeros(nss * neq * 2 * nlu), wig=np.zeros(3 * nd))
+                     rdm=np.zeros(nss * neq * 2 * nlu), wig=np.zeros(3 * nd), cfl=np.zeros(3))
             if neq == 6:
                 # Spalart-Allmaras: the wall distance follows the viscosity
                 # (navier_stokes_struct passes xmut(1+NDIMDX) as dist)
@@ -113,7 +114,7 @@ class Case:
             s.ro, s.ro_m1, s.ro_p1 = (_d(a) for a in e["lv"])
             s.xmut = _d(e["xmut"]); s.drodm = _d(e["drodm"]); s.coe = _d(e["coe"])
             s.ti = _d(e["ti"]); s.tj = _d(e["tj"]); s.tk = _d(e["tk"]); s.vol = _d(e["vol"])
-            s.rdm = _d(e["rdm"]); s.wig = _d(e["wig"])
+            s.rdm = _d(e["rdm"]); s.wig = _d(e["wig"]); s.cfl = _d(e["cfl"])
         tr = (OrTransfer * max(1, len(self.tr)))()
         for s, t in zip(tr, self.tr):
             s.dnr_zone, s.rcv_zone, s.n = t["dnr"], t["rcv"], t["dnr_idx"].size
@@ -147,6 +148,10 @@ class Case:
         for s, e in zip(arr, self.z):
             by_addr = {a.ctypes.data: a for a in e["lv"]}
             e["lv"] = [by_addr[C.cast(p, C.c_void_p).value] for p in (s.ro, s.ro_m1, s.ro_p1)]
+
+    def cfl(self, zone: int):
+        """(max, min, mean) CFL of the last verified iteration (cpcfl3.for)."""
+        return self.z[zone]["cfl"].copy()
 
     def residual_norms(self, zone: int, nit: int):
         e = self.z[zone]

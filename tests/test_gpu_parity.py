@@ -584,3 +584,33 @@ def test_roe_vanalbada_explicit(oracle_mod, wavy, two_d):
         s.compute(it, 1, 3, 1, 1)
     _check_levels(ref, s)
     s.close()
+
+
+@pytest.mark.parametrize("case", ["tgv_implicit", "wavy_sa", "vortex_2d", "box_2d_laminar"])
+def test_cfl_statistics(oracle_mod, case):
+    """cpcfl3.for on the GPU (fgb_cfl) against the oracle: max and min bit
+    for bit, the mean (a reduction in another order) to 1e-12."""
+    if case == "tgv_implicit":
+        t = cases.taylor_green(n=(12, 10, 8), ss_iteration=2)
+        nfin, mv = 3, 1
+    elif case == "wavy_sa":
+        t = cases.bc_box(n=(12, 10, 6), model="NSTurbulent", wavy=0.3, temporal="explicit",
+                         reynolds=500.0, time_step=0.02)
+        nfin, mv = 3, 1
+    elif case == "vortex_2d":
+        t = cases.isentropic_vortex(n=(24, 20, 1), two_d=True, wavy=0.3,
+                                    numz={"scheme": "roe", "slope": "o3", "time_step": 0.05})
+        nfin, mv = 3, 1
+    else:
+        t = cases.bc_box(n=(16, 12, 1), two_d=True, model="NSLaminar", wavy=0.3,
+                         temporal="explicit", reynolds=100.0, time_step=0.01)
+        nfin, mv = 3, 1
+    zd, ref, s = _pair(t, oracle_mod, mv)
+    for it in range(1, 3):
+        ref.compute(it, 1, nfin, 1, modulo_verif=mv)
+        s.compute(it, 1, nfin, 1, 1)
+    got, exp = s.cfl(0), ref.cfl(0)
+    assert got[0] == exp[0] and got[1] == exp[1], (got, exp)
+    assert abs(got[2] - exp[2]) <= 1e-12 * exp[2]
+    assert 0 < exp[1] <= exp[2] <= exp[0]
+    s.close()

@@ -170,3 +170,38 @@ def test_roe_slip_wall_keeps_parallel_free_stream(oracle_mod):
     for it in range(1, 4):
         c.compute(it, 1, 3, 1, modulo_verif=1000)
     assert np.max(np.abs(c.z[0]["lv"][0] - q0)) < 1e-14
+
+
+@pytest.mark.parametrize("model", ["Euler", "NSLaminar"])
+def test_cfl_statistics_uniform_flow(oracle_mod, model):
+    """cpcfl3.for on a uniform flow in a cartesian box: every cell has the
+    same CFL dt (|u| + c) / (2 vol surf) (Euler) or dt / min(vis, conv), so
+    max = min = mean = the closed form."""
+    import math
+    from fast_gb300 import cases, fasts
+    t = cases.bc_box(n=(12, 10, 6), model=model, wall="BCWallInviscid" if model == "Euler" else "BCWallViscous",
+                     perturb=0.0, temporal="explicit", reynolds=50.0, time_step=0.01)
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    c = oracle_mod.Case(zd)
+    c.apply_bc(0)
+    c.apply_bc(1)
+    c.compute(1, 1, 3, 1, modulo_verif=1)
+    cmax, cmin, cmean = c.cfl(0)
+    pr = zd[0]["pr"]
+    gam, cv, dt = pr[1], pr[2], pr[0]
+    hx, hy, hz = 1 / 12, 1 / 10, 1 / 12
+    vol = hx * hy * hz
+    surf = 1.0 / (2 * max(hy * hz, hx * hz, hx * hy))
+    q = zd[0]["ro"].reshape(5, -1)[:, 0]
+    snd = math.sqrt(gam * cv * (gam - 1) * q[4])
+    conv = 2 * vol * surf / (math.sqrt(q[1] ** 2 + q[2] ** 2 + q[3] ** 2) + snd)
+    comp = conv
+    if model != "Euler":
+        nip, njp = 12 + 4, 10 + 4
+        mu = c.z[0]["xmut"][2 + 2 * nip + 2 * nip * njp]     # first interior cell
+        assert mu > 0
+        vis = 2 * q[0] * vol * vol * surf * surf * (gam / pr[10]) / mu
+        comp = min(vis, conv)
+    exp = dt / comp
+    assert abs(cmax - exp) <= 1e-13 * exp and abs(cmin - exp) <= 1e-13 * exp
+    assert abs(cmean - exp) <= 1e-12 * exp
