@@ -134,6 +134,14 @@ struct fgb_solver {
     double* lam0 = nullptr;        // lamW as allocated (the parity of rev)
   } adj;
   bool graph = true;               // replay the adjoint driver loops as CUDA graphs
+  // several zones: their per-zone kernels run on ZS side streams (zone m on
+  // stream m mod ZS), forked from and joined back into the solver stream
+  // around each per-zone phase, so that the small launches overlap
+  static constexpr int ZS = 8;
+  bool zone_streams = true;
+  cudaStream_t zst[ZS] = {};
+  cudaEvent_t zev[ZS] = {};
+  cudaEvent_t fork_ev = nullptr;
   int first_it = 0;
   int modulo_verif = 200;
   int lu_precision = 64;
@@ -188,6 +196,36 @@ static int capture_graph(fgb_solver* s, cudaGraphExec_t* out, F&& body) {
   const cudaError_t ei = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
   CK(ei);
+  return FGB_OK;
+}
+
+// Per-zone launches issued on another stream: every launch helper reads
+// s->st, so the zone's stream stands in for it until the guard ends.
+struct StreamSwap {
+  fgb_solver* s; cudaStream_t saved;
+  StreamSwap(fgb_solver* s_, cudaStream_t st) : s(s_), saved(s_->st) { s->st = st; }
+  ~StreamSwap() { s->st = saved; }
+};
+
+// fork: the side streams wait for the work issued so far on the solver
+// stream; join: the solver stream waits for every side stream
+static int zone_fork(fgb_solver* s) {
+  if (!s->fork_ev) {
+    CK(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
+    for (int k = 0; k < fgb_solver::ZS; k++) {
+      CK(cudaStreamCreateWithFlags(&s->zst[k], cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&s->zev[k], cudaEventDisableTiming));
+    }
+  }
+  CK(cudaEventRecord(s->fork_ev, s->st));
+  for (int k = 0; k < fgb_solver::ZS; k++) CK(cudaStreamWaitEvent(s->zst[k], s->fork_ev, 0));
+  return FGB_OK;
+}
+static int zone_join(fgb_solver* s) {
+  for (int k = 0; k < fgb_solver::ZS; k++) {
+    CK(cudaEventRecord(s->zev[k], s->zst[k]));
+    CK(cudaStreamWaitEvent(s->st, s->zev[k], 0));
+  }
   return FGB_OK;
 }
 
@@ -555,6 +593,11 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
   for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
+  for (int k = 0; k < fgb_solver::ZS; k++) {
+    if (s->zst[k]) { cudaStreamSynchronize(s->zst[k]); cudaStreamDestroy(s->zst[k]); }
+    if (s->zev[k]) cudaEventDestroy(s->zev[k]);
+  }
+  if (s->fork_ev) cudaEventDestroy(s->fork_ev);
   for (LuGroupData& g : s->lu_groups) {
     cudaFree(g.cells); cudaFree(g.zid); cudaFree(g.plane); cudaFree(g.nbl); cudaFree(g.nbu);
     cudaFree(g.work); cudaFree(g.tab_dev); cudaFreeHost(g.tab_host);
@@ -722,6 +765,8 @@ int fgb_set_option(fgb_solver* s, const char* key, double value) {
     s->profile = value != 0.;
   } else if (k == "graph") {
     s->graph = value != 0.;
+  } else if (k == "zone_streams") {
+    s->zone_streams = value != 0.;
   } else {
     return fail(FGB_ERR_ARG, "unknown option " + k);
   }
@@ -737,6 +782,7 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value) {
   else if (k == "first_it") *value = s->first_it;
   else if (k == "profile") *value = s->profile;
   else if (k == "graph") *value = s->graph;
+  else if (k == "zone_streams") *value = s->zone_streams;
   else return fail(FGB_ERR_ARG, "unknown option " + k);
   return FGB_OK;
 }
@@ -793,15 +839,49 @@ int fgb_download_work(fgb_solver* s, int zone, const char* which, double* host, 
 }
 
 // ghost fill of one level of every zone: transfers, face BCs, edges/corners
+// The ghost fill of one level.  Transfers read donor interior cells and
+// write receiver ghost cells; a zone's BC lists read its interior and write
+// its own ghost layers; its corner averages read those.  So the fill of
+// zone m = [transfers into m, its BC lists, its corners] depends on no other
+// zone's fill: with several zones each runs on its side stream.
+static int ghost_fill_zone(fgb_solver* s, int m, int level);
 static int ghost_fill(fgb_solver* s, int level) {
-  for (Transfer& T : s->tr) {
-    ZoneData& D = s->zones[T.dnr];
-    ZoneData& R = s->zones[T.rcv];
-    CK(launch_gather(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, T.rcv_idx, T.dnr_idx, T.n,
-                     R.z.neq, 0, 1., s->st));
-    s->launches++;
+  const bool par = s->zone_streams && !s->profile && s->zones.size() > 1;
+  if (!par) {
+    for (Transfer& T : s->tr) {
+      ZoneData& D = s->zones[T.dnr];
+      ZoneData& R = s->zones[T.rcv];
+      CK(launch_gather(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, T.rcv_idx, T.dnr_idx, T.n,
+                       R.z.neq, 0, 1., s->st));
+      s->launches++;
+    }
+    for (int m = 0; m < (int)s->zones.size(); m++) {
+      int rc = ghost_fill_zone(s, m, level);
+      if (rc) return rc;
+    }
+    return FGB_OK;
   }
-  for (ZoneData& Z : s->zones) {
+  int rc = zone_fork(s);
+  if (rc) return rc;
+  for (int m = 0; m < (int)s->zones.size(); m++) {
+    StreamSwap sw(s, s->zst[m % fgb_solver::ZS]);
+    ZoneData& R = s->zones[(size_t)m];
+    for (Transfer& T : s->tr) {
+      if (T.rcv != m) continue;
+      ZoneData& D = s->zones[T.dnr];
+      CK(launch_gather(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, T.rcv_idx, T.dnr_idx, T.n,
+                       R.z.neq, 0, 1., s->st));
+      s->launches++;
+    }
+    if ((rc = ghost_fill_zone(s, m, level))) return rc;
+  }
+  return zone_join(s);
+}
+
+// BC lists and corner averages of zone m
+static int ghost_fill_zone(fgb_solver* s, int m, int level) {
+  {
+    ZoneData& Z = s->zones[(size_t)m];
     for (GatherList& g : Z.bcs) {
       if (g.kind == 0) {
         CK(launch_gather(Z.lvl[level], Z.z.nd, Z.lvl[level], Z.z.nd, g.dst, g.src, g.n, Z.z.neq,
@@ -1146,7 +1226,14 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       }
       if (!verif && nstep == nssiter && p0[ITYPCP] == 1) continue;  // computePT.cpp:581
       if (verif) s->nit_recorded = nstep;
+      const bool par = s->zone_streams && !s->profile && s->zones.size() > 1;
+      if (par) {
+        int rc = zone_fork(s);
+        if (rc) return rc;
+      }
       for (ZoneData& Z : s->zones) {
+        const int zm = (int)(&Z - s->zones.data());
+        StreamSwap sw(s, par ? s->zst[zm % fgb_solver::ZS] : s->st);
         Zone& z = Z.z;
         double* ssiter;
         double* out;
@@ -1237,6 +1324,10 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
                                             inplace ? 1 : 0};
           }
         }
+      }
+      if (par) {
+        int rc = zone_join(s);
+        if (rc) return rc;
       }
       if (implicit && !lexit_lu) {
         for (LuGroupData& g : s->lu_groups) {

@@ -74,7 +74,10 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * HOOK["FIRST_IT"] flag (0 = BDF1 step); "profile": 1 to time every kernel
  * group with CUDA events (see fgb_kernel_stats); "graph": 1 (default) to
  * replay the loops of fgb_adjoint_forward / _backward as CUDA graphs, 0 for
- * stream launches (profiling always uses stream launches). */
+ * stream launches (profiling always uses stream launches); "zone_streams":
+ * 1 (default) to run the per-zone kernels of several zones on 8 side streams
+ * (zone m on stream m mod 8, joined before each LU-SGS solve and after each
+ * ghost fill), 0 for the solver stream alone (profiling uses it alone). */
 int fgb_set_option(fgb_solver* s, const char* key, double value);
 int fgb_get_option(fgb_solver* s, const char* key, double* value);
 
