@@ -134,6 +134,15 @@ __device__ __forceinline__ void vanalbada_grad(double x, double y, double& gx, d
   gy = (xx + e2 + xy2 - 2. * y * va) * iD;
 }
 
+// the same gradient given va and iD = 1 / Dn (from the face tape)
+__device__ __forceinline__ void vanalbada_grad_v(double x, double y, double va, double iD, double& gx,
+                                                 double& gy) {
+  const double e2 = 1e-12;
+  const double xx = x * x, yy = y * y, xy2 = 2. * x * y;
+  gx = (yy + e2 + xy2 - 2. * x * va) * iD;
+  gy = (xx + e2 + xy2 - 2. * y * va) * iD;
+}
+
 // roe_full (fgb_flux.cu) for a 2-d face: tcz = 0, w = 0 (those terms vanish
 // exactly in the primal), s = |(tcx, tcy)|; F[3] = 0
 template <typename T>
@@ -199,33 +208,38 @@ __device__ __forceinline__ void roe2d(const Zone& z, const T qm[5], const T qp[5
 // derivative of the branch the value selects (the dual numbers' rule).
 __device__ __forceinline__ double sgn1(double x) { return x < 0. ? -1. : 1.; }
 
+// TAPED: the square roots and quotients of the forward pass come from the
+// face tape of the recomputation (roe_full<true>: tp[k * ts], k = 0..8)
+template <bool TAPED>
 __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5], double tcx,
-                          double tcy, const double Fb[5], double qmb[5], double qpb[5], double tb[2]) {
+                          double tcy, const double Fb[5], double qmb[5], double qpb[5], double tb[2],
+                          const double* tp = nullptr, int64_t ts = 0) {
   const double rgp = z.rgp, gam1 = z.gam1, g_ = z.gam - 1., psi = z.psiroe;
   // ---- forward
-  const double ss = tcx * tcx + tcy * tcy, s = ::sqrt(ss);
+  const double ss = tcx * tcx + tcy * tcy, s = TAPED ? tp[0] : ::sqrt(ss);
   const double r1 = qp[0], p1 = r1 * qp[4] * rgp;
   const double h1 = gam1 * qp[4] * rgp + .5 * (qp[1] * qp[1] + qp[2] * qp[2]);
   const double r2 = qm[0], p2 = r2 * qm[4] * rgp;
   const double h2 = gam1 * qm[4] * rgp + .5 * (qm[1] * qm[1] + qm[2] * qm[2]);
-  const double s1 = ::sqrt(r1), s2 = ::sqrt(r2);
-  const double r = s1 * s2, r_1 = 1. / (s1 + s2), i_r = 1. / r;
+  const double s1 = TAPED ? tp[ts] : ::sqrt(r1), s2 = TAPED ? tp[2 * ts] : ::sqrt(r2);
+  const double r = s1 * s2, r_1 = TAPED ? tp[3 * ts] : 1. / (s1 + s2);
+  const double i_r = TAPED ? tp[8 * ts] : 1. / r;
   const double t7u = s1 * qp[1] + s2 * qm[1], t7v = s1 * qp[2] + s2 * qm[2];
   const double u = t7u * r_1, v = t7v * r_1;
   const double t8 = s1 * h1 + s2 * h2, h = t8 * r_1;
   const double q = .5 * (u * u + v * v);
-  const double hq = h - q, c = ::sqrt(g_ * ::fabs(hq));
+  const double hq = h - q, c = TAPED ? tp[4 * ts] : ::sqrt(g_ * ::fabs(hq));
   const double qn1 = qp[1] * tcx + qp[2] * tcy, qn2 = qm[1] * tcx + qm[2] * tcy;
   const double du = (qm[1] - qp[1]) * s, dv = (qm[2] - qp[2]) * s;
   const double dp = p2 - p1, dqn = qn2 - qn1;
   const bool smax_on = s > 1.E-30;
-  const double s_1 = 1.0 / (smax_on ? s : 1.E-30);
+  const double s_1 = TAPED ? tp[5 * ts] : 1.0 / (smax_on ? s : 1.E-30);
   const double nx = tcx * s_1, ny = tcy * s_1;
   const double qn = u * nx + v * ny;
-  const double A1 = ::fabs(qn), f4 = psi * (A1 + c), i_f4 = 1. / f4;
+  const double A1 = ::fabs(qn), f4 = psi * (A1 + c), i_f4 = TAPED ? tp[6 * ts] : 1. / f4;
   const double f2a = 0.5 + copysign(0.5, A1 - f4);
   const double f3a = (f2a - 1.0) * (qn * qn * i_f4 + f4) * 0.5 - f2a * A1;
-  const double c2 = c * c, i_c2 = 1. / c2;
+  const double c2 = c * c, i_c2 = TAPED ? tp[7 * ts] : 1. / c2;
   const double Z = r2 - r1 - dp * i_c2, f1a = Z * s;
   const double X2 = f1a * u + r * (du - nx * dqn), X3 = f1a * v + r * (dv - ny * dqn);
   const double Y5 = u * du + v * dv - qn * dqn, X5 = f1a * q + r * Y5;
@@ -349,10 +363,13 @@ __device__ void roe2d_rev(const Zone& z, const double qm[5], const double qp[5],
 // The reconstructed states first (values only), the reverse Roe pass, then
 // per variable the reconstruction derivatives (vanalbada_grad, recomputed:
 // they are not live across the Roe pass) and the scatter.
-template <int D>
+// TAPED: the slopes and their reciprocal denominators, and the Roe values,
+// from the face tape (face-major, stride ts) instead of recomputed
+template <int D, bool TAPED = false>
 __device__ __forceinline__ void face_adjoint(const Zone& z, const double* __restrict__ q,
                                              int64_t l, int64_t lt, const double mu[5],
-                                             double* __restrict__ lamQ, double* __restrict__ lamT) {
+                                             double* __restrict__ lamQ, double* __restrict__ lamT,
+                                             const double* __restrict__ tp = nullptr, int64_t ts = 0) {
   const int64_t inc = z.inc[D], nd = z.nd;
   double qm[5], qp[5];
 #pragma unroll
@@ -360,12 +377,13 @@ __device__ __forceinline__ void face_adjoint(const Zone& z, const double* __rest
     if (v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
     const double* Q = q + v * nd;
     const double a = Q[l - 2 * inc], b = Q[l - inc], c = Q[l], d = Q[l + inc];
-    qm[v] = c - 0.5 * vanalbada_t(c - b, d - c);
-    qp[v] = b + 0.5 * vanalbada_t(b - a, c - b);
+    const int m = v == 4 ? 3 : v;
+    qm[v] = c - 0.5 * (TAPED ? tp[(TAPE_VA + 2 * m) * ts] : vanalbada_t(c - b, d - c));
+    qp[v] = b + 0.5 * (TAPED ? tp[(TAPE_VA + 2 * m + 1) * ts] : vanalbada_t(b - a, c - b));
   }
   const double* M = D == 0 ? z.ti : z.tj;
   double qmb[5] = {0, 0, 0, 0, 0}, qpb[5] = {0, 0, 0, 0, 0}, tb[2] = {0, 0};
-  roe2d_rev(z, qm, qp, M[lt], M[lt + z.ndm], mu, qmb, qpb, tb);
+  roe2d_rev<TAPED>(z, qm, qp, M[lt], M[lt + z.ndm], mu, qmb, qpb, tb, tp, ts);
 #pragma unroll
   for (int m = 0; m < 4; m++) {
     const int v = m == 3 ? 4 : m;
@@ -373,8 +391,13 @@ __device__ __forceinline__ void face_adjoint(const Zone& z, const double* __rest
     const double a = Q[l - 2 * inc], b = Q[l - inc], c = Q[l], d = Q[l + inc];
     // qm = c - va(c - b, d - c) / 2, qp = b + va(b - a, c - b) / 2
     double mx, my, px, py;
-    vanalbada_grad(c - b, d - c, mx, my);
-    vanalbada_grad(b - a, c - b, px, py);
+    if (TAPED) {
+      vanalbada_grad_v(c - b, d - c, tp[(TAPE_VA + 2 * m) * ts], tp[(TAPE_ID + 2 * m) * ts], mx, my);
+      vanalbada_grad_v(b - a, c - b, tp[(TAPE_VA + 2 * m + 1) * ts], tp[(TAPE_ID + 2 * m + 1) * ts], px, py);
+    } else {
+      vanalbada_grad(c - b, d - c, mx, my);
+      vanalbada_grad(b - a, c - b, px, py);
+    }
     const int64_t o = v * nd;
     const double gm = qmb[v], gp = qpb[v];
     atomicAdd(lamQ + l - 2 * inc + o, -0.5 * px * gp);
@@ -440,8 +463,9 @@ __device__ __forceinline__ void face_lin(const Zone& z, const double* __restrict
 // adjoint: mu = lamD(l) [l interior] - lamD(l - inc) [l - inc interior]
 // (register-bounded to 3 blocks of 128 per SM: faster than the unbounded
 // 255-register build, measured on GB300)
-template <int D>
+template <int D, bool TAPED>
 __global__ void __launch_bounds__(128, 3) adj_faces(Zone z, const double* __restrict__ q,
+                                                 const double* __restrict__ tape,
                                                  const double* __restrict__ lamD,
                                                  double* __restrict__ lamQ,
                                                  double* __restrict__ lamT) {
@@ -457,7 +481,7 @@ __global__ void __launch_bounds__(128, 3) adj_faces(Zone z, const double* __rest
 #pragma unroll
   for (int v = 0; v < 5; v++)
     mu[v] = (hi_in ? lamD[l + v * nd] : 0.) - (lo_in ? lamD[l - inc + v * nd] : 0.);
-  face_adjoint<D>(z, q, l, lt, mu, lamQ, lamT);
+  face_adjoint<D, TAPED>(z, q, l, lt, mu, lamQ, lamT, TAPED ? tape + f : nullptr, NI * NJ);
 }
 
 // tangent: dF = J (dq, dt) into the face array (SoA, 5 x faces)
@@ -494,13 +518,20 @@ __global__ void __launch_bounds__(128) tan_faces(Zone z, const double* __restric
   }
 }
 
-cudaError_t launch_adj_faces(const Zone& z, const double* q, const double* lamD, double* lamQ,
+cudaError_t launch_adj_faces(const Zone& z, const double* q, const double* tape,
+                             const double* lamD, double* lamQ,
                              double* lamTi, double* lamTj, cudaStream_t st) {
   if (z.typ != Z2D) return cudaErrorNotSupported;
   const int B = 128;
   const int64_t nfi = (z.ni + 1) * z.nj, nfj = z.ni * (z.nj + 1);
-  adj_faces<0><<<(unsigned)((nfi + B - 1) / B), B, 0, st>>>(z, q, lamD, lamQ, lamTi);
-  adj_faces<1><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, lamD, lamQ, lamTj);
+  const unsigned gi = (unsigned)((nfi + B - 1) / B), gj = (unsigned)((nfj + B - 1) / B);
+  if (tape) {
+    adj_faces<0, true><<<gi, B, 0, st>>>(z, q, tape, lamD, lamQ, lamTi);
+    adj_faces<1, true><<<gj, B, 0, st>>>(z, q, tape + FACE_TAPE * nfi, lamD, lamQ, lamTj);
+  } else {
+    adj_faces<0, false><<<gi, B, 0, st>>>(z, q, nullptr, lamD, lamQ, lamTi);
+    adj_faces<1, false><<<gj, B, 0, st>>>(z, q, nullptr, lamD, lamQ, lamTj);
+  }
   return cudaGetLastError();
 }
 
@@ -976,6 +1007,108 @@ __global__ void __launch_bounds__(128) tan_bc_face(const double* __restrict__ q,
 #pragma unroll
   for (int m = 0; m < 4; m++) dq[l + V4[m] * nd] = out[m];
   dq[l + 3 * nd] = 0.;
+}
+
+// all face-BC windows of a zone in one launch (adj_bc_face / tan_bc_face
+// per entry, the window's parameters from c.lp, the metric adjoint or
+// tangent of the window's direction)
+__global__ void __launch_bounds__(128) adj_bc_face_cat(const double* __restrict__ q,
+                                                       double* __restrict__ lam, BcFaceCat c,
+                                                       int64_t ndm, double* __restrict__ lamTi,
+                                                       double* __restrict__ lamTj,
+                                                       double* __restrict__ lamSt) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t e = gid >> 3;
+  const int k = (int)(gid & 7);
+  const bool act = e < c.n;
+  int64_t l = 0, s = 0;
+  const BcFaceArgs* a = nullptr;
+  double lo[4] = {0., 0., 0., 0.};
+  if (act) {
+    a = c.lp + c.lid[e];
+    l = c.dst[e];
+    s = c.src[e];
+#pragma unroll
+    for (int m = 0; m < 4; m++) lo[m] = lam[l + V4[m] * a->nd];
+  }
+  __syncwarp();
+  if (act && k == 0) {
+#pragma unroll
+    for (int v = 0; v < 5; v++) lam[l + v * a->nd] = 0.;
+  }
+  if (!act) return;
+  const int64_t nd = a->nd;
+  double J[4][1];
+  if (a->op == BCF_SLIP) {
+    if (k >= 6) return;
+    slip_eval<1>(q, nd, s, c.nrm[3 * e], c.nrm[3 * e + 1], k, J);
+  } else {
+    const double t[3] = {c.nrm[3 * e], c.nrm[3 * e + 1], c.nrm[3 * e + 2]};
+    farfield_eval<1>(*a, q, s, t, k, J);
+  }
+  double g = 0.;
+#pragma unroll
+  for (int m = 0; m < 4; m++) g += lo[m] * J[m][0];
+  if (k < 4) atomicAdd(lam + s + V4[k] * nd, g);
+  else if (a->op == BCF_SLIP) atomicAdd((a->dir == 0 ? lamTi : lamTj) + c.mt[e] + (k == 4 ? 0 : ndm), g);
+  else atomicAdd(lamSt + (k == 7 ? 4 : k - 4), g);
+}
+
+__global__ void __launch_bounds__(128) tan_bc_face_cat(const double* __restrict__ q,
+                                                       double* __restrict__ dq, BcFaceCat c,
+                                                       int64_t ndm, const double* __restrict__ dTi,
+                                                       const double* __restrict__ dTj,
+                                                       const double* __restrict__ dSt) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= c.n) return;
+  const BcFaceArgs& a = c.lp[c.lid[e]];
+  const int64_t nd = a.nd, l = c.dst[e], s = c.src[e];
+  const double* dT = a.dir == 0 ? dTi : dTj;
+  double out[4];
+  if (a.op == BCF_SLIP) {
+    double J[4][6];
+    slip_lin(q, nd, s, c.nrm[3 * e], c.nrm[3 * e + 1], J);
+    const double din[6] = {dq[s], dq[s + nd], dq[s + 2 * nd], dq[s + 4 * nd], dT[c.mt[e]],
+                           dT[c.mt[e] + ndm]};
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      double x = 0.;
+#pragma unroll
+      for (int k = 0; k < 6; k++) x += J[m][k] * din[k];
+      out[m] = x;
+    }
+  } else {
+    const double t[3] = {c.nrm[3 * e], c.nrm[3 * e + 1], c.nrm[3 * e + 2]};
+    double J[4][8];
+    farfield_lin(a, q, s, t, J);
+    const double din[8] = {dq[s], dq[s + nd], dq[s + 2 * nd], dq[s + 4 * nd],
+                           dSt[0], dSt[1], dSt[2], dSt[4]};
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      double x = 0.;
+#pragma unroll
+      for (int k = 0; k < 8; k++) x += J[m][k] * din[k];
+      out[m] = x;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 4; m++) dq[l + V4[m] * nd] = out[m];
+  dq[l + 3 * nd] = 0.;
+}
+
+cudaError_t launch_adj_bc_face_cat(const double* q, double* lam, const BcFaceCat& c, int64_t ndm,
+                                   double* lamTi, double* lamTj, double* lamSt, cudaStream_t st) {
+  if (c.n <= 0) return cudaSuccess;
+  adj_bc_face_cat<<<(unsigned)((8 * c.n + 127) / 128), 128, 0, st>>>(q, lam, c, ndm, lamTi, lamTj, lamSt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tan_bc_face_cat(const double* q, double* dq, const BcFaceCat& c, int64_t ndm,
+                                   const double* dTi, const double* dTj, const double* dSt,
+                                   cudaStream_t st) {
+  if (c.n <= 0) return cudaSuccess;
+  tan_bc_face_cat<<<(unsigned)((c.n + 127) / 128), 128, 0, st>>>(q, dq, c, ndm, dTi, dTj, dSt);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_adj_bc_face(const double* q, double* lam, const BcFaceArgs& a, const int32_t* mt,

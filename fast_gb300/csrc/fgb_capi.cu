@@ -73,6 +73,13 @@ struct ZoneData {
   double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
   double* wig = nullptr;            // senseur wiggle flags (KFLUDOM = 2)
   double* dist = nullptr;           // wall distance (Spalart-Allmaras)
+  // the zone's BC lists concatenated by kind (one launch per kind)
+  GatherCat cat0{};
+  BcFaceCat cat1{};
+  BcNextArgs cat2{};
+  std::vector<void*> cat_mem;       // device arrays of the concatenated lists
+  BcFaceArgs* cat_lp = nullptr;     // per-window parameters of cat1
+  bool cat_built = false;
   double* cfl = nullptr;            // CFL max, min, mean of the last verified iteration
   double* cfl_part = nullptr;       // per-CTA partials of the CFL reduction
   bool dist_set = false;
@@ -125,6 +132,7 @@ struct fgb_solver {
     double *lamTi = nullptr, *lamTj = nullptr, *lamVol = nullptr, *lamSt = nullptr;
     double *dW = nullptr, *dWn = nullptr, *dD = nullptr, *dFi = nullptr, *dFj = nullptr;
     double *dTi = nullptr, *dTj = nullptr, *dVol = nullptr, *dSt = nullptr;
+    double* tape = nullptr;        // face tapes of a segment's recomputed stages
     // CUDA graphs of the driver loops: one RK3 step from either ping-pong
     // buffer; a full segment's recomputation; a full segment's reverse sweep
     // for either assignment of the two lambda buffers
@@ -589,6 +597,8 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.dist);
     cudaFree(Z.cfl);
     cudaFree(Z.cfl_part);
+    for (void* m : Z.cat_mem) cudaFree(m);
+    cudaFree(Z.cat_lp);
     for (WallCorrList& w : Z.walls) { cudaFree(w.l); cudaFree(w.l0); cudaFree(w.lt); cudaFree(w.nrm); }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
@@ -839,6 +849,84 @@ int fgb_download_work(fgb_solver* s, int zone, const char* which, double* host, 
 }
 
 // ghost fill of one level of every zone: transfers, face BCs, edges/corners
+static BcFaceArgs face_args(ZoneData& Z, GatherList& g);
+static BcNextArgs next_args(ZoneData& Z, GatherList& g);
+
+// Concatenate a zone's BC lists by kind: face BCs (with the window of each
+// entry and the windows' parameters), gathers (with the operation of each
+// entry), next ranks.  Windows write disjoint ghost cells; face BCs read
+// interior cells, gathers interior cells or the first ghost layer of an
+// outflow (written by the face BCs), next ranks the first ghost layer: so
+// one launch per kind in the order face BCs, gathers, next ranks gives the
+// values of the per-window order.
+static int build_cat(ZoneData& Z) {
+  int64_t n0 = 0, n1 = 0, n2 = 0;
+  for (GatherList& g : Z.bcs) (g.kind == 0 ? n0 : (g.kind == 1 ? n1 : n2)) += g.n;
+  auto alloc_i = [&](int32_t** p, int64_t n) -> int {
+    *p = nullptr;
+    if (n <= 0) return FGB_OK;
+    CK(cudaMalloc(p, sizeof(int32_t) * (size_t)n));
+    Z.cat_mem.push_back(*p);
+    return FGB_OK;
+  };
+  int rc;
+  int32_t *d0, *s0, *o0, *d1, *s1, *l1, *m1, *d2, *q0, *q1, *q2;
+  if ((rc = alloc_i(&d0, n0)) || (rc = alloc_i(&s0, n0)) || (rc = alloc_i(&o0, n0)) ||
+      (rc = alloc_i(&d1, n1)) || (rc = alloc_i(&s1, n1)) || (rc = alloc_i(&l1, n1)) ||
+      (rc = alloc_i(&m1, n1)) || (rc = alloc_i(&d2, n2)) || (rc = alloc_i(&q0, n2)) ||
+      (rc = alloc_i(&q1, n2)) || (rc = alloc_i(&q2, n2)))
+    return rc;
+  double* nr1 = nullptr;
+  if (n1 > 0) {
+    CK(cudaMalloc(&nr1, sizeof(double) * 3 * (size_t)n1));
+    Z.cat_mem.push_back(nr1);
+  }
+  std::vector<int32_t> op0((size_t)n0), lid1((size_t)n1);
+  std::vector<BcFaceArgs> lp;
+  int64_t o0c = 0, o1c = 0, o2c = 0;
+  const size_t I = sizeof(int32_t);
+  for (GatherList& g : Z.bcs) {
+    if (g.n <= 0) continue;
+    if (g.kind == 0) {
+      CK(cudaMemcpy(d0 + o0c, g.dst, I * g.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s0 + o0c, g.src, I * g.n, cudaMemcpyDeviceToDevice));
+      for (int64_t t = 0; t < g.n; t++) op0[(size_t)(o0c + t)] = g.op;
+      o0c += g.n;
+    } else if (g.kind == 1) {
+      CK(cudaMemcpy(d1 + o1c, g.dst, I * g.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s1 + o1c, g.src, I * g.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(m1 + o1c, g.mt, I * g.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(nr1 + 3 * o1c, g.nrm, sizeof(double) * 3 * g.n, cudaMemcpyDeviceToDevice));
+      for (int64_t t = 0; t < g.n; t++) lid1[(size_t)(o1c + t)] = (int32_t)lp.size();
+      BcFaceArgs a = face_args(Z, g);
+      a.dst = nullptr; a.src = nullptr; a.nrm = nullptr;
+      lp.push_back(a);
+      o1c += g.n;
+    } else {
+      CK(cudaMemcpy(d2 + o2c, g.dst, I * g.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(q0 + o2c, g.q0, I * g.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(q1 + o2c, g.q1, I * g.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(q2 + o2c, g.q2, I * g.n, cudaMemcpyDeviceToDevice));
+      o2c += g.n;
+    }
+  }
+  if (n0 > 0) CK(cudaMemcpy(o0, op0.data(), I * n0, cudaMemcpyHostToDevice));
+  if (n1 > 0) CK(cudaMemcpy(l1, lid1.data(), I * n1, cudaMemcpyHostToDevice));
+  cudaFree(Z.cat_lp);
+  Z.cat_lp = nullptr;
+  if (!lp.empty()) {
+    CK(cudaMalloc(&Z.cat_lp, sizeof(BcFaceArgs) * lp.size()));
+    CK(cudaMemcpy(Z.cat_lp, lp.data(), sizeof(BcFaceArgs) * lp.size(), cudaMemcpyHostToDevice));
+  }
+  Z.cat0 = GatherCat{d0, s0, o0, n0};
+  Z.cat1 = BcFaceCat{d1, s1, l1, m1, nr1, n1, Z.cat_lp};
+  GatherList g2;
+  g2.dst = d2; g2.q0 = q0; g2.q1 = q1; g2.q2 = q2; g2.n = n2;
+  Z.cat2 = next_args(Z, g2);
+  Z.cat_built = true;
+  return FGB_OK;
+}
+
 // The ghost fill of one level.  Transfers read donor interior cells and
 // write receiver ghost cells; a zone's BC lists read its interior and write
 // its own ghost layers; its corner averages read those.  So the fill of
@@ -878,40 +966,20 @@ static int ghost_fill(fgb_solver* s, int level) {
   return zone_join(s);
 }
 
-// BC lists and corner averages of zone m
+// BC lists and corner averages of zone m: face BCs, gathers, next ranks
+// (each concatenated over the zone's windows), then the corners
 static int ghost_fill_zone(fgb_solver* s, int m, int level) {
-  {
-    ZoneData& Z = s->zones[(size_t)m];
-    for (GatherList& g : Z.bcs) {
-      if (g.kind == 0) {
-        CK(launch_gather(Z.lvl[level], Z.z.nd, Z.lvl[level], Z.z.nd, g.dst, g.src, g.n, Z.z.neq,
-                         g.op, 1., s->st));
-      } else if (g.kind == 1) {
-        BcFaceArgs a{};
-        a.dst = g.dst; a.src = g.src; a.nrm = g.nrm; a.n = g.n; a.nd = Z.z.nd; a.op = g.op;
-        a.gam = Z.pr[GAMMA]; a.gam1 = Z.pr[GAMMA] - 1.; a.gam1_1 = 1. / a.gam1;
-        a.cv = Z.pr[CVINF]; a.cvinv = 1. / Z.pr[CVINF];
-        for (int m = 0; m < 5; m++) a.st[m] = g.st[m];
-        a.sa = Z.z.neq == 6;
-        a.inflow = g.inflow;
-        a.nue = Z.pr[RONUTILDEINF] / Z.pr[ROINF];   // BCFarfield_init.for: state(6) / state(1)
-        CK(launch_bc_face(Z.lvl[level], a, s->st));
-      } else {
-        // BC_nextrank.for with the MUSCL constants of BCzone.cpp (c4, c5, c6)
-        const double c4 = 5. / 6., c5 = 2. / 6., c6 = -1. / 6.;
-        const double k0 = 1. / c6;
-        BcNextArgs a{};
-        a.dst = g.dst; a.q0 = g.q0; a.q1 = g.q1; a.q2 = g.q2; a.n = g.n; a.nd = Z.z.nd;
-        a.k1 = -(c4 + c5) * k0; a.k2 = -c6 * k0; a.k3 = (2. - c5 - c4) * k0;
-        a.sa = Z.z.neq == 6;
-        CK(launch_bc_next(Z.lvl[level], a, s->st));
-      }
-      s->launches++;
-    }
-    CK(launch_coins(Z.lvl[level], Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n,
-                    Z.z.neq, s->st));
-    s->launches++;
+  ZoneData& Z = s->zones[(size_t)m];
+  if (!Z.cat_built) {
+    int rc = build_cat(Z);
+    if (rc) return rc;
   }
+  double* q = Z.lvl[level];
+  CK(launch_bc_face_cat(q, Z.cat1, s->st));
+  CK(launch_gather_cat(q, Z.z.nd, Z.cat0, Z.z.neq, s->st));
+  CK(launch_bc_next(q, Z.cat2, s->st));
+  CK(launch_coins(q, Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n, Z.z.neq, s->st));
+  s->launches += (Z.cat1.n > 0) + (Z.cat0.n > 0) + (Z.cat2.n > 0) + (Z.co_n > 0);
   return FGB_OK;
 }
 
@@ -933,7 +1001,7 @@ static void adj_free(fgb_solver* s) {
   A.ck.clear();
   double** bufs[] = {&A.W, &A.D, &A.lamW, &A.lamIn, &A.lamD, &A.lamTi, &A.lamTj, &A.lamVol,
                      &A.lamSt, &A.dW, &A.dWn, &A.dD, &A.dFi, &A.dFj, &A.dTi, &A.dTj, &A.dVol,
-                     &A.dSt};
+                     &A.dSt, &A.tape};
   for (double** b : bufs) { cudaFree(*b); *b = nullptr; }
   cudaGraphExec_t* gs[] = {&A.step[0], &A.step[1], &A.rec, &A.rev[0], &A.rev[1]};
   for (cudaGraphExec_t* g : gs) { if (*g) cudaGraphExecDestroy(*g); *g = nullptr; }
@@ -969,6 +1037,7 @@ static BcFaceArgs face_args(ZoneData& Z, GatherList& g) {
   for (int m = 0; m < 5; m++) a.st[m] = g.st[m];
   a.sa = Z.z.neq == 6; a.inflow = g.inflow;
   a.nue = Z.pr[RONUTILDEINF] / Z.pr[ROINF];
+  a.dir = g.dir;
   return a;
 }
 
@@ -986,13 +1055,15 @@ static BcNextArgs next_args(ZoneData& Z, GatherList& g) {
 // order of ghost_fill
 static int zone_fill(fgb_solver* s, int m, double* q) {
   ZoneData& Z = s->zones[m];
+  if (!Z.cat_built) {
+    int rc = build_cat(Z);
+    if (rc) return rc;
+  }
   for (Transfer& T : s->tr)
     if (T.rcv == m) CK(launch_gather(q, Z.z.nd, q, Z.z.nd, T.rcv_idx, T.dnr_idx, T.n, Z.z.neq, 0, 1., s->st));
-  for (GatherList& g : Z.bcs) {
-    if (g.kind == 0) CK(launch_gather(q, Z.z.nd, q, Z.z.nd, g.dst, g.src, g.n, Z.z.neq, g.op, 1., s->st));
-    else if (g.kind == 1) CK(launch_bc_face(q, face_args(Z, g), s->st));
-    else CK(launch_bc_next(q, next_args(Z, g), s->st));
-  }
+  CK(launch_bc_face_cat(q, Z.cat1, s->st));
+  CK(launch_gather_cat(q, Z.z.nd, Z.cat0, Z.z.neq, s->st));
+  CK(launch_bc_next(q, Z.cat2, s->st));
   CK(launch_coins(q, Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n, Z.z.neq, s->st));
   return FGB_OK;
 }
@@ -1001,14 +1072,18 @@ static int zone_fill(fgb_solver* s, int m, double* q) {
 static int zone_fill_tan(fgb_solver* s, int m, const double* q, double* dq) {
   ZoneData& Z = s->zones[m];
   fgb_solver::Adj& A = s->adj;
+  if (!Z.cat_built) {
+    int rc = build_cat(Z);
+    if (rc) return rc;
+  }
   for (Transfer& T : s->tr)
     if (T.rcv == m) CK(launch_gather(dq, Z.z.nd, dq, Z.z.nd, T.rcv_idx, T.dnr_idx, T.n, Z.z.neq, 0, 1., s->st));
-  for (GatherList& g : Z.bcs) {
-    if (g.kind == 0) CK(launch_gather(dq, Z.z.nd, dq, Z.z.nd, g.dst, g.src, g.n, Z.z.neq, 0, 1., s->st));
-    else if (g.kind == 1)
-      CK(launch_tan_bc_face(q, dq, face_args(Z, g), g.mt, Z.z.ndm, g.dir == 0 ? A.dTi : A.dTj, A.dSt, s->st));
-    else CK(launch_lin_bc_next(q, dq, next_args(Z, g), 0, Z.z.neq, s->st));
+  CK(launch_tan_bc_face_cat(q, dq, Z.cat1, Z.z.ndm, A.dTi, A.dTj, A.dSt, s->st));
+  {  // gathers: linear copies (the extrapolation's max(-1e30, x) is the identity here)
+    GatherCat c = Z.cat0;
+    if (c.n > 0) CK(launch_gather(dq, Z.z.nd, dq, Z.z.nd, c.dst, c.src, c.n, Z.z.neq, 0, 1., s->st));
   }
+  CK(launch_lin_bc_next(q, dq, Z.cat2, 0, Z.z.neq, s->st));
   CK(launch_coins(dq, Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n, Z.z.neq, s->st));
   return FGB_OK;
 }
@@ -1018,15 +1093,15 @@ static int zone_fill_tan(fgb_solver* s, int m, const double* q, double* dq) {
 static int zone_fill_adj(fgb_solver* s, int m, const double* q, double* lam) {
   ZoneData& Z = s->zones[m];
   fgb_solver::Adj& A = s->adj;
-  CK(launch_adj_coins(lam, Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n, Z.z.neq, s->st));
-  for (int i = (int)Z.bcs.size() - 1; i >= 0; i--) {
-    GatherList& g = Z.bcs[(size_t)i];
-    if (g.kind == 0) CK(launch_adj_gather(lam, Z.z.nd, g.dst, g.src, g.n, Z.z.neq, s->st));
-    else if (g.kind == 1)
-      CK(launch_adj_bc_face(q, lam, face_args(Z, g), g.mt, Z.z.ndm, g.dir == 0 ? A.lamTi : A.lamTj,
-                            A.lamSt, s->st));
-    else CK(launch_lin_bc_next(q, lam, next_args(Z, g), 1, Z.z.neq, s->st));
+  if (!Z.cat_built) {
+    int rc = build_cat(Z);
+    if (rc) return rc;
   }
+  // the reverse of zone_fill: corners, next ranks, gathers, face BCs
+  CK(launch_adj_coins(lam, Z.z.nd, Z.co_dst, Z.co_a, Z.co_b, Z.co_c, Z.co_nedge, Z.co_n, Z.z.neq, s->st));
+  CK(launch_lin_bc_next(q, lam, Z.cat2, 1, Z.z.neq, s->st));
+  CK(launch_adj_gather(lam, Z.z.nd, Z.cat0.dst, Z.cat0.src, Z.cat0.n, Z.z.neq, s->st));
+  CK(launch_adj_bc_face_cat(q, lam, Z.cat1, Z.z.ndm, A.lamTi, A.lamTj, A.lamSt, s->st));
   for (int i = (int)s->tr.size() - 1; i >= 0; i--) {
     Transfer& T = s->tr[(size_t)i];
     if (T.rcv == m) CK(launch_adj_gather(lam, Z.z.nd, T.rcv_idx, T.dnr_idx, T.n, Z.z.neq, s->st));
@@ -1065,10 +1140,13 @@ static int assemble_stage(fgb_solver* s, ZoneData& Z, StageArgs sa, const double
 static const double kCoefH[4] = {0., 0., -0.6830127018922193, -4. / 3.};
 static const double kCoefW[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
 
-// one RK3 stage of fgb_compute's explicit path on explicit buffers
-static int explicit_stage(fgb_solver* s, int m, int nstep, const double* in, double* out, double* D) {
+// one RK3 stage of fgb_compute's explicit path on explicit buffers; with a
+// tape, the face fluxes also record the values of their reverse pass
+static int explicit_stage(fgb_solver* s, int m, int nstep, const double* in, double* out, double* D,
+                          double* tape = nullptr) {
   ZoneData& Z = s->zones[m];
-  cudaError_t e = launch_faces(Z.z, in, Z.xmut, Z.Fi, Z.Fj, Z.Fk, s->st);
+  cudaError_t e = tape ? launch_faces_tape(Z.z, in, Z.Fi, Z.Fj, tape, s->st)
+                       : launch_faces(Z.z, in, Z.xmut, Z.Fi, Z.Fj, Z.Fk, s->st);
   if (e == cudaErrorNotSupported) return fail(FGB_ERR_ARG, "scheme not implemented");
   CK(e);
   StageArgs sa{};
@@ -1390,6 +1468,13 @@ int fgb_set_bc_state(fgb_solver* s, int zone, const double* st) {
   for (GatherList& g : s->zones[zone].bcs)
     if (g.kind == 1 && (g.op == BCF_FARFIELD || g.op == BCF_OUTFLOW))
       for (int m = 0; m < 5; m++) g.st[m] = st[m];
+  {  // the concatenated lists carry the state in their window parameters
+    ZoneData& Z = s->zones[zone];
+    CK(cudaStreamSynchronize(s->st));
+    for (void* m : Z.cat_mem) cudaFree(m);
+    Z.cat_mem.clear();
+    Z.cat_built = false;
+  }
   return FGB_OK;
 }
 
@@ -1480,6 +1565,8 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
   CK(cudaMemsetAsync(A.lamVol, 0, sizeof(double) * z.ndm, s->st));
   CK(cudaMemsetAsync(A.lamSt, 0, sizeof(double) * 5, s->st));
   if (!A.lam0) A.lam0 = A.lamW;
+  const size_t tstride = (size_t)FACE_TAPE * (size_t)((z.ni + 1) * z.nj + z.ni * (z.nj + 1));
+  if (!A.tape) CK(cudaMalloc(&A.tape, sizeof(double) * tstride * 3 * (size_t)ckpt));
   // recompute a segment: W[3t + st - 1] = input of stage st of step t
   auto recompute = [&](int steps) -> int {
     for (int t = 0; t < steps; t++)
@@ -1489,7 +1576,8 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
         if (st_ > 1)
           CK(cudaMemcpyAsync(A.D + i * nq, A.D + (i - 1) * nq, sizeof(double) * nq,
                              cudaMemcpyDeviceToDevice, s->st));
-        const int r = explicit_stage(s, zone, st_, A.W + i * nq, A.W + (i + 1) * nq, A.D + i * nq);
+        const int r = explicit_stage(s, zone, st_, A.W + i * nq, A.W + (i + 1) * nq, A.D + i * nq,
+                                     A.tape + i * tstride);
         if (r) return r;
       }
     return (int)FGB_OK;
@@ -1513,7 +1601,8 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
         }
         {
           ProfScope ps(s, "adj_faces");
-          CK(launch_adj_faces(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, s->st));
+          CK(launch_adj_faces(z, A.W + i * nq, A.tape + i * tstride, A.lamD, A.lamIn, A.lamTi,
+                              A.lamTj, s->st));
           for (WallCorrList& w : Z.walls)
             CK(launch_adj_wall(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, wall_args(Z, w), s->st));
         }

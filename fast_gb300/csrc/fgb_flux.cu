@@ -126,8 +126,13 @@ __device__ __forceinline__ void roe_cart(const Zone& z, const double qm[5], cons
 
 // ----------------------------------------------------------- Roe (general)
 // Vit_ent/fludiffer_3dfull_i.for with the face normal (tcx,tcy,tcz), |S| = s.
+// TAPE: also store, at tp[k * ts] for k = 1..8, the square roots and
+// quotients that a reverse pass of this flux needs (s1, s2, 1/(s1+s2), c,
+// 1/|S|, and the reciprocals 1/f4, 1/c^2, 1/(s1 s2)); F is unchanged.
+template <bool TAPE = false>
 __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], const double qp[5],
-                                         double tcx, double tcy, double tcz, double s, double F[5]) {
+                                         double tcx, double tcy, double tcz, double s, double F[5],
+                                         double* tp = nullptr, int64_t ts = 0) {
   const double rgp = z.rgp, gam1 = z.gam1;
   double r1 = qp[0], p1 = r1 * qp[4] * rgp;
   double h1 = gam1 * qp[4] * rgp + .5 * (qp[1] * qp[1] + qp[2] * qp[2] + qp[3] * qp[3]);
@@ -150,6 +155,10 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
   double qn = u * nx + v * ny + w * nz;
   double f1 = qn;
   double f4 = z.psiroe * (fabs(f1) + c);
+  if (TAPE) {
+    tp[ts] = s1; tp[2 * ts] = s2; tp[3 * ts] = r_1; tp[4 * ts] = c; tp[5 * ts] = s_1;
+    tp[6 * ts] = 1. / f4; tp[7 * ts] = 1. / (c * c); tp[8 * ts] = 1. / r;
+  }
   double f2 = 0.5 + fsignF(0.5, fabs(f1) - f4);
   double f3 = (f2 - 1.0) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
   f1 = (r2 - r1 - dp / (c * c)) * s;
@@ -915,6 +924,64 @@ cudaError_t launch_sa_source(const Zone& z, const double* q, double* drodm, doub
   else if (z.typ == Z3DFULL) sa_source<Z3DFULL><<<g, B, 0, st>>>(z, q, drodm, coe, coefH, zero_init, lu);
   else if (z.typ == Z2D) sa_source<Z2D><<<g, B, 0, st>>>(z, q, drodm, coe, coefH, zero_init, lu);
   else return cudaErrorNotSupported;
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------- taped faces (adjoint)
+// face_flux<D, Z2D, ROE, VANALBADA, false> that also writes, per face, the
+// values a reverse pass needs and would otherwise recompute with square
+// roots and divisions (FACE_TAPE doubles, face-major stride nf): |S|, the
+// Roe-flux values of roe_full<true>, and per variable (ro, u, v, T) and
+// side the van Albada slope va and the reciprocal of its denominator.  The
+// flux is computed by the same expressions as face_flux: F is the same.
+template <int D>
+__global__ void __launch_bounds__(128) face_flux_tape(Zone z, const double* __restrict__ q,
+                                                      double* __restrict__ Fo,
+                                                      double* __restrict__ tape) {
+  const int64_t NI = z.ni + (D == 0), NJ = z.nj + (D == 1);
+  const int64_t nf = NI * NJ;
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int64_t ii = f % NI, jj = f / NI;
+  const int64_t l = inddm(z, ii + 1, jj + 1, 1);
+  const int64_t inc = z.inc[D], nd = z.nd;
+  double* T = tape + f;
+  double qm[5], qp[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) {
+    if (v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
+    const double* Q = q + v * nd;
+    const double a = Q[l - 2 * inc], b = Q[l - inc], c = Q[l], d = Q[l + inc];
+    const double x1 = c - b, y1 = d - c, x2 = b - a, y2 = c - b;
+    const double vm = vanalbada(x1, y1), vp = vanalbada(x2, y2);
+    qm[v] = c - 0.5 * vm;
+    qp[v] = b + 0.5 * vp;
+    const int m = v == 4 ? 3 : v;
+    T[(TAPE_VA + 2 * m) * nf] = vm;
+    T[(TAPE_VA + 2 * m + 1) * nf] = vp;
+    T[(TAPE_ID + 2 * m) * nf] = 1. / (x1 * x1 + y1 * y1 + 2. * 1e-12);
+    T[(TAPE_ID + 2 * m + 1) * nf] = 1. / (x2 * x2 + y2 * y2 + 2. * 1e-12);
+  }
+  const int64_t lt = indmtr(z, ii + 1, jj + 1, 1);
+  const double* t = D == 0 ? z.ti : z.tj;
+  const double tcx = t[lt], tcy = t[lt + z.ndm];
+  const double s = sqrt(tcx * tcx + tcy * tcy);
+  T[0] = s;
+  double F[5];
+  roe_full<true>(z, qm, qp, tcx, tcy, 0., s, F, T, nf);
+  F[3] = 0.;
+#pragma unroll
+  for (int v = 0; v < 5; v++) Fo[v * nf + f] = F[v];
+}
+
+cudaError_t launch_faces_tape(const Zone& z, const double* q, double* Fi, double* Fj, double* tape,
+                              cudaStream_t st) {
+  if (z.typ != Z2D || z.kflu != ROE || z.slope != VANALBADA || z.iflow != 1)
+    return cudaErrorNotSupported;
+  const int B = 128;
+  const int64_t nfi = (z.ni + 1) * z.nj, nfj = z.ni * (z.nj + 1);
+  face_flux_tape<0><<<(unsigned)((nfi + B - 1) / B), B, 0, st>>>(z, q, Fi, tape);
+  face_flux_tape<1><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, Fj, tape + FACE_TAPE * nfi);
   return cudaGetLastError();
 }
 

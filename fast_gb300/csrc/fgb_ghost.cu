@@ -128,11 +128,9 @@ __device__ __forceinline__ void non_reflection(const BcFaceArgs& a, const double
   o.r = r; o.u = u; o.v = v; o.w = w; o.qn = qn; o.sn = sn;
 }
 
-__global__ void __launch_bounds__(128) bc_face(double* __restrict__ q, BcFaceArgs a) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
-  const int64_t nd = a.nd, l = a.dst[e], s = a.src[e];
-  const double t[3] = {a.nrm[3 * e], a.nrm[3 * e + 1], a.nrm[3 * e + 2]};
+__device__ __forceinline__ void bc_face_entry(double* __restrict__ q, const BcFaceArgs& a,
+                                              int64_t l, int64_t s, const double t[3]) {
+  const int64_t nd = a.nd;
   if (a.op == BCF_SLIP) {
     double tcx = t[0], tcy = t[1], tcz = t[2];
     double surf = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
@@ -183,6 +181,48 @@ __global__ void __launch_bounds__(128) bc_face(double* __restrict__ q, BcFaceArg
     q[l + 4 * nd] = (o.qvar5 * roinv - .5 * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2])) * a.cvinv;
     if (a.sa) q[l + 5 * nd] = q[s + 5 * nd];          // BCOutflow_firstrank_SA.for
   }
+}
+
+__global__ void __launch_bounds__(128) bc_face(double* __restrict__ q, BcFaceArgs a) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  const double t[3] = {a.nrm[3 * e], a.nrm[3 * e + 1], a.nrm[3 * e + 2]};
+  bc_face_entry(q, a, a.dst[e], a.src[e], t);
+}
+
+// every face-BC window of a zone in one launch (the windows write disjoint
+// ghost cells and read interior cells only)
+__global__ void __launch_bounds__(128) bc_face_cat(double* __restrict__ q, BcFaceCat c) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= c.n) return;
+  const double t[3] = {c.nrm[3 * e], c.nrm[3 * e + 1], c.nrm[3 * e + 2]};
+  bc_face_entry(q, c.lp[c.lid[e]], c.dst[e], c.src[e], t);
+}
+
+__global__ void __launch_bounds__(256) gather_cat(double* __restrict__ q, int64_t nd, GatherCat c,
+                                                  int neq) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= c.n) return;
+  const int64_t d = c.dst[t], s = c.src[t];
+  const int op = c.op[t];
+  for (int v = 0; v < neq; v++) {
+    double x = q[s + v * nd];
+    if (op == 1) x = fmaxF(-1.e30, x);
+    if (op != 0) x = x * 1.;
+    q[d + v * nd] = x;
+  }
+}
+
+cudaError_t launch_bc_face_cat(double* q, const BcFaceCat& c, cudaStream_t st) {
+  if (c.n <= 0) return cudaSuccess;
+  bc_face_cat<<<(unsigned)((c.n + 127) / 128), 128, 0, st>>>(q, c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_cat(double* q, int64_t nd, const GatherCat& c, int neq, cudaStream_t st) {
+  if (c.n <= 0) return cudaSuccess;
+  gather_cat<<<(unsigned)((c.n + 255) / 256), 256, 0, st>>>(q, nd, c, neq);
+  return cudaGetLastError();
 }
 
 // BC/BC_nextrank.for: ghost ranks beyond the first of farfield / inflow BCs,

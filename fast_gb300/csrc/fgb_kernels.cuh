@@ -116,6 +116,22 @@ struct BcFaceArgs {            // one face BC window (bc_face)
   double st[5];                // exterior state (conservative)
   int sa, inflow;              // Spalart-Allmaras zone; BCInflow (nutilde imposed)
   double nue;                  // exterior nutilde (state(6) / state(1))
+  int dir;                     // face direction of the window (0 i, 1 j, 2 k)
+};
+// All face-BC windows of a zone as one list: per entry its ghost cell,
+// source cell, raw normal, face metric index and window (lid), the
+// window's parameters in lp[lid] (device memory)
+struct BcFaceCat {
+  const int32_t *dst, *src, *lid, *mt;
+  const double* nrm;
+  int64_t n;
+  const BcFaceArgs* lp;
+};
+// All gather windows of a zone (periodic, extrapolation) as one list with
+// the operation of each entry (0 copy, 1 max(-1e30, x))
+struct GatherCat {
+  const int32_t *dst, *src, *op;
+  int64_t n;
 };
 struct BcNextArgs {            // farfield / inflow ghost ranks past the first
   const int32_t *dst, *q0, *q1, *q2;
@@ -124,6 +140,8 @@ struct BcNextArgs {            // farfield / inflow ghost ranks past the first
   int sa;
 };
 cudaError_t launch_bc_face(double* q, const BcFaceArgs& a, cudaStream_t st);
+cudaError_t launch_bc_face_cat(double* q, const BcFaceCat& c, cudaStream_t st);
+cudaError_t launch_gather_cat(double* q, int64_t nd, const GatherCat& c, int neq, cudaStream_t st);
 cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st);
 cudaError_t launch_coins(double* q, int64_t nd, const int32_t* dst, const int32_t* a,
                          const int32_t* b, const int32_t* c, int64_t n_edge, int64_t n, int neq,
@@ -141,7 +159,16 @@ cudaError_t run_fp64_probe(int nsm, int iters, double* out, cudaStream_t st);
 
 // fgb_adjoint.cu: tangent / adjoint of the explicit 2-d Euler step (Roe +
 // van Albada), from local Jacobians of the face flux, BC and update formulas
-cudaError_t launch_adj_faces(const Zone& z, const double* q, const double* lamD, double* lamQ,
+// Face tape of the adjoint's recomputation (2-d Roe + van Albada faces):
+// FACE_TAPE doubles per face, face-major; slots 0..8 = |S| and the Roe
+// values of roe_full<true>, TAPE_VA.. = van Albada slopes (variable m, side
+// qm / qp), TAPE_ID.. = reciprocals of their denominators.  A stage's tape =
+// FACE_TAPE * (i faces + j faces) doubles, the i faces first.
+constexpr int FACE_TAPE = 25, TAPE_VA = 9, TAPE_ID = 17;
+cudaError_t launch_faces_tape(const Zone& z, const double* q, double* Fi, double* Fj, double* tape,
+                              cudaStream_t st);
+cudaError_t launch_adj_faces(const Zone& z, const double* q, const double* tape,
+                             const double* lamD, double* lamQ,
                              double* lamTi, double* lamTj, cudaStream_t st);
 cudaError_t launch_tan_faces(const Zone& z, const double* q, const double* dq, const double* dTi,
                              const double* dTj, double* dFi, double* dFj, cudaStream_t st);
@@ -157,6 +184,11 @@ cudaError_t launch_adj_wall(const Zone& z, const double* q, const double* lamD, 
                             double* lamTi, double* lamTj, const WallCorrArgs& a, cudaStream_t st);
 cudaError_t launch_tan_wall(const Zone& z, const double* q, const double* dq, const double* dTi,
                             const double* dTj, double* dD, const WallCorrArgs& a, cudaStream_t st);
+cudaError_t launch_adj_bc_face_cat(const double* q, double* lam, const BcFaceCat& c, int64_t ndm,
+                                   double* lamTi, double* lamTj, double* lamSt, cudaStream_t st);
+cudaError_t launch_tan_bc_face_cat(const double* q, double* dq, const BcFaceCat& c, int64_t ndm,
+                                   const double* dTi, const double* dTj, const double* dSt,
+                                   cudaStream_t st);
 cudaError_t launch_adj_bc_face(const double* q, double* lam, const BcFaceArgs& a, const int32_t* mt,
                                int64_t ndm, double* lamT, double* lamSt, cudaStream_t st);
 cudaError_t launch_tan_bc_face(const double* q, double* dq, const BcFaceArgs& a, const int32_t* mt,
