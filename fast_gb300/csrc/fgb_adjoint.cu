@@ -923,95 +923,13 @@ __device__ __forceinline__ void farfield_lin(const BcFaceArgs& a, const double* 
   farfield_eval<8>(a, q, s, t, -1, J);
 }
 
-// adjoint of one face-BC list: lam[src] += J^T lam[dst], lam[dst] = 0;
-// slip: lamT[mt] (metric of the face) += d/d normal; farfield: lamSt += d/d st.
-// Eight lanes per ghost cell, lane k the Jacobian column of input k (one
-// seeded input each, the columns run in parallel); no lane leaves before the
-// warp barrier that orders the reads of lam[dst] before its reset.
-__global__ void __launch_bounds__(128) adj_bc_face(const double* __restrict__ q,
-                                                   double* __restrict__ lam, BcFaceArgs a,
-                                                   const int32_t* __restrict__ mt, int64_t ndm,
-                                                   double* __restrict__ lamT,
-                                                   double* __restrict__ lamSt) {
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t e = gid >> 3;
-  const int k = (int)(gid & 7);
-  const bool act = e < a.n;
-  const int64_t nd = a.nd;
-  int64_t l = 0, s = 0;
-  double lo[4] = {0., 0., 0., 0.};
-  if (act) {
-    l = a.dst[e];
-    s = a.src[e];
-#pragma unroll
-    for (int m = 0; m < 4; m++) lo[m] = lam[l + V4[m] * nd];
-  }
-  __syncwarp();
-  if (act && k == 0) {
-#pragma unroll
-    for (int v = 0; v < 5; v++) lam[l + v * nd] = 0.;
-  }
-  if (!act) return;
-  double J[4][1];
-  if (a.op == BCF_SLIP) {
-    if (k >= 6) return;
-    slip_eval<1>(q, nd, s, a.nrm[3 * e], a.nrm[3 * e + 1], k, J);
-  } else {
-    const double t[3] = {a.nrm[3 * e], a.nrm[3 * e + 1], a.nrm[3 * e + 2]};
-    farfield_eval<1>(a, q, s, t, k, J);
-  }
-  double g = 0.;
-#pragma unroll
-  for (int m = 0; m < 4; m++) g += lo[m] * J[m][0];
-  if (k < 4) atomicAdd(lam + s + V4[k] * nd, g);
-  else if (a.op == BCF_SLIP) atomicAdd(lamT + mt[e] + (k == 4 ? 0 : ndm), g);
-  else atomicAdd(lamSt + (k == 7 ? 4 : k - 4), g);
-}
-
-// tangent of one face-BC list: dq[dst] = J (dq[src], dnormal | dst)
-__global__ void __launch_bounds__(128) tan_bc_face(const double* __restrict__ q,
-                                                   double* __restrict__ dq, BcFaceArgs a,
-                                                   const int32_t* __restrict__ mt, int64_t ndm,
-                                                   const double* __restrict__ dT,
-                                                   const double* __restrict__ dSt) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
-  const int64_t nd = a.nd, l = a.dst[e], s = a.src[e];
-  double out[4];
-  if (a.op == BCF_SLIP) {
-    double J[4][6];
-    slip_lin(q, nd, s, a.nrm[3 * e], a.nrm[3 * e + 1], J);
-    const double din[6] = {dq[s], dq[s + nd], dq[s + 2 * nd], dq[s + 4 * nd], dT[mt[e]],
-                           dT[mt[e] + ndm]};
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      double x = 0.;
-#pragma unroll
-      for (int k = 0; k < 6; k++) x += J[m][k] * din[k];
-      out[m] = x;
-    }
-  } else {
-    const double t[3] = {a.nrm[3 * e], a.nrm[3 * e + 1], a.nrm[3 * e + 2]};
-    double J[4][8];
-    farfield_lin(a, q, s, t, J);
-    const double din[8] = {dq[s], dq[s + nd], dq[s + 2 * nd], dq[s + 4 * nd],
-                           dSt[0], dSt[1], dSt[2], dSt[4]};
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      double x = 0.;
-#pragma unroll
-      for (int k = 0; k < 8; k++) x += J[m][k] * din[k];
-      out[m] = x;
-    }
-  }
-#pragma unroll
-  for (int m = 0; m < 4; m++) dq[l + V4[m] * nd] = out[m];
-  dq[l + 3 * nd] = 0.;
-}
-
-// all face-BC windows of a zone in one launch (adj_bc_face / tan_bc_face
-// per entry, the window's parameters from c.lp, the metric adjoint or
-// tangent of the window's direction)
+// Adjoint of the face-BC windows of a zone (all windows in one launch):
+// lam[src] += J^T lam[dst], lam[dst] = 0; slip: the window direction's
+// metric adjoint (face of the entry) += d/d normal; farfield: lamSt += d/d
+// st.  Eight lanes per ghost cell, lane k the Jacobian column of input k
+// (one seeded input each); no lane leaves before the warp barrier that
+// orders the reads of lam[dst] before its reset.  The tangent kernel applies
+// the full local Jacobian (window parameters from c.lp per entry).
 __global__ void __launch_bounds__(128) adj_bc_face_cat(const double* __restrict__ q,
                                                        double* __restrict__ lam, BcFaceCat c,
                                                        int64_t ndm, double* __restrict__ lamTi,
@@ -1108,22 +1026,6 @@ cudaError_t launch_tan_bc_face_cat(const double* q, double* dq, const BcFaceCat&
                                    cudaStream_t st) {
   if (c.n <= 0) return cudaSuccess;
   tan_bc_face_cat<<<(unsigned)((c.n + 127) / 128), 128, 0, st>>>(q, dq, c, ndm, dTi, dTj, dSt);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_adj_bc_face(const double* q, double* lam, const BcFaceArgs& a, const int32_t* mt,
-                               int64_t ndm, double* lamT, double* lamSt, cudaStream_t st) {
-  if (a.n <= 0) return cudaSuccess;
-  if (a.op != BCF_SLIP && a.op != BCF_FARFIELD) return cudaErrorNotSupported;
-  adj_bc_face<<<(unsigned)((8 * a.n + 127) / 128), 128, 0, st>>>(q, lam, a, mt, ndm, lamT, lamSt);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_tan_bc_face(const double* q, double* dq, const BcFaceArgs& a, const int32_t* mt,
-                               int64_t ndm, const double* dT, const double* dSt, cudaStream_t st) {
-  if (a.n <= 0) return cudaSuccess;
-  if (a.op != BCF_SLIP && a.op != BCF_FARFIELD) return cudaErrorNotSupported;
-  tan_bc_face<<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(q, dq, a, mt, ndm, dT, dSt);
   return cudaGetLastError();
 }
 

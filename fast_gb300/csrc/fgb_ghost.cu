@@ -183,13 +183,6 @@ __device__ __forceinline__ void bc_face_entry(double* __restrict__ q, const BcFa
   }
 }
 
-__global__ void __launch_bounds__(128) bc_face(double* __restrict__ q, BcFaceArgs a) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.n) return;
-  const double t[3] = {a.nrm[3 * e], a.nrm[3 * e + 1], a.nrm[3 * e + 2]};
-  bc_face_entry(q, a, a.dst[e], a.src[e], t);
-}
-
 // every face-BC window of a zone in one launch (the windows write disjoint
 // ghost cells and read interior cells only)
 __global__ void __launch_bounds__(128) bc_face_cat(double* __restrict__ q, BcFaceCat c) {
@@ -242,12 +235,6 @@ __global__ void __launch_bounds__(128) bc_next(double* __restrict__ q, BcNextArg
     q[l] = r;
     for (int v = 1; v < nv; v++) q[l + v * nd] = q[q0 + v * nd] * a.k3 + q[q1 + v * nd] * a.k1 + q[q2 + v * nd] * a.k2;
   }
-}
-
-cudaError_t launch_bc_face(double* q, const BcFaceArgs& a, cudaStream_t st) {
-  if (a.n <= 0) return cudaSuccess;
-  bc_face<<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(q, a);
-  return cudaGetLastError();
 }
 
 cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st) {

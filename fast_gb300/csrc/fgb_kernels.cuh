@@ -139,7 +139,6 @@ struct BcNextArgs {            // farfield / inflow ghost ranks past the first
   double k1, k2, k3;
   int sa;
 };
-cudaError_t launch_bc_face(double* q, const BcFaceArgs& a, cudaStream_t st);
 cudaError_t launch_bc_face_cat(double* q, const BcFaceCat& c, cudaStream_t st);
 cudaError_t launch_gather_cat(double* q, int64_t nd, const GatherCat& c, int neq, cudaStream_t st);
 cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st);
@@ -189,10 +188,6 @@ cudaError_t launch_adj_bc_face_cat(const double* q, double* lam, const BcFaceCat
 cudaError_t launch_tan_bc_face_cat(const double* q, double* dq, const BcFaceCat& c, int64_t ndm,
                                    const double* dTi, const double* dTj, const double* dSt,
                                    cudaStream_t st);
-cudaError_t launch_adj_bc_face(const double* q, double* lam, const BcFaceArgs& a, const int32_t* mt,
-                               int64_t ndm, double* lamT, double* lamSt, cudaStream_t st);
-cudaError_t launch_tan_bc_face(const double* q, double* dq, const BcFaceArgs& a, const int32_t* mt,
-                               int64_t ndm, const double* dT, const double* dSt, cudaStream_t st);
 cudaError_t launch_lin_bc_next(const double* q, double* x, const BcNextArgs& a, int adjoint, int nv,
                                cudaStream_t st);
 cudaError_t launch_adj_gather(double* lam, int64_t nd, const int32_t* d_idx, const int32_t* s_idx,
