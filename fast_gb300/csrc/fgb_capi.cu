@@ -147,6 +147,10 @@ struct fgb_solver {
   // around each per-zone phase, so that the small launches overlap
   static constexpr int ZS = 8;
   bool zone_streams = true;
+  // all transfers as one list (zone ids per entry), built at the first fill
+  int32_t *tr_rz = nullptr, *tr_ri = nullptr, *tr_dz = nullptr, *tr_di = nullptr;
+  int64_t tr_n = 0;
+  size_t tr_built = 0;             // number of transfers the list holds
   cudaStream_t zst[ZS] = {};
   cudaEvent_t zev[ZS] = {};
   cudaEvent_t fork_ev = nullptr;
@@ -603,6 +607,7 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
   for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
+  cudaFree(s->tr_rz); cudaFree(s->tr_ri); cudaFree(s->tr_dz); cudaFree(s->tr_di);
   for (int k = 0; k < fgb_solver::ZS; k++) {
     if (s->zst[k]) { cudaStreamSynchronize(s->zst[k]); cudaStreamDestroy(s->zst[k]); }
     if (s->zev[k]) cudaEventDestroy(s->zev[k]);
@@ -929,38 +934,78 @@ static int build_cat(ZoneData& Z) {
 
 // The ghost fill of one level.  Transfers read donor interior cells and
 // write receiver ghost cells; a zone's BC lists read its interior and write
-// its own ghost layers; its corner averages read those.  So the fill of
-// zone m = [transfers into m, its BC lists, its corners] depends on no other
-// zone's fill: with several zones each runs on its side stream.
+// its own ghost layers; its corner averages read those.  So after the
+// transfers (one launch for all of them) the fill of zone m = [its BC
+// lists, its corners] depends on no other zone's fill: with several zones
+// each runs on its side stream.
 static int ghost_fill_zone(fgb_solver* s, int m, int level);
-static int ghost_fill(fgb_solver* s, int level) {
-  const bool par = s->zone_streams && !s->profile && s->zones.size() > 1;
-  if (!par) {
-    for (Transfer& T : s->tr) {
-      ZoneData& D = s->zones[T.dnr];
-      ZoneData& R = s->zones[T.rcv];
-      CK(launch_gather(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, T.rcv_idx, T.dnr_idx, T.n,
-                       R.z.neq, 0, 1., s->st));
-      s->launches++;
-    }
-    for (int m = 0; m < (int)s->zones.size(); m++) {
-      int rc = ghost_fill_zone(s, m, level);
+
+// the concatenated transfer list (rebuilt when transfers were added)
+static int build_transfers(fgb_solver* s) {
+  cudaFree(s->tr_rz); cudaFree(s->tr_ri); cudaFree(s->tr_dz); cudaFree(s->tr_di);
+  s->tr_rz = s->tr_ri = s->tr_dz = s->tr_di = nullptr;
+  int64_t n = 0;
+  for (Transfer& T : s->tr) n += T.n;
+  s->tr_n = n;
+  s->tr_built = s->tr.size();
+  if (n == 0) return FGB_OK;
+  const size_t B = sizeof(int32_t) * (size_t)n;
+  CK(cudaMalloc(&s->tr_rz, B)); CK(cudaMalloc(&s->tr_ri, B));
+  CK(cudaMalloc(&s->tr_dz, B)); CK(cudaMalloc(&s->tr_di, B));
+  std::vector<int32_t> rz((size_t)n), dz((size_t)n);
+  int64_t o = 0;
+  for (Transfer& T : s->tr) {
+    CK(cudaMemcpy(s->tr_ri + o, T.rcv_idx, sizeof(int32_t) * T.n, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(s->tr_di + o, T.dnr_idx, sizeof(int32_t) * T.n, cudaMemcpyDeviceToDevice));
+    for (int64_t t = 0; t < T.n; t++) { rz[(size_t)(o + t)] = T.rcv; dz[(size_t)(o + t)] = T.dnr; }
+    o += T.n;
+  }
+  CK(cudaMemcpy(s->tr_rz, rz.data(), B, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->tr_dz, dz.data(), B, cudaMemcpyHostToDevice));
+  return FGB_OK;
+}
+
+// every transfer of the solver into level `level`: one launch when the
+// zones fit the kernel's table, else one per transfer
+static int fill_transfers(fgb_solver* s, int level) {
+  if (s->tr.empty()) return FGB_OK;
+  if (s->zones.size() <= (size_t)ZT_MAX) {
+    if (s->tr_built != s->tr.size()) {
+      int rc = build_transfers(s);
       if (rc) return rc;
     }
+    ZoneLevels zl{};
+    for (size_t m = 0; m < s->zones.size(); m++) {
+      zl.q[m] = s->zones[m].lvl[level];
+      zl.nd[m] = s->zones[m].z.nd;
+      zl.neq[m] = s->zones[m].z.neq;
+    }
+    CK(launch_transfer_all(zl, s->tr_rz, s->tr_ri, s->tr_dz, s->tr_di, s->tr_n, s->st));
+    s->launches++;
     return FGB_OK;
   }
-  int rc = zone_fork(s);
+  for (Transfer& T : s->tr) {
+    ZoneData& D = s->zones[T.dnr];
+    ZoneData& R = s->zones[T.rcv];
+    CK(launch_gather(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, T.rcv_idx, T.dnr_idx, T.n,
+                     R.z.neq, 0, 1., s->st));
+    s->launches++;
+  }
+  return FGB_OK;
+}
+
+static int ghost_fill(fgb_solver* s, int level) {
+  const bool par = s->zone_streams && !s->profile && s->zones.size() > 1;
+  int rc = fill_transfers(s, level);   // transfers first (they write receiver ghosts only)
   if (rc) return rc;
+  if (!par) {
+    for (int m = 0; m < (int)s->zones.size(); m++)
+      if ((rc = ghost_fill_zone(s, m, level))) return rc;
+    return FGB_OK;
+  }
+  if ((rc = zone_fork(s))) return rc;
   for (int m = 0; m < (int)s->zones.size(); m++) {
     StreamSwap sw(s, s->zst[m % fgb_solver::ZS]);
-    ZoneData& R = s->zones[(size_t)m];
-    for (Transfer& T : s->tr) {
-      if (T.rcv != m) continue;
-      ZoneData& D = s->zones[T.dnr];
-      CK(launch_gather(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, T.rcv_idx, T.dnr_idx, T.n,
-                       R.z.neq, 0, 1., s->st));
-      s->launches++;
-    }
     if ((rc = ghost_fill_zone(s, m, level))) return rc;
   }
   return zone_join(s);

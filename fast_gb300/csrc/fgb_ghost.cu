@@ -206,6 +206,26 @@ __global__ void __launch_bounds__(256) gather_cat(double* __restrict__ q, int64_
   }
 }
 
+__global__ void __launch_bounds__(256) transfer_all(ZoneLevels zl, const int32_t* __restrict__ rz,
+                                                    const int32_t* __restrict__ ri,
+                                                    const int32_t* __restrict__ dz,
+                                                    const int32_t* __restrict__ di, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int r = rz[t], d = dz[t];
+  double* dst = zl.q[r] + ri[t];
+  const double* src = zl.q[d] + di[t];
+  const int64_t ndr = zl.nd[r], ndd = zl.nd[d];
+  for (int v = 0; v < zl.neq[r]; v++) dst[v * ndr] = src[v * ndd];
+}
+
+cudaError_t launch_transfer_all(const ZoneLevels& zl, const int32_t* rz, const int32_t* ri,
+                                const int32_t* dz, const int32_t* di, int64_t n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  transfer_all<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(zl, rz, ri, dz, di, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_bc_face_cat(double* q, const BcFaceCat& c, cudaStream_t st) {
   if (c.n <= 0) return cudaSuccess;
   bc_face_cat<<<(unsigned)((c.n + 127) / 128), 128, 0, st>>>(q, c);

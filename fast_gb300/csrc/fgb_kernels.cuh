@@ -140,6 +140,13 @@ struct BcNextArgs {            // farfield / inflow ghost ranks past the first
   int sa;
 };
 cudaError_t launch_bc_face_cat(double* q, const BcFaceCat& c, cudaStream_t st);
+// Every 1-to-1 transfer of a solver in one launch: entry t copies cell
+// di[t] of zone dz[t] into ghost cell ri[t] of zone rz[t] (all variables);
+// the zones' current level pointers travel as a kernel parameter
+constexpr int ZT_MAX = 64;
+struct ZoneLevels { double* q[ZT_MAX]; int64_t nd[ZT_MAX]; int neq[ZT_MAX]; };
+cudaError_t launch_transfer_all(const ZoneLevels& zl, const int32_t* rz, const int32_t* ri,
+                                const int32_t* dz, const int32_t* di, int64_t n, cudaStream_t st);
 cudaError_t launch_gather_cat(double* q, int64_t nd, const GatherCat& c, int neq, cudaStream_t st);
 cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st);
 cudaError_t launch_coins(double* q, int64_t nd, const int32_t* dst, const int32_t* a,
