@@ -723,9 +723,12 @@ __device__ __forceinline__ void wallslip_lin(const double* __restrict__ q, int64
   wallslip_eval<10>(q, nd, l, ia, t0v, t1v, rgp, gam2, -1, J);
 }
 
-// the Roe part of the wall correction: the face adjoint with mu = sens_c lamD(l0)
+// the Roe part of the wall correction: the face adjoint with mu = sens_c
+// lamD(l0); the wall face is a face of the stage's face tape (direction D,
+// face (ii, jj) of its high-side cell l), read when a tape is given
 template <int D>
 __global__ void __launch_bounds__(128) adj_wall_roe(Zone z, const double* __restrict__ q,
+                                                    const double* __restrict__ tape,
                                                     const double* __restrict__ lamD,
                                                     double* __restrict__ lamQ,
                                                     double* __restrict__ lamT, WallCorrArgs a) {
@@ -735,7 +738,13 @@ __global__ void __launch_bounds__(128) adj_wall_roe(Zone z, const double* __rest
   double mu[5];
 #pragma unroll
   for (int v = 0; v < 5; v++) mu[v] = lamD[l0 + v * nd] * a.sens_c;
-  face_adjoint<D>(z, q, l, lt, mu, lamQ, lamT);
+  if (tape) {
+    const int64_t NI = z.ni + (D == 0), NJ = z.nj + (D == 1);
+    const int64_t ii = l % z.nip - z.ng, jj = l / z.nip - z.ng;
+    face_adjoint<D, true>(z, q, l, lt, mu, lamQ, lamT, tape + ii + NI * jj, NI * NJ);
+  } else {
+    face_adjoint<D>(z, q, l, lt, mu, lamQ, lamT);
+  }
 }
 
 // the wall-flux part: sixteen lanes per face, lane k < 10 the column of input k
@@ -800,16 +809,18 @@ __global__ void __launch_bounds__(128) tan_wall(Zone z, const double* __restrict
   }
 }
 
-cudaError_t launch_adj_wall(const Zone& z, const double* q, const double* lamD, double* lamQ,
+cudaError_t launch_adj_wall(const Zone& z, const double* q, const double* tape,
+                            const double* lamD, double* lamQ,
                             double* lamTi, double* lamTj, const WallCorrArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
   if (z.typ != Z2D || !a.slip || a.dir > 1) return cudaErrorNotSupported;
   const unsigned g = (unsigned)((a.n + 127) / 128), g16 = (unsigned)((16 * a.n + 127) / 128);
   if (a.dir == 0) {
-    adj_wall_roe<0><<<g, 128, 0, st>>>(z, q, lamD, lamQ, lamTi, a);
+    adj_wall_roe<0><<<g, 128, 0, st>>>(z, q, tape, lamD, lamQ, lamTi, a);
     adj_wall_flux<0><<<g16, 128, 0, st>>>(z, q, lamD, lamQ, lamTi, a);
   } else {
-    adj_wall_roe<1><<<g, 128, 0, st>>>(z, q, lamD, lamQ, lamTj, a);
+    adj_wall_roe<1><<<g, 128, 0, st>>>(z, q, tape ? tape + FACE_TAPE * (z.ni + 1) * z.nj : nullptr,
+                                       lamD, lamQ, lamTj, a);
     adj_wall_flux<1><<<g16, 128, 0, st>>>(z, q, lamD, lamQ, lamTj, a);
   }
   return cudaGetLastError();

@@ -1649,7 +1649,8 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
           CK(launch_adj_faces(z, A.W + i * nq, A.tape + i * tstride, A.lamD, A.lamIn, A.lamTi,
                               A.lamTj, s->st));
           for (WallCorrList& w : Z.walls)
-            CK(launch_adj_wall(z, A.W + i * nq, A.lamD, A.lamIn, A.lamTi, A.lamTj, wall_args(Z, w), s->st));
+            CK(launch_adj_wall(z, A.W + i * nq, A.tape + i * tstride, A.lamD, A.lamIn, A.lamTi,
+                               A.lamTj, wall_args(Z, w), s->st));
         }
         // D_st = coefH_st D_{st-1} + R: the earlier residual's adjoint
         std::swap(A.lamW, A.lamIn);

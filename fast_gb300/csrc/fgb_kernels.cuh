@@ -186,7 +186,8 @@ cudaError_t launch_tan_balance(const Zone& z, double coefH, int zero, const doub
 cudaError_t launch_tan_apply(const Zone& z, const double* q, const double* D, double coefW,
                              const double* dIn, const double* dD, const double* dVol, double* dOut,
                              cudaStream_t st);
-cudaError_t launch_adj_wall(const Zone& z, const double* q, const double* lamD, double* lamQ,
+cudaError_t launch_adj_wall(const Zone& z, const double* q, const double* tape,
+                            const double* lamD, double* lamQ,
                             double* lamTi, double* lamTj, const WallCorrArgs& a, cudaStream_t st);
 cudaError_t launch_tan_wall(const Zone& z, const double* q, const double* dq, const double* dTi,
                             const double* dTj, double* dD, const WallCorrArgs& a, cudaStream_t st);
