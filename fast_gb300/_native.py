@@ -39,6 +39,7 @@ SIGNATURES = {
     "fgb_residual_norms_noalloc": ([_P, C.c_int, _P], C.c_int),
     "fgb_set_bc_state": ([_P, C.c_int, _DP], C.c_int),
     "fgb_cfl": ([_P, C.c_int, _DP], C.c_int),
+    "fgb_pin_host": ([_P, C.c_void_p, C.c_int64], C.c_int),
     "fgb_adjoint_forward": ([_P, C.c_int, C.c_int, C.c_int], C.c_int),
     "fgb_adjoint_backward": ([_P, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP], C.c_int),
     "fgb_tangent": ([_P, C.c_int, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP], C.c_int),
@@ -101,11 +102,20 @@ class Solver:
         _check(self._lib.fgb_create(int(device), C.byref(h)))
         self._h = h
         self.zones = []  # (param_int, param_real) per zone
+        self._pinned = []  # host arrays page-locked for this solver (kept alive)
 
     def close(self):
         if getattr(self, "_h", None):
             self._lib.fgb_destroy(self._h)
             self._h = None
+        self._pinned = []
+
+    def pin(self, arr: np.ndarray):
+        """Page-lock the host array (fgb_pin_host) for the state copies;
+        the solver keeps it alive until close()."""
+        assert arr.flags.c_contiguous
+        _check(self._lib.fgb_pin_host(self._h, C.c_void_p(arr.ctypes.data), arr.nbytes))
+        self._pinned.append(arr)
 
     def __del__(self):
         try:

@@ -147,6 +147,7 @@ struct fgb_solver {
   // around each per-zone phase, so that the small launches overlap
   static constexpr int ZS = 8;
   bool zone_streams = true;
+  std::vector<void*> pinned;       // host buffers page-locked by fgb_pin_host
   // all transfers as one list (zone ids per entry), built at the first fill
   int32_t *tr_rz = nullptr, *tr_ri = nullptr, *tr_dz = nullptr, *tr_di = nullptr;
   int64_t tr_n = 0;
@@ -613,6 +614,7 @@ int fgb_destroy(fgb_solver* s) {
     if (s->zev[k]) cudaEventDestroy(s->zev[k]);
   }
   if (s->fork_ev) cudaEventDestroy(s->fork_ev);
+  for (void* h : s->pinned) cudaHostUnregister(h);
   for (LuGroupData& g : s->lu_groups) {
     cudaFree(g.cells); cudaFree(g.zid); cudaFree(g.plane); cudaFree(g.nbl); cudaFree(g.nbu);
     cudaFree(g.work); cudaFree(g.tab_dev); cudaFreeHost(g.tab_host);
@@ -1494,6 +1496,21 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       Z.lvl[2] = save;
     }
   }
+  return FGB_OK;
+}
+
+int fgb_pin_host(fgb_solver* s, void* ptr, int64_t bytes) {
+  if (!s || !ptr || bytes <= 0) return fail(FGB_ERR_ARG, "bad host buffer");
+  CK(cudaSetDevice(s->device));
+  for (void* h : s->pinned)
+    if (h == ptr) return FGB_OK;
+  const cudaError_t e = cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault);
+  if (e == cudaErrorHostMemoryAlreadyRegistered) {   // page-locked by another owner: keep it so
+    cudaGetLastError();
+    return FGB_OK;
+  }
+  CK(e);
+  s->pinned.push_back(ptr);
   return FGB_OK;
 }
 

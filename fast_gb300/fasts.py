@@ -162,6 +162,13 @@ def warmup(t, tc=None, graph=None, infos_ale=None, Adjoint=False, tmy=None, list
     solver.set_option("first_it", FIRST_IT)
     HOOK = {"solver": solver, "nssiter": nssiter, "FIRST_IT": FIRST_IT,
             "gpu_resident": bool(gpu_resident), "zones": zones, "device_valid": False}
+    # the tree's time levels are what _compute copies in and out: page-lock
+    # them so that those copies are DMA transfers
+    for z in zones:
+        for suf in ("", "_M1", "_P1"):
+            arr = FastC.compactArray(z, suf).reshape(-1)
+            if arr.flags.c_contiguous and arr.nbytes > 0:
+                solver.pin(arr)
     _upload(t)
     for lvl in (0, 1):
         solver.apply_bc(lvl)

@@ -125,6 +125,12 @@ int fgb_residuals(fgb_solver* s, int zone, double* out, int64_t n, int* nit_out)
  * (the convective one for Euler).  Waits for the solver stream. */
 int fgb_cfl(fgb_solver* s, int zone, double* out);
 
+/* Page-lock a host buffer (cudaHostRegister) that fgb_upload_state /
+ * fgb_download_state copy, so that those copies run as DMA at the link's
+ * bandwidth.  The buffer must stay allocated until fgb_destroy, which
+ * unregisters it.  Registering the same pointer twice is a no-op. */
+int fgb_pin_host(fgb_solver* s, void* ptr, int64_t bytes);
+
 /* Exterior state (conservative ro, ro u, ro v, ro w, ro E) of every farfield
  * / inflow / outflow BC of a zone, replacing the free stream (BCzone.cpp
  * DEFAULT_STATE, or the nbdata = 21 per-BC state). */
