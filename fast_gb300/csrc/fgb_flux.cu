@@ -1025,6 +1025,9 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
     if (z.kflu == AUSM && z.slope == O3)
       return cart ? launch_faces_t<Z3DCART, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z3DFULL, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == SENSEUR && z.slope == O3)   // SENSOR/*/fluFaceSA_o3_*: the AUSM form, sensor u / tdu
+      return cart ? launch_faces_t<Z3DCART, SENSEUR, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z3DFULL, SENSEUR, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
     if (z.kflu == ROE && z.slope == O1)
       return cart ? launch_faces_t<Z3DCART, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z3DFULL, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st);

@@ -33,7 +33,8 @@ def _interior(pi, q, nv=6):
 
 
 @pytest.mark.parametrize("temporal,scheme", [("explicit", "ausmpred"), ("implicit", "ausmpred"),
-                                             ("explicit", "roe"), ("implicit", "roe")])
+                                             ("explicit", "roe"), ("implicit", "roe"),
+                                             ("explicit", "senseur")])
 def test_sa_free_stream_curvilinear(oracle_mod, temporal, scheme):
     numb = ({"temporal_scheme": "explicit", "ss_iteration": 1, "modulo_verif": 1000}
             if temporal == "explicit" else None)
