@@ -645,18 +645,14 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   const std::vector<int64_t>& p = Z.pi;
   if (p[ITYPZONE] != Z3DCART && p[ITYPZONE] != Z3DFULL && p[ITYPZONE] != Z2D)
     return fail(FGB_ERR_ARG, "zone type " + std::to_string(p[ITYPZONE]) + " not supported on the GPU path");
-  if (p[ITYPZONE] == Z2D && p[KFLUDOM] == SENSEUR)
-    return fail(FGB_ERR_ARG, "2-d zones are supported with the Roe and AUSM+(P) schemes on the "
-                             "GPU path");
   if (p[NEQ] != (p[IFLOW] == 3 ? 6 : 5))
     return fail(FGB_ERR_ARG, "NEQ must be 5 (Euler, laminar) or 6 (Spalart-Allmaras)");
   if (p[IFLOW] == 3) {
-    const bool ausm_o3 = (p[KFLUDOM] == AUSM || (p[KFLUDOM] == SENSEUR && p[ITYPZONE] != Z2D)) &&
-                         p[SLOPE] == O3;
+    const bool ausm_o3 = (p[KFLUDOM] == AUSM || p[KFLUDOM] == SENSEUR) && p[SLOPE] == O3;
     const bool roe = p[KFLUDOM] == ROE && (p[SLOPE] == O1 || p[SLOPE] == O3 || p[SLOPE] == MINMOD);
     if (!(ausm_o3 || roe) || p[ILES] != 0 || p[SA_INT] != 0)
       return fail(FGB_ERR_ARG, "Spalart-Allmaras is supported with the AUSM+(P) o3, senseur o3 "
-                               "(3-d) or Roe o1 / o3 / minmod schemes (SA, not ZDES) on the GPU path");
+                               "or Roe o1 / o3 / minmod schemes (SA, not ZDES) on the GPU path");
     if (p[ITYPCP] <= 1 && p[NEQ_COE] < 6)
       return fail(FGB_ERR_ARG, "implicit Spalart-Allmaras needs NEQ_COE = 6");
   }

@@ -605,7 +605,8 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
       roe_full(z, qm, qp, tcx, tcy, 0., s, F);
       if (NV == 6) F[NV - 1] = roe_sa_flux<D, false, true>(z, q, l, l - inc, tcx, tcy, 0., s);
     } else {
-      ausm_face<D, false, false, NV>(z, qm, qp, q[l + 4 * nd], tcx, tcy, 0., s, F);
+      ausm_face<D, false, KF == SENSEUR, NV>(z, qm, qp, q[l + 4 * nd], tcx, tcy, 0., s, F,
+                                            KF == SENSEUR ? z.wig[l + D * nd] : 0.);
     }
     F[3] = 0.;
     if (VISC) visc_2d<D, NV>(z, q, xmut, l, lt, tcx, tcy, F);
@@ -1014,6 +1015,7 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
   const bool visc = z.iflow >= 2;
   if (z.neq == 6 && z.typ == Z2D) {   // Spalart-Allmaras on 2-d zones
     if (z.kflu == AUSM && z.slope == O3) return launch_faces_t<Z2D, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == SENSEUR && z.slope == O3) return launch_faces_t<Z2D, SENSEUR, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
     if (z.kflu == ROE && z.slope == O1) return launch_faces_t<Z2D, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
     if (z.kflu == ROE && z.slope == O3) return launch_faces_t<Z2D, ROE, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
     if (z.kflu == ROE && z.slope == MINMOD) return launch_faces_t<Z2D, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
@@ -1084,6 +1086,9 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
     } else if (z.kflu == AUSM && z.slope == O3) {
       return visc ? launch_faces_t<Z2D, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z2D, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+    } else if (z.kflu == SENSEUR && z.slope == O3) {
+      return visc ? launch_faces_t<Z2D, SENSEUR, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
+                  : launch_faces_t<Z2D, SENSEUR, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
     }
   }
   return cudaErrorNotSupported;
@@ -1198,7 +1203,7 @@ cudaError_t launch_wall_corr(const Zone& z, const double* q, double* drodm, cons
 // planes are included): 1 if, for some variable, both slope products
 // (q_{l-1}-q_{l-2})(q_l-q_{l-1}) and (q_l-q_{l-1})(q_{l+1}-q_l) are
 // negative (min of sign sums < -1e-12), else 0.
-template <int D>
+template <int D, bool TWO_D = false>
 __global__ void __launch_bounds__(128) wiggle(Zone z, const double* __restrict__ q,
                                               double* __restrict__ wig) {
   const int64_t NI = z.ni + (D == 0), NJ = z.nj + (D == 1), NK = z.nk + (D == 2);
@@ -1210,6 +1215,7 @@ __global__ void __launch_bounds__(128) wiggle(Zone z, const double* __restrict__
   double test = 0.;
 #pragma unroll
   for (int v = 0; v < 5; v++) {
+    if (TWO_D && v == 3) continue;   // wiggle2d_{i,j}.for: min(f1, f2, f3, f5)
     const double* Q = q + v * nd;
     const double qm = (Q[nm] - Q[nm2]) * (Q[l] - Q[nm]);
     const double qp = (Q[l] - Q[nm]) * (Q[np] - Q[l]);
@@ -1223,6 +1229,11 @@ cudaError_t launch_wiggle(const Zone& z, const double* q, double* wig, cudaStrea
   const int B = 128;
   const int64_t nfi = (z.ni + 1) * z.nj * z.nk, nfj = z.ni * (z.nj + 1) * z.nk,
                 nfk = z.ni * z.nj * (z.nk + 1);
+  if (z.typ == Z2D) {
+    wiggle<0, true><<<(unsigned)((nfi + B - 1) / B), B, 0, st>>>(z, q, wig);
+    wiggle<1, true><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, wig);
+    return cudaGetLastError();
+  }
   wiggle<0><<<(unsigned)((nfi + B - 1) / B), B, 0, st>>>(z, q, wig);
   wiggle<1><<<(unsigned)((nfj + B - 1) / B), B, 0, st>>>(z, q, wig);
   wiggle<2><<<(unsigned)((nfk + B - 1) / B), B, 0, st>>>(z, q, wig);

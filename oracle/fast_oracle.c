@@ -1104,8 +1104,10 @@ void or_correct_flux(const int64_t* pi, const double* pr, const double* rop, dou
  * the imax+1 / jmax+1 / kmax+1 planes of the last faces. */
 static double wig_face(const int64_t* pi, const double* rop, int64_t l, int64_t inc) {
   const int64_t nd = pi[NDIMDX], nm = l - inc, nm2 = l - 2 * inc, np = l + inc;
+  const int two_d = pi[ITYPZONE] == 3;   /* wiggle2d_{i,j}.for: min(f1, f2, f3, f5) */
   double test = 0.;
   for (int v = 0; v < 5; v++) {
+    if (two_d && v == 3) continue;
     const double* q = rop + v * nd;
     double qm = (q[nm] - q[nm2]) * (q[l] - q[nm]);
     double qp = (q[l] - q[nm]) * (q[np] - q[l]);
@@ -1120,7 +1122,8 @@ void or_wiggle(const int64_t* pi, const int64_t* ind, const double* rop, double*
   const int64_t inc[3] = {1, pi[NIJK], pi[NIJK] * pi[NIJK + 1]};
   const int64_t hi[3] = {ind[1], ind[3], ind[5]};
   const int64_t corr[3] = {ind[1] == pi[IJKV], ind[3] == pi[IJKV + 1], ind[5] == pi[IJKV + 2]};
-  for (int d = 0; d < 3; d++)
+  const int ndir = pi[ITYPZONE] == 3 ? 2 : 3;   /* 2-d: i and j faces */
+  for (int d = 0; d < ndir; d++)
     for (int64_t k = ind[4]; k <= ind[5] + (d == 2 ? corr[2] : 0); k++)
       for (int64_t j = ind[2]; j <= ind[3] + (d == 1 ? corr[1] : 0); j++)
         for (int64_t i = ind[0]; i <= ind[1] + (d == 0 ? corr[0] : 0); i++) {

@@ -343,7 +343,7 @@ def test_roe_wall_flux_correction_implicit(oracle_mod):
 
 
 @pytest.mark.parametrize("scheme,slope,wavy", [("roe_min", "minmod", 0.0), ("roe", "o3", 0.3),
-                                               ("ausmpred", "o3", 0.3)])
+                                               ("ausmpred", "o3", 0.3), ("senseur", "o3", 0.3)])
 def test_2d_explicit(oracle_mod, scheme, slope, wavy):
     """2-d zones (ITYPZONE 3): i and j faces only, no w."""
     t = cases.isentropic_vortex(n=(24, 20, 1), two_d=True, wavy=wavy,
@@ -357,7 +357,8 @@ def test_2d_explicit(oracle_mod, scheme, slope, wavy):
     s.close()
 
 
-@pytest.mark.parametrize("scheme,slope,wavy", [("ausmpred", "o3", 0.0), ("roe_min", "minmod", 0.3)])
+@pytest.mark.parametrize("scheme,slope,wavy", [("ausmpred", "o3", 0.0), ("roe_min", "minmod", 0.3),
+                                               ("senseur", "o3", 0.3)])
 def test_2d_implicit(oracle_mod, scheme, slope, wavy):
     """LU-SGS on 2-d zones (lu_{i,j}_2d.for, 2-d Newton update)."""
     t = cases.isentropic_vortex(n=(20, 16, 1), two_d=True, wavy=wavy,
@@ -495,14 +496,14 @@ def test_spalart_allmaras_mixed_precision(oracle_mod):
 
 
 def test_spalart_allmaras_refusals():
-    """Unsupported SA combinations are reported, never run: senseur on a 2-d
-    zone, and a compute before the wall distance is given."""
+    """Unsupported SA combinations are reported, never run: AUSM+(P) with a
+    minmod slope, and a compute before the wall distance is given."""
     from fast_gb300._native import Solver, FastGB300Error
-    t = cases.bc_box(n=(8, 8, 1), two_d=True, model="NSTurbulent", scheme="senseur",
+    t = cases.bc_box(n=(8, 8, 6), model="NSTurbulent", scheme="ausmpred", slope="minmod",
                      temporal="explicit")
     zd = fasts.zone_data(t, fasts.prepare(t))
     s = Solver(0)
-    with pytest.raises(FastGB300Error, match="2-d zones"):
+    with pytest.raises(FastGB300Error, match="Spalart-Allmaras is supported"):
         s.add_zone(zd[0]["pi"], zd[0]["pr"], zd[0]["ti"], zd[0]["tj"], zd[0]["tk"], zd[0]["vol"])
     t = cases.bc_box(n=(8, 8, 6), model="NSTurbulent", temporal="explicit")
     zd = fasts.zone_data(t, fasts.prepare(t))

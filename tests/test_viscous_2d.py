@@ -62,7 +62,7 @@ def test_2d_laminar_equals_extruded_3d(oracle_mod, scheme, slope, wall, model):
 @pytest.mark.parametrize("scheme,slope,temporal,wavy", [
     ("ausmpred", "o3", "explicit", 0.3), ("roe", "o3", "explicit", 0.3),
     ("roe_min", "minmod", "implicit", 0.3), ("ausmpred", "o3", "implicit", 0.0),
-    ("roe", "o1", "implicit", 0.3)])
+    ("roe", "o1", "implicit", 0.3), ("senseur", "o3", "explicit", 0.3)])
 def test_2d_laminar_gpu_parity(oracle_mod, scheme, slope, temporal, wavy):
     from test_gpu_parity import _check_levels, _pair
     t = cases.bc_box(n=(16, 12, 1), two_d=True, wall="BCWallViscous", model="NSLaminar",
@@ -85,7 +85,8 @@ def test_2d_laminar_gpu_parity(oracle_mod, scheme, slope, temporal, wavy):
 @pytest.mark.gpu
 @pytest.mark.parametrize("scheme,slope,temporal,wavy", [
     ("ausmpred", "o3", "explicit", 0.3), ("roe", "o3", "explicit", 0.0),
-    ("ausmpred", "o3", "implicit", 0.3), ("roe_min", "minmod", "implicit", 0.3)])
+    ("ausmpred", "o3", "implicit", 0.3), ("roe_min", "minmod", "implicit", 0.3),
+    ("senseur", "o3", "implicit", 0.3)])
 def test_2d_spalart_allmaras_gpu_parity(oracle_mod, scheme, slope, temporal, wavy):
     from test_gpu_parity import _check_levels, _pair
     t = cases.bc_box(n=(16, 12, 1), two_d=True, wall="BCWallViscous", model="NSTurbulent",
