@@ -71,7 +71,7 @@ struct ZoneData {
   double *drodm = nullptr, *coe = nullptr, *xmut = nullptr, *rdm = nullptr;
   double *ti = nullptr, *tj = nullptr, *tk = nullptr, *vol = nullptr;
   double *Fi = nullptr, *Fj = nullptr, *Fk = nullptr;
-  double* wig = nullptr;            // senseur wiggle flags (KFLUDOM = 2)
+  double* wig = nullptr;            // senseur wiggle flags (KFLUDOM = 2), o3sc weights
   double* dist = nullptr;           // wall distance (Spalart-Allmaras)
   // the zone's BC lists concatenated by kind (one launch per kind)
   GatherCat cat0{};
@@ -697,9 +697,12 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   CK(dev_upload(&Z.tk, htk)); CK(dev_upload(&Z.vol, hvol));
   Z.z.ti = Z.ti; Z.z.tj = Z.tj; Z.z.tk = Z.tk; Z.z.vol = Z.vol;
   int64_t ni = Z.z.ni, nj = Z.z.nj, nk = Z.z.nk;
-  if (p[KFLUDOM] == SENSEUR) {
-    CK(cudaMalloc(&Z.wig, sizeof(double) * 3 * nd));
-    CK(cudaMemset(Z.wig, 0, sizeof(double) * 3 * nd));
+  // senseur wiggle flags (3 x NDIMDX), then the o3sc shock-sensor weights
+  // (3 x NDIMDX), the layout of FastC's createWorkArrays__ wig array
+  const int64_t nwig = (p[KFLUDOM] == SENSEUR ? 3 : 0) + (p[SLOPE] == O3SC ? 3 : 0);
+  if (nwig > 0) {
+    CK(cudaMalloc(&Z.wig, sizeof(double) * nwig * nd));
+    CK(cudaMemset(Z.wig, 0, sizeof(double) * nwig * nd));
   }
   Z.z.wig = Z.wig;
   Z.z.opt0 = (double)p[SENSORTYPE];
@@ -1389,6 +1392,11 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             CK(launch_cfl(z, ssiter, Z.xmut, Z.cfl_part, Z.cfl, s->st));
             s->launches += 2;
           }
+        }
+        if (z.slope == O3SC) {  // src_term.for:246-255: o3sc sensor on every sub-step
+          ProfScope ps(s, "shock_sensor");
+          CK(launch_shock_sensor(z, ssiter, Z.wig, s->st));
+          s->launches++;
         }
         if (nstep == 1 && z.kflu == SENSEUR) {  // src_term.for:257-266
           ProfScope ps(s, "wiggle");

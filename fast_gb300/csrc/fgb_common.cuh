@@ -33,7 +33,7 @@ enum PR : int {
 enum PI_SA : int { SA_LOW_RE = 130, SA_ROT_CORR = 131 };
 enum ZoneType : int { Z3DFULL = 0, Z3DHOMO = 1, Z3DCART = 2, Z2D = 3 };
 enum Scheme : int { AUSM = 1, SENSEUR = 2, ROE = 5 };
-enum Slope : int { O1 = 1, O3 = 2, MINMOD = 3, VANALBADA = 8 };   // 8: not a FastS slope
+enum Slope : int { O1 = 1, O3 = 2, MINMOD = 3, O3SC = 6, VANALBADA = 8 };   // 8: not a FastS slope
 
 // Everything a kernel needs about one zone; passed by value.
 struct Zone {

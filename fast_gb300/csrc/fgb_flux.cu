@@ -21,9 +21,11 @@
 namespace fgb {
 
 // ---------------------------------------------------------------- slopes
-// Slope/o1_slope_var.for, o3_slope_var.for, minmod_slope_var.for.
-// a = q(l-2*inc), b = q(l-inc), c = q(l), d = q(l+inc); qm = right state of
-// the face (cell l side), qp = left state.
+// Slope/o1_slope_var.for, o3_slope_var.for, o3sc_slope_var.for,
+// minmod_slope_var.for.  a = q(l-2*inc), b = q(l-inc), c = q(l),
+// d = q(l+inc); qm = right state of the face (cell l side), qp = left state.
+// roff: minmod's low-temperature cut-off, or o3sc's shock-sensor weight of
+// the face (the o3 states blended with the first-order ones).
 // van Albada's smooth averaged slope of the differences x, y (VANALBADA;
 // differentiable, for the adjoint): ((y^2 + e) x + (x^2 + e) y) / (x^2 + y^2 + 2e)
 __device__ __forceinline__ double vanalbada(double x, double y) {
@@ -40,9 +42,13 @@ __device__ __forceinline__ void reconstruct(const Zone& z, double a, double b, d
   } else if (SL == O1) {
     qm = c;
     qp = b;
-  } else if (SL == O3) {
+  } else if (SL == O3 || SL == O3SC) {
     qm = z.c4 * c + z.c5 * b + z.c6 * d;
     qp = z.c4 * b + z.c6 * a + z.c5 * c;
+    if (SL == O3SC) {
+      qm = c * (1. - roff) + qm * roff;
+      qp = b * (1. - roff) + qp * roff;
+    }
   } else {  // minmod with the low-temperature cut-off roff
     double delm = c - b, delp = d - c, delq = b - a;
     double sm = fsignF(1., delm);
@@ -583,6 +589,7 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
   double qm[NV], qp[NV];
   double roff = 0.;
   if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
+  if (SL == O3SC) roff = z.wig[l + D * nd + (KF == SENSEUR ? 3 * nd : 0)];
 #pragma unroll
   for (int v = 0; v < NV; v++) {
     if (TYP == Z2D && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }   // 2-d: no w slope
@@ -1041,6 +1048,20 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
                   : launch_faces_t<Z3DFULL, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
     return cudaErrorNotSupported;
   }
+  if (z.slope == O3SC && z.neq == 5 && (z.kflu == ROE || z.kflu == AUSM)) {
+    // *_o3sc_*: the o3 slope blended by the shock sensor, Euler / laminar
+#define FGB_O3SC(TYP)                                                                           \
+  return z.kflu == ROE                                                                          \
+             ? (visc ? launch_faces_t<TYP, ROE, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)          \
+                     : launch_faces_t<TYP, ROE, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st))        \
+             : (visc ? launch_faces_t<TYP, AUSM, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)         \
+                     : launch_faces_t<TYP, AUSM, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st))
+    if (z.typ == Z3DCART) FGB_O3SC(Z3DCART);
+    if (z.typ == Z3DFULL) FGB_O3SC(Z3DFULL);
+    if (z.typ == Z2D) FGB_O3SC(Z2D);
+#undef FGB_O3SC
+    return cudaErrorNotSupported;
+  }
   if (z.typ == Z3DCART) {
     if (z.kflu == ROE) {
       if (z.slope == O1) return visc ? launch_faces_t<Z3DCART, ROE, O1, true>(z, q, xmut, Fi, Fj, Fk, st)
@@ -1110,6 +1131,7 @@ __global__ void __launch_bounds__(128) wall_corr(Zone z, const double* __restric
   double qm[5], qp[5];
   double roff = 0.;
   if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
+  if (SL == O3SC) roff = z.wig[l + D * nd];
 #pragma unroll
   for (int v = 0; v < 5; v++) {
     if (TYP == Z2D && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
@@ -1175,6 +1197,7 @@ static void wall_corr_sl(const Zone& z, const double* q, double* drodm, const Wa
   const unsigned g = (unsigned)((a.n + 127) / 128);
   if (z.slope == O1) wall_corr<D, TYP, O1><<<g, 128, 0, st>>>(z, q, drodm, a);
   else if (z.slope == O3) wall_corr<D, TYP, O3><<<g, 128, 0, st>>>(z, q, drodm, a);
+  else if (z.slope == O3SC) wall_corr<D, TYP, O3SC><<<g, 128, 0, st>>>(z, q, drodm, a);
   else if (z.slope == VANALBADA) wall_corr<D, TYP, VANALBADA><<<g, 128, 0, st>>>(z, q, drodm, a);
   else wall_corr<D, TYP, MINMOD><<<g, 128, 0, st>>>(z, q, drodm, a);
 }
@@ -1194,6 +1217,148 @@ cudaError_t launch_wall_corr(const Zone& z, const double* q, double* drodm, cons
   if (a.dir == 0) cart ? wall_corr_sl<0, Z3DCART>(z, q, drodm, a, st) : wall_corr_sl<0, Z3DFULL>(z, q, drodm, a, st);
   else if (a.dir == 1) cart ? wall_corr_sl<1, Z3DCART>(z, q, drodm, a, st) : wall_corr_sl<1, Z3DFULL>(z, q, drodm, a, st);
   else cart ? wall_corr_sl<2, Z3DCART>(z, q, drodm, a, st) : wall_corr_sl<2, Z3DFULL>(z, q, drodm, a, st);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------- shock sensor
+// SENSOR/sciacovelli.for + shock_sensor.for: weights of the o3sc slope.
+// One thread per cell of the box [1, ni+1] x [1, nj+1] x [1, nk+1]; a cell
+// beyond the interior in direction d writes only its d-weight (the faces
+// that close the zone, as the reference's loopPlan corrections), and cells
+// beyond it in two directions write nothing.  Per cell the velocity
+// divergence and squared vorticity from face-averaged velocities
+// (SA/div_rot_{3dcart,3dfull,2d}.for) and the face-metric norms tc_d
+// (SA/metric_{3dfull,2d}.for), then, per direction,
+//   M = (1 - tanh(2.5 + 10 div / (tc_d c))) / 2,
+//   J = |p_- - 2 p + p_+| / |p_- + 2 p + p_+|   (p = rho T),
+//   wig = 1 - min(2 div^2 / (div^2 + rot + 1e-15) * J * M, 1),
+// at wig[l + d*nd + shift], shift = 3*nd for the senseur scheme (its wiggle
+// flags hold the first three).
+template <int TYP>
+__global__ void __launch_bounds__(128) shock_sensor(Zone z, const double* __restrict__ q,
+                                                    double* __restrict__ wig) {
+  const int64_t NI = z.ni + 1, NJ = z.nj + 1, NK = z.nk + (TYP == Z2D ? 0 : 1);
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= NI * NJ * NK) return;
+  const int64_t ii = f % NI, r = f / NI, jj = r % NJ, kk = r / NJ;
+  const int o0 = ii == z.ni, o1 = jj == z.nj, o2 = (TYP != Z2D) && kk == z.nk;
+  if (o0 + o1 + o2 > 1) return;
+  const int64_t nd = z.nd, l = inddm(z, ii + 1, jj + 1, kk + 1);
+  const int64_t incj = z.inc[1], inck = z.inc[2];
+  const int64_t l1 = l + 1, l2 = l - 1, l3 = l + incj, l4 = l - incj, l5 = l + inck, l6 = l - inck;
+  double u1[3], u2[3], u3[3], u4[3], u5[3], u6[3];
+#pragma unroll
+  for (int m = 0; m < (TYP == Z2D ? 2 : 3); m++) {
+    const double* Q = q + (m + 1) * nd;
+    const double c0 = Q[l];
+    u1[m] = c0 + Q[l2]; u2[m] = c0 + Q[l3]; u3[m] = c0 + Q[l1]; u4[m] = c0 + Q[l4];
+    if (TYP != Z2D) { u5[m] = c0 + Q[l5]; u6[m] = c0 + Q[l6]; }
+  }
+  double div, rot, tc[3], dudx, rotx, roty, rotz;
+  if (TYP == Z3DCART) {
+    const double tix = z.tcx, tjy = z.tcy, tkz = z.tcz, xvol = z.volinv;
+    tc[0] = z.si; tc[1] = z.sj; tc[2] = z.sk;
+    dudx = (u3[0] - u1[0]) * tix;
+    rotz = -(u2[0] - u4[0]) * tjy;
+    roty = (u5[0] - u6[0]) * tkz;
+    div = dudx * xvol;
+    dudx = (u3[1] - u1[1]) * tix;
+    rotz = (rotz + dudx) * xvol;
+    dudx = (u2[1] - u4[1]) * tjy;
+    div = div + dudx * xvol;
+    dudx = (u5[1] - u6[1]) * tkz;
+    rotx = -dudx;
+    dudx = (u3[2] - u1[2]) * tix;
+    roty = (roty - dudx) * xvol;
+    dudx = (u2[2] - u4[2]) * tjy;
+    rotx = (rotx + dudx) * xvol;
+    dudx = (u5[2] - u6[2]) * tkz;
+    div = div + dudx * xvol;
+    rot = rotx * rotx + roty * roty + rotz * rotz;
+  } else {
+    const int64_t lt = indmtr(z, ii + 1, jj + 1, kk + 1), ndm = z.ndm;
+    const double xvol = 0.5 / z.vol[lt];
+    const int64_t im = z.minc[0], jm = z.minc[1], km = z.minc[2];
+    const double tix = z.ti[lt], tiy = z.ti[lt + ndm], tix1 = z.ti[lt + im], tiy1 = z.ti[lt + im + ndm];
+    const double tjx = z.tj[lt], tjy = z.tj[lt + ndm], tjx1 = z.tj[lt + jm], tjy1 = z.tj[lt + jm + ndm];
+    if (TYP == Z2D) {
+      double t = sqrt(tix * tix + tiy * tiy);
+      t = t + sqrt(tix1 * tix1 + tiy1 * tiy1);
+      tc[0] = fmaxF(.5 * t, 1.e-27);
+      t = sqrt(tjx * tjx + tjy * tjy);
+      t = t + sqrt(tjx1 * tjx1 + tjy1 * tjy1);
+      tc[1] = fmaxF(.5 * t, 1.e-27);
+      tc[2] = 1.;
+      dudx = u3[0] * tix1 - u1[0] * tix + u2[0] * tjx1 - u4[0] * tjx;
+      div = dudx * xvol;
+      rotz = -(u3[0] * tiy1 - u1[0] * tiy + u2[0] * tjy1 - u4[0] * tjy);
+      dudx = u3[1] * tix1 - u1[1] * tix + u2[1] * tjx1 - u4[1] * tjx;
+      rotz = (rotz + dudx) * xvol;
+      dudx = u3[1] * tiy1 - u1[1] * tiy + u2[1] * tjy1 - u4[1] * tjy;
+      div = div + dudx * xvol;
+      rot = rotz * rotz;
+    } else {
+      const double tiz = z.ti[lt + 2 * ndm], tiz1 = z.ti[lt + im + 2 * ndm];
+      const double tjz = z.tj[lt + 2 * ndm], tjz1 = z.tj[lt + jm + 2 * ndm];
+      const double tkx = z.tk[lt], tky = z.tk[lt + ndm], tkz = z.tk[lt + 2 * ndm];
+      const double tkx1 = z.tk[lt + km], tky1 = z.tk[lt + km + ndm], tkz1 = z.tk[lt + km + 2 * ndm];
+      double t = sqrt(tix * tix + tiy * tiy + tiz * tiz);
+      t = t + sqrt(tix1 * tix1 + tiy1 * tiy1 + tiz1 * tiz1);
+      tc[0] = fmaxF(.5 * t, 1.e-27);
+      t = sqrt(tjx * tjx + tjy * tjy + tjz * tjz);
+      t = t + sqrt(tjx1 * tjx1 + tjy1 * tjy1 + tjz1 * tjz1);
+      tc[1] = fmaxF(.5 * t, 1.e-27);
+      t = sqrt(tkx * tkx + tky * tky + tkz * tkz);
+      t = t + sqrt(tkx1 * tkx1 + tky1 * tky1 + tkz1 * tkz1);
+      tc[2] = fmaxF(.5 * t, 1.e-27);
+#define FGB_G(m, x) (u3[m] * ti##x##1 - u1[m] * ti##x + u2[m] * tj##x##1 - u4[m] * tj##x + \
+                     u5[m] * tk##x##1 - u6[m] * tk##x)
+      dudx = FGB_G(0, x);
+      div = dudx * xvol;
+      rotz = -FGB_G(0, y);
+      roty = FGB_G(0, z);
+      dudx = FGB_G(1, x);
+      rotz = (rotz + dudx) * xvol;
+      dudx = FGB_G(1, y);
+      div = div + dudx * xvol;
+      dudx = FGB_G(1, z);
+      rotx = -dudx;
+      dudx = FGB_G(2, x);
+      roty = (roty - dudx) * xvol;
+      dudx = FGB_G(2, y);
+      rotx = (rotx + dudx) * xvol;
+      dudx = FGB_G(2, z);
+      div = div + dudx * xvol;
+#undef FGB_G
+      rot = rotx * rotx + roty * roty + rotz * rotz;
+    }
+  }
+  const int64_t shift = z.kflu == SENSEUR ? 3 * nd : 0;
+  const int out[3] = {o0, o1, o2};
+#pragma unroll
+  for (int d = 0; d < (TYP == Z2D ? 2 : 3); d++) {
+    if (out[(d + 1) % 3] || out[(d + 2) % 3]) continue;
+    double mach = sqrt(z.gam * z.rgp * q[l + 4 * nd]);
+    mach = 10.0 * (1.0 / tc[d]) * (1.0 / mach) * div;
+    mach = 0.5 * (1.0 - tanh(2.5 + mach));
+    const int64_t n = z.inc[d];
+    const double p2 = q[l - n] * q[l - n + 4 * nd];
+    const double p0 = q[l] * q[l + 4 * nd];
+    const double p1 = q[l + n] * q[l + n + 4 * nd];
+    double w = fabs(p2 - 2. * p0 + p1) / fabs(p2 + 2. * p0 + p1);
+    w = fminF(2.0 * div * div / (div * div + rot + 1e-15) * w * mach, 1.0);
+    wig[l + d * nd + shift] = 1.0 - w;
+  }
+}
+
+cudaError_t launch_shock_sensor(const Zone& z, const double* q, double* wig, cudaStream_t st) {
+  const int B = 128;
+  const int64_t n = (z.ni + 1) * (z.nj + 1) * (z.nk + (z.typ == Z2D ? 0 : 1));
+  const unsigned g = (unsigned)((n + B - 1) / B);
+  if (z.typ == Z3DCART) shock_sensor<Z3DCART><<<g, B, 0, st>>>(z, q, wig);
+  else if (z.typ == Z3DFULL) shock_sensor<Z3DFULL><<<g, B, 0, st>>>(z, q, wig);
+  else if (z.typ == Z2D) shock_sensor<Z2D><<<g, B, 0, st>>>(z, q, wig);
+  else return cudaErrorNotSupported;
   return cudaGetLastError();
 }
 

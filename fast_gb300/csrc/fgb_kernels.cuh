@@ -34,6 +34,7 @@ cudaError_t launch_wall_corr(const Zone& z, const double* q, double* drodm, cons
 cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
                          double* Fj, double* Fk, cudaStream_t st);
 cudaError_t launch_wiggle(const Zone& z, const double* q, double* wig, cudaStream_t st);
+cudaError_t launch_shock_sensor(const Zone& z, const double* q, double* wig, cudaStream_t st);
 cudaError_t launch_assemble(const Zone& z, const StageArgs& a, bool implicit, cudaStream_t st);
 // Spalart-Allmaras source of the sub-step (init_rhs of equation 6 fused in);
 // lu: also coe(:,6) for the LU-SGS sweeps (first implicit sub-step)

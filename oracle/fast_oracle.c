@@ -517,19 +517,30 @@ static inline double vanalbada(double x, double y) {
   return ((y * y + e2) * x + (x * x + e2) * y) / (x * x + y * y + 2. * e2);
 }
 
-/* Slope/{o1,o3,minmod}_slope_var.for: qm = right state, qp = left state */
-static void slopes(const fctx* c, int64_t l, int64_t inc, double qm[6], double qp[6]) {
+/* Slope/{o1,o3,o3sc,minmod}_slope_var.for: qm = right state, qp = left
+ * state of the d-face of cell l.  o3sc (slope 6) blends the o3 states with
+ * the first-order ones by the shock-sensor weight of the face,
+ * wig(l + sl_d) (e.g. AUSM/3dcart/fluFaceEuler_o3sc_3dcart_i.for:10,
+ * sl_d = d * NDIMDX, shifted by 3 * NDIMDX for the senseur scheme). */
+static void slopes(const fctx* c, int64_t l, int d, double qm[6], double qp[6]) {
   const double* rop = c->rop;
+  const int64_t inc = c->inc[d];
   int64_t nd = c->nd, nm = l - inc, nm2 = l - 2 * inc, np = l + inc;
+  double csc = 0.;
+  if (c->slope == 6) csc = c->wig[l + d * nd + (c->kflu == 2 ? 3 * nd : 0)];
   for (int v = 0; v < c->neq; v++) {
     if (c->typ == 3 && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
     int64_t vs = v * nd;
     if (c->slope == 1) {
       qm[v] = rop[l + vs];
       qp[v] = rop[nm + vs];
-    } else if (c->slope == 2) {
+    } else if (c->slope == 2 || c->slope == 6) {
       qm[v] = c->c4 * rop[l + vs] + c->c5 * rop[nm + vs] + c->c6 * rop[np + vs];
       qp[v] = c->c4 * rop[nm + vs] + c->c6 * rop[nm2 + vs] + c->c5 * rop[l + vs];
+      if (c->slope == 6) {   /* Slope/o3sc_slope_var.for:5-6 */
+        qm[v] = rop[l + vs] * (1. - csc) + qm[v] * csc;
+        qp[v] = rop[nm + vs] * (1. - csc) + qp[v] * csc;
+      }
     } else if (c->slope == 8) { /* van Albada MUSCL */
       double d1 = rop[nm + vs] - rop[nm2 + vs], d2 = rop[l + vs] - rop[nm + vs];
       double d3 = rop[np + vs] - rop[l + vs];
@@ -1007,7 +1018,7 @@ static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, dou
   int64_t l = inddm(c->pi, i, j, k);
   int64_t lt = indmtr(c->pi, i, j, k);
   double qm[6], qp[6], tcx, tcy, tcz, s;
-  slopes(c, l, c->inc[d], qm, qp);
+  slopes(c, l, d, qm, qp);
   if (c->typ == 2) {
     tcx = d == 0 ? c->tcx : 0.; tcy = d == 1 ? c->tcy : 0.; tcz = d == 2 ? c->tcz : 0.;
     s = d == 0 ? c->si : (d == 1 ? c->sj : c->sk);
@@ -1035,12 +1046,13 @@ static void face_flux(const fctx* c, int d, int64_t i, int64_t j, int64_t k, dou
  * BCWall / BCWallViscous). */
 void or_correct_flux(const int64_t* pi, const double* pr, const double* rop, double* drodm,
                      const double* xmut, const double* ti, const double* tj, const double* tk,
-                     const double* vol) {
+                     const double* vol, const double* wig) {
   if (pi[KFLUDOM] != 5) return;
   int64_t pt_bcs = pi[PT_BC];
   if (pt_bcs <= 0) return;
   fctx c;
   fctx_init(&c, pi, pr, rop, xmut, ti, tj, tk, vol);
+  c.wig = wig;   /* o3sc: the shock-sensor weights of the wall faces */
   c.iflow = 1;   /* Euler part only */
   const int64_t nd = pi[NDIMDX];
   const double rgp = pr[CVINF] * (pr[GAMMA] - 1.), gam2 = pr[GAMMA] / (pr[GAMMA] - 1.);
@@ -1131,6 +1143,153 @@ void or_wiggle(const int64_t* pi, const int64_t* ind, const double* rop, double*
           wig[l + d * nd] = wig_face(pi, rop, l, inc[d]);
         }
   (void)hi;
+}
+
+/* The velocity divergence and the squared vorticity of cell (i,j,k) from
+ * the face-averaged velocities (SA/div_rot_3dcart.for, SA/div_rot_3dfull.for,
+ * SA/div_rot_2d.for) and the cell's face-metric norms tc[d]
+ * (SENSOR/sciacovelli.for:186-200 for cartesian zones, SA/metric_3dfull.for,
+ * SA/metric_2d.for). */
+static void div_rot(const int64_t* pi, const double* rop, const double* ti, const double* tj,
+                    const double* tk, const double* vol, int64_t i, int64_t j, int64_t k,
+                    double* div, double* rot, double tc[3]) {
+  const int64_t nd = pi[NDIMDX], l = inddm(pi, i, j, k);
+  const int typ = (int)pi[ITYPZONE];
+  const int64_t incj = pi[NIJK], inck = pi[NIJK] * pi[NIJK + 1];
+  const int64_t l1 = l + 1, l2 = l - 1, l3 = l + incj, l4 = l - incj, l5 = l + inck, l6 = l - inck;
+  double u1[3], u2[3], u3[3], u4[3], u5[3], u6[3];
+  const int nvel = typ == 3 ? 2 : 3;
+  for (int m = 0; m < nvel; m++) {
+    const double* q = rop + (m + 1) * nd;
+    u1[m] = q[l] + q[l2]; u2[m] = q[l] + q[l3]; u3[m] = q[l] + q[l1]; u4[m] = q[l] + q[l4];
+    if (typ != 3) { u5[m] = q[l] + q[l5]; u6[m] = q[l] + q[l6]; }
+  }
+  double dudx, rotx = 0., roty = 0., rotz;
+  if (typ == 2) {
+    const double tix = ti[0], tjy = tj[0], tkz = tk[0], xvol = 0.5 / vol[0];
+    tc[0] = fabs(tix); tc[1] = fabs(tjy); tc[2] = fabs(tkz);
+    dudx = (u3[0] - u1[0]) * tix;
+    rotz = -(u2[0] - u4[0]) * tjy;
+    roty = (u5[0] - u6[0]) * tkz;
+    *div = dudx * xvol;
+    dudx = (u3[1] - u1[1]) * tix;
+    rotz = (rotz + dudx) * xvol;
+    dudx = (u2[1] - u4[1]) * tjy;
+    *div = *div + dudx * xvol;
+    dudx = (u5[1] - u6[1]) * tkz;
+    rotx = -dudx;
+    dudx = (u3[2] - u1[2]) * tix;
+    roty = (roty - dudx) * xvol;
+    dudx = (u2[2] - u4[2]) * tjy;
+    rotx = (rotx + dudx) * xvol;
+    dudx = (u5[2] - u6[2]) * tkz;
+    *div = *div + dudx * xvol;
+    *rot = rotx * rotx + roty * roty + rotz * rotz;
+    return;
+  }
+  const int64_t lt = indmtr(pi, i, j, k), ndm = pi[NDIMDX_MTR];
+  const int64_t im = pi[NIJK_MTR], jm = pi[NIJK_MTR + 1], km = pi[NIJK_MTR + 2];
+  const double xvol = 0.5 / vol[lt];
+  if (typ == 3) {
+    const double tix = ti[lt], tiy = ti[lt + ndm], tix1 = ti[lt + im], tiy1 = ti[lt + im + ndm];
+    const double tjx = tj[lt], tjy = tj[lt + ndm], tjx1 = tj[lt + jm], tjy1 = tj[lt + jm + ndm];
+    double t = sqrt(tix * tix + tiy * tiy);
+    t = t + sqrt(tix1 * tix1 + tiy1 * tiy1);
+    tc[0] = OMAX(.5 * t, 1.e-27);
+    t = sqrt(tjx * tjx + tjy * tjy);
+    t = t + sqrt(tjx1 * tjx1 + tjy1 * tjy1);
+    tc[1] = OMAX(.5 * t, 1.e-27);
+    tc[2] = 1.;
+#define G2(m, x) (u3[m] * ti##x##1 - u1[m] * ti##x + u2[m] * tj##x##1 - u4[m] * tj##x)
+    dudx = G2(0, x);
+    *div = dudx * xvol;
+    rotz = -G2(0, y);
+    dudx = G2(1, x);
+    rotz = (rotz + dudx) * xvol;
+    dudx = G2(1, y);
+    *div = *div + dudx * xvol;
+#undef G2
+    *rot = rotz * rotz;
+    return;
+  }
+  const double tix = ti[lt], tiy = ti[lt + ndm], tiz = ti[lt + 2 * ndm];
+  const double tix1 = ti[lt + im], tiy1 = ti[lt + im + ndm], tiz1 = ti[lt + im + 2 * ndm];
+  const double tjx = tj[lt], tjy = tj[lt + ndm], tjz = tj[lt + 2 * ndm];
+  const double tjx1 = tj[lt + jm], tjy1 = tj[lt + jm + ndm], tjz1 = tj[lt + jm + 2 * ndm];
+  const double tkx = tk[lt], tky = tk[lt + ndm], tkz = tk[lt + 2 * ndm];
+  const double tkx1 = tk[lt + km], tky1 = tk[lt + km + ndm], tkz1 = tk[lt + km + 2 * ndm];
+  double t = sqrt(tix * tix + tiy * tiy + tiz * tiz);
+  t = t + sqrt(tix1 * tix1 + tiy1 * tiy1 + tiz1 * tiz1);
+  tc[0] = OMAX(.5 * t, 1.e-27);
+  t = sqrt(tjx * tjx + tjy * tjy + tjz * tjz);
+  t = t + sqrt(tjx1 * tjx1 + tjy1 * tjy1 + tjz1 * tjz1);
+  tc[1] = OMAX(.5 * t, 1.e-27);
+  t = sqrt(tkx * tkx + tky * tky + tkz * tkz);
+  t = t + sqrt(tkx1 * tkx1 + tky1 * tky1 + tkz1 * tkz1);
+  tc[2] = OMAX(.5 * t, 1.e-27);
+#define G3(m, x) (u3[m] * ti##x##1 - u1[m] * ti##x + u2[m] * tj##x##1 - u4[m] * tj##x + \
+                  u5[m] * tk##x##1 - u6[m] * tk##x)
+  dudx = G3(0, x);
+  *div = dudx * xvol;
+  rotz = -G3(0, y);
+  roty = G3(0, z);
+  dudx = G3(1, x);
+  rotz = (rotz + dudx) * xvol;
+  dudx = G3(1, y);
+  *div = *div + dudx * xvol;
+  dudx = G3(1, z);
+  rotx = -dudx;
+  dudx = G3(2, x);
+  roty = (roty - dudx) * xvol;
+  dudx = G3(2, y);
+  rotx = (rotx + dudx) * xvol;
+  dudx = G3(2, z);
+  *div = *div + dudx * xvol;
+#undef G3
+  *rot = rotx * rotx + roty * roty + rotz * rotz;
+}
+
+/* SENSOR/sciacovelli.for + SENSOR/shock_sensor.for: the directional shock
+ * sensor of the o3sc slope, wig(l + sl_d) = 1 - min(2 div^2 / (div^2 + rot
+ * + 1e-15) * J_d * M, 1), with Jameson's pressure switch J_d =
+ * |p(l-inc) - 2 p(l) + p(l+inc)| / |p(l-inc) + 2 p(l) + p(l+inc)| (p = rho T)
+ * and the dilatation weight M = (1 - tanh(2.5 + 10 div / (tc_d c))) / 2.
+ * Cells of ind plus, at the zone's high edges, the next cell layer of the
+ * direction (its faces close the zone), as the loopPlan corrections do.
+ * sl_d = d * NDIMDX, shifted by 3 * NDIMDX when the senseur scheme keeps its
+ * wiggle flags in the first three. */
+void or_shock_sensor(const int64_t* pi, const double* pr, const int64_t* ind, const double* rop,
+                     const double* ti, const double* tj, const double* tk, const double* vol,
+                     double* wig) {
+  const int64_t nd = pi[NDIMDX];
+  const double gam = pr[GAMMA], rgp = pr[CVINF] * (gam - 1.);
+  const int64_t inc[3] = {1, pi[NIJK], pi[NIJK] * pi[NIJK + 1]};
+  const int64_t corr[3] = {ind[1] == pi[IJKV], ind[3] == pi[IJKV + 1], ind[5] == pi[IJKV + 2]};
+  const int ndir = pi[ITYPZONE] == 3 ? 2 : 3;
+  const int64_t shift = pi[KFLUDOM] == 2 ? 3 * nd : 0;
+  if (ind[0] > ind[1] || ind[2] > ind[3] || ind[4] > ind[5]) return;
+  for (int64_t k = ind[4]; k <= ind[5] + (ndir == 3 ? corr[2] : 0); k++)
+    for (int64_t j = ind[2]; j <= ind[3] + corr[1]; j++)
+      for (int64_t i = ind[0]; i <= ind[1] + corr[0]; i++) {
+        const int out[3] = {i > ind[1], j > ind[3], k > ind[5]};
+        if (out[0] + out[1] + out[2] > 1) continue;
+        const int64_t l = inddm(pi, i, j, k);
+        double div, rot, tc[3];
+        div_rot(pi, rop, ti, tj, tk, vol, i, j, k, &div, &rot, tc);
+        for (int d = 0; d < ndir; d++) {
+          if (out[(d + 1) % 3] || out[(d + 2) % 3]) continue;   /* only the d-layer extends */
+          double mach = sqrt(gam * rgp * rop[l + 4 * nd]);
+          mach = 10.0 * (1.0 / tc[d]) * (1.0 / mach) * div;
+          mach = 0.5 * (1.0 - tanh(2.5 + mach));
+          const int64_t n = inc[d];
+          const double p2 = rop[l - n] * rop[l - n + 4 * nd];
+          const double p0 = rop[l] * rop[l + 4 * nd];
+          const double p1 = rop[l + n] * rop[l + n + 4 * nd];
+          double w = fabs(p2 - 2. * p0 + p1) / fabs(p2 + 2. * p0 + p1);
+          w = OMIN(2.0 * div * div / (div * div + rot + 1e-15) * w * mach, 1.0);
+          wig[l + d * nd + shift] = 1.0 - w;
+        }
+      }
 }
 
 void or_flux(const int64_t* pi, const double* pr, const int64_t* ind,
@@ -2317,11 +2476,14 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
         if (pi[IFLOW] == 3)
           or_spsource(pi, pr, nstep, sdm, ssiter, Z->coe, Z->ti, Z->tj, Z->tk, Z->vol,
                       Z->xmut + pi[NDIMDX], Z->drodm);
+        /* src_term.for:246-255: o3sc shock sensor on every sub-step */
+        if (pi[SLOPE] == 6)
+          or_shock_sensor(pi, pr, sdm, ssiter, Z->ti, Z->tj, Z->tk, Z->vol, Z->wig);
         /* src_term.for:257-266: senseur wiggle on the first sub-step */
         if (pi[KFLUDOM] == 2 && nstep == 1) or_wiggle(pi, sdm, ssiter, Z->wig);
         or_flux(pi, pr, sdm, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol, Z->wig);
         /* navier_stokes_struct.for:378: wall-face correction (Roe) */
-        or_correct_flux(pi, pr, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
+        or_correct_flux(pi, pr, ssiter, Z->drodm, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol, Z->wig);
         if (implicit) {
           or_core3as2(pi, pr, nstep, *first_it, sdm, ssiter, Z->ro, Z->ro_m1, Z->drodm, Z->coe);
           if (lssiter_verif) or_cprdu3s1(pi, nstep, (int)nssiter, Z->drodm, Z->rdm);

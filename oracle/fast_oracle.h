@@ -41,7 +41,7 @@ typedef struct {
   double* coe;    /* dt/vol, spectral radii, LU diagonal: NEQ_COE*NDIMDX   */
   const double* ti; const double* tj; const double* tk; const double* vol;
   double* rdm;    /* Newton residual per LU block: nssiter*neq*2*ndim_rdm  */
-  double* wig;    /* senseur wiggle flags, 3*NDIMDX (KFLUDOM = 2)           */
+  double* wig;    /* senseur wiggle flags (KFLUDOM = 2), then o3sc weights  */
   double* cfl;    /* CFL max, min, mean of the last verified step (3)      */
 } or_zone;
 
@@ -80,7 +80,12 @@ void or_flux(const int64_t* pi, const double* pr, const int64_t* ind,
 /* BC/correct_flux.for for wall BCs with the Roe scheme (lapply = 4) */
 void or_correct_flux(const int64_t* pi, const double* pr, const double* rop, double* drodm,
                      const double* xmut, const double* ti, const double* tj, const double* tk,
-                     const double* vol);
+                     const double* vol, const double* wig);
+/* SENSOR/sciacovelli.for: o3sc shock-sensor weights wig[sl + d*NDIMDX + l]
+ * (sl = 3*NDIMDX for the senseur scheme, else 0) */
+void or_shock_sensor(const int64_t* pi, const double* pr, const int64_t* ind, const double* rop,
+                     const double* ti, const double* tj, const double* tk, const double* vol,
+                     double* wig);
 /* SENSOR/wiggle2001.for: wig[d*NDIMDX + l] = 1 where a slope product of
  * any variable changes sign across the d-face of cell l, else 0 */
 void or_wiggle(const int64_t* pi, const int64_t* ind, const double* rop, double* wig);

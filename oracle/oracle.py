@@ -95,7 +95,7 @@ class Case:
                      vol=np.ascontiguousarray(zd["vol"], dtype=np.float64),
                      lv=[np.array(zd[k], dtype=np.float64).reshape(-1) for k in ("ro", "ro_m1", "ro_p1")],
                      xmut=np.zeros(2 * nd), drodm=np.zeros(neq * nd), coe=np.zeros(neq * nd),
-                     rdm=np.zeros(nss * neq * 2 * nlu), wig=np.zeros(3 * nd), cfl=np.zeros(3))
+                     rdm=np.zeros(nss * neq * 2 * nlu), wig=np.zeros(6 * nd), cfl=np.zeros(3))
             if neq == 6:
                 # Spalart-Allmaras: the wall distance follows the viscosity
                 # (navier_stokes_struct passes xmut(1+NDIMDX) as dist)
