@@ -648,11 +648,14 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   if (p[NEQ] != (p[IFLOW] == 3 ? 6 : 5))
     return fail(FGB_ERR_ARG, "NEQ must be 5 (Euler, laminar) or 6 (Spalart-Allmaras)");
   if (p[IFLOW] == 3) {
-    const bool ausm_o3 = (p[KFLUDOM] == AUSM || p[KFLUDOM] == SENSEUR) && p[SLOPE] == O3;
-    const bool roe = p[KFLUDOM] == ROE && (p[SLOPE] == O1 || p[SLOPE] == O3 || p[SLOPE] == MINMOD);
+    const bool ausm_o3 = (p[KFLUDOM] == AUSM || p[KFLUDOM] == SENSEUR) &&
+                         (p[SLOPE] == O3 || p[SLOPE] == O3SC);
+    const bool roe = p[KFLUDOM] == ROE &&
+                     (p[SLOPE] == O1 || p[SLOPE] == O3 || p[SLOPE] == MINMOD || p[SLOPE] == O3SC);
     if (!(ausm_o3 || roe) || p[ILES] != 0 || p[SA_INT] != 0)
-      return fail(FGB_ERR_ARG, "Spalart-Allmaras is supported with the AUSM+(P) o3, senseur o3 "
-                               "or Roe o1 / o3 / minmod schemes (SA, not ZDES) on the GPU path");
+      return fail(FGB_ERR_ARG, "Spalart-Allmaras is supported with the AUSM+(P) o3 / o3sc, senseur "
+                               "o3 / o3sc or Roe o1 / o3 / o3sc / minmod schemes (SA, not ZDES) on "
+                               "the GPU path");
     if (p[ITYPCP] <= 1 && p[NEQ_COE] < 6)
       return fail(FGB_ERR_ARG, "implicit Spalart-Allmaras needs NEQ_COE = 6");
   }

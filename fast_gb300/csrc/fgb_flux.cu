@@ -1014,12 +1014,39 @@ static cudaError_t launch_faces_t(const Zone& z, const double* q, const double* 
   return cudaSuccess;
 }
 
+// *_o3sc_*: the o3 slope blended by the shock sensor; Euler / laminar /
+// Spalart-Allmaras, AUSM+(P), senseur and Roe.
+template <int TYP>
+static cudaError_t launch_faces_o3sc(const Zone& z, const double* q, const double* xmut,
+                                     double* Fi, double* Fj, double* Fk, cudaStream_t st) {
+  if (z.neq == 6) {
+    if (z.kflu == ROE) return launch_faces_t<TYP, ROE, O3SC, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == AUSM) return launch_faces_t<TYP, AUSM, O3SC, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == SENSEUR) return launch_faces_t<TYP, SENSEUR, O3SC, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    return cudaErrorNotSupported;
+  }
+  const bool visc = z.iflow >= 2;
+  if (z.kflu == ROE) return visc ? launch_faces_t<TYP, ROE, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                 : launch_faces_t<TYP, ROE, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st);
+  if (z.kflu == AUSM) return visc ? launch_faces_t<TYP, AUSM, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                  : launch_faces_t<TYP, AUSM, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st);
+  if (z.kflu == SENSEUR) return visc ? launch_faces_t<TYP, SENSEUR, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)
+                                     : launch_faces_t<TYP, SENSEUR, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st);
+  return cudaErrorNotSupported;
+}
+
 // Dispatch over the (zone type, scheme, slope, viscous) combinations that the
 // reference generates for 3d zones.  Returns cudaErrorNotSupported for the
 // others (host code reports it as an argument error, never falls back).
 cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
                          double* Fj, double* Fk, cudaStream_t st) {
   const bool visc = z.iflow >= 2;
+  if (z.slope == O3SC) {
+    if (z.typ == Z3DCART) return launch_faces_o3sc<Z3DCART>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.typ == Z3DFULL) return launch_faces_o3sc<Z3DFULL>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.typ == Z2D) return launch_faces_o3sc<Z2D>(z, q, xmut, Fi, Fj, Fk, st);
+    return cudaErrorNotSupported;
+  }
   if (z.neq == 6 && z.typ == Z2D) {   // Spalart-Allmaras on 2-d zones
     if (z.kflu == AUSM && z.slope == O3) return launch_faces_t<Z2D, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
     if (z.kflu == SENSEUR && z.slope == O3) return launch_faces_t<Z2D, SENSEUR, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
@@ -1046,20 +1073,6 @@ cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, dou
     if (z.kflu == ROE && z.slope == MINMOD)
       return cart ? launch_faces_t<Z3DCART, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
                   : launch_faces_t<Z3DFULL, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
-    return cudaErrorNotSupported;
-  }
-  if (z.slope == O3SC && z.neq == 5 && (z.kflu == ROE || z.kflu == AUSM)) {
-    // *_o3sc_*: the o3 slope blended by the shock sensor, Euler / laminar
-#define FGB_O3SC(TYP)                                                                           \
-  return z.kflu == ROE                                                                          \
-             ? (visc ? launch_faces_t<TYP, ROE, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)          \
-                     : launch_faces_t<TYP, ROE, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st))        \
-             : (visc ? launch_faces_t<TYP, AUSM, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)         \
-                     : launch_faces_t<TYP, AUSM, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st))
-    if (z.typ == Z3DCART) FGB_O3SC(Z3DCART);
-    if (z.typ == Z3DFULL) FGB_O3SC(Z3DFULL);
-    if (z.typ == Z2D) FGB_O3SC(Z2D);
-#undef FGB_O3SC
     return cudaErrorNotSupported;
   }
   if (z.typ == Z3DCART) {

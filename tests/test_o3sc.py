@@ -6,8 +6,9 @@ AUSM/*/fluFaceEuler_o3sc_*.for and ROE/*/fluFaceEuler_o3sc_*.for.
 CPU: the oracle's sensor weights against a numpy statement of the sensor's
 formula on a cartesian zone.
 GPU: the sm_103a path against the oracle on cartesian, curvilinear and 2-d
-zones, AUSM+(P) and Roe (with its wall-face correction), explicit RK3 and
-implicit LU-SGS.
+zones, AUSM+(P), senseur (its wiggle flags and the o3sc weights side by
+side) and Roe (with its wall-face correction), Euler / laminar /
+Spalart-Allmaras, explicit RK3 and implicit LU-SGS.
 """
 import numpy as np
 import pytest
@@ -82,6 +83,12 @@ def test_sensor_cartesian_known_answer(oracle_mod):
     ("roe", (12, 10, 6), 0.3, "implicit", "Euler", "BCWallInviscid"),
     ("roe", (16, 12, 1), 0.3, "explicit", "NSLaminar", "BCWallViscous"),
     ("ausmpred", (16, 12, 1), 0.3, "implicit", "Euler", "BCWallInviscid"),
+    ("senseur", (12, 10, 6), 0.3, "explicit", "NSLaminar", "BCWallViscous"),
+    ("senseur", (16, 12, 1), 0.0, "implicit", "Euler", "BCWallInviscid"),
+    ("ausmpred", (12, 10, 6), 0.3, "implicit", "NSTurbulent", "BCWallViscous"),
+    ("roe", (12, 10, 6), 0.0, "explicit", "NSTurbulent", "BCWallViscous"),
+    ("senseur", (16, 12, 1), 0.3, "implicit", "NSTurbulent", "BCWallViscous"),
+    ("roe", (16, 12, 1), 0.3, "implicit", "NSTurbulent", "BCWallViscous"),
 ])
 def test_o3sc_gpu_parity(oracle_mod, scheme, n, wavy, temporal, model, wall):
     from test_gpu_parity import TOL, _check_levels, _pair
@@ -99,16 +106,4 @@ def test_o3sc_gpu_parity(oracle_mod, scheme, n, wavy, temporal, model, wall):
     if temporal == "implicit":
         nss = int(zd[0]["pi"][58])
         assert rel_err(s.residuals(0), ref.residual_norms(0, nss)) <= TOL
-    s.close()
-
-
-@pytest.mark.gpu
-def test_o3sc_spalart_refused():
-    """o3sc with Spalart-Allmaras is not built: add_zone refuses it."""
-    from fast_gb300._native import Solver
-    t = cases.bc_box(n=(12, 10, 6), model="NSTurbulent", scheme="ausmpred", slope="o3sc")
-    z = fasts.zone_data(t, fasts.prepare(t))[0]
-    s = Solver(0)
-    with pytest.raises(Exception, match="Spalart"):
-        s.add_zone(z["pi"], z["pr"], z["ti"], z["tj"], z["tk"], z["vol"])
     s.close()
