@@ -73,6 +73,8 @@ def parse():
                    help="adjoint workload: replay the driver loops as CUDA graphs")
     p.add_argument("--adj-checks", type=int, default=1, choices=[0, 1],
                    help="adjoint workload: tangent / FD checks and the per-group breakdown")
+    p.add_argument("--slope", default="o3", choices=["o3", "o3sc"],
+                   help="tgv workload: MUSCL slope of the AUSM+(P) faces (o3sc adds the shock sensor)")
     p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
                    help="64: plain FP64 path; 32: FP32 LU-SGS sweeps (mixed precision)")
     return p.parse_args()
@@ -176,7 +178,7 @@ class Clocks:
 
 
 # ------------------------------------------------------------- CPU side
-def cpu_sample(n, ss, steps=1, min_seconds=0.0):
+def cpu_sample(n, ss, steps=1, min_seconds=0.0, slope="o3"):
     """The oracle (C restatement of the FastS kernels, OpenMP on every host
     core, one LU-SGS block per thread as FastS does) on an n^3 sample of the
     workload: `steps` physical steps, continued until `min_seconds` of CPU
@@ -185,7 +187,7 @@ def cpu_sample(n, ss, steps=1, min_seconds=0.0):
     import oracle
     from fast_gb300 import cases, fasts
     threads = os.cpu_count() or 1
-    t = cases.taylor_green(n=n, ss_iteration=ss)
+    t = cases.taylor_green(n=n, ss_iteration=ss, slope=slope)
     m = fasts.prepare(t)
     c = oracle.Case(fasts.zone_data(t, m))
     oracle.set_threads(threads)
@@ -207,10 +209,10 @@ def run_reference(args, d: Dist):
         return
     n = args.cpu_n
     for _ in range(args.warmup):
-        cpu_sample(n, args.ss, 1)
+        cpu_sample(n, args.ss, 1, slope=args.slope)
     vals, secs = [], 0.0
     for _ in range(args.steps):
-        v, threads, dt, _ = cpu_sample(n, args.ss, 1)
+        v, threads, dt, _ = cpu_sample(n, args.ss, 1, slope=args.slope)
         vals.append(v)
         secs += dt
     value = args.steps * n ** 3 / secs / 1e6
@@ -219,7 +221,7 @@ def run_reference(args, d: Dist):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"taylor_green_{args.n}^3_ausmpred_o3_implicit_lusgs_ss{args.ss}",
+        "config": {"workload": f"taylor_green_{args.n}^3_ausmpred_{args.slope}_implicit_lusgs_ss{args.ss}",
                    "sample": f"{n}^3 cells, 1 physical step ({args.ss} sub-iterations) per step",
                    "parallelism": "host OpenMP"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
@@ -246,7 +248,7 @@ def run_ours(args, d: Dist):
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
 
     # FastS defaults: residual check every 200 steps (modulo_verif)
-    t = cases.taylor_green(n=n, ss_iteration=ss,
+    t = cases.taylor_green(n=n, ss_iteration=ss, slope=args.slope,
                            numb={"temporal_scheme": "implicit", "ss_iteration": ss,
                                  "modulo_verif": 200})
     t, tc, metrics = fasts.warmup(t, None, device=dev, gpu_resident=True)
@@ -349,7 +351,7 @@ def run_ours(args, d: Dist):
 
     cpu = None
     if d.rank == 0 and not args.no_cpu:
-        v, threads, sec, nst = cpu_sample(args.cpu_n, ss, 1, min_seconds=10.0)
+        v, threads, sec, nst = cpu_sample(args.cpu_n, ss, 1, min_seconds=10.0, slope=args.slope)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"taylor_green {args.cpu_n}^3, {nst} physical steps ({ss} LU-SGS "
                          f"sub-iterations each), {sec:.1f} s"}
@@ -361,7 +363,7 @@ def run_ours(args, d: Dist):
             "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.lu_precision == 64 else "f64+f32-sweeps",
             "data": "synthetic",
-            "config": {"workload": f"taylor_green_{n}^3_ausmpred_o3_implicit_lusgs_ss{ss}",
+            "config": {"workload": f"taylor_green_{n}^3_ausmpred_{args.slope}_implicit_lusgs_ss{ss}",
                        "lu_precision": args.lu_precision,
                        "cells": cells, "global_batch": d.world, "sub_iterations": ss,
                        "parallelism": f"replicas x{d.world}",

@@ -1348,18 +1348,29 @@ __global__ void __launch_bounds__(128) shock_sensor(Zone z, const double* __rest
   }
   const int64_t shift = z.kflu == SENSEUR ? 3 * nd : 0;
   const int out[3] = {o0, o1, o2};
+  // the factors that do not depend on the direction are formed once (same
+  // operations, same order: ((10 (1/tc)) (1/c)) div and ((2 div div) / den)
+  // J M), and M is reused when tc_d equals the previous direction's (cubic
+  // cartesian cells): the FP64 pipe, with tanh the largest part, bounds it
+  const double isnd = 1.0 / sqrt(z.gam * z.rgp * q[l + 4 * nd]);
+  const double ratio = 2.0 * div * div / (div * div + rot + 1e-15);
+  const double p0 = q[l] * q[l + 4 * nd];
+  double tc_prev = -1., m_prev = 0.;
 #pragma unroll
   for (int d = 0; d < (TYP == Z2D ? 2 : 3); d++) {
     if (out[(d + 1) % 3] || out[(d + 2) % 3]) continue;
-    double mach = sqrt(z.gam * z.rgp * q[l + 4 * nd]);
-    mach = 10.0 * (1.0 / tc[d]) * (1.0 / mach) * div;
-    mach = 0.5 * (1.0 - tanh(2.5 + mach));
+    double mach = m_prev;
+    if (tc[d] != tc_prev) {
+      mach = 10.0 * (1.0 / tc[d]) * isnd * div;
+      mach = 0.5 * (1.0 - tanh(2.5 + mach));
+      tc_prev = tc[d];
+      m_prev = mach;
+    }
     const int64_t n = z.inc[d];
     const double p2 = q[l - n] * q[l - n + 4 * nd];
-    const double p0 = q[l] * q[l + 4 * nd];
     const double p1 = q[l + n] * q[l + n + 4 * nd];
     double w = fabs(p2 - 2. * p0 + p1) / fabs(p2 + 2. * p0 + p1);
-    w = fminF(2.0 * div * div / (div * div + rot + 1e-15) * w * mach, 1.0);
+    w = fminF(ratio * w * mach, 1.0);
     wig[l + d * nd + shift] = 1.0 - w;
   }
 }
