@@ -126,10 +126,13 @@ def _tree(zones, model, numb, numz, mach, reynolds, gamma=1.4, prandtl=0.72, sut
 
 
 def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0, gamma=1.4,
-                      numb=None, numz=None, wavy=0.0, two_d=False):
+                      numb=None, numz=None, wavy=0.0, two_d=False, cfl=None):
     """Config: plain FP64, 128x128x4 periodic box [-box, box]^2, Euler vortex
     (Mach 0.5, strength 5, core radius 1), Roe + minmod, explicit RK3.
-    wavy > 0: the same box on a periodic curvilinear mesh (see wave)."""
+    wavy > 0: the same box on a periodic curvilinear mesh (see wave).
+    cfl: the time step is the one that gives this CFL number on the initial
+    field (cpcfl3.for's local time step, fasts.cfl_time_step) instead of the
+    numerics' time_step."""
     ni, nj, nk = n
     if two_d:
         nk = 1
@@ -155,7 +158,11 @@ def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0,
     numz = numz or {"scheme": "roe_min", "slope": "minmod", "time_step": 0.01,
                     "cache_blocking_I": 1000000, "cache_blocking_J": 1000000,
                     "cache_blocking_K": 1000000}
-    return _tree([z], "Euler", numb, numz, mach, 0.0, gamma=gamma)
+    t = _tree([z], "Euler", numb, numz, mach, 0.0, gamma=gamma)
+    if cfl is not None:
+        from . import fasts
+        FastC._setNum2Zones(t, {"time_step": fasts.cfl_time_step(t, cfl)})
+    return t
 
 
 def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_iteration=4,
@@ -197,10 +204,20 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
                  sutherland=False, nutilde_ratio=nutilde_ratio)
 
 
+def add_bc_data(bc, arrays):
+    """BC data as FastS reads it: DataArray_t nodes under BCDataSet_t /
+    BCData_t of the BC node, in the given order (name, values)."""
+    ds = I.createChild(bc, "BCDataSet", "BCDataSet_t", "Null")
+    bd = I.createChild(ds, "DirichletData", "BCData_t")
+    for name, val in arrays:
+        I.createChild(bd, name, "DataArray_t", np.asarray(val, dtype=np.float64))
+    return bc
+
+
 def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model="NSLaminar",
            wavy=0.0, perturb=0.05, temporal="explicit", ss_iteration=3, scheme="ausmpred",
            slope="o3", time_step=0.02, gamma=1.4, two_d=False, nutilde_ratio=5.0,
-           extrude=False):
+           extrude=False, outflow="BCOutflow", outpres_form=1, outpres_amp=0.02, bc_data=False):
     """Box [0,1]x[0,1]x[0,dz] exercising the non-periodic BCs of the path:
     inflow at imin (BCInflow), outflow at imax (BCOutflow), a wall at jmin
     (``wall``), farfield at jmax (BCFarfield), periodic in k.  The initial
@@ -210,7 +227,15 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
     adds Spalart-Allmaras: free-stream ro nutilde = nutilde_ratio x mu, the
     same perturbation on nutilde, and the distance to the jmin wall.
     extrude (3-d only): the 2-d case extruded in k -- in-plane displacement,
-    no k dependence of the initial field, w = 0."""
+    no k dependence of the initial field, w = 0.
+    outflow "BCOutpres": imposed static pressure at imax instead, one value
+    per face (p_inf (1 + outpres_amp sin(2 pi y))) given as BC data -- the pressure
+    array alone (outpres_form 1) or after a one-value mobile_coef array
+    (outpres_form 2), the two layouts bvbs_outpres reads.
+    bc_data: the farfield and inflow states come from BC data instead of the
+    free stream (conservative ro, ro u, ro v, ro w, ro E [, ro nutilde],
+    a 2-3 % departure from it): the farfield as one array of those values,
+    the inflow in the 21-array layout of BCzone.cpp's DEFAULT_STATE."""
     ni, nj, nk = n
     if two_d:
         nk = 1
@@ -235,10 +260,32 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
         mu = mach / reynolds
         set_spalart(z, nutilde_ratio * mu * (1.0 + a * np.cos(2 * math.pi * xc) * np.sin(math.pi * yc)) / ro,
                     np.abs(yc))
-    add_bc(z, "in", "BCInflow", "imin")
-    add_bc(z, "out", "BCOutflow", "imax")
+    bin_ = add_bc(z, "in", "BCInflow", "imin")
+    bout = add_bc(z, "out", outflow, "imax")
     add_bc(z, "wall", wall, "jmin")
-    add_bc(z, "far", "BCFarfield", "jmax")
+    bfar = add_bc(z, "far", "BCFarfield", "jmax")
+    if outflow == "BCOutpres":
+        nkf = 1 if two_d else nk
+        yf = (np.arange(nj) + 0.5) / nj
+        pf = np.repeat((1.0 + outpres_amp * np.sin(2 * math.pi * yf))[:, None] / gamma, nkf, axis=1)
+        arrays = [("Pressure", pf.ravel(order="F"))]
+        if outpres_form == 2:
+            arrays = [("mobile_coef", np.array([1.0]))] + arrays
+        add_bc_data(bout, arrays)
+    if bc_data:
+        ro_e, u_e, v_e = 1.02, 1.03 * mach, 0.01 * mach
+        p_e = 1.01 / gamma
+        st = [ro_e, ro_e * u_e, ro_e * v_e, 0.0,
+              p_e / (gamma - 1.0) + 0.5 * ro_e * (u_e * u_e + v_e * v_e)]
+        if model == "NSTurbulent":
+            st.append(ro_e * 1.1 * nutilde_ratio * mach / reynolds)
+        add_bc_data(bfar, [("State", np.array(st))])
+        st21 = [0.0] * 21
+        for m_ in range(5):
+            st21[3 + m_] = st[m_] * (1.0 if m_ != 1 else 0.99)
+        if model == "NSTurbulent":
+            st21[16] = st[5]
+        add_bc_data(bin_, [("d%02d" % m_, np.array([x])) for m_, x in enumerate(st21)])
     if not two_d:
         add_bc(z, "per_kmin", "BCautoperiod", "kmin")
         add_bc(z, "per_kmax", "BCautoperiod", "kmax")

@@ -53,7 +53,9 @@ struct GatherList {
   int32_t* mt = nullptr;          // metric index of the face of each entry (face formulas)
   int dir = 0;                    // face direction (0 i, 1 j, 2 k)
   double st[5] = {0, 0, 0, 0, 0};
+  double nue = 0.;                // exterior nutilde = state(6) / state(1)
   int inflow = 0;                 // BCInflow: nutilde imposed (Spalart-Allmaras)
+  double* aux = nullptr;          // per entry: imposed pressure (BCOutpres)
 };
 struct WallCorrList {             // one wall BC window of a Roe zone (correct_flux.for)
   int32_t *l = nullptr, *l0 = nullptr, *lt = nullptr;
@@ -93,6 +95,7 @@ struct ZoneData {
 };
 struct Transfer {
   int dnr, rcv; int64_t n; int32_t* dnr_idx; int32_t* rcv_idx;
+  std::vector<int32_t> hd, hr;     // host copies (conflict check of the one-launch fill)
 };
 // Zones solved by one LU-SGS launch (same zone type and equation count): the
 // plane table over all of them and a ring of zone tables (the state pointers
@@ -112,6 +115,14 @@ struct LuGroupData {
   cudaEvent_t ev[NSLOT] = {};
   bool ev_used[NSLOT] = {};
   int slot = 0;
+  // dataflow schedule (lu_mode 2): chunk table, dependency ranges, marks
+  int64_t nchunk = 0;
+  int32_t* cplane = nullptr;
+  int64_t* cbase = nullptr;
+  int32_t* dep = nullptr;
+  int* flag = nullptr;
+  unsigned long long* ticket = nullptr;
+  int epoch = 0;
 };
 
 struct fgb_solver {
@@ -152,13 +163,18 @@ struct fgb_solver {
   int32_t *tr_rz = nullptr, *tr_ri = nullptr, *tr_dz = nullptr, *tr_di = nullptr;
   int64_t tr_n = 0;
   size_t tr_built = 0;             // number of transfers the list holds
+  bool tr_ordered = false;         // a cell is written twice or read after a write: ordered fill
   cudaStream_t zst[ZS] = {};
   cudaEvent_t zev[ZS] = {};
   cudaEvent_t fork_ev = nullptr;
   int first_it = 0;
   int modulo_verif = 200;
   int lu_precision = 64;
-  int lu_mode = 1;                 // 1 persistent cooperative sweeps, 0 one launch per plane
+  int lu_mode = 2;                 // 2 dataflow sweeps, 1 persistent grid-barrier sweeps,
+                                   // 0 one launch per plane
+  long long poll_limit = 1ll << 22;  // polls before a dataflow wait gives up
+  int wait_skew = 0;               // test support: added to the marks the dataflow waits expect
+  int lu_grid = 0;                 // > 0: at most this many CTAs in the persistent sweep
   unsigned int* bar = nullptr;     // grid-barrier words
   int* derr = nullptr;             // device error word
   int nit_recorded = 0;
@@ -280,11 +296,58 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
       const bool slip = type == 3 || type == 5 || (type == 4 && p[IFLOW] == 1);
       const bool noslip = (type == 6 || type == 4) && p[IFLOW] > 1;
       const bool charac = type == 1 || type == 13 || type == 10;
-      if (type != 11 && type != 0 && !slip && !noslip && !charac)
+      const bool outpres = type == 16;
+      if (type != 11 && type != 0 && !slip && !noslip && !charac && !outpres)
         return fail(FGB_ERR_ARG, "boundary condition type " + std::to_string(type) +
                                      " is not implemented on the GPU path");
-      if (p[pt + 8] != 0)
-        return fail(FGB_ERR_ARG, "boundary data (nbdata > 0) is not supported on the GPU path");
+      // BC data (BCzone.cpp:324-325, DEFAULT_STATE :26-53): nbdata arrays
+      // concatenated in param_real at param_int[pt_bcs + 1 + nb + n], their
+      // cumulative sizes at param_int[pt + 9 ...]
+      const int64_t nbdata = p[pt + 8];
+      const double* bdata = nullptr;
+      int64_t bsize = 0;
+      if (nbdata > 0) {
+        const int64_t off = p[pt_bcs + 1 + nb + n];
+        bsize = p[pt + 8 + nbdata];
+        if (off < 0 || off + bsize > (int64_t)pr.size())
+          return fail(FGB_ERR_ARG, "boundary data outside Parameter_real");
+        bdata = pr.data() + off;
+      }
+      double bst[6] = {pr[ROINF], pr[VXINF] * pr[ROINF], pr[VYINF] * pr[ROINF],
+                       pr[VZINF] * pr[ROINF], 0., pr[RONUTILDEINF]};
+      bst[4] = pr[PINF] / (pr[GAMMA] - 1.) +
+               0.5 * (pr[VXINF] * bst[1] + pr[VYINF] * bst[2] + pr[VZINF] * bst[3]);
+      if (nbdata > 0 && charac) {
+        if (nbdata == 21) {
+          if (bsize < 17) return fail(FGB_ERR_ARG, "BC data with nbdata = 21 holds fewer than 17 values");
+          for (int m = 0; m < 5; m++) bst[m] = bdata[3 + m];
+          bst[5] = bdata[16];
+        } else {
+          if (type == 13 && p[pt + 9] > 6)
+            return fail(FGB_ERR_ARG, "BCInflow with per-face data (bvbs_inflow_fich) is not "
+                                     "implemented on the GPU path");
+          if (bsize < p[NEQ]) return fail(FGB_ERR_ARG, "BC state data holds fewer than NEQ values");
+          for (int m = 0; m < (int)p[NEQ]; m++) bst[m] = bdata[m];
+        }
+      } else if (nbdata > 0 && type != 11 && type != 0 && !outpres) {
+        return fail(FGB_ERR_ARG, "boundary data (nbdata > 0) of BC type " + std::to_string(type) +
+                                     " is not supported on the GPU path");
+      }
+      // BCOutpres (BCzone.cpp:758-792): the imposed pressure per face of the
+      // window, after a one-value mobile_coef array when there is one
+      const double* pext = nullptr;
+      int64_t npext = 0;
+      if (outpres) {
+        if (nbdata < 1 || nbdata > 2)
+          return fail(FGB_ERR_ARG, "BCOutpres needs its pressure as BC data (1 or 2 arrays)");
+        if (p[pt + 9] == 1) {
+          if (nbdata != 2) return fail(FGB_ERR_ARG, "BCOutpres: a one-value array must be "
+                                                    "followed by the pressure array");
+          pext = bdata + 1; npext = p[pt + 10] - 1;
+        } else {
+          pext = bdata; npext = p[pt + 9];
+        }
+      }
 
       int64_t cl[6];
       bc_window(p, &p[pt + 2], idir, cl);
@@ -366,7 +429,9 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
         Z.walls.push_back(w);
       }
       std::vector<int32_t> fdst, fsrc, fmt, ndst, n0, n1, n2, cdst, csrc;
-      std::vector<double> nrm;
+      std::vector<double> nrm, faux;
+      const int64_t* fen = &p[pt + 2];
+      const int64_t na = fen[2 * ta + 1] - fen[2 * ta] + 1;   // indbci of bvbs_outpres.for
       const int64_t inc = d == 0 ? 1 : (d == 1 ? p[NIJK] : p[NIJK] * p[NIJK + 1]);
       for (int64_t b = cl[2 * tb]; b <= cl[2 * tb + 1]; b++)
         for (int64_t a = cl[2 * ta]; a <= cl[2 * ta + 1]; a++) {
@@ -388,7 +453,13 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
               fdst.push_back((int32_t)l); fsrc.push_back((int32_t)idx(p, m[0], m[1], m[2]));
               fmt.push_back((int32_t)lm);
               for (int q = 0; q < 3; q++) nrm.push_back(t[q] * snorm);
-            } else if (type == 10) {     // BC_extrap.for: copy of the first ghost
+              if (outpres) {
+                const int64_t li = (a - fen[2 * ta]) + (b - fen[2 * tb]) * na;
+                if (li < 0 || li >= npext)
+                  return fail(FGB_ERR_ARG, "BCOutpres: pressure array smaller than the window");
+                faux.push_back(pext[li]);
+              }
+            } else if (type == 10 || outpres) {   // BC_extrap.for: copy of the first ghost
               m[d] = first;
               cdst.push_back((int32_t)l); csrc.push_back((int32_t)idx(p, m[0], m[1], m[2]));
             } else {                     // BC_nextrank.for
@@ -400,19 +471,17 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
         }
       GatherList f;
       f.kind = 1;
-      f.op = slip ? BCF_SLIP : (noslip ? BCF_NOSLIP : (type == 10 ? BCF_OUTFLOW : BCF_FARFIELD));
+      f.op = slip ? BCF_SLIP : (noslip ? BCF_NOSLIP : (type == 10 ? BCF_OUTFLOW :
+                                                      (outpres ? BCF_OUTPRES : BCF_FARFIELD)));
       f.inflow = type == 13;
       f.dir = d;
       f.n = (int64_t)fdst.size();
-      // BCzone.cpp DEFAULT_STATE, nbdata = 0: the free stream
-      f.st[0] = pr[ROINF];
-      f.st[1] = pr[VXINF] * pr[ROINF];
-      f.st[2] = pr[VYINF] * pr[ROINF];
-      f.st[3] = pr[VZINF] * pr[ROINF];
-      f.st[4] = pr[PINF] / (pr[GAMMA] - 1.) +
-                0.5 * (pr[VXINF] * f.st[1] + pr[VYINF] * f.st[2] + pr[VZINF] * f.st[3]);
+      // BCzone.cpp DEFAULT_STATE: the free stream (nbdata = 0) or the BC data
+      for (int m = 0; m < 5; m++) f.st[m] = bst[m];
+      f.nue = bst[5] / bst[0];
       if (dev_upload(&f.dst, fdst) != cudaSuccess || dev_upload(&f.src, fsrc) != cudaSuccess ||
-          dev_upload(&f.nrm, nrm) != cudaSuccess || dev_upload(&f.mt, fmt) != cudaSuccess)
+          dev_upload(&f.nrm, nrm) != cudaSuccess || dev_upload(&f.mt, fmt) != cudaSuccess ||
+          dev_upload(&f.aux, faux) != cudaSuccess)
         return fail(FGB_ERR_CUDA, "cannot upload BC lists");
       Z.bcs.push_back(f);
       if (!cdst.empty()) {
@@ -596,7 +665,7 @@ int fgb_destroy(fgb_solver* s) {
     cudaFree(Z.posmap);
     for (GatherList& g : Z.bcs) {
       cudaFree(g.dst); cudaFree(g.src); cudaFree(g.q0); cudaFree(g.q1); cudaFree(g.q2);
-      cudaFree(g.nrm); cudaFree(g.mt);
+      cudaFree(g.nrm); cudaFree(g.mt); cudaFree(g.aux);
     }
     cudaFree(Z.wig);
     cudaFree(Z.dist);
@@ -618,6 +687,7 @@ int fgb_destroy(fgb_solver* s) {
   for (LuGroupData& g : s->lu_groups) {
     cudaFree(g.cells); cudaFree(g.zid); cudaFree(g.plane); cudaFree(g.nbl); cudaFree(g.nbu);
     cudaFree(g.work); cudaFree(g.tab_dev); cudaFreeHost(g.tab_host);
+    cudaFree(g.cplane); cudaFree(g.cbase); cudaFree(g.dep); cudaFree(g.flag); cudaFree(g.ticket);
     for (int i = 0; i < LuGroupData::NSLOT; i++) if (g.ev[i]) cudaEventDestroy(g.ev[i]);
   }
   adj_free(s);
@@ -749,10 +819,12 @@ int fgb_add_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
     r[t] = (int32_t)rcv_idx[t];
   }
   CK(cudaSetDevice(s->device));
-  Transfer T{dnr_zone, rcv_zone, n, nullptr, nullptr};
+  Transfer T{dnr_zone, rcv_zone, n, nullptr, nullptr, {}, {}};
   CK(dev_upload(&T.dnr_idx, d));
   CK(dev_upload(&T.rcv_idx, r));
-  s->tr.push_back(T);
+  T.hd = std::move(d);
+  T.hr = std::move(r);
+  s->tr.push_back(std::move(T));
   return FGB_OK;
 }
 
@@ -774,8 +846,14 @@ int fgb_set_option(fgb_solver* s, const char* key, double value) {
     if (value != 64. && value != 32.) return fail(FGB_ERR_ARG, "lu_precision must be 64 or 32");
     s->lu_precision = (int)value;
   } else if (k == "lu_mode") {
-    if (value != 0. && value != 1.) return fail(FGB_ERR_ARG, "lu_mode must be 0 or 1");
+    if (value != 0. && value != 1. && value != 2.) return fail(FGB_ERR_ARG, "lu_mode must be 0, 1 or 2");
     s->lu_mode = (int)value;
+  } else if (k == "lu_wait_skew") {
+    if (value < 0 || value > 2) return fail(FGB_ERR_ARG, "lu_wait_skew must be 0, 1 or 2");
+    s->wait_skew = (int)value;
+  } else if (k == "lu_poll_limit") {
+    if (value < 64 || value > 1e12) return fail(FGB_ERR_ARG, "lu_poll_limit must be in [64, 1e12]");
+    s->poll_limit = (long long)value;
   } else if (k == "modulo_verif") {
     if (value < 1) return fail(FGB_ERR_ARG, "modulo_verif must be >= 1");
     s->modulo_verif = (int)value;
@@ -787,6 +865,9 @@ int fgb_set_option(fgb_solver* s, const char* key, double value) {
     s->graph = value != 0.;
   } else if (k == "zone_streams") {
     s->zone_streams = value != 0.;
+  } else if (k == "lu_grid") {
+    if (value < 0 || value > 1e6) return fail(FGB_ERR_ARG, "lu_grid must be in [0, 1e6]");
+    s->lu_grid = (int)value;
   } else {
     return fail(FGB_ERR_ARG, "unknown option " + k);
   }
@@ -803,6 +884,9 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value) {
   else if (k == "profile") *value = s->profile;
   else if (k == "graph") *value = s->graph;
   else if (k == "zone_streams") *value = s->zone_streams;
+  else if (k == "lu_grid") *value = s->lu_grid;
+  else if (k == "lu_poll_limit") *value = (double)s->poll_limit;
+  else if (k == "lu_wait_skew") *value = s->wait_skew;
   else return fail(FGB_ERR_ARG, "unknown option " + k);
   return FGB_OK;
 }
@@ -887,9 +971,13 @@ static int build_cat(ZoneData& Z) {
       (rc = alloc_i(&q1, n2)) || (rc = alloc_i(&q2, n2)))
     return rc;
   double* nr1 = nullptr;
+  double* ax1 = nullptr;
   if (n1 > 0) {
     CK(cudaMalloc(&nr1, sizeof(double) * 3 * (size_t)n1));
     Z.cat_mem.push_back(nr1);
+    CK(cudaMalloc(&ax1, sizeof(double) * (size_t)n1));
+    Z.cat_mem.push_back(ax1);
+    CK(cudaMemset(ax1, 0, sizeof(double) * (size_t)n1));
   }
   std::vector<int32_t> op0((size_t)n0), lid1((size_t)n1);
   std::vector<BcFaceArgs> lp;
@@ -907,6 +995,7 @@ static int build_cat(ZoneData& Z) {
       CK(cudaMemcpy(s1 + o1c, g.src, I * g.n, cudaMemcpyDeviceToDevice));
       CK(cudaMemcpy(m1 + o1c, g.mt, I * g.n, cudaMemcpyDeviceToDevice));
       CK(cudaMemcpy(nr1 + 3 * o1c, g.nrm, sizeof(double) * 3 * g.n, cudaMemcpyDeviceToDevice));
+      if (g.aux) CK(cudaMemcpy(ax1 + o1c, g.aux, sizeof(double) * g.n, cudaMemcpyDeviceToDevice));
       for (int64_t t = 0; t < g.n; t++) lid1[(size_t)(o1c + t)] = (int32_t)lp.size();
       BcFaceArgs a = face_args(Z, g);
       a.dst = nullptr; a.src = nullptr; a.nrm = nullptr;
@@ -929,7 +1018,7 @@ static int build_cat(ZoneData& Z) {
     CK(cudaMemcpy(Z.cat_lp, lp.data(), sizeof(BcFaceArgs) * lp.size(), cudaMemcpyHostToDevice));
   }
   Z.cat0 = GatherCat{d0, s0, o0, n0};
-  Z.cat1 = BcFaceCat{d1, s1, l1, m1, nr1, n1, Z.cat_lp};
+  Z.cat1 = BcFaceCat{d1, s1, l1, m1, nr1, n1, Z.cat_lp, ax1};
   GatherList g2;
   g2.dst = d2; g2.q0 = q0; g2.q1 = q1; g2.q2 = q2; g2.n = n2;
   Z.cat2 = next_args(Z, g2);
@@ -953,7 +1042,24 @@ static int build_transfers(fgb_solver* s) {
   for (Transfer& T : s->tr) n += T.n;
   s->tr_n = n;
   s->tr_built = s->tr.size();
-  if (n == 0) return FGB_OK;
+  // The one-launch fill copies every entry at once.  That equals the
+  // ordered fill (one transfer after the other, as the reference's list is
+  // processed) only if no cell is written twice and no donor cell is also a
+  // receiver; otherwise the fill keeps the ordered launches.
+  {
+    std::vector<std::vector<uint8_t>> rcv(s->zones.size());
+    for (size_t m = 0; m < s->zones.size(); m++) rcv[m].assign((size_t)s->zones[m].z.nd, 0);
+    s->tr_ordered = false;
+    for (Transfer& T : s->tr)
+      for (int32_t r : T.hr) {
+        if (rcv[(size_t)T.rcv][(size_t)r]) s->tr_ordered = true;
+        rcv[(size_t)T.rcv][(size_t)r] = 1;
+      }
+    for (Transfer& T : s->tr)
+      for (int32_t d : T.hd)
+        if (rcv[(size_t)T.dnr][(size_t)d]) s->tr_ordered = true;
+  }
+  if (n == 0 || s->tr_ordered) return FGB_OK;
   const size_t B = sizeof(int32_t) * (size_t)n;
   CK(cudaMalloc(&s->tr_rz, B)); CK(cudaMalloc(&s->tr_ri, B));
   CK(cudaMalloc(&s->tr_dz, B)); CK(cudaMalloc(&s->tr_di, B));
@@ -974,11 +1080,11 @@ static int build_transfers(fgb_solver* s) {
 // zones fit the kernel's table, else one per transfer
 static int fill_transfers(fgb_solver* s, int level) {
   if (s->tr.empty()) return FGB_OK;
-  if (s->zones.size() <= (size_t)ZT_MAX) {
-    if (s->tr_built != s->tr.size()) {
-      int rc = build_transfers(s);
-      if (rc) return rc;
-    }
+  if (s->tr_built != s->tr.size()) {
+    int rc = build_transfers(s);
+    if (rc) return rc;
+  }
+  if (s->zones.size() <= (size_t)ZT_MAX && !s->tr_ordered) {
     ZoneLevels zl{};
     for (size_t m = 0; m < s->zones.size(); m++) {
       zl.q[m] = s->zones[m].lvl[level];
@@ -1086,7 +1192,7 @@ static BcFaceArgs face_args(ZoneData& Z, GatherList& g) {
   a.cv = Z.pr[CVINF]; a.cvinv = 1. / Z.pr[CVINF];
   for (int m = 0; m < 5; m++) a.st[m] = g.st[m];
   a.sa = Z.z.neq == 6; a.inflow = g.inflow;
-  a.nue = Z.pr[RONUTILDEINF] / Z.pr[ROINF];
+  a.nue = g.nue;
   a.dir = g.dir;
   return a;
 }
@@ -1220,6 +1326,7 @@ static void free_lu_groups(fgb_solver* s) {
   for (LuGroupData& g : s->lu_groups) {
     cudaFree(g.cells); cudaFree(g.zid); cudaFree(g.plane); cudaFree(g.nbl); cudaFree(g.nbu);
     cudaFree(g.work); cudaFree(g.tab_dev); cudaFreeHost(g.tab_host);
+    cudaFree(g.cplane); cudaFree(g.cbase); cudaFree(g.dep); cudaFree(g.flag); cudaFree(g.ticket);
     for (int i = 0; i < LuGroupData::NSLOT; i++) if (g.ev[i]) cudaEventDestroy(g.ev[i]);
   }
   s->lu_groups.clear();
@@ -1229,11 +1336,19 @@ static void free_lu_groups(fgb_solver* s) {
 static LuGroup group_launch(fgb_solver* s, LuGroupData& g, LuZone* tab) {
   LuGroup L{};
   L.persistent = s->lu_mode;
+  L.grid_cap = s->lu_grid;
   L.fp32 = s->lu_precision == 32;
   L.bar = s->bar; L.err = s->derr;
   L.work = g.work; L.GG = g.GG; L.smax = g.smax;
   L.cells = g.cells; L.zid = g.zid; L.plane = g.plane; L.plane_host = g.plane_host.data();
   L.nbl = g.nbl; L.nbu = g.nbu; L.ztab = tab; L.nz = (int)g.zones.size();
+  FlowArgs& F = L.flow;
+  F.ticket = g.ticket; F.flag = g.flag; F.cplane = g.cplane; F.cbase = g.cbase; F.dep = g.dep;
+  F.nchunk = g.nchunk;
+  F.lower_mark = 2 * g.epoch + 1; F.upper_mark = 2 * g.epoch + 2;
+  F.wait_skew = s->wait_skew;
+  F.err = s->derr;
+  F.poll_limit = s->poll_limit;
   return L;
 }
 
@@ -1282,10 +1397,12 @@ static int build_lu_groups(fgb_solver* s) {
     if (g.GG >= (int64_t)INT32_MAX) return fail(FGB_ERR_ARG, "LU group larger than 2^31 cells");
     std::vector<uint32_t> cells((size_t)g.GG);
     std::vector<int32_t> zid((size_t)g.GG);
+    std::vector<std::vector<int32_t>> posmaps((size_t)nz);
     for (int q = 0; q < nz; q++) {
       ZoneData& Z = s->zones[g.zones[q]];
       const Zone& z = Z.z;
-      std::vector<int32_t> posmap((size_t)z.nd, -1);
+      std::vector<int32_t>& posmap = posmaps[(size_t)q];
+      posmap.assign((size_t)z.nd, -1);
       for (int64_t k = 0; k < z.nk; k++)
         for (int64_t j = 0; j < z.nj; j++)
           for (int64_t i = 0; i < z.ni; i++) {
@@ -1299,6 +1416,58 @@ static int build_lu_groups(fgb_solver* s) {
     CK(dev_upload(&g.cells, cells));
     CK(dev_upload(&g.zid, zid));
     CK(dev_upload(&g.plane, g.plane_host));
+    {  // dataflow chunks: 32 consecutive cells of a plane; the chunk ranges
+       // of the previous plane of each sweep that hold their neighbours
+      const int64_t C = lusgs_flow_chunk();
+      std::vector<int64_t> cbase((size_t)(np + 1), 0);
+      for (int64_t t = 0; t < np; t++)
+        cbase[(size_t)t + 1] = cbase[(size_t)t] + (g.plane_host[(size_t)t + 1] - g.plane_host[(size_t)t] + C - 1) / C;
+      g.nchunk = cbase[(size_t)np];
+      if (g.nchunk >= (int64_t)INT32_MAX / 4) return fail(FGB_ERR_ARG, "LU group too large");
+      std::vector<int32_t> cplane((size_t)g.nchunk), dep((size_t)(4 * g.nchunk));
+      auto chunk_of = [&](int64_t t, int64_t gg) {
+        return cbase[(size_t)t] + (gg - g.plane_host[(size_t)t]) / C;
+      };
+      for (int64_t t = 0; t < np; t++) {
+        for (int64_t c = cbase[(size_t)t]; c < cbase[(size_t)t + 1]; c++) {
+          cplane[(size_t)c] = (int32_t)t;
+          int64_t lo[2] = {INT64_MAX, INT64_MAX}, hi[2] = {-1, -1};
+          const int64_t g0 = g.plane_host[(size_t)t] + (c - cbase[(size_t)t]) * C;
+          const int64_t g1 = std::min(g0 + C, g.plane_host[(size_t)t + 1]);
+          for (int64_t gg = g0; gg < g1; gg++) {
+            const int q = zid[(size_t)gg];
+            const Zone& z = s->zones[g.zones[q]].z;
+            const std::vector<int32_t>& pm = posmaps[(size_t)q];
+            const uint32_t cc = cells[(size_t)gg];
+            const int64_t ii = cc & 2047u, jj = (cc >> 11) & 2047u, kk = cc >> 22;
+            const int64_t l = idx(s->zones[g.zones[q]].pi, ii + 1, jj + 1, kk + 1);
+            const int64_t ix[3] = {ii, jj, kk}, nn[3] = {z.ni, z.nj, z.nk};
+            for (int d = 0; d < 3; d++) {
+              if (ix[d] > 0) {
+                const int64_t c2 = chunk_of(t - 1, pm[(size_t)(l - z.inc[d])]);
+                lo[0] = std::min(lo[0], c2); hi[0] = std::max(hi[0], c2);
+              }
+              if (ix[d] < nn[d] - 1) {
+                const int64_t c2 = chunk_of(t + 1, pm[(size_t)(l + z.inc[d])]);
+                lo[1] = std::min(lo[1], c2); hi[1] = std::max(hi[1], c2);
+              }
+            }
+          }
+          for (int u = 0; u < 2; u++) {
+            if (hi[u] < 0) { lo[u] = 0; hi[u] = -1; }
+            dep[(size_t)(4 * c + 2 * u)] = (int32_t)lo[u];
+            dep[(size_t)(4 * c + 2 * u + 1)] = (int32_t)hi[u];
+          }
+        }
+      }
+      CK(dev_upload(&g.cplane, cplane));
+      CK(dev_upload(&g.cbase, cbase));
+      CK(dev_upload(&g.dep, dep));
+      CK(cudaMalloc(&g.flag, sizeof(int) * (size_t)g.nchunk));
+      CK(cudaMemset(g.flag, 0, sizeof(int) * (size_t)g.nchunk));
+      CK(cudaMalloc(&g.ticket, sizeof(unsigned long long)));
+      g.epoch = 0;
+    }
     CK(cudaMalloc(&g.nbl, sizeof(int32_t) * 3 * g.GG));
     CK(cudaMalloc(&g.nbu, sizeof(int32_t) * 3 * g.GG));
     CK(cudaMalloc(&g.work, sizeof(double) * g.GG * lusgs_work_words(s->zones[g.zones[0]].z.typ)));
@@ -1477,6 +1646,7 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
           CK(cudaMemcpyAsync(td, th, sizeof(LuZone) * nz, cudaMemcpyHostToDevice, s->st));
           CK(cudaEventRecord(g.ev[slot], s->st));
           g.ev_used[slot] = true;
+          g.epoch++;
           LuGroup L = group_launch(s, g, td);
           {
             ProfScope ps(s, "lu_sgs");
@@ -1814,6 +1984,9 @@ int fgb_residual_norms_noalloc(fgb_solver* s, int zone, double* out_dev) {
   if (!out_dev) return fail(FGB_ERR_ARG, "null output pointer");
   if (s->device < 0 || s->device >= kMaxDevices) return fail(FGB_ERR_ARG, "device index out of range");
   ZoneData& Z = s->zones[zone];
+  if (Z.pi[ITYPCP] > 1)
+    return fail(FGB_ERR_ARG, "residual norms are those of implicit zones (an explicit zone's "
+                             "drodm holds the RK3 stage combination, not a residual)");
   const int neq = Z.z.neq;
   const int64_t nblocks = Z.ijkv_lu[0] * Z.ijkv_lu[1] * Z.ijkv_lu[2];
   if (nblocks * 2 * neq > FGB_NORM_PARTIALS_MAX)
@@ -1852,7 +2025,8 @@ int fgb_synchronize(fgb_solver* s) {
   CK(cudaMemcpy(&h, s->derr, sizeof(int), cudaMemcpyDeviceToHost));
   if (h != 0) {
     CK(cudaMemset(s->derr, 0, sizeof(int)));
-    return fail(FGB_ERR_DEVICE, "a grid barrier of the LU-SGS kernel timed out");
+    return fail(FGB_ERR_DEVICE, h == 2 ? "a dependency wait of the LU-SGS dataflow sweep gave up"
+                                       : "a grid barrier of the LU-SGS kernel timed out");
   }
   return FGB_OK;
 }

@@ -129,9 +129,33 @@ __device__ __forceinline__ void non_reflection(const BcFaceArgs& a, const double
 }
 
 __device__ __forceinline__ void bc_face_entry(double* __restrict__ q, const BcFaceArgs& a,
-                                              int64_t l, int64_t s, const double t[3]) {
+                                              int64_t l, int64_t s, const double t[3],
+                                              double aux = 0.) {
   const int64_t nd = a.nd;
-  if (a.op == BCF_SLIP) {
+  if (a.op == BCF_OUTPRES) {
+    // BC/BCOutpres_i.for with BC/linearization_state.for: pressure pext
+    // imposed through the normal characteristic, linearised about the
+    // interior state (t = raw face normal x snorm)
+    const double tcx = t[0], tcy = t[1], tcz = t[2];
+    const double sn = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
+    const double s_1 = 1. / sn;
+    double tnx, tny, tnz;
+    if (sn == 0.) { tnx = 1.; tny = 0.; tnz = 0.; }
+    else { tnx = tcx * s_1; tny = tcy * s_1; tnz = tcz * s_1; }
+    const double rgp = a.cv * a.gam1;
+    const double roi = q[s], ui = q[s + nd], vi = q[s + 2 * nd], wi = q[s + 3 * nd], Ti = q[s + 4 * nd];
+    const double pi = roi * rgp * Ti;
+    const double ro0 = roi, p0 = ro0 * rgp * Ti;
+    const double roc0 = sqrt(ro0 * a.gam * p0);
+    const double dqn = (aux - pi) / roc0;
+    const double rog = roi + ro0 * ro0 * dqn / roc0;
+    q[l] = rog;
+    q[l + nd] = ui - dqn * tnx;
+    q[l + 2 * nd] = vi - dqn * tny;
+    q[l + 3 * nd] = wi - dqn * tnz;
+    q[l + 4 * nd] = aux / (rog * rgp);
+    if (a.sa) q[l + 5 * nd] = q[s + 5 * nd];          // BCOutpresSA_*.for
+  } else if (a.op == BCF_SLIP) {
     double tcx = t[0], tcy = t[1], tcz = t[2];
     double surf = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
     surf = fmaxF(surf, 1e-30);
@@ -189,7 +213,7 @@ __global__ void __launch_bounds__(128) bc_face_cat(double* __restrict__ q, BcFac
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= c.n) return;
   const double t[3] = {c.nrm[3 * e], c.nrm[3 * e + 1], c.nrm[3 * e + 2]};
-  bc_face_entry(q, c.lp[c.lid[e]], c.dst[e], c.src[e], t);
+  bc_face_entry(q, c.lp[c.lid[e]], c.dst[e], c.src[e], t, c.aux ? c.aux[e] : 0.);
 }
 
 __global__ void __launch_bounds__(256) gather_cat(double* __restrict__ q, int64_t nd, GatherCat c,

@@ -68,8 +68,27 @@ struct LuZone { Zone z; LuFields f; };
 // plane) or one launch per plane sweeps all zones together, so a group of
 // small blocks costs the barriers of its largest block, not of their sum.
 // FP64 or FP32 sweeps (mixed precision; the Newton update stays FP64).
+// Dataflow schedule of the sweeps (lusgs_flow): chunks of 32 consecutive
+// cells of a hyperplane, their completion marks and dependency ranges.
+struct FlowArgs {
+  unsigned long long* ticket;   // zeroed before each launch
+  int* flag;                    // [nchunk] completion mark of each chunk (never cleared)
+  const int32_t* cplane;        // [nchunk] hyperplane of each chunk
+  const int64_t* cbase;         // [smax + 2] first chunk of each hyperplane
+  const int32_t* dep;           // [nchunk][4] chunk ranges [lo, hi] holding the lower
+                                // neighbours (plane s-1) and the upper ones (plane s+1)
+  int64_t nchunk;
+  int lower_mark, upper_mark;   // 2 epoch + 1, 2 epoch + 2 (published)
+  int wait_skew;                // added to the marks a wait expects (0; > 0 only in tests)
+  int* err;                     // device error word (2: a wait gave up)
+  long long poll_limit;
+};
+int lusgs_flow_chunk();
+
 struct LuGroup {
-  int persistent;
+  int persistent;           // 0 one launch per plane, 1 grid barrier, 2 dataflow
+  FlowArgs flow;
+  int grid_cap;             // > 0: at most this many CTAs in the persistent sweep
   int fp32;
   unsigned int* bar;        // barrier counter (zeroed by the launcher)
   int* err;                 // device error word (barrier time-out)
@@ -106,7 +125,7 @@ struct NormArgs {
 cudaError_t launch_gather(double* dst, int64_t nd_dst, const double* src, int64_t nd_src,
                           const int32_t* d_idx, const int32_t* s_idx, int64_t n, int neq,
                           int op, double c, cudaStream_t st);
-enum { BCF_SLIP = 0, BCF_NOSLIP = 1, BCF_FARFIELD = 2, BCF_OUTFLOW = 3 };
+enum { BCF_SLIP = 0, BCF_NOSLIP = 1, BCF_FARFIELD = 2, BCF_OUTFLOW = 3, BCF_OUTPRES = 4 };
 struct BcFaceArgs {            // one face BC window (bc_face)
   const int32_t* dst;          // ghost cells
   const int32_t* src;          // mirror cell (walls) or first interior cell
@@ -127,6 +146,7 @@ struct BcFaceCat {
   const double* nrm;
   int64_t n;
   const BcFaceArgs* lp;
+  const double* aux;           // per entry: imposed pressure (BCOutpres), else 0
 };
 // All gather windows of a zone (periodic, extrapolation) as one list with
 // the operation of each entry (0 copy, 1 max(-1e30, x))

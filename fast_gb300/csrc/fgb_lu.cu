@@ -842,6 +842,80 @@ __global__ void __launch_bounds__(LuThreads<T>::n, 1)
   }
 }
 
+// ------------------------------------------------------- dataflow sweep
+// Lower and upper sweeps as one launch of independent warps, with no grid
+// barrier.  Each hyperplane's cells (contiguous in plane order) are cut into
+// chunks of 32; a warp takes chunks in order from a global ticket counter
+// (all lower chunks by increasing plane, then all upper chunks by decreasing
+// plane), waits until the chunks holding its cells' neighbours in the
+// previous plane of the sweep have published their completion mark, sweeps
+// its 32 cells (one per lane, the cell code of the other schedules) and
+// publishes its own mark.  A warp only ever waits on chunks with smaller
+// tickets, which running warps already hold, so the launch cannot deadlock
+// whatever the number of resident CTAs; a plane starts as soon as the
+// cells it needs are done instead of after the whole previous plane, and the
+// FP64 pipes stay busy across plane boundaries.  An upper chunk also waits on
+// its own lower mark (its cells' lower results).  Marks are 2 e + 1 (lower)
+// and 2 e + 2 (upper) of the solve's epoch e, so the flags are never
+// cleared.  Waits are bounded: past poll_limit polls a lane sets the error
+// word and every warp returns.
+constexpr int FLOW_CHUNK = 32;
+constexpr int FLOW_THREADS = 256;
+
+__device__ __forceinline__ bool flow_poll(const FlowArgs& a, int64_t c, int mark) {
+  long long spins = 0;
+  while (true) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(a.flag + c) : "memory");
+    if (v >= mark) return true;
+    if ((++spins & 63) == 0) {
+      if (*(volatile int*)a.err) return false;
+      if (spins > a.poll_limit) { atomicExch(a.err, 2); return false; }
+    }
+  }
+}
+
+template <int TYP, typename T, int NV, bool MULTI, bool UPPER>
+__device__ __forceinline__ void flow_chunk(const Zone& z, const PlaneData<T>& p, const LuFields& f,
+                                           int64_t g0, int64_t n, int lane) {
+  if (lane < n) {
+    CellOps<TYP, T, NV> o;
+    load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, g0 + lane, o);
+    run_cell_of<TYP, T, UPPER, NV, MULTI>(z, p, f, g0 + lane, o);
+  }
+}
+
+template <int TYP, typename T, int NV, bool MULTI>
+__global__ void __launch_bounds__(FLOW_THREADS)
+    lusgs_flow(Zone z, PlaneData<T> p, LuFields f, FlowArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nc = a.nchunk;
+  while (true) {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(a.ticket, 1ull);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= (unsigned long long)(2 * nc)) return;
+    if (*(volatile int*)a.err) return;
+    const bool upper = t >= (unsigned long long)nc;
+    const int64_t ch = upper ? 2 * nc - 1 - (int64_t)t : (int64_t)t;
+    const int32_t* dp = a.dep + 4 * ch + (upper ? 2 : 0);
+    const int64_t lo = dp[0], hi = dp[1];
+    const int mark = upper ? a.upper_mark : a.lower_mark;
+    bool ok = true;
+    for (int64_t c = lo + lane; c <= hi; c += 32) ok = ok && flow_poll(a, c, mark + a.wait_skew);
+    if (upper && lane == 0) ok = ok && flow_poll(a, ch, a.lower_mark + a.wait_skew);
+    if (!__all_sync(0xffffffffu, ok)) return;
+    const int s = a.cplane[ch];
+    const int64_t g0 = p.plane[s] + (ch - a.cbase[s]) * FLOW_CHUNK;
+    const int64_t n = p.plane[s + 1] - g0;
+    if (upper) flow_chunk<TYP, T, NV, MULTI, true>(z, p, f, g0, n, lane);
+    else flow_chunk<TYP, T, NV, MULTI, false>(z, p, f, g0, n, lane);
+    __syncwarp();
+    if (lane == 0)
+      asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(a.flag + ch), "r"(mark) : "memory");
+  }
+}
+
 // one launch per hyperplane (no inter-CTA waits): cross-check of the
 // persistent kernel
 template <int TYP, typename T, bool UPPER, int NV, bool MULTI>
@@ -945,16 +1019,45 @@ template <int TYP, typename T, int NV, bool MULTI>
 static cudaError_t sweep_t(const Zone& z, const LuFields& f, const PlaneData<T>& p, const LuGroup& L,
                            cudaStream_t st) {
   cudaError_t e;
-  if (L.persistent) {
-    static int grid = 0;   // per instantiation (one device per process in practice)
-    if (grid == 0) {
-      int dev = 0, nsm = 0, per = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T, NV, MULTI>,
-                                                    LuThreads<T>::n, 0);
-      grid = nsm * (per > 0 ? per : 1);
+  if (L.persistent == 2) {
+    static int grids[64] = {};   // per instantiation and device: resident CTAs
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (grids[dev] == 0) {
+      int nsm = 0, per = 0;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_flow<TYP, T, NV, MULTI>,
+                                                        FLOW_THREADS, 0);
+      if (e != cudaSuccess) return e;
+      grids[dev] = nsm * (per > 0 ? per : 1);
     }
+    int grid = grids[dev];
+    if (L.grid_cap > 0 && L.grid_cap < grid) grid = L.grid_cap;
+    e = cudaMemsetAsync(L.flow.ticket, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    lusgs_flow<TYP, T, NV, MULTI><<<grid, FLOW_THREADS, 0, st>>>(z, p, f, L.flow);
+    return cudaGetLastError();
+  }
+  if (L.persistent) {
+    static int grids[64] = {};   // per instantiation and device: resident CTAs of the sweep
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (grids[dev] == 0) {
+      int nsm = 0, per = 0;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_persistent<TYP, T, NV, MULTI>,
+                                                        LuThreads<T>::n, 0);
+      if (e != cudaSuccess) return e;
+      grids[dev] = nsm * (per > 0 ? per : 1);
+    }
+    int grid = grids[dev];
+    if (L.grid_cap > 0 && L.grid_cap < grid) grid = L.grid_cap;
     e = cudaMemsetAsync(L.bar, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     GridBar gb{L.bar, L.err};
@@ -1017,6 +1120,8 @@ static PlaneData<T> plane_data(const LuGroup& L, int rec_size) {
   p.smax = L.smax; p.zid = L.zid; p.zt = L.ztab;
   return p;
 }
+
+int lusgs_flow_chunk() { return FLOW_CHUNK; }
 
 // words of LU work per interior cell (the caller allocates G * this * 8 bytes)
 int64_t lusgs_work_words(int typ) {

@@ -347,26 +347,37 @@ def getDir(ijkv, f):
 
 
 def _BCcompact(t):
-    """Append the BC block to Parameter_int (PyTree.py:2788-3038): at
-    param_int[PT_BC]: [nb_bc, ptr_int(nb_bc), ptr_real(nb_bc)], then per BC
-    [type, idir, window(6), nbdata]."""
+    """Append the BC block to Parameter_int and the BC data to
+    Parameter_real (PyTree.py:2788-3038): at param_int[PT_BC]: [nb_bc,
+    ptr_int(nb_bc), ptr_real(nb_bc)], then per BC [type, idir, window(6),
+    nbdata, cumulative data sizes(nbdata)]; the DataArray_t nodes found
+    within three levels of the BC node (BCDataSet / BCData / DataArray)
+    are concatenated at the end of param_real, in that order, and the
+    tree's data nodes become views of param_real, as FastC does."""
     for z in I.getZones(t):
         o = I.getNodeFromName1(z, ".Solver#ownData")
         pnode = I.getNodeFromName1(o, "Parameter_int")
+        rnode = I.getNodeFromName1(o, "Parameter_real")
         pi = pnode[1]
         bcs = I.getNodesFromType2(z, "BC_t")
         nb = len(bcs)
+        bcdata = [I.getNodesFromType3(bc, "DataArray_t") for bc in bcs]
         c = pi.size
-        size_int = 1 + nb * 2 + 9 * nb
+        size_int = 1 + nb * 2 + 9 * nb + sum(len(d) for d in bcdata)
+        size_real = sum(int(np.asarray(a[1]).size) for d in bcdata for a in d)
         data = np.zeros(c + size_int, dtype=np.int64)
         data[:c] = pi
         data[PT_BC] = c
         data[c] = nb
+        cr = rnode[1].size
+        real = np.zeros(cr + size_real, dtype=np.float64)
+        real[:cr] = rnode[1]
         size = 1 + 2 * nb
+        size_r = 0
         for n, bc in enumerate(bcs):
             pt = c + size
             data[c + 1 + n] = pt
-            data[c + 1 + n + nb] = pnode[1].size if False else 0
+            data[c + 1 + n + nb] = cr + size_r
             btype = I.getValue(bc)
             if btype not in tagBCDict:
                 raise ValueError(f"compact: unknown BC type {btype}")
@@ -377,9 +388,19 @@ def _BCcompact(t):
             f = getRange(in_bc, data)
             data[pt + 2:pt + 8] = f
             data[pt + 1] = getDir(data[IJKV:IJKV + 3], f)
-            data[pt + 8] = 0
-            size += 9
+            data[pt + 8] = len(bcdata[n])
+            ctot = 0
+            for j, arr in enumerate(bcdata[n]):
+                v = np.asarray(arr[1], dtype=np.float64)
+                deb = cr + size_r
+                real[deb:deb + v.size] = v.ravel(order="F")
+                arr[1] = real[deb:deb + v.size]
+                ctot += v.size
+                data[pt + 9 + j] = ctot
+                size_r += v.size
+            size += 9 + len(bcdata[n])
         pnode[1] = data
+        rnode[1] = real
 
 
 # ---------------------------------------------------------- prim vars

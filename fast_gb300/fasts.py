@@ -116,6 +116,72 @@ def prepare(t):
     return metrics
 
 
+def cfl_time_step(t, cfl):
+    """Global time step that gives the CFL number ``cfl`` on the tree's
+    current state, by the local time-step formula of cpcfl3.for
+    (FastS/FastS/Compute/cpcfl3.for:88-140, LALE = 0): per interior cell
+    comp = min(vis, conv) with conv = 2 vol surf / (|u| + c), vis =
+    2 ro vol^2 surf^2 Pr / (gamma mu) (Navier-Stokes only) and surf = 1 /
+    max over directions of the sum of the two face-normal norms; the CFL of a
+    cell is dt / comp, so dt = cfl x the smallest comp over every zone.
+    Euler and laminar zones (mu from invist.for).  The tree is not
+    modified: the state is read from a copy prepared as warmup does."""
+    import copy
+    tt = copy.deepcopy(t)
+    ms = prepare(tt)
+    best = math.inf
+    for zd in zone_data(tt, ms):
+        pi, pr = zd["pi"], zd["pr"]
+        if int(pi[FastC.IFLOW]) > 2:
+            raise ValueError("cfl_time_step: Euler and laminar zones only")
+        nd = int(pi[FastC.NDIMDX])
+        ni, nj, nk = (int(pi[FastC.IJKV + d]) for d in range(3))
+        ng, ngk = int(pi[FastC.NIJK + 3]), int(pi[FastC.NIJK + 4])
+        nip, njp = int(pi[FastC.NIJK]), int(pi[FastC.NIJK + 1])
+        k, j, i = np.meshgrid(np.arange(1, nk + 1), np.arange(1, nj + 1), np.arange(1, ni + 1),
+                              indexing="ij")
+        l = ((i + ng - 1) + (j + ng - 1) * nip + (k + ngk - 1) * nip * njp).reshape(-1)
+        typ = int(pi[FastC.ITYPZONE])
+        ti, tj, tk, vol = zd["ti"], zd["tj"], zd["tk"], zd["vol"]
+        if typ == 2:       # 3-d cartesian: one metric value per family
+            dd = [np.sqrt(a[0] * a[0]) + np.sqrt(a[0] * a[0]) for a in (ti, tj, tk)]
+            surf = 1.0 / max(dd)
+            vv = vol[0]
+        else:
+            minc = [int(pi[FastC.NIJK_MTR + d]) for d in range(3)]
+            mg, mgk = int(pi[FastC.NIJK_MTR + 3]), int(pi[FastC.NIJK_MTR + 4])
+            ndm = int(pi[FastC.NDIMDX_MTR])
+            lt = ((i + mg - 1) * minc[0] + (j + mg - 1) * minc[1] + (k + mgk - 1) * minc[2]).reshape(-1)
+            ncomp = 2 if typ == 3 else 3
+            dd = []
+            for dd_d, a in enumerate((ti, tj, tk)):
+                if typ == 3 and dd_d == 2:
+                    dd.append(np.zeros(lt.size))
+                    continue
+                hi = lt + minc[dd_d]
+                sa = sum(a[hi + c * ndm] * a[hi + c * ndm] for c in range(ncomp))
+                sb = sum(a[lt + c * ndm] * a[lt + c * ndm] for c in range(ncomp))
+                dd.append(np.sqrt(sa) + np.sqrt(sb))
+            surf = 1.0 / np.maximum(np.maximum(dd[0], dd[1]), dd[2])
+            vv = vol[lt]
+        q = zd["ro"]
+        r, u, v, w, temp = (q[l + m * nd] for m in range(5))
+        gam = pr[FastC.GAMMA]
+        rgp = pr[FastC.CVINF] * (gam - 1.0)
+        c = np.sqrt(gam * rgp * temp)
+        conv = 2.0 * vv * surf * (1.0 / (np.sqrt(u * u + v * v + w * w) + c))
+        comp = conv
+        if int(pi[FastC.IFLOW]) == 2:     # invist.for viscosity
+            cs = pr[FastC.CS]
+            temp01 = 1.0 / pr[FastC.TEMP0]
+            coesut = pr[FastC.XMUL0] * (1.0 + cs * temp01) * math.sqrt(temp01)
+            xmut = coesut * np.sqrt(temp) * temp / (temp + cs)
+            vis = 2.0 * r * vv * vv * surf * surf * ((gam / pr[FastC.PRANDT]) / xmut)
+            comp = np.minimum(vis, conv)
+        best = min(best, float(np.min(comp)))
+    return cfl * best
+
+
 def zone_data(t, metrics):
     """Per zone: param_int, param_real, metric views and the three compacted
     time levels (flat float64 views into the tree)."""

@@ -105,6 +105,20 @@ def getNodesFromType2(node, ntype):
     return out
 
 
+def getNodesFromType3(node, ntype):
+    """Nodes of type ntype among the children, grandchildren and
+    great-grandchildren of node, depth first."""
+    out = []
+    for c in node[2]:
+        if c[3] == ntype:
+            out.append(c)
+        for cc in c[2]:
+            if cc[3] == ntype:
+                out.append(cc)
+            out.extend(ccc for ccc in cc[2] if ccc[3] == ntype)
+    return out
+
+
 def getNodesFromType(node, ntype):
     out = [node] if node[3] == ntype else []
     for c in node[2]:

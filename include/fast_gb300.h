@@ -77,7 +77,10 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * stream launches (profiling always uses stream launches); "zone_streams":
  * 1 (default) to run the per-zone kernels of several zones on 8 side streams
  * (zone m on stream m mod 8, joined before each LU-SGS solve and after each
- * ghost fill), 0 for the solver stream alone (profiling uses it alone). */
+ * ghost fill), 0 for the solver stream alone (profiling uses it alone);
+ * "lu_grid": 0 (default) for one persistent LU-SGS sweep CTA per resident
+ * slot of the device, n > 0 for at most n CTAs (each CTA then takes more
+ * cells of a hyperplane: same results, a schedule for testing). */
 int fgb_set_option(fgb_solver* s, const char* key, double value);
 int fgb_get_option(fgb_solver* s, const char* key, double* value);
 
@@ -166,7 +169,9 @@ int fgb_tangent(fgb_solver* s, int zone, int nsteps, const double* dw0, const do
  *   out_dev[ne] = L2,  out_dev[neq + ne] = Loo   (ne < neq)
  * with the LU-block decomposition, summation order and 1/DTC scaling of
  * fgb_residuals, so on the same state the values equal the last column that
- * entry reports.  out_dev: 2*neq doubles of device memory on the solver's
+ * entry reports.  Implicit (dual time, LU-SGS) zones only: an explicit zone's
+ * right-hand-side array holds the RK3 stage combination, not a residual, and
+ * is rejected with FGB_ERR_ARG.  out_dev: 2*neq doubles of device memory on the solver's
  * device.  Asynchronous on the solver stream; fgb_synchronize waits for it.
  *
  * For callers that cannot allocate: a convergence monitor that runs between

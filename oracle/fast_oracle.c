@@ -33,7 +33,7 @@ enum { DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6,
        PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14,
        PSIROE = 34, WIG_AMP = 72, VXINF = 19, VYINF = 20, VZINF = 21,
        RONUTILDEINF = 8, SA_RATIOM_R = 18, PRANDT_TUR = 38 };
-enum { BC_TYPE = 0, BC_IDIR = 1, BC_FEN = 2 };
+enum { BC_TYPE = 0, BC_IDIR = 1, BC_FEN = 2, BC_NBDATA = 8 };
 
 #define OMAX(a, b) ((a) > (b) ? (a) : (b))
 #define OMIN(a, b) ((a) < (b) ? (a) : (b))
@@ -2095,6 +2095,24 @@ void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const dou
       double snorm = low ? -1. : 1.;
       double st[5];
       bc_default_state(pr, st);
+      double nue_bc = nue;
+      /* BC data (BCzone.cpp:324-325 and DEFAULT_STATE): nbdata arrays in
+       * param_real at param_int[pt_bcs + 1 + nb_bc + n], cumulative sizes at
+       * param_int[pt + BC_NBDATA + 1 ...] */
+      int64_t nbdata = pi[pt + BC_NBDATA];
+      const double* bdata = nbdata > 0 ? pr + pi[pt_bcs + 1 + nb_bc + n] : 0;
+      if (nbdata > 0 && (type == 1 || type == 13 || type == 10)) {
+        if (nbdata == 21) {
+          for (int m = 0; m < 5; m++) st[m] = bdata[3 + m];
+          nue_bc = bdata[16] / st[0];
+        } else {
+          for (int m = 0; m < 5; m++) st[m] = bdata[m];
+          if (sa) nue_bc = bdata[5] / st[0];
+        }
+      }
+      const double* pext = 0;  /* BCOutpres: per-face pressure (bvbs_outpres.for) */
+      if (type == 16) pext = pi[pt + BC_NBDATA + 1] == 1 ? bdata + 1 : bdata;
+      const int64_t* fen = pi + pt + BC_FEN;
       for (int64_t b = cl[2 * tb]; b <= cl[2 * tb + 1]; b++)
         for (int64_t a = cl[2 * ta]; a <= cl[2 * ta + 1]; a++) {
           int64_t c[3];
@@ -2144,7 +2162,29 @@ void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const dou
               rop[l + nd] = u; rop[l + 2 * nd] = v; rop[l + 3 * nd] = w;
               rop[l + 4 * nd] = (o.qvar5 * roinv - .5 * (u * u + v * v + w * w)) * cvinv;
               /* BCFarfield_firstrank_SA.for (eigv1 = qn) / BCInflow_firstrank_SA.for */
-              if (sa) rop[l + 5 * nd] = (type == 13 || o.qn < 0.) ? nue : rop[l1 + 5 * nd];
+              if (sa) rop[l + 5 * nd] = (type == 13 || o.qn < 0.) ? nue_bc : rop[l1 + 5 * nd];
+            } else if (rank == 0 && type == 16) {   /* BCOutpres_i.for + linearization_state.for */
+              const double rgp = pr[CVINF] * (pr[GAMMA] - 1.), gam = pr[GAMMA];
+              int64_t li = (a - fen[2 * ta]) + (b - fen[2 * tb]) * (fen[2 * ta + 1] - fen[2 * ta] + 1);
+              double tcx = t[0] * snorm, tcy = t[1] * snorm, tcz = t[2] * snorm;
+              double sn = sqrt(tcx * tcx + tcy * tcy + tcz * tcz);
+              double s_1 = 1. / sn, tnx, tny, tnz;
+              if (sn == 0.) { tnx = 1.; tny = 0.; tnz = 0.; }
+              else { tnx = tcx * s_1; tny = tcy * s_1; tnz = tcz * s_1; }
+              double roi = rop[l1], ui = rop[l1 + nd], vi = rop[l1 + 2 * nd], wi = rop[l1 + 3 * nd],
+                     Ti = rop[l1 + 4 * nd];
+              double pin = roi * rgp * Ti;
+              double ro0 = rop[l1], T0 = rop[l1 + 4 * nd];
+              double p0 = ro0 * rgp * T0;
+              double roc0 = sqrt(ro0 * gam * p0);
+              double dqn = (pext[li] - pin) / roc0;
+              double rog = roi + ro0 * ro0 * dqn / roc0;   /* ro0**2. */
+              rop[l] = rog;
+              rop[l + nd] = ui - dqn * tnx;
+              rop[l + 2 * nd] = vi - dqn * tny;
+              rop[l + 3 * nd] = wi - dqn * tnz;
+              rop[l + 4 * nd] = pext[li] / (rog * rgp);
+              if (sa) rop[l + 5 * nd] = rop[l1 + 5 * nd];   /* BCOutpresSA_i.for */
             } else if (rank == 0 && type == 10) {                  /* BCOutflow.for */
               double roe = rop[l1], rue = rop[l1 + nd] * roe, rve = rop[l1 + 2 * nd] * roe,
                      rwe = rop[l1 + 3 * nd] * roe;
@@ -2179,7 +2219,7 @@ void or_bc_zone(const int64_t* pi, const double* pr, const double* ti, const dou
                 for (int v = 1; v < neq; v++)
                   rop[l + v * nd] = rop[q0 + v * nd] * k3 + rop[q1 + v * nd] * k1 + rop[q2 + v * nd] * k2;
               }
-            } else if (type == 10) {                /* BC_extrap.for: copy of the first ghost */
+            } else if (type == 10 || type == 16) {  /* BC_extrap.for: copy of the first ghost */
               int64_t cf[3] = {c[0], c[1], c[2]};
               cf[d] = first;
               int64_t q0 = inddm(pi, cf[0], cf[1], cf[2]);

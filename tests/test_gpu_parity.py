@@ -151,11 +151,12 @@ def test_errors_are_reported_not_fatal():
 
 
 def test_lu_persistent_equals_plane_launches(oracle_mod):
-    """The persistent cooperative sweep and the one-launch-per-hyperplane
-    sweep give the same bits (same cell arithmetic, different schedule)."""
+    """The dataflow sweep, the persistent grid-barrier sweep and the
+    one-launch-per-hyperplane sweep give the same bits (same cell
+    arithmetic, different schedules)."""
     from fast_gb300._native import Solver
     res = []
-    for mode in (0, 1):
+    for mode in (0, 1, 2):
         t = cases.taylor_green(n=(14, 12, 10), ss_iteration=3)
         zd, ref, s = _pair(t, oracle_mod, 1)
         s.set_option("lu_mode", mode)
@@ -164,8 +165,9 @@ def test_lu_persistent_equals_plane_launches(oracle_mod):
         s.synchronize()
         res.append([s.download(0, lvl) for lvl in range(3)])
         s.close()
-    for a, b in zip(*res):
-        assert np.array_equal(a, b)
+    for other in res[1:]:
+        for a, b in zip(res[0], other):
+            assert np.array_equal(a, b)
 
 
 def test_mixed_precision_sweeps(oracle_mod):

@@ -60,10 +60,16 @@ def test_noalloc_norms_reject_oversized_zone_and_host_buffer():
     from fast_gb300 import cases
     from fast_gb300._native import FastGB300Error
     # 4 x 580 x 580 cells: 1 x 58 x 58 = 3364 LU blocks > 32768 / (2 * 5)
-    t = cases.isentropic_vortex(n=(4, 580, 580))
+    t = cases.taylor_green(n=(4, 580, 580), ss_iteration=1)
     zd, s = _solver(t, modulo_verif=1000)
     out = torch.empty(10, dtype=torch.float64, device="cuda:0")
     with pytest.raises(FastGB300Error, match="FGB_NORM_PARTIALS_MAX"):
+        s.residual_norms_noalloc(0, out.data_ptr())
+    s.close()
+    # an explicit zone has no residual to reduce
+    t = cases.isentropic_vortex(n=(16, 12, 4))
+    zd, s = _solver(t, modulo_verif=1000)
+    with pytest.raises(FastGB300Error, match="implicit zones"):
         s.residual_norms_noalloc(0, out.data_ptr())
     s.close()
     t = cases.taylor_green(n=(12, 10, 8), ss_iteration=1)
