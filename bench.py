@@ -298,6 +298,10 @@ def run_ours(args, d: Dist):
     ms = s.timer_stop()
     clk = clocks.stop()
     launches = s.launch_count() - l0
+    tuned = s.get_option("lu_tuned")
+    lu_sched = {"lu_mode": args.lu_mode,
+                "autotuned": None if tuned < 0 else {"lu_mode": int(tuned) // 10,
+                                                     "ctas_per_sm": int(tuned) % 10}}
     d.barrier()
     value, ms_max = replica_throughput(d, cells, args.steps, ms)
 
@@ -410,6 +414,7 @@ def run_ours(args, d: Dist):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches,
             "kernel_ms_per_step": {k: v[1] for k, v in stats.items()},
+            "lu_schedule": lu_sched,
             "mixed_precision": mixed,
             "ttc": ttc,
             "adjoint": adj,

@@ -27,6 +27,8 @@ SIGNATURES = {
     "fgb_add_zone": ([_P, _I64P, C.c_int64, _DP, C.c_int64, _DP, _DP, _DP, _DP,
                       C.POINTER(C.c_int)], C.c_int),
     "fgb_add_transfer": ([_P, C.c_int, C.c_int, C.c_int64, _I64P, _I64P], C.c_int),
+    "fgb_add_interp_transfer": ([_P, C.c_int, C.c_int, C.c_int64, _I64P, _I64P, _I64P, _DP,
+                                 C.c_int64], C.c_int),
     "fgb_set_wall_distance": ([_P, C.c_int, _DP], C.c_int),
     "fgb_set_option": ([_P, C.c_char_p, C.c_double], C.c_int),
     "fgb_get_option": ([_P, C.c_char_p, _DP], C.c_int),
@@ -137,6 +139,24 @@ class Solver:
         d = np.ascontiguousarray(dnr_idx, dtype=np.int64)
         r = np.ascontiguousarray(rcv_idx, dtype=np.int64)
         _check(self._lib.fgb_add_transfer(self._h, int(dnr), int(rcv), d.size, _ip(d), _ip(r)))
+
+    def add_interp_transfer(self, dnr, rcv, dnr_idx, rcv_idx, types, coefs):
+        """Overset interpolation (types 0/1, 2, 22, 3, 5; coefficients of
+        every point concatenated)."""
+        d = np.ascontiguousarray(dnr_idx, dtype=np.int64)
+        r = np.ascontiguousarray(rcv_idx, dtype=np.int64)
+        ty = np.ascontiguousarray(types, dtype=np.int64)
+        c = np.ascontiguousarray(coefs, dtype=np.float64)
+        _check(self._lib.fgb_add_interp_transfer(self._h, int(dnr), int(rcv), d.size, _ip(d), _ip(r),
+                                                 _ip(ty), _dp(c), c.size))
+
+    def add_any_transfer(self, tr):
+        """A transfer dict (dnr, rcv, dnr_idx, rcv_idx[, types, coefs])."""
+        if "types" in tr:
+            self.add_interp_transfer(tr["dnr"], tr["rcv"], tr["dnr_idx"], tr["rcv_idx"], tr["types"],
+                                     tr["coefs"])
+        else:
+            self.add_transfer(tr["dnr"], tr["rcv"], tr["dnr_idx"], tr["rcv_idx"])
 
     def set_wall_distance(self, zone: int, dist):
         """TurbulentDistance of a Spalart-Allmaras zone (NDIMDX values)."""

@@ -18,6 +18,7 @@ layers), which FastC's getRange converts back to interior windows.
 """
 from __future__ import annotations
 
+import copy
 import math
 
 import numpy as np
@@ -138,7 +139,8 @@ def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0,
         nk = 1
         n = (ni, nj, 1)
     h = (2 * box / ni, 2 * box / nj, 2 * box / ni)
-    z = cart_zone("vortex", (-box, -box, 0.0), h, n, ngk=0 if two_d else None)
+    ng = _ghosts("roe_min", numz)
+    z = cart_zone("vortex", (-box, -box, 0.0), h, n, ng=ng, ngk=0 if two_d else None)
     if wavy:
         wave(z, wavy, (-box, -box, 0.0), (2 * box, 2 * box, h[2] * nk), two_d=two_d)
     xc, yc, _ = cell_centers(z)
@@ -153,7 +155,7 @@ def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0,
     p = ro * T / gamma
     set_conservative(z, ro, mach + du, dv, np.zeros_like(ro), p, gamma)
     for f in ("imin", "imax", "jmin", "jmax") + (() if two_d else ("kmin", "kmax")):
-        add_bc(z, "per_" + f, "BCautoperiod", f)
+        add_bc(z, "per_" + f, "BCautoperiod", f, ng=ng)
     numb = numb or {"temporal_scheme": "explicit", "ss_iteration": 1, "modulo_verif": 1000000}
     numz = numz or {"scheme": "roe_min", "slope": "minmod", "time_step": 0.01,
                     "cache_blocking_I": 1000000, "cache_blocking_J": 1000000,
@@ -163,6 +165,12 @@ def isentropic_vortex(n=(128, 128, 4), mach=0.5, beta=5.0, radius=1.0, box=10.0,
         from . import fasts
         FastC._setNum2Zones(t, {"time_step": fasts.cfl_time_step(t, cfl)})
     return t
+
+
+def _ghosts(slope, numz=None):
+    """Ghost layers of a zone: three for the o5 slopes (o5, o5sc), else two."""
+    sl = (numz or {}).get("slope", slope)
+    return 3 if sl in ("o5", "o5sc") else NG
 
 
 def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_iteration=4,
@@ -176,7 +184,8 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
     N = (n, n, n) if isinstance(n, int) else tuple(n)
     L = 1.0
     h = tuple(2 * math.pi * L / k for k in N)
-    z = cart_zone(name, (0.0, 0.0, 0.0), h, N)
+    ng = _ghosts(slope, numz)
+    z = cart_zone(name, (0.0, 0.0, 0.0), h, N, ng=ng)
     if wavy:
         wave(z, wavy, (0.0, 0.0, 0.0), tuple(2 * math.pi * L for _ in range(3)))
     xc, yc, zc = cell_centers(z)
@@ -192,7 +201,7 @@ def taylor_green(n=256, mach=0.1, reynolds=1600.0, prandtl=0.71, gamma=1.4, ss_i
     if model == "NSTurbulent":
         set_spalart(z, nutilde_ratio * (mach / reynolds) / ro, np.full_like(ro, wall_distance))
     for f in ("imin", "imax", "jmin", "jmax", "kmin", "kmax"):
-        add_bc(z, "per_" + f, "BCautoperiod", f)
+        add_bc(z, "per_" + f, "BCautoperiod", f, ng=ng)
     if dt is None:
         dt = 2.0 * h[0] / (U0 + 1.0)   # acoustic CFL 2 (implicit dual time)
     numb = numb or {"temporal_scheme": "implicit", "ss_iteration": ss_iteration,
@@ -217,7 +226,8 @@ def add_bc_data(bc, arrays):
 def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model="NSLaminar",
            wavy=0.0, perturb=0.05, temporal="explicit", ss_iteration=3, scheme="ausmpred",
            slope="o3", time_step=0.02, gamma=1.4, two_d=False, nutilde_ratio=5.0,
-           extrude=False, outflow="BCOutflow", outpres_form=1, outpres_amp=0.02, bc_data=False):
+           extrude=False, outflow="BCOutflow", outpres_form=1, outpres_amp=0.02, bc_data=False,
+           stretch=0.0):
     """Box [0,1]x[0,1]x[0,dz] exercising the non-periodic BCs of the path:
     inflow at imin (BCInflow), outflow at imax (BCOutflow), a wall at jmin
     (``wall``), farfield at jmax (BCFarfield), periodic in k.  The initial
@@ -232,6 +242,8 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
     per face (p_inf (1 + outpres_amp sin(2 pi y))) given as BC data -- the pressure
     array alone (outpres_form 1) or after a one-value mobile_coef array
     (outpres_form 2), the two layouts bvbs_outpres reads.
+    stretch > 0: the vertex y clustered at the jmin wall, y -> sinh(stretch y)
+    / sinh(stretch) (a mesh homogeneous in k: zone type 1).
     bc_data: the farfield and inflow states come from BC data instead of the
     free stream (conservative ro, ro u, ro v, ro w, ro E [, ro nutilde],
     a 2-3 % departure from it): the farfield as one array of those values,
@@ -241,8 +253,13 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
         nk = 1
         n = (ni, nj, 1)
     h = (1.0 / ni, 1.0 / nj, 1.0 / ni)
-    z = cart_zone("box", (0.0, 0.0, 0.0), h, n, ngk=0 if two_d else None)
+    ng = _ghosts(slope)
+    z = cart_zone("box", (0.0, 0.0, 0.0), h, n, ng=ng, ngk=0 if two_d else None)
     flat = two_d or extrude
+    if stretch:
+        gc = I.getNodeFromName1(z, "GridCoordinates")
+        Y = I.getNodeFromName1(gc, "CoordinateY")[1]
+        Y[:] = np.sinh(stretch * Y) / math.sinh(stretch)
     if wavy:
         wave(z, wavy, (0.0, 0.0, 0.0), (1.0, 1.0, h[2] * nk), two_d=flat)
     xc, yc, zc = cell_centers(z)
@@ -260,10 +277,10 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
         mu = mach / reynolds
         set_spalart(z, nutilde_ratio * mu * (1.0 + a * np.cos(2 * math.pi * xc) * np.sin(math.pi * yc)) / ro,
                     np.abs(yc))
-    bin_ = add_bc(z, "in", "BCInflow", "imin")
-    bout = add_bc(z, "out", outflow, "imax")
-    add_bc(z, "wall", wall, "jmin")
-    bfar = add_bc(z, "far", "BCFarfield", "jmax")
+    bin_ = add_bc(z, "in", "BCInflow", "imin", ng=ng)
+    bout = add_bc(z, "out", outflow, "imax", ng=ng)
+    add_bc(z, "wall", wall, "jmin", ng=ng)
+    bfar = add_bc(z, "far", "BCFarfield", "jmax", ng=ng)
     if outflow == "BCOutpres":
         nkf = 1 if two_d else nk
         yf = (np.arange(nj) + 0.5) / nj
@@ -287,8 +304,8 @@ def bc_box(n=(16, 12, 6), mach=0.3, reynolds=1.0e4, wall="BCWallViscous", model=
             st21[16] = st[5]
         add_bc_data(bin_, [("d%02d" % m_, np.array([x])) for m_, x in enumerate(st21)])
     if not two_d:
-        add_bc(z, "per_kmin", "BCautoperiod", "kmin")
-        add_bc(z, "per_kmax", "BCautoperiod", "kmax")
+        add_bc(z, "per_kmin", "BCautoperiod", "kmin", ng=ng)
+        add_bc(z, "per_kmax", "BCautoperiod", "kmax", ng=ng)
     numb = {"temporal_scheme": temporal, "ss_iteration": ss_iteration, "modulo_verif": 1}
     numz = {"scheme": scheme, "slope": slope, "time_step": time_step,
             "cache_blocking_I": 1000000, "cache_blocking_J": 1000000, "cache_blocking_K": 1000000}
@@ -518,3 +535,93 @@ def tgv_batch(ncases=64, sizes=(48, 64, 80, 96), mach=(0.05, 0.3), reynolds=(400
     FastC._setNum2Base(t, {"temporal_scheme": "implicit", "ss_iteration": ss_iteration,
                            "modulo_verif": modulo_verif})
     return t, params
+
+
+# --------------------------------------------------------- overset patch
+def _lagrange(x, width):
+    """Lagrange weights of the nodes 0..width-1 at position x."""
+    w = np.ones(width)
+    for m in range(width):
+        for q in range(width):
+            if q != m:
+                w[m] *= (x - q) / (m - q)
+    return w
+
+
+def overset_patch(n=(40, 40, 4), patch=(24, 20, 4), box=10.0, mach=0.5, types=(2,), shift=0.3,
+                  linear=False, numz=None):
+    """Overset (chimera) pair: zone 0 the periodic isentropic-vortex box
+    [-box, box]^2 (n cells, periodic in every direction), zone 1 a finer
+    cartesian patch over its centre (patch cells, steps 0.7 x zone 0's, k
+    origin shifted by shift x dz, periodic in k).  Every ghost cell of the
+    patch's i and j bands (edges included) receives an interpolation of
+    zone 0's cell values; receiver t uses types[t % len(types)] (2:
+    trilinear, 3: 27-point Lagrange, 5: 125-point Lagrange, 1: nearest
+    cell), molecules anchored so that they surround the receiver.  The
+    patch's i / j faces carry no BC: their ghosts are the receivers, as
+    behind a BCOverlap.  linear: a field linear in x, y, z instead of the
+    vortex (every interpolation reproduces it to round-off).
+    Returns (t, transfers) with transfers as fgb_add_interp_transfer
+    takes them (one dict)."""
+    t = isentropic_vortex(n=n, box=box, mach=mach, numz=numz)
+    z0 = I.getZones(t)[0]
+    h0 = 2 * box / n[0]
+    h1 = 0.7 * h0
+    ni, nj, nk = patch
+    x1 = (-0.5 * ni * h1, -0.5 * nj * h1, shift * h0)
+    z1 = cart_zone("patch", x1, (h1, h1, h0), patch)
+    xc, yc, zc = cell_centers(z1)
+    x0c, y0c, z0c = cell_centers(z0)
+    if linear:
+        for zz, (X, Y, Z) in ((z0, (x0c, y0c, z0c)), (z1, (xc, yc, zc))):
+            ro = 1.0 + 0.01 * X + 0.02 * Y + 0.001 * Z
+            set_conservative(zz, ro, 0.5 + 0.003 * X, 0.002 * Y, 0.0 * X, 1.0 / 1.4 + 0.001 * X, 1.4)
+    else:
+        r2 = xc * xc + yc * yc
+        e = np.exp(0.5 * (1.0 - r2))
+        du, dv = -5.0 / (2 * math.pi) * yc * e, 5.0 / (2 * math.pi) * xc * e
+        T = 1.0 - 0.4 * 25.0 / (8.0 * 1.4 * math.pi ** 2) * e * e
+        ro = T ** 2.5
+        set_conservative(z1, ro, mach + du, dv, 0.0 * ro, ro * T / 1.4, 1.4)
+    for f in ("kmin", "kmax"):
+        add_bc(z1, "per_" + f, "BCautoperiod", f)
+    I.getBases(t)[0][2].append(z1)
+    z1[2].append(copy.deepcopy(I.getNodeFromName1(z0, ".Solver#define")))
+    # receivers: the ghost cells of the i and j bands of the patch
+    ng = NG
+    nip, njp = ni + 2 * ng, nj + 2 * ng
+    nip0, njp0 = n[0] + 2 * ng, n[1] + 2 * ng
+    rcv, dnr, ty, co = [], [], [], []
+    for k in range(ng, nk + ng):
+        for j in range(njp):
+            for i in range(nip):
+                if ng <= i < ni + ng and ng <= j < nj + ng:
+                    continue
+                x, y, zz = xc[i, j, k], yc[i, j, k], zc[i, j, k]
+                typ = types[len(rcv) % len(types)]
+                # position in zone 0's cell-centre index space (cell l has
+                # centre -box + (l - ng + 0.5) h0 in x and y, (l - ng + 0.5) dz in z)
+                fx = (x + box) / h0 - 0.5 + ng
+                fy = (y + box) / h0 - 0.5 + ng
+                fz = zz / h0 - 0.5 + ng
+                w = {1: 1, 2: 2, 3: 3, 5: 5}[typ]
+                base = [int(math.floor(f)) - (w - 1) // 2 if w > 2 else int(math.floor(f))
+                        for f in (fx, fy, fz)]
+                if w == 1:
+                    base = [int(round(f)) for f in (fx, fy, fz)]
+                rel = [f - b for f, b in zip((fx, fy, fz), base)]
+                if typ == 1:
+                    c = [1.0]
+                elif typ == 2:
+                    wx, wy, wz = ([1 - r, r] for r in rel)
+                    c = [wx[a] * wy[b] * wz[d] for d in range(2) for b in range(2) for a in range(2)]
+                else:
+                    c = np.concatenate([_lagrange(r, w) for r in rel]).tolist()
+                rcv.append(i + j * nip + k * nip * njp)
+                dnr.append(base[0] + base[1] * nip0 + base[2] * nip0 * njp0)
+                ty.append(typ)
+                co.extend(c)
+    tr = dict(dnr=0, rcv=1, dnr_idx=np.array(dnr, dtype=np.int64),
+              rcv_idx=np.array(rcv, dtype=np.int64), types=np.array(ty, dtype=np.int64),
+              coefs=np.array(co, dtype=np.float64))
+    return t, [tr]

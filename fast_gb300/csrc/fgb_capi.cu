@@ -96,6 +96,12 @@ struct ZoneData {
 struct Transfer {
   int dnr, rcv; int64_t n; int32_t* dnr_idx; int32_t* rcv_idx;
   std::vector<int32_t> hd, hr;     // host copies (conflict check of the one-launch fill)
+  // interpolated transfer: type and first coefficient of each point
+  bool interp = false;
+  int32_t* types = nullptr;
+  int64_t* coff = nullptr;
+  double* coefs = nullptr;
+  std::vector<int32_t> ht;
 };
 // Zones solved by one LU-SGS launch (same zone type and equation count): the
 // plane table over all of them and a ring of zone tables (the state pointers
@@ -123,6 +129,11 @@ struct LuGroupData {
   int* flag = nullptr;
   unsigned long long* ticket = nullptr;
   int epoch = 0;
+  // LU schedule picked by the autotuner on the group's first solve of each
+  // sweep precision ([0] FP64, [1] FP32; -1: not tuned): lu_mode 1 or 2, and
+  // dataflow CTAs per SM
+  int tuned_mode[2] = {-1, -1}, tuned_per_sm[2] = {0, 0};
+  double tuned_ms[2][3] = {{0., 0., 0.}, {0., 0., 0.}};
 };
 
 struct fgb_solver {
@@ -164,6 +175,11 @@ struct fgb_solver {
   int64_t tr_n = 0;
   size_t tr_built = 0;             // number of transfers the list holds
   bool tr_ordered = false;         // a cell is written twice or read after a write: ordered fill
+  // every zone's BC lists concatenated (ghost fill of several zones in one launch per kind)
+  FillAll fa{};
+  bool fa_built = false;
+  std::vector<void*> fa_mem;
+  BcFaceArgs* fa_lp = nullptr;
   cudaStream_t zst[ZS] = {};
   cudaEvent_t zev[ZS] = {};
   cudaEvent_t fork_ev = nullptr;
@@ -174,6 +190,8 @@ struct fgb_solver {
                                    // 0 one launch per plane
   long long poll_limit = 1ll << 22;  // polls before a dataflow wait gives up
   int wait_skew = 0;               // test support: added to the marks the dataflow waits expect
+  bool batch = true;               // several zones: per-kind zone batches instead of per-zone launches
+  bool autotune = true;            // batched faces: block size from timed trials
   int lu_grid = 0;                 // > 0: at most this many CTAs in the persistent sweep
   unsigned int* bar = nullptr;     // grid-barrier words
   int* derr = nullptr;             // device error word
@@ -462,8 +480,8 @@ static int build_ghost_lists(ZoneData& Z, const std::vector<double>& hti,
             } else if (type == 10 || outpres) {   // BC_extrap.for: copy of the first ghost
               m[d] = first;
               cdst.push_back((int32_t)l); csrc.push_back((int32_t)idx(p, m[0], m[1], m[2]));
-            } else {                     // BC_nextrank.for
-              const int64_t dl = -step * inc;
+            } else if (rank == 1) {      // BC_nextrank.for: ranks 1 .. nrank-1 of the line,
+              const int64_t dl = -step * inc;   // one after the other by one thread
               ndst.push_back((int32_t)l); n0.push_back((int32_t)(l + dl));
               n1.push_back((int32_t)(l + 2 * dl)); n2.push_back((int32_t)(l + 3 * dl));
             }
@@ -606,6 +624,12 @@ static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const dou
   z.c5 = 2. * c6;
   z.c6 = -1. * c6;
   z.cvisq = 1. / 3;
+  z.c50 = 1. / 60;
+  z.c51 = 27. * z.c50;
+  z.c52 = -13. * z.c50;
+  z.c53 = -3. * z.c50;
+  z.c54 = 2. * z.c50;
+  z.c50 = 47. * z.c50;
   z.tcx = ti[0]; z.tcy = tj[0]; z.tcz = p[NEQ_K] > 0 ? tk[0] : 0.;  // a 2-d zone has no tk
   z.si = std::fabs(z.tcx); z.sj = std::fabs(z.tcy); z.sk = std::fabs(z.tcz);
   z.volinv = 0.5 / vol[0];
@@ -676,8 +700,12 @@ int fgb_destroy(fgb_solver* s) {
     for (WallCorrList& w : Z.walls) { cudaFree(w.l); cudaFree(w.l0); cudaFree(w.lt); cudaFree(w.nrm); }
     cudaFree(Z.co_dst); cudaFree(Z.co_a); cudaFree(Z.co_b); cudaFree(Z.co_c);
   }
-  for (Transfer& t : s->tr) { cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); }
+  for (Transfer& t : s->tr) {
+    cudaFree(t.dnr_idx); cudaFree(t.rcv_idx); cudaFree(t.types); cudaFree(t.coff); cudaFree(t.coefs);
+  }
   cudaFree(s->tr_rz); cudaFree(s->tr_ri); cudaFree(s->tr_dz); cudaFree(s->tr_di);
+  for (void* m : s->fa_mem) cudaFree(m);
+  cudaFree(s->fa_lp);
   for (int k = 0; k < fgb_solver::ZS; k++) {
     if (s->zst[k]) { cudaStreamSynchronize(s->zst[k]); cudaStreamDestroy(s->zst[k]); }
     if (s->zev[k]) cudaEventDestroy(s->zev[k]);
@@ -717,9 +745,13 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
     return fail(FGB_ERR_ARG, "zone type " + std::to_string(p[ITYPZONE]) + " not supported on the GPU path");
   if (p[NEQ] != (p[IFLOW] == 3 ? 6 : 5))
     return fail(FGB_ERR_ARG, "NEQ must be 5 (Euler, laminar) or 6 (Spalart-Allmaras)");
+  const bool o5 = p[SLOPE] == O5 || p[SLOPE] == O5SC;
+  if (o5 && p[KFLUDOM] != AUSM)
+    return fail(FGB_ERR_ARG, "the o5 / o5sc slopes are implemented for AUSM+(P) (the senseur "
+                             "scheme's o5 variant uses the time-dependent wiggle2023 sensor)");
   if (p[IFLOW] == 3) {
-    const bool ausm_o3 = (p[KFLUDOM] == AUSM || p[KFLUDOM] == SENSEUR) &&
-                         (p[SLOPE] == O3 || p[SLOPE] == O3SC);
+    const bool ausm_o3 = ((p[KFLUDOM] == AUSM || p[KFLUDOM] == SENSEUR) &&
+                          (p[SLOPE] == O3 || p[SLOPE] == O3SC)) || (p[KFLUDOM] == AUSM && o5);
     const bool roe = p[KFLUDOM] == ROE &&
                      (p[SLOPE] == O1 || p[SLOPE] == O3 || p[SLOPE] == MINMOD || p[SLOPE] == O3SC);
     if (!(ausm_o3 || roe) || p[ILES] != 0 || p[SA_INT] != 0)
@@ -729,8 +761,11 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
     if (p[ITYPCP] <= 1 && p[NEQ_COE] < 6)
       return fail(FGB_ERR_ARG, "implicit Spalart-Allmaras needs NEQ_COE = 6");
   }
-  if (p[NIJK + 3] != 2 || p[NIJK + 4] != (p[ITYPZONE] == Z2D ? 0 : 2))
-    return fail(FGB_ERR_ARG, "two ghost layers expected (none in k for a 2-d zone)");
+  // allocate_metric.cpp:101-117: three ghost layers for the o5 slopes, two otherwise
+  const int64_t ngx = o5 ? 3 : 2;
+  if (p[NIJK + 3] != ngx || p[NIJK + 4] != (p[ITYPZONE] == Z2D ? 0 : ngx))
+    return fail(FGB_ERR_ARG, o5 ? "the o5 slopes need three ghost layers (Rind 3)"
+                                : "two ghost layers expected (none in k for a 2-d zone)");
   if (p[NDIMDX] != p[NIJK] * p[NIJK + 1] * p[NIJK + 2])
     return fail(FGB_ERR_ARG, "NDIMDX inconsistent with NIJK (shiftvar must be 0)");
   if (p[NDIMDX] >= (int64_t)INT32_MAX / 2) return fail(FGB_ERR_ARG, "zone too large");
@@ -772,7 +807,7 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   int64_t ni = Z.z.ni, nj = Z.z.nj, nk = Z.z.nk;
   // senseur wiggle flags (3 x NDIMDX), then the o3sc shock-sensor weights
   // (3 x NDIMDX), the layout of FastC's createWorkArrays__ wig array
-  const int64_t nwig = (p[KFLUDOM] == SENSEUR ? 3 : 0) + (p[SLOPE] == O3SC ? 3 : 0);
+  const int64_t nwig = (p[KFLUDOM] == SENSEUR ? 3 : 0) + ((p[SLOPE] == O3SC || p[SLOPE] == O5SC) ? 3 : 0);
   if (nwig > 0) {
     CK(cudaMalloc(&Z.wig, sizeof(double) * nwig * nd));
     CK(cudaMemset(Z.wig, 0, sizeof(double) * nwig * nd));
@@ -828,6 +863,54 @@ int fgb_add_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
   return FGB_OK;
 }
 
+int fgb_add_interp_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
+                            const int64_t* dnr_idx, const int64_t* rcv_idx, const int64_t* types,
+                            const double* coefs, int64_t ncoefs) {
+  if (!s) return fail(FGB_ERR_ARG, "null solver");
+  if (dnr_zone < 0 || rcv_zone < 0 || dnr_zone >= (int)s->zones.size() ||
+      rcv_zone >= (int)s->zones.size())
+    return fail(FGB_ERR_ARG, "transfer zone out of range");
+  if (n < 0 || (n > 0 && (!dnr_idx || !rcv_idx || !types || !coefs)))
+    return fail(FGB_ERR_ARG, "bad transfer list");
+  const Zone& zd = s->zones[dnr_zone].z;
+  const int64_t ndd = zd.nd, ndr = s->zones[rcv_zone].z.nd;
+  const int64_t sj = zd.inc[1], sk = zd.inc[2];
+  std::vector<int32_t> d(n), r(n), ty(n);
+  std::vector<int64_t> co(n);
+  int64_t c = 0;
+  for (int64_t t = 0; t < n; t++) {
+    const int64_t tt = types[t];
+    int w, nc;
+    if (tt == 0 || tt == 1) { w = 1; nc = 1; }
+    else if (tt == 2) { w = 2; nc = 8; }
+    else if (tt == 22) { w = 2; nc = 4; }
+    else if (tt == 3) { w = 3; nc = 9; }
+    else if (tt == 5) { w = 5; nc = 15; }
+    else return fail(FGB_ERR_ARG, "interpolation type " + std::to_string(tt) + " is not supported");
+    const int64_t last = dnr_idx[t] + (w - 1) * (1 + sj + (tt == 22 ? 0 : sk));
+    if (dnr_idx[t] < 0 || last >= ndd || rcv_idx[t] < 0 || rcv_idx[t] >= ndr)
+      return fail(FGB_ERR_ARG, "interpolation molecule or receiver out of range");
+    d[t] = (int32_t)dnr_idx[t]; r[t] = (int32_t)rcv_idx[t]; ty[t] = (int32_t)tt;
+    co[t] = c;
+    c += nc;
+  }
+  if (c != ncoefs) return fail(FGB_ERR_ARG, "coefficient count does not match the types");
+  CK(cudaSetDevice(s->device));
+  Transfer T{dnr_zone, rcv_zone, n, nullptr, nullptr, {}, {}};
+  T.interp = true;
+  std::vector<double> cf(coefs, coefs + ncoefs);
+  CK(dev_upload(&T.dnr_idx, d));
+  CK(dev_upload(&T.rcv_idx, r));
+  CK(dev_upload(&T.types, ty));
+  CK(dev_upload(&T.coff, co));
+  CK(dev_upload(&T.coefs, cf));
+  T.hd = std::move(d);
+  T.hr = std::move(r);
+  T.ht = std::move(ty);
+  s->tr.push_back(std::move(T));
+  return FGB_OK;
+}
+
 int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist) {
   if (!s || !dist) return fail(FGB_ERR_ARG, "null argument");
   if (zone < 0 || zone >= (int)s->zones.size()) return fail(FGB_ERR_ARG, "zone out of range");
@@ -848,6 +931,10 @@ int fgb_set_option(fgb_solver* s, const char* key, double value) {
   } else if (k == "lu_mode") {
     if (value != 0. && value != 1. && value != 2.) return fail(FGB_ERR_ARG, "lu_mode must be 0, 1 or 2");
     s->lu_mode = (int)value;
+  } else if (k == "batch") {
+    s->batch = value != 0.;
+  } else if (k == "autotune") {
+    s->autotune = value != 0.;
   } else if (k == "lu_wait_skew") {
     if (value < 0 || value > 2) return fail(FGB_ERR_ARG, "lu_wait_skew must be 0, 1 or 2");
     s->wait_skew = (int)value;
@@ -887,6 +974,12 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value) {
   else if (k == "lu_grid") *value = s->lu_grid;
   else if (k == "lu_poll_limit") *value = (double)s->poll_limit;
   else if (k == "lu_wait_skew") *value = s->wait_skew;
+  else if (k == "batch") *value = s->batch;
+  else if (k == "lu_tuned") {   // first LU group, FP64 sweeps: 10 x lu_mode + CTAs per SM (-1: not tuned)
+    *value = (s->lu_groups.empty() || s->lu_groups[0].tuned_mode[0] < 0)
+                 ? -1. : 10. * s->lu_groups[0].tuned_mode[0] + s->lu_groups[0].tuned_per_sm[0];
+  }
+  else if (k == "autotune") *value = s->autotune;
   else return fail(FGB_ERR_ARG, "unknown option " + k);
   return FGB_OK;
 }
@@ -1039,7 +1132,7 @@ static int build_transfers(fgb_solver* s) {
   cudaFree(s->tr_rz); cudaFree(s->tr_ri); cudaFree(s->tr_dz); cudaFree(s->tr_di);
   s->tr_rz = s->tr_ri = s->tr_dz = s->tr_di = nullptr;
   int64_t n = 0;
-  for (Transfer& T : s->tr) n += T.n;
+  for (Transfer& T : s->tr) if (!T.interp) n += T.n;
   s->tr_n = n;
   s->tr_built = s->tr.size();
   // The one-launch fill copies every entry at once.  That equals the
@@ -1055,9 +1148,20 @@ static int build_transfers(fgb_solver* s) {
         if (rcv[(size_t)T.rcv][(size_t)r]) s->tr_ordered = true;
         rcv[(size_t)T.rcv][(size_t)r] = 1;
       }
-    for (Transfer& T : s->tr)
-      for (int32_t d : T.hd)
-        if (rcv[(size_t)T.dnr][(size_t)d]) s->tr_ordered = true;
+    for (Transfer& T : s->tr) {
+      const Zone& zd = s->zones[(size_t)T.dnr].z;
+      for (size_t t = 0; t < T.hd.size(); t++) {
+        const int ty = T.interp ? T.ht[t] : 0;
+        const int w = ty <= 1 ? 1 : (ty == 2 || ty == 22 ? 2 : (ty == 3 ? 3 : 5));
+        const int wk = ty == 22 ? 1 : w;
+        for (int kk = 0; kk < wk; kk++)
+          for (int jj = 0; jj < w; jj++)
+            for (int ii = 0; ii < w; ii++) {
+              const int64_t c = T.hd[t] + ii + jj * zd.inc[1] + kk * zd.inc[2];
+              if (rcv[(size_t)T.dnr][(size_t)c]) s->tr_ordered = true;
+            }
+      }
+    }
   }
   if (n == 0 || s->tr_ordered) return FGB_OK;
   const size_t B = sizeof(int32_t) * (size_t)n;
@@ -1066,6 +1170,7 @@ static int build_transfers(fgb_solver* s) {
   std::vector<int32_t> rz((size_t)n), dz((size_t)n);
   int64_t o = 0;
   for (Transfer& T : s->tr) {
+    if (T.interp) continue;
     CK(cudaMemcpy(s->tr_ri + o, T.rcv_idx, sizeof(int32_t) * T.n, cudaMemcpyDeviceToDevice));
     CK(cudaMemcpy(s->tr_di + o, T.dnr_idx, sizeof(int32_t) * T.n, cudaMemcpyDeviceToDevice));
     for (int64_t t = 0; t < T.n; t++) { rz[(size_t)(o + t)] = T.rcv; dz[(size_t)(o + t)] = T.dnr; }
@@ -1084,6 +1189,15 @@ static int fill_transfers(fgb_solver* s, int level) {
     int rc = build_transfers(s);
     if (rc) return rc;
   }
+  // interpolated transfers, one launch each in list order
+  auto interp = [&](Transfer& T) -> int {
+    ZoneData& D = s->zones[T.dnr];
+    ZoneData& R = s->zones[T.rcv];
+    CK(launch_transfer_interp(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, D.z.inc[1], D.z.inc[2],
+                              T.rcv_idx, T.dnr_idx, T.types, T.coff, T.coefs, T.n, R.z.neq, s->st));
+    s->launches++;
+    return FGB_OK;
+  };
   if (s->zones.size() <= (size_t)ZT_MAX && !s->tr_ordered) {
     ZoneLevels zl{};
     for (size_t m = 0; m < s->zones.size(); m++) {
@@ -1091,11 +1205,23 @@ static int fill_transfers(fgb_solver* s, int level) {
       zl.nd[m] = s->zones[m].z.nd;
       zl.neq[m] = s->zones[m].z.neq;
     }
-    CK(launch_transfer_all(zl, s->tr_rz, s->tr_ri, s->tr_dz, s->tr_di, s->tr_n, s->st));
-    s->launches++;
+    if (s->tr_n > 0) {
+      CK(launch_transfer_all(zl, s->tr_rz, s->tr_ri, s->tr_dz, s->tr_di, s->tr_n, s->st));
+      s->launches++;
+    }
+    for (Transfer& T : s->tr)
+      if (T.interp) {
+        int rc = interp(T);
+        if (rc) return rc;
+      }
     return FGB_OK;
   }
   for (Transfer& T : s->tr) {
+    if (T.interp) {
+      int rc = interp(T);
+      if (rc) return rc;
+      continue;
+    }
     ZoneData& D = s->zones[T.dnr];
     ZoneData& R = s->zones[T.rcv];
     CK(launch_gather(R.lvl[level], R.z.nd, D.lvl[level], D.z.nd, T.rcv_idx, T.dnr_idx, T.n,
@@ -1105,7 +1231,137 @@ static int fill_transfers(fgb_solver* s, int level) {
   return FGB_OK;
 }
 
+// The BC lists of every zone of the solver concatenated (with the zone of
+// each entry) for the one-launch-per-kind fill of several zones.
+static int build_fill_all(fgb_solver* s) {
+  for (void* m : s->fa_mem) cudaFree(m);
+  s->fa_mem.clear();
+  cudaFree(s->fa_lp);
+  s->fa_lp = nullptr;
+  int64_t n1 = 0, n0 = 0, n2 = 0, nc = 0;
+  for (ZoneData& Z : s->zones) {
+    if (!Z.cat_built) {
+      int rc = build_cat(Z);
+      if (rc) return rc;
+    }
+    n1 += Z.cat1.n; n0 += Z.cat0.n; n2 += Z.cat2.n; nc += Z.co_n;
+  }
+  auto ai = [&](int32_t** p, int64_t n) -> int {
+    *p = nullptr;
+    if (n <= 0) return FGB_OK;
+    CK(cudaMalloc(p, sizeof(int32_t) * (size_t)n));
+    s->fa_mem.push_back(*p);
+    return FGB_OK;
+  };
+  auto ad = [&](double** p, int64_t n) -> int {
+    *p = nullptr;
+    if (n <= 0) return FGB_OK;
+    CK(cudaMalloc(p, sizeof(double) * (size_t)n));
+    s->fa_mem.push_back(*p);
+    return FGB_OK;
+  };
+  int rc;
+  int32_t *d1, *s1, *l1, *m1, *z1, *d0, *s0, *o0, *z0, *d2, *q0, *q1, *q2, *z2, *cd, *ca, *cb, *cc, *zc;
+  double *nr1, *ax1;
+  if ((rc = ai(&d1, n1)) || (rc = ai(&s1, n1)) || (rc = ai(&l1, n1)) || (rc = ai(&m1, n1)) ||
+      (rc = ai(&z1, n1)) || (rc = ad(&nr1, 3 * n1)) || (rc = ad(&ax1, n1)) ||
+      (rc = ai(&d0, n0)) || (rc = ai(&s0, n0)) || (rc = ai(&o0, n0)) || (rc = ai(&z0, n0)) ||
+      (rc = ai(&d2, n2)) || (rc = ai(&q0, n2)) || (rc = ai(&q1, n2)) || (rc = ai(&q2, n2)) ||
+      (rc = ai(&z2, n2)) || (rc = ai(&cd, nc)) || (rc = ai(&ca, nc)) || (rc = ai(&cb, nc)) ||
+      (rc = ai(&cc, nc)) || (rc = ai(&zc, nc)))
+    return rc;
+  std::vector<BcFaceArgs> lp;
+  std::vector<int32_t> zh1((size_t)n1), zh0((size_t)n0), zh2((size_t)n2), zhc((size_t)nc),
+      lid((size_t)n1);
+  int64_t o1 = 0, oo = 0, o2 = 0, oc = 0;
+  const size_t I = sizeof(int32_t), D = sizeof(double);
+  for (size_t m = 0; m < s->zones.size(); m++) {
+    ZoneData& Z = s->zones[m];
+    if (Z.cat1.n > 0) {
+      CK(cudaMemcpy(d1 + o1, Z.cat1.dst, I * Z.cat1.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s1 + o1, Z.cat1.src, I * Z.cat1.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(m1 + o1, Z.cat1.mt, I * Z.cat1.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(nr1 + 3 * o1, Z.cat1.nrm, 3 * D * Z.cat1.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(ax1 + o1, Z.cat1.aux, D * Z.cat1.n, cudaMemcpyDeviceToDevice));
+      std::vector<int32_t> zl((size_t)Z.cat1.n);
+      CK(cudaMemcpy(zl.data(), Z.cat1.lid, I * Z.cat1.n, cudaMemcpyDeviceToHost));
+      std::vector<BcFaceArgs> zlp;
+      int32_t nlp = 0;
+      for (int32_t v : zl) nlp = std::max(nlp, v + 1);
+      zlp.resize((size_t)nlp);
+      CK(cudaMemcpy(zlp.data(), Z.cat_lp, sizeof(BcFaceArgs) * (size_t)nlp, cudaMemcpyDeviceToHost));
+      for (int64_t t = 0; t < Z.cat1.n; t++) {
+        lid[(size_t)(o1 + t)] = (int32_t)lp.size() + zl[(size_t)t];
+        zh1[(size_t)(o1 + t)] = (int32_t)m;
+      }
+      lp.insert(lp.end(), zlp.begin(), zlp.end());
+      o1 += Z.cat1.n;
+    }
+    if (Z.cat0.n > 0) {
+      CK(cudaMemcpy(d0 + oo, Z.cat0.dst, I * Z.cat0.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s0 + oo, Z.cat0.src, I * Z.cat0.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(o0 + oo, Z.cat0.op, I * Z.cat0.n, cudaMemcpyDeviceToDevice));
+      for (int64_t t = 0; t < Z.cat0.n; t++) zh0[(size_t)(oo + t)] = (int32_t)m;
+      oo += Z.cat0.n;
+    }
+    if (Z.cat2.n > 0) {
+      CK(cudaMemcpy(d2 + o2, Z.cat2.dst, I * Z.cat2.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(q0 + o2, Z.cat2.q0, I * Z.cat2.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(q1 + o2, Z.cat2.q1, I * Z.cat2.n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(q2 + o2, Z.cat2.q2, I * Z.cat2.n, cudaMemcpyDeviceToDevice));
+      for (int64_t t = 0; t < Z.cat2.n; t++) zh2[(size_t)(o2 + t)] = (int32_t)m;
+      o2 += Z.cat2.n;
+    }
+    if (Z.co_n > 0) {
+      CK(cudaMemcpy(cd + oc, Z.co_dst, I * Z.co_n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(ca + oc, Z.co_a, I * Z.co_n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(cb + oc, Z.co_b, I * Z.co_n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(cc + oc, Z.co_c, I * Z.co_n, cudaMemcpyDeviceToDevice));
+      if (Z.co_nedge > 0) CK(cudaMemset(cc + oc, 0xFF, I * Z.co_nedge));   // -1: an edge
+      for (int64_t t = 0; t < Z.co_n; t++) zhc[(size_t)(oc + t)] = (int32_t)m;
+      oc += Z.co_n;
+    }
+  }
+  if (n1 > 0) {
+    CK(cudaMemcpy(z1, zh1.data(), I * n1, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(l1, lid.data(), I * n1, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&s->fa_lp, sizeof(BcFaceArgs) * lp.size()));
+    CK(cudaMemcpy(s->fa_lp, lp.data(), sizeof(BcFaceArgs) * lp.size(), cudaMemcpyHostToDevice));
+  }
+  if (n0 > 0) CK(cudaMemcpy(z0, zh0.data(), I * n0, cudaMemcpyHostToDevice));
+  if (n2 > 0) CK(cudaMemcpy(z2, zh2.data(), I * n2, cudaMemcpyHostToDevice));
+  if (nc > 0) CK(cudaMemcpy(zc, zhc.data(), I * nc, cudaMemcpyHostToDevice));
+  FillAll& f = s->fa;
+  f.face = BcFaceCat{d1, s1, l1, m1, nr1, n1, s->fa_lp, ax1};
+  f.zface = z1;
+  f.gat = GatherCat{d0, s0, o0, n0};
+  f.zgat = z0;
+  f.next = s->zones[0].cat2;     // k1..k3 are the same for every zone
+  f.next.dst = d2; f.next.q0 = q0; f.next.q1 = q1; f.next.q2 = q2; f.next.n = n2;
+  f.znext = z2;
+  f.cdst = cd; f.ca = ca; f.cb = cb; f.cc = cc; f.zcoin = zc; f.ncoin = nc;
+  s->fa_built = true;
+  return FGB_OK;
+}
+
 static int ghost_fill(fgb_solver* s, int level) {
+  if (s->batch && s->zones.size() > 1 && s->zones.size() <= (size_t)ZT_MAX) {
+    int rc = fill_transfers(s, level);
+    if (rc) return rc;
+    bool stale = !s->fa_built;
+    for (ZoneData& Z : s->zones) stale = stale || !Z.cat_built;
+    if (stale && (rc = build_fill_all(s))) return rc;
+    ZoneLevels zl{};
+    for (size_t m = 0; m < s->zones.size(); m++) {
+      zl.q[m] = s->zones[m].lvl[level];
+      zl.nd[m] = s->zones[m].z.nd;
+      zl.neq[m] = s->zones[m].z.neq;
+      zl.ng[m] = (int)s->zones[m].z.ng;
+    }
+    CK(launch_fill_all(zl, s->fa, s->st));
+    s->launches += (s->fa.face.n > 0) + (s->fa.gat.n > 0) + (s->fa.next.n > 0) + (s->fa.ncoin > 0);
+    return FGB_OK;
+  }
   const bool par = s->zone_streams && !s->profile && s->zones.size() > 1;
   int rc = fill_transfers(s, level);   // transfers first (they write receiver ghosts only)
   if (rc) return rc;
@@ -1178,7 +1434,7 @@ static int adj_check(fgb_solver* s, int zone) {
     if (g.kind == 1 && g.op != BCF_SLIP && g.op != BCF_FARFIELD)
       return fail(FGB_ERR_ARG, "the adjoint covers slip-wall and farfield / inflow BCs");
   for (Transfer& T : s->tr)
-    if (T.rcv == zone && T.dnr != zone)
+    if ((T.rcv == zone && T.dnr != zone) || T.interp)
       return fail(FGB_ERR_ARG, "the adjoint covers one zone (self 1-to-1 interfaces only)");
   for (WallCorrList& w : Z.walls)
     if (!w.slip) return fail(FGB_ERR_ARG, "the adjoint covers slip walls");
@@ -1204,6 +1460,7 @@ static BcNextArgs next_args(ZoneData& Z, GatherList& g) {
   a.dst = g.dst; a.q0 = g.q0; a.q1 = g.q1; a.q2 = g.q2; a.n = g.n; a.nd = Z.z.nd;
   a.k1 = -(c4 + c5) * k0; a.k2 = -c6 * k0; a.k3 = (2. - c5 - c4) * k0;
   a.sa = Z.z.neq == 6;
+  a.nrank = (int)Z.z.ng - 1;
   return a;
 }
 
@@ -1336,6 +1593,7 @@ static void free_lu_groups(fgb_solver* s) {
 static LuGroup group_launch(fgb_solver* s, LuGroupData& g, LuZone* tab) {
   LuGroup L{};
   L.persistent = s->lu_mode;
+  L.flow_per_sm = 0;
   L.grid_cap = s->lu_grid;
   L.fp32 = s->lu_precision == 32;
   L.bar = s->bar; L.err = s->derr;
@@ -1489,6 +1747,235 @@ static int build_lu_groups(fgb_solver* s) {
   return FGB_OK;
 }
 
+// ------------------------------------------------------- zone batches
+// Block size of the batched face kernels per kind of zone, picked on the
+// first batch of that kind on a device by timing every candidate block
+// size on that batch's faces (CUDA events on the solver stream; the faces
+// are recomputed from the same state, so repeating them changes nothing)
+// and kept for the rest of the process: the project's autotuner.
+struct FaceTune { std::mutex mu; std::vector<std::pair<int64_t, int>> best[64]; };
+static FaceTune g_face_tune;
+
+static int face_block(fgb_solver* s, FaceBatch& b, int* block) {
+  const int64_t key = faces_kind_key(b.e[0].z);
+  {
+    std::lock_guard<std::mutex> lock(g_face_tune.mu);
+    for (auto& kv : g_face_tune.best[s->device])
+      if (kv.first == key) { *block = kv.second; return FGB_OK; }
+  }
+  int cand[4];
+  const int nc = faces_batch_blocks(cand, 4);
+  cudaEvent_t e0 = ev_get(s), e1 = ev_get(s);
+  float best_ms = 1e30f;
+  int best = cand[0];
+  for (int r = 0; r < 2; r++)          // the first round warms up
+    for (int c = 0; c < nc; c++) {
+      b.block = cand[c];
+      CK(cudaEventRecord(e0, s->st));
+      CK(launch_faces_batch(b, s->st));
+      CK(cudaEventRecord(e1, s->st));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (r == 1 && ms < best_ms) { best_ms = ms; best = cand[c]; }
+    }
+  s->pool.push_back(e0);
+  s->pool.push_back(e1);
+  std::lock_guard<std::mutex> lock(g_face_tune.mu);
+  g_face_tune.best[s->device].push_back({key, best});
+  *block = best;
+  return FGB_OK;
+}
+
+// The per-zone kernels of one sub-step for several zones, as launches over
+// zone batches (the zones of one kind, BATCH_MAX at a time) on the solver
+// stream: coefficients, Spalart-Allmaras source, faces and the fused
+// balance / update.  The kernels that only some zones need (CFL statistics,
+// shock sensor, wiggle sensor, the Roe wall-face correction, the residual
+// norms) stay per zone, in the order of the per-zone path; the arithmetic of
+// every cell is that of the per-zone kernels, so the results are the same.
+static int substep_batched(fgb_solver* s, int nstep, bool implicit, int verif, int lexit_lu,
+                           std::vector<LuFields>& lu_fields) {
+  const double cxsi1 = -0.6830127018922193, cxsi2 = -4. / 3.;
+  const double cg[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
+  const int nzn = (int)s->zones.size();
+  std::vector<double*> ssit((size_t)nzn), outp((size_t)nzn);
+  for (int m = 0; m < nzn; m++) {
+    ZoneData& Z = s->zones[(size_t)m];
+    if (nstep == 1) { ssit[m] = Z.lvl[0]; outp[m] = Z.lvl[2]; }
+    else if (implicit) { ssit[m] = Z.lvl[2]; outp[m] = Z.lvl[2]; }
+    else if (nstep % 2 == 0) { ssit[m] = Z.lvl[2]; outp[m] = Z.lvl[0]; }
+    else { ssit[m] = Z.lvl[0]; outp[m] = Z.lvl[2]; }
+  }
+  // zones grouped by a key, in order, BATCH_MAX at a time
+  auto batches = [&](auto keyf, auto body) -> int {
+    std::vector<std::pair<int64_t, std::vector<int>>> groups;
+    for (int m = 0; m < nzn; m++) {
+      const int64_t k = keyf(m);
+      if (k < 0) continue;
+      bool found = false;
+      for (auto& g : groups)
+        if (g.first == k && (int)g.second.size() < BATCH_MAX) { g.second.push_back(m); found = true; break; }
+      if (!found) groups.push_back({k, {m}});
+    }
+    for (auto& g : groups) {
+      int rc = body(g.second);
+      if (rc) return rc;
+    }
+    return FGB_OK;
+  };
+  int rc;
+  if (nstep == 1) {   // navier_stokes_struct.for:226-296 (first sub-step only)
+    ProfScope ps(s, "coefficients");
+    rc = batches([&](int) { return (int64_t)0; }, [&](const std::vector<int>& ms) -> int {
+      static thread_local CoeBatch b;
+      b.nz = (int)ms.size();
+      b.bstart[0] = 0;
+      for (int q = 0; q < b.nz; q++) {
+        ZoneData& Z = s->zones[(size_t)ms[(size_t)q]];
+        const Zone& z = Z.z;
+        CoeArgs ca{};
+        ca.rop = ssit[ms[q]]; ca.xmut_in = Z.xmut; ca.xmut = Z.xmut; ca.coe = Z.coe;
+        const bool wide = implicit || z.iflow == 3;
+        int64_t g = wide ? 2 : (z.iflow == 2 ? 1 : 0);
+        int64_t gk = wide ? z.ngk : (z.iflow == 2 ? (z.ngk ? 1 : 0) : 0);
+        ca.lo[0] = 1 - g; ca.hi[0] = z.ni + g;
+        ca.lo[1] = 1 - g; ca.hi[1] = z.nj + g;
+        ca.lo[2] = 1 - gk; ca.hi[2] = z.nk + gk;
+        ca.do_invist = z.iflow == 2;
+        ca.do_sa = z.iflow == 3;
+        ca.do_lu = implicit;
+        ca.first_it = s->first_it;
+        ca.coesut = Z.coesut; ca.cmus1 = Z.cmus1;
+        b.e[q].z = z;
+        b.e[q].a = ca;
+        const int64_t n = (ca.hi[0] - ca.lo[0] + 1) * (ca.hi[1] - ca.lo[1] + 1) * (ca.hi[2] - ca.lo[2] + 1);
+        b.bstart[q + 1] = b.bstart[q] + (n + 255) / 256;
+      }
+      CK(launch_coefficients_batch(b, s->st));
+      s->launches++;
+      return FGB_OK;
+    });
+    if (rc) return rc;
+  }
+  for (int m = 0; m < nzn; m++) {   // per-zone sensors and statistics
+    ZoneData& Z = s->zones[(size_t)m];
+    Zone& z = Z.z;
+    if (nstep == 1 && verif) {
+      ProfScope ps(s, "cfl");
+      CK(launch_cfl(z, ssit[m], Z.xmut, Z.cfl_part, Z.cfl, s->st));
+      s->launches += 2;
+    }
+    if (z.slope == O3SC || z.slope == O5SC) {
+      ProfScope ps(s, "shock_sensor");
+      CK(launch_shock_sensor(z, ssit[m], Z.wig, s->st));
+      s->launches++;
+    }
+    if (nstep == 1 && z.kflu == SENSEUR) {
+      ProfScope ps(s, "wiggle");
+      CK(launch_wiggle(z, ssit[m], Z.wig, s->st));
+      s->launches += 3;
+    }
+  }
+  {
+    ProfScope ps(s, "sa_source");
+    const int zero6 = implicit ? 1 : nstep == 1;
+    const double coefH6 = implicit ? 0. : (nstep == 2 ? cxsi1 : (nstep == 3 ? cxsi2 : 0.));
+    rc = batches([&](int m) { return s->zones[(size_t)m].z.neq == 6 ? (int64_t)s->zones[(size_t)m].z.typ : -1; },
+                 [&](const std::vector<int>& ms) -> int {
+      static thread_local SaBatch b;
+      b.nz = (int)ms.size();
+      b.coefH = coefH6; b.zero_init = zero6; b.lu = implicit && nstep == 1;
+      for (int q = 0; q < b.nz; q++) {
+        ZoneData& Z = s->zones[(size_t)ms[(size_t)q]];
+        b.e[q] = SaEntry{Z.z, ssit[ms[q]], Z.drodm, Z.coe};
+      }
+      CK(launch_sa_source_batch(b, s->st));
+      s->launches++;
+      return FGB_OK;
+    });
+    if (rc) return rc;
+  }
+  {
+    ProfScope ps(s, "face_flux");
+    rc = batches([&](int m) { return faces_kind_key(s->zones[(size_t)m].z); },
+                 [&](const std::vector<int>& ms) -> int {
+      static thread_local FaceBatch b;
+      b.nz = (int)ms.size();
+      for (int q = 0; q < b.nz; q++) {
+        ZoneData& Z = s->zones[(size_t)ms[(size_t)q]];
+        b.e[q].z = Z.z; b.e[q].q = ssit[ms[q]]; b.e[q].xmut = Z.xmut;
+        b.e[q].F[0] = Z.Fi; b.e[q].F[1] = Z.Fj; b.e[q].F[2] = Z.Fk;
+      }
+      int blk = 128;
+      if (s->autotune) {
+        int r2 = face_block(s, b, &blk);
+        if (r2) return r2;
+      }
+      b.block = blk;
+      cudaError_t e = launch_faces_batch(b, s->st);
+      if (e == cudaErrorNotSupported)
+        return fail(FGB_ERR_ARG, "scheme/slope/zone combination not implemented on the GPU path");
+      CK(e);
+      s->launches += b.e[0].z.typ == Z2D ? 2 : 3;
+      return FGB_OK;
+    });
+    if (rc) return rc;
+  }
+  auto stage_args = [&](int m) {
+    ZoneData& Z = s->zones[(size_t)m];
+    StageArgs sa{};
+    sa.Fi = Z.Fi; sa.Fj = Z.Fj; sa.Fk = Z.Fk; sa.drodm = Z.drodm; sa.coe = Z.coe;
+    sa.rop_in = ssit[m]; sa.rop_out = outp[m]; sa.rop_n = Z.lvl[0]; sa.rop_n1 = Z.lvl[1];
+    if (implicit) {
+      sa.zero_init = 1;
+      if (s->first_it == 0 || Z.z.dtloc == 1) { sa.c1 = -1.; sa.c2 = 1.; sa.c3 = 0.; }
+      else { sa.c1 = -1.5; sa.c2 = 2.; sa.c3 = -0.5; }
+      sa.first_sub = nstep == 1;
+    } else {
+      sa.zero_init = nstep == 1;
+      sa.coefH = nstep == 2 ? cxsi1 : (nstep == 3 ? cxsi2 : 0.);
+      sa.coefW = cg[nstep <= 3 ? nstep : 0];
+    }
+    return sa;
+  };
+  {
+    ProfScope ps(s, implicit ? "assemble_bdf" : "assemble_rk3");
+    rc = batches([&](int m) { return s->zones[(size_t)m].walls.empty() ? (int64_t)s->zones[(size_t)m].z.neq : -1; },
+                 [&](const std::vector<int>& ms) -> int {
+      static thread_local StageBatch b;
+      b.nz = (int)ms.size();
+      for (int q = 0; q < b.nz; q++) b.e[q] = StageEntry{s->zones[(size_t)ms[(size_t)q]].z, stage_args(ms[q])};
+      CK(launch_assemble_batch(b, implicit, s->st));
+      s->launches++;
+      return FGB_OK;
+    });
+    if (rc) return rc;
+    for (int m = 0; m < nzn; m++)    // zones with Roe wall-face corrections
+      if (!s->zones[(size_t)m].walls.empty())
+        if ((rc = assemble_stage(s, s->zones[(size_t)m], stage_args(m), ssit[m], implicit))) return rc;
+  }
+  if (!implicit) return FGB_OK;
+  for (int m = 0; m < nzn; m++) {
+    ZoneData& Z = s->zones[(size_t)m];
+    if (verif) {  // lhs.cpp residus_navier.h -> cprdu3s1
+      NormArgs na{};
+      na.drodm = Z.drodm; na.rdm = Z.rdm; na.nssiter = Z.pi[NSSITER]; na.it_bloc = nstep;
+      na.neq = Z.z.neq;
+      for (int d = 0; d < 3; d++) { na.ijkv_lu[d] = Z.ijkv_lu[d]; na.size[d] = Z.pi[SIZE_SSDOM + d]; }
+      ProfScope ps(s, "block_norms");
+      CK(launch_norms(Z.z, na, s->st));
+      s->launches++;
+    }
+    if (!lexit_lu) {
+      const bool inplace = ssit[m] == outp[m];
+      lu_fields[(size_t)m] = LuFields{ssit[m], inplace ? Z.scratch : outp[m], Z.coe, Z.drodm, Z.posmap,
+                                      inplace ? 1 : 0};
+    }
+  }
+  return FGB_OK;
+}
+
 int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int layer_mode,
                 int nit_c) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
@@ -1523,12 +2010,18 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       }
       if (!verif && nstep == nssiter && p0[ITYPCP] == 1) continue;  // computePT.cpp:581
       if (verif) s->nit_recorded = nstep;
-      const bool par = s->zone_streams && !s->profile && s->zones.size() > 1;
+      const bool batched = s->batch && s->zones.size() > 1;
+      const bool par = !batched && s->zone_streams && !s->profile && s->zones.size() > 1;
+      if (batched) {
+        int rc = substep_batched(s, nstep, implicit, verif, lexit_lu, lu_fields);
+        if (rc) return rc;
+      }
       if (par) {
         int rc = zone_fork(s);
         if (rc) return rc;
       }
       for (ZoneData& Z : s->zones) {
+        if (batched) break;
         const int zm = (int)(&Z - s->zones.data());
         StreamSwap sw(s, par ? s->zst[zm % fgb_solver::ZS] : s->st);
         Zone& z = Z.z;
@@ -1565,7 +2058,7 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             s->launches += 2;
           }
         }
-        if (z.slope == O3SC) {  // src_term.for:246-255: o3sc sensor on every sub-step
+        if (z.slope == O3SC || z.slope == O5SC) {  // src_term.for:246-255: o3sc / o5sc sensor
           ProfScope ps(s, "shock_sensor");
           CK(launch_shock_sensor(z, ssiter, Z.wig, s->st));
           s->launches++;
@@ -1646,8 +2139,41 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
           CK(cudaMemcpyAsync(td, th, sizeof(LuZone) * nz, cudaMemcpyHostToDevice, s->st));
           CK(cudaEventRecord(g.ev[slot], s->st));
           g.ev_used[slot] = true;
+          // autotuner: on the group's first solve (schedule "auto", the
+          // default lu_mode 2 with autotune on), time the grid-barrier sweep
+          // and the dataflow sweep with one and two CTAs per SM on this very
+          // solve -- a solve reads W^p, the residual and the coefficients
+          // and writes only its own outputs, so repeating it changes nothing
+          // -- and keep the fastest for the rest of the run
+          const int pk = s->lu_precision == 32 ? 1 : 0;
+          if (s->autotune && s->lu_mode == 2 && g.tuned_mode[pk] < 0 && !s->profile) {
+            const int cand_mode[3] = {1, 2, 2}, cand_per[3] = {0, 1, 2};
+            cudaEvent_t e0 = ev_get(s), e1 = ev_get(s);
+            float best = 1e30f;
+            for (int c = 0; c < 3; c++) {
+              g.epoch++;
+              LuGroup Lc = group_launch(s, g, td);
+              Lc.persistent = cand_mode[c];
+              Lc.flow_per_sm = cand_per[c];
+              CK(cudaEventRecord(e0, s->st));
+              CK(launch_lusgs(th, Lc, s->st));
+              CK(cudaEventRecord(e1, s->st));
+              CK(cudaEventSynchronize(e1));
+              float ms = 0.f;
+              CK(cudaEventElapsedTime(&ms, e0, e1));
+              g.tuned_ms[pk][c] = ms;
+              if (ms < best) { best = ms; g.tuned_mode[pk] = cand_mode[c]; g.tuned_per_sm[pk] = cand_per[c]; }
+            }
+            s->pool.push_back(e0);
+            s->pool.push_back(e1);
+            s->launches += 3 * (2 * nz + 1);
+          }
           g.epoch++;
           LuGroup L = group_launch(s, g, td);
+          if (g.tuned_mode[pk] > 0 && s->lu_mode == 2 && s->autotune) {
+            L.persistent = g.tuned_mode[pk];
+            L.flow_per_sm = g.tuned_per_sm[pk];
+          }
           {
             ProfScope ps(s, "lu_sgs");
             CK(launch_lusgs(th, L, s->st));
@@ -1714,6 +2240,7 @@ int fgb_set_bc_state(fgb_solver* s, int zone, const double* st) {
     for (void* m : Z.cat_mem) cudaFree(m);
     Z.cat_mem.clear();
     Z.cat_built = false;
+    s->fa_built = false;
   }
   return FGB_OK;
 }

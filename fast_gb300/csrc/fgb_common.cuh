@@ -33,7 +33,7 @@ enum PR : int {
 enum PI_SA : int { SA_LOW_RE = 130, SA_ROT_CORR = 131 };
 enum ZoneType : int { Z3DFULL = 0, Z3DHOMO = 1, Z3DCART = 2, Z2D = 3 };
 enum Scheme : int { AUSM = 1, SENSEUR = 2, ROE = 5 };
-enum Slope : int { O1 = 1, O3 = 2, MINMOD = 3, O3SC = 6, VANALBADA = 8 };   // 8: not a FastS slope
+enum Slope : int { O1 = 1, O3 = 2, MINMOD = 3, O5 = 5, O3SC = 6, O5SC = 7, VANALBADA = 8 };   // 8: not a FastS slope
 
 // Everything a kernel needs about one zone; passed by value.
 struct Zone {
@@ -52,6 +52,7 @@ struct Zone {
   const double* wig;   // senseur wiggle flags, 3 x NDIMDX (KFLUDOM = 2)
   double opt0;         // float(SENSORTYPE)
   double c1, c2, c3, c4, c5, c6, cvisq;
+  double c50, c51, c52, c53, c54;   // o5 reconstruction (template_FluxAndBalance.for:149-154)
   double tcx, tcy, tcz, si, sj, sk, volinv;  // 3d cartesian metric
   double prandt, xmul0, temp0, cs;
   const double *ti, *tj, *tk, *vol;

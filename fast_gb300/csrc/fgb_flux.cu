@@ -573,12 +573,11 @@ __device__ __forceinline__ void visc_2d(const Zone& z, const double* __restrict_
 // NV = 6: Spalart-Allmaras (AUSM+(P): nutilde takes the o3 slope; Roe:
 // first-order nutilde flux, no reconstruction).
 template <int D, int TYP, int KF, int SL, bool VISC, int NV = 5>
-__global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restrict__ q,
-                                                 const double* __restrict__ xmut,
-                                                 double* __restrict__ Fo) {
+__device__ __forceinline__ void face_flux_at(const Zone& z, const double* __restrict__ q,
+                                             const double* __restrict__ xmut,
+                                             double* __restrict__ Fo, const int64_t f) {
   const int64_t NI = z.ni + (D == 0), NJ = z.nj + (D == 1), NK = z.nk + (D == 2);
   const int64_t nf = NI * NJ * NK;
-  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const int64_t ii = f % NI;
   const int64_t r = f / NI;
@@ -589,7 +588,7 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
   double qm[NV], qp[NV];
   double roff = 0.;
   if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
-  if (SL == O3SC) roff = z.wig[l + D * nd + (KF == SENSEUR ? 3 * nd : 0)];
+  if (SL == O3SC || SL == O5SC) roff = z.wig[l + D * nd + (KF == SENSEUR ? 3 * nd : 0)];
 #pragma unroll
   for (int v = 0; v < NV; v++) {
     if (TYP == Z2D && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }   // 2-d: no w slope
@@ -598,6 +597,16 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
     double a = (SL == O1) ? 0. : Q[l - 2 * inc];
     double b = Q[l - inc], c = Q[l];
     double d = (SL == O1) ? 0. : Q[l + inc];
+    if (SL == O5 || SL == O5SC) {   // Slope/o5_slope_var.for, o5sc_slope_var.for
+      const double e = Q[l - 3 * inc], g = Q[l + 2 * inc];
+      qm[v] = z.c50 * c + z.c51 * b + z.c52 * d + z.c53 * a + z.c54 * g;
+      qp[v] = z.c50 * b + z.c52 * a + z.c51 * c + z.c53 * d + z.c54 * e;
+      if (SL == O5SC) {
+        qm[v] = c * (1. - roff) + qm[v] * roff;
+        qp[v] = b * (1. - roff) + qp[v] * roff;
+      }
+      continue;
+    }
     reconstruct<SL>(z, a, b, c, d, roff, qm[v], qp[v]);
   }
   double F[NV];
@@ -644,6 +653,35 @@ __global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restric
   for (int v = 0; v < NV; v++) Fo[v * nf + f] = F[v];
 }
 
+template <int D, int TYP, int KF, int SL, bool VISC, int NV = 5>
+__global__ void __launch_bounds__(128) face_flux(Zone z, const double* __restrict__ q,
+                                                 const double* __restrict__ xmut,
+                                                 double* __restrict__ Fo) {
+  face_flux_at<D, TYP, KF, SL, VISC, NV>(z, q, xmut, Fo, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Zone batches: one launch for the same kernel over several zones of the
+// same kind.  The zones' descriptors and arguments travel in the kernel
+// parameter (__grid_constant__, read in place); block b belongs to the zone
+// m with bstart[m] <= b < bstart[m + 1], and every thread of a block reads
+// the same entry (a uniform constant-bank access).
+__device__ __forceinline__ int batch_zone(const int64_t* bstart, int nz, int64_t b) {
+  int lo = 0, hi = nz - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (bstart[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int D, int TYP, int KF, int SL, bool VISC, int NV = 5>
+__global__ void __launch_bounds__(256) face_flux_batch(const __grid_constant__ FaceBatch b) {
+  const int m = batch_zone(b.bstart, b.nz, blockIdx.x);
+  const FaceEntry& e = b.e[m];
+  face_flux_at<D, TYP, KF, SL, VISC, NV>(e.z, e.q, e.xmut, e.F[D],
+                                         (int64_t)(blockIdx.x - b.bstart[m]) * blockDim.x + threadIdx.x);
+}
+
 // --------------------------------------------------------- assemble+update
 // cons energy of a primitive state (core3ark3.for:127-150 / core3as2.for)
 __device__ __forceinline__ double roe_of(double cv, double r, double u, double v, double w,
@@ -656,9 +694,8 @@ __device__ __forceinline__ double roe_of(double cv, double r, double u, double v
 // are core3ark3.for's nutilde branch (clipped to [0, ratiom nu_lam]) and
 // core3as2.for's sixth residual.
 template <bool IMPL, int NV = 5>
-__global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
+__device__ __forceinline__ void assemble_at(const Zone& z, const StageArgs& a, const int64_t t) {
   const int64_t n = z.ni * z.nj * z.nk;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int64_t ii = t % z.ni;
   const int64_t r = t / z.ni;
@@ -675,8 +712,8 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
 #pragma unroll
     for (int v = 0; v < NV; v++) x[v] = a.drodm[l + v * nd];
   } else {
-#pragma unroll
     const bool two_d = z.typ == Z2D;   // no k faces
+#pragma unroll
     for (int v = 0; v < NV; v++) {
       double s = v == 5 ? a.drodm[l + v * nd] : (a.zero_init ? 0. : a.drodm[l + v * nd] * a.coefH);
       if (!two_d) s = s + a.Fk[v * nfk + ak];
@@ -770,6 +807,18 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
   }
 }
 
+template <bool IMPL, int NV = 5>
+__global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
+  assemble_at<IMPL, NV>(z, a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <bool IMPL, int NV = 5>
+__global__ void __launch_bounds__(256) assemble_batch(const __grid_constant__ StageBatch b) {
+  const int m = batch_zone(b.bstart, b.nz, blockIdx.x);
+  assemble_at<IMPL, NV>(b.e[m].z, b.e[m].a,
+                        (int64_t)(blockIdx.x - b.bstart[m]) * blockDim.x + threadIdx.x);
+}
+
 // -------------------------------------------------- Spalart-Allmaras source
 // SA/spsource_SA.for with sourceSA_grad_3dcart.for / sourceSA_grad_3d.for,
 // sourceSA_prod_dest.for and sourceSA_LU.for, fused with init_rhs.for for
@@ -778,11 +827,10 @@ __global__ void __launch_bounds__(256) assemble(Zone z, StageArgs a) {
 // coe(l,6) = coe(l,5) - min(d source / d(ro nutilde), 0) coe(l,1).  One
 // thread per interior cell (the reference's first ghost ring is never read).
 template <int TYP>
-__global__ void __launch_bounds__(256) sa_source(Zone z, const double* __restrict__ q,
-                                                 double* __restrict__ drodm, double* __restrict__ coe,
-                                                 double coefH, int zero_init, int lu) {
+__device__ __forceinline__ void sa_source_at(const Zone& z, const double* __restrict__ q,
+                                             double* __restrict__ drodm, double* __restrict__ coe,
+                                             double coefH, int zero_init, int lu, const int64_t t) {
   const int64_t n = z.ni * z.nj * z.nk;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int64_t ii = t % z.ni, r0 = t / z.ni, jj = r0 % z.nj, kk = r0 / z.nj;
   const int64_t l = inddm(z, ii + 1, jj + 1, kk + 1);
@@ -923,6 +971,21 @@ __global__ void __launch_bounds__(256) sa_source(Zone z, const double* __restric
   drodm[l + 5 * nd] = init + vol * tsource;
 }
 
+template <int TYP>
+__global__ void __launch_bounds__(256) sa_source(Zone z, const double* __restrict__ q,
+                                                 double* __restrict__ drodm, double* __restrict__ coe,
+                                                 double coefH, int zero_init, int lu) {
+  sa_source_at<TYP>(z, q, drodm, coe, coefH, zero_init, lu, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <int TYP>
+__global__ void __launch_bounds__(256) sa_source_batch(const __grid_constant__ SaBatch b) {
+  const int m = batch_zone(b.bstart, b.nz, blockIdx.x);
+  const SaEntry& e = b.e[m];
+  sa_source_at<TYP>(e.z, e.q, e.drodm, e.coe, b.coefH, b.zero_init, b.lu,
+                    (int64_t)(blockIdx.x - b.bstart[m]) * blockDim.x + threadIdx.x);
+}
+
 cudaError_t launch_sa_source(const Zone& z, const double* q, double* drodm, double* coe,
                              double coefH, int zero_init, int lu, cudaStream_t st) {
   const int B = 256;
@@ -1016,116 +1079,225 @@ static cudaError_t launch_faces_t(const Zone& z, const double* q, const double* 
 
 // *_o3sc_*: the o3 slope blended by the shock sensor; Euler / laminar /
 // Spalart-Allmaras, AUSM+(P), senseur and Roe.
-template <int TYP>
-static cudaError_t launch_faces_o3sc(const Zone& z, const double* q, const double* xmut,
-                                     double* Fi, double* Fj, double* Fk, cudaStream_t st) {
+template <int TYP, class Op>
+static cudaError_t faces_o3sc(const Zone& z, Op& op) {
   if (z.neq == 6) {
-    if (z.kflu == ROE) return launch_faces_t<TYP, ROE, O3SC, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.kflu == AUSM) return launch_faces_t<TYP, AUSM, O3SC, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.kflu == SENSEUR) return launch_faces_t<TYP, SENSEUR, O3SC, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == ROE) return op.template run<TYP, ROE, O3SC, true, 6>();
+    if (z.kflu == AUSM) return op.template run<TYP, AUSM, O3SC, true, 6>();
+    if (z.kflu == SENSEUR) return op.template run<TYP, SENSEUR, O3SC, true, 6>();
     return cudaErrorNotSupported;
   }
   const bool visc = z.iflow >= 2;
-  if (z.kflu == ROE) return visc ? launch_faces_t<TYP, ROE, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                 : launch_faces_t<TYP, ROE, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st);
-  if (z.kflu == AUSM) return visc ? launch_faces_t<TYP, AUSM, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                  : launch_faces_t<TYP, AUSM, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st);
-  if (z.kflu == SENSEUR) return visc ? launch_faces_t<TYP, SENSEUR, O3SC, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                     : launch_faces_t<TYP, SENSEUR, O3SC, false>(z, q, xmut, Fi, Fj, Fk, st);
+  if (z.kflu == ROE) return visc ? op.template run<TYP, ROE, O3SC, true>()
+                                 : op.template run<TYP, ROE, O3SC, false>();
+  if (z.kflu == AUSM) return visc ? op.template run<TYP, AUSM, O3SC, true>()
+                                  : op.template run<TYP, AUSM, O3SC, false>();
+  if (z.kflu == SENSEUR) return visc ? op.template run<TYP, SENSEUR, O3SC, true>()
+                                     : op.template run<TYP, SENSEUR, O3SC, false>();
   return cudaErrorNotSupported;
 }
 
 // Dispatch over the (zone type, scheme, slope, viscous) combinations that the
 // reference generates for 3d zones.  Returns cudaErrorNotSupported for the
 // others (host code reports it as an argument error, never falls back).
-cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
-                         double* Fj, double* Fk, cudaStream_t st) {
+// o5 / o5sc: AUSM+(P) only (the reference's senseur o5 variant needs the
+// time-dependent wiggle2023 sensor)
+template <int TYP, int SL, class Op>
+static cudaError_t faces_o5(const Zone& z, Op& op) {
+  if (z.kflu != AUSM) return cudaErrorNotSupported;
+  if (z.neq == 6) return op.template run<TYP, AUSM, SL, true, 6>();
+  return z.iflow >= 2 ? op.template run<TYP, AUSM, SL, true>() : op.template run<TYP, AUSM, SL, false>();
+}
+
+template <class Op>
+static cudaError_t faces_dispatch(const Zone& z, Op& op) {
   const bool visc = z.iflow >= 2;
+  if (z.slope == O5 || z.slope == O5SC) {
+    const bool sc = z.slope == O5SC;
+    if (z.typ == Z3DCART) return sc ? faces_o5<Z3DCART, O5SC>(z, op) : faces_o5<Z3DCART, O5>(z, op);
+    if (z.typ == Z3DFULL) return sc ? faces_o5<Z3DFULL, O5SC>(z, op) : faces_o5<Z3DFULL, O5>(z, op);
+    if (z.typ == Z2D) return sc ? faces_o5<Z2D, O5SC>(z, op) : faces_o5<Z2D, O5>(z, op);
+    return cudaErrorNotSupported;
+  }
   if (z.slope == O3SC) {
-    if (z.typ == Z3DCART) return launch_faces_o3sc<Z3DCART>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.typ == Z3DFULL) return launch_faces_o3sc<Z3DFULL>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.typ == Z2D) return launch_faces_o3sc<Z2D>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.typ == Z3DCART) return faces_o3sc<Z3DCART>(z, op);
+    if (z.typ == Z3DFULL) return faces_o3sc<Z3DFULL>(z, op);
+    if (z.typ == Z2D) return faces_o3sc<Z2D>(z, op);
     return cudaErrorNotSupported;
   }
   if (z.neq == 6 && z.typ == Z2D) {   // Spalart-Allmaras on 2-d zones
-    if (z.kflu == AUSM && z.slope == O3) return launch_faces_t<Z2D, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.kflu == SENSEUR && z.slope == O3) return launch_faces_t<Z2D, SENSEUR, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.kflu == ROE && z.slope == O1) return launch_faces_t<Z2D, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.kflu == ROE && z.slope == O3) return launch_faces_t<Z2D, ROE, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
-    if (z.kflu == ROE && z.slope == MINMOD) return launch_faces_t<Z2D, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+    if (z.kflu == AUSM && z.slope == O3) return op.template run<Z2D, AUSM, O3, true, 6>();
+    if (z.kflu == SENSEUR && z.slope == O3) return op.template run<Z2D, SENSEUR, O3, true, 6>();
+    if (z.kflu == ROE && z.slope == O1) return op.template run<Z2D, ROE, O1, true, 6>();
+    if (z.kflu == ROE && z.slope == O3) return op.template run<Z2D, ROE, O3, true, 6>();
+    if (z.kflu == ROE && z.slope == MINMOD) return op.template run<Z2D, ROE, MINMOD, true, 6>();
     return cudaErrorNotSupported;
   }
   if (z.neq == 6) {   // Spalart-Allmaras: AUSM+(P) o3 or Roe o1 / o3 / minmod, 3d zones
     const bool cart = z.typ == Z3DCART;
     if (z.typ != Z3DCART && z.typ != Z3DFULL) return cudaErrorNotSupported;
     if (z.kflu == AUSM && z.slope == O3)
-      return cart ? launch_faces_t<Z3DCART, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DFULL, AUSM, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+      return cart ? op.template run<Z3DCART, AUSM, O3, true, 6>()
+                  : op.template run<Z3DFULL, AUSM, O3, true, 6>();
     if (z.kflu == SENSEUR && z.slope == O3)   // SENSOR/*/fluFaceSA_o3_*: the AUSM form, sensor u / tdu
-      return cart ? launch_faces_t<Z3DCART, SENSEUR, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DFULL, SENSEUR, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+      return cart ? op.template run<Z3DCART, SENSEUR, O3, true, 6>()
+                  : op.template run<Z3DFULL, SENSEUR, O3, true, 6>();
     if (z.kflu == ROE && z.slope == O1)
-      return cart ? launch_faces_t<Z3DCART, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DFULL, ROE, O1, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+      return cart ? op.template run<Z3DCART, ROE, O1, true, 6>()
+                  : op.template run<Z3DFULL, ROE, O1, true, 6>();
     if (z.kflu == ROE && z.slope == O3)
-      return cart ? launch_faces_t<Z3DCART, ROE, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DFULL, ROE, O3, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+      return cart ? op.template run<Z3DCART, ROE, O3, true, 6>()
+                  : op.template run<Z3DFULL, ROE, O3, true, 6>();
     if (z.kflu == ROE && z.slope == MINMOD)
-      return cart ? launch_faces_t<Z3DCART, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DFULL, ROE, MINMOD, true, 6>(z, q, xmut, Fi, Fj, Fk, st);
+      return cart ? op.template run<Z3DCART, ROE, MINMOD, true, 6>()
+                  : op.template run<Z3DFULL, ROE, MINMOD, true, 6>();
     return cudaErrorNotSupported;
   }
   if (z.typ == Z3DCART) {
     if (z.kflu == ROE) {
-      if (z.slope == O1) return visc ? launch_faces_t<Z3DCART, ROE, O1, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                     : launch_faces_t<Z3DCART, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == O3) return visc ? launch_faces_t<Z3DCART, ROE, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                     : launch_faces_t<Z3DCART, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == MINMOD) return visc ? launch_faces_t<Z3DCART, ROE, MINMOD, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                         : launch_faces_t<Z3DCART, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == VANALBADA && !visc) return launch_faces_t<Z3DCART, ROE, VANALBADA, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O1) return visc ? op.template run<Z3DCART, ROE, O1, true>()
+                                     : op.template run<Z3DCART, ROE, O1, false>();
+      if (z.slope == O3) return visc ? op.template run<Z3DCART, ROE, O3, true>()
+                                     : op.template run<Z3DCART, ROE, O3, false>();
+      if (z.slope == MINMOD) return visc ? op.template run<Z3DCART, ROE, MINMOD, true>()
+                                         : op.template run<Z3DCART, ROE, MINMOD, false>();
+      if (z.slope == VANALBADA && !visc) return op.template run<Z3DCART, ROE, VANALBADA, false>();
     } else if (z.kflu == AUSM && z.slope == O3) {
-      return visc ? launch_faces_t<Z3DCART, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DCART, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      return visc ? op.template run<Z3DCART, AUSM, O3, true>()
+                  : op.template run<Z3DCART, AUSM, O3, false>();
     } else if (z.kflu == SENSEUR && z.slope == O3) {
-      return visc ? launch_faces_t<Z3DCART, SENSEUR, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DCART, SENSEUR, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      return visc ? op.template run<Z3DCART, SENSEUR, O3, true>()
+                  : op.template run<Z3DCART, SENSEUR, O3, false>();
     }
   } else if (z.typ == Z3DFULL) {
     if (z.kflu == ROE) {
-      if (z.slope == O1) return visc ? launch_faces_t<Z3DFULL, ROE, O1, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                     : launch_faces_t<Z3DFULL, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == O3) return visc ? launch_faces_t<Z3DFULL, ROE, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                     : launch_faces_t<Z3DFULL, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == MINMOD) return visc ? launch_faces_t<Z3DFULL, ROE, MINMOD, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                         : launch_faces_t<Z3DFULL, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == VANALBADA && !visc) return launch_faces_t<Z3DFULL, ROE, VANALBADA, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O1) return visc ? op.template run<Z3DFULL, ROE, O1, true>()
+                                     : op.template run<Z3DFULL, ROE, O1, false>();
+      if (z.slope == O3) return visc ? op.template run<Z3DFULL, ROE, O3, true>()
+                                     : op.template run<Z3DFULL, ROE, O3, false>();
+      if (z.slope == MINMOD) return visc ? op.template run<Z3DFULL, ROE, MINMOD, true>()
+                                         : op.template run<Z3DFULL, ROE, MINMOD, false>();
+      if (z.slope == VANALBADA && !visc) return op.template run<Z3DFULL, ROE, VANALBADA, false>();
     } else if (z.kflu == AUSM && z.slope == O3) {
-      return visc ? launch_faces_t<Z3DFULL, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DFULL, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      return visc ? op.template run<Z3DFULL, AUSM, O3, true>()
+                  : op.template run<Z3DFULL, AUSM, O3, false>();
     } else if (z.kflu == SENSEUR && z.slope == O3) {
-      return visc ? launch_faces_t<Z3DFULL, SENSEUR, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z3DFULL, SENSEUR, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      return visc ? op.template run<Z3DFULL, SENSEUR, O3, true>()
+                  : op.template run<Z3DFULL, SENSEUR, O3, false>();
     }
   }
   if (z.typ == Z2D) {   // 2-d zones: Euler / laminar, Roe o1 / o3 / minmod, AUSM+(P) o3
     if (z.kflu == ROE) {
-      if (z.slope == O1) return visc ? launch_faces_t<Z2D, ROE, O1, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                     : launch_faces_t<Z2D, ROE, O1, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == O3) return visc ? launch_faces_t<Z2D, ROE, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                     : launch_faces_t<Z2D, ROE, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == MINMOD) return visc ? launch_faces_t<Z2D, ROE, MINMOD, true>(z, q, xmut, Fi, Fj, Fk, st)
-                                         : launch_faces_t<Z2D, ROE, MINMOD, false>(z, q, xmut, Fi, Fj, Fk, st);
-      if (z.slope == VANALBADA && !visc) return launch_faces_t<Z2D, ROE, VANALBADA, false>(z, q, xmut, Fi, Fj, Fk, st);
+      if (z.slope == O1) return visc ? op.template run<Z2D, ROE, O1, true>()
+                                     : op.template run<Z2D, ROE, O1, false>();
+      if (z.slope == O3) return visc ? op.template run<Z2D, ROE, O3, true>()
+                                     : op.template run<Z2D, ROE, O3, false>();
+      if (z.slope == MINMOD) return visc ? op.template run<Z2D, ROE, MINMOD, true>()
+                                         : op.template run<Z2D, ROE, MINMOD, false>();
+      if (z.slope == VANALBADA && !visc) return op.template run<Z2D, ROE, VANALBADA, false>();
     } else if (z.kflu == AUSM && z.slope == O3) {
-      return visc ? launch_faces_t<Z2D, AUSM, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z2D, AUSM, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      return visc ? op.template run<Z2D, AUSM, O3, true>()
+                  : op.template run<Z2D, AUSM, O3, false>();
     } else if (z.kflu == SENSEUR && z.slope == O3) {
-      return visc ? launch_faces_t<Z2D, SENSEUR, O3, true>(z, q, xmut, Fi, Fj, Fk, st)
-                  : launch_faces_t<Z2D, SENSEUR, O3, false>(z, q, xmut, Fi, Fj, Fk, st);
+      return visc ? op.template run<Z2D, SENSEUR, O3, true>()
+                  : op.template run<Z2D, SENSEUR, O3, false>();
     }
   }
   return cudaErrorNotSupported;
+}
+
+struct FacesOne {
+  const Zone& z; const double* q; const double* xmut; double *Fi, *Fj, *Fk; cudaStream_t st;
+  template <int TYP, int KF, int SL, bool VISC, int NV = 5>
+  cudaError_t run() { return launch_faces_t<TYP, KF, SL, VISC, NV>(z, q, xmut, Fi, Fj, Fk, st); }
+};
+
+cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
+                         double* Fj, double* Fk, cudaStream_t st) {
+  FacesOne op{z, q, xmut, Fi, Fj, Fk, st};
+  return faces_dispatch(z, op);
+}
+
+// A batch of zones of one kind: the faces of direction D of every zone in
+// one launch, blocks of b.block threads.
+struct FacesBatchOp {
+  FaceBatch& b; cudaStream_t st;
+  template <int TYP, int KF, int SL, bool VISC, int NV = 5>
+  cudaError_t run() {
+    const int B = b.block;
+    for (int D = 0; D < (TYP == Z2D ? 2 : 3); D++) {
+      b.bstart[0] = 0;
+      for (int m = 0; m < b.nz; m++) {
+        const Zone& z = b.e[m].z;
+        const int64_t nf = (z.ni + (D == 0)) * (z.nj + (D == 1)) * (z.nk + (D == 2));
+        b.bstart[m + 1] = b.bstart[m] + (nf + B - 1) / B;
+      }
+      const unsigned g = (unsigned)b.bstart[b.nz];
+      if (D == 0) face_flux_batch<0, TYP, KF, SL, VISC, NV><<<g, B, 0, st>>>(b);
+      else if (D == 1) face_flux_batch<1, TYP, KF, SL, VISC, NV><<<g, B, 0, st>>>(b);
+      else face_flux_batch<2, TYP, KF, SL, VISC, NV><<<g, B, 0, st>>>(b);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+};
+
+cudaError_t launch_faces_batch(FaceBatch& b, cudaStream_t st) {
+  if (b.nz <= 0) return cudaSuccess;
+  if (b.block != 64 && b.block != 128 && b.block != 256) return cudaErrorInvalidValue;
+  FacesBatchOp op{b, st};
+  return faces_dispatch(b.e[0].z, op);
+}
+
+int faces_batch_blocks(int* out, int nmax) {
+  const int c[3] = {64, 128, 256};
+  int n = 0;
+  for (int k = 0; k < 3 && n < nmax; k++) out[n++] = c[k];
+  return n;
+}
+
+// the template instance a zone's faces use
+int64_t faces_kind_key(const Zone& z) {
+  return (int64_t)z.typ | ((int64_t)z.kflu << 4) | ((int64_t)z.slope << 8) |
+         ((int64_t)(z.iflow >= 2) << 12) | ((int64_t)z.neq << 13);
+}
+
+cudaError_t launch_assemble_batch(StageBatch& b, bool implicit, cudaStream_t st) {
+  if (b.nz <= 0) return cudaSuccess;
+  const int B = 256;
+  b.bstart[0] = 0;
+  for (int m = 0; m < b.nz; m++) {
+    const Zone& z = b.e[m].z;
+    b.bstart[m + 1] = b.bstart[m] + (z.ni * z.nj * z.nk + B - 1) / B;
+  }
+  const unsigned g = (unsigned)b.bstart[b.nz];
+  const bool sa = b.e[0].z.neq == 6;
+  if (implicit) {
+    if (sa) assemble_batch<true, 6><<<g, B, 0, st>>>(b);
+    else assemble_batch<true, 5><<<g, B, 0, st>>>(b);
+  } else {
+    if (sa) assemble_batch<false, 6><<<g, B, 0, st>>>(b);
+    else assemble_batch<false, 5><<<g, B, 0, st>>>(b);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sa_source_batch(SaBatch& b, cudaStream_t st) {
+  if (b.nz <= 0) return cudaSuccess;
+  const int B = 256;
+  b.bstart[0] = 0;
+  for (int m = 0; m < b.nz; m++) {
+    const Zone& z = b.e[m].z;
+    b.bstart[m + 1] = b.bstart[m] + (z.ni * z.nj * z.nk + B - 1) / B;
+  }
+  const unsigned g = (unsigned)b.bstart[b.nz];
+  const int typ = b.e[0].z.typ;
+  if (typ == Z3DCART) sa_source_batch<Z3DCART><<<g, B, 0, st>>>(b);
+  else if (typ == Z3DFULL) sa_source_batch<Z3DFULL><<<g, B, 0, st>>>(b);
+  else if (typ == Z2D) sa_source_batch<Z2D><<<g, B, 0, st>>>(b);
+  else return cudaErrorNotSupported;
+  return cudaGetLastError();
 }
 
 // --------------------------------------------------- wall correction (Roe)

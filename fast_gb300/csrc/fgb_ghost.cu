@@ -230,6 +230,57 @@ __global__ void __launch_bounds__(256) gather_cat(double* __restrict__ q, int64_
   }
 }
 
+// Interpolated (overset) transfers of one donor / receiver pair: receiver
+// cell ri[t] <- sum over the molecule of type ty[t] starting at donor cell
+// di[t] of coefficient x donor value.  Types: 0 / 1 one donor; 2 trilinear
+// and 22 bilinear in (i, j) (weights i fastest); 3 and 5 tensor-product
+// Lagrange (separable factors: i, then j, then k); summed i fastest.
+__global__ void __launch_bounds__(256) transfer_interp(double* __restrict__ dst, int64_t nd_dst,
+                                                       const double* __restrict__ src, int64_t nd_src,
+                                                       int64_t sj, int64_t sk,
+                                                       const int32_t* __restrict__ ri,
+                                                       const int32_t* __restrict__ di,
+                                                       const int32_t* __restrict__ ty,
+                                                       const int64_t* __restrict__ coff,
+                                                       const double* __restrict__ coef, int64_t n,
+                                                       int neq) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int typ = ty[t];
+  const int64_t d0 = di[t], r = ri[t];
+  const double* c = coef + coff[t];
+  for (int v = 0; v < neq; v++) {
+    const double* f = src + v * nd_src;
+    double val = 0.;
+    if (typ == 0 || typ == 1) {
+      val = c[0] * f[d0];
+    } else if (typ == 2 || typ == 22) {
+      const int nk = typ == 2 ? 2 : 1;
+      for (int kk = 0; kk < nk; kk++)
+        for (int jj = 0; jj < 2; jj++)
+          for (int ii = 0; ii < 2; ii++)
+            val += c[ii + 2 * jj + 4 * kk] * f[d0 + ii + jj * sj + kk * sk];
+    } else {
+      const int w = typ == 3 ? 3 : 5;
+      for (int kk = 0; kk < w; kk++)
+        for (int jj = 0; jj < w; jj++)
+          for (int ii = 0; ii < w; ii++)
+            val += c[ii] * c[w + jj] * c[2 * w + kk] * f[d0 + ii + jj * sj + kk * sk];
+    }
+    dst[r + v * nd_dst] = val;
+  }
+}
+
+cudaError_t launch_transfer_interp(double* dst, int64_t nd_dst, const double* src, int64_t nd_src,
+                                   int64_t sj, int64_t sk, const int32_t* ri, const int32_t* di,
+                                   const int32_t* ty, const int64_t* coff, const double* coef,
+                                   int64_t n, int neq, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  transfer_interp<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dst, nd_dst, src, nd_src, sj, sk, ri, di,
+                                                               ty, coff, coef, n, neq);
+  return cudaGetLastError();
+}
+
 __global__ void __launch_bounds__(256) transfer_all(ZoneLevels zl, const int32_t* __restrict__ rz,
                                                     const int32_t* __restrict__ ri,
                                                     const int32_t* __restrict__ dz,
@@ -247,6 +298,101 @@ cudaError_t launch_transfer_all(const ZoneLevels& zl, const int32_t* rz, const i
                                 const int32_t* dz, const int32_t* di, int64_t n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   transfer_all<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(zl, rz, ri, dz, di, n);
+  return cudaGetLastError();
+}
+
+// One ghost rank of BC_nextrank.for: cell l from q0 (the rank before it),
+// q1 and q2 (the two before that)
+__device__ __forceinline__ void next_rank(double* __restrict__ q, int64_t nd, bool sa, double k1,
+                                          double k2, double k3, int64_t l, int64_t q0, int64_t q1,
+                                          int64_t q2) {
+  const int nv = sa ? 6 : 5;
+  const double r = q[q0] * k3 + q[q1] * k1 + q[q2] * k2;
+  const bool keep = sa ? r <= 0.3 * q[q0] : fabs(r / q[q0] - 1.) >= 0.7;
+  if (keep) {
+    for (int v = 0; v < nv; v++) q[l + v * nd] = q[q0 + v * nd];
+  } else {
+    q[l] = r;
+    for (int v = 1; v < nv; v++) q[l + v * nd] = q[q0 + v * nd] * k3 + q[q1 + v * nd] * k1 + q[q2 + v * nd] * k2;
+  }
+}
+
+// The ranks past the first of one ghost line, outwards, by one thread (each
+// reads the rank written just before it: three ghost layers chain).
+__device__ __forceinline__ void next_ranks(double* __restrict__ q, int64_t nd, bool sa, int nrank,
+                                           const BcNextArgs& a, int64_t e) {
+  int64_t l = a.dst[e], q0 = a.q0[e], q1 = a.q1[e], q2 = a.q2[e];
+  const int64_t step = l - q0;
+  for (int r = 0; r < nrank; r++) {
+    next_rank(q, nd, sa, a.k1, a.k2, a.k3, l, q0, q1, q2);
+    q2 = q1; q1 = q0; q0 = l; l += step;
+  }
+}
+
+// ------------------------------------------- ghost fill over every zone
+// The BC lists of every zone concatenated, with the zone of each entry:
+// one launch per kind for the whole solver (face BCs, gathers, next ranks,
+// corners, in that order as per zone), the zones' level pointers travelling
+// in the kernel parameter.  No zone's fill reads another zone's cells.
+__global__ void __launch_bounds__(128) bc_face_all(ZoneLevels zl, BcFaceCat c,
+                                                  const int32_t* __restrict__ zid) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= c.n) return;
+  const double t[3] = {c.nrm[3 * e], c.nrm[3 * e + 1], c.nrm[3 * e + 2]};
+  bc_face_entry(zl.q[zid[e]], c.lp[c.lid[e]], c.dst[e], c.src[e], t, c.aux ? c.aux[e] : 0.);
+}
+
+__global__ void __launch_bounds__(256) gather_all(ZoneLevels zl, GatherCat c,
+                                                 const int32_t* __restrict__ zid) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= c.n) return;
+  const int m = zid[t];
+  double* q = zl.q[m];
+  const int64_t nd = zl.nd[m];
+  const int64_t d = c.dst[t], s = c.src[t];
+  const int op = c.op[t];
+  for (int v = 0; v < zl.neq[m]; v++) {
+    double x = q[s + v * nd];
+    if (op == 1) x = fmaxF(-1.e30, x);
+    if (op != 0) x = x * 1.;
+    q[d + v * nd] = x;
+  }
+}
+
+__global__ void __launch_bounds__(128) bc_next_all(ZoneLevels zl, BcNextArgs a,
+                                                  const int32_t* __restrict__ zid) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n) return;
+  const int m = zid[e];
+  next_ranks(zl.q[m], zl.nd[m], zl.neq[m] == 6, zl.ng[m] - 1, a, e);
+}
+
+__global__ void __launch_bounds__(256) coins_all(ZoneLevels zl, const int32_t* __restrict__ dst,
+                                                const int32_t* __restrict__ a,
+                                                const int32_t* __restrict__ b,
+                                                const int32_t* __restrict__ c,
+                                                const int32_t* __restrict__ zid, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int m = zid[t];
+  double* q = zl.q[m];
+  const int64_t nd = zl.nd[m];
+  const double c3 = 1. / 3.;
+  for (int v = 0; v < zl.neq[m]; v++) {
+    const double* Q = q + v * nd;
+    double x;
+    if (c[t] < 0) x = (Q[a[t]] + Q[b[t]]) * 0.5;     // edge (no third cell)
+    else x = (Q[a[t]] + Q[b[t]] + Q[c[t]]) * c3;      // corner
+    q[dst[t] + v * nd] = x;
+  }
+}
+
+cudaError_t launch_fill_all(const ZoneLevels& zl, const FillAll& f, cudaStream_t st) {
+  if (f.face.n > 0) bc_face_all<<<(unsigned)((f.face.n + 127) / 128), 128, 0, st>>>(zl, f.face, f.zface);
+  if (f.gat.n > 0) gather_all<<<(unsigned)((f.gat.n + 255) / 256), 256, 0, st>>>(zl, f.gat, f.zgat);
+  if (f.next.n > 0) bc_next_all<<<(unsigned)((f.next.n + 127) / 128), 128, 0, st>>>(zl, f.next, f.znext);
+  if (f.ncoin > 0)
+    coins_all<<<(unsigned)((f.ncoin + 255) / 256), 256, 0, st>>>(zl, f.cdst, f.ca, f.cb, f.cc, f.zcoin, f.ncoin);
   return cudaGetLastError();
 }
 
@@ -269,16 +415,7 @@ cudaError_t launch_gather_cat(double* q, int64_t nd, const GatherCat& c, int neq
 __global__ void __launch_bounds__(128) bc_next(double* __restrict__ q, BcNextArgs a) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= a.n) return;
-  const int64_t nd = a.nd, l = a.dst[e], q0 = a.q0[e], q1 = a.q1[e], q2 = a.q2[e];
-  const int nv = a.sa ? 6 : 5;
-  const double r = q[q0] * a.k3 + q[q1] * a.k1 + q[q2] * a.k2;
-  const bool keep = a.sa ? r <= 0.3 * q[q0] : fabs(r / q[q0] - 1.) >= 0.7;
-  if (keep) {
-    for (int v = 0; v < nv; v++) q[l + v * nd] = q[q0 + v * nd];
-  } else {
-    q[l] = r;
-    for (int v = 1; v < nv; v++) q[l + v * nd] = q[q0 + v * nd] * a.k3 + q[q1 + v * nd] * a.k1 + q[q2 + v * nd] * a.k2;
-  }
+  next_ranks(q, a.nd, a.sa != 0, a.nrank, a, e);
 }
 
 cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st) {

@@ -31,6 +31,27 @@ struct WallCorrArgs {
 };
 cudaError_t launch_wall_corr(const Zone& z, const double* q, double* drodm, const WallCorrArgs& a,
                              cudaStream_t st);
+
+// Zone batches: one launch of a kernel over up to BATCH_MAX zones of one
+// kind (the same template instance).  The entries travel in the kernel
+// parameter (__grid_constant__, at most 32 KB); block b of the launch works
+// on zone m with bstart[m] <= b < bstart[m + 1] (bstart[nz] = grid size).
+constexpr int BATCH_MAX = 40;
+struct FaceEntry { Zone z; const double* q; const double* xmut; double* F[3]; };
+struct FaceBatch { int nz; int block; int64_t bstart[BATCH_MAX + 1]; FaceEntry e[BATCH_MAX]; };
+struct StageEntry { Zone z; StageArgs a; };
+struct StageBatch { int nz; int64_t bstart[BATCH_MAX + 1]; StageEntry e[BATCH_MAX]; };
+struct SaEntry { Zone z; const double* q; double* drodm; double* coe; };
+struct SaBatch { int nz; double coefH; int zero_init, lu; int64_t bstart[BATCH_MAX + 1]; SaEntry e[BATCH_MAX]; };
+// faces of every direction of a batch (block: threads per block, chosen by
+// the autotuner; the caller fills z, q, xmut, F of each entry); the zones
+// share the kind of e[0].z (zone type, scheme, slope, viscosity, NEQ)
+cudaError_t launch_faces_batch(FaceBatch& b, cudaStream_t st);
+// the block sizes launch_faces_batch may use, and a key of the kind of zone z
+int faces_batch_blocks(int* out, int nmax);
+int64_t faces_kind_key(const Zone& z);
+cudaError_t launch_assemble_batch(StageBatch& b, bool implicit, cudaStream_t st);
+cudaError_t launch_sa_source_batch(SaBatch& b, cudaStream_t st);
 cudaError_t launch_faces(const Zone& z, const double* q, const double* xmut, double* Fi,
                          double* Fj, double* Fk, cudaStream_t st);
 cudaError_t launch_wiggle(const Zone& z, const double* q, double* wig, cudaStream_t st);
@@ -87,6 +108,7 @@ int lusgs_flow_chunk();
 
 struct LuGroup {
   int persistent;           // 0 one launch per plane, 1 grid barrier, 2 dataflow
+  int flow_per_sm;          // dataflow: CTAs per SM (0: one)
   FlowArgs flow;
   int grid_cap;             // > 0: at most this many CTAs in the persistent sweep
   int fp32;
@@ -108,6 +130,9 @@ int64_t lusgs_work_words(int typ);
 // neighbour tables of a group (ztab must hold every zone's z and f.posmap)
 cudaError_t launch_lu_neighbours(const LuGroup& G, cudaStream_t st);
 cudaError_t launch_coefficients(const Zone& z, const CoeArgs& a, cudaStream_t st);
+struct CoeEntry { Zone z; CoeArgs a; };
+struct CoeBatch { int nz; int64_t bstart[BATCH_MAX + 1]; CoeEntry e[BATCH_MAX]; };
+cudaError_t launch_coefficients_batch(const CoeBatch& b, cudaStream_t st);
 // gather of every zone, sweeps, Newton update; ztab_host = the nz entries
 // already copied to G.ztab on the stream
 cudaError_t launch_lusgs(const LuZone* ztab_host, const LuGroup& G, cudaStream_t st);
@@ -155,20 +180,36 @@ struct GatherCat {
   int64_t n;
 };
 struct BcNextArgs {            // farfield / inflow ghost ranks past the first
-  const int32_t *dst, *q0, *q1, *q2;
+  const int32_t *dst, *q0, *q1, *q2;   // one entry per ghost line: its second rank
   int64_t n, nd;
   double k1, k2, k3;
   int sa;
+  int nrank;                   // ranks past the first (ghost layers - 1), one after the other
 };
 cudaError_t launch_bc_face_cat(double* q, const BcFaceCat& c, cudaStream_t st);
 // Every 1-to-1 transfer of a solver in one launch: entry t copies cell
 // di[t] of zone dz[t] into ghost cell ri[t] of zone rz[t] (all variables);
 // the zones' current level pointers travel as a kernel parameter
 constexpr int ZT_MAX = 64;
-struct ZoneLevels { double* q[ZT_MAX]; int64_t nd[ZT_MAX]; int neq[ZT_MAX]; };
+struct ZoneLevels { double* q[ZT_MAX]; int64_t nd[ZT_MAX]; int neq[ZT_MAX]; int ng[ZT_MAX]; };
 cudaError_t launch_transfer_all(const ZoneLevels& zl, const int32_t* rz, const int32_t* ri,
                                 const int32_t* dz, const int32_t* di, int64_t n, cudaStream_t st);
+// Interpolated transfers of one donor / receiver zone pair (sj, sk: the
+// donor's j and k cell strides; coff: first coefficient of each point)
+cudaError_t launch_transfer_interp(double* dst, int64_t nd_dst, const double* src, int64_t nd_src,
+                                   int64_t sj, int64_t sk, const int32_t* ri, const int32_t* di,
+                                   const int32_t* ty, const int64_t* coff, const double* coef,
+                                   int64_t n, int neq, cudaStream_t st);
 cudaError_t launch_gather_cat(double* q, int64_t nd, const GatherCat& c, int neq, cudaStream_t st);
+// The BC lists of every zone of a solver concatenated with the zone of each
+// entry (zface, zgat, znext, zcoin); corners: cc < 0 marks an edge
+struct FillAll {
+  BcFaceCat face; const int32_t* zface;
+  GatherCat gat; const int32_t* zgat;
+  BcNextArgs next; const int32_t* znext;
+  const int32_t *cdst, *ca, *cb, *cc, *zcoin; int64_t ncoin;
+};
+cudaError_t launch_fill_all(const ZoneLevels& zl, const FillAll& f, cudaStream_t st);
 cudaError_t launch_bc_next(double* q, const BcNextArgs& a, cudaStream_t st);
 cudaError_t launch_coins(double* q, int64_t nd, const int32_t* dst, const int32_t* a,
                          const int32_t* b, const int32_t* c, int64_t n_edge, int64_t n, int neq,

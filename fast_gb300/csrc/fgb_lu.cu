@@ -14,14 +14,14 @@
 // neighbour is therefore read after its update while the i+1 / j+1
 // neighbours are read before theirs.  The kernels reproduce that by writing
 // the updated state to a separate buffer and reading the k+1 neighbour from it.
+#include <algorithm>
 #include "fgb_kernels.cuh"
 
 namespace fgb {
 
 // ----------------------------------------------------------- coefficients
-__global__ void __launch_bounds__(256) coefficients(Zone z, CoeArgs a) {
+__device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a, const int64_t t) {
   const int64_t nx = a.hi[0] - a.lo[0] + 1, ny = a.hi[1] - a.lo[1] + 1, nz = a.hi[2] - a.lo[2] + 1;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nx * ny * nz) return;
   const int64_t i = a.lo[0] + t % nx;
   const int64_t r = t / nx;
@@ -125,6 +125,30 @@ __global__ void __launch_bounds__(256) coefficients(Zone z, CoeArgs a) {
   a.coe[l + 2 * nd] = c3;
   a.coe[l + 3 * nd] = c4;
   a.coe[l + 4 * nd] = xid + c1 * (c2 + c3 + c4) * 0.5;
+}
+
+__global__ void __launch_bounds__(256) coefficients(Zone z, CoeArgs a) {
+  coefficients_at(z, a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__device__ __forceinline__ int batch_zone_lu(const int64_t* bstart, int nz, int64_t b) {
+  int lo = 0, hi = nz - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (bstart[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(256) coefficients_batch(const __grid_constant__ CoeBatch b) {
+  const int m = batch_zone_lu(b.bstart, b.nz, blockIdx.x);
+  coefficients_at(b.e[m].z, b.e[m].a, (int64_t)(blockIdx.x - b.bstart[m]) * blockDim.x + threadIdx.x);
+}
+
+cudaError_t launch_coefficients_batch(const CoeBatch& b, cudaStream_t st) {
+  if (b.nz <= 0) return cudaSuccess;
+  coefficients_batch<<<(unsigned)b.bstart[b.nz], 256, 0, st>>>(b);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_coefficients(const Zone& z, const CoeArgs& a, cudaStream_t st) {
@@ -875,6 +899,10 @@ __device__ __forceinline__ bool flow_poll(const FlowArgs& a, int64_t c, int mark
   }
 }
 
+// (Loading the cells' static operands before the wait was measured slower:
+// the operands held across the wait raise the register count to 154 and
+// halve the resident warps; so was splitting the neighbours' wait and the
+// upper chunk's own-lower wait into two rounds.)
 template <int TYP, typename T, int NV, bool MULTI, bool UPPER>
 __device__ __forceinline__ void flow_chunk(const Zone& z, const PlaneData<T>& p, const LuFields& f,
                                            int64_t g0, int64_t n, int lane) {
@@ -1032,9 +1060,18 @@ static cudaError_t sweep_t(const Zone& z, const LuFields& f, const PlaneData<T>&
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_flow<TYP, T, NV, MULTI>,
                                                         FLOW_THREADS, 0);
       if (e != cudaSuccess) return e;
-      grids[dev] = nsm * (per > 0 ? per : 1);
+      if (per < 1) return cudaErrorLaunchOutOfResources;
+      grids[dev] = nsm * per;
     }
-    int grid = grids[dev];
+    // CTAs per SM: L.flow_per_sm (the autotuner's choice), by default one
+    // (8 warps), measured faster than filling every resident slot on one
+    // large zone (256^3 Taylor-Green, FP64: 98 vs 105 ms of LU-SGS per step)
+    int nsm_ = 0;
+    e = cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int per_max = grids[dev] / (nsm_ > 0 ? nsm_ : 1);
+    const int per_use = L.flow_per_sm > 0 ? std::min(L.flow_per_sm, per_max) : 1;
+    int grid = nsm_ * per_use;
     if (L.grid_cap > 0 && L.grid_cap < grid) grid = L.grid_cap;
     e = cudaMemsetAsync(L.flow.ticket, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;

@@ -420,7 +420,19 @@ def _prim_names(z):
 def createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
     """FastC/FastC/PyTree.py:215: conservative -> primitive variables at
     centers, plus the _M1 and _P1 time levels, each level compacted into one
-    contiguous (NEQ, NDIMDX) array (_compact, :2236)."""
+    contiguous (NEQ, NDIMDX) array (_compact, :2236).  Works in place and
+    returns (t, first_iter, vars_zones) as the reference does: first_iter is
+    1 when every zone already holds its _M1 level (a restart: the time
+    levels are kept and the next step is BDF2), 0 otherwise (the levels are
+    created from the current one, FastC/FastC/PyTree.py:497-509)."""
+    first_iter = _createPrimVars(t, omp_mode, rmConsVars, Adjoint)
+    vars_zones = [[z, _prim_names(z)] for z in I.getZones(t)]
+    return t, first_iter, vars_zones
+
+
+def _createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
+    """In-place createPrimVars; returns FIRST_IT."""
+    first_iter = 1
     for z in I.getZones(t):
         sol = I.getNodeFromName1(z, I.__FlowSolutionCenters__)
         o = I.getNodeFromName1(z, ".Solver#ownData")
@@ -454,7 +466,14 @@ def createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
         n = prim[0].size
         for suffix in ("", "_M1", "_P1"):
             buf = np.empty((len(names), n), dtype=np.float64)
-            for v_, arr in enumerate(prim):
+            kept = [I.getNodeFromName1(sol, nm + suffix) for nm in names] if suffix else []
+            if suffix and all(k is not None for k in kept):
+                src = [k[1] for k in kept]          # a restart: the level is kept
+            else:
+                src = prim
+                if suffix == "_M1":
+                    first_iter = 0
+            for v_, arr in enumerate(src):
                 buf[v_] = np.asarray(arr, dtype=np.float64).ravel(order="F")
             for v_, name in enumerate(names):
                 view = buf[v_].reshape(shape, order="F")
@@ -465,7 +484,7 @@ def createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
             I.getNodeFromName1(o_, "compact" + suffix)[1] = buf
         if rmConsVars:
             sol[2] = [c for c in sol[2] if c[0] not in CONS[1:]]
-    return t
+    return first_iter
 
 
 def compactArray(z, level):
@@ -485,3 +504,113 @@ def switchPointers__(zones, case=3):
         for name in _prim_names(z):
             a, b, c = (I.getNodeFromName1(sol, name + s) for s in ("", "_M1", "_P1"))
             a[1], b[1], c[1] = c[1], a[1], b[1]
+
+
+# ------------------------------------------------------------ restart I/O
+# FastC/FastC/PyTree.py:3514-3560 (load / save) write CGNS/HDF5 files
+# through Cassiopee's Converter, which is not available here (neither is
+# h5py).  The same trees are written instead to a numpy .npz container that
+# keeps the CGNS/Python structure node for node: "tree" holds a JSON list of
+# [parent, name, type, value] entries in depth-first order (parent = index
+# of the parent entry, -1 for the root; value = null, a string, or the key
+# of a numpy array stored beside it in the archive, with its dtype, shape and
+# Fortran order preserved).
+def _tree_to_npz(t, path):
+    import json
+    entries, arrays = [], {}
+
+    def walk(node, parent):
+        idx = len(entries)
+        v = node[1]
+        if v is None:
+            val = None
+        elif isinstance(v, np.ndarray) and v.dtype == np.dtype("c"):
+            val = {"str": b"".join(v.ravel(order="F").tolist()).decode()}
+        elif isinstance(v, str):
+            val = {"str": v}
+        else:
+            key = "a%d" % len(arrays)
+            a = np.asarray(v)
+            arrays[key] = a
+            val = {"key": key, "fortran": bool(a.flags.f_contiguous and not a.flags.c_contiguous)}
+        entries.append([parent, node[0], node[3], val])
+        for c in node[2]:
+            walk(c, idx)
+
+    walk(t, -1)
+    np.savez_compressed(path, tree=np.array(json.dumps(entries)), **arrays)
+
+
+def _tree_from_npz(path):
+    import json
+    with np.load(path, allow_pickle=False) as f:
+        entries = json.loads(str(f["tree"]))
+        nodes = []
+        for parent, name, ntype, val in entries:
+            if val is None:
+                v = None
+            elif "str" in val:
+                v = np.array([c for c in val["str"]], dtype="c")
+            else:
+                v = np.array(f[val["key"]])
+                if val.get("fortran"):
+                    v = np.asfortranarray(v)
+            node = [name, v, [], ntype]
+            if parent >= 0:
+                nodes[parent][2].append(node)
+            nodes.append(node)
+    return nodes[0]
+
+
+def saveTree(t, fileName="restart.npz", split="single", compress=0):
+    """FastC/FastC/PyTree.py:3755: the tree without what a restart does not
+    need -- the _P1 time level, the solver's own data (Parameter_int /
+    Parameter_real, compacted levels), motion nodes -- written as one file
+    (split = 'single'; the 'multiple' per-process layout belongs to MPI runs,
+    which this solver does not have)."""
+    import copy
+    if split != "single":
+        raise ValueError("saveTree: only split='single' is supported (one process)")
+    t2 = copy.deepcopy(t)
+    p1 = {n + "_P1" for n in PRIM_SA}
+
+    def strip(node):
+        node[2] = [c for c in node[2]
+                   if c[0] not in (".Solver#ownData", "Displacement#0", "Motion")
+                   and not (node[0] == I.__FlowSolutionCenters__ and c[0] in p1)]
+        for c in node[2]:
+            strip(c)
+
+    strip(t2)
+    _tree_to_npz(t2, fileName)
+
+
+def loadTree(fileName="restart.npz", split="single", graph=False, exploc=0):
+    """FastC/FastC/PyTree.py loadTree: the tree of a file written by
+    saveTree (graph=True also returns the communication graph, None here)."""
+    if split != "single":
+        raise ValueError("loadTree: only split='single' is supported (one process)")
+    t = _tree_from_npz(fileName)
+    return (t, None) if graph else t
+
+
+def save(t, fileName="restart.npz", tc=None, fileNameC="tc_restart.npz", ts=None,
+         fileNameS="tstat_restart.npz", split="single", compress=0):
+    """FastC/FastC/PyTree.py:3542: save t (and tc, ts when given)."""
+    saveTree(t, fileName=fileName, split=split, compress=compress)
+    if tc is not None:
+        saveTree(tc, fileName=fileNameC, split=split, compress=compress)
+    if ts is not None:
+        saveTree(ts, fileName=fileNameS, split=split, compress=compress)
+
+
+def load(fileName="t.npz", fileNameC=None, fileNameS=None, split="single", exploc=0):
+    """FastC/FastC/PyTree.py:3514: (t, tc, ts, graph) from the files written
+    by save."""
+    t = loadTree(fileName=fileName, split=split, graph=False, exploc=exploc)
+    if fileNameC is not None:
+        tc, graph = loadTree(fileName=fileNameC, split=split, graph=True, exploc=exploc)
+    else:
+        tc, graph = None, None
+    ts = loadTree(fileName=fileNameS, split=split) if fileNameS is not None else None
+    return t, tc, ts, graph

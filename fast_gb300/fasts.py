@@ -16,6 +16,7 @@ import sys
 
 import numpy as np
 
+from . import connector
 from . import fastc as FastC
 from . import metric
 from . import pytree as I
@@ -23,6 +24,7 @@ from ._native import Solver
 
 HOOK: dict | None = None
 FIRST_IT = 0
+PREPARED_FIRST_IT = 0   # first_iter of the last prepare (1: a restart with its _M1 level)
 
 
 # --------------------------------------------------------------- metric
@@ -46,8 +48,31 @@ def allocate_metric(z, nssiter, verbose=0):
     pi[FastC.IJKV:FastC.IJKV + 3] = [pi[0] - 2 * pi[3], pi[1] - 2 * pi[3], pi[2] - 2 * pi[4]]
     pi[FastC.NDIMDX] = pi[0] * pi[1] * pi[2]
     pi[FastC.NDIMDX_XYZ] = ni * nj * nk
+    # allocate_metric.cpp:101-117: the o5 slopes (5, 7) need three ghost
+    # layers (a Rind of 3 on every side), the others use two
+    if int(pi[FastC.SLOPE]) in (5, 7):
+        rind = I.getNodeFromName1(z, "Rind")
+        need = 12 if nk == 2 else 18
+        if rind is None or int(np.sum(np.asarray(rind[1])[:4 if nk == 2 else 6])) != need:
+            raise ValueError("Fast: ghostcell number insufficient for o(5) slope (Rind 3 needed)")
+        ific = 3
+        pi[FastC.NIJK_XYZ:FastC.NIJK_XYZ + 5] = [ni, nj, nk, ific, 0 if nk == 2 else ific]
+        pi[FastC.NIJK:FastC.NIJK + 5] = [ni - 1, nj - 1, nk - 1, ific, 0 if nk == 2 else ific]
+        pi[FastC.IJKV:FastC.IJKV + 3] = [pi[0] - 2 * pi[3], pi[1] - 2 * pi[3], pi[2] - 2 * pi[4]]
+        pi[FastC.NDIMDX] = pi[0] * pi[1] * pi[2]
     x, y, z_ = _coords(z)
     typ = _zone_type(x, y, z_, nk)
+    if typ == 1:
+        # A 3-d zone with a homogeneous k direction (nature_geom_dom.for's
+        # type 1: z = z(k) on a constant step, x and y independent of k)
+        # runs as a general 3-d zone: the reference's *_3dhomo_* variants are
+        # the *_3dfull_* formulas with the vanishing metric components
+        # dropped (e.g. Compute/Normale/normale_3dhomo_i.for against
+        # normale_3dfull_i.for), so the general kernels, on the full metric
+        # of the same mesh, compute the same quantities; the one difference
+        # is a k-face norm taken as sqrt(tcz^2) instead of |tcz|, within a
+        # rounding of it.
+        typ = 0
     pi[FastC.ITYPZONE] = typ
     nijk_mtr, ndm, neq_ij, neq_k = metric.dims(pi[FastC.NIJK_XYZ:FastC.NIJK_XYZ + 5], typ)
     pi[FastC.NIJK_MTR:FastC.NIJK_MTR + 5] = nijk_mtr
@@ -112,7 +137,8 @@ def prepare(t):
     nssiter = int(dtloc[0])
     metrics = [allocate_metric(z, nssiter) for z in zones]
     FastC._BCcompact(t)
-    FastC.createPrimVars(t)
+    global PREPARED_FIRST_IT
+    PREPARED_FIRST_IT = FastC._createPrimVars(t)
     return metrics
 
 
@@ -203,13 +229,25 @@ def zone_data(t, metrics):
     return out
 
 
+def transfer_list(t, tc):
+    """The interface transfers of ``tc``: a Connector tc tree (ID_ zone
+    subregions with PointList / PointListDonor / InterpolantsType /
+    InterpolantsDonor, read by fast_gb300.connector), or a list of transfer
+    dicts (dnr, rcv, dnr_idx, rcv_idx[, types, coefs]), or None."""
+    if tc is None:
+        return []
+    if connector.is_tree(tc):
+        return connector.transfers_from_tc(t, tc)
+    return list(tc)
+
+
 def warmup(t, tc=None, graph=None, infos_ale=None, Adjoint=False, tmy=None, list_graph=None,
            Padding=None, verbose=0, device=0, gpu_resident=False):
     """FastS/FastS/PyTree.py:341: numerics, metric, primitive variables,
-    ghost cells; creates the GPU solver in HOOK.  ``tc`` may hold 1-to-1
-    interfaces as produced by fast_gb300.cases (list of dicts with keys
-    dnr, rcv, dnr_idx, rcv_idx); Cassiopee's connectivity trees are not
-    supported.  With ``gpu_resident`` the state stays on the GPU between
+    ghost cells; creates the GPU solver in HOOK.  ``tc`` is the Connector
+    donor tree FastS takes (1-to-1 and overset ID_ subregions, read once
+    here: the connectivity does not change between _compute calls), or a
+    list of transfer dicts (see transfer_list).  With ``gpu_resident`` the state stays on the GPU between
     ``_compute`` calls and the tree is refreshed by ``_syncHost``."""
     global HOOK, FIRST_IT
     metrics = prepare(t)
@@ -221,10 +259,10 @@ def warmup(t, tc=None, graph=None, infos_ale=None, Adjoint=False, tmy=None, list
         solver.add_zone(zd["pi"], zd["pr"], zd["ti"], zd["tj"], zd["tk"], zd["vol"])
         if "dist" in zd:
             solver.set_wall_distance(n, zd["dist"])
-    for tr in (tc or []):
-        solver.add_transfer(tr["dnr"], tr["rcv"], tr["dnr_idx"], tr["rcv_idx"])
+    for tr in transfer_list(t, tc):
+        solver.add_any_transfer(tr)
     solver.set_option("modulo_verif", int(dtloc[1]))
-    FIRST_IT = 0
+    FIRST_IT = PREPARED_FIRST_IT
     solver.set_option("first_it", FIRST_IT)
     HOOK = {"solver": solver, "nssiter": nssiter, "FIRST_IT": FIRST_IT,
             "gpu_resident": bool(gpu_resident), "zones": zones, "device_valid": False}
@@ -312,7 +350,9 @@ def display_temporal_criteria(t, metrics, nitrun, format=None, gmres=None, verbo
                               stopAtNan=True):
     """FastS/FastS/PyTree.py:2039 -> fasts.display_ss_iteration: Newton
     residual norms per zone (L2 = sqrt(sum/ncell)/dt, Loo = max/dt), printed
-    (format None/'double'), or stored in ZoneConvergenceHistory ('store')."""
+    (format None/'double'), stored in ZoneConvergenceHistory ('store'), or
+    the stored records written out: 'flush' to residuals.bin, 'ascii' to
+    residuals.dat (conv2pytree.for, lft = -1 / -2)."""
     s = HOOK["solver"]
     s.synchronize()
     zones = I.getZones(t)
@@ -341,6 +381,8 @@ def display_temporal_criteria(t, metrics, nitrun, format=None, gmres=None, verbo
                               np.log10(np.maximum(Loo[:, -1], cut)) - np.log10(np.maximum(Loo[:, 0], cut))])
         if format == "store":
             _store_history(z, nitrun, neq, cvg)
+        elif format in ("flush", "ascii"):
+            _write_history(z, neq, binary=format == "flush")
         elif format is None or format == "double":
             if verbose != "none":
                 for it in range(L2.shape[1]):
@@ -380,6 +422,83 @@ def _store_history(z, nitrun, neq, cvg):
     for k, name in enumerate(("RSD_L2", "RSD_oo", "RSD_L2_diff", "RSD_oo_diff")):
         I.getNodeFromName1(ch, name)[1][last * neq:(last + 1) * neq] = cvg[k * neq:(k + 1) * neq]
     ch[1] = np.array([last + 1], dtype=np.int64)
+
+
+# INTEGER_E of the reference's Fortran: 4 bytes in Cassiopee's default build
+# (8 with E_DOUBLEINT); the width the residuals.bin records are written with
+RESIDUALS_BIN_INT = np.int32
+
+
+def _write_history(z, neq, binary, directory="."):
+    """conv2pytree.for:22-55 (lft < 0): the records stored in the zone's
+    ZoneConvergenceHistory appended to residuals.bin (format 'flush', lft =
+    -1: one Fortran unformatted sequential record per call -- 4-byte length
+    markers around zone name (40 characters, blank padded), neq, LastRec and,
+    per stored iteration, its number then (L2, Loo) of every equation; the
+    stored records are then released, LastRec = 0) or residuals.dat (format
+    'ascii', lft = -2: the Tecplot text of the same records)."""
+    import os
+    ch = I.getNodeFromName1(z, "ZoneConvergenceHistory")
+    if ch is None:
+        return
+    last = int(I.getValue(ch))
+    it = I.getNodeFromName1(ch, "IterationNumber")[1]
+    l2 = I.getNodeFromName1(ch, "RSD_L2")[1]
+    oo = I.getNodeFromName1(ch, "RSD_oo")[1]
+    name = z[0][:40].ljust(40).encode()
+    if binary:
+        body = bytearray(name)
+        body += np.array([neq, last], dtype=RESIDUALS_BIN_INT).tobytes()
+        for r in range(last):
+            body += np.array([it[r]], dtype=RESIDUALS_BIN_INT).tobytes()
+            pair = np.empty(2 * neq)
+            pair[0::2] = l2[r * neq:(r + 1) * neq]
+            pair[1::2] = oo[r * neq:(r + 1) * neq]
+            body += pair.astype("<f8").tobytes()
+        mark = np.array([len(body)], dtype="<i4").tobytes()
+        with open(os.path.join(directory, "residuals.bin"), "ab") as f:
+            f.write(mark + bytes(body) + mark)
+        ch[1] = np.array([0], dtype=np.int64)
+        return
+    path = os.path.join(directory, "residuals.dat")
+    head = not os.path.exists(path) or os.path.getsize(path) == 0
+    eqs = ["Ro", "RoU", "RoV", "RoW", "RoE"] + (["Nut"] if neq == 6 else [])
+    with open(path, "a") as f:
+        if head:
+            f.write("VARIABLES=\"It\" " + " ".join('"%s_L2"' % e for e in eqs) + " " +
+                    " ".join('"%s_oo"' % e for e in eqs) + "\n")
+        f.write('ZONE T="%s"\n' % z[0][:40])
+        for r in range(last):
+            vals = []
+            for e in range(neq):
+                vals += [l2[r * neq + e], oo[r * neq + e]]
+            f.write("%7d" % it[r] + "".join(" %15.8E" % v for v in vals) + "\n")
+
+
+def read_residuals_bin(path="residuals.bin"):
+    """The records of a residuals.bin file: list of (zone name, iteration
+    numbers (LastRec), L2 (LastRec, neq), Loo (LastRec, neq))."""
+    out = []
+    data = open(path, "rb").read()
+    p = 0
+    isz = np.dtype(RESIDUALS_BIN_INT).itemsize
+    while p < len(data):
+        n = int(np.frombuffer(data, "<i4", 1, p)[0])
+        body = data[p + 4:p + 4 + n]
+        p += 8 + n
+        name = body[:40].decode().rstrip()
+        neq, last = (int(x) for x in np.frombuffer(body, RESIDUALS_BIN_INT, 2, 40))
+        q = 40 + 2 * isz
+        its, l2, oo = [], [], []
+        for _ in range(last):
+            its.append(int(np.frombuffer(body, RESIDUALS_BIN_INT, 1, q)[0]))
+            q += isz
+            pair = np.frombuffer(body, "<f8", 2 * neq, q)
+            q += 16 * neq
+            l2.append(pair[0::2].copy())
+            oo.append(pair[1::2].copy())
+        out.append((name, np.array(its), np.array(l2).reshape(last, neq), np.array(oo).reshape(last, neq)))
+    return out
 
 
 def _extractConvergenceHistory(t, fileout):

@@ -61,6 +61,23 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
 int fgb_add_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
                      const int64_t* dnr_idx, const int64_t* rcv_idx);
 
+/* Add an interpolated (overset) interface: the non-type-0 transfers of
+ * FastC/FastC/Com/setInterpTransfersFast.cpp:804-960, whose arithmetic lives
+ * in Cassiopee Connector (commonInterpTransfers*.h, not part of the
+ * reference tree: the tensor-product formulas are restated, parity
+ * unpinned).  For t < n, receiver cell rcv_idx[t] of zone rcv_zone takes
+ * the sum over the donor molecule of type types[t] whose first cell is
+ * dnr_idx[t] of coefficient x donor value, for every variable: type 0 / 1
+ * one donor (1 coefficient), 2 trilinear 2x2x2 (8, i fastest), 22 bilinear
+ * 2x2 in (i, j) (4), 3 tensor-product Lagrange 3x3x3 (3 + 3 + 3 factors for
+ * i, j, k), 5 Lagrange 5x5x5 (5 + 5 + 5).  coefs: the coefficients of every
+ * point one after the other (ncoefs in all).  The tc tree's ID_ subregions
+ * carry exactly these arrays (PointList, PointListDonor, InterpolantsType,
+ * InterpolantsDonor). */
+int fgb_add_interp_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
+                            const int64_t* dnr_idx, const int64_t* rcv_idx, const int64_t* types,
+                            const double* coefs, int64_t ncoefs);
+
 /* Wall distance of a Spalart-Allmaras zone (IFLOW 3, NEQ 6): NDIMDX doubles
  * at cell centres, ghosts included -- the FlowSolution#Centers
  * "TurbulentDistance" field that FastS reads behind the viscosity array
@@ -80,7 +97,18 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * ghost fill), 0 for the solver stream alone (profiling uses it alone);
  * "lu_grid": 0 (default) for one persistent LU-SGS sweep CTA per resident
  * slot of the device, n > 0 for at most n CTAs (each CTA then takes more
- * cells of a hyperplane: same results, a schedule for testing). */
+ * cells of a hyperplane: same results, a schedule for testing);
+ * "lu_mode": 2 (default) dataflow LU-SGS sweeps (chunks of 32 cells of a
+ * hyperplane, point-to-point completion marks), 1 persistent sweeps with a
+ * grid barrier per hyperplane, 0 one launch per hyperplane (same results);
+ * "lu_poll_limit": polls before a dataflow wait gives up (default 2^22, then
+ * fgb_synchronize reports FGB_ERR_DEVICE); "lu_wait_skew": test support, 0;
+ * "batch": 1 (default) to run the coefficient, Spalart-Allmaras source,
+ * face and balance / update kernels of several zones as one launch per kind
+ * of zone (zone type, scheme, slope, viscosity, NEQ; up to 40 zones a
+ * launch), 0 for per-zone launches (same results); "autotune": 1 (default)
+ * to pick the batched face kernels' block size by timing the candidates on
+ * the first batch of each kind (kept per device for the process). */
 int fgb_set_option(fgb_solver* s, const char* key, double value);
 int fgb_get_option(fgb_solver* s, const char* key, double* value);
 

@@ -457,6 +457,7 @@ typedef struct {
   int64_t inc[3], nd, ndm, inc_mtr[3];
   int typ, iflow, kflu, slope;
   double gam, rgp, gam1, gam3, c1, c2, c3, c4, c5, c6, cvisq, psiroe, wig_cte, tmin_1;
+  double c50, c51, c52, c53, c54;           /* o5 (template_FluxAndBalance.for:149-154) */
   double tcx, tcy, tcz, si, sj, sk, volinv; /* 3d cartesian constants */
   const double* wig; double opt0;           /* senseur (KFLUDOM = 2) */
   int neq;                                  /* 6: Spalart-Allmaras (IFLOW = 3) */
@@ -492,6 +493,12 @@ static void fctx_init(fctx* c, const int64_t* pi, const double* pr, const double
   c->c5 = 2. * c6;
   c->c6 = -1. * c6;
   c->cvisq = 1. / 3;
+  c->c50 = 1. / 60;
+  c->c51 = 27. * c->c50;
+  c->c52 = -13. * c->c50;
+  c->c53 = -3. * c->c50;
+  c->c54 = 2. * c->c50;
+  c->c50 = 47. * c->c50;
   c->wig = NULL;
   c->opt0 = (double)pi[SENSORTYPE];
   /* SA drivers (e.g. AUSM/3dcart/fluausm_SA_o3_3dcart.for:114-127) */
@@ -526,8 +533,9 @@ static void slopes(const fctx* c, int64_t l, int d, double qm[6], double qp[6]) 
   const double* rop = c->rop;
   const int64_t inc = c->inc[d];
   int64_t nd = c->nd, nm = l - inc, nm2 = l - 2 * inc, np = l + inc;
+  int64_t nm3 = l - 3 * inc, np2 = l + 2 * inc;   /* o5: three ghost layers */
   double csc = 0.;
-  if (c->slope == 6) csc = c->wig[l + d * nd + (c->kflu == 2 ? 3 * nd : 0)];
+  if (c->slope == 6 || c->slope == 7) csc = c->wig[l + d * nd + (c->kflu == 2 ? 3 * nd : 0)];
   for (int v = 0; v < c->neq; v++) {
     if (c->typ == 3 && v == 3) { qm[v] = 0.; qp[v] = 0.; continue; }
     int64_t vs = v * nd;
@@ -538,6 +546,15 @@ static void slopes(const fctx* c, int64_t l, int d, double qm[6], double qp[6]) 
       qm[v] = c->c4 * rop[l + vs] + c->c5 * rop[nm + vs] + c->c6 * rop[np + vs];
       qp[v] = c->c4 * rop[nm + vs] + c->c6 * rop[nm2 + vs] + c->c5 * rop[l + vs];
       if (c->slope == 6) {   /* Slope/o3sc_slope_var.for:5-6 */
+        qm[v] = rop[l + vs] * (1. - csc) + qm[v] * csc;
+        qp[v] = rop[nm + vs] * (1. - csc) + qp[v] * csc;
+      }
+    } else if (c->slope == 5 || c->slope == 7) {   /* Slope/o5_slope_var.for */
+      qm[v] = c->c50 * rop[l + vs] + c->c51 * rop[nm + vs] + c->c52 * rop[np + vs] +
+              c->c53 * rop[nm2 + vs] + c->c54 * rop[np2 + vs];
+      qp[v] = c->c50 * rop[nm + vs] + c->c52 * rop[nm2 + vs] + c->c51 * rop[l + vs] +
+              c->c53 * rop[np + vs] + c->c54 * rop[nm3 + vs];
+      if (c->slope == 7) {   /* Slope/o5sc_slope_var.for */
         qm[v] = rop[l + vs] * (1. - csc) + qm[v] * csc;
         qp[v] = rop[nm + vs] * (1. - csc) + qp[v] * csc;
       }
@@ -2334,9 +2351,42 @@ void or_transfers(or_zone* zones, const or_transfer* tr, int ntr, int use_p1) {
     double* dst = use_p1 ? rz->ro_p1 : rz->ro;
     int64_t ndd = dz->param_int[NDIMDX], ndr = rz->param_int[NDIMDX];
     int64_t neq = rz->param_int[NEQ];
-    for (int64_t n = 0; n < tr[t].n; n++)
-      for (int64_t v = 0; v < neq; v++)
-        dst[tr[t].rcv_idx[n] + v * ndr] = src[tr[t].dnr_idx[n] + v * ndd];
+    if (!tr[t].types) {
+      for (int64_t n = 0; n < tr[t].n; n++)
+        for (int64_t v = 0; v < neq; v++)
+          dst[tr[t].rcv_idx[n] + v * ndr] = src[tr[t].dnr_idx[n] + v * ndd];
+      continue;
+    }
+    /* interpolation molecules: the tensor-product formulas (trilinear /
+     * bilinear weights, i fastest; separable Lagrange factors, i then j then
+     * k), summed with i fastest */
+    const int64_t si = 1, sj = dz->param_int[NIJK], sk = dz->param_int[NIJK] * dz->param_int[NIJK + 1];
+    int64_t co = 0;
+    for (int64_t n = 0; n < tr[t].n; n++) {
+      const int64_t ty = tr[t].types[n], d0 = tr[t].dnr_idx[n], r = tr[t].rcv_idx[n];
+      const double* c = tr[t].coefs + co;
+      for (int64_t v = 0; v < neq; v++) {
+        const double* f = src + v * ndd;
+        double val = 0.;
+        if (ty == 0 || ty == 1) {
+          val = c[0] * f[d0];
+        } else if (ty == 2 || ty == 22) {
+          const int nk = ty == 2 ? 2 : 1;
+          for (int kk = 0; kk < nk; kk++)
+            for (int jj = 0; jj < 2; jj++)
+              for (int ii = 0; ii < 2; ii++)
+                val += c[ii + 2 * jj + 4 * kk] * f[d0 + ii * si + jj * sj + kk * sk];
+        } else {
+          const int w = ty == 3 ? 3 : 5;
+          for (int kk = 0; kk < w; kk++)
+            for (int jj = 0; jj < w; jj++)
+              for (int ii = 0; ii < w; ii++)
+                val += c[ii] * c[w + jj] * c[2 * w + kk] * f[d0 + ii * si + jj * sj + kk * sk];
+        }
+        dst[r + v * ndr] = val;
+      }
+      co += ty <= 1 ? 1 : (ty == 2 ? 8 : (ty == 22 ? 4 : (ty == 3 ? 9 : 15)));
+    }
   }
 }
 
@@ -2516,8 +2566,8 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
         if (pi[IFLOW] == 3)
           or_spsource(pi, pr, nstep, sdm, ssiter, Z->coe, Z->ti, Z->tj, Z->tk, Z->vol,
                       Z->xmut + pi[NDIMDX], Z->drodm);
-        /* src_term.for:246-255: o3sc shock sensor on every sub-step */
-        if (pi[SLOPE] == 6)
+        /* src_term.for:246-255: o3sc / o5sc shock sensor on every sub-step */
+        if (pi[SLOPE] == 6 || pi[SLOPE] == 7)
           or_shock_sensor(pi, pr, sdm, ssiter, Z->ti, Z->tj, Z->tk, Z->vol, Z->wig);
         /* src_term.for:257-266: senseur wiggle on the first sub-step */
         if (pi[KFLUDOM] == 2 && nstep == 1) or_wiggle(pi, sdm, ssiter, Z->wig);

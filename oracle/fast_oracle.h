@@ -45,11 +45,17 @@ typedef struct {
   double* cfl;    /* CFL max, min, mean of the last verified step (3)      */
 } or_zone;
 
-/* 1-to-1 (type 0) interface copy: rcv_zone ghost cells <- dnr_zone cells. */
+/* Interface transfer: rcv_zone cells <- dnr_zone cells.  types = NULL: the
+ * 1-to-1 (type 0) copy.  Otherwise per point an interpolation type (0 / 1
+ * one donor, 2 trilinear, 22 bilinear in (i, j), 3 and 5 tensor-product
+ * Lagrange) whose molecule starts at dnr_idx, with its coefficients
+ * concatenated in coefs (1, 1, 8, 4, 9, 15 per point). */
 typedef struct {
   int64_t dnr_zone, rcv_zone, n;
   const int64_t* dnr_idx;  /* 0-based cell indices in the donor zone     */
   const int64_t* rcv_idx;  /* 0-based cell indices in the receiver zone  */
+  const int64_t* types;
+  const double* coefs;
 } or_transfer;
 
 int  or_version(void);

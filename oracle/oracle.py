@@ -47,7 +47,8 @@ class OrZone(C.Structure):
 
 class OrTransfer(C.Structure):
     _fields_ = [("dnr_zone", C.c_int64), ("rcv_zone", C.c_int64), ("n", C.c_int64),
-                ("dnr_idx", C.POINTER(C.c_int64)), ("rcv_idx", C.POINTER(C.c_int64))]
+                ("dnr_idx", C.POINTER(C.c_int64)), ("rcv_idx", C.POINTER(C.c_int64)),
+                ("types", C.POINTER(C.c_int64)), ("coefs", C.POINTER(C.c_double))]
 
 
 def load():
@@ -101,10 +102,15 @@ class Case:
                 # (navier_stokes_struct passes xmut(1+NDIMDX) as dist)
                 e["xmut"][nd:] = np.asarray(zd["dist"], dtype=np.float64).reshape(-1)
             self.z.append(e)
-        self.tr = [dict(dnr=int(t["dnr"]), rcv=int(t["rcv"]),
-                        dnr_idx=np.ascontiguousarray(t["dnr_idx"], dtype=np.int64),
-                        rcv_idx=np.ascontiguousarray(t["rcv_idx"], dtype=np.int64))
-                   for t in transfers]
+        self.tr = []
+        for t in transfers:
+            e = dict(dnr=int(t["dnr"]), rcv=int(t["rcv"]),
+                     dnr_idx=np.ascontiguousarray(t["dnr_idx"], dtype=np.int64),
+                     rcv_idx=np.ascontiguousarray(t["rcv_idx"], dtype=np.int64))
+            if "types" in t:
+                e["types"] = np.ascontiguousarray(t["types"], dtype=np.int64)
+                e["coefs"] = np.ascontiguousarray(t["coefs"], dtype=np.float64)
+            self.tr.append(e)
         self.first_it = 0
 
     def _structs(self):
@@ -119,6 +125,8 @@ class Case:
         for s, t in zip(tr, self.tr):
             s.dnr_zone, s.rcv_zone, s.n = t["dnr"], t["rcv"], t["dnr_idx"].size
             s.dnr_idx = _i(t["dnr_idx"]); s.rcv_idx = _i(t["rcv_idx"])
+            if "types" in t:
+                s.types = _i(t["types"]); s.coefs = _d(t["coefs"])
         return arr, tr
 
     def apply_bc(self, level: int = 0):

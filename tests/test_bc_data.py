@@ -15,6 +15,7 @@ import pytest
 
 from conftest import rel_err
 from fast_gb300 import cases, fasts
+from fast_gb300 import pytree as I
 
 
 def _zd(t):
@@ -150,4 +151,29 @@ def test_bc_data_refusals():
     s = Solver(0)
     with pytest.raises(FastGB300Error, match="BCOutpres"):
         s.add_zone(zd[0]["pi"], zd[0]["pr"], zd[0]["ti"], zd[0]["tj"], zd[0]["tk"], zd[0]["vol"])
+    s.close()
+
+
+def test_homogeneous_k_zone_runs_as_general_zone():
+    """A wall-stretched box is a zone homogeneous in k (nature_geom_dom.for
+    type 1); it is solved by the general 3-d kernels on its full metric."""
+    t = cases.bc_box(n=(12, 10, 6), model="NSLaminar", stretch=2.0)
+    z = I.getZones(t)[0]
+    assert fasts._zone_type(*fasts._coords(z), I.getZoneDim(z)[3]) == 1
+    zd = _zd(t)
+    assert int(zd[0]["pi"][25]) == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("temporal", ["explicit", "implicit"])
+def test_homogeneous_k_zone_gpu_parity(oracle_mod, temporal):
+    from test_gpu_parity import _check_levels, _pair
+    t = cases.bc_box(n=(14, 10, 6), model="NSLaminar", stretch=2.0, temporal=temporal,
+                     ss_iteration=3, time_step=0.02 if temporal == "explicit" else 0.05)
+    zd, ref, s = _pair(t, oracle_mod, 1)
+    nfin = 3 if temporal == "explicit" else 4
+    for it in range(1, 3):
+        ref.compute(it, 1, nfin, 1, modulo_verif=1)
+        s.compute(it, 1, nfin, 1, 1)
+    _check_levels(ref, s)
     s.close()

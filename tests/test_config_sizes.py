@@ -95,6 +95,7 @@ def test_lu_grid_cap_fp64(oracle_mod, kind, mode, cap):
     t, tc = _capped_case(kind)
     zd, ref, s = _pair(t, oracle_mod, 1, tc)
     s.set_option("lu_mode", mode)
+    s.set_option("autotune", 0)
     s.set_option("lu_grid", cap)
     for it in range(1, 3):
         ref.compute(it, 1, 4, 1, modulo_verif=1)
@@ -115,6 +116,7 @@ def test_lu_grid_cap_fp32_same_bits(oracle_mod, kind):
         zd, ref, s = _pair(t, oracle_mod, 1, tc)
         s.set_option("lu_precision", 32)
         s.set_option("lu_mode", mode)
+        s.set_option("autotune", 0)
         s.set_option("lu_grid", cap)
         for it in range(1, 3):
             s.compute(it, 1, 4, 1, 1)
@@ -149,6 +151,7 @@ def test_dataflow_wait_gives_up():
 
     s = solver()
     s.set_option("lu_mode", 2)
+    s.set_option("autotune", 0)
     s.set_option("lu_poll_limit", 4096)
     s.set_option("lu_wait_skew", 2)
     s.compute(1, 1, 3, 1, 1)
@@ -160,3 +163,28 @@ def test_dataflow_wait_gives_up():
     s.synchronize()
     assert np.all(np.isfinite(s.download(0, 0)))
     s.close()
+
+
+@pytest.mark.parametrize("kind", ["single", "grouped"])
+def test_lu_autotuned_schedule_same_bits(oracle_mod, kind):
+    """With the autotuner on (default), the first solve of each LU group
+    times the grid-barrier sweep and the dataflow sweep (one and two CTAs
+    per SM) and keeps the fastest: the results are those of the oracle and of
+    the fixed schedules, bit for bit."""
+    out = []
+    for tune in (0, 1):
+        t, tc = _capped_case(kind)
+        zd, ref, s = _pair(t, oracle_mod, 1, tc)
+        s.set_option("autotune", tune)
+        for it in range(1, 3):
+            if tune:
+                ref.compute(it, 1, 4, 1, modulo_verif=1)
+            s.compute(it, 1, 4, 1, 1)
+        s.synchronize()
+        out.append([s.download(m, 0) for m in range(len(zd))])
+        if tune:
+            for m in range(len(zd)):
+                _check_levels(ref, s, zone=m)
+        s.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)

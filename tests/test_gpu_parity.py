@@ -27,7 +27,7 @@ def _pair(t, oracle_mod, modulo_verif, tc=()):
         if "dist" in z:
             s.set_wall_distance(n, z["dist"])
     for tr in tc:
-        s.add_transfer(tr["dnr"], tr["rcv"], tr["dnr_idx"], tr["rcv_idx"])
+        s.add_any_transfer(tr)
     s.set_option("modulo_verif", modulo_verif)
     for n, z in enumerate(zd):
         for lvl, key in enumerate(("ro", "ro_m1", "ro_p1")):
@@ -160,6 +160,7 @@ def test_lu_persistent_equals_plane_launches(oracle_mod):
         t = cases.taylor_green(n=(14, 12, 10), ss_iteration=3)
         zd, ref, s = _pair(t, oracle_mod, 1)
         s.set_option("lu_mode", mode)
+        s.set_option("autotune", 0)
         for it in range(1, 3):
             s.compute(it, 1, 4, 1, 1)
         s.synchronize()
@@ -621,3 +622,27 @@ def test_cfl_statistics(oracle_mod, case):
     assert abs(got[2] - exp[2]) <= 1e-12 * exp[2]
     assert 0 < exp[1] <= exp[2] <= exp[0]
     s.close()
+
+
+@pytest.mark.parametrize("temporal", ["explicit", "implicit"])
+def test_zone_batches_equal_per_zone_launches(oracle_mod, temporal):
+    """Several zones: the per-kind zone batches (one launch of each kernel
+    over the zones of one kind, face block size from the autotuner) give the
+    bits of the per-zone launches."""
+    kw = dict(CHANNEL, temporal=temporal, ss_iteration=3,
+              time_step=0.004 if temporal == "explicit" else 0.02, modulo_verif=1)
+    out = []
+    for batch in (0, 1):
+        t, tc = cases.sa_channel(**kw)
+        zd, ref, s = _pair(t, oracle_mod, 1, tc)
+        s.set_option("batch", batch)
+        nfin = 3 if temporal == "explicit" else 4
+        for it in range(1, 3):
+            s.compute(it, 1, nfin, 1, 1)
+        s.synchronize()
+        out.append([s.download(m, lvl) for m in range(len(zd)) for lvl in range(3)])
+        if temporal == "implicit":
+            out[-1] += [s.residuals(m) for m in range(len(zd))]
+        s.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
