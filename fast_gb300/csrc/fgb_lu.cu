@@ -750,7 +750,7 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
 // do independent work in between.  The wait is
 // bounded: past 2^24 polls it sets the error word and the kernel returns;
 // the host reports FGB_ERR_DEVICE.
-struct GridBar { unsigned int* count; int* err; };
+struct GridBar { unsigned int* count; int* err; long long limit; unsigned int skew; };
 
 __device__ __forceinline__ void bar_arrive(const GridBar& g) {
   __syncthreads();
@@ -767,7 +767,7 @@ __device__ __forceinline__ bool bar_wait(const GridBar& g, unsigned int target) 
       if ((int)(cur - target) >= 0) break;
       if ((++spins & 63) == 0) {
         if (*(volatile int*)g.err) break;
-        if (spins > (1ll << 24)) { atomicExch(g.err, 1); break; }
+        if (spins > g.limit) { atomicExch(g.err, 1); break; }
       }
     }
   }
@@ -862,7 +862,7 @@ __global__ void __launch_bounds__(LuThreads<T>::n, 1)
       else load_first<TYP, T, true, NV>(p, f, plane_of(t + 1), o);
     }
     round++;
-    if (!bar_wait(gb, round * gridDim.x)) return;
+    if (!bar_wait(gb, round * gridDim.x + gb.skew)) return;
   }
 }
 
@@ -1097,7 +1097,7 @@ static cudaError_t sweep_t(const Zone& z, const LuFields& f, const PlaneData<T>&
     if (L.grid_cap > 0 && L.grid_cap < grid) grid = L.grid_cap;
     e = cudaMemsetAsync(L.bar, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
-    GridBar gb{L.bar, L.err};
+    GridBar gb{L.bar, L.err, L.flow.poll_limit << 2, (unsigned int)L.flow.wait_skew};
     Zone zz = z;
     LuFields ff = f;
     PlaneData<T> pp = p;

@@ -101,8 +101,11 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * "lu_mode": 2 (default) dataflow LU-SGS sweeps (chunks of 32 cells of a
  * hyperplane, point-to-point completion marks), 1 persistent sweeps with a
  * grid barrier per hyperplane, 0 one launch per hyperplane (same results);
- * "lu_poll_limit": polls before a dataflow wait gives up (default 2^22, then
- * fgb_synchronize reports FGB_ERR_DEVICE); "lu_wait_skew": test support, 0;
+ * "lu_poll_limit": polls before a dataflow wait gives up (default 2^22; a
+ * grid-barrier wait gives up after 4 times as many), after which
+ * fgb_synchronize reports FGB_ERR_DEVICE; "lu_wait_skew": test support, 0
+ * (raises the marks and barrier targets the waits expect, so that they run
+ * out);
  * "batch": 1 (default) to run the coefficient, Spalart-Allmaras source,
  * face and balance / update kernels of several zones as one launch per kind
  * of zone (zone type, scheme, slope, viscosity, NEQ; up to 40 zones a

@@ -128,6 +128,40 @@ def test_lu_grid_cap_fp32_same_bits(oracle_mod, kind):
             assert np.array_equal(a, b)
 
 
+def test_grid_barrier_wait_gives_up():
+    """The persistent grid-barrier sweep (lu_mode 1) with a barrier target
+    that no arrival reaches ("lu_wait_skew"): its bounded wait gives up after
+    4 x "lu_poll_limit" polls, the call reports FGB_ERR_DEVICE, every CTA
+    returns, and a fresh solver then computes normally."""
+    from fast_gb300._native import FastGB300Error, Solver
+    t = cases.taylor_green(n=(12, 10, 8), ss_iteration=2)
+    zd = fasts.zone_data(t, fasts.prepare(t))
+
+    def solver():
+        s = Solver(0)
+        s.add_zone(zd[0]["pi"], zd[0]["pr"], zd[0]["ti"], zd[0]["tj"], zd[0]["tk"], zd[0]["vol"])
+        for lvl, key in enumerate(("ro", "ro_m1", "ro_p1")):
+            s.upload(0, lvl, zd[0][key])
+        s.apply_bc(0)
+        s.apply_bc(1)
+        return s
+
+    s = solver()
+    s.set_option("lu_mode", 1)
+    s.set_option("autotune", 0)
+    s.set_option("lu_poll_limit", 4096)
+    s.set_option("lu_wait_skew", 1)
+    s.compute(1, 1, 3, 1, 1)
+    with pytest.raises(FastGB300Error, match="grid barrier"):
+        s.synchronize()
+    s.close()
+    s = solver()
+    s.compute(1, 1, 3, 1, 1)
+    s.synchronize()
+    assert np.all(np.isfinite(s.download(0, 0)))
+    s.close()
+
+
 def test_dataflow_wait_gives_up():
     """A dependency wait of the dataflow sweep whose mark nothing publishes
     ("lu_wait_skew" raises the marks the waits expect) gives up after
