@@ -44,6 +44,15 @@ ALG_BYTES = {"residual": 160.0, "lu_sgs": 320.0}
 # and read by both sweeps, so the traffic scales with the cell count.
 # residual = three face_flux launches (1.01 GB) + assemble (1.03 GB).
 DRAM_BYTES = {"residual": 497.0, "lu_sgs": 1702.0}
+# FP64 arithmetic instructions per cell and launch group (thread level,
+# DADD + DMUL + DFMA counted by ncu, `smsp__sass_thread_inst_executed_op_d*`,
+# 160^3, first sub-iteration): residual = face_flux i + j + k (205 + 205 + 216)
+# + assemble (80); LU-SGS = lu_gather (87) + lower and upper sweep (297) +
+# lu_newton (35).  The in-place sweeps of later sub-iterations also rebuild
+# the k+1 entries and do the Newton update, so for LU-SGS this is a floor.
+# A DADD or DMUL issues at the DFMA rate, so the instruction peak is half the
+# measured FP64 FMA FLOP rate.
+FP64_INST = {"residual": 507.0, "lu_sgs": 419.0}
 
 
 def parse():
@@ -355,6 +364,14 @@ def run_ours(args, d: Dist):
         "peak_source": peak_kind,
         "avg_launch_ms": avg_ms,
         "fp64_fma_peak_gflops_measured": fp64,
+        "fp64_issue": {
+            "unit": "G FP64 instructions/s (DADD + DMUL + DFMA, thread level)",
+            "peak": fp64 / 2.0,
+            "inst_per_cell": FP64_INST,
+            "achieved": {g: FP64_INST[g] * cells / (gt[g][1] / gt[g][0] * 1e-3) / 1e9 for g in gt},
+            "frac": {g: FP64_INST[g] * cells / (gt[g][1] / gt[g][0] * 1e-3) / 1e9 / (fp64 / 2.0)
+                     for g in gt},
+        } if args.lu_precision == 64 else None,
         "kernel_share": {k: round(v[1] / total_prof, 4) for k, v in stats.items()},
     }
 
