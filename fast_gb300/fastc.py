@@ -171,10 +171,20 @@ def _buildOwnData(t):
     rk = int(base.get("rk", 3))
     if temporal in ("implicit", "implicit_local"):
         rk = 3
+    # time level of every zone (PyTree.py:1080-1110): with explicit_local the
+    # value of centers:niveaux_temps in the zone's middle cell, otherwise
+    # .Solver#define/niveaux_temps (default 1)
+    veclevel = [_time_level(z, temporal) for z in I.getZones(t)]
+    maxlevel = max(veclevel)
+    exploc = 0
     if temporal == "explicit":
         nssiter = {1: 1, 2: 2, 3: 3}[rk]
     elif temporal in ("implicit", "implicit_local"):
         nssiter = int(base["ss_iteration"]) + 1
+    elif temporal == "explicit_local":   # PyTree.py:1163-1166: RK3, 4 sub-steps per level
+        nssiter = 4 * maxlevel
+        rk = 3
+        exploc = 1
     else:
         raise NotImplementedError(f"temporal_scheme {temporal} is not supported")
     o = I.createUniqueChild(t, ".Solver#ownData", "UserDefinedData_t")
@@ -182,6 +192,7 @@ def _buildOwnData(t):
     dtloc[0] = nssiter
     dtloc[1] = int(base["modulo_verif"])
     dtloc[6] = rk
+    dtloc[9] = maxlevel
     I.createUniqueChild(o, ".Solver#dtloc", "DataArray_t", dtloc)
     for ndom, (b, z) in enumerate((b, z) for b in I.getBases(t) for z in I.getZones(b)):
         _, zn = _zone_numerics(t, b, z)
@@ -193,7 +204,7 @@ def _buildOwnData(t):
                  "nsles": 2, "NSTurbulent": 3, "nsspalart": 3}.get(model)
         if iflow is None:
             raise ValueError(f"Fast: model {model} is invalid.")
-        itypcp = 2 if temporal == "explicit" else 1
+        itypcp = 2 if temporal in ("explicit", "explicit_local") else 1
         slope = zn["slope"]
         # "vanalbada" (8) is not a FastS slope: a smooth limiter for the adjoint
         islope = {"o1": 1, "o2": 4, "o3": 2, "o5": 5, "minmod": 3, "o3sc": 6, "o5sc": 7,
@@ -230,8 +241,8 @@ def _buildOwnData(t):
         pi[DTLOC] = dtl
         pi[47:52] = [0, 1, 2, 0, 0]
         pi[RK] = rk
-        pi[LEVEL] = 1
-        pi[EXPLOC] = 0
+        pi[LEVEL] = veclevel[ndom]
+        pi[EXPLOC] = exploc
         pi[55] = 0
         pi[56] = 1
         pi[57] = 0
@@ -307,6 +318,22 @@ def _buildOwnData(t):
         I.createUniqueChild(o, "model", "DataArray_t", model)
         I.createUniqueChild(o, "temporal_scheme", "DataArray_t", temporal)
     return None
+
+
+def _time_level(z, temporal):
+    """PyTree.py:1087-1100: the zone's time level.  explicit_local: the cell
+    value at the 1-based (i, j, k) = (vertex count // 2) of each direction,
+    i.e. the 0-based cell (cells + 1) // 2 - 1."""
+    if temporal == "explicit_local":
+        sol = I.getNodeFromName1(z, I.__FlowSolutionCenters__)
+        lv = I.getNodeFromName1(sol, "niveaux_temps") if sol is not None else None
+        if lv is None:
+            raise ValueError("explicit_local: zone %s has no centers:niveaux_temps" % z[0])
+        a = np.asarray(lv[1])
+        return int(a[tuple((n + 1) // 2 - 1 for n in a.shape)])
+    d = I.getNodeFromName1(z, ".Solver#define")
+    a = I.getNodeFromName1(d, "niveaux_temps") if d is not None else None
+    return int(I.getValue(a)) if a is not None else 1
 
 
 def getRange(in_bc, pi):

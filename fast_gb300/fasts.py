@@ -254,6 +254,15 @@ def warmup(t, tc=None, graph=None, infos_ale=None, Adjoint=False, tmy=None, list
     zones = I.getZones(t)
     dtloc = I.getNodeFromName1(I.getNodeFromName1(t, ".Solver#ownData"), ".Solver#dtloc")[1]
     nssiter = int(dtloc[0])
+    if _temporal_scheme(t) == "explicit_local":
+        # FastS prepares an explicit_local tree, but its C layer -- the one
+        # this solver replaces -- refuses to compute it (PyTree.py:75-76);
+        # only its Python layer, through Cassiopee's Connector transfers,
+        # runs it.  No GPU solver is built; _compute raises FastS's error.
+        FIRST_IT = PREPARED_FIRST_IT
+        HOOK = {"solver": None, "nssiter": nssiter, "FIRST_IT": FIRST_IT,
+                "gpu_resident": bool(gpu_resident), "zones": zones, "device_valid": False}
+        return t, tc, metrics
     solver = Solver(device)
     for n, zd in enumerate(zone_data(t, metrics)):
         solver.add_zone(zd["pi"], zd["pr"], zd["ti"], zd["tj"], zd["tk"], zd["vol"])
@@ -295,6 +304,13 @@ def _download(t):
             s.download(n, lvl, FastC.compactArray(z, suf).reshape(-1))
 
 
+def _temporal_scheme(t):
+    """.Solver#define/temporal_scheme of the tree (FastS's default: implicit)."""
+    d = I.getNodeFromName1(t, ".Solver#define")
+    a = I.getNodeFromName1(d, "temporal_scheme") if d is not None else None
+    return I.getValue(a) if a is not None else "implicit"
+
+
 def _itypcp(z):
     o = I.getNodeFromName1(z, ".Solver#ownData")
     return int(I.getNodeFromName1(o, "Parameter_int")[1][FastC.ITYPCP])
@@ -311,6 +327,8 @@ def _compute(t, metrics, nitrun, tc=None, graph=None, tc2=None, graph2=None, lay
     sub-steps through fasts._computePT -> fgb_compute, then the time-level
     rotation (done on the device; the tree arrays receive the new levels)."""
     global FIRST_IT
+    if _temporal_scheme(t) == "explicit_local" and layer == "c":   # PyTree.py:73-76
+        raise ValueError("compute: 'explicit_local' & 'c layer' is not implemented.")
     if HOOK is None:
         raise RuntimeError("warmup must be called before _compute")
     if layer != "c":
