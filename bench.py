@@ -95,6 +95,8 @@ def parse():
                    help="tgv workload: MUSCL slope of the AUSM+(P) faces (o3sc adds the shock sensor)")
     p.add_argument("--lu-mode", type=int, default=2, choices=[0, 1, 2],
                    help="LU-SGS schedule: 2 dataflow (default), 1 grid barrier, 0 plane launches")
+    p.add_argument("--lu-prefetch", type=int, default=1, choices=[0, 1],
+                   help="dataflow LU-SGS sweep: L2 prefetch of each chunk's operands")
     p.add_argument("--lu-grid", type=int, default=0,
                    help="LU-SGS sweep CTAs (0: every resident slot)")
     p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
@@ -288,6 +290,7 @@ def run_ours(args, d: Dist):
     s.set_option("lu_precision", args.lu_precision)
     s.set_option("lu_mode", args.lu_mode)
     s.set_option("lu_grid", args.lu_grid)
+    s.set_option("lu_prefetch", args.lu_prefetch)
     it = 1
     for _ in range(args.warmup):
         fasts._compute(t, metrics, it)
@@ -466,6 +469,7 @@ def run_multizone(args):
     s.set_option("lu_precision", args.lu_precision)
     s.set_option("lu_mode", args.lu_mode)
     s.set_option("lu_grid", args.lu_grid)
+    s.set_option("lu_prefetch", args.lu_prefetch)
     cells = sum(int(np.prod(z[1][:, 0] - 1 - 4)) for z in fasts.HOOK["zones"])
     it = 1
     for _ in range(args.warmup):

@@ -190,6 +190,7 @@ struct fgb_solver {
                                    // 0 one launch per plane
   long long poll_limit = 1ll << 22;  // polls before a dataflow wait gives up
   int wait_skew = 0;               // test support: added to the marks the dataflow waits expect
+  int lu_prefetch = 1;             // dataflow sweep: L2 prefetch of each chunk's operands
   bool batch = true;               // several zones: per-kind zone batches instead of per-zone launches
   bool autotune = true;            // batched faces: block size from timed trials
   int lu_grid = 0;                 // > 0: at most this many CTAs in the persistent sweep
@@ -938,6 +939,9 @@ int fgb_set_option(fgb_solver* s, const char* key, double value) {
   } else if (k == "lu_wait_skew") {
     if (value < 0 || value > 2) return fail(FGB_ERR_ARG, "lu_wait_skew must be 0, 1 or 2");
     s->wait_skew = (int)value;
+  } else if (k == "lu_prefetch") {
+    if (value != 0 && value != 1) return fail(FGB_ERR_ARG, "lu_prefetch must be 0 or 1");
+    s->lu_prefetch = (int)value;
   } else if (k == "lu_poll_limit") {
     if (value < 64 || value > 1e12) return fail(FGB_ERR_ARG, "lu_poll_limit must be in [64, 1e12]");
     s->poll_limit = (long long)value;
@@ -974,6 +978,7 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value) {
   else if (k == "lu_grid") *value = s->lu_grid;
   else if (k == "lu_poll_limit") *value = (double)s->poll_limit;
   else if (k == "lu_wait_skew") *value = s->wait_skew;
+  else if (k == "lu_prefetch") *value = s->lu_prefetch;
   else if (k == "batch") *value = s->batch;
   else if (k == "lu_tuned") {   // first LU group, FP64 sweeps: 10 x lu_mode + CTAs per SM (-1: not tuned)
     *value = (s->lu_groups.empty() || s->lu_groups[0].tuned_mode[0] < 0)
@@ -1607,6 +1612,7 @@ static LuGroup group_launch(fgb_solver* s, LuGroupData& g, LuZone* tab) {
   F.wait_skew = s->wait_skew;
   F.err = s->derr;
   F.poll_limit = s->poll_limit;
+  F.prefetch = s->lu_prefetch;
   return L;
 }
 

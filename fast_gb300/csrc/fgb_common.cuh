@@ -93,6 +93,36 @@ __device__ __forceinline__ double fmaxF(double a, double b) { return a > b ? a :
 __device__ __forceinline__ double fminF(double a, double b) { return a < b ? a : b; }
 __device__ __forceinline__ double fsignF(double a, double b) { return copysign(fabs(a), b); }
 
+// x * (+-2^K) with the bits of the FP64 product, without an FP64 instruction
+// in the common case.  GB300 issues one FP64 warp instruction per 64 cycles
+// per SM sub-partition, so the FP64-bound kernels take products by powers
+// of two off that pipe: when x and the product are normal numbers the
+// product is x with its exponent field moved by K (exact, and so equal to
+// the rounded product), an integer add on the integer pipe; zero, subnormal,
+// infinite or NaN x, or a product leaving the normal range, take the FP64
+// multiply in an out-of-line call (a real branch: an inlined multiply would
+// be predicated and still occupy the FP64 pipe).
+static __device__ __noinline__ double mul_pow2_slow(double x, double f) { return x * f; }
+template <int K, bool NEG = false>
+__device__ __forceinline__ double mul_pow2(double x) {
+  static_assert(K >= -4 && K <= 4 && K != 0, "small power of two");
+  constexpr unsigned lo = K < 0 ? 1u - K : 1u, hi = K > 0 ? 2046u - K : 2046u;
+  const long long b = __double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e - lo <= hi - lo) {
+    long long r = K > 0 ? b + ((long long)K << 52) : b - ((long long)(-K) << 52);
+    if (NEG) r ^= (long long)0x8000000000000000ull;
+    return __longlong_as_double(r);
+  }
+  const double f = K < 0 ? 1.0 / (double)(1 << -K) : (double)(1 << K);
+  return mul_pow2_slow(x, NEG ? -f : f);
+}
+template <int K, bool NEG = false>
+__device__ __forceinline__ float mul_pow2(float x) {   // FP32: the multiply itself
+  const float f = K < 0 ? 1.0f / (float)(1 << -K) : (float)(1 << K);
+  return x * (NEG ? -f : f);
+}
+
 // Device error word shared by all kernels of a solver (bounded waits set it).
 struct DevStatus { int code; int where; };
 

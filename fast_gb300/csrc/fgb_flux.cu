@@ -37,8 +37,8 @@ template <int SL>
 __device__ __forceinline__ void reconstruct(const Zone& z, double a, double b, double c, double d,
                                             double roff, double& qm, double& qp) {
   if (SL == VANALBADA) {
-    qm = c - 0.5 * vanalbada(c - b, d - c);
-    qp = b + 0.5 * vanalbada(b - a, c - b);
+    qm = c - mul_pow2<-1>(vanalbada(c - b, d - c));
+    qp = b + mul_pow2<-1>(vanalbada(b - a, c - b));
   } else if (SL == O1) {
     qm = c;
     qp = b;
@@ -71,10 +71,10 @@ __device__ __forceinline__ void roe_cart(const Zone& z, const double qm[5], cons
   const double rgp = z.rgp, gam1 = z.gam1;
   double r1 = qp[0];
   double p1 = r1 * qp[4] * rgp;
-  double h1 = gam1 * qp[4] * rgp + .5 * (qp[1] * qp[1] + qp[2] * qp[2] + qp[3] * qp[3]);
+  double h1 = gam1 * qp[4] * rgp + mul_pow2<-1>(qp[1] * qp[1] + qp[2] * qp[2] + qp[3] * qp[3]);
   double r2 = qm[0];
   double p2 = r2 * qm[4] * rgp;
-  double h2 = gam1 * qm[4] * rgp + .5 * (qm[1] * qm[1] + qm[2] * qm[2] + qm[3] * qm[3]);
+  double h2 = gam1 * qm[4] * rgp + mul_pow2<-1>(qm[1] * qm[1] + qm[2] * qm[2] + qm[3] * qm[3]);
   double s1 = sqrt(r1), s2 = sqrt(r2);
   double r = s1 * s2;
   double r_1 = 1. / (s1 + s2);
@@ -82,7 +82,7 @@ __device__ __forceinline__ void roe_cart(const Zone& z, const double qm[5], cons
 #pragma unroll
   for (int m = 0; m < 3; m++) vel[m] = (s1 * qp[m + 1] + s2 * qm[m + 1]) * r_1;
   double h = (s1 * h1 + s2 * h2) * r_1;
-  double q = .5 * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+  double q = mul_pow2<-1>(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
   double c = sqrt((z.gam - 1.) * fabs(h - q));
   double qn1 = qp[D + 1] * tc, qn2 = qm[D + 1] * tc;
 #pragma unroll
@@ -94,7 +94,7 @@ __device__ __forceinline__ void roe_cart(const Zone& z, const double qm[5], cons
   double f1 = qn;
   double f4 = z.psiroe * (fabs(f1) + c);
   double f2 = .5 + fsignF(.5, fabs(f1) - f4);
-  double f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  double f3 = mul_pow2<-1>((f2 - 1.) * (f1 * f1 / f4 + f4)) - f2 * fabs(f1);
   f1 = (r2 - r1 - dp / (c * c)) * s;
   double fl[5];
   fl[0] = f3 * (f1);
@@ -106,8 +106,8 @@ __device__ __forceinline__ void roe_cart(const Zone& z, const double qm[5], cons
   // lambda4 = qn + c
   f1 = qn + c;
   f2 = .5 + fsignF(.5, fabs(f1) - f4);
-  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
-  f1 = (dp + r * c * dqn * s_1) / (2. * c * c) * s * f3;
+  f3 = mul_pow2<-1>((f2 - 1.) * (f1 * f1 / f4 + f4)) - f2 * fabs(f1);
+  f1 = (dp + r * c * dqn * s_1) / (mul_pow2<1>(c) * c) * s * f3;
   fl[0] = fl[0] + f1;
 #pragma unroll
   for (int m = 0; m < 3; m++) fl[m + 1] = fl[m + 1] + f1 * ((m == D) ? (vel[m] + nn * c) : vel[m]);
@@ -115,19 +115,19 @@ __device__ __forceinline__ void roe_cart(const Zone& z, const double qm[5], cons
   // lambda5 = qn - c
   f1 = qn - c;
   f2 = .5 + fsignF(.5, fabs(f1) - f4);
-  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
-  f1 = (dp - r * c * dqn * s_1) / (2. * c * c) * f3 * s;
+  f3 = mul_pow2<-1>((f2 - 1.) * (f1 * f1 / f4 + f4)) - f2 * fabs(f1);
+  f1 = (dp - r * c * dqn * s_1) / (mul_pow2<1>(c) * c) * f3 * s;
   fl[0] = fl[0] + f1;
 #pragma unroll
   for (int m = 0; m < 3; m++) fl[m + 1] = fl[m + 1] + f1 * ((m == D) ? (vel[m] - nn * c) : vel[m]);
   fl[4] = fl[4] + f1 * (h - qn * c);
   double rou1 = r1 * qn1, rou2 = r2 * qn2, p1p2 = p1 + p2;
-  F[0] = (fl[0] + rou1 + rou2) * 0.5;
+  F[0] = mul_pow2<-1>(fl[0] + rou1 + rou2);
 #pragma unroll
   for (int m = 0; m < 3; m++)
-    F[m + 1] = (m == D) ? (fl[m + 1] + rou1 * qp[m + 1] + rou2 * qm[m + 1] + tc * p1p2) * 0.5
-                        : (fl[m + 1] + rou1 * qp[m + 1] + rou2 * qm[m + 1]) * 0.5;
-  F[4] = (fl[4] + rou1 * h1 + rou2 * h2) * 0.5;
+    F[m + 1] = (m == D) ? mul_pow2<-1>(fl[m + 1] + rou1 * qp[m + 1] + rou2 * qm[m + 1] + tc * p1p2)
+                        : mul_pow2<-1>(fl[m + 1] + rou1 * qp[m + 1] + rou2 * qm[m + 1]);
+  F[4] = mul_pow2<-1>(fl[4] + rou1 * h1 + rou2 * h2);
 }
 
 // ----------------------------------------------------------- Roe (general)
@@ -141,16 +141,16 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
                                          double* tp = nullptr, int64_t ts = 0) {
   const double rgp = z.rgp, gam1 = z.gam1;
   double r1 = qp[0], p1 = r1 * qp[4] * rgp;
-  double h1 = gam1 * qp[4] * rgp + .5 * (qp[1] * qp[1] + qp[2] * qp[2] + qp[3] * qp[3]);
+  double h1 = gam1 * qp[4] * rgp + mul_pow2<-1>(qp[1] * qp[1] + qp[2] * qp[2] + qp[3] * qp[3]);
   double r2 = qm[0], p2 = r2 * qm[4] * rgp;
-  double h2 = gam1 * qm[4] * rgp + .5 * (qm[1] * qm[1] + qm[2] * qm[2] + qm[3] * qm[3]);
+  double h2 = gam1 * qm[4] * rgp + mul_pow2<-1>(qm[1] * qm[1] + qm[2] * qm[2] + qm[3] * qm[3]);
   double s1 = sqrt(r1), s2 = sqrt(r2);
   double r = s1 * s2, r_1 = 1. / (s1 + s2);
   double u = (s1 * qp[1] + s2 * qm[1]) * r_1;
   double v = (s1 * qp[2] + s2 * qm[2]) * r_1;
   double w = (s1 * qp[3] + s2 * qm[3]) * r_1;
   double h = (s1 * h1 + s2 * h2) * r_1;
-  double q = .5 * (u * u + v * v + w * w);
+  double q = mul_pow2<-1>(u * u + v * v + w * w);
   double c = sqrt((z.gam - 1.) * fabs(h - q));
   double qn1 = qp[1] * tcx + qp[2] * tcy + qp[3] * tcz;
   double qn2 = qm[1] * tcx + qm[2] * tcy + qm[3] * tcz;
@@ -166,7 +166,7 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
     tp[6 * ts] = 1. / f4; tp[7 * ts] = 1. / (c * c); tp[8 * ts] = 1. / r;
   }
   double f2 = 0.5 + fsignF(0.5, fabs(f1) - f4);
-  double f3 = (f2 - 1.0) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
+  double f3 = mul_pow2<-1>((f2 - 1.0) * (f1 * f1 / f4 + f4)) - f2 * fabs(f1);
   f1 = (r2 - r1 - dp / (c * c)) * s;
   double fl1 = f3 * (f1);
   double fl2 = f3 * (f1 * u + r * (du - nx * dqn));
@@ -175,8 +175,8 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
   double fl5 = f3 * (f1 * q + r * (u * du + v * dv + w * dw - qn * dqn));
   f1 = qn + c;
   f2 = 0.5 + fsignF(0.5, fabs(f1) - f4);
-  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
-  f1 = (dp + r * c * dqn * s_1) / (2. * c * c) * s * f3;
+  f3 = mul_pow2<-1>((f2 - 1.) * (f1 * f1 / f4 + f4)) - f2 * fabs(f1);
+  f1 = (dp + r * c * dqn * s_1) / (mul_pow2<1>(c) * c) * s * f3;
   fl1 = fl1 + f1;
   fl2 = fl2 + f1 * (u + nx * c);
   fl3 = fl3 + f1 * (v + ny * c);
@@ -184,19 +184,19 @@ __device__ __forceinline__ void roe_full(const Zone& z, const double qm[5], cons
   fl5 = fl5 + f1 * (h + qn * c);
   f1 = qn - c;
   f2 = 0.5 + fsignF(0.5, fabs(f1) - f4);
-  f3 = (f2 - 1.) * (f1 * f1 / f4 + f4) * 0.5 - f2 * fabs(f1);
-  f1 = (dp - r * c * dqn * s_1) / (2. * c * c) * f3 * s;
+  f3 = mul_pow2<-1>((f2 - 1.) * (f1 * f1 / f4 + f4)) - f2 * fabs(f1);
+  f1 = (dp - r * c * dqn * s_1) / (mul_pow2<1>(c) * c) * f3 * s;
   fl1 = fl1 + f1;
   fl2 = fl2 + f1 * (u - nx * c);
   fl3 = fl3 + f1 * (v - ny * c);
   fl4 = fl4 + f1 * (w - nz * c);
   fl5 = fl5 + f1 * (h - qn * c);
   double rou1 = r1 * qn1, rou2 = r2 * qn2, p1p2 = p1 + p2;
-  F[0] = (fl1 + rou1 + rou2) * 0.5;
-  F[1] = (fl2 + rou1 * qp[1] + rou2 * qm[1] + tcx * p1p2) * 0.5;
-  F[2] = (fl3 + rou1 * qp[2] + rou2 * qm[2] + tcy * p1p2) * 0.5;
-  F[3] = (fl4 + rou1 * qp[3] + rou2 * qm[3] + tcz * p1p2) * 0.5;
-  F[4] = (fl5 + rou1 * h1 + rou2 * h2) * 0.5;
+  F[0] = mul_pow2<-1>(fl1 + rou1 + rou2);
+  F[1] = mul_pow2<-1>(fl2 + rou1 * qp[1] + rou2 * qm[1] + tcx * p1p2);
+  F[2] = mul_pow2<-1>(fl3 + rou1 * qp[2] + rou2 * qm[2] + tcy * p1p2);
+  F[3] = mul_pow2<-1>(fl4 + rou1 * qp[3] + rou2 * qm[3] + tcz * p1p2);
+  F[4] = mul_pow2<-1>(fl5 + rou1 * h1 + rou2 * h2);
 }
 
 // ---------------------------------------------------------- Roe (SA row)
@@ -224,7 +224,7 @@ __device__ __forceinline__ double roe_sa_flux(const Zone& z, const double* __res
   qn1 = CART ? qp[D] * t[D] : (TWO_D ? qp[0] * tcx + qp[1] * tcy : qp[0] * tcx + qp[1] * tcy + qp[2] * tcz);
   const double s_1 = 1.0 / fmaxF(s, 1.E-30);
   const double tdu = fmaxF(z.c1 / s_1, fabs(qn1));
-  return 0.5 * (qm6 + qp6 - tdu * (q[l + 5 * nd] * q[l] - q[nm + 5 * nd] * q[nm]));
+  return mul_pow2<-1>(qm6 + qp6 - tdu * (q[l + 5 * nd] * q[l] - q[nm + 5 * nd] * q[nm]));
 }
 
 // ------------------------------------------------------------- AUSM+(P)
@@ -240,10 +240,10 @@ __device__ __forceinline__ void ausm_face(const Zone& z, const double qm[NV], co
   const double rgp = z.rgp, gam1 = z.gam1;
   double r1 = qp[0], rou1 = r1 * qp[1], rov1 = r1 * qp[2], row1 = r1 * qp[3];
   double p1 = r1 * qp[4] * rgp;
-  double h1 = gam1 * p1 + .5 * (rou1 * qp[1] + rov1 * qp[2] + row1 * qp[3]);
+  double h1 = gam1 * p1 + mul_pow2<-1>(rou1 * qp[1] + rov1 * qp[2] + row1 * qp[3]);
   double r2 = qm[0], rou2 = r2 * qm[1], rov2 = r2 * qm[2], row2 = r2 * qm[3];
   double p2 = r2 * qm[4] * rgp;
-  double h2 = gam1 * p2 + .5 * (rou2 * qm[1] + rov2 * qm[2] + row2 * qm[3]);
+  double h2 = gam1 * p2 + mul_pow2<-1>(rou2 * qm[1] + rov2 * qm[2] + row2 * qm[3]);
   double qn1, qn2;
   if (CART) {
     const double tc = D == 0 ? tcx : (D == 1 ? tcy : tcz);
@@ -255,17 +255,17 @@ __device__ __forceinline__ void ausm_face(const Zone& z, const double qm[NV], co
   }
   double u, tdu;
   if (SENS) {  // SENSOR/fluFaceEuler.for: Rhie-Chow term and dissipation switched by wig
-    u = 0.25 * (qn1 + qn2) - z.c2 * s * (p2 - p1) * (z.opt0 * wg + 1. - z.opt0);
+    u = mul_pow2<-2>(qn1 + qn2) - z.c2 * s * (p2 - p1) * (z.opt0 * wg + 1. - z.opt0);
     tdu = fmaxF(fabs(u), z.c1 * s) * wg;
   } else {
     double cc = rgp * z.gam * tl;  // c^2 from the temperature of cell l
     double son = sqrt(qn1 * qn1 / cc);
     double tam = z.c3 * son + s;
     double tam1 = fmaxF(0., tam) * z.c2;
-    u = 0.25 * (qn1 + qn2) - tam1 * (p2 - p1);
+    u = mul_pow2<-2>(qn1 + qn2) - tam1 * (p2 - p1);
     tdu = fmaxF(fabs(u), z.c1 * s) * z.wig_cte;
   }
-  double p1p2 = (p1 + p2) * 0.5;
+  double p1p2 = mul_pow2<-1>(p1 + p2);
   F[0] = u * (r1 + r2) - tdu * (r2 - r1);
   F[1] = u * (rou1 + rou2) - tdu * (rou2 - rou1);
   F[2] = u * (rov1 + rov2) - tdu * (rov2 - rov1);
@@ -331,7 +331,7 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
   const int64_t il = l - inD, ir = l;
   double fv, fv5;
   if (D == 0) {
-    const double tix = tcx, tjy = .25 * tcy, tkz = .25 * tcz;
+    const double tix = tcx, tjy = mul_pow2<-2>(tcy), tkz = mul_pow2<-2>(tcz);
     double f1 = U[il], f2 = U[ir], s = f1 + f2;
     double f3 = s + U[l - ii - ij] + U[l - ij];
     double f4 = s + U[l - ii + ij] + U[l + ij];
@@ -351,7 +351,7 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     double e1 = gUx - div, e2 = gUy + gVx, e3 = gUz + gWx;
     double xmutvol, xktvol, xsa;
     mut_face<NV>(z, q, xmut, il, ir, z.volinv, xmutvol, xktvol, xsa);
-    fv = -(2. * e1 * tcx) * xmutvol;
+    fv = -(mul_pow2<1>(e1) * tcx) * xmutvol;
     fv5 = fv * (U[ir] + U[il]);
     F[1] = F[1] + fv;
     fv = -(e2 * tcx) * xmutvol;
@@ -360,14 +360,14 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     fv = -(e3 * tcx) * xmutvol;
     fv5 = fv5 + fv * (W[ir] + W[il]);
     F[3] = F[3] + fv;
-    fv = fv5 * 0.5 - (gTx * tcx) * xktvol;
+    fv = mul_pow2<-1>(fv5) - (gTx * tcx) * xktvol;
     F[4] = F[4] + fv;
     if (NV == 6) {
       const double gn = (q[ir + 5 * nd] - q[il + 5 * nd]) * tix;
       F[NV - 1] = F[NV - 1] - xsa * gn * tcx;
     }
   } else if (D == 1) {
-    const double tiy = tcy, tjz = .25 * tcz, tkx = .25 * tcx;
+    const double tiy = tcy, tjz = mul_pow2<-2>(tcz), tkx = mul_pow2<-2>(tcx);
     double f1 = U[il], f2 = U[ir], s = f1 + f2;
     double f5 = s + U[l - ii - ij] + U[l - ii];
     double f6 = s + U[l + ii - ij] + U[l + ii];
@@ -390,20 +390,20 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     fv = -(e2 * tcy) * xmutvol;
     fv5 = fv * (U[ir] + U[il]);
     F[1] = F[1] + fv;
-    fv = -(2. * e4 * tcy) * xmutvol;
+    fv = -(mul_pow2<1>(e4) * tcy) * xmutvol;
     fv5 = fv5 + fv * (V[ir] + V[il]);
     F[2] = F[2] + fv;
     fv = -(e5 * tcy) * xmutvol;
     fv5 = fv5 + fv * (W[ir] + W[il]);
     F[3] = F[3] + fv;
-    fv = fv5 * 0.5 - (gTy * tcy) * xktvol;
+    fv = mul_pow2<-1>(fv5) - (gTy * tcy) * xktvol;
     F[4] = F[4] + fv;
     if (NV == 6) {
       const double gn = (q[ir + 5 * nd] - q[il + 5 * nd]) * tiy;
       F[NV - 1] = F[NV - 1] - xsa * (gn * tcy);
     }
   } else {
-    const double tiz = tcz, tky = 0.25 * tcy, tjx = 0.25 * tcx;
+    const double tiz = tcz, tky = mul_pow2<-2>(tcy), tjx = mul_pow2<-2>(tcx);
     double f1 = U[il], f2 = U[ir], s = f1 + f2;
     double f3 = s + U[l - ii - ik] + U[l - ii];
     double f4 = s + U[l + ii - ik] + U[l + ii];
@@ -429,10 +429,10 @@ __device__ __forceinline__ void visc_cart(const Zone& z, const double* __restric
     fv = -e5 * tcz * xmutvol;
     fv5 = fv5 + fv * (V[ir] + V[il]);
     F[2] = F[2] + fv;
-    fv = -2. * e6 * tcz * xmutvol;
+    fv = mul_pow2<1, true>(e6) * tcz * xmutvol;
     fv5 = fv5 + fv * (W[ir] + W[il]);
     F[3] = F[3] + fv;
-    fv = fv5 * 0.5 - gTz * tcz * xktvol;
+    fv = mul_pow2<-1>(fv5) - gTz * tcz * xktvol;
     F[4] = F[4] + fv;
     if (NV == 6) {
       const double gn = (q[ir + 5 * nd] - q[il + 5 * nd]) * tiz;
@@ -464,8 +464,8 @@ __device__ __forceinline__ void visc_full(const Zone& z, const double* __restric
 #pragma unroll
   for (int m = 0; m < 3; m++) {
     const int64_t o = m * ndm;
-    t0[m] = .5 * (TD[lt + o] + TD[ltm + o]);
-    t1[m] = .5 * (TD[lt + o] + TD[ltp + o]);
+    t0[m] = mul_pow2<-1>(TD[lt + o] + TD[ltm + o]);
+    t1[m] = mul_pow2<-1>(TD[lt + o] + TD[ltp + o]);
     ta0[m] = .125 * (TA[lt + o] + TA[ltm + o]);
     ta1[m] = .125 * (TA[ltA + o] + TA[ltAm + o]);
     tb0[m] = .125 * (TB[lt + o] + TB[ltm + o]);
@@ -493,16 +493,16 @@ __device__ __forceinline__ void visc_full(const Zone& z, const double* __restric
   double xmutvol, xktvol, xsa;
   mut_face<NV>(z, q, xmut, il, ir, volinv, xmutvol, xktvol, xsa);
   double fv, fv5;
-  fv = -(2. * e1 * tcx + e2 * tcy + e3 * tcz) * xmutvol;
+  fv = -(mul_pow2<1>(e1) * tcx + e2 * tcy + e3 * tcz) * xmutvol;
   fv5 = fv * (q[ir + nd] + q[il + nd]);
   F[1] = F[1] + fv;
-  fv = -(e2 * tcx + 2. * e4 * tcy + e5 * tcz) * xmutvol;
+  fv = -(e2 * tcx + mul_pow2<1>(e4) * tcy + e5 * tcz) * xmutvol;
   fv5 = fv5 + fv * (q[ir + 2 * nd] + q[il + 2 * nd]);
   F[2] = F[2] + fv;
-  fv = -(e3 * tcx + e5 * tcy + 2. * e6 * tcz) * xmutvol;
+  fv = -(e3 * tcx + e5 * tcy + mul_pow2<1>(e6) * tcz) * xmutvol;
   fv5 = fv5 + fv * (q[ir + 3 * nd] + q[il + 3 * nd]);
   F[3] = F[3] + fv;
-  fv = fv5 * 0.5 - (g[3][0] * tcx + g[3][1] * tcy + g[3][2] * tcz) * xktvol;
+  fv = mul_pow2<-1>(fv5) - (g[3][0] * tcx + g[3][1] * tcy + g[3][2] * tcz) * xktvol;
   F[4] = F[4] + fv;
   if (NV == 6)   // SA/assemble_tauij_3dfull.for
     F[NV - 1] = F[NV - 1] - xsa * (g[NG - 1][0] * tcx + g[NG - 1][1] * tcy + g[NG - 1][2] * tcz);
@@ -526,8 +526,8 @@ __device__ __forceinline__ void visc_2d(const Zone& z, const double* __restrict_
 #pragma unroll
   for (int m = 0; m < 2; m++) {
     const int64_t o = m * ndm;
-    t0[m] = .5 * (TD[lt + o] + TD[ltm + o]);
-    t1[m] = .5 * (TD[lt + o] + TD[ltp + o]);
+    t0[m] = mul_pow2<-1>(TD[lt + o] + TD[ltm + o]);
+    t1[m] = mul_pow2<-1>(TD[lt + o] + TD[ltp + o]);
     ta0[m] = .125 * (TA[lt + o] + TA[ltm + o]);
     ta1[m] = .125 * (TA[ltA + o] + TA[ltAm + o]);
   }
@@ -548,13 +548,13 @@ __device__ __forceinline__ void visc_2d(const Zone& z, const double* __restrict_
   double xmutvol, xktvol, xsa;
   mut_face<NV>(z, q, xmut, il, ir, volinv, xmutvol, xktvol, xsa);
   double fv, fv5;
-  fv = -(2. * e1 * tcx + e2 * tcy) * xmutvol;
+  fv = -(mul_pow2<1>(e1) * tcx + e2 * tcy) * xmutvol;
   fv5 = fv * (q[ir + nd] + q[il + nd]);
   F[1] = F[1] + fv;
-  fv = -(e2 * tcx + 2. * e4 * tcy) * xmutvol;
+  fv = -(e2 * tcx + mul_pow2<1>(e4) * tcy) * xmutvol;
   fv5 = fv5 + fv * (q[ir + 2 * nd] + q[il + 2 * nd]);
   F[2] = F[2] + fv;
-  fv = fv5 * 0.5 - (g[2][0] * tcx + g[2][1] * tcy) * xktvol;
+  fv = mul_pow2<-1>(fv5) - (g[2][0] * tcx + g[2][1] * tcy) * xktvol;
   F[4] = F[4] + fv;
   if (NV == 6) {   // diffusion of nutilde
     const double* Q = q + 5 * nd;
@@ -587,7 +587,7 @@ __device__ __forceinline__ void face_flux_at(const Zone& z, const double* __rest
   const int64_t nd = z.nd;
   double qm[NV], qp[NV];
   double roff = 0.;
-  if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
+  if (SL == MINMOD) roff = mul_pow2<-1>(fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.)));
   if (SL == O3SC || SL == O5SC) roff = z.wig[l + D * nd + (KF == SENSEUR ? 3 * nd : 0)];
 #pragma unroll
   for (int v = 0; v < NV; v++) {
@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(256) face_flux_batch(const __grid_constant__ F
 // cons energy of a primitive state (core3ark3.for:127-150 / core3as2.for)
 __device__ __forceinline__ double roe_of(double cv, double r, double u, double v, double w,
                                          double t) {
-  return r * (cv * t + 0.5 * (u * u + v * v + w * w));
+  return r * (cv * t + mul_pow2<-1>(u * u + v * v + w * w));
 }
 
 // NV = 6 (Spalart-Allmaras): the ro nutilde balance starts from drodm(:,6),
@@ -744,15 +744,15 @@ __device__ __forceinline__ void assemble_at(const Zone& z, const StageArgs& a, c
     double rr = 1. / n1;
     double n2 = (ro * u + tab2) * rr;
     double n3 = (ro * v + tab3) * rr;
-    double cvinv = 1. / cv, cvinv2 = 0.5 * cvinv;
+    double cvinv = 1. / cv, cvinv2 = mul_pow2<-1>(cvinv);
     double n4, n5;
     if (z.typ == Z2D) {  // core3ark3.for 2-d branch: w = 0
       n4 = 0.;
-      double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v));
+      double roe_old = ro * (cv * tt + mul_pow2<-1>(u * u + v * v));
       n5 = (roe_old + tab5) * rr * cvinv - cvinv2 * (n2 * n2 + n3 * n3);
     } else {
       n4 = (ro * w + tab4) * rr;
-      double roe_old = ro * (cv * tt + 0.5 * (u * u + v * v + w * w));
+      double roe_old = ro * (cv * tt + mul_pow2<-1>(u * u + v * v + w * w));
       n5 = (roe_old + tab5) * rr * cvinv - cvinv2 * (n2 * n2 + n3 * n3 + n4 * n4);
     }
     double* O = a.rop_out;
@@ -921,19 +921,19 @@ __device__ __forceinline__ void sa_source_at(const Zone& z, const double* __rest
   if (TYP == Z2D) {
     const double rotz = g[1][0] - g[0][1];
     rot = fabs(rotz) * xvol;
-    const double S11 = g[0][0], S22 = g[1][1], S12 = 0.5 * (g[0][1] + g[1][0]);
-    St = S11 * S11 + S22 * S22 + 2. * (S12 * S12);
-    St = sqrt(2. * St) * xvol;
+    const double S11 = g[0][0], S22 = g[1][1], S12 = mul_pow2<-1>(g[0][1] + g[1][0]);
+    St = S11 * S11 + S22 * S22 + mul_pow2<1>(S12 * S12);
+    St = sqrt(mul_pow2<1>(St)) * xvol;
     anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1]) * xvol * xvol;
   } else {
     const double rotx = g[2][1] - g[1][2], roty = g[0][2] - g[2][0], rotz = g[1][0] - g[0][1];
     rot = sqrt(rotx * rotx + roty * roty + rotz * rotz) * xvol;
     const double S11 = g[0][0], S22 = g[1][1], S33 = g[2][2];
-    const double S12 = 0.5 * (g[0][1] + g[1][0]), S13 = 0.5 * (g[0][2] + g[2][0]),
-                 S23 = 0.5 * (g[1][2] + g[2][1]);
-    St = S11 * S11 + S22 * S22 + S33 * S33 + 2. * (S12 * S12) + 2. * (S13 * S13) +
-         2. * (S23 * S23);
-    St = sqrt(2. * St) * xvol;
+    const double S12 = mul_pow2<-1>(g[0][1] + g[1][0]), S13 = mul_pow2<-1>(g[0][2] + g[2][0]),
+                 S23 = mul_pow2<-1>(g[1][2] + g[2][1]);
+    St = S11 * S11 + S22 * S22 + S33 * S33 + mul_pow2<1>(S12 * S12) + mul_pow2<1>(S13 * S13) +
+         mul_pow2<1>(S23 * S23);
+    St = sqrt(mul_pow2<1>(St)) * xvol;
     anvisc = c1 * (gn[0] * gr[0] + gn[1] * gr[1] + gn[2] * gr[2]) * xvol * xvol;
   }
   // mulam.for, SA/chi.for
@@ -1025,8 +1025,8 @@ __global__ void __launch_bounds__(128) face_flux_tape(Zone z, const double* __re
     const double a = Q[l - 2 * inc], b = Q[l - inc], c = Q[l], d = Q[l + inc];
     const double x1 = c - b, y1 = d - c, x2 = b - a, y2 = c - b;
     const double vm = vanalbada(x1, y1), vp = vanalbada(x2, y2);
-    qm[v] = c - 0.5 * vm;
-    qp[v] = b + 0.5 * vp;
+    qm[v] = c - mul_pow2<-1>(vm);
+    qp[v] = b + mul_pow2<-1>(vp);
     const int m = v == 4 ? 3 : v;
     T[(TAPE_VA + 2 * m) * nf] = vm;
     T[(TAPE_VA + 2 * m + 1) * nf] = vp;
@@ -1315,7 +1315,7 @@ __global__ void __launch_bounds__(128) wall_corr(Zone z, const double* __restric
   const int64_t l = a.l[e], l0 = a.l0[e], nd = z.nd, inc = z.inc[D];
   double qm[5], qp[5];
   double roff = 0.;
-  if (SL == MINMOD) roff = .5 * fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.));
+  if (SL == MINMOD) roff = mul_pow2<-1>(fmaxF(0., fminF(q[l + 4 * nd] * z.tmin_1 - .5, 1.)));
   if (SL == O3SC) roff = z.wig[l + D * nd];
 #pragma unroll
   for (int v = 0; v < 5; v++) {
@@ -1349,23 +1349,23 @@ __global__ void __launch_bounds__(128) wall_corr(Zone z, const double* __restric
   const int64_t ia = l - inc;   // iadrf
   const double t0 = a.nrm[3 * e], t1 = a.nrm[3 * e + 1], t2 = a.nrm[3 * e + 2];
   const double qen = 0.;
-  const double r = 0.5 * (q[l] + q[ia]);
-  const double u = 0.5 * (q[l + nd] + q[ia + nd]);
-  const double v = 0.5 * (q[l + 2 * nd] + q[ia + 2 * nd]);
-  const double w = 0.5 * (q[l + 3 * nd] + q[ia + 3 * nd]);
+  const double r = mul_pow2<-1>(q[l] + q[ia]);
+  const double u = mul_pow2<-1>(q[l + nd] + q[ia + nd]);
+  const double v = mul_pow2<-1>(q[l + 2 * nd] + q[ia + 2 * nd]);
+  const double w = mul_pow2<-1>(q[l + 3 * nd] + q[ia + 3 * nd]);
   const double u_int = t0 * u + t1 * v + t2 * w - qen;
   double fw[5];
   if (a.slip) {
     double p = q[ia + 4 * nd] * q[ia] * a.rgp;
-    const double h = a.gam2 * p + r * (u * u + v * v + w * w) * 0.5;
-    p = 0.5 * (q[l + 4 * nd] * q[l] + q[ia + 4 * nd] * q[ia]) * a.rgp;
+    const double h = a.gam2 * p + mul_pow2<-1>(r * (u * u + v * v + w * w));
+    p = mul_pow2<-1>(q[l + 4 * nd] * q[l] + q[ia + 4 * nd] * q[ia]) * a.rgp;
     fw[0] = u_int * r;
     fw[1] = t0 * p + u_int * r * u;
     fw[2] = t1 * p + u_int * r * v;
     fw[3] = t2 * p + u_int * r * w;
     fw[4] = u_int * h + p * qen;
   } else {
-    const double p = 0.5 * (q[l + 4 * nd] * q[l] + q[ia + 4 * nd] * q[ia]) * a.rgp;
+    const double p = mul_pow2<-1>(q[l + 4 * nd] * q[l] + q[ia + 4 * nd] * q[ia]) * a.rgp;
     fw[0] = 0.;
     fw[1] = t0 * p + u_int * u * r;
     fw[2] = t1 * p + u_int * v * r;
@@ -1469,10 +1469,10 @@ __global__ void __launch_bounds__(128) shock_sensor(Zone z, const double* __rest
     if (TYP == Z2D) {
       double t = sqrt(tix * tix + tiy * tiy);
       t = t + sqrt(tix1 * tix1 + tiy1 * tiy1);
-      tc[0] = fmaxF(.5 * t, 1.e-27);
+      tc[0] = fmaxF(mul_pow2<-1>(t), 1.e-27);
       t = sqrt(tjx * tjx + tjy * tjy);
       t = t + sqrt(tjx1 * tjx1 + tjy1 * tjy1);
-      tc[1] = fmaxF(.5 * t, 1.e-27);
+      tc[1] = fmaxF(mul_pow2<-1>(t), 1.e-27);
       tc[2] = 1.;
       dudx = u3[0] * tix1 - u1[0] * tix + u2[0] * tjx1 - u4[0] * tjx;
       div = dudx * xvol;
@@ -1489,13 +1489,13 @@ __global__ void __launch_bounds__(128) shock_sensor(Zone z, const double* __rest
       const double tkx1 = z.tk[lt + km], tky1 = z.tk[lt + km + ndm], tkz1 = z.tk[lt + km + 2 * ndm];
       double t = sqrt(tix * tix + tiy * tiy + tiz * tiz);
       t = t + sqrt(tix1 * tix1 + tiy1 * tiy1 + tiz1 * tiz1);
-      tc[0] = fmaxF(.5 * t, 1.e-27);
+      tc[0] = fmaxF(mul_pow2<-1>(t), 1.e-27);
       t = sqrt(tjx * tjx + tjy * tjy + tjz * tjz);
       t = t + sqrt(tjx1 * tjx1 + tjy1 * tjy1 + tjz1 * tjz1);
-      tc[1] = fmaxF(.5 * t, 1.e-27);
+      tc[1] = fmaxF(mul_pow2<-1>(t), 1.e-27);
       t = sqrt(tkx * tkx + tky * tky + tkz * tkz);
       t = t + sqrt(tkx1 * tkx1 + tky1 * tky1 + tkz1 * tkz1);
-      tc[2] = fmaxF(.5 * t, 1.e-27);
+      tc[2] = fmaxF(mul_pow2<-1>(t), 1.e-27);
 #define FGB_G(m, x) (u3[m] * ti##x##1 - u1[m] * ti##x + u2[m] * tj##x##1 - u4[m] * tj##x + \
                      u5[m] * tk##x##1 - u6[m] * tk##x)
       dudx = FGB_G(0, x);
@@ -1534,14 +1534,14 @@ __global__ void __launch_bounds__(128) shock_sensor(Zone z, const double* __rest
     double mach = m_prev;
     if (tc[d] != tc_prev) {
       mach = 10.0 * (1.0 / tc[d]) * isnd * div;
-      mach = 0.5 * (1.0 - tanh(2.5 + mach));
+      mach = mul_pow2<-1>(1.0 - tanh(2.5 + mach));
       tc_prev = tc[d];
       m_prev = mach;
     }
     const int64_t n = z.inc[d];
     const double p2 = q[l - n] * q[l - n + 4 * nd];
     const double p1 = q[l + n] * q[l + n + 4 * nd];
-    double w = fabs(p2 - 2. * p0 + p1) / fabs(p2 + 2. * p0 + p1);
+    double w = fabs(p2 - mul_pow2<1>(p0) + p1) / fabs(p2 + mul_pow2<1>(p0) + p1);
     w = fminF(ratio * w * mach, 1.0);
     wig[l + d * nd + shift] = 1.0 - w;
   }

@@ -103,6 +103,7 @@ struct FlowArgs {
   int wait_skew;                // added to the marks a wait expects (0; > 0 only in tests)
   int* err;                     // device error word (2: a wait gave up)
   long long poll_limit;
+  int prefetch;                 // 1: L2 prefetch of a chunk's cold operands before its wait
 };
 int lusgs_flow_chunk();
 

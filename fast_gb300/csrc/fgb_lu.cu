@@ -72,11 +72,11 @@ __device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a,
     double tcxi = z.ti[0], tcyj = z.tj[0], tczk = z.tk[0];
     double tc2i = sqrt(tcxi * tcxi), tc2j = sqrt(tcyj * tcyj), tc2k = sqrt(tczk * tczk);
     double vmi = fabs(tcxi * u) + c * tc2i;
-    c2 = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+    c2 = mul_pow2<1>(vmi) + mul_pow2<2>(xmvis * tc2i * tc2i);
     double vmj = fabs(tcyj * v) + c * tc2j;
-    c3 = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+    c3 = mul_pow2<1>(vmj) + mul_pow2<2>(xmvis * tc2j * tc2j);
     double vmk = fabs(tczk * w) + c * tc2k;
-    c4 = vmk * 2. + xmvis * tc2k * tc2k * 4.;
+    c4 = mul_pow2<1>(vmk) + mul_pow2<2>(xmvis * tc2k * tc2k);
   } else if (z.typ == Z2D) {  // tstb3c.for 2-d branch: i and j only
     const int64_t lt = indmtr(z, i, j, k), m = z.ndm;
     double detj = fmaxF(z.vol[lt], cut0x);
@@ -88,16 +88,16 @@ __device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a,
     for (int d = 0; d < 2; d++) {
       const double* T = T2[d];
       int64_t l2 = lt + z.minc[d];
-      double tx = .5 * (T[lt] + T[l2]);
-      double ty = .5 * (T[lt + m] + T[l2 + m]);
-      double tc2 = .5 * (sqrt(T[lt] * T[lt] + T[lt + m] * T[lt + m]) + sqrt(T[l2] * T[l2] + T[l2 + m] * T[l2 + m]));
+      double tx = mul_pow2<-1>(T[lt] + T[l2]);
+      double ty = mul_pow2<-1>(T[lt + m] + T[l2 + m]);
+      double tc2 = mul_pow2<-1>(sqrt(T[lt] * T[lt] + T[lt + m] * T[lt + m]) + sqrt(T[l2] * T[l2] + T[l2 + m] * T[l2 + m]));
       double qn = tx * u + ty * v;
       double vm = fabs(qn) + c * tc2;
-      cc[d] = vm * 2. + xmvis * tc2 * tc2 * 4.;
+      cc[d] = mul_pow2<1>(vm) + mul_pow2<2>(xmvis * tc2 * tc2);
     }
     a.coe[l + nd] = cc[0];
     a.coe[l + 2 * nd] = cc[1];
-    a.coe[l + 4 * nd] = xid + c1 * (cc[0] + cc[1]) * 0.5;
+    a.coe[l + 4 * nd] = xid + mul_pow2<-1>(c1 * (cc[0] + cc[1]));
     return;
   } else {
     const int64_t lt = indmtr(z, i, j, k), m = z.ndm;
@@ -110,21 +110,21 @@ __device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a,
     for (int d = 0; d < 3; d++) {
       const double* T = T3[d];
       int64_t l2 = lt + z.minc[d];
-      double tx = .5 * (T[lt] + T[l2]);
-      double ty = .5 * (T[lt + m] + T[l2 + m]);
-      double tz = .5 * (T[lt + 2 * m] + T[l2 + 2 * m]);
-      double tc2 = .5 * (sqrt(T[lt] * T[lt] + T[lt + m] * T[lt + m] + T[lt + 2 * m] * T[lt + 2 * m]) +
+      double tx = mul_pow2<-1>(T[lt] + T[l2]);
+      double ty = mul_pow2<-1>(T[lt + m] + T[l2 + m]);
+      double tz = mul_pow2<-1>(T[lt + 2 * m] + T[l2 + 2 * m]);
+      double tc2 = mul_pow2<-1>(sqrt(T[lt] * T[lt] + T[lt + m] * T[lt + m] + T[lt + 2 * m] * T[lt + 2 * m]) +
                          sqrt(T[l2] * T[l2] + T[l2 + m] * T[l2 + m] + T[l2 + 2 * m] * T[l2 + 2 * m]));
       double qn = tx * u + ty * v + tz * w;
       double vm = fabs(qn) + c * tc2;
-      cc[d] = vm * 2. + xmvis * tc2 * tc2 * 4.;
+      cc[d] = mul_pow2<1>(vm) + mul_pow2<2>(xmvis * tc2 * tc2);
     }
     c2 = cc[0]; c3 = cc[1]; c4 = cc[2];
   }
   a.coe[l + nd] = c2;
   a.coe[l + 2 * nd] = c3;
   a.coe[l + 3 * nd] = c4;
-  a.coe[l + 4 * nd] = xid + c1 * (c2 + c3 + c4) * 0.5;
+  a.coe[l + 4 * nd] = xid + mul_pow2<-1>(c1 * (c2 + c3 + c4));
 }
 
 __global__ void __launch_bounds__(256) coefficients(Zone z, CoeArgs a) {
@@ -899,6 +899,30 @@ __device__ __forceinline__ bool flow_poll(const FlowArgs& a, int64_t c, int mark
   }
 }
 
+// L2 prefetch of what a chunk reads that no earlier plane produced (its
+// cells' records, residuals / lower results and neighbour indices), issued
+// before the dependency wait: those lines are cold in L2 (the records are
+// written by the gather and read once per sweep), so without it the DRAM
+// latency lands between the wait and the cell work.  Lane m takes every
+// 32nd 128-byte line of each span.
+__device__ __forceinline__ void prefetch_span_chunk(const void* base, int64_t bytes, int lane) {
+  const char* b = static_cast<const char*>(base);
+  const int64_t a0 = (int64_t)((uintptr_t)b & 127u);
+  for (int64_t o = (int64_t)lane * 128 - a0; o < bytes; o += 32 * 128)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(b + (o < 0 ? 0 : o)));
+}
+template <int TYP, typename T>
+__device__ __forceinline__ void prefetch_chunk(const PlaneData<T>& p, int64_t g0, int64_t n,
+                                               bool upper, int lane) {
+  using R = Rec<TYP, T>;
+  prefetch_span_chunk(p.rec + g0 * R::SIZE, n * R::SIZE * (int64_t)sizeof(T), lane);
+  prefetch_span_chunk(p.dio + g0 * DIO, n * DIO * (int64_t)sizeof(T), lane);
+  const int32_t* nb = upper ? p.nbu : p.nbl;
+#pragma unroll
+  for (int d = 0; d < 3; d++) prefetch_span_chunk(nb + d * p.G + g0, n * 4, lane);
+  if (upper) prefetch_span_chunk(p.cells + g0, n * 4, lane);   // the in-place Newton update's cells
+}
+
 // (Loading the cells' static operands before the wait was measured slower:
 // the operands held across the wait raise the register count to 154 and
 // halve the resident warps; so was splitting the neighbours' wait and the
@@ -929,13 +953,14 @@ __global__ void __launch_bounds__(FLOW_THREADS)
     const int32_t* dp = a.dep + 4 * ch + (upper ? 2 : 0);
     const int64_t lo = dp[0], hi = dp[1];
     const int mark = upper ? a.upper_mark : a.lower_mark;
+    const int s = a.cplane[ch];
+    const int64_t g0 = p.plane[s] + (ch - a.cbase[s]) * FLOW_CHUNK;
+    const int64_t n = p.plane[s + 1] - g0;
+    if (a.prefetch) prefetch_chunk<TYP, T>(p, g0, n < FLOW_CHUNK ? n : FLOW_CHUNK, upper, lane);
     bool ok = true;
     for (int64_t c = lo + lane; c <= hi; c += 32) ok = ok && flow_poll(a, c, mark + a.wait_skew);
     if (upper && lane == 0) ok = ok && flow_poll(a, ch, a.lower_mark + a.wait_skew);
     if (!__all_sync(0xffffffffu, ok)) return;
-    const int s = a.cplane[ch];
-    const int64_t g0 = p.plane[s] + (ch - a.cbase[s]) * FLOW_CHUNK;
-    const int64_t n = p.plane[s + 1] - g0;
     if (upper) flow_chunk<TYP, T, NV, MULTI, true>(z, p, f, g0, n, lane);
     else flow_chunk<TYP, T, NV, MULTI, false>(z, p, f, g0, n, lane);
     __syncwarp();

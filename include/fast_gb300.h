@@ -105,7 +105,9 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * grid-barrier wait gives up after 4 times as many), after which
  * fgb_synchronize reports FGB_ERR_DEVICE; "lu_wait_skew": test support, 0
  * (raises the marks and barrier targets the waits expect, so that they run
- * out);
+ * out); "lu_prefetch": 1 (default) to prefetch into L2 the operands of a
+ * dataflow chunk that no earlier plane produced before its dependency wait,
+ * 0 not to (same results);
  * "batch": 1 (default) to run the coefficient, Spalart-Allmaras source,
  * face and balance / update kernels of several zones as one launch per kind
  * of zone (zone type, scheme, slope, viscosity, NEQ; up to 40 zones a
