@@ -1687,15 +1687,23 @@ static int build_lu_groups(fgb_solver* s) {
       for (int64_t t = 0; t < np; t++)
         cbase[(size_t)t + 1] = cbase[(size_t)t] + (g.plane_host[(size_t)t + 1] - g.plane_host[(size_t)t] + C - 1) / C;
       g.nchunk = cbase[(size_t)np];
-      if (g.nchunk >= (int64_t)INT32_MAX / 4) return fail(FGB_ERR_ARG, "LU group too large");
-      std::vector<int32_t> cplane((size_t)g.nchunk), dep((size_t)(4 * g.nchunk));
+      if (g.nchunk >= (int64_t)INT32_MAX / FLOW_DEP) return fail(FGB_ERR_ARG, "LU group too large");
+      std::vector<int32_t> cplane((size_t)g.nchunk), dep((size_t)(FLOW_DEP * g.nchunk));
       auto chunk_of = [&](int64_t t, int64_t gg) {
         return cbase[(size_t)t] + (gg - g.plane_host[(size_t)t]) / C;
       };
+      // the chunks a chunk needs, as at most two ranges [lo1, hi1] u [lo2,
+      // hi2] (plane order runs over k, then j, so the i-1 / j-1 neighbours
+      // sit in one or two chunks and the k-1 neighbours a k-row earlier in
+      // one or two more): sorted distinct chunks, split at the widest gap;
+      // more clusters than two merge into the covering ranges (a superset
+      // of the dependencies, which is still a correct wait)
+      std::vector<int64_t> need[2];
       for (int64_t t = 0; t < np; t++) {
         for (int64_t c = cbase[(size_t)t]; c < cbase[(size_t)t + 1]; c++) {
           cplane[(size_t)c] = (int32_t)t;
-          int64_t lo[2] = {INT64_MAX, INT64_MAX}, hi[2] = {-1, -1};
+          need[0].clear();
+          need[1].clear();
           const int64_t g0 = g.plane_host[(size_t)t] + (c - cbase[(size_t)t]) * C;
           const int64_t g1 = std::min(g0 + C, g.plane_host[(size_t)t + 1]);
           for (int64_t gg = g0; gg < g1; gg++) {
@@ -1707,20 +1715,24 @@ static int build_lu_groups(fgb_solver* s) {
             const int64_t l = idx(s->zones[g.zones[q]].pi, ii + 1, jj + 1, kk + 1);
             const int64_t ix[3] = {ii, jj, kk}, nn[3] = {z.ni, z.nj, z.nk};
             for (int d = 0; d < 3; d++) {
-              if (ix[d] > 0) {
-                const int64_t c2 = chunk_of(t - 1, pm[(size_t)(l - z.inc[d])]);
-                lo[0] = std::min(lo[0], c2); hi[0] = std::max(hi[0], c2);
-              }
-              if (ix[d] < nn[d] - 1) {
-                const int64_t c2 = chunk_of(t + 1, pm[(size_t)(l + z.inc[d])]);
-                lo[1] = std::min(lo[1], c2); hi[1] = std::max(hi[1], c2);
-              }
+              if (ix[d] > 0) need[0].push_back(chunk_of(t - 1, pm[(size_t)(l - z.inc[d])]));
+              if (ix[d] < nn[d] - 1) need[1].push_back(chunk_of(t + 1, pm[(size_t)(l + z.inc[d])]));
             }
           }
           for (int u = 0; u < 2; u++) {
-            if (hi[u] < 0) { lo[u] = 0; hi[u] = -1; }
-            dep[(size_t)(4 * c + 2 * u)] = (int32_t)lo[u];
-            dep[(size_t)(4 * c + 2 * u + 1)] = (int32_t)hi[u];
+            std::vector<int64_t>& v = need[u];
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+            int64_t r[4] = {0, -1, 0, -1};   // empty ranges
+            if (!v.empty()) {
+              size_t cut = v.size();   // split before the widest gap
+              int64_t wide = 1;
+              for (size_t m = 1; m < v.size(); m++)
+                if (v[m] - v[m - 1] > wide) { wide = v[m] - v[m - 1]; cut = m; }
+              r[0] = v.front(); r[1] = v[cut - 1];
+              if (cut < v.size()) { r[2] = v[cut]; r[3] = v.back(); }
+            }
+            for (int e = 0; e < 4; e++) dep[(size_t)(FLOW_DEP * c + 4 * u + e)] = (int32_t)r[e];
           }
         }
       }

@@ -91,13 +91,15 @@ struct LuZone { Zone z; LuFields f; };
 // FP64 or FP32 sweeps (mixed precision; the Newton update stays FP64).
 // Dataflow schedule of the sweeps (lusgs_flow): chunks of 32 consecutive
 // cells of a hyperplane, their completion marks and dependency ranges.
+constexpr int FLOW_DEP = 8;     // dependency table entries per dataflow chunk
 struct FlowArgs {
   unsigned long long* ticket;   // zeroed before each launch
   int* flag;                    // [nchunk] completion mark of each chunk (never cleared)
   const int32_t* cplane;        // [nchunk] hyperplane of each chunk
   const int64_t* cbase;         // [smax + 2] first chunk of each hyperplane
-  const int32_t* dep;           // [nchunk][4] chunk ranges [lo, hi] holding the lower
-                                // neighbours (plane s-1) and the upper ones (plane s+1)
+  const int32_t* dep;           // [nchunk][FLOW_DEP]: the chunks holding the lower
+                                // neighbours (plane s-1) as two ranges [lo, hi], then
+                                // the upper ones (plane s+1); an empty range is [0, -1]
   int64_t nchunk;
   int lower_mark, upper_mark;   // 2 epoch + 1, 2 epoch + 2 (published)
   int wait_skew;                // added to the marks a wait expects (0; > 0 only in tests)

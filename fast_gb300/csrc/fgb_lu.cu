@@ -876,7 +876,10 @@ __global__ void __launch_bounds__(LuThreads<T>::n, 1)
 // its 32 cells (one per lane, the cell code of the other schedules) and
 // publishes its own mark.  A warp only ever waits on chunks with smaller
 // tickets, which running warps already hold, so the launch cannot deadlock
-// whatever the number of resident CTAs; a plane starts as soon as the
+// whatever the number of resident CTAs.  Its dependencies are the chunks of
+// the previous plane that hold its cells' neighbours, as at most two ranges
+// of chunk indices per sweep (the i-1 / j-1 and the k-1 neighbours); a
+// plane starts as soon as the
 // cells it needs are done instead of after the whole previous plane, and the
 // FP64 pipes stay busy across plane boundaries.  An upper chunk also waits on
 // its own lower mark (its cells' lower results).  Marks are 2 e + 1 (lower)
@@ -950,15 +953,16 @@ __global__ void __launch_bounds__(FLOW_THREADS)
     if (*(volatile int*)a.err) return;
     const bool upper = t >= (unsigned long long)nc;
     const int64_t ch = upper ? 2 * nc - 1 - (int64_t)t : (int64_t)t;
-    const int32_t* dp = a.dep + 4 * ch + (upper ? 2 : 0);
-    const int64_t lo = dp[0], hi = dp[1];
+    const int32_t* dp = a.dep + FLOW_DEP * ch + (upper ? 4 : 0);
+    const int64_t lo1 = dp[0], n1 = dp[1] - lo1 + 1, lo2 = dp[2], n2 = dp[3] - lo2 + 1;
     const int mark = upper ? a.upper_mark : a.lower_mark;
     const int s = a.cplane[ch];
     const int64_t g0 = p.plane[s] + (ch - a.cbase[s]) * FLOW_CHUNK;
     const int64_t n = p.plane[s + 1] - g0;
     if (a.prefetch) prefetch_chunk<TYP, T>(p, g0, n < FLOW_CHUNK ? n : FLOW_CHUNK, upper, lane);
     bool ok = true;
-    for (int64_t c = lo + lane; c <= hi; c += 32) ok = ok && flow_poll(a, c, mark + a.wait_skew);
+    for (int64_t m = lane; m < n1 + n2; m += 32)
+      ok = ok && flow_poll(a, m < n1 ? lo1 + m : lo2 + (m - n1), mark + a.wait_skew);
     if (upper && lane == 0) ok = ok && flow_poll(a, ch, a.lower_mark + a.wait_skew);
     if (!__all_sync(0xffffffffu, ok)) return;
     if (upper) flow_chunk<TYP, T, NV, MULTI, true>(z, p, f, g0, n, lane);
