@@ -33,6 +33,7 @@ SIGNATURES = {
     "fgb_set_option": ([_P, C.c_char_p, C.c_double], C.c_int),
     "fgb_get_option": ([_P, C.c_char_p, _DP], C.c_int),
     "fgb_upload_state": ([_P, C.c_int, C.c_int, _DP], C.c_int),
+    "fgb_upload_state_async": ([_P, C.c_int, C.c_int, _DP], C.c_int),
     "fgb_download_state": ([_P, C.c_int, C.c_int, _DP], C.c_int),
     "fgb_download_work": ([_P, C.c_int, C.c_char_p, _DP, C.c_int64], C.c_int),
     "fgb_compute": ([_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
@@ -174,6 +175,14 @@ class Solver:
     def upload(self, zone: int, level: int, arr: np.ndarray):
         a = np.ascontiguousarray(arr, dtype=np.float64)
         _check(self._lib.fgb_upload_state(self._h, zone, level, _dp(a)))
+
+    def upload_async(self, zone: int, level: int, arr: np.ndarray):
+        """fgb_upload_state_async: asynchronous when ``arr`` lies in memory
+        this solver page-locked (pin), which keeps it alive; the array must
+        not change until the next synchronizing call."""
+        if arr.dtype != np.float64 or not arr.flags.c_contiguous:
+            return self.upload(zone, level, arr)
+        _check(self._lib.fgb_upload_state_async(self._h, zone, level, _dp(arr)))
 
     def download(self, zone: int, level: int, out: np.ndarray | None = None) -> np.ndarray:
         pi = self.zones[zone][0]

@@ -92,6 +92,11 @@ struct ZoneData {
   int32_t *co_dst = nullptr, *co_a = nullptr, *co_b = nullptr, *co_c = nullptr;
   int64_t co_nedge = 0, co_n = 0;
   double coesut = 0., cmus1 = 0.;
+  // asynchronous uploads of the time levels (fgb_upload_state_async): the
+  // copy's completion event, waited on by the solver stream before the
+  // level's first use
+  cudaEvent_t up_ev[3] = {nullptr, nullptr, nullptr};
+  bool up_pending[3] = {false, false, false};
 };
 struct Transfer {
   int dnr, rcv; int64_t n; int32_t* dnr_idx; int32_t* rcv_idx;
@@ -170,6 +175,9 @@ struct fgb_solver {
   static constexpr int ZS = 8;
   bool zone_streams = true;
   std::vector<void*> pinned;       // host buffers page-locked by fgb_pin_host
+  std::vector<size_t> pinned_bytes;
+  cudaStream_t cst = nullptr;      // copy stream of the asynchronous uploads (created on first use)
+  cudaEvent_t cst_ev = nullptr;    // solver-stream point an asynchronous upload starts after
   // all transfers as one list (zone ids per entry), built at the first fill
   int32_t *tr_rz = nullptr, *tr_ri = nullptr, *tr_dz = nullptr, *tr_di = nullptr;
   int64_t tr_n = 0;
@@ -681,7 +689,12 @@ int fgb_create(int device, fgb_solver** out) {
 int fgb_destroy(fgb_solver* s) {
   if (!s) return FGB_OK;
   cudaSetDevice(s->device);
+  if (s->cst) cudaStreamSynchronize(s->cst);
   cudaStreamSynchronize(s->st);
+  for (ZoneData& Z : s->zones)
+    for (int i = 0; i < 3; i++) if (Z.up_ev[i]) cudaEventDestroy(Z.up_ev[i]);
+  if (s->cst_ev) cudaEventDestroy(s->cst_ev);
+  if (s->cst) cudaStreamDestroy(s->cst);
   for (ZoneData& Z : s->zones) {
     for (int i = 0; i < 3; i++) cudaFree(Z.lvl[i]);
     cudaFree(Z.scratch); cudaFree(Z.drodm); cudaFree(Z.coe); cudaFree(Z.xmut); cudaFree(Z.rdm);
@@ -995,12 +1008,59 @@ static int check_zone(fgb_solver* s, int zone) {
   return FGB_OK;
 }
 
+// the solver stream waits for the pending asynchronous upload of one level
+// of one zone, or of every level of every zone
+static int join_upload(fgb_solver* s, ZoneData& Z, int level) {
+  if (!Z.up_pending[level]) return FGB_OK;
+  CK(cudaStreamWaitEvent(s->st, Z.up_ev[level], 0));
+  Z.up_pending[level] = false;
+  return FGB_OK;
+}
+static int join_uploads(fgb_solver* s) {
+  for (ZoneData& Z : s->zones)
+    for (int lv = 0; lv < 3; lv++) {
+      int rc = join_upload(s, Z, lv);
+      if (rc) return rc;
+    }
+  return FGB_OK;
+}
+
+int fgb_upload_state_async(fgb_solver* s, int zone, int level, const double* host) {
+  int rc = check_zone(s, zone);
+  if (rc) return rc;
+  if (level < 0 || level > 2 || !host) return fail(FGB_ERR_ARG, "bad level or buffer");
+  ZoneData& Z = s->zones[zone];
+  const size_t bytes = sizeof(double) * Z.z.neq * Z.z.nd;
+  bool pinned = false;   // only a buffer page-locked by this solver is copied asynchronously
+  for (size_t q = 0; q < s->pinned.size(); q++) {
+    const char* b = static_cast<const char*>(s->pinned[q]);
+    const char* h = reinterpret_cast<const char*>(host);
+    if (h >= b && h + bytes <= b + s->pinned_bytes[q]) pinned = true;
+  }
+  if (!pinned) return fgb_upload_state(s, zone, level, host);
+  CK(cudaSetDevice(s->device));
+  if (!s->cst) {
+    CK(cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&s->cst_ev, cudaEventDisableTiming));
+  }
+  if (!Z.up_ev[level]) CK(cudaEventCreateWithFlags(&Z.up_ev[level], cudaEventDisableTiming));
+  // the copy overwrites the level only after the solver stream's work so far
+  CK(cudaEventRecord(s->cst_ev, s->st));
+  CK(cudaStreamWaitEvent(s->cst, s->cst_ev, 0));
+  CK(cudaMemcpyAsync(Z.lvl[level], host, bytes, cudaMemcpyHostToDevice, s->cst));
+  CK(cudaEventRecord(Z.up_ev[level], s->cst));
+  Z.up_pending[level] = true;
+  return FGB_OK;
+}
+
 int fgb_upload_state(fgb_solver* s, int zone, int level, const double* host) {
   int rc = check_zone(s, zone);
   if (rc) return rc;
   if (level < 0 || level > 2 || !host) return fail(FGB_ERR_ARG, "bad level or buffer");
   ZoneData& Z = s->zones[zone];
   CK(cudaSetDevice(s->device));
+  rc = join_uploads(s);
+  if (rc) return rc;
   CK(cudaMemcpyAsync(Z.lvl[level], host, sizeof(double) * Z.z.neq * Z.z.nd,
                      cudaMemcpyHostToDevice, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -1013,6 +1073,7 @@ int fgb_download_state(fgb_solver* s, int zone, int level, double* host) {
   if (level < 0 || level > 2 || !host) return fail(FGB_ERR_ARG, "bad level or buffer");
   ZoneData& Z = s->zones[zone];
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   CK(cudaMemcpyAsync(host, Z.lvl[level], sizeof(double) * Z.z.neq * Z.z.nd,
                      cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -1035,6 +1096,7 @@ int fgb_download_work(fgb_solver* s, int zone, const char* which, double* host, 
   else return fail(FGB_ERR_ARG, "unknown work array " + w);
   if (n < need) return fail(FGB_ERR_ARG, "buffer too small for " + w);
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   CK(cudaMemcpyAsync(host, src, sizeof(double) * need, cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
   return FGB_OK;
@@ -1404,6 +1466,7 @@ int fgb_apply_bc(fgb_solver* s, int level) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
   if (level < 0 || level > 2) return fail(FGB_ERR_ARG, "bad level");
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   return ghost_fill(s, level);
 }
 
@@ -1957,6 +2020,10 @@ static int substep_batched(fgb_solver* s, int nstep, bool implicit, int verif, i
     }
     return sa;
   };
+  for (ZoneData& Z : s->zones) {   // the balance reads level n-1 (BDF2)
+    rc = join_upload(s, Z, 1);
+    if (rc) return rc;
+  }
   {
     ProfScope ps(s, implicit ? "assemble_bdf" : "assemble_rk3");
     rc = batches([&](int m) { return s->zones[(size_t)m].walls.empty() ? (int64_t)s->zones[(size_t)m].z.neq : -1; },
@@ -2012,7 +2079,16 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
                                  "(fgb_set_wall_distance)");
   }
   if (implicit && !s->lu_built) {
-    int rc = build_lu_groups(s);
+    int rc = join_uploads(s);
+    if (rc) return rc;
+    rc = build_lu_groups(s);
+    if (rc) return rc;
+  }
+  // an asynchronous upload of level n-1 overlaps the coefficients and the
+  // face fluxes of the first sub-step; levels n and n+1 are read at once
+  for (ZoneData& Z : s->zones) {
+    int rc = join_upload(s, Z, 0);
+    if (!rc) rc = join_upload(s, Z, 2);
     if (rc) return rc;
   }
   const double cxsi1 = -0.6830127018922193, cxsi2 = -4. / 3.;
@@ -2117,7 +2193,9 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
         }
         {
           ProfScope ps(s, implicit ? "assemble_bdf" : "assemble_rk3");
-          int rc = assemble_stage(s, Z, sa, ssiter, implicit);
+          int rc = join_upload(s, Z, 1);   // level n-1, read by the balance (BDF2)
+          if (rc) return rc;
+          rc = assemble_stage(s, Z, sa, ssiter, implicit);
           if (rc) return rc;
         }
         if (implicit) {
@@ -2210,6 +2288,10 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       }
       if (rc) return rc;
     }
+    {
+      int rc = join_uploads(s);   // before the levels rotate
+      if (rc) return rc;
+    }
     s->first_it = 1;
     for (ZoneData& Z : s->zones) {
       double* save = Z.lvl[1];
@@ -2233,6 +2315,7 @@ int fgb_pin_host(fgb_solver* s, void* ptr, int64_t bytes) {
   }
   CK(e);
   s->pinned.push_back(ptr);
+  s->pinned_bytes.push_back((size_t)bytes);
   return FGB_OK;
 }
 
@@ -2241,6 +2324,7 @@ int fgb_cfl(fgb_solver* s, int zone, double* out) {
   if (rc) return rc;
   if (!out) return fail(FGB_ERR_ARG, "null output pointer");
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   CK(cudaStreamSynchronize(s->st));
   CK(cudaMemcpy(out, s->zones[zone].cfl, sizeof(double) * 3, cudaMemcpyDeviceToHost));
   return FGB_OK;
@@ -2268,6 +2352,7 @@ int fgb_adjoint_forward(fgb_solver* s, int zone, int nsteps, int ckpt) {
   if (rc) return rc;
   if (nsteps < 1 || ckpt < 1) return fail(FGB_ERR_ARG, "nsteps and ckpt must be >= 1");
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   CK(cudaStreamSynchronize(s->st));
   adj_free(s);
   fgb_solver::Adj& A = s->adj;
@@ -2333,6 +2418,7 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
   if (!lam_final || !lam_w0 || !lam_ti || !lam_tj || !lam_vol || !lam_st)
     return fail(FGB_ERR_ARG, "null argument");
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   ZoneData& Z = s->zones[zone];
   const Zone& z = Z.z;
   const size_t nq = (size_t)z.neq * z.nd, nm = (size_t)z.ndm * 2;
@@ -2442,6 +2528,7 @@ int fgb_tangent(fgb_solver* s, int zone, int nsteps, const double* dw0, const do
   if (rc) return rc;
   if (!dw0 || !dti || !dtj || !dvol || !dst || !dw_final) return fail(FGB_ERR_ARG, "null argument");
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   CK(cudaStreamSynchronize(s->st));
   fgb_solver::Adj& A = s->adj;
   ZoneData& Z = s->zones[zone];
@@ -2498,6 +2585,7 @@ int fgb_residuals(fgb_solver* s, int zone, double* out, int64_t n, int* nit_out)
   if (!out || n < 2 * neq * nit) return fail(FGB_ERR_ARG, "output buffer too small");
   std::vector<double> h(Z.n_rdm);
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   CK(cudaMemcpyAsync(h.data(), Z.rdm, sizeof(double) * Z.n_rdm, cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
   double xpt_1 = 1. / (double)(Z.z.ni * Z.z.nj * Z.z.nk);
@@ -2538,6 +2626,7 @@ int fgb_residual_norms_noalloc(fgb_solver* s, int zone, double* out_dev) {
     return fail(FGB_ERR_ARG, "zone has too many LU blocks for the fixed norm scratch "
                              "(2 * neq * blocks > FGB_NORM_PARTIALS_MAX)");
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   cudaPointerAttributes pa{};
   CK(cudaPointerGetAttributes(&pa, out_dev));
   if ((pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged) || pa.device != s->device)
@@ -2565,6 +2654,7 @@ int fgb_residual_norms_noalloc(fgb_solver* s, int zone, double* out_dev) {
 int fgb_synchronize(fgb_solver* s) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
   CK(cudaSetDevice(s->device));
+  { int rj = join_uploads(s); if (rj) return rj; }
   CK(cudaStreamSynchronize(s->st));
   int h = 0;
   CK(cudaMemcpy(&h, s->derr, sizeof(int), cudaMemcpyDeviceToHost));

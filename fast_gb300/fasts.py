@@ -336,10 +336,12 @@ def _compute(t, metrics, nitrun, tc=None, graph=None, tc2=None, graph2=None, lay
     s = HOOK["solver"]
     zones = I.getZones(t)
     if not HOOK["gpu_resident"]:
-        # inputs of the step: levels n and n-1 as the tree holds them
+        # inputs of the step: levels n and n-1 as the tree holds them (the
+        # page-locked tree arrays are copied on a side stream; level n-1
+        # arrives while the first sub-step computes its fluxes)
         for n, z in enumerate(zones):
-            s.upload(n, 0, FastC.compactArray(z, "").reshape(-1))
-            s.upload(n, 1, FastC.compactArray(z, "_M1").reshape(-1))
+            s.upload_async(n, 0, FastC.compactArray(z, "").reshape(-1))
+            s.upload_async(n, 1, FastC.compactArray(z, "_M1").reshape(-1))
     s.set_option("first_it", HOOK["FIRST_IT"])
     s.compute(nitrun, 1, HOOK["nssiter"], 1, NIT)
     if not HOOK["gpu_resident"]:

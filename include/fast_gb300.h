@@ -123,6 +123,15 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value);
  * _computePT reads in place through K_PYTREE::getValueAF
  * (FastS/FastS/Compute/computePT.cpp:140-260). */
 int fgb_upload_state(fgb_solver* s, int zone, int level, const double* host);
+/* As fgb_upload_state, without waiting for the copy: when the host buffer
+ * lies in memory page-locked by fgb_pin_host, the copy runs on a side stream
+ * after the solver's work so far, and the solver stream waits for it before
+ * the level's first use (level n-1 of an implicit step: the balance of the
+ * first sub-step, after its coefficients and face fluxes); every other call
+ * waits for it first.  The buffer must not change until a call that
+ * synchronizes (fgb_synchronize, fgb_download_state).  Other buffers: the
+ * synchronous upload. */
+int fgb_upload_state_async(fgb_solver* s, int zone, int level, const double* host);
 int fgb_download_state(fgb_solver* s, int zone, int level, double* host);
 
 /* Work arrays for inspection: which = "drodm" (NEQ*NDIMDX), "coe"
