@@ -46,13 +46,13 @@ ALG_BYTES = {"residual": 160.0, "lu_sgs": 320.0}
 DRAM_BYTES = {"residual": 497.0, "lu_sgs": 1702.0}
 # FP64 arithmetic instructions per cell and launch group (thread level,
 # DADD + DMUL + DFMA counted by ncu, `smsp__sass_thread_inst_executed_op_d*`,
-# 160^3, first sub-iteration): residual = face_flux i + j + k (205 + 205 + 216)
-# + assemble (80); LU-SGS = lu_gather (87) + lower and upper sweep (297) +
-# lu_newton (35).  The in-place sweeps of later sub-iterations also rebuild
-# the k+1 entries and do the Newton update, so for LU-SGS this is a floor.
-# A DADD or DMUL issues at the DFMA rate, so the instruction peak is half the
-# measured FP64 FMA FLOP rate.
-FP64_INST = {"residual": 507.0, "lu_sgs": 419.0}
+# 160^3, a sub-iteration after the first): residual = face_flux i + j + k
+# (197 + 196 + 197) + assemble (78); LU-SGS = lu_gather (87) + lower and
+# upper sweep (297) + lu_newton (35).  The in-place sweeps of later
+# sub-iterations also rebuild the k+1 entries and do the Newton update, so
+# for LU-SGS this is a floor.  A DADD or DMUL issues at the DFMA rate, so the
+# instruction peak is half the measured FP64 FMA FLOP rate.
+FP64_INST = {"residual": 668.0, "lu_sgs": 419.0}
 
 
 def parse():
