@@ -642,6 +642,10 @@ static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const dou
   z.tcx = ti[0]; z.tcy = tj[0]; z.tcz = p[NEQ_K] > 0 ? tk[0] : 0.;  // a 2-d zone has no tk
   z.si = std::fabs(z.tcx); z.sj = std::fabs(z.tcy); z.sk = std::fabs(z.tcz);
   z.volinv = 0.5 / vol[0];
+  z.ctc2[0] = std::sqrt(z.tcx * z.tcx); z.ctc2[1] = std::sqrt(z.tcy * z.tcy);
+  z.ctc2[2] = std::sqrt(z.tcz * z.tcz);
+  z.cdtv = z.dtc / vol[0];
+  z.rgpgam = z.rgp * z.gam;
   z.prandt = r[PRANDT]; z.xmul0 = r[XMUL0]; z.temp0 = r[TEMP0]; z.cs = r[CS];
   Z.cmus1 = r[CS];
   double temp01 = 1. / r[TEMP0];

@@ -54,6 +54,11 @@ struct Zone {
   double c1, c2, c3, c4, c5, c6, cvisq;
   double c50, c51, c52, c53, c54;   // o5 reconstruction (template_FluxAndBalance.for:149-154)
   double tcx, tcy, tcz, si, sj, sk, volinv;  // 3d cartesian metric
+  // cell-independent terms of a 3d cartesian zone's coefficients (the same
+  // IEEE operations as per cell, evaluated once on the host): sqrt(tc^2) of
+  // each direction and dtc / vol
+  double ctc2[3], cdtv;
+  double rgpgam;   // rgp * gam (the sound speed squared is rgp gam T)
   double prandt, xmul0, temp0, cs;
   const double *ti, *tj, *tk, *vol;
   // Spalart-Allmaras (IFLOW 3, neq 6): Sutherland constants in the form of

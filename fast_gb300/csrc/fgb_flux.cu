@@ -16,6 +16,7 @@
 // The cartesian face kernels are specialised per direction at compile time:
 // products with the zero tangential metric components of a cartesian face are
 // not issued at all, which is exact (they are exact zeros in the general form).
+#include <type_traits>
 #include "fgb_kernels.cuh"
 
 namespace fgb {
@@ -258,7 +259,7 @@ __device__ __forceinline__ void ausm_face(const Zone& z, const double qm[NV], co
     u = mul_pow2<-2>(qn1 + qn2) - z.c2 * s * (p2 - p1) * (z.opt0 * wg + 1. - z.opt0);
     tdu = fmaxF(fabs(u), z.c1 * s) * wg;
   } else {
-    double cc = rgp * z.gam * tl;  // c^2 from the temperature of cell l
+    double cc = z.rgpgam * tl;  // c^2 = (rgp gam) T of cell l
     double son = sqrt(qn1 * qn1 / cc);
     double tam = z.c3 * son + s;
     double tam1 = fmaxF(0., tam) * z.c2;
@@ -774,31 +775,42 @@ __device__ __forceinline__ void assemble_at(const Zone& z, const StageArgs& a, c
     double pr_ = P[l], pu = P[l + nd], pv = P[l + 2 * nd], pw = P[l + 3 * nd], pt = P[l + 4 * nd];
     double mr = M[l], mu = M[l + nd], mv = M[l + 2 * nd], mw = M[l + 3 * nd], mt = M[l + 4 * nd];
     double y[NV];
-    if (a.first_sub) {
-      double c4 = a.c1 + a.c2;
-      y[0] = cf * x[0] + c4 * pr_ + a.c3 * mr;
-      y[1] = cf * x[1] + c4 * pu * pr_ + a.c3 * mu * mr;
-      y[2] = cf * x[2] + c4 * pv * pr_ + a.c3 * mv * mr;
-      y[3] = cf * x[3] + c4 * pw * pr_ + a.c3 * mw * mr;
-      double roe = roe_of(cv, pr_, pu, pv, pw, pt);
-      double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
-      y[4] = cf * x[4] + c4 * roe + a.c3 * roe1;
-      if (NV == 6)   // core3as2.for:97-99
-        y[NV - 1] = cf * x[NV - 1] + c4 * P[l + 5 * nd] * pr_ + a.c3 * M[l + 5 * nd] * mr;
-    } else {
-      double nr = N[l], nu = N[l + nd], nv = N[l + 2 * nd], nw = N[l + 3 * nd], nt = N[l + 4 * nd];
-      y[0] = cf * x[0] + a.c1 * pr_ + a.c2 * nr + a.c3 * mr;
-      y[1] = cf * x[1] + a.c1 * pu * pr_ + a.c2 * nu * nr + a.c3 * mu * mr;
-      y[2] = cf * x[2] + a.c1 * pv * pr_ + a.c2 * nv * nr + a.c3 * mv * mr;
-      y[3] = cf * x[3] + a.c1 * pw * pr_ + a.c2 * nw * nr + a.c3 * mw * mr;
-      double roe = roe_of(cv, pr_, pu, pv, pw, pt);
-      double roen = roe_of(cv, nr, nu, nv, nw, nt);
-      double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
-      y[4] = cf * x[4] + a.c1 * roe + a.c2 * roen + a.c3 * roe1;
-      if (NV == 6)   // core3as2.for:187-190
-        y[NV - 1] = cf * x[NV - 1] + a.c1 * P[l + 5 * nd] * pr_ + a.c2 * N[l + 5 * nd] * nr +
-                    a.c3 * M[l + 5 * nd] * mr;
-    }
+    // BDF2 (c1, c2, c3) = (-1.5, 2, -0.5): the products by c2, c3 and
+    // c1 + c2 = 0.5 are products by powers of two (mul_pow2, the same bits);
+    // other coefficients (BDF1) take the FP64 multiplies
+    auto balance = [&](auto bdf2_tag) {
+      constexpr bool B2 = decltype(bdf2_tag)::value;
+      auto c2m = [&](double v) { return B2 ? mul_pow2<1>(v) : a.c2 * v; };
+      auto c3m = [&](double v) { return B2 ? mul_pow2<-1, true>(v) : a.c3 * v; };
+      if (a.first_sub) {
+        double c4 = a.c1 + a.c2;
+        auto c4m = [&](double v) { return B2 ? mul_pow2<-1>(v) : c4 * v; };
+        y[0] = cf * x[0] + c4m(pr_) + c3m(mr);
+        y[1] = cf * x[1] + c4m(pu) * pr_ + c3m(mu) * mr;
+        y[2] = cf * x[2] + c4m(pv) * pr_ + c3m(mv) * mr;
+        y[3] = cf * x[3] + c4m(pw) * pr_ + c3m(mw) * mr;
+        double roe = roe_of(cv, pr_, pu, pv, pw, pt);
+        double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
+        y[4] = cf * x[4] + c4m(roe) + c3m(roe1);
+        if (NV == 6)   // core3as2.for:97-99
+          y[NV - 1] = cf * x[NV - 1] + c4m(P[l + 5 * nd]) * pr_ + c3m(M[l + 5 * nd]) * mr;
+      } else {
+        double nr = N[l], nu = N[l + nd], nv = N[l + 2 * nd], nw = N[l + 3 * nd], nt = N[l + 4 * nd];
+        y[0] = cf * x[0] + a.c1 * pr_ + c2m(nr) + c3m(mr);
+        y[1] = cf * x[1] + a.c1 * pu * pr_ + c2m(nu) * nr + c3m(mu) * mr;
+        y[2] = cf * x[2] + a.c1 * pv * pr_ + c2m(nv) * nr + c3m(mv) * mr;
+        y[3] = cf * x[3] + a.c1 * pw * pr_ + c2m(nw) * nr + c3m(mw) * mr;
+        double roe = roe_of(cv, pr_, pu, pv, pw, pt);
+        double roen = roe_of(cv, nr, nu, nv, nw, nt);
+        double roe1 = roe_of(cv, mr, mu, mv, mw, mt);
+        y[4] = cf * x[4] + a.c1 * roe + c2m(roen) + c3m(roe1);
+        if (NV == 6)   // core3as2.for:187-190
+          y[NV - 1] = cf * x[NV - 1] + a.c1 * P[l + 5 * nd] * pr_ + c2m(N[l + 5 * nd]) * nr +
+                      c3m(M[l + 5 * nd]) * mr;
+      }
+    };
+    if (a.c1 == -1.5 && a.c2 == 2. && a.c3 == -0.5) balance(std::true_type{});
+    else balance(std::false_type{});
     // core3as2.for 2-d branch: the w residual is left as the balance, and
     // the energies have no w term (w = 0 in a 2-d state: the same values)
     if (z.typ == Z2D) y[3] = x[3];

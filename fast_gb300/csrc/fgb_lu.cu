@@ -50,7 +50,7 @@ __device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a,
   // tstb3_global.for:58-64
   double c1;
   if (z.typ != Z3DCART) c1 = z.dtc / z.vol[indmtr(z, i, j, k)];
-  else c1 = z.dtc / z.vol[0];
+  else c1 = z.cdtv;   // dtc / vol[0], once per zone
   a.coe[l] = c1;
   if (!a.do_lu) return;
   // tstb3c.for
@@ -70,7 +70,7 @@ __device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a,
     double volu = detj * rr;
     double xmvis = vmu / volu;
     double tcxi = z.ti[0], tcyj = z.tj[0], tczk = z.tk[0];
-    double tc2i = sqrt(tcxi * tcxi), tc2j = sqrt(tcyj * tcyj), tc2k = sqrt(tczk * tczk);
+    const double tc2i = z.ctc2[0], tc2j = z.ctc2[1], tc2k = z.ctc2[2];   // sqrt(tc^2), once per zone
     double vmi = fabs(tcxi * u) + c * tc2i;
     c2 = mul_pow2<1>(vmi) + mul_pow2<2>(xmvis * tc2i * tc2i);
     double vmj = fabs(tcyj * v) + c * tc2j;
