@@ -645,6 +645,7 @@ static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const dou
   z.ctc2[0] = std::sqrt(z.tcx * z.tcx); z.ctc2[1] = std::sqrt(z.tcy * z.tcy);
   z.ctc2[2] = std::sqrt(z.tcz * z.tcz);
   z.cdtv = z.dtc / vol[0];
+  z.ctcg[0] = z.tcx * (z.gam - 1.); z.ctcg[1] = z.tcy * (z.gam - 1.); z.ctcg[2] = z.tcz * (z.gam - 1.);
   z.rgpgam = z.rgp * z.gam;
   z.prandt = r[PRANDT]; z.xmul0 = r[XMUL0]; z.temp0 = r[TEMP0]; z.cs = r[CS];
   Z.cmus1 = r[CS];

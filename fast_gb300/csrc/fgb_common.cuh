@@ -58,6 +58,7 @@ struct Zone {
   // IEEE operations as per cell, evaluated once on the host): sqrt(tc^2) of
   // each direction and dtc / vol
   double ctc2[3], cdtv;
+  double ctcg[3];  // tc_d (gam - 1) of each direction (LU-SGS B entries)
   double rgpgam;   // rgp * gam (the sound speed squared is rgp gam T)
   double prandt, xmul0, temp0, cs;
   const double *ti, *tj, *tk, *vol;

@@ -324,24 +324,27 @@ __device__ __forceinline__ T qn_entry(const T* e) {
 // b = B . o from the stored entries (cs = coe_{d+2}(nb) * signe)
 template <int TYP, int D, typename T>
 __device__ __forceinline__ void bmatvec(const Zone& z, const T* e, T cs, const T o[5], T b[5]) {
-  const T gamm1 = T(z.gam - 1.);
+  // cartesian: tc_D (gam - 1), a zone constant (FP64: evaluated once on the host)
+  auto tcg = [&](double tc) -> T {
+    return sizeof(T) == 8 ? T(z.ctcg[D]) : T(tc) * T(z.gam - 1.);
+  };
   if (TYP == Z3DCART) {
     if (D == 0) {
-      const T tcx = T(z.tcx), b25 = tcx * gamm1;
+      const T tcx = T(z.tcx), b25 = tcg(z.tcx);
       b[0] = cs * o[0] + tcx * o[1];
       b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[2] + e[3] * o[3] + b25 * o[4];
       b[2] = e[4] * o[0] + e[5] * o[1] + ((e[6]) + cs) * o[2];
       b[3] = e[7] * o[0] + e[8] * o[1] + ((e[6]) + cs) * o[3];
       b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
     } else if (D == 1) {
-      const T tcy = T(z.tcy), b35 = tcy * gamm1;
+      const T tcy = T(z.tcy), b35 = tcg(z.tcy);
       b[0] = cs * o[0] + tcy * o[2];
       b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[2];
       b[2] = e[3] * o[0] + e[4] * o[1] + (e[5] + cs) * o[2] + e[6] * o[3] + b35 * o[4];
       b[3] = e[7] * o[0] + e[8] * o[2] + ((e[1]) + cs) * o[3];
       b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
     } else {
-      const T tcz = T(z.tcz), b45 = tcz * gamm1;
+      const T tcz = T(z.tcz), b45 = tcg(z.tcz);
       b[0] = cs * o[0] + tcz * o[3];
       b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[3];
       b[2] = e[3] * o[0] + (e[1] + cs) * o[2] + e[4] * o[3];
@@ -373,7 +376,7 @@ template <int D> struct DirT { static constexpr int value = D; };
 // consecutive cells of a plane, and on their neighbours in the previous
 // plane, then reads a few contiguous spans instead of one scattered word per
 // array (which thrashed the TLB and sector caches).
-//   rec[g] : coe1, 1/coe5, coe5, coe6 (SA), coe_{2..4}, W^p (5), B entries (3 x NB)
+//   rec[g] : coe1 / 2, 1/coe5, coe5, coe6 (SA), coe_{2..4} / 2, W^p (5), B entries (3 x NB)
 //   dio[g] : residual in / increment out (5 words, 6 with SA, stride 6)
 //   nst[g] : in-place upper sweep: W^{p+1} u, v, w, T (stride 4)
 template <int TYP, typename T> struct Rec {
@@ -506,12 +509,14 @@ __global__ void __launch_bounds__(GT_N) lu_gather(Zone z, LuFields f, PlaneData<
     for (int v = 0; v < NV; v++) x[v] = T(f.din[l + v * nd]);
     T r[R::SIZE];
     const T c5 = T(f.coe[l + 4 * nd]);
-    r[R::COE1] = T(f.coe[l]);
+    // coe1 and coe_{d+2} halved here, off the sweeps' critical path: the
+    // sweeps use coe * (+-0.5), and x * -0.5 = -(x * 0.5) exactly
+    r[R::COE1] = T(f.coe[l]) * T(0.5);
     r[R::DIAG] = T(1.) / c5;
     r[R::COE5] = c5;
     r[R::COE6] = NV == 6 ? T(f.coe[l + 5 * nd]) : T(0);
 #pragma unroll
-    for (int d = 0; d < 3; d++) r[R::COEN + d] = T(f.coe[l + (d + 1) * nd]);
+    for (int d = 0; d < 3; d++) r[R::COEN + d] = T(f.coe[l + (d + 1) * nd]) * T(0.5);
 #pragma unroll
     for (int v = 0; v < 5; v++) r[R::ST + v] = T(f.rop_old[l + v * nd]);
 #pragma unroll
@@ -626,18 +631,18 @@ __device__ __forceinline__ void load_ops(const PlaneData<T>& p, bool inplace, in
 #pragma unroll
     for (int v = 0; v < 5; v++) o.x[v] = o.x[v] * dg;
     if (NV == 6) o.x[NV - 1] = o.x[NV - 1] * o.c6;   // lu_d_SA.for
-    o.xal = me[R::COE1] * T(-0.5);
+    o.xal = -me[R::COE1];
 #pragma unroll
     for (int v = 0; v < 5; v++) o.st[v] = me[R::ST + v];
   } else {
-    o.xal = me[R::COE1] * T(0.5);
+    o.xal = me[R::COE1];
   }
   o.diag = me[R::DIAG];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     if (o.n[d] < 0) continue;
     const T* rn = p.rec + (int64_t)o.n[d] * R::SIZE;
-    o.cs[d] = rn[R::COEN + d] * T(UPPER ? -0.5 : 0.5);
+    o.cs[d] = UPPER ? -rn[R::COEN + d] : rn[R::COEN + d];
     if (CellOps<TYP, T, NV>::HOLD_W && !(UPPER && d == 2 && inplace)) {
 #pragma unroll
       for (int m = 0; m < CellOps<TYP, T, NV>::NW; m++) o.wn[d][m] = rn[R::ST + 1 + m];
