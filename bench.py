@@ -39,20 +39,21 @@ UNIT = "Mcell-updates/s"
 ALG_BYTES = {"residual": 160.0, "lu_sgs": 320.0}
 # DRAM bytes per cell and launch group measured with ncu (dram__bytes_read.sum
 # + dram__bytes_write.sum of every kernel of the group, one sub-iteration of
-# the 160^3 case, FP64): LU-SGS = lu_gather (2.49 GB) + lusgs_persistent
-# (4.48 GB) over 4.10 M cells; the plane-ordered records are written once
-# and read by both sweeps, so the traffic scales with the cell count.
-# residual = three face_flux launches (1.01 GB) + assemble (1.03 GB).
-DRAM_BYTES = {"residual": 497.0, "lu_sgs": 1702.0}
+# the 160^3 case, FP64): LU-SGS = lu_gather (2.75 GB) + the dataflow sweep
+# with one CTA per SM (5.05 GB) over 4.10 M cells; the plane-ordered records
+# (64 words a cell) are written once and read by both sweeps, so the traffic
+# scales with the cell count.  residual = three face_flux launches
+# (1.01 GB) + assemble (1.03 GB).
+DRAM_BYTES = {"residual": 497.0, "lu_sgs": 1904.0}
 # FP64 arithmetic instructions per cell and launch group (thread level,
 # DADD + DMUL + DFMA counted by ncu, `smsp__sass_thread_inst_executed_op_d*`,
 # 160^3, a sub-iteration after the first): residual = face_flux i + j + k
-# (197 + 196 + 197) + assemble (78); LU-SGS = lu_gather (87) + lower and
-# upper sweep (297) + lu_newton (35).  The in-place sweeps of later
+# (197 + 196 + 197) + assemble (78); LU-SGS = lu_gather (109) + lower and
+# upper sweep (260) + lu_newton (35).  The in-place sweeps of later
 # sub-iterations also rebuild the k+1 entries and do the Newton update, so
 # for LU-SGS this is a floor.  A DADD or DMUL issues at the DFMA rate, so the
 # instruction peak is half the measured FP64 FMA FLOP rate.
-FP64_INST = {"residual": 668.0, "lu_sgs": 419.0}
+FP64_INST = {"residual": 668.0, "lu_sgs": 404.0}
 
 
 def parse():

@@ -266,6 +266,23 @@ constexpr int NB_CART = 14;   // entries per direction, 3d cartesian zone
 constexpr int NB_FULL = 25;   // entries per direction, 3d general zone
 constexpr int QN_FULL = 23;   // general layout: qn (entries 0..22 are the B matrix)
 template <int TYP> struct NBE { static constexpr int n = TYP == Z3DCART ? NB_CART : NB_FULL; };
+// Entries that the sweeps only use as (entry + cs), cs = coe_{d+2}(nb) * signe:
+// the diagonal of B and qn (the Spalart-Allmaras row).  The stored table
+// holds them with the lower sweep's cs added (in place) and, after the NB
+// entries, with the upper sweep's (-cs), so the sweeps do not add them.
+constexpr int NS_CART = 3, NS_FULL = 5;
+template <int TYP> struct NSE { static constexpr int n = TYP == Z3DCART ? NS_CART : NS_FULL; };
+template <int TYP>
+__host__ __device__ constexpr int sum_index(int d, int m) {
+  // cartesian: direction 0 {b22, b33 = b44 = qn, b55}, 1 {b22 = b44 = qn, b33,
+  // b55}, 2 {b22 = b33 = qn, b44, b55}; general: b22, b33, b44, b55, qn
+  return TYP == Z3DCART ? (m == 2 ? 13 : (m == 0 ? 1 : (d == 0 ? 6 : (d == 1 ? 5 : 8))))
+                        : (m == 0 ? 4 : (m == 1 ? 10 : (m == 2 ? 16 : (m == 3 ? 22 : QN_FULL))));
+}
+template <int TYP, int D>
+__host__ __device__ constexpr int qn_slot() {   // the slot of qn + cs
+  return TYP == Z3DCART ? (D == 0 ? 1 : 0) : 4;
+}
 // 2-d zones use the general entries with tz = 0 and w = 0 (lu_{i,j}_2d.for
 // is lu_{i,j}_3dfull.for without the w / tz terms, which vanish exactly)
 
@@ -313,56 +330,59 @@ __device__ __forceinline__ void bentries(const Zone& z, int d, T u, T v, T w, T 
   }
 }
 
-// the normal velocity qn of the entries of direction D (the B_66 entry of
-// the Spalart-Allmaras row is qn + cs, LU/lu_*_SA.for)
-template <int TYP, int D, typename T>
-__device__ __forceinline__ T qn_entry(const T* e) {
-  if (TYP == Z3DCART) return D == 0 ? e[6] : e[1];
-  return e[QN_FULL];
-}
 
-// b = B . o from the stored entries (cs = coe_{d+2}(nb) * signe)
-template <int TYP, int D, typename T>
+// b = B . o from the entries e (cs = coe_{d+2}(nb) * signe).  MODE 0: raw
+// entries (the sums formed here); 1: a stored table, lower sweep (sums in
+// place); 2: a stored table, upper sweep (sums after the NB entries).
+template <int TYP, int D, typename T, int MODE>
+__device__ __forceinline__ T bsum(const T* e, T cs, int idx, int slot) {
+  return MODE == 0 ? e[idx] + cs : (MODE == 1 ? e[idx] : e[NBE<TYP>::n + slot]);
+}
+template <int TYP, int D, typename T, int MODE>
 __device__ __forceinline__ void bmatvec(const Zone& z, const T* e, T cs, const T o[5], T b[5]) {
   // cartesian: tc_D (gam - 1), a zone constant (FP64: evaluated once on the host)
   auto tcg = [&](double tc) -> T {
     return sizeof(T) == 8 ? T(z.ctcg[D]) : T(tc) * T(z.gam - 1.);
   };
+  auto S = [&](int m) { return bsum<TYP, D, T, MODE>(e, cs, sum_index<TYP>(D, m), m); };
   if (TYP == Z3DCART) {
     if (D == 0) {
       const T tcx = T(z.tcx), b25 = tcg(z.tcx);
+      const T s22 = S(0), s33 = S(1), s55 = S(2);
       b[0] = cs * o[0] + tcx * o[1];
-      b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[2] + e[3] * o[3] + b25 * o[4];
-      b[2] = e[4] * o[0] + e[5] * o[1] + ((e[6]) + cs) * o[2];
-      b[3] = e[7] * o[0] + e[8] * o[1] + ((e[6]) + cs) * o[3];
-      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
+      b[1] = e[0] * o[0] + s22 * o[1] + e[2] * o[2] + e[3] * o[3] + b25 * o[4];
+      b[2] = e[4] * o[0] + e[5] * o[1] + s33 * o[2];
+      b[3] = e[7] * o[0] + e[8] * o[1] + s33 * o[3];
+      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + s55 * o[4];
     } else if (D == 1) {
       const T tcy = T(z.tcy), b35 = tcg(z.tcy);
+      const T s22 = S(0), s33 = S(1), s55 = S(2);
       b[0] = cs * o[0] + tcy * o[2];
-      b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[2];
-      b[2] = e[3] * o[0] + e[4] * o[1] + (e[5] + cs) * o[2] + e[6] * o[3] + b35 * o[4];
-      b[3] = e[7] * o[0] + e[8] * o[2] + ((e[1]) + cs) * o[3];
-      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
+      b[1] = e[0] * o[0] + s22 * o[1] + e[2] * o[2];
+      b[2] = e[3] * o[0] + e[4] * o[1] + s33 * o[2] + e[6] * o[3] + b35 * o[4];
+      b[3] = e[7] * o[0] + e[8] * o[2] + s22 * o[3];
+      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + s55 * o[4];
     } else {
       const T tcz = T(z.tcz), b45 = tcg(z.tcz);
+      const T s22 = S(0), s44 = S(1), s55 = S(2);
       b[0] = cs * o[0] + tcz * o[3];
-      b[1] = e[0] * o[0] + (e[1] + cs) * o[1] + e[2] * o[3];
-      b[2] = e[3] * o[0] + (e[1] + cs) * o[2] + e[4] * o[3];
-      b[3] = e[5] * o[0] + e[6] * o[1] + e[7] * o[2] + (e[8] + cs) * o[3] + b45 * o[4];
-      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + (e[13] + cs) * o[4];
+      b[1] = e[0] * o[0] + s22 * o[1] + e[2] * o[3];
+      b[2] = e[3] * o[0] + s22 * o[2] + e[4] * o[3];
+      b[3] = e[5] * o[0] + e[6] * o[1] + e[7] * o[2] + s44 * o[3] + b45 * o[4];
+      b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + s55 * o[4];
     }
   } else if (TYP == Z2D) {   // lu_{i,j}_2d.for: no w row
     b[0] = cs * o[0] + e[0] * o[1] + e[1] * o[2];
-    b[1] = e[3] * o[0] + (e[4] + cs) * o[1] + e[5] * o[2] + e[7] * o[4];
-    b[2] = e[8] * o[0] + e[9] * o[1] + (e[10] + cs) * o[2] + e[12] * o[4];
+    b[1] = e[3] * o[0] + S(0) * o[1] + e[5] * o[2] + e[7] * o[4];
+    b[2] = e[8] * o[0] + e[9] * o[1] + S(1) * o[2] + e[12] * o[4];
     b[3] = T(0);
-    b[4] = e[18] * o[0] + e[19] * o[1] + e[20] * o[2] + (e[22] + cs) * o[4];
+    b[4] = e[18] * o[0] + e[19] * o[1] + e[20] * o[2] + S(3) * o[4];
   } else {
     b[0] = cs * o[0] + e[0] * o[1] + e[1] * o[2] + e[2] * o[3];
-    b[1] = e[3] * o[0] + (e[4] + cs) * o[1] + e[5] * o[2] + e[6] * o[3] + e[7] * o[4];
-    b[2] = e[8] * o[0] + e[9] * o[1] + (e[10] + cs) * o[2] + e[11] * o[3] + e[12] * o[4];
-    b[3] = e[13] * o[0] + e[14] * o[1] + e[15] * o[2] + (e[16] + cs) * o[3] + e[17] * o[4];
-    b[4] = e[18] * o[0] + e[19] * o[1] + e[20] * o[2] + e[21] * o[3] + (e[22] + cs) * o[4];
+    b[1] = e[3] * o[0] + S(0) * o[1] + e[5] * o[2] + e[6] * o[3] + e[7] * o[4];
+    b[2] = e[8] * o[0] + e[9] * o[1] + S(1) * o[2] + e[11] * o[3] + e[12] * o[4];
+    b[3] = e[13] * o[0] + e[14] * o[1] + e[15] * o[2] + S(2) * o[3] + e[17] * o[4];
+    b[4] = e[18] * o[0] + e[19] * o[1] + e[20] * o[2] + e[21] * o[3] + S(3) * o[4];
   }
 }
 
@@ -376,7 +396,8 @@ template <int D> struct DirT { static constexpr int value = D; };
 // consecutive cells of a plane, and on their neighbours in the previous
 // plane, then reads a few contiguous spans instead of one scattered word per
 // array (which thrashed the TLB and sector caches).
-//   rec[g] : coe1 / 2, 1/coe5, coe5, coe6 (SA), coe_{2..4} / 2, W^p (5), B entries (3 x NB)
+//   rec[g] : coe1 / 2, 1/coe5, coe5, coe6 (SA), coe_{2..4} / 2, W^p (5), B entries
+//            (3 x NBS: NB entries with the lower sweep's sums, the upper sums)
 //   dio[g] : residual in / increment out (5 words, 6 with SA, stride 6)
 //   nst[g] : in-place upper sweep: W^{p+1} u, v, w, T (stride 4)
 template <int TYP, typename T> struct Rec {
@@ -385,8 +406,9 @@ template <int TYP, typename T> struct Rec {
   // float inputs as the pre-pass, so the same values, in 12 words a cell.
   static constexpr bool HAS_B = !(TYP == Z3DCART && sizeof(T) == 4);
   static constexpr int NB = NBE<TYP>::n;
+  static constexpr int NBS = NB + NSE<TYP>::n;   // per direction: entries, then upper sums
   static constexpr int COE1 = 0, DIAG = 1, COE5 = 2, COE6 = 3, COEN = 4, ST = 7, B = 12;
-  static constexpr int SIZE = HAS_B ? ((B + 3 * NB) + 3) / 4 * 4 : B;   // whole 16-byte vectors
+  static constexpr int SIZE = HAS_B ? ((B + 3 * NBS) + 3) / 4 * 4 : B;   // whole 16-byte vectors
 };
 constexpr int DIO = 6;
 
@@ -526,8 +548,16 @@ __global__ void __launch_bounds__(GT_N) lu_gather(Zone z, LuFields f, PlaneData<
       for (int d = 0; d < 3; d++) {
         T tx, ty, tz;
         nb_normal<TYP, T>(z, d, lt, lt + z.minc[d], tx, ty, tz);
-        bentries<TYP, T>(z, d, r[R::ST + 1], r[R::ST + 2], r[R::ST + 3], r[R::ST + 4], tx, ty, tz,
-                         r + R::B + d * R::NB);
+        T* e = r + R::B + d * R::NBS;
+        bentries<TYP, T>(z, d, r[R::ST + 1], r[R::ST + 2], r[R::ST + 3], r[R::ST + 4], tx, ty, tz, e);
+        // the sums the sweeps use: entry + cs (lower), entry + (-cs) (upper)
+        const T cs = r[R::COEN + d];
+#pragma unroll
+        for (int m = 0; m < NSE<TYP>::n; m++) {
+          const int idx = sum_index<TYP>(d, m);
+          e[R::NB + m] = e[idx] + (-cs);
+          e[idx] = e[idx] + cs;
+        }
       }
     }
     s_g[q] = f.posmap[l];
@@ -668,7 +698,7 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
     const int32_t n = o.n[D];
     if (n < 0) return;
     load_dio<NV>(p.dio, n, od);
-    T qn = T(0);   // SA row: normal velocity of the neighbour
+    T qcs = T(0);   // SA row: qn + cs of the neighbour
     if (fresh) {  // k+1 neighbour updated in place: B from its new state
       T e[NB];
       const T* q = p.nst + (int64_t)n * 4;
@@ -683,8 +713,8 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
         nb_normal<TYP, T>(z, D, lt, lt + z.minc[D], tx, ty, tz);
       }
       bentries<TYP, T>(z, D, u, vv, w, t, tx, ty, tz, e);
-      bmatvec<TYP, D, T>(z, e, o.cs[D], od, b);
-      if (NV == 6) qn = qn_entry<TYP, D, T>(e);
+      bmatvec<TYP, D, T, 0>(z, e, o.cs[D], od, b);
+      if (NV == 6) qcs = bsum<TYP, D, T, 0>(e, o.cs[D], sum_index<TYP>(D, qn_slot<TYP, D>()), 0);
     } else if (C::HOLD_W) {  // cartesian: B from the held state
       T e[NB];
       T tx, ty, tz;
@@ -692,17 +722,19 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
       bentries<TYP, T>(z, D, o.wn[D][0], o.wn[D][C::NW > 1 ? 1 : 0],
                        o.wn[D][C::NW > 2 ? 2 : 0], o.wn[D][C::NW > 3 ? 3 : 0],
                        tx, ty, tz, e);
-      bmatvec<TYP, D, T>(z, e, o.cs[D], od, b);
-      if (NV == 6) qn = qn_entry<TYP, D, T>(e);
+      bmatvec<TYP, D, T, 0>(z, e, o.cs[D], od, b);
+      if (NV == 6) qcs = bsum<TYP, D, T, 0>(e, o.cs[D], sum_index<TYP>(D, qn_slot<TYP, D>()), 0);
     } else {
-      const T* e = p.rec + (int64_t)n * R::SIZE + R::B + D * NB;
-      bmatvec<TYP, D, T>(z, e, o.cs[D], od, b);
-      if (NV == 6) qn = qn_entry<TYP, D, T>(e);
+      constexpr int MODE = UPPER ? 2 : 1;
+      const T* e = p.rec + (int64_t)n * R::SIZE + R::B + D * R::NBS;
+      bmatvec<TYP, D, T, MODE>(z, e, o.cs[D], od, b);
+      if (NV == 6)
+        qcs = bsum<TYP, D, T, MODE>(e, o.cs[D], sum_index<TYP>(D, qn_slot<TYP, D>()), qn_slot<TYP, D>());
     }
 #pragma unroll
     for (int v = 0; v < 5; v++) x[v] = x[v] + b[v] * o.xal;
     if (NV == 6) {   // lu_*_SA.for: b6 = (qn + coe_{d+2}(nb) signe) dW6_nb
-      const T b6 = (qn + o.cs[D]) * od[NV - 1];
+      const T b6 = qcs * od[NV - 1];
       x[NV - 1] = x[NV - 1] + b6 * o.xal;
     }
   };
