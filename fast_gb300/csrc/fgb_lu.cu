@@ -646,21 +646,31 @@ struct CellOps {
   T st[5];        // upper: W^p of the cell (in-place Newton)
 };
 
+// upper sweep: the cell's own lower result times coe5 (lu_d.for; x coe6 for SA)
+template <int TYP, typename T, int NV>
+__device__ __forceinline__ void load_x_upper(const PlaneData<T>& p, int64_t g, CellOps<TYP, T, NV>& o) {
+  using R = Rec<TYP, T>;
+  load_dio<NV>(p.dio, g, o.x);
+  const T dg = p.rec[g * R::SIZE + R::COE5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) o.x[v] = o.x[v] * dg;
+  if (NV == 6) o.x[NV - 1] = o.x[NV - 1] * o.c6;   // lu_d_SA.for
+}
+
+// with_x false: everything but the upper sweep's own lower result (which
+// the caller loads after waiting for it, load_x_upper)
 template <int TYP, typename T, bool UPPER, int NV>
 __device__ __forceinline__ void load_ops(const PlaneData<T>& p, bool inplace, int64_t g,
-                                         CellOps<TYP, T, NV>& o) {
+                                         CellOps<TYP, T, NV>& o, bool with_x = true) {
   using R = Rec<TYP, T>;
   const T* me = p.rec + g * R::SIZE;
   const int32_t* nbt = UPPER ? p.nbu : p.nbl;
 #pragma unroll
   for (int d = 0; d < 3; d++) o.n[d] = nbt[d * p.G + g];
-  load_dio<NV>(p.dio, g, o.x);
+  if (!UPPER) load_dio<NV>(p.dio, g, o.x);
   if (NV == 6) o.c6 = me[R::COE6];
   if (UPPER) {
-    const T dg = me[R::COE5];
-#pragma unroll
-    for (int v = 0; v < 5; v++) o.x[v] = o.x[v] * dg;
-    if (NV == 6) o.x[NV - 1] = o.x[NV - 1] * o.c6;   // lu_d_SA.for
+    if (with_x) load_x_upper<TYP, T, NV>(p, g, o);
     o.xal = -me[R::COE1];
 #pragma unroll
     for (int v = 0; v < 5; v++) o.st[v] = me[R::ST + v];
@@ -977,6 +987,26 @@ __device__ __forceinline__ void flow_chunk(const Zone& z, const PlaneData<T>& p,
   }
 }
 
+// FP32 sweeps (bound by the latency of the hyperplane chain, not by
+// arithmetic): the chunk's static operands -- its records, its neighbours'
+// coefficients and held states, its residual -- are loaded before the
+// dependency wait, so that only the neighbours' increments (and, upper, the
+// cell's own lower result) are read after it.  (FP64 sweeps load them after
+// the wait: held across it they cost registers the FP64 sweep needs.)
+template <int TYP, typename T, int NV, bool MULTI, bool UPPER>
+__device__ __forceinline__ void flow_pre(const PlaneData<T>& p, const LuFields& f, int64_t g0,
+                                         int64_t n, int lane, CellOps<TYP, T, NV>& o) {
+  if (lane < n) load_ops<TYP, T, UPPER, NV>(p, f.inplace != 0, g0 + lane, o, false);
+}
+template <int TYP, typename T, int NV, bool MULTI, bool UPPER>
+__device__ __forceinline__ void flow_run(const Zone& z, const PlaneData<T>& p, const LuFields& f,
+                                         int64_t g0, int64_t n, int lane, CellOps<TYP, T, NV>& o) {
+  if (lane < n) {
+    if (UPPER) load_x_upper<TYP, T, NV>(p, g0 + lane, o);
+    run_cell_of<TYP, T, UPPER, NV, MULTI>(z, p, f, g0 + lane, o);
+  }
+}
+
 template <int TYP, typename T, int NV, bool MULTI>
 __global__ void __launch_bounds__(FLOW_THREADS)
     lusgs_flow(Zone z, PlaneData<T> p, LuFields f, FlowArgs a) {
@@ -997,13 +1027,24 @@ __global__ void __launch_bounds__(FLOW_THREADS)
     const int64_t g0 = p.plane[s] + (ch - a.cbase[s]) * FLOW_CHUNK;
     const int64_t n = p.plane[s + 1] - g0;
     if (a.prefetch) prefetch_chunk<TYP, T>(p, g0, n < FLOW_CHUNK ? n : FLOW_CHUNK, upper, lane);
+    constexpr bool PRE = sizeof(T) == 4;
+    CellOps<TYP, T, NV> o;
+    if (PRE) {
+      if (upper) flow_pre<TYP, T, NV, MULTI, true>(p, f, g0, n, lane, o);
+      else flow_pre<TYP, T, NV, MULTI, false>(p, f, g0, n, lane, o);
+    }
     bool ok = true;
     for (int64_t m = lane; m < n1 + n2; m += 32)
       ok = ok && flow_poll(a, m < n1 ? lo1 + m : lo2 + (m - n1), mark + a.wait_skew);
     if (upper && lane == 0) ok = ok && flow_poll(a, ch, a.lower_mark + a.wait_skew);
     if (!__all_sync(0xffffffffu, ok)) return;
-    if (upper) flow_chunk<TYP, T, NV, MULTI, true>(z, p, f, g0, n, lane);
-    else flow_chunk<TYP, T, NV, MULTI, false>(z, p, f, g0, n, lane);
+    if (PRE) {
+      if (upper) flow_run<TYP, T, NV, MULTI, true>(z, p, f, g0, n, lane, o);
+      else flow_run<TYP, T, NV, MULTI, false>(z, p, f, g0, n, lane, o);
+    } else {
+      if (upper) flow_chunk<TYP, T, NV, MULTI, true>(z, p, f, g0, n, lane);
+      else flow_chunk<TYP, T, NV, MULTI, false>(z, p, f, g0, n, lane);
+    }
     __syncwarp();
     if (lane == 0)
       asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(a.flag + ch), "r"(mark) : "memory");
