@@ -647,6 +647,7 @@ static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const dou
   z.cdtv = z.dtc / vol[0];
   z.ctcg[0] = z.tcx * (z.gam - 1.); z.ctcg[1] = z.tcy * (z.gam - 1.); z.ctcg[2] = z.tcz * (z.gam - 1.);
   z.rgpgam = z.rgp * z.gam;
+  z.cfl = r[CFL];
   z.prandt = r[PRANDT]; z.xmul0 = r[XMUL0]; z.temp0 = r[TEMP0]; z.cs = r[CS];
   Z.cmus1 = r[CS];
   double temp01 = 1. / r[TEMP0];
@@ -791,8 +792,10 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   if (p[ITYPCP] <= 1 && (p[NB_RELAX] > 1 || p[LU_MATCH] != 0))
     return fail(FGB_ERR_ARG, "only nb_relax=1, lu_match=0 LU-SGS is supported");
   if (p[ITYPCP] > 1 && p[RK] != 3) return fail(FGB_ERR_ARG, "explicit path needs rk=3");
-  if (p[EXPLOC] != 0 || p[DTLOC] != 0 || p[LALE] != 0)
-    return fail(FGB_ERR_ARG, "local time stepping and moving meshes are not supported");
+  if (p[EXPLOC] != 0 || p[LALE] != 0)
+    return fail(FGB_ERR_ARG, "explicit local time stepping and moving meshes are not supported");
+  if (p[DTLOC] != 0 && (p[DTLOC] != 1 || p[ITYPCP] > 1))   // cptst3.for: tstb3_impli
+    return fail(FGB_ERR_ARG, "a local time step (time_step_nature 'local') needs an implicit scheme");
   int64_t nd = p[NDIMDX], neq = p[NEQ], ndm = p[NDIMDX_MTR];
   // metric components per face family: NEQ_IJ for ti / tj, NEQ_K for tk
   // (3d cartesian 1 / 1, 3d general 3 / 3, 2d 2 / 0 -- a 2-d zone has no tk)

@@ -27,7 +27,7 @@ enum PI : int {
 };
 enum PR : int {
   DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6, MINF = 7,
-  RONUTILDEINF = 8, PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14,
+  RONUTILDEINF = 8, PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14, CFL = 15,
   SA_RATIOM = 18, VXINF = 19, VYINF = 20, VZINF = 21, PSIROE = 34, PRANDT_TUR = 38, WIG_AMP = 72
 };
 enum PI_SA : int { SA_LOW_RE = 130, SA_ROT_CORR = 131 };
@@ -60,6 +60,7 @@ struct Zone {
   double ctc2[3], cdtv;
   double ctcg[3];  // tc_d (gam - 1) of each direction (LU-SGS B entries)
   double rgpgam;   // rgp * gam (the sound speed squared is rgp gam T)
+  double cfl;      // CFL number of the local time step (DTLOC = 1)
   double prandt, xmul0, temp0, cs;
   const double *ti, *tj, *tk, *vol;
   // Spalart-Allmaras (IFLOW 3, neq 6): Sutherland constants in the form of

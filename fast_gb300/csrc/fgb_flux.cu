@@ -782,7 +782,10 @@ __device__ __forceinline__ void assemble_at(const Zone& z, const StageArgs& a, c
       constexpr bool B2 = decltype(bdf2_tag)::value;
       auto c2m = [&](double v) { return B2 ? mul_pow2<1>(v) : a.c2 * v; };
       auto c3m = [&](double v) { return B2 ? mul_pow2<-1, true>(v) : a.c3 * v; };
-      if (a.first_sub) {
+      if (a.first_sub && NV == 6 && z.dtloc == 1) {   // core3as2.for:57-66, 106-114
+#pragma unroll
+        for (int v = 0; v < NV; v++) y[v] = cf * x[v];
+      } else if (a.first_sub) {
         double c4 = a.c1 + a.c2;
         auto c4m = [&](double v) { return B2 ? mul_pow2<-1>(v) : c4 * v; };
         y[0] = cf * x[0] + c4m(pr_) + c3m(mr);

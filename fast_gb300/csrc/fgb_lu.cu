@@ -20,6 +20,80 @@
 namespace fgb {
 
 // ----------------------------------------------------------- coefficients
+// tstb3_impli.for with dtloc.for (implicit, local time step, DTLOC = 1): the
+// spectral radii coe2..4 as tstb3c.for forms them, then coe1 = CFL x
+// min(dtconv, dtvis) per cell (d = 1 / sum tc2^2, dtvis = 0.5 detj d / gam1
+// / xmut ro, dtconv = sqrt(d) / (|u| + c)) and coe5 = 1 + coe1 sum / 2.
+// Euler: gam1 = 1e-30 (tstb3c.for takes 0); volume floor 1e-30.
+__device__ __forceinline__ void coefficients_local(const Zone& z, const CoeArgs& a, int64_t l,
+                                                   int64_t i, int64_t j, int64_t k, double xm) {
+  const int64_t nd = z.nd;
+  const double* R = a.rop;
+  const double cut0x = 1e-30;
+  const double gamma = z.gam;
+  const double rgp = z.cv * (gamma - 1.);
+  double gam1 = gamma / z.prandt;
+  if (z.iflow == 1) gam1 = cut0x;
+  const double gam1_1 = 1. / gam1;
+  const double gam2 = gamma * rgp;
+  const double r = R[l], u = R[l + nd], v = R[l + 2 * nd], w = z.typ == Z2D ? 0. : R[l + 3 * nd];
+  const double c = sqrt(gam2 * R[l + 4 * nd]);
+  const double vmu = gam1 * xm;
+  double tc2[3], cc[3], detj;
+  if (z.typ == Z3DCART) {
+    detj = fmaxF(z.vol[0], cut0x);
+    const double xmvis = vmu / (detj * r);
+    const double tc[3] = {z.ti[0], z.tj[0], z.tk[0]}, q[3] = {u, v, w};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      tc2[d] = z.ctc2[d];   // sqrt(tc^2), once per zone
+      const double vm = fabs(tc[d] * q[d]) + c * tc2[d];
+      cc[d] = mul_pow2<1>(vm) + mul_pow2<2>(xmvis * tc2[d] * tc2[d]);
+    }
+  } else {
+    const int64_t lt = indmtr(z, i, j, k), m = z.ndm;
+    detj = fmaxF(z.vol[lt], cut0x);
+    const double xmvis = vmu / (detj * r);
+    const double* T3[3] = {z.ti, z.tj, z.tk};
+    const int nd3 = z.typ == Z2D ? 2 : 3;
+    tc2[2] = 0.; cc[2] = 0.;
+    for (int d = 0; d < nd3; d++) {
+      const double* T = T3[d];
+      const int64_t l2 = lt + z.minc[d];
+      const double tx = mul_pow2<-1>(T[lt] + T[l2]);
+      const double ty = mul_pow2<-1>(T[lt + m] + T[l2 + m]);
+      double qn;
+      if (z.typ == Z2D) {
+        tc2[d] = mul_pow2<-1>(sqrt(T[lt] * T[lt] + T[lt + m] * T[lt + m]) +
+                              sqrt(T[l2] * T[l2] + T[l2 + m] * T[l2 + m]));
+        qn = tx * u + ty * v;
+      } else {
+        const double tz = mul_pow2<-1>(T[lt + 2 * m] + T[l2 + 2 * m]);
+        tc2[d] = mul_pow2<-1>(sqrt(T[lt] * T[lt] + T[lt + m] * T[lt + m] + T[lt + 2 * m] * T[lt + 2 * m]) +
+                              sqrt(T[l2] * T[l2] + T[l2 + m] * T[l2 + m] + T[l2 + 2 * m] * T[l2 + 2 * m]));
+        qn = tx * u + ty * v + tz * w;
+      }
+      const double vm = fabs(qn) + c * tc2[d];
+      cc[d] = mul_pow2<1>(vm) + mul_pow2<2>(xmvis * tc2[d] * tc2[d]);
+    }
+  }
+  // dtloc.for
+  const double dd = 1. / (tc2[0] * tc2[0] + tc2[1] * tc2[1] + tc2[2] * tc2[2]);
+  const double dtvis = mul_pow2<-1>(detj) * dd * gam1_1 / xm * r;
+  const double sp = sqrt(u * u + v * v + w * w) + c;
+  const double dtconv = sqrt(dd) / sp;
+  const double c1 = z.cfl * fminF(dtconv, dtvis);
+  a.coe[l] = c1;
+  a.coe[l + nd] = cc[0];
+  a.coe[l + 2 * nd] = cc[1];
+  if (z.typ == Z2D) {
+    a.coe[l + 4 * nd] = 1. + mul_pow2<-1>(c1 * (cc[0] + cc[1]));
+  } else {
+    a.coe[l + 3 * nd] = cc[2];
+    a.coe[l + 4 * nd] = 1. + mul_pow2<-1>(c1 * (cc[0] + cc[1] + cc[2]));
+  }
+}
+
 __device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a, const int64_t t) {
   const int64_t nx = a.hi[0] - a.lo[0] + 1, ny = a.hi[1] - a.lo[1] + 1, nz = a.hi[2] - a.lo[2] + 1;
   if (t >= nx * ny * nz) return;
@@ -46,6 +120,10 @@ __device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a,
     a.xmut[l] = xm;
   } else {
     xm = a.xmut_in[l];
+  }
+  if (a.do_lu && z.dtloc == 1) {
+    coefficients_local(z, a, l, i, j, k, xm);
+    return;
   }
   // tstb3_global.for:58-64
   double c1;

@@ -32,7 +32,7 @@ enum { NIJK = 0, NIJK_MTR = 5, NIJK_XYZ = 10, IJKV = 20, ITYPZONE = 25, IFLOW = 
 enum { DTC = 0, GAMMA = 1, CVINF = 2, ROINF = 3, PINF = 4, VINF = 5, TINF = 6,
        PRANDT = 10, XMUL0 = 11, TEMP0 = 12, CS = 13, EPSI_NEWTON = 14,
        PSIROE = 34, WIG_AMP = 72, VXINF = 19, VYINF = 20, VZINF = 21,
-       RONUTILDEINF = 8, SA_RATIOM_R = 18, PRANDT_TUR = 38 };
+       RONUTILDEINF = 8, SA_RATIOM_R = 18, PRANDT_TUR = 38, CFL = 15 };
 enum { BC_TYPE = 0, BC_IDIR = 1, BC_FEN = 2, BC_NBDATA = 8 };
 
 #define OMAX(a, b) ((a) > (b) ? (a) : (b))
@@ -410,6 +410,102 @@ void or_tstb3c(const int64_t* pi, const double* pr, int first_it, const int64_t*
           c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
           c5[l] = xid + c1[l] * (c2[l] + c3[l]) * 0.5;
         }
+      }
+}
+
+/* ======================================================================
+ * tstb3_impli -- FastS/FastS/Compute/tstb3_impli.for (implicit, local time
+ * step: DTLOC = 1): the spectral radii coe2..4 as tstb3c computes them, then
+ * FastS/FastS/Compute/dtloc.for: coe1 = CFL min(dtconv, dtvis) with
+ * d = 1 / sum tc2^2, dtvis = 0.5 detj d / gam1 / xmut ro,
+ * dtconv = sqrt(d) / (|u| + c), and coe5 = 1 + coe1 sum / 2.  Euler: gam1 is
+ * 1e-30 (not 0), and the volume floor is 1e-30.
+ * ====================================================================== */
+void or_tstb3_impli(const int64_t* pi, const double* pr, const int64_t* ind,
+                    const double* rop, double* coe, const double* xmut,
+                    const double* ti, const double* tj, const double* tk, const double* vol) {
+  const int64_t nd = pi[NDIMDX], ndm = pi[NDIMDX_MTR];
+  const double cut0x = 1e-30;
+  double gamma = pr[GAMMA];
+  double rgp = pr[CVINF] * (gamma - 1.);
+  double prandt = pr[PRANDT];
+  double xid = 1.;
+  double gam1 = gamma / prandt;
+  if (pi[IFLOW] == 1) gam1 = cut0x;
+  double gam1_1 = 1. / gam1;
+  double gam2 = gamma * rgp;
+  double cfl = pr[CFL];
+  const double *r_ = rop, *u_ = rop + nd, *v_ = rop + 2 * nd, *w_ = rop + 3 * nd, *t_ = rop + 4 * nd;
+  double *c1 = coe, *c2 = coe + nd, *c3 = coe + 2 * nd, *c4 = coe + 3 * nd, *c5 = coe + 4 * nd;
+  int typ = (int)pi[ITYPZONE];
+  const int64_t mi = pi[NIJK_MTR], mj = pi[NIJK_MTR + 1], mk = pi[NIJK_MTR + 2];
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (int64_t k = ind[4]; k <= ind[5]; k++)
+    for (int64_t j = ind[2]; j <= ind[3]; j++)
+      for (int64_t i = ind[0]; i <= ind[1]; i++) {
+        int64_t l = inddm(pi, i, j, k);
+        double r = r_[l];
+        double u = u_[l], v = v_[l], w = typ == 3 ? 0. : w_[l];
+        double c = sqrt(gam2 * t_[l]);
+        double vmu = gam1 * xmut[l];
+        double tc2i, tc2j, tc2k, detj;
+        if (typ == 2) {   /* cartesian */
+          double tcxi = ti[0], tcyj = tj[0], tczk = tk[0];
+          tc2i = sqrt(tcxi * tcxi); tc2j = sqrt(tcyj * tcyj); tc2k = sqrt(tczk * tczk);
+          detj = OMAX(vol[0], cut0x);
+          double volu = detj * r, xmvis = vmu / volu;
+          double vmi = fabs(tcxi * u) + c * tc2i;
+          c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+          double vmj = fabs(tcyj * v) + c * tc2j;
+          c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+          double vmk = fabs(tczk * w) + c * tc2k;
+          c4[l] = vmk * 2. + xmvis * tc2k * tc2k * 4.;
+        } else {
+          int64_t lt = indmtr(pi, i, j, k);
+          int64_t li = lt + mi, lj = lt + mj, lk = lt + mk;
+          detj = OMAX(vol[lt], cut0x);
+          double volu = detj * r, xmvis = vmu / volu;
+          if (typ != 3) {
+            const double *tix = ti, *tiy = ti + ndm, *tiz = ti + 2 * ndm;
+            const double *tjx = tj, *tjy = tj + ndm, *tjz = tj + 2 * ndm;
+            const double *tkx = tk, *tky = tk + ndm, *tkz = tk + 2 * ndm;
+            double tcxi = .5 * (tix[lt] + tix[li]), tcyi = .5 * (tiy[lt] + tiy[li]), tczi = .5 * (tiz[lt] + tiz[li]);
+            tc2i = .5 * (sqrt(tix[lt] * tix[lt] + tiy[lt] * tiy[lt] + tiz[lt] * tiz[lt]) +
+                         sqrt(tix[li] * tix[li] + tiy[li] * tiy[li] + tiz[li] * tiz[li]));
+            double vmi = fabs(tcxi * u + tcyi * v + tczi * w) + c * tc2i;
+            c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+            double tcxj = .5 * (tjx[lt] + tjx[lj]), tcyj = .5 * (tjy[lt] + tjy[lj]), tczj = .5 * (tjz[lt] + tjz[lj]);
+            tc2j = .5 * (sqrt(tjx[lt] * tjx[lt] + tjy[lt] * tjy[lt] + tjz[lt] * tjz[lt]) +
+                         sqrt(tjx[lj] * tjx[lj] + tjy[lj] * tjy[lj] + tjz[lj] * tjz[lj]));
+            double vmj = fabs(tcxj * u + tcyj * v + tczj * w) + c * tc2j;
+            c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+            double tcxk = .5 * (tkx[lt] + tkx[lk]), tcyk = .5 * (tky[lt] + tky[lk]), tczk = .5 * (tkz[lt] + tkz[lk]);
+            tc2k = .5 * (sqrt(tkx[lt] * tkx[lt] + tky[lt] * tky[lt] + tkz[lt] * tkz[lt]) +
+                         sqrt(tkx[lk] * tkx[lk] + tky[lk] * tky[lk] + tkz[lk] * tkz[lk]));
+            double vmk = fabs(tcxk * u + tcyk * v + tczk * w) + c * tc2k;
+            c4[l] = vmk * 2. + xmvis * tc2k * tc2k * 4.;
+          } else {   /* 2d: tc2k = 0, w = 0 */
+            const double *tix = ti, *tiy = ti + ndm;
+            const double *tjx = tj, *tjy = tj + ndm;
+            double tcxi = .5 * (tix[lt] + tix[li]), tcyi = .5 * (tiy[lt] + tiy[li]);
+            tc2i = .5 * (sqrt(tix[lt] * tix[lt] + tiy[lt] * tiy[lt]) + sqrt(tix[li] * tix[li] + tiy[li] * tiy[li]));
+            double vmi = fabs(tcxi * u + tcyi * v) + c * tc2i;
+            c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+            double tcxj = .5 * (tjx[lt] + tjx[lj]), tcyj = .5 * (tjy[lt] + tjy[lj]);
+            tc2j = .5 * (sqrt(tjx[lt] * tjx[lt] + tjy[lt] * tjy[lt]) + sqrt(tjx[lj] * tjx[lj] + tjy[lj] * tjy[lj]));
+            double vmj = fabs(tcxj * u + tcyj * v) + c * tc2j;
+            c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+            tc2k = 0.;
+          }
+        }
+        /* dtloc.for */
+        double d = 1. / (tc2i * tc2i + tc2j * tc2j + tc2k * tc2k);
+        double dtvis = 0.5 * detj * d * gam1_1 / xmut[l] * r;
+        double sp = sqrt(u * u + v * v + w * w) + c;
+        double dtconv = sqrt(d) / sp;
+        c1[l] = cfl * OMIN(dtconv, dtvis);
+        if (typ == 3) c5[l] = xid + c1[l] * (c2[l] + c3[l]) * 0.5;
+        else c5[l] = xid + c1[l] * (c2[l] + c3[l] + c4[l]) * 0.5;
       }
 }
 
@@ -1456,7 +1552,12 @@ void or_core3as2(const int64_t* pi, const double* pr, int nitcfg, int first_it,
         int64_t l = inddm(pi, i, j, k);
         const double *a = rop, *b = rop_n, *m = rop_n1;
         double cf = coe[l];
-        if (nitcfg == 1) {
+        if (nitcfg == 1 && sa && pi[DTLOC] == 1) {   /* core3as2.for:57-66, 106-114 */
+          for (int v = 0; v < 6; v++) {
+            if (two_d && v == 3) continue;
+            drodm[l + v * nd] = cf * drodm[l + v * nd];
+          }
+        } else if (nitcfg == 1) {
           drodm[l] = cf * drodm[l] + c4 * a[l] + c3 * m[l];
           for (int v = 1; v <= 3; v++) {
             if (two_d && v == 3) continue;
@@ -2548,7 +2649,9 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
           if (pi[IFLOW] == 2) or_invist(pi, pr, implicit ? coe_r : grad_r, ssiter, Z->xmut);
           /* navier_stokes_struct.for:258-266: SA viscosity on ind_coe */
           if (pi[IFLOW] == 3) or_vispalart(pi, pr, coe_r, ssiter, Z->xmut);
-          if (implicit) {
+          if (implicit && pi[DTLOC] == 1) {   /* cptst3.for: local time step */
+            or_tstb3_impli(pi, pr, coe_r, ssiter, Z->coe, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
+          } else if (implicit) {
             or_tstb3_global(pi, pr, coe_r, Z->coe, Z->vol);
             or_tstb3c(pi, pr, *first_it, coe_r, ssiter, Z->coe, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
           } else {
