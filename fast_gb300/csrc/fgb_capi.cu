@@ -794,8 +794,8 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   if (p[ITYPCP] > 1 && p[RK] != 3) return fail(FGB_ERR_ARG, "explicit path needs rk=3");
   if (p[EXPLOC] != 0 || p[LALE] != 0)
     return fail(FGB_ERR_ARG, "explicit local time stepping and moving meshes are not supported");
-  if (p[DTLOC] != 0 && (p[DTLOC] != 1 || p[ITYPCP] > 1))   // cptst3.for: tstb3_impli
-    return fail(FGB_ERR_ARG, "a local time step (time_step_nature 'local') needs an implicit scheme");
+  if (p[DTLOC] != 0 && p[DTLOC] != 1)   // cptst3.for: tstb3_impli / tstb3_expli
+    return fail(FGB_ERR_ARG, "DTLOC must be 0 (global time step) or 1 (local)");
   int64_t nd = p[NDIMDX], neq = p[NEQ], ndm = p[NDIMDX_MTR];
   // metric components per face family: NEQ_IJ for ti / tj, NEQ_K for tk
   // (3d cartesian 1 / 1, 3d general 3 / 3, 2d 2 / 0 -- a 2-d zone has no tk)

@@ -25,8 +25,10 @@ namespace fgb {
 // min(dtconv, dtvis) per cell (d = 1 / sum tc2^2, dtvis = 0.5 detj d / gam1
 // / xmut ro, dtconv = sqrt(d) / (|u| + c)) and coe5 = 1 + coe1 sum / 2.
 // Euler: gam1 = 1e-30 (tstb3c.for takes 0); volume floor 1e-30.
+// Explicit (tstb3_expli.for): the same time step, coe1 only.
 __device__ __forceinline__ void coefficients_local(const Zone& z, const CoeArgs& a, int64_t l,
                                                    int64_t i, int64_t j, int64_t k, double xm) {
+  const bool lu = a.do_lu;
   const int64_t nd = z.nd;
   const double* R = a.rop;
   const double cut0x = 1e-30;
@@ -39,7 +41,7 @@ __device__ __forceinline__ void coefficients_local(const Zone& z, const CoeArgs&
   const double r = R[l], u = R[l + nd], v = R[l + 2 * nd], w = z.typ == Z2D ? 0. : R[l + 3 * nd];
   const double c = sqrt(gam2 * R[l + 4 * nd]);
   const double vmu = gam1 * xm;
-  double tc2[3], cc[3], detj;
+  double tc2[3], cc[3] = {0., 0., 0.}, detj;
   if (z.typ == Z3DCART) {
     detj = fmaxF(z.vol[0], cut0x);
     const double xmvis = vmu / (detj * r);
@@ -47,8 +49,10 @@ __device__ __forceinline__ void coefficients_local(const Zone& z, const CoeArgs&
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       tc2[d] = z.ctc2[d];   // sqrt(tc^2), once per zone
-      const double vm = fabs(tc[d] * q[d]) + c * tc2[d];
-      cc[d] = mul_pow2<1>(vm) + mul_pow2<2>(xmvis * tc2[d] * tc2[d]);
+      if (lu) {
+        const double vm = fabs(tc[d] * q[d]) + c * tc2[d];
+        cc[d] = mul_pow2<1>(vm) + mul_pow2<2>(xmvis * tc2[d] * tc2[d]);
+      }
     }
   } else {
     const int64_t lt = indmtr(z, i, j, k), m = z.ndm;
@@ -73,8 +77,10 @@ __device__ __forceinline__ void coefficients_local(const Zone& z, const CoeArgs&
                               sqrt(T[l2] * T[l2] + T[l2 + m] * T[l2 + m] + T[l2 + 2 * m] * T[l2 + 2 * m]));
         qn = tx * u + ty * v + tz * w;
       }
-      const double vm = fabs(qn) + c * tc2[d];
-      cc[d] = mul_pow2<1>(vm) + mul_pow2<2>(xmvis * tc2[d] * tc2[d]);
+      if (lu) {
+        const double vm = fabs(qn) + c * tc2[d];
+        cc[d] = mul_pow2<1>(vm) + mul_pow2<2>(xmvis * tc2[d] * tc2[d]);
+      }
     }
   }
   // dtloc.for
@@ -84,6 +90,7 @@ __device__ __forceinline__ void coefficients_local(const Zone& z, const CoeArgs&
   const double dtconv = sqrt(dd) / sp;
   const double c1 = z.cfl * fminF(dtconv, dtvis);
   a.coe[l] = c1;
+  if (!lu) return;
   a.coe[l + nd] = cc[0];
   a.coe[l + 2 * nd] = cc[1];
   if (z.typ == Z2D) {
@@ -121,7 +128,7 @@ __device__ __forceinline__ void coefficients_at(const Zone& z, const CoeArgs& a,
   } else {
     xm = a.xmut_in[l];
   }
-  if (a.do_lu && z.dtloc == 1) {
+  if (z.dtloc == 1) {   // cptst3.for: local time step (tstb3_impli.for / tstb3_expli.for)
     coefficients_local(z, a, l, i, j, k, xm);
     return;
   }

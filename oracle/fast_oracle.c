@@ -421,9 +421,26 @@ void or_tstb3c(const int64_t* pi, const double* pr, int first_it, const int64_t*
  * dtconv = sqrt(d) / (|u| + c), and coe5 = 1 + coe1 sum / 2.  Euler: gam1 is
  * 1e-30 (not 0), and the volume floor is 1e-30.
  * ====================================================================== */
+static void or_local_dt(const int64_t* pi, const double* pr, const int64_t* ind, int lu,
+                        const double* rop, double* coe, const double* xmut,
+                        const double* ti, const double* tj, const double* tk, const double* vol);
+
+/* explicit: FastS/FastS/Compute/tstb3_expli.for, the same time step, coe1 only */
+void or_tstb3_expli(const int64_t* pi, const double* pr, const int64_t* ind,
+                    const double* rop, double* coe, const double* xmut,
+                    const double* ti, const double* tj, const double* tk, const double* vol) {
+  or_local_dt(pi, pr, ind, 0, rop, coe, xmut, ti, tj, tk, vol);
+}
+
 void or_tstb3_impli(const int64_t* pi, const double* pr, const int64_t* ind,
                     const double* rop, double* coe, const double* xmut,
                     const double* ti, const double* tj, const double* tk, const double* vol) {
+  or_local_dt(pi, pr, ind, 1, rop, coe, xmut, ti, tj, tk, vol);
+}
+
+static void or_local_dt(const int64_t* pi, const double* pr, const int64_t* ind, int lu,
+                        const double* rop, double* coe, const double* xmut,
+                        const double* ti, const double* tj, const double* tk, const double* vol) {
   const int64_t nd = pi[NDIMDX], ndm = pi[NDIMDX_MTR];
   const double cut0x = 1e-30;
   double gamma = pr[GAMMA];
@@ -448,18 +465,18 @@ void or_tstb3_impli(const int64_t* pi, const double* pr, const int64_t* ind,
         double u = u_[l], v = v_[l], w = typ == 3 ? 0. : w_[l];
         double c = sqrt(gam2 * t_[l]);
         double vmu = gam1 * xmut[l];
-        double tc2i, tc2j, tc2k, detj;
+        double tc2i, tc2j, tc2k, detj, C2 = 0., C3 = 0., C4 = 0.;
         if (typ == 2) {   /* cartesian */
           double tcxi = ti[0], tcyj = tj[0], tczk = tk[0];
           tc2i = sqrt(tcxi * tcxi); tc2j = sqrt(tcyj * tcyj); tc2k = sqrt(tczk * tczk);
           detj = OMAX(vol[0], cut0x);
           double volu = detj * r, xmvis = vmu / volu;
           double vmi = fabs(tcxi * u) + c * tc2i;
-          c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+          C2 = vmi * 2. + xmvis * tc2i * tc2i * 4.;
           double vmj = fabs(tcyj * v) + c * tc2j;
-          c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+          C3 = vmj * 2. + xmvis * tc2j * tc2j * 4.;
           double vmk = fabs(tczk * w) + c * tc2k;
-          c4[l] = vmk * 2. + xmvis * tc2k * tc2k * 4.;
+          C4 = vmk * 2. + xmvis * tc2k * tc2k * 4.;
         } else {
           int64_t lt = indmtr(pi, i, j, k);
           int64_t li = lt + mi, lj = lt + mj, lk = lt + mk;
@@ -473,28 +490,28 @@ void or_tstb3_impli(const int64_t* pi, const double* pr, const int64_t* ind,
             tc2i = .5 * (sqrt(tix[lt] * tix[lt] + tiy[lt] * tiy[lt] + tiz[lt] * tiz[lt]) +
                          sqrt(tix[li] * tix[li] + tiy[li] * tiy[li] + tiz[li] * tiz[li]));
             double vmi = fabs(tcxi * u + tcyi * v + tczi * w) + c * tc2i;
-            c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+            C2 = vmi * 2. + xmvis * tc2i * tc2i * 4.;
             double tcxj = .5 * (tjx[lt] + tjx[lj]), tcyj = .5 * (tjy[lt] + tjy[lj]), tczj = .5 * (tjz[lt] + tjz[lj]);
             tc2j = .5 * (sqrt(tjx[lt] * tjx[lt] + tjy[lt] * tjy[lt] + tjz[lt] * tjz[lt]) +
                          sqrt(tjx[lj] * tjx[lj] + tjy[lj] * tjy[lj] + tjz[lj] * tjz[lj]));
             double vmj = fabs(tcxj * u + tcyj * v + tczj * w) + c * tc2j;
-            c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+            C3 = vmj * 2. + xmvis * tc2j * tc2j * 4.;
             double tcxk = .5 * (tkx[lt] + tkx[lk]), tcyk = .5 * (tky[lt] + tky[lk]), tczk = .5 * (tkz[lt] + tkz[lk]);
             tc2k = .5 * (sqrt(tkx[lt] * tkx[lt] + tky[lt] * tky[lt] + tkz[lt] * tkz[lt]) +
                          sqrt(tkx[lk] * tkx[lk] + tky[lk] * tky[lk] + tkz[lk] * tkz[lk]));
             double vmk = fabs(tcxk * u + tcyk * v + tczk * w) + c * tc2k;
-            c4[l] = vmk * 2. + xmvis * tc2k * tc2k * 4.;
+            C4 = vmk * 2. + xmvis * tc2k * tc2k * 4.;
           } else {   /* 2d: tc2k = 0, w = 0 */
             const double *tix = ti, *tiy = ti + ndm;
             const double *tjx = tj, *tjy = tj + ndm;
             double tcxi = .5 * (tix[lt] + tix[li]), tcyi = .5 * (tiy[lt] + tiy[li]);
             tc2i = .5 * (sqrt(tix[lt] * tix[lt] + tiy[lt] * tiy[lt]) + sqrt(tix[li] * tix[li] + tiy[li] * tiy[li]));
             double vmi = fabs(tcxi * u + tcyi * v) + c * tc2i;
-            c2[l] = vmi * 2. + xmvis * tc2i * tc2i * 4.;
+            C2 = vmi * 2. + xmvis * tc2i * tc2i * 4.;
             double tcxj = .5 * (tjx[lt] + tjx[lj]), tcyj = .5 * (tjy[lt] + tjy[lj]);
             tc2j = .5 * (sqrt(tjx[lt] * tjx[lt] + tjy[lt] * tjy[lt]) + sqrt(tjx[lj] * tjx[lj] + tjy[lj] * tjy[lj]));
             double vmj = fabs(tcxj * u + tcyj * v) + c * tc2j;
-            c3[l] = vmj * 2. + xmvis * tc2j * tc2j * 4.;
+            C3 = vmj * 2. + xmvis * tc2j * tc2j * 4.;
             tc2k = 0.;
           }
         }
@@ -504,6 +521,10 @@ void or_tstb3_impli(const int64_t* pi, const double* pr, const int64_t* ind,
         double sp = sqrt(u * u + v * v + w * w) + c;
         double dtconv = sqrt(d) / sp;
         c1[l] = cfl * OMIN(dtconv, dtvis);
+        if (!lu) continue;   /* explicit: coe1 only */
+        c2[l] = C2;
+        c3[l] = C3;
+        if (typ != 3) c4[l] = C4;
         if (typ == 3) c5[l] = xid + c1[l] * (c2[l] + c3[l]) * 0.5;
         else c5[l] = xid + c1[l] * (c2[l] + c3[l] + c4[l]) * 0.5;
       }
@@ -2654,6 +2675,8 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
           } else if (implicit) {
             or_tstb3_global(pi, pr, coe_r, Z->coe, Z->vol);
             or_tstb3c(pi, pr, *first_it, coe_r, ssiter, Z->coe, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
+          } else if (pi[DTLOC] == 1) {   /* cptst3.for: local time step, explicit */
+            or_tstb3_expli(pi, pr, sdm, ssiter, Z->coe, Z->xmut, Z->ti, Z->tj, Z->tk, Z->vol);
           } else {
             or_tstb3_global(pi, pr, sdm, Z->coe, Z->vol);
           }

@@ -1,9 +1,10 @@
-"""Implicit local time stepping (time_step_nature = 'local', DTLOC = 1):
+"""Local time stepping (time_step_nature = 'local', DTLOC = 1), implicit:
 cptst3.for takes tstb3_impli.for instead of tstb3_global.for + tstb3c.for --
 the spectral radii as before, then a time step per cell from the CFL number
 (dtloc.for: CFL x min(convective, viscous) time step of the cell), BDF1 in
 the dual-time residual (core3as2.for; Spalart-Allmaras: the first
-sub-iteration's residual is coe1 x balance).  The GPU path against the
+sub-iteration's residual is coe1 x balance); explicit: tstb3_expli.for, the
+same time step as coe1 of the RK3 update.  The GPU path against the
 oracle at 1e-12 per cell; the oracle's coe1 against the formula on a
 uniform state."""
 import math
@@ -20,6 +21,25 @@ def _local(numz=None):
     z = {"time_step_nature": "local", "cfl": 5.0}
     z.update(numz or {})
     return z
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["explicit_euler", "explicit_laminar"])
+def test_explicit_local_time_step_matches_oracle(oracle_mod, kind):
+    """Explicit RK3 with a local time step (tstb3_expli.for: coe1 only)."""
+    if kind == "explicit_euler":
+        t = cases.isentropic_vortex(n=(20, 16, 6), wavy=0.3,
+                                    numz=_local({"scheme": "roe_min", "slope": "minmod", "cfl": 0.5}))
+    else:
+        t = cases.taylor_green(n=(12, 10, 8), numb={"temporal_scheme": "explicit"},
+                               numz=_local({"cfl": 0.5}))
+    zd, ref, s = _pair(t, oracle_mod, 1000)
+    assert int(zd[0]["pi"][46]) == 1 and int(zd[0]["pi"][29]) == 2
+    for it in range(1, 4):
+        ref.compute(it, 1, 3, 1, modulo_verif=1000)
+        s.compute(it, 1, 3, 1, 1)
+    _check_levels(ref, s)
+    s.close()
 
 
 @pytest.mark.gpu
