@@ -791,7 +791,8 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
   if (p[NDIMDX] >= (int64_t)INT32_MAX / 2) return fail(FGB_ERR_ARG, "zone too large");
   if (p[ITYPCP] <= 1 && (p[NB_RELAX] > 1 || p[LU_MATCH] != 0))
     return fail(FGB_ERR_ARG, "only nb_relax=1, lu_match=0 LU-SGS is supported");
-  if (p[ITYPCP] > 1 && p[RK] != 3) return fail(FGB_ERR_ARG, "explicit path needs rk=3");
+  if (p[ITYPCP] > 1 && (p[RK] < 1 || p[RK] > 3 || p[NSSITER] != p[RK]))
+    return fail(FGB_ERR_ARG, "explicit path needs rk 1, 2 or 3 with nssiter = rk");
   if (p[EXPLOC] != 0 || p[LALE] != 0)
     return fail(FGB_ERR_ARG, "explicit local time stepping and moving meshes are not supported");
   if (p[DTLOC] != 0 && p[DTLOC] != 1)   // cptst3.for: tstb3_impli / tstb3_expli
@@ -1629,6 +1630,21 @@ static int assemble_stage(fgb_solver* s, ZoneData& Z, StageArgs sa, const double
 static const double kCoefH[4] = {0., 0., -0.6830127018922193, -4. / 3.};
 static const double kCoefW[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
 
+// explicit Runge-Kutta stage coefficients of order rk at stage nstep:
+// coefH scales the previous stage's residual (init_rhs.for:58-78), coefW the
+// update (core3ark3.for:64-85); stage 1 starts from a zero residual
+static void rk_coefs(int rk, int nstep, double* coefH, double* coefW) {
+  *coefH = 0.; *coefW = 0.;
+  if (rk == 1) {
+    if (nstep == 1) *coefW = 1.;
+  } else if (rk == 2) {
+    if (nstep == 1) *coefW = 1.;
+    else if (nstep == 2) { *coefH = -1.; *coefW = 0.5; }
+  } else if (nstep >= 1 && nstep <= 3) {
+    *coefH = kCoefH[nstep]; *coefW = kCoefW[nstep];
+  }
+}
+
 // one RK3 stage of fgb_compute's explicit path on explicit buffers; with a
 // tape, the face fluxes also record the values of their reverse pass
 static int explicit_stage(fgb_solver* s, int m, int nstep, const double* in, double* out, double* D,
@@ -1885,8 +1901,6 @@ static int face_block(fgb_solver* s, FaceBatch& b, int* block) {
 // every cell is that of the per-zone kernels, so the results are the same.
 static int substep_batched(fgb_solver* s, int nstep, bool implicit, int verif, int lexit_lu,
                            std::vector<LuFields>& lu_fields) {
-  const double cxsi1 = -0.6830127018922193, cxsi2 = -4. / 3.;
-  const double cg[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
   const int nzn = (int)s->zones.size();
   std::vector<double*> ssit((size_t)nzn), outp((size_t)nzn);
   for (int m = 0; m < nzn; m++) {
@@ -1969,7 +1983,8 @@ static int substep_batched(fgb_solver* s, int nstep, bool implicit, int verif, i
   {
     ProfScope ps(s, "sa_source");
     const int zero6 = implicit ? 1 : nstep == 1;
-    const double coefH6 = implicit ? 0. : (nstep == 2 ? cxsi1 : (nstep == 3 ? cxsi2 : 0.));
+    double coefH6 = 0., coefW6;
+    if (!implicit) rk_coefs(s->zones[0].z.rk, nstep, &coefH6, &coefW6);
     rc = batches([&](int m) { return s->zones[(size_t)m].z.neq == 6 ? (int64_t)s->zones[(size_t)m].z.typ : -1; },
                  [&](const std::vector<int>& ms) -> int {
       static thread_local SaBatch b;
@@ -2023,8 +2038,7 @@ static int substep_batched(fgb_solver* s, int nstep, bool implicit, int verif, i
       sa.first_sub = nstep == 1;
     } else {
       sa.zero_init = nstep == 1;
-      sa.coefH = nstep == 2 ? cxsi1 : (nstep == 3 ? cxsi2 : 0.);
-      sa.coefW = cg[nstep <= 3 ? nstep : 0];
+      rk_coefs(Z.z.rk, nstep, &sa.coefH, &sa.coefW);
     }
     return sa;
   };
@@ -2099,8 +2113,6 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
     if (!rc) rc = join_upload(s, Z, 2);
     if (rc) return rc;
   }
-  const double cxsi1 = -0.6830127018922193, cxsi2 = -4. / 3.;
-  const double cg[4] = {0., 0.5, 0.9106836025229591, 0.3660254037844387};
   std::vector<LuFields> lu_fields(s->zones.size());
   for (int it = 0; it < nit_c; it++) {
     int64_t nitrun_loc = (int64_t)nitrun * nit_c + it;
@@ -2173,7 +2185,8 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
         if (z.neq == 6) {  // src_term.for:86-97: SA source (equation 6 initialised here)
           ProfScope ps(s, "sa_source");
           const int zero6 = implicit ? 1 : nstep == 1;
-          const double coefH6 = implicit ? 0. : (nstep == 2 ? cxsi1 : (nstep == 3 ? cxsi2 : 0.));
+          double coefH6 = 0., coefW6;
+          if (!implicit) rk_coefs(z.rk, nstep, &coefH6, &coefW6);
           CK(launch_sa_source(z, ssiter, Z.drodm, Z.coe, coefH6, zero6, implicit && nstep == 1, s->st));
           s->launches++;
         }
@@ -2196,8 +2209,7 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
           sa.first_sub = nstep == 1;
         } else {
           sa.zero_init = nstep == 1;
-          sa.coefH = nstep == 2 ? cxsi1 : (nstep == 3 ? cxsi2 : 0.);
-          sa.coefW = cg[nstep <= 3 ? nstep : 0];
+          rk_coefs(z.rk, nstep, &sa.coefH, &sa.coefW);
         }
         {
           ProfScope ps(s, implicit ? "assemble_bdf" : "assemble_rk3");
@@ -2301,6 +2313,11 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       if (rc) return rc;
     }
     s->first_it = 1;
+    // the levels rotate after every implicit step and after an explicit
+    // step of an odd stage count, whose last stage writes level n+1; the
+    // two stages of RK2 end in level n itself, which keeps its place
+    // (FastS/FastS/PyTree.py:226-228, switchPointers__ order nitmax%2+2)
+    if (!implicit && nssiter % 2 == 0) continue;
     for (ZoneData& Z : s->zones) {
       double* save = Z.lvl[1];
       Z.lvl[1] = Z.lvl[0];

@@ -352,6 +352,16 @@ def _compute(t, metrics, nitrun, tc=None, graph=None, tc2=None, graph2=None, lay
         # which then becomes n-1, so that level is copied back too)
         rot = NIT % 3
         explicit = HOOK["nssiter"] <= 3 and _itypcp(zones[0]) == 2
+        if explicit and HOOK["nssiter"] % 2 == 0:
+            # RK2 ends in level n itself and the levels keep their places
+            # (PyTree.py:228, switchPointers__ order 2); level n+1 holds
+            # the first stage
+            for n, z in enumerate(zones):
+                s.download(n, 0, FastC.compactArray(z, "").reshape(-1))
+                s.download(n, 2, FastC.compactArray(z, "_P1").reshape(-1))
+            HOOK["FIRST_IT"] = 1
+            FIRST_IT = 1
+            return None
         for n, z in enumerate(zones):
             for _ in range(rot):
                 FastC.switchPointers__([z])

@@ -2731,6 +2731,10 @@ int or_compute(or_zone* zones, int nzones, const or_transfer* tr, int ntr,
       }
     }
     *first_it = 1;
+    /* FastS/FastS/PyTree.py:226-228: switchPointers__(zones, case, nitmax%2+2)
+     * for an explicit step -- order 2 (an even stage count, RK2, whose last
+     * stage wrote ro) leaves the levels in place */
+    if (!implicit && nssiter % 2 == 0) continue;
     for (int z = 0; z < nzones; z++) {
       double* save = zones[z].ro_m1;
       zones[z].ro_m1 = zones[z].ro;
