@@ -162,12 +162,13 @@ def test_grid_barrier_wait_gives_up():
     s.close()
 
 
-def test_dataflow_wait_gives_up():
+@pytest.mark.parametrize("precision", [64, 32])
+def test_dataflow_wait_gives_up(precision):
     """A dependency wait of the dataflow sweep whose mark nothing publishes
-    ("lu_wait_skew" raises the marks the waits expect) gives up after
-    "lu_poll_limit" polls: the call reports FGB_ERR_DEVICE, every warp
-    returns, and the device stays usable (a fresh solver then computes
-    normally)."""
+    ("lu_wait_skew" raises the marks -- FP32: the tags of the increment
+    words -- that the waits expect) gives up after "lu_poll_limit" polls: the
+    call reports FGB_ERR_DEVICE, every warp returns, and the device stays
+    usable (a fresh solver then computes normally)."""
     from fast_gb300._native import FastGB300Error
     t = cases.taylor_green(n=(12, 10, 8), ss_iteration=2)
     from fast_gb300._native import Solver
@@ -186,6 +187,7 @@ def test_dataflow_wait_gives_up():
     s = solver()
     s.set_option("lu_mode", 2)
     s.set_option("autotune", 0)
+    s.set_option("lu_precision", precision)
     s.set_option("lu_poll_limit", 4096)
     s.set_option("lu_wait_skew", 2)
     s.compute(1, 1, 3, 1, 1)
