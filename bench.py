@@ -334,8 +334,11 @@ def run_ours(args, d: Dist):
         ms32 = s.timer_stop()
         d.barrier()
         v32, ms32_max = replica_throughput(d, cells, args.steps, ms32)
+        t32 = s.get_option("lu_tuned32")
         mixed = {"value": v32, "unit": UNIT, "ms_per_step": ms32_max / args.steps,
-                 "dtype": "f64+f32-sweeps"}
+                 "dtype": "f64+f32-sweeps",
+                 "lu_autotuned": None if t32 < 0 else {"lu_mode": int(t32) // 10,
+                                                        "ctas_per_sm": int(t32) % 10}}
         s.set_option("lu_precision", 64)
         fasts._compute(t, metrics, it)   # back on the FP64 path before the profiled step
         it += 1

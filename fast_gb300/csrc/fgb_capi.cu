@@ -138,7 +138,8 @@ struct LuGroupData {
   // sweep precision ([0] FP64, [1] FP32; -1: not tuned): lu_mode 1 or 2, and
   // dataflow CTAs per SM
   int tuned_mode[2] = {-1, -1}, tuned_per_sm[2] = {0, 0};
-  double tuned_ms[2][3] = {{0., 0., 0.}, {0., 0., 0.}};
+  static constexpr int NCAND = 4;
+  double tuned_ms[2][NCAND] = {};
 };
 
 struct fgb_solver {
@@ -169,6 +170,30 @@ struct fgb_solver {
     double* lam0 = nullptr;        // lamW as allocated (the parity of rev)
   } adj;
   bool graph = true;               // replay the adjoint driver loops as CUDA graphs
+  // fgb_compute as CUDA graphs: one per call signature (step range, the
+  // verification flags the step numbers give, first_it, sweep precision)
+  // and level pointers, recorded the second time that signature comes and
+  // replayed after that.  A replay redoes the host side of the call (the
+  // level rotation, the LU epochs, the counters) from what the recording
+  // left; the LU zone tables of the recorded solves are copied from the
+  // graph's own page-locked buffers, and the dataflow marks are cleared
+  // before each recorded sweep (their values are fixed in the graph).
+  struct StepGraph {
+    std::vector<uintptr_t> key;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<double*> post;       // per zone: lvl[0..2], scratch after the call
+    std::vector<int> epochs;         // per LU group: epoch after the call
+    int first_it = 1, nit_recorded = 0;
+    int64_t launches = 0;
+    LuZone* tab_host = nullptr;      // LU zone tables of the recorded solves
+    LuZone* tab_dev = nullptr;
+  };
+  bool compute_graph = true;
+  std::vector<StepGraph> step_graphs;
+  std::vector<std::vector<uintptr_t>> step_seen;
+  bool capturing = false;          // recording fgb_compute: LU tables from the arena below
+  LuZone *cap_host = nullptr, *cap_dev = nullptr;
+  size_t cap_used = 0, cap_size = 0;
   // several zones: their per-zone kernels run on ZS side streams (zone m on
   // stream m mod ZS), forked from and joined back into the solver stream
   // around each per-zone phase, so that the small launches overlap
@@ -216,6 +241,18 @@ struct fgb_solver {
 
 extern "C" {
 static void adj_free(fgb_solver* s);   // defined with the C ABI below
+}
+
+static void drop_step_graphs(fgb_solver* s) {
+  if (s->step_graphs.empty() && s->step_seen.empty()) return;
+  if (!s->step_graphs.empty()) cudaStreamSynchronize(s->st);   // no replay in flight
+  for (fgb_solver::StepGraph& g : s->step_graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    cudaFree(g.tab_dev);
+    cudaFreeHost(g.tab_host);
+  }
+  s->step_graphs.clear();
+  s->step_seen.clear();
 }
 
 static cudaEvent_t ev_get(fgb_solver* s) {
@@ -697,6 +734,7 @@ int fgb_destroy(fgb_solver* s) {
   cudaSetDevice(s->device);
   if (s->cst) cudaStreamSynchronize(s->cst);
   cudaStreamSynchronize(s->st);
+  drop_step_graphs(s);
   for (ZoneData& Z : s->zones)
     for (int i = 0; i < 3; i++) if (Z.up_ev[i]) cudaEventDestroy(Z.up_ev[i]);
   if (s->cst_ev) cudaEventDestroy(s->cst_ev);
@@ -755,6 +793,7 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
                  const double* tj, const double* tk, const double* vol, int* zone_id) {
   if (!s || !param_int || !param_real || !ti || !tj || !tk || !vol)
     return fail(FGB_ERR_ARG, "null argument");
+  drop_step_graphs(s);
   if (n_int < 137 || n_real < 73) return fail(FGB_ERR_ARG, "param_int/param_real too short");
   CK(cudaSetDevice(s->device));
   ZoneData Z;
@@ -864,6 +903,7 @@ int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
 int fgb_add_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n,
                      const int64_t* dnr_idx, const int64_t* rcv_idx) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
+  drop_step_graphs(s);
   if (dnr_zone < 0 || rcv_zone < 0 || dnr_zone >= (int)s->zones.size() ||
       rcv_zone >= (int)s->zones.size())
     return fail(FGB_ERR_ARG, "transfer zone out of range");
@@ -890,6 +930,7 @@ int fgb_add_interp_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n
                             const int64_t* dnr_idx, const int64_t* rcv_idx, const int64_t* types,
                             const double* coefs, int64_t ncoefs) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
+  drop_step_graphs(s);
   if (dnr_zone < 0 || rcv_zone < 0 || dnr_zone >= (int)s->zones.size() ||
       rcv_zone >= (int)s->zones.size())
     return fail(FGB_ERR_ARG, "transfer zone out of range");
@@ -936,6 +977,7 @@ int fgb_add_interp_transfer(fgb_solver* s, int dnr_zone, int rcv_zone, int64_t n
 
 int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist) {
   if (!s || !dist) return fail(FGB_ERR_ARG, "null argument");
+  drop_step_graphs(s);
   if (zone < 0 || zone >= (int)s->zones.size()) return fail(FGB_ERR_ARG, "zone out of range");
   ZoneData& Z = s->zones[zone];
   if (Z.z.neq != 6) return fail(FGB_ERR_ARG, "the zone has no Spalart-Allmaras equation");
@@ -945,9 +987,17 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist) {
   return FGB_OK;
 }
 
+static int set_option(fgb_solver* s, const std::string& k, double value);
 int fgb_set_option(fgb_solver* s, const char* key, double value) {
   if (!s || !key) return fail(FGB_ERR_ARG, "null argument");
-  std::string k(key);
+  // a changed option changes what a recorded step would launch
+  double old = 0.;
+  const bool known = fgb_get_option(s, key, &old) == FGB_OK;
+  const int rc = set_option(s, std::string(key), value);
+  if (rc == FGB_OK && (!known || old != value)) drop_step_graphs(s);
+  return rc;
+}
+static int set_option(fgb_solver* s, const std::string& k, double value) {
   if (k == "lu_precision") {
     if (value != 64. && value != 32.) return fail(FGB_ERR_ARG, "lu_precision must be 64 or 32");
     s->lu_precision = (int)value;
@@ -976,6 +1026,8 @@ int fgb_set_option(fgb_solver* s, const char* key, double value) {
     s->profile = value != 0.;
   } else if (k == "graph") {
     s->graph = value != 0.;
+  } else if (k == "compute_graph") {
+    s->compute_graph = value != 0.;
   } else if (k == "zone_streams") {
     s->zone_streams = value != 0.;
   } else if (k == "lu_grid") {
@@ -996,15 +1048,19 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value) {
   else if (k == "first_it") *value = s->first_it;
   else if (k == "profile") *value = s->profile;
   else if (k == "graph") *value = s->graph;
+  else if (k == "compute_graph") *value = s->compute_graph;
+  else if (k == "step_graphs") *value = (double)s->step_graphs.size();
   else if (k == "zone_streams") *value = s->zone_streams;
   else if (k == "lu_grid") *value = s->lu_grid;
   else if (k == "lu_poll_limit") *value = (double)s->poll_limit;
   else if (k == "lu_wait_skew") *value = s->wait_skew;
   else if (k == "lu_prefetch") *value = s->lu_prefetch;
   else if (k == "batch") *value = s->batch;
-  else if (k == "lu_tuned") {   // first LU group, FP64 sweeps: 10 x lu_mode + CTAs per SM (-1: not tuned)
-    *value = (s->lu_groups.empty() || s->lu_groups[0].tuned_mode[0] < 0)
-                 ? -1. : 10. * s->lu_groups[0].tuned_mode[0] + s->lu_groups[0].tuned_per_sm[0];
+  else if (k == "lu_tuned" || k == "lu_tuned32") {
+    // first LU group, FP64 (lu_tuned) or FP32 sweeps: 10 x lu_mode + CTAs per SM (-1: not tuned)
+    const int pk = k == "lu_tuned32" ? 1 : 0;
+    *value = (s->lu_groups.empty() || s->lu_groups[0].tuned_mode[pk] < 0)
+                 ? -1. : 10. * s->lu_groups[0].tuned_mode[pk] + s->lu_groups[0].tuned_per_sm[pk];
   }
   else if (k == "autotune") *value = s->autotune;
   else return fail(FGB_ERR_ARG, "unknown option " + k);
@@ -2083,6 +2139,83 @@ static int substep_batched(fgb_solver* s, int nstep, bool implicit, int verif, i
   return FGB_OK;
 }
 
+static int compute_steps(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int nit_c);
+
+// host side of a call: the level pointers of every zone, the LU epochs
+static void get_levels(const fgb_solver* s, std::vector<double*>& lv) {
+  lv.clear();
+  for (const ZoneData& Z : s->zones) {
+    for (int i = 0; i < 3; i++) lv.push_back(Z.lvl[i]);
+    lv.push_back(Z.scratch);
+  }
+}
+static void set_levels(fgb_solver* s, const std::vector<double*>& lv) {
+  size_t q = 0;
+  for (ZoneData& Z : s->zones) {
+    for (int i = 0; i < 3; i++) Z.lvl[i] = lv[q++];
+    Z.scratch = lv[q++];
+  }
+}
+
+static int replay_step(fgb_solver* s, fgb_solver::StepGraph& g) {
+  CK(cudaGraphLaunch(g.exec, s->st));
+  set_levels(s, g.post);
+  for (size_t i = 0; i < s->lu_groups.size(); i++) s->lu_groups[i].epoch += g.epochs[i];
+  s->first_it = g.first_it;
+  if (g.nit_recorded >= 0) s->nit_recorded = g.nit_recorded;
+  s->launches += g.launches;
+  return FGB_OK;
+}
+
+// record the call into a graph (nothing runs while recording), then launch
+// it; if recording fails, the host state is put back and the call runs as
+// plain launches (and this solver records no more)
+static int record_step(fgb_solver* s, const std::vector<uintptr_t>& key, int nitrun, int nstep_deb,
+                       int nstep_fin, int nit_c) {
+  std::vector<double*> pre;
+  get_levels(s, pre);
+  std::vector<int> ep0;
+  for (LuGroupData& g : s->lu_groups) ep0.push_back(g.epoch);
+  const int first0 = s->first_it, nrec0 = s->nit_recorded;
+  const int64_t l0 = s->launches;
+  size_t need = 0;   // LU solves of the call, at most one per group and sub-step
+  for (LuGroupData& g : s->lu_groups) need += g.zones.size();
+  need *= (size_t)nit_c * (size_t)(nstep_fin - nstep_deb + 1);
+  fgb_solver::StepGraph g;
+  g.key = key;
+  if (need) {
+    CK(cudaMallocHost(&g.tab_host, sizeof(LuZone) * need));
+    const cudaError_t e = cudaMalloc(&g.tab_dev, sizeof(LuZone) * need);
+    if (e != cudaSuccess) { cudaFreeHost(g.tab_host); CK(e); }
+  }
+  s->cap_host = g.tab_host; s->cap_dev = g.tab_dev; s->cap_used = 0; s->cap_size = need;
+  s->nit_recorded = -1;
+  s->capturing = true;
+  const int rc = capture_graph(s, &g.exec, [&]() { return compute_steps(s, nitrun, nstep_deb, nstep_fin, nit_c); });
+  s->capturing = false;
+  s->cap_host = s->cap_dev = nullptr;
+  if (rc) {
+    set_levels(s, pre);
+    for (size_t i = 0; i < s->lu_groups.size(); i++) s->lu_groups[i].epoch = ep0[i];
+    s->first_it = first0; s->nit_recorded = nrec0; s->launches = l0;
+    cudaFree(g.tab_dev); cudaFreeHost(g.tab_host);
+    cudaGetLastError();
+    s->compute_graph = false;
+    return compute_steps(s, nitrun, nstep_deb, nstep_fin, nit_c);
+  }
+  get_levels(s, g.post);
+  for (size_t i = 0; i < s->lu_groups.size(); i++) g.epochs.push_back(s->lu_groups[i].epoch - ep0[i]);
+  g.first_it = s->first_it;
+  g.nit_recorded = s->nit_recorded;
+  if (s->nit_recorded < 0) s->nit_recorded = nrec0;
+  g.launches = s->launches - l0;
+  const cudaError_t e = cudaGraphLaunch(g.exec, s->st);
+  if (s->step_graphs.size() >= 24) drop_step_graphs(s);   // bounded cache
+  s->step_graphs.push_back(g);
+  CK(e);
+  return FGB_OK;
+}
+
 int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int layer_mode,
                 int nit_c) {
   if (!s) return fail(FGB_ERR_ARG, "null solver");
@@ -2106,6 +2239,38 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
     rc = build_lu_groups(s);
     if (rc) return rc;
   }
+  // a recorded call of the same signature and level pointers: replay it
+  bool pending = false;
+  for (ZoneData& Z : s->zones)
+    for (int lv = 0; lv < 3; lv++) pending = pending || Z.up_pending[lv];
+  const bool graphable = s->compute_graph && !s->profile && !pending &&
+                         (s->batch || s->zones.size() == 1);
+  if (graphable) {
+    std::vector<uintptr_t> key;
+    key.push_back((uintptr_t)nstep_deb); key.push_back((uintptr_t)nstep_fin);
+    key.push_back((uintptr_t)nit_c); key.push_back((uintptr_t)s->first_it);
+    key.push_back((uintptr_t)s->lu_precision);
+    for (int it = 0; it < nit_c; it++)
+      key.push_back(((int64_t)nitrun * nit_c + it) % s->modulo_verif == 0 ? 1u : 0u);
+    for (ZoneData& Z : s->zones) {
+      for (int lv = 0; lv < 3; lv++) key.push_back((uintptr_t)Z.lvl[lv]);
+      key.push_back((uintptr_t)Z.scratch);
+    }
+    for (fgb_solver::StepGraph& g : s->step_graphs)
+      if (g.key == key) return replay_step(s, g);
+    bool seen = false;
+    for (auto& k : s->step_seen) seen = seen || k == key;
+    if (seen) return record_step(s, key, nitrun, nstep_deb, nstep_fin, nit_c);
+    s->step_seen.push_back(key);
+  }
+  return compute_steps(s, nitrun, nstep_deb, nstep_fin, nit_c);
+}
+
+// the steps of fgb_compute (uploads joined as the levels are first read)
+static int compute_steps(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int nit_c) {
+  const std::vector<int64_t>& p0 = s->zones[0].pi;
+  const int64_t nssiter = p0[NSSITER];
+  const bool implicit = p0[ITYPCP] <= 1;
   // an asynchronous upload of level n-1 overlaps the coefficients and the
   // face fluxes of the first sub-step; levels n and n+1 are read at once
   for (ZoneData& Z : s->zones) {
@@ -2243,30 +2408,40 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
       if (implicit && !lexit_lu) {
         for (LuGroupData& g : s->lu_groups) {
           const int nz = (int)g.zones.size();
-          const int slot = g.slot;
-          g.slot = (g.slot + 1) % LuGroupData::NSLOT;
-          if (g.ev_used[slot]) CK(cudaEventSynchronize(g.ev[slot]));   // slot's last copy done
-          LuZone* th = g.tab_host + (size_t)slot * nz;
-          LuZone* td = g.tab_dev + (size_t)slot * nz;
+          LuZone *th, *td;
+          if (s->capturing) {   // a recorded step: the graph's own tables
+            if (s->cap_used + (size_t)nz > s->cap_size) return fail(FGB_ERR_STATE, "LU table arena");
+            th = s->cap_host + s->cap_used;
+            td = s->cap_dev + s->cap_used;
+            s->cap_used += (size_t)nz;
+          } else {
+            const int slot = g.slot;
+            g.slot = (g.slot + 1) % LuGroupData::NSLOT;
+            if (g.ev_used[slot]) CK(cudaEventSynchronize(g.ev[slot]));   // slot's last copy done
+            th = g.tab_host + (size_t)slot * nz;
+            td = g.tab_dev + (size_t)slot * nz;
+            g.ev_used[slot] = true;
+          }
           for (int q = 0; q < nz; q++) {
             th[q].z = s->zones[g.zones[q]].z;
             th[q].f = lu_fields[(size_t)g.zones[q]];
           }
           CK(cudaMemcpyAsync(td, th, sizeof(LuZone) * nz, cudaMemcpyHostToDevice, s->st));
-          CK(cudaEventRecord(g.ev[slot], s->st));
-          g.ev_used[slot] = true;
+          if (!s->capturing) CK(cudaEventRecord(g.ev[(g.slot + LuGroupData::NSLOT - 1) % LuGroupData::NSLOT], s->st));
           // autotuner: on the group's first solve (schedule "auto", the
           // default lu_mode 2 with autotune on), time the grid-barrier sweep
-          // and the dataflow sweep with one and two CTAs per SM on this very
-          // solve -- a solve reads W^p, the residual and the coefficients
-          // and writes only its own outputs, so repeating it changes nothing
-          // -- and keep the fastest for the rest of the run
+          // and the dataflow sweep with one, two and four CTAs per SM (as
+          // many as are resident, at most) on this very solve -- a solve
+          // reads W^p, the residual and the coefficients and writes only its
+          // own outputs, so repeating it changes nothing -- and keep the
+          // fastest for the rest of the run
           const int pk = s->lu_precision == 32 ? 1 : 0;
           if (s->autotune && s->lu_mode == 2 && g.tuned_mode[pk] < 0 && !s->profile) {
-            const int cand_mode[3] = {1, 2, 2}, cand_per[3] = {0, 1, 2};
+            constexpr int NC = LuGroupData::NCAND;
+            const int cand_mode[NC] = {1, 2, 2, 2}, cand_per[NC] = {0, 1, 2, 4};
             cudaEvent_t e0 = ev_get(s), e1 = ev_get(s);
             float best = 1e30f;
-            for (int c = 0; c < 3; c++) {
+            for (int c = 0; c < NC; c++) {
               g.epoch++;
               LuGroup Lc = group_launch(s, g, td);
               Lc.persistent = cand_mode[c];
@@ -2282,7 +2457,7 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             }
             s->pool.push_back(e0);
             s->pool.push_back(e1);
-            s->launches += 3 * (2 * nz + 1);
+            s->launches += NC * (2 * nz + 1);
           }
           g.epoch++;
           LuGroup L = group_launch(s, g, td);
@@ -2290,6 +2465,10 @@ int fgb_compute(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin, int lay
             L.persistent = g.tuned_mode[pk];
             L.flow_per_sm = g.tuned_per_sm[pk];
           }
+          // a replayed sweep publishes the marks fixed at recording: clear
+          // what earlier solves left
+          if (s->capturing && L.persistent == 2 && g.flag)
+            CK(cudaMemsetAsync(g.flag, 0, sizeof(int) * (size_t)g.nchunk, s->st));
           {
             ProfScope ps(s, "lu_sgs");
             CK(launch_lusgs(th, L, s->st));
@@ -2357,6 +2536,7 @@ int fgb_cfl(fgb_solver* s, int zone, double* out) {
 
 int fgb_set_bc_state(fgb_solver* s, int zone, const double* st) {
   if (!s || !st) return fail(FGB_ERR_ARG, "null argument");
+  drop_step_graphs(s);
   if (zone < 0 || zone >= (int)s->zones.size()) return fail(FGB_ERR_ARG, "zone out of range");
   for (GatherList& g : s->zones[zone].bcs)
     if (g.kind == 1 && (g.op == BCF_FARFIELD || g.op == BCF_OUTFLOW))
@@ -2375,6 +2555,7 @@ int fgb_set_bc_state(fgb_solver* s, int zone, const double* st) {
 int fgb_adjoint_forward(fgb_solver* s, int zone, int nsteps, int ckpt) {
   int rc = adj_check(s, zone);
   if (rc) return rc;
+  drop_step_graphs(s);
   if (nsteps < 1 || ckpt < 1) return fail(FGB_ERR_ARG, "nsteps and ckpt must be >= 1");
   CK(cudaSetDevice(s->device));
   { int rj = join_uploads(s); if (rj) return rj; }
@@ -2438,6 +2619,7 @@ int fgb_adjoint_backward(fgb_solver* s, int zone, const double* lam_final, doubl
                          double* lam_ti, double* lam_tj, double* lam_vol, double* lam_st) {
   int rc = adj_check(s, zone);
   if (rc) return rc;
+  drop_step_graphs(s);
   fgb_solver::Adj& A = s->adj;
   if (A.zone != zone || A.ck.empty()) return fail(FGB_ERR_STATE, "fgb_adjoint_forward first");
   if (!lam_final || !lam_w0 || !lam_ti || !lam_tj || !lam_vol || !lam_st)
@@ -2551,6 +2733,7 @@ int fgb_tangent(fgb_solver* s, int zone, int nsteps, const double* dw0, const do
                 const double* dtj, const double* dvol, const double* dst, double* dw_final) {
   int rc = adj_check(s, zone);
   if (rc) return rc;
+  drop_step_graphs(s);
   if (!dw0 || !dti || !dtj || !dvol || !dst || !dw_final) return fail(FGB_ERR_ARG, "null argument");
   CK(cudaSetDevice(s->device));
   { int rj = join_uploads(s); if (rj) return rj; }

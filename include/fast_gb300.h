@@ -91,7 +91,17 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * HOOK["FIRST_IT"] flag (0 = BDF1 step); "profile": 1 to time every kernel
  * group with CUDA events (see fgb_kernel_stats); "graph": 1 (default) to
  * replay the loops of fgb_adjoint_forward / _backward as CUDA graphs, 0 for
- * stream launches (profiling always uses stream launches); "zone_streams":
+ * stream launches (profiling always uses stream launches); "compute_graph":
+ * 1 (default) to record an fgb_compute call as a CUDA graph the second time
+ * its signature comes (step range, the verification flags of its step
+ * numbers, first_it, sweep precision, and the level buffers every zone's
+ * time levels are in) and to replay the graph from then on, with the host
+ * side of the call (level rotation) redone -- same results; calls with an
+ * asynchronous upload pending, profiled calls and per-zone side-stream
+ * launches run as stream launches; any state-changing call (a changed
+ * option, a zone, a transfer, a wall distance, a BC state, the adjoint)
+ * drops the recorded graphs; fgb_get_option("step_graphs") counts them;
+ * "zone_streams":
  * 1 (default) to run the per-zone kernels of several zones on 8 side streams
  * (zone m on stream m mod 8, joined before each LU-SGS solve and after each
  * ghost fill), 0 for the solver stream alone (profiling uses it alone);
@@ -113,7 +123,12 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * of zone (zone type, scheme, slope, viscosity, NEQ; up to 40 zones a
  * launch), 0 for per-zone launches (same results); "autotune": 1 (default)
  * to pick the batched face kernels' block size by timing the candidates on
- * the first batch of each kind (kept per device for the process). */
+ * the first batch of each kind (kept per device for the process), and the
+ * LU-SGS schedule of each zone group and sweep precision by timing the
+ * grid-barrier sweep and the dataflow sweep with 1, 2 and 4 CTAs per SM on
+ * its first solve.  fgb_get_option also reads "lu_tuned" / "lu_tuned32":
+ * the first group's FP64 / FP32 choice as 10 x lu_mode + CTAs per SM (-1
+ * before the first solve). */
 int fgb_set_option(fgb_solver* s, const char* key, double value);
 int fgb_get_option(fgb_solver* s, const char* key, double* value);
 
