@@ -98,6 +98,8 @@ def parse():
                    help="LU-SGS schedule: 2 dataflow (default), 1 grid barrier, 0 plane launches")
     p.add_argument("--lu-prefetch", type=int, default=1, choices=[0, 1],
                    help="dataflow LU-SGS sweep: L2 prefetch of each chunk's operands")
+    p.add_argument("--compute-graph", type=int, default=1, choices=[0, 1],
+                   help="record each fgb_compute signature as a CUDA graph and replay it")
     p.add_argument("--lu-grid", type=int, default=0,
                    help="LU-SGS sweep CTAs (0: every resident slot)")
     p.add_argument("--lu-precision", type=int, default=64, choices=[64, 32],
@@ -292,6 +294,7 @@ def run_ours(args, d: Dist):
     s.set_option("lu_mode", args.lu_mode)
     s.set_option("lu_grid", args.lu_grid)
     s.set_option("lu_prefetch", args.lu_prefetch)
+    s.set_option("compute_graph", args.compute_graph)
     it = 1
     for _ in range(args.warmup):
         fasts._compute(t, metrics, it)
@@ -474,6 +477,7 @@ def run_multizone(args):
     s.set_option("lu_mode", args.lu_mode)
     s.set_option("lu_grid", args.lu_grid)
     s.set_option("lu_prefetch", args.lu_prefetch)
+    s.set_option("compute_graph", args.compute_graph)
     cells = sum(int(np.prod(z[1][:, 0] - 1 - 4)) for z in fasts.HOOK["zones"])
     it = 1
     for _ in range(args.warmup):
@@ -501,7 +505,8 @@ def run_multizone(args):
             "vs_baseline": None,
             "dtype": "f64" if args.lu_precision == 64 else "f64+f32-sweeps", "data": "synthetic",
             "config": {"workload": name, "zones": len(fasts.HOOK["zones"]), "cells": cells,
-                       "lu_precision": args.lu_precision, "sub_iterations": args.ss},
+                       "lu_precision": args.lu_precision, "sub_iterations": args.ss,
+                       "compute_graph": args.compute_graph},
             "clocks": clk, "gpu_launches": launches,
             "kernel_ms_per_step": {k: v[1] for k, v in stats.items()}}
     print(json.dumps(line), flush=True)
