@@ -315,9 +315,8 @@ def run_ours(args, d: Dist):
     clk = clocks.stop()
     launches = s.launch_count() - l0
     tuned = s.get_option("lu_tuned")
-    lu_sched = {"lu_mode": args.lu_mode,
-                "autotuned": None if tuned < 0 else {"lu_mode": int(tuned) // 10,
-                                                     "ctas_per_sm": int(tuned) % 10}}
+    lu_sched = {"lu_mode": args.lu_mode, "autotuned": lu_choice(tuned),
+                "trial_ms": lu_trials(s, 64) if tuned >= 0 else None}
     d.barrier()
     value, ms_max = replica_throughput(d, cells, args.steps, ms)
 
@@ -340,8 +339,8 @@ def run_ours(args, d: Dist):
         t32 = s.get_option("lu_tuned32")
         mixed = {"value": v32, "unit": UNIT, "ms_per_step": ms32_max / args.steps,
                  "dtype": "f64+f32-sweeps",
-                 "lu_autotuned": None if t32 < 0 else {"lu_mode": int(t32) // 10,
-                                                        "ctas_per_sm": int(t32) % 10}}
+                 "lu_autotuned": lu_choice(t32),
+                 "lu_trial_ms": lu_trials(s, 32) if t32 >= 0 else None}
         s.set_option("lu_precision", 64)
         fasts._compute(t, metrics, it)   # back on the FP64 path before the profiled step
         it += 1
@@ -447,6 +446,25 @@ def run_ours(args, d: Dist):
             "adjoint": adj,
         }
         print(json.dumps(line), flush=True)
+
+
+def lu_choice(v):
+    """The LU-SGS autotuner's choice from get_option("lu_tuned"):
+    1000 x warps per CTA (dataflow) + 10 x lu_mode + CTAs per SM."""
+    if v < 0:
+        return None
+    v = int(v)
+    out = {"lu_mode": (v % 1000) // 10, "ctas_per_sm": v % 10}
+    if v // 1000:
+        out["warps_per_cta"] = v // 1000
+    return out
+
+
+def lu_trials(s, prec):
+    """The autotuner's trial times (ms) of the first LU group: grid barrier;
+    dataflow 8 warps x 1, 2, 4 CTAs per SM; dataflow 4 warps x 1, 2."""
+    names = ["grid_barrier", "flow_8w_x1", "flow_8w_x2", "flow_8w_x4", "flow_4w_x1", "flow_4w_x2"]
+    return {n: round(s.get_option(f"lu_trial_ms{prec}_{c}"), 3) for c, n in enumerate(names)}
 
 
 def run_multizone(args):

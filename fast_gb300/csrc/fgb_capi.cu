@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -137,8 +138,8 @@ struct LuGroupData {
   // LU schedule picked by the autotuner on the group's first solve of each
   // sweep precision ([0] FP64, [1] FP32; -1: not tuned): lu_mode 1 or 2, and
   // dataflow CTAs per SM
-  int tuned_mode[2] = {-1, -1}, tuned_per_sm[2] = {0, 0};
-  static constexpr int NCAND = 4;
+  int tuned_mode[2] = {-1, -1}, tuned_per_sm[2] = {0, 0}, tuned_threads[2] = {0, 0};
+  static constexpr int NCAND = 6;
   double tuned_ms[2][NCAND] = {};
 };
 
@@ -1056,11 +1057,21 @@ int fgb_get_option(fgb_solver* s, const char* key, double* value) {
   else if (k == "lu_wait_skew") *value = s->wait_skew;
   else if (k == "lu_prefetch") *value = s->lu_prefetch;
   else if (k == "batch") *value = s->batch;
+  else if (k.rfind("lu_trial_ms", 0) == 0) {
+    // "lu_trial_msP_C": the first group's autotuner trial C (0..5) in precision P (64 / 32), ms
+    const int pk = k.compare(11, 2, "32") == 0 ? 1 : 0;
+    const int c = k.size() > 14 ? std::atoi(k.c_str() + 14) : -1;
+    if (c < 0 || c >= LuGroupData::NCAND || s->lu_groups.empty())
+      return fail(FGB_ERR_ARG, "unknown option " + k);
+    *value = s->lu_groups[0].tuned_ms[pk][c];
+  }
   else if (k == "lu_tuned" || k == "lu_tuned32") {
-    // first LU group, FP64 (lu_tuned) or FP32 sweeps: 10 x lu_mode + CTAs per SM (-1: not tuned)
+    // first LU group, FP64 (lu_tuned) or FP32 sweeps: 1000 x warps per CTA
+    // (dataflow) + 10 x lu_mode + CTAs per SM (-1: not tuned)
     const int pk = k == "lu_tuned32" ? 1 : 0;
-    *value = (s->lu_groups.empty() || s->lu_groups[0].tuned_mode[pk] < 0)
-                 ? -1. : 10. * s->lu_groups[0].tuned_mode[pk] + s->lu_groups[0].tuned_per_sm[pk];
+    const LuGroupData* g = s->lu_groups.empty() ? nullptr : &s->lu_groups[0];
+    *value = (!g || g->tuned_mode[pk] < 0)
+                 ? -1. : 1000. * (g->tuned_threads[pk] / 32) + 10. * g->tuned_mode[pk] + g->tuned_per_sm[pk];
   }
   else if (k == "autotune") *value = s->autotune;
   else return fail(FGB_ERR_ARG, "unknown option " + k);
@@ -1742,6 +1753,7 @@ static LuGroup group_launch(fgb_solver* s, LuGroupData& g, LuZone* tab) {
   LuGroup L{};
   L.persistent = s->lu_mode;
   L.flow_per_sm = 0;
+  L.flow_threads = 0;
   L.grid_cap = s->lu_grid;
   L.fp32 = s->lu_precision == 32;
   L.bar = s->bar; L.err = s->derr;
@@ -2430,15 +2442,17 @@ static int compute_steps(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin
           if (!s->capturing) CK(cudaEventRecord(g.ev[(g.slot + LuGroupData::NSLOT - 1) % LuGroupData::NSLOT], s->st));
           // autotuner: on the group's first solve (schedule "auto", the
           // default lu_mode 2 with autotune on), time the grid-barrier sweep
-          // and the dataflow sweep with one, two and four CTAs per SM (as
-          // many as are resident, at most) on this very solve -- a solve
-          // reads W^p, the residual and the coefficients and writes only its
-          // own outputs, so repeating it changes nothing -- and keep the
-          // fastest for the rest of the run
+          // and the dataflow sweep with 8 warps a CTA and one, two or four
+          // CTAs per SM (as many as are resident, at most), or 4 warps a CTA
+          // and one or two, on this very solve -- a solve reads W^p, the
+          // residual and the coefficients and writes only its own outputs,
+          // so repeating it changes nothing -- and keep the fastest for the
+          // rest of the run
           const int pk = s->lu_precision == 32 ? 1 : 0;
           if (s->autotune && s->lu_mode == 2 && g.tuned_mode[pk] < 0 && !s->profile) {
             constexpr int NC = LuGroupData::NCAND;
-            const int cand_mode[NC] = {1, 2, 2, 2}, cand_per[NC] = {0, 1, 2, 4};
+            const int cand_mode[NC] = {1, 2, 2, 2, 2, 2}, cand_per[NC] = {0, 1, 2, 4, 1, 2};
+            const int cand_thr[NC] = {0, 256, 256, 256, 128, 128};
             cudaEvent_t e0 = ev_get(s), e1 = ev_get(s);
             float best = 1e30f;
             for (int c = 0; c < NC; c++) {
@@ -2446,6 +2460,7 @@ static int compute_steps(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin
               LuGroup Lc = group_launch(s, g, td);
               Lc.persistent = cand_mode[c];
               Lc.flow_per_sm = cand_per[c];
+              Lc.flow_threads = cand_thr[c];
               CK(cudaEventRecord(e0, s->st));
               CK(launch_lusgs(th, Lc, s->st));
               CK(cudaEventRecord(e1, s->st));
@@ -2453,7 +2468,11 @@ static int compute_steps(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin
               float ms = 0.f;
               CK(cudaEventElapsedTime(&ms, e0, e1));
               g.tuned_ms[pk][c] = ms;
-              if (ms < best) { best = ms; g.tuned_mode[pk] = cand_mode[c]; g.tuned_per_sm[pk] = cand_per[c]; }
+              if (ms < best) {
+                best = ms;
+                g.tuned_mode[pk] = cand_mode[c]; g.tuned_per_sm[pk] = cand_per[c];
+                g.tuned_threads[pk] = cand_thr[c];
+              }
             }
             s->pool.push_back(e0);
             s->pool.push_back(e1);
@@ -2464,6 +2483,7 @@ static int compute_steps(fgb_solver* s, int nitrun, int nstep_deb, int nstep_fin
           if (g.tuned_mode[pk] > 0 && s->lu_mode == 2 && s->autotune) {
             L.persistent = g.tuned_mode[pk];
             L.flow_per_sm = g.tuned_per_sm[pk];
+            L.flow_threads = g.tuned_threads[pk];
           }
           // a replayed sweep publishes the marks fixed at recording: clear
           // what earlier solves left

@@ -112,6 +112,7 @@ int lusgs_flow_chunk();
 struct LuGroup {
   int persistent;           // 0 one launch per plane, 1 grid barrier, 2 dataflow
   int flow_per_sm;          // dataflow: CTAs per SM (0: one)
+  int flow_threads;         // dataflow: threads per CTA (0: 256; a multiple of 32, at most 256)
   FlowArgs flow;
   int grid_cap;             // > 0: at most this many CTAs in the persistent sweep
   int fp32;

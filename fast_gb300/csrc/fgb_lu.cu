@@ -1240,20 +1240,22 @@ static cudaError_t sweep_t(const Zone& z, const LuFields& f, const PlaneData<T>&
                            cudaStream_t st) {
   cudaError_t e;
   if (L.persistent == 2) {
-    static int grids[64] = {};   // per instantiation and device: resident CTAs
+    // CTA size: L.flow_threads (the autotuner's choice, a whole number of
+    // warps), by default FLOW_THREADS
+    const int threads = L.flow_threads > 0 ? L.flow_threads : FLOW_THREADS;
+    if (threads % 32 != 0 || threads > FLOW_THREADS) return cudaErrorInvalidValue;
+    const int wpc = threads / 32;
+    static int per_sm[64][FLOW_THREADS / 32 + 1] = {};   // per instantiation, device, CTA size
     int dev = 0;
     e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (grids[dev] == 0) {
-      int nsm = 0, per = 0;
-      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      if (e != cudaSuccess) return e;
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_flow<TYP, T, NV, MULTI>,
-                                                        FLOW_THREADS, 0);
+    if (per_sm[dev][wpc] == 0) {
+      int per = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lusgs_flow<TYP, T, NV, MULTI>, threads, 0);
       if (e != cudaSuccess) return e;
       if (per < 1) return cudaErrorLaunchOutOfResources;
-      grids[dev] = nsm * per;
+      per_sm[dev][wpc] = per;
     }
     // CTAs per SM: L.flow_per_sm (the autotuner's choice), by default one
     // (8 warps), measured faster than filling every resident slot on one
@@ -1261,13 +1263,12 @@ static cudaError_t sweep_t(const Zone& z, const LuFields& f, const PlaneData<T>&
     int nsm_ = 0;
     e = cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    const int per_max = grids[dev] / (nsm_ > 0 ? nsm_ : 1);
-    const int per_use = L.flow_per_sm > 0 ? std::min(L.flow_per_sm, per_max) : 1;
+    const int per_use = L.flow_per_sm > 0 ? std::min(L.flow_per_sm, per_sm[dev][wpc]) : 1;
     int grid = nsm_ * per_use;
     if (L.grid_cap > 0 && L.grid_cap < grid) grid = L.grid_cap;
     e = cudaMemsetAsync(L.flow.ticket, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    lusgs_flow<TYP, T, NV, MULTI><<<grid, FLOW_THREADS, 0, st>>>(z, p, f, L.flow);
+    lusgs_flow<TYP, T, NV, MULTI><<<grid, threads, 0, st>>>(z, p, f, L.flow);
     return cudaGetLastError();
   }
   if (L.persistent) {

@@ -125,10 +125,11 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * to pick the batched face kernels' block size by timing the candidates on
  * the first batch of each kind (kept per device for the process), and the
  * LU-SGS schedule of each zone group and sweep precision by timing the
- * grid-barrier sweep and the dataflow sweep with 1, 2 and 4 CTAs per SM on
- * its first solve.  fgb_get_option also reads "lu_tuned" / "lu_tuned32":
- * the first group's FP64 / FP32 choice as 10 x lu_mode + CTAs per SM (-1
- * before the first solve). */
+ * grid-barrier sweep and the dataflow sweep (CTAs of 8 warps, 1, 2 or 4 per
+ * SM; CTAs of 4 warps, 1 or 2 per SM) on its first solve.  fgb_get_option
+ * also reads "lu_tuned" / "lu_tuned32": the first group's FP64 / FP32
+ * choice as 1000 x warps per CTA (dataflow) + 10 x lu_mode + CTAs per SM
+ * (-1 before the first solve). */
 int fgb_set_option(fgb_solver* s, const char* key, double value);
 int fgb_get_option(fgb_solver* s, const char* key, double* value);
 
