@@ -316,9 +316,10 @@ template <int TYP, typename T>
 __device__ __forceinline__ void nb_normal(const Zone& z, int d, int64_t lta, int64_t ltb, T& tx,
                                           T& ty, T& tz) {
   if (TYP == Z3DCART) {
-    tx = d == 0 ? T(z.tcx) : T(0);
-    ty = d == 1 ? T(z.tcy) : T(0);
-    tz = d == 2 ? T(z.tcz) : T(0);
+    constexpr bool F32 = sizeof(T) == 4;
+    tx = d == 0 ? (F32 ? T(z.ftc[0]) : T(z.tcx)) : T(0);
+    ty = d == 1 ? (F32 ? T(z.ftc[1]) : T(z.tcy)) : T(0);
+    tz = d == 2 ? (F32 ? T(z.ftc[2]) : T(z.tcz)) : T(0);
   } else if (TYP == Z2D) {   // lu_{i,j}_2d.for: two components
     const double* M = d == 0 ? z.ti : z.tj;
     const int64_t m = z.ndm;
@@ -374,8 +375,9 @@ __host__ __device__ constexpr int qn_slot() {   // the slot of qn + cs
 template <int TYP, typename T>
 __device__ __forceinline__ void bentries(const Zone& z, int d, T u, T v, T w, T t, T tcx, T tcy,
                                          T tcz, T* e) {
-  const T gam1 = T(z.gam), gamm1 = T(z.gam - 1.), cp = T(z.gam * z.cv),
-          gam2 = T((z.gam - 1.) - 1.);
+  constexpr bool F32 = sizeof(T) == 4;   // the zone's constants in precision T, no conversion
+  const T gam1 = F32 ? T(z.fgam) : T(z.gam), gamm1 = F32 ? T(z.fgm1) : T(z.lgm1),
+          cp = F32 ? T(z.fcp) : T(z.lcp), gam2 = F32 ? T(z.fgm2) : T(z.lgm2);
   T q2 = T(.5) * (u * u + v * v + w * w);
   T h = cp * t + q2;
   T ph2 = gamm1 * q2;
@@ -425,14 +427,14 @@ __device__ __forceinline__ T bsum(const T* e, T cs, int idx, int slot) {
 }
 template <int TYP, int D, typename T, int MODE>
 __device__ __forceinline__ void bmatvec(const Zone& z, const T* e, T cs, const T o[5], T b[5]) {
-  // cartesian: tc_D (gam - 1), a zone constant (FP64: evaluated once on the host)
-  auto tcg = [&](double tc) -> T {
-    return sizeof(T) == 8 ? T(z.ctcg[D]) : T(tc) * T(z.gam - 1.);
-  };
+  // cartesian: tc_D (gam - 1), a zone constant (FP64: evaluated once on the
+  // host; FP32: the product of the two FP32 roundings)
+  constexpr bool F32 = sizeof(T) == 4;
+  auto tcg = [&](double) -> T { return F32 ? T(z.ftc[D]) * T(z.fgm1) : T(z.ctcg[D]); };
   auto S = [&](int m) { return bsum<TYP, D, T, MODE>(e, cs, sum_index<TYP>(D, m), m); };
   if (TYP == Z3DCART) {
     if (D == 0) {
-      const T tcx = T(z.tcx), b25 = tcg(z.tcx);
+      const T tcx = F32 ? T(z.ftc[0]) : T(z.tcx), b25 = tcg(z.tcx);
       const T s22 = S(0), s33 = S(1), s55 = S(2);
       b[0] = cs * o[0] + tcx * o[1];
       b[1] = e[0] * o[0] + s22 * o[1] + e[2] * o[2] + e[3] * o[3] + b25 * o[4];
@@ -440,7 +442,7 @@ __device__ __forceinline__ void bmatvec(const Zone& z, const T* e, T cs, const T
       b[3] = e[7] * o[0] + e[8] * o[1] + s33 * o[3];
       b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + s55 * o[4];
     } else if (D == 1) {
-      const T tcy = T(z.tcy), b35 = tcg(z.tcy);
+      const T tcy = F32 ? T(z.ftc[1]) : T(z.tcy), b35 = tcg(z.tcy);
       const T s22 = S(0), s33 = S(1), s55 = S(2);
       b[0] = cs * o[0] + tcy * o[2];
       b[1] = e[0] * o[0] + s22 * o[1] + e[2] * o[2];
@@ -448,7 +450,7 @@ __device__ __forceinline__ void bmatvec(const Zone& z, const T* e, T cs, const T
       b[3] = e[7] * o[0] + e[8] * o[2] + s22 * o[3];
       b[4] = e[9] * o[0] + e[10] * o[1] + e[11] * o[2] + e[12] * o[3] + s55 * o[4];
     } else {
-      const T tcz = T(z.tcz), b45 = tcg(z.tcz);
+      const T tcz = F32 ? T(z.ftc[2]) : T(z.tcz), b45 = tcg(z.tcz);
       const T s22 = S(0), s44 = S(1), s55 = S(2);
       b[0] = cs * o[0] + tcz * o[3];
       b[1] = e[0] * o[0] + s22 * o[1] + e[2] * o[3];
@@ -575,7 +577,6 @@ __device__ __forceinline__ void store_dio(float* dst, const float (&x)[NV]) {
 // CTA stages its records in shared memory ordered by anti-diagonal and then
 // writes each anti-diagonal as one contiguous span of records.
 constexpr int GT_I = 16, GT_J = 8, GT_N = GT_I * GT_J;
-
 template <int TYP, typename T>
 struct GatherSmem {
   static constexpr int CH = Rec<TYP, T>::SIZE * (int)sizeof(T) / 16;   // 16-byte chunks per record
@@ -800,7 +801,7 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
       T u = __ldcg(q), vv = __ldcg(q + 1), w = __ldcg(q + 2), t = __ldcg(q + 3);
       T tx, ty, tz;
       if (TYP == Z3DCART) {
-        tx = T(0); ty = T(0); tz = T(z.tcz);
+        tx = T(0); ty = T(0); tz = sizeof(T) == 4 ? T(z.ftc[2]) : T(z.tcz);
       } else {
         int64_t ii, jj, kk;
         unpack(p.cells[n], ii, jj, kk);
@@ -855,8 +856,9 @@ __device__ __forceinline__ void run_cell(const Zone& z, const PlaneData<T>& p, c
   if (!UPPER || !f.inplace) return;  // otherwise the Newton update runs after the sweep
   // in place: the k-1 neighbour needs this cell's new state in the next plane
   T nw[5];
-  const T cvinv = sizeof(T) == 8 ? T(z.cvinv) : T(1.) / T(z.cv);
-  newton<T, TYP == Z2D>(T(z.cv), cvinv, o.st[0], o.st[1], o.st[2], o.st[3], o.st[4], x, nw);
+  const T cvinv = sizeof(T) == 8 ? T(z.cvinv) : T(z.fcvinv);
+  newton<T, TYP == Z2D>(sizeof(T) == 8 ? T(z.cv) : T(z.fcv), cvinv, o.st[0], o.st[1], o.st[2], o.st[3],
+                        o.st[4], x, nw);
   T* q = p.nst + g * 4;
 #pragma unroll
   for (int v = 0; v < 4; v++) q[v] = nw[v + 1];
@@ -1201,7 +1203,7 @@ __global__ void __launch_bounds__(GT_N) lu_newton(Zone z, LuFields f, const T* _
               d4 = float(s_dio[q * DIO + 4]);
   const double ron = ro + double(d0);
   const float r1 = 1.f / float(ron);
-  const float fu = float(u), fv = float(v), fw = float(w), cv = float(z.cv);
+  const float fu = float(u), fv = float(v), fw = float(w), cv = z.fcv;
   const float e = cv * float(tt) + 0.5f * (fu * fu + fv * fv + fw * fw);
   const float du = (d1 - fu * d0) * r1, dv = (d2 - fv * d0) * r1;
   const float dw = TWO_D ? 0.f : (d3 - fw * d0) * r1;   // 2-d: w = 0
