@@ -577,6 +577,7 @@ __device__ __forceinline__ void store_dio(float* dst, const float (&x)[NV]) {
 // CTA stages its records in shared memory ordered by anti-diagonal and then
 // writes each anti-diagonal as one contiguous span of records.
 constexpr int GT_I = 16, GT_J = 8, GT_N = GT_I * GT_J;
+
 template <int TYP, typename T>
 struct GatherSmem {
   static constexpr int CH = Rec<TYP, T>::SIZE * (int)sizeof(T) / 16;   // 16-byte chunks per record
