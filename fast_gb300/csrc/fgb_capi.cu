@@ -684,8 +684,8 @@ static void fill_zone(ZoneData& Z, const double* ti, const double* tj, const dou
   z.ctc2[2] = std::sqrt(z.tcz * z.tcz);
   z.cdtv = z.dtc / vol[0];
   z.ctcg[0] = z.tcx * (z.gam - 1.); z.ctcg[1] = z.tcy * (z.gam - 1.); z.ctcg[2] = z.tcz * (z.gam - 1.);
-  z.lgm1 = z.gam - 1.; z.lcp = z.gam * z.cv; z.lgm2 = (z.gam - 1.) - 1.;
-  z.fgam = (float)z.gam; z.fgm1 = (float)z.lgm1; z.fcp = (float)z.lcp; z.fgm2 = (float)z.lgm2;
+  z.fgam = (float)z.gam; z.fgm1 = (float)(z.gam - 1.); z.fcp = (float)(z.gam * z.cv);
+  z.fgm2 = (float)((z.gam - 1.) - 1.);
   z.ftc[0] = (float)z.tcx; z.ftc[1] = (float)z.tcy; z.ftc[2] = (float)z.tcz;
   z.fcv = (float)z.cv;
   { volatile float one = 1.f; z.fcvinv = one / z.fcv; }   // an IEEE FP32 quotient, as the device's

@@ -59,12 +59,11 @@ struct Zone {
   // each direction and dtc / vol
   double ctc2[3], cdtv;
   double ctcg[3];  // tc_d (gam - 1) of each direction (LU-SGS B entries)
-  // the other constants of the LU-SGS B entries (lu_*.for), evaluated once
-  // on the host with the device's IEEE operations: gam - 1, gam cv,
-  // (gam - 1) - 1; and their FP32 roundings with those of gam, tc_d, cv and
-  // 1/cv for the FP32 sweeps (a conversion from FP64 runs on the FP64 pipe,
-  // one warp instruction per 64 cycles, on the sweep's critical path)
-  double lgm1, lcp, lgm2;
+  // FP32 roundings of the constants of the LU-SGS B entries (lu_*.for) and
+  // of the Newton update -- gam, gam - 1, gam cv, (gam - 1) - 1, tc_d, cv,
+  // 1/cv -- evaluated once on the host with the device's IEEE operations, for
+  // the FP32 sweeps (a conversion from FP64 runs on the FP64 pipe, one warp
+  // instruction per 64 cycles, on the sweep's critical path)
   float fgam, fgm1, fcp, fgm2, ftc[3], fcv, fcvinv, fpad;
   double rgpgam;   // rgp * gam (the sound speed squared is rgp gam T)
   double cfl;      // CFL number of the local time step (DTLOC = 1)

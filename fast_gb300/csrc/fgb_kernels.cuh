@@ -36,7 +36,7 @@ cudaError_t launch_wall_corr(const Zone& z, const double* q, double* drodm, cons
 // kind (the same template instance).  The entries travel in the kernel
 // parameter (__grid_constant__, at most 32 KB); block b of the launch works
 // on zone m with bstart[m] <= b < bstart[m + 1] (bstart[nz] = grid size).
-constexpr int BATCH_MAX = 38;
+constexpr int BATCH_MAX = 40;
 struct FaceEntry { Zone z; const double* q; const double* xmut; double* F[3]; };
 struct FaceBatch { int nz; int block; int64_t bstart[BATCH_MAX + 1]; FaceEntry e[BATCH_MAX]; };
 struct StageEntry { Zone z; StageArgs a; };

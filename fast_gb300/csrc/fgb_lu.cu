@@ -375,9 +375,9 @@ __host__ __device__ constexpr int qn_slot() {   // the slot of qn + cs
 template <int TYP, typename T>
 __device__ __forceinline__ void bentries(const Zone& z, int d, T u, T v, T w, T t, T tcx, T tcy,
                                          T tcz, T* e) {
-  constexpr bool F32 = sizeof(T) == 4;   // the zone's constants in precision T, no conversion
-  const T gam1 = F32 ? T(z.fgam) : T(z.gam), gamm1 = F32 ? T(z.fgm1) : T(z.lgm1),
-          cp = F32 ? T(z.fcp) : T(z.lcp), gam2 = F32 ? T(z.fgm2) : T(z.lgm2);
+  constexpr bool F32 = sizeof(T) == 4;   // FP32: the zone's FP32 constants, no conversion
+  const T gam1 = F32 ? T(z.fgam) : T(z.gam), gamm1 = F32 ? T(z.fgm1) : T(z.gam - 1.),
+          cp = F32 ? T(z.fcp) : T(z.gam * z.cv), gam2 = F32 ? T(z.fgm2) : T((z.gam - 1.) - 1.);
   T q2 = T(.5) * (u * u + v * v + w * w);
   T h = cp * t + q2;
   T ph2 = gamm1 * q2;

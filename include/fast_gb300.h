@@ -120,7 +120,7 @@ int fgb_set_wall_distance(fgb_solver* s, int zone, const double* dist);
  * 0 not to (same results);
  * "batch": 1 (default) to run the coefficient, Spalart-Allmaras source,
  * face and balance / update kernels of several zones as one launch per kind
- * of zone (zone type, scheme, slope, viscosity, NEQ; up to 38 zones a
+ * of zone (zone type, scheme, slope, viscosity, NEQ; up to 40 zones a
  * launch), 0 for per-zone launches (same results); "autotune": 1 (default)
  * to pick the batched face kernels' block size by timing the candidates on
  * the first batch of each kind (kept per device for the process), and the
