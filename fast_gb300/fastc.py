@@ -492,7 +492,7 @@ def _createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
         shape = prim[0].shape
         n = prim[0].size
         for suffix in ("", "_M1", "_P1"):
-            buf = np.empty((len(names), n), dtype=np.float64)
+            buf = _level_buffer(len(names), n)
             kept = [I.getNodeFromName1(sol, nm + suffix) for nm in names] if suffix else []
             if suffix and all(k is not None for k in kept):
                 src = [k[1] for k in kept]          # a restart: the level is kept
@@ -512,6 +512,43 @@ def _createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
         if rmConsVars:
             sol[2] = [c for c in sol[2] if c[0] not in CONS[1:]]
     return first_iter
+
+
+def _huge_page_bytes():
+    try:
+        with open("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size") as f:
+            return int(f.read())
+    except (OSError, ValueError):
+        return 0
+
+
+def _level_buffer(rows, n):
+    """The (rows, n) float64 array of one time level.  The solver copies the
+    levels to and from the GPU every step; on Linux, a level of at least one
+    transparent huge page is an anonymous mapping advised for huge pages
+    (madvise MADV_HUGEPAGE, before its pages are first touched), so that the
+    copy engines translate a few huge pages instead of one page-table entry
+    per base page (repeated copies of several 0.7 GB levels missed in the
+    I/O translation caches and ran 20 times slower).  Elsewhere, or if the
+    mapping cannot be made, a plain numpy array."""
+    nbytes = rows * n * 8
+    hp = _huge_page_bytes()
+    if hp <= 0 or nbytes < hp:
+        return np.empty((rows, n), dtype=np.float64)
+    try:
+        import ctypes
+        import mmap
+        size = -(-nbytes // hp) * hp
+        m = mmap.mmap(-1, size + hp, flags=mmap.MAP_PRIVATE | mmap.MAP_ANONYMOUS)
+        base = ctypes.addressof(ctypes.c_char.from_buffer(m))
+        start = -(-base // hp) * hp
+        libc = ctypes.CDLL(None, use_errno=True)
+        libc.madvise.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+        libc.madvise(ctypes.c_void_p(start), ctypes.c_size_t(size), 14)   # MADV_HUGEPAGE
+        return np.frombuffer(m, dtype=np.float64, count=rows * n,
+                             offset=start - base).reshape(rows, n)
+    except (OSError, ValueError, AttributeError, TypeError):
+        return np.empty((rows, n), dtype=np.float64)
 
 
 def compactArray(z, level):

@@ -281,7 +281,10 @@ def warmup(t, tc=None, graph=None, infos_ale=None, Adjoint=False, tmy=None, list
         for suf in ("", "_M1", "_P1"):
             arr = FastC.compactArray(z, suf).reshape(-1)
             if arr.flags.c_contiguous and arr.nbytes > 0:
-                solver.pin(arr)
+                try:
+                    solver.pin(arr)
+                except RuntimeError:   # not page-lockable: copies stay staged by the driver
+                    pass
     _upload(t)
     for lvl in (0, 1):
         solver.apply_bc(lvl)
