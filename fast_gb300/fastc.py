@@ -491,8 +491,10 @@ def _createPrimVars(t, omp_mode=0, rmConsVars=True, Adjoint=False):
                 prim.append((rnu[1] if rnu is not None else ronut_inf) / prim[0])
         shape = prim[0].shape
         n = prim[0].size
-        for suffix in ("", "_M1", "_P1"):
-            buf = _level_buffer(len(names), n)
+        # one mapping per level: the host gave one 512 MB huge page to each of
+        # three mappings, and only one to a single mapping of three levels
+        bufs = [_level_buffers(1, len(names), n)[0] for _ in range(3)]
+        for suffix, buf in zip(("", "_M1", "_P1"), bufs):
             kept = [I.getNodeFromName1(sol, nm + suffix) for nm in names] if suffix else []
             if suffix and all(k is not None for k in kept):
                 src = [k[1] for k in kept]          # a restart: the level is kept
@@ -522,33 +524,36 @@ def _huge_page_bytes():
         return 0
 
 
-def _level_buffer(rows, n):
-    """The (rows, n) float64 array of one time level.  The solver copies the
-    levels to and from the GPU every step; on Linux, a level of at least one
-    transparent huge page is an anonymous mapping advised for huge pages
-    (madvise MADV_HUGEPAGE, before its pages are first touched), so that the
-    copy engines translate a few huge pages instead of one page-table entry
-    per base page (repeated copies of several 0.7 GB levels missed in the
-    I/O translation caches and ran 20 times slower).  Elsewhere, or if the
-    mapping cannot be made, a plain numpy array."""
+def _level_buffers(count, rows, n):
+    """`count` (rows, n) float64 arrays for time levels.  The solver copies
+    the levels to and from the GPU every step; on Linux, levels of at least
+    one transparent huge page live in one anonymous mapping advised for huge
+    pages (madvise MADV_HUGEPAGE before the first touch, MADV_COLLAPSE after
+    it for what fell back to base pages), so that the copy engines translate
+    a few huge pages instead of one page-table entry per base page (repeated
+    copies of three 0.7 GB levels in 64 KB pages missed in the translation
+    caches and ran 20 times slower).  Elsewhere, or if the mapping cannot be
+    made, plain numpy arrays."""
     nbytes = rows * n * 8
     hp = _huge_page_bytes()
     if hp <= 0 or nbytes < hp:
-        return np.empty((rows, n), dtype=np.float64)
+        return [np.empty((rows, n), dtype=np.float64) for _ in range(count)]
     try:
         import ctypes
         import mmap
-        size = -(-nbytes // hp) * hp
+        size = -(-count * nbytes // hp) * hp
         m = mmap.mmap(-1, size + hp, flags=mmap.MAP_PRIVATE | mmap.MAP_ANONYMOUS)
         base = ctypes.addressof(ctypes.c_char.from_buffer(m))
         start = -(-base // hp) * hp
         libc = ctypes.CDLL(None, use_errno=True)
         libc.madvise.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
         libc.madvise(ctypes.c_void_p(start), ctypes.c_size_t(size), 14)   # MADV_HUGEPAGE
-        return np.frombuffer(m, dtype=np.float64, count=rows * n,
-                             offset=start - base).reshape(rows, n)
+        whole = np.frombuffer(m, dtype=np.float64, count=size // 8, offset=start - base)
+        whole.fill(0.)   # first touch: huge pages where the kernel has them
+        libc.madvise(ctypes.c_void_p(start), ctypes.c_size_t(size), 25)   # MADV_COLLAPSE (6.1+)
+        return [whole[q * rows * n:(q + 1) * rows * n].reshape(rows, n) for q in range(count)]
     except (OSError, ValueError, AttributeError, TypeError):
-        return np.empty((rows, n), dtype=np.float64)
+        return [np.empty((rows, n), dtype=np.float64) for _ in range(count)]
 
 
 def compactArray(z, level):

@@ -1,6 +1,6 @@
-"""Time-level arrays (fastc._level_buffer): a level of at least one
-transparent huge page is a huge-page-advised anonymous mapping, aligned to
-the huge page; smaller ones are plain numpy arrays.  Either is a writable,
+"""Time-level arrays (fastc._level_buffers): the levels of a zone of at
+least one transparent huge page each share one huge-page-advised anonymous
+mapping, aligned to the huge page; smaller ones are plain numpy arrays.  Either is a writable,
 C-contiguous (rows, n) float64 array, and a level can be saved, swapped and
 reloaded like any other tree array."""
 import numpy as np
@@ -11,9 +11,9 @@ from fast_gb300 import pytree as I
 
 
 def test_small_level_is_a_plain_array():
-    a = fastc._level_buffer(5, 1000)
-    assert a.shape == (5, 1000) and a.dtype == np.float64
-    assert a.flags.c_contiguous and a.flags.writeable
+    for a in fastc._level_buffers(3, 5, 1000):
+        assert a.shape == (5, 1000) and a.dtype == np.float64
+        assert a.flags.c_contiguous and a.flags.writeable
 
 
 def test_large_level_is_aligned_and_usable():
@@ -21,12 +21,14 @@ def test_large_level_is_aligned_and_usable():
     if hp <= 0:
         pytest.skip("no transparent huge pages on this host")
     n = hp // 8 // 5 + 1000          # a level just over one huge page
-    a = fastc._level_buffer(5, n)
-    assert a.shape == (5, n) and a.flags.c_contiguous and a.flags.writeable
-    assert a.ctypes.data % hp == 0
-    a[:] = 3.0
-    a[4, -1] = 7.0
-    assert float(a.sum()) == 3.0 * (5 * n - 1) + 7.0
+    levels = fastc._level_buffers(3, 5, n)
+    assert levels[0].ctypes.data % hp == 0
+    for q, a in enumerate(levels):
+        assert a.shape == (5, n) and a.flags.c_contiguous and a.flags.writeable
+        a[:] = 3.0 + q
+        a[4, -1] = 7.0
+    for q, a in enumerate(levels):   # disjoint
+        assert float(a.sum()) == (3.0 + q) * (5 * n - 1) + 7.0
 
 
 def test_tree_levels_behave_like_numpy_arrays():
