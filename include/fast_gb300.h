@@ -48,7 +48,12 @@ int fgb_destroy(fgb_solver* s);
  * the BC block appended by _BCcompact, FastC/FastC/PyTree.py:2788).
  * ti, tj, tk, vol: the metric of fasts.allocate_metric
  * (FastS/FastS/Metric/allocate_metric.cpp, list slot METRIC_TI).
- * The returned zone id is the zone's position in the solver (0, 1, ...). */
+ * The returned zone id is the zone's position in the solver (0, 1, ...).
+ * Refused with FGB_ERR_ARG: explicit schemes other than RK1 / RK2 / RK3
+ * with nssiter = rk, explicit local time stepping (EXPLOC != 0, which the
+ * reference's C layer refuses too) and moving meshes (LALE != 0), DTLOC
+ * other than 0 / 1, LU-SGS with nb_relax > 1 or lu_match, and zones or
+ * schemes the kernels do not cover (the message names them). */
 int fgb_add_zone(fgb_solver* s, const int64_t* param_int, int64_t n_int,
                  const double* param_real, int64_t n_real,
                  const double* ti, const double* tj, const double* tk,
