@@ -5,7 +5,8 @@ x = 0.5) on nx x 4 x 4 cells, extrapolation BCs at the x ends
 t = 0.2.  The density matches the exact solution (the exact Riemann solver
 of Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics, ch. 4,
 restated below) with an L1 error that falls with the grid at the rate
-discontinuities allow (about 0.85 with the minmod slope, 0.65 first order),
+discontinuities allow (about 0.85 with the minmod slope, 0.65 first order,
+0.9 for AUSM+(P) with the unlimited o3 slope or with o3sc's shock sensor),
 the Roe (with Harten's fix) and AUSM+(P) fluxes alike, and the solution is
 exactly uniform across y and z.  Slip wall (bvbs_wall_inviscid.for): a
 uniform flow at u = 0.5 into a wall at x = 1 reflects as a shock, the
@@ -105,6 +106,8 @@ def _sod_l1(oracle_mod, nx, scheme, slope, t_end=0.2):
 
 @pytest.mark.parametrize("scheme,slope,bound,rate", [("roe", "minmod", 0.0055, 0.7),
                                                      ("ausmpred", "minmod", 0.0045, 0.7),
+                                                     ("ausmpred", "o3", 0.0035, 0.8),
+                                                     ("ausmpred", "o3sc", 0.0037, 0.8),
                                                      ("roe", "o1", 0.015, 0.5)])
 def test_sod_shock_tube(oracle_mod, scheme, slope, bound, rate):
     e200 = _sod_l1(oracle_mod, 200, scheme, slope)
