@@ -73,7 +73,8 @@ def exact_sod(x, t, x0=0.5, g=1.4, rl=1.0, ul=0.0, pl=1.0, rr=0.125, ur=0.0, pr=
     return out
 
 
-def _sod_l1(oracle_mod, nx, scheme, slope, t_end=0.2):
+def sod_tree(nx, scheme, slope, t_end=0.2):
+    """Sod's tube on nx x 4 x 4 cells and the number of RK3 steps to t_end."""
     g = 1.4
     h = 1.0 / nx
     z = cases.cart_zone("sod", (0.0, 0.0, 0.0), (h, h, h), (nx, 4, 4))
@@ -90,6 +91,12 @@ def _sod_l1(oracle_mod, nx, scheme, slope, t_end=0.2):
     nsteps = int(math.ceil(t_end / (0.4 * h / (math.sqrt(g) + 1.0))))
     t = cases._tree([z], "Euler", {"temporal_scheme": "explicit", "rk": 3, "modulo_verif": 10 ** 6},
                     {"scheme": scheme, "slope": slope, "time_step": t_end / nsteps}, 0.5, 0.0, gamma=g)
+    return t, nsteps
+
+
+def _sod_l1(oracle_mod, nx, scheme, slope, t_end=0.2):
+    h = 1.0 / nx
+    t, nsteps = sod_tree(nx, scheme, slope, t_end)
     zd = fasts.zone_data(t, fasts.prepare(t))
     c = oracle_mod.Case(zd, ())
     c.apply_bc(0)

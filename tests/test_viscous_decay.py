@@ -60,7 +60,9 @@ def test_taylor_green_2d_decay_rate(oracle_mod):
     assert r32 > r64
 
 
-def _shear_decay_rate(oracle_mod, ny, mach=0.1, re=50.0, t_end=10.0):
+def shear_tree(ny, mach=0.1, re=50.0, t_end=10.0):
+    """The shear wave between no-slip walls on 4 x ny x 4 cells and the
+    number of RK3 steps to t_end."""
     gamma = 1.4
     h = 1.0 / ny
     z = cases.cart_zone("shear", (0.0, 0.0, 0.0), (h, h, h), (4, ny, 4))
@@ -77,6 +79,11 @@ def _shear_decay_rate(oracle_mod, ny, mach=0.1, re=50.0, t_end=10.0):
                     {"temporal_scheme": "explicit", "rk": 3, "modulo_verif": 10 ** 6},
                     {"scheme": "ausmpred", "slope": "o3", "time_step": t_end / nsteps},
                     mach, re, gamma=gamma, prandtl=0.71, sutherland=False)
+    return t, nsteps
+
+
+def _shear_decay_rate(oracle_mod, ny, mach=0.1, re=50.0, t_end=10.0):
+    t, nsteps = shear_tree(ny, mach, re, t_end)
     zd = fasts.zone_data(t, fasts.prepare(t))
     nu = float(zd[0]["pr"][11])
     c = oracle_mod.Case(zd, ())
