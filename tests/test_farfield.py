@@ -1,0 +1,51 @@
+"""Farfield boundaries let waves out (oracle, CPU): a small right-going
+acoustic pulse (a linear simple wave: dp = rho c du, drho = dp / c^2) on a
+Mach 0.5 free stream leaves a tube with farfield BCs at both ends
+(bvbs_farfield.for, characteristic states against the reference state);
+after it has crossed the boundary, less than 0.2 % of its amplitude remains
+in the tube (0.04-0.05 % measured), while extrapolation BCs at the same ends
+keep over 1 % (their inflow end is not non-reflecting)."""
+import math
+
+import numpy as np
+import pytest
+
+from fast_gb300 import cases, fasts
+
+
+def _left_over(oracle_mod, nx, bc, mach=0.5, t_end=0.6, amp=1e-3):
+    gamma = 1.4
+    h = 1.0 / nx
+    z = cases.cart_zone("pulse", (0.0, 0.0, 0.0), (h, h, h), (nx, 4, 4))
+    xc, _, _ = cases.cell_centers(z)
+    bump = amp * np.exp(-((xc - 0.5) / 0.05) ** 2)   # T = 1, R = 1 / gamma: c = 1
+    zero = np.zeros_like(xc)
+    cases.set_conservative(z, 1.0 + bump, mach + bump, zero, zero, (1.0 + gamma * bump) / gamma, gamma)
+    cases.add_bc(z, "b_imin", bc, "imin")
+    cases.add_bc(z, "b_imax", bc, "imax")
+    for f in ("jmin", "jmax", "kmin", "kmax"):
+        cases.add_bc(z, "per_" + f, "BCautoperiod", f)
+    nsteps = int(math.ceil(t_end / (0.4 * h / (1.0 + mach))))
+    t = cases._tree([z], "Euler", {"temporal_scheme": "explicit", "rk": 3, "modulo_verif": 10 ** 6},
+                    {"scheme": "ausmpred", "slope": "o3", "time_step": t_end / nsteps}, mach, 0.0,
+                    gamma=gamma)
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    c = oracle_mod.Case(zd, ())
+    c.apply_bc(0)
+    c.apply_bc(1)
+    pi = zd[0]["pi"]
+    nip, njp, nd = int(pi[0]), int(pi[1]), int(pi[41])
+
+    def deviation():
+        ro = np.array(c.z[0]["lv"][0][:nd]).reshape(-1, njp, nip)[2:-2, 2:-2, 2:-2]
+        return float(np.max(np.abs(ro - 1.0)))
+
+    d0 = deviation()
+    for it in range(1, nsteps + 1):
+        c.compute(it, 1, 3, 1, modulo_verif=10 ** 6)
+    return deviation() / d0
+
+
+def test_farfield_lets_an_acoustic_pulse_out(oracle_mod):
+    assert _left_over(oracle_mod, 100, "BCFarfield") < 2e-3
+    assert _left_over(oracle_mod, 100, "BCExtrapolate") > 1e-2
