@@ -49,3 +49,28 @@ def _left_over(oracle_mod, nx, bc, mach=0.5, t_end=0.6, amp=1e-3):
 def test_farfield_lets_an_acoustic_pulse_out(oracle_mod):
     assert _left_over(oracle_mod, 100, "BCFarfield") < 2e-3
     assert _left_over(oracle_mod, 100, "BCExtrapolate") > 1e-2
+
+
+def test_duct_relaxes_to_the_free_stream(oracle_mod):
+    """Inflow at imin (bvbs_inflow.for), outflow at imax (bvbs_outflow.for), a
+    slip wall at jmin and farfield at jmax, periodic in k: a 5 % smooth
+    perturbation of the free stream is carried out of the box and the state
+    relaxes to the reference state itself, geometrically (5e-9 after 1500 RK3
+    steps, 1e-14 after 3000)."""
+    t = cases.bc_box(n=(24, 12, 4), wall="BCWallInviscid", model="Euler", perturb=0.05,
+                     temporal="explicit", time_step=0.01)
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    c = oracle_mod.Case(zd, ())
+    c.apply_bc(0)
+    c.apply_bc(1)
+    pi, pr = zd[0]["pi"], zd[0]["pr"]
+    nip, njp, nd = int(pi[0]), int(pi[1]), int(pi[41])
+    free = np.array([pr[3], pr[19], pr[20], pr[21], pr[6]])   # ro, u, v, w, T of the reference state
+    dev = []
+    for it in range(1, 1501):
+        c.compute(it, 1, 3, 1, modulo_verif=10 ** 6)
+        if it % 500 == 0:
+            q = np.array(c.z[0]["lv"][0][:5 * nd]).reshape(5, -1, njp, nip)[:, 2:-2, 2:-2, 2:-2]
+            dev.append(float(np.max(np.abs(q - free[:, None, None, None]))))
+    assert dev[0] > dev[1] > dev[2]
+    assert dev[2] < 1e-7, dev
