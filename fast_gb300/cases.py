@@ -548,8 +548,25 @@ def _lagrange(x, width):
     return w
 
 
+def poly_field(X, Y, Z, degree):
+    """Density, u, v and temperature polynomial of degree `degree` in x and
+    y (uniform in the periodic z, whose ghost cells then hold the same
+    values), positive on [-10, 10]^2."""
+    s = [X / 10.0, Y / 10.0]
+    terms = [1.0, s[0], s[1]]
+    if degree >= 2:
+        terms += [s[0] * s[0], s[0] * s[1], s[1] * s[1]]
+    if degree >= 3:
+        terms += [s[0] ** 3, s[0] * s[1] ** 2]
+    if degree >= 4:
+        terms += [s[0] ** 4, s[0] ** 2 * s[1] ** 2, s[1] ** 4]
+    def comb(c0, step):
+        return c0 + sum(step * (1.0 + 0.1 * q) * tm for q, tm in enumerate(terms[1:]))
+    return comb(1.0, 0.01), comb(0.5, 0.02), comb(0.0, 0.015), comb(1.0, 0.008)
+
+
 def overset_patch(n=(40, 40, 4), patch=(24, 20, 4), box=10.0, mach=0.5, types=(2,), shift=0.3,
-                  linear=False, numz=None):
+                  linear=False, numz=None, degree=None):
     """Overset (chimera) pair: zone 0 the periodic isentropic-vortex box
     [-box, box]^2 (n cells, periodic in every direction), zone 1 a finer
     cartesian patch over its centre (patch cells, steps 0.7 x zone 0's, k
@@ -560,7 +577,10 @@ def overset_patch(n=(40, 40, 4), patch=(24, 20, 4), box=10.0, mach=0.5, types=(2
     cell), molecules anchored so that they surround the receiver.  The
     patch's i / j faces carry no BC: their ghosts are the receivers, as
     behind a BCOverlap.  linear: a field linear in x, y, z instead of the
-    vortex (every interpolation reproduces it to round-off).
+    vortex (every interpolation reproduces it to round-off); degree d (1, 2,
+    4): primitive fields polynomial of degree d in x and y (the 27- and
+    125-point Lagrange molecules reproduce degree 2, the latter degree 4, to
+    round-off; see poly_field).
     Returns (t, transfers) with transfers as fgb_add_interp_transfer
     takes them (one dict)."""
     t = isentropic_vortex(n=n, box=box, mach=mach, numz=numz)
@@ -572,7 +592,11 @@ def overset_patch(n=(40, 40, 4), patch=(24, 20, 4), box=10.0, mach=0.5, types=(2
     z1 = cart_zone("patch", x1, (h1, h1, h0), patch)
     xc, yc, zc = cell_centers(z1)
     x0c, y0c, z0c = cell_centers(z0)
-    if linear:
+    if degree is not None:
+        for zz, (X, Y, Z) in ((z0, (x0c, y0c, z0c)), (z1, (xc, yc, zc))):
+            ro, u, v, T = poly_field(X, Y, Z, degree)
+            set_conservative(zz, ro, u, v, 0.0 * X, ro * T / 1.4, 1.4)
+    elif linear:
         for zz, (X, Y, Z) in ((z0, (x0c, y0c, z0c)), (z1, (xc, yc, zc))):
             ro = 1.0 + 0.01 * X + 0.02 * Y + 0.001 * Z
             set_conservative(zz, ro, 0.5 + 0.003 * X, 0.002 * Y, 0.0 * X, 1.0 / 1.4 + 0.001 * X, 1.4)

@@ -43,6 +43,28 @@ def test_interpolation_reproduces_linear_fields(oracle_mod, types):
     assert np.max(np.abs(q[2, r] - 0.002 * Y[r])) < 1e-14
 
 
+@pytest.mark.parametrize("typ,exact,inexact", [(2, 1, 2), (3, 2, 4), (5, 4, None)])
+def test_interpolation_polynomial_degree(oracle_mod, typ, exact, inexact):
+    """Each molecule reproduces the polynomials of its degree to round-off
+    and not those of the next one: trilinear (type 2) degree 1, the 27-point
+    Lagrange molecule (type 3) degree 2, the 125-point one (type 5) degree 4
+    in x and y."""
+    def err(deg):
+        t, tc = cases.overset_patch(types=(typ,), degree=deg)
+        zd = fasts.zone_data(t, fasts.prepare(t))
+        c = oracle_mod.Case(zd, tc)
+        c.apply_bc(0)
+        xc, yc, zc = cases.cell_centers(I.getZones(t)[1])
+        X, Y, Z = (a.ravel(order="F") for a in (xc, yc, zc))
+        q = c.z[1]["lv"][0].reshape(5, -1)
+        r = tc[0]["rcv_idx"][_face_band(tc[0])]
+        ro, u, v, T = cases.poly_field(X[r], Y[r], Z[r], deg)
+        return max(float(np.max(np.abs(q[k, r] - f))) for k, f in ((0, ro), (1, u), (2, v), (4, T)))
+    assert err(exact) < 1e-13
+    if inexact is not None:
+        assert err(inexact) > 1e-7
+
+
 def test_tc_tree_round_trip():
     """connector.tc_tree writes the ID_ subregions FastS's tests build by
     hand; transfers_from_tc reads back the same arrays, a 1-to-1 list as
