@@ -5,7 +5,9 @@ U^2/4 (cos 2x + cos 2y) above the mean, T = 1, periodic box [0, 2 pi]^2,
 Laminar AUSM+(P) o3 (fluvisq_3dcart_*.for, mu constant: Sutherland off),
 explicit RK3, Mach 0.1, Re 100 (nu = 1e-3), to t = 20: the measured decay
 rate is 4 nu within 3 % on 32 x 32 cells and 0.5 % on 64 x 64, and it
-converges from above (the scheme's own dissipation vanishes with h).
+converges from above (the scheme's own dissipation vanishes with h).  On a
+curvilinear (wavy, general 3-d) mesh of the same box, fluvisq_3dfull_*.for
+with the full metric: within 6 % on 32 x 32 and 3 % on 64 x 64, converging.
 No-slip walls (bvbs_wall_viscous_adia.for): a shear wave u = U sin(pi y)
 between adiabatic walls at y = 0 and 1 decays as exp(-nu pi^2 t), its
 kinetic energy as exp(-2 nu pi^2 t) (Mach 0.1, Re 50, to t = 10): the
@@ -18,10 +20,12 @@ import numpy as np
 from fast_gb300 import cases, fasts
 
 
-def _decay_rate(oracle_mod, n, mach=0.1, re=100.0, t_end=20.0):
+def _decay_rate(oracle_mod, n, mach=0.1, re=100.0, t_end=20.0, wavy=0.0):
     gamma = 1.4
     h = 2 * math.pi / n
     z = cases.cart_zone("tgv2d", (0.0, 0.0, 0.0), (h, h, h), (n, n, 4))
+    if wavy:
+        cases.wave(z, wavy, (0.0, 0.0, 0.0), (2 * math.pi, 2 * math.pi, 4 * h))
     xc, yc, _ = cases.cell_centers(z)
     u = mach * np.sin(xc) * np.cos(yc)
     v = -mach * np.cos(xc) * np.sin(yc)
@@ -29,12 +33,13 @@ def _decay_rate(oracle_mod, n, mach=0.1, re=100.0, t_end=20.0):
     cases.set_conservative(z, p * gamma, u, v, np.zeros_like(u), p, gamma)
     for f in ("imin", "imax", "jmin", "jmax", "kmin", "kmax"):
         cases.add_bc(z, "per_" + f, "BCautoperiod", f)
-    nsteps = int(math.ceil(t_end / (0.4 * h / (mach + 1.0))))
+    nsteps = int(math.ceil(t_end / ((0.3 if wavy else 0.4) * h / (mach + 1.0))))
     t = cases._tree([z], "NSLaminar",
                     {"temporal_scheme": "explicit", "rk": 3, "modulo_verif": 10 ** 6},
                     {"scheme": "ausmpred", "slope": "o3", "time_step": t_end / nsteps},
                     mach, re, gamma=gamma, prandtl=0.71, sutherland=False)
     zd = fasts.zone_data(t, fasts.prepare(t))
+    assert int(zd[0]["pi"][25]) == (0 if wavy else 2)   # general / cartesian zone
     nu = float(zd[0]["pr"][11])          # mu / ro, ro = 1
     c = oracle_mod.Case(zd, ())
     c.apply_bc(0)
@@ -108,3 +113,11 @@ def test_shear_wave_between_no_slip_walls(oracle_mod):
     assert abs(r16 - 1.0) < 5e-3, r16
     assert abs(r32 - 1.0) < 1.5e-3, r32
     assert abs(r16 - 1.0) > 3.0 * abs(r32 - 1.0)
+
+
+def test_taylor_green_2d_decay_rate_curvilinear(oracle_mod):
+    r32 = _decay_rate(oracle_mod, 32, wavy=0.3)
+    r64 = _decay_rate(oracle_mod, 64, wavy=0.3)
+    assert abs(r32 - 1.0) < 0.07, r32
+    assert abs(r64 - 1.0) < 0.035, r64
+    assert abs(r32 - 1.0) > 1.7 * abs(r64 - 1.0)
