@@ -70,3 +70,25 @@ def test_o5_error_below_o3(oracle_mod):
     e3 = _wave_error(oracle_mod, 16, "ausmpred", "o3")
     p1, p2 = _orders(e5)
     assert e5[0] < 0.25 * e3 and p1 >= 1.6 and p2 >= 1.8, (e5, e3, p1, p2)
+
+
+def test_o3sc_is_o3_on_smooth_flow(oracle_mod):
+    """o3sc (o3_slope_var.for weighted by the shock sensor, sciacovelli.for)
+    keeps the o3 slope where the flow is smooth: the same error as o3 to
+    5e-5 relative, 1e-8 on the finest grid."""
+    for nx, tol in ((16, 1e-4), (32, 1e-4), (64, 1e-6)):
+        e3 = _wave_error(oracle_mod, nx, "ausmpred", "o3")
+        esc = _wave_error(oracle_mod, nx, "ausmpred", "o3sc")
+        assert abs(esc - e3) < tol * e3, (nx, e3, esc)
+
+
+def test_minmod_and_senseur(oracle_mod):
+    """The minmod slope clips the wave's extrema: between first and second
+    order (1.2 measured); the senseur scheme (SENSOR/fluFaceEuler.for, o3,
+    its dissipation switched off by the wiggle sensor on smooth data) is
+    second order with an error seven times below AUSM+(P) o3's on 16 cells."""
+    p1, p2 = _orders([_wave_error(oracle_mod, nx, "roe", "minmod") for nx in (16, 32, 64)])
+    assert 1.0 <= p1 <= 1.5 and 1.0 <= p2 <= 1.5, (p1, p2)
+    es = [_wave_error(oracle_mod, nx, "senseur", "o3") for nx in (16, 32, 64)]
+    assert es[0] < 0.2 * _wave_error(oracle_mod, 16, "ausmpred", "o3")
+    assert _orders(es)[1] >= 1.7, es
