@@ -74,3 +74,32 @@ def test_duct_relaxes_to_the_free_stream(oracle_mod):
             dev.append(float(np.max(np.abs(q - free[:, None, None, None]))))
     assert dev[0] > dev[1] > dev[2]
     assert dev[2] < 1e-7, dev
+
+
+@pytest.mark.parametrize("nature", ["global", "local"])
+def test_implicit_duct_relaxes_to_the_free_stream(oracle_mod, nature):
+    """The same duct with implicit dual time stepping (BDF2, LU-SGS,
+    ss_iteration 3, acoustic CFL about 1.6) and with the local time step
+    (time_step_nature 'local', CFL 10: tstb3_impli.for, BDF1) relaxes to the
+    reference state too: below 1e-4 after 200 steps (global) and 1e-7 after
+    300 (local)."""
+    from fast_gb300 import fastc
+    from fast_gb300 import pytree as I
+    t = cases.bc_box(n=(24, 12, 4), wall="BCWallInviscid", model="Euler", perturb=0.05,
+                     temporal="implicit", ss_iteration=3, time_step=0.05)
+    if nature == "local":
+        for z in I.getZones(t):
+            fastc._setNum2Zones(z, {"time_step_nature": "local", "cfl": 10.0})
+    zd = fasts.zone_data(t, fasts.prepare(t))
+    c = oracle_mod.Case(zd, ())
+    c.apply_bc(0)
+    c.apply_bc(1)
+    pi, pr = zd[0]["pi"], zd[0]["pr"]
+    nip, njp, nd, nss = int(pi[0]), int(pi[1]), int(pi[41]), int(pi[58])
+    assert int(pi[46]) == (1 if nature == "local" else 0)
+    free = np.array([pr[3], pr[19], pr[20], pr[21], pr[6]])
+    nsteps, bound = (200, 1e-4) if nature == "global" else (300, 1e-7)
+    for it in range(1, nsteps + 1):
+        c.compute(it, 1, nss, 1, modulo_verif=10 ** 6)
+    q = np.array(c.z[0]["lv"][0][:5 * nd]).reshape(5, -1, njp, nip)[:, 2:-2, 2:-2, 2:-2]
+    assert float(np.max(np.abs(q - free[:, None, None, None]))) < bound
